@@ -1,0 +1,45 @@
+#!/usr/bin/env bash
+# TEST INFRASTRUCTURE ONLY.
+# Compiles the reference's own poisson.c, metrics.c and implicitsolver.c, where
+# they lie under the reference checkout, unmodified, against the single-process
+# PETSc API shim in oracle/petsc_shim/, into oracle/_ref/libcvbref.so.  Nothing
+# from the reference is copied into this repository; outputs go to oracle/_ref/
+# only.  Entry points the reference calls but the parity path never reaches
+# (SNES, KSP, other CURVIB files) become stubs that return a PETSc error code.
+#
+# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default: /root/reference)
+set -euo pipefail
+REF="${1:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+if [ ! -f "$REF/poisson.c" ]; then
+  echo "build_ref: no reference sources at $REF" >&2
+  exit 2
+fi
+mkdir -p "$OUT"
+CC="${CC:-gcc}"
+CFLAGS="-std=gnu99 -O2 -fPIC -w -I$HERE/petsc_shim/include -I$REF"
+objs=()
+for f in poisson metrics implicitsolver; do
+  $CC $CFLAGS -c "$REF/$f.c" -o "$OUT/ref_$f.o"
+  objs+=("$OUT/ref_$f.o")
+done
+$CC $CFLAGS -c "$HERE/petsc_shim/petsc_shim.c" -o "$OUT/petsc_shim.o"
+$CC $CFLAGS -c "$HERE/petsc_shim/ref_harness.c" -o "$OUT/ref_harness.o"
+objs+=("$OUT/petsc_shim.o" "$OUT/ref_harness.o")
+
+# Find what is still unresolved and give each an inert stub.
+: > "$OUT/ref_stubs.c"
+set +e
+missing=$($CC -shared -o "$OUT/libcvbref.so" "${objs[@]}" -lm -Wl,--no-undefined 2>&1 |
+  sed -n "s/.*undefined reference to \`\([A-Za-z_][A-Za-z0-9_]*\)'.*/\1/p" | sort -u)
+set -e
+{
+  echo '#include <stdio.h>'
+  for s in $missing; do
+    echo "int $s(void) { fprintf(stderr, \"cvbref: $s is outside the parity path\\n\"); return 1; }"
+  done
+} > "$OUT/ref_stubs.c"
+$CC $CFLAGS -c "$OUT/ref_stubs.c" -o "$OUT/ref_stubs.o"
+$CC -shared -o "$OUT/libcvbref.so" "${objs[@]}" "$OUT/ref_stubs.o" -lm -Wl,--no-undefined
+echo "build_ref: $OUT/libcvbref.so ($(echo $missing | wc -w) stubbed entry points)"

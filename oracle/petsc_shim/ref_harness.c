@@ -1,0 +1,393 @@
+/*
+ * TEST INFRASTRUCTURE ONLY.  Drives CURVIB's own poisson.c / metrics.c /
+ * implicitsolver.c (compiled unmodified against the API shim) on the CPU so the
+ * parity tests can compare against the reference's exact arithmetic.
+ *
+ * The level set-up mirrors MG_Initial (init.c:296-1060) for one block on one
+ * rank: level sizes as MGDACreate (init.c:78-107), ghost width 3 when any
+ * direction is periodic else 2 (init.c:116,155), coordinates injected fine ->
+ * coarse (init.c:786-828), then FormMetrics (metrics.c:4) and, with periodic
+ * directions, Update_Metrics_PBC (implicitsolver.c:2174).  The exported entry
+ * points then call the reference functions named in each comment.
+ *
+ * Arrays cross this interface as the owned box [mz][my][mx] (x fastest), with
+ * 3-vectors interleaved (x,y,z), i.e. exactly a PETSc global vector.
+ */
+#include "variables.h"
+
+/* Globals the reference sources expect main.c to define. */
+PetscInt block_number = 1, immersed = 0, MHV = 0, LV = 0, ti = 0, tistart = 0;
+PetscInt NumberOfBodies = 1, blank = 0;
+PetscInt imp_MAX_IT = 1, implicit_type = 0;
+PetscReal imp_atol = 1e-8, imp_rtol = 1e-2, imp_stol = 1e-8;
+PetscInt mg_idx = 0, mg_preItr = 1, mg_poItr = 1, mg_MAX_IT = 1;
+int i_periodic = 0, j_periodic = 0, k_periodic = 0;
+int ii_periodic = 0, jj_periodic = 0, kk_periodic = 0;
+int les = 0, wallfunction = 0, rans = 0;
+int i_homo_filter = 0, j_homo_filter = 0, k_homo_filter = 0;
+int testfilter_ik = 0, testfilter_1d = 0;
+int clark = 0;
+
+/* Projection ends by calling these two (poisson.c:2902-2904); they belong to
+ * the caller's side of the boundary, so the harness compares Ucont before them. */
+PetscErrorCode Contra2Cart(UserCtx *user) { (void)user; return 0; }
+PetscErrorCode GhostNodeVelocity(UserCtx *user) { (void)user; return 0; }
+
+PetscErrorCode FormMetrics(UserCtx *user);
+PetscErrorCode Update_Metrics_PBC(UserCtx *user);
+PetscErrorCode PoissonLHSNew(UserCtx *user);
+PetscErrorCode PoissonRHS(UserCtx *user, Vec B);
+PetscErrorCode VolumeFlux_rev(UserCtx *user, PetscReal *ibm_Flux, PetscReal *ibm_Area, PetscInt flg);
+PetscErrorCode MyNvertRestriction(UserCtx *user_h, UserCtx *user_c);
+PetscErrorCode FullyBlocked(UserCtx *user);
+PetscErrorCode MyRestriction(Mat A, Vec X, Vec F);
+PetscErrorCode MyInterpolation(Mat A, Vec X, Vec F);
+PetscErrorCode PoissonNullSpaceFunction(MatNullSpace nullsp, Vec X, void *ctx);
+PetscErrorCode UpdatePressure(UserCtx *user);
+PetscErrorCode Projection(UserCtx *user);
+PetscErrorCode GridRestriction(PetscInt i, PetscInt j, PetscInt k, PetscInt *ih, PetscInt *jh,
+                               PetscInt *kh, UserCtx *user);
+
+int shim_mat_rows(Mat A);
+int shim_mat_row(Mat A, int r, const int **cols, const double **vals);
+double *shim_vec_data(Vec v);
+int shim_vec_size(Vec v);
+
+static UserMG g_mg;
+static int g_ready = 0;
+
+static UserCtx *U(int l) { return &g_mg.mgctx[l].user[0]; }
+
+static void make_vectors(UserCtx *u, int finest) {
+  DMCreateGlobalVector(u->fda, &u->Csi);
+  VecDuplicate(u->Csi, &u->Eta); VecDuplicate(u->Csi, &u->Zet);
+  VecDuplicate(u->Csi, &u->ICsi); VecDuplicate(u->Csi, &u->IEta); VecDuplicate(u->Csi, &u->IZet);
+  VecDuplicate(u->Csi, &u->JCsi); VecDuplicate(u->Csi, &u->JEta); VecDuplicate(u->Csi, &u->JZet);
+  VecDuplicate(u->Csi, &u->KCsi); VecDuplicate(u->Csi, &u->KEta); VecDuplicate(u->Csi, &u->KZet);
+  VecDuplicate(u->Csi, &u->Cent); VecDuplicate(u->Csi, &u->GridSpace);
+  VecDuplicate(u->Csi, &u->Ucont);
+  (void)finest;
+  DMCreateGlobalVector(u->da, &u->Aj);
+  VecDuplicate(u->Aj, &u->IAj); VecDuplicate(u->Aj, &u->JAj); VecDuplicate(u->Aj, &u->KAj);
+  VecDuplicate(u->Aj, &u->Nvert); VecDuplicate(u->Aj, &u->Phi); VecDuplicate(u->Aj, &u->P);
+  DMCreateLocalVector(u->fda, &u->lCsi);
+  VecDuplicate(u->lCsi, &u->lEta); VecDuplicate(u->lCsi, &u->lZet);
+  VecDuplicate(u->lCsi, &u->lICsi); VecDuplicate(u->lCsi, &u->lIEta); VecDuplicate(u->lCsi, &u->lIZet);
+  VecDuplicate(u->lCsi, &u->lJCsi); VecDuplicate(u->lCsi, &u->lJEta); VecDuplicate(u->lCsi, &u->lJZet);
+  VecDuplicate(u->lCsi, &u->lKCsi); VecDuplicate(u->lCsi, &u->lKEta); VecDuplicate(u->lCsi, &u->lKZet);
+  VecDuplicate(u->lCsi, &u->lGridSpace); VecDuplicate(u->lCsi, &u->lCent);
+  VecDuplicate(u->lCsi, &u->Centx); VecDuplicate(u->lCsi, &u->Centy); VecDuplicate(u->lCsi, &u->Centz);
+  VecDuplicate(u->lCsi, &u->lUcont);
+  DMCreateLocalVector(u->da, &u->lAj);
+  VecDuplicate(u->lAj, &u->lIAj); VecDuplicate(u->lAj, &u->lJAj); VecDuplicate(u->lAj, &u->lKAj);
+  VecDuplicate(u->lAj, &u->lNvert); VecDuplicate(u->lAj, &u->lPhi); VecDuplicate(u->lAj, &u->lP);
+}
+
+void ref_free(void) {
+  /* test-only: the process exits after use, leaks are harmless */
+  g_ready = 0;
+}
+
+/* coords: KM*JM*IM nodes, x fastest, (x,y,z) interleaved. */
+int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
+             const double *coords) {
+  memset(&g_mg, 0, sizeof(g_mg));
+  g_mg.mglevels = nlevels;
+  g_mg.mgctx = (MGCtx *)calloc((size_t)nlevels, sizeof(MGCtx));
+  for (int l = 0; l < nlevels; l++) {
+    g_mg.mgctx[l].user = (UserCtx *)calloc(1, sizeof(UserCtx));
+    g_mg.mgctx[l].thislevel = l;
+    UserCtx *u = U(l);
+    for (int q = 0; q < 6; q++) u->bctype[q] = bctype[q];
+    u->isc = isc; u->jsc = jsc; u->ksc = ksc;
+    u->cgrid = 0;
+    u->st = 1.0; u->dt = 1.0;
+    u->thislevel = l; u->mglevels = nlevels; u->_this = 0;
+    u->assignedA = PETSC_FALSE; u->multinullspace = PETSC_FALSE;
+  }
+  U(nlevels - 1)->IM = IM; U(nlevels - 1)->JM = JM; U(nlevels - 1)->KM = KM;
+  for (int l = nlevels - 2; l >= 0; l--) {
+    UserCtx *u = U(l), *h = U(l + 1);
+    u->IM = u->isc ? h->IM : (h->IM + 1) / 2;
+    u->JM = u->jsc ? h->JM : (h->JM + 1) / 2;
+    u->KM = u->ksc ? h->KM : (h->KM + 1) / 2;
+  }
+  int per = bctype[0] == 7 || bctype[2] == 7 || bctype[4] == 7;
+  int s = per ? 3 : 2;
+  for (int l = 0; l < nlevels; l++) {
+    UserCtx *u = U(l);
+    DMDACreate3d(PETSC_COMM_WORLD, bctype[0] == 7 ? DM_BOUNDARY_PERIODIC : DM_BOUNDARY_NONE,
+                 bctype[2] == 7 ? DM_BOUNDARY_PERIODIC : DM_BOUNDARY_NONE,
+                 bctype[4] == 7 ? DM_BOUNDARY_PERIODIC : DM_BOUNDARY_NONE, DMDA_STENCIL_BOX,
+                 u->IM + 1, u->JM + 1, u->KM + 1, 1, 1, 1, 1, s, NULL, NULL, NULL, &u->da);
+    DMDASetUniformCoordinates(u->da, 0.0, 1.0, 0.0, 1.0, 0.0, 1.0);
+    DMGetCoordinateDM(u->da, &u->fda);
+    DMDAGetLocalInfo(u->da, &u->info);
+  }
+  /* finest coordinates (init.c:655-744) */
+  {
+    UserCtx *u = U(nlevels - 1);
+    Vec Coor, gCoor;
+    Cmpnts ***coor;
+    DMGetCoordinatesLocal(u->da, &Coor);
+    VecSet(Coor, 0.0);
+    DMDAVecGetArray(u->fda, Coor, &coor);
+    for (int k = 0; k < u->info.mz; k++)
+      for (int j = 0; j < u->info.my; j++)
+        for (int i = 0; i < u->info.mx; i++)
+          if (k < KM && j < JM && i < IM) {
+            const double *c = coords + 3 * ((size_t)(k * JM + j) * IM + i);
+            coor[k][j][i].x = c[0]; coor[k][j][i].y = c[1]; coor[k][j][i].z = c[2];
+          }
+    DMDAVecRestoreArray(u->fda, Coor, &coor);
+    DMGetCoordinates(u->da, &gCoor);
+    VecSet(gCoor, 0.0);
+    DMLocalToGlobalBegin(u->fda, Coor, INSERT_VALUES, gCoor);
+    DMLocalToGlobalEnd(u->fda, Coor, INSERT_VALUES, gCoor);
+    DMGlobalToLocalBegin(u->fda, gCoor, INSERT_VALUES, Coor);
+    DMGlobalToLocalEnd(u->fda, gCoor, INSERT_VALUES, Coor);
+  }
+  /* inject fine -> coarse (init.c:786-828) */
+  for (int l = nlevels - 2; l >= 0; l--) {
+    UserCtx *u = U(l), *h = U(l + 1);
+    Vec Coor_high, Coor, gCoor;
+    Cmpnts ***coor, ***coor_high;
+    DMGetCoordinatesLocal(h->da, &Coor_high);
+    DMGetCoordinates(u->da, &Coor);
+    DMDAVecGetArray(h->fda, Coor_high, &coor_high);
+    DMDAVecGetArray(u->fda, Coor, &coor);
+    int xe = u->info.mx - 1, ye = u->info.my - 1, ze = u->info.mz - 1;
+    for (int k = 0; k < ze; k++)
+      for (int j = 0; j < ye; j++)
+        for (int i = 0; i < xe; i++) {
+          PetscInt ih, jh, kh;
+          GridRestriction(i, j, k, &ih, &jh, &kh, u);
+          coor[k][j][i] = coor_high[kh][jh][ih];
+        }
+    DMDAVecRestoreArray(u->fda, Coor, &coor);
+    DMDAVecRestoreArray(h->fda, Coor_high, &coor_high);
+    DMGetCoordinatesLocal(u->da, &gCoor);
+    DMGlobalToLocalBegin(u->fda, Coor, INSERT_VALUES, gCoor);
+    DMGlobalToLocalEnd(u->fda, Coor, INSERT_VALUES, gCoor);
+  }
+  /* level links and vectors (init.c:834-1060) */
+  for (int l = nlevels - 1; l >= 0; l--) {
+    UserCtx *u = U(l);
+    if (l > 0) {
+      u->da_c = &U(l - 1)->da;
+      u->lNvert_c = &U(l - 1)->lNvert;
+      u->user_c = U(l - 1);
+    }
+    if (l < nlevels - 1) {
+      u->da_f = &U(l + 1)->da;
+      u->user_f = U(l + 1);
+    }
+    make_vectors(u, l == nlevels - 1);
+    FormMetrics(u);
+    if (bctype[0] == 7 || bctype[2] == 7 || bctype[4] == 7) Update_Metrics_PBC(u);
+  }
+  g_ready = 1;
+  return 0;
+}
+
+int ref_dims(int level, int *mx, int *my, int *mz) {
+  if (!g_ready || level < 0 || level >= g_mg.mglevels) return 1;
+  *mx = U(level)->info.mx; *my = U(level)->info.my; *mz = U(level)->info.mz;
+  return 0;
+}
+
+static Vec field(UserCtx *u, const char *name, int *dof) {
+  struct { const char *n; Vec v; int dof; } t[] = {
+    {"Csi", u->lCsi, 3}, {"Eta", u->lEta, 3}, {"Zet", u->lZet, 3},
+    {"ICsi", u->lICsi, 3}, {"IEta", u->lIEta, 3}, {"IZet", u->lIZet, 3},
+    {"JCsi", u->lJCsi, 3}, {"JEta", u->lJEta, 3}, {"JZet", u->lJZet, 3},
+    {"KCsi", u->lKCsi, 3}, {"KEta", u->lKEta, 3}, {"KZet", u->lKZet, 3},
+    {"Aj", u->lAj, 1}, {"IAj", u->lIAj, 1}, {"JAj", u->lJAj, 1}, {"KAj", u->lKAj, 1},
+    {"Cent", u->lCent, 3}, {"Nvert", u->lNvert, 1}, {"Ucont", u->lUcont, 3},
+    {"Phi", u->lPhi, 1}, {"P", u->lP, 1},
+    {"gNvert", u->Nvert, 1}, {"gUcont", u->Ucont, 3}, {"gPhi", u->Phi, 1}, {"gP", u->P, 1},
+  };
+  for (size_t q = 0; q < sizeof(t) / sizeof(t[0]); q++)
+    if (!strcmp(t[q].n, name)) { *dof = t[q].dof; return t[q].v; }
+  return NULL;
+}
+
+/* Copy the owned box of a (local or global) vector out as [mz][my][mx](dof). */
+static void copy_owned(UserCtx *u, Vec v, int dof, double *out, int to_vec) {
+  DMDALocalInfo f = u->info;
+  double *a = shim_vec_data(v);
+  int n = shim_vec_size(v);
+  int local = n != f.mx * f.my * f.mz * dof;
+  int gxs = local ? f.gxs : 0, gys = local ? f.gys : 0, gzs = local ? f.gzs : 0;
+  int gxm = local ? f.gxm : f.mx, gym = local ? f.gym : f.my;
+  for (int k = 0; k < f.mz; k++)
+    for (int j = 0; j < f.my; j++)
+      for (int i = 0; i < f.mx; i++) {
+        size_t s = ((size_t)((k - gzs) * gym + (j - gys)) * gxm + (i - gxs)) * dof;
+        size_t d = ((size_t)(k * f.my + j) * f.mx + i) * dof;
+        for (int c = 0; c < dof; c++) {
+          if (to_vec) a[s + c] = out[d + c];
+          else out[d + c] = a[s + c];
+        }
+      }
+}
+
+int ref_get_field(int level, const char *name, double *out) {
+  if (!g_ready || level < 0 || level >= g_mg.mglevels) return 1;
+  int dof;
+  Vec v = field(U(level), name, &dof);
+  if (!v) return 2;
+  copy_owned(U(level), v, dof, out, 0);
+  return 0;
+}
+
+/* Set a global field and refresh its local copy (G2L), as the reference keeps them. */
+static int set_pair(UserCtx *u, Vec g, Vec l, int dof, const double *in, DM dm) {
+  copy_owned(u, g, dof, (double *)in, 1);
+  DMGlobalToLocalBegin(dm, g, INSERT_VALUES, l);
+  DMGlobalToLocalEnd(dm, g, INSERT_VALUES, l);
+  return 0;
+}
+
+int ref_set_nvert(int level, const double *nv) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(level);
+  return set_pair(u, u->Nvert, u->lNvert, 1, nv, u->da);
+}
+int ref_set_ucont(const double *uc) {
+  UserCtx *u = U(g_mg.mglevels - 1);
+  return set_pair(u, u->Ucont, u->lUcont, 3, uc, u->fda);
+}
+
+/* PoissonSolver_MG's immersed block (poisson.c:1794-1806): nvert restriction on
+ * every level pair, then FullyBlocked on the coarsest level.  Returns
+ * multinullspace in *mns and, when set, KSKE (2*mx*my ints) in kske. */
+int ref_nvert_restrict(int *mns, int *kske) {
+  if (!g_ready) return 1;
+  int L = g_mg.mglevels;
+  for (int l = L - 1; l > 0; l--) {
+    U(l)->multinullspace = PETSC_FALSE;
+    MyNvertRestriction(U(l), U(l - 1));
+  }
+  UserCtx *c = U(0);
+  PetscMalloc(c->info.mx * c->info.my * 2 * sizeof(PetscInt), &c->KSKE);
+  FullyBlocked(c);
+  *mns = c->multinullspace;
+  if (kske) memcpy(kske, c->KSKE, sizeof(int) * 2 * c->info.mx * c->info.my);
+  return 0;
+}
+
+/* PoissonLHSNew (poisson.c:600) -> rows of (col,val); returns entries written. */
+int ref_lhs(int level, int *rowptr, int *cols, double *vals, int cap) {
+  if (!g_ready) return -1;
+  UserCtx *u = U(level);
+  u->assignedA = PETSC_FALSE;
+  PoissonLHSNew(u);
+  int nr = shim_mat_rows(u->A), w = 0;
+  rowptr[0] = 0;
+  for (int r = 0; r < nr; r++) {
+    const int *c; const double *v;
+    int n = shim_mat_row(u->A, r, &c, &v);
+    for (int q = 0; q < n; q++) {
+      if (w >= cap) return -2;
+      cols[w] = c[q]; vals[w] = v[q]; w++;
+    }
+    rowptr[r + 1] = w;
+  }
+  MatDestroy(&u->A);
+  u->assignedA = PETSC_FALSE;
+  return w;
+}
+
+/* VolumeFlux_rev (poisson.c:3712) on the finest level; Ucont updated in place. */
+int ref_volume_flux(double flux_intp_sum, int flg, double *ucont_inout, double *flux, double *area) {
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont_inout, u->fda);
+  u->FluxIntpSum = flux_intp_sum;
+  VolumeFlux_rev(u, flux, area, flg);
+  copy_owned(u, u->Ucont, 3, ucont_inout, 0);
+  return 0;
+}
+
+/* PoissonRHS (poisson.c:1509) on the finest level from its current lUcont. */
+int ref_rhs(double dt, double st, double *b, double *compat_sum) {
+  UserCtx *u = U(g_mg.mglevels - 1);
+  u->dt = dt; u->st = st;
+  Vec B;
+  VecDuplicate(u->P, &B);
+  PoissonRHS(u, B);
+  copy_owned(u, B, 1, b, 0);
+  /* the reference prints this sum (poisson.c:1554-1568); recompute it identically */
+  DMDALocalInfo f = u->info;
+  double *bb = shim_vec_data(B), s = 0;
+  double ***aj;
+  DMDAVecGetArray(u->da, u->lAj, &aj);
+  for (int k = 0; k < f.mz; k++)
+    for (int j = 0; j < f.my; j++)
+      for (int i = 0; i < f.mx; i++)
+        s += bb[(size_t)(k * f.my + j) * f.mx + i] / aj[k][j][i] * dt / COEF_TIME_ACCURACY;
+  DMDAVecRestoreArray(u->da, u->lAj, &aj);
+  *compat_sum = s;
+  VecDestroy(&B);
+  return 0;
+}
+
+/* MyRestriction (poisson.c:129): fine level (coarse+1) vector -> coarse level vector. */
+int ref_restrict(int coarse, const double *xf, double *fc) {
+  UserCtx *c = U(coarse), *f = U(coarse + 1);
+  Mat MR;
+  Vec X, F;
+  VecDuplicate(f->P, &X); VecDuplicate(c->P, &F);
+  copy_owned(f, X, 1, (double *)xf, 1);
+  MatCreateShell(PETSC_COMM_WORLD, 0, 0, c->info.mx * c->info.my * c->info.mz, 0, (void *)c, &MR);
+  MatShellSetOperation(MR, MATOP_MULT, (void (*)(void))MyRestriction);
+  MatMult(MR, X, F);
+  copy_owned(c, F, 1, fc, 0);
+  MatDestroy(&MR); VecDestroy(&X); VecDestroy(&F);
+  return 0;
+}
+
+/* MyInterpolation (poisson.c:265): coarse level (fine-1) vector -> fine level vector. */
+int ref_interpolate(int fine, const double *xc, double *ff) {
+  UserCtx *f = U(fine), *c = U(fine - 1);
+  Mat MP;
+  Vec X, F;
+  VecDuplicate(c->P, &X); VecDuplicate(f->P, &F);
+  copy_owned(c, X, 1, (double *)xc, 1);
+  copy_owned(f, F, 1, ff, 1); /* MyInterpolation leaves nothing unset, but be explicit */
+  MatCreateShell(PETSC_COMM_WORLD, 0, 0, f->info.mx * f->info.my * f->info.mz, 0, (void *)f, &MP);
+  MatShellSetOperation(MP, MATOP_MULT, (void (*)(void))MyInterpolation);
+  MatMult(MP, X, F);
+  copy_owned(f, F, 1, ff, 0);
+  MatDestroy(&MP); VecDestroy(&X); VecDestroy(&F);
+  return 0;
+}
+
+/* PoissonNullSpaceFunction (poisson.c:372) applied in place on one level. */
+int ref_nullspace(int level, double *x) {
+  UserCtx *u = U(level);
+  Vec X;
+  VecDuplicate(u->P, &X);
+  copy_owned(u, X, 1, x, 1);
+  PoissonNullSpaceFunction(NULL, X, (void *)u);
+  copy_owned(u, X, 1, x, 0);
+  VecDestroy(&X);
+  return 0;
+}
+
+/* The tail of a time step on the finest level, in the reference's order:
+ * G2L(Phi) (poisson.c:1985), UpdatePressure (poisson.c:2908), Projection
+ * (poisson.c:2281).  p, phi and ucont are updated in place. */
+int ref_update_and_project(double dt, double st, double *p, double *phi, double *ucont) {
+  UserCtx *u = U(g_mg.mglevels - 1);
+  u->dt = dt; u->st = st;
+  set_pair(u, u->P, u->lP, 1, p, u->da);
+  set_pair(u, u->Phi, u->lPhi, 1, phi, u->da);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  UpdatePressure(u);
+  Projection(u);
+  copy_owned(u, u->P, 1, p, 0);
+  copy_owned(u, u->Phi, 1, phi, 0);
+  copy_owned(u, u->Ucont, 3, ucont, 0);
+  return 0;
+}
