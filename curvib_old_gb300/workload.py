@@ -25,8 +25,6 @@ reference bit for bit.
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
-
 import numpy as np
 
 COEF_TIME_ACCURACY = 1.5  # variables.h:421
@@ -275,7 +273,8 @@ def form_metrics(coor: np.ndarray, per=(False, False, False)):
         hi[...] = cm1
         hi[..., 2] = cm1[..., 2] + lgs(mz + 1, mz + 2, j0, j1, i0, i1)[..., 2]
 
-    out = {"Csi": csi, "Eta": eta, "Zet": zet, "Aj": aj, "Cent": cent}
+    out = {"Csi": csi, "Eta": eta, "Zet": zet, "Aj": aj, "Cent": cent,
+           "Centx": centx.to_global(), "Centy": centy.to_global(), "Centz": centz.to_global()}
     # I faces: k,j interior, i in [0, mx-1)  (metrics.c:713-788)
     out.update(_face_metrics("I", centx, (mz, my, mx), per))
     out.update(_face_metrics("J", centy, (mz, my, mx), per))
@@ -373,3 +372,156 @@ def _update_metrics_pbc(m, per):
             src_hi = [slice(None)] * a.ndim; src_hi[ax] = 1
             a[tuple(sl_lo)] = a[tuple(src_lo)]
             a[tuple(sl_hi)] = a[tuple(src_hi)]
+
+
+# ------------------------------------------------------------------ IB flags
+IB_CODE = 1.4     # ibm_search_advanced_rev's immersed-boundary layer (ibm.c:1072-1081)
+SOLID_CODE = 3.4  # ... and its solid cells
+
+
+def sphere_nvert(cent: np.ndarray, spheres, ib_code: float = IB_CODE,
+                 solid_code: float = SOLID_CODE) -> np.ndarray:
+    """nvert of cell centres for a union of spheres [(cx, cy, cz, r), ...].
+
+    Interior cells inside a sphere are solid; fluid interior cells with a solid
+    cell among their 26 neighbours form the IB layer (ibm.c:4407-4438);
+    everything else, the boundary ring included, is fluid (0).  The default
+    codes 1.4 / 3.4 are the ones ibm_search_advanced_rev leaves -- the search
+    the reference's main.c runs (main.c:1020) and whose IB layer VolumeFlux_rev
+    corrects (nvert in (1.1, 1.5), poisson.c:3753).  All bodies share one code
+    (the per-body +ibi/1000 of ibm.c:4651 is not used).
+    """
+    mz, my, mx = cent.shape[:3]
+    solid = np.zeros((mz, my, mx), dtype=bool)
+    c = cent[1:-1, 1:-1, 1:-1]
+    for (cx, cy, cz, r) in spheres:
+        d2 = (c[..., 0] - cx) ** 2 + (c[..., 1] - cy) ** 2 + (c[..., 2] - cz) ** 2
+        solid[1:-1, 1:-1, 1:-1] |= d2 < r * r
+    near = np.zeros_like(solid)
+    for dk in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            for di in (-1, 0, 1):
+                near[1:-1, 1:-1, 1:-1] |= solid[1 + dk:mz - 1 + dk, 1 + dj:my - 1 + dj, 1 + di:mx - 1 + di]
+    nv = np.zeros((mz, my, mx))
+    nv[near & ~solid] = ib_code
+    nv[solid] = solid_code
+    nv[0, :, :] = nv[-1, :, :] = 0.0
+    nv[:, 0, :] = nv[:, -1, :] = 0.0
+    nv[:, :, 0] = nv[:, :, -1] = 0.0
+    return nv
+
+
+# ------------------------------------------------------------------- fluxes
+def ucont_from_velocity(m: dict, vel, per=(False, False, False)) -> np.ndarray:
+    """Contravariant fluxes Ucont (mz, my, mx, 3) of a Cartesian velocity field.
+
+    ``vel(xyz) -> (…, 3)`` is evaluated at the face centres (Centx/Centy/Centz)
+    and dotted with the face area vectors Csi/Eta/Zet: Ucont.x[k][j][i] is the
+    flux through the face between cells i and i+1.  Wall faces carry zero flux;
+    on a periodic seam both copies of the face carry the same flux.
+    """
+    csi, eta, zet = m["Csi"], m["Eta"], m["Zet"]
+    mz, my, mx = csi.shape[:3]
+    uc = np.zeros((mz, my, mx, 3))
+    for comp, (area, fc) in enumerate(((csi, m["Centx"]), (eta, m["Centy"]), (zet, m["Centz"]))):
+        v = vel(fc)
+        flux = v[..., 0] * area[..., 0] + v[..., 1] * area[..., 1] + v[..., 2] * area[..., 2]
+        sl = [slice(1, mz - 1), slice(1, my - 1), slice(1, mx - 1)]
+        ax = 2 - comp                       # comp 0 -> i axis (2), 1 -> j (1), 2 -> k (0)
+        sl[ax] = slice(0, (mz, my, mx)[ax] - 1)
+        uc[tuple(sl) + (comp,)] = flux[tuple(sl)]
+        n = (mz, my, mx)[ax]
+        lo = [slice(None)] * 3; lo[ax] = 0
+        hi = [slice(None)] * 3; hi[ax] = n - 2
+        p = per[comp]
+        if p:
+            uc[tuple(lo) + (comp,)] = uc[tuple(hi) + (comp,)]
+        else:
+            uc[tuple(lo) + (comp,)] = 0.0
+            uc[tuple(hi) + (comp,)] = 0.0
+    return uc
+
+
+def taylor_green(xyz: np.ndarray) -> np.ndarray:
+    """u* = (sin(pi x) cos(pi y), -cos(pi x) sin(pi y), 0)."""
+    x, y = xyz[..., 0], xyz[..., 1]
+    out = np.zeros(xyz.shape)
+    out[..., 0] = np.sin(np.pi * x) * np.cos(np.pi * y)
+    out[..., 1] = -np.cos(np.pi * x) * np.sin(np.pi * y)
+    return out
+
+
+def smoothed_noise_ucont(m: dict, per, sigma: float, passes: int, rng) -> np.ndarray:
+    """Fluxes of a seeded Gaussian cell-centre velocity smoothed by damped-Jacobi passes.
+
+    Each pass is v <- v + (2/3)(mean of the six neighbours - v); periodic
+    directions wrap, wall directions repeat the edge value.  Face velocities are
+    the average of the two adjacent cells; wall faces carry zero flux.
+    """
+    mz, my, mx = m["Aj"].shape
+    v = rng.normal(0.0, sigma, size=(mz - 2, my - 2, mx - 2, 3))
+    for _ in range(passes):
+        pad = np.pad(v, [(1, 1), (1, 1), (1, 1), (0, 0)],
+                     mode="edge")
+        if per[2]:
+            pad[0], pad[-1] = v[-1], v[0]
+        if per[1]:
+            pad[:, 0], pad[:, -1] = pad[:, -2], pad[:, 1]
+        if per[0]:
+            pad[:, :, 0], pad[:, :, -1] = pad[:, :, -2], pad[:, :, 1]
+        nb = (pad[2:, 1:-1, 1:-1] + pad[:-2, 1:-1, 1:-1] + pad[1:-1, 2:, 1:-1] + pad[1:-1, :-2, 1:-1]
+              + pad[1:-1, 1:-1, 2:] + pad[1:-1, 1:-1, :-2]) / 6.0
+        v = v + (2.0 / 3.0) * (nb - v)
+    full = np.zeros((mz, my, mx, 3))
+    full[1:-1, 1:-1, 1:-1] = v
+    for ax, p in ((2, per[0]), (1, per[1]), (0, per[2])):
+        n = full.shape[ax]
+        lo = [slice(None)] * 4; lo[ax] = 0
+        hi = [slice(None)] * 4; hi[ax] = n - 1
+        s1 = [slice(None)] * 4; s1[ax] = 1
+        s2 = [slice(None)] * 4; s2[ax] = n - 2
+        if p:
+            full[tuple(lo)] = full[tuple(s2)]
+            full[tuple(hi)] = full[tuple(s1)]
+        else:
+            full[tuple(lo)] = full[tuple(s1)]
+            full[tuple(hi)] = full[tuple(s2)]
+    uc = np.zeros((mz, my, mx, 3))
+    areas = (m["Csi"], m["Eta"], m["Zet"])
+    for comp in range(3):
+        ax = 2 - comp
+        n = full.shape[ax]
+        a = [slice(None)] * 4; a[ax] = slice(0, n - 1)
+        b = [slice(None)] * 4; b[ax] = slice(1, n)
+        face_v = np.zeros_like(full)
+        face_v[tuple(a)] = 0.5 * (full[tuple(a)] + full[tuple(b)])
+        ar = areas[comp]
+        flux = (face_v[..., 0] * ar[..., 0] + face_v[..., 1] * ar[..., 1]
+                + face_v[..., 2] * ar[..., 2])
+        sl = [slice(1, mz - 1), slice(1, my - 1), slice(1, mx - 1)]
+        sl[ax] = slice(0, n - 1)
+        uc[tuple(sl) + (comp,)] = flux[tuple(sl)]
+        lo = [slice(None)] * 3; lo[ax] = 0
+        hi = [slice(None)] * 3; hi[ax] = n - 2
+        if per[comp]:
+            uc[tuple(lo) + (comp,)] = uc[tuple(hi) + (comp,)]
+        else:
+            uc[tuple(lo) + (comp,)] = 0.0
+            uc[tuple(hi) + (comp,)] = 0.0
+    return uc
+
+
+def compatible(b: np.ndarray, aj: np.ndarray, nvert: np.ndarray) -> np.ndarray:
+    """Project b onto the range of the singular Neumann operator.
+
+    The operator's left null vector is 1/aj on fluid cells (its rows are
+    flux differences scaled by -aj), so b is made to satisfy sum(b/aj) = 0 over
+    fluid cells: b -= aj * mean_fluid(b/aj).  Non-fluid and ring cells stay 0.
+    """
+    mz, my, mx = b.shape
+    fl = np.zeros(b.shape, dtype=bool)
+    fl[1:-1, 1:-1, 1:-1] = nvert[1:-1, 1:-1, 1:-1] < 0.1
+    c = (b[fl] / aj[fl]).mean()
+    out = b.copy()
+    out[fl] -= aj[fl] * c
+    return out

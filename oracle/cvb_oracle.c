@@ -1,0 +1,589 @@
+/*
+ * TEST INFRASTRUCTURE ONLY: CPU oracle for the pressure-projection path.
+ *
+ * Each function restates one routine of the reference (CURVIB poisson.c) on
+ * plain DMDA-layout arrays, keeping the reference's order of floating-point
+ * operations so that results can be compared bit for bit with the reference
+ * itself (compiled against the API shim in oracle/petsc_shim/).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg use this file.
+ *
+ * Build with -ffp-contract=off: the reference's products are not fused.
+ */
+#include "cvb_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define COEF 1.5 /* COEF_TIME_ACCURACY, variables.h:421 */
+
+/* stencil slots in the reference's order (poisson.c:576-594) */
+enum { CP, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW };
+
+static inline size_t ID(const orc_level *L, int i, int j, int k) {
+  return ((size_t)k * L->my + j) * L->mx + i;
+}
+static inline double NV(const orc_level *L, int i, int j, int k) { return L->nvert[ID(L, i, j, k)]; }
+static inline double dot3(const double *a, const double *b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+/* Which one-sided / central form a cross-derivative takes (poisson.c:793-1324
+ * and Projection 2347-2870).  s_up / s_dn: nvert sums of the two cells beside
+ * the face one step up / down the cross direction; c: the cross index; m: that
+ * direction's box size; per: that direction is periodic.
+ * 0 none, 1 central (c+1 vs c-1, x0.25), 2 lower (c vs c-1, x0.5),
+ * 3 upper (c+1 vs c, x0.5).  The reference's second and fourth branches cannot
+ * be reached (each needs the sum its predecessor already rejected). */
+static inline int cross_branch(double s_up, double s_dn, int c, int m, int per) {
+  if ((c == m - 2 && !per) || s_up > 0.1) {
+    if (s_dn < 0.1 && (c != 1 || per)) return 2;
+    return 0;
+  } else if ((c == 1 && !per) || s_dn > 0.1) {
+    if (s_up < 0.1) return 3;
+    return 0;
+  }
+  return 1;
+}
+
+/* Face coefficient g_ab of the reference: (metric_b . metric_a) * face Jacobian. */
+static inline double gcoef(const double *mb, const double *ma, double jac) {
+  return (mb[0] * ma[0] + mb[1] * ma[1] + mb[2] * ma[2]) * jac;
+}
+
+/* Add one cross term to vol[].  sign +1 for the upper face (E,N,T) of the row,
+ * -1 for the lower face (W,S,B).  P/Q: the row's slot and the face neighbour's
+ * slot; Pu,Qu,Pd,Qd: the slots one step up/down the cross direction. */
+static inline void add_cross(double *vol, int br, double g, double sign, int P, int Q, int Pu,
+                             int Qu, int Pd, int Qd) {
+  if (br == 2) {
+    if (sign > 0) { vol[P] += g * 0.5; vol[Q] += g * 0.5; vol[Pd] -= g * 0.5; vol[Qd] -= g * 0.5; }
+    else { vol[P] -= g * 0.5; vol[Q] -= g * 0.5; vol[Pd] += g * 0.5; vol[Qd] += g * 0.5; }
+  } else if (br == 3) {
+    if (sign > 0) { vol[Pu] += g * 0.5; vol[Qu] += g * 0.5; vol[P] -= g * 0.5; vol[Q] -= g * 0.5; }
+    else { vol[Pu] -= g * 0.5; vol[Qu] -= g * 0.5; vol[P] += g * 0.5; vol[Q] += g * 0.5; }
+  } else if (br == 1) {
+    if (sign > 0) { vol[Pu] += g * 0.25; vol[Qu] += g * 0.25; vol[Pd] -= g * 0.25; vol[Qd] -= g * 0.25; }
+    else { vol[Pu] -= g * 0.25; vol[Qu] -= g * 0.25; vol[Pd] += g * 0.25; vol[Qd] += g * 0.25; }
+  }
+}
+
+static inline int wrap_up(int i, int m, int per) { return (per && i == m - 2) ? 1 : i + 1; }
+static inline int wrap_dn(int i, int m, int per) { return (per && i == 1) ? m - 2 : i - 1; }
+
+int orc_lhs_csr(const orc_level *L, int *rowptr, int *cols, double *vals, int cap) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const int px = L->bctype[0] == 7, py = L->bctype[2] == 7, pz = L->bctype[4] == 7;
+  const int x_end = px ? mx - 1 : mx - 2, x_str = px ? 0 : 1;
+  const int y_end = py ? my - 1 : my - 2, y_str = py ? 0 : 1;
+  const int z_end = pz ? mz - 1 : mz - 2, z_str = pz ? 0 : 1;
+  const double thr = 0.1;
+  const size_t N = (size_t)mx * my * mz;
+  /* G coefficients over the box (poisson.c:699-735) */
+  double *g = (double *)malloc(sizeof(double) * 9 * N);
+  for (size_t p = 0; p < N; p++) {
+    const double *ic = L->icsi + 3 * p, *ie = L->ieta + 3 * p, *iz = L->izet + 3 * p;
+    const double *jc = L->jcsi + 3 * p, *je = L->jeta + 3 * p, *jz = L->jzet + 3 * p;
+    const double *kc = L->kcsi + 3 * p, *ke = L->keta + 3 * p, *kz = L->kzet + 3 * p;
+    g[9 * p + 0] = gcoef(ic, ic, L->iaj[p]);
+    g[9 * p + 1] = gcoef(ie, ic, L->iaj[p]);
+    g[9 * p + 2] = gcoef(iz, ic, L->iaj[p]);
+    g[9 * p + 3] = gcoef(jc, je, L->jaj[p]);
+    g[9 * p + 4] = gcoef(je, je, L->jaj[p]);
+    g[9 * p + 5] = gcoef(jz, je, L->jaj[p]);
+    g[9 * p + 6] = gcoef(kc, kz, L->kaj[p]);
+    g[9 * p + 7] = gcoef(ke, kz, L->kaj[p]);
+    g[9 * p + 8] = gcoef(kz, kz, L->kaj[p]);
+  }
+#define G(n, i, j, k) g[9 * ID(L, i, j, k) + (n)]
+  int w = 0;
+  rowptr[0] = 0;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t row = ID(L, i, j, k);
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1 ||
+            NV(L, i, j, k) > 0.1) {
+          if (w + 1 > cap) { free(g); return -1; }
+          cols[w] = (int)row; vals[w] = 1.0; w++;
+          rowptr[row + 1] = w;
+          continue;
+        }
+        double vol[19];
+        for (int m = 0; m < 19; m++) vol[m] = 0.0;
+        double gg;
+        /* i+1 - i (poisson.c:794-869) */
+        if (NV(L, i + 1, j, k) < thr && i != x_end) {
+          vol[CP] -= G(0, i, j, k); vol[EP] += G(0, i, j, k);
+          gg = G(1, i, j, k);
+          add_cross(vol, cross_branch(NV(L, i, j + 1, k) + NV(L, i + 1, j + 1, k),
+                                      NV(L, i, j - 1, k) + NV(L, i + 1, j - 1, k), j, my, py),
+                    gg, +1, CP, EP, NP, NE, SP, SE);
+          gg = G(2, i, j, k);
+          add_cross(vol, cross_branch(NV(L, i, j, k + 1) + NV(L, i + 1, j, k + 1),
+                                      NV(L, i, j, k - 1) + NV(L, i + 1, j, k - 1), k, mz, pz),
+                    gg, +1, CP, EP, TP, TE, BP, BE);
+        }
+        /* i - i-1 (poisson.c:872-946) */
+        if (NV(L, i - 1, j, k) < thr && i != x_str) {
+          vol[CP] -= G(0, i - 1, j, k); vol[WP] += G(0, i - 1, j, k);
+          gg = G(1, i - 1, j, k);
+          add_cross(vol, cross_branch(NV(L, i, j + 1, k) + NV(L, i - 1, j + 1, k),
+                                      NV(L, i, j - 1, k) + NV(L, i - 1, j - 1, k), j, my, py),
+                    gg, -1, CP, WP, NP, NW, SP, SW);
+          gg = G(2, i - 1, j, k);
+          add_cross(vol, cross_branch(NV(L, i, j, k + 1) + NV(L, i - 1, j, k + 1),
+                                      NV(L, i, j, k - 1) + NV(L, i - 1, j, k - 1), k, mz, pz),
+                    gg, -1, CP, WP, TP, TW, BP, BW);
+        }
+        /* j+1 - j (poisson.c:949-1056): cross i, main, cross k */
+        if (NV(L, i, j + 1, k) < thr && j != y_end) {
+          gg = G(3, i, j, k);
+          add_cross(vol, cross_branch(NV(L, i + 1, j, k) + NV(L, i + 1, j + 1, k),
+                                      NV(L, i - 1, j, k) + NV(L, i - 1, j + 1, k), i, mx, px),
+                    gg, +1, CP, NP, EP, NE, WP, NW);
+          vol[CP] -= G(4, i, j, k); vol[NP] += G(4, i, j, k);
+          gg = G(5, i, j, k);
+          add_cross(vol, cross_branch(NV(L, i, j, k + 1) + NV(L, i, j + 1, k + 1),
+                                      NV(L, i, j, k - 1) + NV(L, i, j + 1, k - 1), k, mz, pz),
+                    gg, +1, CP, NP, TP, TN, BP, BN);
+        }
+        /* j - j-1 (poisson.c:1059-1165) */
+        if (NV(L, i, j - 1, k) < thr && j != y_str) {
+          gg = G(3, i, j - 1, k);
+          add_cross(vol, cross_branch(NV(L, i + 1, j, k) + NV(L, i + 1, j - 1, k),
+                                      NV(L, i - 1, j, k) + NV(L, i - 1, j - 1, k), i, mx, px),
+                    gg, -1, CP, SP, EP, SE, WP, SW);
+          vol[CP] -= G(4, i, j - 1, k); vol[SP] += G(4, i, j - 1, k);
+          gg = G(5, i, j - 1, k);
+          add_cross(vol, cross_branch(NV(L, i, j, k + 1) + NV(L, i, j - 1, k + 1),
+                                      NV(L, i, j, k - 1) + NV(L, i, j - 1, k - 1), k, mz, pz),
+                    gg, -1, CP, SP, TP, TS, BP, BS);
+        }
+        /* k+1 - k (poisson.c:1168-1245): cross i, cross j, main */
+        if (NV(L, i, j, k + 1) < thr && k != z_end) {
+          gg = G(6, i, j, k);
+          add_cross(vol, cross_branch(NV(L, i + 1, j, k) + NV(L, i + 1, j, k + 1),
+                                      NV(L, i - 1, j, k) + NV(L, i - 1, j, k + 1), i, mx, px),
+                    gg, +1, CP, TP, EP, TE, WP, TW);
+          gg = G(7, i, j, k);
+          add_cross(vol, cross_branch(NV(L, i, j + 1, k) + NV(L, i, j + 1, k + 1),
+                                      NV(L, i, j - 1, k) + NV(L, i, j - 1, k + 1), j, my, py),
+                    gg, +1, CP, TP, NP, TN, SP, TS);
+          vol[CP] -= G(8, i, j, k); vol[TP] += G(8, i, j, k);
+        }
+        /* k - k-1 (poisson.c:1248-1324) */
+        if (NV(L, i, j, k - 1) < thr && k != z_str) {
+          gg = G(6, i, j, k - 1);
+          add_cross(vol, cross_branch(NV(L, i + 1, j, k) + NV(L, i + 1, j, k - 1),
+                                      NV(L, i - 1, j, k) + NV(L, i - 1, j, k - 1), i, mx, px),
+                    gg, -1, CP, BP, EP, BE, WP, BW);
+          gg = G(7, i, j, k - 1);
+          add_cross(vol, cross_branch(NV(L, i, j + 1, k) + NV(L, i, j + 1, k - 1),
+                                      NV(L, i, j - 1, k) + NV(L, i, j - 1, k - 1), j, my, py),
+                    gg, -1, CP, BP, NP, BN, SP, BS);
+          vol[CP] -= G(8, i, j, k - 1); vol[BP] += G(8, i, j, k - 1);
+        }
+        double a = L->aj[row];
+        for (int m = 0; m < 19; m++) vol[m] *= -a;
+        /* column indices with the periodic wrap (poisson.c:1329-1450) */
+        int iu = wrap_up(i, mx, px), id = wrap_dn(i, mx, px);
+        int ju = wrap_up(j, my, py), jd = wrap_dn(j, my, py);
+        int ku = wrap_up(k, mz, pz), kd = wrap_dn(k, mz, pz);
+        int idx[19];
+        idx[CP] = (int)ID(L, i, j, k);
+        idx[EP] = (int)ID(L, iu, j, k); idx[WP] = (int)ID(L, id, j, k);
+        idx[NP] = (int)ID(L, i, ju, k); idx[SP] = (int)ID(L, i, jd, k);
+        idx[TP] = (int)ID(L, i, j, ku); idx[BP] = (int)ID(L, i, j, kd);
+        idx[NE] = (int)ID(L, iu, ju, k); idx[SE] = (int)ID(L, iu, jd, k);
+        idx[NW] = (int)ID(L, id, ju, k); idx[SW] = (int)ID(L, id, jd, k);
+        idx[TN] = (int)ID(L, i, ju, ku); idx[BN] = (int)ID(L, i, ju, kd);
+        idx[TS] = (int)ID(L, i, jd, ku); idx[BS] = (int)ID(L, i, jd, kd);
+        idx[TE] = (int)ID(L, iu, j, ku); idx[BE] = (int)ID(L, iu, j, kd);
+        idx[TW] = (int)ID(L, id, j, ku); idx[BW] = (int)ID(L, id, j, kd);
+        /* INSERT_VALUES: a repeated column keeps the last value */
+        int start = w;
+        for (int m = 0; m < 19; m++) {
+          int at = -1;
+          for (int q = start; q < w; q++) if (cols[q] == idx[m]) { at = q; break; }
+          if (at < 0) {
+            if (w + 1 > cap) { free(g); return -1; }
+            at = w++;
+            cols[at] = idx[m];
+          }
+          vals[at] = vol[m];
+        }
+        rowptr[row + 1] = w;
+      }
+#undef G
+  free(g);
+  return w;
+}
+
+void orc_csr_mult(int n, const int *rowptr, const int *cols, const double *vals,
+                  const double *x, double *y) {
+  for (int r = 0; r < n; r++) {
+    double s = 0.0;
+    for (int q = rowptr[r]; q < rowptr[r + 1]; q++) s += vals[q] * x[cols[q]];
+    y[r] = s;
+  }
+}
+
+double orc_poisson_rhs(const orc_level *L, const double *uc, double dt, double st, double *b) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t p = ID(L, i, j, k);
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1) b[p] = 0.;
+        else if (L->nvert[p] > 0.1) b[p] = 0;
+        else
+          b[p] = -(uc[3 * p] - uc[3 * ID(L, i - 1, j, k)] + uc[3 * p + 1] - uc[3 * ID(L, i, j - 1, k) + 1] +
+                   uc[3 * p + 2] - uc[3 * ID(L, i, j, k - 1) + 2]) /
+                 dt * L->aj[p] / st * COEF;
+      }
+  double s = 0.;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t p = ID(L, i, j, k);
+        s += b[p] / L->aj[p] * dt / COEF;
+      }
+  return s;
+}
+
+static inline double norm3(const double *v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+/* One pass of VolumeFlux_rev's sums (poisson.c:3750-3798). */
+static void ib_sums(const orc_level *L, const double *uc, double *flux, double *area) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const double ibmval = 1.5;
+  double f = 0, a = 0;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t p = ID(L, i, j, k);
+        double nv = L->nvert[p];
+        if (nv < 0.1) {
+          double n1 = NV(L, i + 1, j, k), n2 = NV(L, i, j + 1, k), n3 = NV(L, i, j, k + 1);
+          if (n1 > ibmval - 0.4 && n1 < ibmval && i < mx - 2) { f += uc[3 * p]; a += norm3(L->csi + 3 * p); }
+          if (n2 > ibmval - 0.4 && n2 < ibmval && j < my - 2) { f += uc[3 * p + 1]; a += norm3(L->eta + 3 * p); }
+          if (n3 > ibmval - 0.4 && n3 < ibmval && k < mz - 2) { f += uc[3 * p + 2]; a += norm3(L->zet + 3 * p); }
+        }
+        if (nv > ibmval - 0.4 && nv < ibmval) {
+          if (NV(L, i + 1, j, k) < 0.1 && i < mx - 2) { f -= uc[3 * p]; a += norm3(L->csi + 3 * p); }
+          if (NV(L, i, j + 1, k) < 0.1 && j < my - 2) { f -= uc[3 * p + 1]; a += norm3(L->eta + 3 * p); }
+          if (NV(L, i, j, k + 1) < 0.1 && k < mz - 2) { f -= uc[3 * p + 2]; a += norm3(L->zet + 3 * p); }
+        }
+      }
+  *flux = f;
+  *area = a;
+}
+
+void orc_volume_flux_rev(const orc_level *L, double *uc, double flux_intp_sum, int flg,
+                         double *flux_out, double *area_out) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const double ibmval = 1.5;
+  double flux, area, corr;
+  ib_sums(L, uc, &flux, &area);
+  if (area > 1.e-15) corr = flg ? (flux + flux_intp_sum) / area : flux / area;
+  else corr = 0;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t p = ID(L, i, j, k);
+        double nv = L->nvert[p];
+        if (nv < 0.1) {
+          double n1 = NV(L, i + 1, j, k), n2 = NV(L, i, j + 1, k), n3 = NV(L, i, j, k + 1);
+          if (n1 > ibmval - 0.4 && n1 < ibmval && i < mx - 2) uc[3 * p] -= norm3(L->csi + 3 * p) * corr;
+          if (n2 > ibmval - 0.4 && n2 < ibmval && j < my - 2) uc[3 * p + 1] -= norm3(L->eta + 3 * p) * corr;
+          if (n3 > ibmval - 0.4 && n3 < ibmval && k < mz - 2) uc[3 * p + 2] -= norm3(L->zet + 3 * p) * corr;
+        }
+        if (nv > ibmval - 0.4 && nv < ibmval) {
+          if (NV(L, i + 1, j, k) < 0.1 && i < mx - 2) uc[3 * p] += norm3(L->csi + 3 * p) * corr;
+          if (NV(L, i, j + 1, k) < 0.1 && j < my - 2) uc[3 * p + 1] += norm3(L->eta + 3 * p) * corr;
+          if (NV(L, i, j, k + 1) < 0.1 && k < mz - 2) uc[3 * p + 2] += norm3(L->zet + 3 * p) * corr;
+        }
+      }
+  ib_sums(L, uc, flux_out, area_out);
+}
+
+void orc_nvert_restrict(const orc_level *F, int cmx, int cmy, int cmz, int coarse_is_level0,
+                        int isc, int jsc, int ksc, double *nc) {
+  (void)coarse_is_level0; /* both branches of the reference are identical */
+  const int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
+  size_t Nc = (size_t)cmx * cmy * cmz;
+  for (size_t p = 0; p < Nc; p++) nc[p] = 0.;
+#define CI(i, j, k) (((size_t)(k) * cmy + (j)) * cmx + (i))
+  for (int k = 1; k < cmz - 1; k++)
+    for (int j = 1; j < cmy - 1; j++)
+      for (int i = 1; i < cmx - 1; i++) {
+        int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+        if (NV(F, ih, jh, kh) * NV(F, ih - ia, jh, kh) * NV(F, ih, jh - ja, kh) * NV(F, ih, jh, kh - ka) *
+                NV(F, ih - ia, jh - ja, kh) * NV(F, ih - ia, jh, kh - ka) * NV(F, ih, jh - ja, kh - ka) *
+                NV(F, ih - ia, jh - ja, kh - ka) >
+            0.1) {
+          double v = nc[CI(i, j, k)];
+          nc[CI(i, j, k)] = (1. < v) ? v : 1.;
+        }
+      }
+  /* second pass reads a snapshot (the reference's lNvert after G2L) */
+  double *snap = (double *)malloc(sizeof(double) * Nc);
+  memcpy(snap, nc, sizeof(double) * Nc);
+  for (int k = 1; k < cmz - 1; k++)
+    for (int j = 1; j < cmy - 1; j++)
+      for (int i = 1; i < cmx - 1; i++) {
+        if (nc[CI(i, j, k)] < 0.1) {
+          if (snap[CI(i + 1, j, k)] + snap[CI(i - 1, j, k)] > 1.1 &&
+              snap[CI(i, j + 1, k)] + snap[CI(i, j - 1, k)] > 1.1 &&
+              snap[CI(i, j, k + 1)] + snap[CI(i, j, k - 1)] > 1.1)
+            nc[CI(i, j, k)] = 1.;
+        }
+      }
+#undef CI
+  free(snap);
+}
+
+int orc_fully_blocked(const orc_level *L, int *kske) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  int all = 1;
+  memset(kske, 0, sizeof(int) * 2 * (size_t)mx * my);
+  for (int j = 1; j < my - 1; j++)
+    for (int i = 1; i < mx - 1; i++) {
+      int blocked = 0;
+      for (int k = 0; k < mz; k++)
+        if (NV(L, i, j, k) > 0.1) {
+          if (!blocked) { kske[2 * (j * mx + i)] = k; blocked = 1; }
+          else if (k < kske[2 * (j * mx + i)]) kske[2 * (j * mx + i)] = k;
+        }
+      if (!blocked) all = 0;
+    }
+  return all;
+}
+
+void orc_restrict(const orc_level *F, const orc_level *C, const double *x, double *f) {
+  const int mx = C->mx, my = C->my, mz = C->mz;
+  const int ia = C->isc ? 0 : 1, ja = C->jsc ? 0 : 1, ka = C->ksc ? 0 : 1;
+#define W(i, j, k) (x[ID(F, i, j, k)] * ((0. < 1 - NV(F, i, j, k)) ? (1 - NV(F, i, j, k)) : 0.))
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t p = ID(C, i, j, k);
+        if (k == 0 || k == mz - 1 || j == 0 || j == my - 1 || i == 0 || i == mx - 1) { f[p] = 0.; continue; }
+        int ih = C->isc ? i : 2 * i, jh = C->jsc ? j : 2 * j, kh = C->ksc ? k : 2 * k;
+        f[p] = 0.125 * (W(ih, jh, kh) + W(ih - ia, jh, kh) + W(ih, jh - ja, kh) + W(ih, jh, kh - ka) +
+                        W(ih - ia, jh - ja, kh) + W(ih, jh - ja, kh - ka) + W(ih - ia, jh, kh - ka) +
+                        W(ih - ia, jh - ja, kh - ka));
+        if (C->nvert[p] > 0.1) f[p] = 0.;
+      }
+#undef W
+}
+
+void orc_interpolate(const orc_level *C, const orc_level *F, const double *x, double *f) {
+  const int mx = F->mx, my = F->my, mz = F->mz;
+#define XC(i, j, k) x[ID(C, i, j, k)]
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        int ic, jc, kc, ia, ja, ka;
+        if (F->isc) { ic = i; ia = 0; }
+        else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == mx - 2) ia = 0; }
+        if (F->jsc) { jc = j; ja = 0; }
+        else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == my - 2) ja = 0; }
+        if (F->ksc) { kc = k; ka = 0; }
+        else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == mz - 2) ka = 0; }
+        if (ka == -1 && NV(C, ic, jc, kc - 1) > 0.1) ka = 0;
+        else if (ka == 1 && NV(C, ic, jc, kc + 1) > 0.1) ka = 0;
+        if (ja == -1 && NV(C, ic, jc - 1, kc) > 0.1) ja = 0;
+        else if (ja == 1 && NV(C, ic, jc + 1, kc) > 0.1) ja = 0;
+        if (ia == -1 && NV(C, ic - 1, jc, kc) > 0.1) ia = 0;
+        else if (ia == 1 && NV(C, ic + 1, jc, kc) > 0.1) ia = 0;
+        f[ID(F, i, j, k)] = (XC(ic, jc, kc) * 9 + XC(ic, jc + ja, kc) * 3 + XC(ic + ia, jc, kc) * 3 +
+                             XC(ic + ia, jc + ja, kc)) * 3. / 64. +
+                            (XC(ic, jc, kc + ka) * 9 + XC(ic, jc + ja, kc + ka) * 3 +
+                             XC(ic + ia, jc, kc + ka) * 3 + XC(ic + ia, jc + ja, kc + ka)) / 64.;
+      }
+#undef XC
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t p = ID(F, i, j, k);
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1) f[p] = 0.;
+        if (F->nvert[p] > 0.1) f[p] = 0.;
+      }
+}
+
+void orc_nullspace(const orc_level *L, int mns, const int *kske, double *x) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  double sum, num;
+  if (!mns) {
+    sum = 0; num = 0;
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          if (NV(L, i, j, k) < 0.1) { sum += x[ID(L, i, j, k)]; num++; }
+    sum = sum / (-1.0 * num);
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          if (NV(L, i, j, k) < 0.1) x[ID(L, i, j, k)] += sum;
+  } else {
+    for (int side = 0; side < 2; side++) {
+      sum = 0; num = 0;
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int k = 1; k < mz - 1; k++) {
+            int below = k < kske[2 * (j * mx + i)];
+            if ((side == 0 ? below : !below) && NV(L, i, j, k) < 0.1) { sum += x[ID(L, i, j, k)]; num++; }
+          }
+      sum /= -num;
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int k = 1; k < mz - 1; k++) {
+            int below = k < kske[2 * (j * mx + i)];
+            if ((side == 0 ? below : !below) && NV(L, i, j, k) < 0.1) x[ID(L, i, j, k)] += sum;
+          }
+    }
+  }
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++)
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1 || NV(L, i, j, k) > 0.1)
+          x[ID(L, i, j, k)] = 0.;
+}
+
+void orc_update_pressure(const orc_level *L, double *p, double *phi) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const int IM = mx - 1, JM = my - 1, KM = mz - 1;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) p[ID(L, i, j, k)] += phi[ID(L, i, j, k)];
+  if (!(L->bctype[0] == 7 || L->bctype[2] == 7 || L->bctype[4] == 7)) return;
+  /* each pass reads the ghost image refreshed before it: [-2] -> m-2, [m+1] -> 1 */
+  if (L->bctype[0] == 7 || L->bctype[1] == 7)
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++)
+        if (k > 0 && k < KM && j > 0 && j < JM) {
+          p[ID(L, 0, j, k)] = p[ID(L, mx - 2, j, k)]; phi[ID(L, 0, j, k)] = phi[ID(L, mx - 2, j, k)];
+          p[ID(L, mx - 1, j, k)] = p[ID(L, 1, j, k)]; phi[ID(L, mx - 1, j, k)] = phi[ID(L, 1, j, k)];
+        }
+  if (L->bctype[2] == 7 || L->bctype[3] == 7)
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < mx; i++)
+        if (k > 0 && k < KM && i > 0 && i < IM) {
+          p[ID(L, i, 0, k)] = p[ID(L, i, my - 2, k)]; phi[ID(L, i, 0, k)] = phi[ID(L, i, my - 2, k)];
+          p[ID(L, i, my - 1, k)] = p[ID(L, i, 1, k)]; phi[ID(L, i, my - 1, k)] = phi[ID(L, i, 1, k)];
+        }
+  if (L->bctype[4] == 7 || L->bctype[5] == 7)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++)
+        if (i > 0 && i < IM && j > 0 && j < JM) {
+          p[ID(L, i, j, 0)] = p[ID(L, i, j, mz - 2)]; phi[ID(L, i, j, 0)] = phi[ID(L, i, j, mz - 2)];
+          p[ID(L, i, j, mz - 1)] = p[ID(L, i, j, 1)]; phi[ID(L, i, j, mz - 1)] = phi[ID(L, i, j, 1)];
+        }
+  /* second round over whole ring planes (poisson.c:3085-3240): x, then y, then z */
+  if (L->bctype[0] == 7 || L->bctype[1] == 7)
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++) {
+        p[ID(L, 0, j, k)] = p[ID(L, mx - 2, j, k)]; phi[ID(L, 0, j, k)] = phi[ID(L, mx - 2, j, k)];
+        p[ID(L, mx - 1, j, k)] = p[ID(L, 1, j, k)]; phi[ID(L, mx - 1, j, k)] = phi[ID(L, 1, j, k)];
+      }
+  if (L->bctype[2] == 7 || L->bctype[3] == 7)
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < mx; i++) {
+        p[ID(L, i, my - 1, k)] = p[ID(L, i, 1, k)]; phi[ID(L, i, my - 1, k)] = phi[ID(L, i, 1, k)];
+        p[ID(L, i, 0, k)] = p[ID(L, i, my - 2, k)]; phi[ID(L, i, 0, k)] = phi[ID(L, i, my - 2, k)];
+      }
+  if (L->bctype[4] == 7 || L->bctype[5] == 7)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        p[ID(L, i, j, mz - 1)] = p[ID(L, i, j, 1)]; phi[ID(L, i, j, mz - 1)] = phi[ID(L, i, j, 1)];
+        p[ID(L, i, j, 0)] = p[ID(L, i, j, mz - 2)]; phi[ID(L, i, j, 0)] = phi[ID(L, i, j, mz - 2)];
+      }
+}
+
+/* Pressure-gradient pieces of Projection for one cross direction: returns the
+ * cross difference (poisson.c:2370-2411 and the five analogues). */
+static inline double cross_diff(int br, double pu0, double pu1, double p0, double p1, double pd0,
+                                double pd1) {
+  if (br == 2) return (p0 + p1 - pd0 - pd1) * 0.5;
+  if (br == 3) return (pu0 + pu1 - p0 - p1) * 0.5;
+  if (br == 1) return (pu0 + pu1 - pd0 - pd1) * 0.25;
+  return 0.;
+}
+
+static void proj_x(const orc_level *L, const double *ph, double dt, double st, double *uc, int i, int j, int k) {
+  const int my = L->my, mz = L->mz;
+  const int py = L->bctype[2] == 7, pz = L->bctype[4] == 7;
+  double dpdc = ph[ID(L, i + 1, j, k)] - ph[ID(L, i, j, k)];
+  int bj = cross_branch(NV(L, i, j + 1, k) + NV(L, i + 1, j + 1, k), NV(L, i, j - 1, k) + NV(L, i + 1, j - 1, k), j, my, py);
+  double dpde = cross_diff(bj, ph[ID(L, i, j + 1, k)], ph[ID(L, i + 1, j + 1, k)], ph[ID(L, i, j, k)],
+                           ph[ID(L, i + 1, j, k)], ph[ID(L, i, j - 1, k)], ph[ID(L, i + 1, j - 1, k)]);
+  int bk = cross_branch(NV(L, i, j, k + 1) + NV(L, i + 1, j, k + 1), NV(L, i, j, k - 1) + NV(L, i + 1, j, k - 1), k, mz, pz);
+  double dpdz = cross_diff(bk, ph[ID(L, i, j, k + 1)], ph[ID(L, i + 1, j, k + 1)], ph[ID(L, i, j, k)],
+                           ph[ID(L, i + 1, j, k)], ph[ID(L, i, j, k - 1)], ph[ID(L, i + 1, j, k - 1)]);
+  if (!(NV(L, i, j, k) + NV(L, i + 1, j, k))) {
+    size_t p = ID(L, i, j, k);
+    const double *ic = L->icsi + 3 * p, *ie = L->ieta + 3 * p, *iz = L->izet + 3 * p;
+    double ia = L->iaj[p];
+    uc[3 * p] -= (dpdc * dot3(ic, ic) * ia + dpde * dot3(ie, ic) * ia + dpdz * dot3(iz, ic) * ia) * dt * st / COEF;
+  }
+}
+
+static void proj_y(const orc_level *L, const double *ph, double dt, double st, double *uc, int i, int j, int k) {
+  const int mx = L->mx, mz = L->mz;
+  const int px = L->bctype[0] == 7, pz = L->bctype[4] == 7;
+  int bi = cross_branch(NV(L, i + 1, j, k) + NV(L, i + 1, j + 1, k), NV(L, i - 1, j, k) + NV(L, i - 1, j + 1, k), i, mx, px);
+  double dpdc = cross_diff(bi, ph[ID(L, i + 1, j, k)], ph[ID(L, i + 1, j + 1, k)], ph[ID(L, i, j, k)],
+                           ph[ID(L, i, j + 1, k)], ph[ID(L, i - 1, j, k)], ph[ID(L, i - 1, j + 1, k)]);
+  double dpde = ph[ID(L, i, j + 1, k)] - ph[ID(L, i, j, k)];
+  int bk = cross_branch(NV(L, i, j, k + 1) + NV(L, i, j + 1, k + 1), NV(L, i, j, k - 1) + NV(L, i, j + 1, k - 1), k, mz, pz);
+  double dpdz = cross_diff(bk, ph[ID(L, i, j, k + 1)], ph[ID(L, i, j + 1, k + 1)], ph[ID(L, i, j, k)],
+                           ph[ID(L, i, j + 1, k)], ph[ID(L, i, j, k - 1)], ph[ID(L, i, j + 1, k - 1)]);
+  if (!(NV(L, i, j, k) + NV(L, i, j + 1, k))) {
+    size_t p = ID(L, i, j, k);
+    const double *jc = L->jcsi + 3 * p, *je = L->jeta + 3 * p, *jz = L->jzet + 3 * p;
+    double ja = L->jaj[p];
+    uc[3 * p + 1] -= (dpdc * dot3(jc, je) * ja + dpde * dot3(je, je) * ja + dpdz * dot3(jz, je) * ja) * dt * st / COEF;
+  }
+}
+
+static void proj_z(const orc_level *L, const double *ph, double dt, double st, double *uc, int i, int j, int k) {
+  const int mx = L->mx, my = L->my;
+  const int px = L->bctype[0] == 7, py = L->bctype[2] == 7;
+  int bi = cross_branch(NV(L, i + 1, j, k) + NV(L, i + 1, j, k + 1), NV(L, i - 1, j, k) + NV(L, i - 1, j, k + 1), i, mx, px);
+  double dpdc = cross_diff(bi, ph[ID(L, i + 1, j, k)], ph[ID(L, i + 1, j, k + 1)], ph[ID(L, i, j, k)],
+                           ph[ID(L, i, j, k + 1)], ph[ID(L, i - 1, j, k)], ph[ID(L, i - 1, j, k + 1)]);
+  int bj = cross_branch(NV(L, i, j + 1, k) + NV(L, i, j + 1, k + 1), NV(L, i, j - 1, k) + NV(L, i, j - 1, k + 1), j, my, py);
+  double dpde = cross_diff(bj, ph[ID(L, i, j + 1, k)], ph[ID(L, i, j + 1, k + 1)], ph[ID(L, i, j, k)],
+                           ph[ID(L, i, j, k + 1)], ph[ID(L, i, j - 1, k)], ph[ID(L, i, j - 1, k + 1)]);
+  double dpdz = ph[ID(L, i, j, k + 1)] - ph[ID(L, i, j, k)];
+  if (!(NV(L, i, j, k) + NV(L, i, j, k + 1))) {
+    size_t p = ID(L, i, j, k);
+    const double *kc = L->kcsi + 3 * p, *ke = L->keta + 3 * p, *kz = L->kzet + 3 * p;
+    double ka = L->kaj[p];
+    uc[3 * p + 2] -= (dpdc * dot3(kc, kz) * ka + dpde * dot3(ke, kz) * ka + dpdz * dot3(kz, kz) * ka) * dt * st / COEF;
+  }
+}
+
+void orc_projection(const orc_level *L, const double *phi, double dt, double st, double *uc) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const int px = L->bctype[0] == 7, py = L->bctype[2] == 7, pz = L->bctype[4] == 7;
+  const int i_end = px ? mx - 1 : mx - 2, j_end = py ? my - 1 : my - 2, k_end = pz ? mz - 1 : mz - 2;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        if (i < i_end) proj_x(L, phi, dt, st, uc, i, j, k);
+        if (j < j_end) proj_y(L, phi, dt, st, uc, i, j, k);
+        if (k < k_end) proj_z(L, phi, dt, st, uc, i, j, k);
+      }
+  if (px)
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++) proj_x(L, phi, dt, st, uc, 0, j, k);
+  if (py)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) proj_y(L, phi, dt, st, uc, i, 0, k);
+  if (pz)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) proj_z(L, phi, dt, st, uc, i, j, 0);
+}

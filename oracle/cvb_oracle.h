@@ -1,0 +1,63 @@
+/*
+ * TEST INFRASTRUCTURE ONLY: the CPU oracle for the pressure-projection path.
+ *
+ * A plain-C restatement of the reference's arithmetic (CURVIB poisson.c), used
+ * by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+ * checker.  The product library never links or calls it.
+ *
+ * Arrays are the reference's DMDA global layout for one level: [mz][my][mx],
+ * i fastest, boundary ring included; 3-vectors (Cmpnts) are interleaved x,y,z.
+ * Periodic ring values are the ones Update_Metrics_PBC / UpdatePressure leave.
+ */
+#ifndef CVB_ORACLE_H
+#define CVB_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int mx, my, mz;
+  int bctype[6];
+  int isc, jsc, ksc;
+  const double *icsi, *ieta, *izet;   /* I-face metrics (ICsi, IEta, IZet) */
+  const double *jcsi, *jeta, *jzet;   /* J-face metrics */
+  const double *kcsi, *keta, *kzet;   /* K-face metrics */
+  const double *iaj, *jaj, *kaj, *aj; /* face and cell Jacobians */
+  const double *csi, *eta, *zet;      /* cell metrics (VolumeFlux_rev) */
+  const double *nvert;
+} orc_level;
+
+/* PoissonLHSNew (poisson.c:600-1507) assembled as CSR, columns in the
+ * reference's CP,EP,WP,NP,SP,TP,BP,NE,SE,NW,SW,TN,BN,TS,BS,TE,BE,TW,BW order.
+ * Returns nnz, or -1 if cap is too small. */
+int orc_lhs_csr(const orc_level *L, int *rowptr, int *cols, double *vals, int cap);
+/* y = A x with the CSR from orc_lhs_csr. */
+void orc_csr_mult(int n, const int *rowptr, const int *cols, const double *vals,
+                  const double *x, double *y);
+/* PoissonRHS (poisson.c:1509-1576); returns the printed compatibility sum. */
+double orc_poisson_rhs(const orc_level *L, const double *ucont, double dt, double st, double *b);
+/* VolumeFlux_rev (poisson.c:3712-3944); ucont updated in place. */
+void orc_volume_flux_rev(const orc_level *L, double *ucont, double flux_intp_sum, int flg,
+                         double *flux_out, double *area_out);
+/* MyNvertRestriction (poisson.c:1662-1773): coarse nvert from fine nvert. */
+void orc_nvert_restrict(const orc_level *fine, int coarse_mx, int coarse_my, int coarse_mz,
+                        int coarse_is_level0, int isc, int jsc, int ksc, double *nvert_c);
+/* FullyBlocked (poisson.c:1578-1660): returns multinullspace; fills KSKE[2*mx*my]. */
+int orc_fully_blocked(const orc_level *L, int *kske);
+/* MyRestriction (poisson.c:129-226). */
+void orc_restrict(const orc_level *fine, const orc_level *coarse, const double *xf, double *fc);
+/* MyInterpolation (poisson.c:265-370). */
+void orc_interpolate(const orc_level *coarse, const orc_level *fine, const double *xc, double *ff);
+/* PoissonNullSpaceFunction (poisson.c:372-563) in place. */
+void orc_nullspace(const orc_level *L, int multinullspace, const int *kske, double *x);
+/* UpdatePressure (poisson.c:2908-3248): p += phi and the periodic ring copies
+ * of p and phi. */
+void orc_update_pressure(const orc_level *L, double *p, double *phi);
+/* Projection (poisson.c:2281-2900), flux correction part; reads phi with its
+ * periodic ring already filled (as after UpdatePressure). */
+void orc_projection(const orc_level *L, const double *phi, double dt, double st, double *ucont);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,279 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front-end of the CPU oracle (cvb_oracle.c).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+checker; the product library never imports it.  ``build()`` compiles the C
+restatement into oracle/_build/; ``build_reference()`` compiles the reference's
+own sources against the API shim into oracle/_ref/ when a reference checkout is
+present (oracle/build_ref.sh).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libcvboracle.so"
+REF_LIB = HERE / "_ref" / "libcvbref.so"
+REF_DIR = Path(os.environ.get("CVB_REFERENCE_DIR", "/root/reference"))
+
+_lib = None
+_ref = None
+
+
+def build(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    srcs = [s for s in (HERE / "cvb_oracle.c", HERE / "cvb_solver.c") if s.exists()]
+    if force or not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in srcs):
+        cmd = ["gcc", "-std=gnu99", "-O3", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+               "-o", str(LIB)] + [str(s) for s in srcs] + ["-lm"]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+def build_reference() -> Path | None:
+    if not (REF_DIR / "poisson.c").exists():
+        return None
+    subprocess.run(["bash", str(HERE / "build_ref.sh"), str(REF_DIR)], check=True,
+                   stdout=subprocess.DEVNULL)
+    return REF_LIB
+
+
+class Level(ctypes.Structure):
+    _fields_ = [("mx", ctypes.c_int), ("my", ctypes.c_int), ("mz", ctypes.c_int),
+                ("bctype", ctypes.c_int * 6),
+                ("isc", ctypes.c_int), ("jsc", ctypes.c_int), ("ksc", ctypes.c_int)] + [
+        (n, ctypes.c_void_p) for n in ("icsi", "ieta", "izet", "jcsi", "jeta", "jzet",
+                                       "kcsi", "keta", "kzet", "iaj", "jaj", "kaj", "aj",
+                                       "csi", "eta", "zet", "nvert")]
+
+
+_FIELD_OF = {"icsi": "ICsi", "ieta": "IEta", "izet": "IZet", "jcsi": "JCsi", "jeta": "JEta",
+             "jzet": "JZet", "kcsi": "KCsi", "keta": "KEta", "kzet": "KZet", "iaj": "IAj",
+             "jaj": "JAj", "kaj": "KAj", "aj": "Aj", "csi": "Csi", "eta": "Eta", "zet": "Zet"}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(str(build()))
+        P = ctypes.c_void_p
+        L = ctypes.POINTER(Level)
+        _lib.orc_lhs_csr.argtypes = [L, P, P, P, ctypes.c_int]
+        _lib.orc_csr_mult.argtypes = [ctypes.c_int, P, P, P, P, P]
+        _lib.orc_poisson_rhs.argtypes = [L, P, ctypes.c_double, ctypes.c_double, P]
+        _lib.orc_poisson_rhs.restype = ctypes.c_double
+        _lib.orc_volume_flux_rev.argtypes = [L, P, ctypes.c_double, ctypes.c_int, P, P]
+        _lib.orc_nvert_restrict.argtypes = [L] + [ctypes.c_int] * 7 + [P]
+        _lib.orc_fully_blocked.argtypes = [L, P]
+        _lib.orc_restrict.argtypes = [L, L, P, P]
+        _lib.orc_interpolate.argtypes = [L, L, P, P]
+        _lib.orc_nullspace.argtypes = [L, ctypes.c_int, P, P]
+        _lib.orc_update_pressure.argtypes = [L, P, P]
+        _lib.orc_projection.argtypes = [L, P, ctypes.c_double, ctypes.c_double, P]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OLevel:
+    """One multigrid level handed to the oracle (keeps its arrays alive)."""
+
+    def __init__(self, metrics: dict, nvert: np.ndarray, bctype, semi=(0, 0, 0)):
+        self.keep = {}
+        mz, my, mx = nvert.shape
+        self.s = Level()
+        self.s.mx, self.s.my, self.s.mz = mx, my, mz
+        for q in range(6):
+            self.s.bctype[q] = int(bctype[q])
+        self.s.isc, self.s.jsc, self.s.ksc = (int(v) for v in semi)
+        for f, name in _FIELD_OF.items():
+            a = np.ascontiguousarray(metrics[name], dtype=np.float64)
+            self.keep[f] = a
+            setattr(self.s, f, _p(a))
+        self.set_nvert(nvert)
+        self.shape = (mz, my, mx)
+
+    def set_nvert(self, nvert):
+        a = np.ascontiguousarray(nvert, dtype=np.float64)
+        self.keep["nvert"] = a
+        self.s.nvert = _p(a)
+
+    @property
+    def nvert(self):
+        return self.keep["nvert"]
+
+    def ref(self):
+        return ctypes.byref(self.s)
+
+
+def lhs_csr(L: OLevel):
+    import scipy.sparse as sp
+    n = int(np.prod(L.shape))
+    cap = 19 * n + 16
+    rp = np.zeros(n + 1, np.int32)
+    cols = np.zeros(cap, np.int32)
+    vals = np.zeros(cap)
+    nnz = lib().orc_lhs_csr(L.ref(), _p(rp), _p(cols), _p(vals), cap)
+    if nnz < 0:
+        raise RuntimeError("orc_lhs_csr: capacity")
+    return sp.csr_matrix((vals[:nnz].copy(), cols[:nnz].copy(), rp.copy()), shape=(n, n))
+
+
+def poisson_rhs(L: OLevel, ucont, dt, st):
+    b = np.zeros(L.shape)
+    uc = np.ascontiguousarray(ucont, dtype=np.float64)
+    s = lib().orc_poisson_rhs(L.ref(), _p(uc), dt, st, _p(b))
+    return b, s
+
+
+def volume_flux_rev(L: OLevel, ucont, flux_intp_sum=0.0, flg=1):
+    uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+    f = ctypes.c_double()
+    a = ctypes.c_double()
+    lib().orc_volume_flux_rev(L.ref(), _p(uc), flux_intp_sum, flg, ctypes.byref(f), ctypes.byref(a))
+    return uc, f.value, a.value
+
+
+def nvert_restrict(F: OLevel, coarse_shape, coarse_is_level0, semi=(0, 0, 0)):
+    mz, my, mx = coarse_shape
+    out = np.zeros(coarse_shape)
+    lib().orc_nvert_restrict(F.ref(), mx, my, mz, int(coarse_is_level0), *[int(v) for v in semi], _p(out))
+    return out
+
+
+def fully_blocked(L: OLevel):
+    mz, my, mx = L.shape
+    k = np.zeros(2 * mx * my, np.int32)
+    mns = lib().orc_fully_blocked(L.ref(), _p(k))
+    return bool(mns), k
+
+
+def restrict(F: OLevel, C: OLevel, xf):
+    x = np.ascontiguousarray(xf, dtype=np.float64)
+    out = np.zeros(C.shape)
+    lib().orc_restrict(F.ref(), C.ref(), _p(x), _p(out))
+    return out
+
+
+def interpolate(C: OLevel, F: OLevel, xc):
+    x = np.ascontiguousarray(xc, dtype=np.float64)
+    out = np.zeros(F.shape)
+    lib().orc_interpolate(C.ref(), F.ref(), _p(x), _p(out))
+    return out
+
+
+def nullspace(L: OLevel, x, mns=False, kske=None):
+    y = np.array(x, dtype=np.float64, copy=True, order="C")
+    k = np.zeros(2, np.int32) if kske is None else np.ascontiguousarray(kske, dtype=np.int32)
+    lib().orc_nullspace(L.ref(), int(mns), _p(k), _p(y))
+    return y
+
+
+def update_and_project(L: OLevel, p, phi, ucont, dt, st):
+    pp = np.array(p, dtype=np.float64, copy=True, order="C")
+    ph = np.array(phi, dtype=np.float64, copy=True, order="C")
+    uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+    lib().orc_update_pressure(L.ref(), _p(pp), _p(ph))
+    lib().orc_projection(L.ref(), _p(ph), dt, st, _p(uc))
+    return pp, ph, uc
+
+
+# ------------------------------------------------------------------ reference
+class Reference:
+    """The reference's own routines, compiled against the API shim (oracle/_ref/)."""
+
+    def __init__(self, nodes, nlevels, bctype, semi=(0, 0, 0)):
+        global _ref
+        if _ref is None:
+            path = build_reference()
+            if path is None:
+                raise FileNotFoundError("reference checkout not present")
+            _ref = ctypes.CDLL(str(path))
+        self.L = _ref
+        KM, JM, IM = nodes.shape[:3]
+        bc = (ctypes.c_int * 6)(*[int(v) for v in bctype])
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        rc = self.L.ref_init(nlevels, IM, JM, KM, bc, *[int(v) for v in semi], _p(self.nodes))
+        if rc:
+            raise RuntimeError("ref_init failed")
+        self.nlevels = nlevels
+
+    def shape(self, level):
+        mx, my, mz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.L.ref_dims(level, ctypes.byref(mx), ctypes.byref(my), ctypes.byref(mz))
+        return (mz.value, my.value, mx.value)
+
+    def field(self, level, name, dof=1):
+        sh = self.shape(level) + ((3,) if dof == 3 else ())
+        out = np.zeros(sh)
+        if self.L.ref_get_field(level, name.encode(), _p(out)):
+            raise KeyError(name)
+        return out
+
+    def set_nvert(self, level, nv):
+        a = np.ascontiguousarray(nv, dtype=np.float64)
+        self.L.ref_set_nvert(level, _p(a))
+
+    def set_ucont(self, uc):
+        a = np.ascontiguousarray(uc, dtype=np.float64)
+        self.L.ref_set_ucont(_p(a))
+
+    def nvert_restrict(self):
+        mz, my, mx = self.shape(0)
+        mns = ctypes.c_int()
+        k = np.zeros(2 * mx * my, np.int32)
+        self.L.ref_nvert_restrict(ctypes.byref(mns), _p(k))
+        return bool(mns.value), k
+
+    def lhs_csr(self, level):
+        import scipy.sparse as sp
+        n = int(np.prod(self.shape(level)))
+        cap = 19 * n + 16
+        rp = np.zeros(n + 1, np.int32)
+        cols = np.zeros(cap, np.int32)
+        vals = np.zeros(cap)
+        nnz = self.L.ref_lhs(level, _p(rp), _p(cols), _p(vals), cap)
+        return sp.csr_matrix((vals[:nnz].copy(), cols[:nnz].copy(), rp.copy()), shape=(n, n))
+
+    def volume_flux(self, ucont, flux_intp_sum=0.0, flg=1):
+        uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+        f, a = ctypes.c_double(), ctypes.c_double()
+        self.L.ref_volume_flux(ctypes.c_double(flux_intp_sum), flg, _p(uc), ctypes.byref(f), ctypes.byref(a))
+        return uc, f.value, a.value
+
+    def rhs(self, dt, st):
+        b = np.zeros(self.shape(self.nlevels - 1))
+        s = ctypes.c_double()
+        self.L.ref_rhs(ctypes.c_double(dt), ctypes.c_double(st), _p(b), ctypes.byref(s))
+        return b, s.value
+
+    def restrict(self, coarse, xf):
+        x = np.ascontiguousarray(xf, dtype=np.float64)
+        out = np.zeros(self.shape(coarse))
+        self.L.ref_restrict(coarse, _p(x), _p(out))
+        return out
+
+    def interpolate(self, fine, xc):
+        x = np.ascontiguousarray(xc, dtype=np.float64)
+        out = np.zeros(self.shape(fine))
+        self.L.ref_interpolate(fine, _p(x), _p(out))
+        return out
+
+    def nullspace(self, level, x):
+        y = np.array(x, dtype=np.float64, copy=True, order="C")
+        self.L.ref_nullspace(level, _p(y))
+        return y
+
+    def update_and_project(self, p, phi, ucont, dt, st):
+        pp = np.array(p, dtype=np.float64, copy=True, order="C")
+        ph = np.array(phi, dtype=np.float64, copy=True, order="C")
+        uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+        self.L.ref_update_and_project(ctypes.c_double(dt), ctypes.c_double(st), _p(pp), _p(ph), _p(uc))
+        return pp, ph, uc

@@ -1,0 +1,48 @@
+"""Small deterministic scenarios shared by the parity tests and the fixture script."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+
+from curvib_old_gb300 import workload as W
+
+# name -> (cells, periodic (x,y,z), spheres, levels, semi-coarsening (i,j,k), y-stretch, slab)
+SCENARIOS = {
+    "box_sphere": ((12, 12, 12), (0, 0, 0), [(0.5, 0.5, 0.5, 0.3)], 3, (0, 0, 0), 2.0, False),
+    "channel_periodic": ((16, 8, 8), (1, 0, 1), [(0.4, 0.5, 0.5, 0.25)], 2, (0, 0, 0), 2.5, False),
+    "ksemi_sphere": ((12, 12, 12), (0, 0, 0), [(0.45, 0.5, 0.55, 0.3)], 2, (0, 0, 1), 2.0, False),
+    "blocked_slab": ((8, 8, 8), (0, 0, 0), [], 2, (0, 0, 0), 1.0, True),
+    "triply_periodic": ((8, 8, 8), (1, 1, 1), [], 2, (0, 0, 0), 1.0, False),
+}
+
+
+def bctype_of(per):
+    return [7 if per[0] else 1] * 2 + [7 if per[1] else 1] * 2 + [7 if per[2] else 1] * 2
+
+
+def build(name, nodes=None):
+    """Inputs of one scenario: nodes, bctype, per-level metrics, fine nvert, fluxes."""
+    cells, per, spheres, nl, semi, beta, slab = SCENARIOS[name]
+    per = tuple(bool(p) for p in per)
+    if nodes is None:
+        nodes = W.box_nodes(cells, (1.0, 1.0, 1.0), beta, True)
+    coords = W.level_coordinates(nodes, nl, semi)
+    mets = [W.form_metrics(c, per) for c in coords]
+    nvf = W.sphere_nvert(mets[-1]["Cent"], spheres)
+    if slab:
+        # a solid plate across the whole x-y section: every k-line is blocked
+        mz = nvf.shape[0]
+        nvf[mz // 2 - 2:mz // 2 + 2, 1:-1, 1:-1] = W.SOLID_CODE
+    uc = W.ucont_from_velocity(mets[-1], W.taylor_green, per)
+    return dict(nodes=nodes, bctype=bctype_of(per), per=per, nl=nl, semi=semi, metrics=mets,
+                nvert=nvf, ucont=uc)
+
+
+def digest(a) -> str:
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.tobytes()).hexdigest()[:32]
+
+
+def seeded(shape, seed):
+    return np.random.default_rng(seed).standard_normal(shape)

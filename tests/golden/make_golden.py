@@ -1,0 +1,83 @@
+"""Generate the golden fixtures from the reference's own routines.
+
+Runs CURVIB's poisson.c / metrics.c / implicitsolver.c, compiled unmodified
+against the single-process PETSc API shim (oracle/build_ref.sh), on the small
+scenarios of tests/cases.py and records SHA-256 digests of every output.  The
+inputs (node coordinates, nvert, fluxes) are stored beside the digests so the
+tests do not depend on the platform's sin/tanh.  Needs the reference checkout
+(default /root/reference, or CVB_REFERENCE_DIR); the fixtures it writes are
+committed and the tests read only those.
+
+usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+from cases import SCENARIOS, build, digest, seeded  # noqa: E402
+from curvib_old_gb300 import workload as W  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+DT, ST = 1e-3, 1.0
+
+
+def csr_digest(A):
+    A = A.tocsr().copy()
+    A.sort_indices()
+    return {"indptr": digest(A.indptr.astype(np.int64)), "indices": digest(A.indices.astype(np.int64)),
+            "data": digest(A.data), "nnz": int(A.nnz)}
+
+
+def run(name):
+    c = build(name)
+    nl = c["nl"]
+    R = O.Reference(c["nodes"], nl, c["bctype"], c["semi"])
+    rec = {"metrics": [], "nvert": [], "lhs": []}
+    for l in range(nl):
+        rec["metrics"].append({nm: digest(R.field(l, nm, 3 if nm in W.METRIC_NAMES else 1))
+                               for nm in W.METRIC_NAMES + W.JACOBIAN_NAMES})
+    R.set_nvert(nl - 1, c["nvert"])
+    mns, kske = R.nvert_restrict()
+    rec["multinullspace"] = bool(mns)
+    mz, my, mx = R.shape(0)
+    rec["kske"] = digest(kske.reshape(my, mx, 2)[1:-1, 1:-1, 0].astype(np.int64)) if mns else None
+    for l in range(nl):
+        rec["nvert"].append(digest(R.field(l, "Nvert")))
+        rec["lhs"].append(csr_digest(R.lhs_csr(l)))
+    uc, f, a = R.volume_flux(c["ucont"], 0.0, 1)
+    rec["volume_flux"] = {"ucont": digest(uc), "flux": repr(f), "area": repr(a)}
+    R.set_ucont(uc)
+    b, s = R.rhs(DT, ST)
+    rec["rhs"] = {"b": digest(b), "compat_sum": repr(s)}
+    rec["restrict"], rec["interpolate"], rec["nullspace"] = [], [], []
+    for l in range(1, nl):
+        rec["restrict"].append(digest(R.restrict(l - 1, seeded(R.shape(l), 100 + l))))
+        rec["interpolate"].append(digest(R.interpolate(l, seeded(R.shape(l - 1), 200 + l))))
+    for l in range(nl):
+        rec["nullspace"].append(digest(R.nullspace(l, seeded(R.shape(l), 300 + l))))
+    fine = R.shape(nl - 1)
+    p, phi, u2 = R.update_and_project(seeded(fine, 400), seeded(fine, 401), uc, DT, ST)
+    rec["update_project"] = {"p": digest(p), "phi": digest(phi), "ucont": digest(u2)}
+    np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
+    return rec
+
+
+def main():
+    out = {"dt": DT, "st": ST, "scenarios": {}}
+    for name in SCENARIOS:
+        out["scenarios"][name] = run(name)
+        print(name, "ok")
+    (OUT / "reference_digests.json").write_text(json.dumps(out, indent=1, sort_keys=True))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,127 @@
+"""The CPU oracle and the workload generator against the reference's own outputs.
+
+The digests in tests/golden/reference_digests.json were produced by the
+reference's poisson.c / metrics.c / implicitsolver.c compiled unmodified against
+a single-process PETSc API shim (tests/golden/make_golden.py).  Everything here
+must agree bit for bit: masks, index maps and FP64 values alike.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from cases import SCENARIOS, build, digest, seeded
+from curvib_old_gb300 import workload as W
+from oracle import oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+REF = json.loads((GOLD / "reference_digests.json").read_text())
+
+
+def csr_digest(A):
+    A = A.tocsr().copy()
+    A.sort_indices()
+    return {"indptr": digest(A.indptr.astype(np.int64)), "indices": digest(A.indices.astype(np.int64)),
+            "data": digest(A.data), "nnz": int(A.nnz)}
+
+
+def _setup(name):
+    z = np.load(GOLD / f"{name}.npz")
+    c = build(name, nodes=z["nodes"])
+    c["nvert"], c["ucont"] = z["nvert"], z["ucont"]
+    return c
+
+
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_metrics_generator_matches_reference(name):
+    c = _setup(name)
+    for l, m in enumerate(c["metrics"]):
+        for nm in W.METRIC_NAMES + W.JACOBIAN_NAMES:
+            assert digest(m[nm]) == REF["scenarios"][name]["metrics"][l][nm], (l, nm)
+
+
+def _levels(c):
+    nl, semi, bct = c["nl"], c["semi"], c["bctype"]
+    Ls = [None] * nl
+    Ls[-1] = O.OLevel(c["metrics"][-1], c["nvert"], bct, semi)
+    for l in range(nl - 2, -1, -1):
+        nvc = O.nvert_restrict(Ls[l + 1], c["metrics"][l]["Aj"].shape, l == 0, semi)
+        Ls[l] = O.OLevel(c["metrics"][l], nvc, bct, semi)
+    return Ls
+
+
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_oracle_matches_reference(name):
+    c = _setup(name)
+    ref = REF["scenarios"][name]
+    dt, st = REF["dt"], REF["st"]
+    Ls = _levels(c)
+    nl = c["nl"]
+    for l in range(nl):
+        assert digest(Ls[l].nvert) == ref["nvert"][l], ("nvert", l)
+        assert csr_digest(O.lhs_csr(Ls[l])) == ref["lhs"][l], ("lhs", l)
+    mns, kske = O.fully_blocked(Ls[0])
+    assert mns == ref["multinullspace"]
+    if mns:
+        mz, my, mx = Ls[0].shape
+        assert digest(kske.reshape(my, mx, 2)[1:-1, 1:-1, 0].astype(np.int64)) == ref["kske"]
+    uc, f, a = O.volume_flux_rev(Ls[-1], c["ucont"], 0.0, 1)
+    assert digest(uc) == ref["volume_flux"]["ucont"]
+    assert repr(f) == ref["volume_flux"]["flux"] and repr(a) == ref["volume_flux"]["area"]
+    b, s = O.poisson_rhs(Ls[-1], uc, dt, st)
+    assert digest(b) == ref["rhs"]["b"] and repr(s) == ref["rhs"]["compat_sum"]
+    for l in range(1, nl):
+        assert digest(O.restrict(Ls[l], Ls[l - 1], seeded(Ls[l].shape, 100 + l))) == ref["restrict"][l - 1]
+        assert digest(O.interpolate(Ls[l - 1], Ls[l], seeded(Ls[l - 1].shape, 200 + l))) == \
+            ref["interpolate"][l - 1]
+    for l in range(nl):
+        y = O.nullspace(Ls[l], seeded(Ls[l].shape, 300 + l), mns if l == 0 else False, kske)
+        assert digest(y) == ref["nullspace"][l], ("nullspace", l)
+    fine = Ls[-1].shape
+    p, phi, u2 = O.update_and_project(Ls[-1], seeded(fine, 400), seeded(fine, 401), uc, dt, st)
+    assert digest(p) == ref["update_project"]["p"]
+    assert digest(phi) == ref["update_project"]["phi"]
+    assert digest(u2) == ref["update_project"]["ucont"]
+
+
+@pytest.mark.parametrize("name", ["box_sphere", "channel_periodic"])
+def test_operator_invariants(name):
+    """A 1 = 0 on fluid rows (right null vector) and (1/aj)^T A = 0 (left null vector)."""
+    c = _setup(name)
+    L = _levels(c)[-1]
+    A = O.lhs_csr(L)
+    nv = L.nvert
+    fluid = np.zeros(nv.shape, bool)
+    fluid[1:-1, 1:-1, 1:-1] = nv[1:-1, 1:-1, 1:-1] < 0.1
+    one = fluid.astype(float).ravel()
+    r = (A @ one).reshape(nv.shape)
+    scale = np.abs(A.diagonal()).max()
+    assert np.abs(r[fluid]).max() < 1e-11 * scale
+    w = np.where(fluid, 1.0 / c["metrics"][-1]["Aj"], 0.0).ravel()
+    lt = (A.T @ w).reshape(nv.shape)
+    assert np.abs(lt[fluid]).max() < 1e-11 * np.abs(w).max() * scale / np.abs(c["metrics"][-1]["Aj"]).min()
+
+
+@pytest.mark.skipif(not (O.REF_DIR / "poisson.c").exists(), reason="reference checkout not present")
+def test_oracle_matches_live_reference_random_grid():
+    """A grid not in the fixtures, run through the reference itself."""
+    cells, per, nl = (10, 14, 6), (True, False, False), 2
+    nodes = W.box_nodes(cells, (2.0, 1.0, 0.5), 1.5, True)
+    bct = [7, 7, 1, 1, 1, 1]
+    coords = W.level_coordinates(nodes, nl)
+    mets = [W.form_metrics(x, per) for x in coords]
+    nvf = W.sphere_nvert(mets[-1]["Cent"], [(1.0, 0.4, 0.25, 0.2)])
+    R = O.Reference(nodes, nl, bct)
+    for l in range(nl):
+        for nm in ("IAj", "ICsi", "KZet", "Aj"):
+            assert np.array_equal(R.field(l, nm, 3 if nm in W.METRIC_NAMES else 1), mets[l][nm])
+    R.set_nvert(nl - 1, nvf)
+    R.nvert_restrict()
+    Lf = O.OLevel(mets[-1], nvf, bct)
+    Lc = O.OLevel(mets[0], O.nvert_restrict(Lf, mets[0]["Aj"].shape, True), bct)
+    assert np.array_equal(R.field(0, "Nvert"), Lc.nvert)
+    for l, L in ((0, Lc), (1, Lf)):
+        d = R.lhs_csr(l) - O.lhs_csr(L)
+        d.eliminate_zeros()
+        assert d.nnz == 0
