@@ -1,0 +1,344 @@
+"""Benchmark: pressure-Poisson solves/s and p50/p99 latency, mixed vs plain FP64.
+
+Workload (default): the channel solve -- 256x128x128 cells, periodic in x and z,
+walls in y with tanh stretching 2.5, no body, RHS the divergence of a seeded
+smoothed Gaussian velocity (sigma 0.1, 3 Jacobi passes) made compatible;
+FGMRES + geometric multigrid to a relative residual of 1e-10.  One step is one
+solve of the resident right-hand side.  The headline `value` is the mixed
+(FP32 V-cycle in FP64 FGMRES) path; the plain FP64 path is timed beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cvb|reference]
+
+--impl reference times the reference's algorithm on the host cores (the CPU
+restatement of PoissonSolver_MG's FGMRES + PCMG with block-Jacobi ILU(0)
+Richardson smoothing), on the same workload.  Under torchrun (N > 1) every rank
+solves its own copy of the workload (replicas); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "solves/s & p50/p99 latency at 1e-8 rel residual, mixed vs plain FP64, 1 GB300"
+RTOL = 1e-10
+DT, ST = 1e-3, 1.0
+CPU_LEVELS = 5  # the multigrid depth the reference's run deck uses for this workload
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cvb", choices=["cvb", "reference"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "box64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as td
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        td.init_process_group("nccl" if args.impl == "cvb" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def max_over_ranks(ws, v, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def problem(args):
+    from curvib_old_gb300 import workload as W
+    if args.workload == "box64":
+        return W.config0_problem(64), "box 64^3 on [0,1]^3, tanh 2.0 in y, distorted, sphere r=0.15 (config 0)"
+    return W.config1_problem(), ("channel 256x128x128 cells on 2pi x 2 x pi, periodic x,z, walls in y with "
+                                 "tanh 2.5, no body, seeded smoothed-Gaussian divergence RHS (config 1)")
+
+
+def rhs_on_gpu(ctx, P):
+    """VolumeFlux_rev + PoissonRHS on the device, then made compatible."""
+    from curvib_old_gb300 import workload as W
+    uc, _, _ = ctx.volume_flux_rev(P.ucont, 0.0, 1)
+    b, _ = ctx.poisson_rhs(uc, DT, ST)
+    return W.compatible(b, P.metrics[-1]["Aj"], P.nvert)
+
+
+def rhs_on_cpu(Ls, P):
+    from curvib_old_gb300 import workload as W
+    from oracle import oracle as O
+    uc, _, _ = O.volume_flux_rev(Ls[-1], P.ucont, 0.0, 1)
+    b, _ = O.poisson_rhs(Ls[-1], uc, DT, ST)
+    return W.compatible(b, P.metrics[-1]["Aj"], P.nvert)
+
+
+class Clocks:
+    """nvidia-smi samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel, cells):
+    """DRAM bytes per launch from the committed ncu summary, scaled to `cells`."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text()).get(kernel)
+    if not d:
+        return None
+    return d["dram_bytes_per_launch"] * cells / d["cells"]
+
+
+def run_cvb(args, ws, rank, local):
+    import torch
+
+    from curvib_old_gb300 import _lib
+    from curvib_old_gb300.solver import PoissonContext
+    torch.cuda.set_device(local)
+    P, desc = problem(args)
+    ctx = PoissonContext(local).setup(P)
+    b = rhs_on_gpu(ctx, P)
+    n_unknown = P.unknowns
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+
+    # resident rhs: one host->device copy through the C ABI, then solves from HBM
+    phi, st0 = ctx.solve(b, precision=_lib.MIXED, rtol=RTOL)
+
+    def timed(precision, steps, warmup, clocks=False):
+        for _ in range(warmup):
+            ctx.solve_resident(precision=precision, rtol=RTOL)
+        barrier(ws)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lat, its, rr = [], [], []
+        launches0 = _lib.lib().cvb_kernel_launches()
+        cl = Clocks(local) if clocks else None
+        if cl:
+            cl.__enter__()
+        e0.record(stream)
+        for _ in range(steps):
+            s = ctx.solve_resident(precision=precision, rtol=RTOL)
+            lat.append(s["device_ms"])
+            its.append(s["iterations"])
+            rr.append(s["rel_residual"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if cl:
+            cl.__exit__()
+        launches = _lib.lib().cvb_kernel_launches() - launches0
+        barrier(ws)
+        ms = max_over_ranks(ws, e0.elapsed_time(e1), torch.device("cuda", local))
+        return ms, lat, its, rr, launches, (cl.summary() if cl else None)
+
+    ms_m, lat_m, its_m, rr_m, launches, clocks = timed(_lib.MIXED, args.steps, args.warmup, clocks=True)
+    ms_d, lat_d, its_d, rr_d, _, _ = timed(_lib.FP64, args.steps, max(1, args.warmup))
+
+    # end to end through the C ABI with pinned host buffers: H2D of b, solve, D2H of phi
+    hb = torch.empty(b.shape, dtype=torch.float64, pin_memory=True)
+    hb.numpy()[...] = b
+    hphi = torch.zeros(b.shape, dtype=torch.float64, pin_memory=True)
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(2):
+        ctx.solve(hb.numpy(), precision=_lib.MIXED, rtol=RTOL)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    o = _lib.default_opts(precision=_lib.MIXED, rtol=RTOL)
+    stt = _lib.SolveStats()
+    hb_p, hphi_p = _lib.ptr(hb.numpy()), _lib.ptr(hphi.numpy())
+    for _ in range(e2e_steps):
+        rc = _lib.lib().cvb_poisson_solve(ctx._ctx, hb_p, hphi_p, ctypes.byref(o), ctypes.byref(stt))
+        assert rc == 0, rc
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    e2e_ms = max_over_ranks(ws, max(e0.elapsed_time(e1), wall * 1e3), torch.device("cuda", local))
+
+    # roofline of the dominant kernel: the fused FP32 line sweep on the finest level
+    k_ms, k_bytes = ctx.time_kernel("line_sweep_f32", level=-1, reps=30)
+    k64_ms, k64_bytes = ctx.time_kernel("residual_f64", level=-1, reps=30)
+    peak, peak_kind = peaks()
+    cells = int(np.prod(ctx.shapes[-1]))
+    roof = {"kernel": "k_line_sweep<float,32> (fused residual + y-line Thomas), finest level",
+            "bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
+            "traffic": traffic_per_launch("line_sweep_f32", cells), "algorithmic_bytes": k_bytes,
+            "avg_launch_ms": k_ms,
+            "fp64_residual": {"achieved_gbs": k64_bytes / (k64_ms * 1e-3) / 1e9, "avg_launch_ms": k64_ms,
+                              "algorithmic_bytes": k64_bytes}}
+    ctx.close()
+
+    value = ws * args.steps / (ms_m * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32 (FP32 V-cycle inside FP64 FGMRES)", "data": "synthetic",
+        "config": {"workload": desc, "unknowns": n_unknown, "levels": len(P.metrics), "rtol": RTOL,
+                   "solver": "FGMRES(30) + V(2,2) y-line-Jacobi multigrid, dense FP64 coarsest",
+                   "l2": "no flush: the finest level's operator data alone (~1 GB FP64, ~0.3 GB FP32) exceeds L2",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "p50_ms": statistics.median(lat_m), "p99_ms": float(np.percentile(lat_m, 99)),
+        "iterations": statistics.median(its_m), "rel_residual": max(rr_m),
+        "unknown_iterations_per_s": ws * n_unknown * sum(its_m) / (ms_m * 1e-3),
+        "fp64": {"solves_per_s": ws * args.steps / (ms_d * 1e-3), "p50_ms": statistics.median(lat_d),
+                 "p99_ms": float(np.percentile(lat_d, 99)), "iterations": statistics.median(its_d),
+                 "rel_residual": max(rr_d)},
+        "mixed_over_fp64": ms_d / ms_m,
+        "roofline": roof,
+        "e2e": {"value": ws * e2e_steps / (e2e_ms * 1e-3), "unit": "solves/s",
+                "h2d_bytes_per_step": int(b.nbytes), "d2h_bytes_per_step": int(b.nbytes)},
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(P, b)
+    return out
+
+
+def cpu_levels(P):
+    from oracle import oracle as O
+    return O.levels_for(P, min(CPU_LEVELS, len(P.metrics)))
+
+
+def cpu_baseline(P, b):
+    """One full solve of the same workload with the reference's algorithm."""
+    from oracle import oracle as O
+    Ls = cpu_levels(P)
+    threads = os.cpu_count() or 1
+    x, its, rr, ts, tv = O.solve_mg(Ls, b, rtol=RTOL, max_it=400, threads=threads)
+    return {"value": 1.0 / tv, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"1 full solve of the same workload to rtol {RTOL:g}: FGMRES(30) + {len(Ls)}-level PCMG, "
+                      f"Richardson/block-Jacobi ILU(0) smoothing, {its} iterations, rel residual {rr:.2e}; "
+                      f"set-up (assembly + ILU) {ts:.2f} s not included",
+            "iterations": its, "setup_s": ts, "solve_s": tv}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    P, desc = problem(args)
+    Ls = cpu_levels(P)
+    b = rhs_on_cpu(Ls, P)
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    _, its0, rr0, ts, tv0 = O.solve_mg(Ls, b, rtol=RTOL, max_it=400, threads=threads)  # warm-up (1 solve)
+    budget_s = 150.0
+    steps = max(1, min(args.steps, int(budget_s / max(tv0, 1e-3))))
+    lat, its = [], []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        _, it, rr, _, tv = O.solve_mg(Ls, b, rtol=RTOL, max_it=400, threads=threads)
+        lat.append(tv * 1e3)
+        its.append(it)
+    wall = time.perf_counter() - t0
+    value = steps / wall
+    return {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": steps,
+            "warmup": 1, "ms_per_step": wall * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": desc, "unknowns": P.unknowns, "levels": len(Ls), "rtol": RTOL,
+                       "solver": "FGMRES(30) + PCMG V-cycle, Richardson/block-Jacobi ILU(0) (reference algorithm)"},
+            "p50_ms": statistics.median(lat), "p99_ms": float(np.percentile(lat, 99)),
+            "iterations": statistics.median(its),
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} full solves (capped to ~{budget_s:.0f} s), set-up {ts:.2f} s "
+                                       "excluded; the reference's PETSc build is absent, its algorithm runs "
+                                       "as the C restatement in oracle/"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        out = run_reference(args, ws, rank)
+    else:
+        out = run_cvb(args, ws, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+"""ctypes view of libcvb.so (include/cvb.h).
+
+There is no fallback: if the CUDA library has not been built, or no GPU is
+present when a context is created, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_build" / "libcvb.so"
+_lib = None
+
+CVB_OK, CVB_NOT_CONVERGED, CVB_NAN_DETECTED, CVB_OOM, CVB_BAD_INPUT, CVB_TIMEOUT, CVB_CUDA_ERROR, \
+    CVB_NOT_SETUP = range(8)
+STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NAN_DETECTED", 3: "OOM", 4: "BAD_INPUT", 5: "TIMEOUT",
+                6: "CUDA_ERROR", 7: "NOT_SETUP"}
+FP64, MIXED = 0, 1
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("device", _I), ("stream", _P)]
+
+
+class LevelDesc(ctypes.Structure):
+    _fields_ = ([(n, _I) for n in ("mx", "my", "mz", "gxs", "gys", "gzs", "gxm", "gym", "gzm")]
+                + [("bctype", _I * 6), ("isc", _I), ("jsc", _I), ("ksc", _I)]
+                + [(n, _P) for n in ("icsi", "ieta", "izet", "jcsi", "jeta", "jzet", "kcsi", "keta", "kzet",
+                                     "iaj", "jaj", "kaj", "aj", "csi", "eta", "zet")])
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("precision", _I), ("rtol", _D), ("atol", _D), ("max_it", _I), ("restart", _I),
+                ("pre_sweeps", _I), ("post_sweeps", _I), ("omega", _D), ("project_rhs", _I),
+                ("warm_start", _I), ("coarse_dense_max", _I), ("cgs_refine", _I)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("status", _I), ("iterations", _I), ("restarts", _I), ("rel_residual", _D),
+                ("abs_residual", _D), ("rhs_norm", _D), ("rhs_projected", _D), ("device_ms", _D)]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["status_name"] = STATUS_NAMES.get(self.status, str(self.status))
+        return d
+
+
+EXPORTS = {
+    "cvb_solve_opts_default": ([_P], _I),
+    "cvb_init": ([_P, _P], _I),
+    "cvb_destroy": ([_P], None),
+    "cvb_last_error": ([_P], ctypes.c_char_p),
+    "cvb_setup_hierarchy": ([_P, _I, _P, _P], _I),
+    "cvb_set_nvert": ([_P, _P], _I),
+    "cvb_get_nvert": ([_P, _I, _P, _P], _I),
+    "cvb_level_dims": ([_P, _I, _P, _P, _P], _I),
+    "cvb_volume_flux_rev": ([_P, _P, _D, _I, _P, _P], _I),
+    "cvb_poisson_rhs": ([_P, _P, _D, _D, _P, _P], _I),
+    "cvb_poisson_solve": ([_P, _P, _P, _P, _P], _I),
+    "cvb_poisson_solver_mg": ([_P, _P, _D, _I, _D, _D, _P, _P, _P], _I),
+    "cvb_update_pressure": ([_P, _P, _P], _I),
+    "cvb_projection": ([_P, _P, _D, _D, _P], _I),
+    "cvb_device_rhs": ([_P], _P),
+    "cvb_device_phi": ([_P], _P),
+    "cvb_solve_resident": ([_P, _P, _P], _I),
+    "cvb_stream": ([_P], _P),
+    "cvb_apply_operator": ([_P, _I, _P, _P], _I),
+    "cvb_apply_operator_f32": ([_P, _I, _P, _P], _I),
+    "cvb_get_weights": ([_P, _I, _P], _I),
+    "cvb_restrict": ([_P, _I, _P, _P], _I),
+    "cvb_interpolate": ([_P, _I, _P, _P], _I),
+    "cvb_nullspace": ([_P, _I, _P], _I),
+    "cvb_kernel_launches": ([], ctypes.c_longlong),
+    "cvb_time_kernel": ([_P, _I, _I, _I, _P, _P], _I),
+}
+KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3}
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def lib():
+    """The loaded libcvb.so with argument types set; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise ImportError(f"{_LIB_PATH} is missing: run curvib_old_gb300.build.build() (nvcc, sm_103a)")
+        L = ctypes.CDLL(str(_LIB_PATH))
+        for name, (args, res) in EXPORTS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class CvbError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def default_opts(**kw) -> SolveOpts:
+    o = SolveOpts()
+    lib().cvb_solve_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o

@@ -1,0 +1,1026 @@
+// Host side of the cvb C ABI (include/cvb.h): device residency of one CURVIB
+// block's multigrid hierarchy, the V-cycle, FP64 FGMRES and the path's entry points.
+#include "../../include/cvb.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cvb_internal.h"
+
+using namespace cvb;
+
+namespace {
+
+constexpr int kMaxRestart = 64;
+
+struct LevelHost {
+  cvb_level_desc d;  // shapes / flags only (pointers are not kept)
+};
+
+}  // namespace
+
+struct cvb_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  std::vector<void *> allocs;
+
+  int nlevels = 0;
+  std::vector<LevelDev> L;       // 0 = coarsest
+  std::vector<LevelHost> H;
+  // per-level raw face metrics (kept for the finest level: Projection reads them)
+  std::vector<std::vector<double *>> fm;  // [level][9] Cmpnts arrays
+  std::vector<double *> iaj, jaj, kaj, aj64;
+  double *area3 = nullptr;       // finest: |csi|,|eta|,|zet| per cell ([3][N])
+  double *nvert_tmp = nullptr;
+  // coarsest-level solver
+  double *Minv = nullptr;
+  int ncoarse = 0;
+  bool coarse_dense = false;
+  int multinullspace = 0;
+  std::vector<int> kske;
+  // finest-level solver workspace
+  double *b = nullptr, *x = nullptr, *w = nullptr, *r = nullptr;
+  double *V[kMaxRestart + 1] = {};
+  double *Z64[kMaxRestart] = {};
+  float *Z32[kMaxRestart] = {};
+  float *b32 = nullptr;
+  double **dV = nullptr;  // device copies of the pointer tables
+  double **dZ64 = nullptr;
+  float **dZ32 = nullptr;
+  double *partial = nullptr, *sums = nullptr, *hdev = nullptr;
+  double *uc_dev = nullptr, *p_dev = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool ready = false;
+};
+
+// ------------------------------------------------------------------ helpers
+static int fail(cvb_ctx *c, int code, const char *fmt, ...) __attribute__((format(printf, 3, 4)));
+static int fail(cvb_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? CVB_OOM : CVB_CUDA_ERROR, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                          \
+  } while (0)
+
+#define CKL()                                                                                  \
+  do {                                                                                         \
+    cudaError_t e_ = cudaGetLastError();                                                       \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(ctx, CVB_CUDA_ERROR, "kernel launch: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                                   \
+  } while (0)
+
+#define TRY(expr)                  \
+  do {                             \
+    int s_ = (expr);               \
+    if (s_ != CVB_OK) return s_;   \
+  } while (0)
+
+template <typename T>
+static int dalloc(cvb_ctx *ctx, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, CVB_OOM, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
+  }
+  ctx->allocs.push_back((void *)*p);
+  return CVB_OK;
+}
+
+static void free_all(cvb_ctx *ctx) {
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (void *p : ctx->allocs) cudaFree(p);
+  ctx->allocs.clear();
+  ctx->L.clear();
+  ctx->H.clear();
+  ctx->fm.clear();
+  ctx->iaj.clear(); ctx->jaj.clear(); ctx->kaj.clear(); ctx->aj64.clear();
+  ctx->ready = false;
+}
+
+// Copy the owned box [0,mx)x[0,my)x[0,mz) out of a ghosted local array.
+static void extract_box(const cvb_level_desc &d, const double *src, int dof, std::vector<double> &out) {
+  size_t n = (size_t)d.mx * d.my * d.mz;
+  out.resize(n * dof);
+  for (int k = 0; k < d.mz; k++)
+    for (int j = 0; j < d.my; j++) {
+      const double *row = src + (((size_t)(k - d.gzs) * d.gym + (j - d.gys)) * d.gxm + (0 - d.gxs)) * dof;
+      std::memcpy(&out[((size_t)k * d.my + j) * d.mx * dof], row, sizeof(double) * d.mx * dof);
+    }
+}
+
+static int upload_box(cvb_ctx *ctx, const cvb_level_desc &d, const double *src, int dof, double **dst) {
+  std::vector<double> h;
+  extract_box(d, src, dof, h);
+  TRY(dalloc(ctx, dst, h.size()));
+  CK(cudaMemcpyAsync(*dst, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+static int check_desc(cvb_ctx *ctx, const cvb_level_desc &d, int level, bool finest) {
+  if (d.mx < 3 || d.my < 3 || d.mz < 3) return fail(ctx, CVB_BAD_INPUT, "level %d: box %dx%dx%d too small", level, d.mx, d.my, d.mz);
+  if (d.gxs > 0 || d.gys > 0 || d.gzs > 0 || d.gxs + d.gxm < d.mx || d.gys + d.gym < d.my || d.gzs + d.gzm < d.mz)
+    return fail(ctx, CVB_BAD_INPUT, "level %d: ghosted box does not cover the owned box", level);
+  const double *req[] = {d.icsi, d.ieta, d.izet, d.jcsi, d.jeta, d.jzet, d.kcsi, d.keta, d.kzet, d.iaj, d.jaj, d.kaj, d.aj};
+  for (const double *p : req)
+    if (!p) return fail(ctx, CVB_BAD_INPUT, "level %d: a metric array is NULL", level);
+  if (finest && (!d.csi || !d.eta || !d.zet)) return fail(ctx, CVB_BAD_INPUT, "finest level needs lCsi/lEta/lZet");
+  for (int a = 0; a < 3; a++) {
+    bool p0 = d.bctype[2 * a] == 7, p1 = d.bctype[2 * a + 1] == 7;
+    if (p0 != p1) return fail(ctx, CVB_BAD_INPUT, "level %d: direction %d is periodic on one side only", level, a);
+    int m = a == 0 ? d.mx : (a == 1 ? d.my : d.mz);
+    if (p0 && m - 2 < 3) return fail(ctx, CVB_BAD_INPUT, "level %d: periodic direction %d needs >= 3 cells", level, a);
+  }
+  return CVB_OK;
+}
+
+// Gauss-Jordan inverse with partial pivoting (coarsest level, n <= a few thousand).
+static bool dense_inverse(std::vector<double> &A, int n, std::vector<double> &Inv) {
+  Inv.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) Inv[(size_t)i * n + i] = 1.0;
+  for (int c = 0; c < n; c++) {
+    int piv = c;
+    double best = std::fabs(A[(size_t)c * n + c]);
+    for (int r = c + 1; r < n; r++) {
+      double v = std::fabs(A[(size_t)r * n + c]);
+      if (v > best) { best = v; piv = r; }
+    }
+    if (!(best > 0.0)) return false;
+    if (piv != c) {
+      for (int q = 0; q < n; q++) {
+        std::swap(A[(size_t)c * n + q], A[(size_t)piv * n + q]);
+        std::swap(Inv[(size_t)c * n + q], Inv[(size_t)piv * n + q]);
+      }
+    }
+    double inv = 1.0 / A[(size_t)c * n + c];
+    for (int q = 0; q < n; q++) { A[(size_t)c * n + q] *= inv; Inv[(size_t)c * n + q] *= inv; }
+    for (int r = 0; r < n; r++) {
+      if (r == c) continue;
+      double f = A[(size_t)r * n + c];
+      if (f == 0.0) continue;
+      double *ar = &A[(size_t)r * n], *ac = &A[(size_t)c * n];
+      double *ir = &Inv[(size_t)r * n], *ic = &Inv[(size_t)c * n];
+      for (int q = 0; q < n; q++) { ar[q] -= f * ac[q]; ir[q] -= f * ic[q]; }
+    }
+  }
+  return true;
+}
+
+// Rows of the coarsest operator, made nonsingular: M = A + sum_r u_r v_r^T with
+// v_r the indicator of fluid region r and u_r = s v_r.  A's left null vector on
+// region r is 1/aj there, which is not orthogonal to u_r, so M is invertible; for a
+// compatible right-hand side M^-1 b solves A e = b with zero region sums of e.
+static int build_coarse(cvb_ctx *ctx, const cvb_solve_opts *opt) {
+  LevelDev &C = ctx->L[0];
+  size_t n = C.g.n();
+  ctx->ncoarse = (int)n;
+  int dense_max = opt ? opt->coarse_dense_max : 2048;
+  ctx->coarse_dense = (int)n <= dense_max;
+  if (!ctx->coarse_dense) return CVB_OK;
+  std::vector<double> w(n * NSLOT), nv(n);
+  CK(cudaMemcpyAsync(w.data(), C.w64, sizeof(double) * n * NSLOT, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(nv.data(), C.nvert, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> A(n * n, 0.0);
+  const Geom &g = C.g;
+  double diag_sum = 0.0;
+  int nfl = 0;
+  std::vector<int> region(n, -1);
+  for (int k = 0; k < g.mz; k++)
+    for (int j = 0; j < g.my; j++)
+      for (int i = 0; i < g.mx; i++) {
+        size_t p = g.id(i, j, k);
+        bool interior = i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2;
+        if (!interior || nv[p] > 0.1) {
+          A[p * n + p] = 1.0;
+          continue;
+        }
+        int iu = g.iu(i), id = g.id_(i), ju = g.ju(j), jd = g.jd(j), ku = g.ku(k), kd = g.kd(k);
+        size_t c[NSLOT] = {g.id(i, j, k), g.id(iu, j, k), g.id(id, j, k), g.id(i, ju, k), g.id(i, jd, k),
+                           g.id(i, j, ku), g.id(i, j, kd), g.id(iu, ju, k), g.id(iu, jd, k), g.id(id, ju, k),
+                           g.id(id, jd, k), g.id(i, ju, ku), g.id(i, ju, kd), g.id(i, jd, ku), g.id(i, jd, kd),
+                           g.id(iu, j, ku), g.id(iu, j, kd), g.id(id, j, ku), g.id(id, j, kd)};
+        for (int m = 0; m < NSLOT; m++) A[p * n + c[m]] += w[(size_t)m * n + p];
+        diag_sum += std::fabs(A[p * n + p]);
+        nfl++;
+        int reg = 0;
+        if (ctx->multinullspace && k >= ctx->kske[2 * (j * g.mx + i)]) reg = 1;
+        region[p] = reg;
+      }
+  if (nfl > 0) {
+    double s = diag_sum / nfl;
+    for (int reg = 0; reg < 2; reg++) {
+      int cnt = 0;
+      for (size_t p = 0; p < n; p++) cnt += region[p] == reg;
+      if (!cnt) continue;
+      double sv = s / cnt;
+      for (size_t p = 0; p < n; p++) {
+        if (region[p] != reg) continue;
+        for (size_t q = 0; q < n; q++)
+          if (region[q] == reg) A[p * n + q] += sv;
+      }
+    }
+  }
+  std::vector<double> Inv;
+  if (!dense_inverse(A, (int)n, Inv)) return fail(ctx, CVB_BAD_INPUT, "coarsest operator is singular after regularisation");
+  if (!ctx->Minv) TRY(dalloc(ctx, &ctx->Minv, n * n));
+  CK(cudaMemcpyAsync(ctx->Minv, Inv.data(), sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+// nvert restriction down the hierarchy and the operator build of every level.
+static int build_operators(cvb_ctx *ctx) {
+  int nl = ctx->nlevels;
+  for (int l = nl - 2; l >= 0; l--) {
+    LevelDev &F = ctx->L[l + 1], &C = ctx->L[l];
+    launch_nvert_restrict(F.g, F.nvert, C.g, C.isc, C.jsc, C.ksc, C.nvert, ctx->nvert_tmp, ctx->stream);
+    CKL();
+  }
+  // FullyBlocked on the coarsest level (poisson.c:1578-1660)
+  {
+    LevelDev &C = ctx->L[0];
+    size_t n = C.g.n();
+    std::vector<double> nv(n);
+    CK(cudaMemcpyAsync(nv.data(), C.nvert, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const Geom &g = C.g;
+    ctx->kske.assign(2 * (size_t)g.mx * g.my, 0);
+    int all = 1;
+    for (int j = 1; j < g.my - 1; j++)
+      for (int i = 1; i < g.mx - 1; i++) {
+        int blocked = 0;
+        for (int k = 0; k < g.mz; k++)
+          if (nv[g.id(i, j, k)] > 0.1) {
+            int &ks = ctx->kske[2 * (j * g.mx + i)];
+            if (!blocked) { ks = k; blocked = 1; }
+            else ks = std::min(ks, k);
+          }
+        if (!blocked) all = 0;
+      }
+    ctx->multinullspace = all;
+  }
+  double *g9 = nullptr;
+  size_t nmax = 0;
+  for (auto &lv : ctx->L) nmax = std::max(nmax, lv.g.n());
+  TRY(dalloc(ctx, &g9, 9 * nmax));
+  for (int l = 0; l < nl; l++) {
+    LevelDev &lv = ctx->L[l];
+    const Geom &g = lv.g;
+    size_t n = g.n();
+    const double *m[9];
+    for (int q = 0; q < 9; q++) m[q] = ctx->fm[l][q];
+    launch_gcoef(g, m, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], g9, ctx->stream);
+    launch_codes(g, lv.nvert, lv.code, ctx->stream);
+    launch_weights(g, g9, ctx->aj64[l], lv.nvert, lv.code, lv.w64, ctx->stream);
+    launch_line_factors(g, lv.w64, lv.line64, lv.line32, ctx->stream);
+    launch_to_f32(g9, lv.gf32, 9 * n, ctx->stream);
+    launch_to_f32(ctx->aj64[l], lv.ajf32, n, ctx->stream);
+    CKL();
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  // g9 is a set-up temporary; return it to the pool
+  auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void *)g9);
+  if (it != ctx->allocs.end()) ctx->allocs.erase(it);
+  cudaFree(g9);
+  return CVB_OK;
+}
+
+// Fills the [3][N] face-area block |csi|, |eta|, |zet| used by VolumeFlux_rev.
+static void face_areas(const std::vector<double> &csi, const std::vector<double> &eta,
+                       const std::vector<double> &zet, std::vector<double> &a3) {
+  size_t n = csi.size() / 3;
+  a3.resize(3 * n);
+  const std::vector<double> *src[3] = {&csi, &eta, &zet};
+  for (int d = 0; d < 3; d++)
+    for (size_t p = 0; p < n; p++) {
+      const double *v = &(*src[d])[3 * p];
+      a3[d * n + p] = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    }
+}
+
+// ------------------------------------------------------------------ V-cycle
+template <typename T>
+static T *vptr(LevelDev &L, int which);
+// which: 0 rhs, 1 e, 2 e2, 3 res.  Layout of the per-level allocation: r=rhs, e=e, t=[e2|res]
+template <>
+float *vptr<float>(LevelDev &L, int which) {
+  size_t n = L.g.n();
+  switch (which) {
+    case 0: return L.r32;
+    case 1: return L.e32;
+    case 2: return L.t32;
+    default: return L.t32 + n;
+  }
+}
+template <>
+double *vptr<double>(LevelDev &L, int which) {
+  size_t n = L.g.n();
+  switch (which) {
+    case 0: return L.r64;
+    case 1: return L.e64;
+    case 2: return L.t64;
+    default: return L.t64 + n;
+  }
+}
+
+template <typename T>
+static void smooth(LevelDev &L, const T *b, T *&x, T *&x2, T omega, int sweeps, bool zero_first, cudaStream_t s);
+template <>
+void smooth<float>(LevelDev &L, const float *b, float *&x, float *&x2, float omega, int sweeps, bool zero_first,
+                   cudaStream_t s) {
+  for (int q = 0; q < sweeps; q++) {
+    bool z = zero_first && q == 0;
+    // residual goes to the res buffer, Thomas writes x2, then swap
+    LevelDev tmp = L;
+    tmp.t32 = vptr<float>(L, 3);
+    launch_line_smooth<float>(tmp, b, z ? nullptr : x, x2, omega, z, s);
+    std::swap(x, x2);
+  }
+}
+template <>
+void smooth<double>(LevelDev &L, const double *b, double *&x, double *&x2, double omega, int sweeps,
+                    bool zero_first, cudaStream_t s) {
+  for (int q = 0; q < sweeps; q++) {
+    bool z = zero_first && q == 0;
+    LevelDev tmp = L;
+    tmp.t64 = vptr<double>(L, 3);
+    launch_line_smooth<double>(tmp, b, z ? nullptr : x, x2, omega, z, s);
+    std::swap(x, x2);
+  }
+}
+
+template <typename T>
+static void coarse_solve(cvb_ctx *ctx, const T *b, T *x, const cvb_solve_opts *o);
+template <>
+void coarse_solve<float>(cvb_ctx *ctx, const float *b, float *x, const cvb_solve_opts *o) {
+  LevelDev &C = ctx->L[0];
+  if (ctx->coarse_dense) { launch_dense_apply_f32(ctx->Minv, ctx->ncoarse, b, x, ctx->stream); return; }
+  float *a = x, *a2 = vptr<float>(C, 2);
+  smooth<float>(C, b, a, a2, (float)o->omega, 30, true, ctx->stream);
+  if (a != x) cudaMemcpyAsync(x, a, sizeof(float) * C.g.n(), cudaMemcpyDeviceToDevice, ctx->stream);
+}
+template <>
+void coarse_solve<double>(cvb_ctx *ctx, const double *b, double *x, const cvb_solve_opts *o) {
+  LevelDev &C = ctx->L[0];
+  if (ctx->coarse_dense) { launch_dense_apply(ctx->Minv, ctx->ncoarse, b, x, ctx->stream); return; }
+  double *a = x, *a2 = vptr<double>(C, 2);
+  smooth<double>(C, b, a, a2, o->omega, 30, true, ctx->stream);
+  if (a != x) cudaMemcpyAsync(x, a, sizeof(double) * C.g.n(), cudaMemcpyDeviceToDevice, ctx->stream);
+}
+
+// One V-cycle on level l for A e = b, zero initial guess; result in `out`.
+template <typename T>
+static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o) {
+  cudaStream_t s = ctx->stream;
+  if (l == 0) { coarse_solve<T>(ctx, b, out, o); return; }
+  LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
+  size_t n = L.g.n();
+  T *x = out, *x2 = vptr<T>(L, 2);
+  if (x2 == b) x2 = vptr<T>(L, 1);
+  T omega = (T)o->omega;
+  smooth<T>(L, b, x, x2, omega, std::max(o->pre_sweeps, 1), true, s);
+  T *res = vptr<T>(L, 3);
+  launch_residual<T>(L, b, x, res, s);
+  T *bc = vptr<T>(C, 0), *ec = vptr<T>(C, 1);
+  launch_restrict<T>(L, C, res, bc, s);
+  vcycle<T>(ctx, l - 1, bc, ec, o);
+  launch_prolong_add<T>(C, L, ec, x, s);
+  smooth<T>(L, b, x, x2, omega, o->post_sweeps, false, s);
+  if (x != out) cudaMemcpyAsync(out, x, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+}
+
+// ------------------------------------------------------------------ solver
+static int reduce_to_host(cvb_ctx *ctx, int nv, double *out) {
+  launch_finish_sums(ctx->partial, nv, reduce_blocks(), ctx->sums, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(out, ctx->sums, sizeof(double) * nv, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+static int norm2(cvb_ctx *ctx, const double *v, size_t n, double *out) {
+  // dot(v, v) with the multi-dot kernel; its one-entry pointer table is dV[kMaxRestart + 1]
+  CK(cudaMemcpyAsync(ctx->dV + kMaxRestart + 1, &v, sizeof(double *), cudaMemcpyHostToDevice, ctx->stream));
+  launch_multidot(ctx->dV + kMaxRestart + 1, 1, v, n, ctx->partial, ctx->stream);
+  CKL();
+  double s;
+  TRY(reduce_to_host(ctx, 1, &s));
+  *out = std::sqrt(s);
+  return CVB_OK;
+}
+
+static int fluid_mean_zero(cvb_ctx *ctx, int level, double *x) {
+  LevelDev &L = ctx->L[level];
+  launch_fluid_mean_partial(L.g, L.nvert, x, ctx->partial, ctx->stream);
+  launch_finish_sums(ctx->partial, 2, reduce_blocks(), ctx->sums, ctx->stream);
+  launch_add_fluid_const(L.g, L.nvert, x, ctx->sums, 1, ctx->stream);
+  CKL();
+  return CVB_OK;
+}
+
+// Projects b onto range(A): b -= aj * (sum_fluid b/aj) / n_fluid on fluid cells.
+static int project_rhs(cvb_ctx *ctx, double *b, double *removed);
+
+static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  cudaStream_t s = ctx->stream;
+  const bool mixed = o->precision == CVB_PRECISION_MIXED;
+  const int m = std::min(std::max(o->restart, 1), kMaxRestart);
+  double bnorm;
+  TRY(norm2(ctx, ctx->b, n, &bnorm));
+  st->rhs_norm = bnorm;
+  if (!std::isfinite(bnorm)) return fail(ctx, CVB_NAN_DETECTED, "right-hand side is not finite");
+  if (bnorm == 0.0) {
+    CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * n, s));
+    st->rel_residual = 0.0;
+    st->abs_residual = 0.0;
+    return CVB_OK;
+  }
+  if (!o->warm_start) CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * n, s));
+  launch_residual<double>(F, ctx->b, ctx->x, ctx->r, s);
+  CKL();
+  double beta;
+  TRY(norm2(ctx, ctx->r, n, &beta));
+  int total = 0, restarts = 0;
+  double H[kMaxRestart + 1][kMaxRestart];
+  double cs[kMaxRestart], sn[kMaxRestart], gv[kMaxRestart + 1], yv[kMaxRestart];
+  int status = CVB_NOT_CONVERGED;
+  const double target = std::max(o->rtol * bnorm, o->atol);
+  while (true) {
+    if (!std::isfinite(beta)) return fail(ctx, CVB_NAN_DETECTED, "residual became %g", beta);
+    if (beta <= target) { status = CVB_OK; break; }
+    if (total >= o->max_it) break;
+    // V[0] = r / beta (k_scale divides by the device scalar)
+    CK(cudaMemcpyAsync(ctx->hdev, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
+    launch_scale(ctx->V[0], ctx->r, ctx->hdev, n, s);
+    CKL();
+    for (int q = 0; q <= m; q++) gv[q] = 0.0;
+    gv[0] = beta;
+    int j = 0;
+    double est = beta;
+    for (; j < m && total < o->max_it; j++) {
+      // z_j = M^-1 v_j
+      if (mixed) {
+        launch_f64_to_f32(ctx->V[j], ctx->b32, n, s);
+        // FP32 V-cycle; its result is widened once into the FP64 basis so the
+        // FP64 operator and the final update read it without per-use conversions
+        // (a conversion costs an FP64-pipe instruction on this part)
+        vcycle<float>(ctx, ctx->nlevels - 1, ctx->b32, ctx->Z32[0], o);
+        launch_f32_to_f64(ctx->Z32[0], ctx->Z64[j], n, s);
+        launch_apply<double>(F, ctx->Z64[j], ctx->w, s);
+      } else {
+        vcycle<double>(ctx, ctx->nlevels - 1, ctx->V[j], ctx->Z64[j], o);
+        launch_apply<double>(F, ctx->Z64[j], ctx->w, s);
+      }
+      CKL();
+      // classical Gram-Schmidt (PETSc's default for GMRES/FGMRES), with a second
+      // pass only when the first one cancelled most of w (||w|| dropped below
+      // half of its length before orthogonalisation).
+      double h[kMaxRestart + 2], h2[kMaxRestart + 1];
+      launch_multidot(ctx->dV, j + 1, ctx->w, n, ctx->partial, s, 1);
+      CKL();
+      TRY(reduce_to_host(ctx, j + 2, h));
+      const double w_before = h[j + 1];
+      CK(cudaMemcpyAsync(ctx->hdev, h, sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
+      launch_multiaxpy_norm(ctx->w, ctx->dV, ctx->hdev, j + 1, n, ctx->partial, s);
+      CKL();
+      double nw2;
+      TRY(reduce_to_host(ctx, 1, &nw2));
+      for (int q = 0; q <= j; q++) h2[q] = 0.0;
+      if (o->cgs_refine && nw2 < 0.25 * w_before) {
+        launch_multidot(ctx->dV, j + 1, ctx->w, n, ctx->partial, s);
+        CKL();
+        TRY(reduce_to_host(ctx, j + 1, h2));
+        CK(cudaMemcpyAsync(ctx->hdev, h2, sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
+        launch_multiaxpy_norm(ctx->w, ctx->dV, ctx->hdev, j + 1, n, ctx->partial, s);
+        CKL();
+        TRY(reduce_to_host(ctx, 1, &nw2));
+      }
+      for (int q = 0; q <= j; q++) H[q][j] = h[q] + h2[q];
+      double hn = std::sqrt(nw2);
+      H[j + 1][j] = hn;
+      total++;
+      if (!std::isfinite(hn)) return fail(ctx, CVB_NAN_DETECTED, "Krylov vector became non-finite");
+      if (hn > 0.0) {
+        CK(cudaMemcpyAsync(ctx->hdev, &hn, sizeof(double), cudaMemcpyHostToDevice, s));
+        launch_scale(ctx->V[j + 1], ctx->w, ctx->hdev, n, s);
+        CKL();
+      }
+      // Givens rotations
+      for (int q = 0; q < j; q++) {
+        double t = cs[q] * H[q][j] + sn[q] * H[q + 1][j];
+        H[q + 1][j] = -sn[q] * H[q][j] + cs[q] * H[q + 1][j];
+        H[q][j] = t;
+      }
+      double a = H[j][j], bb = H[j + 1][j];
+      double rr = std::hypot(a, bb);
+      cs[j] = rr > 0 ? a / rr : 1.0;
+      sn[j] = rr > 0 ? bb / rr : 0.0;
+      H[j][j] = rr;
+      H[j + 1][j] = 0.0;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      est = std::fabs(gv[j + 1]);
+      if (est <= target || hn == 0.0) { j++; break; }
+    }
+    // y = H^-1 g ; x += Z y
+    for (int q = j - 1; q >= 0; q--) {
+      double t = gv[q];
+      for (int c2 = q + 1; c2 < j; c2++) t -= H[q][c2] * yv[c2];
+      yv[q] = t / H[q][q];
+    }
+    CK(cudaMemcpyAsync(ctx->hdev, yv, sizeof(double) * j, cudaMemcpyHostToDevice, s));
+    launch_axpy_z(ctx->x, nullptr, ctx->dZ64, ctx->hdev, j, n, s);
+    launch_residual<double>(F, ctx->b, ctx->x, ctx->r, s);
+    CKL();
+    TRY(norm2(ctx, ctx->r, n, &beta));
+    restarts++;
+  }
+  TRY(fluid_mean_zero(ctx, ctx->nlevels - 1, ctx->x));
+  st->iterations = total;
+  st->restarts = restarts > 0 ? restarts - 1 : 0;
+  st->abs_residual = beta;
+  st->rel_residual = beta / bnorm;
+  st->status = status;
+  if (status != CVB_OK)
+    return fail(ctx, status, "not converged: relative residual %.3e after %d iterations", beta / bnorm, total);
+  return CVB_OK;
+}
+
+static int project_rhs(cvb_ctx *ctx, double *b, double *removed) {
+  int l = ctx->nlevels - 1;
+  LevelDev &F = ctx->L[l];
+  launch_fluid_ratio_partial(F.g, F.nvert, b, ctx->aj64[l], ctx->partial, ctx->stream);
+  launch_finish_sums(ctx->partial, 3, reduce_blocks(), ctx->sums, ctx->stream);
+  launch_remove_aj_mean(F.g, F.nvert, ctx->aj64[l], b, ctx->sums, ctx->stream);
+  CKL();
+  double h[3];
+  CK(cudaMemcpyAsync(h, ctx->sums, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // h = {sum b/aj, fluid count, sum b^2}; the removed part is aj * mean(b/aj) on fluid cells
+  double c = h[1] > 0 ? h[0] / h[1] : 0.0;
+  *removed = c;
+  return CVB_OK;
+}
+
+static int solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  cvb_solve_opts def;
+  if (!o) { cvb_solve_opts_default(&def); o = &def; }
+  if (o->restart < 1 || o->restart > kMaxRestart || o->max_it < 0 || !(o->rtol >= 0) || o->pre_sweeps < 0 ||
+      o->post_sweeps < 0 || (o->precision != CVB_PRECISION_FP64 && o->precision != CVB_PRECISION_MIXED))
+    return fail(ctx, CVB_BAD_INPUT, "bad solve options");
+  cvb_solve_stats local;
+  if (!st) st = &local;
+  std::memset(st, 0, sizeof(*st));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (o->project_rhs) TRY(project_rhs(ctx, ctx->b, &st->rhs_projected));
+  int rc = fgmres(ctx, o, st);
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  cudaEventSynchronize(ctx->ev1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  st->device_ms = ms;
+  st->status = rc;
+  return rc;
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+int cvb_solve_opts_default(cvb_solve_opts *o) {
+  if (!o) return CVB_BAD_INPUT;
+  o->precision = CVB_PRECISION_MIXED;
+  o->rtol = 1e-8;
+  o->atol = 0.0;
+  o->max_it = 200;
+  o->restart = 30;
+  o->pre_sweeps = 2;
+  o->post_sweeps = 2;
+  o->omega = 0.85;
+  o->project_rhs = 1;
+  o->warm_start = 0;
+  o->coarse_dense_max = 2048;
+  o->cgs_refine = 0;
+  return CVB_OK;
+}
+
+int cvb_init(cvb_ctx **out, const cvb_options *opts) {
+  if (!out) return CVB_BAD_INPUT;
+  cvb_ctx *ctx = new cvb_ctx();
+  *out = ctx;
+  ctx->device = opts ? opts->device : 0;
+  CK(cudaSetDevice(ctx->device));
+  if (opts && opts->stream) {
+    ctx->stream = (cudaStream_t)opts->stream;
+  } else {
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    ctx->own_stream = true;
+  }
+  CK(cudaEventCreate(&ctx->ev0));
+  CK(cudaEventCreate(&ctx->ev1));
+  return CVB_OK;
+}
+
+void cvb_destroy(cvb_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  free_all(ctx);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *cvb_last_error(const cvb_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+void *cvb_stream(cvb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, const double *nvert_finest) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (nlevels < 1 || nlevels > 16 || !lv || !nvert_finest) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
+  CK(cudaSetDevice(ctx->device));
+  free_all(ctx);
+  for (int l = 0; l < nlevels; l++) TRY(check_desc(ctx, lv[l], l, l == nlevels - 1));
+  for (int l = 0; l + 1 < nlevels; l++) {
+    const cvb_level_desc &c = lv[l], &f = lv[l + 1];
+    int ex = c.isc ? f.mx : (f.mx - 2) / 2 + 2, ey = c.jsc ? f.my : (f.my - 2) / 2 + 2, ez = c.ksc ? f.mz : (f.mz - 2) / 2 + 2;
+    if (c.mx != ex || c.my != ey || c.mz != ez)
+      return fail(ctx, CVB_BAD_INPUT, "level %d box %dx%dx%d is not the coarsening of level %d (%dx%dx%d expected)", l,
+                  c.mx, c.my, c.mz, l + 1, ex, ey, ez);
+  }
+  ctx->nlevels = nlevels;
+  ctx->L.assign(nlevels, LevelDev());
+  ctx->H.resize(nlevels);
+  ctx->fm.assign(nlevels, std::vector<double *>(9, nullptr));
+  ctx->iaj.assign(nlevels, nullptr); ctx->jaj.assign(nlevels, nullptr);
+  ctx->kaj.assign(nlevels, nullptr); ctx->aj64.assign(nlevels, nullptr);
+  size_t nmax = 0;
+  for (int l = 0; l < nlevels; l++) {
+    const cvb_level_desc &d = lv[l];
+    ctx->H[l].d = d;
+    LevelDev &L = ctx->L[l];
+    L.g.mx = d.mx; L.g.my = d.my; L.g.mz = d.mz;
+    L.g.px = d.bctype[0] == 7; L.g.py = d.bctype[2] == 7; L.g.pz = d.bctype[4] == 7;
+    L.isc = d.isc; L.jsc = d.jsc; L.ksc = d.ksc;
+    size_t n = L.g.n();
+    nmax = std::max(nmax, n);
+    const double *srcs[9] = {d.icsi, d.ieta, d.izet, d.jcsi, d.jeta, d.jzet, d.kcsi, d.keta, d.kzet};
+    for (int q = 0; q < 9; q++) TRY(upload_box(ctx, d, srcs[q], 3, &ctx->fm[l][q]));
+    TRY(upload_box(ctx, d, d.iaj, 1, &ctx->iaj[l]));
+    TRY(upload_box(ctx, d, d.jaj, 1, &ctx->jaj[l]));
+    TRY(upload_box(ctx, d, d.kaj, 1, &ctx->kaj[l]));
+    TRY(upload_box(ctx, d, d.aj, 1, &ctx->aj64[l]));
+    TRY(dalloc(ctx, &L.nvert, n));
+    TRY(dalloc(ctx, &L.code, n));
+    TRY(dalloc(ctx, &L.w64, (size_t)NSLOT * n));
+    TRY(dalloc(ctx, &L.gf32, 9 * n));
+    TRY(dalloc(ctx, &L.ajf32, n));
+    TRY(dalloc(ctx, &L.line32, 3 * n));
+    TRY(dalloc(ctx, &L.line64, 3 * n));
+    TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, 2 * n));
+    TRY(dalloc(ctx, &L.r32, n)); TRY(dalloc(ctx, &L.e32, n)); TRY(dalloc(ctx, &L.t32, 2 * n));
+  }
+  TRY(dalloc(ctx, &ctx->nvert_tmp, nmax));
+  // finest level: nvert, face areas, solver workspace
+  const cvb_level_desc &df = lv[nlevels - 1];
+  LevelDev &F = ctx->L[nlevels - 1];
+  size_t n = F.g.n();
+  {
+    std::vector<double> h;
+    extract_box(df, nvert_finest, 1, h);
+    CK(cudaMemcpyAsync(F.nvert, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<double> c1, c2, c3, a3;
+    extract_box(df, df.csi, 3, c1);
+    extract_box(df, df.eta, 3, c2);
+    extract_box(df, df.zet, 3, c3);
+    face_areas(c1, c2, c3, a3);
+    TRY(dalloc(ctx, &ctx->area3, 3 * n));
+    CK(cudaMemcpyAsync(ctx->area3, a3.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  TRY(dalloc(ctx, &ctx->b, n)); TRY(dalloc(ctx, &ctx->x, n));
+  TRY(dalloc(ctx, &ctx->w, n)); TRY(dalloc(ctx, &ctx->r, n));
+  TRY(dalloc(ctx, &ctx->b32, n));
+  TRY(dalloc(ctx, &ctx->uc_dev, 3 * n)); TRY(dalloc(ctx, &ctx->p_dev, n));
+  for (int q = 0; q <= kMaxRestart; q++) ctx->V[q] = nullptr;
+  TRY(dalloc(ctx, &ctx->dV, kMaxRestart + 2));
+  TRY(dalloc(ctx, &ctx->dZ64, kMaxRestart));
+  TRY(dalloc(ctx, &ctx->dZ32, kMaxRestart));
+  int nb = reduce_blocks();
+  TRY(dalloc(ctx, &ctx->partial, (size_t)nb * (kMaxRestart + 2)));
+  TRY(dalloc(ctx, &ctx->sums, kMaxRestart + 2));
+  TRY(dalloc(ctx, &ctx->hdev, kMaxRestart + 2));
+  TRY(build_operators(ctx));
+  cvb_solve_opts def;
+  cvb_solve_opts_default(&def);
+  TRY(build_coarse(ctx, &def));
+  ctx->ready = true;
+  return CVB_OK;
+}
+
+}  // extern "C"
+
+// Krylov basis is allocated lazily, sized by the largest restart requested.
+static int ensure_basis(cvb_ctx *ctx, int m, bool mixed) {
+  size_t n = ctx->L[ctx->nlevels - 1].g.n();
+  bool changed = false;
+  for (int q = 0; q <= m; q++)
+    if (!ctx->V[q]) { TRY(dalloc(ctx, &ctx->V[q], n)); changed = true; }
+  for (int q = 0; q < m; q++)
+    if (!ctx->Z64[q]) { TRY(dalloc(ctx, &ctx->Z64[q], n)); changed = true; }
+  if (mixed && !ctx->Z32[0]) { TRY(dalloc(ctx, &ctx->Z32[0], n)); changed = true; }
+  if (changed) {
+    CK(cudaMemcpyAsync(ctx->dV, ctx->V, sizeof(double *) * (kMaxRestart + 1), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dZ64, ctx->Z64, sizeof(double *) * kMaxRestart, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dZ32, ctx->Z32, sizeof(float *) * kMaxRestart, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return CVB_OK;
+}
+
+static size_t fine_n(cvb_ctx *ctx) { return ctx->L[ctx->nlevels - 1].g.n(); }
+
+extern "C" {
+
+int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!nvert_finest) return fail(ctx, CVB_BAD_INPUT, "nvert is NULL");
+  const cvb_level_desc &df = ctx->H[ctx->nlevels - 1].d;
+  std::vector<double> h;
+  extract_box(df, nvert_finest, 1, h);
+  CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  TRY(build_operators(ctx));
+  cvb_solve_opts def;
+  cvb_solve_opts_default(&def);
+  TRY(build_coarse(ctx, &def));
+  return CVB_OK;
+}
+
+int cvb_level_dims(const cvb_ctx *ctx, int level, int *mx, int *my, int *mz) {
+  if (!ctx || !ctx->ready || level < 0 || level >= ctx->nlevels) return CVB_BAD_INPUT;
+  *mx = ctx->L[level].g.mx; *my = ctx->L[level].g.my; *mz = ctx->L[level].g.mz;
+  return CVB_OK;
+}
+
+int cvb_get_nvert(cvb_ctx *ctx, int level, double *nvert, int *mns) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (level < 0 || level >= ctx->nlevels) return fail(ctx, CVB_BAD_INPUT, "bad level %d", level);
+  if (nvert)
+    CK(cudaMemcpy(nvert, ctx->L[level].nvert, sizeof(double) * ctx->L[level].g.n(), cudaMemcpyDeviceToHost));
+  if (mns) *mns = ctx->multinullspace;
+  return CVB_OK;
+}
+
+int cvb_volume_flux_rev(cvb_ctx *ctx, double *ucont, double fis, int flg, double *flux, double *area) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ucont) return fail(ctx, CVB_BAD_INPUT, "ucont is NULL");
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  size_t n = F.g.n();
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_ib_sums(F.g, ctx->uc_dev, ctx->area3, nullptr, nullptr, F.nvert, ctx->partial, ctx->stream);
+  launch_finish_sums(ctx->partial, 2, reduce_blocks(), ctx->sums, ctx->stream);
+  launch_ib_correct(F.g, ctx->uc_dev, ctx->area3, nullptr, nullptr, F.nvert, ctx->sums, fis, flg, ctx->stream);
+  launch_ib_sums(F.g, ctx->uc_dev, ctx->area3, nullptr, nullptr, F.nvert, ctx->partial, ctx->stream);
+  CKL();
+  double fa[2];
+  TRY(reduce_to_host(ctx, 2, fa));
+  CK(cudaMemcpy(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost));
+  if (flux) *flux = fa[0];
+  if (area) *area = fa[1];
+  return CVB_OK;
+}
+
+int cvb_poisson_rhs(cvb_ctx *ctx, const double *ucont, double dt, double st, double *b, double *compat) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ucont || !b || !(dt != 0.0) || !(st != 0.0)) return fail(ctx, CVB_BAD_INPUT, "bad PoissonRHS arguments");
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  size_t n = F.g.n();
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_poisson_rhs(F.g, ctx->uc_dev, ctx->aj64[ctx->nlevels - 1], F.nvert, dt, st, ctx->b, ctx->partial, ctx->stream);
+  CKL();
+  double s;
+  TRY(reduce_to_host(ctx, 1, &s));
+  CK(cudaMemcpy(b, ctx->b, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (compat) *compat = s;
+  return CVB_OK;
+}
+
+int cvb_solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  cvb_solve_opts def;
+  if (!o) { cvb_solve_opts_default(&def); o = &def; }
+  TRY(ensure_basis(ctx, std::min(std::max(o->restart, 1), kMaxRestart), o->precision == CVB_PRECISION_MIXED));
+  return solve_resident(ctx, o, st);
+}
+
+double *cvb_device_rhs(cvb_ctx *ctx) { return ctx && ctx->ready ? ctx->b : nullptr; }
+double *cvb_device_phi(cvb_ctx *ctx) { return ctx && ctx->ready ? ctx->x : nullptr; }
+
+int cvb_poisson_solve(cvb_ctx *ctx, const double *b, double *phi, const cvb_solve_opts *o, cvb_solve_stats *st) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!b || !phi) return fail(ctx, CVB_BAD_INPUT, "b/phi is NULL");
+  cvb_solve_opts def;
+  if (!o) { cvb_solve_opts_default(&def); o = &def; }
+  size_t n = fine_n(ctx);
+  CK(cudaMemcpyAsync(ctx->b, b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (o->warm_start) CK(cudaMemcpyAsync(ctx->x, phi, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = cvb_solve_resident(ctx, o, st);
+  if (rc == CVB_OK || rc == CVB_NOT_CONVERGED)
+    CK(cudaMemcpyAsync(phi, ctx->x, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return rc;
+}
+
+int cvb_poisson_solver_mg(cvb_ctx *ctx, double *ucont, double fis, int immersed, double dt, double st, double *phi,
+                          const cvb_solve_opts *o, cvb_solve_stats *stats) {
+  if (!ctx) return CVB_BAD_INPUT;
+  double flux, area, compat;
+  TRY(cvb_volume_flux_rev(ctx, ucont, fis, immersed, &flux, &area));
+  size_t n = ctx->ready ? fine_n(ctx) : 0;
+  std::vector<double> b(n);
+  TRY(cvb_poisson_rhs(ctx, ucont, dt, st, b.data(), &compat));
+  return cvb_poisson_solve(ctx, b.data(), phi, o, stats);
+}
+
+int cvb_update_pressure(cvb_ctx *ctx, double *p, double *phi) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!p || !phi) return fail(ctx, CVB_BAD_INPUT, "p/phi is NULL");
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  size_t n = F.g.n();
+  CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->w, phi, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_update_pressure(F.g, ctx->p_dev, ctx->w, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(p, ctx->p_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(phi, ctx->w, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!phi || !ucont) return fail(ctx, CVB_BAD_INPUT, "phi/ucont is NULL");
+  int l = ctx->nlevels - 1;
+  LevelDev &F = ctx->L[l];
+  size_t n = F.g.n();
+  CK(cudaMemcpyAsync(ctx->w, phi, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  const double *fm[9];
+  for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
+  launch_projection(F.g, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], F.nvert, ctx->w, dt, st, ctx->uc_dev, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+static int level_ok(cvb_ctx *ctx, int level) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (level < 0 || level >= ctx->nlevels) return fail(ctx, CVB_BAD_INPUT, "bad level %d", level);
+  return CVB_OK;
+}
+
+int cvb_apply_operator(cvb_ctx *ctx, int level, const double *x, double *y) {
+  TRY(level_ok(ctx, level));
+  LevelDev &L = ctx->L[level];
+  size_t n = L.g.n();
+  CK(cudaMemcpyAsync(L.r64, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_apply<double>(L, L.r64, L.e64, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(y, L.e64, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_apply_operator_f32(cvb_ctx *ctx, int level, const float *x, float *y) {
+  TRY(level_ok(ctx, level));
+  LevelDev &L = ctx->L[level];
+  size_t n = L.g.n();
+  CK(cudaMemcpyAsync(L.r32, x, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_apply<float>(L, L.r32, L.e32, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(y, L.e32, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_get_weights(cvb_ctx *ctx, int level, double *w) {
+  TRY(level_ok(ctx, level));
+  LevelDev &L = ctx->L[level];
+  CK(cudaMemcpy(w, L.w64, sizeof(double) * NSLOT * L.g.n(), cudaMemcpyDeviceToHost));
+  return CVB_OK;
+}
+
+int cvb_restrict(cvb_ctx *ctx, int coarse, const double *xf, double *xc) {
+  TRY(level_ok(ctx, coarse));
+  TRY(level_ok(ctx, coarse + 1));
+  LevelDev &C = ctx->L[coarse], &F = ctx->L[coarse + 1];
+  CK(cudaMemcpyAsync(F.r64, xf, sizeof(double) * F.g.n(), cudaMemcpyHostToDevice, ctx->stream));
+  launch_restrict<double>(F, C, F.r64, C.e64, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(xc, C.e64, sizeof(double) * C.g.n(), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_interpolate(cvb_ctx *ctx, int fine, const double *xc, double *xf) {
+  TRY(level_ok(ctx, fine));
+  TRY(level_ok(ctx, fine - 1));
+  LevelDev &C = ctx->L[fine - 1], &F = ctx->L[fine];
+  CK(cudaMemcpyAsync(C.r64, xc, sizeof(double) * C.g.n(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(F.e64, 0, sizeof(double) * F.g.n(), ctx->stream));
+  launch_prolong_add<double>(C, F, C.r64, F.e64, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(xf, F.e64, sizeof(double) * F.g.n(), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+long long cvb_kernel_launches(void) { return launch_count(); }
+
+int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_ms, double *bytes) {
+  TRY(level_ok(ctx, level));
+  if (reps < 1) return fail(ctx, CVB_BAD_INPUT, "reps < 1");
+  LevelDev &L = ctx->L[level];
+  size_t n = L.g.n();
+  double per_cell;
+  auto launch = [&]() {
+    switch (kernel) {
+      case CVB_KERNEL_LINE_SWEEP_F32: launch_line_smooth<float>(L, L.r32, L.e32, L.t32 + n, 0.85f, 0, ctx->stream); break;
+      case CVB_KERNEL_LINE_SWEEP_F64: launch_line_smooth<double>(L, L.r64, L.e64, L.t64 + n, 0.85, 0, ctx->stream); break;
+      case CVB_KERNEL_RESIDUAL_F32: launch_residual<float>(L, L.r32, L.e32, L.t32, ctx->stream); break;
+      default: launch_residual<double>(L, L.r64, L.e64, L.t64, ctx->stream); break;
+    }
+  };
+  // algorithmic bytes per cell: every array the kernel needs, touched once
+  switch (kernel) {
+    case CVB_KERNEL_LINE_SWEEP_F32: per_cell = 4 + 4 + 36 + 4 + 4 + 12 + 4; break;   // x b g9 aj code fac xnew
+    case CVB_KERNEL_LINE_SWEEP_F64: per_cell = 8 + 8 + 152 + 4 + 24 + 8; break;      // x b w19 code fac xnew
+    case CVB_KERNEL_RESIDUAL_F32: per_cell = 4 + 4 + 36 + 4 + 4 + 4; break;          // x b g9 aj code r
+    case CVB_KERNEL_RESIDUAL_F64: per_cell = 8 + 8 + 152 + 4 + 8; break;             // x b w19 code r
+    default: return fail(ctx, CVB_BAD_INPUT, "unknown kernel id %d", kernel);
+  }
+  CK(cudaMemsetAsync(L.r32, 0, sizeof(float) * n, ctx->stream));
+  CK(cudaMemsetAsync(L.e32, 0, sizeof(float) * n, ctx->stream));
+  CK(cudaMemsetAsync(L.r64, 0, sizeof(double) * n, ctx->stream));
+  CK(cudaMemsetAsync(L.e64, 0, sizeof(double) * n, ctx->stream));
+  for (int q = 0; q < 3; q++) launch();
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int q = 0; q < reps; q++) launch();
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  CKL();
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  if (avg_ms) *avg_ms = ms / reps;
+  if (bytes) *bytes = per_cell * (double)n;
+  return CVB_OK;
+}
+
+int cvb_nullspace(cvb_ctx *ctx, int level, double *x) {
+  TRY(level_ok(ctx, level));
+  LevelDev &L = ctx->L[level];
+  CK(cudaMemcpyAsync(L.r64, x, sizeof(double) * L.g.n(), cudaMemcpyHostToDevice, ctx->stream));
+  TRY(fluid_mean_zero(ctx, level, L.r64));
+  CK(cudaMemcpyAsync(x, L.r64, sizeof(double) * L.g.n(), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+}  // extern "C"

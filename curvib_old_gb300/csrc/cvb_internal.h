@@ -1,0 +1,135 @@
+// Internal declarations shared by the CUDA kernels and the host library.
+// Grid layout everywhere: one level is the reference's DMDA box [mz][my][mx],
+// i fastest, boundary ring included (mx = IM+1 for IM nodes).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cvb {
+
+// Kernel launches issued by this library (all contexts), for measurement.
+void count_launch(int n = 1);
+long long launch_count();
+
+// Stencil slots, in the order of the reference's PoissonLHSNew (poisson.c:576-594).
+enum Slot { CP, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW, NSLOT };
+
+// Per-cell switching code (built once from nvert by build_codes):
+//   bit 0       identity row (boundary ring, or nvert > 0.1)
+//   bits 1..6   face active from this row's side: E, W, N, S, T, B
+//   bits 8..19  cross-derivative form for this cell's three upper faces, 2 bits each:
+//               E: (j, k)  N: (i, k)  T: (i, j)   0 none, 1 central, 2 lower, 3 upper
+// A lower face (W/S/B) of a row is the upper face of its lower neighbour, so a
+// row reads that neighbour's code for it.
+enum : uint32_t {
+  CODE_IDENTITY = 1u,
+  CODE_ACT_E = 1u << 1, CODE_ACT_W = 1u << 2, CODE_ACT_N = 1u << 3,
+  CODE_ACT_S = 1u << 4, CODE_ACT_T = 1u << 5, CODE_ACT_B = 1u << 6,
+};
+__host__ __device__ inline int code_branch(uint32_t c, int face, int which) {
+  return (c >> (8 + 4 * face + 2 * which)) & 3u;  // face 0=E,1=N,2=T; which 0/1
+}
+
+struct Geom {
+  int mx, my, mz;
+  int px, py, pz;  // periodic directions (bctype 7)
+  __host__ __device__ size_t n() const { return (size_t)mx * my * mz; }
+  __host__ __device__ size_t id(int i, int j, int k) const {
+    return ((size_t)k * my + j) * mx + i;
+  }
+  // neighbour index with the reference's periodic wrap of column indices
+  __host__ __device__ int iu(int i) const { return (px && i == mx - 2) ? 1 : i + 1; }
+  __host__ __device__ int id_(int i) const { return (px && i == 1) ? mx - 2 : i - 1; }
+  __host__ __device__ int ju(int j) const { return (py && j == my - 2) ? 1 : j + 1; }
+  __host__ __device__ int jd(int j) const { return (py && j == 1) ? my - 2 : j - 1; }
+  __host__ __device__ int ku(int k) const { return (pz && k == mz - 2) ? 1 : k + 1; }
+  __host__ __device__ int kd(int k) const { return (pz && k == 1) ? mz - 2 : k - 1; }
+};
+
+// Device data of one multigrid level.
+struct LevelDev {
+  Geom g;
+  int isc, jsc, ksc;     // semi-coarsening flags of this level (GridRestriction)
+  double *nvert;         // [N]
+  uint32_t *code;        // [N]
+  double *w64;           // [19][N] FP64 stencil weights (rows scaled by -aj; identity rows CP=1)
+  float *gf32;           // [9][N]  FP32 face coefficients g11..g33
+  float *ajf32;          // [N]
+  float *line32;         // [3][N]  y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32
+  double *line64;        // [3][N]  ... in FP64
+  // work vectors of this level (the finest level's b/x live in the solver)
+  double *r64, *e64, *t64;  // FP64 V-cycle vectors
+  float *r32, *e32, *t32;   // FP32 V-cycle vectors
+};
+
+// --- kernel launchers (defined in the .cu files) ---------------------------
+// setup
+void launch_gcoef(const Geom &g, const double *const *metric /*12 Cmpnts fields: I(csi,eta,zet) J.. K..*/,
+                  const double *iaj, const double *jaj, const double *kaj, double *g9 /*[9][N]*/,
+                  cudaStream_t s);
+void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s);
+void launch_weights(const Geom &g, const double *g9, const double *aj, const double *nvert,
+                    const uint32_t *code, double *w64, cudaStream_t s);
+void launch_line_factors(const Geom &g, const double *w64, double *line64, float *line32,
+                         cudaStream_t s);
+void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s);
+void launch_nvert_restrict(const Geom &fine, const double *nvf, const Geom &coarse, int isc, int jsc,
+                           int ksc, double *nvc, double *tmp, cudaStream_t s);
+
+// operator / smoother / transfers (T = float or double)
+template <typename T>
+void launch_apply(const LevelDev &L, const T *x, T *y, cudaStream_t s);
+template <typename T>
+void launch_residual(const LevelDev &L, const T *b, const T *x, T *r, cudaStream_t s);
+template <typename T>
+void launch_line_smooth(const LevelDev &L, const T *b, const T *x, T *xnew, T omega, int zero_guess,
+                        cudaStream_t s);
+template <typename T>
+void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s);
+template <typename T>
+void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s);
+
+// mixed-precision glue: FP64 operator on an FP32-stored vector
+void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStream_t s);
+void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s);
+void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s);
+
+// Krylov support (deterministic two-stage reductions)
+int reduce_blocks();
+void launch_multidot(const double *const *V, int nv, const double *w, size_t n, double *partial,
+                     cudaStream_t s, int self = 0);
+void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t n, double *partial,
+                         cudaStream_t s);
+void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s);
+void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_dev, int nv, size_t n,
+                           double *partial, cudaStream_t s);
+void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s);
+void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev,
+                   int nz, size_t n, cudaStream_t s);
+void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial,
+                               cudaStream_t s);
+void launch_add_fluid_const(const Geom &g, const double *nvert, double *x, const double *sumcnt,
+                            int zero_outside, cudaStream_t s);
+// range projection of a right-hand side: sums of b/aj and counts over fluid cells,
+// then b -= aj * sum/count there
+void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double *b, const double *aj,
+                                double *partial, cudaStream_t s);
+void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
+                           cudaStream_t s);
+void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s);
+void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s);
+
+// projection-path kernels (FP64)
+void launch_poisson_rhs(const Geom &g, const double *ucont, const double *aj, const double *nvert,
+                        double dt, double st, double *b, double *partial, cudaStream_t s);
+void launch_ib_sums(const Geom &g, const double *ucont, const double *csi, const double *eta,
+                    const double *zet, const double *nvert, double *partial, cudaStream_t s);
+void launch_ib_correct(const Geom &g, double *ucont, const double *csi, const double *eta,
+                       const double *zet, const double *nvert, const double *flux_area,
+                       double flux_intp_sum, int flg, cudaStream_t s);
+void launch_update_pressure(const Geom &g, double *p, double *phi, cudaStream_t s);
+void launch_projection(const Geom &g, const double *const *fm /*I,J,K csi/eta/zet*/, const double *iaj,
+                       const double *jaj, const double *kaj, const double *nvert, const double *phi,
+                       double dt, double st, double *ucont, cudaStream_t s);
+
+}  // namespace cvb

@@ -1,0 +1,267 @@
+// Krylov support: fused multi-dot products, multi-axpy with norm, null-space
+// removal and the coarsest-level dense solve.  Every reduction is two-stage with
+// a fixed block count and a fixed summation tree, so a solve's result does not
+// depend on timing or on what else shares the GPU.
+#include "cvb_internal.h"
+
+namespace cvb {
+
+static long long g_launches = 0;
+void count_launch(int n) { __atomic_add_fetch(&g_launches, (long long)n, __ATOMIC_RELAXED); }
+long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+static const int kRedThreads = 256;
+static int g_red_blocks = 0;
+
+int reduce_blocks() {
+  if (!g_red_blocks) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_red_blocks = (sms > 0 ? sms : 148) * 4;
+  }
+  return g_red_blocks;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&acc)[NV], double *partial, int nblocks, int base) {
+  __shared__ double sh[NV][kRedThreads / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++) {
+    double v = acc[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[q][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kRedThreads / 32; w++) v += sh[threadIdx.x][w];
+    partial[(size_t)(base + threadIdx.x) * nblocks + blockIdx.x] = v;
+  }
+}
+
+// partial[q][block] = sum over this block's elements of V_q[i] * w[i]; chunks of 8 vectors on blockIdx.y
+// With `self`, chunk 0 also accumulates w.w into row nv of the partials.
+template <typename TV>
+__global__ void __launch_bounds__(kRedThreads) k_multidot(const TV *const *V, int nv, const double *__restrict__ w,
+                                                           size_t n, double *partial, int self) {
+  const int base = blockIdx.y * 8;
+  double acc[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) acc[q] = 0.0;
+  const TV *v[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) v[q] = (base + q < nv) ? V[base + q] : nullptr;
+  const bool ws = self && blockIdx.y == 0;
+  for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
+    double wp = w[p];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      if (v[q]) acc[q] = fma((double)v[q][p], wp, acc[q]);
+    if (ws) acc[8] = fma(wp, wp, acc[8]);
+  }
+  int cnt = nv - base < 8 ? nv - base : 8;
+  __shared__ double sh[9][kRedThreads / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  {
+    double x = acc[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[8][wid] = x;
+  }
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    double x = acc[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[q][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < cnt) {
+    double x = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < kRedThreads / 32; ww++) x += sh[threadIdx.x][ww];
+    partial[(size_t)(base + threadIdx.x) * gridDim.x + blockIdx.x] = x;
+  }
+  if (ws && threadIdx.x == 32) {
+    double x = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < kRedThreads / 32; ww++) x += sh[8][ww];
+    partial[(size_t)nv * gridDim.x + blockIdx.x] = x;
+  }
+}
+
+void launch_multidot(const double *const *V, int nv, const double *w, size_t n, double *partial, cudaStream_t s,
+                     int self) {
+  dim3 grd(reduce_blocks(), (nv + 7) / 8);
+  k_multidot<double><<<grd, kRedThreads, 0, s>>>(V, nv, w, n, partial, self); count_launch();
+}
+void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t n, double *partial, cudaStream_t s) {
+  dim3 grd(reduce_blocks(), (nv + 7) / 8);
+  k_multidot<float><<<grd, kRedThreads, 0, s>>>(V, nv, w, n, partial, 0); count_launch();
+}
+
+// out[q] = sum_b partial[q][b], one block per q, fixed tree.
+__global__ void k_finish(const double *__restrict__ partial, int nblocks, double *__restrict__ out) {
+  __shared__ double sh[kRedThreads];
+  int q = blockIdx.x;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += kRedThreads) v += partial[(size_t)q * nblocks + b];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[q] = sh[0];
+}
+void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s) {
+  k_finish<<<nv, kRedThreads, 0, s>>>(partial, nblocks, out); count_launch();
+}
+
+// w -= sum_q h[q] V_q ; partial[block] = sum of w^2 over the block.
+__global__ void __launch_bounds__(kRedThreads) k_multiaxpy_norm(double *__restrict__ w, const double *const *V,
+                                                                 const double *__restrict__ h, int nv, size_t n,
+                                                                 double *partial) {
+  __shared__ double hs[64];
+  if (threadIdx.x < nv) hs[threadIdx.x] = h[threadIdx.x];
+  __syncthreads();
+  double acc = 0.0;
+  for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
+    double v = w[p];
+    for (int q = 0; q < nv; q++) v = fma(-hs[q], V[q][p], v);
+    w[p] = v;
+    acc = fma(v, v, acc);
+  }
+  double a1[1] = {acc};
+  block_reduce_store<1>(a1, partial, gridDim.x, 0);
+}
+void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_dev, int nv, size_t n,
+                           double *partial, cudaStream_t s) {
+  k_multiaxpy_norm<<<reduce_blocks(), kRedThreads, 0, s>>>(w, V, h_dev, nv, n, partial); count_launch();
+}
+
+// dst = src / *scal
+__global__ void k_scale(double *__restrict__ dst, const double *__restrict__ src, const double *__restrict__ scal,
+                        size_t n) {
+  double inv = 1.0 / *scal;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
+    dst[p] = src[p] * inv;
+}
+void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s) {
+  k_scale<<<reduce_blocks(), 256, 0, s>>>(dst, src, scal_dev, n); count_launch();
+}
+
+// x += sum_q y[q] Z_q (Z stored FP32 in mixed mode, FP64 in plain mode)
+__global__ void k_axpy_z(double *__restrict__ x, const float *const *Z32, const double *const *Z64,
+                         const double *__restrict__ y, int nz, size_t n) {
+  __shared__ double ys[64];
+  if (threadIdx.x < nz) ys[threadIdx.x] = y[threadIdx.x];
+  __syncthreads();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    double v = x[p];
+    if (Z32)
+      for (int q = 0; q < nz; q++) v = fma(ys[q], (double)Z32[q][p], v);
+    else
+      for (int q = 0; q < nz; q++) v = fma(ys[q], Z64[q][p], v);
+    x[p] = v;
+  }
+}
+void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev, int nz,
+                   size_t n, cudaStream_t s) {
+  k_axpy_z<<<reduce_blocks(), 256, 0, s>>>(x, Z32, Z64, y_dev, nz, n); count_launch();
+}
+
+// Null space (PoissonNullSpaceFunction, poisson.c:411-558): sums and counts of x
+// over interior fluid cells (nvert < 0.1).
+__global__ void __launch_bounds__(kRedThreads) k_fluid_sum(Geom g, const double *__restrict__ nv,
+                                                           const double *__restrict__ x, double *partial) {
+  double acc[2] = {0.0, 0.0};
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
+    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    if (i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1) {
+      acc[0] += x[p];
+      acc[1] += 1.0;
+    }
+  }
+  block_reduce_store<2>(acc, partial, gridDim.x, 0);
+}
+void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial, cudaStream_t s) {
+  k_fluid_sum<<<reduce_blocks(), kRedThreads, 0, s>>>(g, nvert, x, partial); count_launch();
+}
+// x += -sum/count on interior fluid cells; with zero_outside the ring and the
+// non-fluid cells are set to zero.
+__global__ void k_add_fluid_const(Geom g, const double *__restrict__ nv, double *__restrict__ x,
+                                  const double *__restrict__ sc, int zero_outside) {
+  double shift = sc[1] > 0.0 ? sc[0] / (-1.0 * sc[1]) : 0.0;
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    bool interior = i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2;
+    if (interior && nv[p] < 0.1) x[p] += shift;
+    if (zero_outside && (!interior || nv[p] > 0.1)) x[p] = 0.0;
+  }
+}
+void launch_add_fluid_const(const Geom &g, const double *nvert, double *x, const double *sumcnt, int zero_outside,
+                            cudaStream_t s) {
+  k_add_fluid_const<<<reduce_blocks(), 256, 0, s>>>(g, nvert, x, sumcnt, zero_outside); count_launch();
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_fluid_ratio(Geom g, const double *__restrict__ nv,
+                                                             const double *__restrict__ b, const double *__restrict__ aj,
+                                                             double *partial) {
+  double acc[3] = {0.0, 0.0, 0.0};
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
+    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    if (i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1) {
+      acc[0] += b[p] / aj[p];
+      acc[1] += 1.0;
+    }
+    acc[2] = fma(b[p], b[p], acc[2]);
+  }
+  block_reduce_store<3>(acc, partial, gridDim.x, 0);
+}
+void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double *b, const double *aj,
+                                double *partial, cudaStream_t s) {
+  k_fluid_ratio<<<reduce_blocks(), kRedThreads, 0, s>>>(g, nvert, b, aj, partial); count_launch();
+}
+__global__ void k_remove_aj_mean(Geom g, const double *__restrict__ nv, const double *__restrict__ aj,
+                                 double *__restrict__ b, const double *__restrict__ sums) {
+  double c = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    if (i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1)
+      b[p] -= aj[p] * c;
+  }
+}
+void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
+                           cudaStream_t s) {
+  k_remove_aj_mean<<<reduce_blocks(), 256, 0, s>>>(g, nvert, aj, b, sums); count_launch();
+}
+
+// Coarsest level: e = Minv r with a dense FP64 inverse (one warp per row).
+template <typename T>
+__global__ void k_dense(const double *__restrict__ M, int n, const T *__restrict__ r, T *__restrict__ e) {
+  int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int c = lane; c < n; c += 32) s = fma(M[(size_t)row * n + c], (double)r[c], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) e[row] = (T)s;
+}
+void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s) {
+  k_dense<double><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e); count_launch();
+}
+void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s) {
+  k_dense<float><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e); count_launch();
+}
+
+}  // namespace cvb

@@ -1,0 +1,263 @@
+// Set-up kernels: face coefficients, switching codes, FP64 stencil weights,
+// y-line Thomas factors and the immersed-boundary restriction of nvert.
+// Run once per problem (or whenever nvert changes); the solve reuses the result.
+#include "cvb_internal.h"
+
+namespace cvb {
+
+static inline unsigned nblk(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// g11..g33 of PoissonLHSNew (poisson.c:699-735): (metric_b . metric_a) * face Jacobian.
+__global__ void k_gcoef(Geom g, const double *__restrict__ ic, const double *__restrict__ ie,
+                        const double *__restrict__ iz, const double *__restrict__ jc,
+                        const double *__restrict__ je, const double *__restrict__ jz,
+                        const double *__restrict__ kc, const double *__restrict__ ke,
+                        const double *__restrict__ kz, const double *__restrict__ iaj,
+                        const double *__restrict__ jaj, const double *__restrict__ kaj,
+                        double *__restrict__ g9) {
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const double *a = ic + 3 * p, *b = ie + 3 * p, *c = iz + 3 * p;
+    double j1 = iaj[p];
+    g9[0 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[0], a[0]), __dmul_rn(a[1], a[1])), __dmul_rn(a[2], a[2])), j1);
+    g9[1 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(b[0], a[0]), __dmul_rn(b[1], a[1])), __dmul_rn(b[2], a[2])), j1);
+    g9[2 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(c[0], a[0]), __dmul_rn(c[1], a[1])), __dmul_rn(c[2], a[2])), j1);
+    a = jc + 3 * p; b = je + 3 * p; c = jz + 3 * p;
+    double j2 = jaj[p];
+    g9[3 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2])), j2);
+    g9[4 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(b[0], b[0]), __dmul_rn(b[1], b[1])), __dmul_rn(b[2], b[2])), j2);
+    g9[5 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(c[0], b[0]), __dmul_rn(c[1], b[1])), __dmul_rn(c[2], b[2])), j2);
+    a = kc + 3 * p; b = ke + 3 * p; c = kz + 3 * p;
+    double j3 = kaj[p];
+    g9[6 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[0], c[0]), __dmul_rn(a[1], c[1])), __dmul_rn(a[2], c[2])), j3);
+    g9[7 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(b[0], c[0]), __dmul_rn(b[1], c[1])), __dmul_rn(b[2], c[2])), j3);
+    g9[8 * n + p] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(c[0], c[0]), __dmul_rn(c[1], c[1])), __dmul_rn(c[2], c[2])), j3);
+  }
+}
+
+void launch_gcoef(const Geom &g, const double *const *m, const double *iaj, const double *jaj,
+                  const double *kaj, double *g9, cudaStream_t s) {
+  k_gcoef<<<nblk(g.n(), 256), 256, 0, s>>>(g, m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8],
+                                           iaj, jaj, kaj, g9); count_launch();
+}
+
+// The cross-derivative form of poisson.c:793-1324: s_up/s_dn are the nvert sums
+// of the two cells beside the face one step up/down the cross direction.
+__device__ __forceinline__ int cross_branch(double s_up, double s_dn, int c, int m, int per) {
+  if ((c == m - 2 && !per) || s_up > 0.1) return (s_dn < 0.1 && (c != 1 || per)) ? 2 : 0;
+  if ((c == 1 && !per) || s_dn > 0.1) return (s_up < 0.1) ? 3 : 0;
+  return 1;
+}
+
+__global__ void k_codes(Geom g, const double *__restrict__ nv, uint32_t *__restrict__ code) {
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    uint32_t c = 0;
+    const int mx = g.mx, my = g.my, mz = g.mz;
+    auto NV = [&](int a, int b, int d) { return nv[g.id(a, b, d)]; };
+    bool inj = j >= 1 && j <= my - 2, ink = k >= 1 && k <= mz - 2, ini = i >= 1 && i <= mx - 2;
+    // upper-face cross branches, for every face some interior row can use
+    if (inj && ink && i <= mx - 2) {  // E face of (i,j,k)
+      c |= (uint32_t)cross_branch(NV(i, j + 1, k) + NV(i + 1, j + 1, k), NV(i, j - 1, k) + NV(i + 1, j - 1, k), j, my, g.py) << 8;
+      c |= (uint32_t)cross_branch(NV(i, j, k + 1) + NV(i + 1, j, k + 1), NV(i, j, k - 1) + NV(i + 1, j, k - 1), k, mz, g.pz) << 10;
+    }
+    if (ini && ink && j <= my - 2) {  // N face
+      c |= (uint32_t)cross_branch(NV(i + 1, j, k) + NV(i + 1, j + 1, k), NV(i - 1, j, k) + NV(i - 1, j + 1, k), i, mx, g.px) << 12;
+      c |= (uint32_t)cross_branch(NV(i, j, k + 1) + NV(i, j + 1, k + 1), NV(i, j, k - 1) + NV(i, j + 1, k - 1), k, mz, g.pz) << 14;
+    }
+    if (ini && inj && k <= mz - 2) {  // T face
+      c |= (uint32_t)cross_branch(NV(i + 1, j, k) + NV(i + 1, j, k + 1), NV(i - 1, j, k) + NV(i - 1, j, k + 1), i, mx, g.px) << 16;
+      c |= (uint32_t)cross_branch(NV(i, j + 1, k) + NV(i, j + 1, k + 1), NV(i, j - 1, k) + NV(i, j - 1, k + 1), j, my, g.py) << 18;
+    }
+    if (!(ini && inj && ink) || NV(i, j, k) > 0.1) {
+      c |= CODE_IDENTITY;
+    } else {
+      const double thr = 0.1;
+      const int x_end = g.px ? mx - 1 : mx - 2, x_str = g.px ? 0 : 1;
+      const int y_end = g.py ? my - 1 : my - 2, y_str = g.py ? 0 : 1;
+      const int z_end = g.pz ? mz - 1 : mz - 2, z_str = g.pz ? 0 : 1;
+      if (NV(i + 1, j, k) < thr && i != x_end) c |= CODE_ACT_E;
+      if (NV(i - 1, j, k) < thr && i != x_str) c |= CODE_ACT_W;
+      if (NV(i, j + 1, k) < thr && j != y_end) c |= CODE_ACT_N;
+      if (NV(i, j - 1, k) < thr && j != y_str) c |= CODE_ACT_S;
+      if (NV(i, j, k + 1) < thr && k != z_end) c |= CODE_ACT_T;
+      if (NV(i, j, k - 1) < thr && k != z_str) c |= CODE_ACT_B;
+    }
+    code[p] = c;
+  }
+}
+
+void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s) {
+  k_codes<<<nblk(g.n(), 256), 256, 0, s>>>(g, nvert, code); count_launch();
+}
+
+// One cross term into vol[] in the reference's order (see add_cross in the oracle).
+__device__ __forceinline__ void add_cross(double *vol, int br, double gg, bool up, int P, int Q, int Pu,
+                                          int Qu, int Pd, int Qd) {
+  double h = __dmul_rn(gg, 0.5), q = __dmul_rn(gg, 0.25);
+  if (br == 2) {
+    if (up) { vol[P] = __dadd_rn(vol[P], h); vol[Q] = __dadd_rn(vol[Q], h); vol[Pd] = __dsub_rn(vol[Pd], h); vol[Qd] = __dsub_rn(vol[Qd], h); }
+    else { vol[P] = __dsub_rn(vol[P], h); vol[Q] = __dsub_rn(vol[Q], h); vol[Pd] = __dadd_rn(vol[Pd], h); vol[Qd] = __dadd_rn(vol[Qd], h); }
+  } else if (br == 3) {
+    if (up) { vol[Pu] = __dadd_rn(vol[Pu], h); vol[Qu] = __dadd_rn(vol[Qu], h); vol[P] = __dsub_rn(vol[P], h); vol[Q] = __dsub_rn(vol[Q], h); }
+    else { vol[Pu] = __dsub_rn(vol[Pu], h); vol[Qu] = __dsub_rn(vol[Qu], h); vol[P] = __dadd_rn(vol[P], h); vol[Q] = __dadd_rn(vol[Q], h); }
+  } else if (br == 1) {
+    if (up) { vol[Pu] = __dadd_rn(vol[Pu], q); vol[Qu] = __dadd_rn(vol[Qu], q); vol[Pd] = __dsub_rn(vol[Pd], q); vol[Qd] = __dsub_rn(vol[Qd], q); }
+    else { vol[Pu] = __dsub_rn(vol[Pu], q); vol[Qu] = __dsub_rn(vol[Qu], q); vol[Pd] = __dadd_rn(vol[Pd], q); vol[Qd] = __dadd_rn(vol[Qd], q); }
+  }
+}
+
+// The 19 matrix entries of one row, accumulated exactly as PoissonLHSNew does
+// (poisson.c:789-1327), so the stored weights equal the reference's assembled
+// matrix bit for bit.
+__global__ void k_weights(Geom g, const double *__restrict__ g9, const double *__restrict__ aj,
+                          const uint32_t *__restrict__ code, double *__restrict__ w) {
+  size_t n = g.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    uint32_t c = code[p];
+    if (c & CODE_IDENTITY) {
+#pragma unroll
+      for (int m = 0; m < NSLOT; m++) w[(size_t)m * n + p] = (m == CP) ? 1.0 : 0.0;
+      continue;
+    }
+    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    double vol[NSLOT];
+#pragma unroll
+    for (int m = 0; m < NSLOT; m++) vol[m] = 0.0;
+    auto G = [&](int q, size_t at) { return g9[(size_t)q * n + at]; };
+    size_t pw = g.id(i - 1, j, k), ps = g.id(i, j - 1, k), pb = g.id(i, j, k - 1);
+    uint32_t cw = code[pw], cs = code[ps], cb = code[pb];
+    if (c & CODE_ACT_E) {
+      vol[CP] = __dsub_rn(vol[CP], G(0, p)); vol[EP] = __dadd_rn(vol[EP], G(0, p));
+      add_cross(vol, code_branch(c, 0, 0), G(1, p), true, CP, EP, NP, NE, SP, SE);
+      add_cross(vol, code_branch(c, 0, 1), G(2, p), true, CP, EP, TP, TE, BP, BE);
+    }
+    if (c & CODE_ACT_W) {
+      vol[CP] = __dsub_rn(vol[CP], G(0, pw)); vol[WP] = __dadd_rn(vol[WP], G(0, pw));
+      add_cross(vol, code_branch(cw, 0, 0), G(1, pw), false, CP, WP, NP, NW, SP, SW);
+      add_cross(vol, code_branch(cw, 0, 1), G(2, pw), false, CP, WP, TP, TW, BP, BW);
+    }
+    if (c & CODE_ACT_N) {
+      add_cross(vol, code_branch(c, 1, 0), G(3, p), true, CP, NP, EP, NE, WP, NW);
+      vol[CP] = __dsub_rn(vol[CP], G(4, p)); vol[NP] = __dadd_rn(vol[NP], G(4, p));
+      add_cross(vol, code_branch(c, 1, 1), G(5, p), true, CP, NP, TP, TN, BP, BN);
+    }
+    if (c & CODE_ACT_S) {
+      add_cross(vol, code_branch(cs, 1, 0), G(3, ps), false, CP, SP, EP, SE, WP, SW);
+      vol[CP] = __dsub_rn(vol[CP], G(4, ps)); vol[SP] = __dadd_rn(vol[SP], G(4, ps));
+      add_cross(vol, code_branch(cs, 1, 1), G(5, ps), false, CP, SP, TP, TS, BP, BS);
+    }
+    if (c & CODE_ACT_T) {
+      add_cross(vol, code_branch(c, 2, 0), G(6, p), true, CP, TP, EP, TE, WP, TW);
+      add_cross(vol, code_branch(c, 2, 1), G(7, p), true, CP, TP, NP, TN, SP, TS);
+      vol[CP] = __dsub_rn(vol[CP], G(8, p)); vol[TP] = __dadd_rn(vol[TP], G(8, p));
+    }
+    if (c & CODE_ACT_B) {
+      add_cross(vol, code_branch(cb, 2, 0), G(6, pb), false, CP, BP, EP, BE, WP, BW);
+      add_cross(vol, code_branch(cb, 2, 1), G(7, pb), false, CP, BP, NP, BN, SP, BS);
+      vol[CP] = __dsub_rn(vol[CP], G(8, pb)); vol[BP] = __dadd_rn(vol[BP], G(8, pb));
+    }
+    double a = -aj[p];
+#pragma unroll
+    for (int m = 0; m < NSLOT; m++) w[(size_t)m * n + p] = __dmul_rn(vol[m], a);
+  }
+}
+
+void launch_weights(const Geom &g, const double *g9, const double *aj, const double *nvert,
+                    const uint32_t *code, double *w64, cudaStream_t s) {
+  (void)nvert;
+  k_weights<<<nblk(g.n(), 128), 128, 0, s>>>(g, g9, aj, code, w64); count_launch();
+}
+
+// Thomas factors of the in-line (j) part of each row: a_j = w[SP], m_j, c'_j.
+// Couplings that wrap around a periodic y seam stay outside the line solve.
+__global__ void k_line_factors(Geom g, const double *__restrict__ w, double *__restrict__ l64,
+                               float *__restrict__ l32) {
+  size_t n = g.n();
+  int lines = g.mx * g.mz;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += gridDim.x * blockDim.x) {
+    int i = t % g.mx, k = t / g.mx;
+    double cprev = 0.0;
+    for (int j = 0; j < g.my; j++) {
+      size_t p = g.id(i, j, k);
+      double a = w[(size_t)SP * n + p], b = w[(size_t)CP * n + p], c = w[(size_t)NP * n + p];
+      if (j == 0 || j == g.my - 1) { a = 0.0; c = 0.0; b = 1.0; }
+      if (g.py && j == 1) a = 0.0;
+      if (g.py && j == g.my - 2) c = 0.0;
+      double m = b - a * cprev;
+      double minv = 1.0 / m;
+      double cp = c * minv;
+      l64[p] = a; l64[n + p] = minv; l64[2 * n + p] = cp;
+      l32[p] = (float)a; l32[n + p] = (float)minv; l32[2 * n + p] = (float)cp;
+      cprev = cp;
+    }
+  }
+}
+
+void launch_line_factors(const Geom &g, const double *w64, double *line64, float *line32,
+                         cudaStream_t s) {
+  int lines = g.mx * g.mz;
+  k_line_factors<<<nblk(lines, 128), 128, 0, s>>>(g, w64, line64, line32); count_launch();
+}
+
+__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
+    b[p] = (float)a[p];
+}
+void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s) {
+  k_to_f32<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n); count_launch();
+}
+void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s) { launch_to_f32(a, b, n, s); }
+
+__global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, size_t n) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
+    b[p] = (double)a[p];
+}
+void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s) {
+  k_to_f64<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n); count_launch();
+}
+
+// MyNvertRestriction (poisson.c:1662-1773): a coarse cell is blocked (1) when the
+// product of its 8 children's nvert exceeds 0.1; then a fluid coarse cell pinched
+// between blocked cells in all three directions is blocked too (second pass reads
+// the first pass's result, as the reference's G2L copy does).
+__global__ void k_nvert_pass1(Geom F, const double *__restrict__ nf, Geom C, int isc, int jsc, int ksc,
+                              double *__restrict__ nc) {
+  size_t n = C.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(p % C.mx), j = (int)((p / C.mx) % C.my), k = (int)(p / ((size_t)C.mx * C.my));
+    double v = 0.0;
+    if (i >= 1 && i <= C.mx - 2 && j >= 1 && j <= C.my - 2 && k >= 1 && k <= C.mz - 2) {
+      int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+      int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
+      auto N = [&](int a, int b, int c) { return nf[F.id(a, b, c)]; };
+      double prod = N(ih, jh, kh) * N(ih - ia, jh, kh) * N(ih, jh - ja, kh) * N(ih, jh, kh - ka) *
+                    N(ih - ia, jh - ja, kh) * N(ih - ia, jh, kh - ka) * N(ih, jh - ja, kh - ka) *
+                    N(ih - ia, jh - ja, kh - ka);
+      if (prod > 0.1) v = 1.0;
+    }
+    nc[p] = v;
+  }
+}
+__global__ void k_nvert_pass2(Geom C, const double *__restrict__ snap, double *__restrict__ nc) {
+  size_t n = C.n();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(p % C.mx), j = (int)((p / C.mx) % C.my), k = (int)(p / ((size_t)C.mx * C.my));
+    if (i >= 1 && i <= C.mx - 2 && j >= 1 && j <= C.my - 2 && k >= 1 && k <= C.mz - 2 && snap[p] < 0.1) {
+      if (snap[C.id(i + 1, j, k)] + snap[C.id(i - 1, j, k)] > 1.1 &&
+          snap[C.id(i, j + 1, k)] + snap[C.id(i, j - 1, k)] > 1.1 &&
+          snap[C.id(i, j, k + 1)] + snap[C.id(i, j, k - 1)] > 1.1)
+        nc[p] = 1.0;
+    }
+  }
+}
+
+void launch_nvert_restrict(const Geom &fine, const double *nvf, const Geom &coarse, int isc, int jsc,
+                           int ksc, double *nvc, double *tmp, cudaStream_t s) {
+  k_nvert_pass1<<<nblk(coarse.n(), 256), 256, 0, s>>>(fine, nvf, coarse, isc, jsc, ksc, tmp); count_launch();
+  cudaMemcpyAsync(nvc, tmp, sizeof(double) * coarse.n(), cudaMemcpyDeviceToDevice, s);
+  k_nvert_pass2<<<nblk(coarse.n(), 256), 256, 0, s>>>(coarse, tmp, nvc); count_launch();
+}
+
+}  // namespace cvb

@@ -1,0 +1,406 @@
+// The curvilinear pressure operator, its y-line smoother and the grid transfers.
+//
+// FP64: y = A x with the 19 stored weights per row (the reference's assembled
+//       PoissonLHSNew rows), 19 FMAs per cell -- the cheapest FP64 form on a
+//       part whose FP64 rate is a small fraction of its FP32 rate.
+// FP32: the same operator matrix-free in flux form: for each face the flux
+//       F = g_nn (x_Q - x_P) + two cross terms whose form (central / one-sided /
+//       none) comes from the cell's switching code; row P is
+//       -aj_P * (F_E - F_W + F_N - F_S + F_T - F_B), each term taken only where
+//       the face is active from P's side.  Reads 9 face coefficients, aj and a
+//       code per cell: ~52 B/cell.
+#include "cvb_internal.h"
+
+namespace cvb {
+
+static inline unsigned nblk(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ------------------------------------------------------------ neighbourhood
+// 32-bit offsets of the six face neighbours, with the reference's periodic wrap
+// of column indices (poisson.c:1329-1450) folded into the offset at seam cells.
+struct Off {
+  int e, w, n, s, t, b;
+};
+__device__ __forceinline__ Off offsets(const Geom &g, int i, int j, int k) {
+  const int sy = g.mx, sz = g.mx * g.my;
+  Off o;
+  o.e = (g.px && i == g.mx - 2) ? -(g.mx - 3) : 1;
+  o.w = (g.px && i == 1) ? (g.mx - 3) : -1;
+  o.n = (g.py && j == g.my - 2) ? -(g.my - 3) * sy : sy;
+  o.s = (g.py && j == 1) ? (g.my - 3) * sy : -sy;
+  o.t = (g.pz && k == g.mz - 2) ? -(g.mz - 3) * sz : sz;
+  o.b = (g.pz && k == 1) ? (g.mz - 3) * sz : -sz;
+  return o;
+}
+
+// The 19 values of x around an interior cell, in registers.
+template <typename T>
+struct Star {
+  T P, E, W, N, S, Tt, B, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW;
+};
+template <typename T, typename TX>
+__device__ __forceinline__ Star<T> load_star(const TX *__restrict__ x, int p, const Off &o) {
+  Star<T> s;
+  s.P = (T)x[p];
+  s.E = (T)x[p + o.e]; s.W = (T)x[p + o.w]; s.N = (T)x[p + o.n]; s.S = (T)x[p + o.s];
+  s.Tt = (T)x[p + o.t]; s.B = (T)x[p + o.b];
+  s.NE = (T)x[p + o.e + o.n]; s.SE = (T)x[p + o.e + o.s]; s.NW = (T)x[p + o.w + o.n]; s.SW = (T)x[p + o.w + o.s];
+  s.TN = (T)x[p + o.t + o.n]; s.BN = (T)x[p + o.b + o.n]; s.TS = (T)x[p + o.t + o.s]; s.BS = (T)x[p + o.b + o.s];
+  s.TE = (T)x[p + o.t + o.e]; s.BE = (T)x[p + o.b + o.e]; s.TW = (T)x[p + o.t + o.w]; s.BW = (T)x[p + o.b + o.w];
+  return s;
+}
+
+// ----------------------------------------------------------------- FP64 rows
+// (A x)_p with the 19 stored weights; identity rows return x_p.
+template <typename TX>
+__device__ __forceinline__ double row64(const Geom &g, const double *__restrict__ w, const uint32_t *__restrict__ code,
+                                        const TX *__restrict__ x, int i, int j, int k, int p, int n) {
+  if (__ldg(code + p) & CODE_IDENTITY) return (double)x[p];
+  Off o = offsets(g, i, j, k);
+  Star<double> s = load_star<double>(x, p, o);
+  const double *wp = w + p;
+  double r = wp[(size_t)CP * n] * s.P;
+  r = fma(wp[(size_t)EP * n], s.E, r); r = fma(wp[(size_t)WP * n], s.W, r);
+  r = fma(wp[(size_t)NP * n], s.N, r); r = fma(wp[(size_t)SP * n], s.S, r);
+  r = fma(wp[(size_t)TP * n], s.Tt, r); r = fma(wp[(size_t)BP * n], s.B, r);
+  r = fma(wp[(size_t)NE * n], s.NE, r); r = fma(wp[(size_t)SE * n], s.SE, r);
+  r = fma(wp[(size_t)NW * n], s.NW, r); r = fma(wp[(size_t)SW * n], s.SW, r);
+  r = fma(wp[(size_t)TN * n], s.TN, r); r = fma(wp[(size_t)BN * n], s.BN, r);
+  r = fma(wp[(size_t)TS * n], s.TS, r); r = fma(wp[(size_t)BS * n], s.BS, r);
+  r = fma(wp[(size_t)TE * n], s.TE, r); r = fma(wp[(size_t)BE * n], s.BE, r);
+  r = fma(wp[(size_t)TW * n], s.TW, r); r = fma(wp[(size_t)BW * n], s.BW, r);
+  return r;
+}
+
+// ----------------------------------------------------------------- FP32 rows
+// Cross term of a face flux: g * (cu*s_up + c0*s_level + cd*s_down) for the
+// central / lower / upper forms (branch 1/2/3), zero for branch 0.
+__device__ __forceinline__ float cross32(int br, float g, float su, float s0, float sd) {
+  float cu = br == 1 ? 0.25f : (br == 3 ? 0.5f : 0.0f);
+  float c0 = br == 2 ? 0.5f : (br == 3 ? -0.5f : 0.0f);
+  float cd = br == 1 ? -0.25f : (br == 2 ? -0.5f : 0.0f);
+  return g * (cu * su + c0 * s0 + cd * sd);
+}
+
+// (A x)_p in flux form: each active face flux from its cell's coefficients and
+// branch codes; the lower faces are the upper faces of the W/S/B neighbours.
+template <typename TX>
+__device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ gf, const float *__restrict__ aj,
+                                       const uint32_t *__restrict__ code, const TX *__restrict__ x, int i, int j,
+                                       int k, int p, int n) {
+  uint32_t c = __ldg(code + p);
+  if (c & CODE_IDENTITY) return (float)x[p];
+  Off o = offsets(g, i, j, k);
+  Star<float> s = load_star<float>(x, p, o);
+  const int pw = p - 1, ps = p - g.mx, pb = p - g.mx * g.my;  // lower neighbours (never wrapped)
+  float acc = 0.0f;
+  if (c & CODE_ACT_E) {
+    float f = gf[p] * (s.E - s.P);
+    f += cross32(code_branch(c, 0, 0), gf[n + p], s.N + s.NE, s.P + s.E, s.S + s.SE);
+    f += cross32(code_branch(c, 0, 1), gf[2 * n + p], s.Tt + s.TE, s.P + s.E, s.B + s.BE);
+    acc += f;
+  }
+  if (c & CODE_ACT_W) {
+    uint32_t cw = __ldg(code + pw);
+    float f = gf[pw] * (s.P - s.W);
+    f += cross32(code_branch(cw, 0, 0), gf[n + pw], s.NW + s.N, s.W + s.P, s.SW + s.S);
+    f += cross32(code_branch(cw, 0, 1), gf[2 * n + pw], s.TW + s.Tt, s.W + s.P, s.BW + s.B);
+    acc -= f;
+  }
+  if (c & CODE_ACT_N) {
+    float f = gf[4 * n + p] * (s.N - s.P);
+    f += cross32(code_branch(c, 1, 0), gf[3 * n + p], s.E + s.NE, s.P + s.N, s.W + s.NW);
+    f += cross32(code_branch(c, 1, 1), gf[5 * n + p], s.Tt + s.TN, s.P + s.N, s.B + s.BN);
+    acc += f;
+  }
+  if (c & CODE_ACT_S) {
+    uint32_t cs = __ldg(code + ps);
+    float f = gf[4 * n + ps] * (s.P - s.S);
+    f += cross32(code_branch(cs, 1, 0), gf[3 * n + ps], s.SE + s.E, s.S + s.P, s.SW + s.W);
+    f += cross32(code_branch(cs, 1, 1), gf[5 * n + ps], s.TS + s.Tt, s.S + s.P, s.BS + s.B);
+    acc -= f;
+  }
+  if (c & CODE_ACT_T) {
+    float f = gf[8 * n + p] * (s.Tt - s.P);
+    f += cross32(code_branch(c, 2, 0), gf[6 * n + p], s.E + s.TE, s.P + s.Tt, s.W + s.TW);
+    f += cross32(code_branch(c, 2, 1), gf[7 * n + p], s.N + s.TN, s.P + s.Tt, s.S + s.TS);
+    acc += f;
+  }
+  if (c & CODE_ACT_B) {
+    uint32_t cb = __ldg(code + pb);
+    float f = gf[8 * n + pb] * (s.P - s.B);
+    f += cross32(code_branch(cb, 2, 0), gf[6 * n + pb], s.BE + s.E, s.B + s.P, s.BW + s.W);
+    f += cross32(code_branch(cb, 2, 1), gf[7 * n + pb], s.BN + s.N, s.B + s.P, s.BS + s.S);
+    acc -= f;
+  }
+  return -aj[p] * acc;
+}
+
+// ------------------------------------------------------- apply / residual
+// y = A x (b == nullptr) or y = b - A x.  One thread per cell.
+template <typename TX>
+__global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restrict__ w, const uint32_t *__restrict__ code,
+                                                 const TX *__restrict__ x, const double *__restrict__ b,
+                                                 double *__restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= g.mx || j >= g.my) return;
+  int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
+  double ax = row64(g, w, code, x, i, j, k, p, n);
+  y[p] = b ? b[p] - ax : ax;
+}
+
+__global__ void __launch_bounds__(128) k_apply32(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
+                                                 const uint32_t *__restrict__ code, const float *__restrict__ x,
+                                                 const float *__restrict__ b, float *__restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= g.mx || j >= g.my) return;
+  int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
+  float ax = row32(g, gf, aj, code, x, i, j, k, p, n);
+  y[p] = b ? b[p] - ax : ax;
+}
+
+static dim3 grid3(const Geom &g) { return dim3(nblk(g.mx, 32), nblk(g.my, 4), g.mz); }
+static const dim3 kBlk(32, 4, 1);
+
+template <>
+void launch_apply<double>(const LevelDev &L, const double *x, double *y, cudaStream_t s) {
+  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y); count_launch();
+}
+template <>
+void launch_residual<double>(const LevelDev &L, const double *b, const double *x, double *r, cudaStream_t s) {
+  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, b, r); count_launch();
+}
+void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStream_t s) {
+  k_apply64<float><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y); count_launch();
+}
+template <>
+void launch_apply<float>(const LevelDev &L, const float *x, float *y, cudaStream_t s) {
+  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, nullptr, y); count_launch();
+}
+template <>
+void launch_residual<float>(const LevelDev &L, const float *b, const float *x, float *r, cudaStream_t s) {
+  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, b, r); count_launch();
+}
+
+// ------------------------------------------------------------ y-line smoother
+// One damped line-Jacobi sweep, fused: xnew = x + omega * T^-1 (b - A x), T the
+// tridiagonal in-line (j) part of A with Thomas factors from set-up.
+// A block owns a tile of TW consecutive i over all j at one k.  Phase 1: all
+// threads compute the tile's residual into shared memory and stage the three
+// factor arrays there (coalesced, many loads in flight).  Phase 2: TW threads
+// run the forward/backward recurrences out of shared memory, one line each.
+// Phase 3: all threads write x + omega*delta.  Zero guess: the residual is b.
+template <typename T>
+struct RowOf;
+template <>
+struct RowOf<float> {
+  __device__ static float r(const Geom &g, const LevelDev &L, const float *x, int i, int j, int k, int p, int n) {
+    return row32(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
+  }
+  __device__ static const float *fac(const LevelDev &L) { return L.line32; }
+};
+template <>
+struct RowOf<double> {
+  __device__ static double r(const Geom &g, const LevelDev &L, const double *x, int i, int j, int k, int p, int n) {
+    return row64(g, L.w64, L.code, x, i, j, k, p, n);
+  }
+  __device__ static const double *fac(const LevelDev &L) { return L.line64; }
+};
+
+template <typename T, int TW>
+__global__ void __launch_bounds__(256) k_line_sweep(LevelDev L, const T *__restrict__ b, const T *__restrict__ x,
+                                                    T *__restrict__ xnew, T omega, int zero_guess) {
+  extern __shared__ unsigned char smem_raw[];
+  T *sr = reinterpret_cast<T *>(smem_raw);  // [my][TW] residual, then delta
+  const Geom g = L.g;
+  const int my = g.my, n = (int)g.n();
+  T *sa = sr + my * TW, *sm = sa + my * TW, *sc = sm + my * TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int i = blockIdx.x * TW + tx, k = blockIdx.y;
+  const bool inside_i = i < g.mx;
+  const bool line = inside_i && i >= 1 && i <= g.mx - 2 && k >= 1 && k <= g.mz - 2;
+  const T *fa = RowOf<T>::fac(L);
+  for (int j = ty; j < my; j += ny) {
+    int p = (k * my + j) * g.mx + i;
+    T r = T(0), a = T(0), m = T(1), c = T(0);
+    if (line && j >= 1 && j <= my - 2) {
+      r = zero_guess ? b[p] : b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n);
+      a = fa[p]; m = fa[n + p]; c = fa[2 * n + p];
+    }
+    sr[j * TW + tx] = r; sa[j * TW + tx] = a; sm[j * TW + tx] = m; sc[j * TW + tx] = c;
+  }
+  __syncthreads();
+  if (ty == 0 && line) {
+    T d = T(0);
+    for (int j = 1; j <= my - 2; j++) {
+      d = (sr[j * TW + tx] - sa[j * TW + tx] * d) * sm[j * TW + tx];
+      sr[j * TW + tx] = d;
+    }
+    T dn = T(0);
+    for (int j = my - 2; j >= 1; j--) {
+      dn = sr[j * TW + tx] - sc[j * TW + tx] * dn;
+      sr[j * TW + tx] = dn;
+    }
+  }
+  __syncthreads();
+  if (!inside_i) return;
+  for (int j = ty; j < my; j += ny) {
+    int p = (k * my + j) * g.mx + i;
+    T d = sr[j * TW + tx];
+    T xo = zero_guess ? T(0) : x[p];
+    xnew[p] = (line && j >= 1 && j <= my - 2) ? xo + omega * d : xo;
+  }
+}
+
+template <typename T, int TW>
+static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T omega, int zero_guess, cudaStream_t s) {
+  size_t smem = sizeof(T) * 4 * (size_t)L.g.my * TW;
+  dim3 grd(nblk(L.g.mx, TW), L.g.mz);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_line_sweep<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  k_line_sweep<T, TW><<<grd, 256, smem, s>>>(L, b, x, xnew, omega, zero_guess); count_launch();
+}
+
+// Lines longer than the shared-memory tile allows fall back to a residual
+// kernel plus a one-thread-per-line Thomas kernel.
+template <typename T>
+__global__ void k_line_thomas(Geom g, const T *__restrict__ fac, const T *__restrict__ r,
+                              const T *__restrict__ x, T *__restrict__ xnew, T omega, int zero_guess) {
+  size_t n = g.n();
+  int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.mx || k >= g.mz) return;
+  bool ring = (i == 0 || i == g.mx - 1 || k == 0 || k == g.mz - 1);
+  if (ring) {
+    for (int j = 0; j < g.my; j++) {
+      size_t p = g.id(i, j, k);
+      xnew[p] = zero_guess ? T(0) : x[p];
+    }
+    return;
+  }
+  const T *a = fac, *minv = fac + n, *cp = fac + 2 * n;
+  T dprev = T(0);
+  size_t p0 = g.id(i, 0, k);
+  xnew[p0] = zero_guess ? T(0) : x[p0];
+  for (int j = 1; j <= g.my - 2; j++) {
+    size_t p = g.id(i, j, k);
+    T d = (r[p] - a[p] * dprev) * minv[p];
+    xnew[p] = d;
+    dprev = d;
+  }
+  size_t pe = g.id(i, g.my - 1, k);
+  xnew[pe] = zero_guess ? T(0) : x[pe];
+  T dn = T(0);
+  for (int j = g.my - 2; j >= 1; j--) {
+    size_t p = g.id(i, j, k);
+    T d = xnew[p] - cp[p] * dn;
+    dn = d;
+    xnew[p] = zero_guess ? omega * d : x[p] + omega * d;
+  }
+}
+
+static const int kMaxFusedRows = 400;
+
+template <>
+void launch_line_smooth<float>(const LevelDev &L, const float *b, const float *x, float *xnew, float omega,
+                               int zero_guess, cudaStream_t s) {
+  if (L.g.my <= kMaxFusedRows) { line_sweep<float, 32>(L, b, x, xnew, omega, zero_guess, s); return; }
+  const float *r = b;
+  if (!zero_guess) { launch_residual<float>(L, b, x, L.t32, s); r = L.t32; }
+  dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
+  k_line_thomas<float><<<grd, blk, 0, s>>>(L.g, L.line32, r, x, xnew, omega, zero_guess); count_launch();
+}
+template <>
+void launch_line_smooth<double>(const LevelDev &L, const double *b, const double *x, double *xnew, double omega,
+                                int zero_guess, cudaStream_t s) {
+  if (L.g.my <= kMaxFusedRows) { line_sweep<double, 16>(L, b, x, xnew, omega, zero_guess, s); return; }
+  const double *r = b;
+  if (!zero_guess) { launch_residual<double>(L, b, x, L.t64, s); r = L.t64; }
+  dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
+  k_line_thomas<double><<<grd, blk, 0, s>>>(L.g, L.line64, r, x, xnew, omega, zero_guess); count_launch();
+}
+
+// ------------------------------------------------------------------ transfers
+// Products in the transfers are rounded on their own (no fused multiply-add), as
+// the reference's C evaluates them, so FP64 transfers match it bit for bit.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+// MyRestriction (poisson.c:129-226): coarse = 0.125 * sum over the 8 children of
+// x * max(0, 1 - nvert_fine); zero on the ring and on blocked coarse cells.
+template <typename T>
+__global__ void k_restrict(Geom F, const double *__restrict__ nvf, Geom C, const double *__restrict__ nvc,
+                           int isc, int jsc, int ksc, const T *__restrict__ xf, T *__restrict__ xc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= C.mx || j >= C.my) return;
+  size_t p = C.id(i, j, k);
+  if (i == 0 || i == C.mx - 1 || j == 0 || j == C.my - 1 || k == 0 || k == C.mz - 1 || nvc[p] > 0.1) {
+    xc[p] = T(0);
+    return;
+  }
+  int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+  int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
+  auto W = [&](int a, int b, int c) {
+    size_t q = F.id(a, b, c);
+    double wt = 1.0 - nvf[q];
+    return mul_rn(xf[q], (T)(wt > 0.0 ? wt : 0.0));
+  };
+  T s = W(ih, jh, kh);
+  s = add_rn(s, W(ih - ia, jh, kh));
+  s = add_rn(s, W(ih, jh - ja, kh));
+  s = add_rn(s, W(ih, jh, kh - ka));
+  s = add_rn(s, W(ih - ia, jh - ja, kh));
+  s = add_rn(s, W(ih, jh - ja, kh - ka));
+  s = add_rn(s, W(ih - ia, jh, kh - ka));
+  s = add_rn(s, W(ih - ia, jh - ja, kh - ka));
+  xc[p] = mul_rn(T(0.125), s);
+}
+
+// MyInterpolation (poisson.c:228-370), added into xf: cell-centred trilinear
+// weights 27/9/9/3/9/3/3/1 over 64 toward the neighbour on the child's side,
+// falling back to injection next to walls and blocked coarse cells.
+template <typename T>
+__global__ void k_prolong_add(Geom C, const double *__restrict__ nvc, Geom F, const double *__restrict__ nvf,
+                              int isc, int jsc, int ksc, const T *__restrict__ xc, T *__restrict__ xf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= F.mx || j >= F.my) return;
+  size_t p = F.id(i, j, k);
+  if (i == 0 || i == F.mx - 1 || j == 0 || j == F.my - 1 || k == 0 || k == F.mz - 1 || nvf[p] > 0.1) return;
+  int ic, jc, kc, ia, ja, ka;
+  if (isc) { ic = i; ia = 0; } else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == F.mx - 2) ia = 0; }
+  if (jsc) { jc = j; ja = 0; } else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == F.my - 2) ja = 0; }
+  if (ksc) { kc = k; ka = 0; } else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == F.mz - 2) ka = 0; }
+  if (ka == -1 && nvc[C.id(ic, jc, kc - 1)] > 0.1) ka = 0;
+  else if (ka == 1 && nvc[C.id(ic, jc, kc + 1)] > 0.1) ka = 0;
+  if (ja == -1 && nvc[C.id(ic, jc - 1, kc)] > 0.1) ja = 0;
+  else if (ja == 1 && nvc[C.id(ic, jc + 1, kc)] > 0.1) ja = 0;
+  if (ia == -1 && nvc[C.id(ic - 1, jc, kc)] > 0.1) ia = 0;
+  else if (ia == 1 && nvc[C.id(ic + 1, jc, kc)] > 0.1) ia = 0;
+  auto X = [&](int a, int b, int c) { return xc[C.id(a, b, c)]; };
+  T s1 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc), T(9)), mul_rn(X(ic, jc + ja, kc), T(3))),
+                       mul_rn(X(ic + ia, jc, kc), T(3))), X(ic + ia, jc + ja, kc));
+  T s2 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc + ka), T(9)), mul_rn(X(ic, jc + ja, kc + ka), T(3))),
+                       mul_rn(X(ic + ia, jc, kc + ka), T(3))), X(ic + ia, jc + ja, kc + ka));
+  T v = add_rn(div_rn(mul_rn(s1, T(3)), T(64)), div_rn(s2, T(64)));
+  xf[p] = add_rn(xf[p], v);
+}
+
+template <typename T>
+void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s) {
+  k_restrict<T><<<grid3(C.g), kBlk, 0, s>>>(F.g, F.nvert, C.g, C.nvert, C.isc, C.jsc, C.ksc, xf, xc); count_launch();
+}
+template <typename T>
+void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s) {
+  k_prolong_add<T><<<grid3(F.g), kBlk, 0, s>>>(C.g, C.nvert, F.g, F.nvert, F.isc, F.jsc, F.ksc, xc, xf); count_launch();
+}
+template void launch_restrict<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t);
+template void launch_restrict<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t);
+template void launch_prolong_add<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t);
+template void launch_prolong_add<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t);
+
+}  // namespace cvb

@@ -1,0 +1,221 @@
+"""Python front-end of the cvb C ABI, named after the reference routines it replaces.
+
+    ctx = PoissonContext()
+    ctx.setup(problem)                       # MG_Initial's hierarchy -> device (once)
+    phi, stats = ctx.poisson_solver_mg(ucont, dt, st)   # PoissonSolver_MG (poisson.c:1775)
+    ctx.update_pressure(p, phi)              # UpdatePressure (poisson.c:2908)
+    ctx.projection(phi, dt, st, ucont)       # Projection (poisson.c:2281)
+
+Every call goes through libcvb.so; errors raise CvbError with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import CvbError, LevelDesc, default_opts, ptr
+
+_FIELDS = {"icsi": "ICsi", "ieta": "IEta", "izet": "IZet", "jcsi": "JCsi", "jeta": "JEta", "jzet": "JZet",
+           "kcsi": "KCsi", "keta": "KEta", "kzet": "KZet", "iaj": "IAj", "jaj": "JAj", "kaj": "KAj",
+           "aj": "Aj", "csi": "Csi", "eta": "Eta", "zet": "Zet"}
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class PoissonContext:
+    """One CURVIB block's pressure-projection path resident on one GPU."""
+
+    def __init__(self, device: int = 0, stream=None):
+        L = _lib.lib()
+        self._L = L
+        self._ctx = ctypes.c_void_p()
+        o = _lib.Options()
+        o.device = device
+        o.stream = stream
+        rc = L.cvb_init(ctypes.byref(self._ctx), ctypes.byref(o))
+        if rc:
+            msg = L.cvb_last_error(self._ctx).decode()
+            L.cvb_destroy(self._ctx)
+            self._ctx = None
+            raise CvbError(rc, msg)
+        self._keep = []
+        self.shapes = []
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.cvb_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
+
+    # ------------------------------------------------------------------ setup
+    def setup(self, problem, ghosts=None):
+        """Upload the hierarchy of a workload.Problem (levels coarsest first).
+
+        ``ghosts``: optional per-level (gxs, gys, gzs) offsets; the arrays of the
+        problem are then expected to be ghosted local arrays of that box.
+        """
+        levels = problem.metrics
+        n = len(levels)
+        descs = (LevelDesc * n)()
+        keep = []
+        for l, m in enumerate(levels):
+            d = descs[l]
+            mz, my, mx = m["Aj"].shape[:3] if ghosts is None else problem.box_shapes[l]
+            d.mx, d.my, d.mz = mx, my, mz
+            if ghosts is None:
+                d.gxs = d.gys = d.gzs = 0
+                d.gxm, d.gym, d.gzm = mx, my, mz
+            else:
+                gx, gy, gz = ghosts[l]
+                d.gxs, d.gys, d.gzs = gx, gy, gz
+                sh = m["Aj"].shape
+                d.gzm, d.gym, d.gxm = sh[0], sh[1], sh[2]
+            for q in range(6):
+                d.bctype[q] = int(problem.bctype[q])
+            d.isc, d.jsc, d.ksc = (int(v) for v in problem.semi)
+            for f, nm in _FIELDS.items():
+                if nm in m and (nm not in ("Csi", "Eta", "Zet") or l == n - 1):
+                    a = _c64(m[nm])
+                    keep.append(a)
+                    setattr(d, f, ptr(a))
+        nv = _c64(problem.nvert)
+        keep.append(nv)
+        self._check(self._L.cvb_setup_hierarchy(self._ctx, n, descs, ptr(nv)))
+        self.shapes = []
+        for l in range(n):
+            a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            self._L.cvb_level_dims(self._ctx, l, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+            self.shapes.append((c.value, b.value, a.value))
+        self.nlevels = n
+        return self
+
+    def set_nvert(self, nvert):
+        a = _c64(nvert)
+        self._check(self._L.cvb_set_nvert(self._ctx, ptr(a)))
+
+    def get_nvert(self, level):
+        out = np.zeros(self.shapes[level])
+        mns = ctypes.c_int()
+        self._check(self._L.cvb_get_nvert(self._ctx, level, ptr(out), ctypes.byref(mns)))
+        return out, bool(mns.value)
+
+    # --------------------------------------------------------------- the path
+    def volume_flux_rev(self, ucont, flux_intp_sum=0.0, flg=1):
+        uc = np.array(ucont, dtype=np.float64, order="C", copy=True)
+        f, a = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.cvb_volume_flux_rev(self._ctx, ptr(uc), flux_intp_sum, flg, ctypes.byref(f),
+                                                ctypes.byref(a)))
+        return uc, f.value, a.value
+
+    def poisson_rhs(self, ucont, dt, st):
+        uc = _c64(ucont)
+        b = np.zeros(self.shapes[-1])
+        s = ctypes.c_double()
+        self._check(self._L.cvb_poisson_rhs(self._ctx, ptr(uc), dt, st, ptr(b), ctypes.byref(s)))
+        return b, s.value
+
+    def solve(self, b, phi0=None, check=True, **opts):
+        o = default_opts(**opts)
+        bb = _c64(b)
+        phi = np.zeros(self.shapes[-1]) if phi0 is None else np.array(phi0, dtype=np.float64, order="C", copy=True)
+        if phi0 is not None:
+            o.warm_start = 1
+        st = _lib.SolveStats()
+        rc = self._L.cvb_poisson_solve(self._ctx, ptr(bb), ptr(phi), ctypes.byref(o), ctypes.byref(st))
+        if check and rc not in (0,):
+            raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
+        return phi, st.as_dict()
+
+    def poisson_solver_mg(self, ucont, dt, st, immersed=1, flux_intp_sum=0.0, **opts):
+        """PoissonSolver_MG: VolumeFlux_rev, PoissonRHS and the solve.  Returns
+        (phi, corrected ucont, stats)."""
+        o = default_opts(**opts)
+        uc = np.array(ucont, dtype=np.float64, order="C", copy=True)
+        phi = np.zeros(self.shapes[-1])
+        s = _lib.SolveStats()
+        self._check(self._L.cvb_poisson_solver_mg(self._ctx, ptr(uc), flux_intp_sum, immersed, dt, st, ptr(phi),
+                                                  ctypes.byref(o), ctypes.byref(s)))
+        return phi, uc, s.as_dict()
+
+    def update_pressure(self, p, phi):
+        pp = np.array(p, dtype=np.float64, order="C", copy=True)
+        ph = np.array(phi, dtype=np.float64, order="C", copy=True)
+        self._check(self._L.cvb_update_pressure(self._ctx, ptr(pp), ptr(ph)))
+        return pp, ph
+
+    def projection(self, phi, dt, st, ucont):
+        uc = np.array(ucont, dtype=np.float64, order="C", copy=True)
+        self._check(self._L.cvb_projection(self._ctx, ptr(_c64(phi)), dt, st, ptr(uc)))
+        return uc
+
+    # ------------------------------------------------------- resident solves
+    def device_rhs(self):
+        return self._L.cvb_device_rhs(self._ctx)
+
+    def device_phi(self):
+        return self._L.cvb_device_phi(self._ctx)
+
+    def stream(self):
+        return self._L.cvb_stream(self._ctx)
+
+    def solve_resident(self, check=True, **opts):
+        o = default_opts(**opts)
+        st = _lib.SolveStats()
+        rc = self._L.cvb_solve_resident(self._ctx, ctypes.byref(o), ctypes.byref(st))
+        if check and rc:
+            raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
+        return st.as_dict()
+
+    def time_kernel(self, name, level=-1, reps=20):
+        """(average ms per launch, algorithmic bytes per launch) of one kernel."""
+        lvl = level % self.nlevels
+        ms, by = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.cvb_time_kernel(self._ctx, _lib.KERNELS[name], lvl, reps, ctypes.byref(ms),
+                                            ctypes.byref(by)))
+        return ms.value, by.value
+
+    # ---------------------------------------------------------- parity hooks
+    def apply(self, level, x):
+        xx = _c64(x)
+        y = np.zeros(self.shapes[level])
+        self._check(self._L.cvb_apply_operator(self._ctx, level, ptr(xx), ptr(y)))
+        return y
+
+    def apply_f32(self, level, x):
+        xx = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros(self.shapes[level], dtype=np.float32)
+        self._check(self._L.cvb_apply_operator_f32(self._ctx, level, ptr(xx), ptr(y)))
+        return y
+
+    def weights(self, level):
+        w = np.zeros((19,) + self.shapes[level])
+        self._check(self._L.cvb_get_weights(self._ctx, level, ptr(w)))
+        return w
+
+    def restrict(self, coarse, xf):
+        out = np.zeros(self.shapes[coarse])
+        self._check(self._L.cvb_restrict(self._ctx, coarse, ptr(_c64(xf)), ptr(out)))
+        return out
+
+    def interpolate(self, fine, xc):
+        out = np.zeros(self.shapes[fine])
+        self._check(self._L.cvb_interpolate(self._ctx, fine, ptr(_c64(xc)), ptr(out)))
+        return out
+
+    def nullspace(self, level, x):
+        y = np.array(x, dtype=np.float64, order="C", copy=True)
+        self._check(self._L.cvb_nullspace(self._ctx, level, ptr(y)))
+        return y

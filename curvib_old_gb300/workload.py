@@ -464,11 +464,11 @@ def smoothed_noise_ucont(m: dict, per, sigma: float, passes: int, rng) -> np.nda
         pad = np.pad(v, [(1, 1), (1, 1), (1, 1), (0, 0)],
                      mode="edge")
         if per[2]:
-            pad[0], pad[-1] = v[-1], v[0]
+            pad[0], pad[-1] = pad[-2].copy(), pad[1].copy()
         if per[1]:
-            pad[:, 0], pad[:, -1] = pad[:, -2], pad[:, 1]
+            pad[:, 0], pad[:, -1] = pad[:, -2].copy(), pad[:, 1].copy()
         if per[0]:
-            pad[:, :, 0], pad[:, :, -1] = pad[:, :, -2], pad[:, :, 1]
+            pad[:, :, 0], pad[:, :, -1] = pad[:, :, -2].copy(), pad[:, :, 1].copy()
         nb = (pad[2:, 1:-1, 1:-1] + pad[:-2, 1:-1, 1:-1] + pad[1:-1, 2:, 1:-1] + pad[1:-1, :-2, 1:-1]
               + pad[1:-1, 1:-1, 2:] + pad[1:-1, 1:-1, :-2]) / 6.0
         v = v + (2.0 / 3.0) * (nb - v)
@@ -525,3 +525,85 @@ def compatible(b: np.ndarray, aj: np.ndarray, nvert: np.ndarray) -> np.ndarray:
     out = b.copy()
     out[fl] -= aj[fl] * c
     return out
+
+
+# ------------------------------------------------------------------ problems
+class Problem:
+    """One block's inputs for the path: per-level metrics (coarsest first), the
+    finest level's nvert and fluxes, boundary types and semi-coarsening flags."""
+
+    def __init__(self, metrics, nvert, ucont, bctype, semi=(0, 0, 0), per=(False, False, False), name=""):
+        self.metrics = metrics
+        self.nvert = nvert
+        self.ucont = ucont
+        self.bctype = list(bctype)
+        self.semi = tuple(semi)
+        self.per = tuple(per)
+        self.name = name
+        self.b = None
+
+    @property
+    def shape(self):
+        return self.nvert.shape
+
+    @property
+    def unknowns(self):
+        mz, my, mx = self.shape
+        return (mx - 2) * (my - 2) * (mz - 2)
+
+
+def auto_levels(cells, per=(False, False, False), semi=(0, 0, 0), max_coarse_box=600):
+    """Number of levels: halve while every halved direction stays even-divisible,
+    keeps >= 2 cells (>= 3 when periodic) and the coarsest box (ring included)
+    is still larger than ``max_coarse_box``."""
+    c = list(cells)
+    levels = 1
+    while True:
+        nxt = [ci if s else ci // 2 for ci, s in zip(c, semi)]
+        ok = all(s or (ci % 2 == 0 and ci // 2 >= (3 if p else 2)) for ci, p, s in zip(c, per, semi))
+        if not ok or (c[0] + 2) * (c[1] + 2) * (c[2] + 2) <= max_coarse_box:
+            return levels
+        c = nxt
+        levels += 1
+
+
+def make_problem(cells, lengths=(1.0, 1.0, 1.0), beta_y=0.0, distort=False, per=(False, False, False),
+                 spheres=(), nlevels=None, semi=(0, 0, 0), velocity="taylor_green", seed=0, name=""):
+    per = tuple(bool(p) for p in per)
+    if nlevels is None:
+        nlevels = auto_levels(cells, per, semi)
+    nodes = box_nodes(cells, lengths, beta_y, distort)
+    coords = level_coordinates(nodes, nlevels, semi)
+    mets = [form_metrics(c, per) for c in coords]
+    nv = sphere_nvert(mets[-1]["Cent"], list(spheres))
+    if velocity == "taylor_green":
+        uc = ucont_from_velocity(mets[-1], taylor_green, per)
+    else:
+        uc = smoothed_noise_ucont(mets[-1], per, 0.1, 3, np.random.default_rng(seed))
+    bct = [7 if per[0] else 1] * 2 + [7 if per[1] else 1] * 2 + [7 if per[2] else 1] * 2
+    return Problem(mets, nv, uc, bct, semi, per, name)
+
+
+def config0_problem(n=64):
+    """64^3 box on [0,1]^3, tanh stretching 2.0 in y, sin distortion, sphere r=0.15 at the centre."""
+    return make_problem((n, n, n), (1.0, 1.0, 1.0), 2.0, True, (False, False, False),
+                        [(0.5, 0.5, 0.5, 0.15)], name=f"box{n}^3-sphere")
+
+
+def config1_problem(cells=(256, 128, 128)):
+    """Channel: periodic x and z, walls in y with tanh stretching 2.5, no body.
+    The box is 2pi x 2 x pi (a standard minimal-channel size; the grid and the
+    stretching are the fixed part of the workload)."""
+    return make_problem(cells, (2 * np.pi, 2.0, np.pi), 2.5, False, (True, False, True), [],
+                        velocity="noise", seed=1, name="channel%dx%dx%d" % tuple(cells))
+
+
+def noisy_rhs(b, nvert, aj, dt, seed, amp=1e-2):
+    """Add seeded uniform noise in [-amp, amp], scaled by 1/dt, on fluid cells, then
+    make the result compatible with the Neumann operator."""
+    rng = np.random.default_rng(seed)
+    fl = np.zeros(b.shape, dtype=bool)
+    fl[1:-1, 1:-1, 1:-1] = nvert[1:-1, 1:-1, 1:-1] < 0.1
+    out = b.copy()
+    out[fl] += rng.uniform(-amp, amp, size=int(fl.sum())) / dt
+    return compatible(out, aj, nvert)

@@ -1,0 +1,185 @@
+/*
+ * cvb -- GB300 implementation of CURVIB's pressure-projection path behind a C ABI.
+ *
+ * Replaces, for one block on one GPU, the reference routines of poisson.c:
+ *   PoissonRHS        (poisson.c:1509)  -> cvb_poisson_rhs
+ *   PoissonLHSNew     (poisson.c:600)   -> built once by cvb_setup_hierarchy,
+ *                                          applied matrix-free (cvb_apply_operator)
+ *   PoissonSolver_MG  (poisson.c:1775)  -> cvb_poisson_solver_mg / cvb_poisson_solve
+ *   VolumeFlux_rev    (poisson.c:3712)  -> cvb_volume_flux_rev
+ *   MyNvertRestriction(poisson.c:1662), FullyBlocked (poisson.c:1578)
+ *                                       -> cvb_setup_hierarchy / cvb_set_nvert
+ *   UpdatePressure    (poisson.c:2908)  -> cvb_update_pressure
+ *   Projection        (poisson.c:2281)  -> cvb_projection (flux correction; the
+ *                                          trailing Contra2Cart/GhostNodeVelocity
+ *                                          stay with the caller)
+ *
+ * Conventions
+ *  - Every entry point returns a cvb_status (0 = success, as PetscErrorCode).
+ *    cvb_last_error() describes the last failure of a context.
+ *  - Arrays are the reference's DMDA layouts, index [k][j][i] with i fastest and
+ *    the boundary ring included (mx = IM+1 for IM grid nodes):
+ *      * level metrics and nvert: the ghosted local arrays (lICsi, lAj, lNvert,
+ *        ...) covering the box gxs..gxs+gxm-1 etc. given in cvb_level_desc;
+ *      * vector fields (Ucont, B, P, Phi): the owned box [mz][my][mx], Ucont as
+ *        Cmpnts (x,y,z interleaved).
+ *  - Host pointers are caller-owned and only read/written during the call.
+ *    Device buffers belong to the context and stay resident across calls.
+ *  - A context is not reentrant; distinct contexts may be used from distinct
+ *    threads (each runs on its own CUDA stream).
+ */
+#ifndef CVB_H
+#define CVB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cvb_ctx cvb_ctx;
+
+typedef enum {
+  CVB_OK = 0,
+  CVB_NOT_CONVERGED = 1, /* iteration budget exhausted above the tolerance */
+  CVB_NAN_DETECTED = 2,  /* a NaN/Inf appeared in the residual */
+  CVB_OOM = 3,           /* device allocation failed */
+  CVB_BAD_INPUT = 4,     /* inconsistent sizes, missing arrays, bad options */
+  CVB_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+  CVB_CUDA_ERROR = 6,    /* any other CUDA runtime error */
+  CVB_NOT_SETUP = 7      /* cvb_setup_hierarchy has not run */
+} cvb_status;
+
+typedef enum { CVB_PRECISION_FP64 = 0, CVB_PRECISION_MIXED = 1 } cvb_precision;
+
+typedef struct {
+  int device;   /* CUDA device ordinal */
+  void *stream; /* cudaStream_t to issue work on; NULL: the context creates one */
+} cvb_options;
+
+/* One multigrid level: a PETSc-free mirror of the UserCtx fields the path reads
+ * (variables.h:155-304).  Level 0 is the coarsest, as mgctx[0] (init.c:839). */
+typedef struct {
+  int mx, my, mz;                   /* DMDALocalInfo mx, my, mz */
+  int gxs, gys, gzs, gxm, gym, gzm; /* ghosted box covered by the arrays below */
+  int bctype[6];                    /* UserCtx.bctype; 7 = periodic */
+  int isc, jsc, ksc;                /* semi-coarsening flags of this level */
+  const double *icsi, *ieta, *izet; /* lICsi, lIEta, lIZet (Cmpnts) */
+  const double *jcsi, *jeta, *jzet; /* lJCsi, lJEta, lJZet */
+  const double *kcsi, *keta, *kzet; /* lKCsi, lKEta, lKZet */
+  const double *iaj, *jaj, *kaj;    /* lIAj, lJAj, lKAj */
+  const double *aj;                 /* lAj */
+  const double *csi, *eta, *zet;    /* lCsi, lEta, lZet: finest level only, else NULL */
+} cvb_level_desc;
+
+/* Solver controls.  The reference reads the equivalent -ps_ksp_* options from
+ * control.dat (poisson.c:1829, 1975; control.dat rtol/atol/max_it). */
+typedef struct {
+  int precision;       /* cvb_precision: FP64 throughout, or FP32 V-cycles in FP64 FGMRES */
+  double rtol;         /* stop when ||b - A phi|| <= rtol ||b|| ... */
+  double atol;         /* ... or <= atol */
+  int max_it;          /* total FGMRES iterations */
+  int restart;         /* FGMRES restart length (<= 64) */
+  int pre_sweeps;      /* y-line Jacobi sweeps before / after the coarse correction */
+  int post_sweeps;
+  double omega;        /* line-Jacobi damping */
+  int project_rhs;     /* remove b's component outside range(A) (fluid-weighted mean of b/aj) */
+  int warm_start;      /* use phi's input values as the initial guess */
+  int coarse_dense_max;/* largest coarsest-level box solved exactly by a dense inverse */
+  int cgs_refine;      /* 1: second Gram-Schmidt pass when the first cancels most of w
+                          (PETSc's KSPGMRESSetCGSRefinementType IFNEEDED); 0: never (its default) */
+} cvb_solve_opts;
+
+typedef struct {
+  int status;            /* cvb_status of the solve */
+  int iterations;        /* FGMRES iterations (preconditioner applications) */
+  int restarts;
+  double rel_residual;   /* true ||b - A phi|| / ||b|| at exit (FP64) */
+  double abs_residual;
+  double rhs_norm;
+  double rhs_projected;  /* size of the removed incompatible part of b, relative to ||b|| */
+  double device_ms;      /* time on the device between the solve's first and last kernel */
+} cvb_solve_stats;
+
+int cvb_solve_opts_default(cvb_solve_opts *opts);
+
+/* --- context ------------------------------------------------------------- */
+int cvb_init(cvb_ctx **ctx, const cvb_options *opts);
+void cvb_destroy(cvb_ctx *ctx);
+const char *cvb_last_error(const cvb_ctx *ctx);
+
+/* Upload the metrics of every level, restrict nvert down the hierarchy
+ * (MyNvertRestriction + FullyBlocked), build each level's operator
+ * (PoissonLHSNew), the smoother factors and the coarsest-level solver.
+ * nvert_finest covers the finest level's ghosted box.  The reference rebuilds
+ * all of this inside every PoissonSolver_MG call; here it stays resident. */
+int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *levels,
+                        const double *nvert_finest);
+/* The immersed body moved: redo the nvert restriction and rebuild the operators. */
+int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest);
+/* Restricted nvert of one level ([mz][my][mx]) and the FullyBlocked result. */
+int cvb_get_nvert(cvb_ctx *ctx, int level, double *nvert, int *multinullspace);
+int cvb_level_dims(const cvb_ctx *ctx, int level, int *mx, int *my, int *mz);
+
+/* --- the path ------------------------------------------------------------ */
+/* VolumeFlux_rev (poisson.c:3712): ucont corrected in place; flux/area are the
+ * sums after the correction, as the reference leaves them in ibm_Flux/ibm_Area. */
+int cvb_volume_flux_rev(cvb_ctx *ctx, double *ucont, double flux_intp_sum, int flg, double *flux,
+                        double *area);
+/* PoissonRHS (poisson.c:1509); compat_sum is the sum it prints ("Summation RHS"). */
+int cvb_poisson_rhs(cvb_ctx *ctx, const double *ucont, double dt, double st, double *b,
+                    double *compat_sum);
+/* The multigrid-preconditioned FGMRES solve of A phi = b (KSPSolve, poisson.c:1983),
+ * phi returned with the fluid mean removed and zero outside the fluid
+ * (PoissonNullSpaceFunction, poisson.c:372). */
+int cvb_poisson_solve(cvb_ctx *ctx, const double *b, double *phi, const cvb_solve_opts *opts,
+                      cvb_solve_stats *stats);
+/* Drop-in for PoissonSolver_MG (poisson.c:1775): VolumeFlux_rev(flg = immersed),
+ * PoissonRHS(dt, st), then the solve.  ucont is corrected in place. */
+int cvb_poisson_solver_mg(cvb_ctx *ctx, double *ucont, double flux_intp_sum, int immersed, double dt,
+                          double st, double *phi, const cvb_solve_opts *opts, cvb_solve_stats *stats);
+/* UpdatePressure (poisson.c:2908): p += phi, periodic ring copies of p and phi. */
+int cvb_update_pressure(cvb_ctx *ctx, double *p, double *phi);
+/* Projection's flux correction (poisson.c:2281-2900) with phi as UpdatePressure left it. */
+int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont);
+
+/* --- device-resident form (inputs already in HBM) ---------------------- */
+/* Device pointers of the context's finest-level rhs and solution ([mz][my][mx] FP64). */
+double *cvb_device_rhs(cvb_ctx *ctx);
+double *cvb_device_phi(cvb_ctx *ctx);
+/* Solve the context's resident rhs into its resident phi. */
+int cvb_solve_resident(cvb_ctx *ctx, const cvb_solve_opts *opts, cvb_solve_stats *stats);
+/* The context's CUDA stream (cudaStream_t). */
+void *cvb_stream(cvb_ctx *ctx);
+
+/* --- parity hooks ------------------------------------------------------- */
+/* y = A_level x in FP64 (the assembled PoissonLHSNew rows), host arrays [mz][my][mx]. */
+int cvb_apply_operator(cvb_ctx *ctx, int level, const double *x, double *y);
+/* The same operator in FP32 flux form (the mixed V-cycle's operator). */
+int cvb_apply_operator_f32(cvb_ctx *ctx, int level, const float *x, float *y);
+/* The 19 stored weights of every row, [19][mz][my][mx], slots in the reference's
+ * CP,EP,WP,NP,SP,TP,BP,NE,SE,NW,SW,TN,BN,TS,BS,TE,BE,TW,BW order. */
+int cvb_get_weights(cvb_ctx *ctx, int level, double *w);
+/* MyRestriction (poisson.c:129) from level+1 to level; MyInterpolation
+ * (poisson.c:265) from level-1 to level (returned, not added). */
+int cvb_restrict(cvb_ctx *ctx, int coarse_level, const double *xf, double *xc);
+int cvb_interpolate(cvb_ctx *ctx, int fine_level, const double *xc, double *xf);
+/* PoissonNullSpaceFunction (poisson.c:372) on one level, in place. */
+int cvb_nullspace(cvb_ctx *ctx, int level, double *x);
+
+/* --- measurement ------------------------------------------------------- */
+/* Kernel launches this library has issued in the process (all contexts). */
+long long cvb_kernel_launches(void);
+enum {
+  CVB_KERNEL_LINE_SWEEP_F32 = 0, /* fused residual + y-line Thomas sweep, FP32 (mixed V-cycle) */
+  CVB_KERNEL_LINE_SWEEP_F64 = 1, /* the same in FP64 (plain FP64 V-cycle) */
+  CVB_KERNEL_RESIDUAL_F32 = 2,   /* b - A x, FP32 flux form */
+  CVB_KERNEL_RESIDUAL_F64 = 3    /* b - A x, FP64 stored rows */
+};
+/* Average duration of `reps` back-to-back launches of one kernel on `level`
+ * (CUDA events on the context's stream) and its algorithmic bytes per launch
+ * (every array it needs, touched once). */
+int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_ms, double *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CVB_H */

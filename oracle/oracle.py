@@ -277,3 +277,37 @@ class Reference:
         uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
         self.L.ref_update_and_project(ctypes.c_double(dt), ctypes.c_double(st), _p(pp), _p(ph), _p(uc))
         return pp, ph, uc
+
+
+def solve_mg(levels, b, rtol=1e-8, max_it=500, restart=30, nu=2, threads=0):
+    """The reference's solver algorithm on the CPU (cvb_solver.c): FGMRES + PCMG
+    with Richardson / block-Jacobi ILU(0).  levels: OLevel list, coarsest first.
+    Returns (x, iterations, relres, setup_seconds, solve_seconds)."""
+    L = lib()
+    f = L.orc_solve_mg
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                  ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_void_p]
+    arr = (ctypes.POINTER(Level) * len(levels))(*[ctypes.pointer(l.s) for l in levels])
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(bb.shape)
+    rr, ts, tv = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    its = f(len(levels), arr, _p(bb), _p(x), rtol, max_it, restart, nu, threads, ctypes.byref(rr),
+            ctypes.byref(ts), ctypes.byref(tv))
+    return x, its, rr.value, ts.value, tv.value
+
+
+def levels_for(problem, nlevels=None):
+    """OLevel hierarchy of a workload.Problem, the coarsest ``nlevels`` dropped
+    from the top when fewer levels are asked for (the reference's -mg_level)."""
+    mets = problem.metrics
+    if nlevels is not None:
+        mets = mets[len(mets) - nlevels:]
+    nl = len(mets)
+    Ls = [None] * nl
+    Ls[-1] = OLevel(mets[-1], problem.nvert, problem.bctype, problem.semi)
+    for l in range(nl - 2, -1, -1):
+        Ls[l] = OLevel(mets[l], nvert_restrict(Ls[l + 1], mets[l]["Aj"].shape, l == 0, problem.semi),
+                       problem.bctype, problem.semi)
+    return Ls
