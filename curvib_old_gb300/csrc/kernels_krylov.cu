@@ -43,65 +43,75 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NV], double *pa
   }
 }
 
-// partial[q][block] = sum over this block's elements of V_q[i] * w[i]; chunks of 8 vectors on blockIdx.y
-// With `self`, chunk 0 also accumulates w.w into row nv of the partials.
-template <typename TV>
-__global__ void __launch_bounds__(kRedThreads) k_multidot(const TV *const *V, int nv, const double *__restrict__ w,
-                                                           size_t n, double *partial, int self) {
-  const int base = blockIdx.y * 8;
-  double acc[9];
+// partial[q][block] = sum over this block's elements of V_q[i] * w[i] for NV
+// vectors starting at `base`; with `self` the w.w sum goes to row `self_row`.
+// The vector count is a template parameter: predicated-off products would still
+// occupy the FP64 pipe, which bounds this kernel on this part.
+template <typename TV, int NV, bool SELF>
+__global__ void __launch_bounds__(kRedThreads) k_multidot(const TV *const *V, int base, const double *__restrict__ w,
+                                                           size_t n, double *partial, int self_row) {
+  double acc[NV + 1];
 #pragma unroll
-  for (int q = 0; q < 9; q++) acc[q] = 0.0;
-  const TV *v[8];
+  for (int q = 0; q <= NV; q++) acc[q] = 0.0;
+  const TV *v[NV];
 #pragma unroll
-  for (int q = 0; q < 8; q++) v[q] = (base + q < nv) ? V[base + q] : nullptr;
-  const bool ws = self && blockIdx.y == 0;
+  for (int q = 0; q < NV; q++) v[q] = V[base + q];
   for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
     double wp = w[p];
 #pragma unroll
-    for (int q = 0; q < 8; q++)
-      if (v[q]) acc[q] = fma((double)v[q][p], wp, acc[q]);
-    if (ws) acc[8] = fma(wp, wp, acc[8]);
+    for (int q = 0; q < NV; q++) acc[q] = fma((double)v[q][p], wp, acc[q]);
+    if (SELF) acc[NV] = fma(wp, wp, acc[NV]);
   }
-  int cnt = nv - base < 8 ? nv - base : 8;
-  __shared__ double sh[9][kRedThreads / 32];
+  __shared__ double sh[NV + 1][kRedThreads / 32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  {
-    double x = acc[8];
+  constexpr int NR = SELF ? NV + 1 : NV;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[8][wid] = x;
-  }
-#pragma unroll
-  for (int q = 0; q < 8; q++) {
+  for (int q = 0; q < NR; q++) {
     double x = acc[q];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) sh[q][wid] = x;
   }
   __syncthreads();
-  if (threadIdx.x < cnt) {
+  if (threadIdx.x < NR) {
     double x = 0.0;
 #pragma unroll
     for (int ww = 0; ww < kRedThreads / 32; ww++) x += sh[threadIdx.x][ww];
-    partial[(size_t)(base + threadIdx.x) * gridDim.x + blockIdx.x] = x;
-  }
-  if (ws && threadIdx.x == 32) {
-    double x = 0.0;
-#pragma unroll
-    for (int ww = 0; ww < kRedThreads / 32; ww++) x += sh[8][ww];
-    partial[(size_t)nv * gridDim.x + blockIdx.x] = x;
+    int row = (SELF && threadIdx.x == NV) ? self_row : base + threadIdx.x;
+    partial[(size_t)row * gridDim.x + blockIdx.x] = x;
   }
 }
 
+template <typename TV, bool SELF>
+static void multidot_chunk(const TV *const *V, int base, int cnt, const double *w, size_t n, double *partial,
+                           int self_row, cudaStream_t s) {
+  int nb = reduce_blocks();
+  switch (cnt) {
+    case 1: k_multidot<TV, 1, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 2: k_multidot<TV, 2, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 3: k_multidot<TV, 3, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 4: k_multidot<TV, 4, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 5: k_multidot<TV, 5, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 6: k_multidot<TV, 6, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 7: k_multidot<TV, 7, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    default: k_multidot<TV, 8, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+  }
+  count_launch();
+}
+
+// Dots of w with V_0..V_{nv-1} in chunks of up to 8 vectors (each chunk reads w
+// once more); with `self`, w.w lands in row nv of the partials.
 void launch_multidot(const double *const *V, int nv, const double *w, size_t n, double *partial, cudaStream_t s,
                      int self) {
-  dim3 grd(reduce_blocks(), (nv + 7) / 8);
-  k_multidot<double><<<grd, kRedThreads, 0, s>>>(V, nv, w, n, partial, self); count_launch();
+  for (int base = 0; base < nv; base += 8) {
+    int cnt = nv - base < 8 ? nv - base : 8;
+    if (self && base == 0) multidot_chunk<double, true>(V, base, cnt, w, n, partial, nv, s);
+    else multidot_chunk<double, false>(V, base, cnt, w, n, partial, nv, s);
+  }
 }
 void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t n, double *partial, cudaStream_t s) {
-  dim3 grd(reduce_blocks(), (nv + 7) / 8);
-  k_multidot<float><<<grd, kRedThreads, 0, s>>>(V, nv, w, n, partial, 0); count_launch();
+  for (int base = 0; base < nv; base += 8)
+    multidot_chunk<float, false>(V, base, nv - base < 8 ? nv - base : 8, w, n, partial, nv, s);
 }
 
 // out[q] = sum_b partial[q][b], one block per q, fixed tree.

@@ -51,25 +51,28 @@ __device__ __forceinline__ Star<T> load_star(const TX *__restrict__ x, int p, co
 }
 
 // ----------------------------------------------------------------- FP64 rows
-// (A x)_p with the 19 stored weights; identity rows return x_p.
+// (A x)_p with the 19 stored weights; identity rows return x_p.  Every load of
+// the row is issued before anything depends on one of them (the row's code
+// included), so a row costs one memory latency, not a chain of them.
 template <typename TX>
 __device__ __forceinline__ double row64(const Geom &g, const double *__restrict__ w, const uint32_t *__restrict__ code,
                                         const TX *__restrict__ x, int i, int j, int k, int p, int n) {
-  if (__ldg(code + p) & CODE_IDENTITY) return (double)x[p];
+  if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return (double)x[p];
   Off o = offsets(g, i, j, k);
+  uint32_t c = __ldg(code + p);
   Star<double> s = load_star<double>(x, p, o);
   const double *wp = w + p;
-  double r = wp[(size_t)CP * n] * s.P;
-  r = fma(wp[(size_t)EP * n], s.E, r); r = fma(wp[(size_t)WP * n], s.W, r);
-  r = fma(wp[(size_t)NP * n], s.N, r); r = fma(wp[(size_t)SP * n], s.S, r);
-  r = fma(wp[(size_t)TP * n], s.Tt, r); r = fma(wp[(size_t)BP * n], s.B, r);
-  r = fma(wp[(size_t)NE * n], s.NE, r); r = fma(wp[(size_t)SE * n], s.SE, r);
-  r = fma(wp[(size_t)NW * n], s.NW, r); r = fma(wp[(size_t)SW * n], s.SW, r);
-  r = fma(wp[(size_t)TN * n], s.TN, r); r = fma(wp[(size_t)BN * n], s.BN, r);
-  r = fma(wp[(size_t)TS * n], s.TS, r); r = fma(wp[(size_t)BS * n], s.BS, r);
-  r = fma(wp[(size_t)TE * n], s.TE, r); r = fma(wp[(size_t)BE * n], s.BE, r);
-  r = fma(wp[(size_t)TW * n], s.TW, r); r = fma(wp[(size_t)BW * n], s.BW, r);
-  return r;
+  double r = __ldg(wp + (size_t)CP * n) * s.P;
+  r = fma(__ldg(wp + (size_t)EP * n), s.E, r); r = fma(__ldg(wp + (size_t)WP * n), s.W, r);
+  r = fma(__ldg(wp + (size_t)NP * n), s.N, r); r = fma(__ldg(wp + (size_t)SP * n), s.S, r);
+  r = fma(__ldg(wp + (size_t)TP * n), s.Tt, r); r = fma(__ldg(wp + (size_t)BP * n), s.B, r);
+  r = fma(__ldg(wp + (size_t)NE * n), s.NE, r); r = fma(__ldg(wp + (size_t)SE * n), s.SE, r);
+  r = fma(__ldg(wp + (size_t)NW * n), s.NW, r); r = fma(__ldg(wp + (size_t)SW * n), s.SW, r);
+  r = fma(__ldg(wp + (size_t)TN * n), s.TN, r); r = fma(__ldg(wp + (size_t)BN * n), s.BN, r);
+  r = fma(__ldg(wp + (size_t)TS * n), s.TS, r); r = fma(__ldg(wp + (size_t)BS * n), s.BS, r);
+  r = fma(__ldg(wp + (size_t)TE * n), s.TE, r); r = fma(__ldg(wp + (size_t)BE * n), s.BE, r);
+  r = fma(__ldg(wp + (size_t)TW * n), s.TW, r); r = fma(__ldg(wp + (size_t)BW * n), s.BW, r);
+  return (c & CODE_IDENTITY) ? s.P : r;
 }
 
 // ----------------------------------------------------------------- FP32 rows
@@ -81,59 +84,43 @@ __device__ __forceinline__ float cross32(int br, float g, float su, float s0, fl
   float cd = br == 1 ? -0.25f : (br == 2 ? -0.5f : 0.0f);
   return g * (cu * su + c0 * s0 + cd * sd);
 }
+__device__ __forceinline__ float act(uint32_t c, uint32_t bit) { return (c & bit) ? 1.0f : 0.0f; }
 
 // (A x)_p in flux form: each active face flux from its cell's coefficients and
 // branch codes; the lower faces are the upper faces of the W/S/B neighbours.
+// Loads first (all unconditional, in bounds for interior cells), then the
+// arithmetic with the activity bits as 0/1 factors.
 template <typename TX>
 __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ gf, const float *__restrict__ aj,
                                        const uint32_t *__restrict__ code, const TX *__restrict__ x, int i, int j,
                                        int k, int p, int n) {
-  uint32_t c = __ldg(code + p);
-  if (c & CODE_IDENTITY) return (float)x[p];
+  if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return (float)x[p];
   Off o = offsets(g, i, j, k);
-  Star<float> s = load_star<float>(x, p, o);
   const int pw = p - 1, ps = p - g.mx, pb = p - g.mx * g.my;  // lower neighbours (never wrapped)
-  float acc = 0.0f;
-  if (c & CODE_ACT_E) {
-    float f = gf[p] * (s.E - s.P);
-    f += cross32(code_branch(c, 0, 0), gf[n + p], s.N + s.NE, s.P + s.E, s.S + s.SE);
-    f += cross32(code_branch(c, 0, 1), gf[2 * n + p], s.Tt + s.TE, s.P + s.E, s.B + s.BE);
-    acc += f;
-  }
-  if (c & CODE_ACT_W) {
-    uint32_t cw = __ldg(code + pw);
-    float f = gf[pw] * (s.P - s.W);
-    f += cross32(code_branch(cw, 0, 0), gf[n + pw], s.NW + s.N, s.W + s.P, s.SW + s.S);
-    f += cross32(code_branch(cw, 0, 1), gf[2 * n + pw], s.TW + s.Tt, s.W + s.P, s.BW + s.B);
-    acc -= f;
-  }
-  if (c & CODE_ACT_N) {
-    float f = gf[4 * n + p] * (s.N - s.P);
-    f += cross32(code_branch(c, 1, 0), gf[3 * n + p], s.E + s.NE, s.P + s.N, s.W + s.NW);
-    f += cross32(code_branch(c, 1, 1), gf[5 * n + p], s.Tt + s.TN, s.P + s.N, s.B + s.BN);
-    acc += f;
-  }
-  if (c & CODE_ACT_S) {
-    uint32_t cs = __ldg(code + ps);
-    float f = gf[4 * n + ps] * (s.P - s.S);
-    f += cross32(code_branch(cs, 1, 0), gf[3 * n + ps], s.SE + s.E, s.S + s.P, s.SW + s.W);
-    f += cross32(code_branch(cs, 1, 1), gf[5 * n + ps], s.TS + s.Tt, s.S + s.P, s.BS + s.B);
-    acc -= f;
-  }
-  if (c & CODE_ACT_T) {
-    float f = gf[8 * n + p] * (s.Tt - s.P);
-    f += cross32(code_branch(c, 2, 0), gf[6 * n + p], s.E + s.TE, s.P + s.Tt, s.W + s.TW);
-    f += cross32(code_branch(c, 2, 1), gf[7 * n + p], s.N + s.TN, s.P + s.Tt, s.S + s.TS);
-    acc += f;
-  }
-  if (c & CODE_ACT_B) {
-    uint32_t cb = __ldg(code + pb);
-    float f = gf[8 * n + pb] * (s.P - s.B);
-    f += cross32(code_branch(cb, 2, 0), gf[6 * n + pb], s.BE + s.E, s.B + s.P, s.BW + s.W);
-    f += cross32(code_branch(cb, 2, 1), gf[7 * n + pb], s.BN + s.N, s.B + s.P, s.BS + s.S);
-    acc -= f;
-  }
-  return -aj[p] * acc;
+  const uint32_t c = __ldg(code + p), cw = __ldg(code + pw), cs = __ldg(code + ps), cb = __ldg(code + pb);
+  Star<float> s = load_star<float>(x, p, o);
+  const float g11 = __ldg(gf + p), g12 = __ldg(gf + n + p), g13 = __ldg(gf + 2 * n + p);
+  const float g21 = __ldg(gf + 3 * n + p), g22 = __ldg(gf + 4 * n + p), g23 = __ldg(gf + 5 * n + p);
+  const float g31 = __ldg(gf + 6 * n + p), g32 = __ldg(gf + 7 * n + p), g33 = __ldg(gf + 8 * n + p);
+  const float w11 = __ldg(gf + pw), w12 = __ldg(gf + n + pw), w13 = __ldg(gf + 2 * n + pw);
+  const float s21 = __ldg(gf + 3 * n + ps), s22 = __ldg(gf + 4 * n + ps), s23 = __ldg(gf + 5 * n + ps);
+  const float b31 = __ldg(gf + 6 * n + pb), b32 = __ldg(gf + 7 * n + pb), b33 = __ldg(gf + 8 * n + pb);
+  const float ajp = __ldg(aj + p);
+  float fe = g11 * (s.E - s.P) + cross32(code_branch(c, 0, 0), g12, s.N + s.NE, s.P + s.E, s.S + s.SE) +
+             cross32(code_branch(c, 0, 1), g13, s.Tt + s.TE, s.P + s.E, s.B + s.BE);
+  float fw = w11 * (s.P - s.W) + cross32(code_branch(cw, 0, 0), w12, s.NW + s.N, s.W + s.P, s.SW + s.S) +
+             cross32(code_branch(cw, 0, 1), w13, s.TW + s.Tt, s.W + s.P, s.BW + s.B);
+  float fn = g22 * (s.N - s.P) + cross32(code_branch(c, 1, 0), g21, s.E + s.NE, s.P + s.N, s.W + s.NW) +
+             cross32(code_branch(c, 1, 1), g23, s.Tt + s.TN, s.P + s.N, s.B + s.BN);
+  float fs = s22 * (s.P - s.S) + cross32(code_branch(cs, 1, 0), s21, s.SE + s.E, s.S + s.P, s.SW + s.W) +
+             cross32(code_branch(cs, 1, 1), s23, s.TS + s.Tt, s.S + s.P, s.BS + s.B);
+  float ft = g33 * (s.Tt - s.P) + cross32(code_branch(c, 2, 0), g31, s.E + s.TE, s.P + s.Tt, s.W + s.TW) +
+             cross32(code_branch(c, 2, 1), g32, s.N + s.TN, s.P + s.Tt, s.S + s.TS);
+  float fb = b33 * (s.P - s.B) + cross32(code_branch(cb, 2, 0), b31, s.BE + s.E, s.B + s.P, s.BW + s.W) +
+             cross32(code_branch(cb, 2, 1), b32, s.BN + s.N, s.B + s.P, s.BS + s.S);
+  float acc = act(c, CODE_ACT_E) * fe - act(c, CODE_ACT_W) * fw + act(c, CODE_ACT_N) * fn -
+              act(c, CODE_ACT_S) * fs + act(c, CODE_ACT_T) * ft - act(c, CODE_ACT_B) * fb;
+  return (c & CODE_IDENTITY) ? s.P : -ajp * acc;
 }
 
 // ------------------------------------------------------- apply / residual
@@ -187,7 +174,8 @@ void launch_residual<float>(const LevelDev &L, const float *b, const float *x, f
 // tridiagonal in-line (j) part of A with Thomas factors from set-up.
 // A block owns a tile of TW consecutive i over all j at one k.  Phase 1: all
 // threads compute the tile's residual into shared memory and stage the three
-// factor arrays there (coalesced, many loads in flight).  Phase 2: TW threads
+// factor arrays there (coalesced, many loads in flight; read from global inside
+// the recurrence they would cost a memory latency per step).  Phase 2: TW threads
 // run the forward/backward recurrences out of shared memory, one line each.
 // Phase 3: all threads write x + omega*delta.  Zero guess: the residual is b.
 template <typename T>
@@ -207,46 +195,99 @@ struct RowOf<double> {
   __device__ static const double *fac(const LevelDev &L) { return L.line64; }
 };
 
+// Solves one line's tridiagonal system in place with one warp.  The Thomas
+// passes are first-order affine recurrences, d_j = gamma_j + beta_j d_{j-1}
+// (forward: gamma = m r, beta = -m a; backward: gamma = d, beta = -c), and
+// affine maps compose associatively: each lane composes the maps of its
+// contiguous rows, a shuffle scan combines the lanes, each lane replays its rows.
+// r/a/m/c: this line's arrays in shared memory, indexed by row j = 1..nr.
+template <typename T>
+__device__ __forceinline__ void warp_line_solve(T *r, const T *a, const T *m, const T *c, int nr, int lane) {
+  const int R = (nr + 31) >> 5;
+  const int q0 = lane * R, q1 = min(q0 + R, nr);
+  // forward: d_q = m_q (r_q - a_q d_{q-1})
+  T B = T(1), G = T(0);
+  for (int q = q0; q < q1; q++) {
+    T mq = m[q + 1];
+    T beta = -mq * a[q + 1], gamma = mq * r[q + 1];
+    B = beta * B;
+    G = beta * G + gamma;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T Bp = __shfl_up_sync(0xffffffffu, B, o), Gp = __shfl_up_sync(0xffffffffu, G, o);
+    if (lane >= o) { G = B * Gp + G; B = B * Bp; }
+  }
+  T d = __shfl_up_sync(0xffffffffu, G, 1);
+  if (lane == 0) d = T(0);
+  for (int q = q0; q < q1; q++) {
+    T mq = m[q + 1];
+    d = mq * r[q + 1] - mq * a[q + 1] * d;
+    r[q + 1] = d;
+  }
+  __syncwarp();
+  // backward: x_q = d_q - c_q x_{q+1}
+  B = T(1); G = T(0);
+  for (int q = q1 - 1; q >= q0; q--) {
+    T beta = -c[q + 1], gamma = r[q + 1];
+    B = beta * B;
+    G = beta * G + gamma;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T Bn = __shfl_down_sync(0xffffffffu, B, o), Gn = __shfl_down_sync(0xffffffffu, G, o);
+    if (lane + o < 32) { G = B * Gn + G; B = B * Bn; }
+  }
+  T xs = __shfl_down_sync(0xffffffffu, G, 1);
+  if (lane == 31) xs = T(0);
+  for (int q = q1 - 1; q >= q0; q--) {
+    xs = r[q + 1] - c[q + 1] * xs;
+    r[q + 1] = xs;
+  }
+  __syncwarp();
+}
+
+// One damped line-Jacobi sweep, fused: xnew = x + omega * T^-1 (b - A x).
+// A block owns TW lines (consecutive i at one k) over all j.  Phase 1: all
+// threads compute the tile's residuals and stage the Thomas factors in shared
+// memory (laid out line by line).  Phase 2: each warp solves TW/8 lines with
+// warp_line_solve.  Phase 3: all threads write x + omega*delta.
 template <typename T, int TW>
-__global__ void __launch_bounds__(256) k_line_sweep(LevelDev L, const T *__restrict__ b, const T *__restrict__ x,
-                                                    T *__restrict__ xnew, T omega, int zero_guess) {
+__global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__restrict__ b, const T *__restrict__ x,
+                                                       T *__restrict__ xnew, T omega, int zero_guess) {
   extern __shared__ unsigned char smem_raw[];
-  T *sr = reinterpret_cast<T *>(smem_raw);  // [my][TW] residual, then delta
   const Geom g = L.g;
   const int my = g.my, n = (int)g.n();
+  T *sr = reinterpret_cast<T *>(smem_raw);  // [TW][my] residual -> line solution
   T *sa = sr + my * TW, *sm = sa + my * TW, *sc = sm + my * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
-  const int i = blockIdx.x * TW + tx, k = blockIdx.y;
-  const bool inside_i = i < g.mx;
-  const bool line = inside_i && i >= 1 && i <= g.mx - 2 && k >= 1 && k <= g.mz - 2;
+  const int i0 = blockIdx.x * TW, k = blockIdx.y;
+  const int i = i0 + tx;
+  const bool kin = k >= 1 && k <= g.mz - 2;
   const T *fa = RowOf<T>::fac(L);
   for (int j = ty; j < my; j += ny) {
+    const bool line = i >= 1 && i <= g.mx - 2 && kin;
     int p = (k * my + j) * g.mx + i;
     T r = T(0), a = T(0), m = T(1), c = T(0);
     if (line && j >= 1 && j <= my - 2) {
+      a = __ldg(fa + p); m = __ldg(fa + n + p); c = __ldg(fa + 2 * n + p);
       r = zero_guess ? b[p] : b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n);
-      a = fa[p]; m = fa[n + p]; c = fa[2 * n + p];
     }
-    sr[j * TW + tx] = r; sa[j * TW + tx] = a; sm[j * TW + tx] = m; sc[j * TW + tx] = c;
+    sr[tx * my + j] = r; sa[tx * my + j] = a; sm[tx * my + j] = m; sc[tx * my + j] = c;
   }
   __syncthreads();
-  if (ty == 0 && line) {
-    T d = T(0);
-    for (int j = 1; j <= my - 2; j++) {
-      d = (sr[j * TW + tx] - sa[j * TW + tx] * d) * sm[j * TW + tx];
-      sr[j * TW + tx] = d;
-    }
-    T dn = T(0);
-    for (int j = my - 2; j >= 1; j--) {
-      dn = sr[j * TW + tx] - sc[j * TW + tx] * dn;
-      sr[j * TW + tx] = dn;
-    }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int t = warp; t < TW; t += nwarps) {
+    int it = i0 + t;
+    if (it >= 1 && it <= g.mx - 2 && kin)
+      warp_line_solve<T>(sr + t * my, sa + t * my, sm + t * my, sc + t * my, my - 2, lane);
   }
   __syncthreads();
-  if (!inside_i) return;
+  if (i >= g.mx) return;
+  const bool line = i >= 1 && i <= g.mx - 2 && kin;
   for (int j = ty; j < my; j += ny) {
     int p = (k * my + j) * g.mx + i;
-    T d = sr[j * TW + tx];
+    T d = sr[tx * my + j];
     T xo = zero_guess ? T(0) : x[p];
     xnew[p] = (line && j >= 1 && j <= my - 2) ? xo + omega * d : xo;
   }
