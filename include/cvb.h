@@ -165,6 +165,32 @@ int cvb_interpolate(cvb_ctx *ctx, int fine_level, const double *xc, double *xf);
 /* PoissonNullSpaceFunction (poisson.c:372) on one level, in place. */
 int cvb_nullspace(cvb_ctx *ctx, int level, double *x);
 
+/* --- allocation-free form ------------------------------------------------ */
+/* PoissonRHS on device arrays without allocating any device memory.  This entry
+ * point has no counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc: code running while a CUDA graph is being captured, hosts whose
+ * device memory comes from their own allocator or pool, and time loops that
+ * forbid allocation after start-up.
+ *
+ * d_ucont ([mz][my][mx] Cmpnts), d_aj, d_nvert ([mz][my][mx]) and the outputs
+ * d_b ([mz][my][mx]) and d_compat_sum (one double, the sum PoissonRHS prints)
+ * are device pointers owned by the caller; stream is a cudaStream_t (NULL: the
+ * legacy default stream).  Results equal cvb_poisson_rhs's bit for bit.
+ *
+ * The only scratch is a fixed file-scope device array of 2*CVB_NOALLOC_MAX_BLOCKS
+ * doubles (32 KB) that every GPU loading this library holds until the process
+ * exits.  Boxes larger than CVB_NOALLOC_MAX_CELLS cells are rejected with
+ * CVB_BAD_INPUT.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call shares the array and leaves its last
+ * contents there; each call overwrites every slot it reads, so nothing needs
+ * clearing, but calls that overlap on the GPU (concurrent streams or host
+ * threads) race on it and must be serialised by the caller. */
+#define CVB_NOALLOC_MAX_BLOCKS 2048
+#define CVB_NOALLOC_MAX_CELLS (64 * 1024 * 1024)
+int cvb_poisson_rhs_noalloc(const double *d_ucont, const double *d_aj, const double *d_nvert, int mx, int my,
+                            int mz, double dt, double st, double *d_b, double *d_compat_sum, void *stream);
+
 /* --- measurement ------------------------------------------------------- */
 /* Kernel launches this library has issued in the process (all contexts). */
 long long cvb_kernel_launches(void);
