@@ -78,6 +78,7 @@ EXPORTS = {
     "cvb_nullspace": ([_P, _I, _P], _I),
     "cvb_kernel_launches": ([], ctypes.c_longlong),
     "cvb_time_kernel": ([_P, _I, _I, _I, _P, _P], _I),
+    "cvb_tuning_report": ([_P, ctypes.c_char_p, _I], _I),
     "cvb_poisson_rhs_noalloc": ([_P, _P, _P, _I, _I, _I, _D, _D, _P, _P, _P], _I),
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3}

@@ -60,6 +60,9 @@ struct cvb_ctx {
   double *uc_dev = nullptr, *p_dev = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;
+  // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
+  struct Tune { int level; size_t cells; double us32[2], us64[2]; };
+  std::vector<Tune> tune;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -306,6 +309,45 @@ static int build_operators(cvb_ctx *ctx) {
   auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void *)g9);
   if (it != ctx->allocs.end()) ctx->allocs.erase(it);
   cudaFree(g9);
+  return CVB_OK;
+}
+
+// Set-up autotuner: times the fused and the split y-line sweep on every level
+// and precision (CUDA events on the context stream, after one warm-up launch)
+// and keeps the faster; the choice depends on the level's size and on how its
+// lines fill the machine.
+static int autotune_sweeps(cvb_ctx *ctx) {
+  ctx->tune.clear();
+  for (int l = 0; l < ctx->nlevels; l++) {
+    LevelDev &L = ctx->L[l];
+    size_t n = L.g.n();
+    cvb_ctx::Tune t;
+    t.level = l;
+    t.cells = n;
+    CK(cudaMemsetAsync(L.r32, 0, sizeof(float) * n, ctx->stream));
+    CK(cudaMemsetAsync(L.e32, 0, sizeof(float) * n, ctx->stream));
+    CK(cudaMemsetAsync(L.r64, 0, sizeof(double) * n, ctx->stream));
+    CK(cudaMemsetAsync(L.e64, 0, sizeof(double) * n, ctx->stream));
+    for (int prec = 0; prec < 2; prec++)
+      for (int v = 0; v < 2; v++) {
+        if (prec == 0) L.sweep32 = v; else L.sweep64 = v;
+        const int reps = 3;
+        for (int q = 0; q <= reps; q++) {
+          if (q == 1) CK(cudaEventRecord(ctx->ev0, ctx->stream));
+          if (prec == 0) launch_line_smooth<float>(L, L.r32, L.e32, L.t32 + n, 0.85f, 0, ctx->stream);
+          else launch_line_smooth<double>(L, L.r64, L.e64, L.t64 + n, 0.85, 0, ctx->stream);
+        }
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        CKL();
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        (prec == 0 ? t.us32 : t.us64)[v] = 1e3 * ms / reps;
+      }
+    L.sweep32 = t.us32[1] < t.us32[0] ? 1 : 0;
+    L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
+    ctx->tune.push_back(t);
+  }
   return CVB_OK;
 }
 
@@ -622,7 +664,7 @@ int cvb_solve_opts_default(cvb_solve_opts *o) {
   o->restart = 30;
   o->pre_sweeps = 2;
   o->post_sweeps = 2;
-  o->omega = 0.85;
+  o->omega = 0.9;
   o->project_rhs = 1;
   o->warm_start = 0;
   o->coarse_dense_max = 2048;
@@ -737,6 +779,7 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, con
   TRY(dalloc(ctx, &ctx->sums, kMaxRestart + 2));
   TRY(dalloc(ctx, &ctx->hdev, kMaxRestart + 2));
   TRY(build_operators(ctx));
+  TRY(autotune_sweeps(ctx));
   cvb_solve_opts def;
   cvb_solve_opts_default(&def);
   TRY(build_coarse(ctx, &def));
@@ -778,6 +821,7 @@ int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
   CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice,
                      ctx->stream));
   TRY(build_operators(ctx));
+  TRY(autotune_sweeps(ctx));
   cvb_solve_opts def;
   cvb_solve_opts_default(&def);
   TRY(build_coarse(ctx, &def));
@@ -973,6 +1017,26 @@ int cvb_interpolate(cvb_ctx *ctx, int fine, const double *xc, double *xf) {
 }
 
 long long cvb_kernel_launches(void) { return launch_count(); }
+
+int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  std::string o = "{\"line_sweep\": [";
+  for (size_t q = 0; q < ctx->tune.size(); q++) {
+    const auto &t = ctx->tune[q];
+    char row[512];
+    snprintf(row, sizeof row,
+             "%s{\"level\": %d, \"cells\": %zu, \"f32\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
+             "\"f64\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}}",
+             q ? ", " : "", t.level, t.cells, t.us32[0], t.us32[1], ctx->L[t.level].sweep32 ? "split" : "fused",
+             t.us64[0], t.us64[1], ctx->L[t.level].sweep64 ? "split" : "fused");
+    o += row;
+  }
+  o += "]}";
+  if (!buf || len <= (int)o.size()) return fail(ctx, CVB_BAD_INPUT, "report needs %zu bytes", o.size() + 1);
+  std::memcpy(buf, o.c_str(), o.size() + 1);
+  return CVB_OK;
+}
 
 int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_ms, double *bytes) {
   TRY(level_ok(ctx, level));

@@ -60,7 +60,14 @@ struct LevelDev {
   // work vectors of this level (the finest level's b/x live in the solver)
   double *r64, *e64, *t64;  // FP64 V-cycle vectors
   float *r32, *e32, *t32;   // FP32 V-cycle vectors
+  int sweep32, sweep64;     // line-sweep variant chosen at set-up: 0 fused, 1 split
+  // When set, every kernel launched for this level returns at once while *gate
+  // is non-zero: an FGMRES iteration issued ahead of the host's convergence
+  // check turns into no-ops once the previous iteration has converged.
+  const int *gate;
 };
+
+__device__ __forceinline__ bool gated(const int *gate) { return gate && *gate; }
 
 // --- kernel launchers (defined in the .cu files) ---------------------------
 // setup
@@ -72,7 +79,7 @@ void launch_weights(const Geom &g, const double *g9, const double *aj, const dou
                     const uint32_t *code, double *w64, cudaStream_t s);
 void launch_line_factors(const Geom &g, const double *w64, double *line64, float *line32,
                          cudaStream_t s);
-void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s);
+void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s, const int *gate = nullptr);
 void launch_nvert_restrict(const Geom &fine, const double *nvf, const Geom &coarse, int isc, int jsc,
                            int ksc, double *nvc, double *tmp, cudaStream_t s);
 
@@ -91,19 +98,21 @@ void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf
 
 // mixed-precision glue: FP64 operator on an FP32-stored vector
 void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStream_t s);
-void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s);
-void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s);
+void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s, const int *gate = nullptr);
+void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s, const int *gate = nullptr);
 
 // Krylov support (deterministic two-stage reductions)
 int reduce_blocks();
 void launch_multidot(const double *const *V, int nv, const double *w, size_t n, double *partial,
-                     cudaStream_t s, int self = 0);
+                     cudaStream_t s, int self = 0, const int *gate = nullptr);
 void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t n, double *partial,
                          cudaStream_t s);
-void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s);
+void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s,
+                        const int *gate = nullptr);
 void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_dev, int nv, size_t n,
-                           double *partial, cudaStream_t s);
-void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s);
+                           double *partial, cudaStream_t s, const int *gate = nullptr);
+void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
+                  const int *gate = nullptr);
 void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev,
                    int nz, size_t n, cudaStream_t s);
 void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial,
@@ -116,8 +125,10 @@ void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double
                                 double *partial, cudaStream_t s);
 void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
                            cudaStream_t s);
-void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s);
-void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s);
+void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s,
+                        const int *gate = nullptr);
+void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s,
+                            const int *gate = nullptr);
 
 // projection-path kernels (FP64)
 void launch_poisson_rhs(const Geom &g, const double *ucont, const double *aj, const double *nvert,

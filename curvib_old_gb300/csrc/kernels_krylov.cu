@@ -49,7 +49,9 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NV], double *pa
 // occupy the FP64 pipe, which bounds this kernel on this part.
 template <typename TV, int NV, bool SELF>
 __global__ void __launch_bounds__(kRedThreads) k_multidot(const TV *const *V, int base, const double *__restrict__ w,
-                                                           size_t n, double *partial, int self_row) {
+                                                           size_t n, double *partial, int self_row,
+                                                           const int *gate) {
+  if (gated(gate)) return;
   double acc[NV + 1];
 #pragma unroll
   for (int q = 0; q <= NV; q++) acc[q] = 0.0;
@@ -84,17 +86,17 @@ __global__ void __launch_bounds__(kRedThreads) k_multidot(const TV *const *V, in
 
 template <typename TV, bool SELF>
 static void multidot_chunk(const TV *const *V, int base, int cnt, const double *w, size_t n, double *partial,
-                           int self_row, cudaStream_t s) {
+                           int self_row, cudaStream_t s, const int *gate = nullptr) {
   int nb = reduce_blocks();
   switch (cnt) {
-    case 1: k_multidot<TV, 1, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    case 2: k_multidot<TV, 2, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    case 3: k_multidot<TV, 3, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    case 4: k_multidot<TV, 4, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    case 5: k_multidot<TV, 5, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    case 6: k_multidot<TV, 6, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    case 7: k_multidot<TV, 7, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
-    default: k_multidot<TV, 8, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row); break;
+    case 1: k_multidot<TV, 1, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 2: k_multidot<TV, 2, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 3: k_multidot<TV, 3, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 4: k_multidot<TV, 4, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 5: k_multidot<TV, 5, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 6: k_multidot<TV, 6, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 7: k_multidot<TV, 7, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    default: k_multidot<TV, 8, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
   }
   count_launch();
 }
@@ -102,11 +104,11 @@ static void multidot_chunk(const TV *const *V, int base, int cnt, const double *
 // Dots of w with V_0..V_{nv-1} in chunks of up to 8 vectors (each chunk reads w
 // once more); with `self`, w.w lands in row nv of the partials.
 void launch_multidot(const double *const *V, int nv, const double *w, size_t n, double *partial, cudaStream_t s,
-                     int self) {
+                     int self, const int *gate) {
   for (int base = 0; base < nv; base += 8) {
     int cnt = nv - base < 8 ? nv - base : 8;
-    if (self && base == 0) multidot_chunk<double, true>(V, base, cnt, w, n, partial, nv, s);
-    else multidot_chunk<double, false>(V, base, cnt, w, n, partial, nv, s);
+    if (self && base == 0) multidot_chunk<double, true>(V, base, cnt, w, n, partial, nv, s, gate);
+    else multidot_chunk<double, false>(V, base, cnt, w, n, partial, nv, s, gate);
   }
 }
 void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t n, double *partial, cudaStream_t s) {
@@ -115,7 +117,9 @@ void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t 
 }
 
 // out[q] = sum_b partial[q][b], one block per q, fixed tree.
-__global__ void k_finish(const double *__restrict__ partial, int nblocks, double *__restrict__ out) {
+__global__ void k_finish(const double *__restrict__ partial, int nblocks, double *__restrict__ out,
+                         const int *gate) {
+  if (gated(gate)) return;
   __shared__ double sh[kRedThreads];
   int q = blockIdx.x;
   double v = 0.0;
@@ -128,14 +132,15 @@ __global__ void k_finish(const double *__restrict__ partial, int nblocks, double
   }
   if (threadIdx.x == 0) out[q] = sh[0];
 }
-void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s) {
-  k_finish<<<nv, kRedThreads, 0, s>>>(partial, nblocks, out); count_launch();
+void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s, const int *gate) {
+  k_finish<<<nv, kRedThreads, 0, s>>>(partial, nblocks, out, gate); count_launch();
 }
 
 // w -= sum_q h[q] V_q ; partial[block] = sum of w^2 over the block.
 __global__ void __launch_bounds__(kRedThreads) k_multiaxpy_norm(double *__restrict__ w, const double *const *V,
                                                                  const double *__restrict__ h, int nv, size_t n,
-                                                                 double *partial) {
+                                                                 double *partial, const int *gate) {
+  if (gated(gate)) return;
   __shared__ double hs[64];
   if (threadIdx.x < nv) hs[threadIdx.x] = h[threadIdx.x];
   __syncthreads();
@@ -150,19 +155,21 @@ __global__ void __launch_bounds__(kRedThreads) k_multiaxpy_norm(double *__restri
   block_reduce_store<1>(a1, partial, gridDim.x, 0);
 }
 void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_dev, int nv, size_t n,
-                           double *partial, cudaStream_t s) {
-  k_multiaxpy_norm<<<reduce_blocks(), kRedThreads, 0, s>>>(w, V, h_dev, nv, n, partial); count_launch();
+                           double *partial, cudaStream_t s, const int *gate) {
+  k_multiaxpy_norm<<<reduce_blocks(), kRedThreads, 0, s>>>(w, V, h_dev, nv, n, partial, gate); count_launch();
 }
 
 // dst = src / *scal
 __global__ void k_scale(double *__restrict__ dst, const double *__restrict__ src, const double *__restrict__ scal,
-                        size_t n) {
+                        size_t n, const int *gate) {
+  if (gated(gate)) return;
   double inv = 1.0 / *scal;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
     dst[p] = src[p] * inv;
 }
-void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s) {
-  k_scale<<<reduce_blocks(), 256, 0, s>>>(dst, src, scal_dev, n); count_launch();
+void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
+                  const int *gate) {
+  k_scale<<<reduce_blocks(), 256, 0, s>>>(dst, src, scal_dev, n, gate); count_launch();
 }
 
 // x += sum_q y[q] Z_q (Z stored FP32 in mixed mode, FP64 in plain mode)
@@ -257,7 +264,9 @@ void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj,
 
 // Coarsest level: e = Minv r with a dense FP64 inverse (one warp per row).
 template <typename T>
-__global__ void k_dense(const double *__restrict__ M, int n, const T *__restrict__ r, T *__restrict__ e) {
+__global__ void k_dense(const double *__restrict__ M, int n, const T *__restrict__ r, T *__restrict__ e,
+                        const int *gate) {
+  if (gated(gate)) return;
   int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -267,11 +276,11 @@ __global__ void k_dense(const double *__restrict__ M, int n, const T *__restrict
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) e[row] = (T)s;
 }
-void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s) {
-  k_dense<double><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e); count_launch();
+void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s, const int *gate) {
+  k_dense<double><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e, gate); count_launch();
 }
-void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s) {
-  k_dense<float><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e); count_launch();
+void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s, const int *gate) {
+  k_dense<float><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e, gate); count_launch();
 }
 
 }  // namespace cvb

@@ -201,21 +201,25 @@ void launch_line_factors(const Geom &g, const double *w64, double *line64, float
   k_line_factors<<<nblk(lines, 128), 128, 0, s>>>(g, w64, line64, line32); count_launch();
 }
 
-__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n) {
+__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n, const int *gate) {
+  if (gated(gate)) return;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
     b[p] = (float)a[p];
 }
-void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s) {
-  k_to_f32<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n); count_launch();
+void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s, const int *gate) {
+  k_to_f32<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n, gate); count_launch();
 }
-void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s) { launch_to_f32(a, b, n, s); }
+void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s, const int *gate) {
+  launch_to_f32(a, b, n, s, gate);
+}
 
-__global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, size_t n) {
+__global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, size_t n, const int *gate) {
+  if (gated(gate)) return;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
     b[p] = (double)a[p];
 }
-void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s) {
-  k_to_f64<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n); count_launch();
+void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s, const int *gate) {
+  k_to_f64<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n, gate); count_launch();
 }
 
 // MyNvertRestriction (poisson.c:1662-1773): a coarse cell is blocked (1) when the

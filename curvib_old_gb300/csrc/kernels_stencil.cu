@@ -128,7 +128,8 @@ __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ 
 template <typename TX>
 __global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restrict__ w, const uint32_t *__restrict__ code,
                                                  const TX *__restrict__ x, const double *__restrict__ b,
-                                                 double *__restrict__ y) {
+                                                 double *__restrict__ y, const int *gate) {
+  if (gated(gate)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= g.mx || j >= g.my) return;
   int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
@@ -138,7 +139,8 @@ __global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restric
 
 __global__ void __launch_bounds__(128) k_apply32(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
                                                  const uint32_t *__restrict__ code, const float *__restrict__ x,
-                                                 const float *__restrict__ b, float *__restrict__ y) {
+                                                 const float *__restrict__ b, float *__restrict__ y, const int *gate) {
+  if (gated(gate)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= g.mx || j >= g.my) return;
   int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
@@ -151,22 +153,22 @@ static const dim3 kBlk(32, 4, 1);
 
 template <>
 void launch_apply<double>(const LevelDev &L, const double *x, double *y, cudaStream_t s) {
-  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y); count_launch();
+  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y, L.gate); count_launch();
 }
 template <>
 void launch_residual<double>(const LevelDev &L, const double *b, const double *x, double *r, cudaStream_t s) {
-  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, b, r); count_launch();
+  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, b, r, L.gate); count_launch();
 }
 void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStream_t s) {
-  k_apply64<float><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y); count_launch();
+  k_apply64<float><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y, L.gate); count_launch();
 }
 template <>
 void launch_apply<float>(const LevelDev &L, const float *x, float *y, cudaStream_t s) {
-  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, nullptr, y); count_launch();
+  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, nullptr, y, L.gate); count_launch();
 }
 template <>
 void launch_residual<float>(const LevelDev &L, const float *b, const float *x, float *r, cudaStream_t s) {
-  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, b, r); count_launch();
+  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, b, r, L.gate); count_launch();
 }
 
 // ------------------------------------------------------------ y-line smoother
@@ -254,7 +256,8 @@ __device__ __forceinline__ void warp_line_solve(T *r, const T *a, const T *m, co
 // warp_line_solve.  Phase 3: all threads write x + omega*delta.
 template <typename T, int TW>
 __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__restrict__ b, const T *__restrict__ x,
-                                                       T *__restrict__ xnew, T omega, int zero_guess) {
+                                                       T *__restrict__ xnew, T omega, int mode) {
+  if (gated(L.gate)) return;
   extern __shared__ unsigned char smem_raw[];
   const Geom g = L.g;
   const int my = g.my, n = (int)g.n();
@@ -265,13 +268,14 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
   const int i = i0 + tx;
   const bool kin = k >= 1 && k <= g.mz - 2;
   const T *fa = RowOf<T>::fac(L);
+#pragma unroll 4
   for (int j = ty; j < my; j += ny) {
     const bool line = i >= 1 && i <= g.mx - 2 && kin;
     int p = (k * my + j) * g.mx + i;
     T r = T(0), a = T(0), m = T(1), c = T(0);
     if (line && j >= 1 && j <= my - 2) {
       a = __ldg(fa + p); m = __ldg(fa + n + p); c = __ldg(fa + 2 * n + p);
-      r = zero_guess ? b[p] : b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n);
+      r = (mode == 1) ? b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n) : b[p];
     }
     sr[tx * my + j] = r; sa[tx * my + j] = a; sm[tx * my + j] = m; sc[tx * my + j] = c;
   }
@@ -285,16 +289,19 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
   __syncthreads();
   if (i >= g.mx) return;
   const bool line = i >= 1 && i <= g.mx - 2 && kin;
+#pragma unroll 4
   for (int j = ty; j < my; j += ny) {
     int p = (k * my + j) * g.mx + i;
     T d = sr[tx * my + j];
-    T xo = zero_guess ? T(0) : x[p];
+    T xo = (mode == 0) ? T(0) : x[p];
     xnew[p] = (line && j >= 1 && j <= my - 2) ? xo + omega * d : xo;
   }
 }
 
+// mode 0: zero initial guess (residual = b); 1: residual b - A x computed in
+// the sweep (fused); 2: `b` already holds the residual of x (split variant).
 template <typename T, int TW>
-static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T omega, int zero_guess, cudaStream_t s) {
+static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T omega, int mode, cudaStream_t s) {
   size_t smem = sizeof(T) * 4 * (size_t)L.g.my * TW;
   dim3 grd(nblk(L.g.mx, TW), L.g.mz);
   static bool attr = false;
@@ -302,14 +309,16 @@ static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T ome
     cudaFuncSetAttribute(k_line_sweep<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_line_sweep<T, TW><<<grd, 256, smem, s>>>(L, b, x, xnew, omega, zero_guess); count_launch();
+  k_line_sweep<T, TW><<<grd, 256, smem, s>>>(L, b, x, xnew, omega, mode); count_launch();
 }
 
 // Lines longer than the shared-memory tile allows fall back to a residual
 // kernel plus a one-thread-per-line Thomas kernel.
 template <typename T>
 __global__ void k_line_thomas(Geom g, const T *__restrict__ fac, const T *__restrict__ r,
-                              const T *__restrict__ x, T *__restrict__ xnew, T omega, int zero_guess) {
+                              const T *__restrict__ x, T *__restrict__ xnew, T omega, int zero_guess,
+                              const int *gate) {
+  if (gated(gate)) return;
   size_t n = g.n();
   int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.mx || k >= g.mz) return;
@@ -344,23 +353,36 @@ __global__ void k_line_thomas(Geom g, const T *__restrict__ fac, const T *__rest
 
 static const int kMaxFusedRows = 400;
 
+// Sweep variants: fused (residual inside the tile kernel) or split (a full-
+// occupancy residual kernel into L.t32 / L.t64, then the tile kernel on it).
+// The set-up autotuner stores the faster one per level in L.sweep32 / L.sweep64.
 template <>
 void launch_line_smooth<float>(const LevelDev &L, const float *b, const float *x, float *xnew, float omega,
                                int zero_guess, cudaStream_t s) {
-  if (L.g.my <= kMaxFusedRows) { line_sweep<float, 32>(L, b, x, xnew, omega, zero_guess, s); return; }
+  if (L.g.my <= kMaxFusedRows) {
+    if (zero_guess) line_sweep<float, 32>(L, b, x, xnew, omega, 0, s);
+    else if (L.sweep32 == 1) { launch_residual<float>(L, b, x, L.t32, s); line_sweep<float, 32>(L, L.t32, x, xnew, omega, 2, s); }
+    else line_sweep<float, 32>(L, b, x, xnew, omega, 1, s);
+    return;
+  }
   const float *r = b;
   if (!zero_guess) { launch_residual<float>(L, b, x, L.t32, s); r = L.t32; }
   dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
-  k_line_thomas<float><<<grd, blk, 0, s>>>(L.g, L.line32, r, x, xnew, omega, zero_guess); count_launch();
+  k_line_thomas<float><<<grd, blk, 0, s>>>(L.g, L.line32, r, x, xnew, omega, zero_guess, L.gate); count_launch();
 }
 template <>
 void launch_line_smooth<double>(const LevelDev &L, const double *b, const double *x, double *xnew, double omega,
                                 int zero_guess, cudaStream_t s) {
-  if (L.g.my <= kMaxFusedRows) { line_sweep<double, 16>(L, b, x, xnew, omega, zero_guess, s); return; }
+  if (L.g.my <= kMaxFusedRows) {
+    if (zero_guess) line_sweep<double, 16>(L, b, x, xnew, omega, 0, s);
+    else if (L.sweep64 == 1) { launch_residual<double>(L, b, x, L.t64, s); line_sweep<double, 16>(L, L.t64, x, xnew, omega, 2, s); }
+    else line_sweep<double, 16>(L, b, x, xnew, omega, 1, s);
+    return;
+  }
   const double *r = b;
   if (!zero_guess) { launch_residual<double>(L, b, x, L.t64, s); r = L.t64; }
   dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
-  k_line_thomas<double><<<grd, blk, 0, s>>>(L.g, L.line64, r, x, xnew, omega, zero_guess); count_launch();
+  k_line_thomas<double><<<grd, blk, 0, s>>>(L.g, L.line64, r, x, xnew, omega, zero_guess, L.gate); count_launch();
 }
 
 // ------------------------------------------------------------------ transfers
@@ -376,7 +398,9 @@ __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, 
 // x * max(0, 1 - nvert_fine); zero on the ring and on blocked coarse cells.
 template <typename T>
 __global__ void k_restrict(Geom F, const double *__restrict__ nvf, Geom C, const double *__restrict__ nvc,
-                           int isc, int jsc, int ksc, const T *__restrict__ xf, T *__restrict__ xc) {
+                           int isc, int jsc, int ksc, const T *__restrict__ xf, T *__restrict__ xc,
+                           const int *gate) {
+  if (gated(gate)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= C.mx || j >= C.my) return;
   size_t p = C.id(i, j, k);
@@ -407,7 +431,9 @@ __global__ void k_restrict(Geom F, const double *__restrict__ nvf, Geom C, const
 // falling back to injection next to walls and blocked coarse cells.
 template <typename T>
 __global__ void k_prolong_add(Geom C, const double *__restrict__ nvc, Geom F, const double *__restrict__ nvf,
-                              int isc, int jsc, int ksc, const T *__restrict__ xc, T *__restrict__ xf) {
+                              int isc, int jsc, int ksc, const T *__restrict__ xc, T *__restrict__ xf,
+                              const int *gate) {
+  if (gated(gate)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= F.mx || j >= F.my) return;
   size_t p = F.id(i, j, k);
@@ -433,11 +459,11 @@ __global__ void k_prolong_add(Geom C, const double *__restrict__ nvc, Geom F, co
 
 template <typename T>
 void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s) {
-  k_restrict<T><<<grid3(C.g), kBlk, 0, s>>>(F.g, F.nvert, C.g, C.nvert, C.isc, C.jsc, C.ksc, xf, xc); count_launch();
+  k_restrict<T><<<grid3(C.g), kBlk, 0, s>>>(F.g, F.nvert, C.g, C.nvert, C.isc, C.jsc, C.ksc, xf, xc, F.gate); count_launch();
 }
 template <typename T>
 void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s) {
-  k_prolong_add<T><<<grid3(F.g), kBlk, 0, s>>>(C.g, C.nvert, F.g, F.nvert, F.isc, F.jsc, F.ksc, xc, xf); count_launch();
+  k_prolong_add<T><<<grid3(F.g), kBlk, 0, s>>>(C.g, C.nvert, F.g, F.nvert, F.isc, F.jsc, F.ksc, xc, xf, F.gate); count_launch();
 }
 template void launch_restrict<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t);
 template void launch_restrict<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t);

@@ -179,6 +179,13 @@ class PoissonContext:
             raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
         return st.as_dict()
 
+    def tuning(self):
+        """The set-up autotuner's measurements and choices (dict)."""
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._L.cvb_tuning_report(self._ctx, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
     def time_kernel(self, name, level=-1, reps=20):
         """(average ms per launch, algorithmic bytes per launch) of one kernel."""
         lvl = level % self.nlevels

@@ -200,6 +200,9 @@ enum {
   CVB_KERNEL_RESIDUAL_F32 = 2,   /* b - A x, FP32 flux form */
   CVB_KERNEL_RESIDUAL_F64 = 3    /* b - A x, FP64 stored rows */
 };
+/* JSON record of the set-up autotuner: per level, the measured time of the
+ * fused and the split y-line sweep in each precision and the variant kept. */
+int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len);
 /* Average duration of `reps` back-to-back launches of one kernel on `level`
  * (CUDA events on the context's stream) and its algorithmic bytes per launch
  * (every array it needs, touched once). */
