@@ -239,7 +239,8 @@ def run_cvb(args, ws, rank, local):
     k64_ms, k64_bytes = ctx.time_kernel("residual_f64", level=-1, reps=30)
     peak, peak_kind = peaks()
     cells = int(np.prod(ctx.shapes[-1]))
-    roof = {"kernel": "k_line_sweep<float,32> (fused residual + y-line Thomas), finest level",
+    roof = {"kernel": "FP32 y-line sweep on the finest level, as the set-up autotuner picks it there "
+                      "(split: k_apply32 residual, then k_line_solve<float,32>)",
             "bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
             "traffic": traffic_per_launch("line_sweep_f32", cells), "algorithmic_bytes": k_bytes,

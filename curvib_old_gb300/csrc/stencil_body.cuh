@@ -1,0 +1,494 @@
+// Device code of the curvilinear pressure operator, its y-line smoother and the
+// grid transfers, shared by the single-problem kernels (kernels_stencil.cu) and
+// the grouped kernels of the batch engine (kernels_batch.cu).
+//
+// FP64: y = A x with the 19 stored weights per row (the reference's assembled
+//       PoissonLHSNew rows), 19 FMAs per cell -- the cheapest FP64 form on a
+//       part whose FP64 rate is a small fraction of its FP32 rate.
+// FP32: the same operator matrix-free in flux form: for each face the flux
+//       F = g_nn (x_Q - x_P) + two cross terms whose form (central / one-sided /
+//       none) comes from the cell's switching code; row P is
+//       -aj_P * (F_E - F_W + F_N - F_S + F_T - F_B), each term taken only where
+//       the face is active from P's side.  Reads 9 face coefficients, aj and a
+//       code per cell: ~52 B/cell.
+#pragma once
+#include "cvb_internal.h"
+
+namespace cvb {
+
+
+// ------------------------------------------------------------ neighbourhood
+// 32-bit offsets of the six face neighbours, with the reference's periodic wrap
+// of column indices (poisson.c:1329-1450) folded into the offset at seam cells.
+struct Off {
+  int e, w, n, s, t, b;
+};
+__device__ __forceinline__ Off offsets(const Geom &g, int i, int j, int k) {
+  const int sy = g.mx, sz = g.mx * g.my;
+  Off o;
+  o.e = (g.px && i == g.mx - 2) ? -(g.mx - 3) : 1;
+  o.w = (g.px && i == 1) ? (g.mx - 3) : -1;
+  o.n = (g.py && j == g.my - 2) ? -(g.my - 3) * sy : sy;
+  o.s = (g.py && j == 1) ? (g.my - 3) * sy : -sy;
+  o.t = (g.pz && k == g.mz - 2) ? -(g.mz - 3) * sz : sz;
+  o.b = (g.pz && k == 1) ? (g.mz - 3) * sz : -sz;
+  return o;
+}
+
+// The 19 values of x around an interior cell, in registers.
+template <typename T>
+struct Star {
+  T P, E, W, N, S, Tt, B, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW;
+};
+template <typename T, typename TX>
+__device__ __forceinline__ Star<T> load_star(const TX *__restrict__ x, int p, const Off &o) {
+  Star<T> s;
+  s.P = (T)x[p];
+  s.E = (T)x[p + o.e]; s.W = (T)x[p + o.w]; s.N = (T)x[p + o.n]; s.S = (T)x[p + o.s];
+  s.Tt = (T)x[p + o.t]; s.B = (T)x[p + o.b];
+  s.NE = (T)x[p + o.e + o.n]; s.SE = (T)x[p + o.e + o.s]; s.NW = (T)x[p + o.w + o.n]; s.SW = (T)x[p + o.w + o.s];
+  s.TN = (T)x[p + o.t + o.n]; s.BN = (T)x[p + o.b + o.n]; s.TS = (T)x[p + o.t + o.s]; s.BS = (T)x[p + o.b + o.s];
+  s.TE = (T)x[p + o.t + o.e]; s.BE = (T)x[p + o.b + o.e]; s.TW = (T)x[p + o.t + o.w]; s.BW = (T)x[p + o.b + o.w];
+  return s;
+}
+
+// ----------------------------------------------------------------- FP64 rows
+// (A x)_p with the 19 stored weights; identity rows return x_p.  Every load of
+// the row is issued before anything depends on one of them (the row's code
+// included), so a row costs one memory latency, not a chain of them.
+template <typename TX>
+__device__ __forceinline__ double row64(const Geom &g, const double *__restrict__ w, const uint32_t *__restrict__ code,
+                                        const TX *__restrict__ x, int i, int j, int k, int p, int n) {
+  if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return (double)x[p];
+  Off o = offsets(g, i, j, k);
+  uint32_t c = __ldg(code + p);
+  Star<double> s = load_star<double>(x, p, o);
+  const double *wp = w + p;
+  double r = __ldg(wp + (size_t)CP * n) * s.P;
+  r = fma(__ldg(wp + (size_t)EP * n), s.E, r); r = fma(__ldg(wp + (size_t)WP * n), s.W, r);
+  r = fma(__ldg(wp + (size_t)NP * n), s.N, r); r = fma(__ldg(wp + (size_t)SP * n), s.S, r);
+  r = fma(__ldg(wp + (size_t)TP * n), s.Tt, r); r = fma(__ldg(wp + (size_t)BP * n), s.B, r);
+  r = fma(__ldg(wp + (size_t)NE * n), s.NE, r); r = fma(__ldg(wp + (size_t)SE * n), s.SE, r);
+  r = fma(__ldg(wp + (size_t)NW * n), s.NW, r); r = fma(__ldg(wp + (size_t)SW * n), s.SW, r);
+  r = fma(__ldg(wp + (size_t)TN * n), s.TN, r); r = fma(__ldg(wp + (size_t)BN * n), s.BN, r);
+  r = fma(__ldg(wp + (size_t)TS * n), s.TS, r); r = fma(__ldg(wp + (size_t)BS * n), s.BS, r);
+  r = fma(__ldg(wp + (size_t)TE * n), s.TE, r); r = fma(__ldg(wp + (size_t)BE * n), s.BE, r);
+  r = fma(__ldg(wp + (size_t)TW * n), s.TW, r); r = fma(__ldg(wp + (size_t)BW * n), s.BW, r);
+  return (c & CODE_IDENTITY) ? s.P : r;
+}
+
+// ----------------------------------------------------------------- FP32 rows
+// Cross term of a face flux: g * (cu*s_up + c0*s_level + cd*s_down) for the
+// central / lower / upper forms (branch 1/2/3), zero for branch 0.
+__device__ __forceinline__ float cross32(int br, float g, float su, float s0, float sd) {
+  float cu = br == 1 ? 0.25f : (br == 3 ? 0.5f : 0.0f);
+  float c0 = br == 2 ? 0.5f : (br == 3 ? -0.5f : 0.0f);
+  float cd = br == 1 ? -0.25f : (br == 2 ? -0.5f : 0.0f);
+  return g * (cu * su + c0 * s0 + cd * sd);
+}
+__device__ __forceinline__ float act(uint32_t c, uint32_t bit) { return (c & bit) ? 1.0f : 0.0f; }
+
+// (A x)_p in flux form: each active face flux from its cell's coefficients and
+// branch codes; the lower faces are the upper faces of the W/S/B neighbours.
+// Loads first (all unconditional, in bounds for interior cells), then the
+// arithmetic with the activity bits as 0/1 factors.
+template <typename TX>
+__device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ gf, const float *__restrict__ aj,
+                                       const uint32_t *__restrict__ code, const TX *__restrict__ x, int i, int j,
+                                       int k, int p, int n) {
+  if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return (float)x[p];
+  Off o = offsets(g, i, j, k);
+  const int pw = p - 1, ps = p - g.mx, pb = p - g.mx * g.my;  // lower neighbours (never wrapped)
+  const uint32_t c = __ldg(code + p), cw = __ldg(code + pw), cs = __ldg(code + ps), cb = __ldg(code + pb);
+  Star<float> s = load_star<float>(x, p, o);
+  const float g11 = __ldg(gf + p), g12 = __ldg(gf + n + p), g13 = __ldg(gf + 2 * n + p);
+  const float g21 = __ldg(gf + 3 * n + p), g22 = __ldg(gf + 4 * n + p), g23 = __ldg(gf + 5 * n + p);
+  const float g31 = __ldg(gf + 6 * n + p), g32 = __ldg(gf + 7 * n + p), g33 = __ldg(gf + 8 * n + p);
+  const float w11 = __ldg(gf + pw), w12 = __ldg(gf + n + pw), w13 = __ldg(gf + 2 * n + pw);
+  const float s21 = __ldg(gf + 3 * n + ps), s22 = __ldg(gf + 4 * n + ps), s23 = __ldg(gf + 5 * n + ps);
+  const float b31 = __ldg(gf + 6 * n + pb), b32 = __ldg(gf + 7 * n + pb), b33 = __ldg(gf + 8 * n + pb);
+  const float ajp = __ldg(aj + p);
+  float fe = g11 * (s.E - s.P) + cross32(code_branch(c, 0, 0), g12, s.N + s.NE, s.P + s.E, s.S + s.SE) +
+             cross32(code_branch(c, 0, 1), g13, s.Tt + s.TE, s.P + s.E, s.B + s.BE);
+  float fw = w11 * (s.P - s.W) + cross32(code_branch(cw, 0, 0), w12, s.NW + s.N, s.W + s.P, s.SW + s.S) +
+             cross32(code_branch(cw, 0, 1), w13, s.TW + s.Tt, s.W + s.P, s.BW + s.B);
+  float fn = g22 * (s.N - s.P) + cross32(code_branch(c, 1, 0), g21, s.E + s.NE, s.P + s.N, s.W + s.NW) +
+             cross32(code_branch(c, 1, 1), g23, s.Tt + s.TN, s.P + s.N, s.B + s.BN);
+  float fs = s22 * (s.P - s.S) + cross32(code_branch(cs, 1, 0), s21, s.SE + s.E, s.S + s.P, s.SW + s.W) +
+             cross32(code_branch(cs, 1, 1), s23, s.TS + s.Tt, s.S + s.P, s.BS + s.B);
+  float ft = g33 * (s.Tt - s.P) + cross32(code_branch(c, 2, 0), g31, s.E + s.TE, s.P + s.Tt, s.W + s.TW) +
+             cross32(code_branch(c, 2, 1), g32, s.N + s.TN, s.P + s.Tt, s.S + s.TS);
+  float fb = b33 * (s.P - s.B) + cross32(code_branch(cb, 2, 0), b31, s.BE + s.E, s.B + s.P, s.BW + s.W) +
+             cross32(code_branch(cb, 2, 1), b32, s.BN + s.N, s.B + s.P, s.BS + s.S);
+  float acc = act(c, CODE_ACT_E) * fe - act(c, CODE_ACT_W) * fw + act(c, CODE_ACT_N) * fn -
+              act(c, CODE_ACT_S) * fs + act(c, CODE_ACT_T) * ft - act(c, CODE_ACT_B) * fb;
+  return (c & CODE_IDENTITY) ? s.P : -ajp * acc;
+}
+
+// ------------------------------------------------------- apply / residual
+// y = A x (b == nullptr) or y = b - A x.  One thread per cell.
+// Bodies take the block's coordinates explicitly so that the grouped (batched)
+// kernels can run them for any problem of a work-list; blocks are 32 x 4.
+template <typename TX>
+__device__ __forceinline__ void apply64_body(const Geom &g, const double *__restrict__ w,
+                                             const uint32_t *__restrict__ code, const TX *__restrict__ x,
+                                             const double *__restrict__ b, double *__restrict__ y, int bx, int by,
+                                             int bz) {
+  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
+  if (i >= g.mx || j >= g.my) return;
+  int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
+  double ax = row64(g, w, code, x, i, j, k, p, n);
+  y[p] = b ? b[p] - ax : ax;
+}
+
+__device__ __forceinline__ void apply32_body(const Geom &g, const float *__restrict__ gf, const float *__restrict__ aj,
+                                             const uint32_t *__restrict__ code, const float *__restrict__ x,
+                                             const float *__restrict__ b, float *__restrict__ y, int bx, int by,
+                                             int bz) {
+  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
+  if (i >= g.mx || j >= g.my) return;
+  int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
+  float ax = row32(g, gf, aj, code, x, i, j, k, p, n);
+  y[p] = b ? b[p] - ax : ax;
+}
+
+
+// ------------------------------------------------------------ y-line smoother
+// One damped line-Jacobi sweep, fused: xnew = x + omega * T^-1 (b - A x), T the
+// tridiagonal in-line (j) part of A with Thomas factors from set-up.
+// A block owns a tile of TW consecutive i over all j at one k.  Phase 1: all
+// threads compute the tile's residual into shared memory and stage the three
+// factor arrays there (coalesced, many loads in flight; read from global inside
+// the recurrence they would cost a memory latency per step).  Phase 2: TW threads
+// run the forward/backward recurrences out of shared memory, one line each.
+// Phase 3: all threads write x + omega*delta.  Zero guess: the residual is b.
+template <typename T>
+struct RowOf;
+template <>
+struct RowOf<float> {
+  __device__ static float r(const Geom &g, const LevelDev &L, const float *x, int i, int j, int k, int p, int n) {
+    return row32(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
+  }
+  __device__ static const float *fac(const LevelDev &L) { return L.line32; }
+};
+template <>
+struct RowOf<double> {
+  __device__ static double r(const Geom &g, const LevelDev &L, const double *x, int i, int j, int k, int p, int n) {
+    return row64(g, L.w64, L.code, x, i, j, k, p, n);
+  }
+  __device__ static const double *fac(const LevelDev &L) { return L.line64; }
+};
+
+// Solves one line's tridiagonal system in place with one warp.  The Thomas
+// passes are first-order affine recurrences, d_j = gamma_j + beta_j d_{j-1}
+// (forward: gamma = m r, beta = -m a; backward: gamma = d, beta = -c), and
+// affine maps compose associatively: each lane composes the maps of its
+// contiguous rows, a shuffle scan combines the lanes, each lane replays its rows.
+// r/a/m/c: this line's arrays in shared memory, indexed by row j = 1..nr.
+template <typename T>
+__device__ __forceinline__ void warp_line_solve(T *r, const T *a, const T *m, const T *c, int nr, int lane) {
+  const int R = (nr + 31) >> 5;
+  const int q0 = lane * R, q1 = min(q0 + R, nr);
+  // forward: d_q = m_q (r_q - a_q d_{q-1})
+  T B = T(1), G = T(0);
+  for (int q = q0; q < q1; q++) {
+    T mq = m[q + 1];
+    T beta = -mq * a[q + 1], gamma = mq * r[q + 1];
+    B = beta * B;
+    G = beta * G + gamma;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T Bp = __shfl_up_sync(0xffffffffu, B, o), Gp = __shfl_up_sync(0xffffffffu, G, o);
+    if (lane >= o) { G = B * Gp + G; B = B * Bp; }
+  }
+  T d = __shfl_up_sync(0xffffffffu, G, 1);
+  if (lane == 0) d = T(0);
+  for (int q = q0; q < q1; q++) {
+    T mq = m[q + 1];
+    d = mq * r[q + 1] - mq * a[q + 1] * d;
+    r[q + 1] = d;
+  }
+  __syncwarp();
+  // backward: x_q = d_q - c_q x_{q+1}
+  B = T(1); G = T(0);
+  for (int q = q1 - 1; q >= q0; q--) {
+    T beta = -c[q + 1], gamma = r[q + 1];
+    B = beta * B;
+    G = beta * G + gamma;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T Bn = __shfl_down_sync(0xffffffffu, B, o), Gn = __shfl_down_sync(0xffffffffu, G, o);
+    if (lane + o < 32) { G = B * Gn + G; B = B * Bn; }
+  }
+  T xs = __shfl_down_sync(0xffffffffu, G, 1);
+  if (lane == 31) xs = T(0);
+  for (int q = q1 - 1; q >= q0; q--) {
+    xs = r[q + 1] - c[q + 1] * xs;
+    r[q + 1] = xs;
+  }
+  __syncwarp();
+}
+
+// One damped line-Jacobi sweep, fused: xnew = x + omega * T^-1 (b - A x).
+// A block owns TW lines (consecutive i at one k) over all j.  Phase 1: all
+// threads compute the tile's residuals and stage the Thomas factors in shared
+// memory (laid out line by line).  Phase 2: each warp solves TW/8 lines with
+// warp_line_solve.  Phase 3: all threads write x + omega*delta.
+template <typename T, int TW>
+__device__ __forceinline__ void line_sweep_body(const LevelDev &L, const T *__restrict__ b, const T *__restrict__ x,
+                                                T *__restrict__ xnew, T omega, int mode, int bx, int bk,
+                                                unsigned char *smem_raw) {
+  const Geom g = L.g;
+  const int my = g.my, n = (int)g.n();
+  T *sr = reinterpret_cast<T *>(smem_raw);  // [TW][my] residual -> line solution
+  T *sa = sr + my * TW, *sm = sa + my * TW, *sc = sm + my * TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int i0 = bx * TW, k = bk;
+  const int i = i0 + tx;
+  const bool kin = k >= 1 && k <= g.mz - 2;
+  const T *fa = RowOf<T>::fac(L);
+#pragma unroll 4
+  for (int j = ty; j < my; j += ny) {
+    const bool line = i >= 1 && i <= g.mx - 2 && kin;
+    int p = (k * my + j) * g.mx + i;
+    T r = T(0), a = T(0), m = T(1), c = T(0);
+    if (line && j >= 1 && j <= my - 2) {
+      a = __ldg(fa + p); m = __ldg(fa + n + p); c = __ldg(fa + 2 * n + p);
+      r = (mode == 1) ? b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n) : b[p];
+    }
+    sr[tx * my + j] = r; sa[tx * my + j] = a; sm[tx * my + j] = m; sc[tx * my + j] = c;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int t = warp; t < TW; t += nwarps) {
+    int it = i0 + t;
+    if (it >= 1 && it <= g.mx - 2 && kin)
+      warp_line_solve<T>(sr + t * my, sa + t * my, sm + t * my, sc + t * my, my - 2, lane);
+  }
+  __syncthreads();
+  if (i >= g.mx) return;
+  const bool line = i >= 1 && i <= g.mx - 2 && kin;
+#pragma unroll 4
+  for (int j = ty; j < my; j += ny) {
+    int p = (k * my + j) * g.mx + i;
+    T d = sr[tx * my + j];
+    T xo = (mode == 0) ? T(0) : x[p];
+    xnew[p] = (line && j >= 1 && j <= my - 2) ? xo + omega * d : xo;
+  }
+}
+
+
+// ---- line solve on a given residual, inputs staged by asynchronous copies ----
+// The row pitch of a level (mx * sizeof(T), mx = IM+1) is not a multiple of 16
+// bytes, so neither TMA tensor maps nor 16-byte bulk copies can address the
+// tile; element-wise cp.async moves it instead.  Every thread issues all of its
+// copies at once (no register staging, so no load latency per row), and the
+// block waits once.
+__device__ __forceinline__ void cp_async_el(float *dst, const float *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_el(double *dst, const double *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Shared-memory layout of one line for the warp solve: lane l owns rows
+// [l*R, l*R + R) and keeps them at [l*S, l*S + R) with S = R or R+1, whichever
+// is odd, so the 32 lanes of a warp hit 32 different banks.  Lines are `ls`
+// apart, ls = 32*S + 1 (odd), so a warp walking one row across 32 lines is also
+// conflict-free.
+struct LineLayout {
+  int nr, R, S, ls;
+  __host__ __device__ static LineLayout of(int my) {
+    LineLayout o;
+    o.nr = my - 2;
+    o.R = (o.nr + 31) >> 5;
+    o.S = o.R | 1;
+    o.ls = 32 * o.S + 1;
+    return o;
+  }
+  __device__ int pos(int q) const { return q + (q / R) * (S - R); }  // q = row - 1
+};
+
+// Dynamic shared memory of the two line kernels for a level.
+template <typename T, int TW>
+inline size_t line_sweep_smem(const Geom &g) { return sizeof(T) * 4 * (size_t)g.my * TW; }
+template <typename T, int TW>
+inline size_t line_solve_smem(const Geom &g) { return sizeof(T) * 5 * (size_t)LineLayout::of(g.my).ls * TW; }
+
+template <typename T>
+__device__ __forceinline__ void warp_line_solve_padded(T *r, const T *a, const T *m, const T *c, const LineLayout &Lo,
+                                                       int lane) {
+  const int q0 = lane * Lo.R, cnt = max(0, min(Lo.R, Lo.nr - q0));
+  const int b0 = lane * Lo.S;
+  T B = T(1), G = T(0);
+  for (int t = 0; t < cnt; t++) {
+    T mq = m[b0 + t];
+    T beta = -mq * a[b0 + t], gamma = mq * r[b0 + t];
+    B = beta * B;
+    G = beta * G + gamma;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T Bp = __shfl_up_sync(0xffffffffu, B, o), Gp = __shfl_up_sync(0xffffffffu, G, o);
+    if (lane >= o) { G = B * Gp + G; B = B * Bp; }
+  }
+  T d = __shfl_up_sync(0xffffffffu, G, 1);
+  if (lane == 0) d = T(0);
+  for (int t = 0; t < cnt; t++) {
+    T mq = m[b0 + t];
+    d = mq * r[b0 + t] - mq * a[b0 + t] * d;
+    r[b0 + t] = d;
+  }
+  __syncwarp();
+  B = T(1); G = T(0);
+  for (int t = cnt - 1; t >= 0; t--) {
+    T beta = -c[b0 + t], gamma = r[b0 + t];
+    B = beta * B;
+    G = beta * G + gamma;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T Bn = __shfl_down_sync(0xffffffffu, B, o), Gn = __shfl_down_sync(0xffffffffu, G, o);
+    if (lane + o < 32) { G = B * Gn + G; B = B * Bn; }
+  }
+  T xs = __shfl_down_sync(0xffffffffu, G, 1);
+  if (lane == 31) xs = T(0);
+  for (int t = cnt - 1; t >= 0; t--) {
+    xs = r[b0 + t] - c[b0 + t] * xs;
+    r[b0 + t] = xs;
+  }
+  __syncwarp();
+}
+
+// xnew = x + omega * T^-1 r on interior lines, x elsewhere; r is the residual of
+// x (split sweep) or, with x == nullptr, the right-hand side (zero guess).
+template <typename T, int TW>
+__device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
+                                                T *__restrict__ xnew, T omega, int bx, int bk,
+                                                unsigned char *smem_raw) {
+  const Geom g = L.g;
+  const int my = g.my;
+  const LineLayout Lo = LineLayout::of(my);
+  const size_t n = g.n();
+  T *sr = reinterpret_cast<T *>(smem_raw);
+  T *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int i0 = bx * TW, k = bk, i = i0 + tx;
+  const bool kin = k >= 1 && k <= g.mz - 2;
+  const bool line = i >= 1 && i <= g.mx - 2 && kin;
+  const T *fa = RowOf<T>::fac(L);
+  if (line) {
+    for (int j = 1 + ty; j <= my - 2; j += ny) {
+      size_t p = ((size_t)k * my + j) * g.mx + i;
+      int s = tx * Lo.ls + Lo.pos(j - 1);
+      cp_async_el(sr + s, r + p);
+      cp_async_el(sa + s, fa + p);
+      cp_async_el(sm + s, fa + n + p);
+      cp_async_el(sc + s, fa + 2 * n + p);
+      if (x) cp_async_el(sx + s, x + p);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int t = warp; t < TW; t += nwarps) {
+    int it = i0 + t;
+    if (it >= 1 && it <= g.mx - 2 && kin)
+      warp_line_solve_padded<T>(sr + t * Lo.ls, sa + t * Lo.ls, sm + t * Lo.ls, sc + t * Lo.ls, Lo, lane);
+  }
+  __syncthreads();
+  if (i >= g.mx) return;
+  for (int j = ty; j < my; j += ny) {
+    size_t p = ((size_t)k * my + j) * g.mx + i;
+    if (line && j >= 1 && j <= my - 2) {
+      int s = tx * Lo.ls + Lo.pos(j - 1);
+      T xo = x ? sx[s] : T(0);
+      xnew[p] = xo + omega * sr[s];
+    } else {
+      xnew[p] = x ? x[p] : T(0);
+    }
+  }
+}
+
+
+
+
+// ------------------------------------------------------------------ transfers
+// Products in the transfers are rounded on their own (no fused multiply-add), as
+// the reference's C evaluates them, so FP64 transfers match it bit for bit.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+// MyRestriction (poisson.c:129-226): coarse = 0.125 * sum over the 8 children of
+// x * max(0, 1 - nvert_fine); zero on the ring and on blocked coarse cells.
+template <typename T>
+__device__ __forceinline__ void restrict_body(const Geom &F, const double *__restrict__ nvf, const Geom &C,
+                                              const double *__restrict__ nvc, int isc, int jsc, int ksc,
+                                              const T *__restrict__ xf, T *__restrict__ xc, int bx, int by, int bz) {
+  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
+  if (i >= C.mx || j >= C.my) return;
+  size_t p = C.id(i, j, k);
+  if (i == 0 || i == C.mx - 1 || j == 0 || j == C.my - 1 || k == 0 || k == C.mz - 1 || nvc[p] > 0.1) {
+    xc[p] = T(0);
+    return;
+  }
+  int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+  int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
+  auto W = [&](int a, int b, int c) {
+    size_t q = F.id(a, b, c);
+    double wt = 1.0 - nvf[q];
+    return mul_rn(xf[q], (T)(wt > 0.0 ? wt : 0.0));
+  };
+  T s = W(ih, jh, kh);
+  s = add_rn(s, W(ih - ia, jh, kh));
+  s = add_rn(s, W(ih, jh - ja, kh));
+  s = add_rn(s, W(ih, jh, kh - ka));
+  s = add_rn(s, W(ih - ia, jh - ja, kh));
+  s = add_rn(s, W(ih, jh - ja, kh - ka));
+  s = add_rn(s, W(ih - ia, jh, kh - ka));
+  s = add_rn(s, W(ih - ia, jh - ja, kh - ka));
+  xc[p] = mul_rn(T(0.125), s);
+}
+
+// MyInterpolation (poisson.c:228-370), added into xf: cell-centred trilinear
+// weights 27/9/9/3/9/3/3/1 over 64 toward the neighbour on the child's side,
+// falling back to injection next to walls and blocked coarse cells.
+template <typename T>
+__device__ __forceinline__ void prolong_body(const Geom &C, const double *__restrict__ nvc, const Geom &F,
+                                             const double *__restrict__ nvf, int isc, int jsc, int ksc,
+                                             const T *__restrict__ xc, T *__restrict__ xf, int bx, int by, int bz) {
+  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
+  if (i >= F.mx || j >= F.my) return;
+  size_t p = F.id(i, j, k);
+  if (i == 0 || i == F.mx - 1 || j == 0 || j == F.my - 1 || k == 0 || k == F.mz - 1 || nvf[p] > 0.1) return;
+  int ic, jc, kc, ia, ja, ka;
+  if (isc) { ic = i; ia = 0; } else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == F.mx - 2) ia = 0; }
+  if (jsc) { jc = j; ja = 0; } else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == F.my - 2) ja = 0; }
+  if (ksc) { kc = k; ka = 0; } else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == F.mz - 2) ka = 0; }
+  if (ka == -1 && nvc[C.id(ic, jc, kc - 1)] > 0.1) ka = 0;
+  else if (ka == 1 && nvc[C.id(ic, jc, kc + 1)] > 0.1) ka = 0;
+  if (ja == -1 && nvc[C.id(ic, jc - 1, kc)] > 0.1) ja = 0;
+  else if (ja == 1 && nvc[C.id(ic, jc + 1, kc)] > 0.1) ja = 0;
+  if (ia == -1 && nvc[C.id(ic - 1, jc, kc)] > 0.1) ia = 0;
+  else if (ia == 1 && nvc[C.id(ic + 1, jc, kc)] > 0.1) ia = 0;
+  auto X = [&](int a, int b, int c) { return xc[C.id(a, b, c)]; };
+  T s1 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc), T(9)), mul_rn(X(ic, jc + ja, kc), T(3))),
+                       mul_rn(X(ic + ia, jc, kc), T(3))), X(ic + ia, jc + ja, kc));
+  T s2 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc + ka), T(9)), mul_rn(X(ic, jc + ja, kc + ka), T(3))),
+                       mul_rn(X(ic + ia, jc, kc + ka), T(3))), X(ic + ia, jc + ja, kc + ka));
+  T v = add_rn(div_rn(mul_rn(s1, T(3)), T(64)), div_rn(s2, T(64)));
+  xf[p] = add_rn(xf[p], v);
+}
+
+
+}  // namespace cvb

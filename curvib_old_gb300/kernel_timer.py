@@ -1,0 +1,58 @@
+"""Times the multigrid kernels of one level with CUDA events.
+
+    python -m curvib_old_gb300.kernel_timer [--cells 256x128x128] [--level -1] [--reps 20] [KERNEL ...]
+
+KERNEL is one of line_sweep_f32, line_sweep_f64, residual_f32, residual_f64
+(default: all four).  The problem is the periodic channel (x and z periodic,
+tanh-stretched walls in y, factor 2.5) at the given cell counts.  Each kernel's
+timed launches run inside an NVTX range named ``timed:<kernel>``, so a profiler
+can be pointed at exactly those launches (``ncu --nvtx --nvtx-include
+"timed:line_sweep_f32/"``) and skip the set-up autotuner's launches.  Prints one
+JSON object per kernel: microseconds per launch, algorithmic bytes per launch
+(every array the kernel needs, read or written once) and the GB/s they imply.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+from . import workload as W
+from ._lib import KERNELS
+from .solver import PoissonContext
+
+
+def _cells(text):
+    parts = [int(v) for v in text.lower().split("x")]
+    if len(parts) != 3 or min(parts) < 4:
+        raise argparse.ArgumentTypeError("cells must look like 256x128x128")
+    return tuple(parts)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("kernels", nargs="*", default=list(KERNELS))
+    ap.add_argument("--cells", type=_cells, default=(256, 128, 128))
+    ap.add_argument("--level", type=int, default=-1, help="multigrid level (0 coarsest, -1 finest)")
+    ap.add_argument("--reps", type=int, default=20)
+    a = ap.parse_args(argv)
+    for k in a.kernels:
+        if k not in KERNELS:
+            ap.error(f"unknown kernel {k!r}; choose from {sorted(KERNELS)}")
+    import torch  # NVTX ranges only; the kernels themselves come from libcvb.so
+
+    problem = W.config1_problem(cells=a.cells)
+    ctx = PoissonContext().setup(problem)
+    for k in a.kernels:
+        torch.cuda.nvtx.range_push(f"timed:{k}")
+        ms, nbytes = ctx.time_kernel(k, level=a.level, reps=a.reps)
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"kernel": k, "level": a.level % ctx.nlevels, "cells": int(np.prod(ctx.shapes[a.level])),
+                          "us": round(ms * 1e3, 2), "bytes": int(nbytes),
+                          "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1)}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
