@@ -80,6 +80,18 @@ EXPORTS = {
     "cvb_time_kernel": ([_P, _I, _I, _I, _P, _P], _I),
     "cvb_tuning_report": ([_P, ctypes.c_char_p, _I], _I),
     "cvb_poisson_rhs_noalloc": ([_P, _P, _P, _I, _I, _I, _D, _D, _P, _P, _P], _I),
+    "cvb_batch_create": ([_P, _P, _P], _I),
+    "cvb_batch_destroy": ([_P], None),
+    "cvb_batch_last_error": ([_P], ctypes.c_char_p),
+    "cvb_batch_submit": ([_P, _P, _P, _D, _D, _I, _I, _I, _P], _I),
+    "cvb_batch_step": ([_P, _P], _I),
+    "cvb_batch_poll": ([_P, _P, _P], _I),
+    "cvb_batch_read_phi": ([_P, _P, _P], _I),
+    "cvb_batch_solve": ([_P, _I, _P, _P], _I),
+    "cvb_batch_in_flight": ([_P], _I),
+    "cvb_device_bytes": ([_P, _P], _I),
+    "cvb_set_rhs": ([_P, _P], _I),
+    "cvb_get_phi": ([_P, _P], _I),
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3}
 

@@ -34,7 +34,7 @@ def _sources():
 
 
 def _headers_mtime():
-    hs = list(SRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    hs = list(SRC.glob("*.h")) + list(SRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 

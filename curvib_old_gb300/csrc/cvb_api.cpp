@@ -12,58 +12,9 @@
 #include <string>
 #include <vector>
 
-#include "cvb_internal.h"
+#include "cvb_ctx.h"
 
 using namespace cvb;
-
-namespace {
-
-constexpr int kMaxRestart = 64;
-
-struct LevelHost {
-  cvb_level_desc d;  // shapes / flags only (pointers are not kept)
-};
-
-}  // namespace
-
-struct cvb_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  std::string err;
-  std::vector<void *> allocs;
-
-  int nlevels = 0;
-  std::vector<LevelDev> L;       // 0 = coarsest
-  std::vector<LevelHost> H;
-  // per-level raw face metrics (kept for the finest level: Projection reads them)
-  std::vector<std::vector<double *>> fm;  // [level][9] Cmpnts arrays
-  std::vector<double *> iaj, jaj, kaj, aj64;
-  double *area3 = nullptr;       // finest: |csi|,|eta|,|zet| per cell ([3][N])
-  double *nvert_tmp = nullptr;
-  // coarsest-level solver
-  double *Minv = nullptr;
-  int ncoarse = 0;
-  bool coarse_dense = false;
-  int multinullspace = 0;
-  std::vector<int> kske;
-  // finest-level solver workspace
-  double *b = nullptr, *x = nullptr, *w = nullptr, *r = nullptr;
-  double *V[kMaxRestart + 1] = {};
-  double *Z64[kMaxRestart] = {};
-  float *Z32[kMaxRestart] = {};
-  float *b32 = nullptr;
-  double **dV = nullptr;  // device copies of the pointer tables
-  double **dZ64 = nullptr;
-  float **dZ32 = nullptr;
-  double *partial = nullptr, *sums = nullptr, *hdev = nullptr;
-  double *uc_dev = nullptr, *p_dev = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  bool ready = false;
-  // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
-  struct Tune { int level; size_t cells; double us32[2], us64[2]; };
-  std::vector<Tune> tune;
-};
 
 // ------------------------------------------------------------------ helpers
 static int fail(cvb_ctx *c, int code, const char *fmt, ...) __attribute__((format(printf, 3, 4)));
@@ -109,6 +60,7 @@ static int dalloc(cvb_ctx *ctx, T **p, size_t count) {
     return fail(ctx, CVB_OOM, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
   }
   ctx->allocs.push_back((void *)*p);
+  ctx->device_bytes += sizeof(T) * count;
   return CVB_OK;
 }
 
@@ -116,6 +68,7 @@ static void free_all(cvb_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (void *p : ctx->allocs) cudaFree(p);
   ctx->allocs.clear();
+  ctx->device_bytes = 0;
   ctx->L.clear();
   ctx->H.clear();
   ctx->fm.clear();
@@ -790,7 +743,7 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, con
 }  // extern "C"
 
 // Krylov basis is allocated lazily, sized by the largest restart requested.
-static int ensure_basis(cvb_ctx *ctx, int m, bool mixed) {
+int cvb_ensure_basis(cvb_ctx *ctx, int m, bool mixed) {
   size_t n = ctx->L[ctx->nlevels - 1].g.n();
   bool changed = false;
   for (int q = 0; q <= m; q++)
@@ -885,7 +838,7 @@ int cvb_solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *s
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
   cvb_solve_opts def;
   if (!o) { cvb_solve_opts_default(&def); o = &def; }
-  TRY(ensure_basis(ctx, std::min(std::max(o->restart, 1), kMaxRestart), o->precision == CVB_PRECISION_MIXED));
+  TRY(cvb_ensure_basis(ctx, std::min(std::max(o->restart, 1), kMaxRestart), o->precision == CVB_PRECISION_MIXED));
   return solve_resident(ctx, o, st);
 }
 
@@ -1017,6 +970,28 @@ int cvb_interpolate(cvb_ctx *ctx, int fine, const double *xc, double *xf) {
 }
 
 long long cvb_kernel_launches(void) { return launch_count(); }
+
+int cvb_set_rhs(cvb_ctx *ctx, const double *b) {
+  if (!ctx || !b) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  CK(cudaMemcpyAsync(ctx->b, b, sizeof(double) * fine_n(ctx), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_get_phi(cvb_ctx *ctx, double *phi) {
+  if (!ctx || !phi) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  CK(cudaMemcpyAsync(phi, ctx->x, sizeof(double) * fine_n(ctx), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes) {
+  if (!ctx || !bytes) return CVB_BAD_INPUT;
+  *bytes = (unsigned long long)ctx->device_bytes;
+  return CVB_OK;
+}
 
 int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
   if (!ctx) return CVB_BAD_INPUT;

@@ -1,0 +1,64 @@
+// The per-block context behind the cvb C ABI, shared by the single-solve host
+// code (cvb_api.cpp) and the batch engine (cvb_batch.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cvb.h"
+#include "cvb_internal.h"
+
+namespace cvb {
+
+constexpr int kMaxRestart = 64;
+
+struct LevelHost {
+  cvb_level_desc d;  // shapes / flags only (pointers are not kept)
+};
+
+}  // namespace cvb
+
+struct cvb_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  std::vector<void *> allocs;
+  size_t device_bytes = 0;  // sum of this context's device allocations
+
+  int nlevels = 0;
+  std::vector<cvb::LevelDev> L;       // 0 = coarsest
+  std::vector<cvb::LevelHost> H;
+  // per-level raw face metrics (kept for the finest level: Projection reads them)
+  std::vector<std::vector<double *>> fm;  // [level][9] Cmpnts arrays
+  std::vector<double *> iaj, jaj, kaj, aj64;
+  double *area3 = nullptr;       // finest: |csi|,|eta|,|zet| per cell ([3][N])
+  double *nvert_tmp = nullptr;
+  // coarsest-level solver
+  double *Minv = nullptr;
+  int ncoarse = 0;
+  bool coarse_dense = false;
+  int multinullspace = 0;
+  std::vector<int> kske;
+  // finest-level solver workspace
+  double *b = nullptr, *x = nullptr, *w = nullptr, *r = nullptr;
+  double *V[cvb::kMaxRestart + 1] = {};
+  double *Z64[cvb::kMaxRestart] = {};
+  float *Z32[cvb::kMaxRestart] = {};
+  float *b32 = nullptr;
+  double **dV = nullptr;  // device copies of the pointer tables
+  double **dZ64 = nullptr;
+  float **dZ32 = nullptr;
+  double *partial = nullptr, *sums = nullptr, *hdev = nullptr;
+  double *uc_dev = nullptr, *p_dev = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool ready = false;
+  // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
+  struct Tune { int level; size_t cells; double us32[2], us64[2]; };
+  std::vector<Tune> tune;
+};
+
+// Allocates the finest level's FGMRES basis V[0..m], Z[0..m-1] (and the FP32
+// V-cycle output in mixed precision) if missing, and refreshes the device tables.
+int cvb_ensure_basis(cvb_ctx *ctx, int m, bool mixed);

@@ -179,6 +179,21 @@ class PoissonContext:
             raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
         return st.as_dict()
 
+    def set_rhs(self, b):
+        """Copy a host right-hand side into the resident rhs."""
+        self._check(self._L.cvb_set_rhs(self._ctx, ptr(_c64(b))))
+
+    def get_phi(self):
+        """The resident solution, copied to the host."""
+        phi = np.zeros(self.shapes[-1])
+        self._check(self._L.cvb_get_phi(self._ctx, ptr(phi)))
+        return phi
+
+    def device_bytes(self):
+        v = ctypes.c_ulonglong()
+        self._check(self._L.cvb_device_bytes(self._ctx, ctypes.byref(v)))
+        return int(v.value)
+
     def tuning(self):
         """The set-up autotuner's measurements and choices (dict)."""
         import json
@@ -226,3 +241,90 @@ class PoissonContext:
         y = np.array(x, dtype=np.float64, order="C", copy=True)
         self._check(self._L.cvb_nullspace(self._ctx, level, ptr(y)))
         return y
+
+
+class SolveBatch:
+    """Many solves at once on set-up PoissonContexts (cvb_batch_*).
+
+    ``solve(ctxs)`` runs a fixed set to completion; ``submit`` / ``step`` /
+    ``poll`` run a stream of solves with continuous batching.  Precision,
+    restart, sweeps and omega are batch-wide (``opts``); tolerances per solve.
+    """
+
+    def __init__(self, device: int = 0, stream=None, **opts):
+        L = _lib.lib()
+        self._L = L
+        self._b = ctypes.c_void_p()
+        o = _lib.Options()
+        o.device = device
+        o.stream = stream
+        self.opts = default_opts(**opts)
+        rc = L.cvb_batch_create(ctypes.byref(self._b), ctypes.byref(o), ctypes.byref(self.opts))
+        if rc:
+            raise CvbError(rc, "cvb_batch_create failed")
+        self._ctx_of = {}
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._L.cvb_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise CvbError(rc, self._L.cvb_batch_last_error(self._b).decode())
+
+    def submit(self, ctx, b=None, rtol=None, atol=None, max_it=None, warm_start=False, project_rhs=True):
+        """Queue a solve of ``ctx``'s resident rhs (or of ``b``); returns its ticket."""
+        t = ctypes.c_int()
+        bb = None if b is None else _c64(b)
+        self._check(self._L.cvb_batch_submit(
+            self._b, ctx._ctx, None if bb is None else ptr(bb),
+            self.opts.rtol if rtol is None else rtol, self.opts.atol if atol is None else atol,
+            self.opts.max_it if max_it is None else max_it, int(warm_start), int(project_rhs), ctypes.byref(t)))
+        self._ctx_of[t.value] = ctx
+        if bb is not None:
+            self._keep[t.value] = bb
+        return t.value
+
+    def step(self):
+        """Admit queued solves and issue one round; returns the solves still in flight."""
+        n = ctypes.c_int()
+        self._check(self._L.cvb_batch_step(self._b, ctypes.byref(n)))
+        return n.value
+
+    def poll(self):
+        """[(ticket, stats dict), ...] of the solves that finished so far."""
+        out = []
+        while True:
+            t = ctypes.c_int()
+            st = _lib.SolveStats()
+            self._check(self._L.cvb_batch_poll(self._b, ctypes.byref(t), ctypes.byref(st)))
+            if t.value < 0:
+                return out
+            self._keep.pop(t.value, None)
+            self._ctx_of.pop(t.value, None)
+            out.append((t.value, st.as_dict()))
+
+    def read_phi(self, ctx):
+        phi = np.zeros(ctx.shapes[-1])
+        self._check(self._L.cvb_batch_read_phi(self._b, ctx._ctx, ptr(phi)))
+        return phi
+
+    def solve(self, ctxs):
+        """Solve every context's resident rhs; returns their stats in order."""
+        n = len(ctxs)
+        arr = (ctypes.c_void_p * n)(*[c._ctx.value for c in ctxs])
+        sts = (_lib.SolveStats * n)()
+        rc = self._L.cvb_batch_solve(self._b, n, arr, sts)
+        out = [s.as_dict() for s in sts]
+        if rc:
+            raise CvbError(rc, self._L.cvb_batch_last_error(self._b).decode())
+        return out
+

@@ -598,6 +598,27 @@ def config1_problem(cells=(256, 128, 128)):
                         velocity="noise", seed=1, name="channel%dx%dx%d" % tuple(cells))
 
 
+CONFIG3_SIZES = ((32, 32, 32), (48, 48, 48), (64, 64, 96), (96, 96, 96), (128, 64, 64))
+
+
+def config3_problems(count=64, seed=3):
+    """Batched uneven solves: sizes drawn uniformly from CONFIG3_SIZES (cells in
+    x, y, z), each a [0,1]^3 box with the box-with-sphere geometry rules
+    (tanh stretching 2.0 in y, sin distortion) and one sphere of radius
+    U[0.1, 0.2] centred in U[0.3, 0.7]^3.  Returns [(problem, rhs seed)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(count):
+        cells = CONFIG3_SIZES[int(rng.integers(len(CONFIG3_SIZES)))]
+        r = float(rng.uniform(0.1, 0.2))
+        c = rng.uniform(0.3, 0.7, size=3)
+        P = make_problem(cells, (1.0, 1.0, 1.0), 2.0, True, (False, False, False),
+                         [(float(c[0]), float(c[1]), float(c[2]), r)],
+                         name="batch%d-%dx%dx%d" % ((q,) + tuple(cells)))
+        out.append((P, int(rng.integers(1 << 30))))
+    return out
+
+
 def noisy_rhs(b, nvert, aj, dt, seed, amp=1e-2):
     """Add seeded uniform noise in [-amp, amp], scaled by 1/dt, on fluid cells, then
     make the result compatible with the Neumann operator."""

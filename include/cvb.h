@@ -145,6 +145,10 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
 /* Device pointers of the context's finest-level rhs and solution ([mz][my][mx] FP64). */
 double *cvb_device_rhs(cvb_ctx *ctx);
 double *cvb_device_phi(cvb_ctx *ctx);
+/* Copy a host rhs into the resident rhs / the resident phi out to the host
+ * ([mz][my][mx] FP64, synchronous). */
+int cvb_set_rhs(cvb_ctx *ctx, const double *b);
+int cvb_get_phi(cvb_ctx *ctx, double *phi);
 /* Solve the context's resident rhs into its resident phi. */
 int cvb_solve_resident(cvb_ctx *ctx, const cvb_solve_opts *opts, cvb_solve_stats *stats);
 /* The context's CUDA stream (cudaStream_t). */
@@ -190,6 +194,47 @@ int cvb_nullspace(cvb_ctx *ctx, int level, double *x);
 #define CVB_NOALLOC_MAX_CELLS (64 * 1024 * 1024)
 int cvb_poisson_rhs_noalloc(const double *d_ucont, const double *d_aj, const double *d_nvert, int mx, int my,
                             int mz, double dt, double st, double *d_b, double *d_compat_sum, void *stream);
+
+/* --- batched and served solves ------------------------------------------ */
+/* A batch runs many independent solves at once, each on its own set-up
+ * context (its hierarchy stays resident there).  The reference has no
+ * counterpart: it solves one block per PoissonSolver_MG call.
+ *
+ * Work proceeds in rounds on the batch's stream.  One round is one FGMRES
+ * iteration of every active solve, and every phase of it (each V-cycle kernel,
+ * each Krylov step) is one grouped kernel launch over a work-list of all the
+ * solves' tiles.  The Krylov scalars (Gram-Schmidt column, Givens rotations,
+ * convergence test) stay on the device; the host reads each solve's state one
+ * round late, so it never stalls the GPU.  Solves may be submitted at any time
+ * and join at the next round (continuous batching); finished ones are handed
+ * back by cvb_batch_poll.  A solve's result does not depend on what else is
+ * in the batch: every reduction has a fixed tree per problem size.
+ *
+ * Batch-wide settings (precision, restart, sweeps, omega) come from the
+ * options given at creation; tolerances are per solve.  Limits: the context's
+ * coarsest level must be solved densely (coarse_dense_max), y-lines of at most
+ * 400 rows, at most 1024 solves in flight. */
+typedef struct cvb_batch cvb_batch;
+int cvb_batch_create(cvb_batch **batch, const cvb_options *opts, const cvb_solve_opts *solve_opts);
+void cvb_batch_destroy(cvb_batch *batch);
+const char *cvb_batch_last_error(const cvb_batch *batch);
+/* Queue a solve of ctx's resident rhs (cvb_device_rhs) into its resident phi.
+ * host_b (optional, [mz][my][mx]) is copied into the resident rhs first; if it
+ * is pinned memory it must stay valid until the solve is polled.  The context
+ * must not be used otherwise until its ticket is polled. */
+int cvb_batch_submit(cvb_batch *batch, cvb_ctx *ctx, const double *host_b, double rtol, double atol, int max_it,
+                     int warm_start, int project_rhs, int *ticket);
+/* Admit queued solves and issue one round; *in_flight = solves not yet polled. */
+int cvb_batch_step(cvb_batch *batch, int *in_flight);
+/* A finished solve: *ticket (-1 if none is ready) and its statistics. */
+int cvb_batch_poll(cvb_batch *batch, int *ticket, cvb_solve_stats *stats);
+/* Copy a finished solve's phi to the host (on the batch's copy stream). */
+int cvb_batch_read_phi(cvb_batch *batch, cvb_ctx *ctx, double *host_phi);
+/* Submit n solves with the batch's options and run them to completion. */
+int cvb_batch_solve(cvb_batch *batch, int n, cvb_ctx *const *ctxs, cvb_solve_stats *stats);
+int cvb_batch_in_flight(const cvb_batch *batch);
+/* Device memory held by a context (its hierarchy, vectors and Krylov basis). */
+int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes);
 
 /* --- measurement ------------------------------------------------------- */
 /* Kernel launches this library has issued in the process (all contexts). */
