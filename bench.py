@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--impl", default="cvb", choices=["cvb", "reference"])
     ap.add_argument("--workload", default="channel", choices=["channel", "box64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-solves measurement")
+    ap.add_argument("--batch-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -271,9 +273,79 @@ def run_cvb(args, ws, rank, local):
         "clocks": clocks,
         "gpu_launches": int(launches),
     }
+    if not args.no_batch:
+        out["batch"] = bench_batch(args, ws, local)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(P, b)
     return out
+
+
+def bench_batch(args, ws, local):
+    """64 uneven problems solved together by the batch engine (grouped launches
+    over all problems' tiles), mixed and FP64, against the same 64 solved one
+    after another by the single-solve path."""
+    import torch
+
+    from curvib_old_gb300 import _lib
+    from curvib_old_gb300 import workload as W
+    from curvib_old_gb300.solver import PoissonContext, SolveBatch
+    rtol = 1e-8
+    items = W.config3_problems()
+    ctxs, bs, unknowns = [], [], 0
+    for P, seed in items:
+        c = PoissonContext(local).setup(P)
+        uc, _, _ = c.volume_flux_rev(P.ucont, 0.0, 1)
+        b, _ = c.poisson_rhs(uc, DT, ST)
+        b = W.noisy_rhs(b, P.nvert, P.metrics[-1]["Aj"], DT, seed=seed)
+        c.set_rhs(b)
+        ctxs.append(c)
+        bs.append(b)
+        unknowns += P.unknowns
+    dev = torch.device("cuda", local)
+
+    def run(precision, steps):
+        B = SolveBatch(local, precision=precision, rtol=rtol, max_it=200)
+        try:
+            sts = B.solve(ctxs)  # warm-up
+            barrier(ws)
+            torch.cuda.synchronize()
+            l0 = _lib.lib().cvb_kernel_launches()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                sts = B.solve(ctxs)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            launches = (_lib.lib().cvb_kernel_launches() - l0) / steps
+        finally:
+            B.close()
+        wall = max_over_ranks(ws, wall, dev)
+        its = [s["iterations"] for s in sts]
+        return {"solves_per_s": ws * len(ctxs) * steps / wall, "ms_per_batch": wall * 1e3 / steps,
+                "iterations_mean": float(np.mean(its)), "iterations_max": int(max(its)),
+                "rel_residual_max": float(max(s["rel_residual"] for s in sts)),
+                "gpu_launches_per_batch": int(launches)}
+
+    mixed = run(_lib.MIXED, args.batch_steps)
+    fp64 = run(_lib.FP64, args.batch_steps)
+    # the same 64 solves, one after another, through the single-solve path
+    for c in ctxs[:2]:
+        c.solve_resident(precision=_lib.MIXED, rtol=rtol, max_it=200)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c in ctxs:
+        c.solve_resident(precision=_lib.MIXED, rtol=rtol, max_it=200)
+    torch.cuda.synchronize()
+    seq = max_over_ranks(ws, time.perf_counter() - t0, dev)
+    dev_bytes = sum(c.device_bytes() for c in ctxs)
+    for c in ctxs:
+        c.close()
+    return {"workload": "64 uneven problems, sizes uniform over 32^3, 48^3, 64x64x96, 96^3, 128x64x64 cells; "
+                        "[0,1]^3 boxes, tanh 2.0 in y, distorted, one seeded sphere each (r 0.1-0.2), "
+                        "noisy-divergence RHS (config 3)",
+            "unknowns": int(unknowns), "rtol": rtol, "mixed": mixed, "fp64": fp64,
+            "mixed_over_fp64": mixed["solves_per_s"] / fp64["solves_per_s"],
+            "sequential_single_solves_per_s": ws * len(ctxs) / seq,
+            "device_bytes": int(dev_bytes)}
 
 
 def cpu_levels(P):

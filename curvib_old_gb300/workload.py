@@ -601,20 +601,39 @@ def config1_problem(cells=(256, 128, 128)):
 CONFIG3_SIZES = ((32, 32, 32), (48, 48, 48), (64, 64, 96), (96, 96, 96), (128, 64, 64))
 
 
+def box_geometry(cells, nlevels=None):
+    """Metrics of every level and the Taylor-Green fluxes of a [0,1]^3 box with
+    the box-with-sphere geometry rules (tanh stretching 2.0 in y, sin
+    distortion, walls everywhere); shared by every problem of that size."""
+    per = (False, False, False)
+    if nlevels is None:
+        nlevels = auto_levels(cells, per)
+    nodes = box_nodes(cells, (1.0, 1.0, 1.0), 2.0, True)
+    coords = level_coordinates(nodes, nlevels, (0, 0, 0))
+    mets = [form_metrics(c, per) for c in coords]
+    uc = ucont_from_velocity(mets[-1], taylor_green, per)
+    return mets, uc
+
+
 def config3_problems(count=64, seed=3):
     """Batched uneven solves: sizes drawn uniformly from CONFIG3_SIZES (cells in
     x, y, z), each a [0,1]^3 box with the box-with-sphere geometry rules
     (tanh stretching 2.0 in y, sin distortion) and one sphere of radius
-    U[0.1, 0.2] centred in U[0.3, 0.7]^3.  Returns [(problem, rhs seed)]."""
+    U[0.1, 0.2] centred in U[0.3, 0.7]^3.  Returns [(problem, rhs seed)]; the
+    metrics of equal sizes are shared."""
     rng = np.random.default_rng(seed)
+    geo = {}
     out = []
     for q in range(count):
         cells = CONFIG3_SIZES[int(rng.integers(len(CONFIG3_SIZES)))]
         r = float(rng.uniform(0.1, 0.2))
         c = rng.uniform(0.3, 0.7, size=3)
-        P = make_problem(cells, (1.0, 1.0, 1.0), 2.0, True, (False, False, False),
-                         [(float(c[0]), float(c[1]), float(c[2]), r)],
-                         name="batch%d-%dx%dx%d" % ((q,) + tuple(cells)))
+        if cells not in geo:
+            geo[cells] = box_geometry(cells)
+        mets, uc = geo[cells]
+        nv = sphere_nvert(mets[-1]["Cent"], [(float(c[0]), float(c[1]), float(c[2]), r)])
+        P = Problem(mets, nv, uc, [1] * 6, (0, 0, 0), (False, False, False),
+                    "batch%d-%dx%dx%d" % ((q,) + tuple(cells)))
         out.append((P, int(rng.integers(1 << 30))))
     return out
 
