@@ -90,7 +90,10 @@ EXPORTS = {
     "cvb_batch_solve": ([_P, _I, _P, _P], _I),
     "cvb_batch_in_flight": ([_P], _I),
     "cvb_device_bytes": ([_P, _P], _I),
+    "cvb_geometry_bytes": ([_P, _P, _P], _I),
+    "cvb_setup_like": ([_P, _P, _P], _I),
     "cvb_set_rhs": ([_P, _P], _I),
+    "cvb_set_phi": ([_P, _P], _I),
     "cvb_get_phi": ([_P, _P], _I),
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3}

@@ -9,7 +9,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "cvb_ctx.h"
@@ -50,8 +53,54 @@ static int fail(cvb_ctx *c, int code, const char *fmt, ...) {
     if (s_ != CVB_OK) return s_;   \
   } while (0)
 
+// Per-problem device memory comes from the device's stream-ordered pool, kept
+// cached (release threshold at its maximum, a setting of this process's pool
+// only): evicting one problem and setting up the next reuse memory without a
+// device-wide synchronisation.
+static void ensure_pool(int dev) {
+  static std::mutex mu;
+  static bool done[64] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev < 0 || dev >= 64 || done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
+}
+
 template <typename T>
 static int dalloc(cvb_ctx *ctx, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMallocAsync((void **)p, sizeof(T) * count, ctx->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, CVB_OOM, "device allocation of %zu bytes failed: %s", sizeof(T) * count,
+                cudaGetErrorString(e));
+  }
+  ctx->allocs.push_back((void *)*p);
+  ctx->alloc_bytes.push_back(sizeof(T) * count);
+  ctx->device_bytes += sizeof(T) * count;
+  return CVB_OK;
+}
+
+// Returns one per-problem allocation to the pool (in stream order).
+static void dfree(cvb_ctx *ctx, void *p) {
+  for (size_t q = 0; q < ctx->allocs.size(); q++)
+    if (ctx->allocs[q] == p) {
+      ctx->device_bytes -= ctx->alloc_bytes[q];
+      ctx->allocs.erase(ctx->allocs.begin() + q);
+      ctx->alloc_bytes.erase(ctx->alloc_bytes.begin() + q);
+      break;
+    }
+  cudaFreeAsync(p, ctx->stream);
+}
+
+// Geometry arrays: plain allocations owned by the shared Geometry.
+template <typename T>
+static int galloc(cvb_ctx *ctx, Geometry &G, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
   cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
@@ -59,20 +108,33 @@ static int dalloc(cvb_ctx *ctx, T **p, size_t count) {
     cudaGetLastError();
     return fail(ctx, CVB_OOM, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
   }
-  ctx->allocs.push_back((void *)*p);
-  ctx->device_bytes += sizeof(T) * count;
+  G.allocs.push_back((void *)*p);
+  G.bytes += sizeof(T) * count;
   return CVB_OK;
 }
 
 static void free_all(cvb_ctx *ctx) {
+  for (void *p : ctx->allocs) cudaFreeAsync(p, ctx->stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (void *p : ctx->allocs) cudaFree(p);
   ctx->allocs.clear();
+  ctx->alloc_bytes.clear();
   ctx->device_bytes = 0;
   ctx->L.clear();
   ctx->H.clear();
+  ctx->geo.reset();
   ctx->fm.clear();
   ctx->iaj.clear(); ctx->jaj.clear(); ctx->kaj.clear(); ctx->aj64.clear();
+  ctx->area3 = nullptr;
+  ctx->nvert_tmp = nullptr;
+  ctx->Minv = nullptr;
+  ctx->cidx = nullptr;
+  ctx->b = ctx->x = ctx->w = ctx->r = nullptr;
+  for (int q = 0; q <= kMaxRestart; q++) ctx->V[q] = nullptr;
+  for (int q = 0; q < kMaxRestart; q++) { ctx->Z64[q] = nullptr; ctx->Z32[q] = nullptr; }
+  ctx->b32 = nullptr;
+  ctx->dV = nullptr; ctx->dZ64 = nullptr; ctx->dZ32 = nullptr;
+  ctx->partial = ctx->sums = ctx->hdev = nullptr;
+  ctx->uc_dev = ctx->p_dev = nullptr;
   ctx->ready = false;
 }
 
@@ -87,10 +149,11 @@ static void extract_box(const cvb_level_desc &d, const double *src, int dof, std
     }
 }
 
-static int upload_box(cvb_ctx *ctx, const cvb_level_desc &d, const double *src, int dof, double **dst) {
+static int upload_box(cvb_ctx *ctx, Geometry &G, const cvb_level_desc &d, const double *src, int dof,
+                      double **dst) {
   std::vector<double> h;
   extract_box(d, src, dof, h);
-  TRY(dalloc(ctx, dst, h.size()));
+  TRY(galloc(ctx, G, dst, h.size()));
   CK(cudaMemcpyAsync(*dst, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return CVB_OK;
@@ -149,6 +212,9 @@ static bool dense_inverse(std::vector<double> &A, int n, std::vector<double> &In
 // v_r the indicator of fluid region r and u_r = s v_r.  A's left null vector on
 // region r is 1/aj there, which is not orthogonal to u_r, so M is invertible; for a
 // compatible right-hand side M^-1 b solves A e = b with zero region sums of e.
+// The ring and the blocked cells are identity rows, so only the fluid block is
+// inverted (e = r elsewhere) -- unless a fluid row couples to a non-fluid cell,
+// in which case the whole box is.  cidx lists the inverted cells first.
 static int build_coarse(cvb_ctx *ctx, const cvb_solve_opts *opt) {
   LevelDev &C = ctx->L[0];
   size_t n = C.g.n();
@@ -160,51 +226,73 @@ static int build_coarse(cvb_ctx *ctx, const cvb_solve_opts *opt) {
   CK(cudaMemcpyAsync(w.data(), C.w64, sizeof(double) * n * NSLOT, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(nv.data(), C.nvert, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  std::vector<double> A(n * n, 0.0);
   const Geom &g = C.g;
-  double diag_sum = 0.0;
-  int nfl = 0;
-  std::vector<int> region(n, -1);
+  std::vector<int> region(n, -1), cols(n * NSLOT);
+  std::vector<char> fluid(n, 0);
   for (int k = 0; k < g.mz; k++)
     for (int j = 0; j < g.my; j++)
       for (int i = 0; i < g.mx; i++) {
         size_t p = g.id(i, j, k);
         bool interior = i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2;
-        if (!interior || nv[p] > 0.1) {
-          A[p * n + p] = 1.0;
-          continue;
-        }
+        if (!interior || nv[p] > 0.1) continue;
+        fluid[p] = 1;
         int iu = g.iu(i), id = g.id_(i), ju = g.ju(j), jd = g.jd(j), ku = g.ku(k), kd = g.kd(k);
         size_t c[NSLOT] = {g.id(i, j, k), g.id(iu, j, k), g.id(id, j, k), g.id(i, ju, k), g.id(i, jd, k),
                            g.id(i, j, ku), g.id(i, j, kd), g.id(iu, ju, k), g.id(iu, jd, k), g.id(id, ju, k),
                            g.id(id, jd, k), g.id(i, ju, ku), g.id(i, ju, kd), g.id(i, jd, ku), g.id(i, jd, kd),
                            g.id(iu, j, ku), g.id(iu, j, kd), g.id(id, j, ku), g.id(id, j, kd)};
-        for (int m = 0; m < NSLOT; m++) A[p * n + c[m]] += w[(size_t)m * n + p];
-        diag_sum += std::fabs(A[p * n + p]);
-        nfl++;
+        for (int m = 0; m < NSLOT; m++) cols[p * NSLOT + m] = (int)c[m];
         int reg = 0;
         if (ctx->multinullspace && k >= ctx->kske[2 * (j * g.mx + i)]) reg = 1;
         region[p] = reg;
       }
+  bool compact = true;
+  for (size_t p = 0; p < n && compact; p++)
+    if (fluid[p])
+      for (int m = 0; m < NSLOT; m++)
+        if (w[(size_t)m * n + p] != 0.0 && !fluid[cols[p * NSLOT + m]]) { compact = false; break; }
+  // the inverted cells first (fluid, or every cell), then the identity ones
+  std::vector<int> idx, pos(n, -1);
+  for (size_t p = 0; p < n; p++)
+    if (!compact || fluid[p]) { pos[p] = (int)idx.size(); idx.push_back((int)p); }
+  const int m = (int)idx.size();
+  for (size_t p = 0; p < n; p++)
+    if (pos[p] < 0) idx.push_back((int)p);
+  std::vector<double> A((size_t)m * m, 0.0);
+  double diag_sum = 0.0;
+  int nfl = 0;
+  for (int r = 0; r < m; r++) {
+    size_t p = (size_t)idx[r];
+    if (!fluid[p]) { A[(size_t)r * m + r] = 1.0; continue; }
+    for (int q = 0; q < NSLOT; q++) A[(size_t)r * m + pos[cols[p * NSLOT + q]]] += w[(size_t)q * n + p];
+    diag_sum += std::fabs(A[(size_t)r * m + r]);
+    nfl++;
+  }
   if (nfl > 0) {
     double s = diag_sum / nfl;
     for (int reg = 0; reg < 2; reg++) {
       int cnt = 0;
-      for (size_t p = 0; p < n; p++) cnt += region[p] == reg;
+      for (int r = 0; r < m; r++) cnt += region[idx[r]] == reg;
       if (!cnt) continue;
       double sv = s / cnt;
-      for (size_t p = 0; p < n; p++) {
-        if (region[p] != reg) continue;
-        for (size_t q = 0; q < n; q++)
-          if (region[q] == reg) A[p * n + q] += sv;
+      for (int r = 0; r < m; r++) {
+        if (region[idx[r]] != reg) continue;
+        for (int q = 0; q < m; q++)
+          if (region[idx[q]] == reg) A[(size_t)r * m + q] += sv;
       }
     }
   }
   std::vector<double> Inv;
-  if (!dense_inverse(A, (int)n, Inv)) return fail(ctx, CVB_BAD_INPUT, "coarsest operator is singular after regularisation");
-  if (!ctx->Minv) TRY(dalloc(ctx, &ctx->Minv, n * n));
-  CK(cudaMemcpyAsync(ctx->Minv, Inv.data(), sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (m > 0 && !dense_inverse(A, m, Inv)) return fail(ctx, CVB_BAD_INPUT, "coarsest operator is singular after regularisation");
+  if (ctx->Minv) dfree(ctx, ctx->Minv);
+  if (ctx->cidx) dfree(ctx, ctx->cidx);
+  TRY(dalloc(ctx, &ctx->Minv, std::max((size_t)m * m, (size_t)1)));
+  TRY(dalloc(ctx, &ctx->cidx, n));
+  if (m > 0) CK(cudaMemcpyAsync(ctx->Minv, Inv.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cidx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  C.cidx = ctx->cidx;
+  C.cm = m;
   return CVB_OK;
 }
 
@@ -257,11 +345,9 @@ static int build_operators(cvb_ctx *ctx) {
     launch_to_f32(ctx->aj64[l], lv.ajf32, n, ctx->stream);
     CKL();
   }
-  CK(cudaStreamSynchronize(ctx->stream));
   // g9 is a set-up temporary; return it to the pool
-  auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void *)g9);
-  if (it != ctx->allocs.end()) ctx->allocs.erase(it);
-  cudaFree(g9);
+  dfree(ctx, g9);
+  CK(cudaStreamSynchronize(ctx->stream));
   return CVB_OK;
 }
 
@@ -269,11 +355,38 @@ static int build_operators(cvb_ctx *ctx) {
 // and precision (CUDA events on the context stream, after one warm-up launch)
 // and keeps the faster; the choice depends on the level's size and on how its
 // lines fill the machine.
+// The sweep variant depends on a level's shape only, so a choice is measured
+// once per shape in the process and reused: contexts set up later (or while
+// other work loads the GPU) take the same variant, and so the same rounding.
+namespace {
+struct ShapeKey {
+  int mx, my, mz, px, py, pz;
+  bool operator<(const ShapeKey &o) const {
+    return std::tie(mx, my, mz, px, py, pz) < std::tie(o.mx, o.my, o.mz, o.px, o.py, o.pz);
+  }
+};
+std::mutex g_tune_mu;
+std::map<ShapeKey, cvb_ctx::Tune> g_tune_cache;
+}  // namespace
+
 static int autotune_sweeps(cvb_ctx *ctx) {
   ctx->tune.clear();
   for (int l = 0; l < ctx->nlevels; l++) {
     LevelDev &L = ctx->L[l];
     size_t n = L.g.n();
+    const ShapeKey key{L.g.mx, L.g.my, L.g.mz, L.g.px, L.g.py, L.g.pz};
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto it = g_tune_cache.find(key);
+      if (it != g_tune_cache.end()) {
+        cvb_ctx::Tune t = it->second;
+        t.level = l;
+        L.sweep32 = t.us32[1] < t.us32[0] ? 1 : 0;
+        L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
+        ctx->tune.push_back(t);
+        continue;
+      }
+    }
     cvb_ctx::Tune t;
     t.level = l;
     t.cells = n;
@@ -300,6 +413,8 @@ static int autotune_sweeps(cvb_ctx *ctx) {
     L.sweep32 = t.us32[1] < t.us32[0] ? 1 : 0;
     L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
     ctx->tune.push_back(t);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache.emplace(key, t);
   }
   return CVB_OK;
 }
@@ -373,7 +488,7 @@ static void coarse_solve(cvb_ctx *ctx, const T *b, T *x, const cvb_solve_opts *o
 template <>
 void coarse_solve<float>(cvb_ctx *ctx, const float *b, float *x, const cvb_solve_opts *o) {
   LevelDev &C = ctx->L[0];
-  if (ctx->coarse_dense) { launch_dense_apply_f32(ctx->Minv, ctx->ncoarse, b, x, ctx->stream); return; }
+  if (ctx->coarse_dense) { launch_dense_apply_f32(C, ctx->Minv, b, x, ctx->stream); return; }
   float *a = x, *a2 = vptr<float>(C, 2);
   smooth<float>(C, b, a, a2, (float)o->omega, 30, true, ctx->stream);
   if (a != x) cudaMemcpyAsync(x, a, sizeof(float) * C.g.n(), cudaMemcpyDeviceToDevice, ctx->stream);
@@ -381,7 +496,7 @@ void coarse_solve<float>(cvb_ctx *ctx, const float *b, float *x, const cvb_solve
 template <>
 void coarse_solve<double>(cvb_ctx *ctx, const double *b, double *x, const cvb_solve_opts *o) {
   LevelDev &C = ctx->L[0];
-  if (ctx->coarse_dense) { launch_dense_apply(ctx->Minv, ctx->ncoarse, b, x, ctx->stream); return; }
+  if (ctx->coarse_dense) { launch_dense_apply(C, ctx->Minv, b, x, ctx->stream); return; }
   double *a = x, *a2 = vptr<double>(C, 2);
   smooth<double>(C, b, a, a2, o->omega, 30, true, ctx->stream);
   if (a != x) cudaMemcpyAsync(x, a, sizeof(double) * C.g.n(), cudaMemcpyDeviceToDevice, ctx->stream);
@@ -605,6 +720,60 @@ static int solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats
   return rc;
 }
 
+// Per-problem part of a set-up on the context's geometry: level arrays, the
+// finest level's nvert (owned box), operators, smoother factors, coarsest solver.
+static int setup_problem(cvb_ctx *ctx, const std::vector<double> &nvert_box) {
+  const int nlevels = ctx->nlevels;
+  Geometry &G = *ctx->geo;
+  ctx->fm = G.fm;
+  ctx->iaj = G.iaj; ctx->jaj = G.jaj; ctx->kaj = G.kaj; ctx->aj64 = G.aj64;
+  ctx->area3 = G.area3;
+  ctx->L.assign(nlevels, LevelDev());
+  size_t nmax = 0;
+  for (int l = 0; l < nlevels; l++) {
+    const cvb_level_desc &d = ctx->H[l].d;
+    LevelDev &L = ctx->L[l];
+    L.g.mx = d.mx; L.g.my = d.my; L.g.mz = d.mz;
+    L.g.px = d.bctype[0] == 7; L.g.py = d.bctype[2] == 7; L.g.pz = d.bctype[4] == 7;
+    L.isc = d.isc; L.jsc = d.jsc; L.ksc = d.ksc;
+    size_t n = L.g.n();
+    nmax = std::max(nmax, n);
+    TRY(dalloc(ctx, &L.nvert, n));
+    TRY(dalloc(ctx, &L.code, n));
+    TRY(dalloc(ctx, &L.w64, (size_t)NSLOT * n));
+    TRY(dalloc(ctx, &L.gf32, 9 * n));
+    TRY(dalloc(ctx, &L.ajf32, n));
+    TRY(dalloc(ctx, &L.line32, 3 * n));
+    TRY(dalloc(ctx, &L.line64, 3 * n));
+    TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, 2 * n));
+    TRY(dalloc(ctx, &L.r32, n)); TRY(dalloc(ctx, &L.e32, n)); TRY(dalloc(ctx, &L.t32, 2 * n));
+  }
+  TRY(dalloc(ctx, &ctx->nvert_tmp, nmax));
+  LevelDev &F = ctx->L[nlevels - 1];
+  size_t n = F.g.n();
+  if (nvert_box.size() != n) return fail(ctx, CVB_BAD_INPUT, "nvert has %zu cells, the finest box %zu", nvert_box.size(), n);
+  CK(cudaMemcpyAsync(F.nvert, nvert_box.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  TRY(dalloc(ctx, &ctx->b, n)); TRY(dalloc(ctx, &ctx->x, n));
+  TRY(dalloc(ctx, &ctx->w, n)); TRY(dalloc(ctx, &ctx->r, n));
+  TRY(dalloc(ctx, &ctx->b32, n));
+  TRY(dalloc(ctx, &ctx->uc_dev, 3 * n)); TRY(dalloc(ctx, &ctx->p_dev, n));
+  TRY(dalloc(ctx, &ctx->dV, kMaxRestart + 2));
+  TRY(dalloc(ctx, &ctx->dZ64, kMaxRestart));
+  TRY(dalloc(ctx, &ctx->dZ32, kMaxRestart));
+  int nb = reduce_blocks();
+  TRY(dalloc(ctx, &ctx->partial, (size_t)nb * (kMaxRestart + 2)));
+  TRY(dalloc(ctx, &ctx->sums, kMaxRestart + 2));
+  TRY(dalloc(ctx, &ctx->hdev, kMaxRestart + 2));
+  TRY(build_operators(ctx));
+  TRY(autotune_sweeps(ctx));
+  cvb_solve_opts def;
+  cvb_solve_opts_default(&def);
+  TRY(build_coarse(ctx, &def));
+  ctx->ready = true;
+  return CVB_OK;
+}
+
 // ------------------------------------------------------------------ C ABI
 extern "C" {
 
@@ -660,6 +829,7 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, con
   if (!ctx) return CVB_BAD_INPUT;
   if (nlevels < 1 || nlevels > 16 || !lv || !nvert_finest) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
   CK(cudaSetDevice(ctx->device));
+  ensure_pool(ctx->device);
   free_all(ctx);
   for (int l = 0; l < nlevels; l++) TRY(check_desc(ctx, lv[l], l, l == nlevels - 1));
   for (int l = 0; l + 1 < nlevels; l++) {
@@ -670,74 +840,58 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, con
                   c.mx, c.my, c.mz, l + 1, ex, ey, ez);
   }
   ctx->nlevels = nlevels;
-  ctx->L.assign(nlevels, LevelDev());
   ctx->H.resize(nlevels);
-  ctx->fm.assign(nlevels, std::vector<double *>(9, nullptr));
-  ctx->iaj.assign(nlevels, nullptr); ctx->jaj.assign(nlevels, nullptr);
-  ctx->kaj.assign(nlevels, nullptr); ctx->aj64.assign(nlevels, nullptr);
-  size_t nmax = 0;
+  for (int l = 0; l < nlevels; l++) ctx->H[l].d = lv[l];
+  // the grid's metrics: uploaded once, owned by a Geometry other contexts may share
+  auto G = std::make_shared<Geometry>();
+  G->device = ctx->device;
+  G->fm.assign(nlevels, std::vector<double *>(9, nullptr));
+  G->iaj.assign(nlevels, nullptr); G->jaj.assign(nlevels, nullptr);
+  G->kaj.assign(nlevels, nullptr); G->aj64.assign(nlevels, nullptr);
   for (int l = 0; l < nlevels; l++) {
     const cvb_level_desc &d = lv[l];
-    ctx->H[l].d = d;
-    LevelDev &L = ctx->L[l];
-    L.g.mx = d.mx; L.g.my = d.my; L.g.mz = d.mz;
-    L.g.px = d.bctype[0] == 7; L.g.py = d.bctype[2] == 7; L.g.pz = d.bctype[4] == 7;
-    L.isc = d.isc; L.jsc = d.jsc; L.ksc = d.ksc;
-    size_t n = L.g.n();
-    nmax = std::max(nmax, n);
     const double *srcs[9] = {d.icsi, d.ieta, d.izet, d.jcsi, d.jeta, d.jzet, d.kcsi, d.keta, d.kzet};
-    for (int q = 0; q < 9; q++) TRY(upload_box(ctx, d, srcs[q], 3, &ctx->fm[l][q]));
-    TRY(upload_box(ctx, d, d.iaj, 1, &ctx->iaj[l]));
-    TRY(upload_box(ctx, d, d.jaj, 1, &ctx->jaj[l]));
-    TRY(upload_box(ctx, d, d.kaj, 1, &ctx->kaj[l]));
-    TRY(upload_box(ctx, d, d.aj, 1, &ctx->aj64[l]));
-    TRY(dalloc(ctx, &L.nvert, n));
-    TRY(dalloc(ctx, &L.code, n));
-    TRY(dalloc(ctx, &L.w64, (size_t)NSLOT * n));
-    TRY(dalloc(ctx, &L.gf32, 9 * n));
-    TRY(dalloc(ctx, &L.ajf32, n));
-    TRY(dalloc(ctx, &L.line32, 3 * n));
-    TRY(dalloc(ctx, &L.line64, 3 * n));
-    TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, 2 * n));
-    TRY(dalloc(ctx, &L.r32, n)); TRY(dalloc(ctx, &L.e32, n)); TRY(dalloc(ctx, &L.t32, 2 * n));
+    for (int q = 0; q < 9; q++) TRY(upload_box(ctx, *G, d, srcs[q], 3, &G->fm[l][q]));
+    TRY(upload_box(ctx, *G, d, d.iaj, 1, &G->iaj[l]));
+    TRY(upload_box(ctx, *G, d, d.jaj, 1, &G->jaj[l]));
+    TRY(upload_box(ctx, *G, d, d.kaj, 1, &G->kaj[l]));
+    TRY(upload_box(ctx, *G, d, d.aj, 1, &G->aj64[l]));
   }
-  TRY(dalloc(ctx, &ctx->nvert_tmp, nmax));
-  // finest level: nvert, face areas, solver workspace
-  const cvb_level_desc &df = lv[nlevels - 1];
-  LevelDev &F = ctx->L[nlevels - 1];
-  size_t n = F.g.n();
   {
-    std::vector<double> h;
-    extract_box(df, nvert_finest, 1, h);
-    CK(cudaMemcpyAsync(F.nvert, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    const cvb_level_desc &df = lv[nlevels - 1];
+    size_t n = (size_t)df.mx * df.my * df.mz;
     std::vector<double> c1, c2, c3, a3;
     extract_box(df, df.csi, 3, c1);
     extract_box(df, df.eta, 3, c2);
     extract_box(df, df.zet, 3, c3);
     face_areas(c1, c2, c3, a3);
-    TRY(dalloc(ctx, &ctx->area3, 3 * n));
-    CK(cudaMemcpyAsync(ctx->area3, a3.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    TRY(galloc(ctx, *G, &G->area3, 3 * n));
+    CK(cudaMemcpyAsync(G->area3, a3.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
-  TRY(dalloc(ctx, &ctx->b, n)); TRY(dalloc(ctx, &ctx->x, n));
-  TRY(dalloc(ctx, &ctx->w, n)); TRY(dalloc(ctx, &ctx->r, n));
-  TRY(dalloc(ctx, &ctx->b32, n));
-  TRY(dalloc(ctx, &ctx->uc_dev, 3 * n)); TRY(dalloc(ctx, &ctx->p_dev, n));
-  for (int q = 0; q <= kMaxRestart; q++) ctx->V[q] = nullptr;
-  TRY(dalloc(ctx, &ctx->dV, kMaxRestart + 2));
-  TRY(dalloc(ctx, &ctx->dZ64, kMaxRestart));
-  TRY(dalloc(ctx, &ctx->dZ32, kMaxRestart));
-  int nb = reduce_blocks();
-  TRY(dalloc(ctx, &ctx->partial, (size_t)nb * (kMaxRestart + 2)));
-  TRY(dalloc(ctx, &ctx->sums, kMaxRestart + 2));
-  TRY(dalloc(ctx, &ctx->hdev, kMaxRestart + 2));
-  TRY(build_operators(ctx));
-  TRY(autotune_sweeps(ctx));
-  cvb_solve_opts def;
-  cvb_solve_opts_default(&def);
-  TRY(build_coarse(ctx, &def));
-  ctx->ready = true;
-  return CVB_OK;
+  ctx->geo = G;
+  std::vector<double> h;
+  extract_box(lv[nlevels - 1], nvert_finest, 1, h);
+  return setup_problem(ctx, h);
+}
+
+int cvb_setup_like(cvb_ctx *ctx, const cvb_ctx *donor, const double *nvert_finest) {
+  if (!ctx || !donor || ctx == donor) return CVB_BAD_INPUT;
+  if (!donor->ready || !donor->geo) return fail(ctx, CVB_NOT_SETUP, "the donor context is not set up");
+  if (!nvert_finest) return fail(ctx, CVB_BAD_INPUT, "nvert is NULL");
+  if (donor->device != ctx->device)
+    return fail(ctx, CVB_BAD_INPUT, "donor is on device %d, context on %d", donor->device, ctx->device);
+  CK(cudaSetDevice(ctx->device));
+  ensure_pool(ctx->device);
+  std::shared_ptr<Geometry> G = donor->geo;  // held before free_all in case the donor is reset meanwhile
+  std::vector<LevelHost> H = donor->H;
+  free_all(ctx);
+  ctx->nlevels = (int)H.size();
+  ctx->H = H;
+  ctx->geo = G;
+  std::vector<double> h;
+  extract_box(ctx->H[ctx->nlevels - 1].d, nvert_finest, 1, h);
+  return setup_problem(ctx, h);
 }
 
 }  // extern "C"
@@ -979,6 +1133,14 @@ int cvb_set_rhs(cvb_ctx *ctx, const double *b) {
   return CVB_OK;
 }
 
+int cvb_set_phi(cvb_ctx *ctx, const double *phi) {
+  if (!ctx || !phi) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  CK(cudaMemcpyAsync(ctx->x, phi, sizeof(double) * fine_n(ctx), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
 int cvb_get_phi(cvb_ctx *ctx, double *phi) {
   if (!ctx || !phi) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
@@ -990,6 +1152,13 @@ int cvb_get_phi(cvb_ctx *ctx, double *phi) {
 int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes) {
   if (!ctx || !bytes) return CVB_BAD_INPUT;
   *bytes = (unsigned long long)ctx->device_bytes;
+  return CVB_OK;
+}
+
+int cvb_geometry_bytes(const cvb_ctx *ctx, unsigned long long *bytes, unsigned long long *id) {
+  if (!ctx || !bytes) return CVB_BAD_INPUT;
+  *bytes = ctx->geo ? (unsigned long long)ctx->geo->bytes : 0ull;
+  if (id) *id = (unsigned long long)(uintptr_t)ctx->geo.get();
   return CVB_OK;
 }
 

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,23 @@ struct LevelHost {
   cvb_level_desc d;  // shapes / flags only (pointers are not kept)
 };
 
+// The grid's resident metrics, shared by every context built on the same grid
+// (cvb_setup_like): problems that differ only in their immersed bodies keep
+// one copy.  Freed with its last context.
+struct Geometry {
+  int device = 0;
+  std::vector<void *> allocs;
+  size_t bytes = 0;
+  std::vector<std::vector<double *>> fm;  // [level][9] raw face metrics (Cmpnts)
+  std::vector<double *> iaj, jaj, kaj, aj64;
+  double *area3 = nullptr;                // finest: |csi|, |eta|, |zet| per cell ([3][N])
+  ~Geometry() {
+    if (allocs.empty()) return;
+    cudaSetDevice(device);
+    for (void *p : allocs) cudaFree(p);
+  }
+};
+
 }  // namespace cvb
 
 struct cvb_ctx {
@@ -25,15 +43,18 @@ struct cvb_ctx {
   bool own_stream = false;
   std::string err;
   std::vector<void *> allocs;
+  std::vector<size_t> alloc_bytes;
   size_t device_bytes = 0;  // sum of this context's device allocations
 
   int nlevels = 0;
   std::vector<cvb::LevelDev> L;       // 0 = coarsest
   std::vector<cvb::LevelHost> H;
-  // per-level raw face metrics (kept for the finest level: Projection reads them)
+  // the grid's metrics (shared) and aliases of its arrays
+  std::shared_ptr<cvb::Geometry> geo;
   std::vector<std::vector<double *>> fm;  // [level][9] Cmpnts arrays
   std::vector<double *> iaj, jaj, kaj, aj64;
   double *area3 = nullptr;       // finest: |csi|,|eta|,|zet| per cell ([3][N])
+  int *cidx = nullptr;           // coarsest level: fluid cells first, then the rest
   double *nvert_tmp = nullptr;
   // coarsest-level solver
   double *Minv = nullptr;

@@ -61,6 +61,10 @@ struct LevelDev {
   double *r64, *e64, *t64;  // FP64 V-cycle vectors
   float *r32, *e32, *t32;   // FP32 V-cycle vectors
   int sweep32, sweep64;     // line-sweep variant chosen at set-up: 0 fused, 1 split
+  // coarsest level only: the densely inverted cells (first cm of cidx) and the
+  // identity ones (the rest of cidx)
+  const int *cidx;
+  int cm;
   // When set, every kernel launched for this level returns at once while *gate
   // is non-zero: an FGMRES iteration issued ahead of the host's convergence
   // check turns into no-ops once the previous iteration has converged.
@@ -125,9 +129,10 @@ void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double
                                 double *partial, cudaStream_t s);
 void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
                            cudaStream_t s);
-void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s,
+// coarsest solve e = M^-1 r on C.cidx[0..C.cm), e = r on the other cells
+void launch_dense_apply(const LevelDev &C, const double *Minv, const double *r, double *e, cudaStream_t s,
                         const int *gate = nullptr);
-void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s,
+void launch_dense_apply_f32(const LevelDev &C, const double *Minv, const float *r, float *e, cudaStream_t s,
                             const int *gate = nullptr);
 
 // projection-path kernels (FP64)

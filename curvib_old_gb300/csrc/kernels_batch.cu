@@ -85,22 +85,30 @@ __global__ void __launch_bounds__(256, 2) kg_line_solve(const __grid_constant__ 
   int lb = blockIdx.x - K.block0;
   line_solve_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw);
 }
-// e = Minv r, one warp per row (8 rows per block)
+// e = Minv r on the coarsest level's inverted cells, e = r on the others; one
+// warp per row (8 rows per block)
+template <typename T>
+__device__ __forceinline__ void dense_rows_g(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
+                                             const T *__restrict__ r, T *__restrict__ e, int row) {
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  if (row >= m) {
+    if (lane == 0) e[idx[row]] = r[idx[row]];
+    return;
+  }
+  double s = 0.0;
+  for (int c = lane; c < m; c += 32) s = fma(M[(size_t)row * m + c], (double)r[idx[c]], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) e[idx[row]] = (T)s;
+}
 template <typename T>
 __global__ void kg_dense(const __grid_constant__ TaskList tl) {
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
-  const int n = K.p0;
-  const double *M = (const double *)K.b;
-  const T *r = (const T *)K.a;
-  T *e = (T *)K.c;
-  int row = (blockIdx.x - K.block0) * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (row >= n) return;
-  double s = 0.0;
-  for (int c = lane; c < n; c += 32) s = fma(M[(size_t)row * n + c], (double)r[c], s);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) e[row] = (T)s;
+  const LevelDev &C = *K.L;
+  const int row = (blockIdx.x - K.block0) * 8 + (threadIdx.x >> 5);
+  dense_rows_g<T>((const double *)K.b, C.cidx, C.cm, K.p0, (const T *)K.a, (T *)K.c, row);
 }
 template <typename TS, typename TD>
 __global__ void kg_elem(const __grid_constant__ TaskList tl) {
@@ -111,10 +119,6 @@ __global__ void kg_elem(const __grid_constant__ TaskList tl) {
   const size_t n = (size_t)K.p0;
   for (size_t p = (size_t)(blockIdx.x - K.block0) * 256 + threadIdx.x; p < n; p += (size_t)K.gx * 256)
     c[p] = (TD)a[p];
-}
-
-static void check_tl(const TaskList &tl) {
-  (void)tl;
 }
 
 void glaunch_residual32(const TaskList &tl, cudaStream_t s) {
@@ -173,7 +177,6 @@ void glaunch_dense(const TaskList &tl, bool f32, cudaStream_t s) {
 }
 void glaunch_elementwise(const TaskList &tl, int kind, cudaStream_t s) {
   if (!tl.n) return;
-  check_tl(tl);
   switch (kind) {
     case 0: kg_elem<float, float><<<tl.nblocks, 256, 0, s>>>(tl); break;
     case 1: kg_elem<double, double><<<tl.nblocks, 256, 0, s>>>(tl); break;

@@ -262,25 +262,38 @@ void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj,
   k_remove_aj_mean<<<reduce_blocks(), 256, 0, s>>>(g, nvert, aj, b, sums); count_launch();
 }
 
-// Coarsest level: e = Minv r with a dense FP64 inverse (one warp per row).
+// Coarsest level: e = Minv r with a dense FP64 inverse over the cells idx[0..m)
+// (one warp per row), e = r on the identity cells idx[m..n).
 template <typename T>
-__global__ void k_dense(const double *__restrict__ M, int n, const T *__restrict__ r, T *__restrict__ e,
-                        const int *gate) {
-  if (gated(gate)) return;
-  int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  int lane = threadIdx.x & 31;
+__device__ __forceinline__ void dense_rows(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
+                                           const T *__restrict__ r, T *__restrict__ e, int row) {
+  const int lane = threadIdx.x & 31;
   if (row >= n) return;
+  if (row >= m) {
+    if (lane == 0) e[idx[row]] = r[idx[row]];
+    return;
+  }
   double s = 0.0;
-  for (int c = lane; c < n; c += 32) s = fma(M[(size_t)row * n + c], (double)r[c], s);
+  for (int c = lane; c < m; c += 32) s = fma(M[(size_t)row * m + c], (double)r[idx[c]], s);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) e[row] = (T)s;
+  if (lane == 0) e[idx[row]] = (T)s;
 }
-void launch_dense_apply(const double *Minv, int n, const double *r, double *e, cudaStream_t s, const int *gate) {
-  k_dense<double><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e, gate); count_launch();
+template <typename T>
+__global__ void k_dense(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
+                        const T *__restrict__ r, T *__restrict__ e, const int *gate) {
+  if (gated(gate)) return;
+  dense_rows<T>(M, idx, m, n, r, e, blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5));
 }
-void launch_dense_apply_f32(const double *Minv, int n, const float *r, float *e, cudaStream_t s, const int *gate) {
-  k_dense<float><<<(n + 7) / 8, 256, 0, s>>>(Minv, n, r, e, gate); count_launch();
+void launch_dense_apply(const LevelDev &C, const double *Minv, const double *r, double *e, cudaStream_t s,
+                        const int *gate) {
+  int n = (int)C.g.n();
+  k_dense<double><<<(n + 7) / 8, 256, 0, s>>>(Minv, C.cidx, C.cm, n, r, e, gate); count_launch();
+}
+void launch_dense_apply_f32(const LevelDev &C, const double *Minv, const float *r, float *e, cudaStream_t s,
+                            const int *gate) {
+  int n = (int)C.g.n();
+  k_dense<float><<<(n + 7) / 8, 256, 0, s>>>(Minv, C.cidx, C.cm, n, r, e, gate); count_launch();
 }
 
 }  // namespace cvb

@@ -186,7 +186,9 @@ __global__ void k_line_factors(Geom g, const double *__restrict__ w, double *__r
       if (g.py && j == 1) a = 0.0;
       if (g.py && j == g.my - 2) c = 0.0;
       double m = b - a * cprev;
-      double minv = 1.0 / m;
+      // an empty row (a fluid cell cut off from all its neighbours) has no
+      // pivot: the sweep leaves it unchanged instead of dividing by zero
+      double minv = m != 0.0 ? 1.0 / m : 0.0;
       double cp = c * minv;
       l64[p] = a; l64[n + p] = minv; l64[2 * n + p] = cp;
       l32[p] = (float)a; l32[n + p] = (float)minv; l32[2 * n + p] = (float)cp;

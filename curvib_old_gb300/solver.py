@@ -183,16 +183,36 @@ class PoissonContext:
         """Copy a host right-hand side into the resident rhs."""
         self._check(self._L.cvb_set_rhs(self._ctx, ptr(_c64(b))))
 
+    def set_phi(self, phi):
+        """Copy a host pressure into the resident phi (a warm start's initial guess)."""
+        self._check(self._L.cvb_set_phi(self._ctx, ptr(_c64(phi))))
+
     def get_phi(self):
         """The resident solution, copied to the host."""
         phi = np.zeros(self.shapes[-1])
         self._check(self._L.cvb_get_phi(self._ctx, ptr(phi)))
         return phi
 
+    def setup_like(self, donor, nvert):
+        """Set up on the grid of a set-up donor context (its resident metrics are
+        shared) with this problem's finest-level nvert."""
+        nv = _c64(nvert)
+        self._check(self._L.cvb_setup_like(self._ctx, donor._ctx, ptr(nv)))
+        self.shapes = list(donor.shapes)
+        self.nlevels = donor.nlevels
+        return self
+
     def device_bytes(self):
+        """Device memory held by this context alone."""
         v = ctypes.c_ulonglong()
         self._check(self._L.cvb_device_bytes(self._ctx, ctypes.byref(v)))
         return int(v.value)
+
+    def geometry_bytes(self):
+        """(bytes, id) of the grid metrics this context shares."""
+        v, i = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        self._check(self._L.cvb_geometry_bytes(self._ctx, ctypes.byref(v), ctypes.byref(i)))
+        return int(v.value), int(i.value)
 
     def tuning(self):
         """The set-up autotuner's measurements and choices (dict)."""

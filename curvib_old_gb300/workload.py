@@ -389,7 +389,9 @@ def sphere_nvert(cent: np.ndarray, spheres, ib_code: float = IB_CODE,
     codes 1.4 / 3.4 are the ones ibm_search_advanced_rev leaves -- the search
     the reference's main.c runs (main.c:1020) and whose IB layer VolumeFlux_rev
     corrects (nvert in (1.1, 1.5), poisson.c:3753).  All bodies share one code
-    (the per-body +ibi/1000 of ibm.c:4651 is not used).
+    (the per-body +ibi/1000 of ibm.c:4651 is not used).  A fluid cell left with
+    no fluid face neighbour is marked IB too.  Boxes with periodic directions
+    count links across the seam as absent (a conservative choice).
     """
     mz, my, mx = cent.shape[:3]
     solid = np.zeros((mz, my, mx), dtype=bool)
@@ -408,7 +410,18 @@ def sphere_nvert(cent: np.ndarray, spheres, ib_code: float = IB_CODE,
     nv[0, :, :] = nv[-1, :, :] = 0.0
     nv[:, 0, :] = nv[:, -1, :] = 0.0
     nv[:, :, 0] = nv[:, :, -1] = 0.0
-    return nv
+    # A fluid cell enclosed on all six faces by IB cells (a gap between two
+    # bodies narrower than a cell) would have an empty pressure row: mark it IB.
+    while True:
+        fl = np.zeros((mz, my, mx), dtype=bool)
+        fl[1:-1, 1:-1, 1:-1] = nv[1:-1, 1:-1, 1:-1] < 0.1
+        c = fl[1:-1, 1:-1, 1:-1]
+        links = (fl[2:, 1:-1, 1:-1].astype(int) + fl[:-2, 1:-1, 1:-1] + fl[1:-1, 2:, 1:-1] + fl[1:-1, :-2, 1:-1]
+                 + fl[1:-1, 1:-1, 2:] + fl[1:-1, 1:-1, :-2])
+        lone = c & (links == 0)
+        if not lone.any():
+            return nv
+        nv[1:-1, 1:-1, 1:-1][lone] = ib_code
 
 
 # ------------------------------------------------------------------- fluxes

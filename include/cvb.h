@@ -113,6 +113,11 @@ const char *cvb_last_error(const cvb_ctx *ctx);
  * all of this inside every PoissonSolver_MG call; here it stays resident. */
 int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *levels,
                         const double *nvert_finest);
+/* Set up a hierarchy on the grid of a set-up donor context, with this
+ * context's own nvert: the metrics stay resident once and are shared (they are
+ * freed with the last context that uses them).  No counterpart in the
+ * reference, which keeps one grid per run. */
+int cvb_setup_like(cvb_ctx *ctx, const cvb_ctx *donor, const double *nvert_finest);
 /* The immersed body moved: redo the nvert restriction and rebuild the operators. */
 int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest);
 /* Restricted nvert of one level ([mz][my][mx]) and the FullyBlocked result. */
@@ -145,9 +150,10 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
 /* Device pointers of the context's finest-level rhs and solution ([mz][my][mx] FP64). */
 double *cvb_device_rhs(cvb_ctx *ctx);
 double *cvb_device_phi(cvb_ctx *ctx);
-/* Copy a host rhs into the resident rhs / the resident phi out to the host
- * ([mz][my][mx] FP64, synchronous). */
+/* Copy a host rhs into the resident rhs, a host phi into the resident phi (a
+ * warm start), the resident phi out to the host ([mz][my][mx] FP64, synchronous). */
 int cvb_set_rhs(cvb_ctx *ctx, const double *b);
+int cvb_set_phi(cvb_ctx *ctx, const double *phi);
 int cvb_get_phi(cvb_ctx *ctx, double *phi);
 /* Solve the context's resident rhs into its resident phi. */
 int cvb_solve_resident(cvb_ctx *ctx, const cvb_solve_opts *opts, cvb_solve_stats *stats);
@@ -233,8 +239,10 @@ int cvb_batch_read_phi(cvb_batch *batch, cvb_ctx *ctx, double *host_phi);
 /* Submit n solves with the batch's options and run them to completion. */
 int cvb_batch_solve(cvb_batch *batch, int n, cvb_ctx *const *ctxs, cvb_solve_stats *stats);
 int cvb_batch_in_flight(const cvb_batch *batch);
-/* Device memory held by a context (its hierarchy, vectors and Krylov basis). */
+/* Device memory held by a context alone (operators, vectors, Krylov basis) and
+ * by its grid's shared metrics, with an id that is equal for contexts sharing them. */
 int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes);
+int cvb_geometry_bytes(const cvb_ctx *ctx, unsigned long long *bytes, unsigned long long *id);
 
 /* --- measurement ------------------------------------------------------- */
 /* Kernel launches this library has issued in the process (all contexts). */
