@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-solves measurement")
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--no-serve", action="store_true", help="skip the served solve stream")
+    ap.add_argument("--serve-requests", type=int, default=120)
     return ap.parse_args()
 
 
@@ -275,6 +277,18 @@ def run_cvb(args, ws, rank, local):
     }
     if not args.no_batch:
         out["batch"] = bench_batch(args, ws, local)
+    if not args.no_serve:
+        from curvib_old_gb300 import serve as S
+        out["serve"] = {
+            "workload": "served solve stream (config 4): Poisson arrivals at 0.8 x the batched capacity of the "
+                        "stream's first problems; n^3 cells log-uniform in [32^3, 256^3] rounded to a multigrid "
+                        "ladder, 0-3 spheres, 30% warm-started follow-ups (rhs perturbed 1%), 150 GB HBM budget; "
+                        "latency = arrival to pressure back in host memory",
+        }
+        inputs = S.Inputs(S.make_stream(args.serve_requests, 1.0, seed=4, max_cells=256), local)
+        for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
+            out["serve"][name] = S.serve(args.serve_requests, 0.8, 150.0, 256, prec, local, inputs=inputs)
+        out["serve"]["mixed_over_fp64"] = out["serve"]["mixed"]["solves_per_s"] / out["serve"]["fp64"]["solves_per_s"]
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(P, b)
     return out

@@ -92,6 +92,7 @@ EXPORTS = {
     "cvb_device_bytes": ([_P, _P], _I),
     "cvb_geometry_bytes": ([_P, _P, _P], _I),
     "cvb_setup_like": ([_P, _P, _P], _I),
+    "cvb_setup_geometry": ([_P, _I, _P], _I),
     "cvb_set_rhs": ([_P, _P], _I),
     "cvb_set_phi": ([_P, _P], _I),
     "cvb_get_phi": ([_P, _P], _I),

@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -113,7 +114,10 @@ static int galloc(cvb_ctx *ctx, Geometry &G, T **p, size_t count) {
   return CVB_OK;
 }
 
+void drop_vcycle_graphs(cvb_ctx *ctx);
+
 static void free_all(cvb_ctx *ctx) {
+  drop_vcycle_graphs(ctx);
   for (void *p : ctx->allocs) cudaFreeAsync(p, ctx->stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->allocs.clear();
@@ -367,6 +371,38 @@ struct ShapeKey {
 };
 std::mutex g_tune_mu;
 std::map<ShapeKey, cvb_ctx::Tune> g_tune_cache;
+bool g_tune_loaded = false;
+
+// With CVB_TUNE_FILE set, measured choices persist in that text file (one
+// shape per line: mx my mz px py pz and the four timings in microseconds), so a
+// later process -- a profiler run, say, whose own timings would be distorted --
+// makes the same choices.  Called with g_tune_mu held.
+void tune_file_load() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char *path = std::getenv("CVB_TUNE_FILE");
+  if (!path || !*path) return;
+  FILE *f = std::fopen(path, "r");
+  if (!f) return;
+  ShapeKey k;
+  cvb_ctx::Tune t;
+  while (std::fscanf(f, "%d %d %d %d %d %d %lf %lf %lf %lf", &k.mx, &k.my, &k.mz, &k.px, &k.py, &k.pz, &t.us32[0],
+                     &t.us32[1], &t.us64[0], &t.us64[1]) == 10) {
+    t.level = 0;
+    t.cells = (size_t)k.mx * k.my * k.mz;
+    g_tune_cache.emplace(k, t);
+  }
+  std::fclose(f);
+}
+void tune_file_append(const ShapeKey &k, const cvb_ctx::Tune &t) {
+  const char *path = std::getenv("CVB_TUNE_FILE");
+  if (!path || !*path) return;
+  FILE *f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%d %d %d %d %d %d %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz, k.px, k.py, k.pz, t.us32[0], t.us32[1],
+               t.us64[0], t.us64[1]);
+  std::fclose(f);
+}
 }  // namespace
 
 static int autotune_sweeps(cvb_ctx *ctx) {
@@ -377,6 +413,7 @@ static int autotune_sweeps(cvb_ctx *ctx) {
     const ShapeKey key{L.g.mx, L.g.my, L.g.mz, L.g.px, L.g.py, L.g.pz};
     {
       std::lock_guard<std::mutex> lock(g_tune_mu);
+      tune_file_load();
       auto it = g_tune_cache.find(key);
       if (it != g_tune_cache.end()) {
         cvb_ctx::Tune t = it->second;
@@ -414,7 +451,7 @@ static int autotune_sweeps(cvb_ctx *ctx) {
     L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
     ctx->tune.push_back(t);
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tune_cache.emplace(key, t);
+    if (g_tune_cache.emplace(key, t).second) tune_file_append(key, t);
   }
   return CVB_OK;
 }
@@ -523,6 +560,62 @@ static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts
   if (x != out) cudaMemcpyAsync(out, x, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
 }
 
+// One V-cycle replayed from a CUDA graph: the first use of a (precision, input,
+// output) triple runs it eagerly (kernel attributes get set outside any
+// capture), the second captures it on the context's stream, later ones replay
+// the graph -- one launch for the cycle's tens of kernels, most of them on
+// coarse levels where a kernel is shorter than its launch.  Graphs are keyed
+// by the cycle's options and dropped whenever the operators are rebuilt.
+void drop_vcycle_graphs(cvb_ctx *ctx) {
+  for (auto &kv : ctx->vgraphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  ctx->vgraphs.clear();
+}
+
+template <typename T>
+static int vcycle_graph(cvb_ctx *ctx, const cvb_solve_opts *o, int slot, const T *b, T *out) {
+  const int key = (sizeof(T) == 4 ? 1000 : 0) + slot;
+  VGraph &g = ctx->vgraphs[key];
+  const bool same = g.omega == o->omega && g.pre == o->pre_sweeps && g.post == o->post_sweeps && g.b == (const void *)b &&
+                    g.out == (void *)out;
+  if (!same) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = VGraph();
+    g.omega = o->omega; g.pre = o->pre_sweeps; g.post = o->post_sweeps; g.b = b; g.out = out;
+  }
+  if (g.exec) {
+    CK(cudaGraphLaunch(g.exec, ctx->stream));
+    count_launch(g.nodes);
+    return CVB_OK;
+  }
+  if (g.uses++ == 0 || g.failed) {
+    vcycle<T>(ctx, ctx->nlevels - 1, b, out, o);
+    CKL();
+    return CVB_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  const long long c0 = launch_count();
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  vcycle<T>(ctx, ctx->nlevels - 1, b, out, o);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+  const long long nodes = launch_count() - c0;
+  count_launch((int)-nodes);  // captured, not launched
+  if (e == cudaSuccess && graph) e = cudaGraphInstantiate(&g.exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess || !g.exec) {
+    cudaGetLastError();
+    g.exec = nullptr;
+    g.failed = true;  // keep to eager launches for this cycle
+    vcycle<T>(ctx, ctx->nlevels - 1, b, out, o);
+    CKL();
+    return CVB_OK;
+  }
+  g.nodes = (int)nodes;
+  CK(cudaGraphLaunch(g.exec, ctx->stream));
+  count_launch(g.nodes);
+  return CVB_OK;
+}
+
 // ------------------------------------------------------------------ solver
 static int reduce_to_host(cvb_ctx *ctx, int nv, double *out) {
   launch_finish_sums(ctx->partial, nv, reduce_blocks(), ctx->sums, ctx->stream);
@@ -600,11 +693,11 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
         // FP32 V-cycle; its result is widened once into the FP64 basis so the
         // FP64 operator and the final update read it without per-use conversions
         // (a conversion costs an FP64-pipe instruction on this part)
-        vcycle<float>(ctx, ctx->nlevels - 1, ctx->b32, ctx->Z32[0], o);
+        TRY(vcycle_graph<float>(ctx, o, 0, ctx->b32, ctx->Z32[0]));
         launch_f32_to_f64(ctx->Z32[0], ctx->Z64[j], n, s);
         launch_apply<double>(F, ctx->Z64[j], ctx->w, s);
       } else {
-        vcycle<double>(ctx, ctx->nlevels - 1, ctx->V[j], ctx->Z64[j], o);
+        TRY(vcycle_graph<double>(ctx, o, j, ctx->V[j], ctx->Z64[j]));
         launch_apply<double>(F, ctx->Z64[j], ctx->w, s);
       }
       CKL();
@@ -825,9 +918,8 @@ const char *cvb_last_error(const cvb_ctx *ctx) { return ctx ? ctx->err.c_str() :
 
 void *cvb_stream(cvb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
-int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, const double *nvert_finest) {
-  if (!ctx) return CVB_BAD_INPUT;
-  if (nlevels < 1 || nlevels > 16 || !lv || !nvert_finest) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
+// Checks the level descriptors and uploads the grid's metrics into a new Geometry.
+static int upload_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv) {
   CK(cudaSetDevice(ctx->device));
   ensure_pool(ctx->device);
   free_all(ctx);
@@ -870,14 +962,27 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, con
     CK(cudaStreamSynchronize(ctx->stream));
   }
   ctx->geo = G;
+  return CVB_OK;
+}
+
+int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, const double *nvert_finest) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (nlevels < 1 || nlevels > 16 || !lv || !nvert_finest) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
+  TRY(upload_geometry(ctx, nlevels, lv));
   std::vector<double> h;
   extract_box(lv[nlevels - 1], nvert_finest, 1, h);
   return setup_problem(ctx, h);
 }
 
+int cvb_setup_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (nlevels < 1 || nlevels > 16 || !lv) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
+  return upload_geometry(ctx, nlevels, lv);
+}
+
 int cvb_setup_like(cvb_ctx *ctx, const cvb_ctx *donor, const double *nvert_finest) {
   if (!ctx || !donor || ctx == donor) return CVB_BAD_INPUT;
-  if (!donor->ready || !donor->geo) return fail(ctx, CVB_NOT_SETUP, "the donor context is not set up");
+  if (!donor->geo) return fail(ctx, CVB_NOT_SETUP, "the donor context holds no grid");
   if (!nvert_finest) return fail(ctx, CVB_BAD_INPUT, "nvert is NULL");
   if (donor->device != ctx->device)
     return fail(ctx, CVB_BAD_INPUT, "donor is on device %d, context on %d", donor->device, ctx->device);
@@ -920,11 +1025,13 @@ extern "C" {
 
 int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
   if (!ctx) return CVB_BAD_INPUT;
+  CK(cudaSetDevice(ctx->device));
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
   if (!nvert_finest) return fail(ctx, CVB_BAD_INPUT, "nvert is NULL");
   const cvb_level_desc &df = ctx->H[ctx->nlevels - 1].d;
   std::vector<double> h;
   extract_box(df, nvert_finest, 1, h);
+  drop_vcycle_graphs(ctx);
   CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice,
                      ctx->stream));
   TRY(build_operators(ctx));

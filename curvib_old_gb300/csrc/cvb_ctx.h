@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -33,6 +34,17 @@ struct Geometry {
     cudaSetDevice(device);
     for (void *p : allocs) cudaFree(p);
   }
+};
+
+// A captured V-cycle of one context (see vcycle_graph).
+struct VGraph {
+  cudaGraphExec_t exec = nullptr;
+  int nodes = 0, uses = 0;
+  bool failed = false;
+  double omega = -1.0;
+  int pre = -1, post = -1;
+  const void *b = nullptr;
+  void *out = nullptr;
 };
 
 }  // namespace cvb
@@ -75,6 +87,7 @@ struct cvb_ctx {
   double *uc_dev = nullptr, *p_dev = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;
+  std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)
   // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
   struct Tune { int level; size_t cells; double us32[2], us64[2]; };
   std::vector<Tune> tune;

@@ -140,8 +140,14 @@ class Inputs:
 
 
 class Server:
+    """Request loop over one batch engine.  Contexts are prepared (operators
+    rebuilt for a new problem's bodies, or a new context set up on its grid's
+    resident metrics) on a worker thread while the main loop keeps the batch's
+    rounds flowing; every piece of bookkeeping stays on the main thread."""
+
     def __init__(self, inputs, device=0, budget_bytes=150e9, precision=_lib.MIXED, rtol=1e-8, max_it=200,
-                 restart=30, keep_results=False):
+                 restart=30, keep_results=False, workers=2):
+        from concurrent.futures import ThreadPoolExecutor
         self.inp = inputs
         self.results = {} if keep_results else None
         self.trace = []             # (request id, warm start, request whose pressure was the initial guess)
@@ -150,78 +156,108 @@ class Server:
         self.batch = SolveBatch(device, precision=precision, rtol=rtol, max_it=max_it, restart=restart)
         self.ctxs = OrderedDict()   # context id -> dict(ctx, n, bytes, busy, owner, last): LRU order
         self.owner = {}             # problem (first request id) -> context id holding it
-        self.geo = {}               # grid size -> shared metrics bytes (while a context of that size lives)
+        self.holders = OrderedDict()  # grid size -> dict(ctx, bytes, ready future): resident metrics, LRU
         self.peak = 0
         self._next = 0
+        self.pool = ThreadPoolExecutor(max_workers=workers)
 
     @property
     def used(self):
-        return sum(c["bytes"] for c in self.ctxs.values()) + sum(self.geo.values())
+        return sum(c["bytes"] for c in self.ctxs.values()) + sum(h["bytes"] for h in self.holders.values())
 
     def close(self):
+        self.pool.shutdown(wait=True)
         for c in self.ctxs.values():
             c["ctx"].close()
+        for h in self.holders.values():
+            h["ctx"].close()
         self.ctxs.clear()
-        self.geo.clear()
+        self.holders.clear()
         self.batch.close()
 
-    def _evict(self, cid):
-        c = self.ctxs.pop(cid)
-        if c["owner"] is not None:
-            self.owner.pop(c["owner"], None)
-        c["ctx"].close()
-        if not any(o["n"] == c["n"] for o in self.ctxs.values()):
-            self.geo.pop(c["n"], None)    # the grid's metrics went with its last context
+    def _evict_one(self, keep_n):
+        """Free the least recently used idle context, else an unused grid's
+        metrics; False when nothing can go."""
+        for cid, c in self.ctxs.items():
+            if not c["busy"]:
+                self.ctxs.pop(cid)
+                if c["owner"] is not None:
+                    self.owner.pop(c["owner"], None)
+                c["ctx"].close()
+                return True
+        for n, h in self.holders.items():
+            if n != keep_n and h["ready"].done() and not any(c["n"] == n for c in self.ctxs.values()):
+                self.holders.pop(n)
+                h["ctx"].close()
+                return True
+        return False
 
-    def _context_for(self, n, problem_id):
-        """An idle context of size n (rebuilt for the new bodies) or a new one on
-        the size's resident metrics (or new metrics); (None, evictions, False)
-        while the budget has no room."""
+    def _holder(self, n):
+        h = self.holders.get(n)
+        if h is None:
+            ctx = PoissonContext(self.device)
+            mets = self.inp.geo[n][0]
+            P = W.Problem(mets, np.zeros(mets[-1]["Aj"].shape[:3]), None, [1] * 6)
+            h = {"ctx": ctx, "bytes": geometry_bytes_estimate(n)}
+            h["ready"] = self.pool.submit(ctx.setup_geometry, P)
+            self.holders[n] = h
+        self.holders.move_to_end(n)
+        return h
+
+    def _prepare(self, n, problem_id):
+        """A context for a new problem: (context id, evictions, reused) or
+        (None, evictions, False) while the budget has no room.  The context is
+        busy until its preparation future completes."""
+        nv = self.inp.nvert[problem_id]
         for cid, c in self.ctxs.items():
             if not c["busy"] and c["n"] == n:
                 if c["owner"] is not None:
                     self.owner.pop(c["owner"], None)
-                c["ctx"].set_nvert(self.inp.nvert[problem_id])
-                c["owner"] = problem_id
+                c.update(owner=problem_id, busy=True, last=None)
+                c["ready"] = self.pool.submit(c["ctx"].set_nvert, nv)
                 self.ctxs.move_to_end(cid)
                 return cid, 0, True
         evicted = 0
 
         def need():
-            return own_bytes_estimate(n) + (0 if n in self.geo else geometry_bytes_estimate(n))
-        for cid in list(self.ctxs):
-            if self.used + need() <= self.budget:
-                break
-            if not self.ctxs[cid]["busy"]:
-                self._evict(cid)
-                evicted += 1
-        if self.used + need() > self.budget:
-            return None, evicted, False
-        donor = next((c["ctx"] for c in self.ctxs.values() if c["n"] == n), None)
+            return own_bytes_estimate(n) + (0 if n in self.holders else geometry_bytes_estimate(n))
+        while self.used + need() > self.budget:
+            if not self._evict_one(n):
+                return None, evicted, False
+            evicted += 1
+        h = self._holder(n)
         ctx = PoissonContext(self.device)
-        if donor is not None:
-            ctx.setup_like(donor, self.inp.nvert[problem_id])
-        else:
-            ctx.setup(self.inp.problem(n, self.inp.nvert[problem_id]))
-            self.geo[n] = ctx.geometry_bytes()[0]
-        # the FGMRES basis is allocated at the first solve: count it now
-        nb = max(ctx.device_bytes(), own_bytes_estimate(n))
+
+        def job():
+            h["ready"].result()
+            ctx.setup_like(h["ctx"], nv)
         cid = self._next
         self._next += 1
-        self.ctxs[cid] = {"ctx": ctx, "n": n, "bytes": nb, "busy": False, "owner": problem_id}
+        self.ctxs[cid] = {"ctx": ctx, "n": n, "bytes": own_bytes_estimate(n), "busy": True, "owner": problem_id,
+                          "last": None, "ready": self.pool.submit(job)}
         self.peak = max(self.peak, self.used)
         return cid, evicted, False
 
     def run(self, stream, time_limit=600.0):
         """Serve `stream` (sorted by arrival); returns the statistics."""
-        queue, inflight = [], {}
+        queue, inflight, preparing = [], {}, []
         lat, warm, cold_followups, evictions, reused = [], 0, 0, 0, 0
+        spent = {"admit_s": 0.0, "step_s": 0.0, "result_s": 0.0, "rounds": 0}
         nxt = 0
         t0 = time.perf_counter()
-        while nxt < len(stream) or queue or inflight:
+
+        def submit(req, cid, ws):
+            c = self.ctxs[cid]
+            self.trace.append((req.rid, ws, c.get("last") if ws else None))
+            c["last"] = req.rid
+            t = self.batch.submit(c["ctx"], b=self.inp.rhs[req.rid], warm_start=ws)
+            inflight[t] = (req, cid)
+
+        while nxt < len(stream) or queue or inflight or preparing:
             now = time.perf_counter() - t0
             if now > time_limit:
                 break
+            ts = time.perf_counter()
             while nxt < len(stream) and stream[nxt].arrival <= now:
                 queue.append(stream[nxt])
                 nxt += 1
@@ -234,28 +270,38 @@ class Server:
                     if c["busy"]:
                         still.append(req)
                         continue
+                    c["busy"] = True
                     self.ctxs.move_to_end(cid)
                     warm += 1
-                    ws = True
-                else:
-                    cid, ev, was_reused = self._context_for(req.n, pid)
-                    evictions += ev
-                    if cid is None:
-                        still.append(req)
-                        continue
-                    reused += int(was_reused)
-                    self.owner[pid] = cid
-                    cold_followups += int(req.base >= 0)
-                    ws = False
-                c = self.ctxs[cid]
-                c["busy"] = True
-                self.trace.append((req.rid, ws, c.get("last") if ws else None))
-                c["last"] = req.rid
-                t = self.batch.submit(c["ctx"], b=self.inp.rhs[req.rid], warm_start=ws)
-                inflight[t] = (req, cid)
+                    submit(req, cid, True)
+                    continue
+                cid, ev, was_reused = self._prepare(req.n, pid)
+                evictions += ev
+                if cid is None:
+                    still.append(req)
+                    continue
+                reused += int(was_reused)
+                self.owner[pid] = cid
+                cold_followups += int(req.base >= 0)
+                preparing.append((req, cid))
             queue = still
+            left = []
+            for req, cid in preparing:
+                c = self.ctxs[cid]
+                if c["ready"].done():
+                    c["ready"].result()           # re-raise a failed preparation
+                    c["bytes"] = max(c["ctx"].device_bytes(), own_bytes_estimate(c["n"]))
+                    submit(req, cid, False)
+                else:
+                    left.append((req, cid))
+            preparing = left
+            spent["admit_s"] += time.perf_counter() - ts
             if inflight:
+                ts = time.perf_counter()
                 self.batch.step()
+                spent["step_s"] += time.perf_counter() - ts
+                spent["rounds"] += 1
+                ts = time.perf_counter()
                 for t, st in self.batch.poll():
                     req, cid = inflight.pop(t)
                     if st["status"] != 0:
@@ -266,15 +312,19 @@ class Server:
                         self.results[req.rid] = (phi, st)
                     c["busy"] = False
                     lat.append((time.perf_counter() - t0 - req.arrival) * 1e3)
-            elif nxt < len(stream):
-                time.sleep(max(0.0, min(0.005, stream[nxt].arrival - (time.perf_counter() - t0))))
+                spent["result_s"] += time.perf_counter() - ts
+            else:
+                wait = 0.002 if preparing else (stream[nxt].arrival - (time.perf_counter() - t0)
+                                                 if nxt < len(stream) else 0.002)
+                time.sleep(max(0.0, min(0.005, wait)))
         wall = time.perf_counter() - t0
         return {"requests": len(stream), "served": len(lat), "wall_s": wall,
                 "solves_per_s": len(lat) / wall if wall > 0 else 0.0,
                 "p50_ms": float(np.percentile(lat, 50)) if lat else None,
                 "p99_ms": float(np.percentile(lat, 99)) if lat else None,
                 "warm_followups": warm, "cold_followups": cold_followups, "contexts_reused": reused,
-                "evictions": evictions, "peak_resident_bytes": int(self.peak), "budget_bytes": int(self.budget)}
+                "evictions": evictions, "peak_resident_bytes": int(self.peak), "budget_bytes": int(self.budget),
+                "loop": spent}
 
 
 def capacity(inputs, stream, device=0, precision=_lib.MIXED, rtol=1e-8, budget_bytes=150e9):
@@ -306,12 +356,14 @@ def capacity(inputs, stream, device=0, precision=_lib.MIXED, rtol=1e-8, budget_b
 
 
 def serve(requests=200, load=0.8, budget_gb=150.0, max_cells=256, precision=_lib.MIXED, device=0,
-          time_limit=600.0, probe=24):
+          time_limit=600.0, probe=24, inputs=None):
     """Measure batched capacity on the stream's first problems, then serve the
-    whole stream at `load` times that rate.  Returns the report."""
+    whole stream at `load` times that rate.  Returns the report.  `inputs`: the
+    prepared Inputs of make_stream(requests, 1.0, 4, max_cells), to reuse."""
     proto = make_stream(requests, 1.0, seed=4, max_cells=max_cells)
     t0 = time.perf_counter()
-    inputs = Inputs(proto, device)
+    if inputs is None:
+        inputs = Inputs(proto, device)
     prep = time.perf_counter() - t0
     cap = capacity(inputs, proto[:probe], device, precision, budget_bytes=budget_gb * 1e9)
     rate = load * cap

@@ -61,12 +61,7 @@ class PoissonContext:
             raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
 
     # ------------------------------------------------------------------ setup
-    def setup(self, problem, ghosts=None):
-        """Upload the hierarchy of a workload.Problem (levels coarsest first).
-
-        ``ghosts``: optional per-level (gxs, gys, gzs) offsets; the arrays of the
-        problem are then expected to be ghosted local arrays of that box.
-        """
+    def _descs(self, problem, ghosts):
         levels = problem.metrics
         n = len(levels)
         descs = (LevelDesc * n)()
@@ -91,15 +86,36 @@ class PoissonContext:
                     a = _c64(m[nm])
                     keep.append(a)
                     setattr(d, f, ptr(a))
-        nv = _c64(problem.nvert)
-        keep.append(nv)
-        self._check(self._L.cvb_setup_hierarchy(self._ctx, n, descs, ptr(nv)))
+        return n, descs, keep
+
+    def _dims(self, n):
         self.shapes = []
         for l in range(n):
             a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
             self._L.cvb_level_dims(self._ctx, l, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
             self.shapes.append((c.value, b.value, a.value))
         self.nlevels = n
+
+    def setup_geometry(self, problem, ghosts=None):
+        """Upload a grid's metrics only (a donor for setup_like; cannot solve)."""
+        n, descs, keep = self._descs(problem, ghosts)
+        self._check(self._L.cvb_setup_geometry(self._ctx, n, descs))
+        self.shapes = [tuple(m["Aj"].shape[:3]) for m in problem.metrics] if ghosts is None else \
+            list(problem.box_shapes)
+        self.nlevels = n
+        return self
+
+    def setup(self, problem, ghosts=None):
+        """Upload the hierarchy of a workload.Problem (levels coarsest first).
+
+        ``ghosts``: optional per-level (gxs, gys, gzs) offsets; the arrays of the
+        problem are then expected to be ghosted local arrays of that box.
+        """
+        n, descs, keep = self._descs(problem, ghosts)
+        nv = _c64(problem.nvert)
+        keep.append(nv)
+        self._check(self._L.cvb_setup_hierarchy(self._ctx, n, descs, ptr(nv)))
+        self._dims(n)
         return self
 
     def set_nvert(self, nvert):

@@ -118,6 +118,9 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *levels,
  * freed with the last context that uses them).  No counterpart in the
  * reference, which keeps one grid per run. */
 int cvb_setup_like(cvb_ctx *ctx, const cvb_ctx *donor, const double *nvert_finest);
+/* Upload a grid's metrics only: the context can then donate them to
+ * cvb_setup_like but cannot solve itself. */
+int cvb_setup_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *levels);
 /* The immersed body moved: redo the nvert restriction and rebuild the operators. */
 int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest);
 /* Restricted nvert of one level ([mz][my][mx]) and the FullyBlocked result. */
