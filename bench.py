@@ -263,6 +263,7 @@ def run_cvb(args, ws, rank, local):
                    "l2": "no flush: the finest level's operator data alone (~1 GB FP64, ~0.3 GB FP32) exceeds L2",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "p50_ms": statistics.median(lat_m), "p99_ms": float(np.percentile(lat_m, 99)),
+        "latencies_ms": [round(v, 3) for v in lat_m],
         "iterations": statistics.median(its_m), "rel_residual": max(rr_m),
         "unknown_iterations_per_s": ws * n_unknown * sum(its_m) / (ms_m * 1e-3),
         "fp64": {"solves_per_s": ws * args.steps / (ms_d * 1e-3), "p50_ms": statistics.median(lat_d),

@@ -346,6 +346,7 @@ static int build_operators(cvb_ctx *ctx) {
     launch_weights(g, g9, ctx->aj64[l], lv.nvert, lv.code, lv.w64, ctx->stream);
     launch_line_factors(g, lv.w64, lv.line64, lv.line32, ctx->stream);
     launch_to_f32(g9, lv.gf32, 9 * n, ctx->stream);
+    launch_scale_cross(g, lv.code, lv.gf32, ctx->stream);
     launch_to_f32(ctx->aj64[l], lv.ajf32, n, ctx->stream);
     CKL();
   }

@@ -180,20 +180,21 @@ template <typename T>
 static void gen_sweep(VSink &vs, long long key0, long long key1, LevelDev &L, const LevelDev *dLv, const T *b,
                       const T *x, T *xnew, bool zero, const int *gate) {
   const bool f32 = sizeof(T) == 4;
-  const int TW = f32 ? 32 : 16;
+  const int TW = f32 ? 32 : 16;                         // fused sweep tiles
+  const int SW = f32 ? kSolveTW32 : kSolveTW64;         // line-solve tiles
   const size_t ssw = f32 ? line_sweep_smem<float, 32>(L.g) : line_sweep_smem<double, 16>(L.g);
-  const size_t sso = f32 ? line_solve_smem<float, 32>(L.g) : line_solve_smem<double, 16>(L.g);
+  const size_t sso = f32 ? line_solve_smem<float, kSolveTW32>(L.g) : line_solve_smem<double, kSolveTW64>(L.g);
   const bool async = sso <= kMaxSmem;
-  const int lblocks = nblk(L.g.mx, TW) * L.g.mz;
+  const int lblocks = nblk(L.g.mx, TW) * L.g.mz, sblocks = nblk(L.g.mx, SW) * L.g.mz;
   const int split = f32 ? L.sweep32 : L.sweep64;
   T *res = lvec<T>(L, 3);
   if (zero) {
-    if (async) vs.add(key1, OK_SOLVE, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, TW)), lblocks, sso);
+    if (async) vs.add(key1, OK_SOLVE, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
     else vs.add(key1, OK_SWEEP, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, TW), 0, 0), lblocks, ssw);
   } else if (split == 1) {
     const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
     vs.add(key0, f32 ? OK_RES32 : OK_RES64, task(dLv, x, b, res, gate, gx, gy), gx * gy * L.g.mz);
-    if (async) vs.add(key1, OK_SOLVE, task(dLv, res, x, xnew, gate, nblk(L.g.mx, TW)), lblocks, sso);
+    if (async) vs.add(key1, OK_SOLVE, task(dLv, res, x, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
     else vs.add(key1, OK_SWEEP, task(dLv, res, x, xnew, gate, nblk(L.g.mx, TW), 0, 2), lblocks, ssw);
   } else {
     vs.add(key1, OK_SWEEP, task(dLv, b, x, xnew, gate, nblk(L.g.mx, TW), 0, 1), lblocks, ssw);

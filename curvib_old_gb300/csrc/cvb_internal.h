@@ -53,7 +53,7 @@ struct LevelDev {
   double *nvert;         // [N]
   uint32_t *code;        // [N]
   double *w64;           // [19][N] FP64 stencil weights (rows scaled by -aj; identity rows CP=1)
-  float *gf32;           // [9][N]  FP32 face coefficients g11..g33
+  float *gf32;           // [9][N]  FP32 face coefficients g11..g33, cross terms pre-scaled by form weight
   float *ajf32;          // [N]
   float *line32;         // [3][N]  y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32
   double *line64;        // [3][N]  ... in FP64
@@ -79,6 +79,8 @@ void launch_gcoef(const Geom &g, const double *const *metric /*12 Cmpnts fields:
                   const double *iaj, const double *jaj, const double *kaj, double *g9 /*[9][N]*/,
                   cudaStream_t s);
 void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s);
+// FP32 face coefficients: cross terms pre-scaled by their form's weight (after launch_codes)
+void launch_scale_cross(const Geom &g, const uint32_t *code, float *gf32, cudaStream_t s);
 void launch_weights(const Geom &g, const double *g9, const double *aj, const double *nvert,
                     const uint32_t *code, double *w64, cudaStream_t s);
 void launch_line_factors(const Geom &g, const double *w64, double *line64, float *line32,
@@ -107,6 +109,7 @@ void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s, cons
 
 // Krylov support (deterministic two-stage reductions)
 int reduce_blocks();
+int sm_count();
 void launch_multidot(const double *const *V, int nv, const double *w, size_t n, double *partial,
                      cudaStream_t s, int self = 0, const int *gate = nullptr);
 void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t n, double *partial,

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256, 2) kg_line_sweep(const __grid_constant__ 
   line_sweep_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, K.p0, lb % K.gx, lb / K.gx, smem_raw);
 }
 template <typename T, int TW>
-__global__ void __launch_bounds__(256, 2) kg_line_solve(const __grid_constant__ TaskList tl, T omega) {
+__global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_constant__ TaskList tl, T omega) {
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -161,12 +161,12 @@ void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omeg
   if (!tl.n) return;
   static bool attr = false;
   if (!attr) {
-    allow_smem(kg_line_solve<float, 32>);
-    allow_smem(kg_line_solve<double, 16>);
+    allow_smem(kg_line_solve<float, kSolveTW32>);
+    allow_smem(kg_line_solve<double, kSolveTW64>);
     attr = true;
   }
-  if (f32) kg_line_solve<float, 32><<<tl.nblocks, 256, smem, s>>>(tl, omega32);
-  else kg_line_solve<double, 16><<<tl.nblocks, 256, smem, s>>>(tl, omega64);
+  if (f32) kg_line_solve<float, kSolveTW32><<<tl.nblocks, kSolveThreads, smem, s>>>(tl, omega32);
+  else kg_line_solve<double, kSolveTW64><<<tl.nblocks, kSolveThreads, smem, s>>>(tl, omega64);
   count_launch();
 }
 void glaunch_dense(const TaskList &tl, bool f32, cudaStream_t s) {

@@ -13,13 +13,19 @@ long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED)
 static const int kRedThreads = 256;
 static int g_red_blocks = 0;
 
-int reduce_blocks() {
-  if (!g_red_blocks) {
-    int dev = 0, sms = 0;
+int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    g_red_blocks = (sms > 0 ? sms : 148) * 4;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    sms = v > 0 ? v : 148;
   }
+  return sms;
+}
+
+int reduce_blocks() {
+  if (!g_red_blocks) g_red_blocks = sm_count() * 4;
   return g_red_blocks;
 }
 

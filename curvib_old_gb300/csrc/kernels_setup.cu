@@ -92,6 +92,26 @@ void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream
   k_codes<<<nblk(g.n(), 256), 256, 0, s>>>(g, nvert, code); count_launch();
 }
 
+// FP32 flux form: scale each cross-term coefficient by the weight of its form
+// (0 none, 1/4 central, 1/2 one-sided), so the apply needs no per-term
+// coefficient selection.  Powers of two: the scaling itself is exact.
+__global__ void k_scale_cross(Geom g, const uint32_t *__restrict__ code, float *__restrict__ gf) {
+  const size_t n = g.n();
+  const float wgt[4] = {0.0f, 0.25f, 0.5f, 0.5f};
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t c = code[p];
+    gf[1 * n + p] *= wgt[code_branch(c, 0, 0)];  // g12 (face E, j-direction term)
+    gf[2 * n + p] *= wgt[code_branch(c, 0, 1)];  // g13 (face E, k)
+    gf[3 * n + p] *= wgt[code_branch(c, 1, 0)];  // g21 (face N, i)
+    gf[5 * n + p] *= wgt[code_branch(c, 1, 1)];  // g23 (face N, k)
+    gf[6 * n + p] *= wgt[code_branch(c, 2, 0)];  // g31 (face T, i)
+    gf[7 * n + p] *= wgt[code_branch(c, 2, 1)];  // g32 (face T, j)
+  }
+}
+void launch_scale_cross(const Geom &g, const uint32_t *code, float *gf32, cudaStream_t s) {
+  k_scale_cross<<<nblk(g.n(), 256) < 4096 ? nblk(g.n(), 256) : 4096, 256, 0, s>>>(g, code, gf32); count_launch();
+}
+
 // One cross term into vol[] in the reference's order (see add_cross in the oracle).
 __device__ __forceinline__ void add_cross(double *vol, int br, double gg, bool up, int P, int Q, int Pu,
                                           int Qu, int Pd, int Qd) {

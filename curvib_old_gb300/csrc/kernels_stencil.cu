@@ -53,13 +53,13 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
 }
 
 template <typename T, int TW>
-__global__ void __launch_bounds__(256, 2) k_line_solve(LevelDev L, const T *__restrict__ r, const T *__restrict__ x,
-                                                       T *__restrict__ xnew, T omega) {
+__global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r,
+                                                                 const T *__restrict__ x, T *__restrict__ xnew,
+                                                                 T omega) {
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   line_solve_body<T, TW>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw);
 }
-
 // mode 0: zero initial guess (residual = b); 1: residual b - A x computed in
 // the sweep (fused); 2: `b` already holds the residual of x (split variant).
 template <typename T, int TW>
@@ -83,7 +83,7 @@ static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T ome
     cudaFuncSetAttribute(k_line_solve<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_line_solve<T, TW><<<grd, 256, line_solve_smem<T, TW>(L.g), s>>>(L, r, x, xnew, omega); count_launch();
+  k_line_solve<T, TW><<<grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s>>>(L, r, x, xnew, omega); count_launch();
 }
 
 // Lines longer than the shared-memory tile allows fall back to a residual
@@ -136,13 +136,13 @@ template <>
 void launch_line_smooth<float>(const LevelDev &L, const float *b, const float *x, float *xnew, float omega,
                                int zero_guess, cudaStream_t s) {
   if (L.g.my <= kMaxFusedRows) {
-    const bool async = line_solve_smem<float, 32>(L.g) <= kMaxSmem;
+    const bool async = line_solve_smem<float, kSolveTW32>(L.g) <= kMaxSmem;
     if (zero_guess) {
-      if (async) line_solve<float, 32>(L, b, nullptr, xnew, omega, s);
+      if (async) line_solve<float, kSolveTW32>(L, b, nullptr, xnew, omega, s);
       else line_sweep<float, 32>(L, b, x, xnew, omega, 0, s);
     } else if (L.sweep32 == 1) {
       launch_residual<float>(L, b, x, L.t32, s);
-      if (async) line_solve<float, 32>(L, L.t32, x, xnew, omega, s);
+      if (async) line_solve<float, kSolveTW32>(L, L.t32, x, xnew, omega, s);
       else line_sweep<float, 32>(L, L.t32, x, xnew, omega, 2, s);
     } else {
       line_sweep<float, 32>(L, b, x, xnew, omega, 1, s);
@@ -158,13 +158,13 @@ template <>
 void launch_line_smooth<double>(const LevelDev &L, const double *b, const double *x, double *xnew, double omega,
                                 int zero_guess, cudaStream_t s) {
   if (L.g.my <= kMaxFusedRows) {
-    const bool async = line_solve_smem<double, 16>(L.g) <= kMaxSmem;
+    const bool async = line_solve_smem<double, kSolveTW64>(L.g) <= kMaxSmem;
     if (zero_guess) {
-      if (async) line_solve<double, 16>(L, b, nullptr, xnew, omega, s);
+      if (async) line_solve<double, kSolveTW64>(L, b, nullptr, xnew, omega, s);
       else line_sweep<double, 16>(L, b, x, xnew, omega, 0, s);
     } else if (L.sweep64 == 1) {
       launch_residual<double>(L, b, x, L.t64, s);
-      if (async) line_solve<double, 16>(L, L.t64, x, xnew, omega, s);
+      if (async) line_solve<double, kSolveTW64>(L, L.t64, x, xnew, omega, s);
       else line_sweep<double, 16>(L, L.t64, x, xnew, omega, 2, s);
     } else {
       line_sweep<double, 16>(L, b, x, xnew, omega, 1, s);

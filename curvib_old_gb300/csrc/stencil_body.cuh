@@ -80,11 +80,12 @@ __device__ __forceinline__ double row64(const Geom &g, const double *__restrict_
 // ----------------------------------------------------------------- FP32 rows
 // Cross term of a face flux: g * (cu*s_up + c0*s_level + cd*s_down) for the
 // central / lower / upper forms (branch 1/2/3), zero for branch 0.
-__device__ __forceinline__ float cross32(int br, float g, float su, float s0, float sd) {
-  float cu = br == 1 ? 0.25f : (br == 3 ? 0.5f : 0.0f);
-  float c0 = br == 2 ? 0.5f : (br == 3 ? -0.5f : 0.0f);
-  float cd = br == 1 ? -0.25f : (br == 2 ? -0.5f : 0.0f);
-  return g * (cu * su + c0 * s0 + cd * sd);
+// Cross term of a face flux.  The coefficient gs was scaled at set-up by the
+// form's weight (central 1/4, one-sided 1/2, none 0), so the term is
+// gs * (sA - sB) with (sA, sB) = (s_up, s_down) central, (s_level, s_down) lower,
+// (s_up, s_level) upper.
+__device__ __forceinline__ float cross32(int br, float gs, float su, float s0, float sd) {
+  return gs * ((br == 2 ? s0 : su) - (br == 3 ? s0 : sd));
 }
 __device__ __forceinline__ float act(uint32_t c, uint32_t bit) { return (c & bit) ? 1.0f : 0.0f; }
 
@@ -304,17 +305,24 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // apart, ls = 32*S + 1 (odd), so a warp walking one row across 32 lines is also
 // conflict-free.
 struct LineLayout {
-  int nr, R, S, ls;
+  int nr, R, S, ls, sh;
   __host__ __device__ static LineLayout of(int my) {
     LineLayout o;
     o.nr = my - 2;
-    o.R = (o.nr + 31) >> 5;
+    int need = (o.nr + 31) >> 5;
+    o.R = 1;
+    o.sh = 0;
+    while (o.R < need) { o.R <<= 1; o.sh++; }  // a power of two: chunk arithmetic by shifts
     o.S = o.R | 1;
     o.ls = 32 * o.S + 1;
     return o;
   }
-  __device__ int pos(int q) const { return q + (q / R) * (S - R); }  // q = row - 1
+  __device__ int pos(int q) const { return q + (q >> sh) * (S - R); }  // q = row - 1
 };
+
+// Lines per block of the line-solve kernel (128 threads): small tiles, so that
+// four of them share an SM and one tile's copies overlap another's solve.
+constexpr int kSolveTW32 = 16, kSolveTW64 = 8, kSolveThreads = 128;
 
 // Dynamic shared memory of the two line kernels for a level.
 template <typename T, int TW>
@@ -367,48 +375,144 @@ __device__ __forceinline__ void warp_line_solve_padded(T *r, const T *a, const T
   __syncwarp();
 }
 
-// xnew = x + omega * T^-1 r on interior lines, x elsewhere; r is the residual of
-// x (split sweep) or, with x == nullptr, the right-hand side (zero guess).
-template <typename T, int TW>
-__device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
-                                                T *__restrict__ xnew, T omega, int bx, int bk,
-                                                unsigned char *smem_raw) {
-  const Geom g = L.g;
-  const int my = g.my;
-  const LineLayout Lo = LineLayout::of(my);
-  const size_t n = g.n();
-  T *sr = reinterpret_cast<T *>(smem_raw);
-  T *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
-  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
-  const int i0 = bx * TW, k = bk, i = i0 + tx;
-  const bool kin = k >= 1 && k <= g.mz - 2;
-  const bool line = i >= 1 && i <= g.mx - 2 && kin;
-  const T *fa = RowOf<T>::fac(L);
-  if (line) {
-    for (int j = 1 + ty; j <= my - 2; j += ny) {
-      size_t p = ((size_t)k * my + j) * g.mx + i;
-      int s = tx * Lo.ls + Lo.pos(j - 1);
-      cp_async_el(sr + s, r + p);
-      cp_async_el(sa + s, fa + p);
-      cp_async_el(sm + s, fa + n + p);
-      cp_async_el(sc + s, fa + 2 * n + p);
-      if (x) cp_async_el(sx + s, x + p);
+// NL lines at once (line l at offset l * stride), interleaved: the recurrences
+// and shuffle scans of different lines are independent, so their latencies
+// overlap.  Per line the arithmetic is that of warp_line_solve_padded.
+template <typename T, int NL>
+__device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm, const T *sc, int stride,
+                                                 const LineLayout &Lo, int lane) {
+  const int q0 = lane * Lo.R, cnt = max(0, min(Lo.R, Lo.nr - q0));
+  const int b0 = lane * Lo.S;
+  T B[NL], G[NL], d[NL];
+#pragma unroll
+  for (int l = 0; l < NL; l++) { B[l] = T(1); G[l] = T(0); }
+  for (int t = 0; t < cnt; t++) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+      const int o = l * stride + b0 + t;
+      T mq = sm[o];
+      T beta = -mq * sa[o], gamma = mq * sr[o];
+      B[l] = beta * B[l];
+      G[l] = beta * G[l] + gamma;
     }
   }
-  cp_async_wait_all();
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  for (int t = warp; t < TW; t += nwarps) {
-    int it = i0 + t;
-    if (it >= 1 && it <= g.mx - 2 && kin)
-      warp_line_solve_padded<T>(sr + t * Lo.ls, sa + t * Lo.ls, sm + t * Lo.ls, sc + t * Lo.ls, Lo, lane);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+      T Bp = __shfl_up_sync(0xffffffffu, B[l], o), Gp = __shfl_up_sync(0xffffffffu, G[l], o);
+      if (lane >= o) { G[l] = B[l] * Gp + G[l]; B[l] = B[l] * Bp; }
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < NL; l++) {
+    d[l] = __shfl_up_sync(0xffffffffu, G[l], 1);
+    if (lane == 0) d[l] = T(0);
+  }
+  for (int t = 0; t < cnt; t++) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+      const int o = l * stride + b0 + t;
+      T mq = sm[o];
+      d[l] = mq * sr[o] - mq * sa[o] * d[l];
+      sr[o] = d[l];
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int l = 0; l < NL; l++) { B[l] = T(1); G[l] = T(0); }
+  for (int t = cnt - 1; t >= 0; t--) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+      const int o = l * stride + b0 + t;
+      T beta = -sc[o], gamma = sr[o];
+      B[l] = beta * B[l];
+      G[l] = beta * G[l] + gamma;
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+      T Bn = __shfl_down_sync(0xffffffffu, B[l], o), Gn = __shfl_down_sync(0xffffffffu, G[l], o);
+      if (lane + o < 32) { G[l] = B[l] * Gn + G[l]; B[l] = B[l] * Bn; }
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < NL; l++) {
+    d[l] = __shfl_down_sync(0xffffffffu, G[l], 1);
+    if (lane == 31) d[l] = T(0);
+  }
+  for (int t = cnt - 1; t >= 0; t--) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+      const int o = l * stride + b0 + t;
+      d[l] = sr[o] - sc[o] * d[l];
+      sr[o] = d[l];
+    }
+  }
+  __syncwarp();
+}
+
+// xnew = x + omega * T^-1 r on interior lines, x elsewhere; r is the residual of
+// x (split sweep) or, with x == nullptr, the right-hand side (zero guess).
+// A tile is TW consecutive lines (i) at one k.  (A persistent, double-buffered
+// form of this kernel -- prefetching a block's next tile while it solves the
+// current one -- ran slower here: with two tiles per block only two blocks fit
+// on an SM, and four independent blocks hide the copies better.)
+
+template <typename T, int TW>
+__device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
+                                                int bx, int k, T *st) {
+  const Geom &g = L.g;
+  const int my = g.my, mx = g.mx;
+  const LineLayout Lo = LineLayout::of(my);
+  const int n = (int)g.n();
+  T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int i = bx * TW + tx;
+  if (!(i >= 1 && i <= mx - 2 && k >= 1 && k <= g.mz - 2)) return;
+  const T *fa = RowOf<T>::fac(L);
+  const int col = (k * my) * mx + i;
+  for (int j = 1 + ty; j <= my - 2; j += ny) {
+    const int p = col + j * mx;
+    const int s = tx * Lo.ls + Lo.pos(j - 1);
+    cp_async_el(sr + s, r + p);
+    cp_async_el(sa + s, fa + p);
+    cp_async_el(sm + s, fa + n + p);
+    cp_async_el(sc + s, fa + 2 * n + p);
+    if (x) cp_async_el(sx + s, x + p);
+  }
+}
+
+// Solve the tile's lines in shared memory and write it out (the tile's copies
+// have landed and the block is synchronised when this is entered).
+template <typename T, int TW>
+__device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__restrict__ x, T *__restrict__ xnew,
+                                                  T omega, int bx, int k, T *st) {
+  const Geom &g = L.g;
+  const int my = g.my, mx = g.mx;
+  const LineLayout Lo = LineLayout::of(my);
+  T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int i = bx * TW + tx;
+  const bool kin = k >= 1 && k <= g.mz - 2;
+  const bool line = i >= 1 && i <= mx - 2 && kin;
+  // every warp solves TW / 4 lines (warp, warp + 4, ...) together; lines off
+  // the interior hold stale shared memory whose results are never read
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NW = kSolveThreads / 32, NL = TW / NW;
+  if (kin) {
+    const int o = warp * Lo.ls;
+    warp_lines_solve<T, NL>(sr + o, sa + o, sm + o, sc + o, NW * Lo.ls, Lo, lane);
   }
   __syncthreads();
-  if (i >= g.mx) return;
+  if (i >= mx) return;
+  const int col = (k * my) * mx + i;
   for (int j = ty; j < my; j += ny) {
-    size_t p = ((size_t)k * my + j) * g.mx + i;
+    const int p = col + j * mx;
     if (line && j >= 1 && j <= my - 2) {
-      int s = tx * Lo.ls + Lo.pos(j - 1);
+      const int s = tx * Lo.ls + Lo.pos(j - 1);
       T xo = x ? sx[s] : T(0);
       xnew[p] = xo + omega * sr[s];
     } else {
@@ -417,8 +521,17 @@ __device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__re
   }
 }
 
-
-
+// One tile per block: issue every copy, wait once, solve, write.
+template <typename T, int TW>
+__device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
+                                                T *__restrict__ xnew, T omega, int bx, int k,
+                                                unsigned char *smem_raw) {
+  T *st = reinterpret_cast<T *>(smem_raw);
+  solve_tile_load<T, TW>(L, r, x, bx, k, st);
+  cp_async_wait_all();
+  __syncthreads();
+  solve_tile_finish<T, TW>(L, x, xnew, omega, bx, k, st);
+}
 
 // ------------------------------------------------------------------ transfers
 // Products in the transfers are rounded on their own (no fused multiply-add), as
