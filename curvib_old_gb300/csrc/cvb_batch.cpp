@@ -176,6 +176,20 @@ double *lvec<double>(LevelDev &L, int which) {
   return which == 0 ? L.r64 : which == 1 ? L.e64 : which == 2 ? L.t64 : L.t64 + n;
 }
 
+// r = b - A x on one level: the FP32 kernel marches tiles of 31 x 7 cells in k,
+// the FP64 one takes 32 x 4 cells per plane.
+template <typename T>
+static void add_residual(VSink &vs, long long key, LevelDev &L, const LevelDev *dLv, const T *x, const T *b, T *r,
+                         const int *gate) {
+  if (sizeof(T) == 4) {
+    const MarchGrid m = MarchGrid::of(L.g);
+    vs.add(key, OK_RES32, task(dLv, x, b, r, gate, m.gx, m.gy), m.blocks());
+  } else {
+    const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
+    vs.add(key, OK_RES64, task(dLv, x, b, r, gate, gx, gy), gx * gy * L.g.mz);
+  }
+}
+
 template <typename T>
 static void gen_sweep(VSink &vs, long long key0, long long key1, LevelDev &L, const LevelDev *dLv, const T *b,
                       const T *x, T *xnew, bool zero, const int *gate) {
@@ -192,8 +206,7 @@ static void gen_sweep(VSink &vs, long long key0, long long key1, LevelDev &L, co
     if (async) vs.add(key1, OK_SOLVE, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
     else vs.add(key1, OK_SWEEP, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, TW), 0, 0), lblocks, ssw);
   } else if (split == 1) {
-    const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
-    vs.add(key0, f32 ? OK_RES32 : OK_RES64, task(dLv, x, b, res, gate, gx, gy), gx * gy * L.g.mz);
+    add_residual<T>(vs, key0, L, dLv, x, b, res, gate);
     if (async) vs.add(key1, OK_SOLVE, task(dLv, res, x, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
     else vs.add(key1, OK_SWEEP, task(dLv, res, x, xnew, gate, nblk(L.g.mx, TW), 0, 2), lblocks, ssw);
   } else {
@@ -219,9 +232,8 @@ static void gen_vcycle(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int 
     std::swap(x, x2);
   }
   T *res = lvec<T>(L, 3);
+  add_residual<T>(vs, key_desc(depth, 100), L, dLv, x, b, res, gate);
   const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
-  vs.add(key_desc(depth, 100), sizeof(T) == 4 ? OK_RES32 : OK_RES64, task(dLv, x, b, res, gate, gx, gy),
-         gx * gy * L.g.mz);
   T *bc = lvec<T>(C, 0), *ec = lvec<T>(C, 1);
   const int cgx = nblk(C.g.mx, 32), cgy = nblk(C.g.my, 4);
   vs.add(key_desc(depth, 101), OK_RESTRICT, task(dLv, res, nullptr, bc, gate, cgx, cgy), cgx * cgy * C.g.mz);

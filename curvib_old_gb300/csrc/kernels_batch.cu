@@ -37,12 +37,13 @@ __device__ __forceinline__ Blk3 blk3(const GTask &T, int b) {
 }
 
 // ------------------------------------------------------------ stencil phases
-__global__ void __launch_bounds__(128) kg_apply32(const __grid_constant__ TaskList tl) {
+__global__ void __launch_bounds__(256) kg_apply32(const __grid_constant__ TaskList tl) {
   const GTask &T = tl.t[find_task(tl, blockIdx.x)];
   if (gated(T.gate)) return;
   const LevelDev L = *T.L;
   Blk3 q = blk3(T, blockIdx.x);
-  apply32_body(L.g, L.gf32, L.ajf32, L.code, (const float *)T.a, (const float *)T.b, (float *)T.c, q.x, q.y, q.z);
+  apply32_march_body(L.g, L.gf32, L.ajf32, L.code, (const float *)T.a, (const float *)T.b, (float *)T.c, q.x, q.y,
+                     q.z);
 }
 __global__ void __launch_bounds__(128) kg_apply64(const __grid_constant__ TaskList tl) {
   const GTask &T = tl.t[find_task(tl, blockIdx.x)];
@@ -123,7 +124,7 @@ __global__ void kg_elem(const __grid_constant__ TaskList tl) {
 
 void glaunch_residual32(const TaskList &tl, cudaStream_t s) {
   if (!tl.n) return;
-  kg_apply32<<<tl.nblocks, dim3(32, 4), 0, s>>>(tl); count_launch();
+  kg_apply32<<<tl.nblocks, dim3(32, 8), 0, s>>>(tl); count_launch();
 }
 void glaunch_residual64(const TaskList &tl, cudaStream_t s) {
   if (!tl.n) return;

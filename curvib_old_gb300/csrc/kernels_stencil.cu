@@ -14,12 +14,17 @@ __global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restric
   apply64_body<TX>(g, w, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
-__global__ void __launch_bounds__(128) k_apply32(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
+__global__ void __launch_bounds__(256) k_apply32(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
                                                  const uint32_t *__restrict__ code, const float *__restrict__ x,
                                                  const float *__restrict__ b, float *__restrict__ y, const int *gate) {
   if (gated(gate)) return;
-  apply32_body(g, gf, aj, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
+  apply32_march_body(g, gf, aj, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
 }
+static dim3 march_grid(const Geom &g) {
+  MarchGrid m = MarchGrid::of(g);
+  return dim3(m.gx, m.gy, m.gz);
+}
+static const dim3 kMarchBlk(32, 8, 1);
 
 static dim3 grid3(const Geom &g) { return dim3(nblk(g.mx, 32), nblk(g.my, 4), g.mz); }
 static const dim3 kBlk(32, 4, 1);
@@ -37,11 +42,11 @@ void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStr
 }
 template <>
 void launch_apply<float>(const LevelDev &L, const float *x, float *y, cudaStream_t s) {
-  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, nullptr, y, L.gate); count_launch();
+  k_apply32<<<march_grid(L.g), kMarchBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, nullptr, y, L.gate); count_launch();
 }
 template <>
 void launch_residual<float>(const LevelDev &L, const float *b, const float *x, float *r, cudaStream_t s) {
-  k_apply32<<<grid3(L.g), kBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, b, r, L.gate); count_launch();
+  k_apply32<<<march_grid(L.g), kMarchBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, b, r, L.gate); count_launch();
 }
 
 template <typename T, int TW>
