@@ -259,7 +259,7 @@ def run_cvb(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+f32 (FP32 V-cycle inside FP64 FGMRES)", "data": "synthetic",
         "config": {"workload": desc, "unknowns": n_unknown, "levels": len(P.metrics), "rtol": RTOL,
-                   "solver": "FGMRES(30) + V(2,2) y-line-Jacobi multigrid, dense FP64 coarsest",
+                   "solver": "FGMRES(30) + V(1,2) multigrid, zebra y-line Gauss-Seidel (omega 1.3), dense FP64 coarsest",
                    "l2": "no flush: the finest level's operator data alone (~1 GB FP64, ~0.3 GB FP32) exceeds L2",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "p50_ms": statistics.median(lat_m), "p99_ms": float(np.percentile(lat_m, 99)),

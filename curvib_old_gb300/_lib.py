@@ -18,6 +18,7 @@ CVB_OK, CVB_NOT_CONVERGED, CVB_NAN_DETECTED, CVB_OOM, CVB_BAD_INPUT, CVB_TIMEOUT
 STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NAN_DETECTED", 3: "OOM", 4: "BAD_INPUT", 5: "TIMEOUT",
                 6: "CUDA_ERROR", 7: "NOT_SETUP"}
 FP64, MIXED = 0, 1
+JACOBI, ZEBRA = 0, 1
 
 _P = ctypes.c_void_p
 _D = ctypes.c_double
@@ -38,7 +39,7 @@ class LevelDesc(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", _I), ("rtol", _D), ("atol", _D), ("max_it", _I), ("restart", _I),
                 ("pre_sweeps", _I), ("post_sweeps", _I), ("omega", _D), ("project_rhs", _I),
-                ("warm_start", _I), ("coarse_dense_max", _I), ("cgs_refine", _I)]
+                ("warm_start", _I), ("coarse_dense_max", _I), ("cgs_refine", _I), ("smoother", _I)]
 
 
 class SolveStats(ctypes.Structure):

@@ -96,9 +96,13 @@ void glaunch_residual32(const TaskList &tl, cudaStream_t s);   // a = x, b = rhs
 void glaunch_residual64(const TaskList &tl, cudaStream_t s);   // a = x, b = rhs or null (apply), c = y
 void glaunch_restrict(const TaskList &tl, bool f32, cudaStream_t s);     // a = fine, c = coarse
 void glaunch_prolong(const TaskList &tl, bool f32, cudaStream_t s);      // a = coarse, c = fine (added)
-// line sweeps: a = rhs (or residual), b = x (null: zero guess), c = xnew, p0 = mode (kernel-specific)
+// line sweeps: a = rhs (or residual), b = x (null: zero guess), c = xnew, p0 = mode (fused sweep);
+// line solve: p1 = zebra color + 1 (0: every line)
 void glaunch_line_sweep(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);
 void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);
+// zebra: residual on the cells of color p0 (a = x, b = rhs, c = r); zero fill of c[0..p0)
+void glaunch_resid_color(const TaskList &tl, bool f32, cudaStream_t s);
+void glaunch_zero(const TaskList &tl, bool f32, cudaStream_t s);
 // dense coarsest solve: a = r, b = Minv, c = e, p0 = n
 void glaunch_dense(const TaskList &tl, bool f32, cudaStream_t s);
 // element-wise: a = src, c = dst, p0 = n; kind 0 copy f32, 1 copy f64, 2 f64->f32, 3 f32->f64

@@ -540,11 +540,36 @@ void coarse_solve<double>(cvb_ctx *ctx, const double *b, double *x, const cvb_so
   if (a != x) cudaMemcpyAsync(x, a, sizeof(double) * C.g.n(), cudaMemcpyDeviceToDevice, ctx->stream);
 }
 
+template <typename T>
+static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o);
+
+// The V-cycle with zebra smoothing: x (= out) is updated in place, each sweep
+// one half-sweep per color.
+template <typename T>
+static void vcycle_zebra(cvb_ctx *ctx, int l, const T *b, T *x, const cvb_solve_opts *o) {
+  cudaStream_t s = ctx->stream;
+  LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
+  T *res = vptr<T>(L, 3);
+  const T omega = (T)o->omega;
+  cudaMemsetAsync(x, 0, sizeof(T) * L.g.n(), s);
+  const int pre = std::max(o->pre_sweeps, 1);
+  for (int q = 0; q < pre; q++)
+    for (int c = 0; c < 2; c++) launch_zebra_half<T>(L, b, x, res, omega, c, q == 0 && c == 0, s);
+  launch_residual<T>(L, b, x, res, s);
+  T *bc = vptr<T>(C, 0), *ec = vptr<T>(C, 1);
+  launch_restrict<T>(L, C, res, bc, s);
+  vcycle<T>(ctx, l - 1, bc, ec, o);
+  launch_prolong_add<T>(C, L, ec, x, s);
+  for (int q = 0; q < o->post_sweeps; q++)
+    for (int c = 0; c < 2; c++) launch_zebra_half<T>(L, b, x, res, omega, c, false, s);
+}
+
 // One V-cycle on level l for A e = b, zero initial guess; result in `out`.
 template <typename T>
 static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o) {
   cudaStream_t s = ctx->stream;
   if (l == 0) { coarse_solve<T>(ctx, b, out, o); return; }
+  if (o->smoother == CVB_SMOOTHER_ZEBRA) { vcycle_zebra<T>(ctx, l, b, out, o); return; }
   LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
   size_t n = L.g.n();
   T *x = out, *x2 = vptr<T>(L, 2);
@@ -578,11 +603,12 @@ static int vcycle_graph(cvb_ctx *ctx, const cvb_solve_opts *o, int slot, const T
   const int key = (sizeof(T) == 4 ? 1000 : 0) + slot;
   VGraph &g = ctx->vgraphs[key];
   const bool same = g.omega == o->omega && g.pre == o->pre_sweeps && g.post == o->post_sweeps && g.b == (const void *)b &&
-                    g.out == (void *)out;
+                    g.out == (void *)out && g.smoother == o->smoother;
   if (!same) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = VGraph();
     g.omega = o->omega; g.pre = o->pre_sweeps; g.post = o->post_sweeps; g.b = b; g.out = out;
+    g.smoother = o->smoother;
   }
   if (g.exec) {
     CK(cudaGraphLaunch(g.exec, ctx->stream));
@@ -797,7 +823,8 @@ static int solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats
   cvb_solve_opts def;
   if (!o) { cvb_solve_opts_default(&def); o = &def; }
   if (o->restart < 1 || o->restart > kMaxRestart || o->max_it < 0 || !(o->rtol >= 0) || o->pre_sweeps < 0 ||
-      o->post_sweeps < 0 || (o->precision != CVB_PRECISION_FP64 && o->precision != CVB_PRECISION_MIXED))
+      o->post_sweeps < 0 || (o->precision != CVB_PRECISION_FP64 && o->precision != CVB_PRECISION_MIXED) ||
+      (o->smoother != CVB_SMOOTHER_JACOBI && o->smoother != CVB_SMOOTHER_ZEBRA))
     return fail(ctx, CVB_BAD_INPUT, "bad solve options");
   cvb_solve_stats local;
   if (!st) st = &local;
@@ -878,13 +905,14 @@ int cvb_solve_opts_default(cvb_solve_opts *o) {
   o->atol = 0.0;
   o->max_it = 200;
   o->restart = 30;
-  o->pre_sweeps = 2;
+  o->pre_sweeps = 1;
   o->post_sweeps = 2;
-  o->omega = 0.9;
+  o->omega = 1.3;
   o->project_rhs = 1;
   o->warm_start = 0;
   o->coarse_dense_max = 2048;
   o->cgs_refine = 0;
+  o->smoother = CVB_SMOOTHER_ZEBRA;
   return CVB_OK;
 }
 

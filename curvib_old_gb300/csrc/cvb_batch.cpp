@@ -60,7 +60,7 @@ struct Done {
 // Sink of the ops of one round, grouped by schedule key and kernel kind.
 enum OpKind {
   OK_RES32, OK_RES64, OK_RESTRICT, OK_PROLONG, OK_SWEEP, OK_SOLVE, OK_DENSE, OK_COPY, OK_CONV, OK_WIDEN,
-  OK_COUNT
+  OK_ZERO, OK_RESC, OK_COUNT
 };
 
 struct OpBatch {
@@ -214,11 +214,65 @@ static void gen_sweep(VSink &vs, long long key0, long long key1, LevelDev &L, co
   }
 }
 
+// One zebra half-sweep of color `color`, in place on x (keys k0: residual, k1: solve).
+template <typename T>
+static void gen_zebra_half(VSink &vs, long long k0, long long k1, LevelDev &L, const LevelDev *dLv, const T *b, T *x,
+                           int color, bool zero, const int *gate) {
+  const bool f32 = sizeof(T) == 4;
+  const int SW = f32 ? kSolveTW32 : kSolveTW64;
+  const size_t sso = f32 ? line_solve_smem<float, kSolveTW32>(L.g) : line_solve_smem<double, kSolveTW64>(L.g);
+  T *res = lvec<T>(L, 3);
+  const T *r = b;
+  if (!zero) {
+    const int gx = color_tiles_x(L.g), gy = nblk(L.g.my, 4);
+    vs.add(k0, OK_RESC, task(dLv, x, b, res, gate, gx, gy, color), gx * gy * L.g.mz);
+    r = res;
+  }
+  const int gx = f32 ? solve_tiles_x<kSolveTW32>(L.g, color) : solve_tiles_x<kSolveTW64>(L.g, color);
+  (void)SW;
+  vs.add(k1, OK_SOLVE, task(dLv, r, zero ? nullptr : x, x, gate, gx, 0, 0, color + 1), gx * L.g.mz, sso);
+}
+
+template <typename T>
+static void gen_vcycle(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int depth, const T *b, T *out,
+                       const cvb_solve_opts &o, const int *gate);
+
+template <typename T>
+static void gen_vcycle_zebra(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int depth, const T *b, T *x,
+                             const cvb_solve_opts &o, const int *gate) {
+  LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
+  const LevelDev *dLv = dLs + l;
+  const size_t n = L.g.n();
+  vs.add(key_desc(depth, 0), OK_ZERO, task(dLv, nullptr, nullptr, x, gate, elem_blocks(n), 0, (int)n),
+         elem_blocks(n));
+  const int pre = std::max(o.pre_sweeps, 1);
+  for (int q = 0; q < pre; q++)
+    for (int c = 0; c < 2; c++)
+      gen_zebra_half<T>(vs, key_desc(depth, 1 + 10 * q + 3 * c), key_desc(depth, 2 + 10 * q + 3 * c), L, dLv, b, x, c,
+                        q == 0 && c == 0, gate);
+  T *res = lvec<T>(L, 3);
+  add_residual<T>(vs, key_desc(depth, 100), L, dLv, x, b, res, gate);
+  T *bc = lvec<T>(C, 0), *ec = lvec<T>(C, 1);
+  const int cgx = nblk(C.g.mx, 32), cgy = nblk(C.g.my, 4);
+  vs.add(key_desc(depth, 101), OK_RESTRICT, task(dLv, res, nullptr, bc, gate, cgx, cgy), cgx * cgy * C.g.mz);
+  gen_vcycle<T>(vs, ctx, dLs, l - 1, depth + 1, bc, ec, o, gate);
+  const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
+  vs.add(key_asc(depth, 0), OK_PROLONG, task(dLv, ec, nullptr, x, gate, gx, gy), gx * gy * L.g.mz);
+  for (int q = 0; q < o.post_sweeps; q++)
+    for (int c = 0; c < 2; c++)
+      gen_zebra_half<T>(vs, key_asc(depth, 1 + 10 * q + 3 * c), key_asc(depth, 2 + 10 * q + 3 * c), L, dLv, b, x, c,
+                        false, gate);
+}
+
 template <typename T>
 static void gen_vcycle(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int depth, const T *b, T *out,
                        const cvb_solve_opts &o, const int *gate) {
   if (l == 0) {
     vs.add(key_coarse(), OK_DENSE, task(dLs, b, ctx->Minv, out, gate, 0, 0, ctx->ncoarse), nblk(ctx->ncoarse, 8));
+    return;
+  }
+  if (o.smoother == CVB_SMOOTHER_ZEBRA) {
+    gen_vcycle_zebra<T>(vs, ctx, dLs, l, depth, b, out, o, gate);
     return;
   }
   LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
@@ -269,6 +323,8 @@ static void run_program(cvb_batch *bt, std::map<long long, std::array<Lists, OK_
           case OK_COPY: glaunch_elementwise(ob.tl, f32 ? 0 : 1, s); break;
           case OK_CONV: glaunch_elementwise(ob.tl, 2, s); break;
           case OK_WIDEN: glaunch_elementwise(ob.tl, 3, s); break;
+          case OK_ZERO: glaunch_zero(ob.tl, f32, s); break;
+          case OK_RESC: glaunch_resid_color(ob.tl, f32, s); break;
           default: break;
         }
       }
@@ -599,7 +655,8 @@ int cvb_batch_create(cvb_batch **out, const cvb_options *opts, const cvb_solve_o
   if (so) bt->opts = *so;
   const cvb_solve_opts &o = bt->opts;
   if (o.restart < 1 || o.restart > kBatchRestart || o.max_it < 0 || o.pre_sweeps < 0 || o.post_sweeps < 0 ||
-      (o.precision != CVB_PRECISION_FP64 && o.precision != CVB_PRECISION_MIXED)) {
+      (o.precision != CVB_PRECISION_FP64 && o.precision != CVB_PRECISION_MIXED) ||
+      (o.smoother != CVB_SMOOTHER_JACOBI && o.smoother != CVB_SMOOTHER_ZEBRA)) {
     delete bt;
     return CVB_BAD_INPUT;
   }

@@ -42,7 +42,7 @@ struct VGraph {
   int nodes = 0, uses = 0;
   bool failed = false;
   double omega = -1.0;
-  int pre = -1, post = -1;
+  int pre = -1, post = -1, smoother = -1;
   const void *b = nullptr;
   void *out = nullptr;
 };

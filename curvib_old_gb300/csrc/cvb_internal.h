@@ -97,6 +97,9 @@ void launch_residual(const LevelDev &L, const T *b, const T *x, T *r, cudaStream
 template <typename T>
 void launch_line_smooth(const LevelDev &L, const T *b, const T *x, T *xnew, T omega, int zero_guess,
                         cudaStream_t s);
+// zebra half-sweep of one color, in place (res: scratch for the residual)
+template <typename T>
+void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s);
 template <typename T>
 void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s);
 template <typename T>

@@ -84,7 +84,38 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_c
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const LevelDev L = *K.L;
   int lb = blockIdx.x - K.block0;
-  line_solve_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw);
+  line_solve_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw,
+                         K.p1 - 1);
+}
+// zebra: residual on the cells of color p0
+template <typename T>
+__global__ void __launch_bounds__(128) kg_resid_color(const __grid_constant__ TaskList tl) {
+  const GTask &K = tl.t[find_task(tl, blockIdx.x)];
+  if (gated(K.gate)) return;
+  const LevelDev L = *K.L;
+  Blk3 q = blk3(K, blockIdx.x);
+  resid_color_body<T>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, K.p0, q.x, q.y, q.z);
+}
+// c[0 .. p0) = 0
+template <typename T>
+__global__ void kg_zero(const __grid_constant__ TaskList tl) {
+  const GTask &K = tl.t[find_task(tl, blockIdx.x)];
+  if (gated(K.gate)) return;
+  T *c = (T *)K.c;
+  const size_t n = (size_t)K.p0;
+  for (size_t p = (size_t)(blockIdx.x - K.block0) * 256 + threadIdx.x; p < n; p += (size_t)K.gx * 256) c[p] = T(0);
+}
+void glaunch_resid_color(const TaskList &tl, bool f32, cudaStream_t s) {
+  if (!tl.n) return;
+  if (f32) kg_resid_color<float><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
+  else kg_resid_color<double><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
+  count_launch();
+}
+void glaunch_zero(const TaskList &tl, bool f32, cudaStream_t s) {
+  if (!tl.n) return;
+  if (f32) kg_zero<float><<<tl.nblocks, 256, 0, s>>>(tl);
+  else kg_zero<double><<<tl.nblocks, 256, 0, s>>>(tl);
+  count_launch();
 }
 // e = Minv r on the coarsest level's inverted cells, e = r on the others; one
 // warp per row (8 rows per block)

@@ -58,12 +58,18 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
 }
 
 template <typename T, int TW>
-__global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r,
-                                                                 const T *__restrict__ x, T *__restrict__ xnew,
-                                                                 T omega) {
+__global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
+                                                                 T *xnew, T omega, int color) {
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  line_solve_body<T, TW>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw);
+  line_solve_body<T, TW>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_resid_color(LevelDev L, const T *__restrict__ x, const T *__restrict__ b,
+                                                     T *__restrict__ r, int color) {
+  if (gated(L.gate)) return;
+  resid_color_body<T>(L, x, b, r, color, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 // mode 0: zero initial guess (residual = b); 1: residual b - A x computed in
 // the sweep (fused); 2: `b` already holds the residual of x (split variant).
@@ -81,14 +87,15 @@ static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T ome
 
 
 template <typename T, int TW>
-static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s) {
-  dim3 grd(nblk(L.g.mx, TW), L.g.mz);
+static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color = -1) {
+  dim3 grd(solve_tiles_x<TW>(L.g, color), L.g.mz);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_line_solve<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_line_solve<T, TW><<<grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s>>>(L, r, x, xnew, omega); count_launch();
+  k_line_solve<T, TW><<<grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s>>>(L, r, x, xnew, omega, color);
+  count_launch();
 }
 
 // Lines longer than the shared-memory tile allows fall back to a residual
@@ -181,6 +188,26 @@ void launch_line_smooth<double>(const LevelDev &L, const double *b, const double
   dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
   k_line_thomas<double><<<grd, blk, 0, s>>>(L.g, L.line64, r, x, xnew, omega, zero_guess, L.gate); count_launch();
 }
+
+// Zebra (two-color) y-line relaxation: one half-sweep updates the lines of one
+// color, (i + k) % 2 == color, in place: residual on those lines, then their
+// line solves.  zero: x is zero on entry (the caller zeroed it); only the
+// solves run, on r = b.
+template <typename T>
+void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s) {
+  constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
+  const T *r = b;
+  if (!zero) {
+    dim3 grd(color_tiles_x(L.g), nblk(L.g.my, 4), L.g.mz);
+    k_resid_color<T><<<grd, dim3(32, 4), 0, s>>>(L, x, b, res, color); count_launch();
+    r = res;
+  }
+  line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color);
+}
+template void launch_zebra_half<float>(const LevelDev &, const float *, float *, float *, float, int, bool,
+                                       cudaStream_t);
+template void launch_zebra_half<double>(const LevelDev &, const double *, double *, double *, double, int, bool,
+                                        cudaStream_t);
 
 // ------------------------------------------------------------------ transfers
 template <typename T>

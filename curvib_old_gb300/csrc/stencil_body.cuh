@@ -576,16 +576,22 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
 // current one -- ran slower here: with two tiles per block only two blocks fit
 // on an SM, and four independent blocks hide the copies better.)
 
+// Line of lane tx in tile bx at plane k: all lines (color < 0), or the lines of
+// one zebra color, (i + k) % 2 == color, two cells apart.
+__device__ __forceinline__ int tile_line(int bx, int tx, int k, int TW, int color) {
+  return color < 0 ? bx * TW + tx : 2 * (bx * TW + tx) + ((color + k) & 1);
+}
+
 template <typename T, int TW>
 __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
-                                                int bx, int k, T *st) {
+                                                int bx, int k, T *st, int color = -1) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   const LineLayout Lo = LineLayout::of(my);
   const int n = (int)g.n();
   T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
-  const int i = bx * TW + tx;
+  const int i = tile_line(bx, tx, k, TW, color);
   if (!(i >= 1 && i <= mx - 2 && k >= 1 && k <= g.mz - 2)) return;
   const T *fa = RowOf<T>::fac(L);
   const int col = (k * my) * mx + i;
@@ -604,13 +610,13 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
 // have landed and the block is synchronised when this is entered).
 template <typename T, int TW>
 __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__restrict__ x, T *__restrict__ xnew,
-                                                  T omega, int bx, int k, T *st) {
+                                                  T omega, int bx, int k, T *st, int color = -1) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   const LineLayout Lo = LineLayout::of(my);
   T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
-  const int i = bx * TW + tx;
+  const int i = tile_line(bx, tx, k, TW, color);
   const bool kin = k >= 1 && k <= g.mz - 2;
   const bool line = i >= 1 && i <= mx - 2 && kin;
   // every warp solves TW / 4 lines (warp, warp + 4, ...) together; lines off
@@ -637,16 +643,51 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
 }
 
 // One tile per block: issue every copy, wait once, solve, write.
+// color >= 0: zebra half-sweep on the lines of that color only, x updated in
+// place (xnew == x; a tile reads its lines' x before it writes them) -- or,
+// with x == nullptr, written on those lines only (the caller zeroed the rest).
 template <typename T, int TW>
-__device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
-                                                T *__restrict__ xnew, T omega, int bx, int k,
-                                                unsigned char *smem_raw) {
+__device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *x, T *xnew,
+                                                T omega, int bx, int k, unsigned char *smem_raw, int color = -1) {
   T *st = reinterpret_cast<T *>(smem_raw);
-  solve_tile_load<T, TW>(L, r, x, bx, k, st);
+  solve_tile_load<T, TW>(L, r, x, bx, k, st, color);
   cp_async_wait_all();
   __syncthreads();
-  solve_tile_finish<T, TW>(L, x, xnew, omega, bx, k, st);
+  solve_tile_finish<T, TW>(L, x, xnew, omega, bx, k, st, color);
 }
+
+// Tiles of a line solve: all lines or one color's.
+template <int TW>
+__host__ __device__ inline int solve_tiles_x(const Geom &g, int color) {
+  return color < 0 ? (g.mx + TW - 1) / TW : ((g.mx + 1) / 2 + TW - 1) / TW;
+}
+
+// Residual b - A x on the cells of one zebra color ((i + k) % 2 == color), one
+// thread per cell of that color, 32 x 4 threads; the other cells are not written.
+template <typename T>
+struct ColorRow;
+template <>
+struct ColorRow<float> {
+  __device__ static float r(const Geom &g, const LevelDev &L, const float *x, int i, int j, int k, int p, int n) {
+    return row32(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
+  }
+};
+template <>
+struct ColorRow<double> {
+  __device__ static double r(const Geom &g, const LevelDev &L, const double *x, int i, int j, int k, int p, int n) {
+    return row64(g, L.w64, L.code, x, i, j, k, p, n);
+  }
+};
+template <typename T>
+__device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__restrict__ x, const T *__restrict__ b,
+                                                 T *__restrict__ r, int color, int bx, int by, int k) {
+  const Geom g = L.g;
+  const int i = 2 * (bx * 32 + threadIdx.x) + ((color + k) & 1), j = by * 4 + threadIdx.y;
+  if (i >= g.mx || j >= g.my) return;
+  const int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
+  r[p] = b[p] - ColorRow<T>::r(g, L, x, i, j, k, p, n);
+}
+__host__ __device__ inline int color_tiles_x(const Geom &g) { return ((g.mx + 1) / 2 + 31) / 32; }
 
 // ------------------------------------------------------------------ transfers
 // Products in the transfers are rounded on their own (no fused multiply-add), as

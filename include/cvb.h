@@ -78,15 +78,22 @@ typedef struct {
   double atol;         /* ... or <= atol */
   int max_it;          /* total FGMRES iterations */
   int restart;         /* FGMRES restart length (<= 64) */
-  int pre_sweeps;      /* y-line Jacobi sweeps before / after the coarse correction */
+  int pre_sweeps;      /* smoothing sweeps before / after the coarse correction (zebra: one
+                          sweep = both colors) */
   int post_sweeps;
-  double omega;        /* line-Jacobi damping */
+  double omega;        /* relaxation factor (Jacobi: damping; zebra: over-relaxation) */
   int project_rhs;     /* remove b's component outside range(A) (fluid-weighted mean of b/aj) */
   int warm_start;      /* use phi's input values as the initial guess */
   int coarse_dense_max;/* largest coarsest-level box solved exactly by a dense inverse */
   int cgs_refine;      /* 1: second Gram-Schmidt pass when the first cancels most of w
                           (PETSc's KSPGMRESSetCGSRefinementType IFNEEDED); 0: never (its default) */
+  int smoother;        /* cvb_smoother: the multigrid smoother */
 } cvb_solve_opts;
+
+typedef enum {
+  CVB_SMOOTHER_JACOBI = 0, /* damped y-line Jacobi: every line from the same iterate */
+  CVB_SMOOTHER_ZEBRA = 1   /* y-line Gauss-Seidel in two colors, (i + k) even then odd, in place */
+} cvb_smoother;
 
 typedef struct {
   int status;            /* cvb_status of the solve */

@@ -48,10 +48,11 @@ def items():
         ctx.close()
 
 
-def _run(items, precision, sel=None):
+def _run(items, precision, sel=None, smoother=0):
     from curvib_old_gb300.solver import SolveBatch
     sel = range(len(items)) if sel is None else sel
-    B = SolveBatch(precision=precision, rtol=RTOL, max_it=100)
+    extra = {} if smoother == 0 else {"smoother": 1, "omega": 1.0, "pre_sweeps": 1, "post_sweeps": 1}
+    B = SolveBatch(precision=precision, rtol=RTOL, max_it=100, **extra)
     try:
         for q in sel:
             items[q][0].set_rhs(items[q][2])
@@ -63,10 +64,11 @@ def _run(items, precision, sel=None):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_alone_equals_in_mix(items, precision):
-    sts_all, phis_all = _run(items, precision)
+@pytest.mark.parametrize("smoother", [0, 1])
+def test_alone_equals_in_mix(items, precision, smoother):
+    sts_all, phis_all = _run(items, precision, smoother=smoother)
     for q in range(len(items)):
-        sts1, phis1 = _run(items, precision, [q])
+        sts1, phis1 = _run(items, precision, [q], smoother=smoother)
         assert sts1[0]["status"] == 0
         assert sts1[0]["iterations"] == sts_all[q]["iterations"]
         assert np.array_equal(phis1[0], phis_all[q]), q

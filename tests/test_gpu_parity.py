@@ -166,7 +166,8 @@ def _direct_solution(A, b, nvert):
 
 @pytest.mark.parametrize("name", ["box_sphere", "channel_periodic", "ksemi_sphere", "triply_periodic"])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_solve_matches_direct(ctxs, name, precision):
+@pytest.mark.parametrize("smoother", [0, 1])
+def test_solve_matches_direct(ctxs, name, precision, smoother):
     from curvib_old_gb300 import workload as W
     ctx, P, Ls = ctxs[name]
     L = Ls[-1]
@@ -175,7 +176,8 @@ def test_solve_matches_direct(ctxs, name, precision):
     b = W.noisy_rhs(b, L.nvert, P.metrics[-1]["Aj"], DT, seed=11)
     A = O.lhs_csr(L)
     x_ref, fl = _direct_solution(A, b, L.nvert)
-    phi, st = ctx.solve(b, precision=precision, rtol=1e-10, max_it=100)
+    phi, st = ctx.solve(b, precision=precision, rtol=1e-10, max_it=100, smoother=smoother,
+                        omega=0.9 if smoother == 0 else 1.0)
     assert st["status"] == 0 and st["rel_residual"] <= 1e-10
     r = b.ravel() - A @ phi.ravel()
     assert np.linalg.norm(r) <= 1.5e-10 * np.linalg.norm(b)
