@@ -33,5 +33,8 @@ def test_library_exports_every_declared_symbol():
 def test_default_options_without_a_gpu():
     from curvib_old_gb300 import _lib
     o = _lib.default_opts()
-    assert o.precision == _lib.MIXED and o.restart == 30 and 0 < o.omega < 1
+    assert o.precision == _lib.MIXED and o.restart == 30
+    # zebra line Gauss-Seidel, over-relaxed (SOR range 0 < omega < 2)
+    assert o.smoother == _lib.ZEBRA and 1.0 < o.omega < 2.0
+    assert (o.pre_sweeps, o.post_sweeps) == (1, 2)
     assert o.rtol == 1e-8 and o.project_rhs == 1
