@@ -98,7 +98,8 @@ EXPORTS = {
     "cvb_set_phi": ([_P, _P], _I),
     "cvb_get_phi": ([_P, _P], _I),
 }
-KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3}
+KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3, "zebra_f32": 4,
+           "zebra_f64": 5}
 
 
 def lib_path() -> Path:

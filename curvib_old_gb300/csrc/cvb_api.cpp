@@ -153,12 +153,21 @@ static void extract_box(const cvb_level_desc &d, const double *src, int dof, std
     }
 }
 
+// The owned box of an array: the array itself when its ghosted box is the owned
+// box (no copy), else extracted into `scratch`.
+static const double *box_view(const cvb_level_desc &d, const double *src, int dof, std::vector<double> &scratch) {
+  if (d.gxs == 0 && d.gys == 0 && d.gzs == 0 && d.gxm == d.mx && d.gym == d.my && d.gzm == d.mz) return src;
+  extract_box(d, src, dof, scratch);
+  return scratch.data();
+}
+
 static int upload_box(cvb_ctx *ctx, Geometry &G, const cvb_level_desc &d, const double *src, int dof,
                       double **dst) {
   std::vector<double> h;
-  extract_box(d, src, dof, h);
-  TRY(galloc(ctx, G, dst, h.size()));
-  CK(cudaMemcpyAsync(*dst, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+  const double *v = box_view(d, src, dof, h);
+  const size_t count = (size_t)d.mx * d.my * d.mz * dof;
+  TRY(galloc(ctx, G, dst, count));
+  CK(cudaMemcpyAsync(*dst, v, sizeof(double) * count, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return CVB_OK;
 }
@@ -843,7 +852,7 @@ static int solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats
 
 // Per-problem part of a set-up on the context's geometry: level arrays, the
 // finest level's nvert (owned box), operators, smoother factors, coarsest solver.
-static int setup_problem(cvb_ctx *ctx, const std::vector<double> &nvert_box) {
+static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
   const int nlevels = ctx->nlevels;
   Geometry &G = *ctx->geo;
   ctx->fm = G.fm;
@@ -872,8 +881,7 @@ static int setup_problem(cvb_ctx *ctx, const std::vector<double> &nvert_box) {
   TRY(dalloc(ctx, &ctx->nvert_tmp, nmax));
   LevelDev &F = ctx->L[nlevels - 1];
   size_t n = F.g.n();
-  if (nvert_box.size() != n) return fail(ctx, CVB_BAD_INPUT, "nvert has %zu cells, the finest box %zu", nvert_box.size(), n);
-  CK(cudaMemcpyAsync(F.nvert, nvert_box.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(F.nvert, nvert_box, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   TRY(dalloc(ctx, &ctx->b, n)); TRY(dalloc(ctx, &ctx->x, n));
   TRY(dalloc(ctx, &ctx->w, n)); TRY(dalloc(ctx, &ctx->r, n));
@@ -999,8 +1007,7 @@ int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, con
   if (nlevels < 1 || nlevels > 16 || !lv || !nvert_finest) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
   TRY(upload_geometry(ctx, nlevels, lv));
   std::vector<double> h;
-  extract_box(lv[nlevels - 1], nvert_finest, 1, h);
-  return setup_problem(ctx, h);
+  return setup_problem(ctx, box_view(lv[nlevels - 1], nvert_finest, 1, h));
 }
 
 int cvb_setup_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv) {
@@ -1024,8 +1031,7 @@ int cvb_setup_like(cvb_ctx *ctx, const cvb_ctx *donor, const double *nvert_fines
   ctx->H = H;
   ctx->geo = G;
   std::vector<double> h;
-  extract_box(ctx->H[ctx->nlevels - 1].d, nvert_finest, 1, h);
-  return setup_problem(ctx, h);
+  return setup_problem(ctx, box_view(ctx->H[ctx->nlevels - 1].d, nvert_finest, 1, h));
 }
 
 }  // extern "C"
@@ -1059,10 +1065,10 @@ int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
   if (!nvert_finest) return fail(ctx, CVB_BAD_INPUT, "nvert is NULL");
   const cvb_level_desc &df = ctx->H[ctx->nlevels - 1].d;
   std::vector<double> h;
-  extract_box(df, nvert_finest, 1, h);
+  const double *v = box_view(df, nvert_finest, 1, h);
   drop_vcycle_graphs(ctx);
-  CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice,
-                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, v, sizeof(double) * ctx->L[ctx->nlevels - 1].g.n(),
+                     cudaMemcpyHostToDevice, ctx->stream));
   TRY(build_operators(ctx));
   TRY(autotune_sweeps(ctx));
   cvb_solve_opts def;
@@ -1329,7 +1335,9 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       case CVB_KERNEL_LINE_SWEEP_F32: launch_line_smooth<float>(L, L.r32, L.e32, L.t32 + n, 0.85f, 0, ctx->stream); break;
       case CVB_KERNEL_LINE_SWEEP_F64: launch_line_smooth<double>(L, L.r64, L.e64, L.t64 + n, 0.85, 0, ctx->stream); break;
       case CVB_KERNEL_RESIDUAL_F32: launch_residual<float>(L, L.r32, L.e32, L.t32, ctx->stream); break;
-      default: launch_residual<double>(L, L.r64, L.e64, L.t64, ctx->stream); break;
+      case CVB_KERNEL_RESIDUAL_F64: launch_residual<double>(L, L.r64, L.e64, L.t64, ctx->stream); break;
+      case CVB_KERNEL_ZEBRA_F32: launch_zebra_half<float>(L, L.r32, L.e32, L.t32 + n, 1.3f, 1, false, ctx->stream); break;
+      default: launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream); break;
     }
   };
   // algorithmic bytes per cell: every array the kernel needs, touched once
@@ -1338,6 +1346,10 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
     case CVB_KERNEL_LINE_SWEEP_F64: per_cell = 8 + 8 + 152 + 4 + 24 + 8; break;      // x b w19 code fac xnew
     case CVB_KERNEL_RESIDUAL_F32: per_cell = 4 + 4 + 36 + 4 + 4 + 4; break;          // x b g9 aj code r
     case CVB_KERNEL_RESIDUAL_F64: per_cell = 8 + 8 + 152 + 4 + 8; break;             // x b w19 code r
+    // one zebra half-sweep: x read everywhere; coefficients, b, r and the line
+    // solve's r, factors, x in/out on the half of the cells of the color
+    case CVB_KERNEL_ZEBRA_F32: per_cell = 4 + 0.5 * (4 + 36 + 4 + 4 + 4) + 0.5 * (4 + 12 + 4 + 4); break;
+    case CVB_KERNEL_ZEBRA_F64: per_cell = 8 + 0.5 * (8 + 152 + 4 + 8) + 0.5 * (8 + 24 + 8 + 8); break;
     default: return fail(ctx, CVB_BAD_INPUT, "unknown kernel id %d", kernel);
   }
   CK(cudaMemsetAsync(L.r32, 0, sizeof(float) * n, ctx->stream));

@@ -2,8 +2,9 @@
 
     python -m curvib_old_gb300.kernel_timer [--cells 256x128x128] [--level -1] [--reps 20] [KERNEL ...]
 
-KERNEL is one of line_sweep_f32, line_sweep_f64, residual_f32, residual_f64
-(default: all four).  The problem is the periodic channel (x and z periodic,
+KERNEL is one of line_sweep_f32, line_sweep_f64 (a damped-Jacobi y-line sweep),
+residual_f32, residual_f64, zebra_f32, zebra_f64 (one half-sweep of the zebra
+smoother: residual on one color, then its line solves); default: all.  The problem is the periodic channel (x and z periodic,
 tanh-stretched walls in y, factor 2.5) at the given cell counts.  Each kernel's
 timed launches run inside an NVTX range named ``timed:<kernel>``, so a profiler
 can be pointed at exactly those launches (``ncu --nvtx --nvtx-include

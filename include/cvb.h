@@ -261,7 +261,9 @@ enum {
   CVB_KERNEL_LINE_SWEEP_F32 = 0, /* fused residual + y-line Thomas sweep, FP32 (mixed V-cycle) */
   CVB_KERNEL_LINE_SWEEP_F64 = 1, /* the same in FP64 (plain FP64 V-cycle) */
   CVB_KERNEL_RESIDUAL_F32 = 2,   /* b - A x, FP32 flux form */
-  CVB_KERNEL_RESIDUAL_F64 = 3    /* b - A x, FP64 stored rows */
+  CVB_KERNEL_RESIDUAL_F64 = 3,   /* b - A x, FP64 stored rows */
+  CVB_KERNEL_ZEBRA_F32 = 4,      /* one zebra half-sweep (residual on one color + its line solves), FP32 */
+  CVB_KERNEL_ZEBRA_F64 = 5       /* the same in FP64 */
 };
 /* JSON record of the set-up autotuner: per level, the measured time of the
  * fused and the split y-line sweep in each precision and the variant kept. */
