@@ -252,7 +252,8 @@ def run_cvb(args, ws, rank, local):
             "traffic": traffic_per_launch("zebra_f32", cells), "algorithmic_bytes": k_bytes,
             "avg_launch_ms": k_ms,
             "fp32_residual": {"achieved_gbs": r32_bytes / (r32_ms * 1e-3) / 1e9, "avg_launch_ms": r32_ms,
-                              "algorithmic_bytes": r32_bytes, "frac": r32_bytes / (r32_ms * 1e-3) / 1e9 / peak},
+                              "algorithmic_bytes": r32_bytes, "frac": r32_bytes / (r32_ms * 1e-3) / 1e9 / peak,
+                              "traffic": traffic_per_launch("residual_f32", cells)},
             "fp64_residual": {"achieved_gbs": k64_bytes / (k64_ms * 1e-3) / 1e9, "avg_launch_ms": k64_ms,
                               "algorithmic_bytes": k64_bytes}}
     ctx.close()
