@@ -435,9 +435,11 @@ struct LineLayout {
   __device__ int pos(int q) const { return q + (q >> sh) * (S - R); }  // q = row - 1
 };
 
-// Lines per block of the line-solve kernel (128 threads): small tiles, so that
-// four of them share an SM and one tile's copies overlap another's solve.
-constexpr int kSolveTW32 = 16, kSolveTW64 = 8, kSolveThreads = 128;
+// Lines per block of the line-solve kernel (128 threads, two lines per warp in
+// FP32): small tiles, so that six share an SM (the register limit) and one
+// tile's copies overlap another's solve.  Measured on the channel's finest
+// level: 16 lines per block 92.9 us per zebra half-sweep, 8 lines 82.1 us.
+constexpr int kSolveTW32 = 8, kSolveTW64 = 4, kSolveThreads = 128;
 
 // Dynamic shared memory of the two line kernels for a level.
 template <typename T, int TW>
