@@ -352,6 +352,7 @@ static int build_operators(cvb_ctx *ctx) {
     for (int q = 0; q < 9; q++) m[q] = ctx->fm[l][q];
     launch_gcoef(g, m, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], g9, ctx->stream);
     launch_codes(g, lv.nvert, lv.code, ctx->stream);
+    launch_weight32(g, lv.nvert, lv.wgt32, ctx->stream);
     launch_weights(g, g9, ctx->aj64[l], lv.nvert, lv.code, lv.w64, ctx->stream);
     launch_line_factors(g, lv.w64, lv.line64, lv.line32, ctx->stream);
     launch_to_f32(g9, lv.gf32, 9 * n, ctx->stream);
@@ -873,6 +874,7 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
     TRY(dalloc(ctx, &L.w64, (size_t)NSLOT * n));
     TRY(dalloc(ctx, &L.gf32, 9 * n));
     TRY(dalloc(ctx, &L.ajf32, n));
+    TRY(dalloc(ctx, &L.wgt32, n));
     TRY(dalloc(ctx, &L.line32, 3 * n));
     TRY(dalloc(ctx, &L.line64, 3 * n));
     TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, 2 * n));

@@ -17,12 +17,14 @@ enum Slot { CP, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, 
 // Per-cell switching code (built once from nvert by build_codes):
 //   bit 0       identity row (boundary ring, or nvert > 0.1)
 //   bits 1..6   face active from this row's side: E, W, N, S, T, B
+//   bit 7       blocked: nvert > 0.1 (read by the grid transfers)
 //   bits 8..19  cross-derivative form for this cell's three upper faces, 2 bits each:
 //               E: (j, k)  N: (i, k)  T: (i, j)   0 none, 1 central, 2 lower, 3 upper
 // A lower face (W/S/B) of a row is the upper face of its lower neighbour, so a
 // row reads that neighbour's code for it.
 enum : uint32_t {
   CODE_IDENTITY = 1u,
+  CODE_BLOCKED = 1u << 7,  // nvert > 0.1 (IB or solid), any cell
   CODE_ACT_E = 1u << 1, CODE_ACT_W = 1u << 2, CODE_ACT_N = 1u << 3,
   CODE_ACT_S = 1u << 4, CODE_ACT_T = 1u << 5, CODE_ACT_B = 1u << 6,
 };
@@ -55,6 +57,7 @@ struct LevelDev {
   double *w64;           // [19][N] FP64 stencil weights (rows scaled by -aj; identity rows CP=1)
   float *gf32;           // [9][N]  FP32 face coefficients g11..g33, cross terms pre-scaled by form weight
   float *ajf32;          // [N]
+  float *wgt32;          // [N]    restriction weight max(0, 1 - nvert), rounded to float
   float *line32;         // [3][N]  y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32
   double *line64;        // [3][N]  ... in FP64
   // work vectors of this level (the finest level's b/x live in the solver)
@@ -79,6 +82,8 @@ void launch_gcoef(const Geom &g, const double *const *metric /*12 Cmpnts fields:
                   const double *iaj, const double *jaj, const double *kaj, double *g9 /*[9][N]*/,
                   cudaStream_t s);
 void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s);
+// wgt32 = (float) max(0, 1 - nvert)
+void launch_weight32(const Geom &g, const double *nvert, float *wgt32, cudaStream_t s);
 // FP32 face coefficients: cross terms pre-scaled by their form's weight (after launch_codes)
 void launch_scale_cross(const Geom &g, const uint32_t *code, float *gf32, cudaStream_t s);
 void launch_weights(const Geom &g, const double *g9, const double *aj, const double *nvert,

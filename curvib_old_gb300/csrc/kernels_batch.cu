@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(128) kg_restrict(const __grid_constant__ TaskL
   if (gated(K.gate)) return;
   const LevelDev F = K.L[0], C = K.L[-1];
   Blk3 q = blk3(K, blockIdx.x);
-  restrict_body<T>(F.g, F.nvert, C.g, C.nvert, C.isc, C.jsc, C.ksc, (const T *)K.a, (T *)K.c, q.x, q.y, q.z);
+  restrict_body<T>(F, C, (const T *)K.a, (T *)K.c, q.x, q.y, q.z);
 }
 template <typename T>
 __global__ void __launch_bounds__(128) kg_prolong(const __grid_constant__ TaskList tl) {
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(128) kg_prolong(const __grid_constant__ TaskLi
   if (gated(K.gate)) return;
   const LevelDev F = K.L[0], C = K.L[-1];
   Blk3 q = blk3(K, blockIdx.x);
-  prolong_body<T>(C.g, C.nvert, F.g, F.nvert, F.isc, F.jsc, F.ksc, (const T *)K.a, (T *)K.c, q.x, q.y, q.z);
+  prolong_body<T>(C, F, (const T *)K.a, (T *)K.c, q.x, q.y, q.z);
 }
 template <typename T, int TW>
 __global__ void __launch_bounds__(256, 2) kg_line_sweep(const __grid_constant__ TaskList tl, T omega) {

@@ -84,8 +84,19 @@ __global__ void k_codes(Geom g, const double *__restrict__ nv, uint32_t *__restr
       if (NV(i, j, k + 1) < thr && k != z_end) c |= CODE_ACT_T;
       if (NV(i, j, k - 1) < thr && k != z_str) c |= CODE_ACT_B;
     }
+    if (NV(i, j, k) > 0.1) c |= CODE_BLOCKED;
     code[p] = c;
   }
+}
+
+__global__ void k_weight32(size_t n, const double *__restrict__ nv, float *__restrict__ w) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    double wt = 1.0 - nv[p];
+    w[p] = (float)(wt > 0.0 ? wt : 0.0);
+  }
+}
+void launch_weight32(const Geom &g, const double *nvert, float *wgt32, cudaStream_t s) {
+  k_weight32<<<nblk(g.n(), 256) < 4096 ? nblk(g.n(), 256) : 4096, 256, 0, s>>>(g.n(), nvert, wgt32); count_launch();
 }
 
 void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s) {

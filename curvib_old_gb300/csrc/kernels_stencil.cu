@@ -211,28 +211,26 @@ template void launch_zebra_half<double>(const LevelDev &, const double *, double
 
 // ------------------------------------------------------------------ transfers
 template <typename T>
-__global__ void k_restrict(Geom F, const double *__restrict__ nvf, Geom C, const double *__restrict__ nvc,
-                           int isc, int jsc, int ksc, const T *__restrict__ xf, T *__restrict__ xc,
-                           const int *gate) {
-  if (gated(gate)) return;
-  restrict_body<T>(F, nvf, C, nvc, isc, jsc, ksc, xf, xc, blockIdx.x, blockIdx.y, blockIdx.z);
+__global__ void k_restrict(const __grid_constant__ LevelDev F, const __grid_constant__ LevelDev C,
+                           const T *__restrict__ xf, T *__restrict__ xc) {
+  if (gated(F.gate)) return;
+  restrict_body<T>(F, C, xf, xc, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 template <typename T>
-__global__ void k_prolong_add(Geom C, const double *__restrict__ nvc, Geom F, const double *__restrict__ nvf,
-                              int isc, int jsc, int ksc, const T *__restrict__ xc, T *__restrict__ xf,
-                              const int *gate) {
-  if (gated(gate)) return;
-  prolong_body<T>(C, nvc, F, nvf, isc, jsc, ksc, xc, xf, blockIdx.x, blockIdx.y, blockIdx.z);
+__global__ void k_prolong_add(const __grid_constant__ LevelDev C, const __grid_constant__ LevelDev F,
+                              const T *__restrict__ xc, T *__restrict__ xf) {
+  if (gated(F.gate)) return;
+  prolong_body<T>(C, F, xc, xf, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 template <typename T>
 void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s) {
-  k_restrict<T><<<grid3(C.g), kBlk, 0, s>>>(F.g, F.nvert, C.g, C.nvert, C.isc, C.jsc, C.ksc, xf, xc, F.gate); count_launch();
+  k_restrict<T><<<grid3(C.g), kBlk, 0, s>>>(F, C, xf, xc); count_launch();
 }
 template <typename T>
 void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s) {
-  k_prolong_add<T><<<grid3(F.g), kBlk, 0, s>>>(C.g, C.nvert, F.g, F.nvert, F.isc, F.jsc, F.ksc, xc, xf, F.gate); count_launch();
+  k_prolong_add<T><<<grid3(F.g), kBlk, 0, s>>>(C, F, xc, xf); count_launch();
 }
 template void launch_restrict<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t);
 template void launch_restrict<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t);

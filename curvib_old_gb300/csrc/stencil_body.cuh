@@ -702,23 +702,40 @@ __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 // MyRestriction (poisson.c:129-226): coarse = 0.125 * sum over the 8 children of
 // x * max(0, 1 - nvert_fine); zero on the ring and on blocked coarse cells.
+// Restriction weight of a fine cell, max(0, 1 - nvert): FP64 from nvert (as the
+// reference), FP32 from the set-up copy of the same value rounded to float.
 template <typename T>
-__device__ __forceinline__ void restrict_body(const Geom &F, const double *__restrict__ nvf, const Geom &C,
-                                              const double *__restrict__ nvc, int isc, int jsc, int ksc,
-                                              const T *__restrict__ xf, T *__restrict__ xc, int bx, int by, int bz) {
+struct FineWeight;
+template <>
+struct FineWeight<double> {
+  __device__ static double w(const LevelDev &F, size_t q) {
+    double wt = 1.0 - F.nvert[q];
+    return wt > 0.0 ? wt : 0.0;
+  }
+};
+template <>
+struct FineWeight<float> {
+  __device__ static float w(const LevelDev &F, size_t q) { return F.wgt32[q]; }
+};
+
+template <typename T>
+__device__ __forceinline__ void restrict_body(const LevelDev &F, const LevelDev &C, const T *__restrict__ xf,
+                                              T *__restrict__ xc, int bx, int by, int bz) {
+  const Geom Fg = F.g, Cg = C.g;
   int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= C.mx || j >= C.my) return;
-  size_t p = C.id(i, j, k);
-  if (i == 0 || i == C.mx - 1 || j == 0 || j == C.my - 1 || k == 0 || k == C.mz - 1 || nvc[p] > 0.1) {
+  if (i >= Cg.mx || j >= Cg.my) return;
+  size_t p = Cg.id(i, j, k);
+  if (i == 0 || i == Cg.mx - 1 || j == 0 || j == Cg.my - 1 || k == 0 || k == Cg.mz - 1 ||
+      (C.code[p] & CODE_BLOCKED)) {
     xc[p] = T(0);
     return;
   }
+  const int isc = C.isc, jsc = C.jsc, ksc = C.ksc;
   int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
   int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
   auto W = [&](int a, int b, int c) {
-    size_t q = F.id(a, b, c);
-    double wt = 1.0 - nvf[q];
-    return mul_rn(xf[q], (T)(wt > 0.0 ? wt : 0.0));
+    size_t q = Fg.id(a, b, c);
+    return mul_rn(xf[q], FineWeight<T>::w(F, q));
   };
   T s = W(ih, jh, kh);
   s = add_rn(s, W(ih - ia, jh, kh));
@@ -733,31 +750,37 @@ __device__ __forceinline__ void restrict_body(const Geom &F, const double *__res
 
 // MyInterpolation (poisson.c:228-370), added into xf: cell-centred trilinear
 // weights 27/9/9/3/9/3/3/1 over 64 toward the neighbour on the child's side,
-// falling back to injection next to walls and blocked coarse cells.
+// falling back to injection next to walls and blocked coarse cells.  The
+// blocked tests read the codes' blocked bit (nvert > 0.1); the divisions by 64
+// are multiplications by 1/64, which round identically (an exact power of two).
 template <typename T>
-__device__ __forceinline__ void prolong_body(const Geom &C, const double *__restrict__ nvc, const Geom &F,
-                                             const double *__restrict__ nvf, int isc, int jsc, int ksc,
-                                             const T *__restrict__ xc, T *__restrict__ xf, int bx, int by, int bz) {
+__device__ __forceinline__ void prolong_body(const LevelDev &C, const LevelDev &F, const T *__restrict__ xc,
+                                             T *__restrict__ xf, int bx, int by, int bz) {
+  const Geom Fg = F.g, Cg = C.g;
   int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= F.mx || j >= F.my) return;
-  size_t p = F.id(i, j, k);
-  if (i == 0 || i == F.mx - 1 || j == 0 || j == F.my - 1 || k == 0 || k == F.mz - 1 || nvf[p] > 0.1) return;
+  if (i >= Fg.mx || j >= Fg.my) return;
+  size_t p = Fg.id(i, j, k);
+  if (i == 0 || i == Fg.mx - 1 || j == 0 || j == Fg.my - 1 || k == 0 || k == Fg.mz - 1 ||
+      (F.code[p] & CODE_BLOCKED))
+    return;
+  const int isc = F.isc, jsc = F.jsc, ksc = F.ksc;
+  const uint32_t *cc = C.code;
   int ic, jc, kc, ia, ja, ka;
-  if (isc) { ic = i; ia = 0; } else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == F.mx - 2) ia = 0; }
-  if (jsc) { jc = j; ja = 0; } else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == F.my - 2) ja = 0; }
-  if (ksc) { kc = k; ka = 0; } else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == F.mz - 2) ka = 0; }
-  if (ka == -1 && nvc[C.id(ic, jc, kc - 1)] > 0.1) ka = 0;
-  else if (ka == 1 && nvc[C.id(ic, jc, kc + 1)] > 0.1) ka = 0;
-  if (ja == -1 && nvc[C.id(ic, jc - 1, kc)] > 0.1) ja = 0;
-  else if (ja == 1 && nvc[C.id(ic, jc + 1, kc)] > 0.1) ja = 0;
-  if (ia == -1 && nvc[C.id(ic - 1, jc, kc)] > 0.1) ia = 0;
-  else if (ia == 1 && nvc[C.id(ic + 1, jc, kc)] > 0.1) ia = 0;
-  auto X = [&](int a, int b, int c) { return xc[C.id(a, b, c)]; };
+  if (isc) { ic = i; ia = 0; } else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == Fg.mx - 2) ia = 0; }
+  if (jsc) { jc = j; ja = 0; } else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == Fg.my - 2) ja = 0; }
+  if (ksc) { kc = k; ka = 0; } else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == Fg.mz - 2) ka = 0; }
+  if (ka == -1 && (cc[Cg.id(ic, jc, kc - 1)] & CODE_BLOCKED)) ka = 0;
+  else if (ka == 1 && (cc[Cg.id(ic, jc, kc + 1)] & CODE_BLOCKED)) ka = 0;
+  if (ja == -1 && (cc[Cg.id(ic, jc - 1, kc)] & CODE_BLOCKED)) ja = 0;
+  else if (ja == 1 && (cc[Cg.id(ic, jc + 1, kc)] & CODE_BLOCKED)) ja = 0;
+  if (ia == -1 && (cc[Cg.id(ic - 1, jc, kc)] & CODE_BLOCKED)) ia = 0;
+  else if (ia == 1 && (cc[Cg.id(ic + 1, jc, kc)] & CODE_BLOCKED)) ia = 0;
+  auto X = [&](int a, int b, int c) { return xc[Cg.id(a, b, c)]; };
   T s1 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc), T(9)), mul_rn(X(ic, jc + ja, kc), T(3))),
                        mul_rn(X(ic + ia, jc, kc), T(3))), X(ic + ia, jc + ja, kc));
   T s2 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc + ka), T(9)), mul_rn(X(ic, jc + ja, kc + ka), T(3))),
                        mul_rn(X(ic + ia, jc, kc + ka), T(3))), X(ic + ia, jc + ja, kc + ka));
-  T v = add_rn(div_rn(mul_rn(s1, T(3)), T(64)), div_rn(s2, T(64)));
+  T v = add_rn(mul_rn(mul_rn(s1, T(3)), T(0.015625)), mul_rn(s2, T(0.015625)));
   xf[p] = add_rn(xf[p], v);
 }
 
