@@ -551,24 +551,26 @@ void coarse_solve<double>(cvb_ctx *ctx, const double *b, double *x, const cvb_so
 }
 
 template <typename T>
-static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o);
+static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o, bool zeroed = false);
 
 // The V-cycle with zebra smoothing: x (= out) is updated in place, each sweep
-// one half-sweep per color.
+// one half-sweep per color.  zeroed: x is already zero (the restriction into
+// this level cleared it).
 template <typename T>
-static void vcycle_zebra(cvb_ctx *ctx, int l, const T *b, T *x, const cvb_solve_opts *o) {
+static void vcycle_zebra(cvb_ctx *ctx, int l, const T *b, T *x, const cvb_solve_opts *o, bool zeroed) {
   cudaStream_t s = ctx->stream;
   LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
   T *res = vptr<T>(L, 3);
   const T omega = (T)o->omega;
-  cudaMemsetAsync(x, 0, sizeof(T) * L.g.n(), s);
+  if (!zeroed) cudaMemsetAsync(x, 0, sizeof(T) * L.g.n(), s);
   const int pre = std::max(o->pre_sweeps, 1);
   for (int q = 0; q < pre; q++)
     for (int c = 0; c < 2; c++) launch_zebra_half<T>(L, b, x, res, omega, c, q == 0 && c == 0, s);
   launch_residual<T>(L, b, x, res, s);
   T *bc = vptr<T>(C, 0), *ec = vptr<T>(C, 1);
-  launch_restrict<T>(L, C, res, bc, s);
-  vcycle<T>(ctx, l - 1, bc, ec, o);
+  const bool clear = l - 1 > 0;  // the coarsest solve writes all of ec itself
+  launch_restrict<T>(L, C, res, bc, s, clear ? ec : nullptr);
+  vcycle<T>(ctx, l - 1, bc, ec, o, clear);
   launch_prolong_add<T>(C, L, ec, x, s);
   for (int q = 0; q < o->post_sweeps; q++)
     for (int c = 0; c < 2; c++) launch_zebra_half<T>(L, b, x, res, omega, c, false, s);
@@ -576,10 +578,10 @@ static void vcycle_zebra(cvb_ctx *ctx, int l, const T *b, T *x, const cvb_solve_
 
 // One V-cycle on level l for A e = b, zero initial guess; result in `out`.
 template <typename T>
-static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o) {
+static void vcycle(cvb_ctx *ctx, int l, const T *b, T *out, const cvb_solve_opts *o, bool zeroed) {
   cudaStream_t s = ctx->stream;
   if (l == 0) { coarse_solve<T>(ctx, b, out, o); return; }
-  if (o->smoother == CVB_SMOOTHER_ZEBRA) { vcycle_zebra<T>(ctx, l, b, out, o); return; }
+  if (o->smoother == CVB_SMOOTHER_ZEBRA) { vcycle_zebra<T>(ctx, l, b, out, o, zeroed); return; }
   LevelDev &L = ctx->L[l], &C = ctx->L[l - 1];
   size_t n = L.g.n();
   T *x = out, *x2 = vptr<T>(L, 2);

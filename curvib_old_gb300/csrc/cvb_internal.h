@@ -105,8 +105,9 @@ void launch_line_smooth(const LevelDev &L, const T *b, const T *x, T *xnew, T om
 // zebra half-sweep of one color, in place (res: scratch for the residual)
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s);
+// restriction of xf into xc; zero_c, when set, is zeroed over the coarse grid too
 template <typename T>
-void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s);
+void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s, T *zero_c = nullptr);
 template <typename T>
 void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s);
 

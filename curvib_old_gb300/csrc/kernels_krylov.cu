@@ -2,7 +2,7 @@
 // removal and the coarsest-level dense solve.  Every reduction is two-stage with
 // a fixed block count and a fixed summation tree, so a solve's result does not
 // depend on timing or on what else shares the GPU.
-#include "cvb_internal.h"
+#include "launch.cuh"
 
 namespace cvb {
 
@@ -57,6 +57,7 @@ template <typename TV, int NV, bool SELF>
 __global__ void __launch_bounds__(kRedThreads) k_multidot(const TV *const *V, int base, const double *__restrict__ w,
                                                            size_t n, double *partial, int self_row,
                                                            const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   double acc[NV + 1];
 #pragma unroll
@@ -95,16 +96,15 @@ static void multidot_chunk(const TV *const *V, int base, int cnt, const double *
                            int self_row, cudaStream_t s, const int *gate = nullptr) {
   int nb = reduce_blocks();
   switch (cnt) {
-    case 1: k_multidot<TV, 1, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    case 2: k_multidot<TV, 2, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    case 3: k_multidot<TV, 3, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    case 4: k_multidot<TV, 4, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    case 5: k_multidot<TV, 5, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    case 6: k_multidot<TV, 6, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    case 7: k_multidot<TV, 7, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
-    default: k_multidot<TV, 8, SELF><<<nb, kRedThreads, 0, s>>>(V, base, w, n, partial, self_row, gate); break;
+    case 1: launch_dep(k_multidot<TV, 1, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    case 2: launch_dep(k_multidot<TV, 2, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    case 3: launch_dep(k_multidot<TV, 3, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    case 4: launch_dep(k_multidot<TV, 4, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    case 5: launch_dep(k_multidot<TV, 5, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    case 6: launch_dep(k_multidot<TV, 6, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    case 7: launch_dep(k_multidot<TV, 7, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
+    default: launch_dep(k_multidot<TV, 8, SELF>, nb, kRedThreads, 0, s, V, base, w, n, partial, self_row, gate); break;
   }
-  count_launch();
 }
 
 // Dots of w with V_0..V_{nv-1} in chunks of up to 8 vectors (each chunk reads w
@@ -125,6 +125,7 @@ void launch_multidot_f32(const float *const *V, int nv, const double *w, size_t 
 // out[q] = sum_b partial[q][b], one block per q, fixed tree.
 __global__ void k_finish(const double *__restrict__ partial, int nblocks, double *__restrict__ out,
                          const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   __shared__ double sh[kRedThreads];
   int q = blockIdx.x;
@@ -139,13 +140,14 @@ __global__ void k_finish(const double *__restrict__ partial, int nblocks, double
   if (threadIdx.x == 0) out[q] = sh[0];
 }
 void launch_finish_sums(const double *partial, int nv, int nblocks, double *out, cudaStream_t s, const int *gate) {
-  k_finish<<<nv, kRedThreads, 0, s>>>(partial, nblocks, out, gate); count_launch();
+  launch_dep(k_finish, nv, kRedThreads, 0, s, partial, nblocks, out, gate);
 }
 
 // w -= sum_q h[q] V_q ; partial[block] = sum of w^2 over the block.
 __global__ void __launch_bounds__(kRedThreads) k_multiaxpy_norm(double *__restrict__ w, const double *const *V,
                                                                  const double *__restrict__ h, int nv, size_t n,
                                                                  double *partial, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   __shared__ double hs[64];
   if (threadIdx.x < nv) hs[threadIdx.x] = h[threadIdx.x];
@@ -162,12 +164,13 @@ __global__ void __launch_bounds__(kRedThreads) k_multiaxpy_norm(double *__restri
 }
 void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_dev, int nv, size_t n,
                            double *partial, cudaStream_t s, const int *gate) {
-  k_multiaxpy_norm<<<reduce_blocks(), kRedThreads, 0, s>>>(w, V, h_dev, nv, n, partial, gate); count_launch();
+  launch_dep(k_multiaxpy_norm, reduce_blocks(), kRedThreads, 0, s, w, V, h_dev, nv, n, partial, gate);
 }
 
 // dst = src / *scal
 __global__ void k_scale(double *__restrict__ dst, const double *__restrict__ src, const double *__restrict__ scal,
                         size_t n, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   double inv = 1.0 / *scal;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
@@ -175,12 +178,13 @@ __global__ void k_scale(double *__restrict__ dst, const double *__restrict__ src
 }
 void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
                   const int *gate) {
-  k_scale<<<reduce_blocks(), 256, 0, s>>>(dst, src, scal_dev, n, gate); count_launch();
+  launch_dep(k_scale, reduce_blocks(), 256, 0, s, dst, src, scal_dev, n, gate);
 }
 
 // x += sum_q y[q] Z_q (Z stored FP32 in mixed mode, FP64 in plain mode)
 __global__ void k_axpy_z(double *__restrict__ x, const float *const *Z32, const double *const *Z64,
                          const double *__restrict__ y, int nz, size_t n) {
+  dep_sync();
   __shared__ double ys[64];
   if (threadIdx.x < nz) ys[threadIdx.x] = y[threadIdx.x];
   __syncthreads();
@@ -195,13 +199,14 @@ __global__ void k_axpy_z(double *__restrict__ x, const float *const *Z32, const 
 }
 void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev, int nz,
                    size_t n, cudaStream_t s) {
-  k_axpy_z<<<reduce_blocks(), 256, 0, s>>>(x, Z32, Z64, y_dev, nz, n); count_launch();
+  launch_dep(k_axpy_z, reduce_blocks(), 256, 0, s, x, Z32, Z64, y_dev, nz, n);
 }
 
 // Null space (PoissonNullSpaceFunction, poisson.c:411-558): sums and counts of x
 // over interior fluid cells (nvert < 0.1).
 __global__ void __launch_bounds__(kRedThreads) k_fluid_sum(Geom g, const double *__restrict__ nv,
                                                            const double *__restrict__ x, double *partial) {
+  dep_sync();
   double acc[2] = {0.0, 0.0};
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
@@ -214,12 +219,13 @@ __global__ void __launch_bounds__(kRedThreads) k_fluid_sum(Geom g, const double 
   block_reduce_store<2>(acc, partial, gridDim.x, 0);
 }
 void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial, cudaStream_t s) {
-  k_fluid_sum<<<reduce_blocks(), kRedThreads, 0, s>>>(g, nvert, x, partial); count_launch();
+  launch_dep(k_fluid_sum, reduce_blocks(), kRedThreads, 0, s, g, nvert, x, partial);
 }
 // x += -sum/count on interior fluid cells; with zero_outside the ring and the
 // non-fluid cells are set to zero.
 __global__ void k_add_fluid_const(Geom g, const double *__restrict__ nv, double *__restrict__ x,
                                   const double *__restrict__ sc, int zero_outside) {
+  dep_sync();
   double shift = sc[1] > 0.0 ? sc[0] / (-1.0 * sc[1]) : 0.0;
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
@@ -231,12 +237,13 @@ __global__ void k_add_fluid_const(Geom g, const double *__restrict__ nv, double 
 }
 void launch_add_fluid_const(const Geom &g, const double *nvert, double *x, const double *sumcnt, int zero_outside,
                             cudaStream_t s) {
-  k_add_fluid_const<<<reduce_blocks(), 256, 0, s>>>(g, nvert, x, sumcnt, zero_outside); count_launch();
+  launch_dep(k_add_fluid_const, reduce_blocks(), 256, 0, s, g, nvert, x, sumcnt, zero_outside);
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_fluid_ratio(Geom g, const double *__restrict__ nv,
                                                              const double *__restrict__ b, const double *__restrict__ aj,
                                                              double *partial) {
+  dep_sync();
   double acc[3] = {0.0, 0.0, 0.0};
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
@@ -251,10 +258,11 @@ __global__ void __launch_bounds__(kRedThreads) k_fluid_ratio(Geom g, const doubl
 }
 void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double *b, const double *aj,
                                 double *partial, cudaStream_t s) {
-  k_fluid_ratio<<<reduce_blocks(), kRedThreads, 0, s>>>(g, nvert, b, aj, partial); count_launch();
+  launch_dep(k_fluid_ratio, reduce_blocks(), kRedThreads, 0, s, g, nvert, b, aj, partial);
 }
 __global__ void k_remove_aj_mean(Geom g, const double *__restrict__ nv, const double *__restrict__ aj,
                                  double *__restrict__ b, const double *__restrict__ sums) {
+  dep_sync();
   double c = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
@@ -265,7 +273,7 @@ __global__ void k_remove_aj_mean(Geom g, const double *__restrict__ nv, const do
 }
 void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
                            cudaStream_t s) {
-  k_remove_aj_mean<<<reduce_blocks(), 256, 0, s>>>(g, nvert, aj, b, sums); count_launch();
+  launch_dep(k_remove_aj_mean, reduce_blocks(), 256, 0, s, g, nvert, aj, b, sums);
 }
 
 // Coarsest level: e = Minv r with a dense FP64 inverse over the cells idx[0..m)
@@ -288,18 +296,19 @@ __device__ __forceinline__ void dense_rows(const double *__restrict__ M, const i
 template <typename T>
 __global__ void k_dense(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
                         const T *__restrict__ r, T *__restrict__ e, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   dense_rows<T>(M, idx, m, n, r, e, blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5));
 }
 void launch_dense_apply(const LevelDev &C, const double *Minv, const double *r, double *e, cudaStream_t s,
                         const int *gate) {
   int n = (int)C.g.n();
-  k_dense<double><<<(n + 7) / 8, 256, 0, s>>>(Minv, C.cidx, C.cm, n, r, e, gate); count_launch();
+  launch_dep(k_dense<double>, (n + 7) / 8, 256, 0, s, Minv, C.cidx, C.cm, n, r, e, gate);
 }
 void launch_dense_apply_f32(const LevelDev &C, const double *Minv, const float *r, float *e, cudaStream_t s,
                             const int *gate) {
   int n = (int)C.g.n();
-  k_dense<float><<<(n + 7) / 8, 256, 0, s>>>(Minv, C.cidx, C.cm, n, r, e, gate); count_launch();
+  launch_dep(k_dense<float>, (n + 7) / 8, 256, 0, s, Minv, C.cidx, C.cm, n, r, e, gate);
 }
 
 }  // namespace cvb

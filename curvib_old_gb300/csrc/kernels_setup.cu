@@ -1,7 +1,7 @@
 // Set-up kernels: face coefficients, switching codes, FP64 stencil weights,
 // y-line Thomas factors and the immersed-boundary restriction of nvert.
 // Run once per problem (or whenever nvert changes); the solve reuses the result.
-#include "cvb_internal.h"
+#include "launch.cuh"
 
 namespace cvb {
 
@@ -235,24 +235,26 @@ void launch_line_factors(const Geom &g, const double *w64, double *line64, float
 }
 
 __global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
     b[p] = (float)a[p];
 }
 void launch_to_f32(const double *a, float *b, size_t n, cudaStream_t s, const int *gate) {
-  k_to_f32<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n, gate); count_launch();
+  launch_dep(k_to_f32, dim3(nblk(n, 256) < 4096 ? nblk(n, 256) : 4096), 256, 0, s, a, b, n, gate);
 }
 void launch_f64_to_f32(const double *a, float *b, size_t n, cudaStream_t s, const int *gate) {
   launch_to_f32(a, b, n, s, gate);
 }
 
 __global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, size_t n, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
     b[p] = (double)a[p];
 }
 void launch_f32_to_f64(const float *a, double *b, size_t n, cudaStream_t s, const int *gate) {
-  k_to_f64<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, s>>>(a, b, n, gate); count_launch();
+  launch_dep(k_to_f64, dim3(nblk(n, 256) < 4096 ? nblk(n, 256) : 4096), 256, 0, s, a, b, n, gate);
 }
 
 // MyNvertRestriction (poisson.c:1662-1773): a coarse cell is blocked (1) when the

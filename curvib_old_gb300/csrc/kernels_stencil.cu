@@ -10,6 +10,7 @@ template <typename TX>
 __global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restrict__ w, const uint32_t *__restrict__ code,
                                                  const TX *__restrict__ x, const double *__restrict__ b,
                                                  double *__restrict__ y, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   apply64_body<TX>(g, w, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
 }
@@ -17,6 +18,7 @@ __global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restric
 __global__ void __launch_bounds__(256) k_apply32(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
                                                  const uint32_t *__restrict__ code, const float *__restrict__ x,
                                                  const float *__restrict__ b, float *__restrict__ y, const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   apply32_march_body(g, gf, aj, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
 }
@@ -31,27 +33,28 @@ static const dim3 kBlk(32, 4, 1);
 
 template <>
 void launch_apply<double>(const LevelDev &L, const double *x, double *y, cudaStream_t s) {
-  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y, L.gate); count_launch();
+  launch_dep(k_apply64<double>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, nullptr, y, L.gate);
 }
 template <>
 void launch_residual<double>(const LevelDev &L, const double *b, const double *x, double *r, cudaStream_t s) {
-  k_apply64<double><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, b, r, L.gate); count_launch();
+  launch_dep(k_apply64<double>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, b, r, L.gate);
 }
 void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStream_t s) {
-  k_apply64<float><<<grid3(L.g), kBlk, 0, s>>>(L.g, L.w64, L.code, x, nullptr, y, L.gate); count_launch();
+  launch_dep(k_apply64<float>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, nullptr, y, L.gate);
 }
 template <>
 void launch_apply<float>(const LevelDev &L, const float *x, float *y, cudaStream_t s) {
-  k_apply32<<<march_grid(L.g), kMarchBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, nullptr, y, L.gate); count_launch();
+  launch_dep(k_apply32, march_grid(L.g), kMarchBlk, 0, s, L.g, L.gf32, L.ajf32, L.code, x, nullptr, y, L.gate);
 }
 template <>
 void launch_residual<float>(const LevelDev &L, const float *b, const float *x, float *r, cudaStream_t s) {
-  k_apply32<<<march_grid(L.g), kMarchBlk, 0, s>>>(L.g, L.gf32, L.ajf32, L.code, x, b, r, L.gate); count_launch();
+  launch_dep(k_apply32, march_grid(L.g), kMarchBlk, 0, s, L.g, L.gf32, L.ajf32, L.code, x, b, r, L.gate);
 }
 
 template <typename T, int TW>
 __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__restrict__ b, const T *__restrict__ x,
                                                        T *__restrict__ xnew, T omega, int mode) {
+  dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   line_sweep_body<T, TW>(L, b, x, xnew, omega, mode, blockIdx.x, blockIdx.y, smem_raw);
@@ -60,6 +63,7 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
 template <typename T, int TW>
 __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
                                                                  T *xnew, T omega, int color) {
+  dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   line_solve_body<T, TW>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color);
@@ -68,6 +72,7 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, con
 template <typename T>
 __global__ void __launch_bounds__(128) k_resid_color(LevelDev L, const T *__restrict__ x, const T *__restrict__ b,
                                                      T *__restrict__ r, int color) {
+  dep_sync();
   if (gated(L.gate)) return;
   resid_color_body<T>(L, x, b, r, color, blockIdx.x, blockIdx.y, blockIdx.z);
 }
@@ -82,7 +87,7 @@ static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T ome
     cudaFuncSetAttribute(k_line_sweep<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_line_sweep<T, TW><<<grd, 256, smem, s>>>(L, b, x, xnew, omega, mode); count_launch();
+  launch_dep(k_line_sweep<T, TW>, grd, 256, smem, s, L, b, x, xnew, omega, mode);
 }
 
 
@@ -94,8 +99,7 @@ static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T ome
     cudaFuncSetAttribute(k_line_solve<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_line_solve<T, TW><<<grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s>>>(L, r, x, xnew, omega, color);
-  count_launch();
+  launch_dep(k_line_solve<T, TW>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, r, x, xnew, omega, color);
 }
 
 // Lines longer than the shared-memory tile allows fall back to a residual
@@ -104,6 +108,7 @@ template <typename T>
 __global__ void k_line_thomas(Geom g, const T *__restrict__ fac, const T *__restrict__ r,
                               const T *__restrict__ x, T *__restrict__ xnew, T omega, int zero_guess,
                               const int *gate) {
+  dep_sync();
   if (gated(gate)) return;
   size_t n = g.n();
   int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
@@ -164,7 +169,7 @@ void launch_line_smooth<float>(const LevelDev &L, const float *b, const float *x
   const float *r = b;
   if (!zero_guess) { launch_residual<float>(L, b, x, L.t32, s); r = L.t32; }
   dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
-  k_line_thomas<float><<<grd, blk, 0, s>>>(L.g, L.line32, r, x, xnew, omega, zero_guess, L.gate); count_launch();
+  launch_dep(k_line_thomas<float>, grd, blk, 0, s, L.g, L.line32, r, x, xnew, omega, zero_guess, L.gate);
 }
 template <>
 void launch_line_smooth<double>(const LevelDev &L, const double *b, const double *x, double *xnew, double omega,
@@ -186,7 +191,7 @@ void launch_line_smooth<double>(const LevelDev &L, const double *b, const double
   const double *r = b;
   if (!zero_guess) { launch_residual<double>(L, b, x, L.t64, s); r = L.t64; }
   dim3 blk(32, 4), grd(nblk(L.g.mx, 32), nblk(L.g.mz, 4));
-  k_line_thomas<double><<<grd, blk, 0, s>>>(L.g, L.line64, r, x, xnew, omega, zero_guess, L.gate); count_launch();
+  launch_dep(k_line_thomas<double>, grd, blk, 0, s, L.g, L.line64, r, x, xnew, omega, zero_guess, L.gate);
 }
 
 // Zebra (two-color) y-line relaxation: one half-sweep updates the lines of one
@@ -199,7 +204,7 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
   const T *r = b;
   if (!zero) {
     dim3 grd(color_tiles_x(L.g), nblk(L.g.my, 4), L.g.mz);
-    k_resid_color<T><<<grd, dim3(32, 4), 0, s>>>(L, x, b, res, color); count_launch();
+    launch_dep(k_resid_color<T>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
     r = res;
   }
   line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color);
@@ -210,30 +215,40 @@ template void launch_zebra_half<double>(const LevelDev &, const double *, double
                                         cudaStream_t);
 
 // ------------------------------------------------------------------ transfers
+// zero_c, when set, is zeroed over the coarse grid in the same pass (the next
+// level's correction, which its V-cycle updates in place).
 template <typename T>
 __global__ void k_restrict(const __grid_constant__ LevelDev F, const __grid_constant__ LevelDev C,
-                           const T *__restrict__ xf, T *__restrict__ xc) {
+                           const T *__restrict__ xf, T *__restrict__ xc, T *__restrict__ zero_c) {
+  dep_sync();
   if (gated(F.gate)) return;
+  if (zero_c) {
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
+    if (i < C.g.mx && j < C.g.my) zero_c[C.g.id(i, j, blockIdx.z)] = T(0);
+  }
   restrict_body<T>(F, C, xf, xc, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 template <typename T>
 __global__ void k_prolong_add(const __grid_constant__ LevelDev C, const __grid_constant__ LevelDev F,
                               const T *__restrict__ xc, T *__restrict__ xf) {
+  dep_sync();
   if (gated(F.gate)) return;
   prolong_body<T>(C, F, xc, xf, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 template <typename T>
-void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s) {
-  k_restrict<T><<<grid3(C.g), kBlk, 0, s>>>(F, C, xf, xc); count_launch();
+void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s, T *zero_c) {
+  launch_dep(k_restrict<T>, grid3(C.g), kBlk, 0, s, F, C, xf, xc, zero_c);
 }
 template <typename T>
 void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s) {
-  k_prolong_add<T><<<grid3(F.g), kBlk, 0, s>>>(C, F, xc, xf); count_launch();
+  launch_dep(k_prolong_add<T>, grid3(F.g), kBlk, 0, s, C, F, xc, xf);
 }
-template void launch_restrict<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t);
-template void launch_restrict<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t);
+template void launch_restrict<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t,
+                                     float *);
+template void launch_restrict<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t,
+                                      double *);
 template void launch_prolong_add<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t);
 template void launch_prolong_add<double>(const LevelDev &, const LevelDev &, const double *, double *, cudaStream_t);
 

@@ -13,6 +13,7 @@
 //       code per cell: ~52 B/cell.
 #pragma once
 #include "cvb_internal.h"
+#include "launch.cuh"
 
 namespace cvb {
 
