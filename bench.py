@@ -239,7 +239,7 @@ def run_cvb(args, ws, rank, local):
     e2e_ms = max_over_ranks(ws, max(e0.elapsed_time(e1), wall * 1e3), torch.device("cuda", local))
 
     # roofline of the dominant kernel pair: one FP32 zebra half-sweep on the
-    # finest level (five residual + six line-solve launches per V(1,2) cycle there)
+    # finest level (seven residual + eight line-solve launches per V(2,2) cycle there)
     k_ms, k_bytes = ctx.time_kernel("zebra_f32", level=-1, reps=30)
     r32_ms, r32_bytes = ctx.time_kernel("residual_f32", level=-1, reps=30)
     k64_ms, k64_bytes = ctx.time_kernel("residual_f64", level=-1, reps=30)
@@ -264,7 +264,7 @@ def run_cvb(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+f32 (FP32 V-cycle inside FP64 FGMRES)", "data": "synthetic",
         "config": {"workload": desc, "unknowns": n_unknown, "levels": len(P.metrics), "rtol": RTOL,
-                   "solver": "FGMRES(30) + V(1,2) multigrid, zebra y-line Gauss-Seidel (omega 1.3), dense FP64 coarsest",
+                   "solver": "FGMRES(30) + V(2,2) multigrid, zebra y-line Gauss-Seidel (omega 1.3), dense FP64 coarsest",
                    "l2": "no flush: the finest level's operator data alone (~1 GB FP64, ~0.3 GB FP32) exceeds L2",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "p50_ms": statistics.median(lat_m), "p99_ms": float(np.percentile(lat_m, 99)),

@@ -99,7 +99,7 @@ EXPORTS = {
     "cvb_get_phi": ([_P, _P], _I),
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3, "zebra_f32": 4,
-           "zebra_f64": 5}
+           "zebra_f64": 5, "vcycle_f32": 6, "vcycle_f64": 7}
 
 
 def lib_path() -> Path:

@@ -917,7 +917,7 @@ int cvb_solve_opts_default(cvb_solve_opts *o) {
   o->atol = 0.0;
   o->max_it = 200;
   o->restart = 30;
-  o->pre_sweeps = 1;
+  o->pre_sweeps = 2;
   o->post_sweeps = 2;
   o->omega = 1.3;
   o->project_rhs = 1;
@@ -1328,6 +1328,48 @@ int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
   return CVB_OK;
 }
 
+// One V-cycle from `level` down with the default options: run once eagerly,
+// captured into a graph, then the graph replayed `reps` times between events.
+static int time_vcycle(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_ms, double *bytes) {
+  if (level < 1) return fail(ctx, CVB_BAD_INPUT, "a V-cycle needs a level above the coarsest");
+  cvb_solve_opts o;
+  cvb_solve_opts_default(&o);
+  LevelDev &L = ctx->L[level];
+  const size_t n = L.g.n();
+  const bool f32 = kernel == CVB_KERNEL_VCYCLE_F32;
+  auto run = [&]() {
+    if (f32) vcycle<float>(ctx, level, L.r32, L.e32, &o);
+    else vcycle<double>(ctx, level, L.r64, L.e64, &o);
+  };
+  CK(cudaMemsetAsync(L.r32, 0, sizeof(float) * n, ctx->stream));
+  CK(cudaMemsetAsync(L.r64, 0, sizeof(double) * n, ctx->stream));
+  run();
+  CKL();
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const long long c0 = launch_count();
+  run();
+  count_launch((int)(c0 - launch_count()));  // captured, not launched
+  CK(cudaStreamEndCapture(ctx->stream, &graph));
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+  for (int q = 0; q < 3; q++) cudaGraphLaunch(exec, ctx->stream);
+  cudaEventRecord(ctx->ev0, ctx->stream);
+  for (int q = 0; q < reps; q++) cudaGraphLaunch(exec, ctx->stream);
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  e = cudaEventSynchronize(ctx->ev1);
+  cudaGraphExecDestroy(exec);
+  CK(e);
+  CKL();
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  if (avg_ms) *avg_ms = ms / reps;
+  if (bytes) *bytes = 0.0;
+  return CVB_OK;
+}
+
 int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_ms, double *bytes) {
   TRY(level_ok(ctx, level));
   if (reps < 1) return fail(ctx, CVB_BAD_INPUT, "reps < 1");
@@ -1344,6 +1386,7 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       default: launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream); break;
     }
   };
+  if (kernel == CVB_KERNEL_VCYCLE_F32 || kernel == CVB_KERNEL_VCYCLE_F64) return time_vcycle(ctx, kernel, level, reps, avg_ms, bytes);
   // algorithmic bytes per cell: every array the kernel needs, touched once
   switch (kernel) {
     case CVB_KERNEL_LINE_SWEEP_F32: per_cell = 4 + 4 + 36 + 4 + 4 + 12 + 4; break;   // x b g9 aj code fac xnew

@@ -38,6 +38,7 @@ __device__ __forceinline__ Blk3 blk3(const GTask &T, int b) {
 
 // ------------------------------------------------------------ stencil phases
 __global__ void __launch_bounds__(256) kg_apply32(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &T = tl.t[find_task(tl, blockIdx.x)];
   if (gated(T.gate)) return;
   const LevelDev L = *T.L;
@@ -46,6 +47,7 @@ __global__ void __launch_bounds__(256) kg_apply32(const __grid_constant__ TaskLi
                      q.z);
 }
 __global__ void __launch_bounds__(128) kg_apply64(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &T = tl.t[find_task(tl, blockIdx.x)];
   if (gated(T.gate)) return;
   const LevelDev L = *T.L;
@@ -54,6 +56,7 @@ __global__ void __launch_bounds__(128) kg_apply64(const __grid_constant__ TaskLi
 }
 template <typename T>
 __global__ void __launch_bounds__(128) kg_restrict(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const LevelDev F = K.L[0], C = K.L[-1];
@@ -62,6 +65,7 @@ __global__ void __launch_bounds__(128) kg_restrict(const __grid_constant__ TaskL
 }
 template <typename T>
 __global__ void __launch_bounds__(128) kg_prolong(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const LevelDev F = K.L[0], C = K.L[-1];
@@ -70,6 +74,7 @@ __global__ void __launch_bounds__(128) kg_prolong(const __grid_constant__ TaskLi
 }
 template <typename T, int TW>
 __global__ void __launch_bounds__(256, 2) kg_line_sweep(const __grid_constant__ TaskList tl, T omega) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -79,6 +84,7 @@ __global__ void __launch_bounds__(256, 2) kg_line_sweep(const __grid_constant__ 
 }
 template <typename T, int TW>
 __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_constant__ TaskList tl, T omega) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -90,6 +96,7 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_c
 // zebra: residual on the cells of color p0
 template <typename T>
 __global__ void __launch_bounds__(128) kg_resid_color(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const LevelDev L = *K.L;
@@ -99,6 +106,7 @@ __global__ void __launch_bounds__(128) kg_resid_color(const __grid_constant__ Ta
 // c[0 .. p0) = 0
 template <typename T>
 __global__ void kg_zero(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   T *c = (T *)K.c;
@@ -107,15 +115,13 @@ __global__ void kg_zero(const __grid_constant__ TaskList tl) {
 }
 void glaunch_resid_color(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) kg_resid_color<float><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
-  else kg_resid_color<double><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
-  count_launch();
+  if (f32) launch_dep(kg_resid_color<float>, tl.nblocks, dim3(32, 4), 0, s, tl);
+  else launch_dep(kg_resid_color<double>, tl.nblocks, dim3(32, 4), 0, s, tl);
 }
 void glaunch_zero(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) kg_zero<float><<<tl.nblocks, 256, 0, s>>>(tl);
-  else kg_zero<double><<<tl.nblocks, 256, 0, s>>>(tl);
-  count_launch();
+  if (f32) launch_dep(kg_zero<float>, tl.nblocks, 256, 0, s, tl);
+  else launch_dep(kg_zero<double>, tl.nblocks, 256, 0, s, tl);
 }
 // e = Minv r on the coarsest level's inverted cells, e = r on the others; one
 // warp per row (8 rows per block)
@@ -136,6 +142,7 @@ __device__ __forceinline__ void dense_rows_g(const double *__restrict__ M, const
 }
 template <typename T>
 __global__ void kg_dense(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const LevelDev &C = *K.L;
@@ -144,6 +151,7 @@ __global__ void kg_dense(const __grid_constant__ TaskList tl) {
 }
 template <typename TS, typename TD>
 __global__ void kg_elem(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const TS *a = (const TS *)K.a;
@@ -155,23 +163,21 @@ __global__ void kg_elem(const __grid_constant__ TaskList tl) {
 
 void glaunch_residual32(const TaskList &tl, cudaStream_t s) {
   if (!tl.n) return;
-  kg_apply32<<<tl.nblocks, dim3(32, 8), 0, s>>>(tl); count_launch();
+  launch_dep(kg_apply32, tl.nblocks, dim3(32, 8), 0, s, tl);
 }
 void glaunch_residual64(const TaskList &tl, cudaStream_t s) {
   if (!tl.n) return;
-  kg_apply64<<<tl.nblocks, dim3(32, 4), 0, s>>>(tl); count_launch();
+  launch_dep(kg_apply64, tl.nblocks, dim3(32, 4), 0, s, tl);
 }
 void glaunch_restrict(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) kg_restrict<float><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
-  else kg_restrict<double><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
-  count_launch();
+  if (f32) launch_dep(kg_restrict<float>, tl.nblocks, dim3(32, 4), 0, s, tl);
+  else launch_dep(kg_restrict<double>, tl.nblocks, dim3(32, 4), 0, s, tl);
 }
 void glaunch_prolong(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) kg_prolong<float><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
-  else kg_prolong<double><<<tl.nblocks, dim3(32, 4), 0, s>>>(tl);
-  count_launch();
+  if (f32) launch_dep(kg_prolong<float>, tl.nblocks, dim3(32, 4), 0, s, tl);
+  else launch_dep(kg_prolong<double>, tl.nblocks, dim3(32, 4), 0, s, tl);
 }
 template <typename K>
 static void allow_smem(K kernel) {
@@ -185,9 +191,8 @@ void glaunch_line_sweep(const TaskList &tl, bool f32, float omega32, double omeg
     allow_smem(kg_line_sweep<double, 16>);
     attr = true;
   }
-  if (f32) kg_line_sweep<float, 32><<<tl.nblocks, 256, smem, s>>>(tl, omega32);
-  else kg_line_sweep<double, 16><<<tl.nblocks, 256, smem, s>>>(tl, omega64);
-  count_launch();
+  if (f32) launch_dep(kg_line_sweep<float, 32>, tl.nblocks, 256, smem, s, tl, omega32);
+  else launch_dep(kg_line_sweep<double, 16>, tl.nblocks, 256, smem, s, tl, omega64);
 }
 void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s) {
   if (!tl.n) return;
@@ -197,25 +202,22 @@ void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omeg
     allow_smem(kg_line_solve<double, kSolveTW64>);
     attr = true;
   }
-  if (f32) kg_line_solve<float, kSolveTW32><<<tl.nblocks, kSolveThreads, smem, s>>>(tl, omega32);
-  else kg_line_solve<double, kSolveTW64><<<tl.nblocks, kSolveThreads, smem, s>>>(tl, omega64);
-  count_launch();
+  if (f32) launch_dep(kg_line_solve<float, kSolveTW32>, tl.nblocks, kSolveThreads, smem, s, tl, omega32);
+  else launch_dep(kg_line_solve<double, kSolveTW64>, tl.nblocks, kSolveThreads, smem, s, tl, omega64);
 }
 void glaunch_dense(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) kg_dense<float><<<tl.nblocks, 256, 0, s>>>(tl);
-  else kg_dense<double><<<tl.nblocks, 256, 0, s>>>(tl);
-  count_launch();
+  if (f32) launch_dep(kg_dense<float>, tl.nblocks, 256, 0, s, tl);
+  else launch_dep(kg_dense<double>, tl.nblocks, 256, 0, s, tl);
 }
 void glaunch_elementwise(const TaskList &tl, int kind, cudaStream_t s) {
   if (!tl.n) return;
   switch (kind) {
-    case 0: kg_elem<float, float><<<tl.nblocks, 256, 0, s>>>(tl); break;
-    case 1: kg_elem<double, double><<<tl.nblocks, 256, 0, s>>>(tl); break;
-    case 2: kg_elem<double, float><<<tl.nblocks, 256, 0, s>>>(tl); break;
-    default: kg_elem<float, double><<<tl.nblocks, 256, 0, s>>>(tl); break;
+    case 0: launch_dep(kg_elem<float, float>, tl.nblocks, 256, 0, s, tl); break;
+    case 1: launch_dep(kg_elem<double, double>, tl.nblocks, 256, 0, s, tl); break;
+    case 2: launch_dep(kg_elem<double, float>, tl.nblocks, 256, 0, s, tl); break;
+    default: launch_dep(kg_elem<float, double>, tl.nblocks, 256, 0, s, tl); break;
   }
-  count_launch();
 }
 
 // ------------------------------------------------------------ Krylov phases
@@ -264,6 +266,7 @@ __device__ __forceinline__ void multidot_body(const BProblem &P, const double *w
 }
 
 __global__ void __launch_bounds__(kRed) kg_multidot(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -297,11 +300,12 @@ __global__ void __launch_bounds__(kRed) kg_multidot(const __grid_constant__ Task
 }
 void glaunch_multidot(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_multidot<<<tl.nblocks, kRed, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_multidot, tl.nblocks, kRed, 0, s, tl, P);
 }
 
 // sums[p1 + r] = sum_b partial[p1 + r][b], one block per row r < gx
 __global__ void __launch_bounds__(kRed) kg_finish(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -319,12 +323,13 @@ __global__ void __launch_bounds__(kRed) kg_finish(const __grid_constant__ TaskLi
 }
 void glaunch_finish(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_finish<<<tl.nblocks, kRed, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_finish, tl.nblocks, kRed, 0, s, tl, P);
 }
 
 // w -= sum_{q < nv} sums[q] V_q ; partial[kNormRow][lb] = sum of w^2 over the block
 __global__ void __launch_bounds__(kRed) kg_multiaxpy_norm(const __grid_constant__ TaskList tl,
                                                           const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -346,11 +351,12 @@ __global__ void __launch_bounds__(kRed) kg_multiaxpy_norm(const __grid_constant_
 }
 void glaunch_multiaxpy_norm(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_multiaxpy_norm<<<tl.nblocks, kRed, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_multiaxpy_norm, tl.nblocks, kRed, 0, s, tl, P);
 }
 
 // dst = src / *scal
 __global__ void kg_scale(const __grid_constant__ TaskList tl) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const double inv = 1.0 / *(const double *)K.b;
@@ -362,11 +368,12 @@ __global__ void kg_scale(const __grid_constant__ TaskList tl) {
 }
 void glaunch_scale(const TaskList &tl, cudaStream_t s) {
   if (!tl.n) return;
-  kg_scale<<<tl.nblocks, 256, 0, s>>>(tl); count_launch();
+  launch_dep(kg_scale, tl.nblocks, 256, 0, s, tl);
 }
 
 // x += sum_{q < j} y[q] Z_q with j and y from the problem's Krylov state
 __global__ void kg_update(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -382,7 +389,7 @@ __global__ void kg_update(const __grid_constant__ TaskList tl, const BProblem *_
 }
 void glaunch_update(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_update<<<tl.nblocks, 256, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_update, tl.nblocks, 256, 0, s, tl, P);
 }
 
 // Null space (PoissonNullSpaceFunction, poisson.c:411-558) on the finest level:
@@ -392,6 +399,7 @@ __device__ __forceinline__ bool fluid_cell(const Geom &g, const double *nv, size
   return i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1;
 }
 __global__ void __launch_bounds__(kRed) kg_fluid_sum(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -408,6 +416,7 @@ __global__ void __launch_bounds__(kRed) kg_fluid_sum(const __grid_constant__ Tas
   block_store<2>(acc, P.partial, P.nb, lb, rows);
 }
 __global__ void kg_add_fluid_const(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -422,6 +431,7 @@ __global__ void kg_add_fluid_const(const __grid_constant__ TaskList tl, const BP
 // range projection of b: sums of b/aj and counts over fluid cells (rows 0, 1)
 __global__ void __launch_bounds__(kRed) kg_fluid_ratio(const __grid_constant__ TaskList tl,
                                                        const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -438,6 +448,7 @@ __global__ void __launch_bounds__(kRed) kg_fluid_ratio(const __grid_constant__ T
   block_store<2>(acc, P.partial, P.nb, lb, rows);
 }
 __global__ void kg_remove_aj_mean(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
+  dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
@@ -449,24 +460,25 @@ __global__ void kg_remove_aj_mean(const __grid_constant__ TaskList tl, const BPr
 }
 void glaunch_fluid_sum(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_fluid_sum<<<tl.nblocks, kRed, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_fluid_sum, tl.nblocks, kRed, 0, s, tl, P);
 }
 void glaunch_add_fluid_const(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_add_fluid_const<<<tl.nblocks, 256, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_add_fluid_const, tl.nblocks, 256, 0, s, tl, P);
 }
 void glaunch_fluid_ratio(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_fluid_ratio<<<tl.nblocks, kRed, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_fluid_ratio, tl.nblocks, kRed, 0, s, tl, P);
 }
 void glaunch_remove_aj_mean(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;
-  kg_remove_aj_mean<<<tl.nblocks, 256, 0, s>>>(tl, P); count_launch();
+  launch_dep(kg_remove_aj_mean, tl.nblocks, 256, 0, s, tl, P);
 }
 
 // ------------------------------------------------------------ control kernels
 // One thread per problem does the scalar work (a few hundred flops at most).
 __global__ void k_init(const __grid_constant__ InitList il, const BProblem *__restrict__ PP) {
+  dep_sync();
   if (threadIdx.x != 0) return;
   const int q = blockIdx.x;
   const BProblem &P = PP[il.idx[q]];
@@ -500,10 +512,11 @@ __global__ void k_init(const __grid_constant__ InitList il, const BProblem *__re
 }
 void launch_k_init(const InitList &il, const BProblem *P, cudaStream_t s) {
   if (!il.n) return;
-  k_init<<<il.n, 32, 0, s>>>(il, P); count_launch();
+  launch_dep(k_init, il.n, 32, 0, s, il, P);
 }
 
 __global__ void k_removed(const __grid_constant__ ProbList pl, const BProblem *__restrict__ PP) {
+  dep_sync();
   if (threadIdx.x != 0) return;
   const BProblem &P = PP[pl.idx[blockIdx.x]];
   double c = P.sums[1] > 0.0 ? P.sums[0] / P.sums[1] : 0.0;
@@ -512,12 +525,13 @@ __global__ void k_removed(const __grid_constant__ ProbList pl, const BProblem *_
 }
 void launch_k_removed(const ProbList &pl, const BProblem *P, cudaStream_t s) {
   if (!pl.n) return;
-  k_removed<<<pl.n, 32, 0, s>>>(pl, P); count_launch();
+  launch_dep(k_removed, pl.n, 32, 0, s, pl, P);
 }
 
 // After r = b - A x and sums[kNormRow] = |r|^2: stop (converged, budget spent,
 // NaN) or open a new cycle with beta = |r| (V_0 = r / beta follows, gated).
 __global__ void k_cycle_start(const __grid_constant__ ProbList pl, const BProblem *__restrict__ PP) {
+  dep_sync();
   if (threadIdx.x != 0) return;
   const BProblem &P = PP[pl.idx[blockIdx.x]];
   KState *ks = P.ks;
@@ -549,13 +563,14 @@ __global__ void k_cycle_start(const __grid_constant__ ProbList pl, const BProble
 }
 void launch_k_cycle_start(const ProbList &pl, const BProblem *P, cudaStream_t s) {
   if (!pl.n) return;
-  k_cycle_start<<<pl.n, 32, 0, s>>>(pl, P); count_launch();
+  launch_dep(k_cycle_start, pl.n, 32, 0, s, pl, P);
 }
 
 // After the Gram-Schmidt sums of iteration j: H(:, j), the Givens rotations and
 // the residual estimate; closes the cycle (gate) when it converged, broke down,
 // is full or spent the iteration budget.
 __global__ void k_arnoldi(const __grid_constant__ ProbList pl, const BProblem *__restrict__ PP) {
+  dep_sync();
   if (threadIdx.x != 0) return;
   const BProblem &P = PP[pl.idx[blockIdx.x]];
   KState *ks = P.ks;
@@ -591,11 +606,12 @@ __global__ void k_arnoldi(const __grid_constant__ ProbList pl, const BProblem *_
 }
 void launch_k_arnoldi(const ProbList &pl, const BProblem *P, cudaStream_t s) {
   if (!pl.n) return;
-  k_arnoldi<<<pl.n, 32, 0, s>>>(pl, P); count_launch();
+  launch_dep(k_arnoldi, pl.n, 32, 0, s, pl, P);
 }
 
 // y = R^-1 g over the cycle's j basis vectors (back substitution).
 __global__ void k_solve_y(const __grid_constant__ ProbList pl, const BProblem *__restrict__ PP) {
+  dep_sync();
   if (threadIdx.x != 0) return;
   const BProblem &P = PP[pl.idx[blockIdx.x]];
   KState *ks = P.ks;
@@ -610,7 +626,7 @@ __global__ void k_solve_y(const __grid_constant__ ProbList pl, const BProblem *_
 }
 void launch_k_solve_y(const ProbList &pl, const BProblem *P, cudaStream_t s) {
   if (!pl.n) return;
-  k_solve_y<<<pl.n, 32, 0, s>>>(pl, P); count_launch();
+  launch_dep(k_solve_y, pl.n, 32, 0, s, pl, P);
 }
 
 }  // namespace cvb

@@ -263,7 +263,9 @@ enum {
   CVB_KERNEL_RESIDUAL_F32 = 2,   /* b - A x, FP32 flux form */
   CVB_KERNEL_RESIDUAL_F64 = 3,   /* b - A x, FP64 stored rows */
   CVB_KERNEL_ZEBRA_F32 = 4,      /* one zebra half-sweep (residual on one color + its line solves), FP32 */
-  CVB_KERNEL_ZEBRA_F64 = 5       /* the same in FP64 */
+  CVB_KERNEL_ZEBRA_F64 = 5,      /* the same in FP64 */
+  CVB_KERNEL_VCYCLE_F32 = 6,     /* one FP32 V-cycle (default options) from the level down, replayed from a CUDA graph */
+  CVB_KERNEL_VCYCLE_F64 = 7      /* the same in FP64 */
 };
 /* JSON record of the set-up autotuner: per level, the measured time of the
  * fused and the split y-line sweep in each precision and the variant kept. */

@@ -36,5 +36,5 @@ def test_default_options_without_a_gpu():
     assert o.precision == _lib.MIXED and o.restart == 30
     # zebra line Gauss-Seidel, over-relaxed (SOR range 0 < omega < 2)
     assert o.smoother == _lib.ZEBRA and 1.0 < o.omega < 2.0
-    assert (o.pre_sweeps, o.post_sweeps) == (1, 2)
+    assert (o.pre_sweeps, o.post_sweeps) == (2, 2)
     assert o.rtol == 1e-8 and o.project_rhs == 1
