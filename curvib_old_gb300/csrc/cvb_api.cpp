@@ -877,8 +877,8 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
     TRY(dalloc(ctx, &L.gf32, 9 * n));
     TRY(dalloc(ctx, &L.ajf32, n));
     TRY(dalloc(ctx, &L.wgt32, n));
-    TRY(dalloc(ctx, &L.line32, 3 * n));
-    TRY(dalloc(ctx, &L.line64, 3 * n));
+    TRY(dalloc(ctx, &L.line32, LineFac::of(L.g).count(L.g)));
+    TRY(dalloc(ctx, &L.line64, LineFac::of(L.g).count(L.g)));
     TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, 2 * n));
     TRY(dalloc(ctx, &L.r32, n)); TRY(dalloc(ctx, &L.e32, n)); TRY(dalloc(ctx, &L.t32, 2 * n));
   }

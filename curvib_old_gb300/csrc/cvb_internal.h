@@ -48,6 +48,26 @@ struct Geom {
   __host__ __device__ int kd(int k) const { return (pz && k == 1) ? mz - 2 : k - 1; }
 };
 
+// Thomas factors in global memory, line by line: line (i, k) holds a_j, 1/m_j
+// and c'_j for j = 1..my-2 as three runs of Q = my-2 rounded up to 4 values
+// (zero-padded), so that a line's factors are 16-byte aligned and contiguous.
+// Lines are ordered by plane k, then zebra colour (i + k) % 2, then i / 2: the
+// lines of one colour in one plane -- the tile of a zebra line solve -- follow
+// one another.
+struct LineFac {
+  int nt, Q;
+  __host__ __device__ static LineFac of(const Geom &g) {
+    LineFac f;
+    f.nt = (g.mx + 1) >> 1;
+    f.Q = (g.my - 2 + 3) & ~3;
+    return f;
+  }
+  __host__ __device__ size_t line(int i, int k) const {
+    return (((size_t)k * 2 + ((i + k) & 1)) * nt + (i >> 1)) * 3 * (size_t)Q;
+  }
+  __host__ __device__ size_t count(const Geom &g) const { return (size_t)g.mz * 2 * nt * 3 * Q; }
+};
+
 // Device data of one multigrid level.
 struct LevelDev {
   Geom g;
@@ -58,8 +78,8 @@ struct LevelDev {
   float *gf32;           // [9][N]  FP32 face coefficients g11..g33, cross terms pre-scaled by form weight
   float *ajf32;          // [N]
   float *wgt32;          // [N]    restriction weight max(0, 1 - nvert), rounded to float
-  float *line32;         // [3][N]  y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32
-  double *line64;        // [3][N]  ... in FP64
+  float *line32;         // y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32, LineFac layout
+  double *line64;        // ... in FP64
   // work vectors of this level (the finest level's b/x live in the solver)
   double *r64, *e64, *t64;  // FP64 V-cycle vectors
   float *r32, *e32, *t32;   // FP32 V-cycle vectors

@@ -206,9 +206,12 @@ void launch_weights(const Geom &g, const double *g9, const double *aj, const dou
 __global__ void k_line_factors(Geom g, const double *__restrict__ w, double *__restrict__ l64,
                                float *__restrict__ l32) {
   size_t n = g.n();
+  const LineFac F = LineFac::of(g);
+  const int Q = F.Q;
   int lines = g.mx * g.mz;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += gridDim.x * blockDim.x) {
     int i = t % g.mx, k = t / g.mx;
+    const size_t base = F.line(i, k);
     double cprev = 0.0;
     for (int j = 0; j < g.my; j++) {
       size_t p = g.id(i, j, k);
@@ -221,10 +224,15 @@ __global__ void k_line_factors(Geom g, const double *__restrict__ w, double *__r
       // pivot: the sweep leaves it unchanged instead of dividing by zero
       double minv = m != 0.0 ? 1.0 / m : 0.0;
       double cp = c * minv;
-      l64[p] = a; l64[n + p] = minv; l64[2 * n + p] = cp;
-      l32[p] = (float)a; l32[n + p] = (float)minv; l32[2 * n + p] = (float)cp;
+      if (j >= 1 && j <= g.my - 2) {
+        const size_t q = base + (j - 1);
+        l64[q] = a; l64[Q + q] = minv; l64[2 * Q + q] = cp;
+        l32[q] = (float)a; l32[Q + q] = (float)minv; l32[2 * Q + q] = (float)cp;
+      }
       cprev = cp;
     }
+    for (int q = g.my - 2; q < Q; q++)  // padding of the runs
+      for (int r = 0; r < 3; r++) { l64[base + r * Q + q] = 0.0; l32[base + r * Q + q] = 0.0f; }
   }
 }
 

@@ -121,13 +121,14 @@ __global__ void k_line_thomas(Geom g, const T *__restrict__ fac, const T *__rest
     }
     return;
   }
-  const T *a = fac, *minv = fac + n, *cp = fac + 2 * n;
+  const LineFac F = LineFac::of(g);
+  const T *a = fac + F.line(i, k) - 1, *minv = a + F.Q, *cp = minv + F.Q;  // indexed by j
   T dprev = T(0);
   size_t p0 = g.id(i, 0, k);
   xnew[p0] = zero_guess ? T(0) : x[p0];
   for (int j = 1; j <= g.my - 2; j++) {
     size_t p = g.id(i, j, k);
-    T d = (r[p] - a[p] * dprev) * minv[p];
+    T d = (r[p] - a[j] * dprev) * minv[j];
     xnew[p] = d;
     dprev = d;
   }
@@ -136,7 +137,7 @@ __global__ void k_line_thomas(Geom g, const T *__restrict__ fac, const T *__rest
   T dn = T(0);
   for (int j = g.my - 2; j >= 1; j--) {
     size_t p = g.id(i, j, k);
-    T d = xnew[p] - cp[p] * dn;
+    T d = xnew[p] - cp[j] * dn;
     dn = d;
     xnew[p] = zero_guess ? omega * d : x[p] + omega * d;
   }

@@ -154,15 +154,23 @@ __device__ __forceinline__ void apply64_body(const Geom &g, const double *__rest
 // coefficients and codes at the cell's own position -- as row32 does, with the
 // same operations in the same order.  About 20 loads and 3 face fluxes per
 // cell instead of 42 and 6.
-constexpr int kMarchX = 31, kMarchY = 7, kMarchK = 16;
+// A tile marches kd planes: 16 where the level has blocks to spare, fewer
+// (down to 2) until the grid has kMarchMinBlocks blocks, so that small levels
+// still spread over the SMs instead of running a few long marches.
+#ifndef CVB_MARCH_MIN_BLOCKS
+#define CVB_MARCH_MIN_BLOCKS 2432
+#endif
+constexpr int kMarchX = 31, kMarchY = 7, kMarchK = 16, kMarchMinBlocks = CVB_MARCH_MIN_BLOCKS;
 
 struct MarchGrid {
-  int gx, gy, gz;
+  int gx, gy, gz, kd;
   __host__ __device__ static MarchGrid of(const Geom &g) {
     MarchGrid m;
     m.gx = (g.mx + kMarchX - 1) / kMarchX;
     m.gy = (g.my + kMarchY - 1) / kMarchY;
-    m.gz = (g.mz + kMarchK - 1) / kMarchK;
+    m.kd = kMarchK;
+    while (m.kd > 2 && m.gx * m.gy * ((g.mz + m.kd - 1) / m.kd) < kMarchMinBlocks) m.kd >>= 1;
+    m.gz = (g.mz + m.kd - 1) / m.kd;
     return m;
   }
   __host__ __device__ int blocks() const { return gx * gy * gz; }
@@ -187,7 +195,8 @@ __device__ __forceinline__ void apply32_march_body(const Geom &g, const float *_
   const int lane = threadIdx.x, w = threadIdx.y;
   const int mx = g.mx, my = g.my, mz = g.mz, n = (int)g.n(), pl = mx * my;
   const int i = bx * kMarchX - 1 + lane, j = by * kMarchY - 1 + w;
-  const int k0 = bz * kMarchK, k1 = min(k0 + kMarchK, mz);
+  const int kd = MarchGrid::of(g).kd;
+  const int k0 = bz * kd, k1 = min(k0 + kd, mz);
   const bool col = i >= 0 && i < mx && j >= 0 && j < my;
   const bool out = col && lane >= 1 && w >= 1;
   // columns (wrapped) of the values this thread reads in every plane
@@ -366,13 +375,15 @@ __device__ __forceinline__ void line_sweep_body(const LevelDev &L, const T *__re
   const int i = i0 + tx;
   const bool kin = k >= 1 && k <= g.mz - 2;
   const T *fa = RowOf<T>::fac(L);
+  const LineFac F = LineFac::of(g);
 #pragma unroll 4
   for (int j = ty; j < my; j += ny) {
     const bool line = i >= 1 && i <= g.mx - 2 && kin;
     int p = (k * my + j) * g.mx + i;
     T r = T(0), a = T(0), m = T(1), c = T(0);
     if (line && j >= 1 && j <= my - 2) {
-      a = __ldg(fa + p); m = __ldg(fa + n + p); c = __ldg(fa + 2 * n + p);
+      const T *f = fa + F.line(i, k) + (j - 1);
+      a = __ldg(f); m = __ldg(f + F.Q); c = __ldg(f + 2 * F.Q);
       r = (mode == 1) ? b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n) : b[p];
     }
     sr[tx * my + j] = r; sa[tx * my + j] = a; sm[tx * my + j] = m; sc[tx * my + j] = c;
@@ -416,24 +427,23 @@ __device__ __forceinline__ void cp_async_el(double *dst, const double *src) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Shared-memory layout of one line for the warp solve: lane l owns rows
-// [l*R, l*R + R) and keeps them at [l*S, l*S + R) with S = R or R+1, whichever
-// is odd, so the 32 lanes of a warp hit 32 different banks.  Lines are `ls`
-// apart, ls = 32*S + 1 (odd), so a warp walking one row across 32 lines is also
-// conflict-free.
+// [l*R, l*R + R) (R a power of two) and keeps row l*R + t at t*33 + l, so at
+// each step of its serial passes a warp reads 32 consecutive words of a row of
+// 33 (no bank conflicts), and the four rows of a 16-byte load of the factors
+// land in four different banks.  Lines are ls = 33*R words apart.
 struct LineLayout {
-  int nr, R, S, ls, sh;
+  int nr, R, ls, sh;
   __host__ __device__ static LineLayout of(int my) {
     LineLayout o;
     o.nr = my - 2;
     int need = (o.nr + 31) >> 5;
     o.R = 1;
     o.sh = 0;
-    while (o.R < need) { o.R <<= 1; o.sh++; }  // a power of two: chunk arithmetic by shifts
-    o.S = o.R | 1;
-    o.ls = 32 * o.S + 1;
+    while (o.R < need) { o.R <<= 1; o.sh++; }
+    o.ls = 33 * o.R;
     return o;
   }
-  __device__ int pos(int q) const { return q + (q >> sh) * (S - R); }  // q = row - 1
+  __device__ int pos(int q) const { return (q & (R - 1)) * 33 + (q >> sh); }  // q = row - 1
 };
 
 // Lines per block of the line-solve kernel (128 threads, two lines per warp in
@@ -448,66 +458,24 @@ inline size_t line_sweep_smem(const Geom &g) { return sizeof(T) * 4 * (size_t)g.
 template <typename T, int TW>
 inline size_t line_solve_smem(const Geom &g) { return sizeof(T) * 5 * (size_t)LineLayout::of(g.my).ls * TW; }
 
-template <typename T>
-__device__ __forceinline__ void warp_line_solve_padded(T *r, const T *a, const T *m, const T *c, const LineLayout &Lo,
-                                                       int lane) {
-  const int q0 = lane * Lo.R, cnt = max(0, min(Lo.R, Lo.nr - q0));
-  const int b0 = lane * Lo.S;
-  T B = T(1), G = T(0);
-  for (int t = 0; t < cnt; t++) {
-    T mq = m[b0 + t];
-    T beta = -mq * a[b0 + t], gamma = mq * r[b0 + t];
-    B = beta * B;
-    G = beta * G + gamma;
-  }
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    T Bp = __shfl_up_sync(0xffffffffu, B, o), Gp = __shfl_up_sync(0xffffffffu, G, o);
-    if (lane >= o) { G = B * Gp + G; B = B * Bp; }
-  }
-  T d = __shfl_up_sync(0xffffffffu, G, 1);
-  if (lane == 0) d = T(0);
-  for (int t = 0; t < cnt; t++) {
-    T mq = m[b0 + t];
-    d = mq * r[b0 + t] - mq * a[b0 + t] * d;
-    r[b0 + t] = d;
-  }
-  __syncwarp();
-  B = T(1); G = T(0);
-  for (int t = cnt - 1; t >= 0; t--) {
-    T beta = -c[b0 + t], gamma = r[b0 + t];
-    B = beta * B;
-    G = beta * G + gamma;
-  }
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    T Bn = __shfl_down_sync(0xffffffffu, B, o), Gn = __shfl_down_sync(0xffffffffu, G, o);
-    if (lane + o < 32) { G = B * Gn + G; B = B * Bn; }
-  }
-  T xs = __shfl_down_sync(0xffffffffu, G, 1);
-  if (lane == 31) xs = T(0);
-  for (int t = cnt - 1; t >= 0; t--) {
-    xs = r[b0 + t] - c[b0 + t] * xs;
-    r[b0 + t] = xs;
-  }
-  __syncwarp();
-}
-
-// NL lines at once (line l at offset l * stride), interleaved: the recurrences
-// and shuffle scans of different lines are independent, so their latencies
-// overlap.  Per line the arithmetic is that of warp_line_solve_padded.
+// Solves NL lines at once with one warp (line l at offset l * stride, laid out
+// as LineLayout), interleaved: the recurrences and shuffle scans of different
+// lines are independent, so their latencies overlap.  The Thomas passes are
+// first-order affine recurrences, d_j = gamma_j + beta_j d_{j-1} (forward:
+// gamma = m r, beta = -m a; backward: gamma = d, beta = -c), and affine maps
+// compose associatively: each lane composes the maps of its R rows, a shuffle
+// scan combines the lanes, each lane replays its rows.
 template <typename T, int NL>
 __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm, const T *sc, int stride,
                                                  const LineLayout &Lo, int lane) {
   const int q0 = lane * Lo.R, cnt = max(0, min(Lo.R, Lo.nr - q0));
-  const int b0 = lane * Lo.S;
   T B[NL], G[NL], d[NL];
 #pragma unroll
   for (int l = 0; l < NL; l++) { B[l] = T(1); G[l] = T(0); }
   for (int t = 0; t < cnt; t++) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
-      const int o = l * stride + b0 + t;
+      const int o = l * stride + t * 33 + lane;
       T mq = sm[o];
       T beta = -mq * sa[o], gamma = mq * sr[o];
       B[l] = beta * B[l];
@@ -530,7 +498,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
   for (int t = 0; t < cnt; t++) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
-      const int o = l * stride + b0 + t;
+      const int o = l * stride + t * 33 + lane;
       T mq = sm[o];
       d[l] = mq * sr[o] - mq * sa[o] * d[l];
       sr[o] = d[l];
@@ -542,7 +510,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
   for (int t = cnt - 1; t >= 0; t--) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
-      const int o = l * stride + b0 + t;
+      const int o = l * stride + t * 33 + lane;
       T beta = -sc[o], gamma = sr[o];
       B[l] = beta * B[l];
       G[l] = beta * G[l] + gamma;
@@ -564,7 +532,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
   for (int t = cnt - 1; t >= 0; t--) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
-      const int o = l * stride + b0 + t;
+      const int o = l * stride + t * 33 + lane;
       d[l] = sr[o] - sc[o] * d[l];
       sr[o] = d[l];
     }
@@ -585,27 +553,72 @@ __device__ __forceinline__ int tile_line(int bx, int tx, int k, int TW, int colo
   return color < 0 ? bx * TW + tx : 2 * (bx * TW + tx) + ((color + k) & 1);
 }
 
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using V = float4;
+  static constexpr int W = 4;
+  __device__ static float at(const V &v, int u) { return u == 0 ? v.x : u == 1 ? v.y : u == 2 ? v.z : v.w; }
+};
+template <>
+struct Vec16<double> {
+  using V = double2;
+  static constexpr int W = 2;
+  __device__ static double at(const V &v, int u) { return u == 0 ? v.x : v.y; }
+};
+
+// Stage a tile: the residual (and x) rows by element copies (the lines are one
+// or two cells apart in rows of the caller's layout), the Thomas factors by
+// 16-byte loads of the lines' contiguous runs, four in flight per thread.
 template <typename T, int TW>
 __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
                                                 int bx, int k, T *st, int color = -1) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
+  if (!(k >= 1 && k <= g.mz - 2)) return;
   const LineLayout Lo = LineLayout::of(my);
-  const int n = (int)g.n();
-  T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
+  T *sr = st, *sa = sr + Lo.ls * TW, *sx = sa + 3 * Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
   const int i = tile_line(bx, tx, k, TW, color);
-  if (!(i >= 1 && i <= mx - 2 && k >= 1 && k <= g.mz - 2)) return;
+  if (i >= 1 && i <= mx - 2) {
+    const int col = (k * my) * mx + i;
+    for (int j = 1 + ty; j <= my - 2; j += ny) {
+      const int p = col + j * mx;
+      const int s = tx * Lo.ls + Lo.pos(j - 1);
+      cp_async_el(sr + s, r + p);
+      if (x) cp_async_el(sx + s, x + p);
+    }
+  }
+  using VT = Vec16<T>;
+  using V = typename VT::V;
+  constexpr int W = VT::W, U = 4;
+  const LineFac F = LineFac::of(g);
+  const int per_arr = F.Q / W, per_line = 3 * per_arr, total = TW * per_line;
   const T *fa = RowOf<T>::fac(L);
-  const int col = (k * my) * mx + i;
-  for (int j = 1 + ty; j <= my - 2; j += ny) {
-    const int p = col + j * mx;
-    const int s = tx * Lo.ls + Lo.pos(j - 1);
-    cp_async_el(sr + s, r + p);
-    cp_async_el(sa + s, fa + p);
-    cp_async_el(sm + s, fa + n + p);
-    cp_async_el(sc + s, fa + 2 * n + p);
-    if (x) cp_async_el(sx + s, x + p);
+  for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+    V v[U];
+    int dst[U], rows[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = e0 + u * blockDim.x;
+      rows[u] = 0;
+      if (e >= total) continue;
+      const int lt = e / per_line, rem = e - lt * per_line, arr = rem / per_arr, q0 = (rem - arr * per_arr) * W;
+      const int il = tile_line(bx, lt, k, TW, color);
+      if (il < 1 || il > mx - 2) continue;
+      v[u] = __ldg(reinterpret_cast<const V *>(fa + F.line(il, k) + (size_t)arr * F.Q + q0));
+      dst[u] = (arr * TW + lt) * Lo.ls;
+      rows[u] = q0 + 1;  // first row + 1 (0: nothing to store)
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (!rows[u]) continue;
+      const int q0 = rows[u] - 1;
+#pragma unroll
+      for (int w = 0; w < W; w++)
+        if (q0 + w < Lo.nr) sa[dst[u] + Lo.pos(q0 + w)] = VT::at(v[u], w);
+    }
   }
 }
 
