@@ -60,13 +60,14 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
   line_sweep_body<T, TW>(L, b, x, xnew, omega, mode, blockIdx.x, blockIdx.y, smem_raw);
 }
 
-template <typename T, int TW>
+// RR: the line layout's rows per lane fixed at compile time (0: read from my)
+template <typename T, int TW, int RR>
 __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
                                                                  T *xnew, T omega, int color) {
   dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  line_solve_body<T, TW>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color);
+  line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color);
 }
 
 template <typename T>
@@ -91,15 +92,26 @@ static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T ome
 }
 
 
-template <typename T, int TW>
-static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color = -1) {
+template <typename T, int TW, int RR>
+static void line_solve_r(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color) {
   dim3 grd(solve_tiles_x<TW>(L.g, color), L.g.mz);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_line_solve<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_line_solve<T, TW, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  launch_dep(k_line_solve<T, TW>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, r, x, xnew, omega, color);
+  launch_dep(k_line_solve<T, TW, RR>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, r, x, xnew, omega,
+             color);
+}
+template <typename T, int TW>
+static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color = -1) {
+  switch (LineLayout::of(L.g.my).R) {
+    case 1: line_solve_r<T, TW, 1>(L, r, x, xnew, omega, s, color); break;
+    case 2: line_solve_r<T, TW, 2>(L, r, x, xnew, omega, s, color); break;
+    case 4: line_solve_r<T, TW, 4>(L, r, x, xnew, omega, s, color); break;
+    case 8: line_solve_r<T, TW, 8>(L, r, x, xnew, omega, s, color); break;
+    default: line_solve_r<T, TW, 0>(L, r, x, xnew, omega, s, color); break;
+  }
 }
 
 // Lines longer than the shared-memory tile allows fall back to a residual

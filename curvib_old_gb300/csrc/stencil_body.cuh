@@ -443,8 +443,42 @@ struct LineLayout {
     o.ls = 33 * o.R;
     return o;
   }
+  // the layout with R fixed at compile time (RR > 0; the caller checked that it
+  // is the layout of `my`), else the layout of `my`
+  template <int RR>
+  __host__ __device__ static LineLayout fixed(int my) {
+    if (RR == 0) return of(my);
+    LineLayout o;
+    o.nr = my - 2;
+    o.R = RR;
+    o.sh = RR >= 16 ? 4 : RR >= 8 ? 3 : RR >= 4 ? 2 : RR >= 2 ? 1 : 0;
+    o.ls = 33 * RR;
+    return o;
+  }
   __device__ int pos(int q) const { return (q & (R - 1)) * 33 + (q >> sh); }  // q = row - 1
 };
+
+// Runs f(t) for t = 0..cnt-1 (cnt <= R): unrolled when R is a compile-time RR.
+template <int RR, typename F>
+__device__ __forceinline__ void rows_up(int cnt, F f) {
+  if constexpr (RR > 0) {
+#pragma unroll
+    for (int t = 0; t < RR; t++)
+      if (t < cnt) f(t);
+  } else {
+    for (int t = 0; t < cnt; t++) f(t);
+  }
+}
+template <int RR, typename F>
+__device__ __forceinline__ void rows_down(int cnt, F f) {
+  if constexpr (RR > 0) {
+#pragma unroll
+    for (int t = RR - 1; t >= 0; t--)
+      if (t < cnt) f(t);
+  } else {
+    for (int t = cnt - 1; t >= 0; t--) f(t);
+  }
+}
 
 // Lines per block of the line-solve kernel (128 threads, two lines per warp in
 // FP32): small tiles, so that six share an SM (the register limit) and one
@@ -465,14 +499,14 @@ inline size_t line_solve_smem(const Geom &g) { return sizeof(T) * 5 * (size_t)Li
 // gamma = m r, beta = -m a; backward: gamma = d, beta = -c), and affine maps
 // compose associatively: each lane composes the maps of its R rows, a shuffle
 // scan combines the lanes, each lane replays its rows.
-template <typename T, int NL>
+template <typename T, int NL, int RR = 0>
 __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm, const T *sc, int stride,
                                                  const LineLayout &Lo, int lane) {
   const int q0 = lane * Lo.R, cnt = max(0, min(Lo.R, Lo.nr - q0));
   T B[NL], G[NL], d[NL];
 #pragma unroll
   for (int l = 0; l < NL; l++) { B[l] = T(1); G[l] = T(0); }
-  for (int t = 0; t < cnt; t++) {
+  rows_up<RR>(cnt, [&](int t) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
@@ -481,7 +515,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
       B[l] = beta * B[l];
       G[l] = beta * G[l] + gamma;
     }
-  }
+  });
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
 #pragma unroll
@@ -495,7 +529,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
     d[l] = __shfl_up_sync(0xffffffffu, G[l], 1);
     if (lane == 0) d[l] = T(0);
   }
-  for (int t = 0; t < cnt; t++) {
+  rows_up<RR>(cnt, [&](int t) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
@@ -503,11 +537,11 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
       d[l] = mq * sr[o] - mq * sa[o] * d[l];
       sr[o] = d[l];
     }
-  }
+  });
   __syncwarp();
 #pragma unroll
   for (int l = 0; l < NL; l++) { B[l] = T(1); G[l] = T(0); }
-  for (int t = cnt - 1; t >= 0; t--) {
+  rows_down<RR>(cnt, [&](int t) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
@@ -515,7 +549,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
       B[l] = beta * B[l];
       G[l] = beta * G[l] + gamma;
     }
-  }
+  });
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
 #pragma unroll
@@ -529,14 +563,14 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
     d[l] = __shfl_down_sync(0xffffffffu, G[l], 1);
     if (lane == 31) d[l] = T(0);
   }
-  for (int t = cnt - 1; t >= 0; t--) {
+  rows_down<RR>(cnt, [&](int t) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
       d[l] = sr[o] - sc[o] * d[l];
       sr[o] = d[l];
     }
-  }
+  });
   __syncwarp();
 }
 
@@ -570,16 +604,18 @@ struct Vec16<double> {
 
 // Stage a tile: the residual (and x) rows by element copies (the lines are one
 // or two cells apart in rows of the caller's layout), the Thomas factors by
-// 16-byte loads of the lines' contiguous runs, four in flight per thread.
-template <typename T, int TW>
+// 16-byte loads of the lines' contiguous runs -- each warp takes whole runs,
+// all of its loads in flight before it stores any.
+template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
                                                 int bx, int k, T *st, int color = -1) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   if (!(k >= 1 && k <= g.mz - 2)) return;
-  const LineLayout Lo = LineLayout::of(my);
+  const LineLayout Lo = LineLayout::fixed<RR>(my);
   T *sr = st, *sa = sr + Lo.ls * TW, *sx = sa + 3 * Lo.ls * TW;
-  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
+  constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
   if (i >= 1 && i <= mx - 2) {
     const int col = (k * my) * mx + i;
@@ -592,46 +628,45 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
   }
   using VT = Vec16<T>;
   using V = typename VT::V;
-  constexpr int W = VT::W, U = 4;
+  constexpr int W = VT::W, NW = kSolveThreads / 32, RUNS = (3 * TW + NW - 1) / NW;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const LineFac F = LineFac::of(g);
-  const int per_arr = F.Q / W, per_line = 3 * per_arr, total = TW * per_line;
+  const int per_arr = F.Q / W;
   const T *fa = RowOf<T>::fac(L);
-  for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
-    V v[U];
-    int dst[U], rows[U];
+  for (int v0 = 0; v0 < per_arr; v0 += 32) {
+    const int v = v0 + lane;
+    V val[RUNS];
+    bool ok[RUNS];
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int e = e0 + u * blockDim.x;
-      rows[u] = 0;
-      if (e >= total) continue;
-      const int lt = e / per_line, rem = e - lt * per_line, arr = rem / per_arr, q0 = (rem - arr * per_arr) * W;
+    for (int u = 0; u < RUNS; u++) {
+      const int run = warp + u * NW, lt = run / 3, arr = run - 3 * lt;
       const int il = tile_line(bx, lt, k, TW, color);
-      if (il < 1 || il > mx - 2) continue;
-      v[u] = __ldg(reinterpret_cast<const V *>(fa + F.line(il, k) + (size_t)arr * F.Q + q0));
-      dst[u] = (arr * TW + lt) * Lo.ls;
-      rows[u] = q0 + 1;  // first row + 1 (0: nothing to store)
+      ok[u] = run < 3 * TW && v < per_arr && il >= 1 && il <= mx - 2;
+      if (ok[u]) val[u] = __ldg(reinterpret_cast<const V *>(fa + F.line(il, k) + (size_t)arr * F.Q) + v);
     }
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      if (!rows[u]) continue;
-      const int q0 = rows[u] - 1;
+    for (int u = 0; u < RUNS; u++) {
+      if (!ok[u]) continue;
+      const int run = warp + u * NW, lt = run / 3, arr = run - 3 * lt;
+      T *dst = sa + (arr * TW + lt) * Lo.ls;
 #pragma unroll
       for (int w = 0; w < W; w++)
-        if (q0 + w < Lo.nr) sa[dst[u] + Lo.pos(q0 + w)] = VT::at(v[u], w);
+        if (v * W + w < Lo.nr) dst[Lo.pos(v * W + w)] = VT::at(val[u], w);
     }
   }
 }
 
 // Solve the tile's lines in shared memory and write it out (the tile's copies
 // have landed and the block is synchronised when this is entered).
-template <typename T, int TW>
+template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__restrict__ x, T *__restrict__ xnew,
                                                   T omega, int bx, int k, T *st, int color = -1) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
-  const LineLayout Lo = LineLayout::of(my);
+  const LineLayout Lo = LineLayout::fixed<RR>(my);
   T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
-  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW, ny = blockDim.x / TW;
+  const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
+  constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
   const bool kin = k >= 1 && k <= g.mz - 2;
   const bool line = i >= 1 && i <= mx - 2 && kin;
@@ -641,11 +676,22 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
   constexpr int NW = kSolveThreads / 32, NL = TW / NW;
   if (kin) {
     const int o = warp * Lo.ls;
-    warp_lines_solve<T, NL>(sr + o, sa + o, sm + o, sc + o, NW * Lo.ls, Lo, lane);
+    warp_lines_solve<T, NL, RR>(sr + o, sa + o, sm + o, sc + o, NW * Lo.ls, Lo, lane);
   }
   __syncthreads();
   if (i >= mx) return;
   const int col = (k * my) * mx + i;
+  if (color >= 0) {
+    // zebra: only the colour's interior rows change (x in place, or zeroed by
+    // the caller for a zero guess)
+    if (!line) return;
+    for (int j = 1 + ty; j <= my - 2; j += ny) {
+      const int s = tx * Lo.ls + Lo.pos(j - 1);
+      const T xo = x ? sx[s] : T(0);
+      xnew[col + j * mx] = xo + omega * sr[s];
+    }
+    return;
+  }
   for (int j = ty; j < my; j += ny) {
     const int p = col + j * mx;
     if (line && j >= 1 && j <= my - 2) {
@@ -662,14 +708,14 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
 // color >= 0: zebra half-sweep on the lines of that color only, x updated in
 // place (xnew == x; a tile reads its lines' x before it writes them) -- or,
 // with x == nullptr, written on those lines only (the caller zeroed the rest).
-template <typename T, int TW>
+template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *x, T *xnew,
                                                 T omega, int bx, int k, unsigned char *smem_raw, int color = -1) {
   T *st = reinterpret_cast<T *>(smem_raw);
-  solve_tile_load<T, TW>(L, r, x, bx, k, st, color);
+  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color);
   cp_async_wait_all();
   __syncthreads();
-  solve_tile_finish<T, TW>(L, x, xnew, omega, bx, k, st, color);
+  solve_tile_finish<T, TW, RR>(L, x, xnew, omega, bx, k, st, color);
 }
 
 // Tiles of a line solve: all lines or one color's.
