@@ -174,6 +174,8 @@ static int upload_box(cvb_ctx *ctx, Geometry &G, const cvb_level_desc &d, const 
 
 static int check_desc(cvb_ctx *ctx, const cvb_level_desc &d, int level, bool finest) {
   if (d.mx < 3 || d.my < 3 || d.mz < 3) return fail(ctx, CVB_BAD_INPUT, "level %d: box %dx%dx%d too small", level, d.mx, d.my, d.mz);
+  if ((long long)d.mx * d.my * d.mz >= (1LL << 31))
+    return fail(ctx, CVB_BAD_INPUT, "level %d: box %dx%dx%d holds 2^31 cells or more", level, d.mx, d.my, d.mz);
   if (d.gxs > 0 || d.gys > 0 || d.gzs > 0 || d.gxs + d.gxm < d.mx || d.gys + d.gym < d.my || d.gzs + d.gzm < d.mz)
     return fail(ctx, CVB_BAD_INPUT, "level %d: ghosted box does not cover the owned box", level);
   const double *req[] = {d.icsi, d.ieta, d.izet, d.jcsi, d.jeta, d.jzet, d.kcsi, d.keta, d.kzet, d.iaj, d.jaj, d.kaj, d.aj};

@@ -760,51 +760,52 @@ __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
-// MyRestriction (poisson.c:129-226): coarse = 0.125 * sum over the 8 children of
-// x * max(0, 1 - nvert_fine); zero on the ring and on blocked coarse cells.
 // Restriction weight of a fine cell, max(0, 1 - nvert): FP64 from nvert (as the
 // reference), FP32 from the set-up copy of the same value rounded to float.
 template <typename T>
 struct FineWeight;
 template <>
 struct FineWeight<double> {
-  __device__ static double w(const LevelDev &F, size_t q) {
+  __device__ static double w(const LevelDev &F, int q) {
     double wt = 1.0 - F.nvert[q];
     return wt > 0.0 ? wt : 0.0;
   }
 };
 template <>
 struct FineWeight<float> {
-  __device__ static float w(const LevelDev &F, size_t q) { return F.wgt32[q]; }
+  __device__ static float w(const LevelDev &F, int q) { return F.wgt32[q]; }
 };
 
+// MyRestriction (poisson.c:129-226): coarse = 0.125 * sum over the 8 children of
+// x * max(0, 1 - nvert_fine) (children coincide along a semi-coarsened
+// direction); zero on the ring and on blocked coarse cells.  The children are
+// summed in the reference's order.  Index arithmetic in int: a level holds
+// fewer than 2^31 cells (checked at set-up).
 template <typename T>
 __device__ __forceinline__ void restrict_body(const LevelDev &F, const LevelDev &C, const T *__restrict__ xf,
                                               T *__restrict__ xc, int bx, int by, int bz) {
-  const Geom Fg = F.g, Cg = C.g;
-  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= Cg.mx || j >= Cg.my) return;
-  size_t p = Cg.id(i, j, k);
-  if (i == 0 || i == Cg.mx - 1 || j == 0 || j == Cg.my - 1 || k == 0 || k == Cg.mz - 1 ||
-      (C.code[p] & CODE_BLOCKED)) {
+  const int cmx = C.g.mx, cmy = C.g.my, cmz = C.g.mz;
+  const int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
+  if (i >= cmx || j >= cmy) return;
+  const int p = (k * cmy + j) * cmx + i;
+  if (i == 0 || i == cmx - 1 || j == 0 || j == cmy - 1 || k == 0 || k == cmz - 1 || (C.code[p] & CODE_BLOCKED)) {
     xc[p] = T(0);
     return;
   }
   const int isc = C.isc, jsc = C.jsc, ksc = C.ksc;
-  int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
-  int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
-  auto W = [&](int a, int b, int c) {
-    size_t q = Fg.id(a, b, c);
-    return mul_rn(xf[q], FineWeight<T>::w(F, q));
-  };
-  T s = W(ih, jh, kh);
-  s = add_rn(s, W(ih - ia, jh, kh));
-  s = add_rn(s, W(ih, jh - ja, kh));
-  s = add_rn(s, W(ih, jh, kh - ka));
-  s = add_rn(s, W(ih - ia, jh - ja, kh));
-  s = add_rn(s, W(ih, jh - ja, kh - ka));
-  s = add_rn(s, W(ih - ia, jh, kh - ka));
-  s = add_rn(s, W(ih - ia, jh - ja, kh - ka));
+  const int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+  const int fmx = F.g.mx, fpl = fmx * F.g.my;
+  const int q = (kh * F.g.my + jh) * fmx + ih;
+  const int oi = isc ? 0 : 1, oj = jsc ? 0 : fmx, ok = ksc ? 0 : fpl;
+  auto W = [&](int o) { return mul_rn(xf[q - o], FineWeight<T>::w(F, q - o)); };
+  T s = W(0);
+  s = add_rn(s, W(oi));
+  s = add_rn(s, W(oj));
+  s = add_rn(s, W(ok));
+  s = add_rn(s, W(oi + oj));
+  s = add_rn(s, W(oj + ok));
+  s = add_rn(s, W(oi + ok));
+  s = add_rn(s, W(oi + oj + ok));
   xc[p] = mul_rn(T(0.125), s);
 }
 
@@ -816,30 +817,28 @@ __device__ __forceinline__ void restrict_body(const LevelDev &F, const LevelDev 
 template <typename T>
 __device__ __forceinline__ void prolong_body(const LevelDev &C, const LevelDev &F, const T *__restrict__ xc,
                                              T *__restrict__ xf, int bx, int by, int bz) {
-  const Geom Fg = F.g, Cg = C.g;
-  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= Fg.mx || j >= Fg.my) return;
-  size_t p = Fg.id(i, j, k);
-  if (i == 0 || i == Fg.mx - 1 || j == 0 || j == Fg.my - 1 || k == 0 || k == Fg.mz - 1 ||
-      (F.code[p] & CODE_BLOCKED))
-    return;
+  const int fmx = F.g.mx, fmy = F.g.my, fmz = F.g.mz;
+  const int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
+  if (i >= fmx || j >= fmy) return;
+  if (i == 0 || i == fmx - 1 || j == 0 || j == fmy - 1 || k == 0 || k == fmz - 1) return;
+  const int p = (k * fmy + j) * fmx + i;
+  if (F.code[p] & CODE_BLOCKED) return;
   const int isc = F.isc, jsc = F.jsc, ksc = F.ksc;
-  const uint32_t *cc = C.code;
   int ic, jc, kc, ia, ja, ka;
-  if (isc) { ic = i; ia = 0; } else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == Fg.mx - 2) ia = 0; }
-  if (jsc) { jc = j; ja = 0; } else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == Fg.my - 2) ja = 0; }
-  if (ksc) { kc = k; ka = 0; } else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == Fg.mz - 2) ka = 0; }
-  if (ka == -1 && (cc[Cg.id(ic, jc, kc - 1)] & CODE_BLOCKED)) ka = 0;
-  else if (ka == 1 && (cc[Cg.id(ic, jc, kc + 1)] & CODE_BLOCKED)) ka = 0;
-  if (ja == -1 && (cc[Cg.id(ic, jc - 1, kc)] & CODE_BLOCKED)) ja = 0;
-  else if (ja == 1 && (cc[Cg.id(ic, jc + 1, kc)] & CODE_BLOCKED)) ja = 0;
-  if (ia == -1 && (cc[Cg.id(ic - 1, jc, kc)] & CODE_BLOCKED)) ia = 0;
-  else if (ia == 1 && (cc[Cg.id(ic + 1, jc, kc)] & CODE_BLOCKED)) ia = 0;
-  auto X = [&](int a, int b, int c) { return xc[Cg.id(a, b, c)]; };
-  T s1 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc), T(9)), mul_rn(X(ic, jc + ja, kc), T(3))),
-                       mul_rn(X(ic + ia, jc, kc), T(3))), X(ic + ia, jc + ja, kc));
-  T s2 = add_rn(add_rn(add_rn(mul_rn(X(ic, jc, kc + ka), T(9)), mul_rn(X(ic, jc + ja, kc + ka), T(3))),
-                       mul_rn(X(ic + ia, jc, kc + ka), T(3))), X(ic + ia, jc + ja, kc + ka));
+  if (isc) { ic = i; ia = 0; } else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == fmx - 2) ia = 0; }
+  if (jsc) { jc = j; ja = 0; } else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == fmy - 2) ja = 0; }
+  if (ksc) { kc = k; ka = 0; } else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == fmz - 2) ka = 0; }
+  const int cmx = C.g.mx, cpl = cmx * C.g.my;
+  const int q = (kc * C.g.my + jc) * cmx + ic;
+  const uint32_t *cc = C.code;
+  if (ka != 0 && (cc[q + ka * cpl] & CODE_BLOCKED)) ka = 0;
+  if (ja != 0 && (cc[q + ja * cmx] & CODE_BLOCKED)) ja = 0;
+  if (ia != 0 && (cc[q + ia] & CODE_BLOCKED)) ia = 0;
+  const int oj = ja * cmx, ok = ka * cpl;
+  T s1 = add_rn(add_rn(add_rn(mul_rn(xc[q], T(9)), mul_rn(xc[q + oj], T(3))), mul_rn(xc[q + ia], T(3))),
+                xc[q + ia + oj]);
+  T s2 = add_rn(add_rn(add_rn(mul_rn(xc[q + ok], T(9)), mul_rn(xc[q + oj + ok], T(3))), mul_rn(xc[q + ia + ok], T(3))),
+                xc[q + ia + oj + ok]);
   T v = add_rn(mul_rn(mul_rn(s1, T(3)), T(0.015625)), mul_rn(s2, T(0.015625)));
   xf[p] = add_rn(xf[p], v);
 }
