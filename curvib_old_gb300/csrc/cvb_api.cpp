@@ -705,11 +705,18 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
     st->abs_residual = 0.0;
     return CVB_OK;
   }
-  if (!o->warm_start) CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * n, s));
-  launch_residual<double>(F, ctx->b, ctx->x, ctx->r, s);
-  CKL();
+  // r0 = b - A x0: b itself for the zero initial guess (same bits, no apply)
+  const double *rcur = ctx->r;
   double beta;
-  TRY(norm2(ctx, ctx->r, n, &beta));
+  if (!o->warm_start) {
+    CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * n, s));
+    rcur = ctx->b;
+    beta = bnorm;
+  } else {
+    launch_residual<double>(F, ctx->b, ctx->x, ctx->r, s);
+    CKL();
+    TRY(norm2(ctx, ctx->r, n, &beta));
+  }
   int total = 0, restarts = 0;
   double H[kMaxRestart + 1][kMaxRestart];
   double cs[kMaxRestart], sn[kMaxRestart], gv[kMaxRestart + 1], yv[kMaxRestart];
@@ -721,7 +728,7 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
     if (total >= o->max_it) break;
     // V[0] = r / beta (k_scale divides by the device scalar)
     CK(cudaMemcpyAsync(ctx->hdev, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
-    launch_scale(ctx->V[0], ctx->r, ctx->hdev, n, s);
+    launch_scale(ctx->V[0], rcur, ctx->hdev, n, s);
     CKL();
     for (int q = 0; q <= m; q++) gv[q] = 0.0;
     gv[0] = beta;
@@ -744,37 +751,38 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
       CKL();
       // classical Gram-Schmidt (PETSc's default for GMRES/FGMRES), with a second
       // pass only when the first one cancelled most of w (||w|| dropped below
-      // half of its length before orthogonalisation).
-      double h[kMaxRestart + 2], h2[kMaxRestart + 1];
+      // half of its length before orthogonalisation).  The projections and the
+      // norm stay on the device between the kernels (V_{j+1} = w / ||w|| is
+      // formed there too); the host reads them back once per iteration.
+      double h[kMaxRestart + 2], h2[kMaxRestart + 1], nw2;
+      double *dsum = ctx->sums, *dnorm = ctx->sums + kMaxRestart + 2;
       launch_multidot(ctx->dV, j + 1, ctx->w, n, ctx->partial, s, 1);
+      launch_finish_sums(ctx->partial, j + 2, reduce_blocks(), dsum, s);
+      launch_multiaxpy_norm(ctx->w, ctx->dV, dsum, j + 1, n, ctx->partial, s);
+      launch_finish_sums(ctx->partial, 1, reduce_blocks(), dnorm, s);
+      launch_scale_sqrt(ctx->V[j + 1], ctx->w, dnorm, n, s);
       CKL();
-      TRY(reduce_to_host(ctx, j + 2, h));
+      CK(cudaMemcpyAsync(h, dsum, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&nw2, dnorm, sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
       const double w_before = h[j + 1];
-      CK(cudaMemcpyAsync(ctx->hdev, h, sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
-      launch_multiaxpy_norm(ctx->w, ctx->dV, ctx->hdev, j + 1, n, ctx->partial, s);
-      CKL();
-      double nw2;
-      TRY(reduce_to_host(ctx, 1, &nw2));
       for (int q = 0; q <= j; q++) h2[q] = 0.0;
       if (o->cgs_refine && nw2 < 0.25 * w_before) {
         launch_multidot(ctx->dV, j + 1, ctx->w, n, ctx->partial, s);
+        launch_finish_sums(ctx->partial, j + 1, reduce_blocks(), dsum, s);
+        launch_multiaxpy_norm(ctx->w, ctx->dV, dsum, j + 1, n, ctx->partial, s);
+        launch_finish_sums(ctx->partial, 1, reduce_blocks(), dnorm, s);
+        launch_scale_sqrt(ctx->V[j + 1], ctx->w, dnorm, n, s);
         CKL();
-        TRY(reduce_to_host(ctx, j + 1, h2));
-        CK(cudaMemcpyAsync(ctx->hdev, h2, sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
-        launch_multiaxpy_norm(ctx->w, ctx->dV, ctx->hdev, j + 1, n, ctx->partial, s);
-        CKL();
-        TRY(reduce_to_host(ctx, 1, &nw2));
+        CK(cudaMemcpyAsync(h2, dsum, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&nw2, dnorm, sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
       }
       for (int q = 0; q <= j; q++) H[q][j] = h[q] + h2[q];
       double hn = std::sqrt(nw2);
       H[j + 1][j] = hn;
       total++;
       if (!std::isfinite(hn)) return fail(ctx, CVB_NAN_DETECTED, "Krylov vector became non-finite");
-      if (hn > 0.0) {
-        CK(cudaMemcpyAsync(ctx->hdev, &hn, sizeof(double), cudaMemcpyHostToDevice, s));
-        launch_scale(ctx->V[j + 1], ctx->w, ctx->hdev, n, s);
-        CKL();
-      }
       // Givens rotations
       for (int q = 0; q < j; q++) {
         double t = cs[q] * H[q][j] + sn[q] * H[q + 1][j];
@@ -803,6 +811,7 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
     launch_residual<double>(F, ctx->b, ctx->x, ctx->r, s);
     CKL();
     TRY(norm2(ctx, ctx->r, n, &beta));
+    rcur = ctx->r;
     restarts++;
   }
   TRY(fluid_mean_zero(ctx, ctx->nlevels - 1, ctx->x));
@@ -898,7 +907,7 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
   TRY(dalloc(ctx, &ctx->dZ32, kMaxRestart));
   int nb = reduce_blocks();
   TRY(dalloc(ctx, &ctx->partial, (size_t)nb * (kMaxRestart + 2)));
-  TRY(dalloc(ctx, &ctx->sums, kMaxRestart + 2));
+  TRY(dalloc(ctx, &ctx->sums, 2 * (kMaxRestart + 2)));
   TRY(dalloc(ctx, &ctx->hdev, kMaxRestart + 2));
   TRY(build_operators(ctx));
   TRY(autotune_sweeps(ctx));

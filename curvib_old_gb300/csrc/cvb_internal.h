@@ -149,6 +149,8 @@ void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_de
                            double *partial, cudaStream_t s, const int *gate = nullptr);
 void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
                   const int *gate = nullptr);
+// dst = src / sqrt(*sq_dev)
+void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s);
 void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev,
                    int nz, size_t n, cudaStream_t s);
 void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial,

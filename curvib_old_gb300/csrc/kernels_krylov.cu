@@ -167,18 +167,22 @@ void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_de
   launch_dep(k_multiaxpy_norm, reduce_blocks(), kRedThreads, 0, s, w, V, h_dev, nv, n, partial, gate);
 }
 
-// dst = src / *scal
+// dst = src / *scal, or src / sqrt(*scal)
+template <bool SQRT>
 __global__ void k_scale(double *__restrict__ dst, const double *__restrict__ src, const double *__restrict__ scal,
                         size_t n, const int *gate) {
   dep_sync();
   if (gated(gate)) return;
-  double inv = 1.0 / *scal;
+  double inv = 1.0 / (SQRT ? sqrt(*scal) : *scal);
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
     dst[p] = src[p] * inv;
 }
 void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
                   const int *gate) {
-  launch_dep(k_scale, reduce_blocks(), 256, 0, s, dst, src, scal_dev, n, gate);
+  launch_dep(k_scale<false>, reduce_blocks(), 256, 0, s, dst, src, scal_dev, n, gate);
+}
+void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s) {
+  launch_dep(k_scale<true>, reduce_blocks(), 256, 0, s, dst, src, sq_dev, n, nullptr);
 }
 
 // x += sum_q y[q] Z_q (Z stored FP32 in mixed mode, FP64 in plain mode)
