@@ -890,8 +890,10 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
     TRY(dalloc(ctx, &L.wgt32, n));
     TRY(dalloc(ctx, &L.line32, LineFac::of(L.g).count(L.g)));
     TRY(dalloc(ctx, &L.line64, LineFac::of(L.g).count(L.g)));
-    TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, 2 * n));
-    TRY(dalloc(ctx, &L.r32, n)); TRY(dalloc(ctx, &L.e32, n)); TRY(dalloc(ctx, &L.t32, 2 * n));
+    // t: [e2 | res]; res also holds a zebra residual in colour-split rows
+    const size_t nt = n + std::max(n, SplitRow::count(L.g));
+    TRY(dalloc(ctx, &L.r64, n)); TRY(dalloc(ctx, &L.e64, n)); TRY(dalloc(ctx, &L.t64, nt));
+    TRY(dalloc(ctx, &L.r32, n)); TRY(dalloc(ctx, &L.e32, n)); TRY(dalloc(ctx, &L.t32, nt));
   }
   TRY(dalloc(ctx, &ctx->nvert_tmp, nmax));
   LevelDev &F = ctx->L[nlevels - 1];

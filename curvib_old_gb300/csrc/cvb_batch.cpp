@@ -230,7 +230,8 @@ static void gen_zebra_half(VSink &vs, long long k0, long long k1, LevelDev &L, c
   }
   const int gx = f32 ? solve_tiles_x<kSolveTW32>(L.g, color) : solve_tiles_x<kSolveTW64>(L.g, color);
   (void)SW;
-  vs.add(k1, OK_SOLVE, task(dLv, r, zero ? nullptr : x, x, gate, gx, 0, 0, color + 1), gx * L.g.mz, sso);
+  vs.add(k1, OK_SOLVE, task(dLv, r, zero ? nullptr : x, x, gate, gx, 0, 0, color + 1 + (zero ? 0 : 16)),
+         gx * L.g.mz, sso);
 }
 
 template <typename T>

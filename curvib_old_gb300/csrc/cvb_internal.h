@@ -68,6 +68,19 @@ struct LineFac {
   __host__ __device__ size_t count(const Geom &g) const { return (size_t)g.mz * 2 * nt * 3 * Q; }
 };
 
+// Colour-split rows: the cells of zebra colour (i + k) % 2 == c of row (j, k)
+// at c * half + i / 2 of a row of 2 * half slots.  A zebra half-sweep passes
+// its residual to the line solves in this layout, so that the lines of one
+// colour are adjacent in memory.
+struct SplitRow {
+  __host__ __device__ static int half(const Geom &g) { return (g.mx + 1) >> 1; }
+  __host__ __device__ static size_t count(const Geom &g) { return (size_t)g.my * g.mz * 2 * half(g); }
+  __host__ __device__ static int at(const Geom &g, int i, int j, int k) {
+    const int h = half(g);
+    return (k * g.my + j) * 2 * h + ((i + k) & 1) * h + (i >> 1);
+  }
+};
+
 // Device data of one multigrid level.
 struct LevelDev {
   Geom g;

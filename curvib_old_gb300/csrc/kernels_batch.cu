@@ -90,8 +90,9 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_c
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const LevelDev L = *K.L;
   int lb = blockIdx.x - K.block0;
+  // p1: colour + 1 (0: all lines), plus 16 when the residual is colour-split
   line_solve_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw,
-                         K.p1 - 1);
+                         (K.p1 & 15) - 1, (K.p1 >> 4) != 0);
 }
 // zebra: residual on the cells of color p0
 template <typename T>

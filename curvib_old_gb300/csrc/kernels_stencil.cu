@@ -63,11 +63,11 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
 // RR: the line layout's rows per lane fixed at compile time (0: read from my)
 template <typename T, int TW, int RR>
 __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
-                                                                 T *xnew, T omega, int color) {
+                                                                 T *xnew, T omega, int color, int rsplit) {
   dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color);
+  line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color, rsplit != 0);
 }
 
 template <typename T>
@@ -93,7 +93,8 @@ static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T ome
 
 
 template <typename T, int TW, int RR>
-static void line_solve_r(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color) {
+static void line_solve_r(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color,
+                         int rsplit) {
   dim3 grd(solve_tiles_x<TW>(L.g, color), L.g.mz);
   static bool attr = false;
   if (!attr) {
@@ -101,16 +102,17 @@ static void line_solve_r(const LevelDev &L, const T *r, const T *x, T *xnew, T o
     attr = true;
   }
   launch_dep(k_line_solve<T, TW, RR>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, r, x, xnew, omega,
-             color);
+             color, rsplit);
 }
 template <typename T, int TW>
-static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color = -1) {
+static void line_solve(const LevelDev &L, const T *r, const T *x, T *xnew, T omega, cudaStream_t s, int color = -1,
+                       int rsplit = 0) {
   switch (LineLayout::of(L.g.my).R) {
-    case 1: line_solve_r<T, TW, 1>(L, r, x, xnew, omega, s, color); break;
-    case 2: line_solve_r<T, TW, 2>(L, r, x, xnew, omega, s, color); break;
-    case 4: line_solve_r<T, TW, 4>(L, r, x, xnew, omega, s, color); break;
-    case 8: line_solve_r<T, TW, 8>(L, r, x, xnew, omega, s, color); break;
-    default: line_solve_r<T, TW, 0>(L, r, x, xnew, omega, s, color); break;
+    case 1: line_solve_r<T, TW, 1>(L, r, x, xnew, omega, s, color, rsplit); break;
+    case 2: line_solve_r<T, TW, 2>(L, r, x, xnew, omega, s, color, rsplit); break;
+    case 4: line_solve_r<T, TW, 4>(L, r, x, xnew, omega, s, color, rsplit); break;
+    case 8: line_solve_r<T, TW, 8>(L, r, x, xnew, omega, s, color, rsplit); break;
+    default: line_solve_r<T, TW, 0>(L, r, x, xnew, omega, s, color, rsplit); break;
   }
 }
 
@@ -220,7 +222,7 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
     launch_dep(k_resid_color<T>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
     r = res;
   }
-  line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color);
+  line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);
 }
 template void launch_zebra_half<float>(const LevelDev &, const float *, float *, float *, float, int, bool,
                                        cudaStream_t);

@@ -608,7 +608,7 @@ struct Vec16<double> {
 // all of its loads in flight before it stores any.
 template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
-                                                int bx, int k, T *st, int color = -1) {
+                                                int bx, int k, T *st, int color = -1, bool rsplit = false) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   if (!(k >= 1 && k <= g.mz - 2)) return;
@@ -622,7 +622,7 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
     for (int j = 1 + ty; j <= my - 2; j += ny) {
       const int p = col + j * mx;
       const int s = tx * Lo.ls + Lo.pos(j - 1);
-      cp_async_el(sr + s, r + p);
+      cp_async_el(sr + s, r + (rsplit ? SplitRow::at(g, i, j, k) : p));
       if (x) cp_async_el(sx + s, x + p);
     }
   }
@@ -708,11 +708,14 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
 // color >= 0: zebra half-sweep on the lines of that color only, x updated in
 // place (xnew == x; a tile reads its lines' x before it writes them) -- or,
 // with x == nullptr, written on those lines only (the caller zeroed the rest).
+// rsplit: r is in the colour-split row layout (a zebra residual), else in the
+// level's own layout.
 template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__restrict__ r, const T *x, T *xnew,
-                                                T omega, int bx, int k, unsigned char *smem_raw, int color = -1) {
+                                                T omega, int bx, int k, unsigned char *smem_raw, int color = -1,
+                                                bool rsplit = false) {
   T *st = reinterpret_cast<T *>(smem_raw);
-  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color);
+  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color, rsplit);
   cp_async_wait_all();
   __syncthreads();
   solve_tile_finish<T, TW, RR>(L, x, xnew, omega, bx, k, st, color);
@@ -725,7 +728,8 @@ __host__ __device__ inline int solve_tiles_x(const Geom &g, int color) {
 }
 
 // Residual b - A x on the cells of one zebra color ((i + k) % 2 == color), one
-// thread per cell of that color, 32 x 4 threads; the other cells are not written.
+// thread per cell of that color, 32 x 4 threads, written in the colour-split
+// row layout (SplitRow).
 template <typename T>
 struct ColorRow;
 template <>
@@ -747,7 +751,7 @@ __device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__r
   const int i = 2 * (bx * 32 + threadIdx.x) + ((color + k) & 1), j = by * 4 + threadIdx.y;
   if (i >= g.mx || j >= g.my) return;
   const int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
-  r[p] = b[p] - ColorRow<T>::r(g, L, x, i, j, k, p, n);
+  r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::r(g, L, x, i, j, k, p, n);
 }
 __host__ __device__ inline int color_tiles_x(const Geom &g) { return ((g.mx + 1) / 2 + 31) / 32; }
 
