@@ -74,6 +74,7 @@ EXPORTS = {
     "cvb_apply_operator": ([_P, _I, _P, _P], _I),
     "cvb_apply_operator_f32": ([_P, _I, _P, _P], _I),
     "cvb_get_weights": ([_P, _I, _P], _I),
+    "cvb_level_cross": ([_P, _I, _P, _P], _I),
     "cvb_restrict": ([_P, _I, _P, _P], _I),
     "cvb_interpolate": ([_P, _I, _P, _P], _I),
     "cvb_nullspace": ([_P, _I, _P], _I),

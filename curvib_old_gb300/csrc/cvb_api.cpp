@@ -364,6 +364,21 @@ static int build_operators(cvb_ctx *ctx) {
   }
   // g9 is a set-up temporary; return it to the pool
   dfree(ctx, g9);
+  // which levels have cross-derivative terms (the kernels read 7 points on the
+  // others, with the same results)
+  int *flags = nullptr;
+  TRY(dalloc(ctx, &flags, 2 * (size_t)nl));
+  CK(cudaMemsetAsync(flags, 0, sizeof(int) * 2 * nl, ctx->stream));
+  for (int l = 0; l < nl; l++) launch_cross_flags(ctx->L[l].g, ctx->L[l].gf32, ctx->L[l].w64, flags + 2 * l, ctx->stream);
+  CKL();
+  std::vector<int> hf(2 * nl);
+  CK(cudaMemcpyAsync(hf.data(), flags, sizeof(int) * 2 * nl, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, flags);
+  for (int l = 0; l < nl; l++) {
+    ctx->L[l].cross32 = hf[2 * l];
+    ctx->L[l].cross64 = hf[2 * l + 1];
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   return CVB_OK;
 }
@@ -1250,6 +1265,13 @@ int cvb_apply_operator_f32(cvb_ctx *ctx, int level, const float *x, float *y) {
   return CVB_OK;
 }
 
+int cvb_level_cross(const cvb_ctx *ctx, int level, int *cross32, int *cross64) {
+  if (!ctx || !ctx->ready || level < 0 || level >= ctx->nlevels) return CVB_BAD_INPUT;
+  if (cross32) *cross32 = ctx->L[level].cross32;
+  if (cross64) *cross64 = ctx->L[level].cross64;
+  return CVB_OK;
+}
+
 int cvb_get_weights(cvb_ctx *ctx, int level, double *w) {
   TRY(level_ok(ctx, level));
   LevelDev &L = ctx->L[level];
@@ -1400,16 +1422,19 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
     }
   };
   if (kernel == CVB_KERNEL_VCYCLE_F32 || kernel == CVB_KERNEL_VCYCLE_F64) return time_vcycle(ctx, kernel, level, reps, avg_ms, bytes);
-  // algorithmic bytes per cell: every array the kernel needs, touched once
+  // algorithmic bytes per cell: every array the kernel needs, touched once.
+  // The coefficients are the 9 face coefficients (FP32) or 19 weights (FP64),
+  // 3 or 7 on a level without cross-derivative terms (an orthogonal grid).
+  const double g32 = L.cross32 ? 36 : 12, w64 = L.cross64 ? 152 : 56;
   switch (kernel) {
-    case CVB_KERNEL_LINE_SWEEP_F32: per_cell = 4 + 4 + 36 + 4 + 4 + 12 + 4; break;   // x b g9 aj code fac xnew
-    case CVB_KERNEL_LINE_SWEEP_F64: per_cell = 8 + 8 + 152 + 4 + 24 + 8; break;      // x b w19 code fac xnew
-    case CVB_KERNEL_RESIDUAL_F32: per_cell = 4 + 4 + 36 + 4 + 4 + 4; break;          // x b g9 aj code r
-    case CVB_KERNEL_RESIDUAL_F64: per_cell = 8 + 8 + 152 + 4 + 8; break;             // x b w19 code r
+    case CVB_KERNEL_LINE_SWEEP_F32: per_cell = 4 + 4 + g32 + 4 + 4 + 12 + 4; break;   // x b g aj code fac xnew
+    case CVB_KERNEL_LINE_SWEEP_F64: per_cell = 8 + 8 + w64 + 4 + 24 + 8; break;       // x b w code fac xnew
+    case CVB_KERNEL_RESIDUAL_F32: per_cell = 4 + 4 + g32 + 4 + 4 + 4; break;          // x b g aj code r
+    case CVB_KERNEL_RESIDUAL_F64: per_cell = 8 + 8 + w64 + 4 + 8; break;              // x b w code r
     // one zebra half-sweep: x read everywhere; coefficients, b, r and the line
     // solve's r, factors, x in/out on the half of the cells of the color
-    case CVB_KERNEL_ZEBRA_F32: per_cell = 4 + 0.5 * (4 + 36 + 4 + 4 + 4) + 0.5 * (4 + 12 + 4 + 4); break;
-    case CVB_KERNEL_ZEBRA_F64: per_cell = 8 + 0.5 * (8 + 152 + 4 + 8) + 0.5 * (8 + 24 + 8 + 8); break;
+    case CVB_KERNEL_ZEBRA_F32: per_cell = 4 + 0.5 * (4 + g32 + 4 + 4 + 4) + 0.5 * (4 + 12 + 4 + 4); break;
+    case CVB_KERNEL_ZEBRA_F64: per_cell = 8 + 0.5 * (8 + w64 + 4 + 8) + 0.5 * (8 + 24 + 8 + 8); break;
     default: return fail(ctx, CVB_BAD_INPUT, "unknown kernel id %d", kernel);
   }
   CK(cudaMemsetAsync(L.r32, 0, sizeof(float) * n, ctx->stream));

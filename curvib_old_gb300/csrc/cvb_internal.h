@@ -97,6 +97,9 @@ struct LevelDev {
   double *r64, *e64, *t64;  // FP64 V-cycle vectors
   float *r32, *e32, *t32;   // FP32 V-cycle vectors
   int sweep32, sweep64;     // line-sweep variant chosen at set-up: 0 fused, 1 split
+  // the operator has cross-derivative terms (FP32 flux form / FP64 edge
+  // weights); 0 on an orthogonal grid, where the kernels read 7 points
+  int cross32, cross64;
   // coarsest level only: the densely inverted cells (first cm of cidx) and the
   // identity ones (the rest of cidx)
   const int *cidx;
@@ -117,6 +120,9 @@ void launch_gcoef(const Geom &g, const double *const *metric /*12 Cmpnts fields:
 void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s);
 // wgt32 = (float) max(0, 1 - nvert)
 void launch_weight32(const Geom &g, const double *nvert, float *wgt32, cudaStream_t s);
+// flags[0] |= some FP32 cross coefficient is non-zero, flags[1] |= some FP64
+// edge weight is non-zero (flags zeroed by the caller)
+void launch_cross_flags(const Geom &g, const float *gf32, const double *w64, int *flags, cudaStream_t s);
 // FP32 face coefficients: cross terms pre-scaled by their form's weight (after launch_codes)
 void launch_scale_cross(const Geom &g, const uint32_t *code, float *gf32, cudaStream_t s);
 void launch_weights(const Geom &g, const double *g9, const double *aj, const double *nvert,

@@ -43,8 +43,12 @@ __global__ void __launch_bounds__(256) kg_apply32(const __grid_constant__ TaskLi
   if (gated(T.gate)) return;
   const LevelDev L = *T.L;
   Blk3 q = blk3(T, blockIdx.x);
-  apply32_march_body(L.g, L.gf32, L.ajf32, L.code, (const float *)T.a, (const float *)T.b, (float *)T.c, q.x, q.y,
-                     q.z);
+  if (L.cross32)
+    apply32_march_body<true>(L.g, L.gf32, L.ajf32, L.code, (const float *)T.a, (const float *)T.b, (float *)T.c, q.x,
+                             q.y, q.z);
+  else
+    apply32_march_body<false>(L.g, L.gf32, L.ajf32, L.code, (const float *)T.a, (const float *)T.b, (float *)T.c,
+                              q.x, q.y, q.z);
 }
 __global__ void __launch_bounds__(128) kg_apply64(const __grid_constant__ TaskList tl) {
   dep_sync();
@@ -52,7 +56,12 @@ __global__ void __launch_bounds__(128) kg_apply64(const __grid_constant__ TaskLi
   if (gated(T.gate)) return;
   const LevelDev L = *T.L;
   Blk3 q = blk3(T, blockIdx.x);
-  apply64_body<double>(L.g, L.w64, L.code, (const double *)T.a, (const double *)T.b, (double *)T.c, q.x, q.y, q.z);
+  if (L.cross64)
+    apply64_body<double, true>(L.g, L.w64, L.code, (const double *)T.a, (const double *)T.b, (double *)T.c, q.x, q.y,
+                               q.z);
+  else
+    apply64_body<double, false>(L.g, L.w64, L.code, (const double *)T.a, (const double *)T.b, (double *)T.c, q.x, q.y,
+                                q.z);
 }
 template <typename T>
 __global__ void __launch_bounds__(128) kg_restrict(const __grid_constant__ TaskList tl) {
@@ -80,7 +89,12 @@ __global__ void __launch_bounds__(256, 2) kg_line_sweep(const __grid_constant__ 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const LevelDev L = *K.L;
   int lb = blockIdx.x - K.block0;
-  line_sweep_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, K.p0, lb % K.gx, lb / K.gx, smem_raw);
+  if (has_cross<T>(L))
+    line_sweep_body<T, TW, true>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, K.p0, lb % K.gx, lb / K.gx,
+                                 smem_raw);
+  else
+    line_sweep_body<T, TW, false>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, K.p0, lb % K.gx, lb / K.gx,
+                                  smem_raw);
 }
 template <typename T, int TW>
 __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_constant__ TaskList tl, T omega) {
@@ -102,7 +116,8 @@ __global__ void __launch_bounds__(128) kg_resid_color(const __grid_constant__ Ta
   if (gated(K.gate)) return;
   const LevelDev L = *K.L;
   Blk3 q = blk3(K, blockIdx.x);
-  resid_color_body<T>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, K.p0, q.x, q.y, q.z);
+  if (has_cross<T>(L)) resid_color_body<T, true>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, K.p0, q.x, q.y, q.z);
+  else resid_color_body<T, false>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, K.p0, q.x, q.y, q.z);
 }
 // c[0 .. p0) = 0
 template <typename T>

@@ -99,6 +99,23 @@ void launch_weight32(const Geom &g, const double *nvert, float *wgt32, cudaStrea
   k_weight32<<<nblk(g.n(), 256) < 4096 ? nblk(g.n(), 256) : 4096, 256, 0, s>>>(g.n(), nvert, wgt32); count_launch();
 }
 
+// Any non-zero cross-derivative coefficient (FP32 flux form, after the form
+// scaling) or edge weight (FP64 rows) on the level.
+__global__ void k_cross_flags(size_t n, const float *__restrict__ gf, const double *__restrict__ w, int *flags) {
+  bool f32 = false, f64 = false;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    f32 |= gf[1 * n + p] != 0.0f || gf[2 * n + p] != 0.0f || gf[3 * n + p] != 0.0f || gf[5 * n + p] != 0.0f ||
+           gf[6 * n + p] != 0.0f || gf[7 * n + p] != 0.0f;
+    for (int s = NE; s <= BW; s++) f64 |= w[(size_t)s * n + p] != 0.0;
+  }
+  if (__any_sync(0xffffffffu, f32) && (threadIdx.x & 31) == 0) flags[0] = 1;
+  if (__any_sync(0xffffffffu, f64) && (threadIdx.x & 31) == 0) flags[1] = 1;
+}
+void launch_cross_flags(const Geom &g, const float *gf32, const double *w64, int *flags, cudaStream_t s) {
+  k_cross_flags<<<nblk(g.n(), 256) < 4096 ? nblk(g.n(), 256) : 4096, 256, 0, s>>>(g.n(), gf32, w64, flags);
+  count_launch();
+}
+
 void launch_codes(const Geom &g, const double *nvert, uint32_t *code, cudaStream_t s) {
   k_codes<<<nblk(g.n(), 256), 256, 0, s>>>(g, nvert, code); count_launch();
 }

@@ -6,21 +6,24 @@ namespace cvb {
 
 static inline unsigned nblk(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-template <typename TX>
+// X (every operator kernel): the level has cross-derivative terms; kernels for
+// an orthogonal level (X false) read the seven face points only.
+template <typename TX, bool X>
 __global__ void __launch_bounds__(128) k_apply64(Geom g, const double *__restrict__ w, const uint32_t *__restrict__ code,
                                                  const TX *__restrict__ x, const double *__restrict__ b,
                                                  double *__restrict__ y, const int *gate) {
   dep_sync();
   if (gated(gate)) return;
-  apply64_body<TX>(g, w, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
+  apply64_body<TX, X>(g, w, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+template <bool X>
 __global__ void __launch_bounds__(256) k_apply32(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
                                                  const uint32_t *__restrict__ code, const float *__restrict__ x,
                                                  const float *__restrict__ b, float *__restrict__ y, const int *gate) {
   dep_sync();
   if (gated(gate)) return;
-  apply32_march_body(g, gf, aj, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
+  apply32_march_body<X>(g, gf, aj, code, x, b, y, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 static dim3 march_grid(const Geom &g) {
   MarchGrid m = MarchGrid::of(g);
@@ -31,33 +34,44 @@ static const dim3 kMarchBlk(32, 8, 1);
 static dim3 grid3(const Geom &g) { return dim3(nblk(g.mx, 32), nblk(g.my, 4), g.mz); }
 static const dim3 kBlk(32, 4, 1);
 
+template <typename TX>
+static void apply64(const LevelDev &L, const TX *x, const double *b, double *y, cudaStream_t s) {
+  if (L.cross64) launch_dep(k_apply64<TX, true>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, b, y, L.gate);
+  else launch_dep(k_apply64<TX, false>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, b, y, L.gate);
+}
+static void apply32(const LevelDev &L, const float *x, const float *b, float *y, cudaStream_t s) {
+  if (L.cross32)
+    launch_dep(k_apply32<true>, march_grid(L.g), kMarchBlk, 0, s, L.g, L.gf32, L.ajf32, L.code, x, b, y, L.gate);
+  else
+    launch_dep(k_apply32<false>, march_grid(L.g), kMarchBlk, 0, s, L.g, L.gf32, L.ajf32, L.code, x, b, y, L.gate);
+}
 template <>
 void launch_apply<double>(const LevelDev &L, const double *x, double *y, cudaStream_t s) {
-  launch_dep(k_apply64<double>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, nullptr, y, L.gate);
+  apply64<double>(L, x, nullptr, y, s);
 }
 template <>
 void launch_residual<double>(const LevelDev &L, const double *b, const double *x, double *r, cudaStream_t s) {
-  launch_dep(k_apply64<double>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, b, r, L.gate);
+  apply64<double>(L, x, b, r, s);
 }
 void launch_apply64_from32(const LevelDev &L, const float *x, double *y, cudaStream_t s) {
-  launch_dep(k_apply64<float>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, nullptr, y, L.gate);
+  apply64<float>(L, x, nullptr, y, s);
 }
 template <>
 void launch_apply<float>(const LevelDev &L, const float *x, float *y, cudaStream_t s) {
-  launch_dep(k_apply32, march_grid(L.g), kMarchBlk, 0, s, L.g, L.gf32, L.ajf32, L.code, x, nullptr, y, L.gate);
+  apply32(L, x, nullptr, y, s);
 }
 template <>
 void launch_residual<float>(const LevelDev &L, const float *b, const float *x, float *r, cudaStream_t s) {
-  launch_dep(k_apply32, march_grid(L.g), kMarchBlk, 0, s, L.g, L.gf32, L.ajf32, L.code, x, b, r, L.gate);
+  apply32(L, x, b, r, s);
 }
 
-template <typename T, int TW>
+template <typename T, int TW, bool X>
 __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__restrict__ b, const T *__restrict__ x,
                                                        T *__restrict__ xnew, T omega, int mode) {
   dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  line_sweep_body<T, TW>(L, b, x, xnew, omega, mode, blockIdx.x, blockIdx.y, smem_raw);
+  line_sweep_body<T, TW, X>(L, b, x, xnew, omega, mode, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // RR: the line layout's rows per lane fixed at compile time (0: read from my)
@@ -70,12 +84,12 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, con
   line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color, rsplit != 0);
 }
 
-template <typename T>
+template <typename T, bool X>
 __global__ void __launch_bounds__(128) k_resid_color(LevelDev L, const T *__restrict__ x, const T *__restrict__ b,
                                                      T *__restrict__ r, int color) {
   dep_sync();
   if (gated(L.gate)) return;
-  resid_color_body<T>(L, x, b, r, color, blockIdx.x, blockIdx.y, blockIdx.z);
+  resid_color_body<T, X>(L, x, b, r, color, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 // mode 0: zero initial guess (residual = b); 1: residual b - A x computed in
 // the sweep (fused); 2: `b` already holds the residual of x (split variant).
@@ -85,10 +99,12 @@ static void line_sweep(const LevelDev &L, const T *b, const T *x, T *xnew, T ome
   dim3 grd(nblk(L.g.mx, TW), L.g.mz);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_line_sweep<T, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_line_sweep<T, TW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_line_sweep<T, TW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  launch_dep(k_line_sweep<T, TW>, grd, 256, smem, s, L, b, x, xnew, omega, mode);
+  if (has_cross<T>(L)) launch_dep(k_line_sweep<T, TW, true>, grd, 256, smem, s, L, b, x, xnew, omega, mode);
+  else launch_dep(k_line_sweep<T, TW, false>, grd, 256, smem, s, L, b, x, xnew, omega, mode);
 }
 
 
@@ -219,7 +235,8 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
   const T *r = b;
   if (!zero) {
     dim3 grd(color_tiles_x(L.g), nblk(L.g.my, 4), L.g.mz);
-    launch_dep(k_resid_color<T>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
+    if (has_cross<T>(L)) launch_dep(k_resid_color<T, true>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
+    else launch_dep(k_resid_color<T, false>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
     r = res;
   }
   line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);

@@ -57,7 +57,10 @@ __device__ __forceinline__ Star<T> load_star(const TX *__restrict__ x, int p, co
 // (A x)_p with the 19 stored weights; identity rows return x_p.  Every load of
 // the row is issued before anything depends on one of them (the row's code
 // included), so a row costs one memory latency, not a chain of them.
-template <typename TX>
+// X: the level has cross-derivative weights; without them (an orthogonal grid,
+// the 12 edge slots all zero) only the seven face slots are read, which gives
+// the same sum: every skipped term is an fma with a zero weight.
+template <typename TX, bool X = true>
 __device__ __forceinline__ double row64(const Geom &g, const double *__restrict__ w, const uint32_t *__restrict__ code,
                                         const TX *__restrict__ x, int i, int j, int k, int p, int n) {
   if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return (double)x[p];
@@ -69,12 +72,14 @@ __device__ __forceinline__ double row64(const Geom &g, const double *__restrict_
   r = fma(__ldg(wp + (size_t)EP * n), s.E, r); r = fma(__ldg(wp + (size_t)WP * n), s.W, r);
   r = fma(__ldg(wp + (size_t)NP * n), s.N, r); r = fma(__ldg(wp + (size_t)SP * n), s.S, r);
   r = fma(__ldg(wp + (size_t)TP * n), s.Tt, r); r = fma(__ldg(wp + (size_t)BP * n), s.B, r);
-  r = fma(__ldg(wp + (size_t)NE * n), s.NE, r); r = fma(__ldg(wp + (size_t)SE * n), s.SE, r);
-  r = fma(__ldg(wp + (size_t)NW * n), s.NW, r); r = fma(__ldg(wp + (size_t)SW * n), s.SW, r);
-  r = fma(__ldg(wp + (size_t)TN * n), s.TN, r); r = fma(__ldg(wp + (size_t)BN * n), s.BN, r);
-  r = fma(__ldg(wp + (size_t)TS * n), s.TS, r); r = fma(__ldg(wp + (size_t)BS * n), s.BS, r);
-  r = fma(__ldg(wp + (size_t)TE * n), s.TE, r); r = fma(__ldg(wp + (size_t)BE * n), s.BE, r);
-  r = fma(__ldg(wp + (size_t)TW * n), s.TW, r); r = fma(__ldg(wp + (size_t)BW * n), s.BW, r);
+  if constexpr (X) {
+    r = fma(__ldg(wp + (size_t)NE * n), s.NE, r); r = fma(__ldg(wp + (size_t)SE * n), s.SE, r);
+    r = fma(__ldg(wp + (size_t)NW * n), s.NW, r); r = fma(__ldg(wp + (size_t)SW * n), s.SW, r);
+    r = fma(__ldg(wp + (size_t)TN * n), s.TN, r); r = fma(__ldg(wp + (size_t)BN * n), s.BN, r);
+    r = fma(__ldg(wp + (size_t)TS * n), s.TS, r); r = fma(__ldg(wp + (size_t)BS * n), s.BS, r);
+    r = fma(__ldg(wp + (size_t)TE * n), s.TE, r); r = fma(__ldg(wp + (size_t)BE * n), s.BE, r);
+    r = fma(__ldg(wp + (size_t)TW * n), s.TW, r); r = fma(__ldg(wp + (size_t)BW * n), s.BW, r);
+  }
   return (c & CODE_IDENTITY) ? s.P : r;
 }
 
@@ -94,7 +99,10 @@ __device__ __forceinline__ float act(uint32_t c, uint32_t bit) { return (c & bit
 // branch codes; the lower faces are the upper faces of the W/S/B neighbours.
 // Loads first (all unconditional, in bounds for interior cells), then the
 // arithmetic with the activity bits as 0/1 factors.
-template <typename TX>
+// X: the level has cross-derivative coefficients; without them (an orthogonal
+// grid) each face flux is its normal term alone and only the seven face
+// values of x are read.
+template <typename TX, bool X = true>
 __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ gf, const float *__restrict__ aj,
                                        const uint32_t *__restrict__ code, const TX *__restrict__ x, int i, int j,
                                        int k, int p, int n) {
@@ -110,18 +118,22 @@ __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ 
   const float s21 = __ldg(gf + 3 * n + ps), s22 = __ldg(gf + 4 * n + ps), s23 = __ldg(gf + 5 * n + ps);
   const float b31 = __ldg(gf + 6 * n + pb), b32 = __ldg(gf + 7 * n + pb), b33 = __ldg(gf + 8 * n + pb);
   const float ajp = __ldg(aj + p);
-  float fe = g11 * (s.E - s.P) + cross32(code_branch(c, 0, 0), g12, s.N + s.NE, s.P + s.E, s.S + s.SE) +
-             cross32(code_branch(c, 0, 1), g13, s.Tt + s.TE, s.P + s.E, s.B + s.BE);
-  float fw = w11 * (s.P - s.W) + cross32(code_branch(cw, 0, 0), w12, s.NW + s.N, s.W + s.P, s.SW + s.S) +
-             cross32(code_branch(cw, 0, 1), w13, s.TW + s.Tt, s.W + s.P, s.BW + s.B);
-  float fn = g22 * (s.N - s.P) + cross32(code_branch(c, 1, 0), g21, s.E + s.NE, s.P + s.N, s.W + s.NW) +
-             cross32(code_branch(c, 1, 1), g23, s.Tt + s.TN, s.P + s.N, s.B + s.BN);
-  float fs = s22 * (s.P - s.S) + cross32(code_branch(cs, 1, 0), s21, s.SE + s.E, s.S + s.P, s.SW + s.W) +
-             cross32(code_branch(cs, 1, 1), s23, s.TS + s.Tt, s.S + s.P, s.BS + s.B);
-  float ft = g33 * (s.Tt - s.P) + cross32(code_branch(c, 2, 0), g31, s.E + s.TE, s.P + s.Tt, s.W + s.TW) +
-             cross32(code_branch(c, 2, 1), g32, s.N + s.TN, s.P + s.Tt, s.S + s.TS);
-  float fb = b33 * (s.P - s.B) + cross32(code_branch(cb, 2, 0), b31, s.BE + s.E, s.B + s.P, s.BW + s.W) +
-             cross32(code_branch(cb, 2, 1), b32, s.BN + s.N, s.B + s.P, s.BS + s.S);
+  float fe = g11 * (s.E - s.P), fw = w11 * (s.P - s.W), fn = g22 * (s.N - s.P);
+  float fs = s22 * (s.P - s.S), ft = g33 * (s.Tt - s.P), fb = b33 * (s.P - s.B);
+  if constexpr (X) {
+    fe = fe + cross32(code_branch(c, 0, 0), g12, s.N + s.NE, s.P + s.E, s.S + s.SE) +
+         cross32(code_branch(c, 0, 1), g13, s.Tt + s.TE, s.P + s.E, s.B + s.BE);
+    fw = fw + cross32(code_branch(cw, 0, 0), w12, s.NW + s.N, s.W + s.P, s.SW + s.S) +
+         cross32(code_branch(cw, 0, 1), w13, s.TW + s.Tt, s.W + s.P, s.BW + s.B);
+    fn = fn + cross32(code_branch(c, 1, 0), g21, s.E + s.NE, s.P + s.N, s.W + s.NW) +
+         cross32(code_branch(c, 1, 1), g23, s.Tt + s.TN, s.P + s.N, s.B + s.BN);
+    fs = fs + cross32(code_branch(cs, 1, 0), s21, s.SE + s.E, s.S + s.P, s.SW + s.W) +
+         cross32(code_branch(cs, 1, 1), s23, s.TS + s.Tt, s.S + s.P, s.BS + s.B);
+    ft = ft + cross32(code_branch(c, 2, 0), g31, s.E + s.TE, s.P + s.Tt, s.W + s.TW) +
+         cross32(code_branch(c, 2, 1), g32, s.N + s.TN, s.P + s.Tt, s.S + s.TS);
+    fb = fb + cross32(code_branch(cb, 2, 0), b31, s.BE + s.E, s.B + s.P, s.BW + s.W) +
+         cross32(code_branch(cb, 2, 1), b32, s.BN + s.N, s.B + s.P, s.BS + s.S);
+  }
   float acc = act(c, CODE_ACT_E) * fe - act(c, CODE_ACT_W) * fw + act(c, CODE_ACT_N) * fn -
               act(c, CODE_ACT_S) * fs + act(c, CODE_ACT_T) * ft - act(c, CODE_ACT_B) * fb;
   return (c & CODE_IDENTITY) ? s.P : -ajp * acc;
@@ -131,7 +143,7 @@ __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ 
 // y = A x (b == nullptr) or y = b - A x.  One thread per cell.
 // Bodies take the block's coordinates explicitly so that the grouped (batched)
 // kernels can run them for any problem of a work-list; blocks are 32 x 4.
-template <typename TX>
+template <typename TX, bool X = true>
 __device__ __forceinline__ void apply64_body(const Geom &g, const double *__restrict__ w,
                                              const uint32_t *__restrict__ code, const TX *__restrict__ x,
                                              const double *__restrict__ b, double *__restrict__ y, int bx, int by,
@@ -139,7 +151,7 @@ __device__ __forceinline__ void apply64_body(const Geom &g, const double *__rest
   int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
   if (i >= g.mx || j >= g.my) return;
   int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
-  double ax = row64(g, w, code, x, i, j, k, p, n);
+  double ax = row64<TX, X>(g, w, code, x, i, j, k, p, n);
   y[p] = b ? b[p] - ax : ax;
 }
 
@@ -187,6 +199,8 @@ __device__ __forceinline__ int wrap_read(int i, int m, int per) {
 }
 
 // y = A x (b == nullptr) or y = b - A x on the tile (bx, by, bz); 32 x 8 threads.
+// X: the level has cross-derivative coefficients (see row32).
+template <bool X = true>
 __device__ __forceinline__ void apply32_march_body(const Geom &g, const float *__restrict__ gf,
                                                    const float *__restrict__ aj, const uint32_t *__restrict__ code,
                                                    const float *__restrict__ x, const float *__restrict__ b,
@@ -210,14 +224,21 @@ __device__ __forceinline__ void apply32_march_body(const Geom &g, const float *_
   {
     const int kb = k0 - 1;
     const int ob = wrap_read(kb, mz, g.pz) * pl, ot = wrap_read(k0, mz, g.pz) * pl;
-    P = x[ob + cP]; E = x[ob + cE]; N = x[ob + cN]; W = x[ob + cW]; S = x[ob + cS];
-    const float T = x[ot + cP], TE = x[ot + cE], TN = x[ot + cN], TW = x[ot + cW], TS = x[ot + cS];
+    P = x[ob + cP]; E = x[ob + cE]; N = x[ob + cN];
+    W = X ? x[ob + cW] : 0.f;
+    S = X ? x[ob + cS] : 0.f;
+    const float T = x[ot + cP], TE = x[ot + cE], TN = x[ot + cN];
+    const float TW = X ? x[ot + cW] : 0.f, TS = X ? x[ot + cS] : 0.f;
     if (kb >= 0 && col) {
       const int q = kb * pl + cown;
-      const uint32_t c = __ldg(code + q);
-      const float g31 = __ldg(gf + 6 * n + q), g32 = __ldg(gf + 7 * n + q), g33 = __ldg(gf + 8 * n + q);
-      ftp = g33 * (T - P) + cross32(code_branch(c, 2, 0), g31, E + TE, P + T, W + TW) +
-            cross32(code_branch(c, 2, 1), g32, N + TN, P + T, S + TS);
+      const float g33 = __ldg(gf + 8 * n + q);
+      ftp = g33 * (T - P);
+      if constexpr (X) {
+        const uint32_t c = __ldg(code + q);
+        const float g31 = __ldg(gf + 6 * n + q), g32 = __ldg(gf + 7 * n + q);
+        ftp = ftp + cross32(code_branch(c, 2, 0), g31, E + TE, P + T, W + TW) +
+              cross32(code_branch(c, 2, 1), g32, N + TN, P + T, S + TS);
+      }
     }
     B = P; BE = E; BN = N;
     P = T; E = TE; N = TN; W = TW; S = TS;
@@ -230,17 +251,24 @@ __device__ __forceinline__ void apply32_march_body(const Geom &g, const float *_
   };
   auto load = [&](int k, Plane &v) {
     const int op = wrap_read(k, mz, g.pz) * pl, ot = wrap_read(k + 1, mz, g.pz) * pl;
-    v.T = x[ot + cP]; v.TE = x[ot + cE]; v.TN = x[ot + cN]; v.TW = x[ot + cW]; v.TS = x[ot + cS];
-    v.NE = x[op + cNE]; v.SE = x[op + cSE]; v.NW = x[op + cNW];
+    v.T = x[ot + cP]; v.TE = x[ot + cE]; v.TN = x[ot + cN];
+    v.TW = v.TS = v.NE = v.SE = v.NW = 0.f;
+    if constexpr (X) {
+      v.TW = x[ot + cW]; v.TS = x[ot + cS];
+      v.NE = x[op + cNE]; v.SE = x[op + cSE]; v.NW = x[op + cNW];
+    }
     v.c = CODE_IDENTITY;
     v.g11 = v.g12 = v.g13 = v.g21 = v.g22 = v.g23 = v.g31 = v.g32 = v.g33 = 0.f;
     v.ajp = v.bp = v.xo = 0.f;
     if (col) {
       const int q = k * pl + cown;
       v.c = __ldg(code + q);
-      v.g11 = __ldg(gf + q); v.g12 = __ldg(gf + n + q); v.g13 = __ldg(gf + 2 * n + q);
-      v.g21 = __ldg(gf + 3 * n + q); v.g22 = __ldg(gf + 4 * n + q); v.g23 = __ldg(gf + 5 * n + q);
-      v.g31 = __ldg(gf + 6 * n + q); v.g32 = __ldg(gf + 7 * n + q); v.g33 = __ldg(gf + 8 * n + q);
+      v.g11 = __ldg(gf + q); v.g22 = __ldg(gf + 4 * n + q); v.g33 = __ldg(gf + 8 * n + q);
+      if constexpr (X) {
+        v.g12 = __ldg(gf + n + q); v.g13 = __ldg(gf + 2 * n + q);
+        v.g21 = __ldg(gf + 3 * n + q); v.g23 = __ldg(gf + 5 * n + q);
+        v.g31 = __ldg(gf + 6 * n + q); v.g32 = __ldg(gf + 7 * n + q);
+      }
       v.ajp = __ldg(aj + q);
       if (b && out) v.bp = b[q];
       if (out && (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1)) v.xo = x[q];
@@ -256,12 +284,15 @@ __device__ __forceinline__ void apply32_march_body(const Geom &g, const float *_
     const int q = k * pl + cown;
     const bool ring = i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1;
     const float xo = ring ? v.xo : P;
-    const float fe = v.g11 * (E - P) + cross32(code_branch(c, 0, 0), v.g12, N + NE, P + E, S + SE) +
-                     cross32(code_branch(c, 0, 1), v.g13, T + TE, P + E, B + BE);
-    const float fn = v.g22 * (N - P) + cross32(code_branch(c, 1, 0), v.g21, E + NE, P + N, W + NW) +
-                     cross32(code_branch(c, 1, 1), v.g23, T + TN, P + N, B + BN);
-    const float ft = v.g33 * (T - P) + cross32(code_branch(c, 2, 0), v.g31, E + TE, P + T, W + TW) +
-                     cross32(code_branch(c, 2, 1), v.g32, N + TN, P + T, S + TS);
+    float fe = v.g11 * (E - P), fn = v.g22 * (N - P), ft = v.g33 * (T - P);
+    if constexpr (X) {
+      fe = fe + cross32(code_branch(c, 0, 0), v.g12, N + NE, P + E, S + SE) +
+           cross32(code_branch(c, 0, 1), v.g13, T + TE, P + E, B + BE);
+      fn = fn + cross32(code_branch(c, 1, 0), v.g21, E + NE, P + N, W + NW) +
+           cross32(code_branch(c, 1, 1), v.g23, T + TN, P + N, B + BN);
+      ft = ft + cross32(code_branch(c, 2, 0), v.g31, E + TE, P + T, W + TW) +
+           cross32(code_branch(c, 2, 1), v.g32, N + TN, P + T, S + TS);
+    }
     const float fw = __shfl_up_sync(0xffffffffu, fe, 1);
     shn[k & 1][w][lane] = fn;
     __syncthreads();
@@ -292,15 +323,17 @@ template <typename T>
 struct RowOf;
 template <>
 struct RowOf<float> {
+  template <bool X = true>
   __device__ static float r(const Geom &g, const LevelDev &L, const float *x, int i, int j, int k, int p, int n) {
-    return row32(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
+    return row32<float, X>(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
   }
   __device__ static const float *fac(const LevelDev &L) { return L.line32; }
 };
 template <>
 struct RowOf<double> {
+  template <bool X = true>
   __device__ static double r(const Geom &g, const LevelDev &L, const double *x, int i, int j, int k, int p, int n) {
-    return row64(g, L.w64, L.code, x, i, j, k, p, n);
+    return row64<double, X>(g, L.w64, L.code, x, i, j, k, p, n);
   }
   __device__ static const double *fac(const LevelDev &L) { return L.line64; }
 };
@@ -362,7 +395,7 @@ __device__ __forceinline__ void warp_line_solve(T *r, const T *a, const T *m, co
 // threads compute the tile's residuals and stage the Thomas factors in shared
 // memory (laid out line by line).  Phase 2: each warp solves TW/8 lines with
 // warp_line_solve.  Phase 3: all threads write x + omega*delta.
-template <typename T, int TW>
+template <typename T, int TW, bool X = true>
 __device__ __forceinline__ void line_sweep_body(const LevelDev &L, const T *__restrict__ b, const T *__restrict__ x,
                                                 T *__restrict__ xnew, T omega, int mode, int bx, int bk,
                                                 unsigned char *smem_raw) {
@@ -384,7 +417,7 @@ __device__ __forceinline__ void line_sweep_body(const LevelDev &L, const T *__re
     if (line && j >= 1 && j <= my - 2) {
       const T *f = fa + F.line(i, k) + (j - 1);
       a = __ldg(f); m = __ldg(f + F.Q); c = __ldg(f + 2 * F.Q);
-      r = (mode == 1) ? b[p] - RowOf<T>::r(g, L, x, i, j, k, p, n) : b[p];
+      r = (mode == 1) ? b[p] - RowOf<T>::template r<X>(g, L, x, i, j, k, p, n) : b[p];
     }
     sr[tx * my + j] = r; sa[tx * my + j] = a; sm[tx * my + j] = m; sc[tx * my + j] = c;
   }
@@ -727,6 +760,12 @@ __host__ __device__ inline int solve_tiles_x(const Geom &g, int color) {
   return color < 0 ? (g.mx + TW - 1) / TW : ((g.mx + 1) / 2 + TW - 1) / TW;
 }
 
+// Whether a level's operator in precision T has cross-derivative terms.
+template <typename T>
+__host__ __device__ inline bool has_cross(const LevelDev &L) {
+  return sizeof(T) == 4 ? L.cross32 != 0 : L.cross64 != 0;
+}
+
 // Residual b - A x on the cells of one zebra color ((i + k) % 2 == color), one
 // thread per cell of that color, 32 x 4 threads, written in the colour-split
 // row layout (SplitRow).
@@ -734,24 +773,26 @@ template <typename T>
 struct ColorRow;
 template <>
 struct ColorRow<float> {
+  template <bool X>
   __device__ static float r(const Geom &g, const LevelDev &L, const float *x, int i, int j, int k, int p, int n) {
-    return row32(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
+    return row32<float, X>(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
   }
 };
 template <>
 struct ColorRow<double> {
+  template <bool X>
   __device__ static double r(const Geom &g, const LevelDev &L, const double *x, int i, int j, int k, int p, int n) {
-    return row64(g, L.w64, L.code, x, i, j, k, p, n);
+    return row64<double, X>(g, L.w64, L.code, x, i, j, k, p, n);
   }
 };
-template <typename T>
+template <typename T, bool X = true>
 __device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__restrict__ x, const T *__restrict__ b,
                                                  T *__restrict__ r, int color, int bx, int by, int k) {
   const Geom g = L.g;
   const int i = 2 * (bx * 32 + threadIdx.x) + ((color + k) & 1), j = by * 4 + threadIdx.y;
   if (i >= g.mx || j >= g.my) return;
   const int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
-  r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::r(g, L, x, i, j, k, p, n);
+  r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::template r<X>(g, L, x, i, j, k, p, n);
 }
 __host__ __device__ inline int color_tiles_x(const Geom &g) { return ((g.mx + 1) / 2 + 31) / 32; }
 

@@ -258,6 +258,12 @@ class PoissonContext:
         self._check(self._L.cvb_apply_operator_f32(self._ctx, level, ptr(xx), ptr(y)))
         return y
 
+    def level_cross(self, level):
+        """(FP32, FP64) flags: the level's operator has cross-derivative terms."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.cvb_level_cross(self._ctx, level, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def weights(self, level):
         w = np.zeros((19,) + self.shapes[level])
         self._check(self._L.cvb_get_weights(self._ctx, level, ptr(w)))

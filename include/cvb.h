@@ -178,6 +178,11 @@ int cvb_apply_operator_f32(cvb_ctx *ctx, int level, const float *x, float *y);
 /* The 19 stored weights of every row, [19][mz][my][mx], slots in the reference's
  * CP,EP,WP,NP,SP,TP,BP,NE,SE,NW,SW,TN,BN,TS,BS,TE,BE,TW,BW order. */
 int cvb_get_weights(cvb_ctx *ctx, int level, double *w);
+/* Whether the level's operator has cross-derivative terms: *cross32 for the FP32
+ * flux form, *cross64 for the FP64 rows (any of the 12 edge weights non-zero).
+ * On an orthogonal grid both are 0 and the operator kernels read the seven face
+ * points only.  No counterpart in the reference (which always assembles 19). */
+int cvb_level_cross(const cvb_ctx *ctx, int level, int *cross32, int *cross64);
 /* MyRestriction (poisson.c:129) from level+1 to level; MyInterpolation
  * (poisson.c:265) from level-1 to level (returned, not added). */
 int cvb_restrict(cvb_ctx *ctx, int coarse_level, const double *xf, double *xc);
