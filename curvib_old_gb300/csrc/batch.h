@@ -102,6 +102,7 @@ void glaunch_line_sweep(const TaskList &tl, bool f32, float omega32, double omeg
 void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);
 // zebra: residual on the cells of color p0 (a = x, b = rhs, c = r); zero fill of c[0..p0)
 void glaunch_resid_color(const TaskList &tl, bool f32, cudaStream_t s);
+void glaunch_zebra_fused(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);
 void glaunch_zero(const TaskList &tl, bool f32, cudaStream_t s);
 // dense coarsest solve: a = r, b = Minv, c = e, p0 = n
 void glaunch_dense(const TaskList &tl, bool f32, cudaStream_t s);

@@ -392,9 +392,9 @@ static int build_operators(cvb_ctx *ctx) {
 // other work loads the GPU) take the same variant, and so the same rounding.
 namespace {
 struct ShapeKey {
-  int mx, my, mz, px, py, pz;
+  int mx, my, mz, px, py, pz, c32, c64;  // box, periodicity, cross-derivative flags
   bool operator<(const ShapeKey &o) const {
-    return std::tie(mx, my, mz, px, py, pz) < std::tie(o.mx, o.my, o.mz, o.px, o.py, o.pz);
+    return std::tie(mx, my, mz, px, py, pz, c32, c64) < std::tie(o.mx, o.my, o.mz, o.px, o.py, o.pz, o.c32, o.c64);
   }
 };
 std::mutex g_tune_mu;
@@ -402,7 +402,8 @@ std::map<ShapeKey, cvb_ctx::Tune> g_tune_cache;
 bool g_tune_loaded = false;
 
 // With CVB_TUNE_FILE set, measured choices persist in that text file (one
-// shape per line: mx my mz px py pz and the four timings in microseconds), so a
+// shape per line: mx my mz px py pz, the two cross-term flags and the eight
+// timings in microseconds), so a
 // later process -- a profiler run, say, whose own timings would be distorted --
 // makes the same choices.  Called with g_tune_mu held.
 void tune_file_load() {
@@ -414,8 +415,9 @@ void tune_file_load() {
   if (!f) return;
   ShapeKey k;
   cvb_ctx::Tune t;
-  while (std::fscanf(f, "%d %d %d %d %d %d %lf %lf %lf %lf", &k.mx, &k.my, &k.mz, &k.px, &k.py, &k.pz, &t.us32[0],
-                     &t.us32[1], &t.us64[0], &t.us64[1]) == 10) {
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf", &k.mx, &k.my, &k.mz, &k.px, &k.py,
+                     &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0], &t.us64[1], &t.zb32[0], &t.zb32[1],
+                     &t.zb64[0], &t.zb64[1]) == 16) {
     t.level = 0;
     t.cells = (size_t)k.mx * k.my * k.mz;
     g_tune_cache.emplace(k, t);
@@ -427,8 +429,9 @@ void tune_file_append(const ShapeKey &k, const cvb_ctx::Tune &t) {
   if (!path || !*path) return;
   FILE *f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "%d %d %d %d %d %d %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz, k.px, k.py, k.pz, t.us32[0], t.us32[1],
-               t.us64[0], t.us64[1]);
+  std::fprintf(f, "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz, k.px, k.py,
+               k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0], t.zb32[1], t.zb64[0],
+               t.zb64[1]);
   std::fclose(f);
 }
 }  // namespace
@@ -438,7 +441,14 @@ static int autotune_sweeps(cvb_ctx *ctx) {
   for (int l = 0; l < ctx->nlevels; l++) {
     LevelDev &L = ctx->L[l];
     size_t n = L.g.n();
-    const ShapeKey key{L.g.mx, L.g.my, L.g.mz, L.g.px, L.g.py, L.g.pz};
+    const ShapeKey key{L.g.mx, L.g.my, L.g.mz, L.g.px, L.g.py, L.g.pz, L.cross32, L.cross64};
+    // the faster form of each sweep: a zero fused timing means not fusable
+    auto pick = [&L](const cvb_ctx::Tune &t) {
+      L.sweep32 = t.us32[1] < t.us32[0] ? 1 : 0;
+      L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
+      L.zfuse32 = t.zb32[1] > 0.0 && t.zb32[1] < t.zb32[0] ? 1 : 0;
+      L.zfuse64 = t.zb64[1] > 0.0 && t.zb64[1] < t.zb64[0] ? 1 : 0;
+    };
     {
       std::lock_guard<std::mutex> lock(g_tune_mu);
       tune_file_load();
@@ -446,8 +456,7 @@ static int autotune_sweeps(cvb_ctx *ctx) {
       if (it != g_tune_cache.end()) {
         cvb_ctx::Tune t = it->second;
         t.level = l;
-        L.sweep32 = t.us32[1] < t.us32[0] ? 1 : 0;
-        L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
+        pick(t);
         ctx->tune.push_back(t);
         continue;
       }
@@ -475,8 +484,27 @@ static int autotune_sweeps(cvb_ctx *ctx) {
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         (prec == 0 ? t.us32 : t.us64)[v] = 1e3 * ms / reps;
       }
-    L.sweep32 = t.us32[1] < t.us32[0] ? 1 : 0;
-    L.sweep64 = t.us64[1] < t.us64[0] ? 1 : 0;
+    // zebra half-sweep: two kernels, then (where possible) the fused kernel
+    for (int prec = 0; prec < 2; prec++)
+      for (int v = 0; v < 2; v++) {
+        double *zb = prec == 0 ? t.zb32 : t.zb64;
+        const bool ok = prec == 0 ? zebra_fusable<float>(L) : zebra_fusable<double>(L);
+        if (v == 1 && !ok) { zb[1] = 0.0; continue; }
+        if (prec == 0) L.zfuse32 = v; else L.zfuse64 = v;
+        const int reps = 3;
+        for (int q = 0; q <= reps; q++) {
+          if (q == 1) CK(cudaEventRecord(ctx->ev0, ctx->stream));
+          if (prec == 0) launch_zebra_half<float>(L, L.r32, L.e32, L.t32 + n, 1.3f, 1, false, ctx->stream);
+          else launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream);
+        }
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        CKL();
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        zb[v] = 1e3 * ms / reps;
+      }
+    pick(t);
     ctx->tune.push_back(t);
     std::lock_guard<std::mutex> lock(g_tune_mu);
     if (g_tune_cache.emplace(key, t).second) tune_file_append(key, t);
@@ -1350,11 +1378,15 @@ int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
   for (size_t q = 0; q < ctx->tune.size(); q++) {
     const auto &t = ctx->tune[q];
     char row[512];
+    const LevelDev &L = ctx->L[t.level];
     snprintf(row, sizeof row,
              "%s{\"level\": %d, \"cells\": %zu, \"f32\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
-             "\"f64\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}}",
-             q ? ", " : "", t.level, t.cells, t.us32[0], t.us32[1], ctx->L[t.level].sweep32 ? "split" : "fused",
-             t.us64[0], t.us64[1], ctx->L[t.level].sweep64 ? "split" : "fused");
+             "\"f64\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
+             "\"zebra_f32\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"choice\": \"%s\"}, "
+             "\"zebra_f64\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"choice\": \"%s\"}}",
+             q ? ", " : "", t.level, t.cells, t.us32[0], t.us32[1], L.sweep32 ? "split" : "fused", t.us64[0],
+             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], L.zfuse32 ? "fused" : "split", t.zb64[0],
+             t.zb64[1], L.zfuse64 ? "fused" : "split");
     o += row;
   }
   o += "]}";

@@ -60,7 +60,7 @@ struct Done {
 // Sink of the ops of one round, grouped by schedule key and kernel kind.
 enum OpKind {
   OK_RES32, OK_RES64, OK_RESTRICT, OK_PROLONG, OK_SWEEP, OK_SOLVE, OK_DENSE, OK_COPY, OK_CONV, OK_WIDEN,
-  OK_ZERO, OK_RESC, OK_COUNT
+  OK_ZERO, OK_RESC, OK_ZFUSED, OK_COUNT
 };
 
 struct OpBatch {
@@ -222,6 +222,12 @@ static void gen_zebra_half(VSink &vs, long long k0, long long k1, LevelDev &L, c
   const int SW = f32 ? kSolveTW32 : kSolveTW64;
   const size_t sso = f32 ? line_solve_smem<float, kSolveTW32>(L.g) : line_solve_smem<double, kSolveTW64>(L.g);
   T *res = lvec<T>(L, 3);
+  const bool fuse = f32 ? L.zfuse32 != 0 : L.zfuse64 != 0;
+  if (!zero && fuse && zebra_fusable<T>(L) && L.g.my <= 400 && sso <= 200 * 1024) {
+    const int gx = f32 ? solve_tiles_x<kSolveTW32>(L.g, color) : solve_tiles_x<kSolveTW64>(L.g, color);
+    vs.add(k1, OK_ZFUSED, task(dLv, b, nullptr, x, gate, gx, 0, 0, color + 1), gx * L.g.mz, sso);
+    return;
+  }
   const T *r = b;
   if (!zero) {
     const int gx = color_tiles_x(L.g), gy = nblk(L.g.my, 4);
@@ -326,6 +332,7 @@ static void run_program(cvb_batch *bt, std::map<long long, std::array<Lists, OK_
           case OK_WIDEN: glaunch_elementwise(ob.tl, 3, s); break;
           case OK_ZERO: glaunch_zero(ob.tl, f32, s); break;
           case OK_RESC: glaunch_resid_color(ob.tl, f32, s); break;
+          case OK_ZFUSED: glaunch_zebra_fused(ob.tl, f32, w32, w64, ob.smem, s); break;
           default: break;
         }
       }

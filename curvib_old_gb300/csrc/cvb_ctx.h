@@ -89,7 +89,9 @@ struct cvb_ctx {
   bool ready = false;
   std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)
   // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
-  struct Tune { int level; size_t cells; double us32[2], us64[2]; };
+  // set-up timings (microseconds): Jacobi line sweep fused / split, zebra
+  // half-sweep split / fused (0 where the level cannot use the fused form)
+  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2]; };
   std::vector<Tune> tune;
 };
 

@@ -100,6 +100,7 @@ struct LevelDev {
   // the operator has cross-derivative terms (FP32 flux form / FP64 edge
   // weights); 0 on an orthogonal grid, where the kernels read 7 points
   int cross32, cross64;
+  int zfuse32, zfuse64;     // zebra half-sweep variant chosen at set-up: 0 two kernels, 1 fused
   // coarsest level only: the densely inverted cells (first cm of cidx) and the
   // identity ones (the rest of cidx)
   const int *cidx;
@@ -111,6 +112,20 @@ struct LevelDev {
 };
 
 __device__ __forceinline__ bool gated(const int *gate) { return gate && *gate; }
+
+// Whether a level's operator in precision T has cross-derivative terms.
+template <typename T>
+__host__ __device__ inline bool has_cross(const LevelDev &L) {
+  return sizeof(T) == 4 ? L.cross32 != 0 : L.cross64 != 0;
+}
+
+// The fused zebra half-sweep's condition (see zebra_fused_body): no
+// cross-derivative terms, and colours kept apart across periodic seams.
+template <typename T>
+__host__ __device__ inline bool zebra_fusable(const LevelDev &L) {
+  return !has_cross<T>(L) && (!L.g.px || (L.g.mx & 1) == 0) && (!L.g.pz || (L.g.mz & 1) == 0);
+}
+
 
 // --- kernel launchers (defined in the .cu files) ---------------------------
 // setup

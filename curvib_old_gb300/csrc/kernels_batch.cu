@@ -108,6 +108,18 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_c
   line_solve_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw,
                          (K.p1 & 15) - 1, (K.p1 >> 4) != 0);
 }
+// zebra half-sweep in one kernel (levels without cross terms): b = a, x = c,
+// colour p1 - 1
+template <typename T, int TW>
+__global__ void __launch_bounds__(kSolveThreads, 4) kg_zebra_fused(const __grid_constant__ TaskList tl, T omega) {
+  dep_sync();
+  const GTask &K = tl.t[find_task(tl, blockIdx.x)];
+  if (gated(K.gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const LevelDev L = *K.L;
+  int lb = blockIdx.x - K.block0;
+  zebra_fused_body<T, TW>(L, (const T *)K.a, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw, K.p1 - 1);
+}
 // zebra: residual on the cells of color p0
 template <typename T>
 __global__ void __launch_bounds__(128) kg_resid_color(const __grid_constant__ TaskList tl) {
@@ -220,6 +232,17 @@ void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omeg
   }
   if (f32) launch_dep(kg_line_solve<float, kSolveTW32>, tl.nblocks, kSolveThreads, smem, s, tl, omega32);
   else launch_dep(kg_line_solve<double, kSolveTW64>, tl.nblocks, kSolveThreads, smem, s, tl, omega64);
+}
+void glaunch_zebra_fused(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s) {
+  if (!tl.n) return;
+  static bool attr = false;
+  if (!attr) {
+    allow_smem(kg_zebra_fused<float, kSolveTW32>);
+    allow_smem(kg_zebra_fused<double, kSolveTW64>);
+    attr = true;
+  }
+  if (f32) launch_dep(kg_zebra_fused<float, kSolveTW32>, tl.nblocks, kSolveThreads, smem, s, tl, omega32);
+  else launch_dep(kg_zebra_fused<double, kSolveTW64>, tl.nblocks, kSolveThreads, smem, s, tl, omega64);
 }
 void glaunch_dense(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;

@@ -84,6 +84,15 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, con
   line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color, rsplit != 0);
 }
 
+template <typename T, int TW, int RR>
+__global__ void __launch_bounds__(kSolveThreads, 4) k_zebra_fused(LevelDev L, const T *__restrict__ b, T *x, T omega,
+                                                                  int color) {
+  dep_sync();
+  if (gated(L.gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  zebra_fused_body<T, TW, RR>(L, b, x, omega, blockIdx.x, blockIdx.y, smem_raw, color);
+}
+
 template <typename T, bool X>
 __global__ void __launch_bounds__(128) k_resid_color(LevelDev L, const T *__restrict__ x, const T *__restrict__ b,
                                                      T *__restrict__ r, int color) {
@@ -229,9 +238,31 @@ void launch_line_smooth<double>(const LevelDev &L, const double *b, const double
 // color, (i + k) % 2 == color, in place: residual on those lines, then their
 // line solves.  zero: x is zero on entry (the caller zeroed it); only the
 // solves run, on r = b.
+template <typename T, int TW, int RR>
+static void zebra_fused_r(const LevelDev &L, const T *b, T *x, T omega, int color, cudaStream_t s) {
+  dim3 grd(solve_tiles_x<TW>(L.g, color), L.g.mz);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_zebra_fused<T, TW, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  launch_dep(k_zebra_fused<T, TW, RR>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, b, x, omega, color);
+}
+
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s) {
   constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
+  const bool fuse = sizeof(T) == 4 ? L.zfuse32 != 0 : L.zfuse64 != 0;
+  if (!zero && fuse && zebra_fusable<T>(L) && L.g.my <= kMaxFusedRows && line_solve_smem<T, TW>(L.g) <= kMaxSmem) {
+    switch (LineLayout::of(L.g.my).R) {
+      case 1: zebra_fused_r<T, TW, 1>(L, b, x, omega, color, s); break;
+      case 2: zebra_fused_r<T, TW, 2>(L, b, x, omega, color, s); break;
+      case 4: zebra_fused_r<T, TW, 4>(L, b, x, omega, color, s); break;
+      case 8: zebra_fused_r<T, TW, 8>(L, b, x, omega, color, s); break;
+      default: zebra_fused_r<T, TW, 0>(L, b, x, omega, color, s); break;
+    }
+    return;
+  }
   const T *r = b;
   if (!zero) {
     dim3 grd(color_tiles_x(L.g), nblk(L.g.my, 4), L.g.mz);

@@ -639,9 +639,11 @@ struct Vec16<double> {
 // or two cells apart in rows of the caller's layout), the Thomas factors by
 // 16-byte loads of the lines' contiguous runs -- each warp takes whole runs,
 // all of its loads in flight before it stores any.
+// rx: stage r and x (else only the factors, the caller fills r and x).
 template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
-                                                int bx, int k, T *st, int color = -1, bool rsplit = false) {
+                                                int bx, int k, T *st, int color = -1, bool rsplit = false,
+                                                bool rx = true) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   if (!(k >= 1 && k <= g.mz - 2)) return;
@@ -650,7 +652,7 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
   constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
-  if (i >= 1 && i <= mx - 2) {
+  if (rx && i >= 1 && i <= mx - 2) {
     const int col = (k * my) * mx + i;
     for (int j = 1 + ty; j <= my - 2; j += ny) {
       const int p = col + j * mx;
@@ -760,12 +762,6 @@ __host__ __device__ inline int solve_tiles_x(const Geom &g, int color) {
   return color < 0 ? (g.mx + TW - 1) / TW : ((g.mx + 1) / 2 + TW - 1) / TW;
 }
 
-// Whether a level's operator in precision T has cross-derivative terms.
-template <typename T>
-__host__ __device__ inline bool has_cross(const LevelDev &L) {
-  return sizeof(T) == 4 ? L.cross32 != 0 : L.cross64 != 0;
-}
-
 // Residual b - A x on the cells of one zebra color ((i + k) % 2 == color), one
 // thread per cell of that color, 32 x 4 threads, written in the colour-split
 // row layout (SplitRow).
@@ -794,6 +790,44 @@ __device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__r
   const int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
   r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::template r<X>(g, L, x, i, j, k, p, n);
 }
+
+// A zebra half-sweep in one kernel, for levels whose operator has no
+// cross-derivative terms: the 7-point rows couple a line (i, k) only to the
+// lines (i +- 1, k) and (i, k +- 1), all of the other colour, so the lines of
+// one colour are independent and a tile can compute its residual, solve and
+// update its own lines in place without racing another tile.  A periodic wrap
+// in x (z) keeps the colours apart only when mx (mz) is even.  The residual
+// goes straight into shared memory; results equal the two-kernel form.
+
+template <typename T, int TW, int RR = 0>
+__device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__restrict__ b, T *x, T omega, int bx,
+                                                 int k, unsigned char *smem_raw, int color) {
+  const Geom &g = L.g;
+  const int my = g.my, mx = g.mx, n = (int)g.n();
+  T *st = reinterpret_cast<T *>(smem_raw);
+  if (k >= 1 && k <= g.mz - 2) {
+    const LineLayout Lo = LineLayout::fixed<RR>(my);
+    T *sr = st, *sx = st + 4 * Lo.ls * TW;
+    const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
+    constexpr int ny = kSolveThreads / TW;
+    const int i = tile_line(bx, tx, k, TW, color);
+    if (i >= 1 && i <= mx - 2) {
+      const int col = (k * my) * mx + i;
+#pragma unroll 4
+      for (int j = 1 + ty; j <= my - 2; j += ny) {
+        const int p = col + j * mx;
+        const int s = tx * Lo.ls + Lo.pos(j - 1);
+        sr[s] = b[p] - ColorRow<T>::template r<false>(g, L, x, i, j, k, p, n);
+        sx[s] = x[p];
+      }
+    }
+    // the factors, as the line solve stages them (nothing to copy asynchronously)
+    solve_tile_load<T, TW, RR>(L, nullptr, nullptr, bx, k, st, color, false, false);
+  }
+  __syncthreads();
+  solve_tile_finish<T, TW, RR>(L, x, x, omega, bx, k, st, color);
+}
+
 __host__ __device__ inline int color_tiles_x(const Geom &g) { return ((g.mx + 1) / 2 + 31) / 32; }
 
 // ------------------------------------------------------------------ transfers
