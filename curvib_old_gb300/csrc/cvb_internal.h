@@ -181,10 +181,12 @@ void launch_finish_sums(const double *partial, int nv, int nblocks, double *out,
                         const int *gate = nullptr);
 void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_dev, int nv, size_t n,
                            double *partial, cudaStream_t s, const int *gate = nullptr);
+// dst = src / *scal_dev (and, with dst32, its FP32 copy)
 void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
-                  const int *gate = nullptr);
-// dst = src / sqrt(*sq_dev)
-void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s);
+                  const int *gate = nullptr, float *dst32 = nullptr);
+// dst = src / sqrt(*sq_dev) (and, with dst32, its FP32 copy)
+void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s,
+                       float *dst32 = nullptr);
 void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev,
                    int nz, size_t n, cudaStream_t s);
 void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial,

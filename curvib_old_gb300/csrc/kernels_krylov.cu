@@ -167,22 +167,27 @@ void launch_multiaxpy_norm(double *w, const double *const *V, const double *h_de
   launch_dep(k_multiaxpy_norm, reduce_blocks(), kRedThreads, 0, s, w, V, h_dev, nv, n, partial, gate);
 }
 
-// dst = src / *scal, or src / sqrt(*scal)
+// dst = src / *scal, or src / sqrt(*scal); with dst32 also its FP32 copy (the
+// next V-cycle's input in mixed precision)
 template <bool SQRT>
 __global__ void k_scale(double *__restrict__ dst, const double *__restrict__ src, const double *__restrict__ scal,
-                        size_t n, const int *gate) {
+                        size_t n, const int *gate, float *__restrict__ dst32) {
   dep_sync();
   if (gated(gate)) return;
   double inv = 1.0 / (SQRT ? sqrt(*scal) : *scal);
-  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
-    dst[p] = src[p] * inv;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const double v = src[p] * inv;
+    dst[p] = v;
+    if (dst32) dst32[p] = (float)v;
+  }
 }
 void launch_scale(double *dst, const double *src, const double *scal_dev, size_t n, cudaStream_t s,
-                  const int *gate) {
-  launch_dep(k_scale<false>, reduce_blocks(), 256, 0, s, dst, src, scal_dev, n, gate);
+                  const int *gate, float *dst32) {
+  launch_dep(k_scale<false>, reduce_blocks(), 256, 0, s, dst, src, scal_dev, n, gate, dst32);
 }
-void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s) {
-  launch_dep(k_scale<true>, reduce_blocks(), 256, 0, s, dst, src, sq_dev, n, nullptr);
+void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s,
+                       float *dst32) {
+  launch_dep(k_scale<true>, reduce_blocks(), 256, 0, s, dst, src, sq_dev, n, (const int *)nullptr, dst32);
 }
 
 // x += sum_q y[q] Z_q (Z stored FP32 in mixed mode, FP64 in plain mode)
