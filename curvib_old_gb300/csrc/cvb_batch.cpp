@@ -185,8 +185,8 @@ static void add_residual(VSink &vs, long long key, LevelDev &L, const LevelDev *
     const MarchGrid m = MarchGrid::of(L.g);
     vs.add(key, OK_RES32, task(dLv, x, b, r, gate, m.gx, m.gy), m.blocks());
   } else {
-    const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
-    vs.add(key, OK_RES64, task(dLv, x, b, r, gate, gx, gy), gx * gy * L.g.mz);
+    const int gx = plane_blocks(L.g);
+    vs.add(key, OK_RES64, task(dLv, x, b, r, gate, gx, 1), gx * L.g.mz);
   }
 }
 
@@ -230,8 +230,8 @@ static void gen_zebra_half(VSink &vs, long long k0, long long k1, LevelDev &L, c
   }
   const T *r = b;
   if (!zero) {
-    const int gx = color_tiles_x(L.g), gy = nblk(L.g.my, 4);
-    vs.add(k0, OK_RESC, task(dLv, x, b, res, gate, gx, gy, color), gx * gy * L.g.mz);
+    const int gx = color_plane_blocks(L.g);
+    vs.add(k0, OK_RESC, task(dLv, x, b, res, gate, gx, 1, color), gx * (L.g.mz - 2));
     r = res;
   }
   const int gx = f32 ? solve_tiles_x<kSolveTW32>(L.g, color) : solve_tiles_x<kSolveTW64>(L.g, color);
@@ -260,11 +260,11 @@ static void gen_vcycle_zebra(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l
   T *res = lvec<T>(L, 3);
   add_residual<T>(vs, key_desc(depth, 100), L, dLv, x, b, res, gate);
   T *bc = lvec<T>(C, 0), *ec = lvec<T>(C, 1);
-  const int cgx = nblk(C.g.mx, 32), cgy = nblk(C.g.my, 4);
-  vs.add(key_desc(depth, 101), OK_RESTRICT, task(dLv, res, nullptr, bc, gate, cgx, cgy), cgx * cgy * C.g.mz);
+  const int cgx = plane_blocks(C.g);
+  vs.add(key_desc(depth, 101), OK_RESTRICT, task(dLv, res, nullptr, bc, gate, cgx, 1), cgx * C.g.mz);
   gen_vcycle<T>(vs, ctx, dLs, l - 1, depth + 1, bc, ec, o, gate);
-  const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
-  vs.add(key_asc(depth, 0), OK_PROLONG, task(dLv, ec, nullptr, x, gate, gx, gy), gx * gy * L.g.mz);
+  vs.add(key_asc(depth, 0), OK_PROLONG, task(dLv, ec, nullptr, x, gate, plane_blocks(L.g), 1),
+         plane_blocks(L.g) * L.g.mz);
   for (int q = 0; q < o.post_sweeps; q++)
     for (int c = 0; c < 2; c++)
       gen_zebra_half<T>(vs, key_asc(depth, 1 + 10 * q + 3 * c), key_asc(depth, 2 + 10 * q + 3 * c), L, dLv, b, x, c,
@@ -294,12 +294,12 @@ static void gen_vcycle(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int 
   }
   T *res = lvec<T>(L, 3);
   add_residual<T>(vs, key_desc(depth, 100), L, dLv, x, b, res, gate);
-  const int gx = nblk(L.g.mx, 32), gy = nblk(L.g.my, 4);
   T *bc = lvec<T>(C, 0), *ec = lvec<T>(C, 1);
-  const int cgx = nblk(C.g.mx, 32), cgy = nblk(C.g.my, 4);
-  vs.add(key_desc(depth, 101), OK_RESTRICT, task(dLv, res, nullptr, bc, gate, cgx, cgy), cgx * cgy * C.g.mz);
+  const int cgx = plane_blocks(C.g);
+  vs.add(key_desc(depth, 101), OK_RESTRICT, task(dLv, res, nullptr, bc, gate, cgx, 1), cgx * C.g.mz);
   gen_vcycle<T>(vs, ctx, dLs, l - 1, depth + 1, bc, ec, o, gate);
-  vs.add(key_asc(depth, 0), OK_PROLONG, task(dLv, ec, nullptr, x, gate, gx, gy), gx * gy * L.g.mz);
+  vs.add(key_asc(depth, 0), OK_PROLONG, task(dLv, ec, nullptr, x, gate, plane_blocks(L.g), 1),
+         plane_blocks(L.g) * L.g.mz);
   for (int q = 0; q < o.post_sweeps; q++) {
     gen_sweep<T>(vs, key_asc(depth, 1 + 2 * q), key_asc(depth, 2 + 2 * q), L, dLv, b, x, x2, false, gate);
     std::swap(x, x2);
@@ -488,8 +488,8 @@ static int issue_round(cvb_batch *bt, std::vector<Prob *> &starting, std::vector
       const size_t n = F.g.n();
       const int *gfin = &dfl(bt, p->slot)->fin, *ggate = &dfl(bt, p->slot)->gate,
                 *gnot = &dfl(bt, p->slot)->notfin;
-      const int gx = nblk(F.g.mx, 32), gy = nblk(F.g.my, 4);
-      res.add(task(dlev(bt, p->slot) + (c->nlevels - 1), c->x, c->b, c->r, gfin, gx, gy), gx * gy * F.g.mz);
+      const int gx = plane_blocks(F.g);
+      res.add(task(dlev(bt, p->slot) + (c->nlevels - 1), c->x, c->b, c->r, gfin, gx, 1), gx * F.g.mz);
       add_multidot(norm, *p, c->r, 0, kNormRow, gfin);
       add_finish(finn, *p, kNormRow, 1, gfin);
       scale.add(task(nullptr, c->r, &dks(bt, p->slot)->beta, c->V[0], ggate, elem_blocks(n), 0, (int)n),
@@ -529,8 +529,8 @@ static int issue_round(cvb_batch *bt, std::vector<Prob *> &starting, std::vector
       } else {
         gen_vcycle<double>(vs, c, dLs, nl - 1, 0, c->V[j], c->Z64[j], bt->opts, gate);
       }
-      const int gx = nblk(F.g.mx, 32), gy = nblk(F.g.my, 4);
-      apply.add(task(dLs + (nl - 1), c->Z64[j], nullptr, c->w, gate, gx, gy), gx * gy * F.g.mz);
+      const int gx = plane_blocks(F.g);
+      apply.add(task(dLs + (nl - 1), c->Z64[j], nullptr, c->w, gate, gx, 1), gx * F.g.mz);
       add_multidot(mdot, *p, c->w, j + 1, j + 1, gate);
       add_finish(fin, *p, 0, j + 2, gate);
       maxpy.add(task(nullptr, nullptr, nullptr, nullptr, gate, 0, 0, p->slot, j + 1), batch_reduce_blocks(n));

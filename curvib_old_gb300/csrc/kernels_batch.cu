@@ -143,8 +143,8 @@ __global__ void kg_zero(const __grid_constant__ TaskList tl) {
 }
 void glaunch_resid_color(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) launch_dep(kg_resid_color<float>, tl.nblocks, dim3(32, 4), 0, s, tl);
-  else launch_dep(kg_resid_color<double>, tl.nblocks, dim3(32, 4), 0, s, tl);
+  if (f32) launch_dep(kg_resid_color<float>, tl.nblocks, kFlat, 0, s, tl);
+  else launch_dep(kg_resid_color<double>, tl.nblocks, kFlat, 0, s, tl);
 }
 void glaunch_zero(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
@@ -195,17 +195,17 @@ void glaunch_residual32(const TaskList &tl, cudaStream_t s) {
 }
 void glaunch_residual64(const TaskList &tl, cudaStream_t s) {
   if (!tl.n) return;
-  launch_dep(kg_apply64, tl.nblocks, dim3(32, 4), 0, s, tl);
+  launch_dep(kg_apply64, tl.nblocks, kFlat, 0, s, tl);
 }
 void glaunch_restrict(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) launch_dep(kg_restrict<float>, tl.nblocks, dim3(32, 4), 0, s, tl);
-  else launch_dep(kg_restrict<double>, tl.nblocks, dim3(32, 4), 0, s, tl);
+  if (f32) launch_dep(kg_restrict<float>, tl.nblocks, kFlat, 0, s, tl);
+  else launch_dep(kg_restrict<double>, tl.nblocks, kFlat, 0, s, tl);
 }
 void glaunch_prolong(const TaskList &tl, bool f32, cudaStream_t s) {
   if (!tl.n) return;
-  if (f32) launch_dep(kg_prolong<float>, tl.nblocks, dim3(32, 4), 0, s, tl);
-  else launch_dep(kg_prolong<double>, tl.nblocks, dim3(32, 4), 0, s, tl);
+  if (f32) launch_dep(kg_prolong<float>, tl.nblocks, kFlat, 0, s, tl);
+  else launch_dep(kg_prolong<double>, tl.nblocks, kFlat, 0, s, tl);
 }
 template <typename K>
 static void allow_smem(K kernel) {

@@ -36,8 +36,9 @@ static const dim3 kBlk(32, 4, 1);
 
 template <typename TX>
 static void apply64(const LevelDev &L, const TX *x, const double *b, double *y, cudaStream_t s) {
-  if (L.cross64) launch_dep(k_apply64<TX, true>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, b, y, L.gate);
-  else launch_dep(k_apply64<TX, false>, grid3(L.g), kBlk, 0, s, L.g, L.w64, L.code, x, b, y, L.gate);
+  const dim3 grd(plane_blocks(L.g), 1, L.g.mz);
+  if (L.cross64) launch_dep(k_apply64<TX, true>, grd, kFlat, 0, s, L.g, L.w64, L.code, x, b, y, L.gate);
+  else launch_dep(k_apply64<TX, false>, grd, kFlat, 0, s, L.g, L.w64, L.code, x, b, y, L.gate);
 }
 static void apply32(const LevelDev &L, const float *x, const float *b, float *y, cudaStream_t s) {
   if (L.cross32)
@@ -265,9 +266,9 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
   }
   const T *r = b;
   if (!zero) {
-    dim3 grd(color_tiles_x(L.g), nblk(L.g.my, 4), L.g.mz);
-    if (has_cross<T>(L)) launch_dep(k_resid_color<T, true>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
-    else launch_dep(k_resid_color<T, false>, grd, dim3(32, 4), 0, s, L, x, b, res, color);
+    dim3 grd(color_plane_blocks(L.g), 1, L.g.mz - 2);
+    if (has_cross<T>(L)) launch_dep(k_resid_color<T, true>, grd, kFlat, 0, s, L, x, b, res, color);
+    else launch_dep(k_resid_color<T, false>, grd, kFlat, 0, s, L, x, b, res, color);
     r = res;
   }
   line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);
@@ -286,8 +287,8 @@ __global__ void k_restrict(const __grid_constant__ LevelDev F, const __grid_cons
   dep_sync();
   if (gated(F.gate)) return;
   if (zero_c) {
-    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
-    if (i < C.g.mx && j < C.g.my) zero_c[C.g.id(i, j, blockIdx.z)] = T(0);
+    const int idx = blockIdx.x * kFlat + threadIdx.x, pl = C.g.mx * C.g.my;
+    if (idx < pl) zero_c[(size_t)blockIdx.z * pl + idx] = T(0);
   }
   restrict_body<T>(F, C, xf, xc, blockIdx.x, blockIdx.y, blockIdx.z);
 }
@@ -302,11 +303,11 @@ __global__ void k_prolong_add(const __grid_constant__ LevelDev C, const __grid_c
 
 template <typename T>
 void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s, T *zero_c) {
-  launch_dep(k_restrict<T>, grid3(C.g), kBlk, 0, s, F, C, xf, xc, zero_c);
+  launch_dep(k_restrict<T>, dim3(plane_blocks(C.g), 1, C.g.mz), kFlat, 0, s, F, C, xf, xc, zero_c);
 }
 template <typename T>
 void launch_prolong_add(const LevelDev &C, const LevelDev &F, const T *xc, T *xf, cudaStream_t s) {
-  launch_dep(k_prolong_add<T>, grid3(F.g), kBlk, 0, s, C, F, xc, xf);
+  launch_dep(k_prolong_add<T>, dim3(plane_blocks(F.g), 1, F.g.mz), kFlat, 0, s, C, F, xc, xf);
 }
 template void launch_restrict<float>(const LevelDev &, const LevelDev &, const float *, float *, cudaStream_t,
                                      float *);

@@ -18,6 +18,18 @@
 namespace cvb {
 
 
+// ------------------------------------------------------ per-plane blocks
+// The per-cell kernels (FP64 rows, zebra residual, transfers) take 1-D blocks
+// of kFlat threads over the cells of one plane, flattened i-fastest: a warp
+// covers 32 consecutive cells whatever the row length, so narrow boxes (the
+// 32^3..128^3 problems of a batch) leave no lanes idle at the row ends.
+constexpr int kFlat = 128;
+__host__ __device__ inline int plane_blocks(const Geom &g) { return (g.mx * g.my + kFlat - 1) / kFlat; }
+// interior cells of one zebra colour in a plane: at most (mx-1)/2 per row
+__host__ __device__ inline int color_plane_blocks(const Geom &g) {
+  return (((g.mx - 1) / 2) * (g.my - 2) + kFlat - 1) / kFlat;
+}
+
 // ------------------------------------------------------------ neighbourhood
 // 32-bit offsets of the six face neighbours, with the reference's periodic wrap
 // of column indices (poisson.c:1329-1450) folded into the offset at seam cells.
@@ -142,15 +154,18 @@ __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ 
 // ------------------------------------------------------- apply / residual
 // y = A x (b == nullptr) or y = b - A x.  One thread per cell.
 // Bodies take the block's coordinates explicitly so that the grouped (batched)
-// kernels can run them for any problem of a work-list; blocks are 32 x 4.
+// kernels can run them for any problem of a work-list: (bx, bz) = (block of the
+// plane, plane), kFlat threads.
 template <typename TX, bool X = true>
 __device__ __forceinline__ void apply64_body(const Geom &g, const double *__restrict__ w,
                                              const uint32_t *__restrict__ code, const TX *__restrict__ x,
                                              const double *__restrict__ b, double *__restrict__ y, int bx, int by,
                                              int bz) {
-  int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= g.mx || j >= g.my) return;
-  int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
+  (void)by;
+  const int pl = g.mx * g.my, idx = bx * kFlat + threadIdx.x;
+  if (idx >= pl) return;
+  const int j = idx / g.mx, i = idx - j * g.mx, k = bz;
+  const int n = (int)g.n(), p = k * pl + idx;
   double ax = row64<TX, X>(g, w, code, x, i, j, k, p, n);
   y[p] = b ? b[p] - ax : ax;
 }
@@ -762,9 +777,9 @@ __host__ __device__ inline int solve_tiles_x(const Geom &g, int color) {
   return color < 0 ? (g.mx + TW - 1) / TW : ((g.mx + 1) / 2 + TW - 1) / TW;
 }
 
-// Residual b - A x on the cells of one zebra color ((i + k) % 2 == color), one
-// thread per cell of that color, 32 x 4 threads, written in the colour-split
-// row layout (SplitRow).
+// Residual b - A x on the interior cells of one zebra color ((i + k) % 2 ==
+// color), one thread per cell, kFlat threads per block over the colour's cells
+// of one interior plane, written in the colour-split row layout (SplitRow).
 template <typename T>
 struct ColorRow;
 template <>
@@ -783,10 +798,17 @@ struct ColorRow<double> {
 };
 template <typename T, bool X = true>
 __device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__restrict__ x, const T *__restrict__ b,
-                                                 T *__restrict__ r, int color, int bx, int by, int k) {
+                                                 T *__restrict__ r, int color, int bx, int by, int plane) {
   const Geom g = L.g;
-  const int i = 2 * (bx * 32 + threadIdx.x) + ((color + k) & 1), j = by * 4 + threadIdx.y;
-  if (i >= g.mx || j >= g.my) return;
+  // interior plane k = plane + 1; the colour's interior cells of the plane, row
+  // by row, i = first, first + 2, ...
+  (void)by;
+  const int k = plane + 1;
+  const int first = ((color + k) & 1) ? 1 : 2;
+  const int nci = first <= g.mx - 2 ? (g.mx - 2 - first) / 2 + 1 : 0;
+  const int idx = bx * kFlat + threadIdx.x;
+  if (idx >= nci * (g.my - 2)) return;
+  const int jj = idx / nci, i = first + 2 * (idx - jj * nci), j = 1 + jj;
   const int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
   r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::template r<X>(g, L, x, i, j, k, p, n);
 }
@@ -828,7 +850,6 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
   solve_tile_finish<T, TW, RR>(L, x, x, omega, bx, k, st, color);
 }
 
-__host__ __device__ inline int color_tiles_x(const Geom &g) { return ((g.mx + 1) / 2 + 31) / 32; }
 
 // ------------------------------------------------------------------ transfers
 // Products in the transfers are rounded on their own (no fused multiply-add), as
@@ -864,9 +885,11 @@ template <typename T>
 __device__ __forceinline__ void restrict_body(const LevelDev &F, const LevelDev &C, const T *__restrict__ xf,
                                               T *__restrict__ xc, int bx, int by, int bz) {
   const int cmx = C.g.mx, cmy = C.g.my, cmz = C.g.mz;
-  const int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= cmx || j >= cmy) return;
-  const int p = (k * cmy + j) * cmx + i;
+  (void)by;
+  const int idx = bx * kFlat + threadIdx.x;
+  if (idx >= cmx * cmy) return;
+  const int j = idx / cmx, i = idx - j * cmx, k = bz;
+  const int p = k * cmx * cmy + idx;
   if (i == 0 || i == cmx - 1 || j == 0 || j == cmy - 1 || k == 0 || k == cmz - 1 || (C.code[p] & CODE_BLOCKED)) {
     xc[p] = T(0);
     return;
@@ -897,10 +920,12 @@ template <typename T>
 __device__ __forceinline__ void prolong_body(const LevelDev &C, const LevelDev &F, const T *__restrict__ xc,
                                              T *__restrict__ xf, int bx, int by, int bz) {
   const int fmx = F.g.mx, fmy = F.g.my, fmz = F.g.mz;
-  const int i = bx * 32 + threadIdx.x, j = by * 4 + threadIdx.y, k = bz;
-  if (i >= fmx || j >= fmy) return;
+  (void)by;
+  const int idx = bx * kFlat + threadIdx.x;
+  if (idx >= fmx * fmy) return;
+  const int j = idx / fmx, i = idx - j * fmx, k = bz;
   if (i == 0 || i == fmx - 1 || j == 0 || j == fmy - 1 || k == 0 || k == fmz - 1) return;
-  const int p = (k * fmy + j) * fmx + i;
+  const int p = k * fmx * fmy + idx;
   if (F.code[p] & CODE_BLOCKED) return;
   const int isc = F.isc, jsc = F.jsc, ksc = F.ksc;
   int ic, jc, kc, ia, ja, ka;
