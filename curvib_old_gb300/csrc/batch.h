@@ -99,7 +99,9 @@ void glaunch_prolong(const TaskList &tl, bool f32, cudaStream_t s);      // a = 
 // line sweeps: a = rhs (or residual), b = x (null: zero guess), c = xnew, p0 = mode (fused sweep);
 // line solve: p1 = zebra color + 1 (0: every line)
 void glaunch_line_sweep(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);
-void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);
+// rr: the rows per lane shared by every task's level (1, 2, 4, 8), or 0
+void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, int rr,
+                        cudaStream_t s);
 // zebra: residual on the cells of color p0 (a = x, b = rhs, c = r); zero fill of c[0..p0)
 void glaunch_resid_color(const TaskList &tl, bool f32, cudaStream_t s);
 void glaunch_zebra_fused(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s);

@@ -60,8 +60,23 @@ struct Done {
 // Sink of the ops of one round, grouped by schedule key and kernel kind.
 enum OpKind {
   OK_RES32, OK_RES64, OK_RESTRICT, OK_PROLONG, OK_SWEEP, OK_SOLVE, OK_DENSE, OK_COPY, OK_CONV, OK_WIDEN,
-  OK_ZERO, OK_RESC, OK_ZFUSED, OK_COUNT
+  OK_ZERO, OK_RESC, OK_ZFUSED,
+  // line solves of levels whose lines have 1, 2, 4 or 8 rows per lane: one
+  // launch each, so each runs the kernel specialised for its layout
+  OK_SOLVE_R1, OK_SOLVE_R2, OK_SOLVE_R4, OK_SOLVE_R8, OK_COUNT
 };
+
+// The line-solve op kind of a level: by its lines' rows per lane.
+static OpKind solve_kind(const LevelDev &L) {
+  switch (LineLayout::of(L.g.my).R) {
+    case 1: return OK_SOLVE_R1;
+    case 2: return OK_SOLVE_R2;
+    case 4: return OK_SOLVE_R4;
+    case 8: return OK_SOLVE_R8;
+    default: return OK_SOLVE;
+  }
+}
+
 
 struct OpBatch {
   TaskList tl;
@@ -203,11 +218,11 @@ static void gen_sweep(VSink &vs, long long key0, long long key1, LevelDev &L, co
   const int split = f32 ? L.sweep32 : L.sweep64;
   T *res = lvec<T>(L, 3);
   if (zero) {
-    if (async) vs.add(key1, OK_SOLVE, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
+    if (async) vs.add(key1, solve_kind(L), task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
     else vs.add(key1, OK_SWEEP, task(dLv, b, nullptr, xnew, gate, nblk(L.g.mx, TW), 0, 0), lblocks, ssw);
   } else if (split == 1) {
     add_residual<T>(vs, key0, L, dLv, x, b, res, gate);
-    if (async) vs.add(key1, OK_SOLVE, task(dLv, res, x, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
+    if (async) vs.add(key1, solve_kind(L), task(dLv, res, x, xnew, gate, nblk(L.g.mx, SW)), sblocks, sso);
     else vs.add(key1, OK_SWEEP, task(dLv, res, x, xnew, gate, nblk(L.g.mx, TW), 0, 2), lblocks, ssw);
   } else {
     vs.add(key1, OK_SWEEP, task(dLv, b, x, xnew, gate, nblk(L.g.mx, TW), 0, 1), lblocks, ssw);
@@ -236,7 +251,7 @@ static void gen_zebra_half(VSink &vs, long long k0, long long k1, LevelDev &L, c
   }
   const int gx = f32 ? solve_tiles_x<kSolveTW32>(L.g, color) : solve_tiles_x<kSolveTW64>(L.g, color);
   (void)SW;
-  vs.add(k1, OK_SOLVE, task(dLv, r, zero ? nullptr : x, x, gate, gx, 0, 0, color + 1 + (zero ? 0 : 16)),
+  vs.add(k1, solve_kind(L), task(dLv, r, zero ? nullptr : x, x, gate, gx, 0, 0, color + 1 + (zero ? 0 : 16)),
          gx * L.g.mz, sso);
 }
 
@@ -325,7 +340,11 @@ static void run_program(cvb_batch *bt, std::map<long long, std::array<Lists, OK_
           case OK_RESTRICT: glaunch_restrict(ob.tl, f32, s); break;
           case OK_PROLONG: glaunch_prolong(ob.tl, f32, s); break;
           case OK_SWEEP: glaunch_line_sweep(ob.tl, f32, w32, w64, ob.smem, s); break;
-          case OK_SOLVE: glaunch_line_solve(ob.tl, f32, w32, w64, ob.smem, s); break;
+          case OK_SOLVE: glaunch_line_solve(ob.tl, f32, w32, w64, ob.smem, 0, s); break;
+          case OK_SOLVE_R1: glaunch_line_solve(ob.tl, f32, w32, w64, ob.smem, 1, s); break;
+          case OK_SOLVE_R2: glaunch_line_solve(ob.tl, f32, w32, w64, ob.smem, 2, s); break;
+          case OK_SOLVE_R4: glaunch_line_solve(ob.tl, f32, w32, w64, ob.smem, 4, s); break;
+          case OK_SOLVE_R8: glaunch_line_solve(ob.tl, f32, w32, w64, ob.smem, 8, s); break;
           case OK_DENSE: glaunch_dense(ob.tl, f32, s); break;
           case OK_COPY: glaunch_elementwise(ob.tl, f32 ? 0 : 1, s); break;
           case OK_CONV: glaunch_elementwise(ob.tl, 2, s); break;

@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(256, 2) kg_line_sweep(const __grid_constant__ 
     line_sweep_body<T, TW, false>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, K.p0, lb % K.gx, lb / K.gx,
                                   smem_raw);
 }
-template <typename T, int TW>
+// RR: rows per lane of every task's level (0: each task's own, at run time)
+template <typename T, int TW, int RR>
 __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_constant__ TaskList tl, T omega) {
   dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
@@ -105,8 +106,8 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_c
   const LevelDev L = *K.L;
   int lb = blockIdx.x - K.block0;
   // p1: colour + 1 (0: all lines), plus 16 when the residual is colour-split
-  line_solve_body<T, TW>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw,
-                         (K.p1 & 15) - 1, (K.p1 >> 4) != 0);
+  line_solve_body<T, TW, RR>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw,
+                             (K.p1 & 15) - 1, (K.p1 >> 4) != 0);
 }
 // zebra half-sweep in one kernel (levels without cross terms): b = a, x = c,
 // colour p1 - 1
@@ -222,16 +223,30 @@ void glaunch_line_sweep(const TaskList &tl, bool f32, float omega32, double omeg
   if (f32) launch_dep(kg_line_sweep<float, 32>, tl.nblocks, 256, smem, s, tl, omega32);
   else launch_dep(kg_line_sweep<double, 16>, tl.nblocks, 256, smem, s, tl, omega64);
 }
-void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s) {
-  if (!tl.n) return;
+template <typename T, int TW, int RR>
+static void line_solve_rr(const TaskList &tl, T omega, size_t smem, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    allow_smem(kg_line_solve<float, kSolveTW32>);
-    allow_smem(kg_line_solve<double, kSolveTW64>);
+    allow_smem(kg_line_solve<T, TW, RR>);
     attr = true;
   }
-  if (f32) launch_dep(kg_line_solve<float, kSolveTW32>, tl.nblocks, kSolveThreads, smem, s, tl, omega32);
-  else launch_dep(kg_line_solve<double, kSolveTW64>, tl.nblocks, kSolveThreads, smem, s, tl, omega64);
+  launch_dep(kg_line_solve<T, TW, RR>, tl.nblocks, kSolveThreads, smem, s, tl, omega);
+}
+template <typename T, int TW>
+static void line_solve_r(const TaskList &tl, T omega, size_t smem, int rr, cudaStream_t s) {
+  switch (rr) {
+    case 1: line_solve_rr<T, TW, 1>(tl, omega, smem, s); break;
+    case 2: line_solve_rr<T, TW, 2>(tl, omega, smem, s); break;
+    case 4: line_solve_rr<T, TW, 4>(tl, omega, smem, s); break;
+    case 8: line_solve_rr<T, TW, 8>(tl, omega, smem, s); break;
+    default: line_solve_rr<T, TW, 0>(tl, omega, smem, s); break;
+  }
+}
+void glaunch_line_solve(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, int rr,
+                        cudaStream_t s) {
+  if (!tl.n) return;
+  if (f32) line_solve_r<float, kSolveTW32>(tl, omega32, smem, rr, s);
+  else line_solve_r<double, kSolveTW64>(tl, omega64, smem, rr, s);
 }
 void glaunch_zebra_fused(const TaskList &tl, bool f32, float omega32, double omega64, size_t smem, cudaStream_t s) {
   if (!tl.n) return;
