@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-serve", action="store_true", help="skip the served solve stream")
     ap.add_argument("--serve-requests", type=int, default=120)
+    ap.add_argument("--no-step", action="store_true", help="skip the projection step at 192^3 (config 2)")
+    ap.add_argument("--step-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -282,6 +284,8 @@ def run_cvb(args, ws, rank, local):
         "clocks": clocks,
         "gpu_launches": int(launches),
     }
+    if not args.no_step:
+        out["projection_step"] = bench_step(args, ws, local)
     if not args.no_batch:
         out["batch"] = bench_batch(args, ws, local)
     if not args.no_serve:
@@ -298,6 +302,69 @@ def run_cvb(args, ws, rank, local):
         out["serve"]["mixed_over_fp64"] = out["serve"]["mixed"]["solves_per_s"] / out["serve"]["fp64"]["solves_per_s"]
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(P, b)
+    return out
+
+
+def bench_step(args, ws, local):
+    """The pressure-projection part of config 2's time step at 192^3 cells, as the
+    reference's Flow_Solver calls it on host arrays: PoissonSolver_MG
+    (VolumeFlux_rev, PoissonRHS, the solve to 1e-8), UpdatePressure and
+    Projection, each through the C ABI with pinned host buffers (copies inside
+    the timed region).  The momentum right-hand side that produces u* in the
+    reference's step is outside this path; u* here is the Taylor-Green field."""
+    import torch
+
+    from curvib_old_gb300 import _lib
+    from curvib_old_gb300 import workload as W
+    from curvib_old_gb300.solver import PoissonContext
+    dt, st, rtol = 2e-3, 1.0, 1e-8
+    P = W.make_problem((192, 192, 192), (1.0, 1.0, 1.0), 2.0, True, (False, False, False), [(0.5, 0.5, 0.5, 0.25)],
+                       name="box192-sphere")
+    ctx = PoissonContext(local).setup(P)
+    shape = P.nvert.shape
+    L = _lib.lib()
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = a
+        return t
+
+    uc0 = pinned(P.ucont)
+    uc, phi, p = pinned(P.ucont), pinned(np.zeros(shape)), pinned(np.zeros(shape))
+    ptr = _lib.ptr
+    dev = torch.device("cuda", local)
+
+    def run(precision, steps):
+        o = _lib.default_opts(precision=precision, rtol=rtol, max_it=200)
+        stt = _lib.SolveStats()
+        its = []
+        wall = 0.0
+        for _ in range(steps):
+            uc.numpy()[...] = uc0.numpy()  # this step's u* (outside the timed calls)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = L.cvb_poisson_solver_mg(ctx._ctx, ptr(uc.numpy()), 0.0, 1, dt, st, ptr(phi.numpy()),
+                                         ctypes.byref(o), ctypes.byref(stt))
+            assert rc == 0, rc
+            assert L.cvb_update_pressure(ctx._ctx, ptr(p.numpy()), ptr(phi.numpy())) == 0
+            assert L.cvb_projection(ctx._ctx, ptr(phi.numpy()), dt, st, ptr(uc.numpy())) == 0
+            torch.cuda.synchronize()
+            wall += time.perf_counter() - t0
+            its.append(stt.iterations)
+        wall = max_over_ranks(ws, wall, dev)
+        return {"ms_per_step": wall * 1e3 / steps, "steps_per_s": ws * steps / wall,
+                "iterations": float(np.mean(its)), "rel_residual": stt.rel_residual}
+
+    out = {"workload": "192^3 cells, [0,1]^3 box, tanh 2.0 in y, distorted (config 0's law), sphere r=0.25 at the "
+                       "centre; PoissonSolver_MG (VolumeFlux_rev + PoissonRHS + solve to 1e-8) + UpdatePressure + "
+                       "Projection on pinned host arrays, Taylor-Green u* (config 2 without its momentum step)",
+           "unknowns": int(P.unknowns)}
+    for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
+        run(prec, 2)
+        barrier(ws)
+        out[name] = run(prec, args.step_steps)
+    out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    ctx.close()
     return out
 
 

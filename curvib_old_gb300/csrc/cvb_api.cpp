@@ -1171,7 +1171,8 @@ int cvb_volume_flux_rev(cvb_ctx *ctx, double *ucont, double fis, int flg, double
   CKL();
   double fa[2];
   TRY(reduce_to_host(ctx, 2, fa));
-  CK(cudaMemcpy(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   if (flux) *flux = fa[0];
   if (area) *area = fa[1];
   return CVB_OK;
@@ -1221,15 +1222,27 @@ int cvb_poisson_solve(cvb_ctx *ctx, const double *b, double *phi, const cvb_solv
   return rc;
 }
 
+// VolumeFlux_rev, PoissonRHS and the solve.  The corrected fluxes stay on the
+// device for PoissonRHS and its right-hand side for the solve; the host gets
+// the corrected ucont and phi back.
 int cvb_poisson_solver_mg(cvb_ctx *ctx, double *ucont, double fis, int immersed, double dt, double st, double *phi,
                           const cvb_solve_opts *o, cvb_solve_stats *stats) {
   if (!ctx) return CVB_BAD_INPUT;
-  double flux, area, compat;
+  if (!phi || !(dt != 0.0) || !(st != 0.0)) return fail(ctx, CVB_BAD_INPUT, "bad PoissonSolver_MG arguments");
+  double flux, area;
   TRY(cvb_volume_flux_rev(ctx, ucont, fis, immersed, &flux, &area));
-  size_t n = ctx->ready ? fine_n(ctx) : 0;
-  std::vector<double> b(n);
-  TRY(cvb_poisson_rhs(ctx, ucont, dt, st, b.data(), &compat));
-  return cvb_poisson_solve(ctx, b.data(), phi, o, stats);
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  launch_poisson_rhs(F.g, ctx->uc_dev, ctx->aj64[ctx->nlevels - 1], F.nvert, dt, st, ctx->b, ctx->partial, ctx->stream);
+  CKL();
+  cvb_solve_opts def;
+  if (!o) { cvb_solve_opts_default(&def); o = &def; }
+  if (o->warm_start) CK(cudaMemcpyAsync(ctx->x, phi, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = cvb_solve_resident(ctx, o, stats);
+  if (rc == CVB_OK || rc == CVB_NOT_CONVERGED)
+    CK(cudaMemcpyAsync(phi, ctx->x, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return rc;
 }
 
 int cvb_update_pressure(cvb_ctx *ctx, double *p, double *phi) {
