@@ -486,18 +486,17 @@ static int autotune_sweeps(cvb_ctx *ctx) {
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         (prec == 0 ? t.us32 : t.us64)[v] = 1e3 * ms / reps;
       }
-    // zebra half-sweep: two kernels, then (where possible) the fused kernel
+    // zebra sweep (both colours): two kernels per half-sweep, then one (in place
+    // without cross terms, else out of place through t)
     for (int prec = 0; prec < 2; prec++)
       for (int v = 0; v < 2; v++) {
         double *zb = prec == 0 ? t.zb32 : t.zb64;
-        const bool ok = prec == 0 ? zebra_fusable<float>(L) : zebra_fusable<double>(L);
-        if (v == 1 && !ok) { zb[1] = 0.0; continue; }
         if (prec == 0) L.zfuse32 = v; else L.zfuse64 = v;
         const int reps = 5;
         for (int q = 0; q <= reps; q++) {
           if (q == 1) CK(cudaEventRecord(ctx->ev0, ctx->stream));
-          if (prec == 0) launch_zebra_half<float>(L, L.r32, L.e32, L.t32 + n, 1.3f, 1, false, ctx->stream);
-          else launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream);
+          if (prec == 0) launch_zebra_sweep<float>(L, L.r32, L.e32, L.t32, L.t32 + n, 1.3f, false, ctx->stream);
+          else launch_zebra_sweep<double>(L, L.r64, L.e64, L.t64, L.t64 + n, 1.3, false, ctx->stream);
         }
         CK(cudaEventRecord(ctx->ev1, ctx->stream));
         CK(cudaEventSynchronize(ctx->ev1));
@@ -610,17 +609,16 @@ static void vcycle_zebra(cvb_ctx *ctx, int l, const T *b, T *x, const cvb_solve_
   T *res = vptr<T>(L, 3);
   const T omega = (T)o->omega;
   if (!zeroed) cudaMemsetAsync(x, 0, sizeof(T) * L.g.n(), s);
+  T *tmp = vptr<T>(L, 2);
   const int pre = std::max(o->pre_sweeps, 1);
-  for (int q = 0; q < pre; q++)
-    for (int c = 0; c < 2; c++) launch_zebra_half<T>(L, b, x, res, omega, c, q == 0 && c == 0, s);
+  for (int q = 0; q < pre; q++) launch_zebra_sweep<T>(L, b, x, tmp, res, omega, q == 0, s);
   launch_residual<T>(L, b, x, res, s);
   T *bc = vptr<T>(C, 0), *ec = vptr<T>(C, 1);
   const bool clear = l - 1 > 0;  // the coarsest solve writes all of ec itself
   launch_restrict<T>(L, C, res, bc, s, clear ? ec : nullptr);
   vcycle<T>(ctx, l - 1, bc, ec, o, clear);
   launch_prolong_add<T>(C, L, ec, x, s);
-  for (int q = 0; q < o->post_sweeps; q++)
-    for (int c = 0; c < 2; c++) launch_zebra_half<T>(L, b, x, res, omega, c, false, s);
+  for (int q = 0; q < o->post_sweeps; q++) launch_zebra_sweep<T>(L, b, x, tmp, res, omega, false, s);
 }
 
 // One V-cycle on level l for A e = b, zero initial guess; result in `out`.

@@ -240,7 +240,7 @@ static void gen_zebra_half(VSink &vs, long long k0, long long k1, LevelDev &L, c
   const bool fuse = f32 ? L.zfuse32 != 0 : L.zfuse64 != 0;
   if (!zero && fuse && zebra_fusable<T>(L) && L.g.my <= 400 && sso <= 200 * 1024) {
     const int gx = f32 ? solve_tiles_x<kSolveTW32>(L.g, color) : solve_tiles_x<kSolveTW64>(L.g, color);
-    vs.add(k1, OK_ZFUSED, task(dLv, b, nullptr, x, gate, gx, 0, 0, color + 1), gx * L.g.mz, sso);
+    vs.add(k1, OK_ZFUSED, task(dLv, b, x, x, gate, gx, 0, 0, color + 1), gx * L.g.mz, sso);
     return;
   }
   const T *r = b;
@@ -259,6 +259,26 @@ template <typename T>
 static void gen_vcycle(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int depth, const T *b, T *out,
                        const cvb_solve_opts &o, const int *gate);
 
+// One zebra sweep (both colours) on x: the out-of-place one-kernel form through
+// tmp (x -> tmp -> x) where the set-up chose it for a level with cross terms,
+// else two half-sweeps.  ka/kb: the keys of the two colours' residual and solve.
+template <typename T>
+static void gen_zebra_sweep(VSink &vs, long long ka0, long long ka1, long long kb0, long long kb1, LevelDev &L,
+                            const LevelDev *dLv, const T *b, T *x, T *tmp, bool zero_first, const int *gate) {
+  const bool f32 = sizeof(T) == 4;
+  const size_t sso = f32 ? line_solve_smem<float, kSolveTW32>(L.g) : line_solve_smem<double, kSolveTW64>(L.g);
+  const bool fuse = f32 ? L.zfuse32 != 0 : L.zfuse64 != 0;
+  if (!zero_first && fuse && !zebra_fusable<T>(L) && L.g.my <= 400 && sso <= 200 * 1024) {
+    const int g0 = f32 ? solve_tiles_x<kSolveTW32>(L.g, 0) : solve_tiles_x<kSolveTW64>(L.g, 0);
+    const int g1 = f32 ? solve_tiles_x<kSolveTW32>(L.g, 1) : solve_tiles_x<kSolveTW64>(L.g, 1);
+    vs.add(ka1, OK_ZFUSED, task(dLv, b, x, tmp, gate, g0, 0, 0, 1), g0 * L.g.mz, sso);
+    vs.add(kb1, OK_ZFUSED, task(dLv, b, tmp, x, gate, g1, 0, 0, 2), g1 * L.g.mz, sso);
+    return;
+  }
+  gen_zebra_half<T>(vs, ka0, ka1, L, dLv, b, x, 0, zero_first, gate);
+  gen_zebra_half<T>(vs, kb0, kb1, L, dLv, b, x, 1, false, gate);
+}
+
 template <typename T>
 static void gen_vcycle_zebra(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l, int depth, const T *b, T *x,
                              const cvb_solve_opts &o, const int *gate) {
@@ -267,11 +287,11 @@ static void gen_vcycle_zebra(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l
   const size_t n = L.g.n();
   vs.add(key_desc(depth, 0), OK_ZERO, task(dLv, nullptr, nullptr, x, gate, elem_blocks(n), 0, (int)n),
          elem_blocks(n));
+  T *tmp = lvec<T>(L, 2);
   const int pre = std::max(o.pre_sweeps, 1);
   for (int q = 0; q < pre; q++)
-    for (int c = 0; c < 2; c++)
-      gen_zebra_half<T>(vs, key_desc(depth, 1 + 10 * q + 3 * c), key_desc(depth, 2 + 10 * q + 3 * c), L, dLv, b, x, c,
-                        q == 0 && c == 0, gate);
+    gen_zebra_sweep<T>(vs, key_desc(depth, 1 + 10 * q), key_desc(depth, 2 + 10 * q), key_desc(depth, 4 + 10 * q),
+                       key_desc(depth, 5 + 10 * q), L, dLv, b, x, tmp, q == 0, gate);
   T *res = lvec<T>(L, 3);
   add_residual<T>(vs, key_desc(depth, 100), L, dLv, x, b, res, gate);
   T *bc = lvec<T>(C, 0), *ec = lvec<T>(C, 1);
@@ -281,9 +301,8 @@ static void gen_vcycle_zebra(VSink &vs, cvb_ctx *ctx, const LevelDev *dLs, int l
   vs.add(key_asc(depth, 0), OK_PROLONG, task(dLv, ec, nullptr, x, gate, plane_blocks(L.g), 1),
          plane_blocks(L.g) * L.g.mz);
   for (int q = 0; q < o.post_sweeps; q++)
-    for (int c = 0; c < 2; c++)
-      gen_zebra_half<T>(vs, key_asc(depth, 1 + 10 * q + 3 * c), key_asc(depth, 2 + 10 * q + 3 * c), L, dLv, b, x, c,
-                        false, gate);
+    gen_zebra_sweep<T>(vs, key_asc(depth, 1 + 10 * q), key_asc(depth, 2 + 10 * q), key_asc(depth, 4 + 10 * q),
+                       key_asc(depth, 5 + 10 * q), L, dLv, b, x, tmp, false, gate);
 }
 
 template <typename T>

@@ -90,7 +90,7 @@ struct cvb_ctx {
   std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)
   // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
   // set-up timings (microseconds): Jacobi line sweep fused / split, zebra
-  // half-sweep split / fused (0 where the level cannot use the fused form)
+  // sweep two kernels / one kernel per half-sweep
   struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2]; };
   std::vector<Tune> tune;
 };

@@ -100,7 +100,8 @@ struct LevelDev {
   // the operator has cross-derivative terms (FP32 flux form / FP64 edge
   // weights); 0 on an orthogonal grid, where the kernels read 7 points
   int cross32, cross64;
-  int zfuse32, zfuse64;     // zebra half-sweep variant chosen at set-up: 0 two kernels, 1 fused
+  int zfuse32, zfuse64;     // zebra variant chosen at set-up: 0 two kernels per half-sweep, 1 one
+                            // (in place without cross terms, else out of place)
   // coarsest level only: the densely inverted cells (first cm of cidx) and the
   // identity ones (the rest of cidx)
   const int *cidx;
@@ -159,6 +160,10 @@ void launch_line_smooth(const LevelDev &L, const T *b, const T *x, T *xnew, T om
 // zebra half-sweep of one color, in place (res: scratch for the residual)
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s);
+// one zebra sweep (both colours) on x; tmp: a level-sized buffer for the
+// out-of-place one-kernel form; zero_first: x is zero on entry
+template <typename T>
+void launch_zebra_sweep(const LevelDev &L, const T *b, T *x, T *tmp, T *res, T omega, bool zero_first, cudaStream_t s);
 // restriction of xf into xc; zero_c, when set, is zeroed over the coarse grid too
 template <typename T>
 void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s, T *zero_c = nullptr);

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_line_solve(const __grid_c
   line_solve_body<T, TW, RR>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw,
                              (K.p1 & 15) - 1, (K.p1 >> 4) != 0);
 }
-// zebra half-sweep in one kernel (levels without cross terms): b = a, x = c,
+// zebra half-sweep in one kernel: b = a, x from b into c (in place when b == c),
 // colour p1 - 1
 template <typename T, int TW>
 __global__ void __launch_bounds__(kSolveThreads, 4) kg_zebra_fused(const __grid_constant__ TaskList tl, T omega) {
@@ -119,7 +119,12 @@ __global__ void __launch_bounds__(kSolveThreads, 4) kg_zebra_fused(const __grid_
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const LevelDev L = *K.L;
   int lb = blockIdx.x - K.block0;
-  zebra_fused_body<T, TW>(L, (const T *)K.a, (T *)K.c, omega, lb % K.gx, lb / K.gx, smem_raw, K.p1 - 1);
+  if (has_cross<T>(L))
+    zebra_fused_body<T, TW, 0, true>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx,
+                                     smem_raw, K.p1 - 1);
+  else
+    zebra_fused_body<T, TW, 0, false>(L, (const T *)K.a, (const T *)K.b, (T *)K.c, omega, lb % K.gx, lb / K.gx,
+                                      smem_raw, K.p1 - 1);
 }
 // zebra: residual on the cells of color p0
 template <typename T>

@@ -85,13 +85,13 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, con
   line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color, rsplit != 0);
 }
 
-template <typename T, int TW, int RR>
-__global__ void __launch_bounds__(kSolveThreads, 4) k_zebra_fused(LevelDev L, const T *__restrict__ b, T *x, T omega,
-                                                                  int color) {
+template <typename T, int TW, int RR, bool X>
+__global__ void __launch_bounds__(kSolveThreads, 4) k_zebra_fused(LevelDev L, const T *__restrict__ b, const T *xin,
+                                                                  T *xout, T omega, int color) {
   dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  zebra_fused_body<T, TW, RR>(L, b, x, omega, blockIdx.x, blockIdx.y, smem_raw, color);
+  zebra_fused_body<T, TW, RR, X>(L, b, xin, xout, omega, blockIdx.x, blockIdx.y, smem_raw, color);
 }
 
 template <typename T, bool X>
@@ -239,29 +239,46 @@ void launch_line_smooth<double>(const LevelDev &L, const double *b, const double
 // color, (i + k) % 2 == color, in place: residual on those lines, then their
 // line solves.  zero: x is zero on entry (the caller zeroed it); only the
 // solves run, on r = b.
-template <typename T, int TW, int RR>
-static void zebra_fused_r(const LevelDev &L, const T *b, T *x, T omega, int color, cudaStream_t s) {
+template <typename T, int TW, int RR, bool X>
+static void zebra_fused_rx(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
   dim3 grd(solve_tiles_x<TW>(L.g, color), L.g.mz);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_zebra_fused<T, TW, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_zebra_fused<T, TW, RR, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  launch_dep(k_zebra_fused<T, TW, RR>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, b, x, omega, color);
+  launch_dep(k_zebra_fused<T, TW, RR, X>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, b, xin, xout, omega,
+             color);
+}
+template <typename T, int TW, int RR>
+static void zebra_fused_r(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
+  if (has_cross<T>(L)) zebra_fused_rx<T, TW, RR, true>(L, b, xin, xout, omega, color, s);
+  else zebra_fused_rx<T, TW, RR, false>(L, b, xin, xout, omega, color, s);
+}
+// One-kernel half-sweep, xin -> xout (in place when they are equal).
+template <typename T>
+static void zebra_fused(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
+  constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
+  switch (LineLayout::of(L.g.my).R) {
+    case 1: zebra_fused_r<T, TW, 1>(L, b, xin, xout, omega, color, s); break;
+    case 2: zebra_fused_r<T, TW, 2>(L, b, xin, xout, omega, color, s); break;
+    case 4: zebra_fused_r<T, TW, 4>(L, b, xin, xout, omega, color, s); break;
+    case 8: zebra_fused_r<T, TW, 8>(L, b, xin, xout, omega, color, s); break;
+    default: zebra_fused_r<T, TW, 0>(L, b, xin, xout, omega, color, s); break;
+  }
+}
+template <typename T>
+static bool fused_ok(const LevelDev &L) {
+  constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
+  const bool chosen = sizeof(T) == 4 ? L.zfuse32 != 0 : L.zfuse64 != 0;
+  return chosen && L.g.my <= kMaxFusedRows && line_solve_smem<T, TW>(L.g) <= kMaxSmem;
 }
 
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s) {
   constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
-  const bool fuse = sizeof(T) == 4 ? L.zfuse32 != 0 : L.zfuse64 != 0;
-  if (!zero && fuse && zebra_fusable<T>(L) && L.g.my <= kMaxFusedRows && line_solve_smem<T, TW>(L.g) <= kMaxSmem) {
-    switch (LineLayout::of(L.g.my).R) {
-      case 1: zebra_fused_r<T, TW, 1>(L, b, x, omega, color, s); break;
-      case 2: zebra_fused_r<T, TW, 2>(L, b, x, omega, color, s); break;
-      case 4: zebra_fused_r<T, TW, 4>(L, b, x, omega, color, s); break;
-      case 8: zebra_fused_r<T, TW, 8>(L, b, x, omega, color, s); break;
-      default: zebra_fused_r<T, TW, 0>(L, b, x, omega, color, s); break;
-    }
+  if (!zero && fused_ok<T>(L) && zebra_fusable<T>(L)) {
+    zebra_fused<T>(L, b, x, x, omega, color, s);
     return;
   }
   const T *r = b;
@@ -273,6 +290,23 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
   }
   line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);
 }
+
+template <typename T>
+void launch_zebra_sweep(const LevelDev &L, const T *b, T *x, T *tmp, T *res, T omega, bool zero_first,
+                        cudaStream_t s) {
+  if (!zero_first && fused_ok<T>(L) && !zebra_fusable<T>(L)) {
+    // one-kernel half-sweeps out of place: x -> tmp -> x
+    zebra_fused<T>(L, b, x, tmp, omega, 0, s);
+    zebra_fused<T>(L, b, tmp, x, omega, 1, s);
+    return;
+  }
+  launch_zebra_half<T>(L, b, x, res, omega, 0, zero_first, s);
+  launch_zebra_half<T>(L, b, x, res, omega, 1, false, s);
+}
+template void launch_zebra_sweep<float>(const LevelDev &, const float *, float *, float *, float *, float, bool,
+                                        cudaStream_t);
+template void launch_zebra_sweep<double>(const LevelDev &, const double *, double *, double *, double *, double, bool,
+                                         cudaStream_t);
 template void launch_zebra_half<float>(const LevelDev &, const float *, float *, float *, float, int, bool,
                                        cudaStream_t);
 template void launch_zebra_half<double>(const LevelDev &, const double *, double *, double *, double, int, bool,

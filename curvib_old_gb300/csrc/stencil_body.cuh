@@ -813,21 +813,28 @@ __device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__r
   r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::template r<X>(g, L, x, i, j, k, p, n);
 }
 
-// A zebra half-sweep in one kernel, for levels whose operator has no
-// cross-derivative terms: the 7-point rows couple a line (i, k) only to the
-// lines (i +- 1, k) and (i, k +- 1), all of the other colour, so the lines of
-// one colour are independent and a tile can compute its residual, solve and
-// update its own lines in place without racing another tile.  A periodic wrap
-// in x (z) keeps the colours apart only when mx (mz) is even.  The residual
-// goes straight into shared memory; results equal the two-kernel form.
-
-template <typename T, int TW, int RR = 0>
-__device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__restrict__ b, T *x, T omega, int bx,
-                                                 int k, unsigned char *smem_raw, int color) {
+// A zebra half-sweep in one kernel: a tile of one colour's lines computes its
+// residual straight into shared memory, solves, and writes its lines.
+//  - In place (xout == xin), for levels without cross-derivative terms: the
+//    7-point rows couple a line (i, k) only to the lines (i +- 1, k) and
+//    (i, k +- 1), all of the other colour, so a tile never reads a line that
+//    another tile writes.  A periodic wrap in x (z) keeps the colours apart only
+//    when mx (mz) is even (zebra_fusable).
+//  - Out of place (xout != xin), for any level: the residual reads xin only,
+//    which no tile writes, so the diagonal couplings of the 19-point rows are
+//    no race either.  Each block also copies the rest of its 2 TW columns of the
+//    plane (the other colour's lines and the ring) from xin to xout, so xout is
+//    complete after the launch.
+// Either way the results equal the two-kernel form, whose residual also sees x
+// as it was before the half-sweep.
+template <typename T, int TW, int RR = 0, bool X = false>
+__device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__restrict__ b, const T *xin, T *xout,
+                                                 T omega, int bx, int k, unsigned char *smem_raw, int color) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx, n = (int)g.n();
   T *st = reinterpret_cast<T *>(smem_raw);
-  if (k >= 1 && k <= g.mz - 2) {
+  const bool kin = k >= 1 && k <= g.mz - 2;
+  if (kin) {
     const LineLayout Lo = LineLayout::fixed<RR>(my);
     T *sr = st, *sx = st + 4 * Lo.ls * TW;
     const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
@@ -839,15 +846,29 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
       for (int j = 1 + ty; j <= my - 2; j += ny) {
         const int p = col + j * mx;
         const int s = tx * Lo.ls + Lo.pos(j - 1);
-        sr[s] = b[p] - ColorRow<T>::template r<false>(g, L, x, i, j, k, p, n);
-        sx[s] = x[p];
+        sr[s] = b[p] - ColorRow<T>::template r<X>(g, L, xin, i, j, k, p, n);
+        sx[s] = xin[p];
       }
     }
     // the factors, as the line solve stages them (nothing to copy asynchronously)
     solve_tile_load<T, TW, RR>(L, nullptr, nullptr, bx, k, st, color, false, false);
   }
+  if (xout != xin) {
+    // the block's columns [2 TW bx, 2 TW (bx + 1)) of plane k, except the cells
+    // its line solves write
+    const int c0 = 2 * TW * bx, par = (color + k) & 1;
+    for (int e = threadIdx.x; e < 2 * TW * my; e += kSolveThreads) {
+      const int j = e / (2 * TW), i = c0 + (e - j * 2 * TW);
+      if (i >= mx) continue;
+      const bool solved = kin && i >= 1 && i <= mx - 2 && j >= 1 && j <= my - 2 && (i & 1) == par;
+      if (!solved) {
+        const int p = (k * my + j) * mx + i;
+        xout[p] = xin[p];
+      }
+    }
+  }
   __syncthreads();
-  solve_tile_finish<T, TW, RR>(L, x, x, omega, bx, k, st, color);
+  solve_tile_finish<T, TW, RR>(L, xin, xout, omega, bx, k, st, color);
 }
 
 
