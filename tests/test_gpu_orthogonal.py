@@ -24,6 +24,9 @@ DT, ST = 1e-3, 1.0
 ORTHO = {
     "channel_sphere": ((16, 8, 8), (2.0, 1.0, 1.0), 2.5, (True, False, True), [(0.4, 0.5, 0.5, 0.25)], 2),
     "box_sphere": ((12, 12, 12), (1.0, 1.0, 1.0), 2.0, (False, False, False), [(0.5, 0.45, 0.55, 0.3)], 3),
+    # odd mx with a periodic x seam: the colours meet across the seam, so the
+    # in-place one-kernel zebra form is not allowed on the finest level
+    "odd_periodic": ((15, 8, 8), (1.5, 1.0, 1.0), 2.0, (True, False, False), [(0.5, 0.5, 0.5, 0.2)], 2),
 }
 
 
@@ -68,6 +71,14 @@ def test_flags_and_apply(ctxs, name):
         y32 = ctx.apply_f32(l, x.astype(np.float32)).astype(np.float64)
         y_ref32 = (A @ x.astype(np.float32).astype(np.float64).ravel()).reshape(x.shape)
         assert np.abs(y32 - y_ref32).max() <= 2e-6 * np.abs(A).max() * np.abs(x).max() * 4
+
+
+def test_odd_periodic_level_is_not_fused_in_place(ctxs):
+    ctx, P, Ls = ctxs["odd_periodic"]
+    assert ctx.shapes[-1][2] % 2 == 1  # mx odd
+    fine = ctx.tuning()["line_sweep"][-1]
+    assert fine["level"] == ctx.nlevels - 1
+    # whichever form the autotuner kept, the solve below must match the direct solve
 
 
 def test_distorted_grid_keeps_cross_terms():
