@@ -92,6 +92,7 @@ EXPORTS = {
     "cvb_batch_solve": ([_P, _I, _P, _P], _I),
     "cvb_batch_in_flight": ([_P], _I),
     "cvb_device_bytes": ([_P, _P], _I),
+    "cvb_set_device_limit": ([_P, ctypes.c_ulonglong], _I),
     "cvb_geometry_bytes": ([_P, _P, _P], _I),
     "cvb_setup_like": ([_P, _P, _P], _I),
     "cvb_setup_geometry": ([_P, _I, _P], _I),

@@ -75,6 +75,9 @@ template <typename T>
 static int dalloc(cvb_ctx *ctx, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
+  if (ctx->device_limit && ctx->device_bytes + sizeof(T) * count > ctx->device_limit)
+    return fail(ctx, CVB_OOM, "device allocation of %zu bytes exceeds the context's limit (%zu of %zu bytes in use)",
+                sizeof(T) * count, ctx->device_bytes, ctx->device_limit);
   cudaError_t e = cudaMallocAsync((void **)p, sizeof(T) * count, ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -104,6 +107,9 @@ template <typename T>
 static int galloc(cvb_ctx *ctx, Geometry &G, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
+  if (ctx->device_limit && G.bytes + sizeof(T) * count > ctx->device_limit)
+    return fail(ctx, CVB_OOM, "grid allocation of %zu bytes exceeds the context's limit (%zu of %zu bytes in use)",
+                sizeof(T) * count, (size_t)G.bytes, ctx->device_limit);
   cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -911,8 +917,21 @@ static int solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats
 
 // Per-problem part of a set-up on the context's geometry: level arrays, the
 // finest level's nvert (owned box), operators, smoother factors, coarsest solver.
+// nvert holds the reference's cell codes (0 fluid, 1..2 immersed boundary, 3+
+// solid, ibm.c:4332-4438): finite and non-negative.
+static int check_nvert(cvb_ctx *ctx, const double *v, size_t n) {
+  for (size_t p = 0; p < n; p++)
+    if (!std::isfinite(v[p]) || v[p] < 0.0)
+      return fail(ctx, CVB_BAD_INPUT, "nvert[%zu] = %g is not a cell code (finite, >= 0)", p, v[p]);
+  return CVB_OK;
+}
+
 static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
   const int nlevels = ctx->nlevels;
+  {
+    const cvb_level_desc &d = ctx->H[nlevels - 1].d;
+    TRY(check_nvert(ctx, nvert_box, (size_t)d.mx * d.my * d.mz));
+  }
   Geometry &G = *ctx->geo;
   ctx->fm = G.fm;
   ctx->iaj = G.iaj; ctx->jaj = G.jaj; ctx->kaj = G.kaj; ctx->aj64 = G.aj64;
@@ -1128,6 +1147,7 @@ int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
   const cvb_level_desc &df = ctx->H[ctx->nlevels - 1].d;
   std::vector<double> h;
   const double *v = box_view(df, nvert_finest, 1, h);
+  TRY(check_nvert(ctx, v, (size_t)df.mx * df.my * df.mz));
   drop_vcycle_graphs(ctx);
   CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, v, sizeof(double) * ctx->L[ctx->nlevels - 1].g.n(),
                      cudaMemcpyHostToDevice, ctx->stream));
@@ -1305,6 +1325,12 @@ int cvb_apply_operator_f32(cvb_ctx *ctx, int level, const float *x, float *y) {
   CKL();
   CK(cudaMemcpyAsync(y, L.e32, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_set_device_limit(cvb_ctx *ctx, unsigned long long bytes) {
+  if (!ctx) return CVB_BAD_INPUT;
+  ctx->device_limit = (size_t)bytes;
   return CVB_OK;
 }
 

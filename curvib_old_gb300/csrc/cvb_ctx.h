@@ -57,6 +57,7 @@ struct cvb_ctx {
   std::vector<void *> allocs;
   std::vector<size_t> alloc_bytes;
   size_t device_bytes = 0;  // sum of this context's device allocations
+  size_t device_limit = 0;  // cap on device_bytes + geometry bytes this context allocates (0: none)
 
   int nlevels = 0;
   std::vector<cvb::LevelDev> L;       // 0 = coarsest

@@ -258,6 +258,10 @@ class PoissonContext:
         self._check(self._L.cvb_apply_operator_f32(self._ctx, level, ptr(xx), ptr(y)))
         return y
 
+    def set_device_limit(self, nbytes):
+        """Cap the device memory this context may allocate (0: no cap)."""
+        self._check(self._L.cvb_set_device_limit(self._ctx, int(nbytes)))
+
     def level_cross(self, level):
         """(FP32, FP64) flags: the level's operator has cross-derivative terms."""
         a, b = ctypes.c_int(), ctypes.c_int()

@@ -257,6 +257,12 @@ int cvb_batch_in_flight(const cvb_batch *batch);
 /* Device memory held by a context alone (operators, vectors, Krylov basis) and
  * by its grid's shared metrics, with an id that is equal for contexts sharing them. */
 int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes);
+/* Cap the device memory this context may allocate (its own arrays, and the
+ * grid's when it uploads one); 0 removes the cap.  An allocation beyond it
+ * fails with CVB_OOM as a failed cudaMalloc would, and the context stays
+ * usable: raise the cap and set up again.  For callers sharing a GPU, and for
+ * exercising the out-of-memory paths.  No counterpart in the reference. */
+int cvb_set_device_limit(cvb_ctx *ctx, unsigned long long bytes);
 int cvb_geometry_bytes(const cvb_ctx *ctx, unsigned long long *bytes, unsigned long long *id);
 
 /* --- measurement ------------------------------------------------------- */
