@@ -93,6 +93,8 @@ EXPORTS = {
     "cvb_batch_in_flight": ([_P], _I),
     "cvb_device_bytes": ([_P, _P], _I),
     "cvb_set_device_limit": ([_P, ctypes.c_ulonglong], _I),
+    "cvb_solve_opts_from_file": ([ctypes.c_char_p, _P, ctypes.c_char_p, _I], _I),
+    "cvb_solve_opts_from_args": ([_I, _P, _P, ctypes.c_char_p, _I], _I),
     "cvb_geometry_bytes": ([_P, _P, _P], _I),
     "cvb_setup_like": ([_P, _P, _P], _I),
     "cvb_setup_geometry": ([_P, _I, _P], _I),
@@ -131,6 +133,25 @@ class CvbError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
         self.status = status
+
+
+def opts_from_control(path, args=(), **kw) -> SolveOpts:
+    """Solve options from a control.dat file, then argv-style overrides, then kw."""
+    o = SolveOpts()
+    lib().cvb_solve_opts_default(ctypes.byref(o))
+    bad = ctypes.create_string_buffer(256)
+    if path is not None:
+        rc = lib().cvb_solve_opts_from_file(str(path).encode(), ctypes.byref(o), bad, len(bad))
+        if rc:
+            raise CvbError(rc, f"control file: {bad.value.decode()}")
+    if args:
+        arr = (ctypes.c_char_p * len(args))(*[a.encode() for a in args])
+        rc = lib().cvb_solve_opts_from_args(len(args), arr, ctypes.byref(o), bad, len(bad))
+        if rc:
+            raise CvbError(rc, f"option: {bad.value.decode()}")
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
 
 
 def default_opts(**kw) -> SolveOpts:

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
@@ -1003,6 +1004,94 @@ int cvb_solve_opts_default(cvb_solve_opts *o) {
   o->cgs_refine = 0;
   o->smoother = CVB_SMOOTHER_ZEBRA;
   return CVB_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// One "-name value" pair into opts; false when the value does not parse.
+bool apply_option(const std::string &name, const std::string &val, cvb_solve_opts *o) {
+  char *end = nullptr;
+  auto real = [&](double *dst) {
+    double v = std::strtod(val.c_str(), &end);
+    if (val.empty() || *end || !std::isfinite(v)) return false;
+    *dst = v;
+    return true;
+  };
+  auto integer = [&](int *dst) {
+    long v = std::strtol(val.c_str(), &end, 10);
+    if (val.empty() || *end) return false;
+    *dst = (int)v;
+    return true;
+  };
+  if (name == "-ps_ksp_rtol") return real(&o->rtol);
+  if (name == "-ps_ksp_atol") return real(&o->atol);
+  if (name == "-ps_ksp_max_it") return integer(&o->max_it);
+  if (name == "-ps_ksp_gmres_restart") return integer(&o->restart);
+  if (name == "-cvb_pre_sweeps") return integer(&o->pre_sweeps);
+  if (name == "-cvb_post_sweeps") return integer(&o->post_sweeps);
+  if (name == "-cvb_omega") return real(&o->omega);
+  if (name == "-cvb_coarse_dense_max") return integer(&o->coarse_dense_max);
+  if (name == "-cvb_precision") {
+    if (val == "fp64") o->precision = CVB_PRECISION_FP64;
+    else if (val == "mixed") o->precision = CVB_PRECISION_MIXED;
+    else return false;
+    return true;
+  }
+  if (name == "-cvb_smoother") {
+    if (val == "zebra") o->smoother = CVB_SMOOTHER_ZEBRA;
+    else if (val == "jacobi") o->smoother = CVB_SMOOTHER_JACOBI;
+    else return false;
+    return true;
+  }
+  return true;  // not a solver option: ignored, as PETSc ignores unused options
+}
+
+// Tokens "-name [value]": a name followed by a token that is not itself an
+// option name takes it as its value (a negative number is a value).
+int apply_tokens(const std::vector<std::string> &tok, cvb_solve_opts *o, char *bad, int bad_len) {
+  auto is_name = [](const std::string &t) {
+    return t.size() > 1 && t[0] == '-' && !(std::isdigit((unsigned char)t[1]) || t[1] == '.');
+  };
+  for (size_t q = 0; q < tok.size(); q++) {
+    if (!is_name(tok[q])) continue;
+    std::string val;
+    if (q + 1 < tok.size() && !is_name(tok[q + 1])) val = tok[++q];
+    if (!apply_option(tok[q - (val.empty() ? 0 : 1)], val, o)) {
+      if (bad && bad_len > 0) std::snprintf(bad, bad_len, "%s %s", tok[q - (val.empty() ? 0 : 1)].c_str(), val.c_str());
+      return CVB_BAD_INPUT;
+    }
+  }
+  return CVB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int cvb_solve_opts_from_args(int argc, const char *const *argv, cvb_solve_opts *opts, char *bad, int bad_len) {
+  if (!opts || argc < 0 || (argc > 0 && !argv)) return CVB_BAD_INPUT;
+  std::vector<std::string> tok;
+  for (int q = 0; q < argc; q++)
+    if (argv[q]) tok.emplace_back(argv[q]);
+  return apply_tokens(tok, opts, bad, bad_len);
+}
+
+int cvb_solve_opts_from_file(const char *path, cvb_solve_opts *opts, char *bad, int bad_len) {
+  if (!opts || !path) return CVB_BAD_INPUT;
+  FILE *f = std::fopen(path, "r");
+  if (!f) {
+    if (bad && bad_len > 0) std::snprintf(bad, bad_len, "cannot read %s", path);
+    return CVB_BAD_INPUT;
+  }
+  std::vector<std::string> tok;
+  char line[4096];
+  while (std::fgets(line, sizeof line, f)) {
+    char *hash = std::strchr(line, '#');
+    if (hash) *hash = 0;
+    for (char *t = std::strtok(line, " \t\r\n"); t; t = std::strtok(nullptr, " \t\r\n")) tok.emplace_back(t);
+  }
+  std::fclose(f);
+  return apply_tokens(tok, opts, bad, bad_len);
 }
 
 int cvb_init(cvb_ctx **out, const cvb_options *opts) {

@@ -107,6 +107,18 @@ typedef struct {
 } cvb_solve_stats;
 
 int cvb_solve_opts_default(cvb_solve_opts *opts);
+/* Update opts from options in the reference's control.dat syntax ("-name value"
+ * per line, '#' starts a comment, later occurrences win), as PETSc's options
+ * database reads them for PoissonSolver_MG (poisson.c:1829-1983;
+ * control.dat~:65-74): -ps_ksp_rtol, -ps_ksp_atol, -ps_ksp_max_it,
+ * -ps_ksp_gmres_restart, and this library's -cvb_precision {fp64|mixed},
+ * -cvb_smoother {zebra|jacobi}, -cvb_pre_sweeps, -cvb_post_sweeps, -cvb_omega,
+ * -cvb_coarse_dense_max.  Other options are ignored.  The _args form takes
+ * argv-style tokens (command-line options override control.dat when applied
+ * after it).  Returns CVB_BAD_INPUT, with the offending option in *bad (may be
+ * NULL), for an unreadable file or a malformed value. */
+int cvb_solve_opts_from_file(const char *path, cvb_solve_opts *opts, char *bad, int bad_len);
+int cvb_solve_opts_from_args(int argc, const char *const *argv, cvb_solve_opts *opts, char *bad, int bad_len);
 
 /* --- context ------------------------------------------------------------- */
 int cvb_init(cvb_ctx **ctx, const cvb_options *opts);
