@@ -729,9 +729,9 @@ static int norm2(cvb_ctx *ctx, const double *v, size_t n, double *out) {
 
 static int fluid_mean_zero(cvb_ctx *ctx, int level, double *x) {
   LevelDev &L = ctx->L[level];
-  launch_fluid_mean_partial(L.g, L.nvert, x, ctx->partial, ctx->stream);
+  launch_fluid_mean_partial(L.g, L.code, x, ctx->partial, ctx->stream);
   launch_finish_sums(ctx->partial, 2, reduce_blocks(), ctx->sums, ctx->stream);
-  launch_add_fluid_const(L.g, L.nvert, x, ctx->sums, 1, ctx->stream);
+  launch_add_fluid_const(L.g, L.code, x, ctx->sums, 1, ctx->stream);
   CKL();
   return CVB_OK;
 }
@@ -880,9 +880,9 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
 static int project_rhs(cvb_ctx *ctx, double *b, double *removed) {
   int l = ctx->nlevels - 1;
   LevelDev &F = ctx->L[l];
-  launch_fluid_ratio_partial(F.g, F.nvert, b, ctx->aj64[l], ctx->partial, ctx->stream);
+  launch_fluid_ratio_partial(F.g, F.code, b, ctx->aj64[l], ctx->partial, ctx->stream);
   launch_finish_sums(ctx->partial, 3, reduce_blocks(), ctx->sums, ctx->stream);
-  launch_remove_aj_mean(F.g, F.nvert, ctx->aj64[l], b, ctx->sums, ctx->stream);
+  launch_remove_aj_mean(F.g, F.code, ctx->aj64[l], b, ctx->sums, ctx->stream);
   CKL();
   double h[3];
   CK(cudaMemcpyAsync(h, ctx->sums, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));

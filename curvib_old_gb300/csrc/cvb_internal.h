@@ -18,6 +18,7 @@ enum Slot { CP, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, 
 //   bit 0       identity row (boundary ring, or nvert > 0.1)
 //   bits 1..6   face active from this row's side: E, W, N, S, T, B
 //   bit 7       blocked: nvert > 0.1 (read by the grid transfers)
+//   bit 20      fluid: interior and nvert < 0.1
 //   bits 8..19  cross-derivative form for this cell's three upper faces, 2 bits each:
 //               E: (j, k)  N: (i, k)  T: (i, j)   0 none, 1 central, 2 lower, 3 upper
 // A lower face (W/S/B) of a row is the upper face of its lower neighbour, so a
@@ -25,6 +26,7 @@ enum Slot { CP, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, 
 enum : uint32_t {
   CODE_IDENTITY = 1u,
   CODE_BLOCKED = 1u << 7,  // nvert > 0.1 (IB or solid), any cell
+  CODE_FLUID = 1u << 20,   // interior cell with nvert < 0.1 (the null space's and range projection's cells)
   CODE_ACT_E = 1u << 1, CODE_ACT_W = 1u << 2, CODE_ACT_N = 1u << 3,
   CODE_ACT_S = 1u << 4, CODE_ACT_T = 1u << 5, CODE_ACT_B = 1u << 6,
 };
@@ -194,16 +196,29 @@ void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, siz
                        float *dst32 = nullptr);
 void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev,
                    int nz, size_t n, cudaStream_t s);
-void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial,
+void launch_fluid_mean_partial(const Geom &g, const uint32_t *code, const double *x, double *partial,
                                cudaStream_t s);
-void launch_add_fluid_const(const Geom &g, const double *nvert, double *x, const double *sumcnt,
+void launch_add_fluid_const(const Geom &g, const uint32_t *code, double *x, const double *sumcnt,
                             int zero_outside, cudaStream_t s);
 // range projection of a right-hand side: sums of b/aj and counts over fluid cells,
 // then b -= aj * sum/count there
-void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double *b, const double *aj,
+void launch_fluid_ratio_partial(const Geom &g, const uint32_t *code, const double *b, const double *aj,
                                 double *partial, cudaStream_t s);
-void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
+void launch_remove_aj_mean(const Geom &g, const uint32_t *code, const double *aj, double *b, const double *sums,
                            cudaStream_t s);
+// b / a for the range projection's sum: an FP32 reciprocal refined by two
+// Newton-Raphson steps in FP64 (r <- r + r (1 - a r)), within a unit or so in
+// the last place of the quotient, at a fraction of an FP64 division's cost on
+// this part (whose FP64 rate is low); a plain division where the FP32
+// reciprocal cannot represent 1/a.
+__device__ __forceinline__ double quot_newton(double b, double a) {
+  const float af = (float)a;
+  double r = (double)__frcp_rn(af);
+  if (!(r != 0.0 && r * 0.0 == 0.0)) return b / a;
+  r = fma(r, fma(-a, r, 1.0), r);
+  r = fma(r, fma(-a, r, 1.0), r);
+  return b * r;
+}
 // coarsest solve e = M^-1 r on C.cidx[0..C.cm), e = r on the other cells
 void launch_dense_apply(const LevelDev &C, const double *Minv, const double *r, double *e, cudaStream_t s,
                         const int *gate = nullptr);

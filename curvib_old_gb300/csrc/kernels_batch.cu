@@ -453,21 +453,18 @@ void glaunch_update(const TaskList &tl, const BProblem *P, cudaStream_t s) {
 
 // Null space (PoissonNullSpaceFunction, poisson.c:411-558) on the finest level:
 // sums and counts of x over interior fluid cells into partial rows 0, 1.
-__device__ __forceinline__ bool fluid_cell(const Geom &g, const double *nv, size_t p) {
-  int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
-  return i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1;
-}
+__device__ __forceinline__ bool fluid_cell(const uint32_t *code, size_t p) { return (code[p] & CODE_FLUID) != 0; }
 __global__ void __launch_bounds__(kRed) kg_fluid_sum(const __grid_constant__ TaskList tl, const BProblem *__restrict__ PP) {
   dep_sync();
   const GTask &K = tl.t[find_task(tl, blockIdx.x)];
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
   const Geom g = P.F->g;
-  const double *nv = P.F->nvert;
+  const uint32_t *cd = P.F->code;
   const int lb = blockIdx.x - K.block0;
   double acc[2] = {0.0, 0.0};
   for (size_t p = (size_t)lb * kRed + threadIdx.x; p < P.n; p += (size_t)P.nb * kRed)
-    if (fluid_cell(g, nv, p)) {
+    if (fluid_cell(cd, p)) {
       acc[0] += P.x[p];
       acc[1] += 1.0;
     }
@@ -480,10 +477,10 @@ __global__ void kg_add_fluid_const(const __grid_constant__ TaskList tl, const BP
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
   const Geom g = P.F->g;
-  const double *nv = P.F->nvert;
+  const uint32_t *cd = P.F->code;
   const double shift = P.sums[1] > 0.0 ? P.sums[0] / (-1.0 * P.sums[1]) : 0.0;
   for (size_t p = (size_t)(blockIdx.x - K.block0) * 256 + threadIdx.x; p < P.n; p += (size_t)K.gx * 256) {
-    if (fluid_cell(g, nv, p)) P.x[p] += shift;
+    if (fluid_cell(cd, p)) P.x[p] += shift;
     else P.x[p] = 0.0;
   }
 }
@@ -495,12 +492,12 @@ __global__ void __launch_bounds__(kRed) kg_fluid_ratio(const __grid_constant__ T
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
   const Geom g = P.F->g;
-  const double *nv = P.F->nvert;
+  const uint32_t *cd = P.F->code;
   const int lb = blockIdx.x - K.block0;
   double acc[2] = {0.0, 0.0};
   for (size_t p = (size_t)lb * kRed + threadIdx.x; p < P.n; p += (size_t)P.nb * kRed)
-    if (fluid_cell(g, nv, p)) {
-      acc[0] += P.b[p] / P.aj[p];
+    if (fluid_cell(cd, p)) {
+      acc[0] += quot_newton(P.b[p], P.aj[p]);
       acc[1] += 1.0;
     }
   int rows[2] = {0, 1};
@@ -512,10 +509,10 @@ __global__ void kg_remove_aj_mean(const __grid_constant__ TaskList tl, const BPr
   if (gated(K.gate)) return;
   const BProblem P = PP[K.p0];
   const Geom g = P.F->g;
-  const double *nv = P.F->nvert;
+  const uint32_t *cd = P.F->code;
   const double c = P.sums[1] > 0.0 ? P.sums[0] / P.sums[1] : 0.0;
   for (size_t p = (size_t)(blockIdx.x - K.block0) * 256 + threadIdx.x; p < P.n; p += (size_t)K.gx * 256)
-    if (fluid_cell(g, nv, p)) P.b[p] -= P.aj[p] * c;
+    if (fluid_cell(cd, p)) P.b[p] -= P.aj[p] * c;
 }
 void glaunch_fluid_sum(const TaskList &tl, const BProblem *P, cudaStream_t s) {
   if (!tl.n) return;

@@ -213,76 +213,73 @@ void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64,
 
 // Null space (PoissonNullSpaceFunction, poisson.c:411-558): sums and counts of x
 // over interior fluid cells (nvert < 0.1).
-__global__ void __launch_bounds__(kRedThreads) k_fluid_sum(Geom g, const double *__restrict__ nv,
+__global__ void __launch_bounds__(kRedThreads) k_fluid_sum(Geom g, const uint32_t *__restrict__ code,
                                                            const double *__restrict__ x, double *partial) {
   dep_sync();
   double acc[2] = {0.0, 0.0};
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
-    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
-    if (i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1) {
+    if (code[p] & CODE_FLUID) {
       acc[0] += x[p];
       acc[1] += 1.0;
     }
   }
   block_reduce_store<2>(acc, partial, gridDim.x, 0);
 }
-void launch_fluid_mean_partial(const Geom &g, const double *nvert, const double *x, double *partial, cudaStream_t s) {
-  launch_dep(k_fluid_sum, reduce_blocks(), kRedThreads, 0, s, g, nvert, x, partial);
+void launch_fluid_mean_partial(const Geom &g, const uint32_t *code, const double *x, double *partial,
+                               cudaStream_t s) {
+  launch_dep(k_fluid_sum, reduce_blocks(), kRedThreads, 0, s, g, code, x, partial);
 }
 // x += -sum/count on interior fluid cells; with zero_outside the ring and the
 // non-fluid cells are set to zero.
-__global__ void k_add_fluid_const(Geom g, const double *__restrict__ nv, double *__restrict__ x,
+__global__ void k_add_fluid_const(Geom g, const uint32_t *__restrict__ code, double *__restrict__ x,
                                   const double *__restrict__ sc, int zero_outside) {
   dep_sync();
   double shift = sc[1] > 0.0 ? sc[0] / (-1.0 * sc[1]) : 0.0;
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
-    bool interior = i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2;
-    if (interior && nv[p] < 0.1) x[p] += shift;
-    if (zero_outside && (!interior || nv[p] > 0.1)) x[p] = 0.0;
+    const uint32_t c = code[p];
+    if (c & CODE_FLUID) x[p] += shift;
+    if (zero_outside && (c & CODE_IDENTITY)) x[p] = 0.0;  // the ring and nvert > 0.1
   }
 }
-void launch_add_fluid_const(const Geom &g, const double *nvert, double *x, const double *sumcnt, int zero_outside,
+void launch_add_fluid_const(const Geom &g, const uint32_t *code, double *x, const double *sumcnt, int zero_outside,
                             cudaStream_t s) {
-  launch_dep(k_add_fluid_const, reduce_blocks(), 256, 0, s, g, nvert, x, sumcnt, zero_outside);
+  launch_dep(k_add_fluid_const, reduce_blocks(), 256, 0, s, g, code, x, sumcnt, zero_outside);
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_fluid_ratio(Geom g, const double *__restrict__ nv,
+__global__ void __launch_bounds__(kRedThreads) k_fluid_ratio(Geom g, const uint32_t *__restrict__ code,
                                                              const double *__restrict__ b, const double *__restrict__ aj,
                                                              double *partial) {
   dep_sync();
   double acc[3] = {0.0, 0.0, 0.0};
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
-    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
-    if (i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1) {
-      acc[0] += b[p] / aj[p];
+    if (code[p] & CODE_FLUID) {
+      acc[0] += quot_newton(b[p], aj[p]);
       acc[1] += 1.0;
     }
     acc[2] = fma(b[p], b[p], acc[2]);
   }
   block_reduce_store<3>(acc, partial, gridDim.x, 0);
 }
-void launch_fluid_ratio_partial(const Geom &g, const double *nvert, const double *b, const double *aj,
+void launch_fluid_ratio_partial(const Geom &g, const uint32_t *code, const double *b, const double *aj,
                                 double *partial, cudaStream_t s) {
-  launch_dep(k_fluid_ratio, reduce_blocks(), kRedThreads, 0, s, g, nvert, b, aj, partial);
+  launch_dep(k_fluid_ratio, reduce_blocks(), kRedThreads, 0, s, g, code, b, aj, partial);
 }
-__global__ void k_remove_aj_mean(Geom g, const double *__restrict__ nv, const double *__restrict__ aj,
+__global__ void k_remove_aj_mean(Geom g, const uint32_t *__restrict__ code, const double *__restrict__ aj,
                                  double *__restrict__ b, const double *__restrict__ sums) {
   dep_sync();
   double c = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
-    if (i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2 && nv[p] < 0.1)
+    if (code[p] & CODE_FLUID)
       b[p] -= aj[p] * c;
   }
 }
-void launch_remove_aj_mean(const Geom &g, const double *nvert, const double *aj, double *b, const double *sums,
+void launch_remove_aj_mean(const Geom &g, const uint32_t *code, const double *aj, double *b, const double *sums,
                            cudaStream_t s) {
-  launch_dep(k_remove_aj_mean, reduce_blocks(), 256, 0, s, g, nvert, aj, b, sums);
+  launch_dep(k_remove_aj_mean, reduce_blocks(), 256, 0, s, g, code, aj, b, sums);
 }
 
 // Coarsest level: e = Minv r with a dense FP64 inverse over the cells idx[0..m)

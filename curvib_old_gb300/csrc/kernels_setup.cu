@@ -85,6 +85,7 @@ __global__ void k_codes(Geom g, const double *__restrict__ nv, uint32_t *__restr
       if (NV(i, j, k - 1) < thr && k != z_str) c |= CODE_ACT_B;
     }
     if (NV(i, j, k) > 0.1) c |= CODE_BLOCKED;
+    if (ini && inj && ink && NV(i, j, k) < 0.1) c |= CODE_FLUID;
     code[p] = c;
   }
 }
