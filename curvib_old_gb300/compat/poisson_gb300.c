@@ -1,0 +1,190 @@
+/*
+ * Source-level drop-in of CURVIB's pressure-projection path onto libcvb (see
+ * poisson_gb300.h for what it replaces).  Compiled in the CURVIB tree:
+ *
+ *   cc -c poisson_gb300.c -I<curvib> -I<this repo>/include $(PETSC_CC_INCLUDES)
+ *   link with -L<this repo>/curvib_old_gb300/_build -lcvb
+ *
+ * The arrays handed to libcvb are the PETSc vectors' own storage: VecGetArray
+ * on a DMDA vector of one rank gives its box [k][j][i], i fastest, with
+ * Cmpnts interleaved -- the layout cvb.h takes.  Local (ghosted) vectors give
+ * the ghosted box that cvb_level_desc's gxs..gzm describe.  Nothing is
+ * converted or copied on the host.
+ */
+#include <string.h>
+#include "variables.h"
+#include "cvb.h"
+#include "poisson_gb300.h"
+
+extern PetscInt block_number, immersed; /* main.c, as poisson.c:6-7 declares them */
+PetscErrorCode Contra2Cart(UserCtx *user);
+PetscErrorCode GhostNodeVelocity(UserCtx *user);
+
+static cvb_ctx *g_cvb = NULL;
+static cvb_solve_opts g_opts;
+
+static PetscErrorCode report(int rc, const char *where) {
+  if (rc)
+    PetscPrintf(PETSC_COMM_WORLD, "%s: %s\n", where,
+                g_cvb ? cvb_last_error(g_cvb) : "libcvb context not created");
+  return rc;
+}
+
+static UserCtx *finest(UserMG *usermg) { return &usermg->mgctx[usermg->mglevels - 1].user[0]; }
+
+/* The ghosted arrays of one level: the nine face-metric fields, the four
+ * Jacobian fields, and on the finest level the three cell-centre metric fields
+ * Projection reads.  Level 0 is the coarsest, as mgctx[0] (init.c:839-850). */
+#define DESC_ARRAYS 16
+static void desc_get(UserCtx *u, cvb_level_desc *d, int fine, PetscScalar *hold[DESC_ARRAYS]) {
+  PetscInt gxs, gys, gzs, gxm, gym, gzm;
+  DMDAGetGhostCorners(u->da, &gxs, &gys, &gzs, &gxm, &gym, &gzm);
+  memset(d, 0, sizeof *d);
+  d->mx = u->info.mx; d->my = u->info.my; d->mz = u->info.mz;
+  d->gxs = gxs; d->gys = gys; d->gzs = gzs;
+  d->gxm = gxm; d->gym = gym; d->gzm = gzm;
+  for (int f = 0; f < 6; f++) d->bctype[f] = u->bctype[f];
+  d->isc = u->isc; d->jsc = u->jsc; d->ksc = u->ksc;
+  Vec v[DESC_ARRAYS] = {u->lICsi, u->lIEta, u->lIZet, u->lJCsi, u->lJEta, u->lJZet,
+                        u->lKCsi, u->lKEta, u->lKZet, u->lIAj,  u->lJAj,  u->lKAj,
+                        u->lAj,   u->lCsi,  u->lEta,  u->lZet};
+  for (int q = 0; q < DESC_ARRAYS; q++) {
+    hold[q] = NULL;
+    if (q < 13 || fine) VecGetArray(v[q], &hold[q]);
+  }
+  d->icsi = hold[0]; d->ieta = hold[1]; d->izet = hold[2];
+  d->jcsi = hold[3]; d->jeta = hold[4]; d->jzet = hold[5];
+  d->kcsi = hold[6]; d->keta = hold[7]; d->kzet = hold[8];
+  d->iaj = hold[9]; d->jaj = hold[10]; d->kaj = hold[11]; d->aj = hold[12];
+  d->csi = hold[13]; d->eta = hold[14]; d->zet = hold[15];
+}
+
+static void desc_restore(UserCtx *u, PetscScalar *hold[DESC_ARRAYS]) {
+  Vec v[DESC_ARRAYS] = {u->lICsi, u->lIEta, u->lIZet, u->lJCsi, u->lJEta, u->lJZet,
+                        u->lKCsi, u->lKEta, u->lKZet, u->lIAj,  u->lJAj,  u->lKAj,
+                        u->lAj,   u->lCsi,  u->lEta,  u->lZet};
+  for (int q = 0; q < DESC_ARRAYS; q++)
+    if (hold[q]) VecRestoreArray(v[q], &hold[q]);
+}
+
+/* PETSc's options database -> cvb_solve_opts.  The names are the ones the
+ * reference's KSP reads under its "ps_" prefix (poisson.c:1829) and the
+ * library's own; libcvb parses and checks the values. */
+static PetscErrorCode read_options(void) {
+  static const char *const names[] = {"-ps_ksp_rtol",    "-ps_ksp_atol",     "-ps_ksp_max_it",
+                                      "-ps_ksp_gmres_restart", "-cvb_precision", "-cvb_smoother",
+                                      "-cvb_pre_sweeps", "-cvb_post_sweeps", "-cvb_omega",
+                                      "-cvb_coarse_dense_max"};
+  enum { NOPT = sizeof names / sizeof names[0] };
+  char values[NOPT][64];
+  const char *tok[2 * NOPT];
+  int n = 0;
+  cvb_solve_opts_default(&g_opts);
+  for (int q = 0; q < NOPT; q++) {
+    PetscBool set = PETSC_FALSE;
+    values[q][0] = 0;
+    PetscOptionsGetString(PETSC_NULL, names[q], values[q], sizeof values[q], &set);
+    if (set) { tok[n++] = names[q]; tok[n++] = values[q]; }
+  }
+  char bad[96] = "";
+  int rc = cvb_solve_opts_from_args(n, tok, &g_opts, bad, (int)sizeof bad);
+  if (rc) PetscPrintf(PETSC_COMM_WORLD, "PoissonSetup_GB300: bad option %s\n", bad);
+  return rc;
+}
+
+PetscErrorCode PoissonSetup_GB300(UserMG *usermg) {
+  const int nl = usermg->mglevels;
+  if (block_number != 1 || nl < 1 || nl > 16) {
+    PetscPrintf(PETSC_COMM_WORLD, "PoissonSetup_GB300: one block and 1-16 levels only\n");
+    return CVB_BAD_INPUT;
+  }
+  int rc = read_options();
+  if (rc) return rc;
+  if (!g_cvb) {
+    cvb_options o;
+    memset(&o, 0, sizeof o); /* device 0, the context's own stream */
+    rc = cvb_init(&g_cvb, &o);
+    if (rc) return report(rc, "PoissonSetup_GB300");
+  }
+  cvb_level_desc d[16];
+  PetscScalar *hold[16][DESC_ARRAYS];
+  for (int l = 0; l < nl; l++) desc_get(&usermg->mgctx[l].user[0], &d[l], l == nl - 1, hold[l]);
+  PetscScalar *nv;
+  VecGetArray(finest(usermg)->lNvert, &nv);
+  rc = cvb_setup_hierarchy(g_cvb, nl, d, nv);
+  VecRestoreArray(finest(usermg)->lNvert, &nv);
+  for (int l = 0; l < nl; l++) desc_restore(&usermg->mgctx[l].user[0], hold[l]);
+  return report(rc, "PoissonSetup_GB300");
+}
+
+PetscErrorCode PoissonSetNvert_GB300(UserMG *usermg) {
+  PetscScalar *nv;
+  VecGetArray(finest(usermg)->lNvert, &nv);
+  int rc = cvb_set_nvert(g_cvb, nv);
+  VecRestoreArray(finest(usermg)->lNvert, &nv);
+  return report(rc, "PoissonSetNvert_GB300");
+}
+
+/* VolumeFlux_rev(flg = immersed) corrects Ucont in place, PoissonRHS forms B
+ * from it, and the solve writes Phi (poisson.c:1775-2017).  The ghosted copies
+ * of what changed are refreshed as the reference leaves them: lPhi after the
+ * solve (poisson.c:1985-1986) and lUcont, which VolumeFlux_rev's corrections
+ * reach through the global vector. */
+PetscErrorCode PoissonSolver_MG_GB300(UserMG *usermg) {
+  UserCtx *u = finest(usermg);
+  cvb_solve_stats st;
+  PetscScalar *uc, *phi;
+  memset(&st, 0, sizeof st);
+  VecGetArray(u->Ucont, &uc);
+  VecGetArray(u->Phi, &phi);
+  int rc = cvb_poisson_solver_mg(g_cvb, uc, u->FluxIntpSum, (int)immersed, u->dt, u->st, phi, &g_opts, &st);
+  VecRestoreArray(u->Phi, &phi);
+  VecRestoreArray(u->Ucont, &uc);
+  PetscPrintf(PETSC_COMM_WORLD, "PoissonSolver_MG_GB300: %d iterations, relative residual %e\n",
+              st.iterations, st.rel_residual);
+  DMGlobalToLocalBegin(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+  DMGlobalToLocalEnd(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+  DMGlobalToLocalBegin(u->da, u->Phi, INSERT_VALUES, u->lPhi);
+  DMGlobalToLocalEnd(u->da, u->Phi, INSERT_VALUES, u->lPhi);
+  return report(rc, "PoissonSolver_MG_GB300");
+}
+
+/* P += Phi with the periodic ring copies of both, then the ghosted copies
+ * (poisson.c:2908-3248 ends with lP and lPhi refreshed). */
+PetscErrorCode UpdatePressure_GB300(UserCtx *u) {
+  PetscScalar *p, *phi;
+  VecGetArray(u->P, &p);
+  VecGetArray(u->Phi, &phi);
+  int rc = cvb_update_pressure(g_cvb, p, phi);
+  VecRestoreArray(u->Phi, &phi);
+  VecRestoreArray(u->P, &p);
+  DMGlobalToLocalBegin(u->da, u->P, INSERT_VALUES, u->lP);
+  DMGlobalToLocalEnd(u->da, u->P, INSERT_VALUES, u->lP);
+  DMGlobalToLocalBegin(u->da, u->Phi, INSERT_VALUES, u->lPhi);
+  DMGlobalToLocalEnd(u->da, u->Phi, INSERT_VALUES, u->lPhi);
+  return report(rc, "UpdatePressure_GB300");
+}
+
+/* The flux correction of Projection, then what the reference does after it on
+ * the caller's side of the boundary (poisson.c:2897-2904): lUcont refreshed,
+ * Contra2Cart, GhostNodeVelocity. */
+PetscErrorCode Projection_GB300(UserCtx *u) {
+  PetscScalar *phi, *uc;
+  VecGetArray(u->Phi, &phi);
+  VecGetArray(u->Ucont, &uc);
+  int rc = cvb_projection(g_cvb, phi, u->dt, u->st, uc);
+  VecRestoreArray(u->Ucont, &uc);
+  VecRestoreArray(u->Phi, &phi);
+  if (rc) return report(rc, "Projection_GB300");
+  DMGlobalToLocalBegin(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+  DMGlobalToLocalEnd(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+  Contra2Cart(u);
+  GhostNodeVelocity(u);
+  return 0;
+}
+
+PetscErrorCode PoissonFinalize_GB300(void) {
+  if (g_cvb) cvb_destroy(g_cvb);
+  g_cvb = NULL;
+  return 0;
+}

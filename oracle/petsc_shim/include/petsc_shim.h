@@ -229,6 +229,22 @@ PetscErrorCode VecGetArray3d(Vec x, PetscInt m, PetscInt n, PetscInt p, PetscInt
                              PetscInt ps, PetscScalar ****a);
 PetscErrorCode VecRestoreArray3d(Vec x, PetscInt m, PetscInt n, PetscInt p, PetscInt ms,
                                  PetscInt ns, PetscInt ps, PetscScalar ****a);
+/* The vector's own storage (a DMDA vector's box, dof interleaved).  Every Get
+ * must be matched by a Restore; shim_arrays_out() counts the unmatched ones. */
+PetscErrorCode VecGetArray(Vec x, PetscScalar **a);
+PetscErrorCode VecRestoreArray(Vec x, PetscScalar **a);
+int shim_arrays_out(void);
+PetscErrorCode DMDAGetGhostCorners(DM da, PetscInt *x, PetscInt *y, PetscInt *z, PetscInt *m,
+                                   PetscInt *n, PetscInt *p);
+/* A flat options table ("-name" -> value string), as PETSc's options database
+ * holds control.dat and the command line.  Get* leave the value untouched and
+ * set *set = PETSC_FALSE when the option is absent. */
+PetscErrorCode PetscOptionsSetValue(const char name[], const char value[]);
+PetscErrorCode PetscOptionsClear(void);
+PetscErrorCode PetscOptionsGetString(const char pre[], const char name[], char s[], size_t len,
+                                     PetscBool *set);
+PetscErrorCode PetscOptionsGetReal(const char pre[], const char name[], PetscReal *v, PetscBool *set);
+PetscErrorCode PetscOptionsGetInt(const char pre[], const char name[], PetscInt *v, PetscBool *set);
 PetscErrorCode VecScatterCreateToZero(Vec x, VecScatter *ctx, Vec *out);
 PetscErrorCode VecScatterBegin(VecScatter ctx, Vec x, Vec y, InsertMode m, ScatterMode s);
 PetscErrorCode VecScatterEnd(VecScatter ctx, Vec x, Vec y, InsertMode m, ScatterMode s);

@@ -419,6 +419,71 @@ PetscErrorCode VecGetSize(Vec x, PetscInt *n) { *n = x->n; return 0; }
 PetscErrorCode VecAssemblyBegin(Vec x) { (void)x; return 0; }
 PetscErrorCode VecAssemblyEnd(Vec x) { (void)x; return 0; }
 
+static int g_arrays_out = 0;
+PetscErrorCode VecGetArray(Vec x, PetscScalar **a) {
+  *a = x->a;
+  g_arrays_out++;
+  return 0;
+}
+PetscErrorCode VecRestoreArray(Vec x, PetscScalar **a) {
+  if (*a != x->a) return 1;
+  *a = NULL;
+  g_arrays_out--;
+  return 0;
+}
+int shim_arrays_out(void) { return g_arrays_out; }
+PetscErrorCode DMDAGetGhostCorners(DM da, PetscInt *x, PetscInt *y, PetscInt *z, PetscInt *m,
+                                   PetscInt *n, PetscInt *p) {
+  if (x) *x = da->info.gxs;
+  if (y) *y = da->info.gys;
+  if (z) *z = da->info.gzs;
+  if (m) *m = da->info.gxm;
+  if (n) *n = da->info.gym;
+  if (p) *p = da->info.gzm;
+  return 0;
+}
+
+#define MAXOPT 64
+static struct { char name[64], value[64]; } g_opt[MAXOPT];
+static int g_nopt = 0;
+PetscErrorCode PetscOptionsSetValue(const char name[], const char value[]) {
+  int q = 0;
+  while (q < g_nopt && strcmp(g_opt[q].name, name)) q++;
+  if (q == MAXOPT || strlen(name) >= 64 || (value && strlen(value) >= 64)) return 1;
+  if (q == g_nopt) g_nopt++;
+  strcpy(g_opt[q].name, name);
+  strcpy(g_opt[q].value, value ? value : "");
+  return 0;
+}
+PetscErrorCode PetscOptionsClear(void) { g_nopt = 0; return 0; }
+static const char *opt_find(const char pre[], const char name[]) {
+  char full[160];
+  /* PETSc inserts the prefix after the leading dash */
+  snprintf(full, sizeof full, "-%s%s", pre ? pre : "", name[0] == '-' ? name + 1 : name);
+  for (int q = 0; q < g_nopt; q++)
+    if (!strcmp(g_opt[q].name, full)) return g_opt[q].value;
+  return NULL;
+}
+PetscErrorCode PetscOptionsGetString(const char pre[], const char name[], char s[], size_t len,
+                                     PetscBool *set) {
+  const char *v = opt_find(pre, name);
+  if (set) *set = v ? PETSC_TRUE : PETSC_FALSE;
+  if (v && len) { strncpy(s, v, len - 1); s[len - 1] = 0; }
+  return 0;
+}
+PetscErrorCode PetscOptionsGetReal(const char pre[], const char name[], PetscReal *r, PetscBool *set) {
+  const char *v = opt_find(pre, name);
+  if (set) *set = v ? PETSC_TRUE : PETSC_FALSE;
+  if (v) *r = strtod(v, NULL);
+  return 0;
+}
+PetscErrorCode PetscOptionsGetInt(const char pre[], const char name[], PetscInt *r, PetscBool *set) {
+  const char *v = opt_find(pre, name);
+  if (set) *set = v ? PETSC_TRUE : PETSC_FALSE;
+  if (v) *r = (PetscInt)strtol(v, NULL, 10);
+  return 0;
+}
+
 PetscErrorCode VecGetArray3d(Vec x, PetscInt m, PetscInt n, PetscInt p, PetscInt ms, PetscInt ns,
                              PetscInt ps, PetscScalar ****a) {
   (void)ms; (void)ns; (void)ps;

@@ -190,6 +190,10 @@ int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, in
   return 0;
 }
 
+/* The hierarchy ref_init built, for drivers that call CURVIB-side code taking a
+ * UserMG (the source-level binding's tests). */
+UserMG *ref_usermg(void) { return g_ready ? &g_mg : NULL; }
+
 int ref_dims(int level, int *mx, int *my, int *mz) {
   if (!g_ready || level < 0 || level >= g_mg.mglevels) return 1;
   *mx = U(level)->info.mx; *my = U(level)->info.my; *mz = U(level)->info.mz;

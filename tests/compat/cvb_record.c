@@ -1,0 +1,102 @@
+/* TEST INFRASTRUCTURE ONLY: see cvb_record.h. */
+#include <stdlib.h>
+#include <string.h>
+#include "cvb_record.h"
+
+cvb_record REC;
+static int g_ctx_token;
+
+int cvb_solve_opts_default(cvb_solve_opts *o) {
+  memset(o, 0, sizeof *o);
+  o->precision = CVB_PRECISION_MIXED;
+  o->rtol = 1e-8;
+  o->max_it = 200;
+  o->restart = 30;
+  return CVB_OK;
+}
+
+/* Keeps the tokens; understands -ps_ksp_rtol and -cvb_precision, and refuses
+ * the value "bad", which is all the binding's test needs (the real parser has
+ * its own tests). */
+int cvb_solve_opts_from_args(int argc, const char *const *argv, cvb_solve_opts *o, char *bad, int bad_len) {
+  REC.ntok = 0;
+  for (int q = 0; q < argc && q < REC_MAXTOK; q++) {
+    strncpy(REC.tok[q], argv[q], 63);
+    REC.tok[q][63] = 0;
+    REC.ntok++;
+  }
+  for (int q = 0; q + 1 < argc; q += 2) {
+    if (!strcmp(argv[q + 1], "bad")) {
+      if (bad && bad_len > 0) { strncpy(bad, argv[q], (size_t)bad_len - 1); bad[bad_len - 1] = 0; }
+      return CVB_BAD_INPUT;
+    }
+    if (!strcmp(argv[q], "-ps_ksp_rtol")) o->rtol = strtod(argv[q + 1], NULL);
+    if (!strcmp(argv[q], "-cvb_precision")) o->precision = strcmp(argv[q + 1], "fp64") ? CVB_PRECISION_MIXED : CVB_PRECISION_FP64;
+  }
+  return CVB_OK;
+}
+
+int cvb_init(cvb_ctx **ctx, const cvb_options *opts) {
+  (void)opts;
+  REC.n_init++;
+  *ctx = (cvb_ctx *)&g_ctx_token;
+  return CVB_OK;
+}
+void cvb_destroy(cvb_ctx *ctx) {
+  (void)ctx;
+  REC.n_destroy++;
+}
+const char *cvb_last_error(const cvb_ctx *ctx) {
+  (void)ctx;
+  REC.n_last_error++;
+  return "recorded failure";
+}
+
+static int take_status(void) {
+  int rc = REC.fail_next;
+  REC.fail_next = 0;
+  return rc;
+}
+
+int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *levels, const double *nvert_finest) {
+  (void)ctx;
+  REC.n_setup++;
+  REC.nlevels = nlevels;
+  for (int l = 0; l < nlevels && l < 16; l++) REC.levels[l] = levels[l];
+  REC.nvert = nvert_finest;
+  return take_status();
+}
+int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
+  (void)ctx;
+  REC.n_set_nvert++;
+  REC.nvert = nvert_finest;
+  return take_status();
+}
+int cvb_poisson_solver_mg(cvb_ctx *ctx, double *ucont, double flux_intp_sum, int immersed, double dt, double st,
+                          double *phi, const cvb_solve_opts *opts, cvb_solve_stats *stats) {
+  (void)ctx;
+  REC.n_solver_mg++;
+  REC.ucont = ucont; REC.phi = phi;
+  REC.flux_intp_sum = flux_intp_sum; REC.immersed = immersed; REC.dt = dt; REC.st = st;
+  REC.opts = *opts;
+  ucont[3 * REC.mark + 1] = 42.0;
+  phi[REC.mark] = 3.0;
+  memset(stats, 0, sizeof *stats);
+  stats->iterations = 6;
+  stats->status = REC.fail_next;
+  return take_status();
+}
+int cvb_update_pressure(cvb_ctx *ctx, double *p, double *phi) {
+  (void)ctx;
+  REC.n_update++;
+  REC.p = p; REC.phi_up = phi;
+  p[REC.mark] = 7.0;
+  return take_status();
+}
+int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont) {
+  (void)ctx;
+  REC.n_projection++;
+  REC.phi_proj = phi; REC.dt_proj = dt; REC.st_proj = st; REC.ucont_proj = ucont;
+  ucont[3 * REC.mark] = 5.0;
+  return take_status();
+}

@@ -1,0 +1,40 @@
+/*
+ * TEST INFRASTRUCTURE ONLY.  A recording stand-in for the libcvb entry points
+ * the source-level binding (curvib_old_gb300/compat/poisson_gb300.c) calls, so
+ * that the binding can run on a CPU against a real UserMG and the test can see
+ * exactly which arrays and values reach the library.  Each path call also
+ * writes one marked cell of the arrays it may change, so the test can check
+ * that the binding refreshes the ghosted copies afterwards.
+ */
+#ifndef CVB_RECORD_H
+#define CVB_RECORD_H
+#include "cvb.h"
+
+#define REC_MAXTOK 32
+
+typedef struct {
+  int n_init, n_destroy, n_last_error, n_setup, n_set_nvert, n_solver_mg, n_update, n_projection;
+  int ntok;
+  char tok[REC_MAXTOK][64];
+  int nlevels;
+  cvb_level_desc levels[16];
+  const double *nvert;
+  /* cvb_poisson_solver_mg */
+  double *ucont, *phi, flux_intp_sum, dt, st;
+  int immersed;
+  cvb_solve_opts opts;
+  /* cvb_update_pressure */
+  double *p, *phi_up;
+  /* cvb_projection */
+  const double *phi_proj;
+  double *ucont_proj, dt_proj, st_proj;
+  /* the status the next path call returns, then 0 again */
+  int fail_next;
+  /* cell (box index) the path calls write: solver_mg sets ucont[3m+1] = 42 and
+   * phi[m] = 3; update_pressure sets p[m] = 7; projection sets ucont[3m] = 5 */
+  long mark;
+} cvb_record;
+
+extern cvb_record REC;
+
+#endif
