@@ -547,9 +547,27 @@ inline size_t line_solve_smem(const Geom &g) { return sizeof(T) * 5 * (size_t)Li
 // gamma = m r, beta = -m a; backward: gamma = d, beta = -c), and affine maps
 // compose associatively: each lane composes the maps of its R rows, a shuffle
 // scan combines the lanes, each lane replays its rows.
-template <typename T, int NL, int RR = 0>
-__device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm, const T *sc, int stride,
-                                                 const LineLayout &Lo, int lane) {
+// Where the warp solve finds the Thomas factors of row t of its line l: in
+// shared memory beside the residual (offset o of the line layout), or in the
+// lane's registers (LaneFactors).
+template <typename T>
+struct SmemFactors {
+  const T *sa, *sm, *sc;
+  __device__ T a(int, int, int o) const { return sa[o]; }
+  __device__ T m(int, int, int o) const { return sm[o]; }
+  __device__ T c(int, int, int o) const { return sc[o]; }
+};
+template <typename T, int NL, int R>
+struct LaneFactors {
+  T a_[NL][R], m_[NL][R], c_[NL][R];
+  __device__ T a(int l, int t, int) const { return a_[l][t]; }
+  __device__ T m(int l, int t, int) const { return m_[l][t]; }
+  __device__ T c(int l, int t, int) const { return c_[l][t]; }
+};
+
+template <typename T, int NL, int RR = 0, typename FAC>
+__device__ __forceinline__ void warp_lines_solve(T *sr, const FAC &fac, int stride, const LineLayout &Lo,
+                                                 int lane) {
   const int q0 = lane * Lo.R, cnt = max(0, min(Lo.R, Lo.nr - q0));
   T B[NL], G[NL], d[NL];
 #pragma unroll
@@ -558,8 +576,8 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
-      T mq = sm[o];
-      T beta = -mq * sa[o], gamma = mq * sr[o];
+      T mq = fac.m(l, t, o);
+      T beta = -mq * fac.a(l, t, o), gamma = mq * sr[o];
       B[l] = beta * B[l];
       G[l] = beta * G[l] + gamma;
     }
@@ -581,8 +599,8 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
-      T mq = sm[o];
-      d[l] = mq * sr[o] - mq * sa[o] * d[l];
+      T mq = fac.m(l, t, o);
+      d[l] = mq * sr[o] - mq * fac.a(l, t, o) * d[l];
       sr[o] = d[l];
     }
   });
@@ -593,7 +611,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
-      T beta = -sc[o], gamma = sr[o];
+      T beta = -fac.c(l, t, o), gamma = sr[o];
       B[l] = beta * B[l];
       G[l] = beta * G[l] + gamma;
     }
@@ -615,7 +633,7 @@ __device__ __forceinline__ void warp_lines_solve(T *sr, const T *sa, const T *sm
 #pragma unroll
     for (int l = 0; l < NL; l++) {
       const int o = l * stride + t * 33 + lane;
-      d[l] = sr[o] - sc[o] * d[l];
+      d[l] = sr[o] - fac.c(l, t, o) * d[l];
       sr[o] = d[l];
     }
   });
@@ -650,15 +668,78 @@ struct Vec16<double> {
   __device__ static double at(const V &v, int u) { return u == 0 ? v.x : v.y; }
 };
 
+// Thomas factors straight into the lanes' registers, for R <= 4 rows per
+// lane: a lane's rows q0 .. q0 + R - 1 of a line are one piece of each of the
+// line's runs (a, 1/m, c'), aligned to R values since runs hold a multiple of 4
+// values and start 16-byte aligned.  Saves the factors' trip through shared
+// memory (a store and two to four loads per value).
+template <int RR>
+constexpr bool kRegFactors = RR >= 1 && RR <= 4;
+
+template <int N>
+__device__ __forceinline__ void ld_run(const float *p, float (&o)[N]) {
+  if constexpr (N == 4) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  } else if constexpr (N == 2) {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+  } else {
+    o[0] = __ldg(p);
+  }
+}
+template <int N>
+__device__ __forceinline__ void ld_run(const double *p, double (&o)[N]) {
+  if constexpr (N == 4) {
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 w = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    o[0] = v.x; o[1] = v.y; o[2] = w.x; o[3] = w.y;
+  } else if constexpr (N == 2) {
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+  } else {
+    o[0] = __ldg(p);
+  }
+}
+
+// The factors of the lines one warp solves in a tile: lines warp, warp + NW, ...
+template <typename T, int TW, int RR>
+using TileLaneFactors = LaneFactors<T, TW / (kSolveThreads / 32), (RR > 0 ? RR : 1)>;
+
+template <typename T, int TW, int RR>
+__device__ __forceinline__ void lane_factors_load(const LevelDev &L, int bx, int k, int color,
+                                                  TileLaneFactors<T, TW, RR> &f) {
+  constexpr int NW = kSolveThreads / 32, NL = TW / NW, R = RR > 0 ? RR : 1;
+  const Geom &g = L.g;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q0 = lane * R;
+  const bool kin = k >= 1 && k <= g.mz - 2;
+  const LineFac F = LineFac::of(g);
+  const T *fa = RowOf<T>::fac(L);
+#pragma unroll
+  for (int l = 0; l < NL; l++) {
+    const int il = tile_line(bx, warp + l * NW, k, TW, color);
+    if (kin && il >= 1 && il <= g.mx - 2 && q0 < g.my - 2) {
+      const T *p = fa + F.line(il, k) + q0;
+      ld_run<R>(p, f.a_[l]);
+      ld_run<R>(p + F.Q, f.m_[l]);
+      ld_run<R>(p + 2 * (size_t)F.Q, f.c_[l]);
+    } else {
+#pragma unroll
+      for (int t = 0; t < R; t++) f.a_[l][t] = f.m_[l][t] = f.c_[l][t] = T(0);
+    }
+  }
+}
+
 // Stage a tile: the residual (and x) rows by element copies (the lines are one
 // or two cells apart in rows of the caller's layout), the Thomas factors by
 // 16-byte loads of the lines' contiguous runs -- each warp takes whole runs,
 // all of its loads in flight before it stores any.
 // rx: stage r and x (else only the factors, the caller fills r and x).
+// fac: stage the factors (else the caller holds them in registers).
 template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__restrict__ r, const T *__restrict__ x,
                                                 int bx, int k, T *st, int color = -1, bool rsplit = false,
-                                                bool rx = true) {
+                                                bool rx = true, bool fac = true) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   if (!(k >= 1 && k <= g.mz - 2)) return;
@@ -676,6 +757,7 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
       if (x) cp_async_el(sx + s, x + p);
     }
   }
+  if (!fac) return;
   using VT = Vec16<T>;
   using V = typename VT::V;
   constexpr int W = VT::W, NW = kSolveThreads / 32, RUNS = (3 * TW + NW - 1) / NW;
@@ -710,7 +792,8 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
 // have landed and the block is synchronised when this is entered).
 template <typename T, int TW, int RR = 0>
 __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__restrict__ x, T *__restrict__ xnew,
-                                                  T omega, int bx, int k, T *st, int color = -1) {
+                                                  T omega, int bx, int k, T *st, int color,
+                                                  const TileLaneFactors<T, TW, RR> &lf) {
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   const LineLayout Lo = LineLayout::fixed<RR>(my);
@@ -726,7 +809,12 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
   constexpr int NW = kSolveThreads / 32, NL = TW / NW;
   if (kin) {
     const int o = warp * Lo.ls;
-    warp_lines_solve<T, NL, RR>(sr + o, sa + o, sm + o, sc + o, NW * Lo.ls, Lo, lane);
+    if constexpr (kRegFactors<RR>) {
+      warp_lines_solve<T, NL, RR>(sr + o, lf, NW * Lo.ls, Lo, lane);
+    } else {
+      const SmemFactors<T> fac{sa + o, sm + o, sc + o};
+      warp_lines_solve<T, NL, RR>(sr + o, fac, NW * Lo.ls, Lo, lane);
+    }
   }
   __syncthreads();
   if (i >= mx) return;
@@ -765,10 +853,12 @@ __device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__re
                                                 T omega, int bx, int k, unsigned char *smem_raw, int color = -1,
                                                 bool rsplit = false) {
   T *st = reinterpret_cast<T *>(smem_raw);
-  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color, rsplit);
+  TileLaneFactors<T, TW, RR> lf;
+  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color, rsplit, true, !kRegFactors<RR>);
+  if constexpr (kRegFactors<RR>) lane_factors_load<T, TW, RR>(L, bx, k, color, lf);
   cp_async_wait_all();
   __syncthreads();
-  solve_tile_finish<T, TW, RR>(L, x, xnew, omega, bx, k, st, color);
+  solve_tile_finish<T, TW, RR>(L, x, xnew, omega, bx, k, st, color, lf);
 }
 
 // Tiles of a line solve: all lines or one color's.
@@ -851,7 +941,7 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
       }
     }
     // the factors, as the line solve stages them (nothing to copy asynchronously)
-    solve_tile_load<T, TW, RR>(L, nullptr, nullptr, bx, k, st, color, false, false);
+    if constexpr (!kRegFactors<RR>) solve_tile_load<T, TW, RR>(L, nullptr, nullptr, bx, k, st, color, false, false);
   }
   if (xout != xin) {
     // the block's columns [2 TW bx, 2 TW (bx + 1)) of plane k, except the cells
@@ -867,8 +957,12 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
       }
     }
   }
+  // register factors after the residual loop, so that they do not add to its
+  // registers
+  TileLaneFactors<T, TW, RR> lf;
+  if constexpr (kRegFactors<RR>) lane_factors_load<T, TW, RR>(L, bx, k, color, lf);
   __syncthreads();
-  solve_tile_finish<T, TW, RR>(L, xin, xout, omega, bx, k, st, color);
+  solve_tile_finish<T, TW, RR>(L, xin, xout, omega, bx, k, st, color, lf);
 }
 
 
