@@ -1,8 +1,13 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE ONLY.
-# Compiles the reference's own poisson.c, metrics.c and implicitsolver.c, where
-# they lie under the reference checkout, unmodified, against the single-process
-# PETSc API shim in oracle/petsc_shim/, into oracle/_ref/libcvbref.so.  Nothing
+# Compiles the reference's own poisson.c, metrics.c, implicitsolver.c, rhs.c and
+# bcs.c, where they lie under the reference checkout, unmodified, against the
+# single-process PETSc API shim in oracle/petsc_shim/, into
+# oracle/_ref/libcvbref.so.  In the objects of rhs.c and bcs.c, Contra2Cart and
+# GhostNodeVelocity are renamed cvbref_Contra2Cart / cvbref_GhostNodeVelocity
+# (objcopy), so that Projection's own calls still reach the harness's inert
+# versions (its parity is checked before those two run) while the harness can
+# call the real ones directly.  Nothing
 # from the reference is copied into this repository; outputs go to oracle/_ref/
 # only.  Entry points the reference calls but the parity path never reaches
 # (SNES, KSP, other CURVIB files) become stubs that return a PETSc error code.
@@ -20,9 +25,13 @@ mkdir -p "$OUT"
 CC="${CC:-gcc}"
 CFLAGS="-std=gnu99 -O2 -fPIC -w -I$HERE/petsc_shim/include -I$REF"
 objs=()
-for f in poisson metrics implicitsolver; do
+for f in poisson metrics implicitsolver rhs bcs; do
   $CC $CFLAGS -c "$REF/$f.c" -o "$OUT/ref_$f.o"
   objs+=("$OUT/ref_$f.o")
+done
+for f in rhs bcs; do
+  objcopy --redefine-sym Contra2Cart=cvbref_Contra2Cart \
+          --redefine-sym GhostNodeVelocity=cvbref_GhostNodeVelocity "$OUT/ref_$f.o"
 done
 $CC $CFLAGS -c "$HERE/petsc_shim/petsc_shim.c" -o "$OUT/petsc_shim.o"
 $CC $CFLAGS -c "$HERE/petsc_shim/ref_harness.c" -o "$OUT/ref_harness.o"
@@ -34,10 +43,21 @@ set +e
 missing=$($CC -shared -o "$OUT/libcvbref.so" "${objs[@]}" -lm -Wl,--no-undefined 2>&1 |
   sed -n "s/.*undefined reference to \`\([A-Za-z_][A-Za-z0-9_]*\)'.*/\1/p" | sort -u)
 set -e
+# A symbol the reference declares as an extern variable (main.c's globals)
+# becomes zero-filled data, as main.c's defaults are; the rest become
+# functions that report themselves and return a PETSc error code.
+is_data() {
+  grep -qE "^[[:space:]]*extern[^;(]*[^A-Za-z0-9_]$1[^A-Za-z0-9_(][^(]*;|^[[:space:]]*extern[^;(]*[^A-Za-z0-9_]$1;" \
+    "$REF"/*.c "$REF"/*.h 2>/dev/null
+}
 {
   echo '#include <stdio.h>'
   for s in $missing; do
-    echo "int $s(void) { fprintf(stderr, \"cvbref: $s is outside the parity path\\n\"); return 1; }"
+    if is_data "$s"; then
+      echo "__attribute__((aligned(64))) char $s[4096];"
+    else
+      echo "int $s(void) { fprintf(stderr, \"cvbref: $s is outside the parity path\\n\"); return 1; }"
+    fi
   done
 } > "$OUT/ref_stubs.c"
 $CC $CFLAGS -c "$OUT/ref_stubs.c" -o "$OUT/ref_stubs.o"

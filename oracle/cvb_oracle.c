@@ -587,3 +587,185 @@ void orc_projection(const orc_level *L, const double *phi, double dt, double st,
     for (int j = 1; j < my - 1; j++)
       for (int i = 1; i < mx - 1; i++) proj_z(L, phi, dt, st, uc, i, j, 0);
 }
+
+/* Contra2Cart (rhs.c:25-143).  Each metric row and flux is the mean of the two
+ * faces of the cell; the 3x3 system is solved by Cramer's rule, terms in the
+ * reference's order. */
+void orc_contra2cart(const orc_level *L, const double *uc, double *ucat) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const size_t p = ID(L, i, j, k);
+        const double nv = L->nvert[p];
+        if (!(nv < 0.1 || nv > 7.0)) continue;
+        const size_t pw = ID(L, i - 1, j, k), ps = ID(L, i, j - 1, k), pb = ID(L, i, j, k - 1);
+        double m[3][3], q[3];
+        for (int c = 0; c < 3; c++) {
+          m[0][c] = 0.5 * (L->csi[3 * pw + c] + L->csi[3 * p + c]);
+          m[1][c] = 0.5 * (L->eta[3 * ps + c] + L->eta[3 * p + c]);
+          m[2][c] = 0.5 * (L->zet[3 * pb + c] + L->zet[3 * p + c]);
+        }
+        q[0] = 0.5 * (uc[3 * pw + 0] + uc[3 * p + 0]);
+        q[1] = 0.5 * (uc[3 * ps + 1] + uc[3 * p + 1]);
+        q[2] = 0.5 * (uc[3 * pb + 2] + uc[3 * p + 2]);
+        const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                           m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                           m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        const double d0 = q[0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                          q[1] * (m[0][1] * m[2][2] - m[0][2] * m[2][1]) +
+                          q[2] * (m[0][1] * m[1][2] - m[0][2] * m[1][1]);
+        const double d1 = -q[0] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                          q[1] * (m[0][0] * m[2][2] - m[0][2] * m[2][0]) -
+                          q[2] * (m[0][0] * m[1][2] - m[0][2] * m[1][0]);
+        const double d2 = q[0] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]) -
+                          q[1] * (m[0][0] * m[2][1] - m[0][1] * m[2][0]) +
+                          q[2] * (m[0][0] * m[1][1] - m[0][1] * m[1][0]);
+        ucat[3 * p + 0] = d0 / det;
+        ucat[3 * p + 1] = d1 / det;
+        ucat[3 * p + 2] = d2 / det;
+      }
+}
+
+/* Slip face (bcs.c:3827-3944): the tangential part of the velocity u next to
+ * the face, with n the unit vector of metric m. */
+static void slip(const double *m, const double *u, double *ub) {
+  const double A = sqrt(m[2] * m[2] + m[1] * m[1] + m[0] * m[0]);
+  const double nx = m[0] / A, ny = m[1] / A, nz = m[2] / A;
+  const double Un = u[0] * nx + u[1] * ny + u[2] * nz;
+  ub[0] = u[0] - Un * nx;
+  ub[1] = u[1] - Un * ny;
+  ub[2] = u[2] - Un * nz;
+}
+
+static inline void copy3(double *d, const double *s) { d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; }
+static inline void ghost3(double *g, const double *ub, const double *in) {
+  for (int c = 0; c < 3; c++) g[c] = 2 * ub[c] - in[c];
+}
+static inline void avg3(double *d, const double *a, const double *b) {
+  for (int c = 0; c < 3; c++) d[c] = 0.5 * (a[c] + b[c]);
+}
+
+int orc_ghost_node_velocity(const orc_level *L, double *ub, double *u) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const int *bc = L->bctype;
+  const int IM = mx - 1, JM = my - 1, KM = mz - 1;
+  if (bc[2] == 11) return -1;
+  for (int f = 2; f < 6; f++)
+    if (bc[f] == 13) return -1;
+  for (int d = 0; d < 3; d++)
+    if ((bc[2 * d] == 7) != (bc[2 * d + 1] == 7)) return -1;
+#define U3(i, j, k) (u + 3 * ID(L, (i), (j), (k)))
+#define B3(i, j, k) (ub + 3 * ID(L, (i), (j), (k)))
+  /* boundary velocity of the special wall types (bcs.c:3776-3975); the loops
+   * skip the ring of the face */
+  if (bc[5] == 2)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double *b = B3(i, j, mz - 1);
+        b[0] = 0.; b[1] = 1.; b[2] = 0.;
+      }
+  if (bc[3] == 12)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) {
+        double *b = B3(i, my - 1, k);
+        b[0] = 0.; b[1] = 0.; b[2] = 1.;
+      }
+  if (bc[0] == 3)
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++) slip(L->csi + 3 * ID(L, 0, j, k), U3(1, j, k), B3(0, j, k));
+  if (bc[1] == 3)
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        slip(L->csi + 3 * ID(L, mx - 2, j, k), U3(mx - 2, j, k), B3(mx - 1, j, k));
+  if (bc[2] == 3)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) slip(L->eta + 3 * ID(L, i, 0, k), U3(i, 1, k), B3(i, 0, k));
+  if (bc[3] == 3)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++)
+        slip(L->eta + 3 * ID(L, i, my - 2, k), U3(i, my - 2, k), B3(i, my - 1, k));
+  /* the k = 0 face takes the velocity of its own (ghost) cell (bcs.c:3918-3926) */
+  if (bc[4] == 3)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) slip(L->zet + 3 * ID(L, i, j, 0), U3(i, j, 0), B3(i, j, 0));
+  if (bc[5] == 3)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++)
+        slip(L->zet + 3 * ID(L, i, j, mz - 2), U3(i, j, mz - 2), B3(i, j, mz - 1));
+  /* non-periodic ghost faces, whole faces, x then y then z (bcs.c:4015-4076) */
+  if (bc[0] != 7)
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++) {
+        ghost3(U3(0, j, k), B3(0, j, k), U3(1, j, k));
+        ghost3(U3(mx - 1, j, k), B3(mx - 1, j, k), U3(mx - 2, j, k));
+      }
+  if (bc[2] != 7)
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < mx; i++) {
+        ghost3(U3(i, 0, k), B3(i, 0, k), U3(i, 1, k));
+        ghost3(U3(i, my - 1, k), B3(i, my - 1, k), U3(i, my - 2, k));
+      }
+  if (bc[4] != 7)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        ghost3(U3(i, j, 0), B3(i, j, 0), U3(i, j, 1));
+        ghost3(U3(i, j, mz - 1), B3(i, j, mz - 1), U3(i, j, mz - 2));
+      }
+  /* periodic ring copies, first round: off the box's edges; the upper z face
+   * takes only the x component (bcs.c:4083-4170) */
+  if (bc[0] == 7)
+    for (int k = 1; k < KM; k++)
+      for (int j = 1; j < JM; j++) {
+        copy3(U3(0, j, k), U3(mx - 2, j, k));
+        copy3(U3(mx - 1, j, k), U3(1, j, k));
+      }
+  if (bc[2] == 7)
+    for (int k = 1; k < KM; k++)
+      for (int i = 1; i < IM; i++) {
+        copy3(U3(i, 0, k), U3(i, my - 2, k));
+        copy3(U3(i, my - 1, k), U3(i, 1, k));
+      }
+  if (bc[4] == 7)
+    for (int j = 1; j < JM; j++)
+      for (int i = 1; i < IM; i++) {
+        copy3(U3(i, j, 0), U3(i, j, mz - 2));
+        U3(i, j, mz - 1)[0] = U3(i, j, 1)[0];
+      }
+  /* the 12 edges, in the reference's order (bcs.c:4176-4283) */
+  for (int j = 0; j < my; j++) avg3(U3(0, j, 0), U3(0, j, 1), U3(1, j, 0));
+  for (int j = 0; j < my; j++) avg3(U3(mx - 1, j, 0), U3(mx - 1, j, 1), U3(mx - 2, j, 0));
+  for (int i = 0; i < mx; i++) avg3(U3(i, 0, 0), U3(i, 0, 1), U3(i, 1, 0));
+  for (int i = 0; i < mx; i++) avg3(U3(i, my - 1, 0), U3(i, my - 1, 1), U3(i, my - 2, 0));
+  for (int j = 0; j < my; j++) avg3(U3(0, j, mz - 1), U3(0, j, mz - 2), U3(1, j, mz - 1));
+  for (int j = 0; j < my; j++) avg3(U3(mx - 1, j, mz - 1), U3(mx - 1, j, mz - 2), U3(mx - 2, j, mz - 1));
+  for (int i = 0; i < mx; i++) avg3(U3(i, 0, mz - 1), U3(i, 0, mz - 2), U3(i, 1, mz - 1));
+  for (int i = 0; i < mx; i++) avg3(U3(i, my - 1, mz - 1), U3(i, my - 1, mz - 2), U3(i, my - 2, mz - 1));
+  for (int k = 0; k < mz; k++) avg3(U3(0, 0, k), U3(0, 1, k), U3(1, 0, k));
+  for (int k = 0; k < mz; k++) avg3(U3(mx - 1, 0, k), U3(mx - 1, 1, k), U3(mx - 2, 0, k));
+  for (int k = 0; k < mz; k++) avg3(U3(0, my - 1, k), U3(0, my - 2, k), U3(1, my - 1, k));
+  for (int k = 0; k < mz; k++) avg3(U3(mx - 1, my - 1, k), U3(mx - 1, my - 2, k), U3(mx - 2, my - 1, k));
+  /* second round over whole faces, x, then y, then z; the upper z face again
+   * only the x component (bcs.c:4287-4405) */
+  if (bc[0] == 7)
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++) {
+        copy3(U3(0, j, k), U3(mx - 2, j, k));
+        copy3(U3(mx - 1, j, k), U3(1, j, k));
+      }
+  if (bc[2] == 7)
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < mx; i++) {
+        copy3(U3(i, 0, k), U3(i, my - 2, k));
+        copy3(U3(i, my - 1, k), U3(i, 1, k));
+      }
+  if (bc[4] == 7)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        copy3(U3(i, j, 0), U3(i, j, mz - 2));
+        U3(i, j, mz - 1)[0] = U3(i, j, 1)[0];
+      }
+#undef U3
+#undef B3
+  return 0;
+}

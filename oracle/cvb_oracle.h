@@ -56,6 +56,17 @@ void orc_update_pressure(const orc_level *L, double *p, double *phi);
 /* Projection (poisson.c:2281-2900), flux correction part; reads phi with its
  * periodic ring already filled (as after UpdatePressure). */
 void orc_projection(const orc_level *L, const double *phi, double dt, double st, double *ucont);
+/* Contra2Cart (rhs.c:25-143): Cartesian velocity at the centre of every
+ * interior cell with nvert < 0.1 or nvert > 7, from the averaged contravariant
+ * fluxes and centre metrics by Cramer's rule; other cells keep their ucat. */
+void orc_contra2cart(const orc_level *L, const double *ucont, double *ucat);
+/* GhostNodeVelocity (bcs.c:3645-4435) without the wall function: the boundary
+ * velocity of moving-lid (bctype[5] 2), O-grid (bctype[3] 12) and slip (3)
+ * faces into ubcs; every non-periodic ghost face from 2 ubcs - inner; the
+ * periodic ring copies; the averages on the box's 12 edges; the second round
+ * of ring copies.  Returns 0, or -1 (nothing written) for what it does not
+ * restate: bctype 11 or 13, or a periodic face whose opposite is not. */
+int orc_ghost_node_velocity(const orc_level *L, double *ubcs, double *ucat);
 
 #ifdef __cplusplus
 }

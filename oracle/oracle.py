@@ -75,6 +75,9 @@ def lib():
         _lib.orc_nullspace.argtypes = [L, ctypes.c_int, P, P]
         _lib.orc_update_pressure.argtypes = [L, P, P]
         _lib.orc_projection.argtypes = [L, P, ctypes.c_double, ctypes.c_double, P]
+        _lib.orc_contra2cart.argtypes = [L, P, P]
+        _lib.orc_ghost_node_velocity.argtypes = [L, P, P]
+        _lib.orc_ghost_node_velocity.restype = ctypes.c_int
     return _lib
 
 
@@ -185,6 +188,22 @@ def update_and_project(L: OLevel, p, phi, ucont, dt, st):
     return pp, ph, uc
 
 
+def contra2cart(L: OLevel, ucont, ucat):
+    """Contra2Cart (rhs.c:25-143): returns the new ucat ([mz][my][mx][3])."""
+    uc = np.ascontiguousarray(ucont, dtype=np.float64)
+    out = np.array(ucat, dtype=np.float64, copy=True, order="C")
+    lib().orc_contra2cart(L.ref(), _p(uc), _p(out))
+    return out
+
+
+def ghost_node_velocity(L: OLevel, ubcs, ucat):
+    """GhostNodeVelocity (bcs.c:3645-4435): returns (status, ubcs, ucat)."""
+    ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
+    u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+    rc = lib().orc_ghost_node_velocity(L.ref(), _p(ub), _p(u))
+    return rc, ub, u
+
+
 # ------------------------------------------------------------------ reference
 class Reference:
     """The reference's own routines, compiled against the API shim (oracle/_ref/)."""
@@ -277,6 +296,19 @@ class Reference:
         uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
         self.L.ref_update_and_project(ctypes.c_double(dt), ctypes.c_double(st), _p(pp), _p(ph), _p(uc))
         return pp, ph, uc
+
+
+    def contra2cart(self, ucont, ucat):
+        uc = np.ascontiguousarray(ucont, dtype=np.float64)
+        out = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        self.L.ref_contra2cart(_p(uc), _p(out))
+        return out
+
+    def ghost_node_velocity(self, ubcs, ucat):
+        ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        self.L.ref_ghost_node_velocity(_p(ub), _p(u))
+        return ub, u
 
 
 def solve_mg(levels, b, rtol=1e-8, max_it=500, restart=30, nu=2, threads=0):

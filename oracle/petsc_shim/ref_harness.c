@@ -32,6 +32,10 @@ int clark = 0;
  * the caller's side of the boundary, so the harness compares Ucont before them. */
 PetscErrorCode Contra2Cart(UserCtx *user) { (void)user; return 0; }
 PetscErrorCode GhostNodeVelocity(UserCtx *user) { (void)user; return 0; }
+/* The reference's own two (rhs.c:25, bcs.c:3645), renamed in their objects by
+ * oracle/build_ref.sh so that they do not collide with the inert pair above. */
+PetscErrorCode cvbref_Contra2Cart(UserCtx *user);
+PetscErrorCode cvbref_GhostNodeVelocity(UserCtx *user);
 
 PetscErrorCode FormMetrics(UserCtx *user);
 PetscErrorCode Update_Metrics_PBC(UserCtx *user);
@@ -66,6 +70,8 @@ static void make_vectors(UserCtx *u, int finest) {
   VecDuplicate(u->Csi, &u->KCsi); VecDuplicate(u->Csi, &u->KEta); VecDuplicate(u->Csi, &u->KZet);
   VecDuplicate(u->Csi, &u->Cent); VecDuplicate(u->Csi, &u->GridSpace);
   VecDuplicate(u->Csi, &u->Ucont);
+  VecDuplicate(u->Csi, &u->Ucat);
+  VecDuplicate(u->Csi, &u->Bcs.Ubcs);
   (void)finest;
   DMCreateGlobalVector(u->da, &u->Aj);
   VecDuplicate(u->Aj, &u->IAj); VecDuplicate(u->Aj, &u->JAj); VecDuplicate(u->Aj, &u->KAj);
@@ -78,6 +84,7 @@ static void make_vectors(UserCtx *u, int finest) {
   VecDuplicate(u->lCsi, &u->lGridSpace); VecDuplicate(u->lCsi, &u->lCent);
   VecDuplicate(u->lCsi, &u->Centx); VecDuplicate(u->lCsi, &u->Centy); VecDuplicate(u->lCsi, &u->Centz);
   VecDuplicate(u->lCsi, &u->lUcont);
+  VecDuplicate(u->lCsi, &u->lUcat);
   DMCreateLocalVector(u->da, &u->lAj);
   VecDuplicate(u->lAj, &u->lIAj); VecDuplicate(u->lAj, &u->lJAj); VecDuplicate(u->lAj, &u->lKAj);
   VecDuplicate(u->lAj, &u->lNvert); VecDuplicate(u->lAj, &u->lPhi); VecDuplicate(u->lAj, &u->lP);
@@ -393,5 +400,33 @@ int ref_update_and_project(double dt, double st, double *p, double *phi, double 
   copy_owned(u, u->P, 1, p, 0);
   copy_owned(u, u->Phi, 1, phi, 0);
   copy_owned(u, u->Ucont, 3, ucont, 0);
+  return 0;
+}
+
+/* Contra2Cart (rhs.c:25-143) on the finest level: the Cartesian velocity at
+ * the centres of the interior cells that are fluid (nvert < 0.1) or inside a
+ * body (nvert > 7), from Ucont and the centre metrics.  ucont is the global
+ * Ucont box; ucat (global Ucat box) is read for the cells the routine leaves
+ * alone and written. */
+int ref_contra2cart(const double *ucont, double *ucat) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  cvbref_Contra2Cart(u);
+  copy_owned(u, u->Ucat, 3, ucat, 0);
+  return 0;
+}
+
+/* GhostNodeVelocity (bcs.c:3645-4435) on the finest level: ubcs (Bcs.Ubcs) and
+ * ucat (Ucat), global boxes, both read and written. */
+int ref_ghost_node_velocity(double *ubcs, double *ucat) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 1);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  cvbref_GhostNodeVelocity(u);
+  copy_owned(u, u->Ucat, 3, ucat, 0);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 0);
   return 0;
 }

@@ -17,6 +17,24 @@ SCENARIOS = {
 }
 
 
+# Post-projection variants (Contra2Cart, GhostNodeVelocity): a scenario's grid
+# with other boundary types -- slip walls (3), a moving lid (bctype[5] 2), an
+# O-grid outer face (bctype[3] 12) -- and interior cells blanked (nvert 8 > 7,
+# which Contra2Cart treats as fluid).  name -> (scenario, bctype, blanked
+# (k, j, i) cells, seed of the ucat / ubcs inputs)
+POST_VARIANTS = {
+    "slip_lid_ogrid": ("box_sphere", [3, 3, 1, 12, 3, 2], [(2, 3, 4), (2, 3, 5), (9, 8, 2)], 1),
+    "walls_slip_y": ("box_sphere", [1, 1, 3, 3, 1, 1], [(5, 5, 5)], 2),
+    "periodic_slip_y": ("channel_periodic", [7, 7, 3, 3, 7, 7], [(3, 4, 6)], 3),
+}
+
+
+def post_inputs(shape, seed):
+    """ucat and ubcs ([mz][my][mx][3]) the post-projection steps start from."""
+    sh = tuple(shape) + (3,)
+    return seeded(sh, 500 + seed), seeded(sh, 600 + seed)
+
+
 def bctype_of(per):
     return [7 if per[0] else 1] * 2 + [7 if per[1] else 1] * 2 + [7 if per[2] else 1] * 2
 

@@ -1,8 +1,11 @@
 """Generate the golden fixtures from the reference's own routines.
 
-Runs CURVIB's poisson.c / metrics.c / implicitsolver.c, compiled unmodified
-against the single-process PETSc API shim (oracle/build_ref.sh), on the small
-scenarios of tests/cases.py and records SHA-256 digests of every output.  The
+Runs CURVIB's poisson.c / metrics.c / implicitsolver.c / rhs.c / bcs.c,
+compiled unmodified against the single-process PETSc API shim
+(oracle/build_ref.sh), on the small scenarios of tests/cases.py and records
+SHA-256 digests of every output.  The post-projection steps (Contra2Cart,
+GhostNodeVelocity) also run on the variants of cases.POST_VARIANTS, which put
+slip, moving-lid and O-grid faces and blanked cells on the same grids.  The
 inputs (node coordinates, nvert, fluxes) are stored beside the digests so the
 tests do not depend on the platform's sin/tanh.  Needs the reference checkout
 (default /root/reference, or CVB_REFERENCE_DIR); the fixtures it writes are
@@ -22,7 +25,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from cases import SCENARIOS, build, digest, seeded  # noqa: E402
+from cases import POST_VARIANTS, SCENARIOS, build, digest, post_inputs, seeded  # noqa: E402
 from curvib_old_gb300 import workload as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
@@ -67,15 +70,38 @@ def run(name):
     fine = R.shape(nl - 1)
     p, phi, u2 = R.update_and_project(seeded(fine, 400), seeded(fine, 401), uc, DT, ST)
     rec["update_project"] = {"p": digest(p), "phi": digest(phi), "ucont": digest(u2)}
+    rec["post"] = post(R, c["nvert"], c["ucont"], 0)
     np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
     return rec
 
 
+def post(R, nvert, ucont, seed):
+    """Contra2Cart, then GhostNodeVelocity on its result."""
+    ucat0, ubcs0 = post_inputs(nvert.shape, seed)
+    R.set_nvert(R.nlevels - 1, nvert)
+    c2c = R.contra2cart(ucont, ucat0)
+    ub, u = R.ghost_node_velocity(ubcs0, c2c)
+    return {"contra2cart": digest(c2c), "ghost_ubcs": digest(ub), "ghost_ucat": digest(u)}
+
+
+def run_variant(vname):
+    scen, bct, blank, seed = POST_VARIANTS[vname]
+    c = build(scen)
+    nv = c["nvert"].copy()
+    for (k, j, i) in blank:
+        nv[k, j, i] = 8.0
+    R = O.Reference(c["nodes"], c["nl"], bct, c["semi"])
+    return post(R, nv, c["ucont"], seed)
+
+
 def main():
-    out = {"dt": DT, "st": ST, "scenarios": {}}
+    out = {"dt": DT, "st": ST, "scenarios": {}, "post_variants": {}}
     for name in SCENARIOS:
         out["scenarios"][name] = run(name)
         print(name, "ok")
+    for vname in POST_VARIANTS:
+        out["post_variants"][vname] = run_variant(vname)
+        print(vname, "ok")
     (OUT / "reference_digests.json").write_text(json.dumps(out, indent=1, sort_keys=True))
 
 

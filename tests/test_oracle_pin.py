@@ -11,7 +11,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from cases import SCENARIOS, build, digest, seeded
+from cases import POST_VARIANTS, SCENARIOS, build, digest, post_inputs, seeded
 from curvib_old_gb300 import workload as W
 from oracle import oracle as O
 
@@ -83,6 +83,39 @@ def test_oracle_matches_reference(name):
     assert digest(p) == ref["update_project"]["p"]
     assert digest(phi) == ref["update_project"]["phi"]
     assert digest(u2) == ref["update_project"]["ucont"]
+    _check_post(Ls[-1], c["ucont"], 0, ref["post"])
+
+
+def _check_post(L, ucont, seed, want):
+    ucat0, ubcs0 = post_inputs(L.shape, seed)
+    c2c = O.contra2cart(L, ucont, ucat0)
+    assert digest(c2c) == want["contra2cart"]
+    rc, ub, u = O.ghost_node_velocity(L, ubcs0, c2c)
+    assert rc == 0
+    assert digest(ub) == want["ghost_ubcs"]
+    assert digest(u) == want["ghost_ucat"]
+
+
+@pytest.mark.parametrize("vname", sorted(POST_VARIANTS))
+def test_post_projection_variants_match_reference(vname):
+    """Contra2Cart and GhostNodeVelocity with slip, moving-lid and O-grid faces
+    and blanked cells (nvert > 7) against the reference's own bcs.c / rhs.c."""
+    scen, bct, blank, seed = POST_VARIANTS[vname]
+    c = _setup(scen)
+    nv = c["nvert"].copy()
+    for (k, j, i) in blank:
+        nv[k, j, i] = 8.0
+    L = O.OLevel(c["metrics"][-1], nv, bct, c["semi"])
+    _check_post(L, c["ucont"], seed, REF["post_variants"][vname])
+
+
+def test_ghost_node_velocity_refuses_unrestated_types():
+    c = _setup("box_sphere")
+    ucat0, ubcs0 = post_inputs(c["nvert"].shape, 0)
+    for bct in ([1, 1, 11, 1, 1, 1], [1, 1, 1, 1, 13, 1], [7, 1, 1, 1, 1, 1]):
+        L = O.OLevel(c["metrics"][-1], c["nvert"], bct, c["semi"])
+        rc, ub, u = O.ghost_node_velocity(L, ubcs0, ucat0)
+        assert rc == -1 and np.array_equal(u, ucat0) and np.array_equal(ub, ubcs0)
 
 
 @pytest.mark.parametrize("name", ["box_sphere", "channel_periodic"])
