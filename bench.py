@@ -309,9 +309,10 @@ def bench_step(args, ws, local):
     """The pressure-projection part of config 2's time step at 192^3 cells, as the
     reference's Flow_Solver calls it on host arrays: PoissonSolver_MG
     (VolumeFlux_rev, PoissonRHS, the solve to 1e-8), UpdatePressure and
-    Projection, each through the C ABI with pinned host buffers (copies inside
-    the timed region).  The momentum right-hand side that produces u* in the
-    reference's step is outside this path; u* here is the Taylor-Green field."""
+    Projection with the Contra2Cart and GhostNodeVelocity it ends with, each
+    through the C ABI with pinned host buffers (copies inside the timed
+    region).  The momentum right-hand side that produces u* in the reference's
+    step is outside this path; u* here is the Taylor-Green field."""
     import torch
 
     from curvib_old_gb300 import _lib
@@ -331,6 +332,8 @@ def bench_step(args, ws, local):
 
     uc0 = pinned(P.ucont)
     uc, phi, p = pinned(P.ucont), pinned(np.zeros(shape)), pinned(np.zeros(shape))
+    # Ucat and the no-slip walls' Bcs.Ubcs
+    ucat, ubcs = pinned(np.zeros(shape + (3,))), pinned(np.zeros(shape + (3,)))
     ptr = _lib.ptr
     dev = torch.device("cuda", local)
 
@@ -339,6 +342,7 @@ def bench_step(args, ws, local):
         stt = _lib.SolveStats()
         its = []
         wall = 0.0
+        part = np.zeros(3)
         for _ in range(steps):
             uc.numpy()[...] = uc0.numpy()  # this step's u* (outside the timed calls)
             torch.cuda.synchronize()
@@ -346,24 +350,40 @@ def bench_step(args, ws, local):
             rc = L.cvb_poisson_solver_mg(ctx._ctx, ptr(uc.numpy()), 0.0, 1, dt, st, ptr(phi.numpy()),
                                          ctypes.byref(o), ctypes.byref(stt))
             assert rc == 0, rc
+            t1 = time.perf_counter()
             assert L.cvb_update_pressure(ctx._ctx, ptr(p.numpy()), ptr(phi.numpy())) == 0
-            assert L.cvb_projection(ctx._ctx, ptr(phi.numpy()), dt, st, ptr(uc.numpy())) == 0
+            t2 = time.perf_counter()
+            assert L.cvb_projection_cart(ctx._ctx, ptr(phi.numpy()), dt, st, ptr(uc.numpy()), ptr(ubcs.numpy()),
+                                         ptr(ucat.numpy())) == 0
             torch.cuda.synchronize()
-            wall += time.perf_counter() - t0
+            t3 = time.perf_counter()
+            wall += t3 - t0
+            part += (t1 - t0, t2 - t1, t3 - t2)
             its.append(stt.iterations)
         wall = max_over_ranks(ws, wall, dev)
         return {"ms_per_step": wall * 1e3 / steps, "steps_per_s": ws * steps / wall,
-                "iterations": float(np.mean(its)), "rel_residual": stt.rel_residual}
+                "iterations": float(np.mean(its)), "rel_residual": stt.rel_residual,
+                "solver_mg_ms": part[0] * 1e3 / steps, "update_pressure_ms": part[1] * 1e3 / steps,
+                "projection_ms": part[2] * 1e3 / steps}
 
     out = {"workload": "192^3 cells, [0,1]^3 box, tanh 2.0 in y, distorted (config 0's law), sphere r=0.25 at the "
                        "centre; PoissonSolver_MG (VolumeFlux_rev + PoissonRHS + solve to 1e-8) + UpdatePressure + "
-                       "Projection on pinned host arrays, Taylor-Green u* (config 2 without its momentum step)",
+                       "Projection (flux correction, Contra2Cart, GhostNodeVelocity) on pinned host arrays, "
+                       "Taylor-Green u* (config 2 without its momentum step)",
            "unknowns": int(P.unknowns)}
     for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
         run(prec, 2)
         barrier(ws)
         out[name] = run(prec, args.step_steps)
     out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    # the post-projection kernels alone, device-timed: Contra2Cart is bound by
+    # the FP64 pipe (every operation rounded on its own, three divisions a cell)
+    kt = {}
+    for name, kid in (("contra2cart", _lib.KERNELS["contra2cart"]), ("ghost_nodes", _lib.KERNELS["ghost_nodes"])):
+        ms, nbytes = ctypes.c_double(), ctypes.c_double()
+        assert L.cvb_time_kernel(ctx._ctx, kid, ctx.nlevels - 1, 20, ctypes.byref(ms), ctypes.byref(nbytes)) == 0
+        kt[name + "_us"] = ms.value * 1e3
+    out["post_projection_kernels"] = kt
     ctx.close()
     return out
 

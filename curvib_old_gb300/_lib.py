@@ -67,6 +67,9 @@ EXPORTS = {
     "cvb_poisson_solver_mg": ([_P, _P, _D, _I, _D, _D, _P, _P, _P], _I),
     "cvb_update_pressure": ([_P, _P, _P], _I),
     "cvb_projection": ([_P, _P, _D, _D, _P], _I),
+    "cvb_contra2cart": ([_P, _P, _P], _I),
+    "cvb_ghost_node_velocity": ([_P, _P, _P], _I),
+    "cvb_projection_cart": ([_P, _P, _D, _D, _P, _P, _P], _I),
     "cvb_device_rhs": ([_P], _P),
     "cvb_device_phi": ([_P], _P),
     "cvb_solve_resident": ([_P, _P, _P], _I),
@@ -103,7 +106,7 @@ EXPORTS = {
     "cvb_get_phi": ([_P, _P], _I),
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3, "zebra_f32": 4,
-           "zebra_f64": 5, "vcycle_f32": 6, "vcycle_f64": 7}
+           "zebra_f64": 5, "vcycle_f32": 6, "vcycle_f64": 7, "contra2cart": 8, "ghost_nodes": 9}
 
 
 def lib_path() -> Path:

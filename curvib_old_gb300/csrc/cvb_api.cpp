@@ -136,6 +136,7 @@ static void free_all(cvb_ctx *ctx) {
   ctx->fm.clear();
   ctx->iaj.clear(); ctx->jaj.clear(); ctx->kaj.clear(); ctx->aj64.clear();
   ctx->area3 = nullptr;
+  ctx->cm[0] = ctx->cm[1] = ctx->cm[2] = nullptr;
   ctx->nvert_tmp = nullptr;
   ctx->Minv = nullptr;
   ctx->cidx = nullptr;
@@ -146,6 +147,7 @@ static void free_all(cvb_ctx *ctx) {
   ctx->dV = nullptr; ctx->dZ64 = nullptr; ctx->dZ32 = nullptr;
   ctx->partial = ctx->sums = ctx->hdev = nullptr;
   ctx->uc_dev = ctx->p_dev = nullptr;
+  ctx->ucat_dev = ctx->ubcs_dev = nullptr;
   ctx->ready = false;
 }
 
@@ -937,6 +939,7 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
   ctx->fm = G.fm;
   ctx->iaj = G.iaj; ctx->jaj = G.jaj; ctx->kaj = G.kaj; ctx->aj64 = G.aj64;
   ctx->area3 = G.area3;
+  for (int c = 0; c < 3; c++) ctx->cm[c] = G.cm[c];
   ctx->L.assign(nlevels, LevelDev());
   size_t nmax = 0;
   for (int l = 0; l < nlevels; l++) {
@@ -1167,6 +1170,13 @@ static int upload_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv) 
     TRY(galloc(ctx, *G, &G->area3, 3 * n));
     CK(cudaMemcpyAsync(G->area3, a3.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    // centre metrics for Contra2Cart and the slip faces of GhostNodeVelocity
+    const std::vector<double> *cv[3] = {&c1, &c2, &c3};
+    for (int c = 0; c < 3; c++) {
+      TRY(galloc(ctx, *G, &G->cm[c], 3 * n));
+      CK(cudaMemcpyAsync(G->cm[c], cv[c]->data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
   }
   ctx->geo = G;
   return CVB_OK;
@@ -1386,6 +1396,89 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
   return CVB_OK;
 }
 
+// The boundary types GhostNodeVelocity is restated for: all but the annulus
+// (bctype[2] 11, which reads cell centres), the rheology plate (13 on faces
+// 2-5, which reads a global of the caller's main program), and periodic
+// faces without a periodic opposite.
+static int ghost_types_ok(cvb_ctx *ctx, const int *bc) {
+  if (bc[2] == 11) return fail(ctx, CVB_BAD_INPUT, "GhostNodeVelocity: bctype 11 (annulus) is not covered");
+  for (int f = 2; f < 6; f++)
+    if (bc[f] == 13) return fail(ctx, CVB_BAD_INPUT, "GhostNodeVelocity: bctype 13 (rheology) is not covered");
+  for (int d = 0; d < 3; d++)
+    if ((bc[2 * d] == 7) != (bc[2 * d + 1] == 7))
+      return fail(ctx, CVB_BAD_INPUT, "GhostNodeVelocity: periodic face %d without a periodic opposite", 2 * d);
+  return CVB_OK;
+}
+
+static int post_buffers(cvb_ctx *ctx, size_t n) {
+  if (!ctx->ucat_dev) TRY(dalloc(ctx, &ctx->ucat_dev, 3 * n));
+  if (!ctx->ubcs_dev) TRY(dalloc(ctx, &ctx->ubcs_dev, 3 * n));
+  return CVB_OK;
+}
+
+int cvb_contra2cart(cvb_ctx *ctx, const double *ucont, double *ucat) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ucont || !ucat) return fail(ctx, CVB_BAD_INPUT, "ucont/ucat is NULL");
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  TRY(post_buffers(ctx, n));
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ubcs || !ucat) return fail(ctx, CVB_BAD_INPUT, "ubcs/ucat is NULL");
+  const int *bc = ctx->H[ctx->nlevels - 1].d.bctype;
+  TRY(ghost_types_ok(ctx, bc));
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  TRY(post_buffers(ctx, n));
+  CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,
+                        double *ucat) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!phi || !ucont || !ubcs || !ucat) return fail(ctx, CVB_BAD_INPUT, "phi/ucont/ubcs/ucat is NULL");
+  const int l = ctx->nlevels - 1;
+  const int *bc = ctx->H[l].d.bctype;
+  TRY(ghost_types_ok(ctx, bc));
+  LevelDev &F = ctx->L[l];
+  const size_t n = F.g.n();
+  TRY(post_buffers(ctx, n));
+  CK(cudaMemcpyAsync(ctx->w, phi, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  const double *fm[9];
+  for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
+  launch_projection(F.g, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], F.nvert, ctx->w, dt, st, ctx->uc_dev, ctx->stream);
+  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+  launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
 static int level_ok(cvb_ctx *ctx, int level) {
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
@@ -1580,10 +1673,25 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       case CVB_KERNEL_RESIDUAL_F32: launch_residual<float>(L, L.r32, L.e32, L.t32, ctx->stream); break;
       case CVB_KERNEL_RESIDUAL_F64: launch_residual<double>(L, L.r64, L.e64, L.t64, ctx->stream); break;
       case CVB_KERNEL_ZEBRA_F32: launch_zebra_half<float>(L, L.r32, L.e32, L.t32 + n, 1.3f, 1, false, ctx->stream); break;
+      case CVB_KERNEL_CONTRA2CART:
+        launch_contra2cart(L.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], L.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+        break;
+      case CVB_KERNEL_GHOST_NODES:
+        launch_ghost_node_velocity(L.g, ctx->H[level].d.bctype, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev,
+                                   ctx->ucat_dev, ctx->stream);
+        break;
       default: launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream); break;
     }
   };
   if (kernel == CVB_KERNEL_VCYCLE_F32 || kernel == CVB_KERNEL_VCYCLE_F64) return time_vcycle(ctx, kernel, level, reps, avg_ms, bytes);
+  if (kernel == CVB_KERNEL_CONTRA2CART || kernel == CVB_KERNEL_GHOST_NODES) {
+    if (level != ctx->nlevels - 1) return fail(ctx, CVB_BAD_INPUT, "kernel %d runs on the finest level only", kernel);
+    if (kernel == CVB_KERNEL_GHOST_NODES) TRY(ghost_types_ok(ctx, ctx->H[level].d.bctype));
+    TRY(post_buffers(ctx, n));
+    CK(cudaMemsetAsync(ctx->uc_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+    CK(cudaMemsetAsync(ctx->ucat_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+    CK(cudaMemsetAsync(ctx->ubcs_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+  }
   // algorithmic bytes per cell: every array the kernel needs, touched once.
   // The coefficients are the 9 face coefficients (FP32) or 19 weights (FP64),
   // 3 or 7 on a level without cross-derivative terms (an orthogonal grid).
@@ -1597,6 +1705,13 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
     // solve's r, factors, x in/out on the half of the cells of the color
     case CVB_KERNEL_ZEBRA_F32: per_cell = 4 + 0.5 * (4 + g32 + 4 + 4 + 4) + 0.5 * (4 + 12 + 4 + 4); break;
     case CVB_KERNEL_ZEBRA_F64: per_cell = 8 + 0.5 * (8 + w64 + 4 + 8) + 0.5 * (8 + 24 + 8 + 8); break;
+    case CVB_KERNEL_CONTRA2CART: per_cell = 72 + 24 + 8 + 24; break;  // centre metrics, ucont, nvert, ucat
+    case CVB_KERNEL_GHOST_NODES: {
+      // the ring cells only: ucat read and written, ubcs read
+      const double inner = (double)(L.g.mx - 2) * (L.g.my - 2) * (L.g.mz - 2);
+      per_cell = 72 * ((double)n - inner) / (double)n;
+      break;
+    }
     default: return fail(ctx, CVB_BAD_INPUT, "unknown kernel id %d", kernel);
   }
   CK(cudaMemsetAsync(L.r32, 0, sizeof(float) * n, ctx->stream));

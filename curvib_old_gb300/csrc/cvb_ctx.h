@@ -29,6 +29,7 @@ struct Geometry {
   std::vector<std::vector<double *>> fm;  // [level][9] raw face metrics (Cmpnts)
   std::vector<double *> iaj, jaj, kaj, aj64;
   double *area3 = nullptr;                // finest: |csi|, |eta|, |zet| per cell ([3][N])
+  double *cm[3] = {};                     // finest: centre metrics csi, eta, zet (Cmpnts, [N][3])
   ~Geometry() {
     if (allocs.empty()) return;
     cudaSetDevice(device);
@@ -67,6 +68,7 @@ struct cvb_ctx {
   std::vector<std::vector<double *>> fm;  // [level][9] Cmpnts arrays
   std::vector<double *> iaj, jaj, kaj, aj64;
   double *area3 = nullptr;       // finest: |csi|,|eta|,|zet| per cell ([3][N])
+  double *cm[3] = {};            // finest: centre metrics csi, eta, zet (Cmpnts)
   int *cidx = nullptr;           // coarsest level: fluid cells first, then the rest
   double *nvert_tmp = nullptr;
   // coarsest-level solver
@@ -86,6 +88,7 @@ struct cvb_ctx {
   float **dZ32 = nullptr;
   double *partial = nullptr, *sums = nullptr, *hdev = nullptr;
   double *uc_dev = nullptr, *p_dev = nullptr;
+  double *ucat_dev = nullptr, *ubcs_dev = nullptr;  // Contra2Cart / GhostNodeVelocity (allocated on first use)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;
   std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)

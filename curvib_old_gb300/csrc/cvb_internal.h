@@ -237,5 +237,10 @@ void launch_update_pressure(const Geom &g, double *p, double *phi, cudaStream_t 
 void launch_projection(const Geom &g, const double *const *fm /*I,J,K csi/eta/zet*/, const double *iaj,
                        const double *jaj, const double *kaj, const double *nvert, const double *phi,
                        double dt, double st, double *ucont, cudaStream_t s);
+void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
+                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s);
+// bc: the level's bctype[6]; the host has refused the types it does not cover
+void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
+                                const double *zet, double *ubcs, double *ucat, cudaStream_t s);
 
 }  // namespace cvb

@@ -1,0 +1,235 @@
+// The steps that follow the flux correction in the reference's Projection
+// (poisson.c:2897-2904): Contra2Cart (rhs.c:25-143), the Cartesian velocity at
+// the cell centres, and GhostNodeVelocity (bcs.c:3645-4435), its values on the
+// boundary ring.  FP64 with every operation rounded on its own, in the
+// reference's order (no fused multiply-add), so results equal the reference's
+// bit for bit.  Arrays are the finest level's [mz][my][mx] box, Cmpnts
+// interleaved.
+#include "cvb_internal.h"
+
+namespace cvb {
+
+static inline unsigned nblk(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mean2(double a, double b) { return dm(0.5, da(a, b)); }
+// a*(b*c - d*e), the cofactor product of Cramer's rule
+__device__ __forceinline__ double cof(double a, double b, double c, double d, double e) {
+  return dm(a, ds(dm(b, c), dm(d, e)));
+}
+
+// Contra2Cart: one thread per interior cell; cells with 0.1 <= nvert <= 7 keep
+// their ucat.  The metric rows and fluxes are the means of the cell's two
+// faces in each direction.
+__global__ void __launch_bounds__(256) k_contra2cart(Geom g, const double *__restrict__ csi,
+                                                     const double *__restrict__ eta, const double *__restrict__ zet,
+                                                     const double *__restrict__ nvert, const double *__restrict__ uc,
+                                                     double *__restrict__ ucat) {
+  const int ni = g.mx - 2, nj = g.my - 2;
+  const size_t cells = (size_t)ni * nj * (g.mz - 2);
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cells) return;
+  const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = 1 + (int)(t / ((size_t)ni * nj));
+  const size_t p = ((size_t)k * g.my + j) * g.mx + i;
+  const double nv = nvert[p];
+  if (!(nv < 0.1 || nv > 7.0)) return;
+  const size_t pw = p - 1, ps = p - g.mx, pb = p - (size_t)g.mx * g.my;
+  double m[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    m[0][c] = mean2(csi[3 * pw + c], csi[3 * p + c]);
+    m[1][c] = mean2(eta[3 * ps + c], eta[3 * p + c]);
+    m[2][c] = mean2(zet[3 * pb + c], zet[3 * p + c]);
+  }
+  const double q0 = mean2(uc[3 * pw + 0], uc[3 * p + 0]);
+  const double q1 = mean2(uc[3 * ps + 1], uc[3 * p + 1]);
+  const double q2 = mean2(uc[3 * pb + 2], uc[3 * p + 2]);
+  const double det = da(ds(cof(m[0][0], m[1][1], m[2][2], m[1][2], m[2][1]),
+                           cof(m[0][1], m[1][0], m[2][2], m[1][2], m[2][0])),
+                        cof(m[0][2], m[1][0], m[2][1], m[1][1], m[2][0]));
+  const double d0 = da(ds(cof(q0, m[1][1], m[2][2], m[1][2], m[2][1]), cof(q1, m[0][1], m[2][2], m[0][2], m[2][1])),
+                       cof(q2, m[0][1], m[1][2], m[0][2], m[1][1]));
+  const double d1 = ds(da(cof(-q0, m[1][0], m[2][2], m[1][2], m[2][0]), cof(q1, m[0][0], m[2][2], m[0][2], m[2][0])),
+                       cof(q2, m[0][0], m[1][2], m[0][2], m[1][0]));
+  const double d2 = da(ds(cof(q0, m[1][0], m[2][1], m[1][1], m[2][0]), cof(q1, m[0][0], m[2][1], m[0][1], m[2][0])),
+                       cof(q2, m[0][0], m[1][1], m[0][1], m[1][0]));
+  ucat[3 * p + 0] = __ddiv_rn(d0, det);
+  ucat[3 * p + 1] = __ddiv_rn(d1, det);
+  ucat[3 * p + 2] = __ddiv_rn(d2, det);
+}
+
+void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
+                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s) {
+  const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  if (!cells) return;
+  k_contra2cart<<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, nvert, ucont, ucat);
+  count_launch();
+}
+
+// ---------------------------------------------------------------- ghost nodes
+// A face of the box: f = 2 * axis + side (0: x low, 1: x high, 2: y low, ...).
+// Cell (a, b) of face f: for x faces a = j, b = k; for y faces a = i, b = k;
+// for z faces a = i, b = j.
+struct Face {
+  int axis, side;
+  __device__ size_t at(const Geom &g, int a, int b, int layer) const {
+    // layer: 0 = the ring cell, 1 = its inner neighbour, ... counted from the face
+    const int n = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
+    const int c = side ? n - 1 - layer : layer;
+    const int i = axis == 0 ? c : a, j = axis == 1 ? c : (axis == 0 ? a : b), k = axis == 2 ? c : b;
+    return ((size_t)k * g.my + j) * g.mx + i;
+  }
+  __device__ int na(const Geom &g) const { return axis == 0 ? g.my : g.mx; }
+  __device__ int nb(const Geom &g) const { return axis == 2 ? g.my : g.mz; }
+};
+
+struct GhostArgs {
+  Geom g;
+  int bc[6];
+  const double *csi, *eta, *zet;  // centre metrics
+  double *ub, *u;                 // ubcs, ucat
+};
+
+// The boundary velocity of the special wall types (bcs.c:3776-3975), one face
+// per blockIdx.z, the face's interior cells only.  Moving lid (bctype[5] 2)
+// and O-grid (bctype[3] 12) faces get a fixed velocity; a slip face (3) the
+// tangential part of the velocity next to it, n from the metric of the
+// face's outer cell on the low side and of its inner cell on the high side.
+// The z-low slip face reads the velocity of its own ring cell, as the
+// reference does.
+__global__ void k_ghost_special(GhostArgs A) {
+  const Geom &g = A.g;
+  const int f = blockIdx.z;
+  const Face F{f >> 1, f & 1};
+  const int a = 1 + blockIdx.x * blockDim.x + threadIdx.x, b = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (a > F.na(g) - 2 || b > F.nb(g) - 2) return;
+  const size_t p0 = F.at(g, a, b, 0);
+  double *ub = A.ub + 3 * p0;
+  if (f == 5 && A.bc[5] == 2) { ub[0] = 0.; ub[1] = 1.; ub[2] = 0.; return; }
+  if (f == 3 && A.bc[3] == 12) { ub[0] = 0.; ub[1] = 0.; ub[2] = 1.; return; }
+  if (A.bc[f] != 3) return;
+  const double *met = F.axis == 0 ? A.csi : F.axis == 1 ? A.eta : A.zet;
+  const size_t pm = F.side ? F.at(g, a, b, 1) : p0;
+  const size_t pu = F.side ? F.at(g, a, b, 1) : (f == 4 ? p0 : F.at(g, a, b, 1));
+  const double *m = met + 3 * pm, *u = A.u + 3 * pu;
+  const double A2 = __dsqrt_rn(da(da(dm(m[2], m[2]), dm(m[1], m[1])), dm(m[0], m[0])));
+  const double nx = __ddiv_rn(m[0], A2), ny = __ddiv_rn(m[1], A2), nz = __ddiv_rn(m[2], A2);
+  const double un = da(da(dm(u[0], nx), dm(u[1], ny)), dm(u[2], nz));
+  ub[0] = ds(u[0], dm(un, nx));
+  ub[1] = ds(u[1], dm(un, ny));
+  ub[2] = ds(u[2], dm(un, nz));
+}
+
+// Non-periodic ghost faces of one axis (bcs.c:4015-4076): the whole face,
+// u = 2 ubcs - u(inner neighbour).
+__global__ void k_ghost_faces(GhostArgs A, int axis) {
+  const Geom &g = A.g;
+  const Face F{axis, (int)blockIdx.z};
+  const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= F.na(g) || b >= F.nb(g)) return;
+  const size_t p0 = F.at(g, a, b, 0), p1 = F.at(g, a, b, 1);
+#pragma unroll
+  for (int c = 0; c < 3; c++) A.u[3 * p0 + c] = ds(dm(2.0, A.ub[3 * p0 + c]), A.u[3 * p1 + c]);
+}
+
+// Periodic ring copies of one axis: the ring cell takes the value of the cell
+// one period away (cell m-2 for ring cell 0, cell 1 for ring cell m-1).  The
+// upper z face copies the x component only, in both rounds, as the reference
+// does.  First round (bcs.c:4083-4170): off the face's edges; second round
+// (bcs.c:4287-4405): the whole face.
+__global__ void k_ghost_ring(GhostArgs A, int axis, int whole) {
+  const Geom &g = A.g;
+  const Face F{axis, (int)blockIdx.z};
+  const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= F.na(g) || b >= F.nb(g)) return;
+  if (!whole && (a < 1 || a > F.na(g) - 2 || b < 1 || b > F.nb(g) - 2)) return;
+  const int n = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
+  const size_t p0 = F.at(g, a, b, 0), ps = F.at(g, a, b, n - 2);  // ring cell 0 <- m-2, m-1 <- 1
+  if (axis == 2 && F.side) {
+    A.u[3 * p0] = A.u[3 * ps];
+    return;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) A.u[3 * p0 + c] = A.u[3 * ps + c];
+}
+
+// The 12 edges of the box (bcs.c:4176-4283), each the mean of its two
+// neighbours across the edge, in the reference's order: one block, one edge
+// after the other (edges share corner cells).
+__global__ void k_ghost_edges(GhostArgs A) {
+  const Geom &g = A.g;
+  const int mx = g.mx, my = g.my, mz = g.mz;
+  auto P = [&](int i, int j, int k) { return ((size_t)k * my + j) * mx + i; };
+  auto avg = [&](size_t d, size_t a, size_t b) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) A.u[3 * d + c] = mean2(A.u[3 * a + c], A.u[3 * b + c]);
+  };
+  for (int e = 0; e < 12; e++) {
+    const int len = e < 8 ? ((e & 3) < 2 ? my : mx) : mz;
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      switch (e) {
+        case 0: avg(P(0, t, 0), P(0, t, 1), P(1, t, 0)); break;
+        case 1: avg(P(mx - 1, t, 0), P(mx - 1, t, 1), P(mx - 2, t, 0)); break;
+        case 2: avg(P(t, 0, 0), P(t, 0, 1), P(t, 1, 0)); break;
+        case 3: avg(P(t, my - 1, 0), P(t, my - 1, 1), P(t, my - 2, 0)); break;
+        case 4: avg(P(0, t, mz - 1), P(0, t, mz - 2), P(1, t, mz - 1)); break;
+        case 5: avg(P(mx - 1, t, mz - 1), P(mx - 1, t, mz - 2), P(mx - 2, t, mz - 1)); break;
+        case 6: avg(P(t, 0, mz - 1), P(t, 0, mz - 2), P(t, 1, mz - 1)); break;
+        case 7: avg(P(t, my - 1, mz - 1), P(t, my - 1, mz - 2), P(t, my - 2, mz - 1)); break;
+        case 8: avg(P(0, 0, t), P(0, 1, t), P(1, 0, t)); break;
+        case 9: avg(P(mx - 1, 0, t), P(mx - 1, 1, t), P(mx - 2, 0, t)); break;
+        case 10: avg(P(0, my - 1, t), P(0, my - 2, t), P(1, my - 1, t)); break;
+        default: avg(P(mx - 1, my - 1, t), P(mx - 1, my - 2, t), P(mx - 2, my - 1, t)); break;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+static void face_grid(const Geom &g, int axis, int faces, dim3 &grd, dim3 &blk) {
+  const int na = axis == 0 ? g.my : g.mx, nb = axis == 2 ? g.my : g.mz;
+  blk = dim3(32, 8, 1);
+  grd = dim3(nblk(na, 32), nblk(nb, 8), faces);
+}
+
+void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
+                                const double *zet, double *ubcs, double *ucat, cudaStream_t s) {
+  GhostArgs A;
+  A.g = g;
+  for (int f = 0; f < 6; f++) A.bc[f] = bc[f];
+  A.csi = csi; A.eta = eta; A.zet = zet; A.ub = ubcs; A.u = ucat;
+  dim3 grd, blk;
+  bool special = bc[5] == 2 || bc[3] == 12;
+  for (int f = 0; f < 6; f++) special = special || bc[f] == 3;
+  if (special) {
+    const int nmax = g.mx > g.my ? (g.mx > g.mz ? g.mx : g.mz) : (g.my > g.mz ? g.my : g.mz);
+    k_ghost_special<<<dim3(nblk(nmax, 32), nblk(nmax, 8), 6), dim3(32, 8, 1), 0, s>>>(A);
+    count_launch();
+  }
+  for (int axis = 0; axis < 3; axis++) {
+    if (bc[2 * axis] == 7) continue;
+    face_grid(g, axis, 2, grd, blk);
+    k_ghost_faces<<<grd, blk, 0, s>>>(A, axis);
+    count_launch();
+  }
+  // first round: the three axes touch disjoint cells and read only interior
+  // cells, so their order does not matter
+  for (int axis = 0; axis < 3; axis++) {
+    if (bc[2 * axis] != 7) continue;
+    face_grid(g, axis, 2, grd, blk);
+    k_ghost_ring<<<grd, blk, 0, s>>>(A, axis, 0);
+    count_launch();
+  }
+  k_ghost_edges<<<1, 256, 0, s>>>(A);
+  count_launch();
+  for (int axis = 0; axis < 3; axis++) {
+    if (bc[2 * axis] != 7) continue;
+    face_grid(g, axis, 2, grd, blk);
+    k_ghost_ring<<<grd, blk, 0, s>>>(A, axis, 1);
+    count_launch();
+  }
+}
+
+}  // namespace cvb

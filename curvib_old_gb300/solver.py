@@ -177,6 +177,28 @@ class PoissonContext:
         self._check(self._L.cvb_projection(self._ctx, ptr(_c64(phi)), dt, st, ptr(uc)))
         return uc
 
+    def contra2cart(self, ucont, ucat):
+        """Contra2Cart (rhs.c:25): returns the new ucat ([mz][my][mx][3])."""
+        out = np.array(ucat, dtype=np.float64, order="C", copy=True)
+        self._check(self._L.cvb_contra2cart(self._ctx, ptr(_c64(ucont)), ptr(out)))
+        return out
+
+    def ghost_node_velocity(self, ubcs, ucat):
+        """GhostNodeVelocity (bcs.c:3645): returns (ubcs, ucat)."""
+        ub = np.array(ubcs, dtype=np.float64, order="C", copy=True)
+        u = np.array(ucat, dtype=np.float64, order="C", copy=True)
+        self._check(self._L.cvb_ghost_node_velocity(self._ctx, ptr(ub), ptr(u)))
+        return ub, u
+
+    def projection_cart(self, phi, dt, st, ucont, ubcs, ucat):
+        """Projection, Contra2Cart and GhostNodeVelocity in one call: returns
+        (ucont, ubcs, ucat)."""
+        uc = np.array(ucont, dtype=np.float64, order="C", copy=True)
+        ub = np.array(ubcs, dtype=np.float64, order="C", copy=True)
+        u = np.array(ucat, dtype=np.float64, order="C", copy=True)
+        self._check(self._L.cvb_projection_cart(self._ctx, ptr(_c64(phi)), dt, st, ptr(uc), ptr(ub), ptr(u)))
+        return uc, ub, u
+
     # ------------------------------------------------------- resident solves
     def device_rhs(self):
         return self._L.cvb_device_rhs(self._ctx)

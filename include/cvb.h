@@ -10,9 +10,11 @@
  *   MyNvertRestriction(poisson.c:1662), FullyBlocked (poisson.c:1578)
  *                                       -> cvb_setup_hierarchy / cvb_set_nvert
  *   UpdatePressure    (poisson.c:2908)  -> cvb_update_pressure
- *   Projection        (poisson.c:2281)  -> cvb_projection (flux correction; the
- *                                          trailing Contra2Cart/GhostNodeVelocity
- *                                          stay with the caller)
+ *   Projection        (poisson.c:2281)  -> cvb_projection (flux correction), or
+ *                                          cvb_projection_cart (with the trailing
+ *                                          Contra2Cart and GhostNodeVelocity)
+ *   Contra2Cart       (rhs.c:25)        -> cvb_contra2cart
+ *   GhostNodeVelocity (bcs.c:3645)      -> cvb_ghost_node_velocity
  *
  * Conventions
  *  - Every entry point returns a cvb_status (0 = success, as PetscErrorCode).
@@ -167,6 +169,23 @@ int cvb_poisson_solver_mg(cvb_ctx *ctx, double *ucont, double flux_intp_sum, int
 int cvb_update_pressure(cvb_ctx *ctx, double *p, double *phi);
 /* Projection's flux correction (poisson.c:2281-2900) with phi as UpdatePressure left it. */
 int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont);
+/* Contra2Cart (rhs.c:25-143), which Projection calls next (poisson.c:2902): the
+ * Cartesian velocity at the centre of every interior cell with nvert < 0.1 or
+ * nvert > 7, from ucont and the finest level's centre metrics.  ucont and ucat
+ * are [mz][my][mx][3]; ucat is read for the cells the routine leaves alone. */
+int cvb_contra2cart(cvb_ctx *ctx, const double *ucont, double *ucat);
+/* GhostNodeVelocity (bcs.c:3645-4435), Projection's last call (poisson.c:2904),
+ * without the wall function: boundary velocities of slip (3), moving-lid
+ * (bctype[5] 2) and O-grid (bctype[3] 12) faces into ubcs (Bcs.Ubcs), the ring
+ * of ucat from ubcs and the periodic images, the box's edges.  ubcs and ucat
+ * ([mz][my][mx][3]) are read and written.  CVB_BAD_INPUT, with nothing
+ * written, for bctype 11 or 13, or a periodic face whose opposite is not. */
+int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat);
+/* Projection as Flow_Solver calls it (solvers.c:1068, poisson.c:2281-2904):
+ * the flux correction, Contra2Cart and GhostNodeVelocity on the device in one
+ * call, each array copied in and out once. */
+int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,
+                        double *ucat);
 
 /* --- device-resident form (inputs already in HBM) ---------------------- */
 /* Device pointers of the context's finest-level rhs and solution ([mz][my][mx] FP64). */
@@ -288,7 +307,9 @@ enum {
   CVB_KERNEL_ZEBRA_F32 = 4,      /* one zebra half-sweep (residual on one color + its line solves), FP32 */
   CVB_KERNEL_ZEBRA_F64 = 5,      /* the same in FP64 */
   CVB_KERNEL_VCYCLE_F32 = 6,     /* one FP32 V-cycle (default options) from the level down, replayed from a CUDA graph */
-  CVB_KERNEL_VCYCLE_F64 = 7      /* the same in FP64 */
+  CVB_KERNEL_VCYCLE_F64 = 7,     /* the same in FP64 */
+  CVB_KERNEL_CONTRA2CART = 8,    /* Contra2Cart on the finest level (the level argument must name it) */
+  CVB_KERNEL_GHOST_NODES = 9     /* GhostNodeVelocity on the finest level */
 };
 /* JSON record of the set-up autotuner: per level, the measured time of the
  * fused and the split y-line sweep in each precision and the variant kept. */

@@ -62,5 +62,13 @@ def digest(a) -> str:
     return hashlib.sha256(a.tobytes()).hexdigest()[:32]
 
 
+def digest_nan(a) -> str:
+    """digest() with every NaN replaced by one quiet NaN: the sign and payload
+    of a NaN from 0/0 differ between x86 and Arm."""
+    a = np.array(a, dtype=np.float64, copy=True)
+    a[np.isnan(a)] = np.nan
+    return digest(a)
+
+
 def seeded(shape, seed):
     return np.random.default_rng(seed).standard_normal(shape)

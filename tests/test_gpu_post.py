@@ -1,0 +1,103 @@
+"""The steps after Projection's flux correction on the GPU (libcvb.so through
+its C ABI) against the CPU oracle: Contra2Cart (rhs.c:25) and
+GhostNodeVelocity (bcs.c:3645), bit for bit, on the parity scenarios and on
+the slip / moving-lid / O-grid variants with blanked cells (nvert > 7); the
+one-call projection against the three steps; boundary types that are not
+covered refused with nothing written.  A slip face on the low y side gives NaN,
+as in the reference (its normal comes from the ring cell's eta, which
+FormMetrics leaves zero), so arrays compare with NaN equal to NaN.
+"""
+import types
+
+import numpy as np
+import pytest
+
+from cases import POST_VARIANTS, SCENARIOS, build, post_inputs, seeded
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DT, ST = 1e-3, 1.0
+# key -> (scenario, bctype or None for the scenario's own, blanked cells, seed)
+CASES = {name: (name, None, [], 0) for name in SCENARIOS}
+CASES.update(POST_VARIANTS)
+
+
+def _problem(key):
+    scen, bct, blank, seed = CASES[key]
+    c = build(scen)
+    nv = c["nvert"].copy()
+    for (k, j, i) in blank:
+        nv[k, j, i] = 8.0
+    P = types.SimpleNamespace(metrics=c["metrics"], nvert=nv, ucont=c["ucont"], bctype=bct or c["bctype"],
+                              semi=c["semi"], per=c["per"], nl=c["nl"])
+    return P, seed
+
+
+@pytest.fixture(scope="module")
+def ctxs():
+    from curvib_old_gb300.solver import PoissonContext
+    out = {}
+    for key in CASES:
+        P, seed = _problem(key)
+        out[key] = (PoissonContext().setup(P), P, O.OLevel(P.metrics[-1], P.nvert, P.bctype, P.semi), seed)
+    yield out
+    for c, _, _, _ in out.values():
+        c.close()
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_contra2cart_and_ghost_nodes_bit_exact(ctxs, key):
+    ctx, P, L, seed = ctxs[key]
+    ucat0, ubcs0 = post_inputs(P.nvert.shape, seed)
+    c_g = ctx.contra2cart(P.ucont, ucat0)
+    c_o = O.contra2cart(L, P.ucont, ucat0)
+    assert np.array_equal(c_g, c_o)
+    # the cells Contra2Cart leaves alone keep their input
+    untouched = (P.nvert >= 0.1) & (P.nvert <= 7.0)
+    untouched[[0, -1], :, :] = untouched[:, [0, -1], :] = untouched[:, :, [0, -1]] = True
+    assert untouched.any() and not untouched.all()
+    assert np.array_equal(c_g[untouched], ucat0[untouched])
+    ub_g, u_g = ctx.ghost_node_velocity(ubcs0, c_o)
+    rc, ub_o, u_o = O.ghost_node_velocity(L, ubcs0, c_o)
+    assert rc == 0
+    assert np.array_equal(ub_g, ub_o, equal_nan=True)
+    assert np.array_equal(u_g, u_o, equal_nan=True)
+
+
+@pytest.mark.parametrize("key", ["box_sphere", "channel_periodic", "triply_periodic", "slip_lid_ogrid",
+                                 "periodic_slip_y"])
+def test_projection_cart_equals_the_three_steps(ctxs, key):
+    ctx, P, L, seed = ctxs[key]
+    fine = P.nvert.shape
+    _, phi_o, uc_o = O.update_and_project(L, seeded(fine, 400), seeded(fine, 401), P.ucont, DT, ST)
+    ucat0, ubcs0 = post_inputs(fine, seed)
+    uc_g, ub_g, u_g = ctx.projection_cart(phi_o, DT, ST, P.ucont, ubcs0, ucat0)
+    assert np.array_equal(uc_g, uc_o)
+    rc, ub_o, u_o = O.ghost_node_velocity(L, ubcs0, O.contra2cart(L, uc_o, ucat0))
+    assert rc == 0
+    assert np.array_equal(ub_g, ub_o, equal_nan=True)
+    assert np.array_equal(u_g, u_o, equal_nan=True)
+
+
+@pytest.mark.parametrize("bct", [[1, 1, 11, 1, 1, 1], [1, 1, 1, 1, 13, 1], [1, 1, 1, 13, 1, 1]])
+def test_uncovered_boundary_types_refused(bct):
+    from curvib_old_gb300._lib import CvbError
+    from curvib_old_gb300.solver import PoissonContext
+    c = build("box_sphere")
+    P = types.SimpleNamespace(metrics=c["metrics"], nvert=c["nvert"], ucont=c["ucont"], bctype=bct,
+                              semi=c["semi"], per=c["per"], nl=c["nl"])
+    ctx = PoissonContext().setup(P)
+    try:
+        ucat0, ubcs0 = post_inputs(c["nvert"].shape, 0)
+        with pytest.raises(CvbError) as e:
+            ctx.ghost_node_velocity(ubcs0, ucat0)
+        assert e.value.status == 4  # CVB_BAD_INPUT
+        with pytest.raises(CvbError):
+            ctx.projection_cart(np.zeros(c["nvert"].shape), DT, ST, c["ucont"], ubcs0, ucat0)
+        # the context stays usable: Contra2Cart does not depend on the types
+        assert np.array_equal(ctx.contra2cart(c["ucont"], ucat0),
+                              O.contra2cart(O.OLevel(c["metrics"][-1], c["nvert"], bct, c["semi"]),
+                                            c["ucont"], ucat0))
+    finally:
+        ctx.close()
