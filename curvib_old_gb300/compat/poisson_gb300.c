@@ -17,6 +17,7 @@
 #include "poisson_gb300.h"
 
 extern PetscInt block_number, immersed; /* main.c, as poisson.c:6-7 declares them */
+extern PetscInt wallfunction;           /* main.c, as bcs.c:3689 declares it */
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 
@@ -165,14 +166,44 @@ PetscErrorCode UpdatePressure_GB300(UserCtx *u) {
   return report(rc, "UpdatePressure_GB300");
 }
 
-/* The flux correction of Projection, then what the reference does after it on
- * the caller's side of the boundary (poisson.c:2897-2904): lUcont refreshed,
- * Contra2Cart, GhostNodeVelocity. */
+/* GhostNodeVelocity's boundary types libcvb covers (all but the wall function,
+ * the annulus bctype[2] 11 and the rheology plate 13). */
+static int ghost_on_device(const UserCtx *u) {
+  if (wallfunction) return 0;
+  if (u->bctype[2] == 11) return 0;
+  for (int f = 2; f < 6; f++)
+    if (u->bctype[f] == 13) return 0;
+  return 1;
+}
+
+/* Projection (poisson.c:2281-2904): the flux correction, lUcont refreshed,
+ * Contra2Cart and GhostNodeVelocity.  With covered boundary types all of it
+ * runs on the device in one call (Ucat, Bcs.Ubcs and Ucont copied once);
+ * otherwise the flux correction does, and the reference's own Contra2Cart and
+ * GhostNodeVelocity follow on the host.  lUcont and lUcat end refreshed, as
+ * the reference leaves them. */
 PetscErrorCode Projection_GB300(UserCtx *u) {
   PetscScalar *phi, *uc;
+  int rc;
   VecGetArray(u->Phi, &phi);
   VecGetArray(u->Ucont, &uc);
-  int rc = cvb_projection(g_cvb, phi, u->dt, u->st, uc);
+  if (ghost_on_device(u)) {
+    PetscScalar *ub, *ucat;
+    VecGetArray(u->Bcs.Ubcs, &ub);
+    VecGetArray(u->Ucat, &ucat);
+    rc = cvb_projection_cart(g_cvb, phi, u->dt, u->st, uc, ub, ucat);
+    VecRestoreArray(u->Ucat, &ucat);
+    VecRestoreArray(u->Bcs.Ubcs, &ub);
+    VecRestoreArray(u->Ucont, &uc);
+    VecRestoreArray(u->Phi, &phi);
+    if (rc) return report(rc, "Projection_GB300");
+    DMGlobalToLocalBegin(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+    DMGlobalToLocalEnd(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+    DMGlobalToLocalBegin(u->fda, u->Ucat, INSERT_VALUES, u->lUcat);
+    DMGlobalToLocalEnd(u->fda, u->Ucat, INSERT_VALUES, u->lUcat);
+    return 0;
+  }
+  rc = cvb_projection(g_cvb, phi, u->dt, u->st, uc);
   VecRestoreArray(u->Ucont, &uc);
   VecRestoreArray(u->Phi, &phi);
   if (rc) return report(rc, "Projection_GB300");

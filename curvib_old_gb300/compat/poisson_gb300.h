@@ -5,7 +5,9 @@
  * against CURVIB's own variables.h and PETSc.  It replaces, one for one:
  *   PoissonSolver_MG(usermg)  (poisson.c:1775; called at solvers.c:1052)
  *   UpdatePressure(&user[bi]) (poisson.c:2908; called at solvers.c:1066)
- *   Projection(&user[bi])     (poisson.c:2281; called at solvers.c:1068)
+ *   Projection(&user[bi])     (poisson.c:2281; called at solvers.c:1068),
+ *                             with its Contra2Cart (rhs.c:25) and
+ *                             GhostNodeVelocity (bcs.c:3645)
  * and adds the set-up the reference does inside every PoissonSolver_MG call
  * (PoissonLHSNew on every level, MyNvertRestriction, FullyBlocked), which here
  * runs once and stays resident on the GPU.

@@ -100,3 +100,13 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
   ucont[3 * REC.mark] = 5.0;
   return take_status();
 }
+int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,
+                        double *ucat) {
+  (void)ctx;
+  REC.n_projection_cart++;
+  REC.phi_proj = phi; REC.dt_proj = dt; REC.st_proj = st; REC.ucont_proj = ucont;
+  REC.ubcs_proj = ubcs; REC.ucat_proj = ucat;
+  ucont[3 * REC.mark] = 5.0;
+  ucat[3 * REC.mark + 2] = 9.0;
+  return take_status();
+}

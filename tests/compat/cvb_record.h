@@ -13,7 +13,8 @@
 #define REC_MAXTOK 32
 
 typedef struct {
-  int n_init, n_destroy, n_last_error, n_setup, n_set_nvert, n_solver_mg, n_update, n_projection;
+  int n_init, n_destroy, n_last_error, n_setup, n_set_nvert, n_solver_mg, n_update, n_projection,
+      n_projection_cart;
   int ntok;
   char tok[REC_MAXTOK][64];
   int nlevels;
@@ -25,13 +26,15 @@ typedef struct {
   cvb_solve_opts opts;
   /* cvb_update_pressure */
   double *p, *phi_up;
-  /* cvb_projection */
+  /* cvb_projection, cvb_projection_cart */
   const double *phi_proj;
   double *ucont_proj, dt_proj, st_proj;
+  double *ubcs_proj, *ucat_proj;
   /* the status the next path call returns, then 0 again */
   int fail_next;
   /* cell (box index) the path calls write: solver_mg sets ucont[3m+1] = 42 and
-   * phi[m] = 3; update_pressure sets p[m] = 7; projection sets ucont[3m] = 5 */
+   * phi[m] = 3; update_pressure sets p[m] = 7; projection sets ucont[3m] = 5;
+   * projection_cart sets ucont[3m] = 5 and ucat[3m+2] = 9 */
   long mark;
 } cvb_record;
 

@@ -17,7 +17,7 @@
 #include "cvb_record.h"
 #include "poisson_gb300.h"
 
-extern PetscInt block_number, immersed;
+extern PetscInt block_number, immersed, wallfunction;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
 UserMG *ref_usermg(void);
@@ -124,13 +124,27 @@ int main(void) {
   CHECK(shim_vec_data(fine->lP)[loc] == 7.0, "lP not refreshed");
   CHECK(shim_arrays_out() == 0, "update left %d arrays out", shim_arrays_out());
 
-  /* --- Projection --- */
+  /* --- Projection: covered boundary types, all on the device in one call --- */
   CHECK(Projection_GB300(fine) == 0, "Projection_GB300 failed");
-  CHECK(REC.phi_proj == shim_vec_data(fine->Phi) && REC.ucont_proj == shim_vec_data(fine->Ucont),
-        "Phi / Ucont storage");
+  CHECK(REC.n_projection_cart == 1 && REC.n_projection == 0, "one-call projection not used");
+  CHECK(REC.phi_proj == shim_vec_data(fine->Phi) && REC.ucont_proj == shim_vec_data(fine->Ucont) &&
+            REC.ubcs_proj == shim_vec_data(fine->Bcs.Ubcs) && REC.ucat_proj == shim_vec_data(fine->Ucat),
+        "Phi / Ucont / Bcs.Ubcs / Ucat storage");
   CHECK(REC.dt_proj == 0.01 && REC.st_proj == 2.0, "projection dt %g st %g", REC.dt_proj, REC.st_proj);
   CHECK(shim_vec_data(fine->lUcont)[3 * loc] == 5.0, "lUcont not refreshed after the projection");
+  CHECK(shim_vec_data(fine->lUcat)[3 * loc + 2] == 9.0, "lUcat not refreshed after the projection");
   CHECK(shim_arrays_out() == 0, "projection left %d arrays out", shim_arrays_out());
+  /* uncovered types (annulus face, wall function): flux correction on the
+   * device, the reference's own Contra2Cart / GhostNodeVelocity on the host */
+  fine->bctype[2] = 11;
+  CHECK(Projection_GB300(fine) == 0 && REC.n_projection == 1 && REC.n_projection_cart == 1,
+        "annulus face: host post-projection not used");
+  fine->bctype[2] = 1;
+  wallfunction = 1;
+  CHECK(Projection_GB300(fine) == 0 && REC.n_projection == 2 && REC.n_projection_cart == 1,
+        "wall function: host post-projection not used");
+  wallfunction = 0;
+  CHECK(shim_arrays_out() == 0, "host-path projections left %d arrays out", shim_arrays_out());
 
   /* --- failures come back as the call's status, arrays restored --- */
   REC.fail_next = CVB_NOT_CONVERGED;
@@ -140,6 +154,10 @@ int main(void) {
   CHECK(shim_arrays_out() == 0, "failed solve left %d arrays out", shim_arrays_out());
   REC.fail_next = CVB_CUDA_ERROR;
   CHECK(Projection_GB300(fine) == CVB_CUDA_ERROR, "projection failure not returned");
+  fine->bctype[4] = 13;
+  REC.fail_next = CVB_CUDA_ERROR;
+  CHECK(Projection_GB300(fine) == CVB_CUDA_ERROR, "host-path projection failure not returned");
+  fine->bctype[4] = 1;
   CHECK(shim_arrays_out() == 0, "failed projection left %d arrays out", shim_arrays_out());
 
   /* --- moving body: new nvert --- */
