@@ -240,19 +240,26 @@ def run_cvb(args, ws, rank, local):
     wall = time.perf_counter() - t0
     e2e_ms = max_over_ranks(ws, max(e0.elapsed_time(e1), wall * 1e3), torch.device("cuda", local))
 
-    # roofline of the dominant kernel pair: one FP32 zebra half-sweep on the
-    # finest level (seven residual + eight line-solve launches per V(2,2) cycle there)
+    # roofline of the dominant kernel: one FP32 zebra half-sweep on the finest
+    # level (eight per V(2,2) cycle there), in the form the set-up autotuner
+    # chose for that level -- one kernel, or a residual and a line-solve kernel
     k_ms, k_bytes = ctx.time_kernel("zebra_f32", level=-1, reps=30)
+    fine_tune = [t for t in ctx.tuning()["line_sweep"] if t["level"] == ctx.nlevels - 1]
+    zebra_form = fine_tune[0]["zebra_f32"]["choice"] if fine_tune else "split"
     r32_ms, r32_bytes = ctx.time_kernel("residual_f32", level=-1, reps=30)
     k64_ms, k64_bytes = ctx.time_kernel("residual_f64", level=-1, reps=30)
     peak, peak_kind = peaks()
     cells = int(np.prod(ctx.shapes[-1]))
-    roof = {"kernel": "FP32 zebra half-sweep on the finest level: k_resid_color<float,0> (7-point residual on one "
-                      "color; the channel grid is orthogonal, so the cross-derivative terms are exactly zero and are "
-                      "skipped) + k_line_solve<float,8,4> (that color's y-line solves)",
+    forms = {"fused": "k_zebra_fused<float,8,4,0> (one kernel: that color's 7-point residual into shared memory, "
+                      "then its y-line solves, in place)",
+             "split": "k_resid_color<float,0> (7-point residual on one color) + k_line_solve<float,8,4> (that "
+                      "color's y-line solves)"}
+    roof = {"kernel": "FP32 zebra half-sweep on the finest level, " + forms[zebra_form] + "; the channel grid is "
+                      "orthogonal, so the cross-derivative terms are exactly zero and are skipped",
+            "zebra_form": zebra_form,
             "bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
-            "traffic": traffic_per_launch("zebra_f32", cells), "algorithmic_bytes": k_bytes,
+            "traffic": traffic_per_launch("zebra_f32_" + zebra_form, cells), "algorithmic_bytes": k_bytes,
             "avg_launch_ms": k_ms,
             "fp32_residual": {"achieved_gbs": r32_bytes / (r32_ms * 1e-3) / 1e9, "avg_launch_ms": r32_ms,
                               "algorithmic_bytes": r32_bytes, "frac": r32_bytes / (r32_ms * 1e-3) / 1e9 / peak,

@@ -6,7 +6,8 @@ KERNEL is one of line_sweep_f32, line_sweep_f64 (a damped-Jacobi y-line sweep),
 residual_f32, residual_f64, zebra_f32, zebra_f64 (one half-sweep of the zebra
 smoother: residual on one color, then its line solves), vcycle_f32, vcycle_f64
 (one V-cycle with the default options from the level down, replayed from a
-CUDA graph; no byte count); default: all.  The problem is the periodic channel (x and z periodic,
+CUDA graph; no byte count), contra2cart, ghost_nodes (Contra2Cart and
+GhostNodeVelocity; finest level only); default: all.  The problem is the periodic channel (x and z periodic,
 tanh-stretched walls in y, factor 2.5) at the given cell counts.  Each kernel's
 timed launches run inside an NVTX range named ``timed:<kernel>``, so a profiler
 can be pointed at exactly those launches (``ncu --nvtx --nvtx-include
