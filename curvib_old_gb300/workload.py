@@ -660,3 +660,45 @@ def noisy_rhs(b, nvert, aj, dt, seed, amp=1e-2):
     out = b.copy()
     out[fl] += rng.uniform(-amp, amp, size=int(fl.sum())) / dt
     return compatible(out, aj, nvert)
+
+
+def sphere_mesh(center, radius: float, subdivisions: int = 3):
+    """A closed triangulated sphere, as the immersed-body meshes ibm_search_advanced
+    (ibm.c:4197) classifies cells against: an icosahedron whose faces are split
+    in four `subdivisions` times, nodes pushed out to the sphere.  Returns
+    (xyz [n_v, 3], tri [n_elmt, 3] int32 node indices, nf [n_elmt, 3] unit
+    normals pointing out of the body)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nf_ = []
+        for (a, b, c) in f:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf_ += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        f = nf_
+    xyz = np.array(verts) * radius + np.asarray(center, dtype=np.float64)
+    tri = np.array(f, dtype=np.int32)
+    e1 = xyz[tri[:, 1]] - xyz[tri[:, 0]]
+    e2 = xyz[tri[:, 2]] - xyz[tri[:, 0]]
+    n = np.cross(e1, e2)
+    n /= np.linalg.norm(n, axis=1)[:, None]
+    out = (xyz[tri].mean(axis=1) - np.asarray(center)) @ np.eye(3)
+    flip = np.einsum("ij,ij->i", n, out) < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    n[flip] = -n[flip]
+    return xyz, tri, n

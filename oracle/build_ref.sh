@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE ONLY.
-# Compiles the reference's own poisson.c, metrics.c, implicitsolver.c, rhs.c and
-# bcs.c, where they lie under the reference checkout, unmodified, against the
+# Compiles the reference's own poisson.c, metrics.c, implicitsolver.c, rhs.c,
+# bcs.c, ibm.c, compgeom.c and variables.c, where they lie under the reference
+# checkout, unmodified, against the
 # single-process PETSc API shim in oracle/petsc_shim/, into
 # oracle/_ref/libcvbref.so.  In the objects of rhs.c and bcs.c, Contra2Cart and
 # GhostNodeVelocity are renamed cvbref_Contra2Cart / cvbref_GhostNodeVelocity
@@ -25,10 +26,14 @@ mkdir -p "$OUT"
 CC="${CC:-gcc}"
 CFLAGS="-std=gnu99 -O2 -fPIC -w -I$HERE/petsc_shim/include -I$REF"
 objs=()
-for f in poisson metrics implicitsolver rhs bcs; do
+for f in poisson metrics implicitsolver rhs bcs compgeom variables; do
   $CC $CFLAGS -c "$REF/$f.c" -o "$OUT/ref_$f.o"
   objs+=("$OUT/ref_$f.o")
 done
+# ibm.c declares point_cell_thin with 19 parameters and defines it with 13;
+# ibm_compile_fix.h names the two forms apart so the file compiles unmodified.
+$CC $CFLAGS -include ibm_compile_fix.h -c "$REF/ibm.c" -o "$OUT/ref_ibm.o"
+objs+=("$OUT/ref_ibm.o")
 for f in rhs bcs; do
   objcopy --redefine-sym Contra2Cart=cvbref_Contra2Cart \
           --redefine-sym GhostNodeVelocity=cvbref_GhostNodeVelocity "$OUT/ref_$f.o"

@@ -769,3 +769,198 @@ int orc_ghost_node_velocity(const orc_level *L, double *ub, double *u) {
 #undef B3
   return 0;
 }
+
+/* ------------------------------------------------------------------ IB search */
+/* intsect_triangle (compgeom.c:17-50): the ray orig + t dir against one
+ * triangle; 1 with (t, u, v) on a hit. */
+static int ray_triangle(const double *o, const double *d, const double *v0, const double *v1, const double *v2,
+                        double *t) {
+  double e1[3], e2[3], pv[3], tv[3], qv[3];
+  for (int c = 0; c < 3; c++) { e1[c] = v1[c] - v0[c]; e2[c] = v2[c] - v0[c]; }
+  pv[0] = d[1] * e2[2] - d[2] * e2[1];
+  pv[1] = d[2] * e2[0] - d[0] * e2[2];
+  pv[2] = d[0] * e2[1] - d[1] * e2[0];
+  const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+  if (det > -0.00000001 && det < 0.00000001) return 0;
+  const double inv = 1.0 / det;
+  for (int c = 0; c < 3; c++) tv[c] = o[c] - v0[c];
+  const double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) * inv;
+  if (u < 0.0 || u > 1.0) return 0;
+  qv[0] = tv[1] * e1[2] - tv[2] * e1[1];
+  qv[1] = tv[2] * e1[0] - tv[0] * e1[2];
+  qv[2] = tv[0] * e1[1] - tv[1] * e1[0];
+  const double v = (d[0] * qv[0] + d[1] * qv[1] + d[2] * qv[2]) * inv;
+  if (v < 0.0 || u + v > 1.0) return 0;
+  *t = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) * inv;
+  return 1;
+}
+
+enum { IBM_NC = 40, IBM_MAX_HITS = 1000 };
+
+typedef struct {
+  double min[3], max[3], dc[3];
+  int *col_start, *col_tri, *col_jmax;  /* bucket column (i, k) -> triangles and their j range end */
+} ibm_grid;
+
+static void ibm_grid_build(ibm_grid *G, int n_v, const double *xyz, int n_elmt, const int *tri) {
+  for (int c = 0; c < 3; c++) { G->min[c] = 1.e23; G->max[c] = -1.e23; }
+  for (int q = 0; q < n_v; q++)
+    for (int c = 0; c < 3; c++) {
+      const double x = xyz[3 * q + c];
+      G->min[c] = G->min[c] < x ? G->min[c] : x;
+      G->max[c] = G->max[c] < x ? x : G->max[c];
+    }
+  for (int c = 0; c < 3; c++) G->dc[c] = (G->max[c] - G->min[c]) / (IBM_NC - 1.);
+  /* bucket ranges of every triangle (ibm.c:4279-4318), then the lists of the
+   * (i, k) columns: a ray from bucket j walks the column's buckets j .. NC-1,
+   * so it meets the triangles whose j range ends above j */
+  int (*rng)[6] = malloc(sizeof(int[6]) * (size_t)(n_elmt > 0 ? n_elmt : 1));
+  G->col_start = calloc(IBM_NC * IBM_NC + 1, sizeof(int));
+  for (int e = 0; e < n_elmt; e++) {
+    for (int c = 0; c < 3; c++) {
+      const double a = xyz[3 * tri[3 * e] + c], b = xyz[3 * tri[3 * e + 1] + c], d = xyz[3 * tri[3 * e + 2] + c];
+      double lo = a < b ? a : b, hi = a < b ? b : a;
+      lo = lo < d ? lo : d;
+      hi = hi < d ? d : hi;
+      int imin = (int)floor((lo - G->min[c]) / G->dc[c]);
+      int imax = (int)floor((hi - G->min[c]) / G->dc[c]) + 1;
+      rng[e][2 * c] = imin < 0 ? 0 : imin;
+      rng[e][2 * c + 1] = imax > IBM_NC ? IBM_NC : imax;
+    }
+    for (int k = rng[e][4]; k < rng[e][5]; k++)
+      for (int i = rng[e][0]; i < rng[e][1]; i++)
+        if (rng[e][2] < rng[e][3]) G->col_start[k * IBM_NC + i + 1]++;
+  }
+  for (int q = 0; q < IBM_NC * IBM_NC; q++) G->col_start[q + 1] += G->col_start[q];
+  const int total = G->col_start[IBM_NC * IBM_NC];
+  G->col_tri = malloc(sizeof(int) * (size_t)(total > 0 ? total : 1));
+  G->col_jmax = malloc(sizeof(int) * (size_t)(total > 0 ? total : 1));
+  int *fill = calloc(IBM_NC * IBM_NC, sizeof(int));
+  for (int e = 0; e < n_elmt; e++) {
+    if (rng[e][2] >= rng[e][3]) continue;
+    for (int k = rng[e][4]; k < rng[e][5]; k++)
+      for (int i = rng[e][0]; i < rng[e][1]; i++) {
+        const int col = k * IBM_NC + i, at = G->col_start[col] + fill[col]++;
+        G->col_tri[at] = e;
+        G->col_jmax[at] = rng[e][3];
+      }
+  }
+  free(fill);
+  free(rng);
+}
+
+/* point_cell_advanced (ibm.c:1285-1400) with randomdirection (ibm.c:87-118):
+ * 4 when p is inside the body, else 0; -1 when max_tries rays all met a
+ * singular pair (two hits at the same distance on faces not facing apart). */
+static int point_inside(const ibm_grid *G, const double *p, int ic, int jc, int kc, const double *xyz, const int *tri,
+                        const double *nf, int max_tries) {
+  static double dt[IBM_MAX_HITS], dn[IBM_MAX_HITS][3];
+  const int col = kc * IBM_NC + ic;
+  for (int seed = 1; seed <= max_tries; seed++) {
+    const double xpc = G->dc[0] * (ic + 0.5) + G->min[0];
+    const double zpc = G->dc[2] * (kc + 0.5) + G->min[2];
+    srand(seed);
+    double s = rand() / ((double)RAND_MAX + 1) - 0.5;
+    double d[3];
+    d[0] = (xpc + s * G->dc[0]) - p[0];
+    d[1] = (G->max[1] + 0.2) - p[1];
+    d[2] = (zpc + s * G->dc[2]) - p[2];
+    s = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    d[0] /= s; d[1] /= s; d[2] /= s;
+    int hits = 0, singular = 0;
+    for (int q = G->col_start[col]; q < G->col_start[col + 1] && !singular; q++) {
+      if (G->col_jmax[q] <= jc) continue;
+      const int e = G->col_tri[q];
+      double t;
+      if (!ray_triangle(p, d, xyz + 3 * tri[3 * e], xyz + 3 * tri[3 * e + 1], xyz + 3 * tri[3 * e + 2], &t)) continue;
+      if (!(t > 0)) continue;
+      const double *n = nf + 3 * e;
+      if (hits == IBM_MAX_HITS) return -1;
+      for (int h = 0; h < hits; h++) {
+        const double ndotn = dn[h][0] * n[0] + dn[h][1] * n[1] + dn[h][2] * n[2];
+        if (fabs(t - dt[h]) < 1.e-8 && ndotn > -0.97) singular = 1;
+      }
+      dt[hits] = t;
+      dn[hits][0] = n[0]; dn[hits][1] = n[1]; dn[hits][2] = n[2];
+      hits++;
+    }
+    if (!singular) return (hits % 2) ? 4 : 0;
+  }
+  return -1;
+}
+
+int orc_ibm_search(int mx, int my, int mz, const double *cent, int n_v, const double *xyz, int n_elmt,
+                   const int *tri, const double *nf, int ibi, int nbodies, const double *nvert_o, double *nvert,
+                   int max_tries) {
+  ibm_grid G;
+  ibm_grid_build(&G, n_v, xyz, n_elmt, tri);
+  const size_t n = (size_t)mx * my * mz;
+  double *nv = malloc(sizeof(double) * n);
+  memcpy(nv, nvert, sizeof(double) * n);
+  int rc = 0;
+#define P(i, j, k) (((size_t)(k) * my + (j)) * mx + (i))
+  /* the inside test on interior cells (ibm.c:4337-4357) */
+  for (int k = 1; k < mz - 1 && !rc; k++)
+    for (int j = 1; j < my - 1 && !rc; j++)
+      for (int i = 1; i < mx - 1 && !rc; i++) {
+        const size_t q = P(i, j, k);
+        if (ibi == 0 && nv[q] < 5.) nv[q] = 0;
+        const double *c = cent + 3 * q;
+        if (c[0] > G.min[0] && c[0] < G.max[0] && c[1] > G.min[1] && c[1] < G.max[1] && c[2] > G.min[2] &&
+            c[2] < G.max[2]) {
+          const int ic = (int)floor((c[0] - G.min[0]) / G.dc[0]);
+          const int jc = (int)floor((c[1] - G.min[1]) / G.dc[1]);
+          const int kc = (int)floor((c[2] - G.min[2]) / G.dc[2]);
+          const int r = point_inside(&G, c, ic, jc, kc, xyz, tri, nf, max_tries);
+          if (r < 0) { rc = -1; break; }
+          if (nv[q] < r) nv[q] = r;
+          if (nv[q] < 0) nv[q] = 0;
+        }
+      }
+  if (!rc) {
+    /* the layer: every cell next to an inside cell (ibm.c:4415-4437); no cell
+     * becomes inside here, so reading the updated array changes nothing */
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++)
+        for (int i = 0; i < mx; i++) {
+          const size_t q = P(i, j, k);
+          if (nv[q] < 0) nv[q] = 0;
+          if ((int)(nv[q] + 0.5) == 4) continue;
+          const int ip = i < mx - 1 ? i + 1 : i, im = i > 0 ? i - 1 : i;
+          const int jp = j < my - 1 ? j + 1 : j, jm = j > 0 ? j - 1 : j;
+          const int kp = k < mz - 1 ? k + 1 : k, km = k > 0 ? k - 1 : k;
+          for (int kk = km; kk <= kp; kk++)
+            for (int jj = jm; jj <= jp; jj++)
+              for (int ii = im; ii <= ip; ii++)
+                if ((int)(nv[P(ii, jj, kk)] + 0.5) == 4) nv[q] = 2 < nv[q] ? nv[q] : 2;
+        }
+    /* a solid cell of the previous step that the search left fluid (ibm.c:4499-4509) */
+    if (ibi == nbodies - 1)
+      for (size_t q = 0; q < n; q++)
+        if (nvert_o[q] > 2.5 && nv[q] < 0.5) nv[q] = 2;
+    /* this body's codes (ibm.c:4651-4659) */
+    for (size_t q = 0; q < n; q++) {
+      if ((int)(nv[q] + 0.5) == 2) nv[q] = 1 + (ibi) / 1000.0;
+      if ((int)(nv[q] + 0.5) == 4) nv[q] = 3 + (ibi) / 1000.0;
+    }
+    /* an IB cell between two fluid cells in k becomes fluid, twice
+     * (ibm.c:4662-4690), in the reference's order */
+    for (int pass = 0; pass < 2; pass++)
+      for (int k = 1; k < mz - 1; k++)
+        for (int j = 1; j < my - 1; j++)
+          for (int i = 1; i < mx - 1; i++) {
+            const size_t q = P(i, j, k);
+            int around = 0;
+            if ((int)(nv[q]) == 1) {
+              if ((int)(nv[P(i, j, k - 1)]) == 0) around++;
+              if ((int)(nv[P(i, j, k + 1)]) == 0) around++;
+            }
+            if (around > 1) nv[q] = 0 < nv[q] ? 0 : nv[q];
+          }
+    memcpy(nvert, nv, sizeof(double) * n);
+  }
+#undef P
+  free(nv);
+  free(G.col_start); free(G.col_tri); free(G.col_jmax);
+  return rc;
+}

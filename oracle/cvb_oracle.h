@@ -67,6 +67,19 @@ void orc_contra2cart(const orc_level *L, const double *ucont, double *ucat);
  * of ring copies.  Returns 0, or -1 (nothing written) for what it does not
  * restate: bctype 11 or 13, or a periodic face whose opposite is not. */
 int orc_ghost_node_velocity(const orc_level *L, double *ubcs, double *ucat);
+/* The nvert classification of ibm_search_advanced (ibm.c:4197-4740) for body
+ * ibi of nbodies, a closed triangle mesh (xyz: n_v nodes; tri: n_elmt node
+ * triples; nf: their unit normals): each interior cell centre (cent,
+ * [mz][my][mx][3]) inside the body's bounding box gets the ray-cast inside test
+ * of point_cell_advanced (ibm.c:1285), rays aimed by randomdirection (ibm.c:87)
+ * through a 40^3 bucket grid; then the 27-cell layer around inside cells, the
+ * phase-change fix against nvert_o, the codes 1 / 3 + ibi/1000, and the two
+ * clean-up passes along k.  nvert ([mz][my][mx]) is read and written.  The
+ * reference retries a ray until it meets no singular pair of intersections;
+ * this gives up after max_tries directions and returns -1 (0 on success). */
+int orc_ibm_search(int mx, int my, int mz, const double *cent, int n_v, const double *xyz, int n_elmt,
+                   const int *tri, const double *nf, int ibi, int nbodies, const double *nvert_o,
+                   double *nvert, int max_tries);
 
 #ifdef __cplusplus
 }

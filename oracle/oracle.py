@@ -78,6 +78,9 @@ def lib():
         _lib.orc_contra2cart.argtypes = [L, P, P]
         _lib.orc_ghost_node_velocity.argtypes = [L, P, P]
         _lib.orc_ghost_node_velocity.restype = ctypes.c_int
+        _lib.orc_ibm_search.argtypes = [ctypes.c_int] * 3 + [P, ctypes.c_int, P, ctypes.c_int, P, P] + \
+            [ctypes.c_int] * 2 + [P, P, ctypes.c_int]
+        _lib.orc_ibm_search.restype = ctypes.c_int
     return _lib
 
 
@@ -204,6 +207,21 @@ def ghost_node_velocity(L: OLevel, ubcs, ucat):
     return rc, ub, u
 
 
+def ibm_search(cent, xyz, tri, nf, ibi, nbodies, nvert_o, nvert, max_tries=64):
+    """The nvert classification of ibm_search_advanced (ibm.c:4197-4740):
+    returns (status, nvert); status -1 if some cell found no clean ray."""
+    mz, my, mx = cent.shape[:3]
+    c = np.ascontiguousarray(cent, dtype=np.float64)
+    x = np.ascontiguousarray(xyz, dtype=np.float64)
+    t = np.ascontiguousarray(tri, dtype=np.int32)
+    n = np.ascontiguousarray(nf, dtype=np.float64)
+    no = np.ascontiguousarray(nvert_o, dtype=np.float64)
+    out = np.array(nvert, dtype=np.float64, copy=True, order="C")
+    rc = lib().orc_ibm_search(mx, my, mz, _p(c), len(x), _p(x), len(t), _p(t), _p(n), ibi, nbodies, _p(no),
+                              _p(out), max_tries)
+    return rc, out
+
+
 # ------------------------------------------------------------------ reference
 class Reference:
     """The reference's own routines, compiled against the API shim (oracle/_ref/)."""
@@ -309,6 +327,18 @@ class Reference:
         u = np.array(ucat, dtype=np.float64, copy=True, order="C")
         self.L.ref_ghost_node_velocity(_p(ub), _p(u))
         return ub, u
+
+
+    def ibm_search(self, xyz, tri, nf, ibi, nbodies, nvert_o, nvert):
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        t = np.ascontiguousarray(tri, dtype=np.int32)
+        n = np.ascontiguousarray(nf, dtype=np.float64)
+        no = np.ascontiguousarray(nvert_o, dtype=np.float64)
+        out = np.array(nvert, dtype=np.float64, copy=True, order="C")
+        rc = self.L.ref_ibm_search(len(x), _p(x), len(t), _p(t), _p(n), ibi, nbodies, _p(no), _p(out))
+        if rc:
+            raise RuntimeError(f"ref_ibm_search failed: {rc}")
+        return out
 
 
 def solve_mg(levels, b, rtol=1e-8, max_it=500, restart=30, nu=2, threads=0):

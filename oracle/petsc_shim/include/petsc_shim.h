@@ -128,6 +128,7 @@ typedef const char *MatType;
 #define PetscSqrtScalar(a) sqrt(a)
 #define PetscMalloc(sz, pp) ((*(void **)(pp) = calloc(1, (size_t)(sz) > 0 ? (size_t)(sz) : 1)) == NULL)
 #define PetscFree(p) (free(p), (p) = NULL, 0)
+#define PetscNew(pp) PetscMalloc(sizeof(**(pp)), (pp))
 #define CHKERRQ(e) do { if (e) return (e); } while (0)
 #define CHKMEMQ
 #define SETERRQ(c, n, s) return (n)

@@ -36,6 +36,7 @@ PetscErrorCode GhostNodeVelocity(UserCtx *user) { (void)user; return 0; }
  * oracle/build_ref.sh so that they do not collide with the inert pair above. */
 PetscErrorCode cvbref_Contra2Cart(UserCtx *user);
 PetscErrorCode cvbref_GhostNodeVelocity(UserCtx *user);
+PetscErrorCode ibm_search_advanced(UserCtx *user, IBMNodes *ibm, PetscInt ibi);
 
 PetscErrorCode FormMetrics(UserCtx *user);
 PetscErrorCode Update_Metrics_PBC(UserCtx *user);
@@ -76,6 +77,7 @@ static void make_vectors(UserCtx *u, int finest) {
   DMCreateGlobalVector(u->da, &u->Aj);
   VecDuplicate(u->Aj, &u->IAj); VecDuplicate(u->Aj, &u->JAj); VecDuplicate(u->Aj, &u->KAj);
   VecDuplicate(u->Aj, &u->Nvert); VecDuplicate(u->Aj, &u->Phi); VecDuplicate(u->Aj, &u->P);
+  VecDuplicate(u->Aj, &u->Nvert_o);
   DMCreateLocalVector(u->fda, &u->lCsi);
   VecDuplicate(u->lCsi, &u->lEta); VecDuplicate(u->lCsi, &u->lZet);
   VecDuplicate(u->lCsi, &u->lICsi); VecDuplicate(u->lCsi, &u->lIEta); VecDuplicate(u->lCsi, &u->lIZet);
@@ -88,6 +90,7 @@ static void make_vectors(UserCtx *u, int finest) {
   DMCreateLocalVector(u->da, &u->lAj);
   VecDuplicate(u->lAj, &u->lIAj); VecDuplicate(u->lAj, &u->lJAj); VecDuplicate(u->lAj, &u->lKAj);
   VecDuplicate(u->lAj, &u->lNvert); VecDuplicate(u->lAj, &u->lPhi); VecDuplicate(u->lAj, &u->lP);
+  VecDuplicate(u->lAj, &u->lNvert_o);
 }
 
 void ref_free(void) {
@@ -429,4 +432,44 @@ int ref_ghost_node_velocity(double *ubcs, double *ucat) {
   copy_owned(u, u->Ucat, 3, ucat, 0);
   copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 0);
   return 0;
+}
+
+/* ibm_search_advanced (ibm.c:4197-4740) on the finest level for body ibi of
+ * nbodies.  The body is a closed triangle mesh: n_v nodes (xyz, x y z per
+ * node), n_elmt triangles (nv, three node indices each) and their unit normals
+ * (nf, x y z per triangle).  nvert_o is the previous step's Nvert_o; nvert is
+ * Nvert, read and written (global boxes).  The routine also builds the body's
+ * interpolation list, which is left in the harness. */
+int ref_ibm_search(int n_v, const double *xyz, int n_elmt, const int *nv, const double *nf, int ibi, int nbodies,
+                   const double *nvert_o, double *nvert) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  IBMNodes *ibm = (IBMNodes *)calloc(1, sizeof(IBMNodes));
+  if (!ibm) return 2;
+  ibm->n_v = n_v;
+  ibm->n_elmt = n_elmt;
+  ibm->x_bp = (double *)malloc(sizeof(double) * n_v);
+  ibm->y_bp = (double *)malloc(sizeof(double) * n_v);
+  ibm->z_bp = (double *)malloc(sizeof(double) * n_v);
+  for (int q = 0; q < n_v; q++) {
+    ibm->x_bp[q] = xyz[3 * q]; ibm->y_bp[q] = xyz[3 * q + 1]; ibm->z_bp[q] = xyz[3 * q + 2];
+  }
+  ibm->nv1 = (int *)malloc(sizeof(int) * n_elmt);
+  ibm->nv2 = (int *)malloc(sizeof(int) * n_elmt);
+  ibm->nv3 = (int *)malloc(sizeof(int) * n_elmt);
+  ibm->nf_x = (double *)malloc(sizeof(double) * n_elmt);
+  ibm->nf_y = (double *)malloc(sizeof(double) * n_elmt);
+  ibm->nf_z = (double *)malloc(sizeof(double) * n_elmt);
+  for (int e = 0; e < n_elmt; e++) {
+    ibm->nv1[e] = nv[3 * e]; ibm->nv2[e] = nv[3 * e + 1]; ibm->nv3[e] = nv[3 * e + 2];
+    ibm->nf_x[e] = nf[3 * e]; ibm->nf_y[e] = nf[3 * e + 1]; ibm->nf_z[e] = nf[3 * e + 2];
+  }
+  NumberOfBodies = nbodies;
+  if (!u->ibmlist) u->ibmlist = (IBMList *)calloc((size_t)(nbodies > 16 ? nbodies : 16), sizeof(IBMList));
+  set_pair(u, u->Nvert, u->lNvert, 1, nvert, u->da);
+  set_pair(u, u->Nvert_o, u->lNvert_o, 1, nvert_o, u->da);
+  int rc = ibm_search_advanced(u, ibm, ibi);
+  copy_owned(u, u->Nvert, 1, nvert, 0);
+  /* the interpolation list stays with the harness (test-only: leaks are harmless) */
+  return rc;
 }

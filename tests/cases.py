@@ -29,6 +29,37 @@ POST_VARIANTS = {
 }
 
 
+# Immersed-body searches (ibm_search_advanced): name -> (scenario whose grid is
+# used, bodies [(centre, radius, subdivisions)], fraction of cells solid in the
+# previous step's nvert_o, seed).  Bodies are classified one after another
+# (ibi = 0, 1, ...), each on the previous one's nvert.
+IBM_CASES = {
+    "one_sphere": ("box_sphere", [((0.5, 0.5, 0.5), 0.3, 3)], 0.0, 0),
+    "periodic_channel": ("channel_periodic", [((0.4, 0.5, 0.5), 0.25, 2)], 0.0, 1),
+    "two_bodies_phase_change": ("ksemi_sphere", [((0.35, 0.45, 0.5), 0.22, 3), ((0.72, 0.55, 0.45), 0.15, 3)],
+                                0.03, 2),
+}
+
+
+def ibm_inputs(name, shape):
+    """The meshes and nvert_o of an IBM_CASES entry (meshes from the committed
+    fixture when present, so that they do not depend on the platform's sqrt)."""
+    from pathlib import Path
+    scen, bodies, frac, seed = IBM_CASES[name]
+    fx = Path(__file__).resolve().parent / "golden" / "ibm_meshes.npz"
+    meshes = []
+    if fx.exists():
+        z = np.load(fx)
+        for b in range(len(bodies)):
+            meshes.append((z[f"{name}_{b}_xyz"], z[f"{name}_{b}_tri"], z[f"{name}_{b}_nf"]))
+    else:
+        for (ctr, r, sub) in bodies:
+            meshes.append(W.sphere_mesh(ctr, r, sub))
+    rng = np.random.default_rng(700 + seed)
+    nvert_o = np.where(rng.random(shape) < frac, 3.0, 0.0)
+    return meshes, nvert_o
+
+
 def post_inputs(shape, seed):
     """ucat and ubcs ([mz][my][mx][3]) the post-projection steps start from."""
     sh = tuple(shape) + (3,)

@@ -3,7 +3,9 @@
 Runs CURVIB's poisson.c / metrics.c / implicitsolver.c / rhs.c / bcs.c,
 compiled unmodified against the single-process PETSc API shim
 (oracle/build_ref.sh), on the small scenarios of tests/cases.py and records
-SHA-256 digests of every output.  The post-projection steps (Contra2Cart,
+SHA-256 digests of every output, including the immersed-body classification
+(ibm_search_advanced, ibm.c) of tests/cases.IBM_CASES, whose meshes are stored
+in ibm_meshes.npz.  The post-projection steps (Contra2Cart,
 GhostNodeVelocity) also run on the variants of cases.POST_VARIANTS, which put
 slip, moving-lid and O-grid faces and blanked cells on the same grids.  The
 inputs (node coordinates, nvert, fluxes) are stored beside the digests so the
@@ -25,7 +27,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from cases import POST_VARIANTS, SCENARIOS, build, digest, digest_nan, post_inputs, seeded  # noqa: E402
+from cases import IBM_CASES, POST_VARIANTS, SCENARIOS, build, digest, digest_nan, ibm_inputs, post_inputs, seeded  # noqa: E402
 from curvib_old_gb300 import workload as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
@@ -96,14 +98,33 @@ def run_variant(vname):
     return post(R, nv, c["ucont"], seed)
 
 
+def run_ibm(name, meshes_out):
+    """ibm_search_advanced for every body of the case, one after another."""
+    scen, bodies, frac, seed = IBM_CASES[name]
+    c = build(scen, nodes=np.load(OUT / f"{scen}.npz")["nodes"])
+    R = O.Reference(c["nodes"], c["nl"], c["bctype"], c["semi"])
+    shape = R.shape(c["nl"] - 1)
+    meshes, nvert_o = ibm_inputs(name, shape)
+    nv = np.zeros(shape)
+    for b, (xyz, tri, nf) in enumerate(meshes):
+        meshes_out[f"{name}_{b}_xyz"], meshes_out[f"{name}_{b}_tri"], meshes_out[f"{name}_{b}_nf"] = xyz, tri, nf
+        nv = R.ibm_search(xyz, tri, nf, b, len(meshes), nvert_o, nv)
+    return digest(nv)
+
+
 def main():
-    out = {"dt": DT, "st": ST, "scenarios": {}, "post_variants": {}}
+    out = {"dt": DT, "st": ST, "scenarios": {}, "post_variants": {}, "ibm": {}}
     for name in SCENARIOS:
         out["scenarios"][name] = run(name)
         print(name, "ok")
     for vname in POST_VARIANTS:
         out["post_variants"][vname] = run_variant(vname)
         print(vname, "ok")
+    meshes = {}
+    for name in IBM_CASES:
+        out["ibm"][name] = run_ibm(name, meshes)
+        print(name, "ok")
+    np.savez_compressed(OUT / "ibm_meshes.npz", **meshes)
     (OUT / "reference_digests.json").write_text(json.dumps(out, indent=1, sort_keys=True))
 
 

@@ -11,7 +11,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from cases import POST_VARIANTS, SCENARIOS, build, digest, digest_nan, post_inputs, seeded
+from cases import IBM_CASES, POST_VARIANTS, SCENARIOS, build, digest, digest_nan, ibm_inputs, post_inputs, seeded
 from curvib_old_gb300 import workload as W
 from oracle import oracle as O
 
@@ -107,6 +107,23 @@ def test_post_projection_variants_match_reference(vname):
         nv[k, j, i] = 8.0
     L = O.OLevel(c["metrics"][-1], nv, bct, c["semi"])
     _check_post(L, c["ucont"], seed, REF["post_variants"][vname])
+
+
+@pytest.mark.parametrize("name", sorted(IBM_CASES))
+def test_ibm_search_matches_reference(name):
+    """The immersed-body classification (ibm_search_advanced, ibm.c:4197-4740):
+    ray-cast inside test, layer, phase-change fix, per-body codes and clean-up,
+    body after body, against the reference's own ibm.c."""
+    scen, bodies, frac, seed = IBM_CASES[name]
+    c = _setup(scen)
+    cent = c["metrics"][-1]["Cent"]
+    meshes, nvert_o = ibm_inputs(name, cent.shape[:3])
+    nv = np.zeros(cent.shape[:3])
+    for b, (xyz, tri, nf) in enumerate(meshes):
+        rc, nv = O.ibm_search(cent, xyz, tri, nf, b, len(meshes), nvert_o, nv)
+        assert rc == 0
+    assert digest(nv) == REF["ibm"][name]
+    assert (nv == 3.0 + (len(meshes) - 1) / 1000.0).any()  # the last body has solid cells
 
 
 def test_ghost_node_velocity_refuses_unrestated_types():
