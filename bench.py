@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--no-step", action="store_true", help="skip the projection step at 192^3 (config 2)")
     ap.add_argument("--step-steps", type=int, default=5)
+    ap.add_argument("--no-ibm", action="store_true", help="skip the immersed-body search at 192^3")
     return ap.parse_args()
 
 
@@ -293,6 +294,8 @@ def run_cvb(args, ws, rank, local):
     }
     if not args.no_step:
         out["projection_step"] = bench_step(args, ws, local)
+    if not args.no_ibm:
+        out["ibm_search"] = bench_ibm(args, ws, local, rank == 0 and not args.no_cpu_baseline)
     if not args.no_batch:
         out["batch"] = bench_batch(args, ws, local)
     if not args.no_serve:
@@ -391,6 +394,55 @@ def bench_step(args, ws, local):
         assert L.cvb_time_kernel(ctx._ctx, kid, ctx.nlevels - 1, 20, ctypes.byref(ms), ctypes.byref(nbytes)) == 0
         kt[name + "_us"] = ms.value * 1e3
     out["post_projection_kernels"] = kt
+    ctx.close()
+    return out
+
+
+def bench_ibm(args, ws, local, with_cpu):
+    """The immersed-body classification the reference reruns for a moving body
+    every step (ibm_search_advanced, ibm.c:4197), on the 192^3 grid of the
+    projection step: a sphere of radius 0.25 triangulated with 20,480 faces,
+    moved by 1 % of its radius between calls, each call classifying against
+    the previous call's nvert.  Host arrays in and out; the cell centres are
+    uploaded by the first call and stay on the device after it.  The CPU
+    baseline is the oracle's restatement of the same search on one core."""
+    import torch
+
+    from curvib_old_gb300 import workload as W
+    from curvib_old_gb300.solver import PoissonContext
+    P = W.make_problem((192, 192, 192), (1.0, 1.0, 1.0), 2.0, True, (False, False, False), [], name="box192")
+    ctx = PoissonContext(local).setup(P)
+    cent = P.metrics[-1]["Cent"]
+    nv = np.zeros(cent.shape[:3])
+    zero = np.zeros_like(nv)
+    meshes = [W.sphere_mesh((0.5 + 0.0025 * q, 0.5, 0.5), 0.25, 5) for q in range(args.step_steps + 1)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nv = ctx.ibm_search(cent, *meshes[0], 0, 1, nv, zero)
+    first = time.perf_counter() - t0
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for q in range(1, len(meshes)):
+        nv_o = nv
+        nv = ctx.ibm_search(None, *meshes[q], 0, 1, nv_o, zero)
+    torch.cuda.synchronize()
+    wall = max_over_ranks(ws, time.perf_counter() - t0, torch.device("cuda", local))
+    calls = len(meshes) - 1
+    out = {"workload": "192^3 cells (config 0's grid law), a sphere r=0.25 of 20,480 triangles moved 1% of r per call, "
+                       "nvert_o = the previous call's result; host arrays, cell centres resident after the first call",
+           "cells": int(nv.size), "triangles": int(len(meshes[0][1])),
+           "first_call_ms": first * 1e3, "ms_per_search": wall * 1e3 / calls,
+           "cells_per_s": ws * calls * nv.size / wall,
+           "codes": {str(k): int(v) for k, v in zip(*np.unique(nv, return_counts=True))}}
+    if with_cpu:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        rc, nv_c = O.ibm_search(cent, *meshes[-1], 0, 1, nv_o, zero)
+        cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": nv.size / cpu, "unit": "cells/s", "cores": 1, "kind": "port",
+                               "seconds_per_search": cpu, "sample": "the last search of the sequence, once",
+                               "same_result": bool(rc == 0 and np.array_equal(nv_c, nv))}
     ctx.close()
     return out
 

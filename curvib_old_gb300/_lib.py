@@ -70,6 +70,8 @@ EXPORTS = {
     "cvb_contra2cart": ([_P, _P, _P], _I),
     "cvb_ghost_node_velocity": ([_P, _P, _P], _I),
     "cvb_projection_cart": ([_P, _P, _D, _D, _P, _P, _P], _I),
+    "cvb_ibm_search": ([_P, _P, _I, _P, _I, _P, _P, _I, _I, _P, _P], _I),
+    "cvb_ibm_ray_offsets": ([_I, _P], _I),
     "cvb_device_rhs": ([_P], _P),
     "cvb_device_phi": ([_P], _P),
     "cvb_solve_resident": ([_P, _P, _P], _I),

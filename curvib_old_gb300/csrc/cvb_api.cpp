@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <cstdarg>
 #include <cmath>
@@ -148,6 +149,7 @@ static void free_all(cvb_ctx *ctx) {
   ctx->partial = ctx->sums = ctx->hdev = nullptr;
   ctx->uc_dev = ctx->p_dev = nullptr;
   ctx->ucat_dev = ctx->ubcs_dev = nullptr;
+  ctx->ibm_cent = nullptr;
   ctx->ready = false;
 }
 
@@ -1476,6 +1478,147 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
   CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+// randomdirection's ray offsets (ibm.c:101-104): the first rand() after
+// srand(seed), scaled to [-0.5, 0.5), for seeds 1 .. n.  They are drawn from a
+// private generator state (initstate / random / setstate; in glibc rand() is
+// random() and srand() seeds the same kind of state), so the caller's own
+// rand() sequence is left where it was.
+int cvb_ibm_ray_offsets(int n, double *s) {
+  if (n < 0 || (n > 0 && !s)) return CVB_BAD_INPUT;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  alignas(16) static char state[128];
+  char *prev = nullptr;
+  for (int q = 0; q < n; q++) {
+    char *old = initstate((unsigned)(q + 1), state, sizeof state);
+    if (q == 0) prev = old;
+    s[q] = random() / ((double)RAND_MAX + 1) - 0.5;
+  }
+  if (prev) setstate(prev);
+  return CVB_OK;
+}
+
+int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz, int n_elmt, const int *tri,
+                   const double *nf, int ibi, int nbodies, const double *nvert_o, double *nvert) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!xyz || !tri || !nf || !nvert_o || !nvert) return fail(ctx, CVB_BAD_INPUT, "NULL array");
+  if (!cent && !ctx->ibm_cent) return fail(ctx, CVB_BAD_INPUT, "cent is NULL and no earlier call gave the centres");
+  if (n_v < 3 || n_elmt < 1) return fail(ctx, CVB_BAD_INPUT, "a body needs 3 nodes and 1 triangle");
+  if (nbodies < 1 || ibi < 0 || ibi >= nbodies) return fail(ctx, CVB_BAD_INPUT, "body %d of %d", ibi, nbodies);
+  for (long e = 0; e < 3L * n_elmt; e++)
+    if (tri[e] < 0 || tri[e] >= n_v) return fail(ctx, CVB_BAD_INPUT, "triangle %ld names node %d", e / 3, tri[e]);
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  IbmArgs A;
+  std::memset(&A, 0, sizeof A);
+  A.g = F.g;
+  // bounding box and buckets (ibm.c:4250-4318)
+  for (int c = 0; c < 3; c++) { A.min[c] = 1.e23; A.max[c] = -1.e23; }
+  for (int q = 0; q < n_v; q++)
+    for (int c = 0; c < 3; c++) {
+      const double x = xyz[3 * q + c];
+      A.min[c] = A.min[c] < x ? A.min[c] : x;
+      A.max[c] = A.max[c] < x ? x : A.max[c];
+    }
+  for (int c = 0; c < 3; c++) {
+    A.dc[c] = (A.max[c] - A.min[c]) / (kIbmBuckets - 1.);
+    if (!(A.dc[c] > 0)) return fail(ctx, CVB_BAD_INPUT, "the body is flat in direction %d", c);
+  }
+  // each triangle's bucket ranges; the column lists keep, per (i, k) column,
+  // its triangles and the end of their range in j
+  const int ncol = kIbmBuckets * kIbmBuckets;
+  std::vector<int> start(ncol + 1, 0);
+  std::vector<std::array<int, 6>> rng(n_elmt);
+  for (int e = 0; e < n_elmt; e++) {
+    for (int c = 0; c < 3; c++) {
+      const double a = xyz[3 * tri[3 * e] + c], b = xyz[3 * tri[3 * e + 1] + c], d = xyz[3 * tri[3 * e + 2] + c];
+      double lo = a < b ? a : b, hi = a < b ? b : a;
+      lo = lo < d ? lo : d;
+      hi = hi < d ? d : hi;
+      const int imin = (int)std::floor((lo - A.min[c]) / A.dc[c]);
+      const int imax = (int)std::floor((hi - A.min[c]) / A.dc[c]) + 1;
+      rng[e][2 * c] = imin < 0 ? 0 : imin;
+      rng[e][2 * c + 1] = imax > kIbmBuckets ? kIbmBuckets : imax;
+    }
+    if (rng[e][2] >= rng[e][3]) continue;
+    for (int k = rng[e][4]; k < rng[e][5]; k++)
+      for (int i = rng[e][0]; i < rng[e][1]; i++) start[k * kIbmBuckets + i + 1]++;
+  }
+  for (int q = 0; q < ncol; q++) start[q + 1] += start[q];
+  std::vector<int2> ent(std::max(start[ncol], 1));
+  {
+    std::vector<int> fill(ncol, 0);
+    for (int e = 0; e < n_elmt; e++) {
+      if (rng[e][2] >= rng[e][3]) continue;
+      for (int k = rng[e][4]; k < rng[e][5]; k++)
+        for (int i = rng[e][0]; i < rng[e][1]; i++) {
+          const int col = k * kIbmBuckets + i;
+          ent[start[col] + fill[col]++] = make_int2(e, rng[e][3]);
+        }
+    }
+  }
+  std::vector<double> tdata(12 * (size_t)n_elmt);
+  for (int e = 0; e < n_elmt; e++) {
+    for (int v = 0; v < 3; v++)
+      for (int c = 0; c < 3; c++) tdata[12 * (size_t)e + 3 * v + c] = xyz[3 * tri[3 * e + v] + c];
+    for (int c = 0; c < 3; c++) tdata[12 * (size_t)e + 9 + c] = nf[3 * e + c];
+  }
+  double off[kIbmMaxTries];
+  cvb_ibm_ray_offsets(kIbmMaxTries, off);
+  // device copies, from the context's pool for this call
+  // the cell centres stay on the device for later calls with cent == NULL
+  if (!ctx->ibm_cent) TRY(dalloc(ctx, &ctx->ibm_cent, 3 * n));
+  double *d_cent = ctx->ibm_cent;
+  double *d_nv = nullptr, *d_nvo = nullptr, *d_tmp = nullptr, *d_tri = nullptr, *d_off = nullptr;
+  int *d_start = nullptr, *d_flag = nullptr;
+  int2 *d_ent = nullptr;
+  void *bufs[9] = {};
+  int rc = CVB_OK;
+  auto release = [&]() {
+    for (void *b : bufs)
+      if (b) dfree(ctx, b);
+  };
+  rc = dalloc(ctx, &d_nv, n);
+  if (!rc) { bufs[1] = d_nv; rc = dalloc(ctx, &d_nvo, n); }
+  if (!rc) { bufs[2] = d_nvo; rc = dalloc(ctx, &d_tmp, n); }
+  if (!rc) { bufs[3] = d_tmp; rc = dalloc(ctx, &d_tri, tdata.size()); }
+  if (!rc) { bufs[4] = d_tri; rc = dalloc(ctx, &d_off, (size_t)kIbmMaxTries); }
+  if (!rc) { bufs[5] = d_off; rc = dalloc(ctx, &d_start, start.size()); }
+  if (!rc) { bufs[6] = d_start; rc = dalloc(ctx, &d_ent, ent.size()); }
+  if (!rc) { bufs[7] = d_ent; rc = dalloc(ctx, &d_flag, 1); }
+  if (rc) {
+    release();
+    return rc;
+  }
+  bufs[8] = d_flag;
+  cudaStream_t s = ctx->stream;
+  if (cent) CK(cudaMemcpyAsync(d_cent, cent, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_nv, nvert, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_nvo, nvert_o, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_tri, tdata.data(), sizeof(double) * tdata.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_off, off, sizeof off, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_ent, ent.data(), sizeof(int2) * ent.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
+  A.col_start = d_start; A.col_ent = d_ent; A.tri = d_tri; A.offsets = d_off; A.tries = kIbmMaxTries;
+  A.cent = d_cent; A.nvert = d_nv; A.nvert_o = d_nvo; A.ibi = ibi; A.nbodies = nbodies; A.failed = d_flag;
+  launch_ibm_search(A, d_tmp, s);
+  CKL();
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (flag) {
+    release();
+    return fail(ctx, CVB_NOT_CONVERGED,
+                "IB search: a cell centre found no ray clear of edges and vertices in %d directions", kIbmMaxTries);
+  }
+  CK(cudaMemcpyAsync(nvert, d_tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  release();
   return CVB_OK;
 }
 

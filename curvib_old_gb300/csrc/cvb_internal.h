@@ -237,6 +237,27 @@ void launch_update_pressure(const Geom &g, double *p, double *phi, cudaStream_t 
 void launch_projection(const Geom &g, const double *const *fm /*I,J,K csi/eta/zet*/, const double *iaj,
                        const double *jaj, const double *kaj, const double *nvert, const double *phi,
                        double dt, double st, double *ucont, cudaStream_t s);
+// Immersed-body classification (kernels_ibm.cu).  The body's bounding box is
+// cut into kIbmBuckets^3 buckets (ibm.c:4213); a ray from a cell centre walks
+// one bucket column upward.
+constexpr int kIbmBuckets = 40, kIbmMaxHits = 32, kIbmMaxTries = 64;
+struct IbmArgs {
+  Geom g;
+  double min[3], max[3], dc[3];  // bounding box and bucket size
+  const int *col_start;          // bucket column (i, k) = k * kIbmBuckets + i -> its entries
+  const int2 *col_ent;           // (triangle, end of the triangle's bucket range in j)
+  const double *tri;             // per triangle: v0, v1, v2, unit normal (12 doubles)
+  const double *offsets;         // ray offset of seeds 1 .. tries (randomdirection's s)
+  int tries;
+  const double *cent;            // cell centres, [mz][my][mx][3]
+  double *nvert;                 // [mz][my][mx], updated in place
+  const double *nvert_o;         // the previous step's nvert
+  int ibi, nbodies;
+  int *failed;                   // set when a cell found no usable ray
+};
+// The search; tmp is one more [mz][my][mx] array.  The result is left in tmp.
+void launch_ibm_search(const IbmArgs &A, double *tmp, cudaStream_t s);
+
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
                         const double *nvert, const double *ucont, double *ucat, cudaStream_t s);
 // bc: the level's bctype[6]; the host has refused the types it does not cover

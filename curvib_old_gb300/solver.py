@@ -190,6 +190,19 @@ class PoissonContext:
         self._check(self._L.cvb_ghost_node_velocity(self._ctx, ptr(ub), ptr(u)))
         return ub, u
 
+    def ibm_search(self, cent, xyz, tri, nf, ibi, nbodies, nvert_o, nvert):
+        """ibm_search_advanced's nvert classification (ibm.c:4197): returns the
+        new nvert ([mz][my][mx]) of body ibi of nbodies.  cent None reuses the
+        cell centres of an earlier call."""
+        out = np.array(nvert, dtype=np.float64, order="C", copy=True)
+        x = _c64(xyz)
+        t = np.ascontiguousarray(tri, dtype=np.int32)
+        c = None if cent is None else _c64(cent)
+        self._check(self._L.cvb_ibm_search(self._ctx, None if c is None else ptr(c), len(x), ptr(x), len(t), ptr(t),
+                                           ptr(_c64(nf)),
+                                           ibi, nbodies, ptr(_c64(nvert_o)), ptr(out)))
+        return out
+
     def projection_cart(self, phi, dt, st, ucont, ubcs, ucat):
         """Projection, Contra2Cart and GhostNodeVelocity in one call: returns
         (ucont, ubcs, ucat)."""

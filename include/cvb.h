@@ -15,6 +15,8 @@
  *                                          Contra2Cart and GhostNodeVelocity)
  *   Contra2Cart       (rhs.c:25)        -> cvb_contra2cart
  *   GhostNodeVelocity (bcs.c:3645)      -> cvb_ghost_node_velocity
+ *   ibm_search_advanced (ibm.c:4197), its nvert classification
+ *                                       -> cvb_ibm_search
  *
  * Conventions
  *  - Every entry point returns a cvb_status (0 = success, as PetscErrorCode).
@@ -186,6 +188,27 @@ int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat);
  * call, each array copied in and out once. */
 int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,
                         double *ucat);
+/* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
+ * reference reruns for moving bodies every step (solvers.c:201-571), for body
+ * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and
+ * n_elmt triangles (tri, three node indices each; nf, their unit normals).
+ * Every interior cell centre (cent, the finest level's lCent, [mz][my][mx][3])
+ * gets the reference's ray-cast inside test; then the layer of cells next to
+ * inside ones, the fix for cells that were solid in the previous step's
+ * nvert_o ([mz][my][mx]), the codes 3 + ibi/1000 (inside) and 1 + ibi/1000
+ * (layer), and the reference's two clean-up passes along k.  nvert
+ * ([mz][my][mx]) is read and written, bit for bit as the reference leaves
+ * it.  Bodies go one after another, ibi = 0 first (ibi 0 clears nvert below 5).
+ * The reference retries singular rays (through an edge or a vertex) without
+ * end; this tries 64 directions and then returns CVB_NOT_CONVERGED with nvert
+ * untouched.  Feed the result to cvb_set_nvert.  cent may be NULL to reuse
+ * the centres an earlier call uploaded (they stay on the device). */
+int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz, int n_elmt, const int *tri,
+                   const double *nf, int ibi, int nbodies, const double *nvert_o, double *nvert);
+/* randomdirection's ray offsets for seeds 1 .. n (srand(seed); rand() scaled to
+ * [-0.5, 0.5), ibm.c:101-104), from a private generator state: the caller's
+ * rand() sequence is not disturbed.  Needs no context or GPU. */
+int cvb_ibm_ray_offsets(int n, double *s);
 
 /* --- device-resident form (inputs already in HBM) ---------------------- */
 /* Device pointers of the context's finest-level rhs and solution ([mz][my][mx] FP64). */

@@ -964,3 +964,10 @@ int orc_ibm_search(int mx, int my, int mz, const double *cent, int n_v, const do
   free(G.col_start); free(G.col_tri); free(G.col_jmax);
   return rc;
 }
+
+void orc_ibm_ray_offsets(int n, double *s) {
+  for (int q = 0; q < n; q++) {
+    srand(q + 1);
+    s[q] = rand() / ((double)RAND_MAX + 1) - 0.5;
+  }
+}

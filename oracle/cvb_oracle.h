@@ -77,6 +77,9 @@ int orc_ghost_node_velocity(const orc_level *L, double *ubcs, double *ucat);
  * clean-up passes along k.  nvert ([mz][my][mx]) is read and written.  The
  * reference retries a ray until it meets no singular pair of intersections;
  * this gives up after max_tries directions and returns -1 (0 on success). */
+/* randomdirection's offsets for seeds 1 .. n: srand(seed); rand() scaled to
+ * [-0.5, 0.5), exactly as ibm.c:101-104 draws them (the global generator). */
+void orc_ibm_ray_offsets(int n, double *s);
 int orc_ibm_search(int mx, int my, int mz, const double *cent, int n_v, const double *xyz, int n_elmt,
                    const int *tri, const double *nf, int ibi, int nbodies, const double *nvert_o,
                    double *nvert, int max_tries);

@@ -81,6 +81,7 @@ def lib():
         _lib.orc_ibm_search.argtypes = [ctypes.c_int] * 3 + [P, ctypes.c_int, P, ctypes.c_int, P, P] + \
             [ctypes.c_int] * 2 + [P, P, ctypes.c_int]
         _lib.orc_ibm_search.restype = ctypes.c_int
+        _lib.orc_ibm_ray_offsets.argtypes = [ctypes.c_int, P]
     return _lib
 
 

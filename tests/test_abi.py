@@ -38,3 +38,28 @@ def test_default_options_without_a_gpu():
     assert o.smoother == _lib.ZEBRA and 1.0 < o.omega < 2.0
     assert (o.pre_sweeps, o.post_sweeps) == (2, 2)
     assert o.rtol == 1e-8 and o.project_rhs == 1
+
+
+def test_ibm_ray_offsets_match_srand_rand_and_leave_the_callers_sequence():
+    """cvb_ibm_ray_offsets draws randomdirection's offsets (ibm.c:101-104) from a
+    private generator state: the values equal srand(seed); rand() (the oracle
+    calls exactly that), and the caller's rand() sequence goes on undisturbed."""
+    import numpy as np
+    from curvib_old_gb300 import build, _lib
+    from oracle import oracle as O
+    build.build()
+    L = _lib.lib()
+    n = 64
+    got = np.zeros(n)
+    assert L.cvb_ibm_ray_offsets(n, _lib.ptr(got)) == 0
+    want = np.zeros(n)
+    O.lib().orc_ibm_ray_offsets(n, want.ctypes.data_as(ctypes.c_void_p))
+    assert np.array_equal(got, want)
+    assert (np.abs(got) <= 0.5).all() and len(set(got.tolist())) == n
+    libc = ctypes.CDLL(None)
+    libc.srand(12345)
+    seq = [libc.rand() for _ in range(3)]
+    libc.srand(12345)
+    first = libc.rand()
+    assert L.cvb_ibm_ray_offsets(n, _lib.ptr(got)) == 0
+    assert [first, libc.rand(), libc.rand()] == seq
