@@ -1574,9 +1574,9 @@ int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz,
   if (!ctx->ibm_cent) TRY(dalloc(ctx, &ctx->ibm_cent, 3 * n));
   double *d_cent = ctx->ibm_cent;
   double *d_nv = nullptr, *d_nvo = nullptr, *d_tmp = nullptr, *d_tri = nullptr, *d_off = nullptr;
-  int *d_start = nullptr, *d_flag = nullptr;
+  int *d_start = nullptr, *d_flag = nullptr, *d_work = nullptr;
   int2 *d_ent = nullptr;
-  void *bufs[9] = {};
+  void *bufs[10] = {};
   int rc = CVB_OK;
   auto release = [&]() {
     for (void *b : bufs)
@@ -1590,11 +1590,21 @@ int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz,
   if (!rc) { bufs[5] = d_off; rc = dalloc(ctx, &d_start, start.size()); }
   if (!rc) { bufs[6] = d_start; rc = dalloc(ctx, &d_ent, ent.size()); }
   if (!rc) { bufs[7] = d_ent; rc = dalloc(ctx, &d_flag, 1); }
+  // key and list per interior cell, count / start / fill per column, a total
+  const size_t inner = (size_t)(F.g.mx - 2) * (F.g.my - 2) * (F.g.mz - 2);
+  if (!rc) { bufs[8] = d_flag; rc = dalloc(ctx, &d_work, 2 * inner + 3 * (size_t)ncol + 1); }
   if (rc) {
     release();
     return rc;
   }
-  bufs[8] = d_flag;
+  bufs[9] = d_work;
+  IbmWork W;
+  W.key = d_work;
+  W.list = d_work + inner;
+  W.count = d_work + 2 * inner;
+  W.start = W.count + ncol;
+  W.fill = W.start + ncol;
+  W.total = W.fill + ncol;
   cudaStream_t s = ctx->stream;
   if (cent) CK(cudaMemcpyAsync(d_cent, cent, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d_nv, nvert, sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -1606,7 +1616,7 @@ int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz,
   CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
   A.col_start = d_start; A.col_ent = d_ent; A.tri = d_tri; A.offsets = d_off; A.tries = kIbmMaxTries;
   A.cent = d_cent; A.nvert = d_nv; A.nvert_o = d_nvo; A.ibi = ibi; A.nbodies = nbodies; A.failed = d_flag;
-  launch_ibm_search(A, d_tmp, s);
+  launch_ibm_search(A, W, d_tmp, s);
   CKL();
   int flag = 0;
   CK(cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -255,8 +255,13 @@ struct IbmArgs {
   int ibi, nbodies;
   int *failed;                   // set when a cell found no usable ray
 };
+// Work arrays of the search: per interior cell its bucket column (key) and
+// the cell list sorted by column (list); per column its count, start and fill.
+struct IbmWork {
+  int *key, *list, *count, *start, *fill, *total;
+};
 // The search; tmp is one more [mz][my][mx] array.  The result is left in tmp.
-void launch_ibm_search(const IbmArgs &A, double *tmp, cudaStream_t s);
+void launch_ibm_search(const IbmArgs &A, const IbmWork &W, double *tmp, cudaStream_t s);
 
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
                         const double *nvert, const double *ucont, double *ucat, cudaStream_t s);

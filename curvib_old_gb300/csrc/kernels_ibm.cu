@@ -88,8 +88,12 @@ __device__ int ibm_point_inside(const IbmArgs &A, const double *p, int ic, int j
   return -1;
 }
 
-// The inside test on the interior cells (ibm.c:4337-4357), one thread a cell.
-__global__ void __launch_bounds__(128) k_ibm_inside(IbmArgs A) {
+// The inside test on the interior cells (ibm.c:4337-4357) in three passes, so
+// that the ray casts run column by column: a warp then takes cells of one
+// bucket column, which walk the same triangle list with nearly the same rays.
+// 1. Every interior cell: the reset of body 0, the bounding-box test, and a
+//    count of the cells in each bucket column.
+__global__ void __launch_bounds__(256) k_ibm_select(IbmArgs A, int *key, int *count) {
   const Geom &g = A.g;
   const int ni = g.mx - 2, nj = g.my - 2;
   const size_t cells = (size_t)ni * nj * (g.mz - 2);
@@ -98,21 +102,87 @@ __global__ void __launch_bounds__(128) k_ibm_inside(IbmArgs A) {
   const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = 1 + (int)(t / ((size_t)ni * nj));
   const size_t q = ((size_t)k * g.my + j) * g.mx + i;
   double nv = A.nvert[q];
-  if (A.ibi == 0 && nv < 5.) nv = 0;
+  if (A.ibi == 0 && nv < 5.) {
+    nv = 0;
+    A.nvert[q] = nv;
+  }
   const double *c = A.cent + 3 * q;
+  int col = -1;
   if (c[0] > A.min[0] && c[0] < A.max[0] && c[1] > A.min[1] && c[1] < A.max[1] && c[2] > A.min[2] &&
       c[2] < A.max[2]) {
     const int ic = (int)floor(__ddiv_rn(is_(c[0], A.min[0]), A.dc[0]));
-    const int jc = (int)floor(__ddiv_rn(is_(c[1], A.min[1]), A.dc[1]));
     const int kc = (int)floor(__ddiv_rn(is_(c[2], A.min[2]), A.dc[2]));
-    const int r = ibm_point_inside(A, c, ic, jc, kc);
-    if (r < 0) {
-      atomicOr(A.failed, 1);
-    } else {
-      if (nv < r) nv = r;
-      if (nv < 0) nv = 0;
+    col = kc * kIbmBuckets + ic;
+    atomicAdd(count + col, 1);
+  }
+  key[t] = col;
+}
+
+// 2. Start of each column's run in the cell list (exclusive scan of the counts;
+//    one block, kIbmBuckets^2 columns).  fill[] is zeroed for pass 3.
+__global__ void __launch_bounds__(1024) k_ibm_scan(const int *count, int *start, int *fill) {
+  constexpr int ncol = kIbmBuckets * kIbmBuckets, per = (ncol + 1023) / 1024;
+  __shared__ int part[1024];
+  const int t = threadIdx.x;
+  int local = 0;
+  for (int u = 0; u < per; u++) {
+    const int c = t * per + u;
+    if (c < ncol) local += count[c];
+  }
+  part[t] = local;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan of the per-thread sums
+    const int v = t >= o ? part[t - o] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = part[t] - local;
+  for (int u = 0; u < per; u++) {
+    const int c = t * per + u;
+    if (c < ncol) {
+      start[c] = run;
+      fill[c] = 0;
+      run += count[c];
     }
   }
+}
+
+// 3. Each selected cell takes a slot in its column's run.
+__global__ void __launch_bounds__(256) k_ibm_scatter(Geom g, const int *key, const int *start, int *fill, int *list) {
+  const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cells) return;
+  const int col = key[t];
+  if (col >= 0) list[start[col] + atomicAdd(fill + col, 1)] = (int)t;
+}
+
+__global__ void k_ibm_total(const int *start, const int *count, int *total) {
+  constexpr int last = kIbmBuckets * kIbmBuckets - 1;
+  *total = start[last] + count[last];
+}
+
+// 4. The ray cast of every listed cell (interior-cell number t).
+__global__ void __launch_bounds__(128) k_ibm_inside(IbmArgs A, const int *list, const int *nlisted) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= *nlisted) return;
+  const Geom &g = A.g;
+  const int ni = g.mx - 2, nj = g.my - 2;
+  const size_t t = (size_t)list[s];
+  const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = 1 + (int)(t / ((size_t)ni * nj));
+  const size_t q = ((size_t)k * g.my + j) * g.mx + i;
+  const double *c = A.cent + 3 * q;
+  const int ic = (int)floor(__ddiv_rn(is_(c[0], A.min[0]), A.dc[0]));
+  const int jc = (int)floor(__ddiv_rn(is_(c[1], A.min[1]), A.dc[1]));
+  const int kc = (int)floor(__ddiv_rn(is_(c[2], A.min[2]), A.dc[2]));
+  const int r = ibm_point_inside(A, c, ic, jc, kc);
+  if (r < 0) {
+    atomicOr(A.failed, 1);
+    return;
+  }
+  double nv = A.nvert[q];
+  if (nv < r) nv = r;
+  if (nv < 0) nv = 0;
   A.nvert[q] = nv;
 }
 
@@ -169,11 +239,23 @@ __global__ void k_ibm_around(Geom g, double *nvert) {
     }
 }
 
-void launch_ibm_search(const IbmArgs &A, double *tmp, cudaStream_t s) {
+void launch_ibm_search(const IbmArgs &A, const IbmWork &W, double *tmp, cudaStream_t s) {
   const Geom &g = A.g;
   const size_t inner = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2), n = g.n();
   if (inner) {
-    k_ibm_inside<<<nblk(inner, 128), 128, 0, s>>>(A);
+    constexpr int ncol = kIbmBuckets * kIbmBuckets;
+    cudaMemsetAsync(W.count, 0, sizeof(int) * ncol, s);
+    k_ibm_select<<<nblk(inner, 256), 256, 0, s>>>(A, W.key, W.count);
+    count_launch();
+    k_ibm_scan<<<1, 1024, 0, s>>>(W.count, W.start, W.fill);
+    count_launch();
+    k_ibm_scatter<<<nblk(inner, 256), 256, 0, s>>>(g, W.key, W.start, W.fill, W.list);
+    count_launch();
+    // the number of listed cells is the last column's start + count; read on
+    // the device, so the grid covers every interior cell and threads past it return
+    k_ibm_total<<<1, 1, 0, s>>>(W.start, W.count, W.total);
+    count_launch();
+    k_ibm_inside<<<nblk(inner, 128), 128, 0, s>>>(A, W.list, W.total);
     count_launch();
   }
   k_ibm_layer<<<nblk(n, 256), 256, 0, s>>>(g, A.nvert, tmp);
