@@ -1592,7 +1592,7 @@ int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz,
   if (!rc) { bufs[7] = d_ent; rc = dalloc(ctx, &d_flag, 1); }
   // key and list per interior cell, count / start / fill per column, a total
   const size_t inner = (size_t)(F.g.mx - 2) * (F.g.my - 2) * (F.g.mz - 2);
-  if (!rc) { bufs[8] = d_flag; rc = dalloc(ctx, &d_work, 2 * inner + 3 * (size_t)ncol + 1); }
+  if (!rc) { bufs[8] = d_flag; rc = dalloc(ctx, &d_work, 2 * inner + 3 * (size_t)ncol + 1 + (n + 3) / 4); }
   if (rc) {
     release();
     return rc;
@@ -1605,6 +1605,7 @@ int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz,
   W.start = W.count + ncol;
   W.fill = W.start + ncol;
   W.total = W.fill + ncol;
+  W.in4 = reinterpret_cast<unsigned char *>(W.total + 1);
   cudaStream_t s = ctx->stream;
   if (cent) CK(cudaMemcpyAsync(d_cent, cent, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d_nv, nvert, sizeof(double) * n, cudaMemcpyHostToDevice, s));

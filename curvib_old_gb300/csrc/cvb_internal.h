@@ -256,9 +256,11 @@ struct IbmArgs {
   int *failed;                   // set when a cell found no usable ray
 };
 // Work arrays of the search: per interior cell its bucket column (key) and
-// the cell list sorted by column (list); per column its count, start and fill.
+// the cell list sorted by column (list); per column its count, start and fill;
+// per cell of the box a byte marking inside cells (in4).
 struct IbmWork {
   int *key, *list, *count, *start, *fill, *total;
+  unsigned char *in4;
 };
 // The search; tmp is one more [mz][my][mx] array.  The result is left in tmp.
 void launch_ibm_search(const IbmArgs &A, const IbmWork &W, double *tmp, cudaStream_t s);
