@@ -1561,11 +1561,18 @@ int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz,
         }
     }
   }
+  // per triangle: v0, the edges v1 - v0 and v2 - v0 (the subtractions the ray
+  // test would repeat for every ray), the unit normal
   std::vector<double> tdata(12 * (size_t)n_elmt);
   for (int e = 0; e < n_elmt; e++) {
-    for (int v = 0; v < 3; v++)
-      for (int c = 0; c < 3; c++) tdata[12 * (size_t)e + 3 * v + c] = xyz[3 * tri[3 * e + v] + c];
-    for (int c = 0; c < 3; c++) tdata[12 * (size_t)e + 9 + c] = nf[3 * e + c];
+    const double *v0 = xyz + 3 * tri[3 * e], *v1 = xyz + 3 * tri[3 * e + 1], *v2 = xyz + 3 * tri[3 * e + 2];
+    double *T = tdata.data() + 12 * (size_t)e;
+    for (int c = 0; c < 3; c++) {
+      T[c] = v0[c];
+      T[3 + c] = v1[c] - v0[c];
+      T[6 + c] = v2[c] - v0[c];
+      T[9 + c] = nf[3 * e + c];
+    }
   }
   double off[kIbmMaxTries];
   cvb_ibm_ray_offsets(kIbmMaxTries, off);

@@ -246,7 +246,7 @@ struct IbmArgs {
   double min[3], max[3], dc[3];  // bounding box and bucket size
   const int *col_start;          // bucket column (i, k) = k * kIbmBuckets + i -> its entries
   const int2 *col_ent;           // (triangle, end of the triangle's bucket range in j)
-  const double *tri;             // per triangle: v0, v1, v2, unit normal (12 doubles)
+  const double *tri;             // per triangle: v0, v1 - v0, v2 - v0, unit normal (12 doubles)
   const double *offsets;         // ray offset of seeds 1 .. tries (randomdirection's s)
   int tries;
   const double *cent;            // cell centres, [mz][my][mx][3]

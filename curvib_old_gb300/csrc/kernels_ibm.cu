@@ -17,21 +17,26 @@ __device__ __forceinline__ double idot(const double *a, const double *b) {
 }
 
 // intsect_triangle (compgeom.c:17-50): the ray o + t d against the triangle
-// (v0, v1, v2); 1 with t on a hit.
-__device__ __forceinline__ int ray_hits(const double *o, const double *d, const double *v0, const double *v1,
-                                        const double *v2, double *t) {
-  double e1[3], e2[3], pv[3], tv[3], qv[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) { e1[c] = is_(v1[c], v0[c]); e2[c] = is_(v2[c], v0[c]); }
+// (v0, v0 + e1, v0 + e2); 1 with t on a hit.  The edges e1 = v1 - v0 and
+// e2 = v2 - v0 come precomputed (the same IEEE subtractions).  The test u < 0,
+// with u = (tv . pv) * (1 / det), is decided from the signs before dividing when
+// the product cannot underflow to -0 (|tv . pv| >= 2^-1000, |det| <= 2^20):
+// a nonzero product has the sign of its factors, so the decision is the
+// reference's.  Everything else is computed as the reference computes it.
+__device__ __forceinline__ int ray_hits(const double *o, const double *d, const double *v0, const double *e1,
+                                        const double *e2, double *t) {
+  double pv[3], tv[3], qv[3];
   pv[0] = is_(im_(d[1], e2[2]), im_(d[2], e2[1]));
   pv[1] = is_(im_(d[2], e2[0]), im_(d[0], e2[2]));
   pv[2] = is_(im_(d[0], e2[1]), im_(d[1], e2[0]));
   const double det = idot(e1, pv);
   if (det > -0.00000001 && det < 0.00000001) return 0;
-  const double inv = __ddiv_rn(1.0, det);
 #pragma unroll
   for (int c = 0; c < 3; c++) tv[c] = is_(o[c], v0[c]);
-  const double u = im_(idot(tv, pv), inv);
+  const double nu = idot(tv, pv);
+  if (fabs(nu) >= 0x1p-1000 && fabs(det) <= 0x1p20 && ((nu < 0.0) != (det < 0.0))) return 0;
+  const double inv = __ddiv_rn(1.0, det);
+  const double u = im_(nu, inv);
   if (u < 0.0 || u > 1.0) return 0;
   qv[0] = is_(im_(tv[1], e1[2]), im_(tv[2], e1[1]));
   qv[1] = is_(im_(tv[2], e1[0]), im_(tv[0], e1[2]));
@@ -71,7 +76,7 @@ __device__ int ibm_point_inside(const IbmArgs &A, const double *p, int ic, int j
     for (int q = q0; q < q1 && !singular; q++) {
       const int2 ent = A.col_ent[q];  // (triangle, end of its bucket range in j)
       if (ent.y <= jc) continue;
-      const double *T = A.tri + 12 * (size_t)ent.x;  // v0, v1, v2, unit normal
+      const double *T = A.tri + 12 * (size_t)ent.x;  // v0, e1, e2, unit normal
       double t;
       if (!ray_hits(p, d, T, T + 3, T + 6, &t)) continue;
       if (!(t > 0)) continue;
