@@ -205,6 +205,32 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
  * the centres an earlier call uploaded (they stay on the device). */
 int cvb_ibm_search(cvb_ctx *ctx, const double *cent, int n_v, const double *xyz, int n_elmt, const int *tri,
                    const double *nf, int ibi, int nbodies, const double *nvert_o, double *nvert);
+/* --- files on either side of the path (host only, no context) ------------ */
+/* PETSc binary vectors as VecView writes and VecLoad reads them: the int32
+ * class id 1211214, the int32 length n, then n IEEE doubles, all big-endian;
+ * with block_size > 1 also "<path>.info" holding "-vecload_block_size <bs>".
+ * A one-rank DMDA vector is written in its [k][j][i] order. */
+int cvb_petsc_vec_write(const char *path, const double *v, long long n, int block_size);
+int cvb_petsc_vec_size(const char *path, long long *n);
+/* CVB_BAD_INPUT unless the file holds a vector of exactly n values. */
+int cvb_petsc_vec_read(const char *path, double *v, long long n);
+/* The restart set of Ucont_P_Binary_Output / _Input (main.c:75-467) for step ti
+ * and block: nvfield (Nvert), vfield (Ucont), ufield (Ucat), pfield (P), each
+ * "<dir>/<name>%05d_%1d.dat" over a box of ncells cells.  NULL arrays are
+ * skipped.  The read side fills Ucont, P and Nvert_o, as _Input does. */
+int cvb_restart_write(const char *dir, int ti, int block, long long ncells, const double *nvert, const double *ucont,
+                      const double *ucat, const double *p);
+int cvb_restart_read(const char *dir, int ti, int block, long long ncells, double *ucont, double *p,
+                     double *nvert_o);
+/* grid.dat as MG_Initial reads it (init.c:339-349, 606-735): the block count,
+ * then per block "IM JM KM" and its nodes: all x, then all y, then all z in
+ * [k][j][i] order, or with grid1d IM + JM + KM lines of "x y z" (one component
+ * used per line).  Fills IM, JM, KM of the given block and, when coords is not
+ * NULL, its node coordinates [KM][JM][IM][3] scaled as the reference does,
+ * c / cl * l_dim; capacity is coords' length in doubles. */
+int cvb_grid_dat_read(const char *path, int block, int grid1d, double cl, double l_dim, int *IM, int *JM, int *KM,
+                      double *coords, long long capacity);
+
 /* randomdirection's ray offsets for seeds 1 .. n (srand(seed); rand() scaled to
  * [-0.5, 0.5), ibm.c:101-104), from a private generator state: the caller's
  * rand() sequence is not disturbed.  Needs no context or GPU. */

@@ -1,0 +1,146 @@
+"""The files on either side of the path (libcvb, host only, no GPU): PETSc
+binary vectors as VecView writes them, the restart set of
+Ucont_P_Binary_Output / _Input (main.c:75-467), and grid.dat as MG_Initial
+reads it (init.c:606-735).  The vector files are checked byte for byte
+against PETSc's published binary layout, packed here independently with
+struct; no reference-written files exist to compare with."""
+import ctypes
+import struct
+
+import numpy as np
+import pytest
+
+from curvib_old_gb300 import _lib
+
+CLASSID = 1211214
+
+
+@pytest.fixture(scope="module")
+def L():
+    from curvib_old_gb300 import build
+    build.build()
+    return _lib.lib()
+
+
+def _b(p):
+    return str(p).encode()
+
+
+def test_vector_file_layout_and_round_trip(L, tmp_path):
+    v = np.random.default_rng(3).standard_normal(3 * 70)
+    v[5] = -0.0
+    v[6] = np.inf
+    path = tmp_path / "vfield00007_0.dat"
+    assert L.cvb_petsc_vec_write(_b(path), _lib.ptr(v), v.size, 3) == 0
+    raw = path.read_bytes()
+    assert raw == struct.pack(">ii", CLASSID, v.size) + struct.pack(f">{v.size}d", *v)
+    assert (tmp_path / "vfield00007_0.dat.info").read_text() == "-vecload_block_size 3\n"
+    n = ctypes.c_longlong()
+    assert L.cvb_petsc_vec_size(_b(path), ctypes.byref(n)) == 0 and n.value == v.size
+    back = np.empty_like(v)
+    assert L.cvb_petsc_vec_read(_b(path), _lib.ptr(back), v.size) == 0
+    assert back.tobytes() == v.tobytes()  # bit for bit, -0.0 and inf included
+
+
+def test_vector_file_written_elsewhere_is_read(L, tmp_path):
+    v = np.linspace(-1.0, 2.0, 11)
+    path = tmp_path / "pfield00000_0.dat"
+    path.write_bytes(struct.pack(">ii", CLASSID, v.size) + struct.pack(f">{v.size}d", *v))
+    out = np.zeros_like(v)
+    assert L.cvb_petsc_vec_read(_b(path), _lib.ptr(out), v.size) == 0
+    assert np.array_equal(out, v)
+    assert not (tmp_path / "pfield00000_0.dat.info").exists()
+
+
+def test_vector_file_refusals(L, tmp_path):
+    out = np.zeros(4)
+    bad = tmp_path / "bad.dat"
+    bad.write_bytes(struct.pack(">ii", 1211215, 4) + bytes(32))
+    assert L.cvb_petsc_vec_read(_b(bad), _lib.ptr(out), 4) == 4
+    short = tmp_path / "short.dat"
+    short.write_bytes(struct.pack(">ii", CLASSID, 4) + bytes(24))
+    assert L.cvb_petsc_vec_read(_b(short), _lib.ptr(out), 4) == 4
+    good = tmp_path / "good.dat"
+    good.write_bytes(struct.pack(">ii", CLASSID, 4) + bytes(32))
+    assert L.cvb_petsc_vec_read(_b(good), _lib.ptr(out), 5) == 4  # length differs
+    assert L.cvb_petsc_vec_read(_b(tmp_path / "missing.dat"), _lib.ptr(out), 4) == 4
+
+
+def test_restart_set_names_and_round_trip(L, tmp_path):
+    shape = (6, 5, 7)
+    n = int(np.prod(shape))
+    rng = np.random.default_rng(9)
+    nvert, p = rng.random(shape), rng.standard_normal(shape)
+    ucont, ucat = rng.standard_normal(shape + (3,)), rng.standard_normal(shape + (3,))
+    assert L.cvb_restart_write(_b(tmp_path), 12, 0, n, _lib.ptr(nvert), _lib.ptr(ucont), _lib.ptr(ucat),
+                               _lib.ptr(p)) == 0
+    names = sorted(f.name for f in tmp_path.iterdir())
+    assert names == ["nvfield00012_0.dat", "pfield00012_0.dat", "ufield00012_0.dat", "ufield00012_0.dat.info",
+                     "vfield00012_0.dat", "vfield00012_0.dat.info"]
+    u2, p2, nv2 = np.zeros_like(ucont), np.zeros_like(p), np.zeros_like(nvert)
+    assert L.cvb_restart_read(_b(tmp_path), 12, 0, n, _lib.ptr(u2), _lib.ptr(p2), _lib.ptr(nv2)) == 0
+    assert np.array_equal(u2, ucont) and np.array_equal(p2, p) and np.array_equal(nv2, nvert)
+    assert L.cvb_restart_read(_b(tmp_path), 13, 0, n, _lib.ptr(u2), None, None) == 4  # no such step
+
+
+def _grid_file(path, blocks, grid1d=False):
+    lines = [str(len(blocks))]
+    for nodes in blocks:
+        KM, JM, IM = nodes.shape[:3]
+        lines.append(f"{IM} {JM} {KM}")
+        if grid1d:
+            for i in range(IM):
+                lines.append(f"{float(nodes[0, 0, i, 0])!r} 0.0 0.0")
+            for j in range(JM):
+                lines.append(f"0.0 {float(nodes[0, j, 0, 1])!r} 0.0")
+            for k in range(KM):
+                lines.append(f"0.0 0.0 {float(nodes[k, 0, 0, 2])!r}")
+        else:
+            for c in range(3):
+                lines.extend(repr(float(x)) for x in nodes[..., c].ravel())
+    path.write_text("\n".join(lines) + "\n")
+
+
+def _read(L, path, block, grid1d, cl, ldim):
+    im, jm, km = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert L.cvb_grid_dat_read(_b(path), block, grid1d, cl, ldim, ctypes.byref(im), ctypes.byref(jm),
+                               ctypes.byref(km), None, 0) == 0
+    out = np.zeros((km.value, jm.value, im.value, 3))
+    assert L.cvb_grid_dat_read(_b(path), block, grid1d, cl, ldim, ctypes.byref(im), ctypes.byref(jm),
+                               ctypes.byref(km), _lib.ptr(out), out.size) == 0
+    return out
+
+
+def test_grid_dat_blocks_and_scaling(L, tmp_path):
+    from curvib_old_gb300 import workload as W
+    a = W.box_nodes((6, 4, 5), (1.0, 2.0, 0.5), 2.0, True)
+    b = W.box_nodes((3, 7, 4), (2.0, 1.0, 1.0), 1.5, True)
+    path = tmp_path / "grid.dat"
+    _grid_file(path, [a, b])
+    assert np.array_equal(_read(L, path, 0, 0, 1.0, 1.0), a)
+    cl, ldim = 0.3, 1.7
+    assert np.array_equal(_read(L, path, 1, 0, cl, ldim), b / cl * ldim)
+    im = ctypes.c_int()
+    assert L.cvb_grid_dat_read(_b(path), 2, 0, 1.0, 1.0, ctypes.byref(im), ctypes.byref(im), ctypes.byref(im),
+                               None, 0) == 4
+    small = np.zeros(3)
+    assert L.cvb_grid_dat_read(_b(path), 0, 0, 1.0, 1.0, ctypes.byref(im), ctypes.byref(im), ctypes.byref(im),
+                               _lib.ptr(small), small.size) == 4
+
+
+def test_grid_dat_one_dimensional_form(L, tmp_path):
+    x, y, z = np.linspace(0, 1, 5), np.linspace(0, 2, 4) ** 1.5, np.linspace(-1, 1, 3)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    nodes = np.stack([X, Y, Z], axis=-1)
+    path = tmp_path / "grid1d.dat"
+    _grid_file(path, [nodes], grid1d=True)
+    assert np.array_equal(_read(L, path, 0, 1, 1.0, 1.0), nodes)
+
+
+def test_grid_dat_malformed(L, tmp_path):
+    path = tmp_path / "grid.dat"
+    path.write_text("1\n3 3 3\n0.0 1.0 oops\n")
+    im = ctypes.c_int()
+    out = np.zeros(81)
+    assert L.cvb_grid_dat_read(_b(path), 0, 0, 1.0, 1.0, ctypes.byref(im), ctypes.byref(im), ctypes.byref(im),
+                               _lib.ptr(out), out.size) == 4
