@@ -1,7 +1,7 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE ONLY.
 # Compiles the reference's own poisson.c, metrics.c, implicitsolver.c, rhs.c,
-# bcs.c, ibm.c, compgeom.c and variables.c, where they lie under the reference
+# bcs.c, ibm.c, compgeom.c, variables.c and init.c, where they lie under the reference
 # checkout, unmodified, against the
 # single-process PETSc API shim in oracle/petsc_shim/, into
 # oracle/_ref/libcvbref.so.  In the objects of rhs.c and bcs.c, Contra2Cart and
@@ -26,7 +26,7 @@ mkdir -p "$OUT"
 CC="${CC:-gcc}"
 CFLAGS="-std=gnu99 -O2 -fPIC -w -I$HERE/petsc_shim/include -I$REF"
 objs=()
-for f in poisson metrics implicitsolver rhs bcs compgeom variables; do
+for f in poisson metrics implicitsolver rhs bcs compgeom variables init; do
   $CC $CFLAGS -c "$REF/$f.c" -o "$OUT/ref_$f.o"
   objs+=("$OUT/ref_$f.o")
 done

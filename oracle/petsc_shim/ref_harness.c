@@ -14,6 +14,7 @@
  * 3-vectors interleaved (x,y,z), i.e. exactly a PETSc global vector.
  */
 #include "variables.h"
+#include <unistd.h>
 
 /* Globals the reference sources expect main.c to define. */
 PetscInt block_number = 1, immersed = 0, MHV = 0, LV = 0, ti = 0, tistart = 0;
@@ -472,4 +473,44 @@ int ref_ibm_search(int n_v, const double *xyz, int n_elmt, const int *nv, const 
   copy_owned(u, u->Nvert, 1, nvert, 0);
   /* the interpolation list stays with the harness (test-only: leaks are harmless) */
   return rc;
+}
+
+/* MG_Initial (init.c:296-1060) run in dir, which holds its grid.dat and
+ * bcs.dat (one block): the node coordinates it leaves on the finest level,
+ * [KM][JM][IM][3], for the grid.dat reader's pinning.  -mg_level, -grid1d and
+ * -chact_leng are set as given; L_dim is main.c's global. */
+PetscErrorCode MG_Initial(UserMG *usermg, IBMNodes *ibm);
+PetscReal L_dim = 1.0; /* main.c's length scale of grid.dat's coordinates */
+int ref_mg_initial_nodes(const char *dir, int nlevels, int grid1d, double cl, double l_dim, int *IM, int *JM,
+                         int *KM, double *coords, long long cap) {
+  char cwd[4096], val[64];
+  if (!getcwd(cwd, sizeof cwd) || chdir(dir)) return 1;
+  PetscOptionsClear();
+  snprintf(val, sizeof val, "%d", nlevels); PetscOptionsSetValue("-mg_level", val);
+  snprintf(val, sizeof val, "%d", grid1d); PetscOptionsSetValue("-grid1d", val);
+  snprintf(val, sizeof val, "%.17g", cl); PetscOptionsSetValue("-chact_leng", val);
+  L_dim = l_dim;
+  block_number = 1;
+  static UserMG mg;
+  memset(&mg, 0, sizeof mg);
+  IBMNodes *ibm = (IBMNodes *)calloc(1, sizeof(IBMNodes));
+  int rc = MG_Initial(&mg, ibm);
+  if (chdir(cwd)) rc = rc ? rc : 2;
+  PetscOptionsClear();
+  if (rc) return rc;
+  UserCtx *u = &mg.mgctx[mg.mglevels - 1].user[0];
+  *IM = u->IM; *JM = u->JM; *KM = u->KM;
+  if ((long long)3 * u->IM * u->JM * u->KM > cap) return 3;
+  Vec Coor;
+  Cmpnts ***coor;
+  DMGetCoordinatesLocal(u->da, &Coor);
+  DMDAVecGetArray(u->fda, Coor, &coor);
+  for (int k = 0; k < u->KM; k++)
+    for (int j = 0; j < u->JM; j++)
+      for (int i = 0; i < u->IM; i++) {
+        double *c = coords + 3 * (((size_t)k * u->JM + j) * u->IM + i);
+        c[0] = coor[k][j][i].x; c[1] = coor[k][j][i].y; c[2] = coor[k][j][i].z;
+      }
+  DMDAVecRestoreArray(u->fda, Coor, &coor);
+  return 0;
 }

@@ -144,3 +144,31 @@ def test_grid_dat_malformed(L, tmp_path):
     out = np.zeros(81)
     assert L.cvb_grid_dat_read(_b(path), 0, 0, 1.0, 1.0, ctypes.byref(im), ctypes.byref(im), ctypes.byref(im),
                                _lib.ptr(out), out.size) == 4
+
+
+@pytest.mark.parametrize("grid1d", [0, 1])
+def test_grid_dat_matches_reference_mg_initial(L, tmp_path, grid1d):
+    """The reference's own MG_Initial (init.c:296-1060, compiled against the
+    oracle's PETSc shim) reads the same grid.dat to the same node coordinates,
+    bit for bit, with the cl / L_dim scaling."""
+    from oracle import oracle as O
+    if not (O.REF_DIR / "init.c").exists():
+        pytest.skip("reference checkout not present")
+    from curvib_old_gb300 import workload as W
+    ref = ctypes.CDLL(str(O.build_reference()))
+    if grid1d:
+        x, y, z = np.linspace(0, 1.3, 9), np.linspace(0, 2, 7) ** 1.5, np.linspace(-1, 1, 11)
+        Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+        nodes = np.stack([X, Y, Z], axis=-1)
+    else:
+        nodes = W.box_nodes((8, 6, 10), (1.0, 2.0, 0.5), 2.0, True)
+    _grid_file(tmp_path / "grid.dat", [nodes], grid1d=bool(grid1d))
+    (tmp_path / "bcs.dat").write_text("1 1 1 1 1 1\n")
+    cl, ldim = 0.3, 1.7
+    got = np.zeros(nodes.size)
+    im, jm, km = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert ref.ref_mg_initial_nodes(_b(tmp_path), 2, grid1d, ctypes.c_double(cl), ctypes.c_double(ldim),
+                                    ctypes.byref(im), ctypes.byref(jm), ctypes.byref(km),
+                                    got.ctypes.data_as(ctypes.c_void_p), ctypes.c_longlong(got.size)) == 0
+    assert (km.value, jm.value, im.value) == nodes.shape[:3]
+    assert np.array_equal(_read(L, tmp_path / "grid.dat", 0, grid1d, cl, ldim).ravel(), got)
