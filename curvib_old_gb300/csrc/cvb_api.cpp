@@ -1481,6 +1481,32 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
   return CVB_OK;
 }
 
+int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long *at) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!maxdiv || !at) return fail(ctx, CVB_BAD_INPUT, "maxdiv/at is NULL");
+  const int l = ctx->nlevels - 1;
+  LevelDev &F = ctx->L[l];
+  const size_t n = F.g.n();
+  if (ucont) CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  // 1024 partial (value, index) pairs and the result, from the pool for this call
+  double *pv = nullptr;
+  TRY(dalloc(ctx, &pv, 2 * 1024 + 2));
+  long long *pi = reinterpret_cast<long long *>(pv + 1024);
+  double *out = pv + 2048;
+  launch_divergence(F.g, ctx->uc_dev, ctx->aj64[l], F.nvert, pv, pi, out, reinterpret_cast<long long *>(out + 1),
+                    ctx->stream);
+  double h[2];
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  dfree(ctx, pv);
+  if (e != cudaSuccess) return fail(ctx, CVB_CUDA_ERROR, "divergence: %s", cudaGetErrorString(e));
+  *maxdiv = h[0];
+  std::memcpy(at, h + 1, sizeof(long long));
+  return CVB_OK;
+}
+
 // randomdirection's ray offsets (ibm.c:101-104): the first rand() after
 // srand(seed), scaled to [-0.5, 0.5), for seeds 1 .. n.  They are drawn from a
 // private generator state (initstate / random / setstate; in glibc rand() is

@@ -267,6 +267,10 @@ void launch_ibm_search(const IbmArgs &A, const IbmWork &W, double *tmp, cudaStre
 
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
                         const double *nvert, const double *ucont, double *ucat, cudaStream_t s);
+// max |div| and its first box index into out_v / out_i (device); pv / pi
+// hold 1024 partial pairs
+void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
+                       long long *pi, double *out_v, long long *out_i, cudaStream_t s);
 // bc: the level's bctype[6]; the host has refused the types it does not cover
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
                                 const double *zet, double *ubcs, double *ucat, cudaStream_t s);

@@ -1,7 +1,7 @@
 // The steps that follow the flux correction in the reference's Projection
 // (poisson.c:2897-2904): Contra2Cart (rhs.c:25-143), the Cartesian velocity at
 // the cell centres, and GhostNodeVelocity (bcs.c:3645-4435), its values on the
-// boundary ring.  FP64 with every operation rounded on its own, in the
+// boundary ring; and Divergence (main.c:469-593), the check after them.  FP64 with every operation rounded on its own, in the
 // reference's order (no fused multiply-add), so results equal the reference's
 // bit for bit.  Arrays are the finest level's [mz][my][mx] box, Cmpnts
 // interleaved.
@@ -65,6 +65,79 @@ void launch_contra2cart(const Geom &g, const double *csi, const double *eta, con
   const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
   if (!cells) return;
   k_contra2cart<<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, nvert, ucont, ucat);
+  count_launch();
+}
+
+// Divergence (main.c:469-593), the check Flow_Solver runs after Projection:
+// |(the cell's three flux differences) * aj| on interior cells, 0 where the
+// cell and its face neighbours' nvert sum above 0.1 and on the ring, and the
+// maximum with its first index, as VecMax scans for it.  The divergences are
+// >= 0, so the pair (largest value, smallest index among equals) is the same
+// whatever the reduction order; a NaN never compares greater, as in the scan.
+constexpr int kDivThreads = 256, kDivBlocks = 1024;
+
+__device__ __forceinline__ void div_better(double &m, long long &at, double v, long long i) {
+  if (v > m || (v == m && i < at)) { m = v; at = i; }
+}
+
+__device__ __forceinline__ void div_block_reduce(double m, long long at, double *sv, long long *si) {
+  const int t = threadIdx.x;
+  sv[t] = m; si[t] = at;
+  __syncthreads();
+  for (int o = kDivThreads / 2; o > 0; o >>= 1) {
+    if (t < o) {
+      double a = sv[t];
+      long long ai = si[t];
+      div_better(a, ai, sv[t + o], si[t + o]);
+      sv[t] = a; si[t] = ai;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kDivThreads) k_divergence(Geom g, const double *__restrict__ uc,
+                                                          const double *__restrict__ aj,
+                                                          const double *__restrict__ nv, double *pv, long long *pi) {
+  __shared__ double sv[kDivThreads];
+  __shared__ long long si[kDivThreads];
+  double m = -HUGE_VAL;
+  long long at = -1;
+  const size_t n = g.n(), plane = (size_t)g.mx * g.my;
+  for (size_t p = (size_t)blockIdx.x * kDivThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kDivThreads) {
+    const int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / plane);
+    double d = 0.0;
+    if (i > 0 && i < g.mx - 1 && j > 0 && j < g.my - 1 && k > 0 && k < g.mz - 1) {
+      const size_t w = p - 1, s = p - g.mx, b = p - plane;
+      // ((((ux - ux_w) + uy) - uy_s) + uz) - uz_b, left to right as the C
+      const double sum =
+          ds(da(ds(da(ds(uc[3 * p], uc[3 * w]), uc[3 * p + 1]), uc[3 * s + 1]), uc[3 * p + 2]), uc[3 * b + 2]);
+      d = fabs(dm(sum, aj[p]));
+      const double ns = da(da(da(da(da(da(nv[p], nv[p + plane]), nv[p - plane]), nv[p + g.mx]), nv[p - g.mx]),
+                              nv[p + 1]), nv[p - 1]);
+      if (ns > 0.1) d = 0.;
+    }
+    div_better(m, at, d, (long long)p);
+  }
+  div_block_reduce(m, at, sv, si);
+  if (threadIdx.x == 0) { pv[blockIdx.x] = sv[0]; pi[blockIdx.x] = si[0]; }
+}
+
+__global__ void __launch_bounds__(kDivThreads) k_divergence_final(const double *pv, const long long *pi, int nb,
+                                                                double *out_v, long long *out_i) {
+  __shared__ double sv[kDivThreads];
+  __shared__ long long si[kDivThreads];
+  double m = -HUGE_VAL;
+  long long at = -1;
+  for (int b = threadIdx.x; b < nb; b += kDivThreads) div_better(m, at, pv[b], pi[b]);
+  div_block_reduce(m, at, sv, si);
+  if (threadIdx.x == 0) { *out_v = sv[0]; *out_i = si[0]; }
+}
+
+void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
+                       long long *pi, double *out_v, long long *out_i, cudaStream_t s) {
+  k_divergence<<<kDivBlocks, kDivThreads, 0, s>>>(g, ucont, aj, nvert, pv, pi);
+  count_launch();
+  k_divergence_final<<<1, kDivThreads, 0, s>>>(pv, pi, kDivBlocks, out_v, out_i);
   count_launch();
 }
 

@@ -190,6 +190,14 @@ class PoissonContext:
         self._check(self._L.cvb_ghost_node_velocity(self._ctx, ptr(ub), ptr(u)))
         return ub, u
 
+    def divergence(self, ucont=None):
+        """Divergence (main.c:469): (max |div|, its index in the box); ucont None
+        uses the device copy the last projection left."""
+        m, at = ctypes.c_double(), ctypes.c_longlong()
+        self._check(self._L.cvb_divergence(self._ctx, None if ucont is None else ptr(_c64(ucont)), ctypes.byref(m),
+                                           ctypes.byref(at)))
+        return m.value, at.value
+
     def ibm_search(self, cent, xyz, tri, nf, ibi, nbodies, nvert_o, nvert):
         """ibm_search_advanced's nvert classification (ibm.c:4197): returns the
         new nvert ([mz][my][mx]) of body ibi of nbodies.  cent None reuses the

@@ -15,6 +15,7 @@
  *                                          Contra2Cart and GhostNodeVelocity)
  *   Contra2Cart       (rhs.c:25)        -> cvb_contra2cart
  *   GhostNodeVelocity (bcs.c:3645)      -> cvb_ghost_node_velocity
+ *   Divergence        (main.c:469)      -> cvb_divergence
  *   ibm_search_advanced (ibm.c:4197), its nvert classification
  *                                       -> cvb_ibm_search
  *
@@ -188,6 +189,13 @@ int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat);
  * call, each array copied in and out once. */
 int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,
                         double *ucat);
+/* Divergence (main.c:469-593), the check Flow_Solver runs after Projection
+ * (solvers.c:1084): the largest |(the cell's three flux differences) * aj|
+ * over the interior cells, 0 where nvert of the cell and its face neighbours
+ * sums above 0.1, and its index in the [mz][my][mx] box (the first one, as
+ * VecMax).  ucont NULL uses the context's device copy of Ucont as the last
+ * projection or VolumeFlux_rev left it. */
+int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long *at);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
  * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and

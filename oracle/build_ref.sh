@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE ONLY.
 # Compiles the reference's own poisson.c, metrics.c, implicitsolver.c, rhs.c,
-# bcs.c, ibm.c, compgeom.c, variables.c and init.c, where they lie under the reference
+# bcs.c, ibm.c, compgeom.c, variables.c, init.c and (for Divergence) main.c,
+# where they lie under the reference
 # checkout, unmodified, against the
 # single-process PETSc API shim in oracle/petsc_shim/, into
 # oracle/_ref/libcvbref.so.  In the objects of rhs.c and bcs.c, Contra2Cart and
@@ -30,6 +31,12 @@ for f in poisson metrics implicitsolver rhs bcs compgeom variables init; do
   $CC $CFLAGS -c "$REF/$f.c" -o "$OUT/ref_$f.o"
   objs+=("$OUT/ref_$f.o")
 done
+# main.c holds Divergence (main.c:469) beside main() and the globals the
+# harness defines itself: every symbol of its object but Divergence is made
+# local, so only that routine joins the library.
+$CC $CFLAGS -c "$REF/main.c" -o "$OUT/ref_main.o"
+objcopy --keep-global-symbol=Divergence "$OUT/ref_main.o"
+objs+=("$OUT/ref_main.o")
 # ibm.c declares point_cell_thin with 19 parameters and defines it with 13;
 # ibm_compile_fix.h names the two forms apart so the file compiles unmodified.
 $CC $CFLAGS -include ibm_compile_fix.h -c "$REF/ibm.c" -o "$OUT/ref_ibm.o"

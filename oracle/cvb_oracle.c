@@ -971,3 +971,25 @@ void orc_ibm_ray_offsets(int n, double *s) {
     s[q] = rand() / ((double)RAND_MAX + 1) - 0.5;
   }
 }
+
+void orc_divergence(const orc_level *L, const double *uc, double *maxdiv, long long *at) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  double m = -HUGE_VAL;
+  long long where = -1;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        double d = 0.0;
+        if (i > 0 && i < mx - 1 && j > 0 && j < my - 1 && k > 0 && k < mz - 1) {
+          const size_t p = ID(L, i, j, k);
+          const size_t w = ID(L, i - 1, j, k), s = ID(L, i, j - 1, k), b = ID(L, i, j, k - 1);
+          d = fabs((uc[3 * p] - uc[3 * w] + uc[3 * p + 1] - uc[3 * s + 1] + uc[3 * p + 2] - uc[3 * b + 2]) * L->aj[p]);
+          if (NV(L, i, j, k) + NV(L, i, j, k + 1) + NV(L, i, j, k - 1) + NV(L, i, j + 1, k) + NV(L, i, j - 1, k) +
+                  NV(L, i + 1, j, k) + NV(L, i - 1, j, k) > 0.1)
+            d = 0.;
+        }
+        if (d > m) { m = d; where = (long long)ID(L, i, j, k); }
+      }
+  *maxdiv = m;
+  *at = where;
+}

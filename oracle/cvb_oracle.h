@@ -77,6 +77,11 @@ int orc_ghost_node_velocity(const orc_level *L, double *ubcs, double *ucat);
  * clean-up passes along k.  nvert ([mz][my][mx]) is read and written.  The
  * reference retries a ray until it meets no singular pair of intersections;
  * this gives up after max_tries directions and returns -1 (0 on success). */
+/* Divergence (main.c:469-593): |(the flux differences of the cell) * aj| on
+ * interior cells, 0 where the cell or a face neighbour has nvert summing above
+ * 0.1, 0 on the ring; returns the maximum and its first index in the box (as
+ * VecMax). */
+void orc_divergence(const orc_level *L, const double *ucont, double *maxdiv, long long *at);
 /* randomdirection's offsets for seeds 1 .. n: srand(seed); rand() scaled to
  * [-0.5, 0.5), exactly as ibm.c:101-104 draws them (the global generator). */
 void orc_ibm_ray_offsets(int n, double *s);

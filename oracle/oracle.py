@@ -82,6 +82,7 @@ def lib():
             [ctypes.c_int] * 2 + [P, P, ctypes.c_int]
         _lib.orc_ibm_search.restype = ctypes.c_int
         _lib.orc_ibm_ray_offsets.argtypes = [ctypes.c_int, P]
+        _lib.orc_divergence.argtypes = [L, P, P, P]
     return _lib
 
 
@@ -208,6 +209,14 @@ def ghost_node_velocity(L: OLevel, ubcs, ucat):
     return rc, ub, u
 
 
+def divergence(L: OLevel, ucont):
+    """Divergence (main.c:469-593): (max |div|, its index in the box)."""
+    uc = np.ascontiguousarray(ucont, dtype=np.float64)
+    m, at = ctypes.c_double(), ctypes.c_longlong()
+    lib().orc_divergence(L.ref(), _p(uc), ctypes.byref(m), ctypes.byref(at))
+    return m.value, at.value
+
+
 def ibm_search(cent, xyz, tri, nf, ibi, nbodies, nvert_o, nvert, max_tries=64):
     """The nvert classification of ibm_search_advanced (ibm.c:4197-4740):
     returns (status, nvert); status -1 if some cell found no clean ray."""
@@ -329,6 +338,13 @@ class Reference:
         self.L.ref_ghost_node_velocity(_p(ub), _p(u))
         return ub, u
 
+
+    def divergence(self, ucont):
+        uc = np.ascontiguousarray(ucont, dtype=np.float64)
+        m, at = ctypes.c_double(), ctypes.c_int()
+        if self.L.ref_divergence(_p(uc), ctypes.byref(m), ctypes.byref(at)):
+            raise RuntimeError("ref_divergence failed")
+        return m.value, at.value
 
     def ibm_search(self, xyz, tri, nf, ibi, nbodies, nvert_o, nvert):
         x = np.ascontiguousarray(xyz, dtype=np.float64)

@@ -384,11 +384,17 @@ PetscErrorCode VecNorm(Vec x, NormType t, PetscReal *r) {
   *r = (t == NORM_2) ? sqrt(s) : s;
   return 0;
 }
+/* The last VecMax result, for drivers of routines that only print it. */
+static double g_last_max = 0.0;
+static int g_last_at = -1;
+void shim_last_vecmax(double *v, int *at) { *v = g_last_max; *at = g_last_at; }
 PetscErrorCode VecMax(Vec x, PetscInt *p, PetscReal *r) {
   double m = -HUGE_VAL; int at = -1;
   for (PetscInt i = 0; i < x->n; i++) if (x->a[i] > m) { m = x->a[i]; at = i; }
   if (p) *p = at;
   *r = m;
+  g_last_max = m;
+  g_last_at = at;
   return 0;
 }
 PetscErrorCode VecMin(Vec x, PetscInt *p, PetscReal *r) {

@@ -514,3 +514,18 @@ int ref_mg_initial_nodes(const char *dir, int nlevels, int grid1d, double cl, do
   DMDAVecRestoreArray(u->fda, Coor, &coor);
   return 0;
 }
+
+/* Divergence (main.c:469-593), run after Projection in Flow_Solver
+ * (solvers.c:1084): max over the interior of |div Ucont| aj, zero next to a
+ * body and on the ring, and its index in the [mz][my][mx] box, as VecMax
+ * returns them (the routine itself only prints them). */
+PetscErrorCode Divergence(UserCtx *user);
+void shim_last_vecmax(double *v, int *at);
+int ref_divergence(const double *ucont, double *maxdiv, int *at) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  int rc = Divergence(u);
+  shim_last_vecmax(maxdiv, at);
+  return rc;
+}

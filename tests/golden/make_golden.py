@@ -73,6 +73,9 @@ def run(name):
     p, phi, u2 = R.update_and_project(seeded(fine, 400), seeded(fine, 401), uc, DT, ST)
     rec["update_project"] = {"p": digest(p), "phi": digest(phi), "ucont": digest(u2)}
     rec["post"] = post(R, c["nvert"], c["ucont"], 0)
+    R.set_nvert(nl - 1, c["nvert"])
+    m, at = R.divergence(c["ucont"])
+    rec["divergence"] = {"max": repr(m), "at": at}
     np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
     return rec
 

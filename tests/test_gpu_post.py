@@ -101,3 +101,17 @@ def test_uncovered_boundary_types_refused(bct):
                                             c["ucont"], ucat0))
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_divergence_matches_oracle(ctxs, key):
+    """Divergence (main.c:469-593): the maximum and its first index, from a host
+    Ucont and from the device copy the one-call projection leaves."""
+    ctx, P, L, seed = ctxs[key]
+    assert ctx.divergence(P.ucont) == O.divergence(L, P.ucont)
+    fine = P.nvert.shape
+    _, phi_o, uc_o = O.update_and_project(L, seeded(fine, 400), seeded(fine, 401), P.ucont, DT, ST)
+    ucat0, ubcs0 = post_inputs(fine, seed)
+    ctx.projection_cart(phi_o, DT, ST, P.ucont, ubcs0, ucat0)
+    m, at = ctx.divergence()
+    assert (m, at) == O.divergence(L, uc_o)

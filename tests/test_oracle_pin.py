@@ -84,6 +84,8 @@ def test_oracle_matches_reference(name):
     assert digest(phi) == ref["update_project"]["phi"]
     assert digest(u2) == ref["update_project"]["ucont"]
     _check_post(Ls[-1], c["ucont"], 0, ref["post"])
+    m, at = O.divergence(Ls[-1], c["ucont"])
+    assert repr(m) == ref["divergence"]["max"] and at == ref["divergence"]["at"]
 
 
 def _check_post(L, ucont, seed, want):
