@@ -73,6 +73,7 @@ EXPORTS = {
     "cvb_ibm_search": ([_P, _P, _I, _P, _I, _P, _P, _I, _I, _P, _P], _I),
     "cvb_ibm_ray_offsets": ([_I, _P], _I),
     "cvb_divergence": ([_P, _P, _P, _P], _I),
+    "cvb_metrics_divergence": ([_P, _P, _P], _I),
     "cvb_petsc_vec_write": ([ctypes.c_char_p, _P, ctypes.c_longlong, _I], _I),
     "cvb_petsc_vec_size": ([ctypes.c_char_p, _P], _I),
     "cvb_petsc_vec_read": ([ctypes.c_char_p, _P, ctypes.c_longlong], _I),

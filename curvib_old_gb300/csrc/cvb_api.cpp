@@ -1481,7 +1481,8 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
   return CVB_OK;
 }
 
-int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long *at) {
+// Divergence (flow) or MetricsDivergence (metrics) of the finest level.
+static int max_divergence(cvb_ctx *ctx, bool metrics, const double *ucont, double *maxdiv, long long *at) {
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
   if (!maxdiv || !at) return fail(ctx, CVB_BAD_INPUT, "maxdiv/at is NULL");
@@ -1494,8 +1495,12 @@ int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long 
   TRY(dalloc(ctx, &pv, 2 * 1024 + 2));
   long long *pi = reinterpret_cast<long long *>(pv + 1024);
   double *out = pv + 2048;
-  launch_divergence(F.g, ctx->uc_dev, ctx->aj64[l], F.nvert, pv, pi, out, reinterpret_cast<long long *>(out + 1),
-                    ctx->stream);
+  if (metrics)
+    launch_metrics_divergence(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->aj64[l], pv, pi, out,
+                              reinterpret_cast<long long *>(out + 1), ctx->stream);
+  else
+    launch_divergence(F.g, ctx->uc_dev, ctx->aj64[l], F.nvert, pv, pi, out, reinterpret_cast<long long *>(out + 1),
+                      ctx->stream);
   double h[2];
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
@@ -1505,6 +1510,14 @@ int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long 
   *maxdiv = h[0];
   std::memcpy(at, h + 1, sizeof(long long));
   return CVB_OK;
+}
+
+int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long *at) {
+  return max_divergence(ctx, false, ucont, maxdiv, at);
+}
+
+int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at) {
+  return max_divergence(ctx, true, nullptr, maxdiv, at);
 }
 
 // randomdirection's ray offsets (ibm.c:101-104): the first rand() after

@@ -271,6 +271,9 @@ void launch_contra2cart(const Geom &g, const double *csi, const double *eta, con
 // hold 1024 partial pairs
 void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
                        long long *pi, double *out_v, long long *out_i, cudaStream_t s);
+void launch_metrics_divergence(const Geom &g, const double *csi, const double *eta, const double *zet,
+                               const double *aj, double *pv, long long *pi, double *out_v, long long *out_i,
+                               cudaStream_t s);
 // bc: the level's bctype[6]; the host has refused the types it does not cover
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
                                 const double *zet, double *ubcs, double *ucat, cudaStream_t s);

@@ -1,7 +1,8 @@
 // The steps that follow the flux correction in the reference's Projection
 // (poisson.c:2897-2904): Contra2Cart (rhs.c:25-143), the Cartesian velocity at
 // the cell centres, and GhostNodeVelocity (bcs.c:3645-4435), its values on the
-// boundary ring; and Divergence (main.c:469-593), the check after them.  FP64 with every operation rounded on its own, in the
+// boundary ring; Divergence (main.c:469-593), the check after them; and
+// MetricsDivergence (metrics.c:1551-1625), the set-up check of the metrics.  FP64 with every operation rounded on its own, in the
 // reference's order (no fused multiply-add), so results equal the reference's
 // bit for bit.  Arrays are the finest level's [mz][my][mx] box, Cmpnts
 // interleaved.
@@ -95,9 +96,40 @@ __device__ __forceinline__ void div_block_reduce(double m, long long at, double 
   }
 }
 
+// The quantity of one interior cell p: the flow's divergence (Divergence),
+// or with metrics, the divergence of the centre metrics (MetricsDivergence,
+// metrics.c:1551-1625), each sum left to right as the C.
+__device__ __forceinline__ double flow_div(const Geom &g, const double *uc, const double *aj, const double *nv,
+                                          size_t p) {
+  const size_t plane = (size_t)g.mx * g.my, w = p - 1, s = p - g.mx, b = p - plane;
+  // ((((ux - ux_w) + uy) - uy_s) + uz) - uz_b
+  const double sum =
+      ds(da(ds(da(ds(uc[3 * p], uc[3 * w]), uc[3 * p + 1]), uc[3 * s + 1]), uc[3 * p + 2]), uc[3 * b + 2]);
+  double d = fabs(dm(sum, aj[p]));
+  const double ns =
+      da(da(da(da(da(da(nv[p], nv[p + plane]), nv[p - plane]), nv[p + g.mx]), nv[p - g.mx]), nv[p + 1]), nv[p - 1]);
+  if (ns > 0.1) d = 0.;
+  return d;
+}
+__device__ __forceinline__ double metrics_div(const Geom &g, const double *csi, const double *eta, const double *zet,
+                                             const double *aj, size_t p) {
+  const size_t w = p - 1, s = p - g.mx, b = p - (size_t)g.mx * g.my;
+  double sum = 0.0;
+  // csi.x - csi_w.x + eta.x - eta_s.x + zet.x - zet_b.x + (the same for y, z)
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const double t0 = c == 0 ? ds(csi[3 * p], csi[3 * w]) : ds(da(sum, csi[3 * p + c]), csi[3 * w + c]);
+    sum = ds(da(ds(da(t0, eta[3 * p + c]), eta[3 * s + c]), zet[3 * p + c]), zet[3 * b + c]);
+  }
+  return fabs(dm(sum, aj[p]));
+}
+
+template <bool METRICS>
 __global__ void __launch_bounds__(kDivThreads) k_divergence(Geom g, const double *__restrict__ uc,
                                                           const double *__restrict__ aj,
-                                                          const double *__restrict__ nv, double *pv, long long *pi) {
+                                                          const double *__restrict__ nv, const double *__restrict__ csi,
+                                                          const double *__restrict__ eta,
+                                                          const double *__restrict__ zet, double *pv, long long *pi) {
   __shared__ double sv[kDivThreads];
   __shared__ long long si[kDivThreads];
   double m = -HUGE_VAL;
@@ -106,16 +138,8 @@ __global__ void __launch_bounds__(kDivThreads) k_divergence(Geom g, const double
   for (size_t p = (size_t)blockIdx.x * kDivThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kDivThreads) {
     const int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / plane);
     double d = 0.0;
-    if (i > 0 && i < g.mx - 1 && j > 0 && j < g.my - 1 && k > 0 && k < g.mz - 1) {
-      const size_t w = p - 1, s = p - g.mx, b = p - plane;
-      // ((((ux - ux_w) + uy) - uy_s) + uz) - uz_b, left to right as the C
-      const double sum =
-          ds(da(ds(da(ds(uc[3 * p], uc[3 * w]), uc[3 * p + 1]), uc[3 * s + 1]), uc[3 * p + 2]), uc[3 * b + 2]);
-      d = fabs(dm(sum, aj[p]));
-      const double ns = da(da(da(da(da(da(nv[p], nv[p + plane]), nv[p - plane]), nv[p + g.mx]), nv[p - g.mx]),
-                              nv[p + 1]), nv[p - 1]);
-      if (ns > 0.1) d = 0.;
-    }
+    if (i > 0 && i < g.mx - 1 && j > 0 && j < g.my - 1 && k > 0 && k < g.mz - 1)
+      d = METRICS ? metrics_div(g, csi, eta, zet, aj, p) : flow_div(g, uc, aj, nv, p);
     div_better(m, at, d, (long long)p);
   }
   div_block_reduce(m, at, sv, si);
@@ -135,7 +159,16 @@ __global__ void __launch_bounds__(kDivThreads) k_divergence_final(const double *
 
 void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
                        long long *pi, double *out_v, long long *out_i, cudaStream_t s) {
-  k_divergence<<<kDivBlocks, kDivThreads, 0, s>>>(g, ucont, aj, nvert, pv, pi);
+  k_divergence<false><<<kDivBlocks, kDivThreads, 0, s>>>(g, ucont, aj, nvert, nullptr, nullptr, nullptr, pv, pi);
+  count_launch();
+  k_divergence_final<<<1, kDivThreads, 0, s>>>(pv, pi, kDivBlocks, out_v, out_i);
+  count_launch();
+}
+
+void launch_metrics_divergence(const Geom &g, const double *csi, const double *eta, const double *zet,
+                               const double *aj, double *pv, long long *pi, double *out_v, long long *out_i,
+                               cudaStream_t s) {
+  k_divergence<true><<<kDivBlocks, kDivThreads, 0, s>>>(g, nullptr, aj, nullptr, csi, eta, zet, pv, pi);
   count_launch();
   k_divergence_final<<<1, kDivThreads, 0, s>>>(pv, pi, kDivBlocks, out_v, out_i);
   count_launch();

@@ -198,6 +198,13 @@ class PoissonContext:
                                            ctypes.byref(at)))
         return m.value, at.value
 
+    def metrics_divergence(self):
+        """MetricsDivergence (metrics.c:1551): (max |div of the metrics|, its
+        index in the box) on the finest level."""
+        m, at = ctypes.c_double(), ctypes.c_longlong()
+        self._check(self._L.cvb_metrics_divergence(self._ctx, ctypes.byref(m), ctypes.byref(at)))
+        return m.value, at.value
+
     def ibm_search(self, cent, xyz, tri, nf, ibi, nbodies, nvert_o, nvert):
         """ibm_search_advanced's nvert classification (ibm.c:4197): returns the
         new nvert ([mz][my][mx]) of body ibi of nbodies.  cent None reuses the

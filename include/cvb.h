@@ -16,6 +16,7 @@
  *   Contra2Cart       (rhs.c:25)        -> cvb_contra2cart
  *   GhostNodeVelocity (bcs.c:3645)      -> cvb_ghost_node_velocity
  *   Divergence        (main.c:469)      -> cvb_divergence
+ *   MetricsDivergence (metrics.c:1551)  -> cvb_metrics_divergence
  *   ibm_search_advanced (ibm.c:4197), its nvert classification
  *                                       -> cvb_ibm_search
  *
@@ -196,6 +197,13 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
  * VecMax).  ucont NULL uses the context's device copy of Ucont as the last
  * projection or VolumeFlux_rev left it. */
 int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long *at);
+/* MetricsDivergence (metrics.c:1551-1625), the check of the finest level's
+ * metrics MG_Initial runs once they are formed (init.c:1054): the largest
+ * |(the nine differences of the centre metrics csi, eta, zet across the cell)
+ * * aj| over the interior cells, 0 on the ring, and its first index in the
+ * [mz][my][mx] box, as VecMax returns them.  Reads the metrics the context
+ * holds on the device. */
+int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
  * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and

@@ -993,3 +993,28 @@ void orc_divergence(const orc_level *L, const double *uc, double *maxdiv, long l
   *maxdiv = m;
   *at = where;
 }
+
+void orc_metrics_divergence(const orc_level *L, double *maxdiv, long long *at) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const double *cs = L->csi, *et = L->eta, *ze = L->zet;
+  double m = -HUGE_VAL;
+  long long where = -1;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        double d = 0.0;
+        if (i > 0 && i < mx - 1 && j > 0 && j < my - 1 && k > 0 && k < mz - 1) {
+          const size_t p = ID(L, i, j, k);
+          const size_t w = ID(L, i - 1, j, k), s = ID(L, i, j - 1, k), b = ID(L, i, j, k - 1);
+          double sum = 0.0;
+          for (int c = 0; c < 3; c++) {
+            const double t = c == 0 ? cs[3 * p] - cs[3 * w] : sum + cs[3 * p + c] - cs[3 * w + c];
+            sum = t + et[3 * p + c] - et[3 * s + c] + ze[3 * p + c] - ze[3 * b + c];
+          }
+          d = fabs(sum * L->aj[p]);
+        }
+        if (d > m) { m = d; where = (long long)ID(L, i, j, k); }
+      }
+  *maxdiv = m;
+  *at = where;
+}

@@ -82,6 +82,10 @@ int orc_ghost_node_velocity(const orc_level *L, double *ubcs, double *ucat);
  * 0.1, 0 on the ring; returns the maximum and its first index in the box (as
  * VecMax). */
 void orc_divergence(const orc_level *L, const double *ucont, double *maxdiv, long long *at);
+/* MetricsDivergence (metrics.c:1551-1625): |(csi.x - csi_w.x + eta.x - eta_s.x
+ * + zet.x - zet_b.x + the same for y and z) * aj| on interior cells, summed
+ * left to right, 0 on the ring; the maximum and its first index (VecMax). */
+void orc_metrics_divergence(const orc_level *L, double *maxdiv, long long *at);
 /* randomdirection's offsets for seeds 1 .. n: srand(seed); rand() scaled to
  * [-0.5, 0.5), exactly as ibm.c:101-104 draws them (the global generator). */
 void orc_ibm_ray_offsets(int n, double *s);

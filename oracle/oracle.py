@@ -83,6 +83,7 @@ def lib():
         _lib.orc_ibm_search.restype = ctypes.c_int
         _lib.orc_ibm_ray_offsets.argtypes = [ctypes.c_int, P]
         _lib.orc_divergence.argtypes = [L, P, P, P]
+        _lib.orc_metrics_divergence.argtypes = [L, P, P]
     return _lib
 
 
@@ -217,6 +218,14 @@ def divergence(L: OLevel, ucont):
     return m.value, at.value
 
 
+def metrics_divergence(L: OLevel):
+    """MetricsDivergence (metrics.c:1551-1625): (max |div of the metrics|, its
+    index in the box)."""
+    m, at = ctypes.c_double(), ctypes.c_longlong()
+    lib().orc_metrics_divergence(L.ref(), ctypes.byref(m), ctypes.byref(at))
+    return m.value, at.value
+
+
 def ibm_search(cent, xyz, tri, nf, ibi, nbodies, nvert_o, nvert, max_tries=64):
     """The nvert classification of ibm_search_advanced (ibm.c:4197-4740):
     returns (status, nvert); status -1 if some cell found no clean ray."""
@@ -344,6 +353,12 @@ class Reference:
         m, at = ctypes.c_double(), ctypes.c_int()
         if self.L.ref_divergence(_p(uc), ctypes.byref(m), ctypes.byref(at)):
             raise RuntimeError("ref_divergence failed")
+        return m.value, at.value
+
+    def metrics_divergence(self):
+        m, at = ctypes.c_double(), ctypes.c_int()
+        if self.L.ref_metrics_divergence(ctypes.byref(m), ctypes.byref(at)):
+            raise RuntimeError("ref_metrics_divergence failed")
         return m.value, at.value
 
     def ibm_search(self, xyz, tri, nf, ibi, nbodies, nvert_o, nvert):

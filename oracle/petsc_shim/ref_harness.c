@@ -529,3 +529,14 @@ int ref_divergence(const double *ucont, double *maxdiv, int *at) {
   shim_last_vecmax(maxdiv, at);
   return rc;
 }
+
+/* MetricsDivergence (metrics.c:1551-1625), which MG_Initial runs on the
+ * finest level once its metrics are formed (init.c:1054), over the metrics
+ * this harness formed with the reference's FormMetrics. */
+PetscErrorCode MetricsDivergence(UserCtx *user);
+int ref_metrics_divergence(double *maxdiv, int *at) {
+  if (!g_ready) return 1;
+  int rc = MetricsDivergence(U(g_mg.mglevels - 1));
+  shim_last_vecmax(maxdiv, at);
+  return rc;
+}

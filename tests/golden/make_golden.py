@@ -5,7 +5,8 @@ compiled unmodified against the single-process PETSc API shim
 (oracle/build_ref.sh), on the small scenarios of tests/cases.py and records
 SHA-256 digests of every output, including the immersed-body classification
 (ibm_search_advanced, ibm.c) of tests/cases.IBM_CASES, whose meshes are stored
-in ibm_meshes.npz.  The post-projection steps (Contra2Cart,
+in ibm_meshes.npz, and the checks Divergence (main.c) and MetricsDivergence
+(metrics.c).  The post-projection steps (Contra2Cart,
 GhostNodeVelocity) also run on the variants of cases.POST_VARIANTS, which put
 slip, moving-lid and O-grid faces and blanked cells on the same grids.  The
 inputs (node coordinates, nvert, fluxes) are stored beside the digests so the
@@ -76,6 +77,8 @@ def run(name):
     R.set_nvert(nl - 1, c["nvert"])
     m, at = R.divergence(c["ucont"])
     rec["divergence"] = {"max": repr(m), "at": at}
+    m, at = R.metrics_divergence()
+    rec["metrics_divergence"] = {"max": repr(m), "at": at}
     np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
     return rec
 

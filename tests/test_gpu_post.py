@@ -115,3 +115,11 @@ def test_divergence_matches_oracle(ctxs, key):
     ctx.projection_cart(phi_o, DT, ST, P.ucont, ubcs0, ucat0)
     m, at = ctx.divergence()
     assert (m, at) == O.divergence(L, uc_o)
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_metrics_divergence_matches_oracle(ctxs, key):
+    """MetricsDivergence (metrics.c:1551-1625) of the metrics the context holds:
+    the maximum and its first index, bit for bit."""
+    ctx, P, L, seed = ctxs[key]
+    assert ctx.metrics_divergence() == O.metrics_divergence(L)

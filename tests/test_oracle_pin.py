@@ -86,6 +86,8 @@ def test_oracle_matches_reference(name):
     _check_post(Ls[-1], c["ucont"], 0, ref["post"])
     m, at = O.divergence(Ls[-1], c["ucont"])
     assert repr(m) == ref["divergence"]["max"] and at == ref["divergence"]["at"]
+    m, at = O.metrics_divergence(Ls[-1])
+    assert repr(m) == ref["metrics_divergence"]["max"] and at == ref["metrics_divergence"]["at"]
 
 
 def _check_post(L, ucont, seed, want):
