@@ -386,13 +386,17 @@ def bench_step(args, ws, local):
         barrier(ws)
         out[name] = run(prec, args.step_steps)
     out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
-    # the post-projection kernels alone, device-timed: Contra2Cart is bound by
-    # the FP64 pipe (every operation rounded on its own, three divisions a cell)
+    # the post-projection kernels and the momentum step's convective term
+    # (Convection, QUICK) alone, device-timed: both are bound by the FP64 pipe
+    # (every operation rounded on its own; three divisions a cell in
+    # Contra2Cart, 18 face-flux components a cell in Convection)
     kt = {}
-    for name, kid in (("contra2cart", _lib.KERNELS["contra2cart"]), ("ghost_nodes", _lib.KERNELS["ghost_nodes"])):
+    for name in ("contra2cart", "ghost_nodes", "convection"):
         ms, nbytes = ctypes.c_double(), ctypes.c_double()
-        assert L.cvb_time_kernel(ctx._ctx, kid, ctx.nlevels - 1, 20, ctypes.byref(ms), ctypes.byref(nbytes)) == 0
+        assert L.cvb_time_kernel(ctx._ctx, _lib.KERNELS[name], ctx.nlevels - 1, 20, ctypes.byref(ms),
+                                 ctypes.byref(nbytes)) == 0
         kt[name + "_us"] = ms.value * 1e3
+        kt[name + "_algorithmic_gbs"] = nbytes.value / (ms.value * 1e-3) / 1e9
     out["post_projection_kernels"] = kt
     ctx.close()
     return out

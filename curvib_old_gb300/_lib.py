@@ -74,6 +74,7 @@ EXPORTS = {
     "cvb_ibm_ray_offsets": ([_I, _P], _I),
     "cvb_divergence": ([_P, _P, _P, _P], _I),
     "cvb_metrics_divergence": ([_P, _P, _P], _I),
+    "cvb_convection": ([_P, _P, _P, _I, _P], _I),
     "cvb_petsc_vec_write": ([ctypes.c_char_p, _P, ctypes.c_longlong, _I], _I),
     "cvb_petsc_vec_size": ([ctypes.c_char_p, _P], _I),
     "cvb_petsc_vec_read": ([ctypes.c_char_p, _P, ctypes.c_longlong], _I),
@@ -116,7 +117,8 @@ EXPORTS = {
     "cvb_get_phi": ([_P, _P], _I),
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3, "zebra_f32": 4,
-           "zebra_f64": 5, "vcycle_f32": 6, "vcycle_f64": 7, "contra2cart": 8, "ghost_nodes": 9}
+           "zebra_f64": 5, "vcycle_f32": 6, "vcycle_f64": 7, "contra2cart": 8, "ghost_nodes": 9,
+           "convection": 10}
 
 
 def lib_path() -> Path:

@@ -1481,6 +1481,28 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
   return CVB_OK;
 }
 
+int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!conv) return fail(ctx, CVB_BAD_INPUT, "conv is NULL");
+  const int *bc = ctx->H[ctx->nlevels - 1].d.bctype;
+  for (int f = 0; f < 6; f++)
+    if (bc[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Convection: periodic faces (bctype 7) are not covered");
+  if (!ucat && !ctx->ucat_dev) return fail(ctx, CVB_BAD_INPUT, "ucat is NULL and no projection has left Ucat on the device");
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  TRY(post_buffers(ctx, n));
+  if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, 3 * n));
+  if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+  if (ucont) CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (ucat) CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_convection(F.g, ctx->uc_dev, ctx->ucat_dev, F.nvert, central != 0, ctx->conv_fp, ctx->conv_dev, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(conv, ctx->conv_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
 // Divergence (flow) or MetricsDivergence (metrics) of the finest level.
 static int max_divergence(cvb_ctx *ctx, bool metrics, const double *ucont, double *maxdiv, long long *at) {
   if (!ctx) return CVB_BAD_INPUT;
@@ -1880,14 +1902,24 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
         launch_ghost_node_velocity(L.g, ctx->H[level].d.bctype, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev,
                                    ctx->ucat_dev, ctx->stream);
         break;
+      case CVB_KERNEL_CONVECTION:
+        launch_convection(L.g, ctx->uc_dev, ctx->ucat_dev, L.nvert, 0, ctx->conv_fp, ctx->conv_dev, ctx->stream);
+        break;
       default: launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream); break;
     }
   };
   if (kernel == CVB_KERNEL_VCYCLE_F32 || kernel == CVB_KERNEL_VCYCLE_F64) return time_vcycle(ctx, kernel, level, reps, avg_ms, bytes);
-  if (kernel == CVB_KERNEL_CONTRA2CART || kernel == CVB_KERNEL_GHOST_NODES) {
+  if (kernel == CVB_KERNEL_CONTRA2CART || kernel == CVB_KERNEL_GHOST_NODES || kernel == CVB_KERNEL_CONVECTION) {
     if (level != ctx->nlevels - 1) return fail(ctx, CVB_BAD_INPUT, "kernel %d runs on the finest level only", kernel);
     if (kernel == CVB_KERNEL_GHOST_NODES) TRY(ghost_types_ok(ctx, ctx->H[level].d.bctype));
+    if (kernel == CVB_KERNEL_CONVECTION)
+      for (int f = 0; f < 6; f++)
+        if (ctx->H[level].d.bctype[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Convection: periodic faces are not covered");
     TRY(post_buffers(ctx, n));
+    if (kernel == CVB_KERNEL_CONVECTION) {
+      if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, 3 * n));
+      if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+    }
     CK(cudaMemsetAsync(ctx->uc_dev, 0, sizeof(double) * 3 * n, ctx->stream));
     CK(cudaMemsetAsync(ctx->ucat_dev, 0, sizeof(double) * 3 * n, ctx->stream));
     CK(cudaMemsetAsync(ctx->ubcs_dev, 0, sizeof(double) * 3 * n, ctx->stream));
@@ -1906,6 +1938,7 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
     case CVB_KERNEL_ZEBRA_F32: per_cell = 4 + 0.5 * (4 + g32 + 4 + 4 + 4) + 0.5 * (4 + 12 + 4 + 4); break;
     case CVB_KERNEL_ZEBRA_F64: per_cell = 8 + 0.5 * (8 + w64 + 4 + 8) + 0.5 * (8 + 24 + 8 + 8); break;
     case CVB_KERNEL_CONTRA2CART: per_cell = 72 + 24 + 8 + 24; break;  // centre metrics, ucont, nvert, ucat
+    case CVB_KERNEL_CONVECTION: per_cell = 24 + 24 + 8 + 24; break;   // ucont, ucat, nvert, conv
     case CVB_KERNEL_GHOST_NODES: {
       // the ring cells only: ucat read and written, ubcs read
       const double inner = (double)(L.g.mx - 2) * (L.g.my - 2) * (L.g.mz - 2);

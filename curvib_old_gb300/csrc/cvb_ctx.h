@@ -89,6 +89,7 @@ struct cvb_ctx {
   double *partial = nullptr, *sums = nullptr, *hdev = nullptr;
   double *uc_dev = nullptr, *p_dev = nullptr;
   double *ucat_dev = nullptr, *ubcs_dev = nullptr;  // Contra2Cart / GhostNodeVelocity (allocated on first use)
+  double *conv_dev = nullptr, *conv_fp = nullptr;    // Convection: result and face fluxes (allocated on first use)
   double *ibm_cent = nullptr;  // cell centres of the last cvb_ibm_search that gave them
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;

@@ -271,6 +271,8 @@ void launch_contra2cart(const Geom &g, const double *csi, const double *eta, con
 // hold 1024 partial pairs
 void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
                        long long *pi, double *out_v, long long *out_i, cudaStream_t s);
+void launch_convection(const Geom &g, const double *ucont, const double *ucat, const double *nvert, int central,
+                       double *fp, double *conv, cudaStream_t s);
 void launch_metrics_divergence(const Geom &g, const double *csi, const double *eta, const double *zet,
                                const double *aj, double *pv, long long *pi, double *out_v, long long *out_i,
                                cudaStream_t s);

@@ -1,8 +1,10 @@
 // The steps that follow the flux correction in the reference's Projection
 // (poisson.c:2897-2904): Contra2Cart (rhs.c:25-143), the Cartesian velocity at
 // the cell centres, and GhostNodeVelocity (bcs.c:3645-4435), its values on the
-// boundary ring; Divergence (main.c:469-593), the check after them; and
-// MetricsDivergence (metrics.c:1551-1625), the set-up check of the metrics.  FP64 with every operation rounded on its own, in the
+// boundary ring; Divergence (main.c:469-593), the check after them;
+// MetricsDivergence (metrics.c:1551-1625), the set-up check of the metrics;
+// and Convection (rhs.c:1463-1946), the convective term of the momentum
+// right-hand side.  FP64 with every operation rounded on its own, in the
 // reference's order (no fused multiply-add), so results equal the reference's
 // bit for bit.  Arrays are the finest level's [mz][my][mx] box, Cmpnts
 // interleaved.
@@ -336,6 +338,108 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
     k_ghost_ring<<<grd, blk, 0, s>>>(A, axis, 1);
     count_launch();
   }
+}
+
+
+// ---------------------------------------------------------------------------
+// Convection (rhs.c:1463-1946), for boxes with no periodic face.  The face
+// fluxes of ucat carried by Ucont/2 are formed once per face by k_conv_faces
+// into nine component planes (fp[(3d + c) n + p], coalesced), then
+// k_conv_diff takes their differences over each interior cell.  Every product
+// and sum is rounded as the C rounds it (no contraction), so the result is the
+// reference's bit for bit.  Where the reference reads two cells past the i or
+// j end of a row (a face next to the high end whose lower neighbour has nvert
+// above 0.1) it reads, on one rank, the first cells of the next row: the flat
+// index p + 2 st reads the same, and stays inside the box because the other
+// indices are interior.
+
+// um * (coef * (-u[hi] - 2 u[1] + 3 u[0]) + u[1]) + up * (coef * (-u[lo] - 2 u[0] + 3 u[1]) + u[0])
+__device__ __forceinline__ double conv_quick(const double *uc, long long p, long long st, int c, int lo, int hi,
+                                            double um, double up) {
+  const double coef = 0.125;
+  const double uh = uc[3 * (p + hi * st) + c], u1 = uc[3 * (p + st) + c], u0 = uc[3 * p + c],
+               ul = uc[3 * (p + lo * st) + c];
+  const double a = da(dm(coef, da(ds(-uh, dm(2., u1)), dm(3., u0))), u1);
+  const double b = da(dm(coef, da(ds(-ul, dm(2., u0)), dm(3., u1))), u0);
+  return da(dm(um, a), dm(up, b));
+}
+
+__device__ __forceinline__ bool conv_fluid(double n) { return n < 0.1 || n > 7.; }
+
+__global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__restrict__ ucont,
+                                                   const double *__restrict__ ucat, const double *__restrict__ nv,
+                                                   int central, double *__restrict__ fp) {
+  const size_t n = g.n(), plane = (size_t)g.mx * g.my;
+  for (size_t pu = (size_t)blockIdx.x * blockDim.x + threadIdx.x; pu < n; pu += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(pu % g.mx), j = (int)((pu / g.mx) % g.my), k = (int)(pu / plane);
+    const long long p = (long long)pu;
+    const int idx[3] = {i, j, k}, ext[3] = {g.mx, g.my, g.mz};
+    const long long st[3] = {1, g.mx, (long long)plane};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      double f[3] = {0., 0., 0.};
+      const int q = idx[d], m = ext[d];
+      // the face sweep along d covers q in [0, m-2] with the other two indices interior
+      bool on = q <= m - 2;
+#pragma unroll
+      for (int e = 0; e < 3; e++)
+        if (e != d) on = on && idx[e] > 0 && idx[e] < ext[e] - 1;
+      if (on) {
+        const double ucon = dm(ucont[3 * p + d], 0.5);
+        const double up = da(ucon, fabs(ucon)), um = ds(ucon, fabs(ucon));
+        const long long s = st[d];
+        // the j sweep tests i (not j) against my-2 for its central end faces
+        const bool end2 = d == 1 ? (j == 0 || i == g.my - 2) : (q == 0 || q == m - 2);
+        int lo = 0, hi = 0, cen = 0, any = 1;
+        if (q > 0 && q < m - 2 && conv_fluid(nv[p + s]) && conv_fluid(nv[p - s])) {
+          if (central) cen = 1; else { lo = -1; hi = 2; }
+        } else if (central && end2 && conv_fluid(nv[p + s]) && conv_fluid(nv[p])) {
+          cen = 1;
+        } else if ((d < 2 || q < m - 2) && (q == 0 || nv[p - s] > 0.1)) {
+          lo = 0; hi = 2;
+        } else if ((d < 2 || q > 0) && (q == m - 2 || nv[p + s] > 0.1)) {
+          lo = -1; hi = 1;
+        } else {
+          any = 0;
+        }
+        if (any)
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            f[c] = cen ? dm(ucon, da(ucat[3 * p + c], ucat[3 * (p + s) + c])) : conv_quick(ucat, p, s, c, lo, hi, um, up);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) fp[(size_t)(3 * d + c) * n + pu] = f[c];
+    }
+  }
+}
+
+// conv = fp1 - fp1_w + fp2 - fp2_s + fp3 - fp3_b per component, left to right
+// as the C; 0 on the ring.
+__global__ void __launch_bounds__(256) k_conv_diff(Geom g, const double *__restrict__ fp, double *__restrict__ conv) {
+  const size_t n = g.n(), plane = (size_t)g.mx * g.my;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / plane);
+    const bool in = i > 0 && i < g.mx - 1 && j > 0 && j < g.my - 1 && k > 0 && k < g.mz - 1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double v = 0.;
+      if (in) {
+        const double *f1 = fp + (size_t)c * n, *f2 = fp + (size_t)(3 + c) * n, *f3 = fp + (size_t)(6 + c) * n;
+        v = ds(da(ds(da(ds(f1[p], f1[p - 1]), f2[p]), f2[p - g.mx]), f3[p]), f3[p - plane]);
+      }
+      conv[3 * p + c] = v;
+    }
+  }
+}
+
+void launch_convection(const Geom &g, const double *ucont, const double *ucat, const double *nvert, int central,
+                       double *fp, double *conv, cudaStream_t s) {
+  const size_t n = g.n();
+  const unsigned blocks = nblk(n, 256) < 152u * 8 ? nblk(n, 256) : 152u * 8;
+  k_conv_faces<<<blocks, 256, 0, s>>>(g, ucont, ucat, nvert, central, fp);
+  count_launch();
+  k_conv_diff<<<blocks, 256, 0, s>>>(g, fp, conv);
+  count_launch();
 }
 
 }  // namespace cvb

@@ -6,8 +6,10 @@ KERNEL is one of line_sweep_f32, line_sweep_f64 (a damped-Jacobi y-line sweep),
 residual_f32, residual_f64, zebra_f32, zebra_f64 (one half-sweep of the zebra
 smoother: residual on one color, then its line solves), vcycle_f32, vcycle_f64
 (one V-cycle with the default options from the level down, replayed from a
-CUDA graph; no byte count), contra2cart, ghost_nodes (Contra2Cart and
-GhostNodeVelocity; finest level only); default: all.  The problem is the periodic channel (x and z periodic,
+CUDA graph; no byte count), contra2cart, ghost_nodes, convection
+(Contra2Cart, GhostNodeVelocity and Convection; finest level only); default:
+all.  Convection runs on a walled box of the same cell counts (distorted, tanh
+2.0 in y), since it does not cover periodic faces.  The problem is the periodic channel (x and z periodic,
 tanh-stretched walls in y, factor 2.5) at the given cell counts.  Each kernel's
 timed launches run inside an NVTX range named ``timed:<kernel>``, so a profiler
 can be pointed at exactly those launches (``ncu --nvtx --nvtx-include
@@ -46,16 +48,23 @@ def main(argv=None):
             ap.error(f"unknown kernel {k!r}; choose from {sorted(KERNELS)}")
     import torch  # NVTX ranges only; the kernels themselves come from libcvb.so
 
-    problem = W.config1_problem(cells=a.cells)
-    ctx = PoissonContext().setup(problem)
+    ctx = box = None
     for k in a.kernels:
+        if k == "convection":
+            box = box or PoissonContext().setup(W.make_problem(a.cells, (1.0, 1.0, 1.0), 2.0, True,
+                                                               (False, False, False), [], name="box"))
+        else:
+            ctx = ctx or PoissonContext().setup(W.config1_problem(cells=a.cells))
+        c = box if k == "convection" else ctx
         torch.cuda.nvtx.range_push(f"timed:{k}")
-        ms, nbytes = ctx.time_kernel(k, level=a.level, reps=a.reps)
+        ms, nbytes = c.time_kernel(k, level=a.level, reps=a.reps)
         torch.cuda.nvtx.range_pop()
-        print(json.dumps({"kernel": k, "level": a.level % ctx.nlevels, "cells": int(np.prod(ctx.shapes[a.level])),
+        print(json.dumps({"kernel": k, "level": a.level % c.nlevels, "cells": int(np.prod(c.shapes[a.level])),
                           "us": round(ms * 1e3, 2), "bytes": int(nbytes),
                           "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1)}))
-    ctx.close()
+    for c in (ctx, box):
+        if c:
+            c.close()
 
 
 if __name__ == "__main__":

@@ -198,6 +198,16 @@ class PoissonContext:
                                            ctypes.byref(at)))
         return m.value, at.value
 
+    def convection(self, ucont=None, ucat=None, central=False):
+        """Convection (rhs.c:1463): the convective term at the cell centres,
+        [mz][my][mx][3]; None for ucont / ucat uses the device copies the last
+        projection left."""
+        shape = tuple(self.shapes[-1]) + (3,)
+        out = np.empty(shape, dtype=np.float64)
+        self._check(self._L.cvb_convection(self._ctx, None if ucont is None else ptr(_c64(ucont)),
+                                           None if ucat is None else ptr(_c64(ucat)), int(bool(central)), ptr(out)))
+        return out
+
     def metrics_divergence(self):
         """MetricsDivergence (metrics.c:1551): (max |div of the metrics|, its
         index in the box) on the finest level."""

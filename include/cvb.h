@@ -17,6 +17,7 @@
  *   GhostNodeVelocity (bcs.c:3645)      -> cvb_ghost_node_velocity
  *   Divergence        (main.c:469)      -> cvb_divergence
  *   MetricsDivergence (metrics.c:1551)  -> cvb_metrics_divergence
+ *   Convection        (rhs.c:1463)      -> cvb_convection
  *   ibm_search_advanced (ibm.c:4197), its nvert classification
  *                                       -> cvb_ibm_search
  *
@@ -204,6 +205,16 @@ int cvb_divergence(cvb_ctx *ctx, const double *ucont, double *maxdiv, long long 
  * [mz][my][mx] box, as VecMax returns them.  Reads the metrics the context
  * holds on the device. */
 int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at);
+/* Convection (rhs.c:1463-1946), the convective term FormFunction1 starts the
+ * momentum right-hand side with (rhs.c:2651): at every interior cell the sum
+ * over its six faces of the face flux of ucat carried by Ucont/2, QUICK
+ * upwinded (central != 0: central, the -central option), with the one-sided
+ * forms of the reference next to the ring and next to cells of nvert above
+ * 0.1; 0 on the ring.  ucont, ucat and conv are [mz][my][mx][3].  ucont NULL
+ * uses the device copy of Ucont the last projection left, ucat NULL the device
+ * Ucat of the last cvb_projection_cart.  Boxes with a periodic face (bctype
+ * 7) are refused with CVB_BAD_INPUT. */
+int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
  * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and
@@ -374,7 +385,8 @@ enum {
   CVB_KERNEL_VCYCLE_F32 = 6,     /* one FP32 V-cycle (default options) from the level down, replayed from a CUDA graph */
   CVB_KERNEL_VCYCLE_F64 = 7,     /* the same in FP64 */
   CVB_KERNEL_CONTRA2CART = 8,    /* Contra2Cart on the finest level (the level argument must name it) */
-  CVB_KERNEL_GHOST_NODES = 9     /* GhostNodeVelocity on the finest level */
+  CVB_KERNEL_GHOST_NODES = 9,    /* GhostNodeVelocity on the finest level */
+  CVB_KERNEL_CONVECTION = 10     /* Convection (QUICK) on the finest level: face fluxes, then their differences */
 };
 /* JSON record of the set-up autotuner: per level, the measured time of the
  * fused and the split y-line sweep in each precision and the variant kept. */

@@ -994,6 +994,71 @@ void orc_divergence(const orc_level *L, const double *uc, double *maxdiv, long l
   *at = where;
 }
 
+/* One face flux component of Convection (rhs.c:1628-1918): lo is the offset of
+ * the upwind cell below (-1 interior, 0 next to the low end), hi the one above
+ * (2 interior, 1 next to the high end), st the stride along the direction. */
+static double conv_quick(const double *uc, size_t p, long st, int c, int lo, int hi, double um, double up) {
+  const double coef = 0.125;
+#define UC(o) uc[3 * (size_t)((long)p + (long)(o) * st) + c]
+  return um * (coef * (-UC(hi) - 2. * UC(1) + 3. * UC(0)) + UC(1)) +
+         up * (coef * (-UC(lo) - 2. * UC(0) + 3. * UC(1)) + UC(0));
+#undef UC
+}
+
+static int conv_fluid(double n) { return n < 0.1 || n > 7.; }
+
+int orc_convection(const orc_level *L, const double *ucont, const double *ucat, int central, double *conv) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  for (int f = 0; f < 6; f++)
+    if (L->bctype[f] == 7) return -1;
+  const size_t n = (size_t)mx * my * mz;
+  const long st[3] = {1, mx, (long)mx * my};
+  const int ext[3] = {mx, my, mz};
+  double *fp = (double *)calloc(9 * n, sizeof(double));
+  for (int d = 0; d < 3; d++)
+    for (int k = d == 2 ? 0 : 1; k < mz - 1; k++)
+      for (int j = d == 1 ? 0 : 1; j < my - 1; j++)
+        for (int i = d == 0 ? 0 : 1; i < mx - 1; i++) {
+          const size_t p = ID(L, i, j, k);
+          const int q = d == 0 ? i : d == 1 ? j : k, m = ext[d];
+          const double *nv = L->nvert;
+          const double ucon = ucont[3 * p + d] * 0.5;
+          const double up = ucon + fabs(ucon), um = ucon - fabs(ucon);
+          double *o = fp + 9 * p + 3 * d;
+#define NV(off) nv[(size_t)((long)p + (long)(off) * st[d])]
+#define UC(off, c) ucat[3 * (size_t)((long)p + (long)(off) * st[d]) + c]
+          int lo = 0, hi = 0, cen = 0;
+          /* the j sweep tests i (not j) against my-2 for its central end faces */
+          const int end2 = d == 1 ? (j == 0 || i == my - 2) : (q == 0 || q == m - 2);
+          if (q > 0 && q < m - 2 && conv_fluid(NV(1)) && conv_fluid(NV(-1))) {
+            if (central) cen = 1; else { lo = -1; hi = 2; }
+          } else if (central && end2 && conv_fluid(NV(1)) && conv_fluid(NV(0))) {
+            cen = 1;
+          } else if ((d < 2 || q < m - 2) && (q == 0 || NV(-1) > 0.1)) {
+            lo = 0; hi = 2;
+          } else if ((d < 2 || q > 0) && (q == m - 2 || NV(1) > 0.1)) {
+            lo = -1; hi = 1;
+          } else {
+            continue;
+          }
+          for (int c = 0; c < 3; c++)
+            o[c] = cen ? ucon * (UC(0, c) + UC(1, c)) : conv_quick(ucat, p, st[d], c, lo, hi, um, up);
+#undef NV
+#undef UC
+        }
+  memset(conv, 0, sizeof(double) * 3 * n);
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const size_t p = ID(L, i, j, k), w = p - 1, s = p - mx, b = p - (size_t)mx * my;
+        for (int c = 0; c < 3; c++)
+          conv[3 * p + c] = fp[9 * p + c] - fp[9 * w + c] + fp[9 * p + 3 + c] - fp[9 * s + 3 + c] +
+                            fp[9 * p + 6 + c] - fp[9 * b + 6 + c];
+      }
+  free(fp);
+  return 0;
+}
+
 void orc_metrics_divergence(const orc_level *L, double *maxdiv, long long *at) {
   const int mx = L->mx, my = L->my, mz = L->mz;
   const double *cs = L->csi, *et = L->eta, *ze = L->zet;

@@ -86,6 +86,14 @@ void orc_divergence(const orc_level *L, const double *ucont, double *maxdiv, lon
  * + zet.x - zet_b.x + the same for y and z) * aj| on interior cells, summed
  * left to right, 0 on the ring; the maximum and its first index (VecMax). */
 void orc_metrics_divergence(const orc_level *L, double *maxdiv, long long *at);
+/* Convection (rhs.c:1463-1946) for boxes with no periodic face: the face
+ * fluxes of ucat carried by Ucont/2, QUICK (central != 0: central), with the
+ * one-sided forms next to the ring and next to cells of nvert above 0.1, then
+ * conv = the flux differences over each interior cell, 0 on the ring.  Where
+ * the reference reads two cells past the i or j end of a row it reads, on one
+ * rank, the first cells of the next row; flat indexing reads the same.
+ * Returns -1 (conv untouched) when a face is periodic, else 0. */
+int orc_convection(const orc_level *L, const double *ucont, const double *ucat, int central, double *conv);
 /* randomdirection's offsets for seeds 1 .. n: srand(seed); rand() scaled to
  * [-0.5, 0.5), exactly as ibm.c:101-104 draws them (the global generator). */
 void orc_ibm_ray_offsets(int n, double *s);

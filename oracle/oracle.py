@@ -84,6 +84,7 @@ def lib():
         _lib.orc_ibm_ray_offsets.argtypes = [ctypes.c_int, P]
         _lib.orc_divergence.argtypes = [L, P, P, P]
         _lib.orc_metrics_divergence.argtypes = [L, P, P]
+        _lib.orc_convection.argtypes = [L, P, P, ctypes.c_int, P]
     return _lib
 
 
@@ -216,6 +217,16 @@ def divergence(L: OLevel, ucont):
     m, at = ctypes.c_double(), ctypes.c_longlong()
     lib().orc_divergence(L.ref(), _p(uc), ctypes.byref(m), ctypes.byref(at))
     return m.value, at.value
+
+
+def convection(L: OLevel, ucont, ucat, central=0):
+    """Convection (rhs.c:1463-1946): (status, conv); status -1 for a periodic
+    face, with conv zero."""
+    uc = np.ascontiguousarray(ucont, dtype=np.float64)
+    u = np.ascontiguousarray(ucat, dtype=np.float64)
+    out = np.zeros_like(u)
+    rc = lib().orc_convection(L.ref(), _p(uc), _p(u), int(central), _p(out))
+    return rc, out
 
 
 def metrics_divergence(L: OLevel):
@@ -354,6 +365,14 @@ class Reference:
         if self.L.ref_divergence(_p(uc), ctypes.byref(m), ctypes.byref(at)):
             raise RuntimeError("ref_divergence failed")
         return m.value, at.value
+
+    def convection(self, ucont, ucat, central=0):
+        uc = np.ascontiguousarray(ucont, dtype=np.float64)
+        u = np.ascontiguousarray(ucat, dtype=np.float64)
+        out = np.zeros_like(u)
+        if self.L.ref_convection(_p(uc), _p(u), int(central), _p(out)):
+            raise RuntimeError("ref_convection failed")
+        return out
 
     def metrics_divergence(self):
         m, at = ctypes.c_double(), ctypes.c_int()

@@ -530,6 +530,25 @@ int ref_divergence(const double *ucont, double *maxdiv, int *at) {
   return rc;
 }
 
+/* Convection (rhs.c:1463-1946) as FormFunction1 calls it (rhs.c:2651), on
+ * lUcont and lUcat of the finest level, with -central set as given; conv is
+ * the [mz][my][mx] box of the result. */
+PetscErrorCode Convection(UserCtx *user, Vec Ucont, Vec Ucat, Vec Conv);
+int ref_convection(const double *ucont, const double *ucat, int central, double *conv) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  PetscOptionsSetValue("-central", central ? "1" : "0");
+  Vec Conv;
+  VecDuplicate(u->Ucont, &Conv);
+  int rc = Convection(u, u->lUcont, u->lUcat, Conv);
+  copy_owned(u, Conv, 3, conv, 0);
+  VecDestroy(&Conv);
+  PetscOptionsSetValue("-central", "0");
+  return rc;
+}
+
 /* MetricsDivergence (metrics.c:1551-1625), which MG_Initial runs on the
  * finest level once its metrics are formed (init.c:1054), over the metrics
  * this harness formed with the reference's FormMetrics. */

@@ -66,6 +66,22 @@ def post_inputs(shape, seed):
     return seeded(sh, 500 + seed), seeded(sh, 600 + seed)
 
 
+# Convection's edge cases on box_sphere's nvert, (k, j, i, value), negative
+# indices counting from the high end: a body cell two cells from the high i,
+# j and k ends (the reference's one-sided forms, which past the i and j ends
+# read the next row), neighbours of nvert exactly 0.1 (no form applies: the
+# face flux stays 0), and a blanked cell (nvert 8, treated as fluid).
+CONV_EDGES = [(5, 5, -3, 3.0), (6, -3, 4, 1.3), (-3, 4, 4, 2.0), (3, 3, 2, 0.1), (8, 2, 9, 0.1),
+              (7, 7, 7, 8.0), (2, -2, 6, 1.2)]
+
+
+def conv_edge_nvert(nvert):
+    nv = np.array(nvert, dtype=np.float64, copy=True)
+    for (k, j, i, v) in CONV_EDGES:
+        nv[k, j, i] = v
+    return nv
+
+
 def bctype_of(per):
     return [7 if per[0] else 1] * 2 + [7 if per[1] else 1] * 2 + [7 if per[2] else 1] * 2
 

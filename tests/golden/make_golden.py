@@ -6,7 +6,7 @@ compiled unmodified against the single-process PETSc API shim
 SHA-256 digests of every output, including the immersed-body classification
 (ibm_search_advanced, ibm.c) of tests/cases.IBM_CASES, whose meshes are stored
 in ibm_meshes.npz, and the checks Divergence (main.c) and MetricsDivergence
-(metrics.c).  The post-projection steps (Contra2Cart,
+(metrics.c), and the convective term Convection (rhs.c).  The post-projection steps (Contra2Cart,
 GhostNodeVelocity) also run on the variants of cases.POST_VARIANTS, which put
 slip, moving-lid and O-grid faces and blanked cells on the same grids.  The
 inputs (node coordinates, nvert, fluxes) are stored beside the digests so the
@@ -28,7 +28,8 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from cases import IBM_CASES, POST_VARIANTS, SCENARIOS, build, digest, digest_nan, ibm_inputs, post_inputs, seeded  # noqa: E402
+from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
+                   ibm_inputs, post_inputs, seeded)
 from curvib_old_gb300 import workload as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
@@ -79,8 +80,22 @@ def run(name):
     rec["divergence"] = {"max": repr(m), "at": at}
     m, at = R.metrics_divergence()
     rec["metrics_divergence"] = {"max": repr(m), "at": at}
+    rec["convection"] = convection(R, c["nvert"], c["ucont"], c["bctype"])
+    if name == "box_sphere":
+        rec["convection_edges"] = convection(R, conv_edge_nvert(c["nvert"]), c["ucont"], c["bctype"])
+        R.set_nvert(nl - 1, c["nvert"])
     np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
     return rec
+
+
+def convection(R, nvert, ucont, bctype):
+    """Convection (rhs.c:1463) on the ucat of post_inputs(seed 0), QUICK and
+    central; None for a box with a periodic face (not covered)."""
+    if 7 in list(bctype):
+        return None
+    R.set_nvert(R.nlevels - 1, nvert)
+    ucat0, _ = post_inputs(nvert.shape, 0)
+    return {"quick": digest(R.convection(ucont, ucat0, 0)), "central": digest(R.convection(ucont, ucat0, 1))}
 
 
 def post(R, nvert, ucont, seed):

@@ -5,14 +5,15 @@ the slip / moving-lid / O-grid variants with blanked cells (nvert > 7); the
 one-call projection against the three steps; boundary types that are not
 covered refused with nothing written.  A slip face on the low y side gives NaN,
 as in the reference (its normal comes from the ring cell's eta, which
-FormMetrics leaves zero), so arrays compare with NaN equal to NaN.
+FormMetrics leaves zero), so arrays compare with NaN equal to NaN.  Convection (rhs.c:1463), the first
+term of the momentum right-hand side, bit for bit on the same boxes.
 """
 import types
 
 import numpy as np
 import pytest
 
-from cases import POST_VARIANTS, SCENARIOS, build, post_inputs, seeded
+from cases import POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, post_inputs, seeded
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -115,6 +116,47 @@ def test_divergence_matches_oracle(ctxs, key):
     ctx.projection_cart(phi_o, DT, ST, P.ucont, ubcs0, ucat0)
     m, at = ctx.divergence()
     assert (m, at) == O.divergence(L, uc_o)
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_convection_bit_exact(ctxs, key):
+    """Convection (rhs.c:1463-1946), QUICK and central, bit for bit against the
+    oracle; a box with a periodic face is refused."""
+    from curvib_old_gb300._lib import CvbError
+    ctx, P, L, seed = ctxs[key]
+    ucat0, _ = post_inputs(P.nvert.shape, seed)
+    if 7 in list(P.bctype):
+        with pytest.raises(CvbError) as e:
+            ctx.convection(P.ucont, ucat0)
+        assert e.value.status == 4  # CVB_BAD_INPUT
+        return
+    for central in (False, True):
+        rc, want = O.convection(L, P.ucont, ucat0, int(central))
+        assert rc == 0
+        got = ctx.convection(P.ucont, ucat0, central)
+        assert np.array_equal(got, want), central
+        assert want[1:-1, 1:-1, 1:-1].any()
+
+
+def test_convection_edges_and_device_inputs():
+    """Convection next to the high ends, beside nvert of exactly 0.1 and blanked
+    cells (the reference's one-sided forms and its reads past the row ends);
+    then on the Ucont and Ucat the one-call projection leaves on the device."""
+    from curvib_old_gb300.solver import PoissonContext
+    P, seed = _problem("box_sphere")
+    P.nvert = conv_edge_nvert(P.nvert)
+    L = O.OLevel(P.metrics[-1], P.nvert, P.bctype, P.semi)
+    ctx = PoissonContext().setup(P)
+    try:
+        ucat0, ubcs0 = post_inputs(P.nvert.shape, seed)
+        for central in (0, 1):
+            assert np.array_equal(ctx.convection(P.ucont, ucat0, central), O.convection(L, P.ucont, ucat0, central)[1])
+        fine = P.nvert.shape
+        _, phi_o, _ = O.update_and_project(L, seeded(fine, 400), seeded(fine, 401), P.ucont, DT, ST)
+        uc, _, u = ctx.projection_cart(phi_o, DT, ST, P.ucont, ubcs0, ucat0)
+        assert np.array_equal(ctx.convection(), O.convection(L, uc, u)[1])
+    finally:
+        ctx.close()
 
 
 @pytest.mark.parametrize("key", sorted(CASES))

@@ -11,7 +11,8 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from cases import IBM_CASES, POST_VARIANTS, SCENARIOS, build, digest, digest_nan, ibm_inputs, post_inputs, seeded
+from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan, ibm_inputs,
+                   post_inputs, seeded)
 from curvib_old_gb300 import workload as W
 from oracle import oracle as O
 
@@ -88,6 +89,23 @@ def test_oracle_matches_reference(name):
     assert repr(m) == ref["divergence"]["max"] and at == ref["divergence"]["at"]
     m, at = O.metrics_divergence(Ls[-1])
     assert repr(m) == ref["metrics_divergence"]["max"] and at == ref["metrics_divergence"]["at"]
+    _check_convection(c, Ls[-1], ref["convection"])
+    if "convection_edges" in ref:
+        Le = O.OLevel(c["metrics"][-1], conv_edge_nvert(c["nvert"]), c["bctype"], c["semi"])
+        _check_convection(c, Le, ref["convection_edges"])
+
+
+def _check_convection(c, L, want):
+    """Convection (rhs.c:1463-1946), QUICK and central; a periodic box is
+    refused (status -1, nothing written)."""
+    ucat0, _ = post_inputs(L.shape, 0)
+    if want is None:
+        rc, conv = O.convection(L, c["ucont"], ucat0)
+        assert rc == -1 and not conv.any()
+        return
+    for key, central in (("quick", 0), ("central", 1)):
+        rc, conv = O.convection(L, c["ucont"], ucat0, central)
+        assert rc == 0 and digest(conv) == want[key], key
 
 
 def _check_post(L, ucont, seed, want):
