@@ -1916,13 +1916,21 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       for (int f = 0; f < 6; f++)
         if (ctx->H[level].d.bctype[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Convection: periodic faces are not covered");
     TRY(post_buffers(ctx, n));
-    if (kernel == CVB_KERNEL_CONVECTION) {
-      if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, 3 * n));
-      if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
-    }
     CK(cudaMemsetAsync(ctx->uc_dev, 0, sizeof(double) * 3 * n, ctx->stream));
     CK(cudaMemsetAsync(ctx->ucat_dev, 0, sizeof(double) * 3 * n, ctx->stream));
     CK(cudaMemsetAsync(ctx->ubcs_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+  }
+  if (kernel == CVB_KERNEL_CONVECTION) {
+    if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, 3 * n));
+    if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+    // a velocity field of mixed signs in [-1, 1] (zero fluxes would send every
+    // face through the full QUICK expression)
+    std::vector<double> v(3 * n);
+    for (size_t q = 0; q < v.size(); q++) v[q] = (double)((q * 2654435761ull) % 2001) / 1000.0 - 1.0;
+    CK(cudaMemcpyAsync(ctx->uc_dev, v.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->ucat_dev, v.data() + 1, sizeof(double) * (3 * n - 1), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
   }
   // algorithmic bytes per cell: every array the kernel needs, touched once.
   // The coefficients are the 9 face coefficients (FP32) or 19 weights (FP64),

@@ -353,15 +353,42 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
 // index p + 2 st reads the same, and stays inside the box because the other
 // indices are interior.
 
-// um * (coef * (-u[hi] - 2 u[1] + 3 u[0]) + u[1]) + up * (coef * (-u[lo] - 2 u[0] + 3 u[1]) + u[0])
+// |x| < 2^1000 (and not NaN), from the exponent field alone
+__device__ __forceinline__ bool conv_tame(double x) {
+  return (__double_as_longlong(x) & 0x7ff0000000000000LL) < (0x3ffLL + 1000) << 52;
+}
+__device__ __forceinline__ bool conv_nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+
+// coef * (-x2 - 2 x1 + 3 x0) + x1, the QUICK bracket of either side
+__device__ __forceinline__ double conv_bracket(double x2, double x1, double x0) {
+  return da(dm(0.125, da(ds(-x2, dm(2., x1)), dm(3., x0))), x1);
+}
+
+// The full face flux um * bracket(u[hi], u[1], u[0]) + up * bracket(u[lo], u[0], u[1]),
+// with um = ucon - |ucon|, up = ucon + |ucon|.  Out of line, so that its
+// second bracket is evaluated only on this path.
+__device__ __noinline__ double conv_quick_full(double ucon, double uh, double u1, double u0, double ul) {
+  const double up = da(ucon, fabs(ucon)), um = ds(ucon, fabs(ucon));
+  return da(dm(um, conv_bracket(uh, u1, u0)), dm(up, conv_bracket(ul, u0, u1)));
+}
+
+// The QUICK face flux of component c.  One of um and up is +0 and the other
+// is ucon + ucon.  When ucon and every input are below 2^1000 in magnitude and
+// nonzero where it matters, the dead bracket is finite, its product with +0 is
+// a zero, and a zero added to the nonzero live product leaves it unchanged: the
+// flux is the live product alone, bit for bit, from one bracket on the inputs
+// of the upwind side.  A zero live product (whose sign the dead zero could
+// change), ucon = 0, NaN or huge values take the full expression.
 __device__ __forceinline__ double conv_quick(const double *uc, long long p, long long st, int c, int lo, int hi,
-                                            double um, double up) {
-  const double coef = 0.125;
+                                            double ucon, bool tame) {
   const double uh = uc[3 * (p + hi * st) + c], u1 = uc[3 * (p + st) + c], u0 = uc[3 * p + c],
                ul = uc[3 * (p + lo * st) + c];
-  const double a = da(dm(coef, da(ds(-uh, dm(2., u1)), dm(3., u0))), u1);
-  const double b = da(dm(coef, da(ds(-ul, dm(2., u0)), dm(3., u1))), u0);
-  return da(dm(um, a), dm(up, b));
+  if (tame && conv_tame(uh) && conv_tame(u1) && conv_tame(u0) && conv_tame(ul)) {
+    const bool pos = __double_as_longlong(ucon) >= 0;  // up live (ucon > 0), else um
+    const double r = dm(da(ucon, ucon), conv_bracket(pos ? ul : uh, pos ? u0 : u1, pos ? u1 : u0));
+    if (conv_nonzero(r)) return r;
+  }
+  return conv_quick_full(ucon, uh, u1, u0, ul);
 }
 
 __device__ __forceinline__ bool conv_fluid(double n) { return n < 0.1 || n > 7.; }
@@ -386,7 +413,6 @@ __global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__rest
         if (e != d) on = on && idx[e] > 0 && idx[e] < ext[e] - 1;
       if (on) {
         const double ucon = dm(ucont[3 * p + d], 0.5);
-        const double up = da(ucon, fabs(ucon)), um = ds(ucon, fabs(ucon));
         const long long s = st[d];
         // the j sweep tests i (not j) against my-2 for its central end faces
         const bool end2 = d == 1 ? (j == 0 || i == g.my - 2) : (q == 0 || q == m - 2);
@@ -405,7 +431,8 @@ __global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__rest
         if (any)
 #pragma unroll
           for (int c = 0; c < 3; c++)
-            f[c] = cen ? dm(ucon, da(ucat[3 * p + c], ucat[3 * (p + s) + c])) : conv_quick(ucat, p, s, c, lo, hi, um, up);
+            f[c] = cen ? dm(ucon, da(ucat[3 * p + c], ucat[3 * (p + s) + c]))
+                       : conv_quick(ucat, p, s, c, lo, hi, ucon, conv_nonzero(ucon) && conv_tame(ucon));
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) fp[(size_t)(3 * d + c) * n + pu] = f[c];

@@ -134,7 +134,7 @@ def test_convection_bit_exact(ctxs, key):
         rc, want = O.convection(L, P.ucont, ucat0, int(central))
         assert rc == 0
         got = ctx.convection(P.ucont, ucat0, central)
-        assert np.array_equal(got, want), central
+        assert got.tobytes() == want.tobytes(), central  # signed zeros included
         assert want[1:-1, 1:-1, 1:-1].any()
 
 
@@ -151,6 +151,19 @@ def test_convection_edges_and_device_inputs():
         ucat0, ubcs0 = post_inputs(P.nvert.shape, seed)
         for central in (0, 1):
             assert np.array_equal(ctx.convection(P.ucont, ucat0, central), O.convection(L, P.ucont, ucat0, central)[1])
+        # zero fluxes and velocities of either sign, and values above 2^1000,
+        # where the kernel takes the full QUICK expression
+        uc_sp, u_sp = P.ucont.copy(), ucat0.copy()
+        uc_sp[5, 5, 5] = (0.0, -0.0, 0.0)
+        uc_sp[7, 3, 4, 0] = -0.0
+        u_sp[4, 5, 6] = (0.0, -0.0, 2.0 ** 1010)
+        u_sp[6, 6, 3, 1] = -(2.0 ** 1005)
+        u_sp[3, 8, 8] = 0.0
+        u_sp[3, 8, 9] = -0.0
+        for central in (0, 1):
+            want = O.convection(L, uc_sp, u_sp, central)[1]
+            assert np.isfinite(want).all()
+            assert ctx.convection(uc_sp, u_sp, central).tobytes() == want.tobytes(), central
         fine = P.nvert.shape
         _, phi_o, _ = O.update_and_project(L, seeded(fine, 400), seeded(fine, 401), P.ucont, DT, ST)
         uc, _, u = ctx.projection_cart(phi_o, DT, ST, P.ucont, ubcs0, ucat0)
