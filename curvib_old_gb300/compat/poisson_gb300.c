@@ -18,6 +18,8 @@
 
 extern PetscInt block_number, immersed; /* main.c, as poisson.c:6-7 declares them */
 extern PetscInt wallfunction;           /* main.c, as bcs.c:3689 declares it */
+extern PetscInt les;                    /* main.c, as rhs.c declares it */
+PetscErrorCode Convection(UserCtx *user, Vec Ucont, Vec Ucat, Vec Conv);
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 
@@ -212,6 +214,27 @@ PetscErrorCode Projection_GB300(UserCtx *u) {
   Contra2Cart(u);
   GhostNodeVelocity(u);
   return 0;
+}
+
+/* Convection (rhs.c:1463-1946) with the reference's arguments (FormFunction1
+ * passes lUcont and lUcat, rhs.c:2651).  Without a periodic face it runs on
+ * the device; with one, the reference's own routine runs, since it first
+ * fills ghost layers of the periodic DMDA.  -central or les selects the
+ * central form, as in the reference. */
+PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
+  for (int f = 0; f < 6; f++)
+    if (u->bctype[f] == 7) return Convection(u, Ucont, Ucat, Conv);
+  PetscInt central = 0;
+  PetscOptionsGetInt(PETSC_NULL, "-central", &central, PETSC_NULL);
+  PetscScalar *uc, *ucat, *conv;
+  VecGetArray(Ucont, &uc);
+  VecGetArray(Ucat, &ucat);
+  VecGetArray(Conv, &conv);
+  int rc = cvb_convection(g_cvb, uc, ucat, (les || central) ? 1 : 0, conv);
+  VecRestoreArray(Conv, &conv);
+  VecRestoreArray(Ucat, &ucat);
+  VecRestoreArray(Ucont, &uc);
+  return report(rc, "Convection_GB300");
 }
 
 PetscErrorCode PoissonFinalize_GB300(void) {

@@ -29,6 +29,8 @@ PetscErrorCode PoissonSetNvert_GB300(UserMG *usermg);
 PetscErrorCode PoissonSolver_MG_GB300(UserMG *usermg);
 PetscErrorCode UpdatePressure_GB300(UserCtx *user);
 PetscErrorCode Projection_GB300(UserCtx *user);
+/* In place of Convection (rhs.c:1463), same arguments. */
+PetscErrorCode Convection_GB300(UserCtx *user, Vec Ucont, Vec Ucat, Vec Conv);
 /* At the end of the run. */
 PetscErrorCode PoissonFinalize_GB300(void);
 

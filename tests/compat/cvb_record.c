@@ -100,6 +100,13 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
   ucont[3 * REC.mark] = 5.0;
   return take_status();
 }
+int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv) {
+  (void)ctx;
+  REC.n_convection++;
+  REC.ucont_conv = ucont; REC.ucat_conv = ucat; REC.central_conv = central; REC.conv_conv = conv;
+  conv[3 * REC.mark] = 7.0;
+  return take_status();
+}
 int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,
                         double *ucat) {
   (void)ctx;

@@ -14,7 +14,7 @@
 
 typedef struct {
   int n_init, n_destroy, n_last_error, n_setup, n_set_nvert, n_solver_mg, n_update, n_projection,
-      n_projection_cart;
+      n_projection_cart, n_convection, central_conv;
   int ntok;
   char tok[REC_MAXTOK][64];
   int nlevels;
@@ -30,6 +30,8 @@ typedef struct {
   const double *phi_proj;
   double *ucont_proj, dt_proj, st_proj;
   double *ubcs_proj, *ucat_proj;
+  const double *ucont_conv, *ucat_conv;
+  double *conv_conv;
   /* the status the next path call returns, then 0 again */
   int fail_next;
   /* cell (box index) the path calls write: solver_mg sets ucont[3m+1] = 42 and

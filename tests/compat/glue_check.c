@@ -17,7 +17,7 @@
 #include "cvb_record.h"
 #include "poisson_gb300.h"
 
-extern PetscInt block_number, immersed, wallfunction;
+extern PetscInt block_number, immersed, wallfunction, les;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
 UserMG *ref_usermg(void);
@@ -145,6 +145,28 @@ int main(void) {
         "wall function: host post-projection not used");
   wallfunction = 0;
   CHECK(shim_arrays_out() == 0, "host-path projections left %d arrays out", shim_arrays_out());
+
+  /* --- Convection: walled faces on the device, -central and les passed on.
+   * This box is periodic in x, so the faces are made walled for these calls
+   * and the box-shaped global vectors stand in for lUcont and lUcat (on one
+   * rank without periodic faces the two have the same layout). --- */
+  Vec Conv;
+  VecDuplicate(fine->Ucont, &Conv);
+  fine->bctype[0] = fine->bctype[1] = 1;
+  CHECK(Convection_GB300(fine, fine->Ucont, fine->Ucat, Conv) == 0 && REC.n_convection == 1 &&
+            REC.central_conv == 0, "convection not on the device");
+  CHECK(REC.ucont_conv == shim_vec_data(fine->Ucont) && REC.ucat_conv == shim_vec_data(fine->Ucat) &&
+            REC.conv_conv == shim_vec_data(Conv), "Ucont / Ucat / Conv storage");
+  CHECK(shim_vec_data(Conv)[3 * REC.mark] == 7.0, "Conv not written");
+  PetscOptionsSetValue("-central", "1");
+  CHECK(Convection_GB300(fine, fine->Ucont, fine->Ucat, Conv) == 0 && REC.central_conv == 1, "-central not passed");
+  PetscOptionsSetValue("-central", "0");
+  les = 1;
+  CHECK(Convection_GB300(fine, fine->Ucont, fine->Ucat, Conv) == 0 && REC.central_conv == 1, "les not passed");
+  les = 0;
+  fine->bctype[0] = fine->bctype[1] = 7;
+  VecDestroy(&Conv);
+  CHECK(shim_arrays_out() == 0, "convection left %d arrays out", shim_arrays_out());
 
   /* --- failures come back as the call's status, arrays restored --- */
   REC.fail_next = CVB_NOT_CONVERGED;
