@@ -364,6 +364,28 @@ __device__ __forceinline__ double conv_bracket(double x2, double x1, double x0) 
   return da(dm(0.125, da(ds(-x2, dm(2., x1)), dm(3., x0))), x1);
 }
 
+// 2 x, exactly, for |x| < 2^1000, on the integer pipe: one more in the
+// exponent field; a zero or subnormal x doubles its magnitude bits (the IEEE
+// encoding runs on from the subnormals into the normals without a seam).
+__device__ __forceinline__ double conv_twice(double x) {
+  const long long b = __double_as_longlong(x), mag = b & 0x7fffffffffffffffLL;
+  return __longlong_as_double((mag >> 52) ? b + (1LL << 52) : (b ^ mag) | (mag << 1));
+}
+// x / 8 where the result is subnormal: rounded by the FP64 multiply, out of line
+__device__ __noinline__ double conv_eighth_tiny(double x) { return dm(0.125, x); }
+// 0.125 x, exactly, for finite x: three less in the exponent field while the
+// result stays normal; a zero stays itself.
+__device__ __forceinline__ double conv_eighth(double x) {
+  const long long b = __double_as_longlong(x), e = (b >> 52) & 0x7ff;
+  if (e > 3) return __longlong_as_double(b - (3LL << 52));
+  if ((b & 0x7fffffffffffffffLL) == 0) return x;
+  return conv_eighth_tiny(x);
+}
+// conv_bracket for inputs below 2^1000, its exact scalings on the integer pipe
+__device__ __forceinline__ double conv_bracket_tame(double x2, double x1, double x0) {
+  return da(conv_eighth(da(ds(-x2, conv_twice(x1)), dm(3., x0))), x1);
+}
+
 // The full face flux um * bracket(u[hi], u[1], u[0]) + up * bracket(u[lo], u[0], u[1]),
 // with um = ucon - |ucon|, up = ucon + |ucon|.  Out of line, so that its
 // second bracket is evaluated only on this path.
@@ -385,7 +407,7 @@ __device__ __forceinline__ double conv_quick(const double *uc, long long p, long
                ul = uc[3 * (p + lo * st) + c];
   if (tame && conv_tame(uh) && conv_tame(u1) && conv_tame(u0) && conv_tame(ul)) {
     const bool pos = __double_as_longlong(ucon) >= 0;  // up live (ucon > 0), else um
-    const double r = dm(da(ucon, ucon), conv_bracket(pos ? ul : uh, pos ? u0 : u1, pos ? u1 : u0));
+    const double r = dm(conv_twice(ucon), conv_bracket_tame(pos ? ul : uh, pos ? u0 : u1, pos ? u1 : u0));
     if (conv_nonzero(r)) return r;
   }
   return conv_quick_full(ucon, uh, u1, u0, ul);
