@@ -413,7 +413,18 @@ __device__ __forceinline__ double conv_quick(const double *uc, long long p, long
   return conv_quick_full(ucon, uh, u1, u0, ul);
 }
 
-__device__ __forceinline__ bool conv_fluid(double n) { return n < 0.1 || n > 7.; }
+// n < c and n > c for a positive constant c, as IEEE compares, on the integer
+// pipe: a NaN compares false both ways, a negative n (or -0) is below c, and a
+// non-negative n orders as its bit pattern does.
+__device__ __forceinline__ bool conv_below(double n, double c) {
+  const long long b = __double_as_longlong(n), mag = b & 0x7fffffffffffffffLL;
+  return mag <= 0x7ff0000000000000LL && (b < 0 || mag < __double_as_longlong(c));
+}
+__device__ __forceinline__ bool conv_above(double n, double c) {
+  const long long b = __double_as_longlong(n);
+  return b >= 0 && b <= 0x7ff0000000000000LL && b > __double_as_longlong(c);
+}
+__device__ __forceinline__ bool conv_fluid(double n) { return conv_below(n, 0.1) || conv_above(n, 7.); }
 
 __global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__restrict__ ucont,
                                                    const double *__restrict__ ucat, const double *__restrict__ nv,
@@ -443,9 +454,9 @@ __global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__rest
           if (central) cen = 1; else { lo = -1; hi = 2; }
         } else if (central && end2 && conv_fluid(nv[p + s]) && conv_fluid(nv[p])) {
           cen = 1;
-        } else if ((d < 2 || q < m - 2) && (q == 0 || nv[p - s] > 0.1)) {
+        } else if ((d < 2 || q < m - 2) && (q == 0 || conv_above(nv[p - s], 0.1))) {
           lo = 0; hi = 2;
-        } else if ((d < 2 || q > 0) && (q == m - 2 || nv[p + s] > 0.1)) {
+        } else if ((d < 2 || q > 0) && (q == m - 2 || conv_above(nv[p + s], 0.1))) {
           lo = -1; hi = 1;
         } else {
           any = 0;
