@@ -17,7 +17,17 @@ static inline unsigned nblk(size_t n, int t) { return (unsigned)((n + t - 1) / t
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double mean2(double a, double b) { return dm(0.5, da(a, b)); }
+__device__ __noinline__ double half_slow(double x) { return dm(0.5, x); }
+// 0.5 x, as the FP64 multiply gives it, on the integer pipe: one less in the
+// exponent field while the result stays normal, and a zero stays itself.
+// Subnormal results, inf and NaN go through the multiply, out of line.
+__device__ __forceinline__ double half_exact(double x) {
+  const long long b = __double_as_longlong(x), e = (b >> 52) & 0x7ff;
+  if (e > 1 && e < 0x7ff) return __longlong_as_double(b - (1LL << 52));
+  if ((b & 0x7fffffffffffffffLL) == 0) return x;
+  return half_slow(x);
+}
+__device__ __forceinline__ double mean2(double a, double b) { return half_exact(da(a, b)); }
 // a*(b*c - d*e), the cofactor product of Cramer's rule
 __device__ __forceinline__ double cof(double a, double b, double c, double d, double e) {
   return dm(a, ds(dm(b, c), dm(d, e)));
