@@ -224,6 +224,19 @@ PetscErrorCode Projection_GB300(UserCtx *u) {
 PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
   for (int f = 0; f < 6; f++)
     if (u->bctype[f] == 7) return Convection(u, Ucont, Ucat, Conv);
+  /* one rank owning the whole box: each vector holds exactly its 3 mx my mz
+   * values (the library copies that many); nvert is the one the context was
+   * last given (PoissonSetNvert_GB300 after a body moves) */
+  const PetscInt want = 3 * (PetscInt)u->info.mx * u->info.my * u->info.mz;
+  PetscInt n_uc = -1, n_ucat = -1, n_conv = -1;
+  VecGetLocalSize(Ucont, &n_uc);
+  VecGetLocalSize(Ucat, &n_ucat);
+  VecGetLocalSize(Conv, &n_conv);
+  if (n_uc != want || n_ucat != want || n_conv != want) {
+    PetscPrintf(PETSC_COMM_WORLD, "Convection_GB300: vectors of %d/%d/%d values, box needs %d (one rank only)\n",
+                (int)n_uc, (int)n_ucat, (int)n_conv, (int)want);
+    return CVB_BAD_INPUT;
+  }
   PetscInt central = 0;
   PetscOptionsGetInt(PETSC_NULL, "-central", &central, PETSC_NULL);
   PetscScalar *uc, *ucat, *conv;

@@ -85,6 +85,9 @@ struct OpBatch {
 
 }  // namespace
 
+// cvb_batch_solve's bound on its host loop when the caller sets none
+constexpr long long kDefaultRoundLimit = 1000000;
+
 struct cvb_batch {
   int device = 0;
   cudaStream_t stream = nullptr, copy_stream = nullptr;
@@ -108,6 +111,7 @@ struct cvb_batch {
   std::deque<Done> done;
   int next_ticket = 0;
   long long launches_per_round = 0;
+  long long round_limit = kDefaultRoundLimit;  // rounds cvb_batch_solve issues before CVB_TIMEOUT
 };
 
 // ------------------------------------------------------------------ helpers
@@ -831,7 +835,12 @@ int cvb_batch_solve(cvb_batch *bt, int n, cvb_ctx *const *ctxs, cvb_solve_stats 
         left--;
       }
     }
-    if (++guard > 1000000) return bfail(bt, CVB_TIMEOUT, "batch did not finish");
+    if (++guard >= bt->round_limit && left > 0) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return bfail(bt, CVB_TIMEOUT, "batch did not finish within %lld rounds; %d solves still in flight",
+                   bt->round_limit, left);
+    }
   }
   BCK(cudaEventRecord(e1, bt->stream));
   BCK(cudaEventSynchronize(e1));
@@ -842,6 +851,12 @@ int cvb_batch_solve(cvb_batch *bt, int n, cvb_ctx *const *ctxs, cvb_solve_stats 
   if (stats)
     for (int q = 0; q < n; q++) stats[q].device_ms = ms;
   if (worst != CVB_OK) return bfail(bt, worst, "%s", "at least one solve of the batch did not converge");
+  return CVB_OK;
+}
+
+int cvb_batch_set_round_limit(cvb_batch *bt, long long rounds) {
+  if (!bt || rounds < 0) return CVB_BAD_INPUT;
+  bt->round_limit = rounds == 0 ? kDefaultRoundLimit : rounds;
   return CVB_OK;
 }
 

@@ -1,12 +1,14 @@
 // PoissonRHS on caller-owned device arrays with no device allocation at all.
 //
-// For callers that cannot call cudaMalloc: code running while a CUDA graph is
-// being captured, hosts whose device memory is handed out by their own
-// allocator (a PETSc or framework memory pool) and must not be fragmented, and
-// time-stepping loops that forbid allocation after start-up.  Inputs and outputs
-// are passed in; the only scratch -- one slot per reduction block for the
-// compatibility sum -- is the file-scope array below, which every GPU that loads
-// this library holds until the process exits.
+// For callers that cannot call cudaMalloc: hosts whose device memory is handed
+// out by their own allocator (a PETSc or framework memory pool) and must not be
+// fragmented or exceeded behind the pool's back, and time-stepping loops that
+// forbid allocation after start-up so that a long run cannot fail half-way on
+// memory.  Inputs and outputs are passed in; the only scratch -- one slot per
+// reduction block for the compatibility sum -- is the file-scope array below,
+// which every GPU that loads this library holds until the process exits.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "../../include/cvb.h"
@@ -19,22 +21,45 @@ static __device__ __align__(256) double g_rhs_scratch[2 * CVB_NOALLOC_MAX_BLOCKS
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-double *g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+  CUcontext ctx = nullptr;  // the context the address belongs to
+  double *ptr = nullptr;
+};
+ScratchAddr g_scratch[kMaxDevices];
 
-// Device address of g_rhs_scratch on the current device, looked up once per
-// device.  In host code the symbol is only a host-side stand-in; a kernel must
-// be given this address instead.
+// Device address of g_rhs_scratch in the current context.  In host code the
+// symbol is only a host-side stand-in; a kernel must be given this address.
+// The lookup runs once per device (the first call there, with that device
+// current) and again only if the device's context was replaced since
+// (cudaDeviceReset and a new primary context can load the module elsewhere).
 int scratch_for_current_device(double **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CVB_CUDA_ERROR;
+  // binds the device's primary context to this thread (CUDA 12+ initialises it here)
+  if (cudaSetDevice(dev) != cudaSuccess) return CVB_CUDA_ERROR;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
+  // cuCtxGetCurrent through the runtime's driver entry point: the library
+  // does not link the driver library itself
+  static CUresult (*get_current)(CUcontext *) = nullptr;
+  if (!get_current) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return CVB_CUDA_ERROR;
+    get_current = reinterpret_cast<CUresult (*)(CUcontext *)>(fn);
+  }
+  CUcontext cur = nullptr;
+  if (get_current(&cur) != CUDA_SUCCESS || !cur) return CVB_CUDA_ERROR;
+  ScratchAddr &a = g_scratch[dev];
+  if (!a.ptr || a.ctx != cur) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_rhs_scratch);
     if (e != cudaSuccess || !p) return CVB_CUDA_ERROR;
-    g_scratch_addr[dev] = static_cast<double *>(p);
+    a.ptr = static_cast<double *>(p);
+    a.ctx = cur;
   }
-  *out = g_scratch_addr[dev];
+  *out = a.ptr;
   return CVB_OK;
 }
 

@@ -423,6 +423,11 @@ class SolveBatch:
         self._check(self._L.cvb_batch_read_phi(self._b, ctx._ctx, ptr(phi)))
         return phi
 
+    def set_round_limit(self, rounds):
+        """Bound ``solve``'s loop to ``rounds`` rounds (0: the default); past it
+        ``solve`` raises CVB_TIMEOUT with the unfinished solves still in flight."""
+        self._check(self._L.cvb_batch_set_round_limit(self._b, int(rounds)))
+
     def solve(self, ctxs):
         """Solve every context's resident rhs; returns their stats in order."""
         n = len(ctxs)

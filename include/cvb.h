@@ -212,8 +212,11 @@ int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at);
  * forms of the reference next to the ring and next to cells of nvert above
  * 0.1; 0 on the ring.  ucont, ucat and conv are [mz][my][mx][3].  ucont NULL
  * uses the device copy of Ucont the last projection left, ucat NULL the device
- * Ucat of the last cvb_projection_cart.  Boxes with a periodic face (bctype
- * 7) are refused with CVB_BAD_INPUT. */
+ * Ucat of the last cvb_projection_cart.  The nvert it tests is the context's
+ * finest-level nvert, as the last cvb_setup_hierarchy or cvb_set_nvert gave it
+ * (the reference reads lNvert on every call: after a body moves, call
+ * cvb_set_nvert first).  Boxes with a periodic face (bctype 7) are refused with
+ * CVB_BAD_INPUT. */
 int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
@@ -300,23 +303,26 @@ int cvb_nullspace(cvb_ctx *ctx, int level, double *x);
 /* --- allocation-free form ------------------------------------------------ */
 /* PoissonRHS on device arrays without allocating any device memory.  This entry
  * point has no counterpart in the reference.  It is for callers that cannot call
- * cudaMalloc: code running while a CUDA graph is being captured, hosts whose
- * device memory comes from their own allocator or pool, and time loops that
- * forbid allocation after start-up.
+ * cudaMalloc: hosts whose device memory is handed out by their own allocator or
+ * pool (a PETSc or framework pool that must not be bypassed or fragmented), and
+ * time-stepping loops that forbid allocation after start-up so that a long run
+ * cannot fail half-way on memory.
  *
  * d_ucont ([mz][my][mx] Cmpnts), d_aj, d_nvert ([mz][my][mx]) and the outputs
  * d_b ([mz][my][mx]) and d_compat_sum (one double, the sum PoissonRHS prints)
- * are device pointers owned by the caller; stream is a cudaStream_t (NULL: the
- * legacy default stream).  Results equal cvb_poisson_rhs's bit for bit.
+ * are device pointers owned by the caller; stream is a cudaStream_t of the
+ * current device (NULL: the legacy default stream).  Results equal
+ * cvb_poisson_rhs's bit for bit.
  *
  * The only scratch is a fixed file-scope device array of 2*CVB_NOALLOC_MAX_BLOCKS
  * doubles (32 KB) that every GPU loading this library holds until the process
  * exits.  Boxes larger than CVB_NOALLOC_MAX_CELLS cells are rejected with
- * CVB_BAD_INPUT.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Every call shares the array and leaves its last
- * contents there; each call overwrites every slot it reads, so nothing needs
- * clearing, but calls that overlap on the GPU (concurrent streams or host
+ * CVB_BAD_INPUT.  The first call on each device (and the first after that
+ * device's context was replaced, e.g. by cudaDeviceReset) looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  Every call shares the array and leaves
+ * its last contents there; each call overwrites every slot it reads, so nothing
+ * needs clearing, but calls that overlap on the GPU (concurrent streams or host
  * threads) race on it and must be serialised by the caller. */
 #define CVB_NOALLOC_MAX_BLOCKS 2048
 #define CVB_NOALLOC_MAX_CELLS (64 * 1024 * 1024)
@@ -361,6 +367,12 @@ int cvb_batch_read_phi(cvb_batch *batch, cvb_ctx *ctx, double *host_phi);
 /* Submit n solves with the batch's options and run them to completion. */
 int cvb_batch_solve(cvb_batch *batch, int n, cvb_ctx *const *ctxs, cvb_solve_stats *stats);
 int cvb_batch_in_flight(const cvb_batch *batch);
+/* Bound cvb_batch_solve's loop to `rounds` rounds (0: the default, 10^6).  When
+ * the bound is reached with solves unfinished it returns CVB_TIMEOUT and the
+ * batch stays usable: the unfinished solves are still in flight, and
+ * cvb_batch_step / cvb_batch_poll carry them on to their results.  No
+ * counterpart in the reference, whose KSPSolve has only max_it. */
+int cvb_batch_set_round_limit(cvb_batch *batch, long long rounds);
 /* Device memory held by a context alone (operators, vectors, Krylov basis) and
  * by its grid's shared metrics, with an id that is equal for contexts sharing them. */
 int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes);

@@ -14,9 +14,13 @@
 # only.  Entry points the reference calls but the parity path never reaches
 # (SNES, KSP, other CURVIB files) become stubs that return a PETSc error code.
 #
-# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default: /root/reference)
+# usage: oracle/build_ref.sh REFERENCE_DIR
 set -euo pipefail
-REF="${1:-/root/reference}"
+if [ $# -lt 1 ]; then
+  echo "usage: $0 REFERENCE_DIR" >&2
+  exit 2
+fi
+REF="$1"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/poisson.c" ]; then

@@ -19,7 +19,20 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libcvboracle.so"
 REF_LIB = HERE / "_ref" / "libcvbref.so"
-REF_DIR = Path(os.environ.get("CVB_REFERENCE_DIR", "/root/reference"))
+# The reference checkout: CVB_REFERENCE_DIR, else the directory the last
+# build_reference() compiled from (recorded in oracle/_ref/), else none.
+_REF_RECORD = HERE / "_ref" / "REFERENCE_DIR"
+
+
+def _reference_dir() -> Path:
+    if os.environ.get("CVB_REFERENCE_DIR"):
+        return Path(os.environ["CVB_REFERENCE_DIR"])
+    if _REF_RECORD.exists():
+        return Path(_REF_RECORD.read_text().strip())
+    return HERE / "_ref" / "no-reference-checkout"
+
+
+REF_DIR = _reference_dir()
 
 _lib = None
 _ref = None
@@ -35,11 +48,20 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
-def build_reference() -> Path | None:
-    if not (REF_DIR / "poisson.c").exists():
+def build_reference(ref_dir=None) -> Path | None:
+    """Compile the reference's sources in ``ref_dir`` (default: CVB_REFERENCE_DIR,
+    else the checkout recorded by the last build) against the API shim into
+    oracle/_ref/; None when there is no checkout or it holds no poisson.c."""
+    global REF_DIR
+    if ref_dir is None:
+        ref_dir = os.environ.get("CVB_REFERENCE_DIR") or _reference_dir()
+    if not ref_dir or not (Path(ref_dir) / "poisson.c").exists():
         return None
-    subprocess.run(["bash", str(HERE / "build_ref.sh"), str(REF_DIR)], check=True,
+    ref_dir = Path(ref_dir).resolve()
+    subprocess.run(["bash", str(HERE / "build_ref.sh"), str(ref_dir)], check=True,
                    stdout=subprocess.DEVNULL)
+    _REF_RECORD.write_text(str(ref_dir) + "\n")
+    REF_DIR = ref_dir
     return REF_LIB
 
 

@@ -10,11 +10,11 @@ in ibm_meshes.npz, and the checks Divergence (main.c) and MetricsDivergence
 GhostNodeVelocity) also run on the variants of cases.POST_VARIANTS, which put
 slip, moving-lid and O-grid faces and blanked cells on the same grids.  The
 inputs (node coordinates, nvert, fluxes) are stored beside the digests so the
-tests do not depend on the platform's sin/tanh.  Needs the reference checkout
-(default /root/reference, or CVB_REFERENCE_DIR); the fixtures it writes are
+tests do not depend on the platform's sin/tanh.  Needs the reference checkout,
+given as the argument or in CVB_REFERENCE_DIR; the fixtures it writes are
 committed and the tests read only those.
 
-usage: python tests/golden/make_golden.py
+usage: python tests/golden/make_golden.py REFERENCE_DIR
 """
 from __future__ import annotations
 
@@ -134,6 +134,10 @@ def run_ibm(name, meshes_out):
 
 
 def main():
+    import os
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CVB_REFERENCE_DIR")
+    if not ref or O.build_reference(ref) is None:
+        sys.exit("usage: make_golden.py REFERENCE_DIR (or set CVB_REFERENCE_DIR): no reference sources given")
     out = {"dt": DT, "st": ST, "scenarios": {}, "post_variants": {}, "ibm": {}}
     for name in SCENARIOS:
         out["scenarios"][name] = run(name)

@@ -134,3 +134,43 @@ def test_rejects_a_context_twice(items):
         assert len(B.poll()) == 1
     finally:
         B.close()
+
+
+def test_round_limit_times_out_and_batch_stays_usable(items):
+    """A round limit below what the solves need makes cvb_batch_solve return
+    CVB_TIMEOUT with the solves still in flight; stepping and polling then carry
+    them to the results they give without a limit, and the batch solves again
+    once the limit is lifted."""
+    from curvib_old_gb300._lib import CVB_TIMEOUT, CvbError
+    from curvib_old_gb300.solver import SolveBatch
+    sel = [0, 1, 2]
+    _, alone = _run(items, 1, sel)
+    B = SolveBatch(precision=1, rtol=RTOL, max_it=100)
+    try:
+        for q in sel:
+            items[q][0].set_rhs(items[q][2])
+        B.set_round_limit(2)
+        with pytest.raises(CvbError) as e:
+            B.solve([items[q][0] for q in sel])
+        assert e.value.status == CVB_TIMEOUT
+        assert B.step() > 0
+        done = 0
+        for _ in range(10000):
+            left = B.step()
+            for t, st in B.poll():
+                assert st["status"] == 0, st
+                done += 1
+            if left == 0:
+                break
+        assert done == len(sel)
+        for k, q in enumerate(sel):
+            assert np.array_equal(items[q][0].get_phi(), alone[k]), q
+        B.set_round_limit(0)
+        for q in sel:
+            items[q][0].set_rhs(items[q][2])
+        sts = B.solve([items[q][0] for q in sel])
+        assert all(st["status"] == 0 for st in sts)
+        for k, q in enumerate(sel):
+            assert np.array_equal(items[q][0].get_phi(), alone[k]), q
+    finally:
+        B.close()
