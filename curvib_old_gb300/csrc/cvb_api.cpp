@@ -202,7 +202,13 @@ static int check_desc(cvb_ctx *ctx, const cvb_level_desc &d, int level, bool fin
   return CVB_OK;
 }
 
-// Gauss-Jordan inverse with partial pivoting (coarsest level, n <= a few thousand).
+// Largest coarsest box (ring included) solved by a dense inverse unless the
+// options say otherwise: 18^3 = 5832 holds a 16^3-cell coarsest level.
+constexpr int kCoarseDenseMaxDefault = 6000;
+// Largest coarsest block inverted on the host; larger ones go to the device.
+constexpr int kHostInverseMax = 384;
+
+// Gauss-Jordan inverse with partial pivoting (coarsest level, n <= kHostInverseMax).
 static bool dense_inverse(std::vector<double> &A, int n, std::vector<double> &Inv) {
   Inv.assign((size_t)n * n, 0.0);
   for (int i = 0; i < n; i++) Inv[(size_t)i * n + i] = 1.0;
@@ -245,7 +251,7 @@ static int build_coarse(cvb_ctx *ctx, const cvb_solve_opts *opt) {
   LevelDev &C = ctx->L[0];
   size_t n = C.g.n();
   ctx->ncoarse = (int)n;
-  int dense_max = opt ? opt->coarse_dense_max : 2048;
+  int dense_max = opt ? opt->coarse_dense_max : kCoarseDenseMaxDefault;
   ctx->coarse_dense = (int)n <= dense_max;
   if (!ctx->coarse_dense) return CVB_OK;
   std::vector<double> w(n * NSLOT), nv(n);
@@ -308,13 +314,35 @@ static int build_coarse(cvb_ctx *ctx, const cvb_solve_opts *opt) {
       }
     }
   }
-  std::vector<double> Inv;
-  if (m > 0 && !dense_inverse(A, m, Inv)) return fail(ctx, CVB_BAD_INPUT, "coarsest operator is singular after regularisation");
   if (ctx->Minv) dfree(ctx, ctx->Minv);
   if (ctx->cidx) dfree(ctx, ctx->cidx);
+  ctx->Minv = nullptr;
+  ctx->cidx = nullptr;
   TRY(dalloc(ctx, &ctx->Minv, std::max((size_t)m * m, (size_t)1)));
   TRY(dalloc(ctx, &ctx->cidx, n));
-  if (m > 0) CK(cudaMemcpyAsync(ctx->Minv, Inv.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
+  if (m > kHostInverseMax) {
+    // thousands of unknowns (a 16^3 coarsest level): Gauss-Jordan on the device
+    double *dA = nullptr, *dwork = nullptr;
+    int *iwork = nullptr;
+    TRY(dalloc(ctx, &dA, (size_t)m * m));
+    int rc = dalloc(ctx, &dwork, 2 * (size_t)m);
+    if (rc == CVB_OK) rc = dalloc(ctx, &iwork, 2 * (size_t)m + 1);
+    bool ok = false;
+    if (rc == CVB_OK && cudaMemcpyAsync(dA, A.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice,
+                                        ctx->stream) == cudaSuccess)
+      ok = device_dense_inverse(dA, m, ctx->Minv, iwork, iwork + m, dwork, dwork + m, iwork + 2 * m, ctx->stream);
+    if (iwork) dfree(ctx, iwork);
+    if (dwork) dfree(ctx, dwork);
+    dfree(ctx, dA);
+    if (rc != CVB_OK) return rc;
+    CK(cudaGetLastError());
+    if (!ok) return fail(ctx, CVB_BAD_INPUT, "coarsest operator is singular after regularisation");
+  } else if (m > 0) {
+    std::vector<double> Inv;
+    if (!dense_inverse(A, m, Inv)) return fail(ctx, CVB_BAD_INPUT, "coarsest operator is singular after regularisation");
+    CK(cudaMemcpyAsync(ctx->Minv, Inv.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   CK(cudaMemcpyAsync(ctx->cidx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   C.cidx = ctx->cidx;
@@ -1005,7 +1033,7 @@ int cvb_solve_opts_default(cvb_solve_opts *o) {
   o->omega = 1.3;
   o->project_rhs = 1;
   o->warm_start = 0;
-  o->coarse_dense_max = 2048;
+  o->coarse_dense_max = kCoarseDenseMaxDefault;
   o->cgs_refine = 0;
   o->smoother = CVB_SMOOTHER_ZEBRA;
   return CVB_OK;

@@ -220,6 +220,11 @@ __device__ __forceinline__ double quot_newton(double b, double a) {
   return b * r;
 }
 // coarsest solve e = M^-1 r on C.cidx[0..C.cm), e = r on the other cells
+// In-place Gauss-Jordan inverse of the n x n row-major A on the device into
+// out (kernels_setup.cu); false for a singular matrix.  Work arrays: perm and
+// colmap n ints, prow and fcol n doubles, status one int.
+bool device_dense_inverse(double *A, int n, double *out, int *perm, int *colmap, double *prow, double *fcol,
+                          int *status, cudaStream_t s);
 void launch_dense_apply(const LevelDev &C, const double *Minv, const double *r, double *e, cudaStream_t s,
                         const int *gate = nullptr);
 void launch_dense_apply_f32(const LevelDev &C, const double *Minv, const float *r, float *e, cudaStream_t s,

@@ -1,6 +1,9 @@
 // Set-up kernels: face coefficients, switching codes, FP64 stencil weights,
 // y-line Thomas factors and the immersed-boundary restriction of nvert.
 // Run once per problem (or whenever nvert changes); the solve reuses the result.
+#include <algorithm>
+#include <vector>
+
 #include "launch.cuh"
 
 namespace cvb {
@@ -323,6 +326,123 @@ void launch_nvert_restrict(const Geom &fine, const double *nvf, const Geom &coar
   k_nvert_pass1<<<nblk(coarse.n(), 256), 256, 0, s>>>(fine, nvf, coarse, isc, jsc, ksc, tmp); count_launch();
   cudaMemcpyAsync(nvc, tmp, sizeof(double) * coarse.n(), cudaMemcpyDeviceToDevice, s);
   k_nvert_pass2<<<nblk(coarse.n(), 256), 256, 0, s>>>(coarse, tmp, nvc); count_launch();
+}
+
+}  // namespace cvb
+
+namespace cvb {
+
+// ------------------------------------------------------------------ dense inverse
+// Gauss-Jordan inversion in place with partial pivoting, one column per step,
+// for the coarsest level's matrix when it is too large to invert on the host
+// in reasonable time (thousands of unknowns).  Step c: k_gj_pivot (one block)
+// picks the row of largest |A[r][c]| at or below c (the first of equal ones),
+// swaps it into row c, and stages the scaled pivot row (A[c][q] / A[c][c], with
+// 1 / A[c][c] in column c, the inverse's column) and the multipliers A[r][c];
+// k_gj_elim then updates every row from the staged copies, so no thread reads
+// what another writes.  The row swaps become column swaps of the result,
+// undone by k_gj_unpermute from the composed column map.
+constexpr int kGjThreads = 1024;
+
+__global__ void __launch_bounds__(kGjThreads) k_gj_pivot(double *__restrict__ A, int n, int c, int *__restrict__ perm,
+                                                         double *__restrict__ prow, double *__restrict__ fcol,
+                                                         int *__restrict__ status) {
+  if (*status) return;
+  __shared__ double sv[kGjThreads / 32];
+  __shared__ int si[kGjThreads / 32];
+  __shared__ int s_piv;
+  double best = -1.0;
+  int bi = n;
+  for (int r = c + threadIdx.x; r < n; r += blockDim.x) {
+    double v = fabs(A[(size_t)r * n + c]);
+    if (v > best) { best = v; bi = r; }  // NaN never wins
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_down_sync(0xffffffffu, best, o);
+    int oi = __shfl_down_sync(0xffffffffu, bi, o);
+    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sv[wid] = best; si[wid] = bi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = sv[0];
+    int i = si[0];
+    for (int w = 1; w < (int)(blockDim.x / 32); w++)
+      if (sv[w] > b || (sv[w] == b && si[w] < i)) { b = sv[w]; i = si[w]; }
+    if (!(b > 0.0) || i >= n) {
+      *status = 1;
+      i = -1;
+    } else {
+      perm[c] = i;
+    }
+    s_piv = i;
+  }
+  __syncthreads();
+  const int p = s_piv;
+  if (p < 0) return;
+  if (p != c)
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      double a = A[(size_t)c * n + q];
+      A[(size_t)c * n + q] = A[(size_t)p * n + q];
+      A[(size_t)p * n + q] = a;
+    }
+  __syncthreads();
+  const double inv = 1.0 / A[(size_t)c * n + c];
+  for (int q = threadIdx.x; q < n; q += blockDim.x)
+    prow[q] = q == c ? inv : __dmul_rn(A[(size_t)c * n + q], inv);
+  for (int r = threadIdx.x; r < n; r += blockDim.x) fcol[r] = r == c ? 0.0 : A[(size_t)r * n + c];
+}
+
+__global__ void k_gj_elim(double *__restrict__ A, int n, int c, const double *__restrict__ prow,
+                          const double *__restrict__ fcol, const int *__restrict__ status) {
+  if (*status) return;
+  const size_t nn = (size_t)n * n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(e / n), q = (int)(e % n);
+    if (r == c) {
+      A[e] = prow[q];
+      continue;
+    }
+    double f = fcol[r];
+    if (f == 0.0) continue;  // column c of this row is already 0
+    double a = q == c ? 0.0 : A[e];
+    A[e] = __dsub_rn(a, __dmul_rn(f, prow[q]));
+  }
+}
+
+__global__ void k_gj_unpermute(const double *__restrict__ A, int n, const int *__restrict__ colmap,
+                               double *__restrict__ out) {
+  const size_t nn = (size_t)n * n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(e / n), q = (int)(e % n);
+    out[e] = A[(size_t)r * n + colmap[q]];
+  }
+}
+
+// Inverts the n x n row-major A (device, overwritten) into out (device).
+// perm / colmap are n ints, prow / fcol n doubles, status one int (device).
+// Returns false if a pivot column was all zero (a singular matrix).
+bool device_dense_inverse(double *A, int n, double *out, int *perm, int *colmap, double *prow, double *fcol,
+                          int *status, cudaStream_t s) {
+  cudaMemsetAsync(status, 0, sizeof(int), s);
+  const unsigned eb = (unsigned)std::min<size_t>(((size_t)n * n + 255) / 256, (size_t)152 * 16);
+  for (int c = 0; c < n; c++) {
+    k_gj_pivot<<<1, kGjThreads, 0, s>>>(A, n, c, perm, prow, fcol, status); count_launch();
+    k_gj_elim<<<eb, 256, 0, s>>>(A, n, c, prow, fcol, status); count_launch();
+  }
+  int h_status = 0;
+  std::vector<int> h_perm(n), map(n);
+  cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(h_perm.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess || h_status) return false;
+  // row swaps (c, perm[c]) in order become column swaps of the inverse in
+  // reverse order: out[:, q] = A[:, map[q]]
+  for (int q = 0; q < n; q++) map[q] = q;
+  for (int c = n - 1; c >= 0; c--) std::swap(map[c], map[h_perm[c]]);
+  cudaMemcpyAsync(colmap, map.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+  k_gj_unpermute<<<eb, 256, 0, s>>>(A, n, colmap, out); count_launch();
+  return cudaStreamSynchronize(s) == cudaSuccess;
 }
 
 }  // namespace cvb

@@ -358,12 +358,14 @@ def capacity(inputs, stream, device=0, precision=_lib.MIXED, rtol=1e-8, budget_b
 
 
 def serve(requests=200, load=0.8, budget_gb=150.0, max_cells=256, precision=_lib.MIXED, device=0,
-          time_limit=600.0, probe=24, inputs=None):
+          time_limit=600.0, probe=24, inputs=None, results=None):
     """Measure the batched capacity of the served workload -- the whole stream
     queued at once, set-ups included -- then serve the stream with Poisson
     arrivals at `load` times that rate.  Returns the report, with the solve-only
     batched capacity of the stream's first problems beside it.  `inputs`: the
-    prepared Inputs of make_stream(requests, 1.0, 4, max_cells), to reuse."""
+    prepared Inputs of make_stream(requests, 1.0, 4, max_cells), to reuse.
+    `results`: a dict to fill with request id -> (pressure, statistics) of the
+    paced run."""
     proto = make_stream(requests, 1.0, seed=4, max_cells=max_cells)
     t0 = time.perf_counter()
     if inputs is None:
@@ -379,9 +381,11 @@ def serve(requests=200, load=0.8, budget_gb=150.0, max_cells=256, precision=_lib
     cap = sat["solves_per_s"]
     rate = load * cap
     stream = [dataclasses.replace(r, arrival=r.arrival / rate) for r in proto]
-    srv = Server(inputs, device, budget_gb * 1e9, precision)
+    srv = Server(inputs, device, budget_gb * 1e9, precision, keep_results=results is not None)
     try:
         out = srv.run(stream, time_limit)
+        if results is not None:
+            results.update(srv.results)
     finally:
         srv.close()
     sizes = [r.n for r in stream]

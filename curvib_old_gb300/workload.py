@@ -597,18 +597,23 @@ def make_problem(cells, lengths=(1.0, 1.0, 1.0), beta_y=0.0, distort=False, per=
     return Problem(mets, nv, uc, bct, semi, per, name)
 
 
-def config0_problem(n=64):
-    """64^3 box on [0,1]^3, tanh stretching 2.0 in y, sin distortion, sphere r=0.15 at the centre."""
+def config0_problem(n=64, nlevels=3):
+    """64^3 box on [0,1]^3, tanh stretching 2.0 in y, sin distortion, sphere
+    r=0.15 at the centre; 3 multigrid levels (64, 32, 16 cells) as the
+    workload states (None: as many as auto_levels allows)."""
     return make_problem((n, n, n), (1.0, 1.0, 1.0), 2.0, True, (False, False, False),
-                        [(0.5, 0.5, 0.5, 0.15)], name=f"box{n}^3-sphere")
+                        [(0.5, 0.5, 0.5, 0.15)], nlevels=nlevels, name=f"box{n}^3-sphere")
 
 
-def config1_problem(cells=(256, 128, 128)):
+def config1_problem(cells=(256, 128, 128), nlevels=5):
     """Channel: periodic x and z, walls in y with tanh stretching 2.5, no body.
     The box is 2pi x 2 x pi (a standard minimal-channel size; the grid and the
-    stretching are the fixed part of the workload)."""
+    stretching are the fixed part of the workload).  5 multigrid levels as the
+    workload states (None: as many as auto_levels allows)."""
+    if nlevels is not None:
+        nlevels = min(nlevels, auto_levels(cells, (True, False, True), max_coarse_box=0))
     return make_problem(cells, (2 * np.pi, 2.0, np.pi), 2.5, False, (True, False, True), [],
-                        velocity="noise", seed=1, name="channel%dx%dx%d" % tuple(cells))
+                        velocity="noise", seed=1, nlevels=nlevels, name="channel%dx%dx%d" % tuple(cells))
 
 
 CONFIG3_SIZES = ((32, 32, 32), (48, 48, 48), (64, 64, 96), (96, 96, 96), (128, 64, 64))

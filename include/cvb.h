@@ -91,7 +91,8 @@ typedef struct {
   double omega;        /* relaxation factor (Jacobi: damping; zebra: over-relaxation) */
   int project_rhs;     /* remove b's component outside range(A) (fluid-weighted mean of b/aj) */
   int warm_start;      /* use phi's input values as the initial guess */
-  int coarse_dense_max;/* largest coarsest-level box solved exactly by a dense inverse */
+  int coarse_dense_max;/* largest coarsest-level box (ring included) solved exactly by a dense
+                          inverse (default 6000); larger ones get 30 smoothing sweeps */
   int cgs_refine;      /* 1: second Gram-Schmidt pass when the first cancels most of w
                           (PETSc's KSPGMRESSetCGSRefinementType IFNEEDED); 0: never (its default) */
   int smoother;        /* cvb_smoother: the multigrid smoother */

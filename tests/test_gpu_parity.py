@@ -14,6 +14,7 @@ import pytest
 
 from cases import SCENARIOS, build, seeded
 from oracle import oracle as O
+from parity_util import weights_to_csr as _weights_to_csr
 
 pytestmark = pytest.mark.gpu
 
@@ -45,40 +46,6 @@ def ctxs():
     yield out
     for c, _, _ in out.values():
         c.close()
-
-
-SLOTS = ["CP", "EP", "WP", "NP", "SP", "TP", "BP", "NE", "SE", "NW", "SW", "TN", "BN", "TS", "BS", "TE", "BE",
-         "TW", "BW"]
-
-
-def _weights_to_csr(w, shape, bctype):
-    """The stored rows as a sparse matrix, columns wrapped like the reference."""
-    import scipy.sparse as sp
-    mz, my, mx = shape
-    px, py, pz = bctype[0] == 7, bctype[2] == 7, bctype[4] == 7
-    K, J, I = np.meshgrid(np.arange(mz), np.arange(my), np.arange(mx), indexing="ij")
-
-    def up(a, m, p):
-        return np.where(p & (a == m - 2), 1, a + 1)
-
-    def dn(a, m, p):
-        return np.where(p & (a == 1), m - 2, a - 1)
-    iu, id_, ju, jd, ku, kd = up(I, mx, px), dn(I, mx, px), up(J, my, py), dn(J, my, py), up(K, mz, pz), dn(K, mz, pz)
-    off = {"CP": (I, J, K), "EP": (iu, J, K), "WP": (id_, J, K), "NP": (I, ju, K), "SP": (I, jd, K),
-           "TP": (I, J, ku), "BP": (I, J, kd), "NE": (iu, ju, K), "SE": (iu, jd, K), "NW": (id_, ju, K),
-           "SW": (id_, jd, K), "TN": (I, ju, ku), "BN": (I, ju, kd), "TS": (I, jd, ku), "BS": (I, jd, kd),
-           "TE": (iu, J, ku), "BE": (iu, J, kd), "TW": (id_, J, ku), "BW": (id_, J, kd)}
-    rows, cols, vals = [], [], []
-    n = mx * my * mz
-    for s, nm in enumerate(SLOTS):
-        a, b, c = off[nm]
-        ok = (a >= 0) & (a < mx) & (b >= 0) & (b < my) & (c >= 0) & (c < mz) & (w[s] != 0)
-        r = np.arange(n).reshape(shape)[ok]
-        cc = (c * my + b) * mx + a
-        rows.append(r)
-        cols.append(cc[ok])
-        vals.append(w[s][ok])
-    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
 
 
 @pytest.mark.parametrize("name", sorted(SCENARIOS))
