@@ -20,9 +20,11 @@
   reference operator with both region means pinned.
 
 The pressure bar is the one the port states: within 1e-8 relative L2, mean
-removed, of an FP64 solve (here the GPU at rtol 1e-10 against the oracle at
-1e-12; the oracle at 1e-10 is itself within about 5e-10 of its 1e-12 answer on
-the 64^3 box).
+removed, of an FP64 solve.  Both sides are converged to rtol 1e-12 first: the
+solution error of a solve stopped at rtol r is up to the operator's condition
+number times r, and the stretched 256x128x128 channel stopped at 1e-10 is
+already 1.6e-8 from its converged pressure (the oracle's own 1e-10 answer on
+the 64^3 box is 4e-10 from its 1e-12 one).
 """
 import numpy as np
 import pytest
@@ -33,7 +35,7 @@ from parity_util import direct_solution, fluid_mask, mean_removed_error, weights
 pytestmark = pytest.mark.gpu
 
 DT, ST = 1e-3, 1.0
-GPU_RTOL, ORACLE_RTOL = 1e-10, 1e-12
+GPU_RTOL, ORACLE_RTOL = 1e-12, 1e-12
 PHI_BAR = 1e-8
 
 
@@ -74,10 +76,10 @@ def _check_applies(ctx, Ls, levels):
 def _check_solves(ctx, P, Ls, b, x_ref, regions):
     A = O.lhs_csr(Ls[-1])
     for precision in (0, 1):
-        phi, st = ctx.solve(b, precision=precision, rtol=GPU_RTOL, max_it=200)
+        phi, st = ctx.solve(b, precision=precision, rtol=GPU_RTOL, max_it=400)
         assert st["status"] == 0 and st["rel_residual"] <= GPU_RTOL, st
         r = b.ravel() - A @ phi.ravel()
-        assert np.linalg.norm(r) <= 1.5 * GPU_RTOL * np.linalg.norm(b), precision
+        assert np.linalg.norm(r) <= 2 * GPU_RTOL * np.linalg.norm(b), precision
         err = mean_removed_error(phi, x_ref, regions)
         assert err <= PHI_BAR, (precision, err)
         fl = np.zeros(b.shape, dtype=bool)
@@ -159,7 +161,7 @@ def test_box_classes_batched_vs_oracle():
     assert seen == set(W.CONFIG3_SIZES)
     try:
         for precision in (0, 1):
-            B = SolveBatch(precision=precision, rtol=GPU_RTOL, max_it=200)
+            B = SolveBatch(precision=precision, rtol=GPU_RTOL, max_it=400)
             try:
                 for _, _, b, ctx in items:
                     ctx.set_rhs(b)
