@@ -454,9 +454,9 @@ void tune_file_load() {
   if (!f) return;
   ShapeKey k;
   cvb_ctx::Tune t;
-  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf", &k.mx, &k.my, &k.mz, &k.px, &k.py,
-                     &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0], &t.us64[1], &t.zb32[0], &t.zb32[1],
-                     &t.zb64[0], &t.zb64[1]) == 16) {
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf", &k.mx, &k.my, &k.mz,
+                     &k.px, &k.py, &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0], &t.us64[1], &t.zb32[0],
+                     &t.zb32[1], &t.zb64[0], &t.zb64[1], &t.zt32[0], &t.zt32[1], &t.zt32[2]) == 19) {
     t.level = 0;
     t.cells = (size_t)k.mx * k.my * k.mz;
     g_tune_cache.emplace(k, t);
@@ -468,9 +468,9 @@ void tune_file_append(const ShapeKey &k, const cvb_ctx::Tune &t) {
   if (!path || !*path) return;
   FILE *f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz, k.px, k.py,
-               k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0], t.zb32[1], t.zb64[0],
-               t.zb64[1]);
+  std::fprintf(f, "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz,
+               k.px, k.py, k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0], t.zb32[1],
+               t.zb64[0], t.zb64[1], t.zt32[0], t.zt32[1], t.zt32[2]);
   std::fclose(f);
 }
 }  // namespace
@@ -489,6 +489,14 @@ static int autotune_sweeps(cvb_ctx *ctx) {
       // two-kernel form, so the choice does not flip with timing noise
       L.zfuse32 = t.zb32[1] > 0.0 && t.zb32[1] < 0.97 * t.zb32[0] ? 1 : 0;
       L.zfuse64 = t.zb64[1] > 0.0 && t.zb64[1] < 0.97 * t.zb64[0] ? 1 : 0;
+      // the TMA-staged FP32 half-sweep and its chunk of row pairs, on the same
+      // 3 % rule against the better of the other two forms
+      const double other = L.zfuse32 ? t.zb32[1] : t.zb32[0];
+      L.ztma32 = 0;
+      double best = 0.97 * other;
+      const int rps[3] = {4, 8, 16};
+      for (int v = 0; v < 3; v++)
+        if (t.zt32[v] > 0.0 && t.zt32[v] < best) { best = t.zt32[v]; L.ztma32 = rps[v]; }
     };
     {
       std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -525,6 +533,7 @@ static int autotune_sweeps(cvb_ctx *ctx) {
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         (prec == 0 ? t.us32 : t.us64)[v] = 1e3 * ms / reps;
       }
+    L.ztma32 = 0;
     // zebra sweep (both colours): two kernels per half-sweep, then one (in place
     // without cross terms, else out of place through t)
     for (int prec = 0; prec < 2; prec++)
@@ -544,6 +553,30 @@ static int autotune_sweeps(cvb_ctx *ctx) {
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         zb[v] = 1e3 * ms / reps;
       }
+    // the FP32 zebra sweep with TMA-staged tiles, each chunk size
+    for (int v = 0; v < 3; v++) {
+      t.zt32[v] = 0.0;
+      const int rps[3] = {4, 8, 16};
+      if (!zebra_tma_ok(L)) continue;
+      const int reps = 5;
+      bool ran = true;
+      for (int q = 0; q <= reps && ran; q++) {
+        if (q == 1) CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        for (int color = 0; color < 2 && ran; color++)
+          ran = launch_zebra_tma(L, L.r32, L.e32, 1.3f, color, rps[v], ctx->stream);
+      }
+      if (!ran) {  // the tensor maps were refused: the form is not available here
+        CK(cudaStreamSynchronize(ctx->stream));
+        continue;
+      }
+      CK(cudaEventRecord(ctx->ev1, ctx->stream));
+      CK(cudaEventSynchronize(ctx->ev1));
+      CKL();
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      t.zt32[v] = 1e3 * ms / reps;
+    }
+    if (tma_timeout_take(ctx->stream) != 0) return fail(ctx, CVB_TIMEOUT, "a TMA-staged half-sweep gave up waiting");
     pick(t);
     ctx->tune.push_back(t);
     std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -945,6 +978,12 @@ static int solve_resident(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   st->device_ms = ms;
   st->status = rc;
+  bool tma = false;
+  for (int l = 0; l < ctx->nlevels; l++) tma = tma || ctx->L[l].ztma32 != 0;
+  if (tma && tma_timeout_take(ctx->stream) != 0) {
+    st->status = CVB_TIMEOUT;
+    return fail(ctx, CVB_TIMEOUT, "a TMA-staged half-sweep gave up waiting for its tiles; the result is not valid");
+  }
   return rc;
 }
 
@@ -1760,6 +1799,45 @@ int cvb_apply_operator_f32(cvb_ctx *ctx, int level, const float *x, float *y) {
   return CVB_OK;
 }
 
+int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega, const float *b, float *x) {
+  TRY(level_ok(ctx, level));
+  LevelDev &L = ctx->L[level];
+  if (color != 0 && color != 1) return fail(ctx, CVB_BAD_INPUT, "colour %d is not 0 or 1", color);
+  const int keep_tma = L.ztma32, keep_fuse = L.zfuse32;
+  switch (form) {
+    case CVB_ZEBRA_SPLIT: L.ztma32 = 0; L.zfuse32 = 0; break;
+    case CVB_ZEBRA_FUSED: L.ztma32 = 0; L.zfuse32 = 1; break;
+    case CVB_ZEBRA_TMA4: case CVB_ZEBRA_TMA8: case CVB_ZEBRA_TMA16: L.ztma32 = form; L.zfuse32 = 0; break;
+    default: return fail(ctx, CVB_BAD_INPUT, "unknown zebra form %d", form);
+  }
+  const bool ok = form == CVB_ZEBRA_SPLIT ? true
+                  : form == CVB_ZEBRA_FUSED ? zebra_fusable<float>(L)
+                                           : zebra_tma_ok(L);
+  if (!ok) {
+    L.ztma32 = keep_tma;
+    L.zfuse32 = keep_fuse;
+    return fail(ctx, CVB_BAD_INPUT, "zebra form %d cannot run on level %d", form, level);
+  }
+  const size_t n = L.g.n();
+  int rc = CVB_OK;
+  if (cudaMemcpyAsync(L.r32, b, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+      cudaMemcpyAsync(L.e32, x, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+    rc = CVB_CUDA_ERROR;
+  if (rc == CVB_OK) {
+    launch_zebra_half<float>(L, L.r32, L.e32, L.t32 + n, omega, color, false, ctx->stream);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(x, L.e32, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      rc = CVB_CUDA_ERROR;
+  }
+  L.ztma32 = keep_tma;
+  L.zfuse32 = keep_fuse;
+  if (rc != CVB_OK) return fail(ctx, rc, "zebra half-sweep failed");
+  if (form >= CVB_ZEBRA_TMA4 && tma_timeout_take(ctx->stream) != 0)
+    return fail(ctx, CVB_TIMEOUT, "a TMA-staged half-sweep gave up waiting for its tiles");
+  return CVB_OK;
+}
+
 int cvb_set_device_limit(cvb_ctx *ctx, unsigned long long bytes) {
   if (!ctx) return CVB_BAD_INPUT;
   ctx->device_limit = (size_t)bytes;
@@ -1850,16 +1928,20 @@ int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
   std::string o = "{\"line_sweep\": [";
   for (size_t q = 0; q < ctx->tune.size(); q++) {
     const auto &t = ctx->tune[q];
-    char row[512];
+    char row[768];
     const LevelDev &L = ctx->L[t.level];
+    char z32[16];
+    if (L.ztma32) snprintf(z32, sizeof z32, "tma%d", L.ztma32);
+    else snprintf(z32, sizeof z32, "%s", L.zfuse32 ? "fused" : "split");
     snprintf(row, sizeof row,
              "%s{\"level\": %d, \"cells\": %zu, \"f32\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
              "\"f64\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
-             "\"zebra_f32\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"choice\": \"%s\"}, "
+             "\"zebra_f32\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"tma4_us\": %.2f, \"tma8_us\": %.2f, "
+             "\"tma16_us\": %.2f, \"choice\": \"%s\"}, "
              "\"zebra_f64\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"choice\": \"%s\"}}",
              q ? ", " : "", t.level, t.cells, t.us32[0], t.us32[1], L.sweep32 ? "split" : "fused", t.us64[0],
-             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], L.zfuse32 ? "fused" : "split", t.zb64[0],
-             t.zb64[1], L.zfuse64 ? "fused" : "split");
+             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], t.zt32[0], t.zt32[1], t.zt32[2], z32,
+             t.zb64[0], t.zb64[1], L.zfuse64 ? "fused" : "split");
     o += row;
   }
   o += "]}";

@@ -97,7 +97,10 @@ struct cvb_ctx {
   // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
   // set-up timings (microseconds): Jacobi line sweep fused / split, zebra
   // sweep two kernels / one kernel per half-sweep
-  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2]; };
+  // measured sweep times (us): line sweeps fused / split, zebra sweeps two-kernel /
+  // one-kernel, and the FP32 zebra sweep with TMA-staged tiles of 4, 8, 16 row
+  // pairs (0: not run on this level)
+  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2], zt32[3]; };
   std::vector<Tune> tune;
 };
 

@@ -104,6 +104,8 @@ struct LevelDev {
   int cross32, cross64;
   int zfuse32, zfuse64;     // zebra variant chosen at set-up: 0 two kernels per half-sweep, 1 one
                             // (in place without cross terms, else out of place)
+  int ztma32;               // FP32 zebra half-sweep with TMA-staged tiles (kernels_tma.cu): the
+                            // row pairs per chunk (4, 8, 16) the autotuner chose, 0 off
   // coarsest level only: the densely inverted cells (first cm of cidx) and the
   // identity ones (the rest of cidx)
   const int *cidx;
@@ -159,6 +161,13 @@ void launch_residual(const LevelDev &L, const T *b, const T *x, T *r, cudaStream
 template <typename T>
 void launch_line_smooth(const LevelDev &L, const T *b, const T *x, T *xnew, T omega, int zero_guess,
                         cudaStream_t s);
+// The FP32 zebra half-sweep of one colour in place with TMA-staged tiles of
+// rp row pairs (kernels_tma.cu); false when the level does not allow it.
+bool zebra_tma_ok(const LevelDev &L);
+bool launch_zebra_tma(const LevelDev &L, const float *b, float *x, float omega, int color, int rp, cudaStream_t s);
+// 1 if a TMA kernel's bounded wait gave up since the last call (cleared), 0 if
+// not, -1 on a CUDA error; synchronises the stream.
+int tma_timeout_take(cudaStream_t s);
 // zebra half-sweep of one color, in place (res: scratch for the residual)
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s);

@@ -277,6 +277,12 @@ static bool fused_ok(const LevelDev &L) {
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s) {
   constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
+  if constexpr (sizeof(T) == 4) {
+    if (!zero && L.ztma32 &&
+        launch_zebra_tma(L, reinterpret_cast<const float *>(b), reinterpret_cast<float *>(x), (float)omega, color,
+                         L.ztma32, s))
+      return;
+  }
   if (!zero && fused_ok<T>(L) && zebra_fusable<T>(L)) {
     zebra_fused<T>(L, b, x, x, omega, color, s);
     return;

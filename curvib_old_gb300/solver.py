@@ -328,6 +328,17 @@ class PoissonContext:
         self._check(self._L.cvb_level_cross(self._ctx, level, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    ZEBRA_FORMS = {"split": 0, "fused": 1, "tma4": 4, "tma8": 8, "tma16": 16}
+
+    def zebra_half_f32(self, level, form, color, b, x, omega=1.3):
+        """One FP32 zebra half-sweep of x (returned) in the named form."""
+        xb = np.ascontiguousarray(x, dtype=np.float32).copy()
+        bb = np.ascontiguousarray(b, dtype=np.float32)
+        rc = self._L.cvb_zebra_half_f32(self._ctx, level, self.ZEBRA_FORMS[form], color, omega, ptr(bb), ptr(xb))
+        if rc:
+            raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
+        return xb
+
     def weights(self, level):
         w = np.zeros((19,) + self.shapes[level])
         self._check(self._L.cvb_get_weights(self._ctx, level, ptr(w)))

@@ -294,6 +294,23 @@ int cvb_get_weights(cvb_ctx *ctx, int level, double *w);
  * On an orthogonal grid both are 0 and the operator kernels read the seven face
  * points only.  No counterpart in the reference (which always assembles 19). */
 int cvb_level_cross(const cvb_ctx *ctx, int level, int *cross32, int *cross64);
+/* One FP32 zebra half-sweep (the mixed V-cycle's smoother, y-line
+ * Gauss-Seidel on the lines (i + k) % 2 == color, over-relaxed by omega) of
+ * x in place for right-hand side b, host arrays [mz][my][mx], in a given
+ * form: two kernels (residual, then line solves), one kernel, or one kernel
+ * with its tiles staged by TMA bulk tensor copies in chunks of 4, 8 or 16 row
+ * pairs.  The forms compute the same update; the set-up autotuner picks the
+ * fastest per level (cvb_tuning_report).  CVB_BAD_INPUT when the form cannot
+ * run on the level.  A parity and measurement hook with no counterpart in the
+ * reference (its smoother is Richardson + ILU, poisson.c:1906-1935). */
+enum {
+  CVB_ZEBRA_SPLIT = 0,
+  CVB_ZEBRA_FUSED = 1,
+  CVB_ZEBRA_TMA4 = 4,
+  CVB_ZEBRA_TMA8 = 8,
+  CVB_ZEBRA_TMA16 = 16
+};
+int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega, const float *b, float *x);
 /* MyRestriction (poisson.c:129) from level+1 to level; MyInterpolation
  * (poisson.c:265) from level-1 to level (returned, not added). */
 int cvb_restrict(cvb_ctx *ctx, int coarse_level, const double *xf, double *xc);

@@ -35,11 +35,14 @@ for f in poisson metrics implicitsolver rhs bcs compgeom variables init; do
   $CC $CFLAGS -c "$REF/$f.c" -o "$OUT/ref_$f.o"
   objs+=("$OUT/ref_$f.o")
 done
-# main.c holds Divergence (main.c:469) beside main() and the globals the
-# harness defines itself: every symbol of its object but Divergence is made
-# local, so only that routine joins the library.
+# main.c holds Divergence (main.c:469) and the restart routines
+# Ucont_P_Binary_Output / _Input (main.c:75-467) beside main() and the globals
+# the harness defines itself: every symbol of its object but those three and
+# the time step ti they name files by is made local, so only they join the
+# library.
 $CC $CFLAGS -c "$REF/main.c" -o "$OUT/ref_main.o"
-objcopy --keep-global-symbol=Divergence "$OUT/ref_main.o"
+objcopy --keep-global-symbol=Divergence --keep-global-symbol=Ucont_P_Binary_Output \
+        --keep-global-symbol=Ucont_P_Binary_Input --keep-global-symbol=ti "$OUT/ref_main.o"
 objs+=("$OUT/ref_main.o")
 # ibm.c declares point_cell_thin with 19 parameters and defines it with 13;
 # ibm_compile_fix.h names the two forms apart so the file compiles unmodified.

@@ -314,6 +314,22 @@ class Reference:
         a = np.ascontiguousarray(uc, dtype=np.float64)
         self.L.ref_set_ucont(_p(a))
 
+    def restart_write(self, directory, ti, block, nvert, ucont, ucat, p):
+        """Ucont_P_Binary_Output (main.c:285) of the finest level's fields into directory."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (nvert, ucont, ucat, p)]
+        rc = self.L.ref_restart_write(str(directory).encode(), ti, block, *[_p(a) for a in arrs])
+        if rc:
+            raise RuntimeError(f"ref_restart_write failed: {rc}")
+
+    def restart_read(self, directory, ti, block):
+        """Ucont_P_Binary_Input (main.c:75): (Ucont, P, Nvert_o) as the reference reads them."""
+        sh = self.shape(self.nlevels - 1)
+        uc, p, nv = np.zeros(sh + (3,)), np.zeros(sh), np.zeros(sh)
+        rc = self.L.ref_restart_read(str(directory).encode(), ti, block, _p(uc), _p(p), _p(nv))
+        if rc:
+            raise RuntimeError(f"ref_restart_read failed: {rc}")
+        return uc, p, nv
+
     def nvert_restrict(self):
         mz, my, mx = self.shape(0)
         mns = ctypes.c_int()

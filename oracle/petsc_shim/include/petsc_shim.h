@@ -223,6 +223,12 @@ PetscErrorCode VecMin(Vec x, PetscInt *p, PetscReal *r);
 PetscErrorCode VecStrideMax(Vec x, PetscInt start, PetscInt *p, PetscReal *r);
 PetscErrorCode VecStrideMin(Vec x, PetscInt start, PetscInt *p, PetscReal *r);
 PetscErrorCode VecGetLocalSize(Vec x, PetscInt *n);
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm comm, const char name[], PetscFileMode mode, PetscViewer *v);
+PetscErrorCode PetscViewerDestroy(PetscViewer *v);
+PetscErrorCode VecView(Vec x, PetscViewer v);
+PetscErrorCode VecLoad(Vec x, PetscViewer v);
+PetscErrorCode PetscOptionsClearValue(const char name[]);
+void shim_set_viewer_dir(const char *dir);
 PetscErrorCode VecGetSize(Vec x, PetscInt *n);
 PetscErrorCode VecAssemblyBegin(Vec x);
 PetscErrorCode VecAssemblyEnd(Vec x);

@@ -622,3 +622,92 @@ PetscErrorCode MatNullSpaceSetFunction(MatNullSpace sp, PetscErrorCode (*f)(MatN
 }
 PetscErrorCode MatNullSpaceDestroy(MatNullSpace *sp) { free(*sp); *sp = NULL; return 0; }
 PetscErrorCode MatSetNullSpace(Mat A, MatNullSpace sp) { (void)A; (void)sp; return 0; }
+
+/* ---- binary viewer: VecView / VecLoad in PETSc's published binary layout
+ * (big-endian int32 class id 1211214, int32 length, then the values as
+ * big-endian doubles; with a block size above 1 a "<file>.info" holding
+ * "-vecload_block_size <bs>").  A one-rank DMDA vector is written in its
+ * [k][j][i] order with the DMDA's dof as block size.  Files are opened in the
+ * directory shim_set_viewer_dir names (the harness points it at a test's
+ * scratch directory; the reference names files relative to its cwd). */
+struct _p_PetscViewer {
+  FILE *f;
+  int mode;
+  char path[512];
+};
+static char g_viewer_dir[400] = ".";
+void shim_set_viewer_dir(const char *dir) {
+  snprintf(g_viewer_dir, sizeof g_viewer_dir, "%s", dir && *dir ? dir : ".");
+}
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm comm, const char name[], PetscFileMode mode, PetscViewer *v) {
+  (void)comm;
+  PetscViewer p = (PetscViewer)calloc(1, sizeof(*p));
+  if (!p) return 1;
+  snprintf(p->path, sizeof p->path, "%s/%s", g_viewer_dir, name);
+  p->mode = mode;
+  p->f = fopen(p->path, mode == FILE_MODE_WRITE ? "wb" : "rb");
+  if (!p->f) { free(p); *v = NULL; return 1; }
+  *v = p;
+  return 0;
+}
+PetscErrorCode PetscViewerDestroy(PetscViewer *v) {
+  if (v && *v) {
+    if ((*v)->f) fclose((*v)->f);
+    free(*v);
+    *v = NULL;
+  }
+  return 0;
+}
+static void put_be32(FILE *f, uint32_t x) {
+  unsigned char b[4] = {(unsigned char)(x >> 24), (unsigned char)(x >> 16), (unsigned char)(x >> 8), (unsigned char)x};
+  fwrite(b, 1, 4, f);
+}
+static int get_be32(FILE *f, uint32_t *x) {
+  unsigned char b[4];
+  if (fread(b, 1, 4, f) != 4) return 1;
+  *x = ((uint32_t)b[0] << 24) | ((uint32_t)b[1] << 16) | ((uint32_t)b[2] << 8) | b[3];
+  return 0;
+}
+PetscErrorCode VecView(Vec x, PetscViewer v) {
+  if (!v || !v->f || v->mode != FILE_MODE_WRITE) return 1;
+  put_be32(v->f, 1211214u);
+  put_be32(v->f, (uint32_t)x->n);
+  for (PetscInt q = 0; q < x->n; q++) {
+    uint64_t u;
+    memcpy(&u, &x->a[q], 8);
+    unsigned char b[8];
+    for (int t = 0; t < 8; t++) b[t] = (unsigned char)(u >> (56 - 8 * t));
+    fwrite(b, 1, 8, v->f);
+  }
+  const int bs = x->dm ? (int)x->dm->dof : 1;
+  if (bs > 1) {
+    char info[520];
+    snprintf(info, sizeof info, "%s.info", v->path);
+    FILE *g = fopen(info, "w");
+    if (!g) return 1;
+    fprintf(g, "-vecload_block_size %d\n", bs);
+    fclose(g);
+  }
+  return 0;
+}
+PetscErrorCode VecLoad(Vec x, PetscViewer v) {
+  if (!v || !v->f || v->mode != FILE_MODE_READ) return 1;
+  uint32_t id, n;
+  if (get_be32(v->f, &id) || id != 1211214u || get_be32(v->f, &n) || (PetscInt)n != x->n) return 1;
+  for (PetscInt q = 0; q < x->n; q++) {
+    unsigned char b[8];
+    if (fread(b, 1, 8, v->f) != 8) return 1;
+    uint64_t u = 0;
+    for (int t = 0; t < 8; t++) u = (u << 8) | b[t];
+    memcpy(&x->a[q], &u, 8);
+  }
+  return 0;
+}
+PetscErrorCode PetscOptionsClearValue(const char name[]) {
+  for (int q = 0; q < g_nopt; q++)
+    if (!strcmp(g_opt[q].name, name)) {
+      g_opt[q] = g_opt[--g_nopt];
+      break;
+    }
+  return 0;
+}

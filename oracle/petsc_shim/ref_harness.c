@@ -17,7 +17,10 @@
 #include <unistd.h>
 
 /* Globals the reference sources expect main.c to define. */
-PetscInt block_number = 1, immersed = 0, MHV = 0, LV = 0, ti = 0, tistart = 0;
+PetscInt block_number = 1, immersed = 0, MHV = 0, LV = 0, tistart = 0;
+/* ti (the time step) is main.c's own: its object keeps that symbol global for
+ * the restart routines, which name their files by it. */
+extern PetscInt ti;
 PetscInt NumberOfBodies = 1, blank = 0;
 PetscInt imp_MAX_IT = 1, implicit_type = 0;
 PetscReal imp_atol = 1e-8, imp_rtol = 1e-2, imp_stol = 1e-8;
@@ -558,4 +561,41 @@ int ref_metrics_divergence(double *maxdiv, int *at) {
   int rc = MetricsDivergence(U(g_mg.mglevels - 1));
   shim_last_vecmax(maxdiv, at);
   return rc;
+}
+
+
+/* Ucont_P_Binary_Output (main.c:285): the reference's restart files for step
+ * ti_ and block (user->_this) into dir -- nvert, ucont, ucat, p are the finest
+ * level's global boxes Nvert, Ucont, Ucat, P. */
+PetscErrorCode Ucont_P_Binary_Output(UserCtx *user);
+PetscErrorCode Ucont_P_Binary_Input(UserCtx *user);
+int ref_restart_write(const char *dir, int ti_, int block, const double *nvert, const double *ucont,
+                      const double *ucat, const double *p) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  copy_owned(u, u->Nvert, 1, (double *)nvert, 1);
+  copy_owned(u, u->Ucont, 3, (double *)ucont, 1);
+  copy_owned(u, u->Ucat, 3, (double *)ucat, 1);
+  copy_owned(u, u->P, 1, (double *)p, 1);
+  ti = ti_;
+  u->_this = block;
+  shim_set_viewer_dir(dir);
+  int rc = Ucont_P_Binary_Output(u);
+  shim_set_viewer_dir(".");
+  return rc;
+}
+/* Ucont_P_Binary_Input (main.c:75): reads Ucont, P and Nvert_o back. */
+int ref_restart_read(const char *dir, int ti_, int block, double *ucont, double *p, double *nvert_o) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  ti = ti_;
+  u->_this = block;
+  shim_set_viewer_dir(dir);
+  int rc = Ucont_P_Binary_Input(u);
+  shim_set_viewer_dir(".");
+  if (rc) return rc;
+  copy_owned(u, u->Ucont, 3, ucont, 0);
+  copy_owned(u, u->P, 1, p, 0);
+  copy_owned(u, u->Nvert_o, 1, nvert_o, 0);
+  return 0;
 }

@@ -133,6 +133,21 @@ def run_ibm(name, meshes_out):
     return digest(nv)
 
 
+def run_restart():
+    """Digests of the files the reference's Ucont_P_Binary_Output (main.c:285)
+    writes for step 37, block 0, on box_sphere's grid (the fields of
+    tests/test_io.py::_restart_fields, seed 21)."""
+    import hashlib
+    import tempfile
+    from test_io import _restart_fields
+    c = build("box_sphere")
+    R = O.Reference(c["nodes"], c["nl"], c["bctype"], c["semi"])
+    nvert, ucont, ucat, p = _restart_fields(c["nvert"].shape, 21)
+    with tempfile.TemporaryDirectory() as d:
+        R.restart_write(d, 37, 0, nvert, ucont, ucat, p)
+        return {f.name: hashlib.sha256(f.read_bytes()).hexdigest()[:32] for f in sorted(Path(d).iterdir())}
+
+
 def main():
     import os
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CVB_REFERENCE_DIR")
@@ -149,6 +164,8 @@ def main():
     for name in IBM_CASES:
         out["ibm"][name] = run_ibm(name, meshes)
         print(name, "ok")
+    out["restart"] = run_restart()
+    print("restart ok")
     np.savez_compressed(OUT / "ibm_meshes.npz", **meshes)
     (OUT / "reference_digests.json").write_text(json.dumps(out, indent=1, sort_keys=True))
 

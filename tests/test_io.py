@@ -3,7 +3,13 @@ binary vectors as VecView writes them, the restart set of
 Ucont_P_Binary_Output / _Input (main.c:75-467), and grid.dat as MG_Initial
 reads it (init.c:606-735).  The vector files are checked byte for byte
 against PETSc's published binary layout, packed here independently with
-struct; no reference-written files exist to compare with."""
+struct, and the restart set against the files the reference's own
+Ucont_P_Binary_Output writes (main.c compiled against the oracle's PETSc
+shim, whose VecView / VecLoad follow the same published layout): the same
+file names, block sizes and bytes, and the reference's Ucont_P_Binary_Input
+reads the library's files to the same arrays.  Where the reference checkout
+is absent (the GPU machine) the digests recorded from those reference-written
+files stand in."""
 import ctypes
 import struct
 
@@ -172,3 +178,44 @@ def test_grid_dat_matches_reference_mg_initial(L, tmp_path, grid1d):
                                     got.ctypes.data_as(ctypes.c_void_p), ctypes.c_longlong(got.size)) == 0
     assert (km.value, jm.value, im.value) == nodes.shape[:3]
     assert np.array_equal(_read(L, tmp_path / "grid.dat", 0, grid1d, cl, ldim).ravel(), got)
+
+
+def _restart_fields(shape, seed):
+    rng = np.random.default_rng(seed)
+    nvert = np.where(rng.random(shape) < 0.2, 3.0, 0.0)
+    p = rng.standard_normal(shape)
+    p[0, 0, 0] = -0.0
+    return nvert, rng.standard_normal(shape + (3,)), rng.standard_normal(shape + (3,)), p
+
+
+def test_restart_set_matches_reference_output(L, tmp_path):
+    """The reference's Ucont_P_Binary_Output and cvb_restart_write produce the
+    same files byte for byte; the reference's Ucont_P_Binary_Input reads the
+    library's files to the arrays that were written."""
+    from oracle import oracle as O
+    import hashlib
+    import json
+    from pathlib import Path
+    from cases import build
+    c = build("box_sphere")
+    shape = c["nvert"].shape
+    nvert, ucont, ucat, p = _restart_fields(shape, 21)
+    n = int(np.prod(shape))
+    ours = tmp_path / "ours"
+    ours.mkdir()
+    assert L.cvb_restart_write(_b(ours), 37, 0, n, _lib.ptr(nvert), _lib.ptr(ucont), _lib.ptr(ucat),
+                               _lib.ptr(p)) == 0
+    got = {f.name: hashlib.sha256(f.read_bytes()).hexdigest()[:32] for f in sorted(ours.iterdir())}
+    golden = json.loads((Path(__file__).parent / "golden" / "reference_digests.json").read_text())
+    if (O.REF_DIR / "main.c").exists():
+        R = O.Reference(c["nodes"], c["nl"], c["bctype"], c["semi"])
+        theirs = tmp_path / "theirs"
+        theirs.mkdir()
+        R.restart_write(theirs, 37, 0, nvert, ucont, ucat, p)
+        ref = {f.name: hashlib.sha256(f.read_bytes()).hexdigest()[:32] for f in sorted(theirs.iterdir())}
+        assert got == ref
+        assert ref == golden["restart"]
+        uc2, p2, nv2 = R.restart_read(ours, 37, 0)
+        assert uc2.tobytes() == ucont.tobytes() and p2.tobytes() == p.tobytes() and nv2.tobytes() == nvert.tobytes()
+    else:
+        assert got == golden["restart"]
