@@ -1083,3 +1083,238 @@ void orc_metrics_divergence(const orc_level *L, double *maxdiv, long long *at) {
   *maxdiv = m;
   *at = where;
 }
+
+/* ------------------------------------------------------------------ momentum
+ * Viscous (rhs.c:1947-2566), laminar (no LES/RANS model, no Clark term): the
+ * viscous flux nu (G grad u) on every cell face, then its differences over
+ * each interior cell; the ring of visc is 0 (VecSet).  Face d of cell P lies
+ * between P and P + e_d; its tangential derivatives are one-sided next to cells
+ * with nvert in (0.5, 7) (rhs.c:2056-2110).  Operation order as the reference's. */
+static int visc_blocked(double n) { return n > 0.5 && n < 7.; }
+
+void orc_viscous(const orc_level *L, const double *ucat, double ren, double *visc) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  const size_t n = (size_t)mx * my * mz;
+  const long st[3] = {1, mx, (long)mx * my};
+  const double *mi[3][3] = {{L->icsi, L->ieta, L->izet}, {L->jcsi, L->jeta, L->jzet}, {L->kcsi, L->keta, L->kzet}};
+  const double *fa[3] = {L->iaj, L->jaj, L->kaj};
+  const double nu = 1. / ren;
+  double *fp = (double *)calloc(9 * n, sizeof(double));
+  for (int d = 0; d < 3; d++)
+    for (int k = d == 2 ? 0 : 1; k < mz - 1; k++)
+      for (int j = d == 1 ? 0 : 1; j < my - 1; j++)
+        for (int i = d == 0 ? 0 : 1; i < mx - 1; i++) {
+          const long p = (long)ID(L, i, j, k), sd = st[d];
+          double D[3][3]; /* D[a][c]: derivative of component c along direction a */
+          for (int c = 0; c < 3; c++) D[d][c] = ucat[3 * (p + sd) + c] - ucat[3 * p + c];
+          for (int t = 0; t < 3; t++) {
+            if (t == d) continue;
+            const long s = st[t];
+            const double *nv = L->nvert;
+            const int up = visc_blocked(nv[p + s]) || visc_blocked(nv[p + sd + s]);
+            const int dn = visc_blocked(nv[p - s]) || visc_blocked(nv[p + sd - s]);
+            for (int c = 0; c < 3; c++) {
+#define U(off) ucat[3 * (p + (off)) + c]
+              if (up) D[t][c] = (U(sd) + U(0) - U(sd - s) - U(-s)) * 0.5;
+              else if (dn) D[t][c] = (U(sd + s) + U(s) - U(sd) - U(0)) * 0.5;
+              else D[t][c] = (U(sd + s) + U(s) - U(sd - s) - U(-s)) * 0.25;
+#undef U
+            }
+          }
+          const double *m[3] = {mi[d][0] + 3 * p, mi[d][1] + 3 * p, mi[d][2] + 3 * p}; /* csi, eta, zet */
+          const double *nd = m[d];
+          double g[3];
+          for (int a = 0; a < 3; a++) g[a] = m[a][0] * nd[0] + m[a][1] * nd[1] + m[a][2] * nd[2];
+          double r[3][3]; /* r[q][c]: grad of component q against metric component c */
+          for (int q = 0; q < 3; q++)
+            for (int c = 0; c < 3; c++) r[q][c] = D[0][q] * m[0][c] + D[1][q] * m[1][c] + D[2][q] * m[2][c];
+          const double ajc = fa[d][p];
+          for (int c = 0; c < 3; c++) {
+            double v = 0;
+            v += (g[0] * D[0][c] + g[1] * D[1][c] + g[2] * D[2][c] + r[0][c] * nd[0] + r[1][c] * nd[1] +
+                  r[2][c] * nd[2]) * ajc * (nu);
+            fp[9 * p + 3 * d + c] = v;
+          }
+        }
+  memset(visc, 0, sizeof(double) * 3 * n);
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const size_t p = ID(L, i, j, k), w = p - 1, s = p - mx, b = p - (size_t)mx * my;
+        for (int c = 0; c < 3; c++)
+          visc[3 * p + c] = (fp[9 * p + c] - fp[9 * w + c] + fp[9 * p + 3 + c] - fp[9 * s + 3 + c] +
+                             fp[9 * p + 6 + c] - fp[9 * b + 6 + c]);
+      }
+  free(fp);
+}
+
+/* One of FormFunction1's tangential pressure derivatives at face d of cell P
+ * (rhs.c:2803-2849 and its five siblings), walled boxes: one-sided next to a
+ * wall or a blocked pair of cells, central otherwise.  Returns 0 where the
+ * reference assigns nothing (the variable then keeps its previous value). */
+static int ff_dp(const orc_level *L, const double *p, long P, long sd, long s, int q, int m, double *val) {
+  const double *nv = L->nvert;
+  const double up = nv[P + s] + nv[P + sd + s], dn = nv[P - s] + nv[P + sd - s];
+  if (q == m - 2 || up > 0.1) {
+    if (dn < 0.1 && q != 1) {
+      *val = (p[P] + p[P + sd] - p[P - s] - p[P + sd - s]) * 0.5;
+      return 1;
+    }
+    return 0;
+  }
+  if (q == 1 || dn > 0.1) {
+    if (up < 0.1) {
+      *val = (p[P + s] + p[P + sd + s] - p[P] - p[P + sd]) * 0.5;
+      return 1;
+    }
+    return 0;
+  }
+  *val = (p[P + s] + p[P + sd + s] - p[P - s] - p[P + sd - s]) * 0.25;
+  return 1;
+}
+
+/* FormFunction1 (rhs.c:2567-3351) for a box with no periodic face: Contra2Cart
+ * (ucat's interior cells from ucont), Convection, Viscous, rc = visc - conv,
+ * its contravariant form rct at the cell centres, then on every face the
+ * average of rct minus the pressure gradient (G grad p) and the blocked-face
+ * masks.  rhs ([mz][my][mx][3]) is written on the interior cells only.  The
+ * pressure derivatives keep the reference's loop order: where a branch assigns
+ * nothing, the value of the previous assignment in that order stands (the
+ * reference leaves the variables uninitialised before the first cell; they
+ * start at 0 here).  Returns -1 for a periodic box. */
+int orc_form_function1(const orc_level *L, const double *ucont, double *ucat, const double *p, double ren,
+                       int central, double *rhs) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  for (int f = 0; f < 6; f++)
+    if (L->bctype[f] == 7) return -1;
+  const size_t n = (size_t)mx * my * mz;
+  orc_contra2cart(L, ucont, ucat);
+  double *conv = (double *)malloc(sizeof(double) * 3 * n), *visc = (double *)malloc(sizeof(double) * 3 * n);
+  double *rct = (double *)calloc(3 * n, sizeof(double));
+  orc_convection(L, ucont, ucat, central, conv);
+  orc_viscous(L, ucat, ren, visc);
+  const long sx = 1, sy = mx, sz = (long)mx * my;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const long P = (long)ID(L, i, j, k);
+        double rc[3];
+        for (int c = 0; c < 3; c++) rc[c] = -1.0 * conv[3 * P + c] + visc[3 * P + c];
+        const double *cs = L->csi, *et = L->eta, *ze = L->zet;
+        const double a = L->aj[P];
+        rct[3 * P + 0] = a * (0.5 * (cs[3 * P] + cs[3 * (P - sx)]) * rc[0] +
+                              0.5 * (cs[3 * P + 1] + cs[3 * (P - sx) + 1]) * rc[1] +
+                              0.5 * (cs[3 * P + 2] + cs[3 * (P - sx) + 2]) * rc[2]);
+        rct[3 * P + 1] = a * (0.5 * (et[3 * P] + et[3 * (P - sy)]) * rc[0] +
+                              0.5 * (et[3 * P + 1] + et[3 * (P - sy) + 1]) * rc[1] +
+                              0.5 * (et[3 * P + 2] + et[3 * (P - sy) + 2]) * rc[2]);
+        rct[3 * P + 2] = a * (0.5 * (ze[3 * P] + ze[3 * (P - sz)]) * rc[0] +
+                              0.5 * (ze[3 * P + 1] + ze[3 * (P - sz) + 1]) * rc[1] +
+                              0.5 * (ze[3 * P + 2] + ze[3 * (P - sz) + 2]) * rc[2]);
+      }
+  double dpdc = 0.0, dpde = 0.0, dpdz = 0.0;
+  const double *fm[3][3] = {{L->icsi, L->ieta, L->izet}, {L->jcsi, L->jeta, L->jzet}, {L->kcsi, L->keta, L->kzet}};
+  const double *fa[3] = {L->iaj, L->jaj, L->kaj};
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const long P = (long)ID(L, i, j, k);
+        const long st[3] = {sx, sy, sz};
+        for (int d = 0; d < 3; d++) {
+          double *dp[3] = {&dpdc, &dpde, &dpdz};
+          const int q[3] = {i, j, k}, m[3] = {mx, my, mz};
+          for (int t = 0; t < 3; t++) {
+            if (t == d) *dp[t] = p[P + st[d]] - p[P];
+            else ff_dp(L, p, P, st[d], st[t], q[t], m[t], dp[t]);
+          }
+          const double *cs = fm[d][0] + 3 * P, *et = fm[d][1] + 3 * P, *zt = fm[d][2] + 3 * P;
+          const double *nd = d == 0 ? cs : d == 1 ? et : zt;
+          double v = 0.5 * (rct[3 * P + d] + rct[3 * (P + st[d]) + d]);
+          v -= (dpdc * (cs[0] * nd[0] + cs[1] * nd[1] + cs[2] * nd[2]) +
+                dpde * (et[0] * nd[0] + et[1] * nd[1] + et[2] * nd[2]) +
+                dpdz * (zt[0] * nd[0] + zt[1] * nd[1] + zt[2] * nd[2])) * fa[d][P];
+          rhs[3 * P + d] = v;
+        }
+      }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const long P = (long)ID(L, i, j, k);
+        const double *nv = L->nvert;
+        if (nv[P] > 0.1) rhs[3 * P] = rhs[3 * P + 1] = rhs[3 * P + 2] = 0;
+        if (nv[P + sx] > 0.1) rhs[3 * P] = 0;
+        if (nv[P + sy] > 0.1) rhs[3 * P + 1] = 0;
+        if (nv[P + sz] > 0.1) rhs[3 * P + 2] = 0;
+      }
+  free(conv);
+  free(visc);
+  free(rct);
+  return 0;
+}
+
+/* CalcRHS (implicitsolver.c:6449-6713) for a box with no periodic face:
+ * FormFunction1, the time derivative subtracted -- second-order backward
+ * (1.5 u - 2 u_o + 0.5 u_rm1, COEF_TIME_ACCURACY 1.5, variables.h:421) unless
+ * this is the first step (ti == tistart or ti == 1), then u - u_o -- divided
+ * by dt over every entry, the faces next to blocked cells and the walls
+ * zeroed, the convective-outflow term on the last k face when bctype[5] is 8,
+ * and the boundary ring zeroed as the reference's six boundary loops do. */
+int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o, const double *ucont_rm1,
+                 double *ucat, const double *p, double ren, double dt, int ti, int tistart, int central,
+                 double *rhs) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  if (orc_form_function1(L, ucont, ucat, p, ren, central, rhs)) return -1;
+  const size_t n3 = 3 * (size_t)mx * my * mz;
+  double *du = (double *)malloc(sizeof(double) * n3);
+  if (1.5 > 1.1 && ti != tistart && ti != 1) {
+    memcpy(du, ucont, sizeof(double) * n3);
+    for (size_t q = 0; q < n3; q++) du[q] *= 1.5;
+    for (size_t q = 0; q < n3; q++) du[q] += -2. * ucont_o[q];
+    for (size_t q = 0; q < n3; q++) du[q] += 0.5 * ucont_rm1[q];
+  } else {
+    for (size_t q = 0; q < n3; q++) du[q] = -1. * ucont_o[q] + ucont[q];
+  }
+  const double a = -1. / dt;
+  for (size_t q = 0; q < n3; q++) rhs[q] += a * du[q];
+  free(du);
+  const double c = 0.8;
+  const int mz_end = L->bctype[5] == 8 ? mz - 2 : mz - 3;
+  const long sx = 1, sy = mx, sz = (long)mx * my;
+  const double *nv = L->nvert;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const long P = (long)ID(L, i, j, k);
+        if ((nv[P] + nv[P + sx]) > 0.1 || i > mx - 3) rhs[3 * P] = 0.;
+        if ((nv[P] + nv[P + sy]) > 0.1 || j > my - 3) rhs[3 * P + 1] = 0.;
+        if ((nv[P] + nv[P + sz]) > 0.1 || k > mz_end) rhs[3 * P + 2] = 0.;
+        if (mz_end == mz - 2 && k == mz - 2) rhs[3 * P + 2] += c * (ucont[3 * P + 2] - ucont[3 * (P - sz) + 2]);
+      }
+#define R3(i, j, k) (rhs + 3 * ID(L, i, j, k))
+  for (int k = 0; k < mz - 1; k++)
+    for (int j = 0; j < my - 1; j++) {
+      double *r = R3(0, j, k);
+      r[0] = r[1] = r[2] = 0;
+      R3(mx - 2, j, k)[0] = 0;
+      r = R3(mx - 1, j, k);
+      r[0] = r[1] = r[2] = 0;
+    }
+  for (int k = 0; k < mz - 1; k++)
+    for (int i = 0; i < mx - 1; i++) {
+      double *r = R3(i, 0, k);
+      r[0] = r[1] = r[2] = 0;
+      R3(i, my - 2, k)[1] = 0;
+      r = R3(i, my - 1, k);
+      r[0] = r[1] = r[2] = 0;
+    }
+  for (int j = 0; j < my - 1; j++)
+    for (int i = 0; i < mx - 1; i++) {
+      double *r = R3(i, j, 0);
+      r[0] = r[1] = r[2] = 0;
+      R3(i, j, mz - 2)[2] = 0;
+      r = R3(i, j, mz - 1);
+      r[0] = r[1] = r[2] = 0;
+    }
+#undef R3
+  return 0;
+}

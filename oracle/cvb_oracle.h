@@ -104,4 +104,16 @@ int orc_ibm_search(int mx, int my, int mz, const double *cent, int n_v, const do
 #ifdef __cplusplus
 }
 #endif
+/* Viscous (rhs.c:1947-2566), laminar: visc ([mz][my][mx][3]) from ucat with
+ * nu = 1 / ren; 0 on the ring. */
+void orc_viscous(const orc_level *L, const double *ucat, double ren, double *visc);
+/* FormFunction1 (rhs.c:2567-3351) for a box with no periodic face: ucat's
+ * interior is refreshed from ucont (Contra2Cart), rhs's interior cells are
+ * written; -1 for a periodic box. */
+int orc_form_function1(const orc_level *L, const double *ucont, double *ucat, const double *p, double ren,
+                       int central, double *rhs);
+/* CalcRHS (implicitsolver.c:6449-6713) for a box with no periodic face. */
+int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o, const double *ucont_rm1,
+                 double *ucat, const double *p, double ren, double dt, int ti, int tistart, int central,
+                 double *rhs);
 #endif

@@ -107,6 +107,10 @@ def lib():
         _lib.orc_divergence.argtypes = [L, P, P, P]
         _lib.orc_metrics_divergence.argtypes = [L, P, P]
         _lib.orc_convection.argtypes = [L, P, P, ctypes.c_int, P]
+        D, I = ctypes.c_double, ctypes.c_int
+        _lib.orc_viscous.argtypes = [L, P, D, P]
+        _lib.orc_form_function1.argtypes = [L, P, P, P, D, I, P]
+        _lib.orc_calc_rhs.argtypes = [L, P, P, P, P, P, D, D, I, I, I, P]
     return _lib
 
 
@@ -249,6 +253,36 @@ def convection(L: OLevel, ucont, ucat, central=0):
     out = np.zeros_like(u)
     rc = lib().orc_convection(L.ref(), _p(uc), _p(u), int(central), _p(out))
     return rc, out
+
+
+def viscous(L: OLevel, ucat, ren):
+    """Viscous (rhs.c:1947-2566), laminar: visc with nu = 1/ren, 0 on the ring."""
+    u = np.ascontiguousarray(ucat, dtype=np.float64)
+    out = np.zeros_like(u)
+    lib().orc_viscous(L.ref(), _p(u), float(ren), _p(out))
+    return out
+
+
+def form_function1(L: OLevel, ucont, ucat, p, ren, central=0, rhs=None):
+    """FormFunction1 (rhs.c:2567-3351), walled boxes: (status, rhs, ucat after
+    its Contra2Cart); rhs's ring is what was passed (zeros by default)."""
+    uc = np.ascontiguousarray(ucont, dtype=np.float64)
+    u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+    pp = np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros_like(uc) if rhs is None else np.array(rhs, dtype=np.float64, copy=True, order="C")
+    rc = lib().orc_form_function1(L.ref(), _p(uc), _p(u), _p(pp), float(ren), int(central), _p(out))
+    return rc, out, u
+
+
+def calc_rhs(L: OLevel, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central=0, rhs=None):
+    """CalcRHS (implicitsolver.c:6449-6713), walled boxes: (status, rhs, ucat)."""
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont, ucont_o, ucont_rm1)]
+    u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+    pp = np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros_like(a[0]) if rhs is None else np.array(rhs, dtype=np.float64, copy=True, order="C")
+    rc = lib().orc_calc_rhs(L.ref(), *[_p(x) for x in a], _p(u), _p(pp), float(ren), float(dt), int(ti),
+                            int(tistart), int(central), _p(out))
+    return rc, out, u
 
 
 def metrics_divergence(L: OLevel):
@@ -411,6 +445,32 @@ class Reference:
         if self.L.ref_convection(_p(uc), _p(u), int(central), _p(out)):
             raise RuntimeError("ref_convection failed")
         return out
+
+    def viscous(self, ucat, ren):
+        u = np.ascontiguousarray(ucat, dtype=np.float64)
+        out = np.zeros_like(u)
+        if self.L.ref_viscous(_p(u), ctypes.c_double(ren), _p(out)):
+            raise RuntimeError("ref_viscous failed")
+        return out
+
+    def form_function1(self, ucont, ucat, p, ren, central=0, rhs=None):
+        uc = np.ascontiguousarray(ucont, dtype=np.float64)
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        pp = np.ascontiguousarray(p, dtype=np.float64)
+        out = np.zeros_like(uc) if rhs is None else np.array(rhs, dtype=np.float64, copy=True, order="C")
+        if self.L.ref_form_function1(_p(uc), _p(u), _p(pp), ctypes.c_double(ren), int(central), _p(out)):
+            raise RuntimeError("ref_form_function1 failed")
+        return out, u
+
+    def calc_rhs(self, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central=0, rhs=None):
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont, ucont_o, ucont_rm1)]
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        pp = np.ascontiguousarray(p, dtype=np.float64)
+        out = np.zeros_like(a[0]) if rhs is None else np.array(rhs, dtype=np.float64, copy=True, order="C")
+        if self.L.ref_calc_rhs(*[_p(x) for x in a], _p(u), _p(pp), ctypes.c_double(ren), ctypes.c_double(dt),
+                               int(ti), int(tistart), int(central), _p(out)):
+            raise RuntimeError("ref_calc_rhs failed")
+        return out, u
 
     def metrics_divergence(self):
         m, at = ctypes.c_double(), ctypes.c_int()

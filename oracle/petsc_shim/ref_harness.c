@@ -599,3 +599,72 @@ int ref_restart_read(const char *dir, int ti_, int block, double *ucont, double 
   copy_owned(u, u->Nvert_o, 1, nvert_o, 0);
   return 0;
 }
+
+/* Viscous (rhs.c:1947), FormFunction1 (rhs.c:2567) and CalcRHS
+ * (implicitsolver.c:6449) on the finest level.  FormFunction1 starts with
+ * Contra2Cart, which in this library is the inert stand-in (see the top of
+ * this file), so the harness runs the reference's own Contra2Cart first: its
+ * result is what FormFunction1's call leaves. */
+PetscErrorCode Viscous(UserCtx *user, Vec Ucont, Vec Ucat, Vec Visc);
+PetscErrorCode FormFunction1(UserCtx *user, Vec Rhs);
+PetscErrorCode CalcRHS(UserCtx *user, FSInfo *fsi);
+
+int ref_viscous(const double *ucat, double ren, double *visc) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  u->ren = ren;
+  Vec V;
+  VecDuplicate(u->lUcat, &V);
+  int rc = Viscous(u, u->lUcont, u->lUcat, V);
+  copy_owned(u, V, 3, visc, 0);
+  VecDestroy(&V);
+  return rc;
+}
+
+static void momentum_inputs(UserCtx *u, const double *ucont, const double *ucat, const double *p, double ren,
+                            int central) {
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  set_pair(u, u->P, u->lP, 1, p, u->da);
+  u->ren = ren;
+  PetscOptionsSetValue("-central", central ? "1" : "0");
+  cvbref_Contra2Cart(u);
+}
+
+int ref_form_function1(const double *ucont, double *ucat, const double *p, double ren, int central, double *rhs) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  momentum_inputs(u, ucont, ucat, p, ren, central);
+  Vec R;
+  VecDuplicate(u->Ucont, &R);
+  copy_owned(u, R, 3, rhs, 1);
+  int rc = FormFunction1(u, R);
+  copy_owned(u, R, 3, rhs, 0);
+  copy_owned(u, u->Ucat, 3, ucat, 0);
+  VecDestroy(&R);
+  PetscOptionsSetValue("-central", "0");
+  return rc;
+}
+
+int ref_calc_rhs(const double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, const double *p,
+                 double ren, double dt, int ti_, int tistart_, int central, double *rhs) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  momentum_inputs(u, ucont, ucat, p, ren, central);
+  if (!u->Ucont_o) VecDuplicate(u->Ucont, &u->Ucont_o);
+  if (!u->Ucont_rm1) VecDuplicate(u->Ucont, &u->Ucont_rm1);
+  copy_owned(u, u->Ucont_o, 3, (double *)ucont_o, 1);
+  copy_owned(u, u->Ucont_rm1, 3, (double *)ucont_rm1, 1);
+  VecDuplicate(u->Ucont, &u->Rhs);
+  copy_owned(u, u->Rhs, 3, rhs, 1);
+  u->dt = dt;
+  ti = ti_;
+  tistart = tistart_;
+  int rc = CalcRHS(u, NULL);
+  copy_owned(u, u->Rhs, 3, rhs, 0);
+  copy_owned(u, u->Ucat, 3, ucat, 0);
+  VecDestroy(&u->Rhs);
+  PetscOptionsSetValue("-central", "0");
+  return rc;
+}

@@ -119,3 +119,26 @@ def digest_nan(a) -> str:
 
 def seeded(shape, seed):
     return np.random.default_rng(seed).standard_normal(shape)
+
+
+# The momentum right-hand side (Viscous, FormFunction1, CalcRHS): Reynolds
+# number and time step of the fractional-step workload, and edge cases on
+# box_sphere's nvert, (k, j, i, value): a fluid cell with blocked cells above
+# and below it in j, and one below the top wall with a blocked cell under it,
+# where FormFunction1 assigns no tangential pressure derivative and the value
+# of the previous assignment in its loop order stands (rhs.c:2803-2849).
+MOM_REN, MOM_DT = 300.0, 2e-3
+MOM_EDGES = [(5, 3, 4, 3.0), (5, 5, 4, 3.0), (6, -3, 6, 3.0), (8, 4, 7, 1.2), (8, 6, 7, 1.3)]
+
+
+def mom_edge_nvert(nvert):
+    nv = np.array(nvert, dtype=np.float64, copy=True)
+    for (k, j, i, v) in MOM_EDGES:
+        nv[k, j, i] = v
+    return nv
+
+
+def momentum_inputs(shape):
+    """ucat, p, ucont_o and ucont_rm1 ([mz][my][mx](x3)) of the momentum checks."""
+    sh3 = tuple(shape) + (3,)
+    return seeded(sh3, 810), seeded(shape, 811), seeded(sh3, 812), seeded(sh3, 813)

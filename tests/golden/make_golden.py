@@ -28,6 +28,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
+from cases import (MOM_DT, MOM_REN, mom_edge_nvert, momentum_inputs)  # noqa: E402
 from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
 from curvib_old_gb300 import workload as W  # noqa: E402
@@ -84,6 +85,15 @@ def run(name):
     if name == "box_sphere":
         rec["convection_edges"] = convection(R, conv_edge_nvert(c["nvert"]), c["ucont"], c["bctype"])
         R.set_nvert(nl - 1, c["nvert"])
+    rec["momentum"] = momentum(R, c["nvert"], c["ucont"], c["bctype"])
+    if name == "box_sphere":
+        rec["momentum_edges"] = momentum(R, mom_edge_nvert(c["nvert"]), c["ucont"], c["bctype"])
+        R.set_nvert(nl - 1, c["nvert"])
+        bct = list(c["bctype"][:5]) + [8]  # convective outflow on the last k face
+        R8 = O.Reference(c["nodes"], nl, bct, c["semi"])
+        R8.set_nvert(nl - 1, c["nvert"])
+        rec["momentum_outflow8"] = momentum(R8, c["nvert"], c["ucont"], bct)
+        R = O.Reference(c["nodes"], nl, c["bctype"], c["semi"])
     np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
     return rec
 
@@ -96,6 +106,25 @@ def convection(R, nvert, ucont, bctype):
     R.set_nvert(R.nlevels - 1, nvert)
     ucat0, _ = post_inputs(nvert.shape, 0)
     return {"quick": digest(R.convection(ucont, ucat0, 0)), "central": digest(R.convection(ucont, ucat0, 1))}
+
+
+def momentum(R, nvert, ucont, bctype):
+    """Viscous, FormFunction1 (QUICK and central) and CalcRHS (first step and
+    second-order backward) on cases.momentum_inputs; None for a box with a
+    periodic face (not covered)."""
+    if 7 in list(bctype):
+        return None
+    R.set_nvert(R.nlevels - 1, nvert)
+    ucat0, p, uo, urm = momentum_inputs(nvert.shape)
+    out = {"viscous": digest(R.viscous(ucat0, MOM_REN))}
+    for central in (0, 1):
+        f, u = R.form_function1(ucont, ucat0, p, MOM_REN, central)
+        out[f"ff1_{central}"] = digest(f)
+        out[f"ff1_ucat_{central}"] = digest(u)
+    for ti in (1, 5):
+        r, _ = R.calc_rhs(ucont, uo, urm, ucat0, p, MOM_REN, MOM_DT, ti, 0)
+        out[f"calc_rhs_{ti}"] = digest(r)
+    return out
 
 
 def post(R, nvert, ucont, seed):

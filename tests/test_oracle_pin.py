@@ -197,3 +197,35 @@ def test_oracle_matches_live_reference_random_grid():
         d = R.lhs_csr(l) - O.lhs_csr(L)
         d.eliminate_zeros()
         assert d.nnz == 0
+
+
+def _check_momentum(c, nvert, bctype, want):
+    from cases import MOM_DT, MOM_REN, momentum_inputs
+    L = O.OLevel(c["metrics"][-1], nvert, bctype, c["semi"])
+    ucat0, p, uo, urm = momentum_inputs(nvert.shape)
+    if want is None:
+        rc, _, _ = O.form_function1(L, c["ucont"], ucat0, p, MOM_REN)
+        assert rc == -1
+        return
+    assert digest(O.viscous(L, ucat0, MOM_REN)) == want["viscous"]
+    for central in (0, 1):
+        rc, f, u = O.form_function1(L, c["ucont"], ucat0, p, MOM_REN, central)
+        assert rc == 0 and digest(f) == want[f"ff1_{central}"] and digest(u) == want[f"ff1_ucat_{central}"]
+    for ti in (1, 5):
+        rc, r, _ = O.calc_rhs(L, c["ucont"], uo, urm, ucat0, p, MOM_REN, MOM_DT, ti, 0)
+        assert rc == 0 and digest(r) == want[f"calc_rhs_{ti}"], ti
+
+
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_momentum_rhs_matches_reference(name):
+    """Viscous, FormFunction1 and CalcRHS (rhs.c:1947-3351, implicitsolver.c:
+    6449-6713) bit for bit; on box_sphere also with cells whose tangential
+    pressure derivative the reference leaves unassigned (cases.MOM_EDGES) and
+    with a convective-outflow face (bctype[5] 8)."""
+    from cases import mom_edge_nvert
+    c = _setup(name)
+    ref = REF["scenarios"][name]
+    _check_momentum(c, c["nvert"], c["bctype"], ref["momentum"])
+    if "momentum_edges" in ref:
+        _check_momentum(c, mom_edge_nvert(c["nvert"]), c["bctype"], ref["momentum_edges"])
+        _check_momentum(c, c["nvert"], list(c["bctype"][:5]) + [8], ref["momentum_outflow8"])
