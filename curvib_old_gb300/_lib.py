@@ -107,6 +107,9 @@ EXPORTS = {
     "cvb_batch_in_flight": ([_P], _I),
     "cvb_batch_set_round_limit": ([_P, ctypes.c_longlong], _I),
     "cvb_zebra_half_f32": ([_P, _I, _I, _I, ctypes.c_float, _P, _P], _I),
+    "cvb_viscous": ([_P, _P, _D, _P], _I),
+    "cvb_form_function1": ([_P, _P, _P, _P, _D, _I, _P], _I),
+    "cvb_calc_rhs": ([_P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P], _I),
     "cvb_device_bytes": ([_P, _P], _I),
     "cvb_set_device_limit": ([_P, ctypes.c_ulonglong], _I),
     "cvb_solve_opts_from_file": ([ctypes.c_char_p, _P, ctypes.c_char_p, _I], _I),

@@ -38,10 +38,16 @@ def _headers_mtime():
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 
+# Files whose arithmetic must round operation by operation as the reference's
+# C does: no multiply-add contraction.
+PER_FILE_FLAGS = {"kernels_momentum.cu": ["--fmad=false"]}
+
+
 def _compile(src: Path, extra) -> Path:
     obj = OUT / (src.stem + ".o")
     if obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, _headers_mtime()):
         return obj
+    extra = list(extra) + PER_FILE_FLAGS.get(src.name, [])
     cmd = [nvcc()] + NVCC_FLAGS + list(extra) + ["-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
         cmd = [nvcc(), "-x", "cu"] + NVCC_FLAGS + list(extra) + ["-c", str(src), "-o", str(obj)]

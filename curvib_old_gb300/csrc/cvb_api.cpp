@@ -1570,6 +1570,114 @@ int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int ce
   return CVB_OK;
 }
 
+// --- the momentum right-hand side ------------------------------------------
+// Device inputs of FormFunction1 / CalcRHS on the finest level: ucont, ucat,
+// p and the incoming rhs copied in (NULL ucont / ucat: the device copies the
+// last projection left), the scratch allocated on first use.
+static int momentum_prepare(cvb_ctx *ctx, const char *who, const double *ucont, const double *ucat, const double *p,
+                            const double *rhs) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  const int *bc = ctx->H[ctx->nlevels - 1].d.bctype;
+  for (int f = 0; f < 6; f++)
+    if (bc[f] == 7) return fail(ctx, CVB_BAD_INPUT, "%s: periodic faces (bctype 7) are not covered", who);
+  if (!p || !rhs) return fail(ctx, CVB_BAD_INPUT, "%s: p / rhs is NULL", who);
+  if (!ucat && !ctx->ucat_dev) return fail(ctx, CVB_BAD_INPUT, "%s: ucat is NULL and no projection has left Ucat on the device", who);
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const size_t n = F.g.n();
+  TRY(post_buffers(ctx, n));
+  if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, 3 * n));
+  if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+  if (!ctx->visc_dev) TRY(dalloc(ctx, &ctx->visc_dev, 3 * n));
+  if (!ctx->rct_dev) TRY(dalloc(ctx, &ctx->rct_dev, 3 * n));
+  if (!ctx->rhs_dev) TRY(dalloc(ctx, &ctx->rhs_dev, 3 * n));
+  if (ucont) CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (ucat) CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rhs_dev, rhs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  return CVB_OK;
+}
+
+// FormFunction1's kernels on the device copies: Contra2Cart, Convection,
+// Viscous, then the face values into rhs_dev.
+static void momentum_ff1(cvb_ctx *ctx, double ren, int central) {
+  const int l = ctx->nlevels - 1;
+  LevelDev &F = ctx->L[l];
+  const double *fm[9];
+  for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
+  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+  launch_convection(F.g, ctx->uc_dev, ctx->ucat_dev, F.nvert, central != 0, ctx->conv_fp, ctx->conv_dev, ctx->stream);
+  launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], 1. / ren, ctx->conv_fp,
+                 ctx->visc_dev, ctx->stream);
+  launch_form_function1(F.g, F.nvert, ctx->p_dev, ctx->conv_dev, ctx->visc_dev, ctx->cm[0], ctx->cm[1], ctx->cm[2],
+                        ctx->aj64[l], fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], ctx->rct_dev, ctx->rhs_dev,
+                        ctx->stream);
+}
+
+static int momentum_finish(cvb_ctx *ctx, double *ucat, double *rhs) {
+  const size_t n = ctx->L[ctx->nlevels - 1].g.n();
+  CKL();
+  CK(cudaMemcpyAsync(rhs, ctx->rhs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  if (ucat) CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_viscous(cvb_ctx *ctx, const double *ucat, double ren, double *visc) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!visc || !(ren != 0.0)) return fail(ctx, CVB_BAD_INPUT, "Viscous: visc is NULL or ren is 0");
+  const int l = ctx->nlevels - 1;
+  const int *bc = ctx->H[l].d.bctype;
+  for (int f = 0; f < 6; f++)
+    if (bc[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Viscous: periodic faces (bctype 7) are not covered");
+  if (!ucat && !ctx->ucat_dev) return fail(ctx, CVB_BAD_INPUT, "Viscous: ucat is NULL and no projection has left Ucat on the device");
+  LevelDev &F = ctx->L[l];
+  const size_t n = F.g.n();
+  TRY(post_buffers(ctx, n));
+  if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+  if (!ctx->visc_dev) TRY(dalloc(ctx, &ctx->visc_dev, 3 * n));
+  if (ucat) CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  const double *fm[9];
+  for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
+  launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], 1. / ren, ctx->conv_fp,
+                 ctx->visc_dev, ctx->stream);
+  CKL();
+  CK(cudaMemcpyAsync(visc, ctx->visc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_form_function1(cvb_ctx *ctx, const double *ucont, double *ucat, const double *p, double ren, int central,
+                       double *rhs) {
+  TRY(momentum_prepare(ctx, "FormFunction1", ucont, ucat, p, rhs));
+  if (!(ren != 0.0)) return fail(ctx, CVB_BAD_INPUT, "FormFunction1: ren is 0");
+  momentum_ff1(ctx, ren, central);
+  return momentum_finish(ctx, ucat, rhs);
+}
+
+int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
+                 const double *p, double ren, double dt, int ti, int tistart, int central, double *rhs) {
+  TRY(momentum_prepare(ctx, "CalcRHS", ucont, ucat, p, rhs));
+  if (!(ren != 0.0) || !(dt != 0.0) || !ucont_o || !ucont_rm1)
+    return fail(ctx, CVB_BAD_INPUT, "CalcRHS: ren / dt is 0 or ucont_o / ucont_rm1 is NULL");
+  const int l = ctx->nlevels - 1;
+  LevelDev &F = ctx->L[l];
+  const size_t n = F.g.n();
+  if (!ctx->uo_dev) TRY(dalloc(ctx, &ctx->uo_dev, 3 * n));
+  if (!ctx->urm_dev) TRY(dalloc(ctx, &ctx->urm_dev, 3 * n));
+  CK(cudaMemcpyAsync(ctx->uo_dev, ucont_o, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->urm_dev, ucont_rm1, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  momentum_ff1(ctx, ren, central);
+  // COEF_TIME_ACCURACY is 1.5 in the reference (variables.h:421): second-order
+  // backward except on the first step
+  const int bdf2 = (ti != tistart && ti != 1) ? 1 : 0;
+  const int mz_end = ctx->H[l].d.bctype[5] == 8 ? F.g.mz - 2 : F.g.mz - 3;
+  launch_calc_rhs(F.g, F.nvert, ctx->uc_dev, ctx->uo_dev, ctx->urm_dev, bdf2, -1. / dt, mz_end, ctx->rhs_dev,
+                  ctx->stream);
+  return momentum_finish(ctx, ucat, rhs);
+}
+
 // Divergence (flow) or MetricsDivergence (metrics) of the finest level.
 static int max_divergence(cvb_ctx *ctx, bool metrics, const double *ucont, double *maxdiv, long long *at) {
   if (!ctx) return CVB_BAD_INPUT;

@@ -90,13 +90,12 @@ struct cvb_ctx {
   double *uc_dev = nullptr, *p_dev = nullptr;
   double *ucat_dev = nullptr, *ubcs_dev = nullptr;  // Contra2Cart / GhostNodeVelocity (allocated on first use)
   double *conv_dev = nullptr, *conv_fp = nullptr;    // Convection: result and face fluxes (allocated on first use)
+  // momentum right-hand side (Viscous, FormFunction1, CalcRHS; allocated on first use)
+  double *visc_dev = nullptr, *rct_dev = nullptr, *rhs_dev = nullptr, *uo_dev = nullptr, *urm_dev = nullptr;
   double *ibm_cent = nullptr;  // cell centres of the last cvb_ibm_search that gave them
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;
   std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)
-  // set-up autotuner's measurements: per level, {fused, split} microseconds per precision
-  // set-up timings (microseconds): Jacobi line sweep fused / split, zebra
-  // sweep two kernels / one kernel per half-sweep
   // measured sweep times (us): line sweeps fused / split, zebra sweeps two-kernel /
   // one-kernel, and the FP32 zebra sweep with TMA-staged tiles of 4, 8, 16 row
   // pairs (0: not run on this level)

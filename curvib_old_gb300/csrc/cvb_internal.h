@@ -290,6 +290,18 @@ void launch_convection(const Geom &g, const double *ucont, const double *ucat, c
 void launch_metrics_divergence(const Geom &g, const double *csi, const double *eta, const double *zet,
                                const double *aj, double *pv, long long *pi, double *out_v, long long *out_i,
                                cudaStream_t s);
+// The momentum right-hand side (kernels_momentum.cu), boxes with no periodic
+// face.  fm: the nine face-metric arrays (I, J, K x csi, eta, zet); fp: 9 N
+// doubles of scratch; rct: 3 N doubles of scratch.
+void launch_viscous(const Geom &g, const double *nvert, const double *ucat, const double *const *fm,
+                    const double *iaj, const double *jaj, const double *kaj, double nu, double *fp, double *visc,
+                    cudaStream_t s);
+void launch_form_function1(const Geom &g, const double *nvert, const double *p, const double *conv,
+                           const double *visc, const double *csi, const double *eta, const double *zet,
+                           const double *aj, const double *const *fm, const double *iaj, const double *jaj,
+                           const double *kaj, double *rct, double *rhs, cudaStream_t s);
+void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, const double *ucont_o,
+                     const double *ucont_rm1, int bdf2, double neg_inv_dt, int mz_end, double *rhs, cudaStream_t s);
 // bc: the level's bctype[6]; the host has refused the types it does not cover
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
                                 const double *zet, double *ubcs, double *ucat, cudaStream_t s);

@@ -1,0 +1,288 @@
+// The momentum right-hand side of the fractional step on the finest level, for
+// boxes with no periodic face: Viscous (rhs.c:1947-2566, laminar), FormFunction1
+// (rhs.c:2567-3351) and CalcRHS (implicitsolver.c:6449-6713).  FP64, one thread
+// per cell.  This file is compiled without multiply-add contraction
+// (--fmad=false, build.py), so every product and sum rounds on its own in the
+// order the expressions are written -- the reference's C order -- and the
+// results equal the reference's bit for bit.
+#include "cvb_internal.h"
+#include "launch.cuh"
+
+namespace cvb {
+
+namespace {
+
+inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+__device__ __forceinline__ bool visc_blocked(double v) { return v > 0.5 && v < 7.; }
+
+struct FaceMetrics {
+  const double *m[3][3];  // [face direction][csi, eta, zet] Cmpnts arrays
+  const double *aj[3];    // IAj, JAj, KAj
+};
+
+}  // namespace
+
+// The viscous flux of every face (rhs.c:2056-2487): face d of cell P, between P
+// and P + e_d, into fp[(3 d + c) N + P]; the derivatives across the face's two
+// tangential directions are one-sided next to cells with nvert in (0.5, 7).
+__global__ void k_visc_faces(Geom g, const double *__restrict__ nv, const double *__restrict__ ucat, FaceMetrics M,
+                             double nu, double *__restrict__ fp) {
+  const size_t n = g.n();
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.mx), j = (int)((e / g.mx) % g.my), k = (int)(e / ((size_t)g.mx * g.my));
+    const long P = (long)e;
+    const long st[3] = {1, g.mx, (long)g.mx * g.my};
+    const int q[3] = {i, j, k}, m[3] = {g.mx, g.my, g.mz};
+    for (int d = 0; d < 3; d++) {
+      bool in = q[d] <= m[d] - 2;
+      for (int t = 0; t < 3; t++)
+        if (t != d) in = in && q[t] >= 1 && q[t] <= m[t] - 2;
+      if (!in) continue;
+      const long sd = st[d];
+      double D[3][3];
+      for (int c = 0; c < 3; c++) D[d][c] = ucat[3 * (P + sd) + c] - ucat[3 * P + c];
+      for (int t = 0; t < 3; t++) {
+        if (t == d) continue;
+        const long s = st[t];
+        const bool up = visc_blocked(nv[P + s]) || visc_blocked(nv[P + sd + s]);
+        const bool dn = visc_blocked(nv[P - s]) || visc_blocked(nv[P + sd - s]);
+        for (int c = 0; c < 3; c++) {
+#define U(off) ucat[3 * (P + (off)) + c]
+          if (up) D[t][c] = (U(sd) + U(0) - U(sd - s) - U(-s)) * 0.5;
+          else if (dn) D[t][c] = (U(sd + s) + U(s) - U(sd) - U(0)) * 0.5;
+          else D[t][c] = (U(sd + s) + U(s) - U(sd - s) - U(-s)) * 0.25;
+#undef U
+        }
+      }
+      const double *mc = M.m[d][0] + 3 * P, *me = M.m[d][1] + 3 * P, *mz = M.m[d][2] + 3 * P;
+      const double *mm[3] = {mc, me, mz};
+      const double *nd = mm[d];
+      double gg[3];
+      for (int a = 0; a < 3; a++) gg[a] = mm[a][0] * nd[0] + mm[a][1] * nd[1] + mm[a][2] * nd[2];
+      double r[3][3];
+      for (int qq = 0; qq < 3; qq++)
+        for (int c = 0; c < 3; c++) r[qq][c] = D[0][qq] * mm[0][c] + D[1][qq] * mm[1][c] + D[2][qq] * mm[2][c];
+      const double ajc = M.aj[d][P];
+      for (int c = 0; c < 3; c++) {
+        double v = 0;
+        v += (gg[0] * D[0][c] + gg[1] * D[1][c] + gg[2] * D[2][c] + r[0][c] * nd[0] + r[1][c] * nd[1] +
+              r[2][c] * nd[2]) * ajc * (nu);
+        fp[(size_t)(3 * d + c) * n + e] = v;
+      }
+    }
+  }
+}
+
+// visc = the flux differences over each interior cell (rhs.c:2490-2511); 0 on
+// the ring (the reference's VecSet before the loops).
+__global__ void k_visc_div(Geom g, const double *__restrict__ fp, double *__restrict__ visc) {
+  const size_t n = g.n();
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.mx), j = (int)((e / g.mx) % g.my), k = (int)(e / ((size_t)g.mx * g.my));
+    const bool in = i >= 1 && i <= g.mx - 2 && j >= 1 && j <= g.my - 2 && k >= 1 && k <= g.mz - 2;
+    const size_t w = e - 1, s = e - g.mx, b = e - (size_t)g.mx * g.my;
+    for (int c = 0; c < 3; c++)
+      visc[3 * e + c] = in ? (fp[(size_t)c * n + e] - fp[(size_t)c * n + w] + fp[(size_t)(3 + c) * n + e] -
+                              fp[(size_t)(3 + c) * n + s] + fp[(size_t)(6 + c) * n + e] - fp[(size_t)(6 + c) * n + b])
+                           : 0.0;
+  }
+}
+
+void launch_viscous(const Geom &g, const double *nvert, const double *ucat, const double *const *fm,
+                    const double *iaj, const double *jaj, const double *kaj, double nu, double *fp, double *visc,
+                    cudaStream_t s) {
+  FaceMetrics M;
+  for (int d = 0; d < 3; d++)
+    for (int a = 0; a < 3; a++) M.m[d][a] = fm[3 * d + a];
+  M.aj[0] = iaj; M.aj[1] = jaj; M.aj[2] = kaj;
+  const unsigned nb = blocks_for(g.n(), 128);
+  k_visc_faces<<<nb, 128, 0, s>>>(g, nvert, ucat, M, nu, fp); count_launch();
+  k_visc_div<<<blocks_for(g.n(), 256), 256, 0, s>>>(g, fp, visc); count_launch();
+}
+
+// ------------------------------------------------------------- FormFunction1
+// rct: the contravariant form of rc = visc - conv at the cell centres
+// (rhs.c:2682-2700), interior cells; the ring stays 0 (a new vector).
+__global__ void k_ff1_rct(Geom g, const double *__restrict__ conv, const double *__restrict__ visc,
+                          const double *__restrict__ csi, const double *__restrict__ eta,
+                          const double *__restrict__ zet, const double *__restrict__ aj, double *__restrict__ rct) {
+  const size_t n = g.n();
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.mx), j = (int)((e / g.mx) % g.my), k = (int)(e / ((size_t)g.mx * g.my));
+    if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) {
+      rct[3 * e] = rct[3 * e + 1] = rct[3 * e + 2] = 0.0;
+      continue;
+    }
+    const long P = (long)e, sx = 1, sy = g.mx, sz = (long)g.mx * g.my;
+    double rc[3];
+    for (int c = 0; c < 3; c++) rc[c] = -1.0 * conv[3 * P + c] + visc[3 * P + c];
+    const double a = aj[P];
+    rct[3 * P + 0] = a * (0.5 * (csi[3 * P] + csi[3 * (P - sx)]) * rc[0] +
+                          0.5 * (csi[3 * P + 1] + csi[3 * (P - sx) + 1]) * rc[1] +
+                          0.5 * (csi[3 * P + 2] + csi[3 * (P - sx) + 2]) * rc[2]);
+    rct[3 * P + 1] = a * (0.5 * (eta[3 * P] + eta[3 * (P - sy)]) * rc[0] +
+                          0.5 * (eta[3 * P + 1] + eta[3 * (P - sy) + 1]) * rc[1] +
+                          0.5 * (eta[3 * P + 2] + eta[3 * (P - sy) + 2]) * rc[2]);
+    rct[3 * P + 2] = a * (0.5 * (zet[3 * P] + zet[3 * (P - sz)]) * rc[0] +
+                          0.5 * (zet[3 * P + 1] + zet[3 * (P - sz) + 1]) * rc[1] +
+                          0.5 * (zet[3 * P + 2] + zet[3 * (P - sz) + 2]) * rc[2]);
+  }
+}
+
+namespace {
+
+// One tangential pressure derivative of face d of cell P (rhs.c:2803-2849 and
+// its siblings, walled boxes); false where the reference assigns nothing.
+__device__ __forceinline__ bool ff_dp(const double *__restrict__ nv, const double *__restrict__ p, long P, long sd,
+                                      long s, int q, int m, double &val) {
+  const double up = nv[P + s] + nv[P + sd + s], dn = nv[P - s] + nv[P + sd - s];
+  if (q == m - 2 || up > 0.1) {
+    if (dn < 0.1 && q != 1) {
+      val = (p[P] + p[P + sd] - p[P - s] - p[P + sd - s]) * 0.5;
+      return true;
+    }
+    return false;
+  }
+  if (q == 1 || dn > 0.1) {
+    if (up < 0.1) {
+      val = (p[P + s] + p[P + sd + s] - p[P] - p[P + sd]) * 0.5;
+      return true;
+    }
+    return false;
+  }
+  val = (p[P + s] + p[P + sd + s] - p[P - s] - p[P + sd - s]) * 0.25;
+  return true;
+}
+
+}  // namespace
+
+// The face values of FormFunction1 (rhs.c:2760-3222) and its blocked-face masks
+// (rhs.c:3225-3262) on the interior cells.  The reference keeps the three
+// derivative variables across its loop: where a branch assigns nothing the
+// value of the previous assignment stands.  Within a cell that is the previous
+// section's value; entering a cell it is what the previous cell in loop order
+// (k, j, i ascending over the interior) left -- its z-section pressure
+// derivatives, where its own branch or, failing that, its y-section assigned
+// dpde, and its dpdz = p[k+1] - p[k] -- and 0 before the first cell.
+__global__ void k_ff1_faces(Geom g, const double *__restrict__ nv, const double *__restrict__ p,
+                            const double *__restrict__ rct, FaceMetrics M, double *__restrict__ rhs) {
+  const size_t n = g.n();
+  const long st[3] = {1, g.mx, (long)g.mx * g.my};
+  const int m[3] = {g.mx, g.my, g.mz};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.mx), j = (int)((e / g.mx) % g.my), k = (int)(e / ((size_t)g.mx * g.my));
+    if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) continue;
+    const long P = (long)e;
+    // the previous cell's end values
+    double dp[3] = {0.0, 0.0, 0.0};
+    {
+      int pi = i - 1, pj = j, pk = k;
+      if (pi < 1) { pi = g.mx - 2; pj = j - 1; }
+      if (pj < 1) { pj = g.my - 2; pk = k - 1; }
+      if (pk >= 1) {
+        const long Q = ((long)pk * g.my + pj) * g.mx + pi;
+        const int qq[3] = {pi, pj, pk};
+        // its z section: dpde from the branch, else its y section's p[j+1] - p[j]
+        double de;
+        if (!ff_dp(nv, p, Q, st[2], st[1], qq[1], m[1], de)) de = p[Q + st[1]] - p[Q];
+        dp[1] = de;
+        dp[2] = p[Q + st[2]] - p[Q];
+        // its final dpdc (the z section's branch, else the y section's, else
+        // its x section's p[i+1] - p[i]) is assigned again by this cell's x
+        // section before any use
+      }
+    }
+    const int q[3] = {i, j, k};
+    double out[3];
+    for (int d = 0; d < 3; d++) {
+      for (int t = 0; t < 3; t++) {
+        if (t == d) dp[t] = p[P + st[d]] - p[P];
+        else ff_dp(nv, p, P, st[d], st[t], q[t], m[t], dp[t]);
+      }
+      const double *cs = M.m[d][0] + 3 * P, *et = M.m[d][1] + 3 * P, *zt = M.m[d][2] + 3 * P;
+      const double *nd = d == 0 ? cs : d == 1 ? et : zt;
+      double v = 0.5 * (rct[3 * P + d] + rct[3 * (P + st[d]) + d]);
+      v -= (dp[0] * (cs[0] * nd[0] + cs[1] * nd[1] + cs[2] * nd[2]) +
+            dp[1] * (et[0] * nd[0] + et[1] * nd[1] + et[2] * nd[2]) +
+            dp[2] * (zt[0] * nd[0] + zt[1] * nd[1] + zt[2] * nd[2])) * M.aj[d][P];
+      out[d] = v;
+    }
+    if (nv[P] > 0.1) out[0] = out[1] = out[2] = 0;
+    if (nv[P + st[0]] > 0.1) out[0] = 0;
+    if (nv[P + st[1]] > 0.1) out[1] = 0;
+    if (nv[P + st[2]] > 0.1) out[2] = 0;
+    for (int c = 0; c < 3; c++) rhs[3 * P + c] = out[c];
+  }
+}
+
+void launch_form_function1(const Geom &g, const double *nvert, const double *p, const double *conv,
+                           const double *visc, const double *csi, const double *eta, const double *zet,
+                           const double *aj, const double *const *fm, const double *iaj, const double *jaj,
+                           const double *kaj, double *rct, double *rhs, cudaStream_t s) {
+  FaceMetrics M;
+  for (int d = 0; d < 3; d++)
+    for (int a = 0; a < 3; a++) M.m[d][a] = fm[3 * d + a];
+  M.aj[0] = iaj; M.aj[1] = jaj; M.aj[2] = kaj;
+  k_ff1_rct<<<blocks_for(g.n(), 256), 256, 0, s>>>(g, conv, visc, csi, eta, zet, aj, rct); count_launch();
+  k_ff1_faces<<<blocks_for(g.n(), 128), 128, 0, s>>>(g, nvert, p, rct, M, rhs); count_launch();
+}
+
+// ------------------------------------------------------------------ CalcRHS
+// After FormFunction1: rhs -= dU / dt over every entry (second-order backward
+// dU = 1.5 u - 2 u_o + 0.5 u_rm1, or u - u_o on the first step), the faces
+// next to blocked cells and the walls zeroed, the convective-outflow term on
+// the last k face (bctype[5] 8), then the reference's six boundary loops,
+// which zero the ring except on the box's last row in each direction
+// (implicitsolver.c:6519-6713).
+__global__ void k_calc_rhs(Geom g, const double *__restrict__ nv, const double *__restrict__ uc,
+                           const double *__restrict__ uo, const double *__restrict__ urm, int bdf2, double a,
+                           int mz_end, double *__restrict__ rhs) {
+  const size_t n = g.n();
+  const int mx = g.mx, my = g.my, mz = g.mz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % mx), j = (int)((e / mx) % my), k = (int)(e / ((size_t)mx * my));
+    double r[3];
+    for (int c = 0; c < 3; c++) {
+      const size_t q = 3 * e + c;
+      double du;
+      if (bdf2) {
+        du = uc[q];
+        du *= 1.5;
+        du += -2. * uo[q];
+        du += 0.5 * urm[q];
+      } else {
+        du = -1. * uo[q] + uc[q];
+      }
+      r[c] = rhs[q];
+      r[c] += a * du;
+    }
+    const bool in = i >= 1 && i <= mx - 2 && j >= 1 && j <= my - 2 && k >= 1 && k <= mz - 2;
+    if (in) {
+      const size_t sx = 1, sy = mx, sz = (size_t)mx * my;
+      if ((nv[e] + nv[e + sx]) > 0.1 || i > mx - 3) r[0] = 0.;
+      if ((nv[e] + nv[e + sy]) > 0.1 || j > my - 3) r[1] = 0.;
+      if ((nv[e] + nv[e + sz]) > 0.1 || k > mz_end) r[2] = 0.;
+      if (mz_end == mz - 2 && k == mz - 2) r[2] += 0.8 * (uc[3 * e + 2] - uc[3 * (e - sz) + 2]);
+    }
+    // the six boundary loops (each covers its face minus the last row of the
+    // other two directions)
+    const bool kin = k < mz - 1, jin = j < my - 1, iin = i < mx - 1;
+    const bool all = ((i == 0 || i == mx - 1) && kin && jin) || ((j == 0 || j == my - 1) && kin && iin) ||
+                     ((k == 0 || k == mz - 1) && jin && iin);
+    if (all) r[0] = r[1] = r[2] = 0;
+    if (i == mx - 2 && kin && jin) r[0] = 0;
+    if (j == my - 2 && kin && iin) r[1] = 0;
+    if (k == mz - 2 && jin && iin) r[2] = 0;
+    for (int c = 0; c < 3; c++) rhs[3 * e + c] = r[c];
+  }
+}
+
+void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, const double *ucont_o,
+                     const double *ucont_rm1, int bdf2, double neg_inv_dt, int mz_end, double *rhs, cudaStream_t s) {
+  k_calc_rhs<<<blocks_for(g.n(), 256), 256, 0, s>>>(g, nvert, ucont, ucont_o, ucont_rm1, bdf2, neg_inv_dt, mz_end,
+                                                     rhs);
+  count_launch();
+}
+
+}  // namespace cvb

@@ -208,6 +208,31 @@ class PoissonContext:
                                            None if ucat is None else ptr(_c64(ucat)), int(bool(central)), ptr(out)))
         return out
 
+    def viscous(self, ucat, ren):
+        """Viscous (rhs.c:1947), laminar: visc [mz][my][mx][3]."""
+        u = None if ucat is None else _c64(ucat)
+        out = np.zeros(self.shapes[-1] + (3,))
+        self._check(self._L.cvb_viscous(self._ctx, None if u is None else ptr(u), float(ren), ptr(out)))
+        return out
+
+    def form_function1(self, ucont, ucat, p, ren, central=False, rhs=None):
+        """FormFunction1 (rhs.c:2567): (rhs, ucat after its Contra2Cart)."""
+        uc = _c64(ucont)
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        out = np.zeros(uc.shape) if rhs is None else np.array(rhs, dtype=np.float64, copy=True, order="C")
+        self._check(self._L.cvb_form_function1(self._ctx, ptr(uc), ptr(u), ptr(_c64(p)), float(ren), int(central),
+                                               ptr(out)))
+        return out, u
+
+    def calc_rhs(self, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central=False, rhs=None):
+        """CalcRHS (implicitsolver.c:6449): (rhs, ucat after its Contra2Cart)."""
+        uc, uo, urm = _c64(ucont), _c64(ucont_o), _c64(ucont_rm1)
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        out = np.zeros(uc.shape) if rhs is None else np.array(rhs, dtype=np.float64, copy=True, order="C")
+        self._check(self._L.cvb_calc_rhs(self._ctx, ptr(uc), ptr(uo), ptr(urm), ptr(u), ptr(_c64(p)), float(ren),
+                                         float(dt), int(ti), int(tistart), int(central), ptr(out)))
+        return out, u
+
     def metrics_divergence(self):
         """MetricsDivergence (metrics.c:1551): (max |div of the metrics|, its
         index in the box) on the finest level."""

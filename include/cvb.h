@@ -18,6 +18,9 @@
  *   Divergence        (main.c:469)      -> cvb_divergence
  *   MetricsDivergence (metrics.c:1551)  -> cvb_metrics_divergence
  *   Convection        (rhs.c:1463)      -> cvb_convection
+ *   Viscous           (rhs.c:1947)      -> cvb_viscous
+ *   FormFunction1     (rhs.c:2567)      -> cvb_form_function1
+ *   CalcRHS   (implicitsolver.c:6449)   -> cvb_calc_rhs
  *   ibm_search_advanced (ibm.c:4197), its nvert classification
  *                                       -> cvb_ibm_search
  *
@@ -219,6 +222,36 @@ int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at);
  * cvb_set_nvert first).  Boxes with a periodic face (bctype 7) are refused with
  * CVB_BAD_INPUT. */
 int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv);
+/* The momentum right-hand side on the finest level, for boxes with no periodic
+ * face (bctype 7 is refused with CVB_BAD_INPUT).  Vector fields are
+ * [mz][my][mx][3], p is [mz][my][mx]; nvert is the context's (the last
+ * cvb_setup_hierarchy or cvb_set_nvert); ucont / ucat NULL use the device copies
+ * the last projection left.  Results equal the reference's bit for bit.
+ *
+ * Viscous (rhs.c:1947-2566), laminar (no LES / RANS model): at every interior
+ * cell the sum over its faces of the viscous flux nu (G grad ucat), nu =
+ * 1 / ren, with the reference's one-sided derivatives next to cells of nvert
+ * in (0.5, 7); 0 on the ring. */
+int cvb_viscous(cvb_ctx *ctx, const double *ucat, double ren, double *visc);
+/* FormFunction1 (rhs.c:2567-3351): Contra2Cart (ucat's interior cells from
+ * ucont; ucat is written back), Convection (QUICK, or central with central !=
+ * 0), Viscous, their contravariant difference at the cell centres, and on
+ * every face its average minus the pressure gradient (G grad p) with the
+ * reference's one-sided differences, zero on faces next to blocked cells.
+ * rhs's interior cells are written, its ring is left as passed.  Where the
+ * reference assigns no tangential pressure derivative (a fluid cell between
+ * two blocked cells, or under a wall with a blocked cell on the other side),
+ * the value of the previous assignment in its loop order stands, as there. */
+int cvb_form_function1(cvb_ctx *ctx, const double *ucont, double *ucat, const double *p, double ren, int central,
+                       double *rhs);
+/* CalcRHS (implicitsolver.c:6449-6713): FormFunction1, then rhs -= dU / dt with
+ * dU = 1.5 ucont - 2 ucont_o + 0.5 ucont_rm1 (second-order backward,
+ * COEF_TIME_ACCURACY 1.5) unless ti == tistart or ti == 1 (then ucont -
+ * ucont_o), the faces next to blocked cells and walls zeroed, and the boundary
+ * ring zeroed as the reference's six boundary loops leave it (bctype[5] 8 adds
+ * the convective-outflow term on the last k face before those loops). */
+int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
+                 const double *p, double ren, double dt, int ti, int tistart, int central, double *rhs);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
  * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and

@@ -1,0 +1,70 @@
+"""The momentum right-hand side on the GPU against the CPU oracle, bit for bit.
+
+Viscous (rhs.c:1947), FormFunction1 (rhs.c:2567) and CalcRHS
+(implicitsolver.c:6449) through the C ABI on the walled scenarios, QUICK and
+central, first step and second-order backward; on box_sphere also with the
+cells whose tangential pressure derivative the reference leaves unassigned
+(cases.MOM_EDGES: the value of the previous cell in its loop order stands)
+and with a convective-outflow face.  The oracle is pinned to the reference's
+own routines (tests/test_oracle_pin.py).  Results are compared as bytes, so
+signed zeros count; the periodic boxes are refused.
+"""
+import types
+
+import numpy as np
+import pytest
+
+from cases import MOM_DT, MOM_REN, SCENARIOS, build, mom_edge_nvert, momentum_inputs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(c, nvert, bctype):
+    from curvib_old_gb300.solver import PoissonContext
+    P = types.SimpleNamespace(metrics=c["metrics"], nvert=nvert, ucont=c["ucont"], bctype=bctype, semi=c["semi"])
+    return PoissonContext().setup(P)
+
+
+def _same(a, b):
+    return np.ascontiguousarray(a).tobytes() == np.ascontiguousarray(b).tobytes()
+
+
+CASES = [(n, "plain") for n in sorted(SCENARIOS) if not SCENARIOS[n][1][0] and not any(SCENARIOS[n][1])] + \
+        [("box_sphere", "edges"), ("box_sphere", "outflow8")]
+
+
+@pytest.mark.parametrize("name,variant", CASES)
+def test_momentum_rhs_matches_oracle(name, variant):
+    c = build(name)
+    nvert = mom_edge_nvert(c["nvert"]) if variant == "edges" else c["nvert"]
+    bctype = list(c["bctype"][:5]) + [8] if variant == "outflow8" else list(c["bctype"])
+    ctx = _ctx(c, nvert, bctype)
+    try:
+        L = O.OLevel(c["metrics"][-1], nvert, bctype, c["semi"])
+        ucat0, p, uo, urm = momentum_inputs(nvert.shape)
+        assert _same(ctx.viscous(ucat0, MOM_REN), O.viscous(L, ucat0, MOM_REN))
+        ring = np.random.default_rng(3).standard_normal(nvert.shape + (3,))  # rhs's incoming ring stays
+        for central in (0, 1):
+            f_g, u_g = ctx.form_function1(c["ucont"], ucat0, p, MOM_REN, central, rhs=ring)
+            rc, f_o, u_o = O.form_function1(L, c["ucont"], ucat0, p, MOM_REN, central, rhs=ring)
+            assert rc == 0 and _same(u_g, u_o) and _same(f_g, f_o), central
+        for ti in (1, 5):
+            r_g, _ = ctx.calc_rhs(c["ucont"], uo, urm, ucat0, p, MOM_REN, MOM_DT, ti, 0, rhs=ring)
+            rc, r_o, _ = O.calc_rhs(L, c["ucont"], uo, urm, ucat0, p, MOM_REN, MOM_DT, ti, 0, rhs=ring)
+            assert rc == 0 and _same(r_g, r_o), ti
+    finally:
+        ctx.close()
+
+
+def test_momentum_rhs_refuses_periodic_boxes():
+    from curvib_old_gb300._lib import CVB_BAD_INPUT, CvbError
+    c = build("channel_periodic")
+    ctx = _ctx(c, c["nvert"], c["bctype"])
+    try:
+        ucat0, p, _, _ = momentum_inputs(c["nvert"].shape)
+        with pytest.raises(CvbError) as e:
+            ctx.form_function1(c["ucont"], ucat0, p, MOM_REN)
+        assert e.value.status == CVB_BAD_INPUT
+    finally:
+        ctx.close()
