@@ -462,6 +462,10 @@ def bench_step(args, ws, local):
 
     uc0 = pinned(P.ucont)
     uc, phi, p = pinned(P.ucont), pinned(np.zeros(shape)), pinned(np.zeros(shape))
+    # the momentum right-hand side's inputs: the previous two steps' fluxes and
+    # its output
+    uo, urm, rhs = pinned(P.ucont * 0.999), pinned(P.ucont * 0.998), pinned(np.zeros(shape + (3,)))
+    ren = 300.0
     # Ucat and the no-slip walls' Bcs.Ubcs
     ucat, ubcs = pinned(np.zeros(shape + (3,))), pinned(np.zeros(shape + (3,)))
     ptr = _lib.ptr
@@ -472,11 +476,18 @@ def bench_step(args, ws, local):
         stt = _lib.SolveStats()
         its = []
         wall = 0.0
+        mom = 0.0
         part = np.zeros(3)
         for _ in range(steps):
             uc.numpy()[...] = uc0.numpy()  # this step's u* (outside the timed calls)
             torch.cuda.synchronize()
+            tm = time.perf_counter()
+            # CalcRHS (FormFunction1 with Convection and Viscous, BDF2 term) on host arrays
+            rc = L.cvb_calc_rhs(ctx._ctx, ptr(uc.numpy()), ptr(uo.numpy()), ptr(urm.numpy()), ptr(ucat.numpy()),
+                                ptr(p.numpy()), ren, dt, 5, 0, 0, ptr(rhs.numpy()))
+            assert rc == 0, rc
             t0 = time.perf_counter()
+            mom += t0 - tm
             rc = L.cvb_poisson_solver_mg(ctx._ctx, ptr(uc.numpy()), 0.0, 1, dt, st, ptr(phi.numpy()),
                                          ctypes.byref(o), ctypes.byref(stt))
             assert rc == 0, rc
@@ -491,15 +502,19 @@ def bench_step(args, ws, local):
             part += (t1 - t0, t2 - t1, t3 - t2)
             its.append(stt.iterations)
         wall = max_over_ranks(ws, wall, dev)
+        mom = max_over_ranks(ws, mom, dev)
         return {"ms_per_step": wall * 1e3 / steps, "steps_per_s": ws * steps / wall,
                 "iterations": float(np.mean(its)), "rel_residual": stt.rel_residual,
                 "solver_mg_ms": part[0] * 1e3 / steps, "update_pressure_ms": part[1] * 1e3 / steps,
-                "projection_ms": part[2] * 1e3 / steps}
+                "projection_ms": part[2] * 1e3 / steps, "momentum_rhs_ms": mom * 1e3 / steps,
+                "ms_per_step_with_momentum_rhs": (wall + mom) * 1e3 / steps}
 
     out = {"workload": "192^3 cells, [0,1]^3 box, tanh 2.0 in y, distorted (config 0's law), sphere r=0.25 at the "
                        "centre; PoissonSolver_MG (VolumeFlux_rev + PoissonRHS + solve to 1e-8) + UpdatePressure + "
                        "Projection (flux correction, Contra2Cart, GhostNodeVelocity) on pinned host arrays, "
-                       "Taylor-Green u* (config 2 without its momentum step)",
+                       "Taylor-Green u*; beside it CalcRHS (the momentum right-hand side: FormFunction1 with "
+                       "Convection and Viscous at Re 300, the BDF2 term) on the same host arrays, timed apart "
+                       "(momentum_rhs_ms); the pseudo-time stages and their boundary conditions are not built",
            "unknowns": int(P.unknowns)}
     phis = {}
     for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
@@ -516,7 +531,7 @@ def bench_step(args, ws, local):
     # (every operation rounded on its own; three divisions a cell in
     # Contra2Cart, 18 face-flux components a cell in Convection)
     kt = {}
-    for name in ("contra2cart", "ghost_nodes", "convection"):
+    for name in ("contra2cart", "ghost_nodes", "convection", "viscous", "momentum_rhs"):
         ms, nbytes = ctypes.c_double(), ctypes.c_double()
         assert L.cvb_time_kernel(ctx._ctx, _lib.KERNELS[name], ctx.nlevels - 1, 20, ctypes.byref(ms),
                                  ctypes.byref(nbytes)) == 0

@@ -123,7 +123,7 @@ EXPORTS = {
 }
 KERNELS = {"line_sweep_f32": 0, "line_sweep_f64": 1, "residual_f32": 2, "residual_f64": 3, "zebra_f32": 4,
            "zebra_f64": 5, "vcycle_f32": 6, "vcycle_f64": 7, "contra2cart": 8, "ghost_nodes": 9,
-           "convection": 10}
+           "convection": 10, "viscous": 11, "momentum_rhs": 12}
 
 
 def lib_path() -> Path:

@@ -2123,24 +2123,46 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       case CVB_KERNEL_CONVECTION:
         launch_convection(L.g, ctx->uc_dev, ctx->ucat_dev, L.nvert, 0, ctx->conv_fp, ctx->conv_dev, ctx->stream);
         break;
+      case CVB_KERNEL_VISCOUS: {
+        const double *fm[9];
+        for (int q = 0; q < 9; q++) fm[q] = ctx->fm[level][q];
+        launch_viscous(L.g, L.nvert, ctx->ucat_dev, fm, ctx->iaj[level], ctx->jaj[level], ctx->kaj[level], 1. / 300.,
+                       ctx->conv_fp, ctx->visc_dev, ctx->stream);
+        break;
+      }
+      case CVB_KERNEL_MOMENTUM_RHS:
+        momentum_ff1(ctx, 300., 0);
+        launch_calc_rhs(L.g, L.nvert, ctx->uc_dev, ctx->uo_dev, ctx->urm_dev, 1, -1. / 2e-3, L.g.mz - 3, ctx->rhs_dev,
+                        ctx->stream);
+        break;
       default: launch_zebra_half<double>(L, L.r64, L.e64, L.t64 + n, 1.3, 1, false, ctx->stream); break;
     }
   };
   if (kernel == CVB_KERNEL_VCYCLE_F32 || kernel == CVB_KERNEL_VCYCLE_F64) return time_vcycle(ctx, kernel, level, reps, avg_ms, bytes);
-  if (kernel == CVB_KERNEL_CONTRA2CART || kernel == CVB_KERNEL_GHOST_NODES || kernel == CVB_KERNEL_CONVECTION) {
+  const bool momentum = kernel == CVB_KERNEL_VISCOUS || kernel == CVB_KERNEL_MOMENTUM_RHS;
+  if (kernel == CVB_KERNEL_CONTRA2CART || kernel == CVB_KERNEL_GHOST_NODES || kernel == CVB_KERNEL_CONVECTION ||
+      momentum) {
     if (level != ctx->nlevels - 1) return fail(ctx, CVB_BAD_INPUT, "kernel %d runs on the finest level only", kernel);
     if (kernel == CVB_KERNEL_GHOST_NODES) TRY(ghost_types_ok(ctx, ctx->H[level].d.bctype));
-    if (kernel == CVB_KERNEL_CONVECTION)
+    if (kernel == CVB_KERNEL_CONVECTION || momentum)
       for (int f = 0; f < 6; f++)
-        if (ctx->H[level].d.bctype[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Convection: periodic faces are not covered");
+        if (ctx->H[level].d.bctype[f] == 7) return fail(ctx, CVB_BAD_INPUT, "periodic faces are not covered");
     TRY(post_buffers(ctx, n));
     CK(cudaMemsetAsync(ctx->uc_dev, 0, sizeof(double) * 3 * n, ctx->stream));
     CK(cudaMemsetAsync(ctx->ucat_dev, 0, sizeof(double) * 3 * n, ctx->stream));
     CK(cudaMemsetAsync(ctx->ubcs_dev, 0, sizeof(double) * 3 * n, ctx->stream));
   }
-  if (kernel == CVB_KERNEL_CONVECTION) {
+  if (kernel == CVB_KERNEL_CONVECTION || momentum) {
     if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, 3 * n));
     if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+    if (momentum) {
+      for (double **b : {&ctx->visc_dev, &ctx->rct_dev, &ctx->rhs_dev, &ctx->uo_dev, &ctx->urm_dev})
+        if (!*b) TRY(dalloc(ctx, b, 3 * n));
+      CK(cudaMemsetAsync(ctx->p_dev, 0, sizeof(double) * n, ctx->stream));
+      CK(cudaMemsetAsync(ctx->rhs_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+      CK(cudaMemsetAsync(ctx->uo_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+      CK(cudaMemsetAsync(ctx->urm_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+    }
     // a velocity field of mixed signs in [-1, 1] (zero fluxes would send every
     // face through the full QUICK expression)
     std::vector<double> v(3 * n);
@@ -2165,6 +2187,15 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
     case CVB_KERNEL_ZEBRA_F64: per_cell = 8 + 0.5 * (8 + w64 + 4 + 8) + 0.5 * (8 + 24 + 8 + 8); break;
     case CVB_KERNEL_CONTRA2CART: per_cell = 72 + 24 + 8 + 24; break;  // centre metrics, ucont, nvert, ucat
     case CVB_KERNEL_CONVECTION: per_cell = 24 + 24 + 8 + 24; break;   // ucont, ucat, nvert, conv
+    // ucat, nvert, the nine face metrics and three face Jacobians, visc
+    case CVB_KERNEL_VISCOUS: per_cell = 24 + 8 + 216 + 24 + 24; break;
+    // Contra2Cart (centre metrics, ucont, nvert, ucat), Convection and Viscous
+    // as above, FormFunction1's faces (conv, visc, aj, rct, p, face metrics and
+    // Jacobians, rhs) and the time term (ucont, ucont_o, ucont_rm1, rhs in/out)
+    case CVB_KERNEL_MOMENTUM_RHS:
+      per_cell = (72 + 24 + 8 + 24) + (24 + 24 + 8 + 24) + (24 + 8 + 216 + 24 + 24) +
+                 (24 + 24 + 8 + 24 + 8 + 216 + 24 + 24) + (24 * 3 + 48);
+      break;
     case CVB_KERNEL_GHOST_NODES: {
       // the ring cells only: ucat read and written, ubcs read
       const double inner = (double)(L.g.mx - 2) * (L.g.my - 2) * (L.g.mz - 2);

@@ -449,7 +449,10 @@ enum {
   CVB_KERNEL_VCYCLE_F64 = 7,     /* the same in FP64 */
   CVB_KERNEL_CONTRA2CART = 8,    /* Contra2Cart on the finest level (the level argument must name it) */
   CVB_KERNEL_GHOST_NODES = 9,    /* GhostNodeVelocity on the finest level */
-  CVB_KERNEL_CONVECTION = 10     /* Convection (QUICK) on the finest level: face fluxes, then their differences */
+  CVB_KERNEL_CONVECTION = 10,    /* Convection (QUICK) on the finest level: face fluxes, then their differences */
+  CVB_KERNEL_VISCOUS = 11,       /* Viscous (laminar) on the finest level: face fluxes, then their differences */
+  CVB_KERNEL_MOMENTUM_RHS = 12   /* CalcRHS on the finest level on device arrays: Contra2Cart, Convection,
+                                    Viscous, FormFunction1's face values, the time term and masks */
 };
 /* JSON record of the set-up autotuner: per level, the measured time of the
  * fused and the split y-line sweep in each precision and the variant kept. */
