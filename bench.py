@@ -342,8 +342,13 @@ def roofline(ctx, orthogonal):
     note = ("; the grid is orthogonal, so the cross-derivative terms are exactly zero and are skipped" if orthogonal
             else "; the grid is distorted, so all 19 points are read")
     tag = "" if orthogonal else "_x"
+    if zebra_form.startswith("tma"):
+        forms[zebra_form] = (f"k_zebra_tma<{zebra_form[3:]},R> (one kernel: that color's {pts} residual from tiles "
+                             f"staged by TMA bulk tensor copies, {zebra_form[3:]} row pairs per chunk, then its "
+                             "y-line solves, in place)")
     return {"kernel": "FP32 zebra half-sweep on the finest level, " + forms[zebra_form] + note,
             "zebra_form": zebra_form,
+            "zebra_tuning_us_per_sweep": fine_tune[0]["zebra_f32"] if fine_tune else None,
             "bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
             "traffic": traffic_per_launch("zebra_f32_" + zebra_form + tag, cells), "algorithmic_bytes": k_bytes,

@@ -63,7 +63,10 @@ static double maxabs(const double *a, size_t n) {
   return m;
 }
 
+#define STEP(name) (printf("step: %s\n", name), fflush(stdout))
+
 int main(int argc, char **argv) {
+  setvbuf(stdout, NULL, _IONBF, 0);
   const int mixed = argc > 1 && !strcmp(argv[1], "mixed");
   /* 16 x 12 x 10 cells, walls everywhere, stretched and sheared, three levels */
   enum { IM = 17, JM = 13, KM = 11, NL = 3 };
@@ -78,6 +81,7 @@ int main(int argc, char **argv) {
         c[2] = (double)k / (KM - 1);
       }
   const int bctype[6] = {1, 1, 1, 1, 1, 1};
+  STEP("ref_init");
   if (ref_init(NL, IM, JM, KM, bctype, 0, 0, 0, coords)) { printf("FAIL ref_init\n"); return 1; }
   UserMG *mg = ref_usermg();
   UserCtx *fine = &mg->mgctx[NL - 1].user[0];
@@ -93,6 +97,7 @@ int main(int argc, char **argv) {
         const int near = i >= 5 && i <= 10 && j >= 4 && j <= 8 && k >= 3 && k <= 7;
         nv[((size_t)k * my + j) * mx + i] = in ? 3.0 : near ? 1.0 : 0.0;
       }
+  STEP("nvert");
   ref_set_nvert(NL - 1, nv);
   /* fluxes on the interior faces, zero on the walls */
   double *uc0 = (double *)calloc(3 * n, sizeof(double));
@@ -105,6 +110,7 @@ int main(int argc, char **argv) {
           s = s * 1664525u + 1013904223u;
           if (q[c] < m[c] - 2) uc0[3 * (((size_t)k * my + j) * mx + i) + c] = (double)(s >> 8) / 16777216.0 - 0.5;
         }
+  STEP("ucont");
   ref_set_ucont(uc0);
 
   PetscOptionsClear();
@@ -117,20 +123,26 @@ int main(int argc, char **argv) {
   fine->st = 1.0;
 
   /* --- the binding on the real library --- */
+  STEP("PoissonSetup_GB300");
   CHECK(PoissonSetup_GB300(mg) == 0, "PoissonSetup_GB300 failed");
+  STEP("PoissonSolver_MG_GB300");
   CHECK(PoissonSolver_MG_GB300(mg) == 0, "PoissonSolver_MG_GB300 failed");
   double *uc_b = copy_of(shim_vec_data(fine->Ucont), 3 * n), *phi_b = copy_of(shim_vec_data(fine->Phi), n);
+  STEP("UpdatePressure_GB300");
   CHECK(UpdatePressure_GB300(fine) == 0, "UpdatePressure_GB300 failed");
   double *p_b = copy_of(shim_vec_data(fine->P), n), *phi_b2 = copy_of(shim_vec_data(fine->Phi), n);
+  STEP("Projection_GB300");
   CHECK(Projection_GB300(fine) == 0, "Projection_GB300 failed");
   double *uc_b2 = copy_of(shim_vec_data(fine->Ucont), 3 * n), *ucat_b = copy_of(shim_vec_data(fine->Ucat), 3 * n);
   Vec Conv;
   VecDuplicate(fine->Ucont, &Conv);
+  STEP("Convection_GB300");
   CHECK(Convection_GB300(fine, fine->Ucont, fine->Ucat, Conv) == 0, "Convection_GB300 failed");
   double *conv_b = copy_of(shim_vec_data(Conv), 3 * n);
   CHECK(PoissonFinalize_GB300() == 0, "PoissonFinalize_GB300 failed");
 
   /* --- the reference's own routines on the same inputs --- */
+  STEP("reference routines");
   double *uc_r = copy_of(uc0, 3 * n), flux, area;
   ref_volume_flux(0.0, 1, uc_r, &flux, &area);
   double dmax = 0;
