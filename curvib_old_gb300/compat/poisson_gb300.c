@@ -11,6 +11,7 @@
  * the ghosted box that cvb_level_desc's gxs..gzm describe.  Nothing is
  * converted or copied on the host.
  */
+#include <stdlib.h>
 #include <string.h>
 #include "variables.h"
 #include "cvb.h"
@@ -19,7 +20,6 @@
 extern PetscInt block_number, immersed; /* main.c, as poisson.c:6-7 declares them */
 extern PetscInt wallfunction;           /* main.c, as bcs.c:3689 declares it */
 extern PetscInt les;                    /* main.c, as rhs.c declares it */
-PetscErrorCode Convection(UserCtx *user, Vec Ucont, Vec Ucat, Vec Conv);
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 
@@ -217,24 +217,30 @@ PetscErrorCode Projection_GB300(UserCtx *u) {
 }
 
 /* Convection (rhs.c:1463-1946) with the reference's arguments (FormFunction1
- * passes lUcont and lUcat, rhs.c:2651).  Without a periodic face it runs on
- * the device; with one, the reference's own routine runs, since it first
- * fills ghost layers of the periodic DMDA.  -central or les selects the
- * central form, as in the reference. */
+ * passes lUcont and lUcat, rhs.c:2651), on the device for every boundary type.
+ * -central or les selects the central form, as in the reference.  On one rank
+ * without periodic faces the local vectors are the box itself and go to the
+ * library as they are; a periodic DMDA's local vectors carry ghost planes, so
+ * the owned box is taken out of them and Conv is written back into its owned
+ * part (its ghost cells are 0, as the reference's VecSet leaves them).  nvert
+ * is the one the context was last given (PoissonSetNvert_GB300 after a body
+ * moves). */
 PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
-  for (int f = 0; f < 6; f++)
-    if (u->bctype[f] == 7) return Convection(u, Ucont, Ucat, Conv);
-  /* one rank owning the whole box: each vector holds exactly its 3 mx my mz
-   * values (the library copies that many); nvert is the one the context was
-   * last given (PoissonSetNvert_GB300 after a body moves) */
-  const PetscInt want = 3 * (PetscInt)u->info.mx * u->info.my * u->info.mz;
+  const int mx = u->info.mx, my = u->info.my, mz = u->info.mz;
+  const PetscInt box = 3 * (PetscInt)mx * my * mz;
+  PetscInt gxs, gys, gzs, gxm, gym, gzm;
+  DMDAGetGhostCorners(u->fda, &gxs, &gys, &gzs, &gxm, &gym, &gzm);
+  const PetscInt ghosted = 3 * (PetscInt)gxm * gym * gzm;
   PetscInt n_uc = -1, n_ucat = -1, n_conv = -1;
   VecGetLocalSize(Ucont, &n_uc);
   VecGetLocalSize(Ucat, &n_ucat);
   VecGetLocalSize(Conv, &n_conv);
-  if (n_uc != want || n_ucat != want || n_conv != want) {
+  const int as_box = n_uc == box && n_ucat == box && n_conv == box;
+  const int as_ghosted = n_uc == ghosted && n_ucat == ghosted && n_conv == ghosted && gxs <= 0 && gys <= 0 &&
+                         gzs <= 0 && gxs + gxm >= mx && gys + gym >= my && gzs + gzm >= mz;
+  if (!as_box && !as_ghosted) {
     PetscPrintf(PETSC_COMM_WORLD, "Convection_GB300: vectors of %d/%d/%d values, box needs %d (one rank only)\n",
-                (int)n_uc, (int)n_ucat, (int)n_conv, (int)want);
+                (int)n_uc, (int)n_ucat, (int)n_conv, (int)box);
     return CVB_BAD_INPUT;
   }
   PetscInt central = 0;
@@ -243,7 +249,35 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
   VecGetArray(Ucont, &uc);
   VecGetArray(Ucat, &ucat);
   VecGetArray(Conv, &conv);
-  int rc = cvb_convection(g_cvb, uc, ucat, (les || central) ? 1 : 0, conv);
+  int rc;
+  if (as_box) {
+    rc = cvb_convection(g_cvb, uc, ucat, (les || central) ? 1 : 0, conv);
+  } else {
+    double *bu = (double *)malloc(sizeof(double) * box), *bc = (double *)malloc(sizeof(double) * box),
+           *bo = (double *)malloc(sizeof(double) * box);
+    rc = (bu && bc && bo) ? CVB_OK : CVB_OOM;
+    for (int k = 0; k < mz && rc == CVB_OK; k++)
+      for (int j = 0; j < my; j++)
+        for (int i = 0; i < mx; i++) {
+          const size_t b = 3 * (((size_t)k * my + j) * mx + i);
+          const size_t l = 3 * (((size_t)(k - gzs) * gym + (j - gys)) * gxm + (i - gxs));
+          for (int c = 0; c < 3; c++) { bu[b + c] = uc[l + c]; bc[b + c] = ucat[l + c]; }
+        }
+    if (rc == CVB_OK) rc = cvb_convection(g_cvb, bu, bc, (les || central) ? 1 : 0, bo);
+    if (rc == CVB_OK) {
+      memset(conv, 0, sizeof(double) * ghosted);
+      for (int k = 0; k < mz; k++)
+        for (int j = 0; j < my; j++)
+          for (int i = 0; i < mx; i++) {
+            const size_t b = 3 * (((size_t)k * my + j) * mx + i);
+            const size_t l = 3 * (((size_t)(k - gzs) * gym + (j - gys)) * gxm + (i - gxs));
+            for (int c = 0; c < 3; c++) conv[l + c] = bo[b + c];
+          }
+    }
+    free(bu);
+    free(bc);
+    free(bo);
+  }
   VecRestoreArray(Conv, &conv);
   VecRestoreArray(Ucat, &ucat);
   VecRestoreArray(Ucont, &uc);

@@ -1552,9 +1552,6 @@ int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int ce
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
   if (!conv) return fail(ctx, CVB_BAD_INPUT, "conv is NULL");
-  const int *bc = ctx->H[ctx->nlevels - 1].d.bctype;
-  for (int f = 0; f < 6; f++)
-    if (bc[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Convection: periodic faces (bctype 7) are not covered");
   if (!ucat && !ctx->ucat_dev) return fail(ctx, CVB_BAD_INPUT, "ucat is NULL and no projection has left Ucat on the device");
   LevelDev &F = ctx->L[ctx->nlevels - 1];
   const size_t n = F.g.n();
@@ -2144,7 +2141,7 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       momentum) {
     if (level != ctx->nlevels - 1) return fail(ctx, CVB_BAD_INPUT, "kernel %d runs on the finest level only", kernel);
     if (kernel == CVB_KERNEL_GHOST_NODES) TRY(ghost_types_ok(ctx, ctx->H[level].d.bctype));
-    if (kernel == CVB_KERNEL_CONVECTION || momentum)
+    if (momentum)
       for (int f = 0; f < 6; f++)
         if (ctx->H[level].d.bctype[f] == 7) return fail(ctx, CVB_BAD_INPUT, "periodic faces are not covered");
     TRY(post_buffers(ctx, n));

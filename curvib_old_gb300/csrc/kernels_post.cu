@@ -352,7 +352,7 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
 
 
 // ---------------------------------------------------------------------------
-// Convection (rhs.c:1463-1946), for boxes with no periodic face.  The face
+// Convection (rhs.c:1463-1946).  The face
 // fluxes of ucat carried by Ucont/2 are formed once per face by k_conv_faces
 // into nine component planes (fp[(3d + c) n + p], coalesced), then
 // k_conv_diff takes their differences over each interior cell.  Every product
@@ -361,7 +361,10 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
 // j end of a row (a face next to the high end whose lower neighbour has nvert
 // above 0.1) it reads, on one rank, the first cells of the next row: the flat
 // index p + 2 st reads the same, and stays inside the box because the other
-// indices are interior.
+// indices are interior.  Along a periodic direction the reference first sets
+// the ghost cells just outside the box to the images two cells further out
+// (rhs.c:1546-1620) and takes the full QUICK form across the seam where both
+// sides are fluid: index -1 reads cell m - 3, index m reads cell 2.
 
 // |x| < 2^1000 (and not NaN), from the exponent field alone
 __device__ __forceinline__ bool conv_tame(double x) {
@@ -443,7 +446,7 @@ __global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__rest
   for (size_t pu = (size_t)blockIdx.x * blockDim.x + threadIdx.x; pu < n; pu += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(pu % g.mx), j = (int)((pu / g.mx) % g.my), k = (int)(pu / plane);
     const long long p = (long long)pu;
-    const int idx[3] = {i, j, k}, ext[3] = {g.mx, g.my, g.mz};
+    const int idx[3] = {i, j, k}, ext[3] = {g.mx, g.my, g.mz}, per[3] = {g.px, g.py, g.pz};
     const long long st[3] = {1, g.mx, (long long)plane};
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -465,9 +468,20 @@ __global__ void __launch_bounds__(256) k_conv_faces(Geom g, const double *__rest
         } else if (central && end2 && conv_fluid(nv[p + s]) && conv_fluid(nv[p])) {
           cen = 1;
         } else if ((d < 2 || q < m - 2) && (q == 0 || conv_above(nv[p - s], 0.1))) {
-          lo = 0; hi = 2;
+          // a periodic seam with fluid on both sides takes the full form across
+          // it; the reference's ghost cell -1 holds the image of m - 3
+          if (per[d] && q == 0 && conv_below(nv[p + (long long)(m - 3) * s], 0.1) && conv_below(nv[p + s], 0.1)) {
+            lo = m - 3; hi = 2;
+          } else {
+            lo = 0; hi = 2;
+          }
         } else if ((d < 2 || q > 0) && (q == m - 2 || conv_above(nv[p + s], 0.1))) {
-          lo = -1; hi = 1;
+          // ... and its ghost cell m the image of 2
+          if (per[d] && q == m - 2 && conv_below(nv[p - s], 0.1) && conv_below(nv[p + s], 0.1)) {
+            lo = -1; hi = 4 - m;
+          } else {
+            lo = -1; hi = 1;
+          }
         } else {
           any = 0;
         }

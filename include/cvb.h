@@ -219,8 +219,10 @@ int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at);
  * Ucat of the last cvb_projection_cart.  The nvert it tests is the context's
  * finest-level nvert, as the last cvb_setup_hierarchy or cvb_set_nvert gave it
  * (the reference reads lNvert on every call: after a body moves, call
- * cvb_set_nvert first).  Boxes with a periodic face (bctype 7) are refused with
- * CVB_BAD_INPUT. */
+ * cvb_set_nvert first).  Along a periodic direction (bctype 7) the faces at
+ * the seam read the periodic images the reference's ghost cells hold (cell
+ * m - 3 for index -1, cell 2 for index m) and take the full QUICK form where
+ * both sides are fluid, as the reference does (rhs.c:1546-1620). */
 int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv);
 /* The momentum right-hand side on the finest level, for boxes with no periodic
  * face (bctype 7 is refused with CVB_BAD_INPUT).  Vector fields are

@@ -1009,8 +1009,11 @@ static int conv_fluid(double n) { return n < 0.1 || n > 7.; }
 
 int orc_convection(const orc_level *L, const double *ucont, const double *ucat, int central, double *conv) {
   const int mx = L->mx, my = L->my, mz = L->mz;
-  for (int f = 0; f < 6; f++)
-    if (L->bctype[f] == 7) return -1;
+  /* a periodic direction: the reference first sets the ghost cells just
+   * outside the box to the images two cells further out (rhs.c:1546-1620):
+   * index -1 reads m - 3, index m reads 2 (ucat and nvert alike) */
+  const int per[3] = {L->bctype[0] == 7 || L->bctype[1] == 7, L->bctype[2] == 7 || L->bctype[3] == 7,
+                      L->bctype[4] == 7 || L->bctype[5] == 7};
   const size_t n = (size_t)mx * my * mz;
   const long st[3] = {1, mx, (long)mx * my};
   const int ext[3] = {mx, my, mz};
@@ -1035,9 +1038,13 @@ int orc_convection(const orc_level *L, const double *ucont, const double *ucat, 
           } else if (central && end2 && conv_fluid(NV(1)) && conv_fluid(NV(0))) {
             cen = 1;
           } else if ((d < 2 || q < m - 2) && (q == 0 || NV(-1) > 0.1)) {
-            lo = 0; hi = 2;
+            /* periodic low end with fluid on both sides: the full QUICK form
+             * across the seam (rhs.c:1675-1685 and its j, k siblings) */
+            if (per[d] && q == 0 && NV(m - 3) < 0.1 && NV(1) < 0.1) { lo = m - 3; hi = 2; }
+            else { lo = 0; hi = 2; }
           } else if ((d < 2 || q > 0) && (q == m - 2 || NV(1) > 0.1)) {
-            lo = -1; hi = 1;
+            if (per[d] && q == m - 2 && NV(-1) < 0.1 && NV(1) < 0.1) { lo = -1; hi = 4 - m; }
+            else { lo = -1; hi = 1; }
           } else {
             continue;
           }

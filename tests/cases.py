@@ -75,6 +75,20 @@ CONV_EDGES = [(5, 5, -3, 3.0), (6, -3, 4, 1.3), (-3, 4, 4, 2.0), (3, 3, 2, 0.1),
               (7, 7, 7, 8.0), (2, -2, 6, 1.2)]
 
 
+# Convection across the periodic seams of channel_periodic, (k, j, i, value):
+# blocked cells next to the seam in x (i = mx-3, whose image the seam face at
+# i = 0 reads, and i = 1) and in z, so that the seam faces take both the full
+# QUICK form across the seam and the one-sided forms.
+CONV_SEAM = [(4, 4, -3, 3.0), (3, 2, 1, 2.0), (-3, 5, 6, 3.0), (1, 3, 9, 1.3)]
+
+
+def conv_seam_nvert(nvert):
+    nv = np.array(nvert, dtype=np.float64, copy=True)
+    for (k, j, i, v) in CONV_SEAM:
+        nv[k, j, i] = v
+    return nv
+
+
 def conv_edge_nvert(nvert):
     nv = np.array(nvert, dtype=np.float64, copy=True)
     for (k, j, i, v) in CONV_EDGES:

@@ -166,6 +166,18 @@ int main(void) {
   les = 0;
   fine->bctype[0] = fine->bctype[1] = 7;
   VecDestroy(&Conv);
+  /* the periodic box as FormFunction1 passes it: ghosted local vectors; the
+   * owned box goes to the library and Conv's owned part comes back */
+  Vec ConvL;
+  VecDuplicate(fine->lUcont, &ConvL);
+  const int nconv = REC.n_convection;
+  CHECK(Convection_GB300(fine, fine->lUcont, fine->lUcat, ConvL) == 0 && REC.n_convection == nconv + 1,
+        "periodic convection not on the device");
+  CHECK(REC.ucont_conv != shim_vec_data(fine->lUcont) && REC.conv_conv != shim_vec_data(ConvL),
+        "ghosted vectors passed as boxes");
+  CHECK(shim_vec_data(ConvL)[3 * loc] == 7.0, "Conv's owned part not written back");
+  CHECK(shim_vec_data(ConvL)[0] == 0.0, "Conv's ghost cells not 0");
+  VecDestroy(&ConvL);
   CHECK(shim_arrays_out() == 0, "convection left %d arrays out", shim_arrays_out());
 
   /* --- failures come back as the call's status, arrays restored --- */

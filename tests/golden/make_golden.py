@@ -28,7 +28,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from cases import (MOM_DT, MOM_REN, mom_edge_nvert, momentum_inputs)  # noqa: E402
+from cases import (MOM_DT, MOM_REN, conv_seam_nvert, mom_edge_nvert, momentum_inputs)  # noqa: E402
 from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
 from curvib_old_gb300 import workload as W  # noqa: E402
@@ -85,6 +85,9 @@ def run(name):
     if name == "box_sphere":
         rec["convection_edges"] = convection(R, conv_edge_nvert(c["nvert"]), c["ucont"], c["bctype"])
         R.set_nvert(nl - 1, c["nvert"])
+    if name == "channel_periodic":
+        rec["convection_seam"] = convection(R, conv_seam_nvert(c["nvert"]), c["ucont"], c["bctype"])
+        R.set_nvert(nl - 1, c["nvert"])
     rec["momentum"] = momentum(R, c["nvert"], c["ucont"], c["bctype"])
     if name == "box_sphere":
         rec["momentum_edges"] = momentum(R, mom_edge_nvert(c["nvert"]), c["ucont"], c["bctype"])
@@ -100,9 +103,7 @@ def run(name):
 
 def convection(R, nvert, ucont, bctype):
     """Convection (rhs.c:1463) on the ucat of post_inputs(seed 0), QUICK and
-    central; None for a box with a periodic face (not covered)."""
-    if 7 in list(bctype):
-        return None
+    central (periodic faces included)."""
     R.set_nvert(R.nlevels - 1, nvert)
     ucat0, _ = post_inputs(nvert.shape, 0)
     return {"quick": digest(R.convection(ucont, ucat0, 0)), "central": digest(R.convection(ucont, ucat0, 1))}

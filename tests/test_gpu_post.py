@@ -121,15 +121,9 @@ def test_divergence_matches_oracle(ctxs, key):
 @pytest.mark.parametrize("key", sorted(CASES))
 def test_convection_bit_exact(ctxs, key):
     """Convection (rhs.c:1463-1946), QUICK and central, bit for bit against the
-    oracle; a box with a periodic face is refused."""
-    from curvib_old_gb300._lib import CvbError
+    oracle, periodic seams included."""
     ctx, P, L, seed = ctxs[key]
     ucat0, _ = post_inputs(P.nvert.shape, seed)
-    if 7 in list(P.bctype):
-        with pytest.raises(CvbError) as e:
-            ctx.convection(P.ucont, ucat0)
-        assert e.value.status == 4  # CVB_BAD_INPUT
-        return
     for central in (False, True):
         rc, want = O.convection(L, P.ucont, ucat0, int(central))
         assert rc == 0
@@ -178,3 +172,22 @@ def test_metrics_divergence_matches_oracle(ctxs, key):
     the maximum and its first index, bit for bit."""
     ctx, P, L, seed = ctxs[key]
     assert ctx.metrics_divergence() == O.metrics_divergence(L)
+
+
+def test_convection_across_periodic_seams():
+    """The periodic channel with blocked cells next to its x and z seams
+    (cases.CONV_SEAM): the seam faces take the full QUICK form across the seam
+    where both sides are fluid and the one-sided forms beside the blocked cells."""
+    from cases import conv_seam_nvert
+    from curvib_old_gb300.solver import PoissonContext
+    P, seed = _problem("channel_periodic")
+    P.nvert = conv_seam_nvert(P.nvert)
+    L = O.OLevel(P.metrics[-1], P.nvert, P.bctype, P.semi)
+    ctx = PoissonContext().setup(P)
+    try:
+        ucat0, _ = post_inputs(P.nvert.shape, seed)
+        for central in (0, 1):
+            rc, want = O.convection(L, P.ucont, ucat0, central)
+            assert rc == 0 and ctx.convection(P.ucont, ucat0, central).tobytes() == want.tobytes(), central
+    finally:
+        ctx.close()

@@ -93,16 +93,15 @@ def test_oracle_matches_reference(name):
     if "convection_edges" in ref:
         Le = O.OLevel(c["metrics"][-1], conv_edge_nvert(c["nvert"]), c["bctype"], c["semi"])
         _check_convection(c, Le, ref["convection_edges"])
+    if "convection_seam" in ref:
+        from cases import conv_seam_nvert
+        Ls_ = O.OLevel(c["metrics"][-1], conv_seam_nvert(c["nvert"]), c["bctype"], c["semi"])
+        _check_convection(c, Ls_, ref["convection_seam"])
 
 
 def _check_convection(c, L, want):
-    """Convection (rhs.c:1463-1946), QUICK and central; a periodic box is
-    refused (status -1, nothing written)."""
+    """Convection (rhs.c:1463-1946), QUICK and central, periodic faces included."""
     ucat0, _ = post_inputs(L.shape, 0)
-    if want is None:
-        rc, conv = O.convection(L, c["ucont"], ucat0)
-        assert rc == -1 and not conv.any()
-        return
     for key, central in (("quick", 0), ("central", 1)):
         rc, conv = O.convection(L, c["ucont"], ucat0, central)
         assert rc == 0 and digest(conv) == want[key], key
