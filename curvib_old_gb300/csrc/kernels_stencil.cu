@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
 
 // RR: the line layout's rows per lane fixed at compile time (0: read from my)
 template <typename T, int TW, int RR>
-__global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
+__global__ void __launch_bounds__(kSolveThreads, kTileMinBlocks<RR>) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
                                                                  T *xnew, T omega, int color, int rsplit) {
   dep_sync();
   if (gated(L.gate)) return;
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_line_solve(LevelDev L, con
 }
 
 template <typename T, int TW, int RR, bool X>
-__global__ void __launch_bounds__(kSolveThreads, 4) k_zebra_fused(LevelDev L, const T *__restrict__ b, const T *xin,
+__global__ void __launch_bounds__(kSolveThreads, X ? 4 : kTileMinBlocks<RR>) k_zebra_fused(LevelDev L, const T *__restrict__ b, const T *xin,
                                                                   T *xout, T omega, int color) {
   dep_sync();
   if (gated(L.gate)) return;
@@ -127,7 +127,7 @@ static void line_solve_r(const LevelDev &L, const T *r, const T *x, T *xnew, T o
     cudaFuncSetAttribute(k_line_solve<T, TW, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  launch_dep(k_line_solve<T, TW, RR>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, r, x, xnew, omega,
+  launch_dep(k_line_solve<T, TW, RR>, grd, kSolveThreads, line_solve_smem_rr<T, TW>(L.g, RR), s, L, r, x, xnew, omega,
              color, rsplit);
 }
 template <typename T, int TW>
@@ -247,7 +247,7 @@ static void zebra_fused_rx(const LevelDev &L, const T *b, const T *xin, T *xout,
     cudaFuncSetAttribute(k_zebra_fused<T, TW, RR, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  launch_dep(k_zebra_fused<T, TW, RR, X>, grd, kSolveThreads, line_solve_smem<T, TW>(L.g), s, L, b, xin, xout, omega,
+  launch_dep(k_zebra_fused<T, TW, RR, X>, grd, kSolveThreads, line_solve_smem_rr<T, TW>(L.g, RR), s, L, b, xin, xout, omega,
              color);
 }
 template <typename T, int TW, int RR>

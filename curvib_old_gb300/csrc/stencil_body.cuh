@@ -675,6 +675,20 @@ struct Vec16<double> {
 // memory (a store and two to four loads per value).
 template <int RR>
 constexpr bool kRegFactors = RR >= 1 && RR <= 4;
+// Rows of a line-solve tile in shared memory: the residual, then the three
+// Thomas factor runs (only where they are not in registers), then x.
+template <int RR>
+constexpr int kTileRows = kRegFactors<RR> ? 2 : 5;
+// Shared memory of a line-solve / one-kernel zebra tile for a kernel compiled
+// with RR (R at compile time; 0 = at run time).
+template <typename T, int TW>
+inline size_t line_solve_smem_rr(const Geom &g, int rr) {
+  return sizeof(T) * ((rr >= 1 && rr <= 4) ? 2 : 5) * (size_t)LineLayout::of(g.my).ls * TW;
+}
+// Resident blocks per SM the tile kernels are compiled for: with the factors in
+// registers they fit in 48 registers, ten blocks of 128 threads.
+template <int RR>
+constexpr int kTileMinBlocks = kRegFactors<RR> ? 10 : 4;
 
 template <int N>
 __device__ __forceinline__ void ld_run(const float *p, float (&o)[N]) {
@@ -744,7 +758,7 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
   const int my = g.my, mx = g.mx;
   if (!(k >= 1 && k <= g.mz - 2)) return;
   const LineLayout Lo = LineLayout::fixed<RR>(my);
-  T *sr = st, *sa = sr + Lo.ls * TW, *sx = sa + 3 * Lo.ls * TW;
+  T *sr = st, *sa = sr + Lo.ls * TW, *sx = st + (kTileRows<RR> - 1) * Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
   constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
@@ -797,7 +811,8 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
   const Geom &g = L.g;
   const int my = g.my, mx = g.mx;
   const LineLayout Lo = LineLayout::fixed<RR>(my);
-  T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW, *sx = sc + Lo.ls * TW;
+  T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW;
+  T *sx = st + (kTileRows<RR> - 1) * Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
   constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
@@ -926,7 +941,7 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
   const bool kin = k >= 1 && k <= g.mz - 2;
   if (kin) {
     const LineLayout Lo = LineLayout::fixed<RR>(my);
-    T *sr = st, *sx = st + 4 * Lo.ls * TW;
+    T *sr = st, *sx = st + (kTileRows<RR> - 1) * Lo.ls * TW;
     const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
     constexpr int ny = kSolveThreads / TW;
     const int i = tile_line(bx, tx, k, TW, color);

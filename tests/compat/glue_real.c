@@ -122,7 +122,38 @@ int main(int argc, char **argv) {
   fine->dt = 0.01;
   fine->st = 1.0;
 
-  /* --- the binding on the real library --- */
+  /* --- the binding on the real library (refonly: skipped, the reference half
+   * runs on the initial fields, to check this driver without a GPU) --- */
+  const int refonly = argc > 2 && !strcmp(argv[2], "refonly");
+  if (refonly) {
+    double *z = (double *)calloc(3 * n, sizeof(double));
+    double *uc_b = copy_of(uc0, 3 * n), *phi_b = z, *p_b = z, *phi_b2 = z, *uc_b2 = uc_b, *ucat_b = z, *conv_b = z;
+    (void)p_b; (void)phi_b2; (void)ucat_b; (void)conv_b;
+    STEP("reference routines");
+    double *uc_r = copy_of(uc0, 3 * n), flux, area;
+    ref_volume_flux(0.0, 1, uc_r, &flux, &area);
+    STEP("rhs");
+    double *b = (double *)malloc(sizeof(double) * n), sum;
+    ref_rhs(fine->dt, fine->st, b, &sum);
+    STEP("lhs");
+    const int cap = (int)n * 19;
+    int *rowptr = (int *)malloc(sizeof(int) * (n + 1)), *cols = (int *)malloc(sizeof(int) * cap);
+    double *vals = (double *)malloc(sizeof(double) * cap);
+    printf("lhs entries %d\n", ref_lhs(NL - 1, rowptr, cols, vals, cap));
+    STEP("update_and_project");
+    double *p_r = (double *)calloc(n, sizeof(double)), *phi_r = copy_of(phi_b, n), *uc_r2 = copy_of(uc_b, 3 * n);
+    ref_update_and_project(fine->dt, fine->st, p_r, phi_r, uc_r2);
+    STEP("contra2cart");
+    double *ucat_r = (double *)calloc(3 * n, sizeof(double)), *ubcs_r = (double *)calloc(3 * n, sizeof(double));
+    ref_contra2cart(uc_r2, ucat_r);
+    STEP("ghost");
+    ref_ghost_node_velocity(ubcs_r, ucat_r);
+    STEP("convection");
+    double *conv_r = (double *)calloc(3 * n, sizeof(double));
+    ref_convection(uc_b2, ucat_r, 0, conv_r);
+    STEP("done");
+    return 0;
+  }
   STEP("PoissonSetup_GB300");
   CHECK(PoissonSetup_GB300(mg) == 0, "PoissonSetup_GB300 failed");
   STEP("PoissonSolver_MG_GB300");
