@@ -1,16 +1,23 @@
 """Times the multigrid kernels of one level with CUDA events.
 
-    python -m curvib_old_gb300.kernel_timer [--cells 256x128x128] [--level -1] [--reps 20] [KERNEL ...]
+    python -m curvib_old_gb300.kernel_timer [--cells 256x128x128] [--level -1] [--reps 20]
+                                            [--grid channel|box] [KERNEL ...]
 
 KERNEL is one of line_sweep_f32, line_sweep_f64 (a damped-Jacobi y-line sweep),
 residual_f32, residual_f64, zebra_f32, zebra_f64 (one half-sweep of the zebra
 smoother: residual on one color, then its line solves), vcycle_f32, vcycle_f64
 (one V-cycle with the default options from the level down, replayed from a
 CUDA graph; no byte count), contra2cart, ghost_nodes, convection
-(Contra2Cart, GhostNodeVelocity and Convection; finest level only); default:
-all.  Convection runs on a walled box of the same cell counts (distorted, tanh
-2.0 in y), since it does not cover periodic faces.  The problem is the periodic channel (x and z periodic,
-tanh-stretched walls in y, factor 2.5) at the given cell counts.  Each kernel's
+(Contra2Cart, GhostNodeVelocity and Convection; finest level only), viscous,
+momentum_rhs (Viscous, and CalcRHS with FormFunction1's Convection and
+pressure gradient; finest level only); default: all.  ``--grid channel`` (the
+default) is the periodic channel (x and z periodic, tanh-stretched walls in y,
+factor 2.5) at the given cell counts, whose operator is 7-point; ``--grid box``
+is a walled box of the same cell counts (tanh 2.0 in y, nodes moved by sine
+waves in x and z), so
+every level keeps the 19-point operator with its cross-derivative terms.
+Convection, viscous and momentum_rhs always run on the box: the momentum
+right-hand side does not cover periodic faces.  Each kernel's
 timed launches run inside an NVTX range named ``timed:<kernel>``, so a profiler
 can be pointed at exactly those launches (``ncu --nvtx --nvtx-include
 "timed:line_sweep_f32/"``) and skip the set-up autotuner's launches.  Prints one
@@ -42,6 +49,7 @@ def main(argv=None):
     ap.add_argument("--cells", type=_cells, default=(256, 128, 128))
     ap.add_argument("--level", type=int, default=-1, help="multigrid level (0 coarsest, -1 finest)")
     ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--grid", choices=["channel", "box"], default="channel")
     a = ap.parse_args(argv)
     for k in a.kernels:
         if k not in KERNELS:
@@ -49,13 +57,15 @@ def main(argv=None):
     import torch  # NVTX ranges only; the kernels themselves come from libcvb.so
 
     ctx = box = None
+    on_box = {"convection", "viscous", "momentum_rhs"}
     for k in a.kernels:
-        if k == "convection":
+        if k in on_box or a.grid == "box":
             box = box or PoissonContext().setup(W.make_problem(a.cells, (1.0, 1.0, 1.0), 2.0, True,
                                                                (False, False, False), [], name="box"))
+            c = box
         else:
             ctx = ctx or PoissonContext().setup(W.config1_problem(cells=a.cells))
-        c = box if k == "convection" else ctx
+            c = ctx
         torch.cuda.nvtx.range_push(f"timed:{k}")
         ms, nbytes = c.time_kernel(k, level=a.level, reps=a.reps)
         torch.cuda.nvtx.range_pop()

@@ -16,7 +16,9 @@
  *
  * usage: glue_real fp64|mixed  -> prints one line per failed check, exits with their count
  */
+#include <execinfo.h>
 #include <math.h>
+#include <signal.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -63,10 +65,22 @@ static double maxabs(const double *a, size_t n) {
   return m;
 }
 
-#define STEP(name) (printf("step: %s\n", name), fflush(stdout))
+static const char *volatile g_step = "start";
+#define STEP(name) (g_step = name, printf("step: %s\n", name), fflush(stdout))
+
+/* a fault names the step it came in and the call stack (link with -rdynamic) */
+static void on_fault(int sig) {
+  fprintf(stderr, "signal %d in step %s\n", sig, g_step);
+  void *pc[48];
+  backtrace_symbols_fd(pc, backtrace(pc, 48), 2);
+  signal(sig, SIG_DFL);
+  raise(sig);
+}
 
 int main(int argc, char **argv) {
   setvbuf(stdout, NULL, _IONBF, 0);
+  signal(SIGSEGV, on_fault);
+  signal(SIGBUS, on_fault);
   const int mixed = argc > 1 && !strcmp(argv[1], "mixed");
   /* 16 x 12 x 10 cells, walls everywhere, stretched and sheared, three levels */
   enum { IM = 17, JM = 13, KM = 11, NL = 3 };
