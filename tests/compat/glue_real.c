@@ -201,7 +201,9 @@ int main(int argc, char **argv) {
   CHECK(ref_lhs(NL - 1, rowptr, cols, vals, cap) > 0, "ref_lhs failed");
   /* residual of the binding's Phi on the fluid cells, after removing the part
    * of b outside the operator's range (aj times the fluid mean of b / aj) */
-  double *aj = shim_vec_data(fine->Aj);
+  /* FormMetrics destroys the global Aj (metrics.c:1221); on this walled box
+   * the ghosted lAj is the box itself */
+  double *aj = shim_vec_data(fine->lAj);
   double cs = 0, cn = 0;
   for (size_t q = 0; q < n; q++) {
     const int i = (int)(q % mx), j = (int)((q / mx) % my), k = (int)(q / ((size_t)mx * my));
