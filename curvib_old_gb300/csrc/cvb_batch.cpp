@@ -112,6 +112,13 @@ struct cvb_batch {
   int next_ticket = 0;
   long long launches_per_round = 0;
   long long round_limit = kDefaultRoundLimit;  // rounds cvb_batch_solve issues before CVB_TIMEOUT
+  // the mixed-precision rounds' V-cycles as a CUDA graph (run_vcycles)
+  bool graphs = true;
+  std::vector<unsigned long long> vkey;  // (slot, ctx set-up id) of the iterating problems it was made for
+  int vkey_rounds = 0;                   // rounds run with that key so far
+  cudaGraphExec_t vexec = nullptr;
+  bool vexec_ok = false;                 // vexec holds the program of vkey
+  long long graph_captures = 0, graph_updates = 0, graph_replays = 0;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -382,6 +389,74 @@ static void run_program(cvb_batch *bt, std::map<long long, std::array<Lists, OK_
   }
 }
 
+// The V-cycles of one round.  In mixed precision they read each problem's FP32
+// input and write its FP32 output, whatever its Krylov index, so the round's
+// V-cycle program depends only on which problems iterate: it is captured in a
+// CUDA graph and replayed while that set stays the same.  A set's first round
+// runs the launches eagerly (kernel attributes are set outside any capture), its
+// second captures them -- updating the previous graph in place when the launch
+// structure is the same, instantiating a new one otherwise -- and every round
+// from the second on launches the graph alone.  FP64 rounds (whose V-cycles
+// read V_j and write Z_j) run eagerly.  A capture the runtime refuses turns the
+// graphs off for the batch; the launches then run eagerly, with the same result.
+static void run_vcycles(cvb_batch *bt, std::map<long long, std::array<Lists, OK_COUNT>> &prog, bool f32,
+                        const std::vector<Prob *> &iterating) {
+  cudaStream_t s = bt->stream;
+  if (!f32 || !bt->graphs || s == nullptr) {
+    run_program(bt, prog, f32);
+    return;
+  }
+  std::vector<unsigned long long> key;
+  key.reserve(2 * iterating.size());
+  for (Prob *p : iterating) {
+    key.push_back((unsigned long long)p->slot);
+    key.push_back(p->ctx->setup_id);
+  }
+  if (key != bt->vkey) {
+    bt->vkey.swap(key);
+    bt->vkey_rounds = 0;
+    bt->vexec_ok = false;
+  }
+  if (++bt->vkey_rounds == 1) {
+    run_program(bt, prog, f32);
+    return;
+  }
+  if (!bt->vexec_ok) {
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      run_program(bt, prog, f32);
+      e = cudaStreamEndCapture(s, &graph);
+    }
+    if (e == cudaSuccess && graph && bt->vexec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(bt->vexec, graph, &info) == cudaSuccess) {
+        bt->graph_updates++;
+      } else {
+        cudaGetLastError();
+        cudaGraphExecDestroy(bt->vexec);
+        bt->vexec = nullptr;
+      }
+    }
+    if (e == cudaSuccess && graph && !bt->vexec) {
+      e = cudaGraphInstantiate(&bt->vexec, graph, 0);
+      if (e == cudaSuccess) bt->graph_captures++;
+      else bt->vexec = nullptr;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess || !bt->vexec) {
+      cudaGetLastError();
+      bt->graphs = false;
+      run_program(bt, prog, f32);
+      return;
+    }
+    bt->vexec_ok = true;
+  }
+  cudaGraphLaunch(bt->vexec, s);
+  count_launch();
+  bt->graph_replays++;
+}
+
 // ------------------------------------------------------------ Krylov rounds
 static BProblem *dprob(cvb_batch *bt, int slot) { return bt->dP + slot; }
 static KState *dks(cvb_batch *bt, int slot) { return bt->dK + slot; }
@@ -582,7 +657,7 @@ static int issue_round(cvb_batch *bt, std::vector<Prob *> &starting, std::vector
       slots.push_back(p->slot);
     }
     for (OpBatch &ob : conv.v) glaunch_elementwise(ob.tl, 2, s);
-    run_program(bt, prog, f32);
+    run_vcycles(bt, prog, f32, iterating);
     for (OpBatch &ob : widen.v) glaunch_elementwise(ob.tl, 3, s);
     launch_lists2(apply, glaunch_residual64, bt);
     launch_lists(mdot, glaunch_multidot, bt);
@@ -688,6 +763,7 @@ static void destroy(cvb_batch *bt) {
     if (bt->hF[q]) cudaFreeHost(bt->hF[q]);
     if (bt->ev[q]) cudaEventDestroy(bt->ev[q]);
   }
+  if (bt->vexec) cudaGraphExecDestroy(bt->vexec);
   if (bt->copy_stream) cudaStreamDestroy(bt->copy_stream);
   if (bt->own_stream && bt->stream) cudaStreamDestroy(bt->stream);
   delete bt;
@@ -857,6 +933,23 @@ int cvb_batch_solve(cvb_batch *bt, int n, cvb_ctx *const *ctxs, cvb_solve_stats 
 int cvb_batch_set_round_limit(cvb_batch *bt, long long rounds) {
   if (!bt || rounds < 0) return CVB_BAD_INPUT;
   bt->round_limit = rounds == 0 ? kDefaultRoundLimit : rounds;
+  return CVB_OK;
+}
+
+int cvb_batch_set_graphs(cvb_batch *bt, int on) {
+  if (!bt) return CVB_BAD_INPUT;
+  bt->graphs = on != 0;
+  bt->vkey.clear();
+  bt->vkey_rounds = 0;
+  bt->vexec_ok = false;
+  return CVB_OK;
+}
+
+int cvb_batch_graph_stats(const cvb_batch *bt, long long *captures, long long *updates, long long *replays) {
+  if (!bt) return CVB_BAD_INPUT;
+  if (captures) *captures = bt->graph_captures;
+  if (updates) *updates = bt->graph_updates;
+  if (replays) *replays = bt->graph_replays;
   return CVB_OK;
 }
 

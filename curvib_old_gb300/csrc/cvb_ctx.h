@@ -95,11 +95,14 @@ struct cvb_ctx {
   double *ibm_cent = nullptr;  // cell centres of the last cvb_ibm_search that gave them
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;
+  // changes with every set-up of the operators (process-wide counter): the
+  // batch engine's captured V-cycles are valid for one value
+  unsigned long long setup_id = 0;
   std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)
   // measured sweep times (us): line sweeps fused / split, zebra sweeps two-kernel /
   // one-kernel, and the FP32 zebra sweep with TMA-staged tiles of 4, 8, 16 row
   // pairs (0: not run on this level)
-  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2], zt32[3]; };
+  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2], zt32[3], zs32[3], zs64[3]; };
   std::vector<Tune> tune;
 };
 

@@ -364,6 +364,18 @@ class PoissonContext:
             raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
         return xb
 
+    def zebra_sweep_slabs(self, level, slabs, b, x, precision="mixed", omega=1.3):
+        """One zebra sweep of x (returned) in place with the one-kernel form over
+        `slabs` plane slabs: FP32 arrays for "mixed", FP64 for "fp64"."""
+        dt = np.float32 if precision == "mixed" else np.float64
+        prec = _lib.MIXED if precision == "mixed" else _lib.FP64
+        xb = np.ascontiguousarray(x, dtype=dt).copy()
+        bb = np.ascontiguousarray(b, dtype=dt)
+        rc = self._L.cvb_zebra_sweep_slabs(self._ctx, level, prec, slabs, omega, ptr(bb), ptr(xb))
+        if rc:
+            raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
+        return xb
+
     def weights(self, level):
         w = np.zeros((19,) + self.shapes[level])
         self._check(self._L.cvb_get_weights(self._ctx, level, ptr(w)))
@@ -463,6 +475,16 @@ class SolveBatch:
         """Bound ``solve``'s loop to ``rounds`` rounds (0: the default); past it
         ``solve`` raises CVB_TIMEOUT with the unfinished solves still in flight."""
         self._check(self._L.cvb_batch_set_round_limit(self._b, int(rounds)))
+
+    def set_graphs(self, on):
+        """Replay the mixed rounds' V-cycles from CUDA graphs (on by default)."""
+        self._check(self._L.cvb_batch_set_graphs(self._b, 1 if on else 0))
+
+    def graph_stats(self):
+        """{"captures", "updates", "replays"} of the V-cycle graphs so far."""
+        v = [ctypes.c_longlong() for _ in range(3)]
+        self._check(self._L.cvb_batch_graph_stats(self._b, *[ctypes.byref(q) for q in v]))
+        return {"captures": v[0].value, "updates": v[1].value, "replays": v[2].value}
 
     def solve(self, ctxs):
         """Solve every context's resident rhs; returns their stats in order."""

@@ -346,6 +346,17 @@ enum {
   CVB_ZEBRA_TMA16 = 16
 };
 int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega, const float *b, float *x);
+/* One zebra sweep (colour 0, then colour 1) on a level, in place, with the
+ * one-kernel half-sweep launched over `slabs` slabs of planes (1 to 64):
+ * colour 0 on a slab, then colour 1 one plane behind it, then the next slab,
+ * so that colour 1 reads the slab's arrays while colour 0's launch has left
+ * them in L2.  The result is the one of the two whole-level half-sweeps.
+ * precision CVB_PRECISION_MIXED: FP32 arrays (the V-cycle's precision there),
+ * CVB_PRECISION_FP64: FP64.  b, x: host arrays of the level's box.  Levels
+ * with cross-derivative terms, or periodic in x (z) with an odd mx (mz), are
+ * refused (CVB_BAD_INPUT).  Part of the same smoother as PoissonSolver_MG's
+ * (poisson.c:1775); the set-up autotuner picks the slab count per level. */
+int cvb_zebra_sweep_slabs(cvb_ctx *ctx, int level, int precision, int slabs, double omega, const void *b, void *x);
 /* MyRestriction (poisson.c:129) from level+1 to level; MyInterpolation
  * (poisson.c:265) from level-1 to level (returned, not added). */
 int cvb_restrict(cvb_ctx *ctx, int coarse_level, const double *xf, double *xc);
@@ -426,6 +437,13 @@ int cvb_batch_in_flight(const cvb_batch *batch);
  * cvb_batch_step / cvb_batch_poll carry them on to their results.  No
  * counterpart in the reference, whose KSPSolve has only max_it. */
 int cvb_batch_set_round_limit(cvb_batch *batch, long long rounds);
+/* Mixed-precision rounds replay their V-cycles from a CUDA graph while the set
+ * of iterating problems stays the same (on by default; 0 turns it off, the
+ * launches then run one by one with the same result).  No counterpart in the
+ * reference, whose solves run one at a time (poisson.c:1775). */
+int cvb_batch_set_graphs(cvb_batch *batch, int on);
+/* Graphs instantiated, graphs updated in place, and graph launches so far. */
+int cvb_batch_graph_stats(const cvb_batch *batch, long long *captures, long long *updates, long long *replays);
 /* Device memory held by a context alone (operators, vectors, Krylov basis) and
  * by its grid's shared metrics, with an id that is equal for contexts sharing them. */
 int cvb_device_bytes(const cvb_ctx *ctx, unsigned long long *bytes);

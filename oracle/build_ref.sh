@@ -63,7 +63,7 @@ if [ "$1" != "--preprocessed" ]; then
   fi
   # the stubs: what the linked units leave unresolved
   for u in $UNITS; do
-    $CC -std=gnu99 -O2 -fPIC -w -c "$SRC/$u.i" -o "$OUT/ref_$u.o"
+    $CC -std=gnu99 -O2 -ffp-contract=off -fPIC -w -c "$SRC/$u.i" -o "$OUT/ref_$u.o"
   done
   objcopy --keep-global-symbol=Divergence --keep-global-symbol=Ucont_P_Binary_Output \
           --keep-global-symbol=Ucont_P_Binary_Input --keep-global-symbol=ti "$OUT/ref_main.o"
@@ -99,7 +99,10 @@ if [ ! -f "$SRC/poisson.i" ] || [ ! -f "$SRC/ref_stubs.c" ]; then
   echo "build_ref: no preprocessed reference units in $SRC" >&2
   exit 2
 fi
-CFLAGS="-std=gnu99 -O2 -fPIC -w"
+# -ffp-contract=off: every product and sum rounds on its own, in the C order
+# of the source, on every architecture (gcc fuses a*b+c into one multiply-add
+# by default where the target has one, as aarch64 does)
+CFLAGS="-std=gnu99 -O2 -ffp-contract=off -fPIC -w"
 objs=()
 for u in $UNITS; do
   $CC $CFLAGS -c "$SRC/$u.i" -o "$OUT/ref_$u.o"

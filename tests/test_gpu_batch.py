@@ -174,3 +174,26 @@ def test_round_limit_times_out_and_batch_stays_usable(items):
             assert np.array_equal(items[q][0].get_phi(), alone[k]), q
     finally:
         B.close()
+
+
+def test_graph_replay_equals_eager_launches(items):
+    """Mixed rounds replay their V-cycles from CUDA graphs while the iterating
+    set is unchanged; the results must be the eager launches' bit for bit."""
+    from curvib_old_gb300.solver import SolveBatch
+    out = {}
+    for graphs in (True, False):
+        B = SolveBatch(precision=1, rtol=RTOL, max_it=100)
+        try:
+            B.set_graphs(graphs)
+            for ctx, _, b in items:
+                ctx.set_rhs(b)
+            sts = B.solve([ctx for ctx, _, _ in items])
+            out[graphs] = (sts, [ctx.get_phi() for ctx, _, _ in items], B.graph_stats())
+        finally:
+            B.close()
+    (s1, p1, g1), (s0, p0, g0) = out[True], out[False]
+    assert g1["replays"] > 0 and g1["captures"] >= 1
+    assert g0["replays"] == 0
+    for q in range(len(items)):
+        assert s1[q]["status"] == 0 and s1[q]["iterations"] == s0[q]["iterations"]
+        assert np.array_equal(p1[q], p0[q]), q

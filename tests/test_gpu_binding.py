@@ -35,7 +35,7 @@ def test_binding_on_the_real_library_matches_reference(tmp_path, precision):
     lib = Path(_lib.lib_path())
     _lib.lib()
     exe = tmp_path / "glue_real"
-    subprocess.run(["gcc", "-std=gnu99", "-O1", "-g", "-rdynamic", "-w", str(PRE / "poisson_gb300.i"), str(PRE / "glue_real.i"),
+    subprocess.run(["gcc", "-std=gnu99", "-O1", "-ffp-contract=off", "-g", "-rdynamic", "-w", str(PRE / "poisson_gb300.i"), str(PRE / "glue_real.i"),
                     "-L", str(lib.parent), "-lcvb", f"-Wl,-rpath,{lib.parent}", "-L", str(ref.parent), "-lcvbref",
                     f"-Wl,-rpath,{ref.parent}", "-lm", "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), precision], capture_output=True, text=True, timeout=300)
