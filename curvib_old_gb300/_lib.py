@@ -109,7 +109,6 @@ EXPORTS = {
     "cvb_batch_set_graphs": ([_P, _I], _I),
     "cvb_batch_graph_stats": ([_P, _P, _P, _P], _I),
     "cvb_zebra_half_f32": ([_P, _I, _I, _I, ctypes.c_float, _P, _P], _I),
-    "cvb_zebra_sweep_slabs": ([_P, _I, _I, _I, ctypes.c_double, _P, _P], _I),
     "cvb_viscous": ([_P, _P, _D, _P], _I),
     "cvb_form_function1": ([_P, _P, _P, _P, _D, _I, _P], _I),
     "cvb_calc_rhs": ([_P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P], _I),

@@ -443,7 +443,7 @@ bool g_tune_loaded = false;
 
 // With CVB_TUNE_FILE set, measured choices persist in that text file (one
 // shape per line: mx my mz px py pz, the two cross-term flags and the
-// seventeen timings in microseconds), so a
+// eleven timings in microseconds), so a
 // later process -- a profiler run, say, whose own timings would be distorted --
 // makes the same choices.  Called with g_tune_mu held.
 void tune_file_load() {
@@ -455,10 +455,9 @@ void tune_file_load() {
   if (!f) return;
   ShapeKey k;
   cvb_ctx::Tune t;
-  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf",
-                     &k.mx, &k.my, &k.mz, &k.px, &k.py, &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0],
-                     &t.us64[1], &t.zb32[0], &t.zb32[1], &t.zb64[0], &t.zb64[1], &t.zt32[0], &t.zt32[1], &t.zt32[2],
-                     &t.zs32[0], &t.zs32[1], &t.zs32[2], &t.zs64[0], &t.zs64[1], &t.zs64[2]) == 25) {
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf", &k.mx, &k.my, &k.mz,
+                     &k.px, &k.py, &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0], &t.us64[1], &t.zb32[0],
+                     &t.zb32[1], &t.zb64[0], &t.zb64[1], &t.zt32[0], &t.zt32[1], &t.zt32[2]) == 19) {
     t.level = 0;
     t.cells = (size_t)k.mx * k.my * k.mz;
     g_tune_cache.emplace(k, t);
@@ -470,18 +469,12 @@ void tune_file_append(const ShapeKey &k, const cvb_ctx::Tune &t) {
   if (!path || !*path) return;
   FILE *f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f,
-               "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f "
-               "%.3f %.3f\n",
-               k.mx, k.my, k.mz, k.px, k.py, k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0],
-               t.zb32[1], t.zb64[0], t.zb64[1], t.zt32[0], t.zt32[1], t.zt32[2], t.zs32[0], t.zs32[1], t.zs32[2],
-               t.zs64[0], t.zs64[1], t.zs64[2]);
+  std::fprintf(f, "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz,
+               k.px, k.py, k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0], t.zb32[1],
+               t.zb64[0], t.zb64[1], t.zt32[0], t.zt32[1], t.zt32[2]);
   std::fclose(f);
 }
 }  // namespace
-
-// slab counts the autotuner times for the zebra sweep in plane slabs
-static const int kTuneSlabs[3] = {2, 4, 8};
 
 static int autotune_sweeps(cvb_ctx *ctx) {
   ctx->tune.clear();
@@ -505,14 +498,6 @@ static int autotune_sweeps(cvb_ctx *ctx) {
       const int rps[3] = {4, 8, 16};
       for (int v = 0; v < 3; v++)
         if (t.zt32[v] > 0.0 && t.zt32[v] < best) { best = t.zt32[v]; L.ztma32 = rps[v]; }
-      // the sweep in plane slabs, against the best whole-level form, same rule
-      L.zslab32 = L.zslab64 = 0;
-      double best32 = 0.97 * (L.ztma32 ? best / 0.97 : other);
-      double best64 = 0.97 * (L.zfuse64 ? t.zb64[1] : t.zb64[0]);
-      for (int v = 0; v < 3; v++) {
-        if (t.zs32[v] > 0.0 && t.zs32[v] < best32) { best32 = t.zs32[v]; L.zslab32 = kTuneSlabs[v]; }
-        if (t.zs64[v] > 0.0 && t.zs64[v] < best64) { best64 = t.zs64[v]; L.zslab64 = kTuneSlabs[v]; }
-      }
     };
     {
       std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -593,27 +578,6 @@ static int autotune_sweeps(cvb_ctx *ctx) {
       t.zt32[v] = 1e3 * ms / reps;
     }
     if (tma_timeout_take(ctx->stream) != 0) return fail(ctx, CVB_TIMEOUT, "a TMA-staged half-sweep gave up waiting");
-    // the zebra sweep in plane slabs, each slab count
-    for (int prec = 0; prec < 2; prec++)
-      for (int v = 0; v < 3; v++) {
-        double *zs = prec == 0 ? t.zs32 : t.zs64;
-        zs[v] = 0.0;
-        const int slabs = kTuneSlabs[v];
-        if (prec == 0 ? !zebra_slabs_ok<float>(L, slabs) : !zebra_slabs_ok<double>(L, slabs)) continue;
-        if (2 * slabs + 3 > L.g.mz) continue;  // slabs of at least two planes
-        const int reps = 5;
-        for (int q = 0; q <= reps; q++) {
-          if (q == 1) CK(cudaEventRecord(ctx->ev0, ctx->stream));
-          if (prec == 0) launch_zebra_sweep_slabs<float>(L, L.r32, L.e32, 1.3f, slabs, ctx->stream);
-          else launch_zebra_sweep_slabs<double>(L, L.r64, L.e64, 1.3, slabs, ctx->stream);
-        }
-        CK(cudaEventRecord(ctx->ev1, ctx->stream));
-        CK(cudaEventSynchronize(ctx->ev1));
-        CKL();
-        float ms = 0;
-        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-        zs[v] = 1e3 * ms / reps;
-      }
     pick(t);
     ctx->tune.push_back(t);
     std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -1982,32 +1946,6 @@ int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega
   return CVB_OK;
 }
 
-int cvb_zebra_sweep_slabs(cvb_ctx *ctx, int level, int precision, int slabs, double omega, const void *b, void *x) {
-  TRY(level_ok(ctx, level));
-  LevelDev &L = ctx->L[level];
-  const bool f32 = precision == CVB_PRECISION_MIXED;
-  if (!f32 && precision != CVB_PRECISION_FP64) return fail(ctx, CVB_BAD_INPUT, "precision %d unknown", precision);
-  if (!b || !x) return fail(ctx, CVB_BAD_INPUT, "null array");
-  if (f32 ? !zebra_slabs_ok<float>(L, slabs) : !zebra_slabs_ok<double>(L, slabs))
-    return fail(ctx, CVB_BAD_INPUT, "the sweep in %d plane slabs cannot run on level %d", slabs, level);
-  const size_t n = L.g.n(), es = f32 ? sizeof(float) : sizeof(double);
-  void *db = f32 ? (void *)L.r32 : (void *)L.r64, *dx = f32 ? (void *)L.e32 : (void *)L.e64;
-  int rc = CVB_OK;
-  if (cudaMemcpyAsync(db, b, es * n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
-      cudaMemcpyAsync(dx, x, es * n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
-    rc = CVB_CUDA_ERROR;
-  if (rc == CVB_OK) {
-    if (f32) launch_zebra_sweep_slabs<float>(L, L.r32, L.e32, (float)omega, slabs, ctx->stream);
-    else launch_zebra_sweep_slabs<double>(L, L.r64, L.e64, omega, slabs, ctx->stream);
-    if (cudaGetLastError() != cudaSuccess ||
-        cudaMemcpyAsync(x, dx, es * n, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
-        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
-      rc = CVB_CUDA_ERROR;
-  }
-  if (rc != CVB_OK) return fail(ctx, rc, "zebra sweep in slabs failed");
-  return CVB_OK;
-}
-
 int cvb_set_device_limit(cvb_ctx *ctx, unsigned long long bytes) {
   if (!ctx) return CVB_BAD_INPUT;
   ctx->device_limit = (size_t)bytes;
@@ -2101,22 +2039,17 @@ int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
     char row[768];
     const LevelDev &L = ctx->L[t.level];
     char z32[16];
-    if (L.zslab32) snprintf(z32, sizeof z32, "slabs%d", L.zslab32);
-    else if (L.ztma32) snprintf(z32, sizeof z32, "tma%d", L.ztma32);
+    if (L.ztma32) snprintf(z32, sizeof z32, "tma%d", L.ztma32);
     else snprintf(z32, sizeof z32, "%s", L.zfuse32 ? "fused" : "split");
-    char z64[16];
-    if (L.zslab64) snprintf(z64, sizeof z64, "slabs%d", L.zslab64);
-    else snprintf(z64, sizeof z64, "%s", L.zfuse64 ? "fused" : "split");
     snprintf(row, sizeof row,
              "%s{\"level\": %d, \"cells\": %zu, \"f32\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
              "\"f64\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
              "\"zebra_f32\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"tma4_us\": %.2f, \"tma8_us\": %.2f, "
-             "\"tma16_us\": %.2f, \"slabs2_us\": %.2f, \"slabs4_us\": %.2f, \"slabs8_us\": %.2f, \"choice\": \"%s\"}, "
-             "\"zebra_f64\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"slabs2_us\": %.2f, \"slabs4_us\": %.2f, "
-             "\"slabs8_us\": %.2f, \"choice\": \"%s\"}}",
+             "\"tma16_us\": %.2f, \"choice\": \"%s\"}, "
+             "\"zebra_f64\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"choice\": \"%s\"}}",
              q ? ", " : "", t.level, t.cells, t.us32[0], t.us32[1], L.sweep32 ? "split" : "fused", t.us64[0],
-             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], t.zt32[0], t.zt32[1], t.zt32[2],
-             t.zs32[0], t.zs32[1], t.zs32[2], z32, t.zb64[0], t.zb64[1], t.zs64[0], t.zs64[1], t.zs64[2], z64);
+             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], t.zt32[0], t.zt32[1], t.zt32[2], z32,
+             t.zb64[0], t.zb64[1], L.zfuse64 ? "fused" : "split");
     o += row;
   }
   o += "]}";
@@ -2173,13 +2106,7 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
   LevelDev &L = ctx->L[level];
   size_t n = L.g.n();
   double per_cell;
-  // a level whose zebra sweeps run in plane slabs times a whole sweep in that
-  // form and reports half of it (the two colours' half-sweeps move the same bytes)
-  const bool slab32 = kernel == CVB_KERNEL_ZEBRA_F32 && L.zslab32 > 1 && zebra_slabs_ok<float>(L, L.zslab32);
-  const bool slab64 = kernel == CVB_KERNEL_ZEBRA_F64 && L.zslab64 > 1 && zebra_slabs_ok<double>(L, L.zslab64);
   auto launch = [&]() {
-    if (slab32) { launch_zebra_sweep_slabs<float>(L, L.r32, L.e32, 1.3f, L.zslab32, ctx->stream); return; }
-    if (slab64) { launch_zebra_sweep_slabs<double>(L, L.r64, L.e64, 1.3, L.zslab64, ctx->stream); return; }
     switch (kernel) {
       case CVB_KERNEL_LINE_SWEEP_F32: launch_line_smooth<float>(L, L.r32, L.e32, L.t32 + n, 0.85f, 0, ctx->stream); break;
       case CVB_KERNEL_LINE_SWEEP_F64: launch_line_smooth<double>(L, L.r64, L.e64, L.t64 + n, 0.85, 0, ctx->stream); break;
@@ -2289,7 +2216,7 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
   CKL();
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  if (avg_ms) *avg_ms = ms / reps / (slab32 || slab64 ? 2 : 1);
+  if (avg_ms) *avg_ms = ms / reps;
   if (bytes) *bytes = per_cell * (double)n;
   return CVB_OK;
 }

@@ -106,8 +106,6 @@ struct LevelDev {
                             // (in place without cross terms, else out of place)
   int ztma32;               // FP32 zebra half-sweep with TMA-staged tiles (kernels_tma.cu): the
                             // row pairs per chunk (4, 8, 16) the autotuner chose, 0 off
-  int zslab32, zslab64;     // zebra sweep in plane slabs (launch_zebra_sweep_slabs): the slab
-                            // count the autotuner chose, 0 off
   // coarsest level only: the densely inverted cells (first cm of cidx) and the
   // identity ones (the rest of cidx)
   const int *cidx;
@@ -177,14 +175,6 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
 // out-of-place one-kernel form; zero_first: x is zero on entry
 template <typename T>
 void launch_zebra_sweep(const LevelDev &L, const T *b, T *x, T *tmp, T *res, T omega, bool zero_first, cudaStream_t s);
-// one zebra sweep in place with the one-kernel form over `slabs` plane slabs,
-// colour 1 trailing colour 0 by a plane (the same result as the two
-// whole-level half-sweeps); zebra_slabs_ok: the level allows it
-constexpr int kMaxZebraSlabs = 64;
-template <typename T>
-bool zebra_slabs_ok(const LevelDev &L, int slabs);
-template <typename T>
-void launch_zebra_sweep_slabs(const LevelDev &L, const T *b, T *x, T omega, int slabs, cudaStream_t s);
 // restriction of xf into xc; zero_c, when set, is zeroed over the coarse grid too
 template <typename T>
 void launch_restrict(const LevelDev &F, const LevelDev &C, const T *xf, T *xc, cudaStream_t s, T *zero_c = nullptr);

@@ -85,14 +85,13 @@ __global__ void __launch_bounds__(kSolveThreads, kTileMinBlocks<RR>) k_line_solv
   line_solve_body<T, TW, RR>(L, r, x, xnew, omega, blockIdx.x, blockIdx.y, smem_raw, color, rsplit != 0);
 }
 
-// k0: the first plane of the launch (blockIdx.y counts planes from it)
 template <typename T, int TW, int RR, bool X>
 __global__ void __launch_bounds__(kSolveThreads, X ? 4 : kTileMinBlocks<RR>) k_zebra_fused(LevelDev L, const T *__restrict__ b, const T *xin,
-                                                                  T *xout, T omega, int color, int k0) {
+                                                                  T *xout, T omega, int color) {
   dep_sync();
   if (gated(L.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  zebra_fused_body<T, TW, RR, X>(L, b, xin, xout, omega, blockIdx.x, k0 + (int)blockIdx.y, smem_raw, color);
+  zebra_fused_body<T, TW, RR, X>(L, b, xin, xout, omega, blockIdx.x, blockIdx.y, smem_raw, color);
 }
 
 template <typename T, bool X>
@@ -241,95 +240,39 @@ void launch_line_smooth<double>(const LevelDev &L, const double *b, const double
 // line solves.  zero: x is zero on entry (the caller zeroed it); only the
 // solves run, on r = b.
 template <typename T, int TW, int RR, bool X>
-static void zebra_fused_rx(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, int k0, int nk,
-                           cudaStream_t s) {
-  dim3 grd(solve_tiles_x<TW>(L.g, color), nk);
+static void zebra_fused_rx(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
+  dim3 grd(solve_tiles_x<TW>(L.g, color), L.g.mz);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_zebra_fused<T, TW, RR, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
   launch_dep(k_zebra_fused<T, TW, RR, X>, grd, kSolveThreads, line_solve_smem_rr<T, TW>(L.g, RR), s, L, b, xin, xout, omega,
-             color, k0);
+             color);
 }
 template <typename T, int TW, int RR>
-static void zebra_fused_r(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, int k0, int nk,
-                          cudaStream_t s) {
-  if (has_cross<T>(L)) zebra_fused_rx<T, TW, RR, true>(L, b, xin, xout, omega, color, k0, nk, s);
-  else zebra_fused_rx<T, TW, RR, false>(L, b, xin, xout, omega, color, k0, nk, s);
+static void zebra_fused_r(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
+  if (has_cross<T>(L)) zebra_fused_rx<T, TW, RR, true>(L, b, xin, xout, omega, color, s);
+  else zebra_fused_rx<T, TW, RR, false>(L, b, xin, xout, omega, color, s);
 }
-// One-kernel half-sweep, xin -> xout (in place when they are equal), on the
-// planes [k0, k0 + nk) (nk < 0: every plane).
+// One-kernel half-sweep, xin -> xout (in place when they are equal).
 template <typename T>
-static void zebra_fused(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s,
-                        int k0 = 0, int nk = -1) {
+static void zebra_fused(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
   constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
-  if (nk < 0) nk = L.g.mz;
   switch (LineLayout::of(L.g.my).R) {
-    case 1: zebra_fused_r<T, TW, 1>(L, b, xin, xout, omega, color, k0, nk, s); break;
-    case 2: zebra_fused_r<T, TW, 2>(L, b, xin, xout, omega, color, k0, nk, s); break;
-    case 4: zebra_fused_r<T, TW, 4>(L, b, xin, xout, omega, color, k0, nk, s); break;
-    case 8: zebra_fused_r<T, TW, 8>(L, b, xin, xout, omega, color, k0, nk, s); break;
-    default: zebra_fused_r<T, TW, 0>(L, b, xin, xout, omega, color, k0, nk, s); break;
+    case 1: zebra_fused_r<T, TW, 1>(L, b, xin, xout, omega, color, s); break;
+    case 2: zebra_fused_r<T, TW, 2>(L, b, xin, xout, omega, color, s); break;
+    case 4: zebra_fused_r<T, TW, 4>(L, b, xin, xout, omega, color, s); break;
+    case 8: zebra_fused_r<T, TW, 8>(L, b, xin, xout, omega, color, s); break;
+    default: zebra_fused_r<T, TW, 0>(L, b, xin, xout, omega, color, s); break;
   }
-}
-// The one-kernel form fits the level (its lines' tile in shared memory).
-template <typename T>
-static bool fused_fits(const LevelDev &L) {
-  constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
-  return L.g.my <= kMaxFusedRows && line_solve_smem<T, TW>(L.g) <= kMaxSmem;
 }
 template <typename T>
 static bool fused_ok(const LevelDev &L) {
+  constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
   const bool chosen = sizeof(T) == 4 ? L.zfuse32 != 0 : L.zfuse64 != 0;
-  return chosen && fused_fits<T>(L);
+  return chosen && L.g.my <= kMaxFusedRows && line_solve_smem<T, TW>(L.g) <= kMaxSmem;
 }
-
-// One zebra sweep (colour 0, then colour 1) in place with the one-kernel form,
-// its planes taken in `slabs` slabs so that the second colour reads the slab's
-// coefficients and x while the first colour's launch has left them in L2:
-// colour 0 on slab q, then colour 1 one plane behind it, then slab q + 1.
-// Each line sees the values the two whole-level half-sweeps would give it:
-//  - colour 1 on plane p runs after colour 0 on p - 1 and p + 1 (colour 0's
-//    launches stay one plane ahead of colour 1's);
-//  - colour 0 on plane p runs before colour 1 on p - 1 and p + 1 (colour 1's
-//    launches have not reached p - 1 when colour 0's reach p).
-// With a periodic z the first and last interior planes are neighbours: colour 0
-// runs first on plane mz - 2, whose colour-1 neighbours (mz - 3 and 1) are
-// still untouched then; colour 1 on plane 1 and on mz - 2 then sees both of its
-// colour-0 neighbours done.  Needs zebra_fusable (the in-place form).
-template <typename T>
-static void zebra_sweep_slabs(const LevelDev &L, const T *b, T *x, T omega, int slabs, cudaStream_t s) {
-  const int mz = L.g.mz;
-  int top = mz - 1;  // colour 0 runs on the planes [1, top) in slabs
-  if (L.g.pz) {
-    zebra_fused<T>(L, b, x, x, omega, 0, s, mz - 2, 1);
-    top = mz - 2;
-  }
-  int lo0 = 1, lo1 = 1;
-  for (int q = 1; q <= slabs; q++) {
-    const int hi0 = q == slabs ? top : 1 + (int)((long long)(top - 1) * q / slabs);
-    const int hi1 = q == slabs ? mz - 1 : std::max(lo1, hi0 - 1);
-    if (hi0 > lo0) zebra_fused<T>(L, b, x, x, omega, 0, s, lo0, hi0 - lo0);
-    if (hi1 > lo1) zebra_fused<T>(L, b, x, x, omega, 1, s, lo1, hi1 - lo1);
-    lo0 = std::max(lo0, hi0);
-    lo1 = std::max(lo1, hi1);
-  }
-}
-
-template <typename T>
-bool zebra_slabs_ok(const LevelDev &L, int slabs) {
-  return slabs >= 1 && slabs <= kMaxZebraSlabs && zebra_fusable<T>(L) && fused_fits<T>(L) && L.g.mz >= 5;
-}
-template bool zebra_slabs_ok<float>(const LevelDev &, int);
-template bool zebra_slabs_ok<double>(const LevelDev &, int);
-
-template <typename T>
-void launch_zebra_sweep_slabs(const LevelDev &L, const T *b, T *x, T omega, int slabs, cudaStream_t s) {
-  zebra_sweep_slabs<T>(L, b, x, omega, slabs, s);
-}
-template void launch_zebra_sweep_slabs<float>(const LevelDev &, const float *, float *, float, int, cudaStream_t);
-template void launch_zebra_sweep_slabs<double>(const LevelDev &, const double *, double *, double, int, cudaStream_t);
 
 template <typename T>
 void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int color, bool zero, cudaStream_t s) {
@@ -357,11 +300,6 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
 template <typename T>
 void launch_zebra_sweep(const LevelDev &L, const T *b, T *x, T *tmp, T *res, T omega, bool zero_first,
                         cudaStream_t s) {
-  const int slabs = sizeof(T) == 4 ? L.zslab32 : L.zslab64;
-  if (!zero_first && slabs > 1 && zebra_slabs_ok<T>(L, slabs)) {
-    zebra_sweep_slabs<T>(L, b, x, omega, slabs, s);
-    return;
-  }
   if (!zero_first && fused_ok<T>(L) && !zebra_fusable<T>(L)) {
     // one-kernel half-sweeps out of place: x -> tmp -> x
     zebra_fused<T>(L, b, x, tmp, omega, 0, s);

@@ -364,18 +364,6 @@ class PoissonContext:
             raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
         return xb
 
-    def zebra_sweep_slabs(self, level, slabs, b, x, precision="mixed", omega=1.3):
-        """One zebra sweep of x (returned) in place with the one-kernel form over
-        `slabs` plane slabs: FP32 arrays for "mixed", FP64 for "fp64"."""
-        dt = np.float32 if precision == "mixed" else np.float64
-        prec = _lib.MIXED if precision == "mixed" else _lib.FP64
-        xb = np.ascontiguousarray(x, dtype=dt).copy()
-        bb = np.ascontiguousarray(b, dtype=dt)
-        rc = self._L.cvb_zebra_sweep_slabs(self._ctx, level, prec, slabs, omega, ptr(bb), ptr(xb))
-        if rc:
-            raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
-        return xb
-
     def weights(self, level):
         w = np.zeros((19,) + self.shapes[level])
         self._check(self._L.cvb_get_weights(self._ctx, level, ptr(w)))

@@ -346,17 +346,6 @@ enum {
   CVB_ZEBRA_TMA16 = 16
 };
 int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega, const float *b, float *x);
-/* One zebra sweep (colour 0, then colour 1) on a level, in place, with the
- * one-kernel half-sweep launched over `slabs` slabs of planes (1 to 64):
- * colour 0 on a slab, then colour 1 one plane behind it, then the next slab,
- * so that colour 1 reads the slab's arrays while colour 0's launch has left
- * them in L2.  The result is the one of the two whole-level half-sweeps.
- * precision CVB_PRECISION_MIXED: FP32 arrays (the V-cycle's precision there),
- * CVB_PRECISION_FP64: FP64.  b, x: host arrays of the level's box.  Levels
- * with cross-derivative terms, or periodic in x (z) with an odd mx (mz), are
- * refused (CVB_BAD_INPUT).  Part of the same smoother as PoissonSolver_MG's
- * (poisson.c:1775); the set-up autotuner picks the slab count per level. */
-int cvb_zebra_sweep_slabs(cvb_ctx *ctx, int level, int precision, int slabs, double omega, const void *b, void *x);
 /* MyRestriction (poisson.c:129) from level+1 to level; MyInterpolation
  * (poisson.c:265) from level-1 to level (returned, not added). */
 int cvb_restrict(cvb_ctx *ctx, int coarse_level, const double *xf, double *xc);
