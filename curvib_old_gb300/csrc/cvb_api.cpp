@@ -138,6 +138,7 @@ static void free_all(cvb_ctx *ctx) {
   ctx->fm.clear();
   ctx->iaj.clear(); ctx->jaj.clear(); ctx->kaj.clear(); ctx->aj64.clear();
   ctx->area3 = nullptr;
+  ctx->inv_aj = nullptr;
   ctx->cm[0] = ctx->cm[1] = ctx->cm[2] = nullptr;
   ctx->nvert_tmp = nullptr;
   ctx->Minv = nullptr;
@@ -150,6 +151,8 @@ static void free_all(cvb_ctx *ctx) {
   ctx->partial = ctx->sums = ctx->hdev = nullptr;
   ctx->uc_dev = ctx->p_dev = nullptr;
   ctx->ucat_dev = ctx->ubcs_dev = nullptr;
+  ctx->conv_dev = ctx->conv_fp = nullptr;
+  ctx->visc_dev = ctx->rct_dev = ctx->rhs_dev = ctx->uo_dev = ctx->urm_dev = nullptr;
   ctx->ibm_cent = nullptr;
   ctx->ready = false;
 }
@@ -418,6 +421,14 @@ static int build_operators(cvb_ctx *ctx) {
   for (int l = 0; l < nl; l++) {
     ctx->L[l].cross32 = hf[2 * l];
     ctx->L[l].cross64 = hf[2 * l + 1];
+  }
+  // the colour-split coefficient copies of the levels without FP32 cross terms
+  for (int l = 0; l < nl; l++) {
+    LevelDev &lv = ctx->L[l];
+    if (lv.cross32) continue;
+    if (!lv.cs32) TRY(dalloc(ctx, &lv.cs32, 5 * SplitRow::count(lv.g)));
+    launch_split_coef(lv.g, lv.gf32, lv.ajf32, lv.code, lv.cs32, ctx->stream);
+    CKL();
   }
   CK(cudaStreamSynchronize(ctx->stream));
   return CVB_OK;
@@ -871,7 +882,11 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
       // pass only when the first one cancelled most of w (||w|| dropped below
       // half of its length before orthogonalisation).  The projections and the
       // norm stay on the device between the kernels (V_{j+1} = w / ||w|| is
-      // formed there too); the host reads them back once per iteration.
+      // formed there too); the host reads them back once per iteration.  The
+      // norm of the updated w is summed from w itself: ||w||^2 - ||h||^2 would
+      // save a pass, but on a basis whose orthogonality classical Gram-Schmidt
+      // has eroded it is off by far more than rounding, and FGMRES then needed
+      // 32 iterations instead of 6 on the channel.
       double h[kMaxRestart + 2], h2[kMaxRestart + 1], nw2;
       double *dsum = ctx->sums, *dnorm = ctx->sums + kMaxRestart + 2;
       launch_multidot(ctx->dV, j + 1, ctx->w, n, ctx->partial, s, 1);
@@ -946,14 +961,14 @@ static int fgmres(cvb_ctx *ctx, const cvb_solve_opts *o, cvb_solve_stats *st) {
 static int project_rhs(cvb_ctx *ctx, double *b, double *removed) {
   int l = ctx->nlevels - 1;
   LevelDev &F = ctx->L[l];
-  launch_fluid_ratio_partial(F.g, F.code, b, ctx->aj64[l], ctx->partial, ctx->stream);
-  launch_finish_sums(ctx->partial, 3, reduce_blocks(), ctx->sums, ctx->stream);
+  launch_fluid_ratio_partial(F.g, F.code, b, ctx->inv_aj, ctx->partial, ctx->stream);
+  launch_finish_sums(ctx->partial, 2, reduce_blocks(), ctx->sums, ctx->stream);
   launch_remove_aj_mean(F.g, F.code, ctx->aj64[l], b, ctx->sums, ctx->stream);
   CKL();
-  double h[3];
-  CK(cudaMemcpyAsync(h, ctx->sums, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+  double h[2];
+  CK(cudaMemcpyAsync(h, ctx->sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  // h = {sum b/aj, fluid count, sum b^2}; the removed part is aj * mean(b/aj) on fluid cells
+  // h = {sum b/aj, fluid count}; the removed part is aj * mean(b/aj) on fluid cells
   double c = h[1] > 0 ? h[0] / h[1] : 0.0;
   *removed = c;
   return CVB_OK;
@@ -1009,6 +1024,7 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
   ctx->fm = G.fm;
   ctx->iaj = G.iaj; ctx->jaj = G.jaj; ctx->kaj = G.kaj; ctx->aj64 = G.aj64;
   ctx->area3 = G.area3;
+  ctx->inv_aj = G.inv_aj;
   for (int c = 0; c < 3; c++) ctx->cm[c] = G.cm[c];
   ctx->L.assign(nlevels, LevelDev());
   size_t nmax = 0;
@@ -1249,6 +1265,9 @@ static int upload_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv) 
       CK(cudaMemcpyAsync(G->cm[c], cv[c]->data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
+    TRY(galloc(ctx, *G, &G->inv_aj, n));
+    launch_reciprocal(G->aj64[nlevels - 1], G->inv_aj, n, ctx->stream);
+    CKL();
   }
   ctx->geo = G;
   return CVB_OK;

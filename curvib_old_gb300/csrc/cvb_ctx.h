@@ -30,6 +30,7 @@ struct Geometry {
   std::vector<double *> iaj, jaj, kaj, aj64;
   double *area3 = nullptr;                // finest: |csi|, |eta|, |zet| per cell ([3][N])
   double *cm[3] = {};                     // finest: centre metrics csi, eta, zet (Cmpnts, [N][3])
+  double *inv_aj = nullptr;               // finest: 1 / aj, for the range projection's sum of b / aj
   ~Geometry() {
     if (allocs.empty()) return;
     cudaSetDevice(device);
@@ -69,6 +70,7 @@ struct cvb_ctx {
   std::vector<double *> iaj, jaj, kaj, aj64;
   double *area3 = nullptr;       // finest: |csi|,|eta|,|zet| per cell ([3][N])
   double *cm[3] = {};            // finest: centre metrics csi, eta, zet (Cmpnts)
+  double *inv_aj = nullptr;      // finest: 1 / aj (the Geometry's)
   int *cidx = nullptr;           // coarsest level: fluid cells first, then the rest
   double *nvert_tmp = nullptr;
   // coarsest-level solver

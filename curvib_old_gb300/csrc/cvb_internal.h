@@ -94,6 +94,8 @@ struct LevelDev {
   float *ajf32;          // [N]
   float *wgt32;          // [N]    restriction weight max(0, 1 - nvert), rounded to float
   float *line32;         // y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32, LineFac layout
+  float *cs32;           // levels without FP32 cross terms: g11, g22, g33, aj and the code (its bits)
+                         // in colour-split rows ([5][SplitRow::count]), else null
   double *line64;        // ... in FP64
   // work vectors of this level (the finest level's b/x live in the solver)
   double *r64, *e64, *t64;  // FP64 V-cycle vectors
@@ -202,16 +204,22 @@ void launch_scale(double *dst, const double *src, const double *scal_dev, size_t
                   const int *gate = nullptr, float *dst32 = nullptr);
 // dst = src / sqrt(*sq_dev) (and, with dst32, its FP32 copy)
 void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s,
-                       float *dst32 = nullptr);
+                       float *dst32 = nullptr, const int *gate = nullptr);
+// cs[5][SplitRow::count] = g11, g22, g33 (gf32 slots 0, 4, 8), aj and the code's
+// bits, each cell at its colour-split position
+void launch_split_coef(const Geom &g, const float *gf32, const float *ajf32, const uint32_t *code, float *cs,
+                       cudaStream_t s);
+// out = 1 / a, element by element (correctly rounded)
+void launch_reciprocal(const double *a, double *out, size_t n, cudaStream_t s);
 void launch_axpy_z(double *x, const float *const *Z32, const double *const *Z64, const double *y_dev,
                    int nz, size_t n, cudaStream_t s);
 void launch_fluid_mean_partial(const Geom &g, const uint32_t *code, const double *x, double *partial,
                                cudaStream_t s);
 void launch_add_fluid_const(const Geom &g, const uint32_t *code, double *x, const double *sumcnt,
                             int zero_outside, cudaStream_t s);
-// range projection of a right-hand side: sums of b/aj and counts over fluid cells,
-// then b -= aj * sum/count there
-void launch_fluid_ratio_partial(const Geom &g, const uint32_t *code, const double *b, const double *aj,
+// range projection of a right-hand side: sums of b/aj (b times the stored 1/aj)
+// and counts over fluid cells, then b -= aj * sum/count there
+void launch_fluid_ratio_partial(const Geom &g, const uint32_t *code, const double *b, const double *inv_aj,
                                 double *partial, cudaStream_t s);
 void launch_remove_aj_mean(const Geom &g, const uint32_t *code, const double *aj, double *b, const double *sums,
                            cudaStream_t s);

@@ -186,8 +186,17 @@ void launch_scale(double *dst, const double *src, const double *scal_dev, size_t
   launch_dep(k_scale<false>, reduce_blocks(), 256, 0, s, dst, src, scal_dev, n, gate, dst32);
 }
 void launch_scale_sqrt(double *dst, const double *src, const double *sq_dev, size_t n, cudaStream_t s,
-                       float *dst32) {
-  launch_dep(k_scale<true>, reduce_blocks(), 256, 0, s, dst, src, sq_dev, n, (const int *)nullptr, dst32);
+                       float *dst32, const int *gate) {
+  launch_dep(k_scale<true>, reduce_blocks(), 256, 0, s, dst, src, sq_dev, n, gate, dst32);
+}
+
+__global__ void k_reciprocal(const double *__restrict__ a, double *__restrict__ out, size_t n) {
+  dep_sync();
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x)
+    out[p] = 1.0 / a[p];
+}
+void launch_reciprocal(const double *a, double *out, size_t n, cudaStream_t s) {
+  launch_dep(k_reciprocal, reduce_blocks(), 256, 0, s, a, out, n);
 }
 
 // x += sum_q y[q] Z_q (Z stored FP32 in mixed mode, FP64 in plain mode)
@@ -248,24 +257,28 @@ void launch_add_fluid_const(const Geom &g, const uint32_t *code, double *x, cons
   launch_dep(k_add_fluid_const, reduce_blocks(), 256, 0, s, g, code, x, sumcnt, zero_outside);
 }
 
+// The range projection's sums over the fluid cells: of b / aj, as b times the
+// stored 1 / aj (the FP64 pipe is this part's bound, and a division costs
+// several of its instructions), and the cell count, counted in an integer.
 __global__ void __launch_bounds__(kRedThreads) k_fluid_ratio(Geom g, const uint32_t *__restrict__ code,
-                                                             const double *__restrict__ b, const double *__restrict__ aj,
-                                                             double *partial) {
+                                                             const double *__restrict__ b,
+                                                             const double *__restrict__ inv_aj, double *partial) {
   dep_sync();
-  double acc[3] = {0.0, 0.0, 0.0};
+  double acc[2] = {0.0, 0.0};
+  unsigned cnt = 0;
   size_t n = g.n();
   for (size_t p = blockIdx.x * (size_t)kRedThreads + threadIdx.x; p < n; p += (size_t)gridDim.x * kRedThreads) {
     if (code[p] & CODE_FLUID) {
-      acc[0] += quot_newton(b[p], aj[p]);
-      acc[1] += 1.0;
+      acc[0] = fma(b[p], inv_aj[p], acc[0]);
+      cnt++;
     }
-    acc[2] = fma(b[p], b[p], acc[2]);
   }
-  block_reduce_store<3>(acc, partial, gridDim.x, 0);
+  acc[1] = (double)cnt;
+  block_reduce_store<2>(acc, partial, gridDim.x, 0);
 }
-void launch_fluid_ratio_partial(const Geom &g, const uint32_t *code, const double *b, const double *aj,
+void launch_fluid_ratio_partial(const Geom &g, const uint32_t *code, const double *b, const double *inv_aj,
                                 double *partial, cudaStream_t s) {
-  launch_dep(k_fluid_ratio, reduce_blocks(), kRedThreads, 0, s, g, code, b, aj, partial);
+  launch_dep(k_fluid_ratio, reduce_blocks(), kRedThreads, 0, s, g, code, b, inv_aj, partial);
 }
 __global__ void k_remove_aj_mean(Geom g, const uint32_t *__restrict__ code, const double *__restrict__ aj,
                                  double *__restrict__ b, const double *__restrict__ sums) {

@@ -144,6 +144,26 @@ void launch_scale_cross(const Geom &g, const uint32_t *code, float *gf32, cudaSt
   k_scale_cross<<<nblk(g.n(), 256) < 4096 ? nblk(g.n(), 256) : 4096, 256, 0, s>>>(g, code, gf32); count_launch();
 }
 
+// The colour-split copies of a level's 7-point coefficients (row32_split).
+__global__ void k_split_coef(Geom g, const float *__restrict__ gf, const float *__restrict__ aj,
+                             const uint32_t *__restrict__ code, float *__restrict__ cs) {
+  const size_t n = g.n(), S = SplitRow::count(g);
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p % g.mx), j = (int)((p / g.mx) % g.my), k = (int)(p / ((size_t)g.mx * g.my));
+    const size_t q = SplitRow::at(g, i, j, k);
+    cs[q] = gf[p];
+    cs[S + q] = gf[4 * n + p];
+    cs[2 * S + q] = gf[8 * n + p];
+    cs[3 * S + q] = aj[p];
+    cs[4 * S + q] = __uint_as_float(code[p]);
+  }
+}
+void launch_split_coef(const Geom &g, const float *gf32, const float *ajf32, const uint32_t *code, float *cs,
+                       cudaStream_t s) {
+  k_split_coef<<<nblk(g.n(), 256) < 4096 ? nblk(g.n(), 256) : 4096, 256, 0, s>>>(g, gf32, ajf32, code, cs);
+  count_launch();
+}
+
 // One cross term into vol[] in the reference's order (see add_cross in the oracle).
 __device__ __forceinline__ void add_cross(double *vol, int br, double gg, bool up, int P, int Q, int Pu,
                                           int Qu, int Pd, int Qd) {

@@ -151,6 +151,31 @@ __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ 
   return (c & CODE_IDENTITY) ? s.P : -ajp * acc;
 }
 
+// (A x)_p without cross terms from the colour-split copies of the coefficients
+// (L.cs32): the cells of one zebra colour sit side by side there, so a
+// half-sweep, which needs the coefficients of one colour's cells, reads whole
+// sectors of them instead of every other value.  The same operands, flux form
+// and order as row32<TX, false>; the W, S and B faces are the E, N and T faces
+// of the neighbours i - 1, j - 1, k - 1 (never wrapped).
+__device__ __forceinline__ float row32_split(const Geom &g, const float *__restrict__ cs,
+                                             const float *__restrict__ x, int i, int j, int k, int p) {
+  if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return x[p];
+  const size_t S = SplitRow::count(g);
+  const int q = SplitRow::at(g, i, j, k), qw = SplitRow::at(g, i - 1, j, k), qs = SplitRow::at(g, i, j - 1, k),
+            qb = SplitRow::at(g, i, j, k - 1);
+  const Off o = offsets(g, i, j, k);
+  const uint32_t c = __float_as_uint(__ldg(cs + 4 * S + q));
+  const float P = x[p], E = x[p + o.e], W = x[p + o.w], N = x[p + o.n], Sv = x[p + o.s], T = x[p + o.t],
+              B = x[p + o.b];
+  const float g11 = __ldg(cs + q), w11 = __ldg(cs + qw), g22 = __ldg(cs + S + q), s22 = __ldg(cs + S + qs);
+  const float g33 = __ldg(cs + 2 * S + q), b33 = __ldg(cs + 2 * S + qb), ajp = __ldg(cs + 3 * S + q);
+  const float fe = g11 * (E - P), fw = w11 * (P - W), fn = g22 * (N - P);
+  const float fs = s22 * (P - Sv), ft = g33 * (T - P), fb = b33 * (P - B);
+  const float acc = act(c, CODE_ACT_E) * fe - act(c, CODE_ACT_W) * fw + act(c, CODE_ACT_N) * fn -
+                    act(c, CODE_ACT_S) * fs + act(c, CODE_ACT_T) * ft - act(c, CODE_ACT_B) * fb;
+  return (c & CODE_IDENTITY) ? P : -ajp * acc;
+}
+
 // ------------------------------------------------------- apply / residual
 // y = A x (b == nullptr) or y = b - A x.  One thread per cell.
 // Bodies take the block's coordinates explicitly so that the grouped (batched)
@@ -891,6 +916,9 @@ template <>
 struct ColorRow<float> {
   template <bool X>
   __device__ static float r(const Geom &g, const LevelDev &L, const float *x, int i, int j, int k, int p, int n) {
+    if constexpr (!X) {
+      if (L.cs32) return row32_split(g, L.cs32, x, i, j, k, p);
+    }
     return row32<float, X>(g, L.gf32, L.ajf32, L.code, x, i, j, k, p, n);
   }
 };

@@ -144,6 +144,20 @@ def test_channel256x128x128_5lev_solve_vs_oracle(channel):
     _check_solves(ctx, P, Ls, b, x_ref, [fluid_mask(Ls[-1].nvert)])
 
 
+@pytest.mark.parametrize("name,rtol,budget", [("channel", 1e-10, 8), ("box64", 1e-8, 10)])
+def test_iteration_counts(request, name, rtol, budget):
+    """The measured configurations' FGMRES iteration counts at the bench's
+    tolerances (channel 6 at 1e-10, box 8 at 1e-8 on the GB300, in both
+    precisions) guard the Krylov loop's numerics: a change that still reaches
+    the right answer but erodes the basis (a norm taken from ||w||^2 - ||h||^2,
+    say) shows up here as many more iterations."""
+    ctx, P, Ls = request.getfixturevalue(name)
+    b = _rhs(P, Ls, seed=0, noise=name == "box64")
+    for precision in (0, 1):
+        _, st = ctx.solve(b, precision=precision, rtol=rtol, max_it=400)
+        assert st["status"] == 0 and st["iterations"] <= budget, (name, precision, st)
+
+
 def test_box_classes_batched_vs_oracle():
     from curvib_old_gb300 import workload as W
     from curvib_old_gb300.solver import PoissonContext, SolveBatch
