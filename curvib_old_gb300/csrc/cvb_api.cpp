@@ -423,9 +423,14 @@ static int build_operators(cvb_ctx *ctx) {
     ctx->L[l].cross64 = hf[2 * l + 1];
   }
   // the colour-split coefficient copies of the levels without FP32 cross terms
+  // (dropped where a rebuild gave the level cross terms)
   for (int l = 0; l < nl; l++) {
     LevelDev &lv = ctx->L[l];
-    if (lv.cross32) continue;
+    if (lv.cross32) {
+      if (lv.cs32) dfree(ctx, lv.cs32);
+      lv.cs32 = nullptr;
+      continue;
+    }
     if (!lv.cs32) TRY(dalloc(ctx, &lv.cs32, 5 * SplitRow::count(lv.g)));
     launch_split_coef(lv.g, lv.gf32, lv.ajf32, lv.code, lv.cs32, ctx->stream);
     CKL();

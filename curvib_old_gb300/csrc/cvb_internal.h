@@ -95,7 +95,7 @@ struct LevelDev {
   float *wgt32;          // [N]    restriction weight max(0, 1 - nvert), rounded to float
   float *line32;         // y-line Thomas factors (a_j, 1/m_j, c'_j) in FP32, LineFac layout
   float *cs32;           // levels without FP32 cross terms: g11, g22, g33, aj and the code (its bits)
-                         // in colour-split rows ([5][SplitRow::count]), else null
+                         // in colour-split rows ([5][SplitRow::count]) for the zebra residual; else null
   double *line64;        // ... in FP64
   // work vectors of this level (the finest level's b/x live in the solver)
   double *r64, *e64, *t64;  // FP64 V-cycle vectors

@@ -152,17 +152,26 @@ __device__ __forceinline__ float row32(const Geom &g, const float *__restrict__ 
 }
 
 // (A x)_p without cross terms from the colour-split copies of the coefficients
-// (L.cs32): the cells of one zebra colour sit side by side there, so a
-// half-sweep, which needs the coefficients of one colour's cells, reads whole
-// sectors of them instead of every other value.  The same operands, flux form
-// and order as row32<TX, false>; the W, S and B faces are the E, N and T faces
-// of the neighbours i - 1, j - 1, k - 1 (never wrapped).
+// (L.cs32: g11, g22, g33, aj and the code's bits, SplitRow::count values each):
+// the cells of one zebra colour sit side by side there, so a half-sweep, which
+// needs the coefficients of one colour's cells, reads whole sectors of them
+// instead of every other value.  The same operands, flux form and order as
+// row32<TX, false>; the W, S and B faces are the E, N and T faces of the
+// neighbours i - 1, j - 1, k - 1 (never wrapped).  Interior cells only (the
+// zebra kernels' cells): their split positions follow from the cell's own, q,
+// with the row of the other colour h away -- i - 1 and k - 1 are of the other
+// colour, j - 1 of the same.  (The same copies of the nine 19-point
+// coefficients made that residual slower on the GB300, 119 against 115 us per
+// half-sweep at 192^3: there the W, S and B neighbours' reads share cache lines
+// with the other cells' own in the caller's layout, and the kernel is bound by
+// its instructions more than by DRAM.)
 __device__ __forceinline__ float row32_split(const Geom &g, const float *__restrict__ cs,
                                              const float *__restrict__ x, int i, int j, int k, int p) {
-  if (i < 1 || i > g.mx - 2 || j < 1 || j > g.my - 2 || k < 1 || k > g.mz - 2) return x[p];
-  const size_t S = SplitRow::count(g);
-  const int q = SplitRow::at(g, i, j, k), qw = SplitRow::at(g, i - 1, j, k), qs = SplitRow::at(g, i, j - 1, k),
-            qb = SplitRow::at(g, i, j, k - 1);
+  const int h = SplitRow::half(g), c2 = (i + k) & 1;
+  const size_t S = (size_t)g.my * g.mz * 2 * h;
+  const int q = ((k * g.my + j) * 2 + c2) * h + (i >> 1);
+  const int other = c2 ? -h : h;  // own colour's row -> the other colour's
+  const int qw = q + other + ((i - 1) >> 1) - (i >> 1), qs = q - 2 * h, qb = q - g.my * 2 * h + other;
   const Off o = offsets(g, i, j, k);
   const uint32_t c = __float_as_uint(__ldg(cs + 4 * S + q));
   const float P = x[p], E = x[p + o.e], W = x[p + o.w], N = x[p + o.n], Sv = x[p + o.s], T = x[p + o.t],
@@ -941,7 +950,11 @@ __device__ __forceinline__ void resid_color_body(const LevelDev &L, const T *__r
   const int nci = first <= g.mx - 2 ? (g.mx - 2 - first) / 2 + 1 : 0;
   const int idx = bx * kFlat + threadIdx.x;
   if (idx >= nci * (g.my - 2)) return;
-  const int jj = idx / nci, i = first + 2 * (idx - jj * nci), j = 1 + jj;
+  // idx / nci from a float reciprocal, corrected to the exact quotient
+  int jj = (int)(((float)idx + 0.5f) * __frcp_rn((float)nci));
+  jj -= jj * nci > idx;
+  jj += (jj + 1) * nci <= idx;
+  const int i = first + 2 * (idx - jj * nci), j = 1 + jj;
   const int n = (int)g.n(), p = (k * g.my + j) * g.mx + i;
   r[SplitRow::at(g, i, j, k)] = b[p] - ColorRow<T>::template r<X>(g, L, x, i, j, k, p, n);
 }
