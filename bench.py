@@ -342,6 +342,8 @@ def roofline(ctx, orthogonal):
     note = ("; the grid is orthogonal, so the cross-derivative terms are exactly zero and are skipped" if orthogonal
             else "; the grid is distorted, so all 19 points are read")
     tag = "" if orthogonal else "_x"
+    forms["fused4"] = forms["fused"].replace(",8,R,", ",4,R,") + ", 4 lines per block"
+    forms["split4"] = forms["split"].replace("<float,8,R>", "<float,4,R>") + ", 4 lines per block"
     if zebra_form.startswith("tma"):
         forms[zebra_form] = (f"k_zebra_tma<{zebra_form[3:]},R> (one kernel: that color's {pts} residual from tiles "
                              f"staged by TMA bulk tensor copies, {zebra_form[3:]} row pairs per chunk, then its "

@@ -459,7 +459,7 @@ bool g_tune_loaded = false;
 
 // With CVB_TUNE_FILE set, measured choices persist in that text file (one
 // shape per line: mx my mz px py pz, the two cross-term flags and the
-// eleven timings in microseconds), so a
+// thirteen timings in microseconds), so a
 // later process -- a profiler run, say, whose own timings would be distorted --
 // makes the same choices.  Called with g_tune_mu held.
 void tune_file_load() {
@@ -471,9 +471,10 @@ void tune_file_load() {
   if (!f) return;
   ShapeKey k;
   cvb_ctx::Tune t;
-  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf", &k.mx, &k.my, &k.mz,
-                     &k.px, &k.py, &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0], &t.us64[1], &t.zb32[0],
-                     &t.zb32[1], &t.zb64[0], &t.zb64[1], &t.zt32[0], &t.zt32[1], &t.zt32[2]) == 19) {
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf %lf", &k.mx, &k.my,
+                     &k.mz, &k.px, &k.py, &k.pz, &k.c32, &k.c64, &t.us32[0], &t.us32[1], &t.us64[0], &t.us64[1],
+                     &t.zb32[0], &t.zb32[1], &t.zb64[0], &t.zb64[1], &t.zt32[0], &t.zt32[1], &t.zt32[2], &t.zw32[0],
+                     &t.zw32[1]) == 21) {
     t.level = 0;
     t.cells = (size_t)k.mx * k.my * k.mz;
     g_tune_cache.emplace(k, t);
@@ -485,9 +486,9 @@ void tune_file_append(const ShapeKey &k, const cvb_ctx::Tune &t) {
   if (!path || !*path) return;
   FILE *f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", k.mx, k.my, k.mz,
-               k.px, k.py, k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0], t.zb32[1],
-               t.zb64[0], t.zb64[1], t.zt32[0], t.zt32[1], t.zt32[2]);
+  std::fprintf(f, "%d %d %d %d %d %d %d %d %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", k.mx,
+               k.my, k.mz, k.px, k.py, k.pz, k.c32, k.c64, t.us32[0], t.us32[1], t.us64[0], t.us64[1], t.zb32[0],
+               t.zb32[1], t.zb64[0], t.zb64[1], t.zt32[0], t.zt32[1], t.zt32[2], t.zw32[0], t.zw32[1]);
   std::fclose(f);
 }
 }  // namespace
@@ -506,9 +507,20 @@ static int autotune_sweeps(cvb_ctx *ctx) {
       // two-kernel form, so the choice does not flip with timing noise
       L.zfuse32 = t.zb32[1] > 0.0 && t.zb32[1] < 0.97 * t.zb32[0] ? 1 : 0;
       L.zfuse64 = t.zb64[1] > 0.0 && t.zb64[1] < 0.97 * t.zb64[0] ? 1 : 0;
+      // the FP32 forms with 4 lines per tile instead of 8, same rule
+      L.ztw32 = 0;
+      {
+        double cur = L.zfuse32 ? t.zb32[1] : t.zb32[0];
+        for (int v = 0; v < 2; v++)
+          if (t.zw32[v] > 0.0 && t.zw32[v] < 0.97 * cur) {
+            cur = t.zw32[v];
+            L.ztw32 = 4;
+            L.zfuse32 = v;
+          }
+      }
       // the TMA-staged FP32 half-sweep and its chunk of row pairs, on the same
       // 3 % rule against the better of the other two forms
-      const double other = L.zfuse32 ? t.zb32[1] : t.zb32[0];
+      const double other = L.ztw32 ? t.zw32[L.zfuse32] : L.zfuse32 ? t.zb32[1] : t.zb32[0];
       L.ztma32 = 0;
       double best = 0.97 * other;
       const int rps[3] = {4, 8, 16};
@@ -570,6 +582,24 @@ static int autotune_sweeps(cvb_ctx *ctx) {
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         zb[v] = 1e3 * ms / reps;
       }
+    // the FP32 zebra sweep's two forms with 4 lines per tile
+    L.ztw32 = 4;
+    for (int v = 0; v < 2; v++) {
+      t.zw32[v] = 0.0;
+      L.zfuse32 = v;
+      const int reps = 5;
+      for (int q = 0; q <= reps; q++) {
+        if (q == 1) CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        launch_zebra_sweep<float>(L, L.r32, L.e32, L.t32, L.t32 + n, 1.3f, false, ctx->stream);
+      }
+      CK(cudaEventRecord(ctx->ev1, ctx->stream));
+      CK(cudaEventSynchronize(ctx->ev1));
+      CKL();
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      t.zw32[v] = 1e3 * ms / reps;
+    }
+    L.ztw32 = 0;
     // the FP32 zebra sweep with TMA-staged tiles, each chunk size
     for (int v = 0; v < 3; v++) {
       t.zt32[v] = 0.0;
@@ -1935,19 +1965,23 @@ int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega
   TRY(level_ok(ctx, level));
   LevelDev &L = ctx->L[level];
   if (color != 0 && color != 1) return fail(ctx, CVB_BAD_INPUT, "colour %d is not 0 or 1", color);
-  const int keep_tma = L.ztma32, keep_fuse = L.zfuse32;
+  const int keep_tma = L.ztma32, keep_fuse = L.zfuse32, keep_tw = L.ztw32;
+  L.ztw32 = 0;
   switch (form) {
     case CVB_ZEBRA_SPLIT: L.ztma32 = 0; L.zfuse32 = 0; break;
     case CVB_ZEBRA_FUSED: L.ztma32 = 0; L.zfuse32 = 1; break;
+    case CVB_ZEBRA_SPLIT4: L.ztma32 = 0; L.zfuse32 = 0; L.ztw32 = 4; break;
+    case CVB_ZEBRA_FUSED4: L.ztma32 = 0; L.zfuse32 = 1; L.ztw32 = 4; break;
     case CVB_ZEBRA_TMA4: case CVB_ZEBRA_TMA8: case CVB_ZEBRA_TMA16: L.ztma32 = form; L.zfuse32 = 0; break;
     default: return fail(ctx, CVB_BAD_INPUT, "unknown zebra form %d", form);
   }
-  const bool ok = form == CVB_ZEBRA_SPLIT ? true
-                  : form == CVB_ZEBRA_FUSED ? zebra_fusable<float>(L)
-                                           : zebra_tma_ok(L);
+  const bool ok = form == CVB_ZEBRA_SPLIT || form == CVB_ZEBRA_SPLIT4 ? true
+                  : form == CVB_ZEBRA_FUSED || form == CVB_ZEBRA_FUSED4 ? zebra_fusable<float>(L)
+                                                                        : zebra_tma_ok(L);
   if (!ok) {
     L.ztma32 = keep_tma;
     L.zfuse32 = keep_fuse;
+    L.ztw32 = keep_tw;
     return fail(ctx, CVB_BAD_INPUT, "zebra form %d cannot run on level %d", form, level);
   }
   const size_t n = L.g.n();
@@ -1964,6 +1998,7 @@ int cvb_zebra_half_f32(cvb_ctx *ctx, int level, int form, int color, float omega
   }
   L.ztma32 = keep_tma;
   L.zfuse32 = keep_fuse;
+  L.ztw32 = keep_tw;
   if (rc != CVB_OK) return fail(ctx, rc, "zebra half-sweep failed");
   if (form >= CVB_ZEBRA_TMA4 && tma_timeout_take(ctx->stream) != 0)
     return fail(ctx, CVB_TIMEOUT, "a TMA-staged half-sweep gave up waiting for its tiles");
@@ -2064,15 +2099,16 @@ int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len) {
     const LevelDev &L = ctx->L[t.level];
     char z32[16];
     if (L.ztma32) snprintf(z32, sizeof z32, "tma%d", L.ztma32);
-    else snprintf(z32, sizeof z32, "%s", L.zfuse32 ? "fused" : "split");
+    else snprintf(z32, sizeof z32, "%s%s", L.zfuse32 ? "fused" : "split", L.ztw32 == 4 ? "4" : "");
     snprintf(row, sizeof row,
              "%s{\"level\": %d, \"cells\": %zu, \"f32\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
              "\"f64\": {\"fused_us\": %.2f, \"split_us\": %.2f, \"choice\": \"%s\"}, "
-             "\"zebra_f32\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"tma4_us\": %.2f, \"tma8_us\": %.2f, "
-             "\"tma16_us\": %.2f, \"choice\": \"%s\"}, "
+             "\"zebra_f32\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"split4_us\": %.2f, \"fused4_us\": %.2f, "
+             "\"tma4_us\": %.2f, \"tma8_us\": %.2f, \"tma16_us\": %.2f, \"choice\": \"%s\"}, "
              "\"zebra_f64\": {\"split_us\": %.2f, \"fused_us\": %.2f, \"choice\": \"%s\"}}",
              q ? ", " : "", t.level, t.cells, t.us32[0], t.us32[1], L.sweep32 ? "split" : "fused", t.us64[0],
-             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], t.zt32[0], t.zt32[1], t.zt32[2], z32,
+             t.us64[1], L.sweep64 ? "split" : "fused", t.zb32[0], t.zb32[1], t.zw32[0], t.zw32[1], t.zt32[0],
+             t.zt32[1], t.zt32[2], z32,
              t.zb64[0], t.zb64[1], L.zfuse64 ? "fused" : "split");
     o += row;
   }

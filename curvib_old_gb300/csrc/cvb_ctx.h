@@ -104,7 +104,7 @@ struct cvb_ctx {
   // measured sweep times (us): line sweeps fused / split, zebra sweeps two-kernel /
   // one-kernel, and the FP32 zebra sweep with TMA-staged tiles of 4, 8, 16 row
   // pairs (0: not run on this level)
-  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2], zt32[3]; };
+  struct Tune { int level; size_t cells; double us32[2], us64[2], zb32[2], zb64[2], zt32[3], zw32[2]; };
   std::vector<Tune> tune;
 };
 

@@ -108,6 +108,7 @@ struct LevelDev {
                             // (in place without cross terms, else out of place)
   int ztma32;               // FP32 zebra half-sweep with TMA-staged tiles (kernels_tma.cu): the
                             // row pairs per chunk (4, 8, 16) the autotuner chose, 0 off
+  int ztw32;                // lines per block of the FP32 zebra line-solve tiles (4 or 8; 0: 8)
   // coarsest level only: the densely inverted cells (first cm of cidx) and the
   // identity ones (the rest of cidx)
   const int *cidx;

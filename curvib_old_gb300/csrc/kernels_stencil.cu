@@ -255,10 +255,11 @@ static void zebra_fused_r(const LevelDev &L, const T *b, const T *xin, T *xout, 
   if (has_cross<T>(L)) zebra_fused_rx<T, TW, RR, true>(L, b, xin, xout, omega, color, s);
   else zebra_fused_rx<T, TW, RR, false>(L, b, xin, xout, omega, color, s);
 }
-// One-kernel half-sweep, xin -> xout (in place when they are equal).
-template <typename T>
-static void zebra_fused(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
-  constexpr int TW = sizeof(T) == 4 ? kSolveTW32 : kSolveTW64;
+// One-kernel half-sweep, xin -> xout (in place when they are equal), TW lines
+// per block.
+template <typename T, int TW>
+static void zebra_fused_tw(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color,
+                           cudaStream_t s) {
   switch (LineLayout::of(L.g.my).R) {
     case 1: zebra_fused_r<T, TW, 1>(L, b, xin, xout, omega, color, s); break;
     case 2: zebra_fused_r<T, TW, 2>(L, b, xin, xout, omega, color, s); break;
@@ -266,6 +267,12 @@ static void zebra_fused(const LevelDev &L, const T *b, const T *xin, T *xout, T 
     case 8: zebra_fused_r<T, TW, 8>(L, b, xin, xout, omega, color, s); break;
     default: zebra_fused_r<T, TW, 0>(L, b, xin, xout, omega, color, s); break;
   }
+}
+// The tile width the level's set-up chose: FP32 4 or 8 lines per block, FP64 4.
+template <typename T>
+static void zebra_fused(const LevelDev &L, const T *b, const T *xin, T *xout, T omega, int color, cudaStream_t s) {
+  if (sizeof(T) == 4 && L.ztw32 == 4) zebra_fused_tw<T, 4>(L, b, xin, xout, omega, color, s);
+  else zebra_fused_tw<T, sizeof(T) == 4 ? kSolveTW32 : kSolveTW64>(L, b, xin, xout, omega, color, s);
 }
 template <typename T>
 static bool fused_ok(const LevelDev &L) {
@@ -294,7 +301,8 @@ void launch_zebra_half(const LevelDev &L, const T *b, T *x, T *res, T omega, int
     else launch_dep(k_resid_color<T, false>, grd, kFlat, 0, s, L, x, b, res, color);
     r = res;
   }
-  line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);
+  if (sizeof(T) == 4 && L.ztw32 == 4) line_solve<T, 4>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);
+  else line_solve<T, TW>(L, r, zero ? nullptr : x, x, omega, s, color, zero ? 0 : 1);
 }
 
 template <typename T>

@@ -353,7 +353,7 @@ class PoissonContext:
         self._check(self._L.cvb_level_cross(self._ctx, level, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
-    ZEBRA_FORMS = {"split": 0, "fused": 1, "tma4": 4, "tma8": 8, "tma16": 16}
+    ZEBRA_FORMS = {"split": 0, "fused": 1, "split4": 2, "fused4": 3, "tma4": 4, "tma8": 8, "tma16": 16}
 
     def zebra_half_f32(self, level, form, color, b, x, omega=1.3):
         """One FP32 zebra half-sweep of x (returned) in the named form."""

@@ -341,6 +341,8 @@ int cvb_level_cross(const cvb_ctx *ctx, int level, int *cross32, int *cross64);
 enum {
   CVB_ZEBRA_SPLIT = 0,
   CVB_ZEBRA_FUSED = 1,
+  CVB_ZEBRA_SPLIT4 = 2, /* the two forms above with 4 lines per line-solve tile instead of 8 */
+  CVB_ZEBRA_FUSED4 = 3,
   CVB_ZEBRA_TMA4 = 4,
   CVB_ZEBRA_TMA8 = 8,
   CVB_ZEBRA_TMA16 = 16

@@ -2,10 +2,11 @@
 
 The mixed V-cycle's smoother relaxes the y-lines of one colour per half-sweep.
 The set-up autotuner chooses per level between two kernels (residual, then
-line solves), one kernel (residual straight into shared memory), and one
-kernel whose tiles are staged by TMA bulk tensor copies in chunks of 4, 8 or
-16 row pairs (cvb_zebra_half_f32 runs a named form).  On levels without
-cross-derivative terms all five must give the same x: checked here against the
+line solves), one kernel (residual straight into shared memory), either with 8
+or with 4 lines per tile, and one kernel whose tiles are staged by TMA bulk
+tensor copies in chunks of 4, 8 or 16 row pairs (cvb_zebra_half_f32 runs a
+named form).  On levels without cross-derivative terms all seven must give the
+same x: checked here against the
 two-kernel form, within 1e-5 of the size of the update (FP32 sums whose
 multiply-adds the compiler may contract differently per kernel), on a periodic
 channel (mx = 2 mod 4), a walled box (mx = 0 mod 4) and the finest level of
@@ -18,7 +19,7 @@ from curvib_old_gb300._lib import CVB_BAD_INPUT, CvbError
 
 pytestmark = pytest.mark.gpu
 
-FORMS = ["fused", "tma4", "tma8", "tma16"]
+FORMS = ["fused", "split4", "fused4", "tma4", "tma8", "tma16"]
 
 
 def _problems():
