@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256, 3) k_line_sweep(LevelDev L, const T *__re
 
 // RR: the line layout's rows per lane fixed at compile time (0: read from my)
 template <typename T, int TW, int RR>
-__global__ void __launch_bounds__(kSolveThreads, kTileMinBlocks<RR>) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
+__global__ void __launch_bounds__(kSolveThreads, kTileMinBlocks<T, TW, RR>) k_line_solve(LevelDev L, const T *__restrict__ r, const T *x,
                                                                  T *xnew, T omega, int color, int rsplit) {
   dep_sync();
   if (gated(L.gate)) return;
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kSolveThreads, kTileMinBlocks<RR>) k_line_solv
 }
 
 template <typename T, int TW, int RR, bool X>
-__global__ void __launch_bounds__(kSolveThreads, X ? 4 : kTileMinBlocks<RR>) k_zebra_fused(LevelDev L, const T *__restrict__ b, const T *xin,
+__global__ void __launch_bounds__(kSolveThreads, X ? 4 : kTileMinBlocks<T, TW, RR>) k_zebra_fused(LevelDev L, const T *__restrict__ b, const T *xin,
                                                                   T *xout, T omega, int color) {
   dep_sync();
   if (gated(L.gate)) return;

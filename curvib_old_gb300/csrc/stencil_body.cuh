@@ -707,26 +707,36 @@ struct Vec16<double> {
 // line's runs (a, 1/m, c'), aligned to R values since runs hold a multiple of 4
 // values and start 16-byte aligned.  Saves the factors' trip through shared
 // memory (a store and two to four loads per value).
-template <int RR>
-constexpr bool kRegFactors = RR >= 1 && RR <= 4;
+// Also for R = 8 in FP32 where a warp solves one line (tiles of 4 lines): the
+// same 3 R values per lane as two lines of R = 4.
+__host__ __device__ constexpr bool reg_factors(int bytes, int tw, int rr) {
+  return rr >= 1 && (rr <= 4 || (rr == 8 && bytes == 4 && tw == kSolveThreads / 32));
+}
+template <typename T, int TW, int RR>
+constexpr bool kRegFactors = reg_factors(sizeof(T), TW, RR);
 // Rows of a line-solve tile in shared memory: the residual, then the three
 // Thomas factor runs (only where they are not in registers), then x.
-template <int RR>
-constexpr int kTileRows = kRegFactors<RR> ? 2 : 5;
+template <typename T, int TW, int RR>
+constexpr int kTileRows = kRegFactors<T, TW, RR> ? 2 : 5;
 // Shared memory of a line-solve / one-kernel zebra tile for a kernel compiled
 // with RR (R at compile time; 0 = at run time).
 template <typename T, int TW>
 inline size_t line_solve_smem_rr(const Geom &g, int rr) {
-  return sizeof(T) * ((rr >= 1 && rr <= 4) ? 2 : 5) * (size_t)LineLayout::of(g.my).ls * TW;
+  return sizeof(T) * (reg_factors(sizeof(T), TW, rr) ? 2 : 5) * (size_t)LineLayout::of(g.my).ls * TW;
 }
 // Resident blocks per SM the tile kernels are compiled for: with the factors in
-// registers they fit in 48 registers, ten blocks of 128 threads.
-template <int RR>
-constexpr int kTileMinBlocks = kRegFactors<RR> ? 10 : 4;
+// registers they fit in 48 registers, ten blocks of 128 threads (R = 8: eight).
+template <typename T, int TW, int RR>
+constexpr int kTileMinBlocks = kRegFactors<T, TW, RR> ? (RR == 8 ? 8 : 10) : 4;
 
 template <int N>
 __device__ __forceinline__ void ld_run(const float *p, float (&o)[N]) {
-  if constexpr (N == 4) {
+  if constexpr (N == 8) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    const float4 w = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    o[4] = w.x; o[5] = w.y; o[6] = w.z; o[7] = w.w;
+  } else if constexpr (N == 4) {
     const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
   } else if constexpr (N == 2) {
@@ -792,7 +802,7 @@ __device__ __forceinline__ void solve_tile_load(const LevelDev &L, const T *__re
   const int my = g.my, mx = g.mx;
   if (!(k >= 1 && k <= g.mz - 2)) return;
   const LineLayout Lo = LineLayout::fixed<RR>(my);
-  T *sr = st, *sa = sr + Lo.ls * TW, *sx = st + (kTileRows<RR> - 1) * Lo.ls * TW;
+  T *sr = st, *sa = sr + Lo.ls * TW, *sx = st + (kTileRows<T, TW, RR> - 1) * Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
   constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
@@ -846,7 +856,7 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
   const int my = g.my, mx = g.mx;
   const LineLayout Lo = LineLayout::fixed<RR>(my);
   T *sr = st, *sa = sr + Lo.ls * TW, *sm = sa + Lo.ls * TW, *sc = sm + Lo.ls * TW;
-  T *sx = st + (kTileRows<RR> - 1) * Lo.ls * TW;
+  T *sx = st + (kTileRows<T, TW, RR> - 1) * Lo.ls * TW;
   const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
   constexpr int ny = kSolveThreads / TW;
   const int i = tile_line(bx, tx, k, TW, color);
@@ -858,7 +868,7 @@ __device__ __forceinline__ void solve_tile_finish(const LevelDev &L, const T *__
   constexpr int NW = kSolveThreads / 32, NL = TW / NW;
   if (kin) {
     const int o = warp * Lo.ls;
-    if constexpr (kRegFactors<RR>) {
+    if constexpr (kRegFactors<T, TW, RR>) {
       warp_lines_solve<T, NL, RR>(sr + o, lf, NW * Lo.ls, Lo, lane);
     } else {
       const SmemFactors<T> fac{sa + o, sm + o, sc + o};
@@ -903,8 +913,8 @@ __device__ __forceinline__ void line_solve_body(const LevelDev &L, const T *__re
                                                 bool rsplit = false) {
   T *st = reinterpret_cast<T *>(smem_raw);
   TileLaneFactors<T, TW, RR> lf;
-  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color, rsplit, true, !kRegFactors<RR>);
-  if constexpr (kRegFactors<RR>) lane_factors_load<T, TW, RR>(L, bx, k, color, lf);
+  solve_tile_load<T, TW, RR>(L, r, x, bx, k, st, color, rsplit, true, !kRegFactors<T, TW, RR>);
+  if constexpr (kRegFactors<T, TW, RR>) lane_factors_load<T, TW, RR>(L, bx, k, color, lf);
   cp_async_wait_all();
   __syncthreads();
   solve_tile_finish<T, TW, RR>(L, x, xnew, omega, bx, k, st, color, lf);
@@ -982,7 +992,7 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
   const bool kin = k >= 1 && k <= g.mz - 2;
   if (kin) {
     const LineLayout Lo = LineLayout::fixed<RR>(my);
-    T *sr = st, *sx = st + (kTileRows<RR> - 1) * Lo.ls * TW;
+    T *sr = st, *sx = st + (kTileRows<T, TW, RR> - 1) * Lo.ls * TW;
     const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
     constexpr int ny = kSolveThreads / TW;
     const int i = tile_line(bx, tx, k, TW, color);
@@ -997,7 +1007,7 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
       }
     }
     // the factors, as the line solve stages them (nothing to copy asynchronously)
-    if constexpr (!kRegFactors<RR>) solve_tile_load<T, TW, RR>(L, nullptr, nullptr, bx, k, st, color, false, false);
+    if constexpr (!kRegFactors<T, TW, RR>) solve_tile_load<T, TW, RR>(L, nullptr, nullptr, bx, k, st, color, false, false);
   }
   if (xout != xin) {
     // the block's columns [2 TW bx, 2 TW (bx + 1)) of plane k, except the cells
@@ -1016,7 +1026,7 @@ __device__ __forceinline__ void zebra_fused_body(const LevelDev &L, const T *__r
   // register factors after the residual loop, so that they do not add to its
   // registers
   TileLaneFactors<T, TW, RR> lf;
-  if constexpr (kRegFactors<RR>) lane_factors_load<T, TW, RR>(L, bx, k, color, lf);
+  if constexpr (kRegFactors<T, TW, RR>) lane_factors_load<T, TW, RR>(L, bx, k, color, lf);
   __syncthreads();
   solve_tile_finish<T, TW, RR>(L, xin, xout, omega, bx, k, st, color, lf);
 }
