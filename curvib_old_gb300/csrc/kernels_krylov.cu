@@ -2,6 +2,8 @@
 // removal and the coarsest-level dense solve.  Every reduction is two-stage with
 // a fixed block count and a fixed summation tree, so a solve's result does not
 // depend on timing or on what else shares the GPU.
+#include <algorithm>
+
 #include "launch.cuh"
 
 namespace cvb {
@@ -295,39 +297,73 @@ void launch_remove_aj_mean(const Geom &g, const uint32_t *code, const double *aj
   launch_dep(k_remove_aj_mean, reduce_blocks(), 256, 0, s, g, code, aj, b, sums);
 }
 
-// Coarsest level: e = Minv r with a dense FP64 inverse over the cells idx[0..m)
-// (one warp per row), e = r on the identity cells idx[m..n).
-template <typename T>
-__device__ __forceinline__ void dense_rows(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
-                                           const T *__restrict__ r, T *__restrict__ e, int row) {
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  if (row >= m) {
-    if (lane == 0) e[idx[row]] = r[idx[row]];
-    return;
-  }
-  double s = 0.0;
-  for (int c = lane; c < m; c += 32) s = fma(M[(size_t)row * m + c], (double)r[idx[c]], s);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) e[idx[row]] = (T)s;
-}
-template <typename T>
-__global__ void k_dense(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
-                        const T *__restrict__ r, T *__restrict__ e, const int *gate) {
+// Coarsest level: e = Minv r with a dense FP64 inverse over the cells idx[0..m),
+// e = r on the identity cells idx[m..n).  A block first gathers r over the
+// inverted cells into shared memory, in the inverse's column order and in FP64;
+// its warps then take rows, each lane two adjacent columns per step with one
+// 16-byte load of the row (rows are 16-byte aligned for even m) into two
+// accumulators, four steps in flight, then a shuffle sum.  The inverse is the
+// bulk of the bytes (8 m^2), read once per apply.  STAGED false (m beyond what
+// shared memory holds): r is read through idx at every step instead.
+template <typename T, bool STAGED>
+__global__ void __launch_bounds__(256) k_dense(const double *__restrict__ M, const int *__restrict__ idx, int m, int n,
+                                               const T *__restrict__ r, T *__restrict__ e, const int *gate) {
+  extern __shared__ __align__(16) double rc[];
   dep_sync();
   if (gated(gate)) return;
-  dense_rows<T>(M, idx, m, n, r, e, blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5));
+  if (STAGED) {
+    for (int c = threadIdx.x; c < m; c += blockDim.x) rc[c] = (double)r[idx[c]];
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int tw = gridDim.x * nw;
+  for (int row = blockIdx.x * nw + (threadIdx.x >> 5); row < n; row += tw) {
+    if (row >= m) {
+      if (lane == 0) e[idx[row]] = r[idx[row]];
+      continue;
+    }
+    const double *Mr = M + (size_t)row * m;
+    double s0 = 0.0, s1 = 0.0;
+    if (STAGED && (m & 1) == 0) {
+      const double2 *M2 = reinterpret_cast<const double2 *>(Mr);
+      const double2 *R2 = reinterpret_cast<const double2 *>(rc);
+#pragma unroll 4
+      for (int c2 = lane; c2 < (m >> 1); c2 += 32) {
+        const double2 v = __ldg(M2 + c2), x = R2[c2];
+        s0 = fma(v.x, x.x, s0);
+        s1 = fma(v.y, x.y, s1);
+      }
+    } else {
+      for (int c = lane; c < m; c += 32) s0 = fma(__ldg(Mr + c), STAGED ? rc[c] : (double)r[idx[c]], s0);
+    }
+    double sum = s0 + s1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (lane == 0) e[idx[row]] = (T)sum;
+  }
+}
+template <typename T>
+static void dense_apply(const LevelDev &C, const double *Minv, const T *r, T *e, cudaStream_t s, const int *gate) {
+  constexpr int kMaxStaged = 8192;  // 64 KB of staged FP64 input
+  const int n = (int)C.g.n();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_dense<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kMaxStaged);
+    attr = true;
+  }
+  const int rows_per_block = 8, blocks = std::max(1, std::min((n + rows_per_block - 1) / rows_per_block, 4 * sm_count()));
+  if (C.cm <= kMaxStaged)
+    launch_dep(k_dense<T, true>, blocks, 256, sizeof(double) * (size_t)C.cm, s, Minv, C.cidx, C.cm, n, r, e, gate);
+  else
+    launch_dep(k_dense<T, false>, blocks, 256, 0, s, Minv, C.cidx, C.cm, n, r, e, gate);
 }
 void launch_dense_apply(const LevelDev &C, const double *Minv, const double *r, double *e, cudaStream_t s,
                         const int *gate) {
-  int n = (int)C.g.n();
-  launch_dep(k_dense<double>, (n + 7) / 8, 256, 0, s, Minv, C.cidx, C.cm, n, r, e, gate);
+  dense_apply<double>(C, Minv, r, e, s, gate);
 }
 void launch_dense_apply_f32(const LevelDev &C, const double *Minv, const float *r, float *e, cudaStream_t s,
                             const int *gate) {
-  int n = (int)C.g.n();
-  launch_dep(k_dense<float>, (n + 7) / 8, 256, 0, s, Minv, C.cidx, C.cm, n, r, e, gate);
+  dense_apply<float>(C, Minv, r, e, s, gate);
 }
 
 }  // namespace cvb
