@@ -107,6 +107,7 @@ EXPORTS = {
     "cvb_batch_in_flight": ([_P], _I),
     "cvb_batch_set_round_limit": ([_P, ctypes.c_longlong], _I),
     "cvb_batch_set_graphs": ([_P, _I], _I),
+    "cvb_setup_times": ([_P, _P], _I),
     "cvb_batch_graph_stats": ([_P, _P, _P, _P], _I),
     "cvb_zebra_half_f32": ([_P, _I, _I, _I, ctypes.c_float, _P, _P], _I),
     "cvb_viscous": ([_P, _P, _D, _P], _I),

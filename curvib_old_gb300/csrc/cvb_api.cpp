@@ -8,6 +8,7 @@
 #include <atomic>
 #include <array>
 #include <cctype>
+#include <chrono>
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
@@ -1050,6 +1051,9 @@ static int check_nvert(cvb_ctx *ctx, const double *v, size_t n) {
 }
 
 static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
+  using clk = std::chrono::steady_clock;
+  auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+  clk::time_point t = clk::now();
   const int nlevels = ctx->nlevels;
   {
     const cvb_level_desc &d = ctx->H[nlevels - 1].d;
@@ -1100,11 +1104,20 @@ static int setup_problem(cvb_ctx *ctx, const double *nvert_box) {
   TRY(dalloc(ctx, &ctx->partial, (size_t)nb * (kMaxRestart + 2)));
   TRY(dalloc(ctx, &ctx->sums, 2 * (kMaxRestart + 2)));
   TRY(dalloc(ctx, &ctx->hdev, kMaxRestart + 2));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->setup_ms[1] = ms_since(t);
+  t = clk::now();
   TRY(build_operators(ctx));
+  ctx->setup_ms[2] = ms_since(t);
+  t = clk::now();
   TRY(autotune_sweeps(ctx));
+  ctx->setup_ms[3] = ms_since(t);
+  t = clk::now();
   cvb_solve_opts def;
   cvb_solve_opts_default(&def);
   TRY(build_coarse(ctx, &def));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->setup_ms[4] = ms_since(t);
   static std::atomic<unsigned long long> setups{0};
   ctx->setup_id = ++setups;
   ctx->ready = true;
@@ -1311,7 +1324,9 @@ static int upload_geometry(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv) 
 int cvb_setup_hierarchy(cvb_ctx *ctx, int nlevels, const cvb_level_desc *lv, const double *nvert_finest) {
   if (!ctx) return CVB_BAD_INPUT;
   if (nlevels < 1 || nlevels > 16 || !lv || !nvert_finest) return fail(ctx, CVB_BAD_INPUT, "bad hierarchy arguments");
+  const auto t0 = std::chrono::steady_clock::now();
   TRY(upload_geometry(ctx, nlevels, lv));
+  ctx->setup_ms[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   std::vector<double> h;
   return setup_problem(ctx, box_view(lv[nlevels - 1], nvert_finest, 1, h));
 }
@@ -1336,6 +1351,7 @@ int cvb_setup_like(cvb_ctx *ctx, const cvb_ctx *donor, const double *nvert_fines
   ctx->nlevels = (int)H.size();
   ctx->H = H;
   ctx->geo = G;
+  ctx->setup_ms[0] = 0.0;  // the grid is the donor's
   std::vector<double> h;
   return setup_problem(ctx, box_view(ctx->H[ctx->nlevels - 1].d, nvert_finest, 1, h));
 }
@@ -1376,11 +1392,22 @@ int cvb_set_nvert(cvb_ctx *ctx, const double *nvert_finest) {
   drop_vcycle_graphs(ctx);
   CK(cudaMemcpyAsync(ctx->L[ctx->nlevels - 1].nvert, v, sizeof(double) * ctx->L[ctx->nlevels - 1].g.n(),
                      cudaMemcpyHostToDevice, ctx->stream));
+  using clk = std::chrono::steady_clock;
+  auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->setup_ms[0] = ctx->setup_ms[1] = 0.0;  // the grid and the level arrays stay
+  clk::time_point t = clk::now();
   TRY(build_operators(ctx));
+  ctx->setup_ms[2] = ms_since(t);
+  t = clk::now();
   TRY(autotune_sweeps(ctx));
+  ctx->setup_ms[3] = ms_since(t);
+  t = clk::now();
   cvb_solve_opts def;
   cvb_solve_opts_default(&def);
   TRY(build_coarse(ctx, &def));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->setup_ms[4] = ms_since(t);
   return CVB_OK;
 }
 
@@ -2086,6 +2113,12 @@ int cvb_geometry_bytes(const cvb_ctx *ctx, unsigned long long *bytes, unsigned l
   if (!ctx || !bytes) return CVB_BAD_INPUT;
   *bytes = ctx->geo ? (unsigned long long)ctx->geo->bytes : 0ull;
   if (id) *id = (unsigned long long)(uintptr_t)ctx->geo.get();
+  return CVB_OK;
+}
+
+int cvb_setup_times(const cvb_ctx *ctx, double *ms5) {
+  if (!ctx || !ms5) return CVB_BAD_INPUT;
+  for (int q = 0; q < 5; q++) ms5[q] = ctx->setup_ms[q];
   return CVB_OK;
 }
 

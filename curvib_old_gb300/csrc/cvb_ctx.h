@@ -100,6 +100,9 @@ struct cvb_ctx {
   // changes with every set-up of the operators (process-wide counter): the
   // batch engine's captured V-cycles are valid for one value
   unsigned long long setup_id = 0;
+  // wall-clock ms of the last set-up's phases: metrics upload (0 when the grid
+  // was shared), level arrays, operators, autotuner, coarsest solver
+  double setup_ms[5] = {};
   std::map<int, cvb::VGraph> vgraphs;  // captured V-cycles by (precision, basis slot)
   // measured sweep times (us): line sweeps fused / split, zebra sweeps two-kernel /
   // one-kernel, and the FP32 zebra sweep with TMA-staged tiles of 4, 8, 16 row

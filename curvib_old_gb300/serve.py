@@ -244,6 +244,7 @@ class Server:
         """Serve `stream` (sorted by arrival); returns the statistics."""
         queue, inflight, preparing = [], {}, []
         lat, warm, cold_followups, evictions, reused = [], 0, 0, 0, 0
+        prep = []  # set-up phases (ms) of every problem prepared for the stream
         spent = {"admit_s": 0.0, "step_s": 0.0, "result_s": 0.0, "rounds": 0}
         nxt = 0
         t0 = time.perf_counter()
@@ -292,6 +293,7 @@ class Server:
                 c = self.ctxs[cid]
                 if c["ready"].done():
                     c["ready"].result()           # re-raise a failed preparation
+                    prep.append(c["ctx"].setup_times())
                     c["bytes"] = max(c["ctx"].device_bytes(), own_bytes_estimate(c["n"]))
                     submit(req, cid, False)
                 else:
@@ -326,7 +328,9 @@ class Server:
                 "p99_ms": float(np.percentile(lat, 99)) if lat else None,
                 "warm_followups": warm, "cold_followups": cold_followups, "contexts_reused": reused,
                 "evictions": evictions, "peak_resident_bytes": int(self.peak), "budget_bytes": int(self.budget),
-                "loop": spent}
+                "loop": spent,
+                "setup_ms_mean": {k: float(np.mean([q[k] for q in prep])) for k in prep[0]} if prep else None,
+                "setups": len(prep)}
 
 
 def capacity(inputs, stream, device=0, precision=_lib.MIXED, rtol=1e-8, budget_bytes=150e9):

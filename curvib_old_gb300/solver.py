@@ -364,6 +364,14 @@ class PoissonContext:
             raise CvbError(rc, self._L.cvb_last_error(self._ctx).decode())
         return xb
 
+    def setup_times(self):
+        """Milliseconds of the last set-up by phase: metrics upload, level
+        arrays, operators, autotuner, coarsest solver."""
+        v = np.zeros(5)
+        self._check(self._L.cvb_setup_times(self._ctx, ptr(v)))
+        return dict(zip(("metrics_upload", "level_arrays", "operators", "autotuner", "coarse_solver"),
+                        (float(x) for x in v)))
+
     def weights(self, level):
         w = np.zeros((19,) + self.shapes[level])
         self._check(self._L.cvb_get_weights(self._ctx, level, ptr(w)))

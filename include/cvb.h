@@ -468,6 +468,16 @@ enum {
 /* JSON record of the set-up autotuner: per level, the measured time of the
  * fused and the split y-line sweep in each precision and the variant kept. */
 int cvb_tuning_report(cvb_ctx *ctx, char *buf, int len);
+/* Wall-clock milliseconds of the last set-up (cvb_setup_hierarchy,
+ * cvb_setup_like or cvb_set_nvert) by phase: [0] the grid's metrics uploaded
+ * (0 when shared or kept), [1] the level arrays allocated and nvert copied (0 for
+ * cvb_set_nvert), [2] nvert restriction and the operators of every level
+ * (MyNvertRestriction, FullyBlocked, PoissonLHSNew's weights, the FP32 copies,
+ * the line factors), [3] the autotuner (0 when every level shape was timed
+ * before in the process), [4] the coarsest solver (dense inverse).  The
+ * reference rebuilds its operators and factors in every PoissonSolver_MG call
+ * (poisson.c:1775). */
+int cvb_setup_times(const cvb_ctx *ctx, double *ms5);
 /* Average duration of `reps` back-to-back launches of one kernel on `level`
  * (CUDA events on the context's stream) and its algorithmic bytes per launch
  * (every array it needs, touched once). */
