@@ -1325,3 +1325,130 @@ int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o,
 #undef R3
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The momentum equation's pseudo-time iteration for a box whose six faces are
+ * all solid walls (bctype 1), with no immersed-body interpolation (immersed
+ * 0) and one block. */
+
+/* One of FormBCS's edge averages: ucat and p at d become the means of their
+ * values at a and b (bcs.c:5439-5570). */
+static inline void edge_avg(double *u, double *p, long d, long a, long b) {
+  avg3(u + 3 * d, u + 3 * a, u + 3 * b);
+  p[d] = 0.5 * (p[a] + p[b]);
+}
+
+int orc_form_bcs_walls(const orc_level *L, const double *ucont, const double *ub, double *u, double *p) {
+  const int mx = L->mx, my = L->my, mz = L->mz;
+  for (int f = 0; f < 6; f++)
+    if (L->bctype[f] != 1) return -1;
+#define U3(i, j, k) (u + 3 * ID(L, (i), (j), (k)))
+#define B3(i, j, k) (ub + 3 * ID(L, (i), (j), (k)))
+#define Q(i, j, k) ((long)ID(L, (i), (j), (k)))
+  for (int pass = 0; pass < 3; pass++) { /* bcs.c:4483 */
+    orc_contra2cart(L, ucont, u);          /* bcs.c:5159 */
+    /* ghost faces on the faces' interior cells (bcs.c:5250-5318) */
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++) ghost3(U3(0, j, k), B3(0, j, k), U3(1, j, k));
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++) ghost3(U3(mx - 1, j, k), B3(mx - 1, j, k), U3(mx - 2, j, k));
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) ghost3(U3(i, 0, k), B3(i, 0, k), U3(i, 1, k));
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) ghost3(U3(i, my - 1, k), B3(i, my - 1, k), U3(i, my - 2, k));
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) ghost3(U3(i, j, 0), B3(i, j, 0), U3(i, j, 1));
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) ghost3(U3(i, j, mz - 1), B3(i, j, mz - 1), U3(i, j, mz - 2));
+    /* the 12 edges of ucat and p, in the reference's order (bcs.c:5439-5570) */
+    for (int j = 0; j < my; j++) edge_avg(u, p, Q(0, j, 0), Q(0, j, 1), Q(1, j, 0));
+    for (int j = 0; j < my; j++) edge_avg(u, p, Q(mx - 1, j, 0), Q(mx - 1, j, 1), Q(mx - 2, j, 0));
+    for (int i = 0; i < mx; i++) edge_avg(u, p, Q(i, 0, 0), Q(i, 0, 1), Q(i, 1, 0));
+    for (int i = 0; i < mx; i++) edge_avg(u, p, Q(i, my - 1, 0), Q(i, my - 1, 1), Q(i, my - 2, 0));
+    for (int j = 0; j < my; j++) edge_avg(u, p, Q(0, j, mz - 1), Q(0, j, mz - 2), Q(1, j, mz - 1));
+    for (int j = 0; j < my; j++) edge_avg(u, p, Q(mx - 1, j, mz - 1), Q(mx - 1, j, mz - 2), Q(mx - 2, j, mz - 1));
+    for (int i = 0; i < mx; i++) edge_avg(u, p, Q(i, 0, mz - 1), Q(i, 0, mz - 2), Q(i, 1, mz - 1));
+    for (int i = 0; i < mx; i++) edge_avg(u, p, Q(i, my - 1, mz - 1), Q(i, my - 1, mz - 2), Q(i, my - 2, mz - 1));
+    for (int k = 0; k < mz; k++) edge_avg(u, p, Q(0, 0, k), Q(0, 1, k), Q(1, 0, k));
+    for (int k = 0; k < mz; k++) edge_avg(u, p, Q(mx - 1, 0, k), Q(mx - 1, 1, k), Q(mx - 2, 0, k));
+    for (int k = 0; k < mz; k++) edge_avg(u, p, Q(0, my - 1, k), Q(0, my - 2, k), Q(1, my - 1, k));
+    for (int k = 0; k < mz; k++) edge_avg(u, p, Q(mx - 1, my - 1, k), Q(mx - 1, my - 2, k), Q(mx - 2, my - 1, k));
+  }
+#undef U3
+#undef B3
+#undef Q
+  return 0;
+}
+
+/* VecNorm(NORM_INFINITY) as the PETSc shim computes it: the largest |x|. */
+static double max_abs(const double *x, size_t n) {
+  double s = 0;
+  for (size_t q = 0; q < n; q++) {
+    const double v = fabs(x[q]);
+    s = v > s ? v : s;
+  }
+  return s;
+}
+
+int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
+               double *p, const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart,
+               int central, double atol, double rtol, int max_it, orc_imp_rk_stats *out) {
+  const size_t n3 = 3 * (size_t)L->mx * L->my * L->mz;
+  const double alfa[4] = {0.25, 1 / 3., 0.5, 1.}; /* implicitsolver.c:7111 */
+  if (orc_form_bcs_walls(L, ucont, ubcs, ucat, p)) return -1;
+  double *rhs = (double *)calloc(n3, sizeof(double)), *pu = (double *)malloc(sizeof(double) * n3);
+  memcpy(pu, ucont, sizeof(double) * n3);
+  orc_calc_rhs(L, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central, rhs);
+  double normF0 = max_abs(rhs, n3), normF1 = 1000., normdU1 = 1000., lambda = cfl;
+  double normdU = 10., reldU = 1., normdU_bk = 0., reldU_bk = 1., normdU0 = 0., normF_bk = 0., relF_bk = 0.;
+  int pseudot = 0, rejected = 0;
+  /* implicitsolver.c:7149-7239 */
+  while (((normdU > atol && reldU > rtol) || pseudot < 1) && pseudot < max_it) {
+    pseudot++;
+    for (int s = 0; s < 4; s++) {
+      const double a = lambda * alfa[s] * dt * st;
+      for (size_t q = 0; q < n3; q++) ucont[q] = a * rhs[q] + pu[q];
+      orc_form_bcs_walls(L, ucont, ubcs, ucat, p);
+      orc_calc_rhs(L, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central, rhs);
+    }
+    normdU1 = normdU_bk;
+    normdU_bk = 0;
+    for (size_t q = 0; q < n3; q++) {
+      const double v = fabs(-1. * ucont[q] + pu[q]);
+      normdU_bk = v > normdU_bk ? v : normdU_bk;
+    }
+    if (pseudot == 1) {
+      normdU0 = normdU_bk;
+      reldU_bk = 1.;
+    } else if (normdU0 > 1.e-10)
+      reldU_bk = normdU_bk / normdU0;
+    if (pseudot > 1) normF1 = normF_bk;
+    normF_bk = max_abs(rhs, n3);
+    if (pseudot == 1) normF0 = normF_bk;
+    relF_bk = normF_bk / normF0;
+    normdU = normdU_bk;
+    reldU = reldU_bk;
+    if (pseudot > 1 && normF_bk > normF1 && normdU_bk > normdU1 && lambda > 0.001) {
+      lambda = 0.5 * lambda;
+      pseudot--;
+      rejected++;
+      memcpy(ucont, pu, sizeof(double) * n3);
+    } else {
+      memcpy(pu, ucont, sizeof(double) * n3);
+      normF1 = normF_bk;
+      normdU1 = normdU_bk;
+    }
+  }
+  free(rhs);
+  free(pu);
+  if (out) {
+    out->pseudo_iterations = pseudot;
+    out->rejected = rejected;
+    out->norm_du = normdU;
+    out->rel_du = reldU;
+    out->norm_f = normF_bk;
+    out->rel_f = relF_bk;
+    out->lambda = lambda;
+  }
+  return 0;
+}

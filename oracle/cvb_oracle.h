@@ -116,4 +116,24 @@ int orc_form_function1(const orc_level *L, const double *ucont, double *ucat, co
 int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o, const double *ucont_rm1,
                  double *ucat, const double *p, double ren, double dt, int ti, int tistart, int central,
                  double *rhs);
+/* FormBCS (bcs.c:4436-5889) for a box whose six faces are solid walls
+ * (bctype 1): three passes of Contra2Cart, the ghost faces u = 2 ubcs - inner
+ * on the faces' interior cells (bcs.c:5250-5318) and the averages of ucat and
+ * p on the box's 12 edges (bcs.c:5439-5570).  ucat and p are read and
+ * written, ubcs is read.  -1 (nothing written) for any other face type. */
+int orc_form_bcs_walls(const orc_level *L, const double *ucont, const double *ubcs, double *ucat, double *p);
+typedef struct {
+  int pseudo_iterations; /* pseudot at the end */
+  int rejected;          /* iterations undone with the pseudo-time step halved */
+  double norm_du, rel_du, norm_f, rel_f, lambda;
+} orc_imp_rk_stats;
+/* ImpRK (implicitsolver.c:7094-7257) for a walled box, one block, no immersed
+ * body: InflowFlux and OutflowFlux change nothing there, FormBCS as
+ * orc_form_bcs_walls, CalcRHS as orc_calc_rhs; four Runge-Kutta stages per
+ * pseudo-time iteration, the step halved and the iteration undone when both
+ * norms grew, until |dU| <= atol or |dU| / |dU|_1 <= rtol or max_it
+ * iterations.  ucont, ucat and p are read and written. */
+int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
+               double *p, const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart,
+               int central, double atol, double rtol, int max_it, orc_imp_rk_stats *out);
 #endif

@@ -120,6 +120,10 @@ def lib():
         _lib.orc_viscous.argtypes = [L, P, D, P]
         _lib.orc_form_function1.argtypes = [L, P, P, P, D, I, P]
         _lib.orc_calc_rhs.argtypes = [L, P, P, P, P, P, D, D, I, I, I, P]
+        _lib.orc_form_bcs_walls.argtypes = [L, P, P, P, P]
+        _lib.orc_form_bcs_walls.restype = I
+        _lib.orc_imp_rk.argtypes = [L, P, P, P, P, P, P, D, D, D, D, I, I, I, D, D, I, P]
+        _lib.orc_imp_rk.restype = I
     return _lib
 
 
@@ -292,6 +296,37 @@ def calc_rhs(L: OLevel, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart
     rc = lib().orc_calc_rhs(L.ref(), *[_p(x) for x in a], _p(u), _p(pp), float(ren), float(dt), int(ti),
                             int(tistart), int(central), _p(out))
     return rc, out, u
+
+
+class ImpRKStats(ctypes.Structure):
+    _fields_ = [("pseudo_iterations", ctypes.c_int), ("rejected", ctypes.c_int), ("norm_du", ctypes.c_double),
+                ("rel_du", ctypes.c_double), ("norm_f", ctypes.c_double), ("rel_f", ctypes.c_double),
+                ("lambda_", ctypes.c_double)]
+
+
+def form_bcs_walls(L: OLevel, ucont, ubcs, ucat, p):
+    """FormBCS (bcs.c:4436-5889) for an all-wall box: (status, ucat, p)."""
+    uc = np.ascontiguousarray(ucont, dtype=np.float64)
+    ub = np.ascontiguousarray(ubcs, dtype=np.float64)
+    u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+    pp = np.array(p, dtype=np.float64, copy=True, order="C")
+    rc = lib().orc_form_bcs_walls(L.ref(), _p(uc), _p(ub), _p(u), _p(pp))
+    return rc, u, pp
+
+
+def imp_rk(L: OLevel, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=0,
+           atol=1e-7, rtol=1e-4, max_it=50):
+    """ImpRK (implicitsolver.c:7094-7257) for an all-wall box with no immersed
+    body: (status, ucont, ucat, p, stats)."""
+    uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+    uo, urm, ub = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1, ubcs)]
+    u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+    pp = np.array(p, dtype=np.float64, copy=True, order="C")
+    st_ = ImpRKStats()
+    rc = lib().orc_imp_rk(L.ref(), _p(uc), _p(uo), _p(urm), _p(u), _p(pp), _p(ub), float(ren), float(dt), float(st),
+                          float(cfl), int(ti), int(tistart), int(central), float(atol), float(rtol), int(max_it),
+                          ctypes.byref(st_))
+    return rc, uc, u, pp, st_
 
 
 def metrics_divergence(L: OLevel):
@@ -480,6 +515,28 @@ class Reference:
                                int(ti), int(tistart), int(central), _p(out)):
             raise RuntimeError("ref_calc_rhs failed")
         return out, u
+
+    def form_bcs(self, ucont, ubcs, ucat, p):
+        uc, ub = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont, ubcs)]
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        pp = np.array(p, dtype=np.float64, copy=True, order="C")
+        if self.L.ref_form_bcs(_p(uc), _p(ub), _p(u), _p(pp)):
+            raise RuntimeError("ref_form_bcs failed")
+        return u, pp
+
+    def imp_rk(self, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=0,
+               atol=1e-7, rtol=1e-4, max_it=50):
+        """ImpRK through the reference's own routine; it appends to
+        Converge_dU0 in the working directory."""
+        uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+        uo, urm, ub = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1, ubcs)]
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        pp = np.array(p, dtype=np.float64, copy=True, order="C")
+        D = ctypes.c_double
+        if self.L.ref_imp_rk(_p(uc), _p(uo), _p(urm), _p(u), _p(pp), _p(ub), D(ren), D(dt), D(st), D(cfl), int(ti),
+                             int(tistart), int(central), D(atol), D(rtol), int(max_it)):
+            raise RuntimeError("ref_imp_rk failed")
+        return uc, u, pp
 
     def metrics_divergence(self):
         m, at = ctypes.c_double(), ctypes.c_int()

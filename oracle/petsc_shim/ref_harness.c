@@ -668,3 +668,62 @@ int ref_calc_rhs(const double *ucont, const double *ucont_o, const double *ucont
   PetscOptionsSetValue("-central", "0");
   return rc;
 }
+
+/* FormBCS (bcs.c:4436-5889) on the finest level: ucont (Ucont) and ubcs
+ * (Bcs.Ubcs) read, ucat (Ucat) and p (P) read and written, global boxes. */
+int ref_form_bcs(const double *ucont, const double *ubcs, double *ucat, double *p) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  set_pair(u, u->P, u->lP, 1, p, u->da);
+  copy_owned(u, u->Bcs.Ubcs, 3, (double *)ubcs, 1);
+  int rc = FormBCS(u);
+  copy_owned(u, u->Ucat, 3, ucat, 0);
+  copy_owned(u, u->P, 1, p, 0);
+  return rc;
+}
+
+/* ImpRK (implicitsolver.c:7094-7257) on the finest level, one block, no
+ * immersed body: ucont, ucat and p (Ucont, Ucat, P) read and written, ubcs
+ * (Bcs.Ubcs) read, ucont_o / ucont_rm1 the two previous steps' fluxes; cfl,
+ * dt and st the block's, imp_atol / imp_rtol / imp_MAX_IT from the arguments
+ * for this call.  The routine appends to the file Converge_dU0 in the working
+ * directory, as the reference's rank 0 does. */
+int ref_imp_rk(double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
+               const double *ubcs, double ren, double dt, double st, double cfl, int ti_, int tistart_, int central,
+               double atol, double rtol, int max_it) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
+  set_pair(u, u->P, u->lP, 1, p, u->da);
+  copy_owned(u, u->Bcs.Ubcs, 3, (double *)ubcs, 1);
+  if (!u->Ucont_o) VecDuplicate(u->Ucont, &u->Ucont_o);
+  if (!u->Ucont_rm1) VecDuplicate(u->Ucont, &u->Ucont_rm1);
+  copy_owned(u, u->Ucont_o, 3, (double *)ucont_o, 1);
+  copy_owned(u, u->Ucont_rm1, 3, (double *)ucont_rm1, 1);
+  if (!u->psuedot) VecDuplicate(u->Ucont, &u->psuedot);
+  VecSet(u->psuedot, 0.);
+  u->ren = ren;
+  u->dt = dt;
+  u->st = st;
+  u->cfl = cfl;
+  PetscOptionsSetValue("-central", central ? "1" : "0");
+  ti = ti_;
+  tistart = tistart_;
+  const PetscInt it0 = imp_MAX_IT;
+  const PetscReal a0 = imp_atol, r0 = imp_rtol;
+  imp_MAX_IT = max_it;
+  imp_atol = atol;
+  imp_rtol = rtol;
+  int rc = ImpRK(u, NULL, NULL);
+  imp_MAX_IT = it0;
+  imp_atol = a0;
+  imp_rtol = r0;
+  PetscOptionsSetValue("-central", "0");
+  copy_owned(u, u->Ucont, 3, ucont, 0);
+  copy_owned(u, u->Ucat, 3, ucat, 0);
+  copy_owned(u, u->P, 1, p, 0);
+  return rc;
+}

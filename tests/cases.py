@@ -156,3 +156,20 @@ def momentum_inputs(shape):
     """ucat, p, ucont_o and ucont_rm1 ([mz][my][mx](x3)) of the momentum checks."""
     sh3 = tuple(shape) + (3,)
     return seeded(sh3, 810), seeded(shape, 811), seeded(sh3, 812), seeded(sh3, 813)
+
+
+# The pseudo-time iteration of the momentum equation (ImpRK) on the all-wall
+# scenarios: (ti, cfl, imp_MAX_IT) -- converged by the absolute tolerance with
+# no step halved, stopped at imp_MAX_IT, and with the step halved and
+# iterations undone (cfl 3) -- at imp_atol 1e-7, imp_rtol 1e-4 (main.c's
+# defaults).
+IMP_RK_RUNS = [(1, 1.0, 50), (5, 0.5, 4), (5, 3.0, 50)]
+IMP_ATOL, IMP_RTOL = 1e-7, 1e-4
+
+
+def imp_rk_inputs(shape, ucont):
+    """ucat, p, ucont_o, ucont_rm1 and ubcs of the ImpRK checks: the previous
+    steps' fluxes close to ucont, a small pressure, a small wall velocity."""
+    sh3 = tuple(shape) + (3,)
+    return (seeded(sh3, 810), 0.01 * seeded(shape, 811), 0.99 * ucont, 0.97 * ucont,
+            1e-3 * seeded(sh3, 820))

@@ -19,7 +19,9 @@ usage: python tests/golden/make_golden.py REFERENCE_DIR
 from __future__ import annotations
 
 import json
+import os
 import sys
+import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -28,7 +30,8 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from cases import (MOM_DT, MOM_REN, conv_seam_nvert, mom_edge_nvert, momentum_inputs)  # noqa: E402
+from cases import (IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, MOM_DT, MOM_REN, conv_seam_nvert, imp_rk_inputs,  # noqa: E402
+                   mom_edge_nvert, momentum_inputs)
 from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
 from curvib_old_gb300 import workload as W  # noqa: E402
@@ -125,6 +128,21 @@ def momentum(R, nvert, ucont, bctype):
     for ti in (1, 5):
         r, _ = R.calc_rhs(ucont, uo, urm, ucat0, p, MOM_REN, MOM_DT, ti, 0)
         out[f"calc_rhs_{ti}"] = digest(r)
+    if all(b == 1 for b in bctype):
+        # FormBCS and ImpRK (bcs.c:4436, implicitsolver.c:7094), all-wall boxes
+        ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(nvert.shape, ucont)
+        u, pp = R.form_bcs(ucont, ubcs1, ucat1, p1)
+        out["form_bcs"] = {"ucat": digest(u), "p": digest(pp)}
+        with tempfile.TemporaryDirectory() as d:
+            cwd = os.getcwd()
+            os.chdir(d)  # ImpRK appends to Converge_dU0 in the working directory
+            try:
+                for ti, cfl, max_it in IMP_RK_RUNS:
+                    uc, u, pp = R.imp_rk(ucont, uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
+                                         IMP_ATOL, IMP_RTOL, max_it)
+                    out[f"imp_rk_{ti}_{cfl}_{max_it}"] = {"ucont": digest(uc), "ucat": digest(u), "p": digest(pp)}
+            finally:
+                os.chdir(cwd)
     return out
 
 

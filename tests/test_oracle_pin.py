@@ -213,6 +213,19 @@ def _check_momentum(c, nvert, bctype, want):
     for ti in (1, 5):
         rc, r, _ = O.calc_rhs(L, c["ucont"], uo, urm, ucat0, p, MOM_REN, MOM_DT, ti, 0)
         assert rc == 0 and digest(r) == want[f"calc_rhs_{ti}"], ti
+    if "form_bcs" in want:
+        from cases import IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, imp_rk_inputs
+        ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(nvert.shape, c["ucont"])
+        rc, u, pp = O.form_bcs_walls(L, c["ucont"], ubcs1, ucat1, p1)
+        assert rc == 0 and {"ucat": digest(u), "p": digest(pp)} == want["form_bcs"]
+        for ti, cfl, max_it in IMP_RK_RUNS:
+            rc, uc, u, pp, _ = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0,
+                                        0, IMP_ATOL, IMP_RTOL, max_it)
+            assert rc == 0
+            assert {"ucont": digest(uc), "ucat": digest(u), "p": digest(pp)} == want[f"imp_rk_{ti}_{cfl}_{max_it}"], \
+                (ti, cfl, max_it)
+    elif all(b == 1 for b in bctype):
+        raise AssertionError("all-wall scenario without FormBCS / ImpRK digests")
 
 
 @pytest.mark.parametrize("name", sorted(SCENARIOS))
@@ -220,7 +233,10 @@ def test_momentum_rhs_matches_reference(name):
     """Viscous, FormFunction1 and CalcRHS (rhs.c:1947-3351, implicitsolver.c:
     6449-6713) bit for bit; on box_sphere also with cells whose tangential
     pressure derivative the reference leaves unassigned (cases.MOM_EDGES) and
-    with a convective-outflow face (bctype[5] 8)."""
+    with a convective-outflow face (bctype[5] 8).  On the all-wall boxes also
+    FormBCS (bcs.c:4436-5889) and the pseudo-time iteration ImpRK
+    (implicitsolver.c:7094-7257): converged, stopped at imp_MAX_IT, and with
+    the step halved."""
     from cases import mom_edge_nvert
     c = _setup(name)
     ref = REF["scenarios"][name]
