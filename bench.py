@@ -322,7 +322,7 @@ def run_cvb(args, ws, rank, local):
         out["levels_6"] = bench_levels6(args, ws, local, b)
         out["box64"] = bench_box64(args, ws, rank, local)
     if not args.no_step:
-        out["projection_step"] = bench_step(args, ws, local)
+        out["projection_step"] = bench_step(args, ws, local, rank == 0 and not args.no_cpu_baseline)
     if not args.no_ibm:
         out["ibm_search"] = bench_ibm(args, ws, local, rank == 0 and not args.no_cpu_baseline)
     if not args.no_batch:
@@ -458,7 +458,77 @@ def bench_serve(args, local):
     return out
 
 
-def bench_step(args, ws, local):
+def full_step(args, ws, ctx, P, dt, st, rtol, pinned, with_cpu):
+    """Time steps of the fractional-step method on the projection step's box,
+    marching: ImpRK (the momentum equation's pseudo-time iteration, four
+    Runge-Kutta stages of FormBCS + CalcRHS per iteration, imp_atol 1e-7,
+    imp_rtol 1e-4, imp_MAX_IT 50 as the reference's defaults, cfl 0.05), then
+    PoissonSolver_MG (mixed, to 1e-8), UpdatePressure and Projection, then
+    Ucont_rm1 <- Ucont_o <- Ucont; every call through the C ABI on pinned host
+    arrays.  The box's faces are walls; the sphere enters through nvert alone
+    (the reference's immersed-boundary interpolation between iterations is not
+    part of this path)."""
+    import torch
+
+    from curvib_old_gb300 import _lib
+    L, ptr = _lib.lib(), _lib.ptr
+    # cfl: the reference's default 0.2 makes the last stage's pseudo-time step
+    # (0.2 dt) about 9 times the explicit viscous limit of the wall cells of
+    # this stretched grid (h_y 7.6e-4 at Re 300), and the iteration blows up to
+    # NaN in its first iterations, in the reference's arithmetic as here; 0.05
+    # is inside the limit (the 48^3 and 96^3 boxes converge at 0.2)
+    ren, cfl, atol, itol, max_it = 300.0, 0.05, 1e-7, 1e-4, 50
+    shape = P.nvert.shape
+    uc = pinned(P.ucont)
+    uo, urm = pinned(P.ucont), pinned(P.ucont)
+    ucat, ubcs, p, phi = (pinned(np.zeros(shape + (3,))), pinned(np.zeros(shape + (3,))), pinned(np.zeros(shape)),
+                          pinned(np.zeros(shape)))
+    o = _lib.default_opts(precision=_lib.MIXED, rtol=rtol, max_it=200)
+    stt, ist = _lib.SolveStats(), _lib.ImpRKStats()
+    rec = []
+    steps = max(2, min(3, args.step_steps))
+    for ti in range(1, steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = L.cvb_imp_rk(ctx._ctx, ptr(uc.numpy()), ptr(uo.numpy()), ptr(urm.numpy()), ptr(ucat.numpy()),
+                          ptr(p.numpy()), ptr(ubcs.numpy()), ren, dt, st, cfl, ti, 0, 0, atol, itol, max_it,
+                          ctypes.byref(ist))
+        assert rc == 0, rc
+        t1 = time.perf_counter()
+        rc = L.cvb_poisson_solver_mg(ctx._ctx, ptr(uc.numpy()), 0.0, 1, dt, st, ptr(phi.numpy()), ctypes.byref(o),
+                                     ctypes.byref(stt))
+        assert rc == 0, rc
+        assert L.cvb_update_pressure(ctx._ctx, ptr(p.numpy()), ptr(phi.numpy())) == 0
+        assert L.cvb_projection_cart(ctx._ctx, ptr(phi.numpy()), dt, st, ptr(uc.numpy()), ptr(ubcs.numpy()),
+                                     ptr(ucat.numpy())) == 0
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        urm.numpy()[...] = uo.numpy()
+        uo.numpy()[...] = uc.numpy()
+        rec.append({"ti": ti, "imp_rk_ms": (t1 - t0) * 1e3, "pseudo_iterations": ist.pseudo_iterations,
+                    "rejected": ist.rejected, "rel_du": ist.rel_du, "projection_ms": (t2 - t1) * 1e3,
+                    "poisson_iterations": stt.iterations})
+    stages = sum(4 * (r["pseudo_iterations"] + r["rejected"]) for r in rec)
+    imp = sum(r["imp_rk_ms"] for r in rec)
+    out = {"steps": rec, "ms_per_step": sum(r["imp_rk_ms"] + r["projection_ms"] for r in rec) / len(rec),
+           "imp_rk_ms_per_stage": imp / stages,
+           "note": "first-order time term at ti 1, BDF2 after; ubcs 0 (no-slip walls); the pseudo-time loop keeps "
+                   "the reference's order of norms and its halving of the step"}
+    if with_cpu:
+        # the oracle's FormBCS + CalcRHS (one Runge-Kutta stage) on the same
+        # arrays, once, on one core
+        from oracle import oracle as O
+        Lo = O.OLevel(P.metrics[-1], P.nvert, P.bctype, P.semi)
+        t0 = time.perf_counter()
+        O.form_bcs_walls(Lo, uc.numpy(), ubcs.numpy(), ucat.numpy(), p.numpy())
+        O.calc_rhs(Lo, uc.numpy(), uo.numpy(), urm.numpy(), ucat.numpy(), p.numpy(), ren, dt, 5, 0)
+        sec = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sec * 1e3, "unit": "ms per Runge-Kutta stage", "cores": 1, "kind": "port",
+                               "sample": "one FormBCS + CalcRHS stage of the oracle on the same 192^3 arrays"}
+    return out
+
+
+def bench_step(args, ws, local, with_cpu):
     """The pressure-projection part of config 2's time step at 192^3 cells, as the
     reference's Flow_Solver calls it on host arrays: PoissonSolver_MG
     (VolumeFlux_rev, PoissonRHS, the solve to 1e-8), UpdatePressure and
@@ -537,7 +607,8 @@ def bench_step(args, ws, local):
                        "Projection (flux correction, Contra2Cart, GhostNodeVelocity) on pinned host arrays, "
                        "Taylor-Green u*; beside it CalcRHS (the momentum right-hand side: FormFunction1 with "
                        "Convection and Viscous at Re 300, the BDF2 term) on the same host arrays, timed apart "
-                       "(momentum_rhs_ms); the pseudo-time stages and their boundary conditions are not built",
+                       "(momentum_rhs_ms); full_step: whole time steps with the momentum equation's pseudo-time "
+                       "iteration (ImpRK with FormBCS) in front",
            "unknowns": int(P.unknowns)}
     phis = {}
     for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
@@ -547,6 +618,7 @@ def bench_step(args, ws, local):
         phis[name] = phi.numpy().copy()
     out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
     out["err_vs_fp64"] = phi_err(phis["mixed"], phis["fp64"], P.nvert)
+    out["full_step"] = full_step(args, ws, ctx, P, dt, st, rtol, pinned, with_cpu)
     # the 19-point kernels of a distorted grid (7.3 M cells, far beyond L2)
     out["roofline_19pt"] = roofline(ctx, orthogonal=False)
     # the post-projection kernels and the momentum step's convective term

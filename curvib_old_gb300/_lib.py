@@ -52,6 +52,14 @@ class SolveStats(ctypes.Structure):
         return d
 
 
+class ImpRKStats(ctypes.Structure):
+    _fields_ = [("pseudo_iterations", _I), ("rejected", _I), ("norm_du", _D), ("rel_du", _D), ("norm_f", _D),
+                ("rel_f", _D), ("lambda_", _D)]
+
+    def as_dict(self):
+        return {f.rstrip("_"): getattr(self, f) for f, _ in self._fields_}
+
+
 EXPORTS = {
     "cvb_solve_opts_default": ([_P], _I),
     "cvb_init": ([_P, _P], _I),
@@ -113,6 +121,8 @@ EXPORTS = {
     "cvb_viscous": ([_P, _P, _D, _P], _I),
     "cvb_form_function1": ([_P, _P, _P, _P, _D, _I, _P], _I),
     "cvb_calc_rhs": ([_P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P], _I),
+    "cvb_form_bcs": ([_P, _P, _P, _P, _P], _I),
+    "cvb_imp_rk": ([_P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _D, _I, _I, _I, _D, _D, _I, _P], _I),
     "cvb_device_bytes": ([_P, _P], _I),
     "cvb_set_device_limit": ([_P, ctypes.c_ulonglong], _I),
     "cvb_solve_opts_from_file": ([ctypes.c_char_p, _P, ctypes.c_char_p, _I], _I),

@@ -20,8 +20,13 @@
 extern PetscInt block_number, immersed; /* main.c, as poisson.c:6-7 declares them */
 extern PetscInt wallfunction;           /* main.c, as bcs.c:3689 declares it */
 extern PetscInt les;                    /* main.c, as rhs.c declares it */
+extern PetscInt rans;                   /* main.c, as rhs.c declares it */
+extern PetscInt ti, tistart;            /* main.c: the time step, as implicitsolver.c declares them */
+extern PetscInt imp_MAX_IT;             /* main.c: the pseudo-time iteration's controls */
+extern PetscReal imp_atol, imp_rtol;
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
+PetscErrorCode ImpRK(UserCtx *user, IBMNodes *ibm, FSInfo *fsi); /* implicitsolver.c:7094 */
 
 static cvb_ctx *g_cvb = NULL;
 static cvb_solve_opts g_opts;
@@ -282,6 +287,50 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
   VecRestoreArray(Ucat, &ucat);
   VecRestoreArray(Ucont, &uc);
   return report(rc, "Convection_GB300");
+}
+
+/* ImpRK (implicitsolver.c:7094-7257) with the reference's arguments.  On one
+ * block with no immersed body, no LES / RANS / wall model and solid walls on
+ * all six faces, the whole pseudo-time iteration runs on the device
+ * (cvb_imp_rk: FormBCS, CalcRHS, the Runge-Kutta stage updates, the norms and
+ * the step halving), with the reference's -cfl, -imp_atol, -imp_rtol,
+ * -imp_MAX_IT and -central; Ucont, Ucat and P come back and their local
+ * copies are refreshed, as the reference leaves them.  Any other
+ * configuration runs the reference's own ImpRK. */
+PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
+  int walls = 1;
+  for (int f = 0; f < 6; f++) walls = walls && u->bctype[f] == 1;
+  if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !walls || !u->Ucont_o ||
+      !u->Ucont_rm1)
+    return ImpRK(u, ibm, fsi);
+  PetscInt central = 0;
+  PetscOptionsGetInt(PETSC_NULL, "-central", &central, PETSC_NULL);
+  PetscScalar *uc, *uo, *urm, *ucat, *p, *ub;
+  VecGetArray(u->Ucont, &uc);
+  VecGetArray(u->Ucont_o, &uo);
+  VecGetArray(u->Ucont_rm1, &urm);
+  VecGetArray(u->Ucat, &ucat);
+  VecGetArray(u->P, &p);
+  VecGetArray(u->Bcs.Ubcs, &ub);
+  cvb_imp_rk_stats st;
+  int rc = cvb_imp_rk(g_cvb, uc, uo, urm, ucat, p, ub, u->ren, u->dt, u->st, u->cfl, (int)ti, (int)tistart,
+                      central ? 1 : 0, imp_atol, imp_rtol, (int)imp_MAX_IT, &st);
+  VecRestoreArray(u->Bcs.Ubcs, &ub);
+  VecRestoreArray(u->P, &p);
+  VecRestoreArray(u->Ucat, &ucat);
+  VecRestoreArray(u->Ucont_rm1, &urm);
+  VecRestoreArray(u->Ucont_o, &uo);
+  VecRestoreArray(u->Ucont, &uc);
+  if (rc) return report(rc, "ImpRK_GB300");
+  PetscPrintf(PETSC_COMM_WORLD, "ImpRK_GB300: %d pseudo-time iterations (%d undone), |dU| %le, rel %le, |F| %le\n",
+              st.pseudo_iterations, st.rejected, st.norm_du, st.rel_du, st.norm_f);
+  DMGlobalToLocalBegin(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+  DMGlobalToLocalEnd(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);
+  DMGlobalToLocalBegin(u->fda, u->Ucat, INSERT_VALUES, u->lUcat);
+  DMGlobalToLocalEnd(u->fda, u->Ucat, INSERT_VALUES, u->lUcat);
+  DMGlobalToLocalBegin(u->da, u->P, INSERT_VALUES, u->lP);
+  DMGlobalToLocalEnd(u->da, u->P, INSERT_VALUES, u->lP);
+  return 0;
 }
 
 PetscErrorCode PoissonFinalize_GB300(void) {

@@ -31,6 +31,11 @@ PetscErrorCode UpdatePressure_GB300(UserCtx *user);
 PetscErrorCode Projection_GB300(UserCtx *user);
 /* In place of Convection (rhs.c:1463), same arguments. */
 PetscErrorCode Convection_GB300(UserCtx *user, Vec Ucont, Vec Ucat, Vec Conv);
+/* In place of ImpRK (implicitsolver.c:7094; Flow_Solver's momentum solver
+ * for implicit 3 or 7, solvers.c:1028 and 1036), same arguments: on the device
+ * for one block with no immersed body and walls on every face, else the
+ * reference's own ImpRK. */
+PetscErrorCode ImpRK_GB300(UserCtx *user, IBMNodes *ibm, FSInfo *fsi);
 /* At the end of the run. */
 PetscErrorCode PoissonFinalize_GB300(void);
 

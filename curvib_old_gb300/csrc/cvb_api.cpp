@@ -153,7 +153,8 @@ static void free_all(cvb_ctx *ctx) {
   ctx->uc_dev = ctx->p_dev = nullptr;
   ctx->ucat_dev = ctx->ubcs_dev = nullptr;
   ctx->conv_dev = ctx->conv_fp = nullptr;
-  ctx->visc_dev = ctx->rct_dev = ctx->rhs_dev = ctx->uo_dev = ctx->urm_dev = nullptr;
+  ctx->visc_dev = ctx->rct_dev = ctx->rhs_dev = ctx->uo_dev = ctx->urm_dev = ctx->pu_dev = nullptr;
+  ctx->imp_norms = nullptr;
   ctx->ibm_cent = nullptr;
   ctx->ready = false;
 }
@@ -1681,12 +1682,16 @@ static int momentum_prepare(cvb_ctx *ctx, const char *who, const double *ucont, 
 
 // FormFunction1's kernels on the device copies: Contra2Cart, Convection,
 // Viscous, then the face values into rhs_dev.
-static void momentum_ff1(cvb_ctx *ctx, double ren, int central) {
+// cart = false: ucat's interior already holds Contra2Cart of the current
+// ucont (FormBCS ran it), so FormFunction1's own call would rewrite the same
+// values.
+static void momentum_ff1(cvb_ctx *ctx, double ren, int central, bool cart = true) {
   const int l = ctx->nlevels - 1;
   LevelDev &F = ctx->L[l];
   const double *fm[9];
   for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
-  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+  if (cart)
+    launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
   launch_convection(F.g, ctx->uc_dev, ctx->ucat_dev, F.nvert, central != 0, ctx->conv_fp, ctx->conv_dev, ctx->stream);
   launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], 1. / ren, ctx->conv_fp,
                  ctx->visc_dev, ctx->stream);
@@ -1757,6 +1762,155 @@ int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const
   launch_calc_rhs(F.g, F.nvert, ctx->uc_dev, ctx->uo_dev, ctx->urm_dev, bdf2, -1. / dt, mz_end, ctx->rhs_dev,
                   ctx->stream);
   return momentum_finish(ctx, ucat, rhs);
+}
+
+// --- FormBCS and ImpRK, all-wall boxes ---------------------------------------
+static int walls_only(cvb_ctx *ctx, const char *who) {
+  const int *bc = ctx->H[ctx->nlevels - 1].d.bctype;
+  for (int f = 0; f < 6; f++)
+    if (bc[f] != 1)
+      return fail(ctx, CVB_BAD_INPUT, "%s: face %d has bctype %d; only solid walls (1) on every face are covered", who,
+                  f, bc[f]);
+  return CVB_OK;
+}
+
+static void form_bcs_dev(cvb_ctx *ctx) {
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  launch_form_bcs_walls(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ubcs_dev, ctx->ucat_dev,
+                        ctx->p_dev, ctx->stream);
+}
+
+int cvb_form_bcs(cvb_ctx *ctx, const double *ucont, const double *ubcs, double *ucat, double *p) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ucont || !ubcs || !ucat || !p) return fail(ctx, CVB_BAD_INPUT, "FormBCS: ucont/ubcs/ucat/p is NULL");
+  TRY(walls_only(ctx, "FormBCS"));
+  const size_t n = ctx->L[ctx->nlevels - 1].g.n();
+  TRY(post_buffers(ctx, n));
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  form_bcs_dev(ctx);
+  CKL();
+  CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(p, ctx->p_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+// The two norms of k_imp_norms, back on the host.
+static int imp_norms(cvb_ctx *ctx, size_t n3, bool du, double *f, double *d) {
+  launch_imp_norms(n3, ctx->rhs_dev, du ? ctx->pu_dev : nullptr, ctx->uc_dev, ctx->imp_norms, ctx->stream);
+  CKL();
+  unsigned long long h[2];
+  CK(cudaMemcpyAsync(h, ctx->imp_norms, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(f, &h[0], sizeof(double));
+  if (d) std::memcpy(d, &h[1], sizeof(double));
+  return CVB_OK;
+}
+
+int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
+               const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart, int central,
+               double imp_atol, double imp_rtol, int imp_max_it, cvb_imp_rk_stats *stats) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ucont || !ucont_o || !ucont_rm1 || !ucat || !p || !ubcs)
+    return fail(ctx, CVB_BAD_INPUT, "ImpRK: ucont/ucont_o/ucont_rm1/ucat/p/ubcs is NULL");
+  if (!(ren != 0.0) || !(dt != 0.0)) return fail(ctx, CVB_BAD_INPUT, "ImpRK: ren / dt is 0");
+  TRY(walls_only(ctx, "ImpRK"));
+  const int l = ctx->nlevels - 1;
+  LevelDev &F = ctx->L[l];
+  const size_t n = F.g.n(), n3 = 3 * n;
+  TRY(post_buffers(ctx, n));
+  if (!ctx->conv_dev) TRY(dalloc(ctx, &ctx->conv_dev, n3));
+  if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
+  if (!ctx->visc_dev) TRY(dalloc(ctx, &ctx->visc_dev, n3));
+  if (!ctx->rct_dev) TRY(dalloc(ctx, &ctx->rct_dev, n3));
+  if (!ctx->rhs_dev) TRY(dalloc(ctx, &ctx->rhs_dev, n3));
+  if (!ctx->uo_dev) TRY(dalloc(ctx, &ctx->uo_dev, n3));
+  if (!ctx->urm_dev) TRY(dalloc(ctx, &ctx->urm_dev, n3));
+  if (!ctx->pu_dev) TRY(dalloc(ctx, &ctx->pu_dev, n3));
+  if (!ctx->imp_norms) TRY(dalloc(ctx, &ctx->imp_norms, 2));
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->uo_dev, ucont_o, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->urm_dev, ucont_rm1, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  // Rhs starts at 0 (VecSet, implicitsolver.c:7140); CalcRHS leaves part of
+  // its ring as it was
+  CK(cudaMemsetAsync(ctx->rhs_dev, 0, sizeof(double) * n3, ctx->stream));
+  const int bdf2 = (ti != tistart && ti != 1) ? 1 : 0;  // COEF_TIME_ACCURACY 1.5 (variables.h:421)
+  const int mz_end = F.g.mz - 3;                        // no convective outflow on an all-wall box
+  auto calc_rhs = [&]() {
+    momentum_ff1(ctx, ren, central, false);
+    launch_calc_rhs(F.g, F.nvert, ctx->uc_dev, ctx->uo_dev, ctx->urm_dev, bdf2, -1. / dt, mz_end, ctx->rhs_dev,
+                    ctx->stream);
+  };
+  // before the loop (implicitsolver.c:7124-7148): InflowFlux and OutflowFlux
+  // leave an all-wall box as it is; FormBCS, pUcont = Ucont, CalcRHS
+  form_bcs_dev(ctx);
+  CK(cudaMemcpyAsync(ctx->pu_dev, ctx->uc_dev, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+  calc_rhs();
+  double normF0, normF1 = 1000., normdU1 = 1000., lambda = cfl;
+  TRY(imp_norms(ctx, n3, false, &normF0, nullptr));
+  const double alfa[4] = {0.25, 1 / 3., 0.5, 1.};  // implicitsolver.c:7111
+  double normdU = 10., reldU = 1., normdU_bk = 0., reldU_bk = 1., normdU0 = 0., normF_bk = 0., relF_bk = 0.;
+  int pseudot = 0, rejected = 0;
+  // implicitsolver.c:7149-7239; the loop ends: pseudot grows by one per kept
+  // iteration, and an undone one halves lambda, which stops at 0.001
+  while (((normdU > imp_atol && reldU > imp_rtol) || pseudot < 1) && pseudot < imp_max_it) {
+    pseudot++;
+    for (int s = 0; s < 4; s++) {
+      const double a = lambda * alfa[s] * dt * st;
+      launch_imp_waxpy(n3, a, ctx->rhs_dev, ctx->pu_dev, ctx->uc_dev, ctx->stream);
+      form_bcs_dev(ctx);
+      calc_rhs();
+    }
+    normdU1 = normdU_bk;
+    const double normF_prev = normF_bk;
+    TRY(imp_norms(ctx, n3, true, &normF_bk, &normdU_bk));
+    if (pseudot == 1) {
+      normdU0 = normdU_bk;
+      reldU_bk = 1.;
+    } else if (normdU0 > 1.e-10) {
+      reldU_bk = normdU_bk / normdU0;
+    }
+    // normF1 takes the previous iteration's |Rhs|, as the reference orders
+    // its statements (implicitsolver.c:7196-7197)
+    if (pseudot > 1) normF1 = normF_prev;
+    if (pseudot == 1) normF0 = normF_bk;
+    relF_bk = normF_bk / normF0;
+    normdU = normdU_bk;
+    reldU = reldU_bk;
+    if (pseudot > 1 && normF_bk > normF1 && normdU_bk > normdU1 && lambda > 0.001) {
+      lambda = 0.5 * lambda;
+      pseudot--;
+      rejected++;
+      CK(cudaMemcpyAsync(ctx->uc_dev, ctx->pu_dev, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+      CK(cudaMemcpyAsync(ctx->pu_dev, ctx->uc_dev, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+      normF1 = normF_bk;
+      normdU1 = normdU_bk;
+    }
+  }
+  CKL();
+  CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(p, ctx->p_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (stats) {
+    stats->pseudo_iterations = pseudot;
+    stats->rejected = rejected;
+    stats->norm_du = normdU;
+    stats->rel_du = reldU;
+    stats->norm_f = normF_bk;
+    stats->rel_f = relF_bk;
+    stats->lambda = lambda;
+  }
+  return CVB_OK;
 }
 
 // Divergence (flow) or MetricsDivergence (metrics) of the finest level.

@@ -94,6 +94,8 @@ struct cvb_ctx {
   double *conv_dev = nullptr, *conv_fp = nullptr;    // Convection: result and face fluxes (allocated on first use)
   // momentum right-hand side (Viscous, FormFunction1, CalcRHS; allocated on first use)
   double *visc_dev = nullptr, *rct_dev = nullptr, *rhs_dev = nullptr, *uo_dev = nullptr, *urm_dev = nullptr;
+  double *pu_dev = nullptr;                // ImpRK: the last kept iterate (pUcont)
+  unsigned long long *imp_norms = nullptr; // ImpRK: |Rhs| and |dU| as bit patterns
   double *ibm_cent = nullptr;  // cell centres of the last cvb_ibm_search that gave them
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;

@@ -314,5 +314,15 @@ void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, co
 // bc: the level's bctype[6]; the host has refused the types it does not cover
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
                                 const double *zet, double *ubcs, double *ucat, cudaStream_t s);
+// FormBCS for a box whose six faces are walls: Contra2Cart, the ghost faces'
+// interior cells, then three rounds of the 12 edge averages of ucat and p
+void launch_form_bcs_walls(const Geom &g, const double *csi, const double *eta, const double *zet,
+                           const double *nvert, const double *ucont, const double *ubcs, double *ucat, double *p,
+                           cudaStream_t s);
+// ImpRK's stage update u = a rhs + pu, and its two infinity norms (|rhs|,
+// |pu - u|; pu null: |rhs| only) as bit patterns into out[0..1] (device)
+void launch_imp_waxpy(size_t n, double a, const double *rhs, const double *pu, double *u, cudaStream_t s);
+void launch_imp_norms(size_t n, const double *rhs, const double *pu, const double *u, unsigned long long *out,
+                      cudaStream_t s);
 
 }  // namespace cvb

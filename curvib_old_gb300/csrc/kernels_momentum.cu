@@ -285,4 +285,64 @@ void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, co
   count_launch();
 }
 
+// ------------------------------------------------------------------- ImpRK
+// One Runge-Kutta stage's update (implicitsolver.c:7156, VecWAXPY):
+// u = a rhs + pu over every entry.
+__global__ void k_imp_waxpy(size_t n, double a, const double *__restrict__ rhs, const double *__restrict__ pu,
+                            double *__restrict__ u) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    u[e] = a * rhs[e] + pu[e];
+}
+
+// The two infinity norms ImpRK takes after its stages (implicitsolver.c:
+// 7183-7200): |rhs| and |pu - u| (VecWAXPY(dU, -1, u, pu)), or |rhs| alone
+// when pu is null.  The largest |x| is exact in any order; non-negative
+// doubles order as their bit patterns, so blocks combine with an integer
+// atomicMax into out[0..1] (zeroed by the host).  NaN entries are passed
+// over, as a comparison-based maximum passes them.
+__global__ void __launch_bounds__(256) k_imp_norms(size_t n, const double *__restrict__ rhs,
+                                                   const double *__restrict__ pu, const double *__restrict__ u,
+                                                   unsigned long long *out) {
+  double mf = 0., md = 0.;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double f = fabs(rhs[e]);
+    if (f > mf) mf = f;
+    if (pu) {
+      const double d = fabs(-1. * u[e] + pu[e]);
+      if (d > md) md = d;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    const double f = __shfl_xor_sync(0xffffffffu, mf, o), d = __shfl_xor_sync(0xffffffffu, md, o);
+    if (f > mf) mf = f;
+    if (d > md) md = d;
+  }
+  __shared__ double sf[8], sd[8];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sf[w] = mf; sd[w] = md; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+      if (sf[q] > mf) mf = sf[q];
+      if (sd[q] > md) md = sd[q];
+    }
+    atomicMax(out, (unsigned long long)__double_as_longlong(mf));
+    if (pu) atomicMax(out + 1, (unsigned long long)__double_as_longlong(md));
+  }
+}
+
+void launch_imp_waxpy(size_t n, double a, const double *rhs, const double *pu, double *u, cudaStream_t s) {
+  k_imp_waxpy<<<blocks_for(n, 256), 256, 0, s>>>(n, a, rhs, pu, u);
+  count_launch();
+}
+
+void launch_imp_norms(size_t n, const double *rhs, const double *pu, const double *u, unsigned long long *out,
+                      cudaStream_t s) {
+  cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), s);
+  // grid-stride over a few blocks per SM, so that few atomics meet
+  const unsigned nb = blocks_for(n, 256) < 2432u ? blocks_for(n, 256) : 2432u;
+  k_imp_norms<<<nb, 256, 0, s>>>(n, rhs, pu, u, out);
+  count_launch();
+}
+
 }  // namespace cvb

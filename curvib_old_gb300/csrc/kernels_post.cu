@@ -208,6 +208,7 @@ struct GhostArgs {
   int bc[6];
   const double *csi, *eta, *zet;  // centre metrics
   double *ub, *u;                 // ubcs, ucat
+  double *p = nullptr;            // FormBCS: the pressure, averaged on the edges with ucat
 };
 
 // The boundary velocity of the special wall types (bcs.c:3776-3975), one face
@@ -240,13 +241,15 @@ __global__ void k_ghost_special(GhostArgs A) {
   ub[2] = ds(u[2], dm(un, nz));
 }
 
-// Non-periodic ghost faces of one axis (bcs.c:4015-4076): the whole face,
-// u = 2 ubcs - u(inner neighbour).
-__global__ void k_ghost_faces(GhostArgs A, int axis) {
+// Non-periodic ghost faces of one axis, u = 2 ubcs - u(inner neighbour): the
+// whole face in GhostNodeVelocity (bcs.c:4015-4076), the face's interior cells
+// in FormBCS (interior != 0, bcs.c:5250-5318).
+__global__ void k_ghost_faces(GhostArgs A, int axis, int interior) {
   const Geom &g = A.g;
   const Face F{axis, (int)blockIdx.z};
   const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y * blockDim.y + threadIdx.y;
   if (a >= F.na(g) || b >= F.nb(g)) return;
+  if (interior && (a < 1 || a > F.na(g) - 2 || b < 1 || b > F.nb(g) - 2)) return;
   const size_t p0 = F.at(g, a, b, 0), p1 = F.at(g, a, b, 1);
 #pragma unroll
   for (int c = 0; c < 3; c++) A.u[3 * p0 + c] = ds(dm(2.0, A.ub[3 * p0 + c]), A.u[3 * p1 + c]);
@@ -273,9 +276,10 @@ __global__ void k_ghost_ring(GhostArgs A, int axis, int whole) {
   for (int c = 0; c < 3; c++) A.u[3 * p0 + c] = A.u[3 * ps + c];
 }
 
-// The 12 edges of the box (bcs.c:4176-4283), each the mean of its two
-// neighbours across the edge, in the reference's order: one block, one edge
-// after the other (edges share corner cells).
+// The 12 edges of the box (bcs.c:4176-4283; FormBCS's, with p beside ucat,
+// bcs.c:5439-5570), each the mean of its two neighbours across the edge, in
+// the reference's order: one block, one edge after the other (edges share
+// corner cells).
 __global__ void k_ghost_edges(GhostArgs A) {
   const Geom &g = A.g;
   const int mx = g.mx, my = g.my, mz = g.mz;
@@ -283,6 +287,7 @@ __global__ void k_ghost_edges(GhostArgs A) {
   auto avg = [&](size_t d, size_t a, size_t b) {
 #pragma unroll
     for (int c = 0; c < 3; c++) A.u[3 * d + c] = mean2(A.u[3 * a + c], A.u[3 * b + c]);
+    if (A.p) A.p[d] = mean2(A.p[a], A.p[b]);
   };
   for (int e = 0; e < 12; e++) {
     const int len = e < 8 ? ((e & 3) < 2 ? my : mx) : mz;
@@ -329,7 +334,7 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
   for (int axis = 0; axis < 3; axis++) {
     if (bc[2 * axis] == 7) continue;
     face_grid(g, axis, 2, grd, blk);
-    k_ghost_faces<<<grd, blk, 0, s>>>(A, axis);
+    k_ghost_faces<<<grd, blk, 0, s>>>(A, axis, 0);
     count_launch();
   }
   // first round: the three axes touch disjoint cells and read only interior
@@ -350,6 +355,35 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
   }
 }
 
+// FormBCS (bcs.c:4436-5889) for a box whose six faces are walls: its loop of
+// three passes (bcs.c:4483) each runs Contra2Cart, the ghost faces on the
+// faces' interior cells and the 12 edges of ucat and p.  Contra2Cart reads
+// only ucont and the faces read only interior cells, so passes two and three
+// give the first pass's values there; only the edges, which read one another's
+// cells at the corners, change between passes.  So: Contra2Cart and the faces
+// once, the edges three times.
+void launch_form_bcs_walls(const Geom &g, const double *csi, const double *eta, const double *zet,
+                           const double *nvert, const double *ucont, const double *ubcs, double *ucat, double *p,
+                           cudaStream_t s) {
+  launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s);
+  GhostArgs A;
+  A.g = g;
+  for (int f = 0; f < 6; f++) A.bc[f] = 1;
+  A.csi = csi; A.eta = eta; A.zet = zet;
+  A.ub = const_cast<double *>(ubcs);  // read only: no special wall type here
+  A.u = ucat;
+  A.p = p;
+  dim3 grd, blk;
+  for (int axis = 0; axis < 3; axis++) {
+    face_grid(g, axis, 2, grd, blk);
+    k_ghost_faces<<<grd, blk, 0, s>>>(A, axis, 1);
+    count_launch();
+  }
+  for (int pass = 0; pass < 3; pass++) {
+    k_ghost_edges<<<1, 256, 0, s>>>(A);
+    count_launch();
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Convection (rhs.c:1463-1946).  The face

@@ -233,6 +233,27 @@ class PoissonContext:
                                          float(dt), int(ti), int(tistart), int(central), ptr(out)))
         return out, u
 
+    def form_bcs(self, ucont, ubcs, ucat, p):
+        """FormBCS (bcs.c:4436) on an all-wall box: (ucat, p)."""
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        pp = np.array(p, dtype=np.float64, copy=True, order="C")
+        self._check(self._L.cvb_form_bcs(self._ctx, ptr(_c64(ucont)), ptr(_c64(ubcs)), ptr(u), ptr(pp)))
+        return u, pp
+
+    def imp_rk(self, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=False,
+               atol=1e-7, rtol=1e-4, max_it=50):
+        """ImpRK (implicitsolver.c:7094) on an all-wall box with no immersed
+        body: (ucont, ucat, p, stats dict)."""
+        uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        pp = np.array(p, dtype=np.float64, copy=True, order="C")
+        st_ = _lib.ImpRKStats()
+        self._check(self._L.cvb_imp_rk(self._ctx, ptr(uc), ptr(_c64(ucont_o)), ptr(_c64(ucont_rm1)), ptr(u), ptr(pp),
+                                       ptr(_c64(ubcs)), float(ren), float(dt), float(st), float(cfl), int(ti),
+                                       int(tistart), int(central), float(atol), float(rtol), int(max_it),
+                                       ctypes.byref(st_)))
+        return uc, u, pp, st_.as_dict()
+
     def metrics_divergence(self):
         """MetricsDivergence (metrics.c:1551): (max |div of the metrics|, its
         index in the box) on the finest level."""

@@ -21,6 +21,8 @@
  *   Viscous           (rhs.c:1947)      -> cvb_viscous
  *   FormFunction1     (rhs.c:2567)      -> cvb_form_function1
  *   CalcRHS   (implicitsolver.c:6449)   -> cvb_calc_rhs
+ *   FormBCS   (bcs.c:4436), walls       -> cvb_form_bcs
+ *   ImpRK     (implicitsolver.c:7094)   -> cvb_imp_rk
  *   ibm_search_advanced (ibm.c:4197), its nvert classification
  *                                       -> cvb_ibm_search
  *
@@ -254,6 +256,43 @@ int cvb_form_function1(cvb_ctx *ctx, const double *ucont, double *ucat, const do
  * the convective-outflow term on the last k face before those loops). */
 int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
                  const double *p, double ren, double dt, int ti, int tistart, int central, double *rhs);
+/* FormBCS (bcs.c:4436-5889) for a box whose six faces are solid walls
+ * (bctype 1; any other type is refused with CVB_BAD_INPUT): Contra2Cart of
+ * ucont into ucat's interior cells, the ghost faces u = 2 ubcs - inner on the
+ * faces' interior cells, and the means of ucat and p on the box's 12 edges,
+ * through the reference's three passes.  ucat and p ([mz][my][mx](x3) and
+ * [mz][my][mx]) are read and written, ubcs (Bcs.Ubcs) is read.  Bit for bit
+ * the reference's. */
+int cvb_form_bcs(cvb_ctx *ctx, const double *ucont, const double *ubcs, double *ucat, double *p);
+/* What cvb_imp_rk did: the pseudo-time iterations kept (pseudot at the end),
+ * those undone with the step halved, and the last iteration's norms. */
+typedef struct {
+  int pseudo_iterations;
+  int rejected;
+  double norm_du;   /* max |Ucont change| of the last iteration */
+  double rel_du;    /* norm_du / its first value */
+  double norm_f;    /* max |Rhs| after the last iteration */
+  double rel_f;     /* norm_f / its first value */
+  double lambda;    /* the pseudo-time step factor at the end (cfl, halved per undone iteration) */
+} cvb_imp_rk_stats;
+/* ImpRK (implicitsolver.c:7094-7257), the momentum equation's pseudo-time
+ * iteration, for a box whose six faces are solid walls, one block, as the
+ * reference runs it with immersed 0 (no immersed-boundary interpolation
+ * between iterations; nvert's blocked cells still mask the fluxes):
+ * InflowFlux and OutflowFlux change nothing on such a box; FormBCS as
+ * cvb_form_bcs and CalcRHS as cvb_calc_rhs; per pseudo-time iteration four
+ * Runge-Kutta stages Ucont = (lambda alfa_s dt st) Rhs + Ucont_prev with alfa
+ * 1/4, 1/3, 1/2, 1 and lambda starting at cfl; an iteration whose |Rhs| and
+ * |dU| both grew is undone with lambda halved (while lambda > 0.001); the loop
+ * ends when |dU| <= imp_atol or |dU| / |dU|_first <= imp_rtol, or after
+ * imp_max_it iterations.  ucont (Ucont), ucat (Ucat) and p (P) are read and
+ * written, ucont_o / ucont_rm1 are the two previous steps' fluxes, ubcs the
+ * wall velocity.  Results equal the reference's bit for bit; stats may be
+ * NULL.  The iteration runs on the device; the host reads two norms per
+ * iteration. */
+int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
+               const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart, int central,
+               double imp_atol, double imp_rtol, int imp_max_it, cvb_imp_rk_stats *stats);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
  * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and

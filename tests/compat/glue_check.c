@@ -18,6 +18,8 @@
 #include "poisson_gb300.h"
 
 extern PetscInt block_number, immersed, wallfunction, les;
+extern PetscInt ti, tistart, imp_MAX_IT;
+extern PetscReal imp_atol, imp_rtol;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
 UserMG *ref_usermg(void);
@@ -179,6 +181,42 @@ int main(void) {
   CHECK(shim_vec_data(ConvL)[0] == 0.0, "Conv's ghost cells not 0");
   VecDestroy(&ConvL);
   CHECK(shim_arrays_out() == 0, "convection left %d arrays out", shim_arrays_out());
+
+  /* --- ImpRK: one block, immersed 0, walls on every face: on the device with
+   * the block's and the run's controls; a failure comes back as the status --- */
+  int bsave[6];
+  for (int f = 0; f < 6; f++) { bsave[f] = fine->bctype[f]; fine->bctype[f] = 1; }
+  VecDuplicate(fine->Ucont, &fine->Ucont_o);
+  VecDuplicate(fine->Ucont, &fine->Ucont_rm1);
+  const PetscInt imm_keep = immersed;
+  immersed = 0;
+  fine->cfl = 0.3;
+  fine->ren = 250.0;
+  ti = 4;
+  tistart = 1;
+  imp_MAX_IT = 7;
+  imp_atol = 2e-7;
+  imp_rtol = 3e-4;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.n_imp_rk == 1, "ImpRK not on the device");
+  CHECK(REC.ucont_imp == shim_vec_data(fine->Ucont) && REC.uo_imp == shim_vec_data(fine->Ucont_o) &&
+            REC.urm_imp == shim_vec_data(fine->Ucont_rm1) && REC.ucat_imp == shim_vec_data(fine->Ucat) &&
+            REC.p_imp == shim_vec_data(fine->P) && REC.ubcs_imp == shim_vec_data(fine->Bcs.Ubcs),
+        "Ucont / Ucont_o / Ucont_rm1 / Ucat / P / Bcs.Ubcs storage");
+  CHECK(REC.ren_imp == 250.0 && REC.dt_imp == fine->dt && REC.st_imp == fine->st && REC.cfl_imp == 0.3 &&
+            REC.ti_imp == 4 && REC.tistart_imp == 1 && REC.central_imp == 0 && REC.atol_imp == 2e-7 &&
+            REC.rtol_imp == 3e-4 && REC.max_it_imp == 7,
+        "ImpRK controls");
+  CHECK(shim_vec_data(fine->lUcont)[3 * loc] == 11.0 && shim_vec_data(fine->lUcat)[3 * loc + 1] == 12.0 &&
+            shim_vec_data(fine->lP)[loc] == 13.0,
+        "lUcont / lUcat / lP not refreshed after ImpRK");
+  PetscOptionsSetValue("-central", "1");
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.central_imp == 1, "-central not passed to ImpRK");
+  PetscOptionsSetValue("-central", "0");
+  REC.fail_next = CVB_NAN_DETECTED;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == CVB_NAN_DETECTED, "ImpRK failure not returned");
+  CHECK(shim_arrays_out() == 0, "ImpRK left %d arrays out", shim_arrays_out());
+  immersed = imm_keep;
+  for (int f = 0; f < 6; f++) fine->bctype[f] = bsave[f];
 
   /* --- failures come back as the call's status, arrays restored --- */
   REC.fail_next = CVB_NOT_CONVERGED;

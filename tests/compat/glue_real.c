@@ -12,7 +12,9 @@
  *   Projection_GB300        -> Ucont bit for bit (Projection's flux correction)
  *                              and Ucat bit for bit (Contra2Cart, then
  *                              GhostNodeVelocity);
- *   Convection_GB300        -> Conv bit for bit (Convection).
+ *   Convection_GB300        -> Conv bit for bit (Convection);
+ *   ImpRK_GB300             -> Ucont, Ucat and P bit for bit (ImpRK with
+ *                              immersed 0, on the fields the projection left).
  *
  * usage: glue_real fp64|mixed  -> prints one line per failed check, exits with their count
  */
@@ -40,6 +42,11 @@ int ref_update_and_project(double dt, double st, double *p, double *phi, double 
 int ref_contra2cart(const double *ucont, double *ucat);
 int ref_ghost_node_velocity(double *ubcs, double *ucat);
 int ref_convection(const double *ucont, const double *ucat, int central, double *conv);
+int ref_imp_rk(double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
+               const double *ubcs, double ren, double dt, double st, double cfl, int ti_, int tistart_, int central,
+               double atol, double rtol, int max_it);
+extern PetscInt ti, tistart, imp_MAX_IT;
+extern PetscReal imp_atol, imp_rtol;
 
 static int g_checks = 0, g_fail = 0;
 #define CHECK(cond, ...)                          \
@@ -165,6 +172,14 @@ int main(int argc, char **argv) {
     STEP("convection");
     double *conv_r = (double *)calloc(3 * n, sizeof(double));
     ref_convection(uc_b2, ucat_r, 0, conv_r);
+    STEP("imp_rk");
+    double *im_uo = copy_of(uc_r2, 3 * n), *im_urm = copy_of(uc_r2, 3 * n), *im_ub = calloc(3 * n, sizeof(double));
+    for (size_t q = 0; q < 3 * n; q++) { im_uo[q] *= 0.99; im_urm[q] *= 0.97; }
+    immersed = 0;
+    ref_imp_rk(uc_r2, im_uo, im_urm, ucat_r, p_r, im_ub, 300.0, 2e-3, 1.0, 0.5, 5, 0, 0, 1e-7, 1e-4, 6);
+    int finite = 1;
+    for (size_t q = 0; q < 3 * n; q++) finite = finite && isfinite(uc_r2[q]);
+    printf("imp_rk finite %d, max |Ucont| %.3e\n", finite, maxabs(uc_r2, 3 * n));
     STEP("done");
     return 0;
   }
@@ -184,6 +199,36 @@ int main(int argc, char **argv) {
   STEP("Convection_GB300");
   CHECK(Convection_GB300(fine, fine->Ucont, fine->Ucat, Conv) == 0, "Convection_GB300 failed");
   double *conv_b = copy_of(shim_vec_data(Conv), 3 * n);
+  /* the momentum equation's pseudo-time iteration on the projected fields:
+   * previous steps' fluxes close to Ucont, no-slip walls, immersed 0 */
+  STEP("ImpRK_GB300");
+  const double imp_dt = 2e-3, imp_cfl = 0.5, imp_ren = 300.0;
+  double *im_uc = copy_of(uc_b2, 3 * n), *im_uo = copy_of(uc_b2, 3 * n), *im_urm = copy_of(uc_b2, 3 * n);
+  for (size_t q = 0; q < 3 * n; q++) { im_uo[q] *= 0.99; im_urm[q] *= 0.97; }
+  double *im_ucat = copy_of(ucat_b, 3 * n), *im_p = copy_of(p_b, n), *im_ub = (double *)calloc(3 * n, sizeof(double));
+  if (!fine->Ucont_o) VecDuplicate(fine->Ucont, &fine->Ucont_o);
+  if (!fine->Ucont_rm1) VecDuplicate(fine->Ucont, &fine->Ucont_rm1);
+  memcpy(shim_vec_data(fine->Ucont), im_uc, sizeof(double) * 3 * n);
+  memcpy(shim_vec_data(fine->Ucont_o), im_uo, sizeof(double) * 3 * n);
+  memcpy(shim_vec_data(fine->Ucont_rm1), im_urm, sizeof(double) * 3 * n);
+  memcpy(shim_vec_data(fine->Ucat), im_ucat, sizeof(double) * 3 * n);
+  memcpy(shim_vec_data(fine->P), im_p, sizeof(double) * n);
+  memcpy(shim_vec_data(fine->Bcs.Ubcs), im_ub, sizeof(double) * 3 * n);
+  const double dt_keep = fine->dt;
+  fine->dt = imp_dt;
+  fine->cfl = imp_cfl;
+  fine->ren = imp_ren;
+  immersed = 0;
+  ti = 5;
+  tistart = 0;
+  imp_MAX_IT = 6;
+  imp_atol = 1e-7;
+  imp_rtol = 1e-4;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0, "ImpRK_GB300 failed");
+  double *im_uc_b = copy_of(shim_vec_data(fine->Ucont), 3 * n), *im_ucat_b = copy_of(shim_vec_data(fine->Ucat), 3 * n),
+         *im_p_b = copy_of(shim_vec_data(fine->P), n);
+  immersed = 1;
+  fine->dt = dt_keep;
   CHECK(PoissonFinalize_GB300() == 0, "PoissonFinalize_GB300 failed");
 
   /* --- the reference's own routines on the same inputs --- */
@@ -236,6 +281,16 @@ int main(int argc, char **argv) {
   ref_convection(uc_b2, ucat_b, 0, conv_r);
   CHECK(same(conv_r, conv_b, 3 * n), "Convection: Conv differs");
 
+  /* ImpRK's own run on the same inputs (it leaves Converge_dU0 in the
+   * working directory) */
+  STEP("ImpRK");
+  immersed = 0;
+  ref_imp_rk(im_uc, im_uo, im_urm, im_ucat, im_p, im_ub, imp_ren, imp_dt, 1.0, imp_cfl, 5, 0, 0, 1e-7, 1e-4, 6);
+  int finite = 1;
+  for (size_t q = 0; q < 3 * n; q++) finite = finite && isfinite(im_uc[q]);
+  CHECK(finite, "ImpRK: Ucont not finite");
+  CHECK(same(im_uc, im_uc_b, 3 * n) && same(im_ucat, im_ucat_b, 3 * n) && same(im_p, im_p_b, n),
+        "ImpRK: Ucont / Ucat / P differ");
   printf("glue_real (%s): %d checks, %d failures\n", mixed ? "mixed" : "fp64", g_checks, g_fail);
   return g_fail;
 }

@@ -38,7 +38,7 @@ def test_binding_on_the_real_library_matches_reference(tmp_path, precision):
     subprocess.run(["gcc", "-std=gnu99", "-O1", "-ffp-contract=off", "-g", "-rdynamic", "-w", str(PRE / "poisson_gb300.i"), str(PRE / "glue_real.i"),
                     "-L", str(lib.parent), "-lcvb", f"-Wl,-rpath,{lib.parent}", "-L", str(ref.parent), "-lcvbref",
                     f"-Wl,-rpath,{ref.parent}", "-lm", "-o", str(exe)], check=True)
-    r = subprocess.run([str(exe), precision], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([str(exe), precision], capture_output=True, text=True, timeout=300, cwd=tmp_path)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 failures" in r.stdout

@@ -5,8 +5,9 @@ Viscous (rhs.c:1947), FormFunction1 (rhs.c:2567) and CalcRHS
 central, first step and second-order backward; on box_sphere also with the
 cells whose tangential pressure derivative the reference leaves unassigned
 (cases.MOM_EDGES: the value of the previous cell in its loop order stands)
-and with a convective-outflow face.  The oracle is pinned to the reference's
-own routines (tests/test_oracle_pin.py).  Results are compared as bytes, so
+and with a convective-outflow face; FormBCS (bcs.c:4436) and the pseudo-time
+iteration ImpRK (implicitsolver.c:7094) on the all-wall scenarios.  The oracle
+is pinned to the reference's own routines (tests/test_oracle_pin.py).  Results are compared as bytes, so
 signed zeros count; the periodic boxes are refused.
 """
 import types
@@ -66,5 +67,59 @@ def test_momentum_rhs_refuses_periodic_boxes():
         with pytest.raises(CvbError) as e:
             ctx.form_function1(c["ucont"], ucat0, p, MOM_REN)
         assert e.value.status == CVB_BAD_INPUT
+    finally:
+        ctx.close()
+
+
+WALLED = [n for n in sorted(SCENARIOS) if not any(SCENARIOS[n][1])]
+
+
+@pytest.mark.parametrize("name", WALLED)
+def test_form_bcs_and_imp_rk_match_oracle(name):
+    """FormBCS (bcs.c:4436) and the pseudo-time iteration ImpRK
+    (implicitsolver.c:7094) on the all-wall scenarios, bit for bit against the
+    oracle, which is pinned to the reference's own routines: converged, stopped
+    at imp_MAX_IT, and with iterations undone and the step halved (the counts
+    checked too); on box_sphere also with cells.MOM_EDGES' nvert."""
+    from cases import IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, imp_rk_inputs
+    c = build(name)
+    for nvert in ([c["nvert"], mom_edge_nvert(c["nvert"])] if name == "box_sphere" else [c["nvert"]]):
+        bctype = list(c["bctype"])
+        ctx = _ctx(c, nvert, bctype)
+        try:
+            L = O.OLevel(c["metrics"][-1], nvert, bctype, c["semi"])
+            ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(nvert.shape, c["ucont"])
+            u_g, p_g = ctx.form_bcs(c["ucont"], ubcs1, ucat1, p1)
+            rc, u_o, p_o = O.form_bcs_walls(L, c["ucont"], ubcs1, ucat1, p1)
+            assert rc == 0 and _same(u_g, u_o) and _same(p_g, p_o)
+            rejected = 0
+            for ti, cfl, max_it in IMP_RK_RUNS:
+                uc_g, u_g, p_g, st_g = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
+                                                  ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it)
+                rc, uc_o, u_o, p_o, st_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0,
+                                                    cfl, ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it)
+                assert rc == 0
+                assert (st_g["pseudo_iterations"], st_g["rejected"]) == (st_o.pseudo_iterations, st_o.rejected)
+                assert st_g["lambda"] == st_o.lambda_ and st_g["norm_du"] == st_o.norm_du
+                assert _same(uc_g, uc_o) and _same(u_g, u_o) and _same(p_g, p_o), (ti, cfl, max_it)
+                rejected += st_o.rejected
+            assert rejected > 0  # the halving branch ran
+        finally:
+            ctx.close()
+
+
+def test_imp_rk_refuses_other_face_types():
+    from curvib_old_gb300._lib import CVB_BAD_INPUT, CvbError
+    from cases import imp_rk_inputs
+    c = build("box_sphere")
+    bctype = list(c["bctype"][:5]) + [8]
+    ctx = _ctx(c, c["nvert"], bctype)
+    try:
+        ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(c["nvert"].shape, c["ucont"])
+        for call in (lambda: ctx.form_bcs(c["ucont"], ubcs1, ucat1, p1),
+                     lambda: ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, 1.0, 1, 0)):
+            with pytest.raises(CvbError) as e:
+                call()
+            assert e.value.status == CVB_BAD_INPUT
     finally:
         ctx.close()
