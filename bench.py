@@ -458,29 +458,45 @@ def bench_serve(args, local):
     return out
 
 
-def full_step(args, ws, ctx, P, dt, st, rtol, pinned, with_cpu):
-    """Time steps of the fractional-step method on the projection step's box,
-    marching: ImpRK (the momentum equation's pseudo-time iteration, four
-    Runge-Kutta stages of FormBCS + CalcRHS per iteration, imp_atol 1e-7,
-    imp_rtol 1e-4, imp_MAX_IT 50 as the reference's defaults, cfl 0.05), then
+def full_step(args, ws, local, dt, st, rtol, pinned, with_cpu):
+    """Config 2's time step at 192^3 cells: the projection step's distorted box
+    and sphere, Re 300, dt 2e-3, with an inlet on the k = 0 face (bctype[4] 5,
+    the reference's uniform profile 1: speed 2 along the face normal) and an
+    outlet on the last k face (bctype[5] 4: the reference's outflow with its
+    flux correction), walls on the x and y faces.  Marching: ImpRK (the
+    momentum equation's pseudo-time iteration, four Runge-Kutta stages of
+    InflowFlux + FormBCS + CalcRHS per iteration, imp_atol 1e-7, imp_rtol
+    1e-4, imp_MAX_IT 50 as the reference's defaults, cfl 0.05), then
     PoissonSolver_MG (mixed, to 1e-8), UpdatePressure and Projection, then
     Ucont_rm1 <- Ucont_o <- Ucont; every call through the C ABI on pinned host
-    arrays.  The box's faces are walls; the sphere enters through nvert alone
-    (the reference's immersed-boundary interpolation between iterations is not
-    part of this path)."""
+    arrays.  The sphere enters through nvert alone (the reference's
+    immersed-boundary interpolation between iterations is not part of this
+    path).  The start is a uniform stream through the box: Ucont.z = 2 |zet|
+    on the k faces between fluid cells."""
     import torch
 
     from curvib_old_gb300 import _lib
+    from curvib_old_gb300 import workload as W
+    from curvib_old_gb300.solver import PoissonContext
     L, ptr = _lib.lib(), _lib.ptr
     # cfl: the reference's default 0.2 makes the last stage's pseudo-time step
     # (0.2 dt) about 9 times the explicit viscous limit of the wall cells of
     # this stretched grid (h_y 7.6e-4 at Re 300), and the iteration blows up to
     # NaN in its first iterations, in the reference's arithmetic as here; 0.05
     # is inside the limit (the 48^3 and 96^3 boxes converge at 0.2)
-    ren, cfl, atol, itol, max_it = 300.0, 0.05, 1e-7, 1e-4, 50
+    ren, cfl, atol, itol, max_it, profile = 300.0, 0.05, 1e-7, 1e-4, 50, 1
+    P = W.make_problem((192, 192, 192), (1.0, 1.0, 1.0), 2.0, True, (False, False, False), [(0.5, 0.5, 0.5, 0.25)],
+                       name="box192-sphere-inout")
+    P.bctype = [1, 1, 1, 1, 5, 4]
+    ctx = PoissonContext(local).setup(P)
     shape = P.nvert.shape
-    uc = pinned(P.ucont)
-    uo, urm = pinned(P.ucont), pinned(P.ucont)
+    zet = P.metrics[-1]["Zet"]
+    nv = P.nvert
+    u0 = np.zeros(shape + (3,))
+    fluid = (nv[:-1] < 0.1) & (nv[1:] < 0.1)
+    u0[:-1, 1:-1, 1:-1, 2] = np.where(fluid[:, 1:-1, 1:-1], 2.0 * np.sqrt((zet[:-1, 1:-1, 1:-1] ** 2).sum(-1)), 0.0)
+    uc = pinned(u0)
+    uo, urm = pinned(u0), pinned(u0)
     ucat, ubcs, p, phi = (pinned(np.zeros(shape + (3,))), pinned(np.zeros(shape + (3,))), pinned(np.zeros(shape)),
                           pinned(np.zeros(shape)))
     o = _lib.default_opts(precision=_lib.MIXED, rtol=rtol, max_it=200)
@@ -488,16 +504,17 @@ def full_step(args, ws, ctx, P, dt, st, rtol, pinned, with_cpu):
     rec = []
     steps = max(2, min(3, args.step_steps))
     for ti in range(1, steps + 1):
+        io = _lib.imp_rk_opts(ren=ren, dt=dt, st=st, cfl=cfl, ti=ti, tistart=0, imp_atol=atol, imp_rtol=itol,
+                              imp_max_it=max_it, inletprofile=profile)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rc = L.cvb_imp_rk(ctx._ctx, ptr(uc.numpy()), ptr(uo.numpy()), ptr(urm.numpy()), ptr(ucat.numpy()),
-                          ptr(p.numpy()), ptr(ubcs.numpy()), ren, dt, st, cfl, ti, 0, 0, atol, itol, max_it,
-                          ctypes.byref(ist))
-        assert rc == 0, rc
+                          ptr(p.numpy()), ptr(ubcs.numpy()), ctypes.byref(io), ctypes.byref(ist))
+        assert rc == 0, (rc, L.cvb_last_error(ctx._ctx))
         t1 = time.perf_counter()
         rc = L.cvb_poisson_solver_mg(ctx._ctx, ptr(uc.numpy()), 0.0, 1, dt, st, ptr(phi.numpy()), ctypes.byref(o),
                                      ctypes.byref(stt))
-        assert rc == 0, rc
+        assert rc == 0, (rc, L.cvb_last_error(ctx._ctx))
         assert L.cvb_update_pressure(ctx._ctx, ptr(p.numpy()), ptr(phi.numpy())) == 0
         assert L.cvb_projection_cart(ctx._ctx, ptr(phi.numpy()), dt, st, ptr(uc.numpy()), ptr(ubcs.numpy()),
                                      ptr(ucat.numpy())) == 0
@@ -506,25 +523,33 @@ def full_step(args, ws, ctx, P, dt, st, rtol, pinned, with_cpu):
         urm.numpy()[...] = uo.numpy()
         uo.numpy()[...] = uc.numpy()
         rec.append({"ti": ti, "imp_rk_ms": (t1 - t0) * 1e3, "pseudo_iterations": ist.pseudo_iterations,
-                    "rejected": ist.rejected, "rel_du": ist.rel_du, "projection_ms": (t2 - t1) * 1e3,
-                    "poisson_iterations": stt.iterations})
+                    "rejected": ist.rejected, "rel_du": ist.rel_du, "flux_in_sum": ist.flux_in_sum,
+                    "projection_ms": (t2 - t1) * 1e3, "poisson_iterations": stt.iterations,
+                    "rel_residual": stt.rel_residual})
     stages = sum(4 * (r["pseudo_iterations"] + r["rejected"]) for r in rec)
     imp = sum(r["imp_rk_ms"] for r in rec)
-    out = {"steps": rec, "ms_per_step": sum(r["imp_rk_ms"] + r["projection_ms"] for r in rec) / len(rec),
-           "imp_rk_ms_per_stage": imp / stages,
-           "note": "first-order time term at ti 1, BDF2 after; ubcs 0 (no-slip walls); the pseudo-time loop keeps "
-                   "the reference's order of norms and its halving of the step"}
+    maxdiv, at = ctypes.c_double(), ctypes.c_longlong()
+    assert L.cvb_divergence(ctx._ctx, ptr(uc.numpy()), ctypes.byref(maxdiv), ctypes.byref(at)) == 0
+    out = {"workload": "192^3 cells, the projection step's box and sphere, inlet (bctype[4] 5, profile 1) on k = 0, "
+                       "outlet (bctype[5] 4) on the last k face, walls on x and y, Re 300, dt 2e-3",
+           "steps": rec, "ms_per_step": sum(r["imp_rk_ms"] + r["projection_ms"] for r in rec) / len(rec),
+           "imp_rk_ms_per_stage": imp / stages, "max_divergence_after": maxdiv.value,
+           "note": "first-order time term at ti 1, BDF2 after; the pseudo-time loop keeps the reference's order of "
+                   "norms and its halving of the step"}
     if with_cpu:
-        # the oracle's FormBCS + CalcRHS (one Runge-Kutta stage) on the same
-        # arrays, once, on one core
+        # the oracle's InflowFlux + FormBCS + CalcRHS (one Runge-Kutta stage)
+        # on the same arrays, once, on one core
         from oracle import oracle as O
         Lo = O.OLevel(P.metrics[-1], P.nvert, P.bctype, P.semi)
         t0 = time.perf_counter()
-        O.form_bcs_walls(Lo, uc.numpy(), ubcs.numpy(), ucat.numpy(), p.numpy())
-        O.calc_rhs(Lo, uc.numpy(), uo.numpy(), urm.numpy(), ucat.numpy(), p.numpy(), ren, dt, 5, 0)
+        _, ucx, ubx, f = O.inflow_flux(Lo, uc.numpy(), ubcs.numpy(), profile)
+        _, ucx, ubx, ux, px = O.form_bcs(Lo, ucx, ubx, ucat.numpy(), p.numpy(), f, 0.0)
+        O.calc_rhs(Lo, ucx, uo.numpy(), urm.numpy(), ux, px, ren, dt, 5, 0)
         sec = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": sec * 1e3, "unit": "ms per Runge-Kutta stage", "cores": 1, "kind": "port",
-                               "sample": "one FormBCS + CalcRHS stage of the oracle on the same 192^3 arrays"}
+                               "sample": "one InflowFlux + FormBCS + CalcRHS stage of the oracle on the same 192^3 "
+                                         "arrays"}
+    ctx.close()
     return out
 
 
@@ -618,7 +643,7 @@ def bench_step(args, ws, local, with_cpu):
         phis[name] = phi.numpy().copy()
     out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
     out["err_vs_fp64"] = phi_err(phis["mixed"], phis["fp64"], P.nvert)
-    out["full_step"] = full_step(args, ws, ctx, P, dt, st, rtol, pinned, with_cpu)
+    out["full_step"] = full_step(args, ws, local, dt, st, rtol, pinned, with_cpu)
     # the 19-point kernels of a distorted grid (7.3 M cells, far beyond L2)
     out["roofline_19pt"] = roofline(ctx, orthogonal=False)
     # the post-projection kernels and the momentum step's convective term

@@ -52,9 +52,26 @@ class SolveStats(ctypes.Structure):
         return d
 
 
+class ImpRKOpts(ctypes.Structure):
+    _fields_ = [("ren", _D), ("dt", _D), ("st", _D), ("cfl", _D), ("ti", _I), ("tistart", _I), ("central", _I),
+                ("imp_atol", _D), ("imp_rtol", _D), ("imp_max_it", _I), ("inletprofile", _I),
+                ("flux_intp_sum", _D)]
+
+
+def imp_rk_opts(**kw):
+    """cvb_imp_rk_opts with the reference's defaults, overridden by keywords."""
+    o = ImpRKOpts()
+    lib().cvb_imp_rk_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise AttributeError(k)
+        setattr(o, k, v)
+    return o
+
+
 class ImpRKStats(ctypes.Structure):
     _fields_ = [("pseudo_iterations", _I), ("rejected", _I), ("norm_du", _D), ("rel_du", _D), ("norm_f", _D),
-                ("rel_f", _D), ("lambda_", _D)]
+                ("rel_f", _D), ("lambda_", _D), ("flux_in_sum", _D)]
 
     def as_dict(self):
         return {f.rstrip("_"): getattr(self, f) for f, _ in self._fields_}
@@ -121,8 +138,10 @@ EXPORTS = {
     "cvb_viscous": ([_P, _P, _D, _P], _I),
     "cvb_form_function1": ([_P, _P, _P, _P, _D, _I, _P], _I),
     "cvb_calc_rhs": ([_P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P], _I),
-    "cvb_form_bcs": ([_P, _P, _P, _P, _P], _I),
-    "cvb_imp_rk": ([_P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _D, _I, _I, _I, _D, _D, _I, _P], _I),
+    "cvb_inflow_flux": ([_P, _P, _P, _I, _P], _I),
+    "cvb_form_bcs": ([_P, _P, _P, _P, _P, _D, _D], _I),
+    "cvb_imp_rk_opts_default": ([_P], None),
+    "cvb_imp_rk": ([_P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "cvb_device_bytes": ([_P, _P], _I),
     "cvb_set_device_limit": ([_P, ctypes.c_ulonglong], _I),
     "cvb_solve_opts_from_file": ([ctypes.c_char_p, _P, ctypes.c_char_p, _I], _I),

@@ -24,6 +24,8 @@ extern PetscInt rans;                   /* main.c, as rhs.c declares it */
 extern PetscInt ti, tistart;            /* main.c: the time step, as implicitsolver.c declares them */
 extern PetscInt imp_MAX_IT;             /* main.c: the pseudo-time iteration's controls */
 extern PetscReal imp_atol, imp_rtol;
+extern PetscInt inletprofile;           /* main.c: InflowFlux's profile */
+extern PetscReal FluxInSum;             /* main.c: InflowFlux's result, as bcs.c:5 declares it */
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 PetscErrorCode ImpRK(UserCtx *user, IBMNodes *ibm, FSInfo *fsi); /* implicitsolver.c:7094 */
@@ -290,17 +292,21 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
 }
 
 /* ImpRK (implicitsolver.c:7094-7257) with the reference's arguments.  On one
- * block with no immersed body, no LES / RANS / wall model and solid walls on
- * all six faces, the whole pseudo-time iteration runs on the device
- * (cvb_imp_rk: FormBCS, CalcRHS, the Runge-Kutta stage updates, the norms and
- * the step halving), with the reference's -cfl, -imp_atol, -imp_rtol,
- * -imp_MAX_IT and -central; Ucont, Ucat and P come back and their local
- * copies are refreshed, as the reference leaves them.  Any other
- * configuration runs the reference's own ImpRK. */
+ * block with no immersed body, no LES / RANS / wall model, solid walls on the
+ * x and y faces and on the k faces walls or an inlet (5, a constant profile)
+ * with an outlet (4), the whole pseudo-time iteration runs on the device
+ * (cvb_imp_rk: InflowFlux, FormBCS, CalcRHS, the Runge-Kutta stage updates,
+ * the norms and the step halving), with the reference's -cfl, -imp_atol,
+ * -imp_rtol, -imp_MAX_IT, -inlet (inletprofile) and -central and the block's
+ * FluxIntpSum; Ucont, Bcs.Ubcs, Ucat and P come back and the local copies
+ * are refreshed, as the reference leaves them.  Any other configuration runs
+ * the reference's own ImpRK. */
 PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
-  int walls = 1;
-  for (int f = 0; f < 6; f++) walls = walls && u->bctype[f] == 1;
-  if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !walls || !u->Ucont_o ||
+  const PetscInt *bt = u->bctype;
+  int covered = bt[0] == 1 && bt[1] == 1 && bt[2] == 1 && bt[3] == 1 && (bt[4] == 1 || bt[4] == 5) &&
+                (bt[5] == 1 || bt[5] == 4) && ((bt[4] == 5) == (bt[5] == 4));
+  if (bt[4] == 5) covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11);
+  if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !covered || !u->Ucont_o ||
       !u->Ucont_rm1)
     return ImpRK(u, ibm, fsi);
   PetscInt central = 0;
@@ -312,9 +318,22 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
   VecGetArray(u->Ucat, &ucat);
   VecGetArray(u->P, &p);
   VecGetArray(u->Bcs.Ubcs, &ub);
+  cvb_imp_rk_opts o;
+  cvb_imp_rk_opts_default(&o);
+  o.ren = u->ren;
+  o.dt = u->dt;
+  o.st = u->st;
+  o.cfl = u->cfl;
+  o.ti = (int)ti;
+  o.tistart = (int)tistart;
+  o.central = central ? 1 : 0;
+  o.imp_atol = imp_atol;
+  o.imp_rtol = imp_rtol;
+  o.imp_max_it = (int)imp_MAX_IT;
+  o.inletprofile = (int)inletprofile;
+  o.flux_intp_sum = u->FluxIntpSum;
   cvb_imp_rk_stats st;
-  int rc = cvb_imp_rk(g_cvb, uc, uo, urm, ucat, p, ub, u->ren, u->dt, u->st, u->cfl, (int)ti, (int)tistart,
-                      central ? 1 : 0, imp_atol, imp_rtol, (int)imp_MAX_IT, &st);
+  int rc = cvb_imp_rk(g_cvb, uc, uo, urm, ucat, p, ub, &o, &st);
   VecRestoreArray(u->Bcs.Ubcs, &ub);
   VecRestoreArray(u->P, &p);
   VecRestoreArray(u->Ucat, &ucat);
@@ -322,6 +341,7 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
   VecRestoreArray(u->Ucont_o, &uo);
   VecRestoreArray(u->Ucont, &uc);
   if (rc) return report(rc, "ImpRK_GB300");
+  if (bt[4] == 5) FluxInSum = u->FluxInSum = st.flux_in_sum; /* as InflowFlux leaves them (bcs.c:242, 383) */
   PetscPrintf(PETSC_COMM_WORLD, "ImpRK_GB300: %d pseudo-time iterations (%d undone), |dU| %le, rel %le, |F| %le\n",
               st.pseudo_iterations, st.rejected, st.norm_du, st.rel_du, st.norm_f);
   DMGlobalToLocalBegin(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);

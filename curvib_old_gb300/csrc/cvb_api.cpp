@@ -155,6 +155,7 @@ static void free_all(cvb_ctx *ctx) {
   ctx->conv_dev = ctx->conv_fp = nullptr;
   ctx->visc_dev = ctx->rct_dev = ctx->rhs_dev = ctx->uo_dev = ctx->urm_dev = ctx->pu_dev = nullptr;
   ctx->imp_norms = nullptr;
+  ctx->bc_scratch = nullptr;
   ctx->ibm_cent = nullptr;
   ctx->ready = false;
 }
@@ -1764,35 +1765,104 @@ int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const
   return momentum_finish(ctx, ucat, rhs);
 }
 
-// --- FormBCS and ImpRK, all-wall boxes ---------------------------------------
-static int walls_only(cvb_ctx *ctx, const char *who) {
+// --- InflowFlux, FormBCS and ImpRK --------------------------------------------
+// The boxes covered: walls (1) on the x and y faces; on the k faces walls, or
+// an inlet on k = 0 (5) with an outlet on the last (4).
+static int bc_covered(cvb_ctx *ctx, const char *who) {
   const int *bc = ctx->H[ctx->nlevels - 1].d.bctype;
-  for (int f = 0; f < 6; f++)
-    if (bc[f] != 1)
-      return fail(ctx, CVB_BAD_INPUT, "%s: face %d has bctype %d; only solid walls (1) on every face are covered", who,
-                  f, bc[f]);
+  bool ok = true;
+  for (int f = 0; f < 4; f++) ok = ok && bc[f] == 1;
+  ok = ok && (bc[4] == 1 || bc[4] == 5) && (bc[5] == 1 || bc[5] == 4) && ((bc[4] == 5) == (bc[5] == 4));
+  if (!ok)
+    return fail(ctx, CVB_BAD_INPUT,
+                "%s: bctype %d %d %d %d %d %d; covered are walls (1) on the x and y faces and on the k faces walls, "
+                "or an inlet (5) on k = 0 with an outlet (4) on the last",
+                who, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5]);
   return CVB_OK;
 }
 
-static void form_bcs_dev(cvb_ctx *ctx) {
-  LevelDev &F = ctx->L[ctx->nlevels - 1];
-  launch_form_bcs_walls(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ubcs_dev, ctx->ucat_dev,
-                        ctx->p_dev, ctx->stream);
+// InflowFlux's constant profiles (bcs.c:161-200).
+static int inlet_speed(cvb_ctx *ctx, int profile, double *uin) {
+  if (profile == 1) *uin = 2.;
+  else if (profile == -1) *uin = -1.;
+  else if (profile == 11) *uin = 0.185;
+  else
+    return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d is not covered (constant profiles 1, -1, 11 are)",
+                profile);
+  return CVB_OK;
 }
 
-int cvb_form_bcs(cvb_ctx *ctx, const double *ucont, const double *ubcs, double *ucat, double *p) {
+static int bc_buffers(cvb_ctx *ctx) {
+  const Geom &g = ctx->L[ctx->nlevels - 1].g;
+  if (!ctx->bc_scratch) TRY(dalloc(ctx, &ctx->bc_scratch, 2 * (size_t)(g.mx - 2) * (g.my - 2) + 4));
+  return CVB_OK;
+}
+// bc_scratch: [terms: 2 n2 | sums: 2 | FluxInSum | spare]
+static double *bc_flux_in(cvb_ctx *ctx) {
+  const Geom &g = ctx->L[ctx->nlevels - 1].g;
+  return ctx->bc_scratch + 2 * (size_t)(g.mx - 2) * (g.my - 2) + 2;
+}
+
+static void inflow_dev(cvb_ctx *ctx, double uin) {
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  launch_inflow(F.g, F.nvert, ctx->cm[2], uin, ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch, bc_flux_in(ctx),
+                ctx->stream);
+}
+
+static void form_bcs_dev(cvb_ctx *ctx, double flux_intp_sum) {
+  LevelDev &F = ctx->L[ctx->nlevels - 1];
+  const Geom &g = F.g;
+  std::function<void()> outlet;
+  if (ctx->H[ctx->nlevels - 1].d.bctype[5] == 4)
+    outlet = [ctx, &F, &g, flux_intp_sum]() {
+      double *terms = ctx->bc_scratch, *sums = terms + 2 * (size_t)(g.mx - 2) * (g.my - 2);
+      launch_outlet(g, F.nvert, ctx->cm[2], ctx->ucat_dev, bc_flux_in(ctx), flux_intp_sum, ctx->uc_dev,
+                    ctx->ubcs_dev, terms, sums, ctx->stream);
+    };
+  launch_form_bcs(g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ubcs_dev, ctx->ucat_dev,
+                  ctx->p_dev, outlet, ctx->stream);
+}
+
+int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile, double *flux_in_sum) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!ucont || !ubcs || !flux_in_sum) return fail(ctx, CVB_BAD_INPUT, "InflowFlux: ucont/ubcs/flux_in_sum is NULL");
+  TRY(bc_covered(ctx, "InflowFlux"));
+  if (ctx->H[ctx->nlevels - 1].d.bctype[4] != 5) return CVB_OK;  // FluxIn 0; FluxInSum keeps its value
+  double uin;
+  TRY(inlet_speed(ctx, inletprofile, &uin));
+  const size_t n = ctx->L[ctx->nlevels - 1].g.n();
+  TRY(post_buffers(ctx, n));
+  TRY(bc_buffers(ctx));
+  CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  inflow_dev(ctx, uin);
+  CKL();
+  CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(flux_in_sum, bc_flux_in(ctx), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_form_bcs(cvb_ctx *ctx, double *ucont, double *ubcs, double *ucat, double *p, double flux_in_sum,
+                 double flux_intp_sum) {
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
   if (!ucont || !ubcs || !ucat || !p) return fail(ctx, CVB_BAD_INPUT, "FormBCS: ucont/ubcs/ucat/p is NULL");
-  TRY(walls_only(ctx, "FormBCS"));
+  TRY(bc_covered(ctx, "FormBCS"));
   const size_t n = ctx->L[ctx->nlevels - 1].g.n();
   TRY(post_buffers(ctx, n));
+  TRY(bc_buffers(ctx));
   CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-  form_bcs_dev(ctx);
+  CK(cudaMemcpyAsync(bc_flux_in(ctx), &flux_in_sum, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  form_bcs_dev(ctx, flux_intp_sum);
   CKL();
+  CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(p, ctx->p_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1811,15 +1881,35 @@ static int imp_norms(cvb_ctx *ctx, size_t n3, bool du, double *f, double *d) {
   return CVB_OK;
 }
 
+void cvb_imp_rk_opts_default(cvb_imp_rk_opts *o) {
+  if (!o) return;
+  o->ren = 1.;
+  o->dt = 1.;
+  o->st = 1.;
+  o->cfl = 0.2;        // init.c:54
+  o->ti = 1;
+  o->tistart = 0;
+  o->central = 0;
+  o->imp_atol = 1e-7;  // main.c:26
+  o->imp_rtol = 1e-4;
+  o->imp_max_it = 50;  // main.c:21
+  o->inletprofile = 1;
+  o->flux_intp_sum = 0.;
+}
+
 int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
-               const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart, int central,
-               double imp_atol, double imp_rtol, int imp_max_it, cvb_imp_rk_stats *stats) {
+               double *ubcs, const cvb_imp_rk_opts *o, cvb_imp_rk_stats *stats) {
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
-  if (!ucont || !ucont_o || !ucont_rm1 || !ucat || !p || !ubcs)
-    return fail(ctx, CVB_BAD_INPUT, "ImpRK: ucont/ucont_o/ucont_rm1/ucat/p/ubcs is NULL");
+  if (!ucont || !ucont_o || !ucont_rm1 || !ucat || !p || !ubcs || !o)
+    return fail(ctx, CVB_BAD_INPUT, "ImpRK: ucont/ucont_o/ucont_rm1/ucat/p/ubcs/opts is NULL");
+  const double ren = o->ren, dt = o->dt, st = o->st, cfl = o->cfl, imp_atol = o->imp_atol, imp_rtol = o->imp_rtol;
+  const int ti = o->ti, tistart = o->tistart, central = o->central, imp_max_it = o->imp_max_it;
   if (!(ren != 0.0) || !(dt != 0.0)) return fail(ctx, CVB_BAD_INPUT, "ImpRK: ren / dt is 0");
-  TRY(walls_only(ctx, "ImpRK"));
+  TRY(bc_covered(ctx, "ImpRK"));
+  const bool inlet = ctx->H[ctx->nlevels - 1].d.bctype[4] == 5;
+  double uin = 0.;
+  if (inlet) TRY(inlet_speed(ctx, o->inletprofile, &uin));
   const int l = ctx->nlevels - 1;
   LevelDev &F = ctx->L[l];
   const size_t n = F.g.n(), n3 = 3 * n;
@@ -1833,12 +1923,20 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   if (!ctx->urm_dev) TRY(dalloc(ctx, &ctx->urm_dev, n3));
   if (!ctx->pu_dev) TRY(dalloc(ctx, &ctx->pu_dev, n3));
   if (!ctx->imp_norms) TRY(dalloc(ctx, &ctx->imp_norms, 2));
+  TRY(bc_buffers(ctx));
   CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->uo_dev, ucont_o, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->urm_dev, ucont_rm1, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(bc_flux_in(ctx), 0, sizeof(double), ctx->stream));
+  // InflowFlux (a wall k = 0 face: nothing), OutflowFlux (it only sums a flux
+  // nothing here reads), FormBCS
+  auto boundary = [&]() {
+    if (inlet) inflow_dev(ctx, uin);
+    form_bcs_dev(ctx, o->flux_intp_sum);
+  };
   // Rhs starts at 0 (VecSet, implicitsolver.c:7140); CalcRHS leaves part of
   // its ring as it was
   CK(cudaMemsetAsync(ctx->rhs_dev, 0, sizeof(double) * n3, ctx->stream));
@@ -1849,9 +1947,9 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
     launch_calc_rhs(F.g, F.nvert, ctx->uc_dev, ctx->uo_dev, ctx->urm_dev, bdf2, -1. / dt, mz_end, ctx->rhs_dev,
                     ctx->stream);
   };
-  // before the loop (implicitsolver.c:7124-7148): InflowFlux and OutflowFlux
-  // leave an all-wall box as it is; FormBCS, pUcont = Ucont, CalcRHS
-  form_bcs_dev(ctx);
+  // before the loop (implicitsolver.c:7124-7148): the boundary conditions,
+  // pUcont = Ucont, CalcRHS
+  boundary();
   CK(cudaMemcpyAsync(ctx->pu_dev, ctx->uc_dev, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
   calc_rhs();
   double normF0, normF1 = 1000., normdU1 = 1000., lambda = cfl;
@@ -1866,7 +1964,7 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
     for (int s = 0; s < 4; s++) {
       const double a = lambda * alfa[s] * dt * st;
       launch_imp_waxpy(n3, a, ctx->rhs_dev, ctx->pu_dev, ctx->uc_dev, ctx->stream);
-      form_bcs_dev(ctx);
+      boundary();
       calc_rhs();
     }
     normdU1 = normdU_bk;
@@ -1900,8 +1998,12 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(p, ctx->p_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  double flux_in = 0.;
+  CK(cudaMemcpyAsync(&flux_in, bc_flux_in(ctx), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (stats) {
+    stats->flux_in_sum = flux_in;
     stats->pseudo_iterations = pseudot;
     stats->rejected = rejected;
     stats->norm_du = normdU;

@@ -2,6 +2,7 @@
 // Grid layout everywhere: one level is the reference's DMDA box [mz][my][mx],
 // i fastest, boundary ring included (mx = IM+1 for IM nodes).
 #pragma once
+#include <functional>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -289,7 +290,8 @@ struct IbmWork {
 void launch_ibm_search(const IbmArgs &A, const IbmWork &W, double *tmp, cudaStream_t s);
 
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
-                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s);
+                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s, int k0 = 1,
+                        int nk = -1);
 // max |div| and its first box index into out_v / out_i (device); pv / pi
 // hold 1024 partial pairs
 void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
@@ -314,11 +316,25 @@ void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, co
 // bc: the level's bctype[6]; the host has refused the types it does not cover
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
                                 const double *zet, double *ubcs, double *ucat, cudaStream_t s);
-// FormBCS for a box whose six faces are walls: Contra2Cart, the ghost faces'
-// interior cells, then three rounds of the 12 edge averages of ucat and p
-void launch_form_bcs_walls(const Geom &g, const double *csi, const double *eta, const double *zet,
-                           const double *nvert, const double *ucont, const double *ubcs, double *ucat, double *p,
-                           cudaStream_t s);
+// FormBCS with walls on the x and y faces: its three passes of the outlet's
+// flux correction (outlet_pass, empty for a walled k = mz - 1 face; it
+// launches on s), Contra2Cart, the ghost faces' interior cells and the 12
+// edge averages of ucat and p
+void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const double *zet,
+                     const double *nvert, double *ucont, double *ubcs, double *ucat, double *p,
+                     const std::function<void()> &outlet_pass, cudaStream_t s);
+// InflowFlux on an inlet k = 0 face with a constant speed uin: ubcs and
+// Ucont.z there, and their flux summed in the reference's order into
+// *flux_in (device); terms: (mx - 2)(my - 2) doubles of scratch
+void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, double *ucont, double *ubcs,
+                   double *terms, double *flux_in, cudaStream_t s);
+// The outlet's flux correction (one FormBCS pass, bctype[5] 4): the outlet
+// flux and area summed in the reference's order, then ubcs on the last face
+// and Ucont.z of the last interior face; flux_in (device) is FluxInSum; terms:
+// 2 (mx - 2)(my - 2) doubles, sums: 2 doubles of scratch
+void launch_outlet(const Geom &g, const double *nvert, const double *zet, const double *ucat,
+                   const double *flux_in, double flux_intp_sum, double *ucont, double *ubcs, double *terms,
+                   double *sums, cudaStream_t s);
 // ImpRK's stage update u = a rhs + pu, and its two infinity norms (|rhs|,
 // |pu - u|; pu null: |rhs| only) as bit patterns into out[0..1] (device)
 void launch_imp_waxpy(size_t n, double a, const double *rhs, const double *pu, double *u, cudaStream_t s);

@@ -8,6 +8,8 @@
 // reference's order (no fused multiply-add), so results equal the reference's
 // bit for bit.  Arrays are the finest level's [mz][my][mx] box, Cmpnts
 // interleaved.
+#include <functional>
+
 #include "cvb_internal.h"
 
 namespace cvb {
@@ -39,12 +41,12 @@ __device__ __forceinline__ double cof(double a, double b, double c, double d, do
 __global__ void __launch_bounds__(256) k_contra2cart(Geom g, const double *__restrict__ csi,
                                                      const double *__restrict__ eta, const double *__restrict__ zet,
                                                      const double *__restrict__ nvert, const double *__restrict__ uc,
-                                                     double *__restrict__ ucat) {
+                                                     double *__restrict__ ucat, int k0, int nk) {
   const int ni = g.mx - 2, nj = g.my - 2;
-  const size_t cells = (size_t)ni * nj * (g.mz - 2);
+  const size_t cells = (size_t)ni * nj * nk;
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cells) return;
-  const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = 1 + (int)(t / ((size_t)ni * nj));
+  const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = k0 + (int)(t / ((size_t)ni * nj));
   const size_t p = ((size_t)k * g.my + j) * g.mx + i;
   const double nv = nvert[p];
   if (!(nv < 0.1 || nv > 7.0)) return;
@@ -73,11 +75,14 @@ __global__ void __launch_bounds__(256) k_contra2cart(Geom g, const double *__res
   ucat[3 * p + 2] = __ddiv_rn(d2, det);
 }
 
+// Interior cells of the planes k0 .. k0 + nk - 1 (all interior planes by
+// default).
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
-                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s) {
-  const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s, int k0, int nk) {
+  if (nk < 0) nk = g.mz - 2;
+  const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * nk;
   if (!cells) return;
-  k_contra2cart<<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, nvert, ucont, ucat);
+  k_contra2cart<<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, nvert, ucont, ucat, k0, nk);
   count_launch();
 }
 
@@ -355,33 +360,51 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
   }
 }
 
-// FormBCS (bcs.c:4436-5889) for a box whose six faces are walls: its loop of
-// three passes (bcs.c:4483) each runs Contra2Cart, the ghost faces on the
-// faces' interior cells and the 12 edges of ucat and p.  Contra2Cart reads
-// only ucont and the faces read only interior cells, so passes two and three
-// give the first pass's values there; only the edges, which read one another's
-// cells at the corners, change between passes.  So: Contra2Cart and the faces
-// once, the edges three times.
-void launch_form_bcs_walls(const Geom &g, const double *csi, const double *eta, const double *zet,
-                           const double *nvert, const double *ucont, const double *ubcs, double *ucat, double *p,
-                           cudaStream_t s) {
-  launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s);
+// FormBCS (bcs.c:4436-5889) on a box with walls on its x and y faces and
+// walls, or an inlet and an outlet, on its k faces.  Its loop of three passes
+// (bcs.c:4483) each runs the outlet's flux correction (outlet_pass, before
+// Contra2Cart there), Contra2Cart, the ghost faces on the faces' interior cells
+// and the 12 edges of ucat and p.  Contra2Cart reads only ucont, and the faces
+// read only interior cells: with walls on the k faces, passes two and three
+// give the first pass's values there and only the edges, which read one
+// another's cells at the corners, change, so Contra2Cart and the faces run
+// once and the edges three times.  With an outlet, a pass changes Ucont.z of
+// the last interior k face only, so Contra2Cart runs on that plane alone in
+// passes two and three.
+void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const double *zet,
+                     const double *nvert, double *ucont, double *ubcs, double *ucat, double *p,
+                     const std::function<void()> &outlet_pass, cudaStream_t s) {
   GhostArgs A;
   A.g = g;
   for (int f = 0; f < 6; f++) A.bc[f] = 1;
   A.csi = csi; A.eta = eta; A.zet = zet;
-  A.ub = const_cast<double *>(ubcs);  // read only: no special wall type here
+  A.ub = ubcs;
   A.u = ucat;
   A.p = p;
   dim3 grd, blk;
-  for (int axis = 0; axis < 3; axis++) {
-    face_grid(g, axis, 2, grd, blk);
-    k_ghost_faces<<<grd, blk, 0, s>>>(A, axis, 1);
-    count_launch();
-  }
-  for (int pass = 0; pass < 3; pass++) {
+  auto faces = [&]() {
+    for (int axis = 0; axis < 3; axis++) {
+      face_grid(g, axis, 2, grd, blk);
+      k_ghost_faces<<<grd, blk, 0, s>>>(A, axis, 1);
+      count_launch();
+    }
+  };
+  auto edges = [&]() {
     k_ghost_edges<<<1, 256, 0, s>>>(A);
     count_launch();
+  };
+  if (!outlet_pass) {
+    launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s);
+    faces();
+    for (int pass = 0; pass < 3; pass++) edges();
+    return;
+  }
+  for (int pass = 0; pass < 3; pass++) {
+    outlet_pass();
+    if (pass == 0) launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s);
+    else launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s, g.mz - 2, 1);
+    faces();
+    edges();
   }
 }
 

@@ -233,26 +233,33 @@ class PoissonContext:
                                          float(dt), int(ti), int(tistart), int(central), ptr(out)))
         return out, u
 
-    def form_bcs(self, ucont, ubcs, ucat, p):
-        """FormBCS (bcs.c:4436) on an all-wall box: (ucat, p)."""
-        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
-        pp = np.array(p, dtype=np.float64, copy=True, order="C")
-        self._check(self._L.cvb_form_bcs(self._ctx, ptr(_c64(ucont)), ptr(_c64(ubcs)), ptr(u), ptr(pp)))
-        return u, pp
+    def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0):
+        """InflowFlux (bcs.c:99): (ucont, ubcs, FluxInSum)."""
+        uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]
+        f = ctypes.c_double(flux_in_sum)
+        self._check(self._L.cvb_inflow_flux(self._ctx, ptr(uc), ptr(ub), int(inletprofile), ctypes.byref(f)))
+        return uc, ub, f.value
+
+    def form_bcs(self, ucont, ubcs, ucat, p, flux_in_sum=0.0, flux_intp_sum=0.0):
+        """FormBCS (bcs.c:4436): (ucont, ubcs, ucat, p)."""
+        uc, ub, u, pp = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs, ucat, p)]
+        self._check(self._L.cvb_form_bcs(self._ctx, ptr(uc), ptr(ub), ptr(u), ptr(pp), float(flux_in_sum),
+                                         float(flux_intp_sum)))
+        return uc, ub, u, pp
 
     def imp_rk(self, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=False,
-               atol=1e-7, rtol=1e-4, max_it=50):
-        """ImpRK (implicitsolver.c:7094) on an all-wall box with no immersed
-        body: (ucont, ucat, p, stats dict)."""
-        uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
-        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
-        pp = np.array(p, dtype=np.float64, copy=True, order="C")
+               atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0):
+        """ImpRK (implicitsolver.c:7094) with no immersed body: (ucont, ucat, p,
+        stats dict, ubcs)."""
+        uc, u, pp, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ucat, p, ubcs)]
+        o = _lib.imp_rk_opts(ren=float(ren), dt=float(dt), st=float(st), cfl=float(cfl), ti=int(ti),
+                             tistart=int(tistart), central=int(central), imp_atol=float(atol), imp_rtol=float(rtol),
+                             imp_max_it=int(max_it), inletprofile=int(inletprofile),
+                             flux_intp_sum=float(flux_intp_sum))
         st_ = _lib.ImpRKStats()
         self._check(self._L.cvb_imp_rk(self._ctx, ptr(uc), ptr(_c64(ucont_o)), ptr(_c64(ucont_rm1)), ptr(u), ptr(pp),
-                                       ptr(_c64(ubcs)), float(ren), float(dt), float(st), float(cfl), int(ti),
-                                       int(tistart), int(central), float(atol), float(rtol), int(max_it),
-                                       ctypes.byref(st_)))
-        return uc, u, pp, st_.as_dict()
+                                       ptr(ub), ctypes.byref(o), ctypes.byref(st_)))
+        return uc, u, pp, st_.as_dict(), ub
 
     def metrics_divergence(self):
         """MetricsDivergence (metrics.c:1551): (max |div of the metrics|, its

@@ -21,7 +21,8 @@
  *   Viscous           (rhs.c:1947)      -> cvb_viscous
  *   FormFunction1     (rhs.c:2567)      -> cvb_form_function1
  *   CalcRHS   (implicitsolver.c:6449)   -> cvb_calc_rhs
- *   FormBCS   (bcs.c:4436), walls       -> cvb_form_bcs
+ *   InflowFlux (bcs.c:99)               -> cvb_inflow_flux
+ *   FormBCS   (bcs.c:4436)              -> cvb_form_bcs
  *   ImpRK     (implicitsolver.c:7094)   -> cvb_imp_rk
  *   ibm_search_advanced (ibm.c:4197), its nvert classification
  *                                       -> cvb_ibm_search
@@ -256,14 +257,45 @@ int cvb_form_function1(cvb_ctx *ctx, const double *ucont, double *ucat, const do
  * the convective-outflow term on the last k face before those loops). */
 int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
                  const double *p, double ren, double dt, int ti, int tistart, int central, double *rhs);
-/* FormBCS (bcs.c:4436-5889) for a box whose six faces are solid walls
- * (bctype 1; any other type is refused with CVB_BAD_INPUT): Contra2Cart of
- * ucont into ucat's interior cells, the ghost faces u = 2 ubcs - inner on the
- * faces' interior cells, and the means of ucat and p on the box's 12 edges,
- * through the reference's three passes.  ucat and p ([mz][my][mx](x3) and
- * [mz][my][mx]) are read and written, ubcs (Bcs.Ubcs) is read.  Bit for bit
- * the reference's. */
-int cvb_form_bcs(cvb_ctx *ctx, const double *ucont, const double *ubcs, double *ucat, double *p);
+/* The momentum equation's boundary conditions and pseudo-time iteration, one
+ * block, for boxes with solid walls (bctype 1) on the x and y faces and, on
+ * the k faces, walls or an inlet on k = 0 (bctype[4] 5) with an outlet on the
+ * last (bctype[5] 4); other boxes are refused with CVB_BAD_INPUT.  Vector
+ * fields are [mz][my][mx][3], p [mz][my][mx]; results equal the reference's
+ * bit for bit.
+ *
+ * InflowFlux (bcs.c:99-400) on an inlet face with a constant profile
+ * (inletprofile 1: speed 2; -1: speed -1; 11: 0.185; other profiles are
+ * refused): on the face's interior cells above fluid cells ubcs = uin zet /
+ * |zet| and Ucont.z = uin |zet|; *flux_in_sum (FluxInSum) = their sum in the
+ * reference's loop order.  On a walled k = 0 face nothing is written. */
+int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile, double *flux_in_sum);
+/* FormBCS (bcs.c:4436-5889): three passes of the outlet's flux correction
+ * (ratio = (flux_in_sum + flux_intp_sum - the outlet's flux) / its area; ubcs
+ * on the last face = the ucat next to it; Ucont.z of the last interior face =
+ * ubcs . zet + ratio |zet|), Contra2Cart of ucont into ucat's interior cells,
+ * the ghost faces u = 2 ubcs - inner on the faces' interior cells, and the
+ * means of ucat and p on the box's 12 edges.  ucont, ubcs, ucat and p are read
+ * and written; flux_in_sum and flux_intp_sum (the block's FluxIntpSum) matter
+ * only with an outlet. */
+int cvb_form_bcs(cvb_ctx *ctx, double *ucont, double *ubcs, double *ucat, double *p, double flux_in_sum,
+                 double flux_intp_sum);
+/* ImpRK's controls: the block's ren, dt, st and cfl, the time step ti and
+ * tistart (CalcRHS's BDF2 switch), -central, imp_atol / imp_rtol / imp_MAX_IT,
+ * InflowFlux's inletprofile and the block's FluxIntpSum (the immersed-boundary
+ * flux the outlet adds to the inlet's). */
+typedef struct {
+  double ren, dt, st, cfl;
+  int ti, tistart, central;
+  double imp_atol, imp_rtol;
+  int imp_max_it;
+  int inletprofile;
+  double flux_intp_sum;
+} cvb_imp_rk_opts;
+/* The reference's defaults: cfl 0.2 (init.c:54), imp_atol 1e-7, imp_rtol
+ * 1e-4, imp_MAX_IT 50 (main.c:21-26), inletprofile 1; ren, dt, st 1; ti 1,
+ * tistart 0; FluxIntpSum 0. */
+void cvb_imp_rk_opts_default(cvb_imp_rk_opts *opts);
 /* What cvb_imp_rk did: the pseudo-time iterations kept (pseudot at the end),
  * those undone with the step halved, and the last iteration's norms. */
 typedef struct {
@@ -274,25 +306,23 @@ typedef struct {
   double norm_f;    /* max |Rhs| after the last iteration */
   double rel_f;     /* norm_f / its first value */
   double lambda;    /* the pseudo-time step factor at the end (cfl, halved per undone iteration) */
+  double flux_in_sum; /* FluxInSum of the last InflowFlux (0 with a walled k = 0 face) */
 } cvb_imp_rk_stats;
 /* ImpRK (implicitsolver.c:7094-7257), the momentum equation's pseudo-time
- * iteration, for a box whose six faces are solid walls, one block, as the
- * reference runs it with immersed 0 (no immersed-boundary interpolation
- * between iterations; nvert's blocked cells still mask the fluxes):
- * InflowFlux and OutflowFlux change nothing on such a box; FormBCS as
- * cvb_form_bcs and CalcRHS as cvb_calc_rhs; per pseudo-time iteration four
- * Runge-Kutta stages Ucont = (lambda alfa_s dt st) Rhs + Ucont_prev with alfa
- * 1/4, 1/3, 1/2, 1 and lambda starting at cfl; an iteration whose |Rhs| and
- * |dU| both grew is undone with lambda halved (while lambda > 0.001); the loop
- * ends when |dU| <= imp_atol or |dU| / |dU|_first <= imp_rtol, or after
- * imp_max_it iterations.  ucont (Ucont), ucat (Ucat) and p (P) are read and
- * written, ucont_o / ucont_rm1 are the two previous steps' fluxes, ubcs the
- * wall velocity.  Results equal the reference's bit for bit; stats may be
- * NULL.  The iteration runs on the device; the host reads two norms per
+ * iteration, as the reference runs it with immersed 0 (no immersed-boundary
+ * interpolation between iterations; nvert's blocked cells still mask the
+ * fluxes): InflowFlux, OutflowFlux (it only sums a flux nothing here reads),
+ * FormBCS and CalcRHS as above; per pseudo-time iteration four Runge-Kutta
+ * stages Ucont = (lambda alfa_s dt st) Rhs + Ucont_prev with alfa 1/4, 1/3,
+ * 1/2, 1 and lambda starting at cfl; an iteration whose |Rhs| and |dU| both
+ * grew is undone with lambda halved (while lambda > 0.001); the loop ends when
+ * |dU| <= imp_atol or |dU| / |dU|_first <= imp_rtol, or after imp_max_it
+ * iterations.  ucont (Ucont), ucat (Ucat), p (P) and ubcs (Bcs.Ubcs) are read
+ * and written, ucont_o / ucont_rm1 are the two previous steps' fluxes.  stats
+ * may be NULL.  The iteration runs on the device; the host reads two norms per
  * iteration. */
 int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
-               const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart, int central,
-               double imp_atol, double imp_rtol, int imp_max_it, cvb_imp_rk_stats *stats);
+               double *ubcs, const cvb_imp_rk_opts *opts, cvb_imp_rk_stats *stats);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740), which the
  * reference reruns for moving bodies every step (solvers.c:201-571), for body
  * ibi of nbodies: a closed triangle mesh of n_v nodes (xyz, x y z per node) and

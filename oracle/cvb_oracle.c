@@ -1327,9 +1327,52 @@ int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o,
 }
 
 /* ------------------------------------------------------------------------ */
-/* The momentum equation's pseudo-time iteration for a box whose six faces are
- * all solid walls (bctype 1), with no immersed-body interpolation (immersed
- * 0) and one block. */
+/* The momentum equation's pseudo-time iteration, one block, no immersed-body
+ * interpolation (immersed 0), for boxes whose x and y faces are solid walls
+ * (bctype 1) and whose k = 0 and k = mz - 1 faces are walls or an inlet
+ * (bctype[4] 5) and an outlet (bctype[5] 4). */
+
+/* The inlet speed of InflowFlux's constant profiles (bcs.c:161-200); 0 for
+ * the profiles that are not restated. */
+int orc_inlet_speed(int inletprofile, double *uin) {
+  if (inletprofile == 1) *uin = 2.;
+  else if (inletprofile == -1) *uin = -1.;
+  else if (inletprofile == 11) *uin = 0.185;
+  else return 0;
+  return 1;
+}
+
+int orc_bcs_covered(const int *bc) {
+  for (int f = 0; f < 4; f++)
+    if (bc[f] != 1) return 0;
+  if (bc[4] != 1 && bc[4] != 5) return 0;
+  if (bc[5] != 1 && bc[5] != 4) return 0;
+  return (bc[5] == 4) == (bc[4] == 5);
+}
+
+int orc_inflow_flux(const orc_level *L, double *ucont, double *ub, int inletprofile, double *flux_in_sum) {
+  const int mx = L->mx, my = L->my;
+  if (L->bctype[4] != 5) return 0; /* FluxIn is 0 and FluxInSum keeps its value */
+  double uin;
+  if (!orc_inlet_speed(inletprofile, &uin)) return -1;
+  const double *z;
+  for (int j = 1; j < my - 1; j++)
+    for (int i = 1; i < mx - 1; i++) {
+      const size_t q = ID(L, i, j, 0);
+      if (!(L->nvert[ID(L, i, j, 1)] < 0.1)) continue;
+      z = L->zet + 3 * q;
+      ub[3 * q + 1] = uin * z[1] / sqrt(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
+      ub[3 * q + 2] = uin * z[2] / sqrt(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
+      ub[3 * q + 0] = uin * z[0] / sqrt(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
+      ucont[3 * q + 2] = uin * sqrt(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
+    }
+  double f = 0;
+  for (int j = 1; j < my - 1; j++)
+    for (int i = 1; i < mx - 1; i++)
+      if (L->nvert[ID(L, i, j, 1)] < 0.1) f += ucont[3 * ID(L, i, j, 0) + 2];
+  *flux_in_sum = f;
+  return 0;
+}
 
 /* One of FormBCS's edge averages: ucat and p at d become the means of their
  * values at a and b (bcs.c:5439-5570). */
@@ -1338,15 +1381,37 @@ static inline void edge_avg(double *u, double *p, long d, long a, long b) {
   p[d] = 0.5 * (p[a] + p[b]);
 }
 
-int orc_form_bcs_walls(const orc_level *L, const double *ucont, const double *ub, double *u, double *p) {
+int orc_form_bcs(const orc_level *L, double *ucont, double *ub, double *u, double *p, double flux_in_sum,
+                 double flux_intp_sum) {
   const int mx = L->mx, my = L->my, mz = L->mz;
-  for (int f = 0; f < 6; f++)
-    if (L->bctype[f] != 1) return -1;
+  if (!orc_bcs_covered(L->bctype)) return -1;
 #define U3(i, j, k) (u + 3 * ID(L, (i), (j), (k)))
 #define B3(i, j, k) (ub + 3 * ID(L, (i), (j), (k)))
 #define Q(i, j, k) ((long)ID(L, (i), (j), (k)))
   for (int pass = 0; pass < 3; pass++) { /* bcs.c:4483 */
-    orc_contra2cart(L, ucont, u);          /* bcs.c:5159 */
+    if (L->bctype[5] == 4) {             /* the outlet (bcs.c:4914-4998) */
+      const int k = mz - 1;
+      double flux_out = 0, area = 0;
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++) {
+          if (!(L->nvert[ID(L, i, j, k - 1)] < 0.1)) continue;
+          const double *c = U3(i, j, k - 1), *z = L->zet + 3 * ID(L, i, j, k - 1);
+          flux_out += (c[0] * z[0] + c[1] * z[1] + c[2] * z[2]);
+          area += sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+        }
+      const double flux_in = flux_in_sum + 0. + flux_intp_sum; /* + FarFluxInSum, 0 here */
+      const double ratio = (flux_in - flux_out) / area;
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++) {
+          if (!(L->nvert[ID(L, i, j, k - 1)] < 0.1)) continue;
+          double *b = B3(i, j, k);
+          const double *z = L->zet + 3 * ID(L, i, j, k - 1);
+          copy3(b, U3(i, j, k - 1));
+          ucont[3 * ID(L, i, j, k - 1) + 2] =
+              (b[0] * z[0] + b[1] * z[1] + b[2] * z[2]) + ratio * sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+        }
+    }
+    orc_contra2cart(L, ucont, u); /* bcs.c:5159 */
     /* ghost faces on the faces' interior cells (bcs.c:5250-5318) */
     for (int k = 1; k < mz - 1; k++)
       for (int j = 1; j < my - 1; j++) ghost3(U3(0, j, k), B3(0, j, k), U3(1, j, k));
@@ -1391,11 +1456,17 @@ static double max_abs(const double *x, size_t n) {
 }
 
 int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
-               double *p, const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart,
-               int central, double atol, double rtol, int max_it, orc_imp_rk_stats *out) {
+               double *p, double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart,
+               int central, double atol, double rtol, int max_it, int inletprofile, double flux_intp_sum,
+               orc_imp_rk_stats *out) {
   const size_t n3 = 3 * (size_t)L->mx * L->my * L->mz;
   const double alfa[4] = {0.25, 1 / 3., 0.5, 1.}; /* implicitsolver.c:7111 */
-  if (orc_form_bcs_walls(L, ucont, ubcs, ucat, p)) return -1;
+  double flux_in_sum = 0.;
+  double uin;
+  if (!orc_bcs_covered(L->bctype) || (L->bctype[4] == 5 && !orc_inlet_speed(inletprofile, &uin))) return -1;
+  /* InflowFlux, OutflowFlux (only sums what nothing here reads), FormBCS */
+  orc_inflow_flux(L, ucont, ubcs, inletprofile, &flux_in_sum);
+  orc_form_bcs(L, ucont, ubcs, ucat, p, flux_in_sum, flux_intp_sum);
   double *rhs = (double *)calloc(n3, sizeof(double)), *pu = (double *)malloc(sizeof(double) * n3);
   memcpy(pu, ucont, sizeof(double) * n3);
   orc_calc_rhs(L, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central, rhs);
@@ -1408,7 +1479,8 @@ int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const d
     for (int s = 0; s < 4; s++) {
       const double a = lambda * alfa[s] * dt * st;
       for (size_t q = 0; q < n3; q++) ucont[q] = a * rhs[q] + pu[q];
-      orc_form_bcs_walls(L, ucont, ubcs, ucat, p);
+      orc_inflow_flux(L, ucont, ubcs, inletprofile, &flux_in_sum);
+      orc_form_bcs(L, ucont, ubcs, ucat, p, flux_in_sum, flux_intp_sum);
       orc_calc_rhs(L, ucont, ucont_o, ucont_rm1, ucat, p, ren, dt, ti, tistart, central, rhs);
     }
     normdU1 = normdU_bk;

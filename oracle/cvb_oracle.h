@@ -116,24 +116,44 @@ int orc_form_function1(const orc_level *L, const double *ucont, double *ucat, co
 int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o, const double *ucont_rm1,
                  double *ucat, const double *p, double ren, double dt, int ti, int tistart, int central,
                  double *rhs);
-/* FormBCS (bcs.c:4436-5889) for a box whose six faces are solid walls
- * (bctype 1): three passes of Contra2Cart, the ghost faces u = 2 ubcs - inner
- * on the faces' interior cells (bcs.c:5250-5318) and the averages of ucat and
- * p on the box's 12 edges (bcs.c:5439-5570).  ucat and p are read and
- * written, ubcs is read.  -1 (nothing written) for any other face type. */
-int orc_form_bcs_walls(const orc_level *L, const double *ucont, const double *ubcs, double *ucat, double *p);
+/* The boxes the momentum equation's pseudo-time iteration is restated for:
+ * solid walls (bctype 1) on the x and y faces, and on the k faces either
+ * walls or an inlet (bctype[4] 5) with an outlet (bctype[5] 4).  1 if covered. */
+int orc_bcs_covered(const int *bc);
+/* InflowFlux's inlet speed for the constant profiles 1, -1 and 11
+ * (bcs.c:161-200); 0 for the others. */
+int orc_inlet_speed(int inletprofile, double *uin);
+/* InflowFlux (bcs.c:99-400) with an inlet on the k = 0 face (bctype[4] 5) and
+ * a constant profile: on the face's interior cells above fluid cells, ubcs =
+ * uin zet / |zet| and Ucont.z = uin |zet|; *flux_in_sum = their sum, in the
+ * reference's loop order.  Nothing for a wall (FluxInSum keeps its value);
+ * -1 for a profile that is not restated. */
+int orc_inflow_flux(const orc_level *L, double *ucont, double *ubcs, int inletprofile, double *flux_in_sum);
+/* FormBCS (bcs.c:4436-5889) on a covered box (orc_bcs_covered): three passes
+ * of the outlet's flux correction (bctype[5] 4, bcs.c:4914-4998: ubcs on the
+ * last face = the ucat next to it, Ucont.z of the last interior face = ubcs .
+ * zet + ratio |zet| with ratio = (FluxInSum + FluxIntpSum - the outlet flux)
+ * / the outlet area), Contra2Cart, the ghost faces u = 2 ubcs - inner on the
+ * faces' interior cells (bcs.c:5250-5318) and the averages of ucat and p on
+ * the box's 12 edges (bcs.c:5439-5570).  ucont, ubcs, ucat and p are read and
+ * written.  -1 (nothing written) for a box that is not covered. */
+int orc_form_bcs(const orc_level *L, double *ucont, double *ubcs, double *ucat, double *p, double flux_in_sum,
+                 double flux_intp_sum);
 typedef struct {
   int pseudo_iterations; /* pseudot at the end */
   int rejected;          /* iterations undone with the pseudo-time step halved */
   double norm_du, rel_du, norm_f, rel_f, lambda;
 } orc_imp_rk_stats;
-/* ImpRK (implicitsolver.c:7094-7257) for a walled box, one block, no immersed
- * body: InflowFlux and OutflowFlux change nothing there, FormBCS as
- * orc_form_bcs_walls, CalcRHS as orc_calc_rhs; four Runge-Kutta stages per
+/* ImpRK (implicitsolver.c:7094-7257) on a covered box (orc_bcs_covered), one
+ * block, no immersed body: InflowFlux as orc_inflow_flux, OutflowFlux (which
+ * only sums a flux nothing here reads), FormBCS as orc_form_bcs with the
+ * user's FluxIntpSum, CalcRHS as orc_calc_rhs; four Runge-Kutta stages per
  * pseudo-time iteration, the step halved and the iteration undone when both
  * norms grew, until |dU| <= atol or |dU| / |dU|_1 <= rtol or max_it
- * iterations.  ucont, ucat and p are read and written. */
+ * iterations.  ucont, ubcs, ucat and p are read and written; -1 for a box or
+ * inlet profile that is not covered. */
 int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat,
-               double *p, const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart,
-               int central, double atol, double rtol, int max_it, orc_imp_rk_stats *out);
+               double *p, double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart,
+               int central, double atol, double rtol, int max_it, int inletprofile, double flux_intp_sum,
+               orc_imp_rk_stats *out);
 #endif

@@ -120,9 +120,11 @@ def lib():
         _lib.orc_viscous.argtypes = [L, P, D, P]
         _lib.orc_form_function1.argtypes = [L, P, P, P, D, I, P]
         _lib.orc_calc_rhs.argtypes = [L, P, P, P, P, P, D, D, I, I, I, P]
-        _lib.orc_form_bcs_walls.argtypes = [L, P, P, P, P]
-        _lib.orc_form_bcs_walls.restype = I
-        _lib.orc_imp_rk.argtypes = [L, P, P, P, P, P, P, D, D, D, D, I, I, I, D, D, I, P]
+        _lib.orc_inflow_flux.argtypes = [L, P, P, I, P]
+        _lib.orc_inflow_flux.restype = I
+        _lib.orc_form_bcs.argtypes = [L, P, P, P, P, D, D]
+        _lib.orc_form_bcs.restype = I
+        _lib.orc_imp_rk.argtypes = [L, P, P, P, P, P, P, D, D, D, D, I, I, I, D, D, I, I, D, P]
         _lib.orc_imp_rk.restype = I
     return _lib
 
@@ -304,29 +306,37 @@ class ImpRKStats(ctypes.Structure):
                 ("lambda_", ctypes.c_double)]
 
 
-def form_bcs_walls(L: OLevel, ucont, ubcs, ucat, p):
-    """FormBCS (bcs.c:4436-5889) for an all-wall box: (status, ucat, p)."""
-    uc = np.ascontiguousarray(ucont, dtype=np.float64)
-    ub = np.ascontiguousarray(ubcs, dtype=np.float64)
-    u = np.array(ucat, dtype=np.float64, copy=True, order="C")
-    pp = np.array(p, dtype=np.float64, copy=True, order="C")
-    rc = lib().orc_form_bcs_walls(L.ref(), _p(uc), _p(ub), _p(u), _p(pp))
-    return rc, u, pp
+def inflow_flux(L: OLevel, ucont, ubcs, inletprofile, flux_in_sum=0.0):
+    """InflowFlux (bcs.c:99-400), inlet on k = 0 with a constant profile:
+    (status, ucont, ubcs, FluxInSum)."""
+    uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
+    ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
+    f = ctypes.c_double(flux_in_sum)
+    rc = lib().orc_inflow_flux(L.ref(), _p(uc), _p(ub), int(inletprofile), ctypes.byref(f))
+    return rc, uc, ub, f.value
+
+
+def form_bcs(L: OLevel, ucont, ubcs, ucat, p, flux_in_sum=0.0, flux_intp_sum=0.0):
+    """FormBCS (bcs.c:4436-5889): (status, ucont, ubcs, ucat, p)."""
+    uc, ub, u, pp = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs, ucat, p)]
+    rc = lib().orc_form_bcs(L.ref(), _p(uc), _p(ub), _p(u), _p(pp), float(flux_in_sum), float(flux_intp_sum))
+    return rc, uc, ub, u, pp
 
 
 def imp_rk(L: OLevel, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=0,
-           atol=1e-7, rtol=1e-4, max_it=50):
-    """ImpRK (implicitsolver.c:7094-7257) for an all-wall box with no immersed
-    body: (status, ucont, ucat, p, stats)."""
+           atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0):
+    """ImpRK (implicitsolver.c:7094-7257), no immersed body: (status, ucont,
+    ucat, p, stats, ubcs)."""
     uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
-    uo, urm, ub = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1, ubcs)]
+    uo, urm = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1)]
+    ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
     u = np.array(ucat, dtype=np.float64, copy=True, order="C")
     pp = np.array(p, dtype=np.float64, copy=True, order="C")
     st_ = ImpRKStats()
     rc = lib().orc_imp_rk(L.ref(), _p(uc), _p(uo), _p(urm), _p(u), _p(pp), _p(ub), float(ren), float(dt), float(st),
                           float(cfl), int(ti), int(tistart), int(central), float(atol), float(rtol), int(max_it),
-                          ctypes.byref(st_))
-    return rc, uc, u, pp, st_
+                          int(inletprofile), float(flux_intp_sum), ctypes.byref(st_))
+    return rc, uc, u, pp, st_, ub
 
 
 def metrics_divergence(L: OLevel):
@@ -516,27 +526,35 @@ class Reference:
             raise RuntimeError("ref_calc_rhs failed")
         return out, u
 
-    def form_bcs(self, ucont, ubcs, ucat, p):
-        uc, ub = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont, ubcs)]
-        u = np.array(ucat, dtype=np.float64, copy=True, order="C")
-        pp = np.array(p, dtype=np.float64, copy=True, order="C")
-        if self.L.ref_form_bcs(_p(uc), _p(ub), _p(u), _p(pp)):
+    def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0):
+        uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]
+        f = ctypes.c_double(flux_in_sum)
+        if self.L.ref_inflow_flux(_p(uc), _p(ub), int(inletprofile), ctypes.byref(f)):
+            raise RuntimeError("ref_inflow_flux failed")
+        return uc, ub, f.value
+
+    def form_bcs(self, ucont, ubcs, ucat, p, flux_in_sum=0.0, flux_intp_sum=0.0):
+        uc, ub, u, pp = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs, ucat, p)]
+        if self.L.ref_form_bcs(_p(uc), _p(ub), _p(u), _p(pp), ctypes.c_double(flux_in_sum),
+                               ctypes.c_double(flux_intp_sum)):
             raise RuntimeError("ref_form_bcs failed")
-        return u, pp
+        return uc, ub, u, pp
 
     def imp_rk(self, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=0,
-               atol=1e-7, rtol=1e-4, max_it=50):
-        """ImpRK through the reference's own routine; it appends to
-        Converge_dU0 in the working directory."""
+               atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0):
+        """ImpRK through the reference's own routine: (ucont, ucat, p, ubcs);
+        it appends to Converge_dU0 in the working directory."""
         uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
-        uo, urm, ub = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1, ubcs)]
+        uo, urm = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1)]
+        ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
         u = np.array(ucat, dtype=np.float64, copy=True, order="C")
         pp = np.array(p, dtype=np.float64, copy=True, order="C")
         D = ctypes.c_double
         if self.L.ref_imp_rk(_p(uc), _p(uo), _p(urm), _p(u), _p(pp), _p(ub), D(ren), D(dt), D(st), D(cfl), int(ti),
-                             int(tistart), int(central), D(atol), D(rtol), int(max_it)):
+                             int(tistart), int(central), D(atol), D(rtol), int(max_it), int(inletprofile),
+                             D(flux_intp_sum)):
             raise RuntimeError("ref_imp_rk failed")
-        return uc, u, pp
+        return uc, u, pp, ub
 
     def metrics_divergence(self):
         m, at = ctypes.c_double(), ctypes.c_int()

@@ -669,36 +669,61 @@ int ref_calc_rhs(const double *ucont, const double *ucont_o, const double *ucont
   return rc;
 }
 
-/* FormBCS (bcs.c:4436-5889) on the finest level: ucont (Ucont) and ubcs
- * (Bcs.Ubcs) read, ucat (Ucat) and p (P) read and written, global boxes. */
-int ref_form_bcs(const double *ucont, const double *ubcs, double *ucat, double *p) {
+/* InflowFlux (bcs.c:99-400) and FormBCS (bcs.c:4436-5889) on the finest
+ * level.  Both read and write ucont (Ucont) and ubcs (Bcs.Ubcs); FormBCS also
+ * ucat (Ucat) and p (P).  InflowFlux's result is the global FluxInSum, which
+ * FormBCS's outlet reads (flux_in_sum here), beside the user's FluxIntpSum. */
+extern PetscReal FluxInSum;
+extern PetscInt inletprofile;
+PetscErrorCode InflowFlux(UserCtx *user);
+PetscErrorCode FormBCS(UserCtx *user);
+
+int ref_inflow_flux(double *ucont, double *ubcs, int profile, double *flux_in_sum) {
+  if (!g_ready) return 1;
+  UserCtx *u = U(g_mg.mglevels - 1);
+  set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 1);
+  inletprofile = profile;
+  FluxInSum = *flux_in_sum;
+  int rc = InflowFlux(u);
+  *flux_in_sum = FluxInSum;
+  copy_owned(u, u->Ucont, 3, ucont, 0);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 0);
+  return rc;
+}
+
+int ref_form_bcs(double *ucont, double *ubcs, double *ucat, double *p, double flux_in_sum, double flux_intp_sum) {
   if (!g_ready) return 1;
   UserCtx *u = U(g_mg.mglevels - 1);
   set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
   set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
   set_pair(u, u->P, u->lP, 1, p, u->da);
-  copy_owned(u, u->Bcs.Ubcs, 3, (double *)ubcs, 1);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 1);
+  FluxInSum = flux_in_sum;
+  u->FluxIntpSum = flux_intp_sum;
   int rc = FormBCS(u);
+  copy_owned(u, u->Ucont, 3, ucont, 0);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 0);
   copy_owned(u, u->Ucat, 3, ucat, 0);
   copy_owned(u, u->P, 1, p, 0);
   return rc;
 }
 
 /* ImpRK (implicitsolver.c:7094-7257) on the finest level, one block, no
- * immersed body: ucont, ucat and p (Ucont, Ucat, P) read and written, ubcs
- * (Bcs.Ubcs) read, ucont_o / ucont_rm1 the two previous steps' fluxes; cfl,
- * dt and st the block's, imp_atol / imp_rtol / imp_MAX_IT from the arguments
- * for this call.  The routine appends to the file Converge_dU0 in the working
- * directory, as the reference's rank 0 does. */
+ * immersed body: ucont, ubcs, ucat and p (Ucont, Bcs.Ubcs, Ucat, P) read and
+ * written, ucont_o / ucont_rm1 the two previous steps' fluxes; cfl, dt, st and
+ * FluxIntpSum the block's, imp_atol / imp_rtol / imp_MAX_IT and inletprofile
+ * from the arguments for this call.  The routine appends to the file
+ * Converge_dU0 in the working directory, as the reference's rank 0 does. */
 int ref_imp_rk(double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
-               const double *ubcs, double ren, double dt, double st, double cfl, int ti_, int tistart_, int central,
-               double atol, double rtol, int max_it) {
+               double *ubcs, double ren, double dt, double st, double cfl, int ti_, int tistart_, int central,
+               double atol, double rtol, int max_it, int profile, double flux_intp_sum) {
   if (!g_ready) return 1;
   UserCtx *u = U(g_mg.mglevels - 1);
   set_pair(u, u->Ucont, u->lUcont, 3, ucont, u->fda);
   set_pair(u, u->Ucat, u->lUcat, 3, ucat, u->fda);
   set_pair(u, u->P, u->lP, 1, p, u->da);
-  copy_owned(u, u->Bcs.Ubcs, 3, (double *)ubcs, 1);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 1);
   if (!u->Ucont_o) VecDuplicate(u->Ucont, &u->Ucont_o);
   if (!u->Ucont_rm1) VecDuplicate(u->Ucont, &u->Ucont_rm1);
   copy_owned(u, u->Ucont_o, 3, (double *)ucont_o, 1);
@@ -709,6 +734,9 @@ int ref_imp_rk(double *ucont, const double *ucont_o, const double *ucont_rm1, do
   u->dt = dt;
   u->st = st;
   u->cfl = cfl;
+  u->FluxIntpSum = flux_intp_sum;
+  inletprofile = profile;
+  FluxInSum = 0.;
   PetscOptionsSetValue("-central", central ? "1" : "0");
   ti = ti_;
   tistart = tistart_;
@@ -723,6 +751,7 @@ int ref_imp_rk(double *ucont, const double *ucont_o, const double *ucont_rm1, do
   imp_rtol = r0;
   PetscOptionsSetValue("-central", "0");
   copy_owned(u, u->Ucont, 3, ucont, 0);
+  copy_owned(u, u->Bcs.Ubcs, 3, ubcs, 0);
   copy_owned(u, u->Ucat, 3, ucat, 0);
   copy_owned(u, u->P, 1, p, 0);
   return rc;

@@ -165,6 +165,12 @@ def momentum_inputs(shape):
 # defaults).
 IMP_RK_RUNS = [(1, 1.0, 50), (5, 0.5, 4), (5, 3.0, 50)]
 IMP_ATOL, IMP_RTOL = 1e-7, 1e-4
+# The inlet / outlet boxes (bctype[4] 5, bctype[5] 4 on a scenario's grid):
+# InflowFlux's constant profiles, and the immersed-boundary flux FormBCS's
+# outlet adds to the inlet's.
+INLET_OUTLET_SCENARIOS = ("box_sphere", "blocked_slab")
+INLET_PROFILES = (1, -1, 11)
+FLUX_INTP_SUM = 1e-3
 
 
 def imp_rk_inputs(shape, ucont):

@@ -107,19 +107,33 @@ int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int ce
   conv[3 * REC.mark] = 7.0;
   return take_status();
 }
+void cvb_imp_rk_opts_default(cvb_imp_rk_opts *o) {
+  memset(o, 0, sizeof *o);
+  o->ren = o->dt = o->st = 1.;
+  o->cfl = 0.2;
+  o->ti = 1;
+  o->imp_atol = 1e-7;
+  o->imp_rtol = 1e-4;
+  o->imp_max_it = 50;
+  o->inletprofile = 1;
+}
 int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
-               const double *ubcs, double ren, double dt, double st, double cfl, int ti, int tistart, int central,
-               double imp_atol, double imp_rtol, int imp_max_it, cvb_imp_rk_stats *stats) {
+               double *ubcs, const cvb_imp_rk_opts *o, cvb_imp_rk_stats *stats) {
   (void)ctx;
   REC.n_imp_rk++;
   REC.ucont_imp = ucont; REC.uo_imp = ucont_o; REC.urm_imp = ucont_rm1; REC.ucat_imp = ucat; REC.p_imp = p;
-  REC.ubcs_imp = ubcs; REC.ren_imp = ren; REC.dt_imp = dt; REC.st_imp = st; REC.cfl_imp = cfl;
-  REC.ti_imp = ti; REC.tistart_imp = tistart; REC.central_imp = central; REC.atol_imp = imp_atol;
-  REC.rtol_imp = imp_rtol; REC.max_it_imp = imp_max_it;
+  REC.ubcs_imp = ubcs; REC.ren_imp = o->ren; REC.dt_imp = o->dt; REC.st_imp = o->st; REC.cfl_imp = o->cfl;
+  REC.ti_imp = o->ti; REC.tistart_imp = o->tistart; REC.central_imp = o->central; REC.atol_imp = o->imp_atol;
+  REC.rtol_imp = o->imp_rtol; REC.max_it_imp = o->imp_max_it; REC.profile_imp = o->inletprofile;
+  REC.intp_imp = o->flux_intp_sum;
   ucont[3 * REC.mark] = 11.0;
   ucat[3 * REC.mark + 1] = 12.0;
   p[REC.mark] = 13.0;
-  if (stats) memset(stats, 0, sizeof *stats);
+  ubcs[3 * REC.mark + 2] = 14.0;
+  if (stats) {
+    memset(stats, 0, sizeof *stats);
+    stats->flux_in_sum = 0.5;
+  }
   return take_status();
 }
 int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, double *ucont, double *ubcs,

@@ -33,16 +33,17 @@ typedef struct {
   const double *ucont_conv, *ucat_conv;
   double *conv_conv;
   /* cvb_imp_rk */
-  double *ucont_imp, *ucat_imp, *p_imp;
-  const double *uo_imp, *urm_imp, *ubcs_imp;
-  double ren_imp, dt_imp, st_imp, cfl_imp, atol_imp, rtol_imp;
-  int ti_imp, tistart_imp, central_imp, max_it_imp;
+  double *ucont_imp, *ucat_imp, *p_imp, *ubcs_imp;
+  const double *uo_imp, *urm_imp;
+  double ren_imp, dt_imp, st_imp, cfl_imp, atol_imp, rtol_imp, intp_imp;
+  int ti_imp, tistart_imp, central_imp, max_it_imp, profile_imp;
   /* the status the next path call returns, then 0 again */
   int fail_next;
   /* cell (box index) the path calls write: solver_mg sets ucont[3m+1] = 42 and
    * phi[m] = 3; update_pressure sets p[m] = 7; projection sets ucont[3m] = 5;
    * projection_cart sets ucont[3m] = 5 and ucat[3m+2] = 9; imp_rk sets
- * ucont[3m] = 11, ucat[3m+1] = 12 and p[m] = 13 */
+ * ucont[3m] = 11, ucat[3m+1] = 12, p[m] = 13 and ubcs[3m+2] = 14, and
+ * returns FluxInSum 0.5 */
   long mark;
 } cvb_record;
 

@@ -19,7 +19,8 @@
 
 extern PetscInt block_number, immersed, wallfunction, les;
 extern PetscInt ti, tistart, imp_MAX_IT;
-extern PetscReal imp_atol, imp_rtol;
+extern PetscReal imp_atol, imp_rtol, FluxInSum;
+extern PetscInt inletprofile;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
 UserMG *ref_usermg(void);
@@ -209,6 +210,18 @@ int main(void) {
   CHECK(shim_vec_data(fine->lUcont)[3 * loc] == 11.0 && shim_vec_data(fine->lUcat)[3 * loc + 1] == 12.0 &&
             shim_vec_data(fine->lP)[loc] == 13.0,
         "lUcont / lUcat / lP not refreshed after ImpRK");
+  /* an inlet on k = 0 and an outlet on the last face: the profile, the
+   * block's immersed-boundary flux, and FluxInSum back as InflowFlux leaves it */
+  fine->bctype[4] = 5;
+  fine->bctype[5] = 4;
+  inletprofile = 11;
+  fine->FluxIntpSum = 0.25;
+  FluxInSum = 0.0;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.n_imp_rk == 2 && REC.profile_imp == 11 && REC.intp_imp == 0.25,
+        "inlet / outlet ImpRK not on the device with its profile and FluxIntpSum");
+  CHECK(FluxInSum == 0.5 && fine->FluxInSum == 0.5, "FluxInSum not set after ImpRK");
+  CHECK(shim_vec_data(fine->Bcs.Ubcs)[3 * REC.mark + 2] == 14.0, "Bcs.Ubcs not written back");
+  fine->bctype[4] = fine->bctype[5] = 1;
   PetscOptionsSetValue("-central", "1");
   CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.central_imp == 1, "-central not passed to ImpRK");
   PetscOptionsSetValue("-central", "0");

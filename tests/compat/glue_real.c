@@ -43,8 +43,8 @@ int ref_contra2cart(const double *ucont, double *ucat);
 int ref_ghost_node_velocity(double *ubcs, double *ucat);
 int ref_convection(const double *ucont, const double *ucat, int central, double *conv);
 int ref_imp_rk(double *ucont, const double *ucont_o, const double *ucont_rm1, double *ucat, double *p,
-               const double *ubcs, double ren, double dt, double st, double cfl, int ti_, int tistart_, int central,
-               double atol, double rtol, int max_it);
+               double *ubcs, double ren, double dt, double st, double cfl, int ti_, int tistart_, int central,
+               double atol, double rtol, int max_it, int profile, double flux_intp_sum);
 extern PetscInt ti, tistart, imp_MAX_IT;
 extern PetscReal imp_atol, imp_rtol;
 
@@ -176,7 +176,7 @@ int main(int argc, char **argv) {
     double *im_uo = copy_of(uc_r2, 3 * n), *im_urm = copy_of(uc_r2, 3 * n), *im_ub = calloc(3 * n, sizeof(double));
     for (size_t q = 0; q < 3 * n; q++) { im_uo[q] *= 0.99; im_urm[q] *= 0.97; }
     immersed = 0;
-    ref_imp_rk(uc_r2, im_uo, im_urm, ucat_r, p_r, im_ub, 300.0, 2e-3, 1.0, 0.5, 5, 0, 0, 1e-7, 1e-4, 6);
+    ref_imp_rk(uc_r2, im_uo, im_urm, ucat_r, p_r, im_ub, 300.0, 2e-3, 1.0, 0.5, 5, 0, 0, 1e-7, 1e-4, 6, 1, 0.0);
     int finite = 1;
     for (size_t q = 0; q < 3 * n; q++) finite = finite && isfinite(uc_r2[q]);
     printf("imp_rk finite %d, max |Ucont| %.3e\n", finite, maxabs(uc_r2, 3 * n));
@@ -285,7 +285,8 @@ int main(int argc, char **argv) {
    * working directory) */
   STEP("ImpRK");
   immersed = 0;
-  ref_imp_rk(im_uc, im_uo, im_urm, im_ucat, im_p, im_ub, imp_ren, imp_dt, 1.0, imp_cfl, 5, 0, 0, 1e-7, 1e-4, 6);
+  fine->FluxIntpSum = 0.0;
+  ref_imp_rk(im_uc, im_uo, im_urm, im_ucat, im_p, im_ub, imp_ren, imp_dt, 1.0, imp_cfl, 5, 0, 0, 1e-7, 1e-4, 6, 1, 0.0);
   int finite = 1;
   for (size_t q = 0; q < 3 * n; q++) finite = finite && isfinite(im_uc[q]);
   CHECK(finite, "ImpRK: Ucont not finite");

@@ -30,8 +30,9 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from cases import (IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, MOM_DT, MOM_REN, conv_seam_nvert, imp_rk_inputs,  # noqa: E402
-                   mom_edge_nvert, momentum_inputs)
+from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_OUTLET_SCENARIOS, INLET_PROFILES,  # noqa: E402
+                   MOM_DT, MOM_REN,
+                   conv_seam_nvert, imp_rk_inputs, mom_edge_nvert, momentum_inputs)
 from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
 from curvib_old_gb300 import workload as W  # noqa: E402
@@ -100,6 +101,8 @@ def run(name):
         R8.set_nvert(nl - 1, c["nvert"])
         rec["momentum_outflow8"] = momentum(R8, c["nvert"], c["ucont"], bct)
         R = O.Reference(c["nodes"], nl, c["bctype"], c["semi"])
+    if name in INLET_OUTLET_SCENARIOS:
+        rec["inlet_outlet"] = inlet_outlet(c)
     np.savez_compressed(OUT / f"{name}.npz", nodes=c["nodes"], nvert=c["nvert"], ucont=c["ucont"])
     return rec
 
@@ -131,18 +134,50 @@ def momentum(R, nvert, ucont, bctype):
     if all(b == 1 for b in bctype):
         # FormBCS and ImpRK (bcs.c:4436, implicitsolver.c:7094), all-wall boxes
         ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(nvert.shape, ucont)
-        u, pp = R.form_bcs(ucont, ubcs1, ucat1, p1)
+        _, _, u, pp = R.form_bcs(ucont, ubcs1, ucat1, p1)
         out["form_bcs"] = {"ucat": digest(u), "p": digest(pp)}
         with tempfile.TemporaryDirectory() as d:
             cwd = os.getcwd()
             os.chdir(d)  # ImpRK appends to Converge_dU0 in the working directory
             try:
                 for ti, cfl, max_it in IMP_RK_RUNS:
-                    uc, u, pp = R.imp_rk(ucont, uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
-                                         IMP_ATOL, IMP_RTOL, max_it)
+                    uc, u, pp, _ = R.imp_rk(ucont, uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
+                                            IMP_ATOL, IMP_RTOL, max_it)
                     out[f"imp_rk_{ti}_{cfl}_{max_it}"] = {"ucont": digest(uc), "ucat": digest(u), "p": digest(pp)}
             finally:
                 os.chdir(cwd)
+    return out
+
+
+def inlet_outlet(c):
+    """InflowFlux, FormBCS and ImpRK (bcs.c:99, 4436; implicitsolver.c:7094) on
+    the scenario's grid with an inlet on the k = 0 face (bctype[4] 5) and an
+    outlet on the last (bctype[5] 4): the constant inlet profiles, FormBCS with
+    the inlet's flux and an immersed-boundary flux, and cases.IMP_RK_RUNS with
+    profile 1."""
+    bct = [1, 1, 1, 1, 5, 4]
+    nl = c["nl"]
+    R = O.Reference(c["nodes"], nl, bct, c["semi"])
+    R.set_nvert(nl - 1, c["nvert"])
+    ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(c["nvert"].shape, c["ucont"])
+    out = {}
+    for prof in INLET_PROFILES:
+        uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, prof)
+        out[f"inflow_{prof}"] = {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)}
+    uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, 1)
+    uc, ub, u, pp = R.form_bcs(uc, ub, ucat1, p1, f, FLUX_INTP_SUM)
+    out["form_bcs"] = {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)}
+    with tempfile.TemporaryDirectory() as d:
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            for ti, cfl, max_it in IMP_RK_RUNS:
+                uc, u, pp, ub = R.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0,
+                                         0, IMP_ATOL, IMP_RTOL, max_it, 1, FLUX_INTP_SUM)
+                out[f"imp_rk_{ti}_{cfl}_{max_it}"] = {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u),
+                                                      "p": digest(pp)}
+        finally:
+            os.chdir(cwd)
     return out
 
 

@@ -89,15 +89,15 @@ def test_form_bcs_and_imp_rk_match_oracle(name):
         try:
             L = O.OLevel(c["metrics"][-1], nvert, bctype, c["semi"])
             ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(nvert.shape, c["ucont"])
-            u_g, p_g = ctx.form_bcs(c["ucont"], ubcs1, ucat1, p1)
-            rc, u_o, p_o = O.form_bcs_walls(L, c["ucont"], ubcs1, ucat1, p1)
+            _, _, u_g, p_g = ctx.form_bcs(c["ucont"], ubcs1, ucat1, p1)
+            rc, _, _, u_o, p_o = O.form_bcs(L, c["ucont"], ubcs1, ucat1, p1)
             assert rc == 0 and _same(u_g, u_o) and _same(p_g, p_o)
             rejected = 0
             for ti, cfl, max_it in IMP_RK_RUNS:
-                uc_g, u_g, p_g, st_g = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
-                                                  ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it)
-                rc, uc_o, u_o, p_o, st_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0,
-                                                    cfl, ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it)
+                uc_g, u_g, p_g, st_g, _ = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0,
+                                                     cfl, ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it)
+                rc, uc_o, u_o, p_o, st_o, _ = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT,
+                                                       1.0, cfl, ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it)
                 assert rc == 0
                 assert (st_g["pseudo_iterations"], st_g["rejected"]) == (st_o.pseudo_iterations, st_o.rejected)
                 assert st_g["lambda"] == st_o.lambda_ and st_g["norm_du"] == st_o.norm_du
@@ -108,18 +108,56 @@ def test_form_bcs_and_imp_rk_match_oracle(name):
             ctx.close()
 
 
+@pytest.mark.parametrize("name", ["box_sphere", "blocked_slab"])
+def test_inlet_outlet_match_oracle(name):
+    """InflowFlux (bcs.c:99) with the constant profiles, FormBCS's outlet
+    correction with an immersed-boundary flux, and ImpRK on the scenario's grid
+    with an inlet on k = 0 and an outlet on the last k face, bit for bit
+    against the oracle (pinned to the reference's routines): ucont, ubcs, ucat,
+    p, FluxInSum and the iteration counts."""
+    from cases import FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, imp_rk_inputs
+    c = build(name)
+    bctype = [1, 1, 1, 1, 5, 4]
+    ctx = _ctx(c, c["nvert"], bctype)
+    try:
+        L = O.OLevel(c["metrics"][-1], c["nvert"], bctype, c["semi"])
+        ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(c["nvert"].shape, c["ucont"])
+        for prof in INLET_PROFILES:
+            uc_g, ub_g, f_g = ctx.inflow_flux(c["ucont"], ubcs1, prof)
+            rc, uc_o, ub_o, f_o = O.inflow_flux(L, c["ucont"], ubcs1, prof)
+            assert rc == 0 and _same(uc_g, uc_o) and _same(ub_g, ub_o) and f_g == f_o, prof
+        uc_i, ub_i, f = ctx.inflow_flux(c["ucont"], ubcs1, 1)
+        got = ctx.form_bcs(uc_i, ub_i, ucat1, p1, f, FLUX_INTP_SUM)
+        rc, *want = O.form_bcs(L, uc_i, ub_i, ucat1, p1, f, FLUX_INTP_SUM)
+        assert rc == 0 and all(_same(a, b) for a, b in zip(got, want))
+        for ti, cfl, max_it in IMP_RK_RUNS:
+            uc_g, u_g, p_g, st_g, ub_g = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
+                                                    ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, 1, FLUX_INTP_SUM)
+            rc, uc_o, u_o, p_o, st_o, ub_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0,
+                                                      cfl, ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, 1, FLUX_INTP_SUM)
+            assert rc == 0
+            assert (st_g["pseudo_iterations"], st_g["rejected"]) == (st_o.pseudo_iterations, st_o.rejected)
+            assert all(_same(a, b) for a, b in ((uc_g, uc_o), (u_g, u_o), (p_g, p_o), (ub_g, ub_o))), (ti, cfl)
+            assert st_g["flux_in_sum"] == O.inflow_flux(L, uc_g, ub_g, 1)[3]
+    finally:
+        ctx.close()
+
+
 def test_imp_rk_refuses_other_face_types():
     from curvib_old_gb300._lib import CVB_BAD_INPUT, CvbError
     from cases import imp_rk_inputs
     c = build("box_sphere")
-    bctype = list(c["bctype"][:5]) + [8]
-    ctx = _ctx(c, c["nvert"], bctype)
-    try:
-        ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(c["nvert"].shape, c["ucont"])
-        for call in (lambda: ctx.form_bcs(c["ucont"], ubcs1, ucat1, p1),
-                     lambda: ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, 1.0, 1, 0)):
-            with pytest.raises(CvbError) as e:
-                call()
-            assert e.value.status == CVB_BAD_INPUT
-    finally:
-        ctx.close()
+    for bctype, prof in ((list(c["bctype"][:5]) + [8], 1), ([1, 1, 1, 1, 1, 4], 1), ([1, 1, 1, 1, 5, 4], 4)):
+        ctx = _ctx(c, c["nvert"], bctype)
+        try:
+            ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(c["nvert"].shape, c["ucont"])
+            calls = [lambda: ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, 1.0, 1, 0,
+                                        inletprofile=prof)]
+            if prof == 1:
+                calls.append(lambda: ctx.form_bcs(c["ucont"], ubcs1, ucat1, p1))
+            for call in calls:
+                with pytest.raises(CvbError) as e:
+                    call()
+                assert e.value.status == CVB_BAD_INPUT, bctype
+        finally:
+            ctx.close()

@@ -216,16 +216,49 @@ def _check_momentum(c, nvert, bctype, want):
     if "form_bcs" in want:
         from cases import IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, imp_rk_inputs
         ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(nvert.shape, c["ucont"])
-        rc, u, pp = O.form_bcs_walls(L, c["ucont"], ubcs1, ucat1, p1)
+        rc, _, _, u, pp = O.form_bcs(L, c["ucont"], ubcs1, ucat1, p1)
         assert rc == 0 and {"ucat": digest(u), "p": digest(pp)} == want["form_bcs"]
         for ti, cfl, max_it in IMP_RK_RUNS:
-            rc, uc, u, pp, _ = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0,
-                                        0, IMP_ATOL, IMP_RTOL, max_it)
+            rc, uc, u, pp, _, _ = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti,
+                                           0, 0, IMP_ATOL, IMP_RTOL, max_it)
             assert rc == 0
             assert {"ucont": digest(uc), "ucat": digest(u), "p": digest(pp)} == want[f"imp_rk_{ti}_{cfl}_{max_it}"], \
                 (ti, cfl, max_it)
     elif all(b == 1 for b in bctype):
         raise AssertionError("all-wall scenario without FormBCS / ImpRK digests")
+
+
+@pytest.mark.parametrize("name", ["box_sphere", "blocked_slab"])
+def test_inlet_outlet_matches_reference(name):
+    """InflowFlux (bcs.c:99-400) with the constant inlet profiles, FormBCS's
+    outlet flux correction (bcs.c:4914-4998) with an immersed-boundary flux,
+    and ImpRK (implicitsolver.c:7094-7257) on a box with an inlet on k = 0 and
+    an outlet on the last k face, bit for bit."""
+    from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_OUTLET_SCENARIOS, INLET_PROFILES, MOM_DT,
+                       MOM_REN, imp_rk_inputs)
+    assert name in INLET_OUTLET_SCENARIOS
+    c = _setup(name)
+    want = REF["scenarios"][name]["inlet_outlet"]
+    bct = [1, 1, 1, 1, 5, 4]
+    L = O.OLevel(c["metrics"][-1], c["nvert"], bct, c["semi"])
+    ucat1, p1, uo1, urm1, ubcs1 = imp_rk_inputs(c["nvert"].shape, c["ucont"])
+    for prof in INLET_PROFILES:
+        rc, uc, ub, f = O.inflow_flux(L, c["ucont"], ubcs1, prof)
+        assert rc == 0 and {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)} == want[f"inflow_{prof}"]
+    rc, uc, ub, f = O.inflow_flux(L, c["ucont"], ubcs1, 1)
+    rc, uc, ub, u, pp = O.form_bcs(L, uc, ub, ucat1, p1, f, FLUX_INTP_SUM)
+    assert rc == 0 and {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)} == \
+        want["form_bcs"]
+    for ti, cfl, max_it in IMP_RK_RUNS:
+        rc, uc, u, pp, _, ub = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
+                                        IMP_ATOL, IMP_RTOL, max_it, 1, FLUX_INTP_SUM)
+        assert rc == 0
+        assert {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)} == \
+            want[f"imp_rk_{ti}_{cfl}_{max_it}"], (ti, cfl, max_it)
+    # a profile that is not restated, an outlet without the inlet
+    assert O.inflow_flux(L, c["ucont"], ubcs1, 4)[0] == -1
+    L2 = O.OLevel(c["metrics"][-1], c["nvert"], [1, 1, 1, 1, 1, 4], c["semi"])
+    assert O.form_bcs(L2, c["ucont"], ubcs1, ucat1, p1)[0] == -1
 
 
 @pytest.mark.parametrize("name", sorted(SCENARIOS))
