@@ -156,6 +156,8 @@ static void free_all(cvb_ctx *ctx) {
   ctx->visc_dev = ctx->rct_dev = ctx->rhs_dev = ctx->uo_dev = ctx->urm_dev = ctx->pu_dev = nullptr;
   ctx->imp_norms = nullptr;
   ctx->bc_scratch = nullptr;
+  if (ctx->bc_host) cudaFreeHost(ctx->bc_host);
+  ctx->bc_host = nullptr;
   ctx->ibm_cent = nullptr;
   ctx->ready = false;
 }
@@ -1794,33 +1796,83 @@ static int inlet_speed(cvb_ctx *ctx, int profile, double *uin) {
 
 static int bc_buffers(cvb_ctx *ctx) {
   const Geom &g = ctx->L[ctx->nlevels - 1].g;
-  if (!ctx->bc_scratch) TRY(dalloc(ctx, &ctx->bc_scratch, 2 * (size_t)(g.mx - 2) * (g.my - 2) + 4));
+  const size_t n2 = (size_t)(g.mx - 2) * (g.my - 2);
+  if (!ctx->bc_scratch) TRY(dalloc(ctx, &ctx->bc_scratch, 2 * n2));
+  if (!ctx->bc_host) {
+    if (cudaMallocHost((void **)&ctx->bc_host, sizeof(double) * 2 * n2) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->bc_host = nullptr;
+      return fail(ctx, CVB_OOM, "pinned host buffer of %zu bytes failed", sizeof(double) * 2 * n2);
+    }
+  }
   return CVB_OK;
 }
-// bc_scratch: [terms: 2 n2 | sums: 2 | FluxInSum | spare]
-static double *bc_flux_in(cvb_ctx *ctx) {
-  const Geom &g = ctx->L[ctx->nlevels - 1].g;
-  return ctx->bc_scratch + 2 * (size_t)(g.mx - 2) * (g.my - 2) + 2;
+
+// The reference adds a plane's terms one after another in its (j, i) loop;
+// the host does the same with the terms the kernels wrote in that order (a
+// chain of dependent FP64 adds is far slower on the GPU).
+static double ordered_sum(const double *t, size_t n) {
+  double s = 0.;
+  for (size_t q = 0; q < n; q++) s += t[q];
+  return s;
 }
 
-static void inflow_dev(cvb_ctx *ctx, double uin) {
+// What InflowFlux leaves for FormBCS's outlet: FluxInSum, and the outlet's
+// area (a sum over its fluid cells' |zet|, the same in every pass).
+struct BcSums {
+  double flux_in = 0.;
+  bool have_flux_in = false;
+  double area = 0.;
+  bool have_area = false;
+  int rc = CVB_OK;
+};
+
+// InflowFlux: the inlet face's ubcs and Ucont.z, and FluxInSum (summed once:
+// its terms depend on the grid and nvert alone).
+static int inflow_dev(cvb_ctx *ctx, double uin, BcSums &bs) {
   LevelDev &F = ctx->L[ctx->nlevels - 1];
-  launch_inflow(F.g, F.nvert, ctx->cm[2], uin, ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch, bc_flux_in(ctx),
-                ctx->stream);
+  const size_t n2 = (size_t)(F.g.mx - 2) * (F.g.my - 2);
+  launch_inflow(F.g, F.nvert, ctx->cm[2], uin, ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch, ctx->stream);
+  if (bs.have_flux_in) return CVB_OK;
+  CKL();
+  CK(cudaMemcpyAsync(ctx->bc_host, ctx->bc_scratch, sizeof(double) * n2, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  bs.flux_in = ordered_sum(ctx->bc_host, n2);
+  bs.have_flux_in = true;
+  return CVB_OK;
 }
 
-static void form_bcs_dev(cvb_ctx *ctx, double flux_intp_sum) {
+// FormBCS's three passes; with an outlet each pass sums its flux on the host
+// and hands the kernel the ratio (bcs.c:4952-4956: FluxIn = FluxInSum +
+// FarFluxInSum (0: no far-field face) + FluxIntpSum).
+static int form_bcs_dev(cvb_ctx *ctx, double flux_intp_sum, BcSums &bs) {
   LevelDev &F = ctx->L[ctx->nlevels - 1];
   const Geom &g = F.g;
+  const size_t n2 = (size_t)(g.mx - 2) * (g.my - 2);
   std::function<void()> outlet;
   if (ctx->H[ctx->nlevels - 1].d.bctype[5] == 4)
-    outlet = [ctx, &F, &g, flux_intp_sum]() {
-      double *terms = ctx->bc_scratch, *sums = terms + 2 * (size_t)(g.mx - 2) * (g.my - 2);
-      launch_outlet(g, F.nvert, ctx->cm[2], ctx->ucat_dev, bc_flux_in(ctx), flux_intp_sum, ctx->uc_dev,
-                    ctx->ubcs_dev, terms, sums, ctx->stream);
+    outlet = [ctx, &F, &g, n2, flux_intp_sum, &bs]() {
+      if (bs.rc) return;
+      launch_outlet_terms(g, F.nvert, ctx->cm[2], ctx->ucat_dev, ctx->bc_scratch, ctx->stream);
+      const size_t nt = bs.have_area ? n2 : 2 * n2;
+      if (cudaMemcpyAsync(ctx->bc_host, ctx->bc_scratch, sizeof(double) * nt, cudaMemcpyDeviceToHost, ctx->stream) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        bs.rc = fail(ctx, CVB_CUDA_ERROR, "FormBCS outlet: %s", cudaGetErrorString(cudaGetLastError()));
+        return;
+      }
+      const double flux_out = ordered_sum(ctx->bc_host, n2);
+      if (!bs.have_area) {
+        bs.area = ordered_sum(ctx->bc_host + n2, n2);
+        bs.have_area = true;
+      }
+      const double flux_in = bs.flux_in + 0. + flux_intp_sum;
+      const double ratio = (flux_in - flux_out) / bs.area;
+      launch_outlet_apply(g, F.nvert, ctx->cm[2], ctx->ucat_dev, ratio, ctx->uc_dev, ctx->ubcs_dev, ctx->stream);
     };
   launch_form_bcs(g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ubcs_dev, ctx->ucat_dev,
                   ctx->p_dev, outlet, ctx->stream);
+  return bs.rc;
 }
 
 int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile, double *flux_in_sum) {
@@ -1836,12 +1888,13 @@ int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile,
   TRY(bc_buffers(ctx));
   CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
-  inflow_dev(ctx, uin);
+  BcSums bs;
+  TRY(inflow_dev(ctx, uin, bs));
   CKL();
   CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(flux_in_sum, bc_flux_in(ctx), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  *flux_in_sum = bs.flux_in;
   return CVB_OK;
 }
 
@@ -1858,8 +1911,10 @@ int cvb_form_bcs(cvb_ctx *ctx, double *ucont, double *ubcs, double *ucat, double
   CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(bc_flux_in(ctx), &flux_in_sum, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  form_bcs_dev(ctx, flux_intp_sum);
+  BcSums bs;
+  bs.flux_in = flux_in_sum;
+  bs.have_flux_in = true;
+  TRY(form_bcs_dev(ctx, flux_intp_sum, bs));
   CKL();
   CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1930,12 +1985,12 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemsetAsync(bc_flux_in(ctx), 0, sizeof(double), ctx->stream));
   // InflowFlux (a wall k = 0 face: nothing), OutflowFlux (it only sums a flux
   // nothing here reads), FormBCS
-  auto boundary = [&]() {
-    if (inlet) inflow_dev(ctx, uin);
-    form_bcs_dev(ctx, o->flux_intp_sum);
+  BcSums bs;
+  auto boundary = [&]() -> int {
+    if (inlet) TRY(inflow_dev(ctx, uin, bs));
+    return form_bcs_dev(ctx, o->flux_intp_sum, bs);
   };
   // Rhs starts at 0 (VecSet, implicitsolver.c:7140); CalcRHS leaves part of
   // its ring as it was
@@ -1949,7 +2004,7 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   };
   // before the loop (implicitsolver.c:7124-7148): the boundary conditions,
   // pUcont = Ucont, CalcRHS
-  boundary();
+  TRY(boundary());
   CK(cudaMemcpyAsync(ctx->pu_dev, ctx->uc_dev, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
   calc_rhs();
   double normF0, normF1 = 1000., normdU1 = 1000., lambda = cfl;
@@ -1964,7 +2019,7 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
     for (int s = 0; s < 4; s++) {
       const double a = lambda * alfa[s] * dt * st;
       launch_imp_waxpy(n3, a, ctx->rhs_dev, ctx->pu_dev, ctx->uc_dev, ctx->stream);
-      boundary();
+      TRY(boundary());
       calc_rhs();
     }
     normdU1 = normdU_bk;
@@ -1999,11 +2054,9 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(p, ctx->p_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
-  double flux_in = 0.;
-  CK(cudaMemcpyAsync(&flux_in, bc_flux_in(ctx), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (stats) {
-    stats->flux_in_sum = flux_in;
+    stats->flux_in_sum = bs.flux_in;
     stats->pseudo_iterations = pseudot;
     stats->rejected = rejected;
     stats->norm_du = normdU;

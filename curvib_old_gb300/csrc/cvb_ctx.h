@@ -96,7 +96,8 @@ struct cvb_ctx {
   double *visc_dev = nullptr, *rct_dev = nullptr, *rhs_dev = nullptr, *uo_dev = nullptr, *urm_dev = nullptr;
   double *pu_dev = nullptr;                // ImpRK: the last kept iterate (pUcont)
   unsigned long long *imp_norms = nullptr; // ImpRK: |Rhs| and |dU| as bit patterns
-  double *bc_scratch = nullptr;            // InflowFlux / outlet: plane terms, sums, FluxInSum
+  double *bc_scratch = nullptr;            // InflowFlux / outlet: plane terms (device)
+  double *bc_host = nullptr;               // the same terms, pinned host memory, for the host's ordered sums
   double *ibm_cent = nullptr;  // cell centres of the last cvb_ibm_search that gave them
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;

@@ -324,17 +324,18 @@ void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const 
                      const double *nvert, double *ucont, double *ubcs, double *ucat, double *p,
                      const std::function<void()> &outlet_pass, cudaStream_t s);
 // InflowFlux on an inlet k = 0 face with a constant speed uin: ubcs and
-// Ucont.z there, and their flux summed in the reference's order into
-// *flux_in (device); terms: (mx - 2)(my - 2) doubles of scratch
+// Ucont.z there, and the face's flux terms in the reference's loop order into
+// terms ((mx - 2)(my - 2) doubles) for the host to add
 void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, double *ucont, double *ubcs,
-                   double *terms, double *flux_in, cudaStream_t s);
-// The outlet's flux correction (one FormBCS pass, bctype[5] 4): the outlet
-// flux and area summed in the reference's order, then ubcs on the last face
-// and Ucont.z of the last interior face; flux_in (device) is FluxInSum; terms:
-// 2 (mx - 2)(my - 2) doubles, sums: 2 doubles of scratch
-void launch_outlet(const Geom &g, const double *nvert, const double *zet, const double *ucat,
-                   const double *flux_in, double flux_intp_sum, double *ucont, double *ubcs, double *terms,
-                   double *sums, cudaStream_t s);
+                   double *terms, cudaStream_t s);
+// The outlet's flux correction (one FormBCS pass, bctype[5] 4): its flux and
+// area terms in the reference's loop order into terms[0 .. n2) and
+// terms[n2 .. 2 n2); then, with the ratio the host formed from their sums,
+// ubcs on the last face and Ucont.z of the last interior face
+void launch_outlet_terms(const Geom &g, const double *nvert, const double *zet, const double *ucat, double *terms,
+                         cudaStream_t s);
+void launch_outlet_apply(const Geom &g, const double *nvert, const double *zet, const double *ucat, double ratio,
+                         double *ucont, double *ubcs, cudaStream_t s);
 // ImpRK's stage update u = a rhs + pu, and its two infinity norms (|rhs|,
 // |pu - u|; pu null: |rhs| only) as bit patterns into out[0..1] (device)
 void launch_imp_waxpy(size_t n, double a, const double *rhs, const double *pu, double *u, cudaStream_t s);

@@ -332,48 +332,13 @@ __global__ void __launch_bounds__(256) k_imp_norms(size_t n, const double *__res
 }
 
 // ------------------------------------------------- InflowFlux, the outlet
-// t[0 .. n) (and t2[0 .. n)) summed in index order, as the reference's loops
-// add them.  One block: warps 1 .. 7 stage chunks of the terms in shared
-// memory (double-buffered), and one thread of warp 0 adds them in order from
-// there, the two sums interleaved, so the adds wait on one another only.
-// Cells the reference skips carry +0.0, which leaves a sum that started at
-// +0.0 as it was.
-constexpr int kSumChunk = 1024, kSumThreads = 256;
-__global__ void __launch_bounds__(kSumThreads) k_seq_sum(const double *__restrict__ t, const double *__restrict__ t2,
-                                                         int n, double *out) {
-  __shared__ double buf[2][2][kSumChunk];
-  const int nchunk = (n + kSumChunk - 1) / kSumChunk;
-  auto stage = [&](int c) {  // warps 1 .. 7 load chunk c
-    const int base = c * kSumChunk;
-    for (int q = (int)threadIdx.x - 32; q < kSumChunk; q += kSumThreads - 32) {
-      const int e = base + q;
-      buf[c & 1][0][q] = e < n ? t[e] : 0.;
-      buf[c & 1][1][q] = (t2 && e < n) ? t2[e] : 0.;
-    }
-  };
-  double s = 0., s2 = 0.;
-  if (threadIdx.x >= 32 && nchunk > 0) stage(0);
-  __syncthreads();
-  for (int c = 0; c < nchunk; c++) {
-    if (threadIdx.x >= 32) {
-      if (c + 1 < nchunk) stage(c + 1);
-    } else if (threadIdx.x == 0) {
-      const double *a = buf[c & 1][0], *b = buf[c & 1][1];
-      const int m = n - c * kSumChunk < kSumChunk ? n - c * kSumChunk : kSumChunk;
-#pragma unroll 16
-      for (int q = 0; q < m; q++) {
-        s += a[q];
-        s2 += b[q];
-      }
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    out[0] = s;
-    if (t2) out[1] = s2;
-  }
-}
-
+// The reference adds a plane's flux and area terms one after another in its
+// (j, i) loop.  A chain of dependent FP64 adds is slow on this GPU (one
+// thread, about 70 cycles an add: 2.5 ms for a 192 x 192 plane), so the
+// kernels below write the terms, in that order, for the host to add; cells
+// the reference skips carry +0.0, which leaves a sum that started at +0.0 as
+// it was.
+//
 // InflowFlux on the k = 0 face (bcs.c:148-236): above a fluid cell, ubcs =
 // uin zet / |zet| (in the reference's order .y, .z, .x, each its own
 // quotient) and Ucont.z = uin |zet|, |zet| summed z, y, x; the face's flux
@@ -399,11 +364,9 @@ __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__
 }
 
 void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, double *ucont, double *ubcs,
-                   double *terms, double *flux_in, cudaStream_t s) {
+                   double *terms, cudaStream_t s) {
   const int n = (g.mx - 2) * (g.my - 2);
   k_inflow<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, uin, ucont, ubcs, terms);
-  count_launch();
-  k_seq_sum<<<1, kSumThreads, 0, s>>>(terms, nullptr, n, flux_in);
   count_launch();
 }
 
@@ -427,14 +390,12 @@ __global__ void k_outlet_terms(Geom g, const double *__restrict__ nv, const doub
   terms[n + t] = a;
 }
 
-// The outlet's correction (bcs.c:4952-4992): ratio = (FluxInSum + 0 +
-// FluxIntpSum - the outlet flux) / the outlet area (the 0 is FarFluxInSum,
-// which has no far-field face to sum here); on its fluid cells ubcs of the
-// last face = the ucat next to it, and Ucont.z of the last interior face =
-// ubcs . zet + ratio |zet|.
+// The outlet's correction (bcs.c:4960-4992) with the ratio the host formed
+// from the sums: on the outlet's fluid cells ubcs of the last face = the ucat
+// next to it, and Ucont.z of the last interior face = ubcs . zet + ratio
+// |zet|.
 __global__ void k_outlet_apply(Geom g, const double *__restrict__ nv, const double *__restrict__ zet,
-                               const double *__restrict__ ucat, const double *__restrict__ flux_in,
-                               double flux_intp_sum, const double *__restrict__ sums, double *__restrict__ uc,
+                               const double *__restrict__ ucat, double ratio, double *__restrict__ uc,
                                double *__restrict__ ub) {
   const int ni = g.mx - 2, n = ni * (g.my - 2);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -442,23 +403,23 @@ __global__ void k_outlet_apply(Geom g, const double *__restrict__ nv, const doub
   const int i = 1 + t % ni, j = 1 + t / ni;
   const size_t q = ((size_t)(g.mz - 2) * g.my + j) * g.mx + i, qb = q + (size_t)g.mx * g.my;
   if (!(nv[q] < 0.1)) return;
-  const double fin = flux_in[0] + 0. + flux_intp_sum;
-  const double ratio = __ddiv_rn(fin - sums[0], sums[1]);
   const double *c = ucat + 3 * q, *z = zet + 3 * q;
   double b[3];
   for (int k = 0; k < 3; k++) b[k] = ub[3 * qb + k] = c[k];
   uc[3 * q + 2] = (b[0] * z[0] + b[1] * z[1] + b[2] * z[2]) + ratio * __dsqrt_rn(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
 }
 
-void launch_outlet(const Geom &g, const double *nvert, const double *zet, const double *ucat,
-                   const double *flux_in, double flux_intp_sum, double *ucont, double *ubcs, double *terms,
-                   double *sums, cudaStream_t s) {
+void launch_outlet_terms(const Geom &g, const double *nvert, const double *zet, const double *ucat, double *terms,
+                         cudaStream_t s) {
   const int n = (g.mx - 2) * (g.my - 2);
   k_outlet_terms<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, ucat, terms);
   count_launch();
-  k_seq_sum<<<1, kSumThreads, 0, s>>>(terms, terms + n, n, sums);
-  count_launch();
-  k_outlet_apply<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, ucat, flux_in, flux_intp_sum, sums, ucont, ubcs);
+}
+
+void launch_outlet_apply(const Geom &g, const double *nvert, const double *zet, const double *ucat, double ratio,
+                         double *ucont, double *ubcs, cudaStream_t s) {
+  const int n = (g.mx - 2) * (g.my - 2);
+  k_outlet_apply<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, ucat, ratio, ucont, ubcs);
   count_launch();
 }
 
