@@ -151,6 +151,24 @@ int cvb_restart_read(const char *dir, int ti, int block, long long ncells, doubl
   return CVB_OK;
 }
 
+int cvb_bcs_dat_read(const char *path, int nblocks, int *bctype, int *periodic) {
+  if (!path || nblocks < 1 || !bctype) return CVB_BAD_INPUT;
+  File r(path, "r");
+  if (!r.f) return CVB_BAD_INPUT;
+  int per[3] = {0, 0, 0};
+  for (int b = 0; b < nblocks; b++) {
+    int *t = bctype + 6 * b;
+    // "%i": decimal, or 0x hexadecimal, or 0 octal, as the reference's fscanf
+    if (std::fscanf(r.f, "%i %i %i %i %i %i", t, t + 1, t + 2, t + 3, t + 4, t + 5) != 6) return CVB_BAD_INPUT;
+    if (t[0] == 7 || t[1] == 7) per[0] = 1;
+    if (t[2] == 7 || t[3] == 7) per[1] = 1;
+    if (t[4] == 7 || t[5] == 7) per[2] = 1;
+  }
+  if (periodic)
+    for (int d = 0; d < 3; d++) periodic[d] = per[d];
+  return CVB_OK;
+}
+
 int cvb_grid_dat_read(const char *path, int block, int grid1d, double cl, double l_dim, int *IM, int *JM, int *KM,
                       double *coords, long long capacity) {
   if (!path || !IM || !JM || !KM || block < 0 || !(cl != 0.0)) return CVB_BAD_INPUT;

@@ -357,6 +357,13 @@ int cvb_restart_write(const char *dir, int ti, int block, long long ncells, cons
                       const double *ucat, const double *p);
 int cvb_restart_read(const char *dir, int ti, int block, long long ncells, double *ucont, double *p,
                      double *nvert_o);
+/* bcs.dat as MG_Initial reads it (init.c:474-490): for each of nblocks
+ * blocks one line of six boundary types ("%i": decimal, 0x hexadecimal or 0
+ * octal), into bctype[6 b .. 6 b + 5]; periodic (may be NULL) gets the i, j, k
+ * periodic flags the reference sets (1 where a block has type 7 on either
+ * face of that direction).  A file with fewer than 6 nblocks numbers is
+ * CVB_BAD_INPUT (the reference leaves those types unread). */
+int cvb_bcs_dat_read(const char *path, int nblocks, int *bctype, int *periodic);
 /* grid.dat as MG_Initial reads it (init.c:339-349, 606-735): the block count,
  * then per block "IM JM KM" and its nodes: all x, then all y, then all z in
  * [k][j][i] order, or with grid1d IM + JM + KM lines of "x y z" (one component

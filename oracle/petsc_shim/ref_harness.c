@@ -484,6 +484,20 @@ int ref_ibm_search(int n_v, const double *xyz, int n_elmt, const int *nv, const 
  * -chact_leng are set as given; L_dim is main.c's global. */
 PetscErrorCode MG_Initial(UserMG *usermg, IBMNodes *ibm);
 PetscReal L_dim = 1.0; /* main.c's length scale of grid.dat's coordinates */
+static UserMG g_mg_initial;
+
+/* The boundary types MG_Initial read from bcs.dat (init.c:478-490) in the
+ * last ref_mg_initial_nodes call, and the i / j / k periodic flags it set. */
+int ref_mg_initial_bctype(int *bctype, int *periodic) {
+  if (!g_mg_initial.mgctx) return 1;
+  UserCtx *u = &g_mg_initial.mgctx[g_mg_initial.mglevels - 1].user[0];
+  for (int f = 0; f < 6; f++) bctype[f] = u->bctype[f];
+  periodic[0] = i_periodic;
+  periodic[1] = j_periodic;
+  periodic[2] = k_periodic;
+  return 0;
+}
+
 int ref_mg_initial_nodes(const char *dir, int nlevels, int grid1d, double cl, double l_dim, int *IM, int *JM,
                          int *KM, double *coords, long long cap) {
   char cwd[4096], val[64];
@@ -494,14 +508,15 @@ int ref_mg_initial_nodes(const char *dir, int nlevels, int grid1d, double cl, do
   snprintf(val, sizeof val, "%.17g", cl); PetscOptionsSetValue("-chact_leng", val);
   L_dim = l_dim;
   block_number = 1;
-  static UserMG mg;
-  memset(&mg, 0, sizeof mg);
+  i_periodic = j_periodic = k_periodic = 0;
+  UserMG *mgp = &g_mg_initial;
+  memset(mgp, 0, sizeof *mgp);
   IBMNodes *ibm = (IBMNodes *)calloc(1, sizeof(IBMNodes));
-  int rc = MG_Initial(&mg, ibm);
+  int rc = MG_Initial(mgp, ibm);
   if (chdir(cwd)) rc = rc ? rc : 2;
   PetscOptionsClear();
   if (rc) return rc;
-  UserCtx *u = &mg.mgctx[mg.mglevels - 1].user[0];
+  UserCtx *u = &mgp->mgctx[mgp->mglevels - 1].user[0];
   *IM = u->IM; *JM = u->JM; *KM = u->KM;
   if ((long long)3 * u->IM * u->JM * u->KM > cap) return 3;
   Vec Coor;

@@ -180,6 +180,47 @@ def test_grid_dat_matches_reference_mg_initial(L, tmp_path, grid1d):
     assert np.array_equal(_read(L, tmp_path / "grid.dat", 0, grid1d, cl, ldim).ravel(), got)
 
 
+def _bcs(L, path, nblocks=1):
+    bc = (ctypes.c_int * (6 * nblocks))()
+    per = (ctypes.c_int * 3)()
+    rc = L.cvb_bcs_dat_read(_b(path), nblocks, bc, per)
+    return rc, list(bc), list(per)
+
+
+def test_bcs_dat_read(L, tmp_path):
+    """bcs.dat as MG_Initial reads it (init.c:474-490): six types per block,
+    fscanf's %i (0x hexadecimal, 0 octal), and the periodic flags."""
+    p = tmp_path / "bcs.dat"
+    p.write_text("7 7 1 1 5 4\n")
+    assert _bcs(L, p) == (0, [7, 7, 1, 1, 5, 4], [1, 0, 0])
+    p.write_text("0x1 010 1 1 7 7\n1 1 7 7 1 1\n")
+    assert _bcs(L, p, 2) == (0, [1, 8, 1, 1, 7, 7, 1, 1, 7, 7, 1, 1], [0, 1, 1])
+    p.write_text("1 1 1 1 1\n")
+    assert _bcs(L, p)[0] == _lib.CVB_BAD_INPUT
+    assert _bcs(L, tmp_path / "missing.dat")[0] == _lib.CVB_BAD_INPUT
+
+
+def test_bcs_dat_matches_reference_mg_initial(L, tmp_path):
+    """The reference's own MG_Initial reads the same bcs.dat to the same
+    boundary types and periodic flags."""
+    from oracle import oracle as O
+    if not (O.REF_DIR / "init.c").exists():
+        pytest.skip("reference checkout not present")
+    from curvib_old_gb300 import workload as W
+    ref = ctypes.CDLL(str(O.build_reference()))
+    nodes = W.box_nodes((8, 6, 10), (1.0, 2.0, 0.5), 2.0, True)
+    _grid_file(tmp_path / "grid.dat", [nodes])
+    (tmp_path / "bcs.dat").write_text("0x1 01 1 3 5 4\n")
+    got = np.zeros(nodes.size)
+    im, jm, km = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert ref.ref_mg_initial_nodes(_b(tmp_path), 2, 0, ctypes.c_double(1.0), ctypes.c_double(1.0), ctypes.byref(im),
+                                    ctypes.byref(jm), ctypes.byref(km), got.ctypes.data_as(ctypes.c_void_p),
+                                    ctypes.c_longlong(got.size)) == 0
+    bc, per = (ctypes.c_int * 6)(), (ctypes.c_int * 3)()
+    assert ref.ref_mg_initial_bctype(bc, per) == 0
+    assert _bcs(L, tmp_path / "bcs.dat") == (0, list(bc), list(per))
+
+
 def _restart_fields(shape, seed):
     rng = np.random.default_rng(seed)
     nvert = np.where(rng.random(shape) < 0.2, 3.0, 0.0)
