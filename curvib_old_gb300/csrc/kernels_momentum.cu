@@ -14,7 +14,43 @@ namespace {
 
 inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-__device__ __forceinline__ bool visc_blocked(double v) { return v > 0.5 && v < 7.; }
+// v > 0.5 && v < 7, on the integer pipe (the kernels here are bound by the
+// FP64 one).  As signed 64-bit integers, the bit patterns of doubles of one
+// sign compare as the values do; every value with the sign bit (negatives, -0,
+// a NaN) lies below 0.5's pattern, and a NaN without it above 7's, so the
+// result is the two comparisons', NaN included.
+__device__ __forceinline__ bool visc_blocked(double v) {
+  const long long b = __double_as_longlong(v);
+  return b > 0x3FE0000000000000LL && b < 0x401C000000000000LL;
+}
+
+// v > c and v < c for c = 0.1, on the integer pipe.  For c > 0: a pattern
+// above c's is a larger positive value, +inf, or a NaN without the sign bit
+// (above +inf's pattern), which compares false; a pattern below c's is a
+// smaller value of either sign, or a NaN with the sign bit (between -inf's
+// pattern and 0 as signed integers), which compares false.
+constexpr long long kBits01 = 0x3FB999999999999ALL, kBitsInf = 0x7FF0000000000000LL,
+                    kBitsNegInf = (long long)0xFFF0000000000000ULL;
+__device__ __forceinline__ bool gt_01(double v) {
+  const long long b = __double_as_longlong(v);
+  return b > kBits01 && b <= kBitsInf;
+}
+__device__ __forceinline__ bool lt_01(double v) {
+  const long long b = __double_as_longlong(v);
+  return b < kBits01 && !(b > kBitsNegInf && b < 0);
+}
+
+// x * 2^-K (K = 1, 2) as the FP64 multiply gives it, on the integer pipe while
+// the result stays normal: K less in the exponent field; a zero stays itself;
+// subnormal results, inf and NaN go through the multiply, out of line.
+__device__ __noinline__ double scale_slow(double x, double f) { return x * f; }
+template <int K>
+__device__ __forceinline__ double scale_down(double x) {
+  const long long b = __double_as_longlong(x), e = (b >> 52) & 0x7ff;
+  if (e > K && e < 0x7ff) return __longlong_as_double(b - ((long long)K << 52));
+  if ((b & 0x7fffffffffffffffLL) == 0) return x;
+  return scale_slow(x, K == 1 ? 0.5 : 0.25);
+}
 
 struct FaceMetrics {
   const double *m[3][3];  // [face direction][csi, eta, zet] Cmpnts arrays
@@ -49,9 +85,9 @@ __global__ void k_visc_faces(Geom g, const double *__restrict__ nv, const double
         const bool dn = visc_blocked(nv[P - s]) || visc_blocked(nv[P + sd - s]);
         for (int c = 0; c < 3; c++) {
 #define U(off) ucat[3 * (P + (off)) + c]
-          if (up) D[t][c] = (U(sd) + U(0) - U(sd - s) - U(-s)) * 0.5;
-          else if (dn) D[t][c] = (U(sd + s) + U(s) - U(sd) - U(0)) * 0.5;
-          else D[t][c] = (U(sd + s) + U(s) - U(sd - s) - U(-s)) * 0.25;
+          if (up) D[t][c] = scale_down<1>(U(sd) + U(0) - U(sd - s) - U(-s));
+          else if (dn) D[t][c] = scale_down<1>(U(sd + s) + U(s) - U(sd) - U(0));
+          else D[t][c] = scale_down<2>(U(sd + s) + U(s) - U(sd - s) - U(-s));
 #undef U
         }
       }
@@ -118,15 +154,15 @@ __global__ void k_ff1_rct(Geom g, const double *__restrict__ conv, const double 
     double rc[3];
     for (int c = 0; c < 3; c++) rc[c] = -1.0 * conv[3 * P + c] + visc[3 * P + c];
     const double a = aj[P];
-    rct[3 * P + 0] = a * (0.5 * (csi[3 * P] + csi[3 * (P - sx)]) * rc[0] +
-                          0.5 * (csi[3 * P + 1] + csi[3 * (P - sx) + 1]) * rc[1] +
-                          0.5 * (csi[3 * P + 2] + csi[3 * (P - sx) + 2]) * rc[2]);
-    rct[3 * P + 1] = a * (0.5 * (eta[3 * P] + eta[3 * (P - sy)]) * rc[0] +
-                          0.5 * (eta[3 * P + 1] + eta[3 * (P - sy) + 1]) * rc[1] +
-                          0.5 * (eta[3 * P + 2] + eta[3 * (P - sy) + 2]) * rc[2]);
-    rct[3 * P + 2] = a * (0.5 * (zet[3 * P] + zet[3 * (P - sz)]) * rc[0] +
-                          0.5 * (zet[3 * P + 1] + zet[3 * (P - sz) + 1]) * rc[1] +
-                          0.5 * (zet[3 * P + 2] + zet[3 * (P - sz) + 2]) * rc[2]);
+    rct[3 * P + 0] = a * (scale_down<1>(csi[3 * P] + csi[3 * (P - sx)]) * rc[0] +
+                          scale_down<1>(csi[3 * P + 1] + csi[3 * (P - sx) + 1]) * rc[1] +
+                          scale_down<1>(csi[3 * P + 2] + csi[3 * (P - sx) + 2]) * rc[2]);
+    rct[3 * P + 1] = a * (scale_down<1>(eta[3 * P] + eta[3 * (P - sy)]) * rc[0] +
+                          scale_down<1>(eta[3 * P + 1] + eta[3 * (P - sy) + 1]) * rc[1] +
+                          scale_down<1>(eta[3 * P + 2] + eta[3 * (P - sy) + 2]) * rc[2]);
+    rct[3 * P + 2] = a * (scale_down<1>(zet[3 * P] + zet[3 * (P - sz)]) * rc[0] +
+                          scale_down<1>(zet[3 * P + 1] + zet[3 * (P - sz) + 1]) * rc[1] +
+                          scale_down<1>(zet[3 * P + 2] + zet[3 * (P - sz) + 2]) * rc[2]);
   }
 }
 
@@ -137,21 +173,21 @@ namespace {
 __device__ __forceinline__ bool ff_dp(const double *__restrict__ nv, const double *__restrict__ p, long P, long sd,
                                       long s, int q, int m, double &val) {
   const double up = nv[P + s] + nv[P + sd + s], dn = nv[P - s] + nv[P + sd - s];
-  if (q == m - 2 || up > 0.1) {
-    if (dn < 0.1 && q != 1) {
-      val = (p[P] + p[P + sd] - p[P - s] - p[P + sd - s]) * 0.5;
+  if (q == m - 2 || gt_01(up)) {
+    if (lt_01(dn) && q != 1) {
+      val = scale_down<1>(p[P] + p[P + sd] - p[P - s] - p[P + sd - s]);
       return true;
     }
     return false;
   }
-  if (q == 1 || dn > 0.1) {
-    if (up < 0.1) {
-      val = (p[P + s] + p[P + sd + s] - p[P] - p[P + sd]) * 0.5;
+  if (q == 1 || gt_01(dn)) {
+    if (lt_01(up)) {
+      val = scale_down<1>(p[P + s] + p[P + sd + s] - p[P] - p[P + sd]);
       return true;
     }
     return false;
   }
-  val = (p[P + s] + p[P + sd + s] - p[P - s] - p[P + sd - s]) * 0.25;
+  val = scale_down<2>(p[P + s] + p[P + sd + s] - p[P - s] - p[P + sd - s]);
   return true;
 }
 
@@ -202,16 +238,16 @@ __global__ void k_ff1_faces(Geom g, const double *__restrict__ nv, const double 
       }
       const double *cs = M.m[d][0] + 3 * P, *et = M.m[d][1] + 3 * P, *zt = M.m[d][2] + 3 * P;
       const double *nd = d == 0 ? cs : d == 1 ? et : zt;
-      double v = 0.5 * (rct[3 * P + d] + rct[3 * (P + st[d]) + d]);
+      double v = scale_down<1>(rct[3 * P + d] + rct[3 * (P + st[d]) + d]);
       v -= (dp[0] * (cs[0] * nd[0] + cs[1] * nd[1] + cs[2] * nd[2]) +
             dp[1] * (et[0] * nd[0] + et[1] * nd[1] + et[2] * nd[2]) +
             dp[2] * (zt[0] * nd[0] + zt[1] * nd[1] + zt[2] * nd[2])) * M.aj[d][P];
       out[d] = v;
     }
-    if (nv[P] > 0.1) out[0] = out[1] = out[2] = 0;
-    if (nv[P + st[0]] > 0.1) out[0] = 0;
-    if (nv[P + st[1]] > 0.1) out[1] = 0;
-    if (nv[P + st[2]] > 0.1) out[2] = 0;
+    if (gt_01(nv[P])) out[0] = out[1] = out[2] = 0;
+    if (gt_01(nv[P + st[0]])) out[0] = 0;
+    if (gt_01(nv[P + st[1]])) out[1] = 0;
+    if (gt_01(nv[P + st[2]])) out[2] = 0;
     for (int c = 0; c < 3; c++) rhs[3 * P + c] = out[c];
   }
 }
@@ -250,7 +286,7 @@ __global__ void k_calc_rhs(Geom g, const double *__restrict__ nv, const double *
         du = uc[q];
         du *= 1.5;
         du += -2. * uo[q];
-        du += 0.5 * urm[q];
+        du += scale_down<1>(urm[q]);
       } else {
         du = -1. * uo[q] + uc[q];
       }
@@ -260,9 +296,9 @@ __global__ void k_calc_rhs(Geom g, const double *__restrict__ nv, const double *
     const bool in = i >= 1 && i <= mx - 2 && j >= 1 && j <= my - 2 && k >= 1 && k <= mz - 2;
     if (in) {
       const size_t sx = 1, sy = mx, sz = (size_t)mx * my;
-      if ((nv[e] + nv[e + sx]) > 0.1 || i > mx - 3) r[0] = 0.;
-      if ((nv[e] + nv[e + sy]) > 0.1 || j > my - 3) r[1] = 0.;
-      if ((nv[e] + nv[e + sz]) > 0.1 || k > mz_end) r[2] = 0.;
+      if (gt_01(nv[e] + nv[e + sx]) || i > mx - 3) r[0] = 0.;
+      if (gt_01(nv[e] + nv[e + sy]) || j > my - 3) r[1] = 0.;
+      if (gt_01(nv[e] + nv[e + sz]) || k > mz_end) r[2] = 0.;
       if (mz_end == mz - 2 && k == mz - 2) r[2] += 0.8 * (uc[3 * e + 2] - uc[3 * (e - sz) + 2]);
     }
     // the six boundary loops (each covers its face minus the last row of the
