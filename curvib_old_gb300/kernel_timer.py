@@ -10,7 +10,12 @@ smoother: residual on one color, then its line solves), vcycle_f32, vcycle_f64
 CUDA graph; no byte count), contra2cart, ghost_nodes, convection
 (Contra2Cart, GhostNodeVelocity and Convection; finest level only), viscous,
 momentum_rhs (Viscous, and CalcRHS with FormFunction1's Convection and
-pressure gradient; finest level only); default: all.  ``--grid channel`` (the
+pressure gradient; finest level only), imp_rk (one pseudo-time iteration of
+ImpRK -- the boundary conditions and CalcRHS, then four Runge-Kutta stages --
+on the box with a sphere of radius 0.25, an inlet on k = 0 and an outlet on
+the last k face, Re 300, dt 2e-3, cfl 0.05, from a uniform stream; the call
+is timed on the host, twice, the second inside the NVTX range); default: all
+but imp_rk.  ``--grid channel`` (the
 default) is the periodic channel (x and z periodic, tanh-stretched walls in y,
 factor 2.5) at the given cell counts, whose operator is 7-point; ``--grid box``
 is a walled box of the same cell counts (tanh 2.0 in y, nodes moved by sine
@@ -46,19 +51,23 @@ def _cells(text):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("kernels", nargs="*", default=list(KERNELS))
+    extra = {"imp_rk"}
     ap.add_argument("--cells", type=_cells, default=(256, 128, 128))
     ap.add_argument("--level", type=int, default=-1, help="multigrid level (0 coarsest, -1 finest)")
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--grid", choices=["channel", "box"], default="channel")
     a = ap.parse_args(argv)
     for k in a.kernels:
-        if k not in KERNELS:
-            ap.error(f"unknown kernel {k!r}; choose from {sorted(KERNELS)}")
+        if k not in KERNELS and k not in extra:
+            ap.error(f"unknown kernel {k!r}; choose from {sorted(set(KERNELS) | extra)}")
     import torch  # NVTX ranges only; the kernels themselves come from libcvb.so
 
     ctx = box = None
     on_box = {"convection", "viscous", "momentum_rhs"}
     for k in a.kernels:
+        if k == "imp_rk":
+            _imp_rk_iteration(a.cells, torch)
+            continue
         if k in on_box or a.grid == "box":
             box = box or PoissonContext().setup(W.make_problem(a.cells, (1.0, 1.0, 1.0), 2.0, True,
                                                                (False, False, False), [], name="box"))
@@ -75,6 +84,31 @@ def main(argv=None):
     for c in (ctx, box):
         if c:
             c.close()
+
+
+def _imp_rk_iteration(cells, torch):
+    import time
+    P = W.make_problem(cells, (1.0, 1.0, 1.0), 2.0, True, (False, False, False), [(0.5, 0.5, 0.5, 0.25)],
+                       name="box-inout")
+    P.bctype = [1, 1, 1, 1, 5, 4]
+    c = PoissonContext().setup(P)
+    sh = P.nvert.shape
+    zet, nv = P.metrics[-1]["Zet"], P.nvert
+    u0 = np.zeros(sh + (3,))
+    fluid = (nv[:-1] < 0.1) & (nv[1:] < 0.1)
+    u0[:-1, 1:-1, 1:-1, 2] = np.where(fluid[:, 1:-1, 1:-1], 2.0 * np.sqrt((zet[:-1, 1:-1, 1:-1] ** 2).sum(-1)), 0.0)
+    z3, z1 = np.zeros(sh + (3,)), np.zeros(sh)
+    for rep in range(2):
+        if rep:
+            torch.cuda.nvtx.range_push("timed:imp_rk")
+        t0 = time.perf_counter()
+        out = c.imp_rk(u0, u0, u0, z3, z1, z3, 300.0, 2e-3, 1.0, 0.05, 1, 0, 0, 1e-7, 1e-4, 1, 1, 0.0)
+        ms = (time.perf_counter() - t0) * 1e3
+        if rep:
+            torch.cuda.nvtx.range_pop()
+    print(json.dumps({"kernel": "imp_rk", "cells": int(np.prod(sh)), "ms_per_call": round(ms, 2),
+                      "pseudo_iterations": out[3]["pseudo_iterations"], "stages": 5}))
+    c.close()
 
 
 if __name__ == "__main__":
