@@ -1567,10 +1567,11 @@ static int ghost_types_ok(cvb_ctx *ctx, const int *bc) {
   return CVB_OK;
 }
 
+static int ensure_c2c(cvb_ctx *ctx);
 static int post_buffers(cvb_ctx *ctx, size_t n) {
   if (!ctx->ucat_dev) TRY(dalloc(ctx, &ctx->ucat_dev, 3 * n));
   if (!ctx->ubcs_dev) TRY(dalloc(ctx, &ctx->ubcs_dev, 3 * n));
-  return CVB_OK;
+  return ensure_c2c(ctx);
 }
 
 int cvb_contra2cart(cvb_ctx *ctx, const double *ucont, double *ucat) {
@@ -1582,7 +1583,8 @@ int cvb_contra2cart(cvb_ctx *ctx, const double *ucont, double *ucat) {
   TRY(post_buffers(ctx, n));
   CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
-  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream, 1,
+                     -1, ctx->geo->c2c);
   CKL();
   CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1626,7 +1628,8 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
   const double *fm[9];
   for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
   launch_projection(F.g, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], F.nvert, ctx->w, dt, st, ctx->uc_dev, ctx->stream);
-  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+  launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream, 1,
+                     -1, ctx->geo->c2c);
   launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream);
   CKL();
   CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1655,7 +1658,41 @@ int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int ce
   return CVB_OK;
 }
 
+// The grid's Contra2Cart factors (k_c2c_factors: the metric rows' minors and
+// determinant of every interior cell), formed on first use and kept with the
+// grid's metrics.
+static int ensure_c2c(cvb_ctx *ctx) {
+  Geometry &G = *ctx->geo;
+  if (G.c2c) return CVB_OK;
+  const int l = ctx->nlevels - 1;
+  double *fac = nullptr;
+  TRY(galloc(ctx, G, &fac, 10 * ctx->L[l].g.n()));
+  launch_c2c_factors(ctx->L[l].g, ctx->cm[0], ctx->cm[1], ctx->cm[2], fac, ctx->stream);
+  CKL();
+  CK(cudaStreamSynchronize(ctx->stream));
+  G.c2c = fac;
+  return CVB_OK;
+}
+
 // --- the momentum right-hand side ------------------------------------------
+// The grid's face metric products (k_face_gram), formed on first use and kept
+// with the grid's metrics; the stream is synchronised once so that contexts
+// sharing the grid on other streams see them.
+static int ensure_face_gram(cvb_ctx *ctx) {
+  Geometry &G = *ctx->geo;
+  if (G.gram) return CVB_OK;
+  const int l = ctx->nlevels - 1;
+  double *gram = nullptr;
+  TRY(galloc(ctx, G, &gram, 9 * ctx->L[l].g.n()));
+  const double *fm[9];
+  for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
+  launch_face_gram(ctx->L[l].g, fm, gram, ctx->stream);
+  CKL();
+  CK(cudaStreamSynchronize(ctx->stream));
+  G.gram = gram;
+  return CVB_OK;
+}
+
 // Device inputs of FormFunction1 / CalcRHS on the finest level: ucont, ucat,
 // p and the incoming rhs copied in (NULL ucont / ucat: the device copies the
 // last projection left), the scratch allocated on first use.
@@ -1676,6 +1713,7 @@ static int momentum_prepare(cvb_ctx *ctx, const char *who, const double *ucont, 
   if (!ctx->visc_dev) TRY(dalloc(ctx, &ctx->visc_dev, 3 * n));
   if (!ctx->rct_dev) TRY(dalloc(ctx, &ctx->rct_dev, 3 * n));
   if (!ctx->rhs_dev) TRY(dalloc(ctx, &ctx->rhs_dev, 3 * n));
+  TRY(ensure_face_gram(ctx));
   if (ucont) CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   if (ucat) CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->p_dev, p, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -1694,13 +1732,14 @@ static void momentum_ff1(cvb_ctx *ctx, double ren, int central, bool cart = true
   const double *fm[9];
   for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
   if (cart)
-    launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+    launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream, 1,
+                     -1, ctx->geo->c2c);
   launch_convection(F.g, ctx->uc_dev, ctx->ucat_dev, F.nvert, central != 0, ctx->conv_fp, ctx->conv_dev, ctx->stream);
-  launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], 1. / ren, ctx->conv_fp,
-                 ctx->visc_dev, ctx->stream);
+  launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], ctx->geo->gram, 1. / ren,
+                 ctx->conv_fp, ctx->visc_dev, ctx->stream);
   launch_form_function1(F.g, F.nvert, ctx->p_dev, ctx->conv_dev, ctx->visc_dev, ctx->cm[0], ctx->cm[1], ctx->cm[2],
-                        ctx->aj64[l], fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], ctx->rct_dev, ctx->rhs_dev,
-                        ctx->stream);
+                        ctx->aj64[l], fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], ctx->geo->gram, ctx->rct_dev,
+                        ctx->rhs_dev, ctx->stream);
 }
 
 static int momentum_finish(cvb_ctx *ctx, double *ucat, double *rhs) {
@@ -1727,10 +1766,11 @@ int cvb_viscous(cvb_ctx *ctx, const double *ucat, double ren, double *visc) {
   if (!ctx->conv_fp) TRY(dalloc(ctx, &ctx->conv_fp, 9 * n));
   if (!ctx->visc_dev) TRY(dalloc(ctx, &ctx->visc_dev, 3 * n));
   if (ucat) CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  TRY(ensure_face_gram(ctx));
   const double *fm[9];
   for (int q = 0; q < 9; q++) fm[q] = ctx->fm[l][q];
-  launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], 1. / ren, ctx->conv_fp,
-                 ctx->visc_dev, ctx->stream);
+  launch_viscous(F.g, F.nvert, ctx->ucat_dev, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], ctx->geo->gram, 1. / ren,
+                 ctx->conv_fp, ctx->visc_dev, ctx->stream);
   CKL();
   CK(cudaMemcpyAsync(visc, ctx->visc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1870,8 +1910,8 @@ static int form_bcs_dev(cvb_ctx *ctx, double flux_intp_sum, BcSums &bs) {
       const double ratio = (flux_in - flux_out) / bs.area;
       launch_outlet_apply(g, F.nvert, ctx->cm[2], ctx->ucat_dev, ratio, ctx->uc_dev, ctx->ubcs_dev, ctx->stream);
     };
-  launch_form_bcs(g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ubcs_dev, ctx->ucat_dev,
-                  ctx->p_dev, outlet, ctx->stream);
+  launch_form_bcs(g, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->geo->c2c, F.nvert, ctx->uc_dev, ctx->ubcs_dev,
+                  ctx->ucat_dev, ctx->p_dev, outlet, ctx->stream);
   return bs.rc;
 }
 
@@ -1979,6 +2019,7 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   if (!ctx->pu_dev) TRY(dalloc(ctx, &ctx->pu_dev, n3));
   if (!ctx->imp_norms) TRY(dalloc(ctx, &ctx->imp_norms, 2));
   TRY(bc_buffers(ctx));
+  TRY(ensure_face_gram(ctx));
   CK(cudaMemcpyAsync(ctx->uc_dev, ucont, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->uo_dev, ucont_o, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->urm_dev, ucont_rm1, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
@@ -2516,7 +2557,8 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       case CVB_KERNEL_RESIDUAL_F64: launch_residual<double>(L, L.r64, L.e64, L.t64, ctx->stream); break;
       case CVB_KERNEL_ZEBRA_F32: launch_zebra_half<float>(L, L.r32, L.e32, L.t32 + n, 1.3f, 1, false, ctx->stream); break;
       case CVB_KERNEL_CONTRA2CART:
-        launch_contra2cart(L.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], L.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream);
+        launch_contra2cart(L.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], L.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream,
+                           1, -1, ctx->geo->c2c);
         break;
       case CVB_KERNEL_GHOST_NODES:
         launch_ghost_node_velocity(L.g, ctx->H[level].d.bctype, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev,
@@ -2528,8 +2570,8 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       case CVB_KERNEL_VISCOUS: {
         const double *fm[9];
         for (int q = 0; q < 9; q++) fm[q] = ctx->fm[level][q];
-        launch_viscous(L.g, L.nvert, ctx->ucat_dev, fm, ctx->iaj[level], ctx->jaj[level], ctx->kaj[level], 1. / 300.,
-                       ctx->conv_fp, ctx->visc_dev, ctx->stream);
+        launch_viscous(L.g, L.nvert, ctx->ucat_dev, fm, ctx->iaj[level], ctx->jaj[level], ctx->kaj[level],
+                       ctx->geo->gram, 1. / 300., ctx->conv_fp, ctx->visc_dev, ctx->stream);
         break;
       }
       case CVB_KERNEL_MOMENTUM_RHS:
@@ -2564,6 +2606,7 @@ int cvb_time_kernel(cvb_ctx *ctx, int kernel, int level, int reps, double *avg_m
       CK(cudaMemsetAsync(ctx->rhs_dev, 0, sizeof(double) * 3 * n, ctx->stream));
       CK(cudaMemsetAsync(ctx->uo_dev, 0, sizeof(double) * 3 * n, ctx->stream));
       CK(cudaMemsetAsync(ctx->urm_dev, 0, sizeof(double) * 3 * n, ctx->stream));
+      TRY(ensure_face_gram(ctx));
     }
     // a velocity field of mixed signs in [-1, 1] (zero fluxes would send every
     // face through the full QUICK expression)

@@ -31,6 +31,8 @@ struct Geometry {
   double *area3 = nullptr;                // finest: |csi|, |eta|, |zet| per cell ([3][N])
   double *cm[3] = {};                     // finest: centre metrics csi, eta, zet (Cmpnts, [N][3])
   double *inv_aj = nullptr;               // finest: 1 / aj, for the range projection's sum of b / aj
+  double *gram = nullptr;                 // finest, on first use: face metric products ([9][N], see k_face_gram)
+  double *c2c = nullptr;                  // finest, on first use: Contra2Cart's minors and determinant ([10][N])
   ~Geometry() {
     if (allocs.empty()) return;
     cudaSetDevice(device);

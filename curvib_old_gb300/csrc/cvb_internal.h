@@ -289,9 +289,13 @@ struct IbmWork {
 // The search; tmp is one more [mz][my][mx] array.  The result is left in tmp.
 void launch_ibm_search(const IbmArgs &A, const IbmWork &W, double *tmp, cudaStream_t s);
 
+// fac: the grid's Contra2Cart factors (launch_c2c_factors, 10 N doubles), or
+// null to form them in the kernel
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
                         const double *nvert, const double *ucont, double *ucat, cudaStream_t s, int k0 = 1,
-                        int nk = -1);
+                        int nk = -1, const double *fac = nullptr);
+void launch_c2c_factors(const Geom &g, const double *csi, const double *eta, const double *zet, double *fac,
+                        cudaStream_t s);
 // max |div| and its first box index into out_v / out_i (device); pv / pi
 // hold 1024 partial pairs
 void launch_divergence(const Geom &g, const double *ucont, const double *aj, const double *nvert, double *pv,
@@ -304,13 +308,15 @@ void launch_metrics_divergence(const Geom &g, const double *csi, const double *e
 // The momentum right-hand side (kernels_momentum.cu), boxes with no periodic
 // face.  fm: the nine face-metric arrays (I, J, K x csi, eta, zet); fp: 9 N
 // doubles of scratch; rct: 3 N doubles of scratch.
+// gram: the 9 N face metric products of launch_face_gram (formed once per grid)
+void launch_face_gram(const Geom &g, const double *const *fm, double *gram, cudaStream_t s);
 void launch_viscous(const Geom &g, const double *nvert, const double *ucat, const double *const *fm,
-                    const double *iaj, const double *jaj, const double *kaj, double nu, double *fp, double *visc,
-                    cudaStream_t s);
+                    const double *iaj, const double *jaj, const double *kaj, const double *gram, double nu,
+                    double *fp, double *visc, cudaStream_t s);
 void launch_form_function1(const Geom &g, const double *nvert, const double *p, const double *conv,
                            const double *visc, const double *csi, const double *eta, const double *zet,
                            const double *aj, const double *const *fm, const double *iaj, const double *jaj,
-                           const double *kaj, double *rct, double *rhs, cudaStream_t s);
+                           const double *kaj, const double *gram, double *rct, double *rhs, cudaStream_t s);
 void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, const double *ucont_o,
                      const double *ucont_rm1, int bdf2, double neg_inv_dt, int mz_end, double *rhs, cudaStream_t s);
 // bc: the level's bctype[6]; the host has refused the types it does not cover
@@ -320,7 +326,7 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
 // flux correction (outlet_pass, empty for a walled k = mz - 1 face; it
 // launches on s), Contra2Cart, the ghost faces' interior cells and the 12
 // edge averages of ucat and p
-void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const double *zet,
+void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const double *zet, const double *fac,
                      const double *nvert, double *ucont, double *ubcs, double *ucat, double *p,
                      const std::function<void()> &outlet_pass, cudaStream_t s);
 // InflowFlux on an inlet k = 0 face with a constant speed uin: ubcs and

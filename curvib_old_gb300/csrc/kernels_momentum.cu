@@ -63,7 +63,7 @@ struct FaceMetrics {
 // and P + e_d, into fp[(3 d + c) N + P]; the derivatives across the face's two
 // tangential directions are one-sided next to cells with nvert in (0.5, 7).
 __global__ void k_visc_faces(Geom g, const double *__restrict__ nv, const double *__restrict__ ucat, FaceMetrics M,
-                             double nu, double *__restrict__ fp) {
+                             const double *__restrict__ gram, double nu, double *__restrict__ fp) {
   const size_t n = g.n();
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e % g.mx), j = (int)((e / g.mx) % g.my), k = (int)(e / ((size_t)g.mx * g.my));
@@ -94,8 +94,8 @@ __global__ void k_visc_faces(Geom g, const double *__restrict__ nv, const double
       const double *mc = M.m[d][0] + 3 * P, *me = M.m[d][1] + 3 * P, *mz = M.m[d][2] + 3 * P;
       const double *mm[3] = {mc, me, mz};
       const double *nd = mm[d];
-      double gg[3];
-      for (int a = 0; a < 3; a++) gg[a] = mm[a][0] * nd[0] + mm[a][1] * nd[1] + mm[a][2] * nd[2];
+      double gg[3];  // mm[a] . nd, from k_face_gram
+      for (int a = 0; a < 3; a++) gg[a] = gram[(size_t)(3 * d + a) * n + e];
       double r[3][3];
       for (int qq = 0; qq < 3; qq++)
         for (int c = 0; c < 3; c++) r[qq][c] = D[0][qq] * mm[0][c] + D[1][qq] * mm[1][c] + D[2][qq] * mm[2][c];
@@ -125,15 +125,39 @@ __global__ void k_visc_div(Geom g, const double *__restrict__ fp, double *__rest
   }
 }
 
+// The metric products the viscous flux and FormFunction1's pressure gradient
+// both form on every face (rhs.c's g11, g21, g31 of the face): gram[(3 d + a)
+// N + P] = M[d][a] . M[d][d] at cell P (x, y, z products summed in that
+// order, as the two kernels wrote them).  They depend on the grid alone, so
+// they are formed once per grid and read back, the same values bit for bit.
+__global__ void k_face_gram(Geom g, FaceMetrics M, double *__restrict__ gram) {
+  const size_t n = g.n();
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    for (int d = 0; d < 3; d++) {
+      const double *nd = M.m[d][d] + 3 * e;
+      for (int a = 0; a < 3; a++) {
+        const double *mm = M.m[d][a] + 3 * e;
+        gram[(size_t)(3 * d + a) * n + e] = mm[0] * nd[0] + mm[1] * nd[1] + mm[2] * nd[2];
+      }
+    }
+}
+
+void launch_face_gram(const Geom &g, const double *const *fm, double *gram, cudaStream_t s) {
+  FaceMetrics M;
+  for (int d = 0; d < 3; d++)
+    for (int a = 0; a < 3; a++) M.m[d][a] = fm[3 * d + a];
+  k_face_gram<<<blocks_for(g.n(), 256), 256, 0, s>>>(g, M, gram); count_launch();
+}
+
 void launch_viscous(const Geom &g, const double *nvert, const double *ucat, const double *const *fm,
-                    const double *iaj, const double *jaj, const double *kaj, double nu, double *fp, double *visc,
-                    cudaStream_t s) {
+                    const double *iaj, const double *jaj, const double *kaj, const double *gram, double nu, double *fp,
+                    double *visc, cudaStream_t s) {
   FaceMetrics M;
   for (int d = 0; d < 3; d++)
     for (int a = 0; a < 3; a++) M.m[d][a] = fm[3 * d + a];
   M.aj[0] = iaj; M.aj[1] = jaj; M.aj[2] = kaj;
   const unsigned nb = blocks_for(g.n(), 128);
-  k_visc_faces<<<nb, 128, 0, s>>>(g, nvert, ucat, M, nu, fp); count_launch();
+  k_visc_faces<<<nb, 128, 0, s>>>(g, nvert, ucat, M, gram, nu, fp); count_launch();
   k_visc_div<<<blocks_for(g.n(), 256), 256, 0, s>>>(g, fp, visc); count_launch();
 }
 
@@ -202,7 +226,8 @@ __device__ __forceinline__ bool ff_dp(const double *__restrict__ nv, const doubl
 // derivatives, where its own branch or, failing that, its y-section assigned
 // dpde, and its dpdz = p[k+1] - p[k] -- and 0 before the first cell.
 __global__ void k_ff1_faces(Geom g, const double *__restrict__ nv, const double *__restrict__ p,
-                            const double *__restrict__ rct, FaceMetrics M, double *__restrict__ rhs) {
+                            const double *__restrict__ rct, FaceMetrics M, const double *__restrict__ gram,
+                            double *__restrict__ rhs) {
   const size_t n = g.n();
   const long st[3] = {1, g.mx, (long)g.mx * g.my};
   const int m[3] = {g.mx, g.my, g.mz};
@@ -236,12 +261,10 @@ __global__ void k_ff1_faces(Geom g, const double *__restrict__ nv, const double 
         if (t == d) dp[t] = p[P + st[d]] - p[P];
         else ff_dp(nv, p, P, st[d], st[t], q[t], m[t], dp[t]);
       }
-      const double *cs = M.m[d][0] + 3 * P, *et = M.m[d][1] + 3 * P, *zt = M.m[d][2] + 3 * P;
-      const double *nd = d == 0 ? cs : d == 1 ? et : zt;
+      // (csi . nd, eta . nd, zet . nd) of face d, from k_face_gram
+      const double *gr = gram + (size_t)(3 * d) * n + P;
       double v = scale_down<1>(rct[3 * P + d] + rct[3 * (P + st[d]) + d]);
-      v -= (dp[0] * (cs[0] * nd[0] + cs[1] * nd[1] + cs[2] * nd[2]) +
-            dp[1] * (et[0] * nd[0] + et[1] * nd[1] + et[2] * nd[2]) +
-            dp[2] * (zt[0] * nd[0] + zt[1] * nd[1] + zt[2] * nd[2])) * M.aj[d][P];
+      v -= (dp[0] * gr[0] + dp[1] * gr[n] + dp[2] * gr[2 * n]) * M.aj[d][P];
       out[d] = v;
     }
     if (gt_01(nv[P])) out[0] = out[1] = out[2] = 0;
@@ -255,13 +278,13 @@ __global__ void k_ff1_faces(Geom g, const double *__restrict__ nv, const double 
 void launch_form_function1(const Geom &g, const double *nvert, const double *p, const double *conv,
                            const double *visc, const double *csi, const double *eta, const double *zet,
                            const double *aj, const double *const *fm, const double *iaj, const double *jaj,
-                           const double *kaj, double *rct, double *rhs, cudaStream_t s) {
+                           const double *kaj, const double *gram, double *rct, double *rhs, cudaStream_t s) {
   FaceMetrics M;
   for (int d = 0; d < 3; d++)
     for (int a = 0; a < 3; a++) M.m[d][a] = fm[3 * d + a];
   M.aj[0] = iaj; M.aj[1] = jaj; M.aj[2] = kaj;
   k_ff1_rct<<<blocks_for(g.n(), 256), 256, 0, s>>>(g, conv, visc, csi, eta, zet, aj, rct); count_launch();
-  k_ff1_faces<<<blocks_for(g.n(), 128), 128, 0, s>>>(g, nvert, p, rct, M, rhs); count_launch();
+  k_ff1_faces<<<blocks_for(g.n(), 128), 128, 0, s>>>(g, nvert, p, rct, M, gram, rhs); count_launch();
 }
 
 // ------------------------------------------------------------------ CalcRHS

@@ -30,20 +30,70 @@ __device__ __forceinline__ double half_exact(double x) {
   return half_slow(x);
 }
 __device__ __forceinline__ double mean2(double a, double b) { return half_exact(da(a, b)); }
-// a*(b*c - d*e), the cofactor product of Cramer's rule
-__device__ __forceinline__ double cof(double a, double b, double c, double d, double e) {
-  return dm(a, ds(dm(b, c), dm(d, e)));
-}
 
 // Contra2Cart: one thread per interior cell; cells with 0.1 <= nvert <= 7 keep
 // their ucat.  The metric rows and fluxes are the means of the cell's two
-// faces in each direction.
+// faces in each direction.  The metric rows depend on the grid alone, and so
+// do the nine 2 x 2 minors of Cramer's rule and the determinant: FAC reads
+// them from k_c2c_factors' arrays (the same values, bit for bit) and forms
+// only the numerators and the quotients per call.
+constexpr int kC2cFactors = 10;  // minors A..I, then the determinant
+
+// The minors b c - d e of the metric rows m, in the order k_contra2cart uses
+// them: A = m11 m22 - m12 m21, B = m10 m22 - m12 m20, C = m10 m21 - m11 m20,
+// D = m01 m22 - m02 m21, E = m01 m12 - m02 m11, F = m00 m22 - m02 m20,
+// G = m00 m12 - m02 m10, H = m00 m21 - m01 m20, I = m00 m11 - m01 m10; and
+// det = m00 A - m01 B + m02 C.
+__device__ __forceinline__ void c2c_minors(const double (&m)[3][3], double (&f)[kC2cFactors]) {
+  auto mn = [](double b, double c, double d, double e) { return ds(dm(b, c), dm(d, e)); };
+  f[0] = mn(m[1][1], m[2][2], m[1][2], m[2][1]);
+  f[1] = mn(m[1][0], m[2][2], m[1][2], m[2][0]);
+  f[2] = mn(m[1][0], m[2][1], m[1][1], m[2][0]);
+  f[3] = mn(m[0][1], m[2][2], m[0][2], m[2][1]);
+  f[4] = mn(m[0][1], m[1][2], m[0][2], m[1][1]);
+  f[5] = mn(m[0][0], m[2][2], m[0][2], m[2][0]);
+  f[6] = mn(m[0][0], m[1][2], m[0][2], m[1][0]);
+  f[7] = mn(m[0][0], m[2][1], m[0][1], m[2][0]);
+  f[8] = mn(m[0][0], m[1][1], m[0][1], m[1][0]);
+  f[9] = da(ds(dm(m[0][0], f[0]), dm(m[0][1], f[1])), dm(m[0][2], f[2]));
+}
+
+__device__ __forceinline__ void c2c_rows(Geom g, const double *__restrict__ csi, const double *__restrict__ eta,
+                                         const double *__restrict__ zet, size_t p, double (&m)[3][3]) {
+  const size_t pw = p - 1, ps = p - g.mx, pb = p - (size_t)g.mx * g.my;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    m[0][c] = mean2(csi[3 * pw + c], csi[3 * p + c]);
+    m[1][c] = mean2(eta[3 * ps + c], eta[3 * p + c]);
+    m[2][c] = mean2(zet[3 * pb + c], zet[3 * p + c]);
+  }
+}
+
+// The minors and determinant of every interior cell into fac[q N + p].
+__global__ void __launch_bounds__(256) k_c2c_factors(Geom g, const double *__restrict__ csi,
+                                                     const double *__restrict__ eta, const double *__restrict__ zet,
+                                                     double *__restrict__ fac) {
+  const int ni = g.mx - 2, nj = g.my - 2;
+  const size_t cells = (size_t)ni * nj * (g.mz - 2), n = g.n();
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cells) return;
+  const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = 1 + (int)(t / ((size_t)ni * nj));
+  const size_t p = ((size_t)k * g.my + j) * g.mx + i;
+  double m[3][3], f[kC2cFactors];
+  c2c_rows(g, csi, eta, zet, p, m);
+  c2c_minors(m, f);
+#pragma unroll
+  for (int q = 0; q < kC2cFactors; q++) fac[q * n + p] = f[q];
+}
+
+template <bool FAC>
 __global__ void __launch_bounds__(256) k_contra2cart(Geom g, const double *__restrict__ csi,
                                                      const double *__restrict__ eta, const double *__restrict__ zet,
+                                                     const double *__restrict__ fac,
                                                      const double *__restrict__ nvert, const double *__restrict__ uc,
                                                      double *__restrict__ ucat, int k0, int nk) {
   const int ni = g.mx - 2, nj = g.my - 2;
-  const size_t cells = (size_t)ni * nj * nk;
+  const size_t cells = (size_t)ni * nj * nk, n = g.n();
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cells) return;
   const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = k0 + (int)(t / ((size_t)ni * nj));
@@ -51,38 +101,48 @@ __global__ void __launch_bounds__(256) k_contra2cart(Geom g, const double *__res
   const double nv = nvert[p];
   if (!(nv < 0.1 || nv > 7.0)) return;
   const size_t pw = p - 1, ps = p - g.mx, pb = p - (size_t)g.mx * g.my;
-  double m[3][3];
+  double f[kC2cFactors];
+  if (FAC) {
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    m[0][c] = mean2(csi[3 * pw + c], csi[3 * p + c]);
-    m[1][c] = mean2(eta[3 * ps + c], eta[3 * p + c]);
-    m[2][c] = mean2(zet[3 * pb + c], zet[3 * p + c]);
+    for (int q = 0; q < kC2cFactors; q++) f[q] = fac[q * n + p];
+  } else {
+    double m[3][3];
+    c2c_rows(g, csi, eta, zet, p, m);
+    c2c_minors(m, f);
   }
   const double q0 = mean2(uc[3 * pw + 0], uc[3 * p + 0]);
   const double q1 = mean2(uc[3 * ps + 1], uc[3 * p + 1]);
   const double q2 = mean2(uc[3 * pb + 2], uc[3 * p + 2]);
-  const double det = da(ds(cof(m[0][0], m[1][1], m[2][2], m[1][2], m[2][1]),
-                           cof(m[0][1], m[1][0], m[2][2], m[1][2], m[2][0])),
-                        cof(m[0][2], m[1][0], m[2][1], m[1][1], m[2][0]));
-  const double d0 = da(ds(cof(q0, m[1][1], m[2][2], m[1][2], m[2][1]), cof(q1, m[0][1], m[2][2], m[0][2], m[2][1])),
-                       cof(q2, m[0][1], m[1][2], m[0][2], m[1][1]));
-  const double d1 = ds(da(cof(-q0, m[1][0], m[2][2], m[1][2], m[2][0]), cof(q1, m[0][0], m[2][2], m[0][2], m[2][0])),
-                       cof(q2, m[0][0], m[1][2], m[0][2], m[1][0]));
-  const double d2 = da(ds(cof(q0, m[1][0], m[2][1], m[1][1], m[2][0]), cof(q1, m[0][0], m[2][1], m[0][1], m[2][0])),
-                       cof(q2, m[0][0], m[1][1], m[0][1], m[1][0]));
-  ucat[3 * p + 0] = __ddiv_rn(d0, det);
-  ucat[3 * p + 1] = __ddiv_rn(d1, det);
-  ucat[3 * p + 2] = __ddiv_rn(d2, det);
+  // the numerators of Cramer's rule: q times the minors, in the reference's
+  // order (rhs.c:96-118)
+  const double d0 = da(ds(dm(q0, f[0]), dm(q1, f[3])), dm(q2, f[4]));
+  const double d1 = ds(da(dm(-q0, f[1]), dm(q1, f[5])), dm(q2, f[6]));
+  const double d2 = da(ds(dm(q0, f[2]), dm(q1, f[7])), dm(q2, f[8]));
+  ucat[3 * p + 0] = __ddiv_rn(d0, f[9]);
+  ucat[3 * p + 1] = __ddiv_rn(d1, f[9]);
+  ucat[3 * p + 2] = __ddiv_rn(d2, f[9]);
 }
 
 // Interior cells of the planes k0 .. k0 + nk - 1 (all interior planes by
-// default).
+// default); fac: k_c2c_factors' arrays, or null to form the minors here.
 void launch_contra2cart(const Geom &g, const double *csi, const double *eta, const double *zet,
-                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s, int k0, int nk) {
+                        const double *nvert, const double *ucont, double *ucat, cudaStream_t s, int k0, int nk,
+                        const double *fac) {
   if (nk < 0) nk = g.mz - 2;
   const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * nk;
   if (!cells) return;
-  k_contra2cart<<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, nvert, ucont, ucat, k0, nk);
+  if (fac)
+    k_contra2cart<true><<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, fac, nvert, ucont, ucat, k0, nk);
+  else
+    k_contra2cart<false><<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, fac, nvert, ucont, ucat, k0, nk);
+  count_launch();
+}
+
+void launch_c2c_factors(const Geom &g, const double *csi, const double *eta, const double *zet, double *fac,
+                        cudaStream_t s) {
+  const size_t cells = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  if (!cells) return;
+  k_c2c_factors<<<nblk(cells, 256), 256, 0, s>>>(g, csi, eta, zet, fac);
   count_launch();
 }
 
@@ -371,7 +431,7 @@ void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi,
 // once and the edges three times.  With an outlet, a pass changes Ucont.z of
 // the last interior k face only, so Contra2Cart runs on that plane alone in
 // passes two and three.
-void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const double *zet,
+void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const double *zet, const double *fac,
                      const double *nvert, double *ucont, double *ubcs, double *ucat, double *p,
                      const std::function<void()> &outlet_pass, cudaStream_t s) {
   GhostArgs A;
@@ -394,15 +454,15 @@ void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const 
     count_launch();
   };
   if (!outlet_pass) {
-    launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s);
+    launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s, 1, -1, fac);
     faces();
     for (int pass = 0; pass < 3; pass++) edges();
     return;
   }
   for (int pass = 0; pass < 3; pass++) {
     outlet_pass();
-    if (pass == 0) launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s);
-    else launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s, g.mz - 2, 1);
+    if (pass == 0) launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s, 1, -1, fac);
+    else launch_contra2cart(g, csi, eta, zet, nvert, ucont, ucat, s, g.mz - 2, 1, fac);
     faces();
     edges();
   }
