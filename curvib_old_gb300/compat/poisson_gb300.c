@@ -26,12 +26,14 @@ extern PetscInt imp_MAX_IT;             /* main.c: the pseudo-time iteration's c
 extern PetscReal imp_atol, imp_rtol;
 extern PetscInt inletprofile;           /* main.c: InflowFlux's profile */
 extern PetscReal FluxInSum;             /* main.c: InflowFlux's result, as bcs.c:5 declares it */
+extern PetscReal U_bc;                  /* bcs.c:10: the rheology plates' velocity */
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 PetscErrorCode ImpRK(UserCtx *user, IBMNodes *ibm, FSInfo *fsi); /* implicitsolver.c:7094 */
 
 static cvb_ctx *g_cvb = NULL;
 static cvb_solve_opts g_opts;
+static int g_cent_given = 0; /* the cell centres went to the context (an annulus face) */
 
 static PetscErrorCode report(int rc, const char *where) {
   if (rc)
@@ -110,6 +112,7 @@ PetscErrorCode PoissonSetup_GB300(UserMG *usermg) {
   }
   int rc = read_options();
   if (rc) return rc;
+  g_cent_given = 0;
   if (!g_cvb) {
     cvb_options o;
     memset(&o, 0, sizeof o); /* device 0, the context's own stream */
@@ -175,14 +178,28 @@ PetscErrorCode UpdatePressure_GB300(UserCtx *u) {
   return report(rc, "UpdatePressure_GB300");
 }
 
-/* GhostNodeVelocity's boundary types libcvb covers (all but the wall function,
- * the annulus bctype[2] 11 and the rheology plate 13). */
+/* GhostNodeVelocity's boundary types libcvb covers: all but the wall
+ * function.  An annulus face (bctype[2] 11) reads the cell centres and a
+ * rheology plate (13) the velocity U_bc; ghost_inputs hands them over (the
+ * centres once per set-up). */
 static int ghost_on_device(const UserCtx *u) {
-  if (wallfunction) return 0;
-  if (u->bctype[2] == 11) return 0;
+  (void)u;
+  return !wallfunction;
+}
+
+static int ghost_inputs(UserCtx *u) {
+  int rc = 0;
+  if (u->bctype[2] == 11 && !g_cent_given) {
+    PetscScalar *cent;
+    VecGetArray(u->Cent, &cent);
+    rc = cvb_set_cell_centres(g_cvb, cent);
+    VecRestoreArray(u->Cent, &cent);
+    if (rc) return rc;
+    g_cent_given = 1;
+  }
   for (int f = 2; f < 6; f++)
-    if (u->bctype[f] == 13) return 0;
-  return 1;
+    if (u->bctype[f] == 13) return cvb_set_plate_velocity(g_cvb, U_bc);
+  return 0;
 }
 
 /* Projection (poisson.c:2281-2904): the flux correction, lUcont refreshed,
@@ -198,6 +215,12 @@ PetscErrorCode Projection_GB300(UserCtx *u) {
   VecGetArray(u->Ucont, &uc);
   if (ghost_on_device(u)) {
     PetscScalar *ub, *ucat;
+    rc = ghost_inputs(u);
+    if (rc) {
+      VecRestoreArray(u->Ucont, &uc);
+      VecRestoreArray(u->Phi, &phi);
+      return report(rc, "Projection_GB300");
+    }
     VecGetArray(u->Bcs.Ubcs, &ub);
     VecGetArray(u->Ucat, &ucat);
     rc = cvb_projection_cart(g_cvb, phi, u->dt, u->st, uc, ub, ucat);

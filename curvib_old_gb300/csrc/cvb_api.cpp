@@ -1553,14 +1553,15 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
   return CVB_OK;
 }
 
-// The boundary types GhostNodeVelocity is restated for: all but the annulus
-// (bctype[2] 11, which reads cell centres), the rheology plate (13 on faces
-// 2-5, which reads a global of the caller's main program), and periodic
-// faces without a periodic opposite.
+// The boundary types GhostNodeVelocity is restated for: all but an annulus
+// face (bctype[2] 11) before the cell centres it reads were given
+// (cvb_set_cell_centres), and periodic faces without a periodic opposite.  The
+// rheology plates (13 on faces 2-5) take the velocity of
+// cvb_set_plate_velocity (0 until set, as the reference's global starts).
 static int ghost_types_ok(cvb_ctx *ctx, const int *bc) {
-  if (bc[2] == 11) return fail(ctx, CVB_BAD_INPUT, "GhostNodeVelocity: bctype 11 (annulus) is not covered");
-  for (int f = 2; f < 6; f++)
-    if (bc[f] == 13) return fail(ctx, CVB_BAD_INPUT, "GhostNodeVelocity: bctype 13 (rheology) is not covered");
+  if (bc[2] == 11 && !ctx->ibm_cent)
+    return fail(ctx, CVB_BAD_INPUT,
+                "GhostNodeVelocity: an annulus face (bctype 11) needs the cell centres (cvb_set_cell_centres)");
   for (int d = 0; d < 3; d++)
     if ((bc[2 * d] == 7) != (bc[2 * d + 1] == 7))
       return fail(ctx, CVB_BAD_INPUT, "GhostNodeVelocity: periodic face %d without a periodic opposite", 2 * d);
@@ -1591,6 +1592,23 @@ int cvb_contra2cart(cvb_ctx *ctx, const double *ucont, double *ucat) {
   return CVB_OK;
 }
 
+int cvb_set_cell_centres(cvb_ctx *ctx, const double *cent) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!cent) return fail(ctx, CVB_BAD_INPUT, "cent is NULL");
+  const size_t n = ctx->L[ctx->nlevels - 1].g.n();
+  if (!ctx->ibm_cent) TRY(dalloc(ctx, &ctx->ibm_cent, 3 * n));
+  CK(cudaMemcpyAsync(ctx->ibm_cent, cent, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CVB_OK;
+}
+
+int cvb_set_plate_velocity(cvb_ctx *ctx, double u_bc) {
+  if (!ctx) return CVB_BAD_INPUT;
+  ctx->u_bc = u_bc;
+  return CVB_OK;
+}
+
 int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat) {
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
@@ -1602,7 +1620,8 @@ int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat) {
   TRY(post_buffers(ctx, n));
   CK(cudaMemcpyAsync(ctx->ubcs_dev, ubcs, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->ucat_dev, ucat, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
-  launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream);
+  launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream,
+                             ctx->ibm_cent, ctx->u_bc);
   CKL();
   CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ucat, ctx->ucat_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1630,7 +1649,8 @@ int cvb_projection_cart(cvb_ctx *ctx, const double *phi, double dt, double st, d
   launch_projection(F.g, fm, ctx->iaj[l], ctx->jaj[l], ctx->kaj[l], F.nvert, ctx->w, dt, st, ctx->uc_dev, ctx->stream);
   launch_contra2cart(F.g, ctx->cm[0], ctx->cm[1], ctx->cm[2], F.nvert, ctx->uc_dev, ctx->ucat_dev, ctx->stream, 1,
                      -1, ctx->geo->c2c);
-  launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream);
+  launch_ghost_node_velocity(F.g, bc, ctx->cm[0], ctx->cm[1], ctx->cm[2], ctx->ubcs_dev, ctx->ucat_dev, ctx->stream,
+                             ctx->ibm_cent, ctx->u_bc);
   CKL();
   CK(cudaMemcpyAsync(ucont, ctx->uc_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(ubcs, ctx->ubcs_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));

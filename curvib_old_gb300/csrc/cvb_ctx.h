@@ -100,6 +100,7 @@ struct cvb_ctx {
   unsigned long long *imp_norms = nullptr; // ImpRK: |Rhs| and |dU| as bit patterns
   double *bc_scratch = nullptr;            // InflowFlux / outlet: plane terms (device)
   double *bc_host = nullptr;               // the same terms, pinned host memory, for the host's ordered sums
+  double u_bc = 0.;                        // GhostNodeVelocity: the rheology plates' velocity (bcs.c's U_bc)
   double *ibm_cent = nullptr;  // cell centres of the last cvb_ibm_search that gave them
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ready = false;

@@ -319,9 +319,12 @@ void launch_form_function1(const Geom &g, const double *nvert, const double *p, 
                            const double *kaj, const double *gram, double *rct, double *rhs, cudaStream_t s);
 void launch_calc_rhs(const Geom &g, const double *nvert, const double *ucont, const double *ucont_o,
                      const double *ucont_rm1, int bdf2, double neg_inv_dt, int mz_end, double *rhs, cudaStream_t s);
-// bc: the level's bctype[6]; the host has refused the types it does not cover
+// bc: the level's bctype[6]; the host has refused the types it does not cover.
+// cent: the cell centres ([N][3]) an annulus face needs; u_bc: the rheology
+// plates' velocity
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
-                                const double *zet, double *ubcs, double *ucat, cudaStream_t s);
+                                const double *zet, double *ubcs, double *ucat, cudaStream_t s,
+                                const double *cent = nullptr, double u_bc = 0.);
 // FormBCS with walls on the x and y faces: its three passes of the outlet's
 // flux correction (outlet_pass, empty for a walled k = mz - 1 face; it
 // launches on s), Contra2Cart, the ghost faces' interior cells and the 12

@@ -274,6 +274,8 @@ struct GhostArgs {
   const double *csi, *eta, *zet;  // centre metrics
   double *ub, *u;                 // ubcs, ucat
   double *p = nullptr;            // FormBCS: the pressure, averaged on the edges with ucat
+  const double *cent = nullptr;   // the cell centres (an annulus face)
+  double u_bc = 0.;               // the rheology plates' velocity (bcs.c's U_bc)
 };
 
 // The boundary velocity of the special wall types (bcs.c:3776-3975), one face
@@ -293,6 +295,24 @@ __global__ void k_ghost_special(GhostArgs A) {
   double *ub = A.ub + 3 * p0;
   if (f == 5 && A.bc[5] == 2) { ub[0] = 0.; ub[1] = 1.; ub[2] = 0.; return; }
   if (f == 3 && A.bc[3] == 12) { ub[0] = 0.; ub[1] = 0.; ub[2] = 1.; return; }
+  // annulus (bcs.c:3811-3826): (y, -x, 0) / |(x, y)| of the cell centre above
+  if (f == 2 && A.bc[2] == 11) {
+    const double *c = A.cent + 3 * F.at(g, a, b, 1);
+    const double r = __dsqrt_rn(da(dm(c[0], c[0]), dm(c[1], c[1])));
+    ub[0] = __ddiv_rn(c[1], r);
+    ub[1] = __ddiv_rn(-c[0], r);
+    ub[2] = 0.0;
+    return;
+  }
+  // rheology plates (bcs.c:3963-4010): the plate velocity along z on the y
+  // faces, along x on the z faces
+  if (f >= 2 && A.bc[f] == 13) {
+    const double v = (f & 1) ? A.u_bc : -A.u_bc;
+    ub[0] = f >= 4 ? v : 0.;
+    ub[1] = 0.;
+    ub[2] = f >= 4 ? 0. : v;
+    return;
+  }
   if (A.bc[f] != 3) return;
   const double *met = F.axis == 0 ? A.csi : F.axis == 1 ? A.eta : A.zet;
   const size_t pm = F.side ? F.at(g, a, b, 1) : p0;
@@ -383,14 +403,17 @@ static void face_grid(const Geom &g, int axis, int faces, dim3 &grd, dim3 &blk) 
 }
 
 void launch_ghost_node_velocity(const Geom &g, const int *bc, const double *csi, const double *eta,
-                                const double *zet, double *ubcs, double *ucat, cudaStream_t s) {
+                                const double *zet, double *ubcs, double *ucat, cudaStream_t s, const double *cent,
+                                double u_bc) {
   GhostArgs A;
   A.g = g;
   for (int f = 0; f < 6; f++) A.bc[f] = bc[f];
   A.csi = csi; A.eta = eta; A.zet = zet; A.ub = ubcs; A.u = ucat;
+  A.cent = cent;
+  A.u_bc = u_bc;
   dim3 grd, blk;
-  bool special = bc[5] == 2 || bc[3] == 12;
-  for (int f = 0; f < 6; f++) special = special || bc[f] == 3;
+  bool special = bc[5] == 2 || bc[3] == 12 || bc[2] == 11;
+  for (int f = 0; f < 6; f++) special = special || bc[f] == 3 || (f >= 2 && bc[f] == 13);
   if (special) {
     const int nmax = g.mx > g.my ? (g.mx > g.mz ? g.mx : g.mz) : (g.my > g.mz ? g.my : g.mz);
     k_ghost_special<<<dim3(nblk(nmax, 32), nblk(nmax, 8), 6), dim3(32, 8, 1), 0, s>>>(A);

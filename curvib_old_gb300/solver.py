@@ -233,6 +233,14 @@ class PoissonContext:
                                          float(dt), int(ti), int(tistart), int(central), ptr(out)))
         return out, u
 
+    def set_cell_centres(self, cent):
+        """The finest level's cell centres, for an annulus face (bctype[2] 11)."""
+        self._check(self._L.cvb_set_cell_centres(self._ctx, ptr(_c64(cent))))
+
+    def set_plate_velocity(self, u_bc):
+        """The rheology plates' velocity (bctype 13), bcs.c's U_bc."""
+        self._check(self._L.cvb_set_plate_velocity(self._ctx, float(u_bc)))
+
     def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0):
         """InflowFlux (bcs.c:99): (ucont, ubcs, FluxInSum)."""
         uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]

@@ -188,11 +188,21 @@ int cvb_projection(cvb_ctx *ctx, const double *phi, double dt, double st, double
 int cvb_contra2cart(cvb_ctx *ctx, const double *ucont, double *ucat);
 /* GhostNodeVelocity (bcs.c:3645-4435), Projection's last call (poisson.c:2904),
  * without the wall function: boundary velocities of slip (3), moving-lid
- * (bctype[5] 2) and O-grid (bctype[3] 12) faces into ubcs (Bcs.Ubcs), the ring
- * of ucat from ubcs and the periodic images, the box's edges.  ubcs and ucat
+ * (bctype[5] 2), O-grid (bctype[3] 12), annulus (bctype[2] 11: from the cell
+ * centres of cvb_set_cell_centres) and rheology-plate (13 on faces 2-5: the
+ * velocity of cvb_set_plate_velocity) faces into ubcs (Bcs.Ubcs), the ring of
+ * ucat from ubcs and the periodic images, the box's edges.  ubcs and ucat
  * ([mz][my][mx][3]) are read and written.  CVB_BAD_INPUT, with nothing
- * written, for bctype 11 or 13, or a periodic face whose opposite is not. */
+ * written, for an annulus face before the centres were given, or a periodic
+ * face whose opposite is not. */
 int cvb_ghost_node_velocity(cvb_ctx *ctx, double *ubcs, double *ucat);
+/* The finest level's cell centres (FormMetrics' Cent, [mz][my][mx][3]) for an
+ * annulus face's boundary velocity (bcs.c:3811-3826); they stay on the device
+ * and are also the centres cvb_ibm_search reuses when given none. */
+int cvb_set_cell_centres(cvb_ctx *ctx, const double *cent);
+/* The rheology plates' velocity, bcs.c's global U_bc (-U_bc option), for
+ * faces of bctype 13 (bcs.c:3963-4010); 0 until set, as the global starts. */
+int cvb_set_plate_velocity(cvb_ctx *ctx, double u_bc);
 /* Projection as Flow_Solver calls it (solvers.c:1068, poisson.c:2281-2904):
  * the flux correction, Contra2Cart and GhostNodeVelocity on the device in one
  * call, each array copied in and out once. */

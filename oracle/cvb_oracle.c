@@ -647,12 +647,14 @@ static inline void avg3(double *d, const double *a, const double *b) {
 }
 
 int orc_ghost_node_velocity(const orc_level *L, double *ub, double *u) {
+  return orc_ghost_node_velocity_ext(L, ub, u, NULL, 0.0);
+}
+
+int orc_ghost_node_velocity_ext(const orc_level *L, double *ub, double *u, const double *cent, double u_bc) {
   const int mx = L->mx, my = L->my, mz = L->mz;
   const int *bc = L->bctype;
   const int IM = mx - 1, JM = my - 1, KM = mz - 1;
-  if (bc[2] == 11) return -1;
-  for (int f = 2; f < 6; f++)
-    if (bc[f] == 13) return -1;
+  if (bc[2] == 11 && !cent) return -1;
   for (int d = 0; d < 3; d++)
     if ((bc[2 * d] == 7) != (bc[2 * d + 1] == 7)) return -1;
 #define U3(i, j, k) (u + 3 * ID(L, (i), (j), (k)))
@@ -670,6 +672,17 @@ int orc_ghost_node_velocity(const orc_level *L, double *ub, double *u) {
       for (int i = 1; i < mx - 1; i++) {
         double *b = B3(i, my - 1, k);
         b[0] = 0.; b[1] = 0.; b[2] = 1.;
+      }
+  /* annulus (bctype[2] 11, bcs.c:3811-3825): the tangential unit vector of the
+   * cell centre above the face, (y, -x, 0) / |(x, y)| */
+  if (bc[2] == 11)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) {
+        const double *c = cent + 3 * ID(L, i, 1, k);
+        double *b = B3(i, 0, k);
+        b[0] = c[1] / sqrt(c[0] * c[0] + c[1] * c[1]);
+        b[1] = -c[0] / sqrt(c[0] * c[0] + c[1] * c[1]);
+        b[2] = 0.0;
       }
   if (bc[0] == 3)
     for (int k = 1; k < mz - 1; k++)
@@ -693,6 +706,31 @@ int orc_ghost_node_velocity(const orc_level *L, double *ub, double *u) {
     for (int j = 1; j < my - 1; j++)
       for (int i = 1; i < mx - 1; i++)
         slip(L->zet + 3 * ID(L, i, j, mz - 2), U3(i, j, mz - 2), B3(i, j, mz - 1));
+  /* rheology plates (bctype 13, bcs.c:3963-4010): the plate velocity U_bc */
+  if (bc[2] == 13)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) {
+        double *b = B3(i, 0, k);
+        b[0] = 0.; b[1] = 0.; b[2] = -u_bc;
+      }
+  if (bc[3] == 13)
+    for (int k = 1; k < mz - 1; k++)
+      for (int i = 1; i < mx - 1; i++) {
+        double *b = B3(i, my - 1, k);
+        b[0] = 0.; b[1] = 0.; b[2] = u_bc;
+      }
+  if (bc[4] == 13)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double *b = B3(i, j, 0);
+        b[0] = -u_bc; b[1] = 0.; b[2] = 0.;
+      }
+  if (bc[5] == 13)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double *b = B3(i, j, mz - 1);
+        b[0] = u_bc; b[1] = 0.; b[2] = 0.;
+      }
   /* non-periodic ghost faces, whole faces, x then y then z (bcs.c:4015-4076) */
   if (bc[0] != 7)
     for (int k = 0; k < mz; k++)

@@ -65,8 +65,13 @@ void orc_contra2cart(const orc_level *L, const double *ucont, double *ucat);
  * faces into ubcs; every non-periodic ghost face from 2 ubcs - inner; the
  * periodic ring copies; the averages on the box's 12 edges; the second round
  * of ring copies.  Returns 0, or -1 (nothing written) for what it does not
- * restate: bctype 11 or 13, or a periodic face whose opposite is not. */
+ * restate: bctype 11 without the cell centres, or a periodic face whose
+ * opposite is not; rheology faces (13) take a plate velocity of 0. */
 int orc_ghost_node_velocity(const orc_level *L, double *ubcs, double *ucat);
+/* The same with the annulus face (bctype[2] 11: ubcs from the cell centres
+ * cent, [mz][my][mx][3], of the first interior row) and the rheology plates
+ * (bctype 13 on faces 2-5: the plate velocity u_bc, bcs.c's U_bc). */
+int orc_ghost_node_velocity_ext(const orc_level *L, double *ubcs, double *ucat, const double *cent, double u_bc);
 /* The nvert classification of ibm_search_advanced (ibm.c:4197-4740) for body
  * ibi of nbodies, a closed triangle mesh (xyz: n_v nodes; tri: n_elmt node
  * triples; nf: their unit normals): each interior cell centre (cent,

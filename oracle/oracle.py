@@ -109,6 +109,8 @@ def lib():
         _lib.orc_contra2cart.argtypes = [L, P, P]
         _lib.orc_ghost_node_velocity.argtypes = [L, P, P]
         _lib.orc_ghost_node_velocity.restype = ctypes.c_int
+        _lib.orc_ghost_node_velocity_ext.argtypes = [L, P, P, P, ctypes.c_double]
+        _lib.orc_ghost_node_velocity_ext.restype = ctypes.c_int
         _lib.orc_ibm_search.argtypes = [ctypes.c_int] * 3 + [P, ctypes.c_int, P, ctypes.c_int, P, P] + \
             [ctypes.c_int] * 2 + [P, P, ctypes.c_int]
         _lib.orc_ibm_search.restype = ctypes.c_int
@@ -244,11 +246,17 @@ def contra2cart(L: OLevel, ucont, ucat):
     return out
 
 
-def ghost_node_velocity(L: OLevel, ubcs, ucat):
-    """GhostNodeVelocity (bcs.c:3645-4435): returns (status, ubcs, ucat)."""
+def ghost_node_velocity(L: OLevel, ubcs, ucat, cent=None, u_bc=0.0):
+    """GhostNodeVelocity (bcs.c:3645-4435): returns (status, ubcs, ucat).
+    cent: the cell centres an annulus face (bctype[2] 11) needs; u_bc: the
+    rheology plates' velocity (bctype 13)."""
     ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
     u = np.array(ucat, dtype=np.float64, copy=True, order="C")
-    rc = lib().orc_ghost_node_velocity(L.ref(), _p(ub), _p(u))
+    if cent is None:
+        rc = lib().orc_ghost_node_velocity_ext(L.ref(), _p(ub), _p(u), None, float(u_bc))
+    else:
+        c = np.ascontiguousarray(cent, dtype=np.float64)
+        rc = lib().orc_ghost_node_velocity_ext(L.ref(), _p(ub), _p(u), _p(c), float(u_bc))
     return rc, ub, u
 
 
@@ -478,9 +486,12 @@ class Reference:
         self.L.ref_contra2cart(_p(uc), _p(out))
         return out
 
-    def ghost_node_velocity(self, ubcs, ucat):
+    def ghost_node_velocity(self, ubcs, ucat, u_bc=0.0):
+        """The reference's own GhostNodeVelocity; u_bc is bcs.c's U_bc (the
+        rheology plates' velocity), the cell centres its FormMetrics' Cent."""
         ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
         u = np.array(ucat, dtype=np.float64, copy=True, order="C")
+        self.L.ref_set_u_bc(ctypes.c_double(u_bc))
         self.L.ref_ghost_node_velocity(_p(ub), _p(u))
         return ub, u
 

@@ -425,6 +425,10 @@ int ref_contra2cart(const double *ucont, double *ucat) {
   return 0;
 }
 
+/* The rheology plates' velocity (bcs.c's global U_bc) for GhostNodeVelocity. */
+extern PetscReal U_bc;
+void ref_set_u_bc(double v) { U_bc = v; }
+
 /* GhostNodeVelocity (bcs.c:3645-4435) on the finest level: ubcs (Bcs.Ubcs) and
  * ucat (Ucat), global boxes, both read and written. */
 int ref_ghost_node_velocity(double *ubcs, double *ucat) {

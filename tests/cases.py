@@ -26,7 +26,12 @@ POST_VARIANTS = {
     "slip_lid_ogrid": ("box_sphere", [3, 3, 1, 12, 3, 2], [(2, 3, 4), (2, 3, 5), (9, 8, 2)], 1),
     "walls_slip_y": ("box_sphere", [1, 1, 3, 3, 1, 1], [(5, 5, 5)], 2),
     "periodic_slip_y": ("channel_periodic", [7, 7, 3, 3, 7, 7], [(3, 4, 6)], 3),
+    # an annulus face (bctype[2] 11, its ubcs from the cell centres) and the
+    # rheology plates (bctype 13, the plate velocity POST_U_BC)
+    "annulus_y": ("box_sphere", [1, 1, 11, 1, 1, 1], [(5, 5, 5)], 4),
+    "rheology_plates": ("box_sphere", [1, 1, 13, 13, 13, 13], [(6, 4, 5)], 5),
 }
+POST_U_BC = 0.37
 
 
 # Immersed-body searches (ibm_search_advanced): name -> (scenario whose grid is

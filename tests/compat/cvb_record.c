@@ -107,6 +107,17 @@ int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int ce
   conv[3 * REC.mark] = 7.0;
   return take_status();
 }
+int cvb_set_cell_centres(cvb_ctx *ctx, const double *cent) {
+  (void)ctx;
+  REC.n_set_cent++;
+  REC.cent = cent;
+  return CVB_OK;
+}
+int cvb_set_plate_velocity(cvb_ctx *ctx, double u_bc) {
+  (void)ctx;
+  REC.u_bc = u_bc;
+  return CVB_OK;
+}
 void cvb_imp_rk_opts_default(cvb_imp_rk_opts *o) {
   memset(o, 0, sizeof *o);
   o->ren = o->dt = o->st = 1.;

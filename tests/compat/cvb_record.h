@@ -14,7 +14,9 @@
 
 typedef struct {
   int n_init, n_destroy, n_last_error, n_setup, n_set_nvert, n_solver_mg, n_update, n_projection,
-      n_projection_cart, n_convection, central_conv, n_imp_rk;
+      n_projection_cart, n_convection, central_conv, n_imp_rk, n_set_cent;
+  const double *cent;
+  double u_bc;
   int ntok;
   char tok[REC_MAXTOK][64];
   int nlevels;

@@ -19,7 +19,7 @@
 
 extern PetscInt block_number, immersed, wallfunction, les;
 extern PetscInt ti, tistart, imp_MAX_IT;
-extern PetscReal imp_atol, imp_rtol, FluxInSum;
+extern PetscReal imp_atol, imp_rtol, FluxInSum, U_bc;
 extern PetscInt inletprofile;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
@@ -137,14 +137,24 @@ int main(void) {
   CHECK(shim_vec_data(fine->lUcont)[3 * loc] == 5.0, "lUcont not refreshed after the projection");
   CHECK(shim_vec_data(fine->lUcat)[3 * loc + 2] == 9.0, "lUcat not refreshed after the projection");
   CHECK(shim_arrays_out() == 0, "projection left %d arrays out", shim_arrays_out());
-  /* uncovered types (annulus face, wall function): flux correction on the
-   * device, the reference's own Contra2Cart / GhostNodeVelocity on the host */
+  /* an annulus face: its cell centres (Cent's storage) go to the context once,
+   * then the one-call projection; a rheology plate: U_bc goes with it */
   fine->bctype[2] = 11;
-  CHECK(Projection_GB300(fine) == 0 && REC.n_projection == 1 && REC.n_projection_cart == 1,
-        "annulus face: host post-projection not used");
+  CHECK(Projection_GB300(fine) == 0 && REC.n_projection_cart == 2 && REC.n_set_cent == 1 &&
+            REC.cent == shim_vec_data(fine->Cent),
+        "annulus face: centres not given or projection not on the device");
+  CHECK(Projection_GB300(fine) == 0 && REC.n_projection_cart == 3 && REC.n_set_cent == 1,
+        "annulus face: centres given again");
   fine->bctype[2] = 1;
+  fine->bctype[4] = 13;
+  U_bc = 0.625;
+  CHECK(Projection_GB300(fine) == 0 && REC.n_projection_cart == 4 && REC.u_bc == 0.625,
+        "rheology plate: U_bc not passed");
+  fine->bctype[4] = 1;
+  /* the wall function: flux correction on the device, the reference's own
+   * Contra2Cart / GhostNodeVelocity on the host */
   wallfunction = 1;
-  CHECK(Projection_GB300(fine) == 0 && REC.n_projection == 2 && REC.n_projection_cart == 1,
+  CHECK(Projection_GB300(fine) == 0 && REC.n_projection == 1 && REC.n_projection_cart == 4,
         "wall function: host post-projection not used");
   wallfunction = 0;
   CHECK(shim_arrays_out() == 0, "host-path projections left %d arrays out", shim_arrays_out());

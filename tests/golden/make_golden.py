@@ -33,7 +33,7 @@ sys.path.insert(0, str(ROOT / "tests"))
 from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_OUTLET_SCENARIOS, INLET_PROFILES,  # noqa: E402
                    MOM_DT, MOM_REN,
                    conv_seam_nvert, imp_rk_inputs, mom_edge_nvert, momentum_inputs)
-from cases import (IBM_CASES, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
+from cases import (IBM_CASES, POST_U_BC, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
 from curvib_old_gb300 import workload as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
@@ -181,14 +181,14 @@ def inlet_outlet(c):
     return out
 
 
-def post(R, nvert, ucont, seed):
+def post(R, nvert, ucont, seed, u_bc=0.0):
     """Contra2Cart, then GhostNodeVelocity on its result.  A slip face on the
     low y side takes its normal from eta of the ring cell, which FormMetrics
     leaves zero: the reference's values there are NaN (0/0)."""
     ucat0, ubcs0 = post_inputs(nvert.shape, seed)
     R.set_nvert(R.nlevels - 1, nvert)
     c2c = R.contra2cart(ucont, ucat0)
-    ub, u = R.ghost_node_velocity(ubcs0, c2c)
+    ub, u = R.ghost_node_velocity(ubcs0, c2c, u_bc)
     return {"contra2cart": digest_nan(c2c), "ghost_ubcs": digest_nan(ub), "ghost_ucat": digest_nan(u)}
 
 
@@ -199,7 +199,7 @@ def run_variant(vname):
     for (k, j, i) in blank:
         nv[k, j, i] = 8.0
     R = O.Reference(c["nodes"], c["nl"], bct, c["semi"])
-    return post(R, nv, c["ucont"], seed)
+    return post(R, nv, c["ucont"], seed, POST_U_BC)
 
 
 def run_ibm(name, meshes_out):
