@@ -1775,10 +1775,9 @@ int cvb_viscous(cvb_ctx *ctx, const double *ucat, double ren, double *visc) {
   if (!ctx) return CVB_BAD_INPUT;
   if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
   if (!visc || !(ren != 0.0)) return fail(ctx, CVB_BAD_INPUT, "Viscous: visc is NULL or ren is 0");
+  // periodic boxes too: Viscous reads only the box, whose ring holds the
+  // periodic images (rhs.c:2062-2490)
   const int l = ctx->nlevels - 1;
-  const int *bc = ctx->H[l].d.bctype;
-  for (int f = 0; f < 6; f++)
-    if (bc[f] == 7) return fail(ctx, CVB_BAD_INPUT, "Viscous: periodic faces (bctype 7) are not covered");
   if (!ucat && !ctx->ucat_dev) return fail(ctx, CVB_BAD_INPUT, "Viscous: ucat is NULL and no projection has left Ucat on the device");
   LevelDev &F = ctx->L[l];
   const size_t n = F.g.n();

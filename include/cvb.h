@@ -237,8 +237,9 @@ int cvb_metrics_divergence(cvb_ctx *ctx, double *maxdiv, long long *at);
  * m - 3 for index -1, cell 2 for index m) and take the full QUICK form where
  * both sides are fluid, as the reference does (rhs.c:1546-1620). */
 int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int central, double *conv);
-/* The momentum right-hand side on the finest level, for boxes with no periodic
- * face (bctype 7 is refused with CVB_BAD_INPUT).  Vector fields are
+/* The momentum right-hand side on the finest level: Viscous for any box,
+ * FormFunction1 and CalcRHS for boxes with no periodic face (bctype 7 is
+ * refused there with CVB_BAD_INPUT).  Vector fields are
  * [mz][my][mx][3], p is [mz][my][mx]; nvert is the context's (the last
  * cvb_setup_hierarchy or cvb_set_nvert); ucont / ucat NULL use the device copies
  * the last projection left.  Results equal the reference's bit for bit.
@@ -246,7 +247,8 @@ int cvb_convection(cvb_ctx *ctx, const double *ucont, const double *ucat, int ce
  * Viscous (rhs.c:1947-2566), laminar (no LES / RANS model): at every interior
  * cell the sum over its faces of the viscous flux nu (G grad ucat), nu =
  * 1 / ren, with the reference's one-sided derivatives next to cells of nvert
- * in (0.5, 7); 0 on the ring. */
+ * in (0.5, 7); 0 on the ring.  It reads the box alone, so on a periodic box
+ * ucat's ring must hold the periodic images (as GhostNodeVelocity leaves it). */
 int cvb_viscous(cvb_ctx *ctx, const double *ucat, double ren, double *visc);
 /* FormFunction1 (rhs.c:2567-3351): Contra2Cart (ucat's interior cells from
  * ucont; ucat is written back), Convection (QUICK, or central with central !=

@@ -117,13 +117,16 @@ def convection(R, nvert, ucont, bctype):
 
 def momentum(R, nvert, ucont, bctype):
     """Viscous, FormFunction1 (QUICK and central) and CalcRHS (first step and
-    second-order backward) on cases.momentum_inputs; None for a box with a
-    periodic face (not covered)."""
-    if 7 in list(bctype):
-        return None
+    second-order backward) on cases.momentum_inputs; Viscous alone for a box
+    with a periodic face."""
     R.set_nvert(R.nlevels - 1, nvert)
     ucat0, p, uo, urm = momentum_inputs(nvert.shape)
     out = {"viscous": digest(R.viscous(ucat0, MOM_REN))}
+    if 7 in list(bctype):
+        # Viscous reads only the box (its ring holds the periodic images);
+        # FormFunction1 and CalcRHS have periodic seam branches not restated
+        out["periodic"] = True
+        return out
     for central in (0, 1):
         f, u = R.form_function1(ucont, ucat0, p, MOM_REN, central)
         out[f"ff1_{central}"] = digest(f)

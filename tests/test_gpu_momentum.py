@@ -58,12 +58,18 @@ def test_momentum_rhs_matches_oracle(name, variant):
         ctx.close()
 
 
-def test_momentum_rhs_refuses_periodic_boxes():
+@pytest.mark.parametrize("name", ["channel_periodic", "triply_periodic"])
+def test_periodic_boxes_viscous_and_refusals(name):
+    """On periodic boxes Viscous (which reads the box alone) matches the oracle
+    bit for bit; FormFunction1 and CalcRHS, whose periodic seam branches are
+    not restated, are refused."""
     from curvib_old_gb300._lib import CVB_BAD_INPUT, CvbError
-    c = build("channel_periodic")
+    c = build(name)
     ctx = _ctx(c, c["nvert"], c["bctype"])
     try:
+        L = O.OLevel(c["metrics"][-1], c["nvert"], c["bctype"], c["semi"])
         ucat0, p, _, _ = momentum_inputs(c["nvert"].shape)
+        assert _same(ctx.viscous(ucat0, MOM_REN), O.viscous(L, ucat0, MOM_REN))
         with pytest.raises(CvbError) as e:
             ctx.form_function1(c["ucont"], ucat0, p, MOM_REN)
         assert e.value.status == CVB_BAD_INPUT
