@@ -27,6 +27,7 @@ extern PetscReal imp_atol, imp_rtol;
 extern PetscInt inletprofile;           /* main.c: InflowFlux's profile */
 extern PetscReal FluxInSum;             /* main.c: InflowFlux's result, as bcs.c:5 declares it */
 extern PetscReal U_bc;                  /* bcs.c:10: the rheology plates' velocity */
+extern PetscReal CMx_c, CMy_c, CMz_c;   /* main.c: the centre the shaped inlet profiles take from the nodes */
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 PetscErrorCode ImpRK(UserCtx *user, IBMNodes *ibm, FSInfo *fsi); /* implicitsolver.c:7094 */
@@ -316,22 +317,51 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
 
 /* ImpRK (implicitsolver.c:7094-7257) with the reference's arguments.  On one
  * block with no immersed body, no LES / RANS / wall model, solid walls on the
- * x and y faces and on the k faces walls or an inlet (5, a constant profile)
- * with an outlet (4), the whole pseudo-time iteration runs on the device
+ * x and y faces and on the k faces walls or an inlet (5, profile 1, -1, 11, 2,
+ * 4 or 7) with an outlet (4), the whole pseudo-time iteration runs on the device
  * (cvb_imp_rk: InflowFlux, FormBCS, CalcRHS, the Runge-Kutta stage updates,
  * the norms and the step halving), with the reference's -cfl, -imp_atol,
  * -imp_rtol, -imp_MAX_IT, -inlet (inletprofile) and -central and the block's
  * FluxIntpSum; Ucont, Bcs.Ubcs, Ucat and P come back and the local copies
  * are refreshed, as the reference leaves them.  Any other configuration runs
  * the reference's own ImpRK. */
+/* The shaped inlet profiles read the k = 0 node plane of the local
+ * coordinates (bcs.c:130-160) and CMx_c, CMy_c, CMz_c: copied out of the
+ * ghosted local array and handed over before every ImpRK (the centre may
+ * move). */
+static int inlet_nodes(UserCtx *u) {
+  const DMDALocalInfo *f = &u->info;
+  const int mx = f->mx, my = f->my;
+  double *plane = malloc(sizeof(double) * 3 * (size_t)mx * my);
+  if (!plane) return CVB_OOM;
+  Vec Coor;
+  PetscScalar *c;
+  DMGetCoordinatesLocal(u->da, &Coor);
+  VecGetArray(Coor, &c);
+  for (int j = 0; j < my; j++)
+    for (int i = 0; i < mx; i++) {
+      const size_t l = 3 * (((size_t)(0 - f->gzs) * f->gym + (j - f->gys)) * f->gxm + (i - f->gxs));
+      for (int d = 0; d < 3; d++) plane[3 * ((size_t)j * mx + i) + d] = c[l + d];
+    }
+  VecRestoreArray(Coor, &c);
+  const int rc = cvb_set_inlet_nodes(g_cvb, plane, CMx_c, CMy_c, CMz_c);
+  free(plane);
+  return rc;
+}
+
 PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
   const PetscInt *bt = u->bctype;
   int covered = bt[0] == 1 && bt[1] == 1 && bt[2] == 1 && bt[3] == 1 && (bt[4] == 1 || bt[4] == 5) &&
                 (bt[5] == 1 || bt[5] == 4) && ((bt[4] == 5) == (bt[5] == 4));
-  if (bt[4] == 5) covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11);
+  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7;
+  if (bt[4] == 5) covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11 || shaped);
   if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !covered || !u->Ucont_o ||
       !u->Ucont_rm1)
     return ImpRK(u, ibm, fsi);
+  if (bt[4] == 5 && shaped) {
+    const int rc = inlet_nodes(u);
+    if (rc) return report(rc, "ImpRK_GB300");
+  }
   PetscInt central = 0;
   PetscOptionsGetInt(PETSC_NULL, "-central", &central, PETSC_NULL);
   PetscScalar *uc, *uo, *urm, *ucat, *p, *ub;

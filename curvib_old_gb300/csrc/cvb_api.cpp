@@ -1842,14 +1842,42 @@ static int bc_covered(cvb_ctx *ctx, const char *who) {
   return CVB_OK;
 }
 
-// InflowFlux's constant profiles (bcs.c:161-200).
-static int inlet_speed(cvb_ctx *ctx, int profile, double *uin) {
-  if (profile == 1) *uin = 2.;
-  else if (profile == -1) *uin = -1.;
-  else if (profile == 11) *uin = 0.185;
-  else
-    return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d is not covered (constant profiles 1, -1, 11 are)",
+// InflowFlux's profiles (bcs.c:152-200): the constant ones (1, -1, 11) and
+// the shaped ones (2, 4, 7), which need the k = 0 node plane
+// (cvb_set_inlet_nodes).
+struct InletProfile {
+  double uin = 0.;
+  int profile = 0;
+  bool shaped = false;
+};
+static int inlet_speed(cvb_ctx *ctx, int profile, InletProfile *ip) {
+  ip->profile = profile;
+  ip->shaped = profile == 2 || profile == 4 || profile == 7;
+  if (profile == 1) ip->uin = 2.;
+  else if (profile == -1) ip->uin = -1.;
+  else if (profile == 11) ip->uin = 0.185;
+  else if (!ip->shaped)
+    return fail(ctx, CVB_BAD_INPUT,
+                "InflowFlux: inletprofile %d is not covered (constant profiles 1, -1, 11 and shaped 2, 4, 7 are)",
                 profile);
+  else if (!ctx->inlet_coor)
+    return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d needs the inlet's nodes (cvb_set_inlet_nodes)",
+                profile);
+  return CVB_OK;
+}
+
+int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cmy, double cmz) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!ctx->ready) return fail(ctx, CVB_NOT_SETUP, "cvb_setup_hierarchy has not run");
+  if (!coor0) return fail(ctx, CVB_BAD_INPUT, "coor0 is NULL");
+  const Geom &g = ctx->L[ctx->nlevels - 1].g;
+  const size_t n = (size_t)3 * g.mx * g.my;
+  if (!ctx->inlet_coor) TRY(dalloc(ctx, &ctx->inlet_coor, n));
+  CK(cudaMemcpyAsync(ctx->inlet_coor, coor0, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->inlet_cm[0] = cmx;
+  ctx->inlet_cm[1] = cmy;
+  ctx->inlet_cm[2] = cmz;
   return CVB_OK;
 }
 
@@ -1888,10 +1916,11 @@ struct BcSums {
 
 // InflowFlux: the inlet face's ubcs and Ucont.z, and FluxInSum (summed once:
 // its terms depend on the grid and nvert alone).
-static int inflow_dev(cvb_ctx *ctx, double uin, BcSums &bs) {
+static int inflow_dev(cvb_ctx *ctx, const InletProfile &ip, BcSums &bs) {
   LevelDev &F = ctx->L[ctx->nlevels - 1];
   const size_t n2 = (size_t)(F.g.mx - 2) * (F.g.my - 2);
-  launch_inflow(F.g, F.nvert, ctx->cm[2], uin, ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch, ctx->stream);
+  launch_inflow(F.g, F.nvert, ctx->cm[2], ip.uin, ip.shaped ? ctx->inlet_coor : nullptr, ip.profile,
+                ctx->inlet_cm[1], ctx->inlet_cm[2], ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch, ctx->stream);
   if (bs.have_flux_in) return CVB_OK;
   CKL();
   CK(cudaMemcpyAsync(ctx->bc_host, ctx->bc_scratch, sizeof(double) * n2, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1940,7 +1969,7 @@ int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile,
   if (!ucont || !ubcs || !flux_in_sum) return fail(ctx, CVB_BAD_INPUT, "InflowFlux: ucont/ubcs/flux_in_sum is NULL");
   TRY(bc_covered(ctx, "InflowFlux"));
   if (ctx->H[ctx->nlevels - 1].d.bctype[4] != 5) return CVB_OK;  // FluxIn 0; FluxInSum keeps its value
-  double uin;
+  InletProfile uin;
   TRY(inlet_speed(ctx, inletprofile, &uin));
   const size_t n = ctx->L[ctx->nlevels - 1].g.n();
   TRY(post_buffers(ctx, n));
@@ -2022,7 +2051,7 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   if (!(ren != 0.0) || !(dt != 0.0)) return fail(ctx, CVB_BAD_INPUT, "ImpRK: ren / dt is 0");
   TRY(bc_covered(ctx, "ImpRK"));
   const bool inlet = ctx->H[ctx->nlevels - 1].d.bctype[4] == 5;
-  double uin = 0.;
+  InletProfile uin;
   if (inlet) TRY(inlet_speed(ctx, o->inletprofile, &uin));
   const int l = ctx->nlevels - 1;
   LevelDev &F = ctx->L[l];

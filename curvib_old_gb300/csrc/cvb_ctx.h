@@ -98,6 +98,8 @@ struct cvb_ctx {
   double *visc_dev = nullptr, *rct_dev = nullptr, *rhs_dev = nullptr, *uo_dev = nullptr, *urm_dev = nullptr;
   double *pu_dev = nullptr;                // ImpRK: the last kept iterate (pUcont)
   unsigned long long *imp_norms = nullptr; // ImpRK: |Rhs| and |dU| as bit patterns
+  double *inlet_coor = nullptr;  // the k = 0 node plane ([my][mx][3]) for the shaped inlet profiles
+  double inlet_cm[3] = {};       // CMx_c, CMy_c, CMz_c
   double *bc_scratch = nullptr;            // InflowFlux / outlet: plane terms (device)
   double *bc_host = nullptr;               // the same terms, pinned host memory, for the host's ordered sums
   double u_bc = 0.;                        // GhostNodeVelocity: the rheology plates' velocity (bcs.c's U_bc)

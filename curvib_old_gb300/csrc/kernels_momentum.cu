@@ -398,11 +398,34 @@ __global__ void __launch_bounds__(256) k_imp_norms(size_t n, const double *__res
 // the reference skips carry +0.0, which leaves a sum that started at +0.0 as
 // it was.
 //
+// The shaped inlet speeds (bcs.c:152-192) at face cell (i, j): the mean of
+// its four nodes of the k = 0 node plane (coor0, [my][mx][3]) less the centre
+// (cmy, cmz); profile 2 a parabola across y in [0, 4.1] peaking at 1.5, 4 a
+// pipe of radius 0.5 peaking at 2, 7 a parabola across y in [-0.5, 0.5]
+// peaking at 1.5.  Each product and sum rounded on its own, in the
+// reference's order.
+__device__ double inlet_shaped(int profile, const double *__restrict__ coor0, int mx, int i, int j, double cmy,
+                               double cmz) {
+  const double *a = coor0 + 3 * ((size_t)j * mx + i), *b = coor0 + 3 * ((size_t)(j - 1) * mx + i);
+  const double *c = coor0 + 3 * ((size_t)j * mx + i - 1), *d = coor0 + 3 * ((size_t)(j - 1) * mx + i - 1);
+  const double yc = (a[1] + b[1] + c[1] + d[1]) * 0.25 - cmy;
+  const double zc = (a[2] + b[2] + c[2] + d[2]) * 0.25 - cmz;
+  const double H = 4.1, Umax = 1.5;
+  if (profile == 2) return __ddiv_rn(4. * Umax * yc * (H - yc), H * H);
+  if (profile == 4) {
+    const double r = __dsqrt_rn(zc * zc + yc * yc);
+    return r > 0.5 ? 0. : 2. * (1. - 4. * r * r);
+  }
+  return 1.5 * (1. - 4. * yc * yc);
+}
+
 // InflowFlux on the k = 0 face (bcs.c:148-236): above a fluid cell, ubcs =
 // uin zet / |zet| (in the reference's order .y, .z, .x, each its own
 // quotient) and Ucont.z = uin |zet|, |zet| summed z, y, x; the face's flux
-// terms into terms[(j - 1)(mx - 2) + i - 1].
+// terms into terms[(j - 1)(mx - 2) + i - 1].  uin is the constant speed, or
+// with coor0 set the shaped profile's at the cell.
 __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__restrict__ zet, double uin,
+                         const double *__restrict__ coor0, int profile, double cmy, double cmz,
                          double *__restrict__ uc, double *__restrict__ ub, double *__restrict__ terms) {
   const int ni = g.mx - 2, n = ni * (g.my - 2);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -411,6 +434,7 @@ __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__
   const size_t q = (size_t)j * g.mx + i;
   double term = 0.;
   if (nv[q + (size_t)g.mx * g.my] < 0.1) {
+    if (coor0) uin = inlet_shaped(profile, coor0, g.mx, i, j, cmy, cmz);
     const double *z = zet + 3 * q;
     const double a = __dsqrt_rn(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
     ub[3 * q + 1] = __ddiv_rn(uin * z[1], a);
@@ -422,10 +446,10 @@ __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__
   terms[t] = term;
 }
 
-void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, double *ucont, double *ubcs,
-                   double *terms, cudaStream_t s) {
+void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, const double *coor0,
+                   int profile, double cmy, double cmz, double *ucont, double *ubcs, double *terms, cudaStream_t s) {
   const int n = (g.mx - 2) * (g.my - 2);
-  k_inflow<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, uin, ucont, ubcs, terms);
+  k_inflow<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, uin, coor0, profile, cmy, cmz, ucont, ubcs, terms);
   count_launch();
 }
 

@@ -241,6 +241,12 @@ class PoissonContext:
         """The rheology plates' velocity (bctype 13), bcs.c's U_bc."""
         self._check(self._L.cvb_set_plate_velocity(self._ctx, float(u_bc)))
 
+    def set_inlet_nodes(self, coor0, cm=(0.0, 0.0, 0.0)):
+        """The k = 0 node plane ([my][mx][3]) and CMx_c, CMy_c, CMz_c for the
+        shaped inlet profiles 2, 4 and 7 (bcs.c:152-192)."""
+        c = np.ascontiguousarray(coor0, dtype=np.float64)
+        self._check(self._L.cvb_set_inlet_nodes(self._ctx, ptr(c), float(cm[0]), float(cm[1]), float(cm[2])))
+
     def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0):
         """InflowFlux (bcs.c:99): (ucont, ubcs, FluxInSum)."""
         uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]

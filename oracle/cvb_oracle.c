@@ -1388,15 +1388,58 @@ int orc_bcs_covered(const int *bc) {
   return (bc[5] == 4) == (bc[4] == 5);
 }
 
+/* The inlet speed of profiles 2, 4 and 7 (bcs.c:152-192) at face cell (i, j)
+ * of the k = 0 face, from the mean of its four nodes (coor: the node
+ * coordinates in the box layout [mz][my][mx][3]) less cm (CMx_c, CMy_c,
+ * CMz_c). */
+double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, int i, int j, const double *cm) {
+  const double *a = coor + 3 * ((size_t)j * mx + i), *b = coor + 3 * ((size_t)(j - 1) * mx + i);
+  const double *c = coor + 3 * ((size_t)j * mx + i - 1), *d = coor + 3 * ((size_t)(j - 1) * mx + i - 1);
+  const double yc = (a[1] + b[1] + c[1] + d[1]) * 0.25 - cm[1];
+  const double zc = (a[2] + b[2] + c[2] + d[2]) * 0.25 - cm[2];
+  const double r = sqrt(zc * zc + yc * yc);
+  const double H = 4.1, Umax = 1.5;
+  if (inletprofile == 2) return 4. * Umax * yc * (H - yc) / (H * H);
+  if (inletprofile == 4) {
+    double uin = 2. * (1. - 4. * r * r);
+    if (r > 0.5) uin = 0.;
+    return uin;
+  }
+  return 1.5 * (1. - 4. * yc * yc); /* 7 */
+}
+
+/* The inlet's nodes orc_inflow_flux and orc_imp_rk use for the shaped
+ * profiles (the reference reads its coordinates and CMx_c, CMy_c, CMz_c as
+ * globals too). */
+static const double *g_inlet_coor;
+static double g_inlet_cm[3];
+void orc_set_inlet_nodes(const double *coor0, const double *cm) {
+  g_inlet_coor = coor0;
+  for (int d = 0; d < 3; d++) g_inlet_cm[d] = cm ? cm[d] : 0.;
+}
+
+static int inlet_covered(int inletprofile) {
+  double uin;
+  if (inletprofile == 2 || inletprofile == 4 || inletprofile == 7) return g_inlet_coor != NULL;
+  return orc_inlet_speed(inletprofile, &uin);
+}
+
 int orc_inflow_flux(const orc_level *L, double *ucont, double *ub, int inletprofile, double *flux_in_sum) {
+  return orc_inflow_flux_ext(L, ucont, ub, inletprofile, g_inlet_coor, g_inlet_cm, flux_in_sum);
+}
+
+int orc_inflow_flux_ext(const orc_level *L, double *ucont, double *ub, int inletprofile, const double *coor,
+                        const double *cm, double *flux_in_sum) {
   const int mx = L->mx, my = L->my;
   if (L->bctype[4] != 5) return 0; /* FluxIn is 0 and FluxInSum keeps its value */
-  double uin;
-  if (!orc_inlet_speed(inletprofile, &uin)) return -1;
+  double uin0 = 0.;
+  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7;
+  if (shaped ? !(coor && cm) : !orc_inlet_speed(inletprofile, &uin0)) return -1;
   const double *z;
   for (int j = 1; j < my - 1; j++)
     for (int i = 1; i < mx - 1; i++) {
       const size_t q = ID(L, i, j, 0);
+      const double uin = shaped ? orc_inlet_shaped(inletprofile, coor, mx, my, i, j, cm) : uin0;
       if (!(L->nvert[ID(L, i, j, 1)] < 0.1)) continue;
       z = L->zet + 3 * q;
       ub[3 * q + 1] = uin * z[1] / sqrt(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
@@ -1500,8 +1543,7 @@ int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const d
   const size_t n3 = 3 * (size_t)L->mx * L->my * L->mz;
   const double alfa[4] = {0.25, 1 / 3., 0.5, 1.}; /* implicitsolver.c:7111 */
   double flux_in_sum = 0.;
-  double uin;
-  if (!orc_bcs_covered(L->bctype) || (L->bctype[4] == 5 && !orc_inlet_speed(inletprofile, &uin))) return -1;
+  if (!orc_bcs_covered(L->bctype) || (L->bctype[4] == 5 && !inlet_covered(inletprofile))) return -1;
   /* InflowFlux, OutflowFlux (only sums what nothing here reads), FormBCS */
   orc_inflow_flux(L, ucont, ubcs, inletprofile, &flux_in_sum);
   orc_form_bcs(L, ucont, ubcs, ucat, p, flux_in_sum, flux_intp_sum);

@@ -134,6 +134,16 @@ int orc_inlet_speed(int inletprofile, double *uin);
  * reference's loop order.  Nothing for a wall (FluxInSum keeps its value);
  * -1 for a profile that is not restated. */
 int orc_inflow_flux(const orc_level *L, double *ucont, double *ubcs, int inletprofile, double *flux_in_sum);
+/* The same with the shaped profiles 2 (a parabola in y), 4 (a pipe) and 7
+ * (a parabola in y about 0), whose speed depends on the face cell's centre:
+ * coor, the k = 0 node plane in the box layout [my][mx][3] (the first plane
+ * of a [mz][my][mx][3] box), and cm, (CMx_c, CMy_c, CMz_c).  -1 for a shaped
+ * profile without them.  orc_inflow_flux and orc_imp_rk take them from
+ * orc_set_inlet_nodes (NULL: none). */
+void orc_set_inlet_nodes(const double *coor0, const double *cm);
+int orc_inflow_flux_ext(const orc_level *L, double *ucont, double *ubcs, int inletprofile, const double *coor,
+                        const double *cm, double *flux_in_sum);
+double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, int i, int j, const double *cm);
 /* FormBCS (bcs.c:4436-5889) on a covered box (orc_bcs_covered): three passes
  * of the outlet's flux correction (bctype[5] 4, bcs.c:4914-4998: ubcs on the
  * last face = the ucat next to it, Ucont.z of the last interior face = ubcs .

@@ -124,6 +124,10 @@ def lib():
         _lib.orc_calc_rhs.argtypes = [L, P, P, P, P, P, D, D, I, I, I, P]
         _lib.orc_inflow_flux.argtypes = [L, P, P, I, P]
         _lib.orc_inflow_flux.restype = I
+        _lib.orc_inflow_flux_ext.argtypes = [L, P, P, I, P, P, P]
+        _lib.orc_inflow_flux_ext.restype = I
+        _lib.orc_set_inlet_nodes.argtypes = [P, P]
+        _lib.orc_set_inlet_nodes.restype = None
         _lib.orc_form_bcs.argtypes = [L, P, P, P, P, D, D]
         _lib.orc_form_bcs.restype = I
         _lib.orc_imp_rk.argtypes = [L, P, P, P, P, P, P, D, D, D, D, I, I, I, D, D, I, I, D, P]
@@ -314,13 +318,17 @@ class ImpRKStats(ctypes.Structure):
                 ("lambda_", ctypes.c_double)]
 
 
-def inflow_flux(L: OLevel, ucont, ubcs, inletprofile, flux_in_sum=0.0):
-    """InflowFlux (bcs.c:99-400), inlet on k = 0 with a constant profile:
-    (status, ucont, ubcs, FluxInSum)."""
+def inflow_flux(L: OLevel, ucont, ubcs, inletprofile, flux_in_sum=0.0, coor=None, cm=(0.0, 0.0, 0.0)):
+    """InflowFlux (bcs.c:99-400), inlet on k = 0, a constant profile or (with
+    the node coordinates coor, box layout, and cm = CMx_c, CMy_c, CMz_c) a
+    shaped one: (status, ucont, ubcs, FluxInSum)."""
     uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
     ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
     f = ctypes.c_double(flux_in_sum)
-    rc = lib().orc_inflow_flux(L.ref(), _p(uc), _p(ub), int(inletprofile), ctypes.byref(f))
+    cmv = np.array(cm, dtype=np.float64)
+    co = None if coor is None else np.ascontiguousarray(coor, dtype=np.float64)
+    rc = lib().orc_inflow_flux_ext(L.ref(), _p(uc), _p(ub), int(inletprofile), None if co is None else _p(co),
+                                   _p(cmv), ctypes.byref(f))
     return rc, uc, ub, f.value
 
 
@@ -332,9 +340,22 @@ def form_bcs(L: OLevel, ucont, ubcs, ucat, p, flux_in_sum=0.0, flux_intp_sum=0.0
 
 
 def imp_rk(L: OLevel, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=0,
-           atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0):
-    """ImpRK (implicitsolver.c:7094-7257), no immersed body: (status, ucont,
+           atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0, coor=None, cm=(0.0, 0.0, 0.0)):
+    """ImpRK (implicitsolver.c:7094-7257), no immersed body (coor, cm: the
+    k = 0 node plane and centre of a shaped inlet profile): (status, ucont,
     ucat, p, stats, ubcs)."""
+    co = None if coor is None else np.ascontiguousarray(coor, dtype=np.float64)
+    cmv = np.array(cm, dtype=np.float64)
+    lib().orc_set_inlet_nodes(None if co is None else _p(co), _p(cmv))
+    try:
+        return _imp_rk(L, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central, atol, rtol,
+                       max_it, inletprofile, flux_intp_sum)
+    finally:
+        lib().orc_set_inlet_nodes(None, None)
+
+
+def _imp_rk(L, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central, atol, rtol, max_it,
+            inletprofile, flux_intp_sum):
     uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
     uo, urm = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1)]
     ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")
@@ -537,9 +558,10 @@ class Reference:
             raise RuntimeError("ref_calc_rhs failed")
         return out, u
 
-    def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0):
+    def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0, cm=(0.0, 0.0, 0.0)):
         uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]
         f = ctypes.c_double(flux_in_sum)
+        self.L.ref_set_cm(ctypes.c_double(cm[0]), ctypes.c_double(cm[1]), ctypes.c_double(cm[2]))
         if self.L.ref_inflow_flux(_p(uc), _p(ub), int(inletprofile), ctypes.byref(f)):
             raise RuntimeError("ref_inflow_flux failed")
         return uc, ub, f.value
@@ -552,9 +574,11 @@ class Reference:
         return uc, ub, u, pp
 
     def imp_rk(self, ucont, ucont_o, ucont_rm1, ucat, p, ubcs, ren, dt, st, cfl, ti, tistart, central=0,
-               atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0):
-        """ImpRK through the reference's own routine: (ucont, ucat, p, ubcs);
-        it appends to Converge_dU0 in the working directory."""
+               atol=1e-7, rtol=1e-4, max_it=50, inletprofile=1, flux_intp_sum=0.0, cm=(0.0, 0.0, 0.0)):
+        """ImpRK through the reference's own routine (cm: CMx_c, CMy_c, CMz_c):
+        (ucont, ucat, p, ubcs); it appends to Converge_dU0 in the working
+        directory."""
+        self.L.ref_set_cm(ctypes.c_double(cm[0]), ctypes.c_double(cm[1]), ctypes.c_double(cm[2]))
         uc = np.array(ucont, dtype=np.float64, copy=True, order="C")
         uo, urm = [np.ascontiguousarray(x, dtype=np.float64) for x in (ucont_o, ucont_rm1)]
         ub = np.array(ubcs, dtype=np.float64, copy=True, order="C")

@@ -697,6 +697,11 @@ extern PetscInt inletprofile;
 PetscErrorCode InflowFlux(UserCtx *user);
 PetscErrorCode FormBCS(UserCtx *user);
 
+/* CMx_c, CMy_c, CMz_c (main.c's globals), which the shaped inlet profiles
+ * subtract from the face centres. */
+extern PetscReal CMx_c, CMy_c, CMz_c;
+void ref_set_cm(double x, double y, double z) { CMx_c = x; CMy_c = y; CMz_c = z; }
+
 int ref_inflow_flux(double *ucont, double *ubcs, int profile, double *flux_in_sum) {
   if (!g_ready) return 1;
   UserCtx *u = U(g_mg.mglevels - 1);

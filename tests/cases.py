@@ -176,6 +176,19 @@ IMP_ATOL, IMP_RTOL = 1e-7, 1e-4
 INLET_OUTLET_SCENARIOS = ("box_sphere", "blocked_slab")
 INLET_PROFILES = (1, -1, 11)
 FLUX_INTP_SUM = 1e-3
+# The shaped profiles (2: a parabola across y in [0, 4.1]; 4: a pipe of
+# radius 0.5; 7: a parabola across y in [-0.5, 0.5]), each with a centre
+# (CMx_c, CMy_c, CMz_c) that puts the unit box's inlet across its shape.
+SHAPED_INLETS = ((2, (0.0, 0.1, 0.0)), (4, (0.1, 0.45, 0.5)), (7, (0.0, 0.5, 0.0)))
+
+
+def inlet_plane(nodes, shape):
+    """The k = 0 node plane in the box layout ([my][mx][3]) of a case's nodes
+    ([KM][JM][IM][3]) on a box of shape (mz, my, mx)."""
+    _, my, mx = shape
+    plane = np.zeros((my, mx, 3))
+    plane[:nodes.shape[1], :nodes.shape[2]] = nodes[0]
+    return plane
 
 
 def imp_rk_inputs(shape, ucont):

@@ -113,6 +113,15 @@ int cvb_set_cell_centres(cvb_ctx *ctx, const double *cent) {
   REC.cent = cent;
   return CVB_OK;
 }
+int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cmy, double cmz) {
+  (void)ctx;
+  REC.n_inlet_nodes++;
+  memcpy(REC.inlet_plane, coor0, sizeof REC.inlet_plane);
+  REC.inlet_cm[0] = cmx;
+  REC.inlet_cm[1] = cmy;
+  REC.inlet_cm[2] = cmz;
+  return CVB_OK;
+}
 int cvb_set_plate_velocity(cvb_ctx *ctx, double u_bc) {
   (void)ctx;
   REC.u_bc = u_bc;

@@ -39,6 +39,9 @@ typedef struct {
   const double *uo_imp, *urm_imp;
   double ren_imp, dt_imp, st_imp, cfl_imp, atol_imp, rtol_imp, intp_imp;
   int ti_imp, tistart_imp, central_imp, max_it_imp, profile_imp;
+  /* cvb_set_inlet_nodes: calls, a copy of the plane and the centre */
+  int n_inlet_nodes;
+  double inlet_plane[3 * 64 * 64], inlet_cm[3];
   /* the status the next path call returns, then 0 again */
   int fail_next;
   /* cell (box index) the path calls write: solver_mg sets ucont[3m+1] = 42 and

@@ -19,7 +19,7 @@
 
 extern PetscInt block_number, immersed, wallfunction, les;
 extern PetscInt ti, tistart, imp_MAX_IT;
-extern PetscReal imp_atol, imp_rtol, FluxInSum, U_bc;
+extern PetscReal imp_atol, imp_rtol, FluxInSum, U_bc, CMx_c, CMy_c, CMz_c;
 extern PetscInt inletprofile;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
@@ -230,6 +230,23 @@ int main(void) {
   CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.n_imp_rk == 2 && REC.profile_imp == 11 && REC.intp_imp == 0.25,
         "inlet / outlet ImpRK not on the device with its profile and FluxIntpSum");
   CHECK(FluxInSum == 0.5 && fine->FluxInSum == 0.5, "FluxInSum not set after ImpRK");
+  CHECK(REC.n_inlet_nodes == 0, "inlet nodes handed over for a constant profile");
+  /* a shaped profile: the k = 0 node plane and the centre go first */
+  inletprofile = 4;
+  CMx_c = 0.5, CMy_c = 0.25, CMz_c = 0.125;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.n_imp_rk == 3 && REC.profile_imp == 4 && REC.n_inlet_nodes == 1,
+        "shaped-profile ImpRK not on the device with the inlet's nodes");
+  CHECK(REC.inlet_cm[0] == 0.5 && REC.inlet_cm[1] == 0.25 && REC.inlet_cm[2] == 0.125, "CMx_c / CMy_c / CMz_c");
+  {
+    int bad = 0;
+    const int mx = fine->info.mx;
+    for (int j = 0; j < JM; j++)
+      for (int i = 0; i < IM; i++)
+        for (int d = 0; d < 3; d++) bad += REC.inlet_plane[3 * (j * mx + i) + d] != coords[3 * (j * IM + i) + d];
+    CHECK(bad == 0, "k = 0 node plane: %d coordinates differ", bad);
+  }
+  CMx_c = CMy_c = CMz_c = 0.0;
+  inletprofile = 11;
   CHECK(shim_vec_data(fine->Bcs.Ubcs)[3 * REC.mark + 2] == 14.0, "Bcs.Ubcs not written back");
   fine->bctype[4] = fine->bctype[5] = 1;
   PetscOptionsSetValue("-central", "1");

@@ -31,7 +31,7 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
 from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_OUTLET_SCENARIOS, INLET_PROFILES,  # noqa: E402
-                   MOM_DT, MOM_REN,
+                   MOM_DT, MOM_REN, SHAPED_INLETS,
                    conv_seam_nvert, imp_rk_inputs, mom_edge_nvert, momentum_inputs)
 from cases import (IBM_CASES, POST_U_BC, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
@@ -157,7 +157,8 @@ def inlet_outlet(c):
     the scenario's grid with an inlet on the k = 0 face (bctype[4] 5) and an
     outlet on the last (bctype[5] 4): the constant inlet profiles, FormBCS with
     the inlet's flux and an immersed-boundary flux, and cases.IMP_RK_RUNS with
-    profile 1."""
+    profile 1; the shaped profiles (cases.SHAPED_INLETS) and ImpRK's first run
+    with the pipe profile 4."""
     bct = [1, 1, 1, 1, 5, 4]
     nl = c["nl"]
     R = O.Reference(c["nodes"], nl, bct, c["semi"])
@@ -166,6 +167,9 @@ def inlet_outlet(c):
     out = {}
     for prof in INLET_PROFILES:
         uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, prof)
+        out[f"inflow_{prof}"] = {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)}
+    for prof, cm in SHAPED_INLETS:
+        uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, prof, 0.0, cm)
         out[f"inflow_{prof}"] = {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)}
     uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, 1)
     uc, ub, u, pp = R.form_bcs(uc, ub, ucat1, p1, f, FLUX_INTP_SUM)
@@ -179,6 +183,12 @@ def inlet_outlet(c):
                                          0, IMP_ATOL, IMP_RTOL, max_it, 1, FLUX_INTP_SUM)
                 out[f"imp_rk_{ti}_{cfl}_{max_it}"] = {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u),
                                                       "p": digest(pp)}
+            prof, cm = SHAPED_INLETS[1]
+            ti, cfl, max_it = IMP_RK_RUNS[0]
+            uc, u, pp, ub = R.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
+                                     IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM, cm)
+            out[f"imp_rk_shaped_{prof}"] = {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u),
+                                            "p": digest(pp)}
         finally:
             os.chdir(cwd)
     return out

@@ -116,12 +116,13 @@ def test_form_bcs_and_imp_rk_match_oracle(name):
 
 @pytest.mark.parametrize("name", ["box_sphere", "blocked_slab"])
 def test_inlet_outlet_match_oracle(name):
-    """InflowFlux (bcs.c:99) with the constant profiles, FormBCS's outlet
+    """InflowFlux (bcs.c:99) with the constant and shaped profiles, FormBCS's outlet
     correction with an immersed-boundary flux, and ImpRK on the scenario's grid
     with an inlet on k = 0 and an outlet on the last k face, bit for bit
     against the oracle (pinned to the reference's routines): ucont, ubcs, ucat,
     p, FluxInSum and the iteration counts."""
-    from cases import FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, imp_rk_inputs
+    from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, SHAPED_INLETS, imp_rk_inputs,
+                       inlet_plane)
     c = build(name)
     bctype = [1, 1, 1, 1, 5, 4]
     ctx = _ctx(c, c["nvert"], bctype)
@@ -132,6 +133,21 @@ def test_inlet_outlet_match_oracle(name):
             uc_g, ub_g, f_g = ctx.inflow_flux(c["ucont"], ubcs1, prof)
             rc, uc_o, ub_o, f_o = O.inflow_flux(L, c["ucont"], ubcs1, prof)
             assert rc == 0 and _same(uc_g, uc_o) and _same(ub_g, ub_o) and f_g == f_o, prof
+        plane = inlet_plane(c["nodes"], c["nvert"].shape)
+        for prof, cm in SHAPED_INLETS:
+            ctx.set_inlet_nodes(plane, cm)
+            uc_g, ub_g, f_g = ctx.inflow_flux(c["ucont"], ubcs1, prof)
+            rc, uc_o, ub_o, f_o = O.inflow_flux(L, c["ucont"], ubcs1, prof, 0.0, plane, cm)
+            assert rc == 0 and _same(uc_g, uc_o) and _same(ub_g, ub_o) and f_g == f_o, prof
+        prof, cm = SHAPED_INLETS[1]
+        ctx.set_inlet_nodes(plane, cm)
+        ti, cfl, max_it = IMP_RK_RUNS[0]
+        uc_g, u_g, p_g, st_g, ub_g = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti,
+                                                0, 0, IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM)
+        rc, uc_o, u_o, p_o, st_o, ub_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
+                                                  ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM, plane, cm)
+        assert rc == 0 and st_g["pseudo_iterations"] == st_o.pseudo_iterations
+        assert all(_same(a, b) for a, b in ((uc_g, uc_o), (u_g, u_o), (p_g, p_o), (ub_g, ub_o)))
         uc_i, ub_i, f = ctx.inflow_flux(c["ucont"], ubcs1, 1)
         got = ctx.form_bcs(uc_i, ub_i, ucat1, p1, f, FLUX_INTP_SUM)
         rc, *want = O.form_bcs(L, uc_i, ub_i, ucat1, p1, f, FLUX_INTP_SUM)
