@@ -318,7 +318,7 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
 /* ImpRK (implicitsolver.c:7094-7257) with the reference's arguments.  On one
  * block with no immersed body, no LES / RANS / wall model, solid walls on the
  * x and y faces and on the k faces walls or an inlet (5, profile 1, -1, 11, 2,
- * 4 or 7) with an outlet (4), the whole pseudo-time iteration runs on the device
+ * 4, 7 or 10) with an outlet (4), the whole pseudo-time iteration runs on the device
  * (cvb_imp_rk: InflowFlux, FormBCS, CalcRHS, the Runge-Kutta stage updates,
  * the norms and the step halving), with the reference's -cfl, -imp_atol,
  * -imp_rtol, -imp_MAX_IT, -inlet (inletprofile) and -central and the block's
@@ -353,7 +353,7 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
   const PetscInt *bt = u->bctype;
   int covered = bt[0] == 1 && bt[1] == 1 && bt[2] == 1 && bt[3] == 1 && (bt[4] == 1 || bt[4] == 5) &&
                 (bt[5] == 1 || bt[5] == 4) && ((bt[4] == 5) == (bt[5] == 4));
-  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7;
+  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10;
   if (bt[4] == 5) covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11 || shaped);
   if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !covered || !u->Ucont_o ||
       !u->Ucont_rm1)

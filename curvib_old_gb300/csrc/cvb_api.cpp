@@ -1843,26 +1843,68 @@ static int bc_covered(cvb_ctx *ctx, const char *who) {
 }
 
 // InflowFlux's profiles (bcs.c:152-200): the constant ones (1, -1, 11) and
-// the shaped ones (2, 4, 7), which need the k = 0 node plane
+// the shaped ones (2, 4, 7, 10), which need the k = 0 node plane
 // (cvb_set_inlet_nodes).
 struct InletProfile {
   double uin = 0.;
   int profile = 0;
   bool shaped = false;
+  const double *uin_cell = nullptr;
 };
+
+// Profile 10 (bcs.c:180-195): fully developed laminar flow in a square duct,
+// 1 - y'^2 less the first 20 terms of its Fourier series in y' = 2 (y - 1.5),
+// x' = x - 0.5, each term's factors taken left to right.  Its pow, cosh and
+// cos are libm's, as the reference's, so its speeds are formed here on the
+// host, once per set of nodes.
+static double duct_speed(double xc, double yc) {
+  const double pi = 3.14159265358979323846264338327950288;
+  const double y = (yc - 1.5) * 2., x = xc - 0.5, A = 1.;
+  double u = 1 - y * y;
+  for (int n = 0; n < 20; n++)
+    u -= 4. * pow(2. / pi, 3) * pow(-1., n) / pow(2 * n + 1., 3.) * cosh((2 * n + 1) * pi * x / 2.) *
+         cos((2. * n + 1) * pi * y / 2.) / cosh((2 * n + 1) * pi * A / 2.);
+  return u;
+}
+
+static int duct_speeds(cvb_ctx *ctx) {
+  if (ctx->inlet_uin_ready) return CVB_OK;
+  const Geom &g = ctx->L[ctx->nlevels - 1].g;
+  const int ni = g.mx - 2, nj = g.my - 2;
+  const double *P = ctx->inlet_plane_host.data(), *cm = ctx->inlet_cm;
+  std::vector<double> u((size_t)ni * nj);
+  for (int j = 1; j <= nj; j++)
+    for (int i = 1; i <= ni; i++) {
+      const double *a = P + 3 * ((size_t)j * g.mx + i), *b = P + 3 * ((size_t)(j - 1) * g.mx + i);
+      const double *c = P + 3 * ((size_t)j * g.mx + i - 1), *d = P + 3 * ((size_t)(j - 1) * g.mx + i - 1);
+      const double xc = (a[0] + b[0] + c[0] + d[0]) * 0.25 - cm[0];
+      const double yc = (a[1] + b[1] + c[1] + d[1]) * 0.25 - cm[1];
+      u[(size_t)(j - 1) * ni + i - 1] = duct_speed(xc, yc);
+    }
+  if (!ctx->inlet_uin) TRY(dalloc(ctx, &ctx->inlet_uin, u.size()));
+  CK(cudaMemcpyAsync(ctx->inlet_uin, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->inlet_uin_ready = true;
+  return CVB_OK;
+}
+
 static int inlet_speed(cvb_ctx *ctx, int profile, InletProfile *ip) {
   ip->profile = profile;
-  ip->shaped = profile == 2 || profile == 4 || profile == 7;
+  ip->shaped = profile == 2 || profile == 4 || profile == 7 || profile == 10;
   if (profile == 1) ip->uin = 2.;
   else if (profile == -1) ip->uin = -1.;
   else if (profile == 11) ip->uin = 0.185;
   else if (!ip->shaped)
     return fail(ctx, CVB_BAD_INPUT,
-                "InflowFlux: inletprofile %d is not covered (constant profiles 1, -1, 11 and shaped 2, 4, 7 are)",
+                "InflowFlux: inletprofile %d is not covered (constant profiles 1, -1, 11 and shaped 2, 4, 7, 10 are)",
                 profile);
   else if (!ctx->inlet_coor)
     return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d needs the inlet's nodes (cvb_set_inlet_nodes)",
                 profile);
+  if (profile == 10) {
+    TRY(duct_speeds(ctx));
+    ip->uin_cell = ctx->inlet_uin;
+  }
   return CVB_OK;
 }
 
@@ -1875,6 +1917,8 @@ int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cm
   if (!ctx->inlet_coor) TRY(dalloc(ctx, &ctx->inlet_coor, n));
   CK(cudaMemcpyAsync(ctx->inlet_coor, coor0, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->inlet_plane_host.assign(coor0, coor0 + n);
+  ctx->inlet_uin_ready = false;
   ctx->inlet_cm[0] = cmx;
   ctx->inlet_cm[1] = cmy;
   ctx->inlet_cm[2] = cmz;
@@ -1920,7 +1964,8 @@ static int inflow_dev(cvb_ctx *ctx, const InletProfile &ip, BcSums &bs) {
   LevelDev &F = ctx->L[ctx->nlevels - 1];
   const size_t n2 = (size_t)(F.g.mx - 2) * (F.g.my - 2);
   launch_inflow(F.g, F.nvert, ctx->cm[2], ip.uin, ip.shaped ? ctx->inlet_coor : nullptr, ip.profile,
-                ctx->inlet_cm[1], ctx->inlet_cm[2], ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch, ctx->stream);
+                ctx->inlet_cm[1], ctx->inlet_cm[2], ip.uin_cell, ctx->uc_dev, ctx->ubcs_dev, ctx->bc_scratch,
+                ctx->stream);
   if (bs.have_flux_in) return CVB_OK;
   CKL();
   CK(cudaMemcpyAsync(ctx->bc_host, ctx->bc_scratch, sizeof(double) * n2, cudaMemcpyDeviceToHost, ctx->stream));

@@ -100,6 +100,9 @@ struct cvb_ctx {
   unsigned long long *imp_norms = nullptr; // ImpRK: |Rhs| and |dU| as bit patterns
   double *inlet_coor = nullptr;  // the k = 0 node plane ([my][mx][3]) for the shaped inlet profiles
   double inlet_cm[3] = {};       // CMx_c, CMy_c, CMz_c
+  std::vector<double> inlet_plane_host;  // the same plane on the host (profile 10's speeds)
+  double *inlet_uin = nullptr;   // profile 10's speed per inlet face cell ([my - 2][mx - 2]), formed on the host
+  bool inlet_uin_ready = false;
   double *bc_scratch = nullptr;            // InflowFlux / outlet: plane terms (device)
   double *bc_host = nullptr;               // the same terms, pinned host memory, for the host's ordered sums
   double u_bc = 0.;                        // GhostNodeVelocity: the rheology plates' velocity (bcs.c's U_bc)

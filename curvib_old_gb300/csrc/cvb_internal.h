@@ -336,7 +336,8 @@ void launch_form_bcs(const Geom &g, const double *csi, const double *eta, const 
 // Ucont.z there, and the face's flux terms in the reference's loop order into
 // terms ((mx - 2)(my - 2) doubles) for the host to add
 void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, const double *coor0,
-                   int profile, double cmy, double cmz, double *ucont, double *ubcs, double *terms, cudaStream_t s);
+                   int profile, double cmy, double cmz, const double *uin_cell, double *ucont, double *ubcs,
+                   double *terms, cudaStream_t s);
 // The outlet's flux correction (one FormBCS pass, bctype[5] 4): its flux and
 // area terms in the reference's loop order into terms[0 .. n2) and
 // terms[n2 .. 2 n2); then, with the ratio the host formed from their sums,

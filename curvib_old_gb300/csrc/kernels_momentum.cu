@@ -422,11 +422,13 @@ __device__ double inlet_shaped(int profile, const double *__restrict__ coor0, in
 // InflowFlux on the k = 0 face (bcs.c:148-236): above a fluid cell, ubcs =
 // uin zet / |zet| (in the reference's order .y, .z, .x, each its own
 // quotient) and Ucont.z = uin |zet|, |zet| summed z, y, x; the face's flux
-// terms into terms[(j - 1)(mx - 2) + i - 1].  uin is the constant speed, or
-// with coor0 set the shaped profile's at the cell.
+// terms into terms[(j - 1)(mx - 2) + i - 1].  uin is the constant speed; with
+// coor0 set the shaped profile's at the cell, with uin_cell set the speed the
+// host formed for the cell (at the terms' index).
 __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__restrict__ zet, double uin,
                          const double *__restrict__ coor0, int profile, double cmy, double cmz,
-                         double *__restrict__ uc, double *__restrict__ ub, double *__restrict__ terms) {
+                         const double *__restrict__ uin_cell, double *__restrict__ uc, double *__restrict__ ub,
+                         double *__restrict__ terms) {
   const int ni = g.mx - 2, n = ni * (g.my - 2);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
@@ -434,7 +436,8 @@ __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__
   const size_t q = (size_t)j * g.mx + i;
   double term = 0.;
   if (nv[q + (size_t)g.mx * g.my] < 0.1) {
-    if (coor0) uin = inlet_shaped(profile, coor0, g.mx, i, j, cmy, cmz);
+    if (uin_cell) uin = uin_cell[t];
+    else if (coor0) uin = inlet_shaped(profile, coor0, g.mx, i, j, cmy, cmz);
     const double *z = zet + 3 * q;
     const double a = __dsqrt_rn(z[2] * z[2] + z[1] * z[1] + z[0] * z[0]);
     ub[3 * q + 1] = __ddiv_rn(uin * z[1], a);
@@ -447,9 +450,11 @@ __global__ void k_inflow(Geom g, const double *__restrict__ nv, const double *__
 }
 
 void launch_inflow(const Geom &g, const double *nvert, const double *zet, double uin, const double *coor0,
-                   int profile, double cmy, double cmz, double *ucont, double *ubcs, double *terms, cudaStream_t s) {
+                   int profile, double cmy, double cmz, const double *uin_cell, double *ucont, double *ubcs,
+                   double *terms, cudaStream_t s) {
   const int n = (g.mx - 2) * (g.my - 2);
-  k_inflow<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, uin, coor0, profile, cmy, cmz, ucont, ubcs, terms);
+  k_inflow<<<blocks_for(n, 256), 256, 0, s>>>(g, nvert, zet, uin, coor0, profile, cmy, cmz, uin_cell, ucont, ubcs,
+                                              terms);
   count_launch();
 }
 

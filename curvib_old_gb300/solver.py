@@ -243,7 +243,7 @@ class PoissonContext:
 
     def set_inlet_nodes(self, coor0, cm=(0.0, 0.0, 0.0)):
         """The k = 0 node plane ([my][mx][3]) and CMx_c, CMy_c, CMz_c for the
-        shaped inlet profiles 2, 4 and 7 (bcs.c:152-192)."""
+        shaped inlet profiles 2, 4, 7 and 10 (bcs.c:152-195)."""
         c = np.ascontiguousarray(coor0, dtype=np.float64)
         self._check(self._L.cvb_set_inlet_nodes(self._ctx, ptr(c), float(cm[0]), float(cm[1]), float(cm[2])))
 

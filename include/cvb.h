@@ -278,16 +278,18 @@ int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const
  *
  * InflowFlux (bcs.c:99-400) on an inlet face with a constant profile
  * (inletprofile 1: speed 2; -1: speed -1; 11: 0.185) or a shaped one (2, 4,
- * 7, after cvb_set_inlet_nodes; other profiles are refused): on the face's
+ * 7, 10, after cvb_set_inlet_nodes; other profiles are refused): on the face's
  * interior cells above fluid cells ubcs = uin zet / |zet| and Ucont.z = uin
  * |zet|; *flux_in_sum (FluxInSum) = their sum in the reference's loop order.
  * On a walled k = 0 face nothing is written. */
 int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile, double *flux_in_sum);
-/* The inlet's nodes for the shaped profiles (bcs.c:152-192), which take the
+/* The inlet's nodes for the shaped profiles (bcs.c:152-195), which take the
  * speed from each face cell's centre (the mean of its four nodes) less
  * (cmx, cmy, cmz), the reference's CMx_c, CMy_c, CMz_c: profile 2 = 4 (1.5)
  * y (4.1 - y) / 4.1^2, 4 = 2 (1 - 4 r^2) within r = sqrt(y^2 + z^2) <= 0.5
- * and 0 outside, 7 = 1.5 (1 - 4 y^2).  coor0 holds the k = 0 node plane in
+ * and 0 outside, 7 = 1.5 (1 - 4 y^2), 10 = a square duct's fully developed
+ * flow (x in [0, 1], y in [1, 2]; 20 terms of its series, formed on the host
+ * with libm, once per call of this function).  coor0 holds the k = 0 node plane in
  * the box layout, [my][mx][3] (node (i, j) at [j][i], as the reference's
  * local coor array). */
 int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cmy, double cmz);

@@ -1388,13 +1388,29 @@ int orc_bcs_covered(const int *bc) {
   return (bc[5] == 4) == (bc[4] == 5);
 }
 
-/* The inlet speed of profiles 2, 4 and 7 (bcs.c:152-192) at face cell (i, j)
+/* Profile 10 (bcs.c:180-195): fully developed laminar flow in a square duct
+ * (y across [1, 2], x across [0, 1] about the centre), 1 - y'^2 less the
+ * first 20 terms of its Fourier series in y' = 2 (y - 1.5), x' = x - 0.5;
+ * each term's factors multiplied and divided left to right, through libm's
+ * pow, cosh and cos. */
+double orc_duct_speed(double xc, double yc) {
+  const double pi = 3.14159265358979323846264338327950288;
+  const double y = (yc - 1.5) * 2., x = xc - 0.5, A = 1.;
+  double u = 1 - y * y;
+  for (int n = 0; n < 20; n++)
+    u -= 4. * pow(2. / pi, 3) * pow(-1., n) / pow(2 * n + 1., 3.) * cosh((2 * n + 1) * pi * x / 2.) *
+         cos((2. * n + 1) * pi * y / 2.) / cosh((2 * n + 1) * pi * A / 2.);
+  return u;
+}
+
+/* The inlet speed of profiles 2, 4, 7 and 10 (bcs.c:152-195) at face cell (i, j)
  * of the k = 0 face, from the mean of its four nodes (coor: the node
  * coordinates in the box layout [mz][my][mx][3]) less cm (CMx_c, CMy_c,
  * CMz_c). */
 double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, int i, int j, const double *cm) {
   const double *a = coor + 3 * ((size_t)j * mx + i), *b = coor + 3 * ((size_t)(j - 1) * mx + i);
   const double *c = coor + 3 * ((size_t)j * mx + i - 1), *d = coor + 3 * ((size_t)(j - 1) * mx + i - 1);
+  const double xc = (a[0] + b[0] + c[0] + d[0]) * 0.25 - cm[0];
   const double yc = (a[1] + b[1] + c[1] + d[1]) * 0.25 - cm[1];
   const double zc = (a[2] + b[2] + c[2] + d[2]) * 0.25 - cm[2];
   const double r = sqrt(zc * zc + yc * yc);
@@ -1405,6 +1421,7 @@ double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, in
     if (r > 0.5) uin = 0.;
     return uin;
   }
+  if (inletprofile == 10) return orc_duct_speed(xc, yc);
   return 1.5 * (1. - 4. * yc * yc); /* 7 */
 }
 
@@ -1420,7 +1437,7 @@ void orc_set_inlet_nodes(const double *coor0, const double *cm) {
 
 static int inlet_covered(int inletprofile) {
   double uin;
-  if (inletprofile == 2 || inletprofile == 4 || inletprofile == 7) return g_inlet_coor != NULL;
+  if (inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10) return g_inlet_coor != NULL;
   return orc_inlet_speed(inletprofile, &uin);
 }
 
@@ -1433,7 +1450,7 @@ int orc_inflow_flux_ext(const orc_level *L, double *ucont, double *ub, int inlet
   const int mx = L->mx, my = L->my;
   if (L->bctype[4] != 5) return 0; /* FluxIn is 0 and FluxInSum keeps its value */
   double uin0 = 0.;
-  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7;
+  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10;
   if (shaped ? !(coor && cm) : !orc_inlet_speed(inletprofile, &uin0)) return -1;
   const double *z;
   for (int j = 1; j < my - 1; j++)

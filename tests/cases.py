@@ -177,9 +177,10 @@ INLET_OUTLET_SCENARIOS = ("box_sphere", "blocked_slab")
 INLET_PROFILES = (1, -1, 11)
 FLUX_INTP_SUM = 1e-3
 # The shaped profiles (2: a parabola across y in [0, 4.1]; 4: a pipe of
-# radius 0.5; 7: a parabola across y in [-0.5, 0.5]), each with a centre
+# radius 0.5; 7: a parabola across y in [-0.5, 0.5]; 10: a square duct's
+# series solution across x in [0, 1], y in [1, 2]), each with a centre
 # (CMx_c, CMy_c, CMz_c) that puts the unit box's inlet across its shape.
-SHAPED_INLETS = ((2, (0.0, 0.1, 0.0)), (4, (0.1, 0.45, 0.5)), (7, (0.0, 0.5, 0.0)))
+SHAPED_INLETS = ((2, (0.0, 0.1, 0.0)), (4, (0.1, 0.45, 0.5)), (7, (0.0, 0.5, 0.0)), (10, (0.25, -0.8, 0.0)))
 
 
 def inlet_plane(nodes, shape):
