@@ -28,6 +28,7 @@ extern PetscInt inletprofile;           /* main.c: InflowFlux's profile */
 extern PetscReal FluxInSum;             /* main.c: InflowFlux's result, as bcs.c:5 declares it */
 extern PetscReal U_bc;                  /* bcs.c:10: the rheology plates' velocity */
 extern PetscReal CMx_c, CMy_c, CMz_c;   /* main.c: the centre the shaped inlet profiles take from the nodes */
+extern PetscReal Flux_in;               /* main.c: the uniform inlet profiles' speed */
 PetscErrorCode Contra2Cart(UserCtx *user);
 PetscErrorCode GhostNodeVelocity(UserCtx *user);
 PetscErrorCode ImpRK(UserCtx *user, IBMNodes *ibm, FSInfo *fsi); /* implicitsolver.c:7094 */
@@ -317,8 +318,8 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
 
 /* ImpRK (implicitsolver.c:7094-7257) with the reference's arguments.  On one
  * block with no immersed body, no LES / RANS / wall model, solid walls on the
- * x and y faces and on the k faces walls or an inlet (5, profile 1, -1, 11, 2,
- * 4, 7 or 10) with an outlet (4), the whole pseudo-time iteration runs on the device
+ * x and y faces and on the k faces walls or an inlet (5, any profile but the
+ * table ones, 0 and 5) with an outlet (4), the whole pseudo-time iteration runs on the device
  * (cvb_imp_rk: InflowFlux, FormBCS, CalcRHS, the Runge-Kutta stage updates,
  * the norms and the step halving), with the reference's -cfl, -imp_atol,
  * -imp_rtol, -imp_MAX_IT, -inlet (inletprofile) and -central and the block's
@@ -354,7 +355,9 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
   int covered = bt[0] == 1 && bt[1] == 1 && bt[2] == 1 && bt[3] == 1 && (bt[4] == 1 || bt[4] == 5) &&
                 (bt[5] == 1 || bt[5] == 4) && ((bt[4] == 5) == (bt[5] == 4));
   const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10;
-  if (bt[4] == 5) covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11 || shaped);
+  const int uniform = inletprofile == 3 || inletprofile == 6 || inletprofile == 8;
+  if (bt[4] == 5)
+    covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11 || shaped || uniform);
   if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !covered || !u->Ucont_o ||
       !u->Ucont_rm1)
     return ImpRK(u, ibm, fsi);
@@ -362,6 +365,7 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
     const int rc = inlet_nodes(u);
     if (rc) return report(rc, "ImpRK_GB300");
   }
+  if (bt[4] == 5 && uniform) cvb_set_inlet_flux(g_cvb, Flux_in, (int)ti);
   PetscInt central = 0;
   PetscOptionsGetInt(PETSC_NULL, "-central", &central, PETSC_NULL);
   PetscScalar *uc, *uo, *urm, *ucat, *p, *ub;
@@ -395,6 +399,7 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
   VecRestoreArray(u->Ucont, &uc);
   if (rc) return report(rc, "ImpRK_GB300");
   if (bt[4] == 5) FluxInSum = u->FluxInSum = st.flux_in_sum; /* as InflowFlux leaves them (bcs.c:242, 383) */
+  if (bt[4] == 5 && uniform) Flux_in = cvb_inlet_flux_in(g_cvb); /* profile 8 sets it (bcs.c:76) */
   PetscPrintf(PETSC_COMM_WORLD, "ImpRK_GB300: %d pseudo-time iterations (%d undone), |dU| %le, rel %le, |F| %le\n",
               st.pseudo_iterations, st.rejected, st.norm_du, st.rel_du, st.norm_f);
   DMGlobalToLocalBegin(u->fda, u->Ucont, INSERT_VALUES, u->lUcont);

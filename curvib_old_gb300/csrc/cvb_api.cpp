@@ -1894,9 +1894,13 @@ static int inlet_speed(cvb_ctx *ctx, int profile, InletProfile *ip) {
   if (profile == 1) ip->uin = 2.;
   else if (profile == -1) ip->uin = -1.;
   else if (profile == 11) ip->uin = 0.185;
+  else if (profile == 3 || profile == 6) ip->uin = ctx->inlet_flux_in;
+  else if (profile == 8)  // InletInterpolation (bcs.c:75-77) also leaves it in Flux_in
+    ip->uin = ctx->inlet_flux_in = sin(2 * 3.14159 * ctx->inlet_ti / 200.);
   else if (!ip->shaped)
     return fail(ctx, CVB_BAD_INPUT,
-                "InflowFlux: inletprofile %d is not covered (constant profiles 1, -1, 11 and shaped 2, 4, 7, 10 are)",
+                "InflowFlux: inletprofile %d is not covered (uniform profiles 1, -1, 11, 3, 6, 8 and shaped 2, 4, 7, "
+                "10 are)",
                 profile);
   else if (!ctx->inlet_coor)
     return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d needs the inlet's nodes (cvb_set_inlet_nodes)",
@@ -1907,6 +1911,15 @@ static int inlet_speed(cvb_ctx *ctx, int profile, InletProfile *ip) {
   }
   return CVB_OK;
 }
+
+int cvb_set_inlet_flux(cvb_ctx *ctx, double flux_in, int ti) {
+  if (!ctx) return CVB_BAD_INPUT;
+  ctx->inlet_flux_in = flux_in;
+  ctx->inlet_ti = ti;
+  return CVB_OK;
+}
+
+double cvb_inlet_flux_in(const cvb_ctx *ctx) { return ctx ? ctx->inlet_flux_in : 0.; }
 
 int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cmy, double cmz) {
   if (!ctx) return CVB_BAD_INPUT;
@@ -2097,6 +2110,7 @@ int cvb_imp_rk(cvb_ctx *ctx, double *ucont, const double *ucont_o, const double 
   TRY(bc_covered(ctx, "ImpRK"));
   const bool inlet = ctx->H[ctx->nlevels - 1].d.bctype[4] == 5;
   InletProfile uin;
+  ctx->inlet_ti = ti;  // InletInterpolation reads the global ti
   if (inlet) TRY(inlet_speed(ctx, o->inletprofile, &uin));
   const int l = ctx->nlevels - 1;
   LevelDev &F = ctx->L[l];

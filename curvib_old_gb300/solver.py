@@ -247,6 +247,15 @@ class PoissonContext:
         c = np.ascontiguousarray(coor0, dtype=np.float64)
         self._check(self._L.cvb_set_inlet_nodes(self._ctx, ptr(c), float(cm[0]), float(cm[1]), float(cm[2])))
 
+    def set_inlet_flux(self, flux_in, ti):
+        """Flux_in and ti for the uniform inlet profiles 3, 6 and 8
+        (bcs.c:67-82)."""
+        self._check(self._L.cvb_set_inlet_flux(self._ctx, float(flux_in), int(ti)))
+
+    def inlet_flux_in(self):
+        """Flux_in as the last InflowFlux left it (profile 8 sets it)."""
+        return self._L.cvb_inlet_flux_in(self._ctx)
+
     def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0):
         """InflowFlux (bcs.c:99): (ucont, ubcs, FluxInSum)."""
         uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]

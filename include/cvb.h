@@ -277,8 +277,9 @@ int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const
  * bit for bit.
  *
  * InflowFlux (bcs.c:99-400) on an inlet face with a constant profile
- * (inletprofile 1: speed 2; -1: speed -1; 11: 0.185) or a shaped one (2, 4,
- * 7, 10, after cvb_set_inlet_nodes; other profiles are refused): on the face's
+ * (inletprofile 1: speed 2; -1: speed -1; 11: 0.185; 3, 6, 8: see
+ * cvb_set_inlet_flux) or a shaped one (2, 4, 7, 10, after
+ * cvb_set_inlet_nodes; the table profiles 0 and 5 are refused): on the face's
  * interior cells above fluid cells ubcs = uin zet / |zet| and Ucont.z = uin
  * |zet|; *flux_in_sum (FluxInSum) = their sum in the reference's loop order.
  * On a walled k = 0 face nothing is written. */
@@ -293,6 +294,13 @@ int cvb_inflow_flux(cvb_ctx *ctx, double *ucont, double *ubcs, int inletprofile,
  * the box layout, [my][mx][3] (node (i, j) at [j][i], as the reference's
  * local coor array). */
 int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cmy, double cmz);
+/* The reference's Flux_in and ti globals for the uniform profiles that
+ * InletInterpolation gives (bcs.c:67-82): 3 and 6 take uin = Flux_in, 8
+ * uin = sin(2 (3.14159) ti / 200) and leaves it in Flux_in.  Flux_in starts
+ * at the reference's 4.104388e-04 and ti at 0; cvb_imp_rk takes ti from its
+ * options.  cvb_inlet_flux_in returns Flux_in as the last InflowFlux left it. */
+int cvb_set_inlet_flux(cvb_ctx *ctx, double flux_in, int ti);
+double cvb_inlet_flux_in(const cvb_ctx *ctx);
 /* FormBCS (bcs.c:4436-5889): three passes of the outlet's flux correction
  * (ratio = (flux_in_sum + flux_intp_sum - the outlet's flux) / its area; ubcs
  * on the last face = the ucat next to it; Ucont.z of the last interior face =

@@ -1372,10 +1372,21 @@ int orc_calc_rhs(const orc_level *L, const double *ucont, const double *ucont_o,
 
 /* The inlet speed of InflowFlux's constant profiles (bcs.c:161-200); 0 for
  * the profiles that are not restated. */
+/* The reference's Flux_in (main.c:6, its initial value) and ti globals, which
+ * profiles 3, 6 and 8 read (bcs.c:67-82). */
+static double g_flux_in = 4.104388e-04;
+static int g_ti = 0;
+void orc_set_inlet_globals(double flux_in, int ti) {
+  g_flux_in = flux_in;
+  g_ti = ti;
+}
+
 int orc_inlet_speed(int inletprofile, double *uin) {
   if (inletprofile == 1) *uin = 2.;
   else if (inletprofile == -1) *uin = -1.;
   else if (inletprofile == 11) *uin = 0.185;
+  else if (inletprofile == 3 || inletprofile == 6) *uin = g_flux_in;
+  else if (inletprofile == 8) *uin = g_flux_in = sin(2 * 3.14159 * g_ti / 200.); /* and Flux_in keeps it */
   else return 0;
   return 1;
 }
@@ -1560,6 +1571,7 @@ int orc_imp_rk(const orc_level *L, double *ucont, const double *ucont_o, const d
   const size_t n3 = 3 * (size_t)L->mx * L->my * L->mz;
   const double alfa[4] = {0.25, 1 / 3., 0.5, 1.}; /* implicitsolver.c:7111 */
   double flux_in_sum = 0.;
+  g_ti = ti; /* InletInterpolation reads the global ti */
   if (!orc_bcs_covered(L->bctype) || (L->bctype[4] == 5 && !inlet_covered(inletprofile))) return -1;
   /* InflowFlux, OutflowFlux (only sums what nothing here reads), FormBCS */
   orc_inflow_flux(L, ucont, ubcs, inletprofile, &flux_in_sum);

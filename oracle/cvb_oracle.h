@@ -144,6 +144,9 @@ void orc_set_inlet_nodes(const double *coor0, const double *cm);
 int orc_inflow_flux_ext(const orc_level *L, double *ucont, double *ubcs, int inletprofile, const double *coor,
                         const double *cm, double *flux_in_sum);
 double orc_duct_speed(double xc, double yc);
+/* Flux_in and ti for the uniform profiles 3 and 6 (uin = Flux_in) and 8
+ * (uin = Flux_in = sin(2 3.14159 ti / 200)); orc_imp_rk sets ti itself. */
+void orc_set_inlet_globals(double flux_in, int ti);
 double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, int i, int j, const double *cm);
 /* FormBCS (bcs.c:4436-5889) on a covered box (orc_bcs_covered): three passes
  * of the outlet's flux correction (bctype[5] 4, bcs.c:4914-4998: ubcs on the

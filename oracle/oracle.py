@@ -128,6 +128,8 @@ def lib():
         _lib.orc_inflow_flux_ext.restype = I
         _lib.orc_set_inlet_nodes.argtypes = [P, P]
         _lib.orc_set_inlet_nodes.restype = None
+        _lib.orc_set_inlet_globals.argtypes = [ctypes.c_double, I]
+        _lib.orc_set_inlet_globals.restype = None
         _lib.orc_form_bcs.argtypes = [L, P, P, P, P, D, D]
         _lib.orc_form_bcs.restype = I
         _lib.orc_imp_rk.argtypes = [L, P, P, P, P, P, P, D, D, D, D, I, I, I, D, D, I, I, D, P]
@@ -316,6 +318,11 @@ class ImpRKStats(ctypes.Structure):
     _fields_ = [("pseudo_iterations", ctypes.c_int), ("rejected", ctypes.c_int), ("norm_du", ctypes.c_double),
                 ("rel_du", ctypes.c_double), ("norm_f", ctypes.c_double), ("rel_f", ctypes.c_double),
                 ("lambda_", ctypes.c_double)]
+
+
+def set_inlet_globals(flux_in, ti):
+    """Flux_in and ti, which the uniform inlet profiles 3, 6 and 8 read."""
+    lib().orc_set_inlet_globals(float(flux_in), int(ti))
 
 
 def inflow_flux(L: OLevel, ucont, ubcs, inletprofile, flux_in_sum=0.0, coor=None, cm=(0.0, 0.0, 0.0)):
@@ -557,6 +564,10 @@ class Reference:
                                int(ti), int(tistart), int(central), _p(out)):
             raise RuntimeError("ref_calc_rhs failed")
         return out, u
+
+    def set_inlet_globals(self, flux_in, ti):
+        """The reference's Flux_in and ti globals."""
+        self.L.ref_set_inlet_globals(ctypes.c_double(flux_in), int(ti))
 
     def inflow_flux(self, ucont, ubcs, inletprofile, flux_in_sum=0.0, cm=(0.0, 0.0, 0.0)):
         uc, ub = [np.array(x, dtype=np.float64, copy=True, order="C") for x in (ucont, ubcs)]

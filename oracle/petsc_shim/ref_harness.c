@@ -701,6 +701,9 @@ PetscErrorCode FormBCS(UserCtx *user);
  * subtract from the face centres. */
 extern PetscReal CMx_c, CMy_c, CMz_c;
 void ref_set_cm(double x, double y, double z) { CMx_c = x; CMy_c = y; CMz_c = z; }
+/* Flux_in (main.c:6) and ti, which the uniform inlet profiles read. */
+extern PetscReal Flux_in;
+void ref_set_inlet_globals(double flux_in, int ti_) { Flux_in = flux_in; ti = ti_; }
 
 int ref_inflow_flux(double *ucont, double *ubcs, int profile, double *flux_in_sum) {
   if (!g_ready) return 1;

@@ -182,6 +182,10 @@ FLUX_INTP_SUM = 1e-3
 # (CMx_c, CMy_c, CMz_c) that puts the unit box's inlet across its shape.
 SHAPED_INLETS = ((2, (0.0, 0.1, 0.0)), (4, (0.1, 0.45, 0.5)), (7, (0.0, 0.5, 0.0)), (10, (0.25, -0.8, 0.0)))
 
+# The uniform profiles InletInterpolation gives: (profile, Flux_in, ti); 3 and
+# 6 take Flux_in, 8 sin(2 (3.14159) ti / 200).
+UNIFORM_INLETS = ((3, 0.75, 0), (6, -0.3, 0), (8, 0.0, 37))
+
 
 def inlet_plane(nodes, shape):
     """The k = 0 node plane in the box layout ([my][mx][3]) of a case's nodes

@@ -122,6 +122,17 @@ int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cm
   REC.inlet_cm[2] = cmz;
   return CVB_OK;
 }
+int cvb_set_inlet_flux(cvb_ctx *ctx, double flux_in, int ti) {
+  (void)ctx;
+  REC.n_inlet_flux++;
+  REC.inlet_flux_in = flux_in;
+  REC.inlet_ti = ti;
+  return CVB_OK;
+}
+double cvb_inlet_flux_in(const cvb_ctx *ctx) {
+  (void)ctx;
+  return 0.875;
+}
 int cvb_set_plate_velocity(cvb_ctx *ctx, double u_bc) {
   (void)ctx;
   REC.u_bc = u_bc;

@@ -42,6 +42,9 @@ typedef struct {
   /* cvb_set_inlet_nodes: calls, a copy of the plane and the centre */
   int n_inlet_nodes;
   double inlet_plane[3 * 64 * 64], inlet_cm[3];
+  /* cvb_set_inlet_flux (cvb_inlet_flux_in returns 0.875) */
+  int n_inlet_flux, inlet_ti;
+  double inlet_flux_in;
   /* the status the next path call returns, then 0 again */
   int fail_next;
   /* cell (box index) the path calls write: solver_mg sets ucont[3m+1] = 42 and

@@ -19,7 +19,7 @@
 
 extern PetscInt block_number, immersed, wallfunction, les;
 extern PetscInt ti, tistart, imp_MAX_IT;
-extern PetscReal imp_atol, imp_rtol, FluxInSum, U_bc, CMx_c, CMy_c, CMz_c;
+extern PetscReal imp_atol, imp_rtol, FluxInSum, U_bc, CMx_c, CMy_c, CMz_c, Flux_in;
 extern PetscInt inletprofile;
 int ref_init(int nlevels, int IM, int JM, int KM, const int *bctype, int isc, int jsc, int ksc,
              const double *coords);
@@ -246,6 +246,13 @@ int main(void) {
     CHECK(bad == 0, "k = 0 node plane: %d coordinates differ", bad);
   }
   CMx_c = CMy_c = CMz_c = 0.0;
+  /* a uniform profile: Flux_in and ti go first, Flux_in comes back */
+  inletprofile = 8;
+  Flux_in = 0.125;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.n_imp_rk == 4 && REC.profile_imp == 8 && REC.n_inlet_flux == 1 &&
+            REC.inlet_flux_in == 0.125 && REC.inlet_ti == 4,
+        "uniform-profile ImpRK not on the device with Flux_in and ti");
+  CHECK(Flux_in == 0.875, "Flux_in not set after ImpRK with profile 8");
   inletprofile = 11;
   CHECK(shim_vec_data(fine->Bcs.Ubcs)[3 * REC.mark + 2] == 14.0, "Bcs.Ubcs not written back");
   fine->bctype[4] = fine->bctype[5] = 1;

@@ -10,6 +10,7 @@ iteration ImpRK (implicitsolver.c:7094) on the all-wall scenarios.  The oracle
 is pinned to the reference's own routines (tests/test_oracle_pin.py).  Results are compared as bytes, so
 signed zeros count; the periodic boxes are refused.
 """
+import math
 import types
 
 import numpy as np
@@ -121,8 +122,8 @@ def test_inlet_outlet_match_oracle(name):
     with an inlet on k = 0 and an outlet on the last k face, bit for bit
     against the oracle (pinned to the reference's routines): ucont, ubcs, ucat,
     p, FluxInSum and the iteration counts."""
-    from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, SHAPED_INLETS, imp_rk_inputs,
-                       inlet_plane)
+    from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, SHAPED_INLETS, UNIFORM_INLETS,
+                       imp_rk_inputs, inlet_plane)
     c = build(name)
     bctype = [1, 1, 1, 1, 5, 4]
     ctx = _ctx(c, c["nvert"], bctype)
@@ -146,6 +147,19 @@ def test_inlet_outlet_match_oracle(name):
                                                 0, 0, IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM)
         rc, uc_o, u_o, p_o, st_o, ub_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
                                                   ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM, plane, cm)
+        assert rc == 0 and st_g["pseudo_iterations"] == st_o.pseudo_iterations
+        assert all(_same(a, b) for a, b in ((uc_g, uc_o), (u_g, u_o), (p_g, p_o), (ub_g, ub_o)))
+        for prof, flux_in, t in UNIFORM_INLETS:
+            ctx.set_inlet_flux(flux_in, t)
+            O.set_inlet_globals(flux_in, t)
+            uc_g, ub_g, f_g = ctx.inflow_flux(c["ucont"], ubcs1, prof)
+            rc, uc_o, ub_o, f_o = O.inflow_flux(L, c["ucont"], ubcs1, prof)
+            assert rc == 0 and _same(uc_g, uc_o) and _same(ub_g, ub_o) and f_g == f_o, prof
+        assert ctx.inlet_flux_in() == math.sin(2 * 3.14159 * 37 / 200.)
+        uc_g, u_g, p_g, st_g, ub_g = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti,
+                                                0, 0, IMP_ATOL, IMP_RTOL, max_it, 8, FLUX_INTP_SUM)
+        rc, uc_o, u_o, p_o, st_o, ub_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
+                                                  ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, 8, FLUX_INTP_SUM)
         assert rc == 0 and st_g["pseudo_iterations"] == st_o.pseudo_iterations
         assert all(_same(a, b) for a, b in ((uc_g, uc_o), (u_g, u_o), (p_g, p_o), (ub_g, ub_o)))
         uc_i, ub_i, f = ctx.inflow_flux(c["ucont"], ubcs1, 1)
