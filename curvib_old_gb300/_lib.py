@@ -145,6 +145,7 @@ EXPORTS = {
     "cvb_set_inlet_nodes": ([_P, _P, _D, _D, _D], _I),
     "cvb_set_inlet_flux": ([_P, _D, _I], _I),
     "cvb_inlet_flux_in": ([_P], _D),
+    "cvb_set_inlet_table": ([_P, _P], _I),
     "cvb_form_bcs": ([_P, _P, _P, _P, _P, _D, _D], _I),
     "cvb_imp_rk_opts_default": ([_P], None),
     "cvb_imp_rk": ([_P, _P, _P, _P, _P, _P, _P, _P, _P], _I),

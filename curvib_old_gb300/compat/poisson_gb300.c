@@ -318,8 +318,8 @@ PetscErrorCode Convection_GB300(UserCtx *u, Vec Ucont, Vec Ucat, Vec Conv) {
 
 /* ImpRK (implicitsolver.c:7094-7257) with the reference's arguments.  On one
  * block with no immersed body, no LES / RANS / wall model, solid walls on the
- * x and y faces and on the k faces walls or an inlet (5, any profile but the
- * table ones, 0 and 5) with an outlet (4), the whole pseudo-time iteration runs on the device
+ * x and y faces and on the k faces walls or an inlet (5, any profile; the
+ * table ones, 0 and 5, for ti below 2000) with an outlet (4), the whole pseudo-time iteration runs on the device
  * (cvb_imp_rk: InflowFlux, FormBCS, CalcRHS, the Runge-Kutta stage updates,
  * the norms and the step halving), with the reference's -cfl, -imp_atol,
  * -imp_rtol, -imp_MAX_IT, -inlet (inletprofile) and -central and the block's
@@ -356,13 +356,16 @@ PetscErrorCode ImpRK_GB300(UserCtx *u, IBMNodes *ibm, FSInfo *fsi) {
                 (bt[5] == 1 || bt[5] == 4) && ((bt[4] == 5) == (bt[5] == 4));
   const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10;
   const int uniform = inletprofile == 3 || inletprofile == 6 || inletprofile == 8;
+  /* the table profiles, within the table (bcs.c:73) */
+  const int table = (inletprofile == 0 || inletprofile == 5) && ti >= 0 && ti < 2000;
   if (bt[4] == 5)
-    covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11 || shaped || uniform);
+    covered = covered && (inletprofile == 1 || inletprofile == -1 || inletprofile == 11 || shaped || uniform || table);
   if (!g_cvb || block_number != 1 || immersed || les || rans || wallfunction || !covered || !u->Ucont_o ||
       !u->Ucont_rm1)
     return ImpRK(u, ibm, fsi);
-  if (bt[4] == 5 && shaped) {
-    const int rc = inlet_nodes(u);
+  if (bt[4] == 5 && (shaped || table)) {
+    int rc = inlet_nodes(u);
+    if (!rc && table) rc = cvb_set_inlet_table(g_cvb, &u->uinr[0][0]);
     if (rc) return report(rc, "ImpRK_GB300");
   }
   if (bt[4] == 5 && uniform) cvb_set_inlet_flux(g_cvb, Flux_in, (int)ti);

@@ -1867,8 +1867,33 @@ static double duct_speed(double xc, double yc) {
   return u;
 }
 
-static int duct_speeds(cvb_ctx *ctx) {
-  if (ctx->inlet_uin_ready) return CVB_OK;
+// InletInterpolation's table (bcs.c:67-96) at radius r and table column
+// tstep: uinr [101][1001], radius 0.005 i; beyond r = 1 the speed of row 99,
+// between row 100's radius and 1 zero.
+static double table_speed(const double *uinr, int tstep, double r) {
+  const double *U = uinr + tstep;
+  if (r > 1.) return U[99 * 1001];
+  for (int i = 0; i < 100; i++) {
+    const double ri = i * 0.005, ri1 = (i + 1) * 0.005;
+    if (r >= ri && r < ri1) return U[i * 1001] + (U[(i + 1) * 1001] - U[i * 1001]) * (r - ri) / (ri1 - ri);
+  }
+  return 0;
+}
+
+// The reference's table column for time step ti (bcs.c:73), -1 outside the
+// table.
+static int table_step(int ti) {
+  const int tstep = ti / 2 - ((ti / 2000) * 2000);
+  return tstep >= 0 && tstep < 1001 ? tstep : -1;
+}
+
+// Speeds per inlet face cell formed on the host: profile 10 (libm's series)
+// once per set of nodes, the table profiles 0 and 5 once per set of nodes,
+// table and step.
+static int host_speeds(cvb_ctx *ctx, int profile) {
+  const int tstep = profile == 10 ? 0 : table_step(ctx->inlet_ti);
+  const int key = profile * 10000 + tstep;
+  if (ctx->inlet_uin_ready && ctx->inlet_uin_key == key) return CVB_OK;
   const Geom &g = ctx->L[ctx->nlevels - 1].g;
   const int ni = g.mx - 2, nj = g.my - 2;
   const double *P = ctx->inlet_plane_host.data(), *cm = ctx->inlet_cm;
@@ -1879,18 +1904,27 @@ static int duct_speeds(cvb_ctx *ctx) {
       const double *c = P + 3 * ((size_t)j * g.mx + i - 1), *d = P + 3 * ((size_t)(j - 1) * g.mx + i - 1);
       const double xc = (a[0] + b[0] + c[0] + d[0]) * 0.25 - cm[0];
       const double yc = (a[1] + b[1] + c[1] + d[1]) * 0.25 - cm[1];
-      u[(size_t)(j - 1) * ni + i - 1] = duct_speed(xc, yc);
+      const double zc = (a[2] + b[2] + c[2] + d[2]) * 0.25 - cm[2];
+      double s;
+      if (profile == 10) {
+        s = duct_speed(xc, yc);
+      } else {
+        s = table_speed(ctx->inlet_table.data(), tstep, sqrt(zc * zc + yc * yc));
+        if (profile == 5) s = -s;
+      }
+      u[(size_t)(j - 1) * ni + i - 1] = s;
     }
   if (!ctx->inlet_uin) TRY(dalloc(ctx, &ctx->inlet_uin, u.size()));
   CK(cudaMemcpyAsync(ctx->inlet_uin, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->inlet_uin_ready = true;
+  ctx->inlet_uin_key = key;
   return CVB_OK;
 }
 
 static int inlet_speed(cvb_ctx *ctx, int profile, InletProfile *ip) {
   ip->profile = profile;
-  ip->shaped = profile == 2 || profile == 4 || profile == 7 || profile == 10;
+  ip->shaped = profile == 2 || profile == 4 || profile == 7 || profile == 10 || profile == 0 || profile == 5;
   if (profile == 1) ip->uin = 2.;
   else if (profile == -1) ip->uin = -1.;
   else if (profile == 11) ip->uin = 0.185;
@@ -1899,14 +1933,23 @@ static int inlet_speed(cvb_ctx *ctx, int profile, InletProfile *ip) {
     ip->uin = ctx->inlet_flux_in = sin(2 * 3.14159 * ctx->inlet_ti / 200.);
   else if (!ip->shaped)
     return fail(ctx, CVB_BAD_INPUT,
-                "InflowFlux: inletprofile %d is not covered (uniform profiles 1, -1, 11, 3, 6, 8 and shaped 2, 4, 7, "
-                "10 are)",
+                "InflowFlux: inletprofile %d is not covered (uniform profiles 1, -1, 11, 3, 6, 8, shaped 2, 4, 7, "
+                "10 and the table's 0, 5 are)",
                 profile);
   else if (!ctx->inlet_coor)
     return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d needs the inlet's nodes (cvb_set_inlet_nodes)",
                 profile);
-  if (profile == 10) {
-    TRY(duct_speeds(ctx));
+  if (profile == 0 || profile == 5) {
+    if (ctx->inlet_table.empty())
+      return fail(ctx, CVB_BAD_INPUT, "InflowFlux: inletprofile %d needs the inlet table (cvb_set_inlet_table)",
+                  profile);
+    if (table_step(ctx->inlet_ti) < 0)
+      return fail(ctx, CVB_BAD_INPUT,
+                  "InflowFlux: inletprofile %d at ti %d: the table column ti/2 - (ti/2000) 2000 is outside the table",
+                  profile, ctx->inlet_ti);
+  }
+  if (profile == 10 || profile == 0 || profile == 5) {
+    TRY(host_speeds(ctx, profile));
     ip->uin_cell = ctx->inlet_uin;
   }
   return CVB_OK;
@@ -1920,6 +1963,14 @@ int cvb_set_inlet_flux(cvb_ctx *ctx, double flux_in, int ti) {
 }
 
 double cvb_inlet_flux_in(const cvb_ctx *ctx) { return ctx ? ctx->inlet_flux_in : 0.; }
+
+int cvb_set_inlet_table(cvb_ctx *ctx, const double *uinr) {
+  if (!ctx) return CVB_BAD_INPUT;
+  if (!uinr) return fail(ctx, CVB_BAD_INPUT, "uinr is NULL");
+  ctx->inlet_table.assign(uinr, uinr + 101 * 1001);
+  ctx->inlet_uin_ready = false;
+  return CVB_OK;
+}
 
 int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cmy, double cmz) {
   if (!ctx) return CVB_BAD_INPUT;

@@ -103,6 +103,8 @@ struct cvb_ctx {
   std::vector<double> inlet_plane_host;  // the same plane on the host (profile 10's speeds)
   double *inlet_uin = nullptr;   // profile 10's speed per inlet face cell ([my - 2][mx - 2]), formed on the host
   bool inlet_uin_ready = false;
+  int inlet_uin_key = -1;        // the profile (and table step) inlet_uin holds
+  std::vector<double> inlet_table;  // InletRead's uinr [101][1001] (profiles 0 and 5)
   double inlet_flux_in = 4.104388e-04;  // the reference's Flux_in (its initial value), profiles 3 and 6
   int inlet_ti = 0;                     // the time step profile 8 reads
   double *bc_scratch = nullptr;            // InflowFlux / outlet: plane terms (device)

@@ -252,6 +252,14 @@ class PoissonContext:
         (bcs.c:67-82)."""
         self._check(self._L.cvb_set_inlet_flux(self._ctx, float(flux_in), int(ti)))
 
+    def set_inlet_table(self, uinr):
+        """InletRead's table uinr [101][1001] for the inlet profiles 0 and 5
+        (bcs.c:40-96)."""
+        t = np.ascontiguousarray(uinr, dtype=np.float64)
+        if t.size != 101 * 1001:
+            raise ValueError("uinr must hold 101 x 1001 values")
+        self._check(self._L.cvb_set_inlet_table(self._ctx, ptr(t)))
+
     def inlet_flux_in(self):
         """Flux_in as the last InflowFlux left it (profile 8 sets it)."""
         return self._L.cvb_inlet_flux_in(self._ctx)

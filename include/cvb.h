@@ -279,7 +279,8 @@ int cvb_calc_rhs(cvb_ctx *ctx, const double *ucont, const double *ucont_o, const
  * InflowFlux (bcs.c:99-400) on an inlet face with a constant profile
  * (inletprofile 1: speed 2; -1: speed -1; 11: 0.185; 3, 6, 8: see
  * cvb_set_inlet_flux) or a shaped one (2, 4, 7, 10, after
- * cvb_set_inlet_nodes; the table profiles 0 and 5 are refused): on the face's
+ * cvb_set_inlet_nodes; with cvb_set_inlet_table also the table's 0 and 5;
+ * other profiles are refused): on the face's
  * interior cells above fluid cells ubcs = uin zet / |zet| and Ucont.z = uin
  * |zet|; *flux_in_sum (FluxInSum) = their sum in the reference's loop order.
  * On a walled k = 0 face nothing is written. */
@@ -301,6 +302,14 @@ int cvb_set_inlet_nodes(cvb_ctx *ctx, const double *coor0, double cmx, double cm
  * options.  cvb_inlet_flux_in returns Flux_in as the last InflowFlux left it. */
 int cvb_set_inlet_flux(cvb_ctx *ctx, double flux_in, int ti);
 double cvb_inlet_flux_in(const cvb_ctx *ctx);
+/* The table of the profiles 0 and 5 (bcs.c:40-96), InletRead's uinr
+ * [101][1001]: uinr[i][t] the speed at radius 0.005 i in column t.  The speed
+ * of a face cell is (for 5 minus) the table interpolated linearly at its
+ * radius sqrt(y^2 + z^2) about (CMy_c, CMz_c) (cvb_set_inlet_nodes), in
+ * column ti/2 - (ti/2000) 2000 (cvb_set_inlet_flux's or cvb_imp_rk's ti);
+ * beyond radius 1 row 99's, between 0.5 and 1 zero.  Steps whose column
+ * falls outside the table (ti >= 2000) are refused with CVB_BAD_INPUT. */
+int cvb_set_inlet_table(cvb_ctx *ctx, const double *uinr);
 /* FormBCS (bcs.c:4436-5889): three passes of the outlet's flux correction
  * (ratio = (flux_in_sum + flux_intp_sum - the outlet's flux) / its area; ubcs
  * on the last face = the ucat next to it; Ucont.z of the last interior face =

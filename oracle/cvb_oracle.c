@@ -1399,6 +1399,27 @@ int orc_bcs_covered(const int *bc) {
   return (bc[5] == 4) == (bc[4] == 5);
 }
 
+/* InletInterpolation's table (bcs.c:67-96): uinr [101][1001] of InletRead
+ * (bcs.c:40-55; radius r[i] = 0.005 i, one column per time step), at the
+ * step tstep = ti / 2 - (ti / 2000) 2000; beyond r = 1 the speed of r[99],
+ * between r[100] and 1 zero. */
+static const double *g_inlet_table;
+void orc_set_inlet_table(const double *uinr) { g_inlet_table = uinr; }
+static int table_step_ok(void) {
+  const int tstep = g_ti / 2 - ((g_ti / 2000) * 2000);
+  return g_inlet_table && tstep >= 0 && tstep < 1001;
+}
+static double table_speed(double r) {
+  const int tstep = g_ti / 2 - ((g_ti / 2000) * 2000);
+  const double *U = g_inlet_table + tstep;
+  if (r > 1.) return U[99 * 1001];
+  for (int i = 0; i < 100; i++) {
+    const double ri = i * 0.005, ri1 = (i + 1) * 0.005;
+    if (r >= ri && r < ri1) return U[i * 1001] + (U[(i + 1) * 1001] - U[i * 1001]) * (r - ri) / (ri1 - ri);
+  }
+  return 0;
+}
+
 /* Profile 10 (bcs.c:180-195): fully developed laminar flow in a square duct
  * (y across [1, 2], x across [0, 1] about the centre), 1 - y'^2 less the
  * first 20 terms of its Fourier series in y' = 2 (y - 1.5), x' = x - 0.5;
@@ -1433,6 +1454,8 @@ double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, in
     return uin;
   }
   if (inletprofile == 10) return orc_duct_speed(xc, yc);
+  if (inletprofile == 0) return table_speed(r);
+  if (inletprofile == 5) return -table_speed(r);
   return 1.5 * (1. - 4. * yc * yc); /* 7 */
 }
 
@@ -1449,6 +1472,7 @@ void orc_set_inlet_nodes(const double *coor0, const double *cm) {
 static int inlet_covered(int inletprofile) {
   double uin;
   if (inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10) return g_inlet_coor != NULL;
+  if (inletprofile == 0 || inletprofile == 5) return g_inlet_coor != NULL && table_step_ok();
   return orc_inlet_speed(inletprofile, &uin);
 }
 
@@ -1461,7 +1485,9 @@ int orc_inflow_flux_ext(const orc_level *L, double *ucont, double *ub, int inlet
   const int mx = L->mx, my = L->my;
   if (L->bctype[4] != 5) return 0; /* FluxIn is 0 and FluxInSum keeps its value */
   double uin0 = 0.;
-  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10;
+  const int shaped = inletprofile == 2 || inletprofile == 4 || inletprofile == 7 || inletprofile == 10 ||
+                     inletprofile == 0 || inletprofile == 5;
+  if ((inletprofile == 0 || inletprofile == 5) && !table_step_ok()) return -1;
   if (shaped ? !(coor && cm) : !orc_inlet_speed(inletprofile, &uin0)) return -1;
   const double *z;
   for (int j = 1; j < my - 1; j++)

@@ -147,6 +147,10 @@ double orc_duct_speed(double xc, double yc);
 /* Flux_in and ti for the uniform profiles 3 and 6 (uin = Flux_in) and 8
  * (uin = Flux_in = sin(2 3.14159 ti / 200)); orc_imp_rk sets ti itself. */
 void orc_set_inlet_globals(double flux_in, int ti);
+/* The table profiles 0 and 5 (+- InletInterpolation of uinr [101][1001]
+ * at the face cell's radius and ti; NULL: none); -1 where the reference's
+ * step index ti / 2 - (ti / 2000) 2000 falls outside the table. */
+void orc_set_inlet_table(const double *uinr);
 double orc_inlet_shaped(int inletprofile, const double *coor, int mx, int my, int i, int j, const double *cm);
 /* FormBCS (bcs.c:4436-5889) on a covered box (orc_bcs_covered): three passes
  * of the outlet's flux correction (bctype[5] 4, bcs.c:4914-4998: ubcs on the

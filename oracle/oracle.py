@@ -130,6 +130,8 @@ def lib():
         _lib.orc_set_inlet_nodes.restype = None
         _lib.orc_set_inlet_globals.argtypes = [ctypes.c_double, I]
         _lib.orc_set_inlet_globals.restype = None
+        _lib.orc_set_inlet_table.argtypes = [P]
+        _lib.orc_set_inlet_table.restype = None
         _lib.orc_form_bcs.argtypes = [L, P, P, P, P, D, D]
         _lib.orc_form_bcs.restype = I
         _lib.orc_imp_rk.argtypes = [L, P, P, P, P, P, P, D, D, D, D, I, I, I, D, D, I, I, D, P]
@@ -323,6 +325,17 @@ class ImpRKStats(ctypes.Structure):
 def set_inlet_globals(flux_in, ti):
     """Flux_in and ti, which the uniform inlet profiles 3, 6 and 8 read."""
     lib().orc_set_inlet_globals(float(flux_in), int(ti))
+
+
+_TABLE = None
+
+
+def set_inlet_table(uinr):
+    """The inlet table [101][1001] of the profiles 0 and 5 (None: none); kept
+    here while the oracle holds it."""
+    global _TABLE
+    _TABLE = None if uinr is None else np.ascontiguousarray(uinr, dtype=np.float64).reshape(101, 1001)
+    lib().orc_set_inlet_table(None if _TABLE is None else _p(_TABLE))
 
 
 def inflow_flux(L: OLevel, ucont, ubcs, inletprofile, flux_in_sum=0.0, coor=None, cm=(0.0, 0.0, 0.0)):
@@ -564,6 +577,11 @@ class Reference:
                                int(ti), int(tistart), int(central), _p(out)):
             raise RuntimeError("ref_calc_rhs failed")
         return out, u
+
+    def set_inlet_table(self, uinr):
+        """The finest level's InletRead table (r = 0.005 i, uinr [101][1001])."""
+        t = np.ascontiguousarray(uinr, dtype=np.float64)
+        self.L.ref_set_inlet_table(_p(t))
 
     def set_inlet_globals(self, flux_in, ti):
         """The reference's Flux_in and ti globals."""

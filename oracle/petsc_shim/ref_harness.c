@@ -14,6 +14,7 @@
  * 3-vectors interleaved (x,y,z), i.e. exactly a PETSc global vector.
  */
 #include "variables.h"
+#include <string.h>
 #include <unistd.h>
 
 /* Globals the reference sources expect main.c to define. */
@@ -704,6 +705,13 @@ void ref_set_cm(double x, double y, double z) { CMx_c = x; CMy_c = y; CMz_c = z;
 /* Flux_in (main.c:6) and ti, which the uniform inlet profiles read. */
 extern PetscReal Flux_in;
 void ref_set_inlet_globals(double flux_in, int ti_) { Flux_in = flux_in; ti = ti_; }
+/* InletRead's table on the finest level: r as InletRead sets it (bcs.c:46),
+ * uinr [101][1001] as given. */
+void ref_set_inlet_table(const double *uinr) {
+  UserCtx *u = &g_mg.mgctx[g_mg.mglevels - 1].user[0];
+  for (int i = 0; i < 101; i++) u->r[i] = i * 0.005;
+  memcpy(u->uinr, uinr, sizeof(u->uinr));
+}
 
 int ref_inflow_flux(double *ucont, double *ubcs, int profile, double *flux_in_sum) {
   if (!g_ready) return 1;

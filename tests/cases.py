@@ -186,6 +186,16 @@ SHAPED_INLETS = ((2, (0.0, 0.1, 0.0)), (4, (0.1, 0.45, 0.5)), (7, (0.0, 0.5, 0.0
 # 6 take Flux_in, 8 sin(2 (3.14159) ti / 200).
 UNIFORM_INLETS = ((3, 0.75, 0), (6, -0.3, 0), (8, 0.0, 37))
 
+# The table profiles (profile, centre, ti): 0 and 5 interpolate InletRead's
+# table (uinr [101][1001], inlet_table) at the face cell's radius, column
+# ti/2 - (ti/2000) 2000.
+TABLE_INLETS = ((0, (0.0, 0.5, 0.5), 37), (5, (0.1, 0.45, 0.5), 1500))
+
+
+def inlet_table():
+    """A seeded stand-in for InletRead's uinr [101][1001]."""
+    return seeded((101, 1001), 820)
+
 
 def inlet_plane(nodes, shape):
     """The k = 0 node plane in the box layout ([my][mx][3]) of a case's nodes

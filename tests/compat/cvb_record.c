@@ -133,6 +133,11 @@ double cvb_inlet_flux_in(const cvb_ctx *ctx) {
   (void)ctx;
   return 0.875;
 }
+int cvb_set_inlet_table(cvb_ctx *ctx, const double *uinr) {
+  (void)ctx;
+  REC.inlet_table = uinr;
+  return CVB_OK;
+}
 int cvb_set_plate_velocity(cvb_ctx *ctx, double u_bc) {
   (void)ctx;
   REC.u_bc = u_bc;

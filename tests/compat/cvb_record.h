@@ -44,6 +44,7 @@ typedef struct {
   double inlet_plane[3 * 64 * 64], inlet_cm[3];
   /* cvb_set_inlet_flux (cvb_inlet_flux_in returns 0.875) */
   int n_inlet_flux, inlet_ti;
+  const double *inlet_table; /* cvb_set_inlet_table */
   double inlet_flux_in;
   /* the status the next path call returns, then 0 again */
   int fail_next;

@@ -253,6 +253,11 @@ int main(void) {
             REC.inlet_flux_in == 0.125 && REC.inlet_ti == 4,
         "uniform-profile ImpRK not on the device with Flux_in and ti");
   CHECK(Flux_in == 0.875, "Flux_in not set after ImpRK with profile 8");
+  /* a table profile: the nodes and the finest level's uinr go first */
+  inletprofile = 5;
+  CHECK(ImpRK_GB300(fine, NULL, NULL) == 0 && REC.n_imp_rk == 5 && REC.profile_imp == 5 && REC.n_inlet_nodes == 2 &&
+            REC.inlet_table == &fine->uinr[0][0],
+        "table-profile ImpRK not on the device with the nodes and uinr");
   inletprofile = 11;
   CHECK(shim_vec_data(fine->Bcs.Ubcs)[3 * REC.mark + 2] == 14.0, "Bcs.Ubcs not written back");
   fine->bctype[4] = fine->bctype[5] = 1;

@@ -31,7 +31,7 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
 from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_OUTLET_SCENARIOS, INLET_PROFILES,  # noqa: E402
-                   MOM_DT, MOM_REN, SHAPED_INLETS, UNIFORM_INLETS,
+                   MOM_DT, MOM_REN, SHAPED_INLETS, TABLE_INLETS, UNIFORM_INLETS, inlet_table,
                    conv_seam_nvert, imp_rk_inputs, mom_edge_nvert, momentum_inputs)
 from cases import (IBM_CASES, POST_U_BC, POST_VARIANTS, SCENARIOS, build, conv_edge_nvert, digest, digest_nan,  # noqa: E402
                    ibm_inputs, post_inputs, seeded)
@@ -159,7 +159,8 @@ def inlet_outlet(c):
     the inlet's flux and an immersed-boundary flux, and cases.IMP_RK_RUNS with
     profile 1; the shaped profiles (cases.SHAPED_INLETS) and ImpRK's first run
     with the pipe profile 4; the uniform profiles (cases.UNIFORM_INLETS) and
-    ImpRK's first run with profile 8."""
+    ImpRK's first run with profile 8; the table profiles (cases.TABLE_INLETS)
+    and ImpRK's first run with profile 0."""
     bct = [1, 1, 1, 1, 5, 4]
     nl = c["nl"]
     R = O.Reference(c["nodes"], nl, bct, c["semi"])
@@ -175,6 +176,11 @@ def inlet_outlet(c):
     for prof, flux_in, ti in UNIFORM_INLETS:
         R.set_inlet_globals(flux_in, ti)
         uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, prof)
+        out[f"inflow_{prof}"] = {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)}
+    R.set_inlet_table(inlet_table())
+    for prof, cm, ti in TABLE_INLETS:
+        R.set_inlet_globals(0.0, ti)
+        uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, prof, 0.0, cm)
         out[f"inflow_{prof}"] = {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)}
     uc, ub, f = R.inflow_flux(c["ucont"], ubcs1, 1)
     uc, ub, u, pp = R.form_bcs(uc, ub, ucat1, p1, f, FLUX_INTP_SUM)
@@ -197,6 +203,9 @@ def inlet_outlet(c):
             uc, u, pp, ub = R.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
                                      IMP_ATOL, IMP_RTOL, max_it, 8, FLUX_INTP_SUM)
             out["imp_rk_uniform_8"] = {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)}
+            uc, u, pp, ub = R.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0, 0,
+                                     IMP_ATOL, IMP_RTOL, max_it, 0, FLUX_INTP_SUM, TABLE_INLETS[0][1])
+            out["imp_rk_table_0"] = {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)}
         finally:
             os.chdir(cwd)
     return out

@@ -122,8 +122,9 @@ def test_inlet_outlet_match_oracle(name):
     with an inlet on k = 0 and an outlet on the last k face, bit for bit
     against the oracle (pinned to the reference's routines): ucont, ubcs, ucat,
     p, FluxInSum and the iteration counts."""
-    from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, SHAPED_INLETS, UNIFORM_INLETS,
-                       imp_rk_inputs, inlet_plane)
+    from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_PROFILES, SHAPED_INLETS, TABLE_INLETS,
+                       UNIFORM_INLETS, imp_rk_inputs, inlet_plane, inlet_table)
+    from curvib_old_gb300._lib import CVB_BAD_INPUT, CvbError
     c = build(name)
     bctype = [1, 1, 1, 1, 5, 4]
     ctx = _ctx(c, c["nvert"], bctype)
@@ -162,6 +163,32 @@ def test_inlet_outlet_match_oracle(name):
                                                   ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, 8, FLUX_INTP_SUM)
         assert rc == 0 and st_g["pseudo_iterations"] == st_o.pseudo_iterations
         assert all(_same(a, b) for a, b in ((uc_g, uc_o), (u_g, u_o), (p_g, p_o), (ub_g, ub_o)))
+        tbl = inlet_table()
+        ctx.set_inlet_table(tbl)
+        O.set_inlet_table(tbl)
+        try:
+            for prof, cm, t in TABLE_INLETS:
+                ctx.set_inlet_nodes(plane, cm)
+                ctx.set_inlet_flux(0.0, t)
+                O.set_inlet_globals(0.0, t)
+                uc_g, ub_g, f_g = ctx.inflow_flux(c["ucont"], ubcs1, prof)
+                rc, uc_o, ub_o, f_o = O.inflow_flux(L, c["ucont"], ubcs1, prof, 0.0, plane, cm)
+                assert rc == 0 and _same(uc_g, uc_o) and _same(ub_g, ub_o) and f_g == f_o, prof
+            prof, cm, _ = TABLE_INLETS[0]
+            ctx.set_inlet_nodes(plane, cm)
+            uc_g, u_g, p_g, st_g, ub_g = ctx.imp_rk(c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl,
+                                                    ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM)
+            rc, uc_o, u_o, p_o, st_o, ub_o = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0,
+                                                      cfl, ti, 0, 0, IMP_ATOL, IMP_RTOL, max_it, prof, FLUX_INTP_SUM,
+                                                      plane, cm)
+            assert rc == 0 and st_g["pseudo_iterations"] == st_o.pseudo_iterations
+            assert all(_same(a, b) for a, b in ((uc_g, uc_o), (u_g, u_o), (p_g, p_o), (ub_g, ub_o)))
+            ctx.set_inlet_flux(0.0, 2000)  # the reference's column -1000: refused
+            with pytest.raises(CvbError) as e:
+                ctx.inflow_flux(c["ucont"], ubcs1, 0)
+            assert e.value.status == CVB_BAD_INPUT
+        finally:
+            O.set_inlet_table(None)
         uc_i, ub_i, f = ctx.inflow_flux(c["ucont"], ubcs1, 1)
         got = ctx.form_bcs(uc_i, ub_i, ucat1, p1, f, FLUX_INTP_SUM)
         rc, *want = O.form_bcs(L, uc_i, ub_i, ucat1, p1, f, FLUX_INTP_SUM)

@@ -240,7 +240,7 @@ def test_inlet_outlet_matches_reference(name):
     and ImpRK (implicitsolver.c:7094-7257) on a box with an inlet on k = 0 and
     an outlet on the last k face, bit for bit."""
     from cases import (FLUX_INTP_SUM, IMP_ATOL, IMP_RK_RUNS, IMP_RTOL, INLET_OUTLET_SCENARIOS, INLET_PROFILES, MOM_DT,
-                       MOM_REN, SHAPED_INLETS, UNIFORM_INLETS, imp_rk_inputs, inlet_plane)
+                       MOM_REN, SHAPED_INLETS, TABLE_INLETS, UNIFORM_INLETS, imp_rk_inputs, inlet_plane, inlet_table)
     assert name in INLET_OUTLET_SCENARIOS
     c = _setup(name)
     want = REF["scenarios"][name]["inlet_outlet"]
@@ -268,6 +268,21 @@ def test_inlet_outlet_matches_reference(name):
                                     IMP_ATOL, IMP_RTOL, max_it, 8, FLUX_INTP_SUM)
     assert rc == 0 and {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)} == \
         want["imp_rk_uniform_8"]
+    O.set_inlet_table(inlet_table())
+    try:
+        for prof, cm, t in TABLE_INLETS:
+            O.set_inlet_globals(0.0, t)
+            rc, uc, ub, f = O.inflow_flux(L, c["ucont"], ubcs1, prof, 0.0, plane, cm)
+            assert rc == 0 and {"ucont": digest(uc), "ubcs": digest(ub), "flux_in_sum": repr(f)} == \
+                want[f"inflow_{prof}"]
+        rc, uc, u, pp, _, ub = O.imp_rk(L, c["ucont"], uo1, urm1, ucat1, p1, ubcs1, MOM_REN, MOM_DT, 1.0, cfl, ti, 0,
+                                        0, IMP_ATOL, IMP_RTOL, max_it, 0, FLUX_INTP_SUM, plane, TABLE_INLETS[0][1])
+        assert rc == 0 and {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)} == \
+            want["imp_rk_table_0"]
+        O.set_inlet_globals(0.0, 2000)  # the reference's column -1000: outside the table
+        assert O.inflow_flux(L, c["ucont"], ubcs1, 0, 0.0, plane)[0] == -1
+    finally:
+        O.set_inlet_table(None)
     rc, uc, ub, f = O.inflow_flux(L, c["ucont"], ubcs1, 1)
     rc, uc, ub, u, pp = O.form_bcs(L, uc, ub, ucat1, p1, f, FLUX_INTP_SUM)
     assert rc == 0 and {"ucont": digest(uc), "ubcs": digest(ub), "ucat": digest(u), "p": digest(pp)} == \
